@@ -1,0 +1,989 @@
+/*
+ * pump_oracle.c -- CPU restatement of the PUMP hot path (test oracle).
+ *
+ * TEST INFRASTRUCTURE ONLY (see pump_oracle.h).  Build with
+ * -ffp-contract=off so that no multiply-add is fused: every expression below
+ * is written with the evaluation types of the reference's C++ source, one
+ * rounding per operation.
+ */
+#include "pump_oracle.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ======================================================================
+ * Integer powers, correctly rounded for float-valued x (x*x is exact).
+ * The reference writes pow(float, int); C++ promotes it to
+ * pow(double, double) (2pBVP.cu:99-105).
+ * ==================================================================== */
+static inline double p2f(float x) { double d = x; return d * d; }
+static inline double p3f(float x) { double d = x; return (d * d) * d; }
+static inline double p4f(float x) { double d = x; double s = d * d; return s * s; }
+
+/* ======================================================================
+ * Particle stream
+ * ==================================================================== */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ k0;
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ k1;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* ln(x) = e ln2 + 2 atanh(s), s = (m-1)/(m+1), m in [sqrt(1/2), sqrt(2)).
+ * |s| <= 0.1716, s^2 <= 0.0295: 13 odd terms reach 1e-19 relative. */
+double orc_det_log(double x) {
+  int e;
+  double m = frexp(x, &e);                 /* exact: x = m 2^e, m in [0.5,1) */
+  if (m < 0.70710678118654752440) { m = m * 2.0; e = e - 1; }
+  double s = (m - 1.0) / (m + 1.0);
+  double z = s * s;
+  double t = 1.0 / 25.0;
+  t = t * z + 1.0 / 23.0;
+  t = t * z + 1.0 / 21.0;
+  t = t * z + 1.0 / 19.0;
+  t = t * z + 1.0 / 17.0;
+  t = t * z + 1.0 / 15.0;
+  t = t * z + 1.0 / 13.0;
+  t = t * z + 1.0 / 11.0;
+  t = t * z + 1.0 / 9.0;
+  t = t * z + 1.0 / 7.0;
+  t = t * z + 1.0 / 5.0;
+  t = t * z + 1.0 / 3.0;
+  t = t * z + 1.0;
+  double lm = 2.0 * s * t;
+  return (double)e * 0.69314718055994530942 + lm;
+}
+
+/* sin/cos of 2 pi u: quadrant k = floor(4u) (exact), theta = frac(4u) pi/2,
+ * Taylor series in theta^2 to degree 25 (error < 1e-19 for theta <= pi/2). */
+void orc_det_sincos_2pi(double u, double *s, double *c) {
+  double q = u * 4.0;
+  int k = (int)q;
+  double f = q - (double)k;
+  double th = f * 1.57079632679489661923;
+  double z = th * th;
+  double sn = -1.0 / 15511210043330985984000000.0; /* -1/25! */
+  sn = sn * z + 1.0 / 25852016738884976640000.0;    /*  1/23! */
+  sn = sn * z - 1.0 / 51090942171709440000.0;       /* -1/21! */
+  sn = sn * z + 1.0 / 121645100408832000.0;         /*  1/19! */
+  sn = sn * z - 1.0 / 355687428096000.0;            /* -1/17! */
+  sn = sn * z + 1.0 / 1307674368000.0;              /*  1/15! */
+  sn = sn * z - 1.0 / 6227020800.0;                 /* -1/13! */
+  sn = sn * z + 1.0 / 39916800.0;                   /*  1/11! */
+  sn = sn * z - 1.0 / 362880.0;                     /* -1/9! */
+  sn = sn * z + 1.0 / 5040.0;                       /*  1/7! */
+  sn = sn * z - 1.0 / 120.0;                        /* -1/5! */
+  sn = sn * z + 1.0 / 6.0;                          /*  1/3! */
+  sn = sn * z - 1.0;
+  sn = -(sn * th);
+  double cs = 1.0 / 620448401733239439360000.0;     /*  1/24! */
+  cs = cs * z - 1.0 / 1124000727777607680000.0;     /* -1/22! */
+  cs = cs * z + 1.0 / 2432902008176640000.0;        /*  1/20! */
+  cs = cs * z - 1.0 / 6402373705728000.0;           /* -1/18! */
+  cs = cs * z + 1.0 / 20922789888000.0;             /*  1/16! */
+  cs = cs * z - 1.0 / 87178291200.0;                /* -1/14! */
+  cs = cs * z + 1.0 / 479001600.0;                  /*  1/12! */
+  cs = cs * z - 1.0 / 3628800.0;                    /* -1/10! */
+  cs = cs * z + 1.0 / 40320.0;                      /*  1/8! */
+  cs = cs * z - 1.0 / 720.0;                        /* -1/6! */
+  cs = cs * z + 1.0 / 24.0;                         /*  1/4! */
+  cs = cs * z - 0.5;                                /* -1/2! */
+  cs = cs * z + 1.0;
+  switch (k & 3) {
+    case 0: *s = sn; *c = cs; break;
+    case 1: *s = cs; *c = -sn; break;
+    case 2: *s = -sn; *c = -cs; break;
+    default: *s = -cs; *c = sn; break;
+  }
+}
+
+/* Closed-loop tracking error of the double integrator at the reference's
+ * offset step dt = 0.05 s (mainPUMP.cu:60), one axis at a time:
+ *   a_t   = w_t - (KP p_t + KD v_t),   w_t ~ N(0, SIGMA_W^2)
+ *   p_t+1 = (p_t + DT v_t) + H2 a_t,    v_t+1 = v_t + DT a_t,   p_0 = v_0 = 0
+ * with DT = 0.05, H2 = DT^2/2 = 0.00125, KP = 16, KD = 5.6 (a PD tracking
+ * law, closed-loop spectral radius 0.860) and SIGMA_W = 4, giving a
+ * stationary position standard deviation of 0.069 before the noise
+ * multiplier.  Noise for particle p at step t uses Philox counter
+ * (p, t, 0, 0) and key (seed lo, seed hi); its four 32-bit words give
+ * u = (word + 0.5) 2^-32 and Box-Muller pairs (u0,u1) -> axes x,y and
+ * (u2,u3) -> axis z. */
+#define ORC_DT 0.05
+#define ORC_H2 0.00125
+#define ORC_KP 16.0
+#define ORC_KD 5.6
+#define ORC_SIGMA_W 4.0
+
+static void orc_gauss3(uint64_t seed, uint32_t p, uint32_t t, double z[3]) {
+  uint32_t ctr[4] = {p, t, 0u, 0u};
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t o[4];
+  orc_philox4x32_10(ctr, key, o);
+  const double sc = 2.3283064365386962890625e-10; /* 2^-32 */
+  double u0 = ((double)o[0] + 0.5) * sc, u1 = ((double)o[1] + 0.5) * sc;
+  double u2 = ((double)o[2] + 0.5) * sc, u3 = ((double)o[3] + 0.5) * sc;
+  double r0 = sqrt(-2.0 * orc_det_log(u0));
+  double r1 = sqrt(-2.0 * orc_det_log(u2));
+  double s0, c0, s1, c1;
+  orc_det_sincos_2pi(u1, &s0, &c0);
+  orc_det_sincos_2pi(u3, &s1, &c1);
+  z[0] = r0 * c0;
+  z[1] = r0 * s0;
+  z[2] = r1 * c1;
+}
+
+void orc_particle_tables(uint64_t seed, int P, int T, float *tmajor, float *pmajor) {
+  for (int p = 0; p < P; ++p) {
+    double pos[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
+    for (int t = 0; t < T; ++t) {
+      for (int d = 0; d < 3; ++d) {
+        float v = (float)pos[d];
+        if (tmajor) tmajor[((long long)t * P + p) * 3 + d] = v;
+        if (pmajor) pmajor[((long long)p * T + t) * 3 + d] = v;
+      }
+      double z[3];
+      orc_gauss3(seed, (uint32_t)p, (uint32_t)t, z);
+      for (int d = 0; d < 3; ++d) {
+        double a = ORC_SIGMA_W * z[d] - (ORC_KP * pos[d] + ORC_KD * vel[d]);
+        double pn = (pos[d] + ORC_DT * vel[d]) + ORC_H2 * a;
+        double vn = vel[d] + ORC_DT * a;
+        pos[d] = pn;
+        vel[d] = vn;
+      }
+    }
+  }
+}
+
+void orc_particle_cov(int T, double *cov) {
+  /* A_cl = [[1 - H2 KP, DT - H2 KD], [-DT KP, 1 - DT KD]], G = [H2, DT] SIGMA_W */
+  const double a00 = 1.0 - ORC_H2 * ORC_KP, a01 = ORC_DT - ORC_H2 * ORC_KD;
+  const double a10 = -(ORC_DT * ORC_KP), a11 = 1.0 - ORC_DT * ORC_KD;
+  const double g0 = ORC_H2 * ORC_SIGMA_W, g1 = ORC_DT * ORC_SIGMA_W;
+  double spp = 0, spv = 0, svv = 0;
+  for (int t = 0; t < T; ++t) {
+    cov[t * 3 + 0] = spp; cov[t * 3 + 1] = spv; cov[t * 3 + 2] = svv;
+    /* S' = A S A^T + G G^T */
+    double m00 = a00 * spp + a01 * spv, m01 = a00 * spv + a01 * svv;
+    double m10 = a10 * spp + a11 * spv, m11 = a10 * spv + a11 * svv;
+    double npp = m00 * a00 + m01 * a01 + g0 * g0;
+    double npv = m00 * a10 + m01 * a11 + g0 * g1;
+    double nvv = m10 * a10 + m11 * a11 + g1 * g1;
+    spp = npp; spv = npv; svv = nvv;
+  }
+}
+
+/* ======================================================================
+ * 2pBVP (2pBVP.cu)
+ * ==================================================================== */
+/* 2pBVP.cu:3, `const float g = -9.81;` */
+#define ORC_G ((float)-9.81)
+
+float orc_cost(float tau, const float *x0, const float *x1) {
+  const float g = ORC_G;
+  double s;
+  s = 12 * p2f(x0[0]);
+  s = s + 12 * p2f(x0[2]);
+  s = s + 12 * p2f(x0[1]);
+  s = s + 12 * p2f(x1[0]);
+  s = s + 12 * p2f(x1[2]);
+  s = s - (double)(24 * x0[1] * x1[1]);
+  s = s + 12 * p2f(x1[1]);
+  s = s + (double)(12 * x0[4] * x0[1] * tau);
+  s = s + (double)(12 * x0[1] * x1[4] * tau);
+  s = s - (double)(12 * x0[3] * x1[0] * tau);
+  s = s - (double)(12 * x1[3] * x1[0] * tau);
+  s = s - (double)(12 * x0[5] * x1[2] * tau);
+  s = s - (double)(12 * x1[5] * x1[2] * tau);
+  s = s - (double)(12 * x0[4] * x1[1] * tau);
+  s = s - (double)(12 * x1[4] * x1[1] * tau);
+  const double t2 = p2f(tau), t3 = p3f(tau), t4 = p4f(tau);
+  s = s + (4 * p2f(x0[4])) * t2;
+  s = s + (4 * p2f(x0[3])) * t2;
+  s = s + (4 * p2f(x0[5])) * t2;
+  s = s + (double)(4 * x0[4] * x1[4]) * t2;
+  s = s + (4 * p2f(x1[4])) * t2;
+  s = s + (double)(4 * x0[3] * x1[3]) * t2;
+  s = s + (4 * p2f(x1[3])) * t2;
+  s = s + (double)(4 * x0[5] * x1[5]) * t2;
+  s = s + (4 * p2f(x1[5])) * t2;
+  s = s + (double)(2 * g * x0[5]) * t3;
+  s = s - (double)(2 * g * x1[5]) * t3;
+  s = s + t4;
+  s = s + p2f(g) * t4;
+  s = s + (double)(12 * x0[0] * (-2 * x1[0] + (x0[3] + x1[3]) * tau));
+  s = s + (double)(12 * x0[2] * (-2 * x1[2] + (x0[5] + x1[5]) * tau));
+  return (float)((1 / t3) * s);
+}
+
+float orc_dcost(float tau, const float *x0, const float *x1) {
+  const float dtau = (float)0.000001;
+  return (orc_cost(tau + dtau / 2, x0, x1) - orc_cost(tau - dtau / 2, x0, x1)) / dtau;
+}
+
+/* The halving loop of 2pBVP.cu:78-80 has no bound in the reference; it ends
+ * for every state pair with distinct positions.  It is bounded here at 160
+ * halvings (tl below 1e-50 underflows to 0 long before). */
+float orc_topt_bisection(const float *x0, const float *x1, float tmax, int *evals) {
+  int ev = 2;
+  float tu = tmax;
+  if (orc_dcost(tmax, x0, x1) < 0) {
+    if (evals) *evals = ev;
+    return tmax;
+  }
+  float tl = (float)0.01;
+  int halvings = 0;
+  while (ev += 2, orc_dcost(tl, x0, x1) > 0 && halvings < 160) {
+    tl = tl / 2;
+    ++halvings;
+  }
+  float topt = 0;
+  float dcval = 1;
+  int maxItrs = 50;
+  int itr = 0;
+  while ((double)fabsf(dcval) > 0.0001 && itr < maxItrs && ++itr) {
+    topt = (tu + tl) / 2;
+    dcval = orc_dcost(topt, x0, x1);
+    ev += 2;
+    if (dcval > 0)
+      tu = topt;
+    else
+      tl = topt;
+  }
+  if (evals) *evals = ev;
+  return topt;
+}
+
+void orc_path_point(float t, float tau, const float *x0, const float *x1, float *x) {
+  const double t2 = p2f(t), t3 = p3f(t), u2 = p2f(tau), u3 = p3f(tau);
+  /* x[0], x[1]: 2pBVP.cu:119-122 */
+  for (int k = 0; k < 2; ++k) {
+    const int a = k, b = k + 3;
+    double r = (double)(t * x0[b] + x0[a]);
+    r = r + (t3 * (double)(2 * x0[a] - 2 * x1[a] + (x0[b] + x1[b]) * tau)) / u3;
+    r = r - (t2 * (double)(3 * x0[a] - 3 * x1[a] + (2 * x0[b] + x1[b]) * tau)) / u2;
+    x[k] = (float)r;
+  }
+  /* x[2]: 2pBVP.cu:123-124 */
+  {
+    double r = (double)(t * x0[5]) * u3 + (double)x0[2] * u3;
+    double q1 = -3. * x0[2] + 3. * x1[2] - 2. * x0[5] * tau - 1. * x1[5] * tau;
+    r = r + (t2 * (double)tau) * q1;
+    double q2 = 2. * x0[2] - 2. * x1[2] + (double)((x0[5] + x1[5]) * tau);
+    r = r + t3 * q2;
+    x[2] = (float)(r / u3);
+  }
+  /* x[3], x[4]: 2pBVP.cu:125-129 */
+  for (int k = 0; k < 2; ++k) {
+    const int a = k, b = k + 3;
+    float f1 = -(2 * t * (3 * x0[a] - 3 * x1[a] + x1[b] * tau));
+    double r = (double)f1 / u2;
+    r = r + (3 * t2 * (double)(2 * x0[a] - 2 * x1[a] + x1[b] * tau)) / u3;
+    double inner = 3 * t2 - (double)(4 * t * tau) + u2;
+    r = r + ((double)x0[b] * inner) / u2;
+    x[3 + k] = (float)r;
+  }
+  /* x[5]: 2pBVP.cu:130-131 */
+  {
+    double r = (double)x0[5] * u3;
+    double q1 = -6. * x0[2] + 6. * x1[2] - 4. * x0[5] * tau - 2. * x1[5] * tau;
+    r = r + (double)(t * tau) * q1;
+    double q2 = 6. * x0[2] - 6. * x1[2] + 3. * x0[5] * tau + 3. * x1[5] * tau;
+    r = r + t2 * q2;
+    x[5] = (float)(r / u3);
+  }
+}
+
+float orc_find_discretized_path(float *split, const float *x0, const float *x1, int numDisc) {
+  float topt = orc_topt_bisection(x0, x1, 5, NULL);
+  float dt = topt / numDisc;
+  for (int d = 0; d < ORC_DIM; ++d) {
+    split[d] = x0[d];
+    split[d + numDisc * ORC_DIM] = x1[d];
+  }
+  for (int i = 1; i < numDisc; ++i) orc_path_point(dt * i, topt, x0, x1, &split[i * ORC_DIM]);
+  return topt;
+}
+
+float orc_find_optimal_path(float dt, float *split, int cap, const float *xs, int n, int *len) {
+  float tmax = 5;
+  float toff = 0, topt = 0, t = 0, ttotal = 0;
+  int Tprev = 0;
+  for (int i = 0; i < n - 1; ++i) {
+    const float *x0 = &xs[i * ORC_DIM], *x1 = &xs[(i + 1) * ORC_DIM];
+    topt = orc_topt_bisection(x0, x1, tmax, NULL);
+    int T = (int)((topt - toff) / dt + 1);
+    if (T > 0 && Tprev + T > cap) {
+      *len = -1;
+      return ttotal;
+    }
+    for (int tidx = 0; tidx < T; ++tidx) {
+      t = dt * tidx + toff;
+      orc_path_point(t, topt, x0, x1, &split[(Tprev + tidx) * ORC_DIM]);
+    }
+    Tprev += T;
+    toff = (t - topt) + dt;
+    ttotal += topt;
+  }
+  *len = Tprev;
+  return ttotal;
+}
+
+void orc_bvp_pairs(int N, const float *samples, float tmax, float *copts, float *topts) {
+#pragma omp parallel for schedule(dynamic, 64)
+  for (long long tid = 0; tid < (long long)N * N; ++tid) {
+    int i = (int)(tid / N), j = (int)(tid % N);
+    if (i == j) continue;
+    long long idx = (long long)i * (N - 1) + j;
+    if (i < j) idx--;
+    float tp = orc_topt_bisection(&samples[i * ORC_DIM], &samples[j * ORC_DIM], tmax, NULL);
+    topts[idx] = tp;
+    copts[idx] = orc_cost(tp, &samples[i * ORC_DIM], &samples[j * ORC_DIM]);
+  }
+}
+
+/* ======================================================================
+ * Sampler (sampler.cu)
+ * ==================================================================== */
+float orc_halton(int n, int b) {
+  float hn = 0;
+  int n0 = n;
+  float f = 1 / ((float)b);
+  while (n0 > 0) {
+    float n1 = (float)(n0 / b);
+    int r = (int)(n0 - n1 * b);
+    hn += f * r;
+    f = f / b;
+    n0 = (int)n1;
+  }
+  return hn;
+}
+
+void orc_halton_samples(int N, float *samples, const float *init, const float *goal,
+                        const float *lo, const float *hi) {
+  static const int bases[] = {2, 3, 5, 7, 11, 13};
+  for (int d = 0; d < ORC_DIM; ++d)
+    for (int n = 0; n < N; ++n)
+      samples[n * ORC_DIM + d] = orc_halton(n, bases[d]) * (hi[d] - lo[d]) + lo[d];
+  for (int d = 0; d < ORC_DIM; ++d) {
+    samples[d] = init[d];
+    samples[(N - 1) * ORC_DIM + d] = goal[d];
+  }
+}
+
+void orc_sample_free(int N, const float *samples, int nobs, const float *obs, uint8_t *isFree) {
+  for (int node = 0; node < N; ++node) {
+    const float *p = &samples[node * ORC_DIM];
+    uint8_t fr = 1;
+    for (int o = 0; o < nobs && fr; ++o) {
+      int notFree = 1;
+      for (int d = 0; d < 3; ++d) {
+        notFree = notFree && p[d] > obs[o * 12 + d] && p[d] < obs[o * 12 + 6 + d];
+        if (!notFree) break;
+      }
+      if (notFree) fr = 0;
+    }
+    isFree[node] = fr;
+  }
+}
+
+/* ======================================================================
+ * Roadmap (mainPUMP.cu)
+ * ==================================================================== */
+static int cmp_float(const void *a, const void *b) {
+  float x = *(const float *)a, y = *(const float *)b;
+  return (x > y) - (x < y);
+}
+
+float orc_select_kth(long long count, const float *v, long long k) {
+  float *c = (float *)malloc(sizeof(float) * (size_t)count);
+  memcpy(c, v, sizeof(float) * (size_t)count);
+  qsort(c, (size_t)count, sizeof(float), cmp_float);
+  float r = c[k];
+  free(c);
+  return r;
+}
+
+long long orc_build_edges(int N, const float *copts, const float *topts, float rn, int *src,
+                          int *dst, float *coptE, float *toptE) {
+  long long e = 0, idx = 0;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      if (j == i) continue;
+      if (copts[idx] < rn) {
+        if (src) src[e] = i;
+        if (dst) dst[e] = j;
+        if (coptE) coptE[e] = copts[idx];
+        if (toptE) toptE[e] = topts[idx];
+        ++e;
+      }
+      ++idx;
+    }
+  return e;
+}
+
+void orc_discretize_edges(long long E, const int *src, const int *dst, const float *samples,
+                          int numDisc, float *disc) {
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long e = 0; e < E; ++e)
+    orc_find_discretized_path(&disc[e * (numDisc + 1) * ORC_DIM], &samples[src[e] * ORC_DIM],
+                              &samples[dst[e] * ORC_DIM], numDisc);
+}
+
+void orc_heuristic(int N, const float *samples, const float *goal, float *h) {
+  for (int i = 0; i < N - 1; ++i) {
+    float topt = orc_topt_bisection(&samples[i * ORC_DIM], goal, 5, NULL);
+    h[i] = orc_cost(topt, &samples[i * ORC_DIM], goal);
+  }
+  h[N - 1] = 0;
+}
+
+/* ======================================================================
+ * Collision check (collisionCheck.cu)
+ * ==================================================================== */
+static int broadphase_valid(const float *bbMin, const float *bbMax, const float *o) {
+  for (int d = 0; d < 3; ++d)
+    if (bbMax[d] <= o[d] || o[6 + d] <= bbMin[d]) return 1;
+  return 0;
+}
+
+static int face_contains_projection(const float *v, const float *w, float lambda, int j,
+                                    const float *o) {
+  for (int d = 0; d < 3; ++d) {
+    float projection = v[d] + (w[d] - v[d]) * lambda;
+    if (d != j && !(o[d] <= projection && projection <= o[6 + d])) return 0;
+  }
+  return 1;
+}
+
+static int motion_valid_q(const float *v, const float *w, const float *o) {
+  for (int d = 0; d < 3; ++d) {
+    float lambda;
+    float v_to_w = w[d] - v[d];
+    if (v[d] < o[d])
+      lambda = (o[d] - v[d]) / v_to_w;
+    else
+      lambda = (o[6 + d] - v[d]) / v_to_w;
+    if (face_contains_projection(v, w, lambda, d, o)) return 0;
+  }
+  return 1;
+}
+
+int orc_is_motion_valid(const float *v, const float *w, int nobs, const float *obs) {
+  float bbMin[3], bbMax[3];
+  for (int d = 0; d < 3; ++d) {
+    if (v[d] > w[d]) { bbMin[d] = w[d]; bbMax[d] = v[d]; }
+    else { bbMin[d] = v[d]; bbMax[d] = w[d]; }
+  }
+  for (int o = 0; o < nobs; ++o) {
+    const float *ob = &obs[o * 12];
+    if (!broadphase_valid(bbMin, bbMax, ob))
+      if (!motion_valid_q(v, w, ob)) return 0;
+  }
+  return 1;
+}
+
+void orc_free_edges(long long E, int numDisc, const float *disc, int nobs, const float *obs,
+                    uint8_t *isFreeEdge) {
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long e = 0; e < E; ++e) {
+    int ok = 1;
+    for (int i = 0; i < numDisc && ok; ++i) {
+      const float *v = &disc[(e * (numDisc + 1) + i) * ORC_DIM];
+      ok = orc_is_motion_valid(v, v + ORC_DIM, nobs, obs);
+    }
+    isFreeEdge[e] = (uint8_t)ok;
+  }
+}
+
+/* ======================================================================
+ * Half-spaces (hsmc.cu, bvls.cu:259-273)
+ * ==================================================================== */
+void orc_cache_halfspaces(long long E, int W, const float *disc, const uint8_t *isFreeEdge,
+                          int nobs, const float *obs, int maxHS, float maxd2, float *as,
+                          float *bs, int *count) {
+  const long long nhs = E * W * maxHS;
+  for (long long i = 0; i < nhs; ++i) {
+    as[i * 3 + 0] = -1; as[i * 3 + 1] = -1; as[i * 3 + 2] = -1;
+    bs[i] = 1111;
+  }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (long long wp = 0; wp < E * W; ++wp) {
+    if (!isFreeEdge[wp / W]) continue;
+    const float *pos = &disc[wp * ORC_DIM], *vel = pos + 3;
+    long long hsIdx = wp * maxHS;
+    int stored = 0;
+    for (int o = 0; o < nobs; ++o) {
+      const float *l = &obs[o * 12], *u = &obs[o * 12 + 6];
+      float x[3];
+      for (int d = 0; d < 3; ++d) {
+        if (pos[d] <= l[d]) x[d] = l[d];
+        else if (pos[d] >= u[d]) x[d] = u[d];
+        else x[d] = pos[d];
+      }
+      for (int d = 0; d < 3; ++d) x[d] = x[d] - pos[d];
+      float d2 = 0;
+      for (int d = 0; d < 3; ++d) d2 += x[d] * x[d];
+      if (d2 > maxd2) continue;
+      float xdotv = 0, vdotv = 0;
+      for (int d = 0; d < 3; ++d) {
+        xdotv += x[d] * vel[d];
+        vdotv += vel[d] * vel[d];
+      }
+      if (vdotv == 0) vdotv = (float)1e-5;
+      float dotratio = xdotv / vdotv;
+      for (int d = 0; d < 3; ++d) x[d] = x[d] - dotratio * vel[d];
+      float xdotx = 0;
+      for (int d = 0; d < 3; ++d) {
+        as[hsIdx * 3 + d] = x[d];
+        xdotx += x[d] * x[d];
+      }
+      bs[hsIdx] = xdotx;
+      stored++;
+      hsIdx++;
+      if (stored == maxHS) break;
+    }
+    count[wp] = stored;
+  }
+}
+
+/* ======================================================================
+ * HSMC propagation and CP (PUMP.cu:613-655, 745-758)
+ * ==================================================================== */
+void orc_hsmc_propagate(int numNew, int W, const int *wfEdge, const int *wfPrev, int base,
+                        const float *as, const float *bs, const float *times, const float *topts,
+                        float dt, int maxHS, const float *offsetsT, float offsetMult, int Pmc,
+                        uint8_t *valid, int P, float *pathCP) {
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int w = 0; w < numNew; ++w) {
+    const int edge = wfEdge[w], prev = wfPrev[w];
+    const long long pathIdx = (long long)base + w;
+    int collisions = 0;
+    for (int p = 0; p < P; ++p) {
+      int vp = valid[(long long)prev * P + p];
+      float dtLocal = topts[edge] / (W - 1);
+      long long hsHead = (long long)edge * W * maxHS;
+      for (int i = 0; i < W; ++i) {
+        float time = times[prev] + i * dtLocal;
+        int dtIdx = (int)(time / dt);
+        for (int o = 0; o < maxHS; ++o) {
+          const long long h = hsHead + (long long)i * maxHS + o;
+          if (bs[h] >= 1000) continue;
+          float LHS = 0;
+          for (int d = 0; d < 3; ++d)
+            LHS += offsetsT[((long long)dtIdx * Pmc + p) * 3 + d] * as[h * 3 + d];
+          vp &= (LHS * offsetMult < bs[h]);
+        }
+      }
+      valid[pathIdx * P + p] = (uint8_t)vp;
+      if (!vp) collisions++;
+    }
+    if (pathCP) pathCP[pathIdx] = ((float)collisions) / P;
+  }
+}
+
+/* ======================================================================
+ * Monte Carlo CP (collisionProbability.cu:39-92)
+ * ==================================================================== */
+int orc_mccp(const float *path, int T, const float *pmajor, int T_stride, float offsetMult,
+             int nobs, const float *obs, int Pmc, float *cp) {
+  int hits = 0;
+#pragma omp parallel for reduction(+ : hits) schedule(dynamic, 64)
+  for (int p = 0; p < Pmc; ++p) {
+    float v[3], w[3];
+    int coll = 0;
+    for (int t = 0; t < T - 2 && !coll; ++t) {
+      for (int d = 0; d < 3; ++d) {
+        v[d] = path[t * ORC_DIM + d] + pmajor[((long long)p * T_stride + t) * 3 + d] * offsetMult;
+        w[d] = path[(t + 1) * ORC_DIM + d] +
+               pmajor[((long long)p * T_stride + t + 1) * 3 + d] * offsetMult;
+      }
+      if (!orc_is_motion_valid(v, w, nobs, obs)) coll = 1;
+    }
+    hits += coll;
+  }
+  if (cp) *cp = ((float)hits) / ((float)Pmc);
+  return hits;
+}
+
+/* ======================================================================
+ * Frontier compaction (GMT.cu:48-76, 166-176)
+ * ==================================================================== */
+int orc_frontier_compact(int N, const uint8_t *flags, int *active) {
+  int n = 0;
+  for (int i = 0; i < N; ++i)
+    if (flags[i]) active[n++] = i;
+  return n;
+}
+
+/* ======================================================================
+ * Whole query (mainPUMP.cu:248-687, PUMP.cu:3-607)
+ * ==================================================================== */
+static int build_xs(int pathIdx, const int *pathPrev, const int *pathNode, const float *samples,
+                    float *xs, int *nodes, int cap) {
+  /* PUMP.cu:377-386: nodes from the goal back to init, stored init first */
+  int n = 0, p = pathIdx;
+  while (p != -2) { ++n; p = pathPrev[p]; }
+  if (n > cap) return -1;
+  p = pathIdx;
+  for (int k = n - 1; k >= 0; --k) {
+    int node = pathNode[p];
+    if (nodes) nodes[k] = node;
+    for (int d = 0; d < ORC_DIM; ++d) xs[k * ORC_DIM + d] = samples[node * ORC_DIM + d];
+    p = pathPrev[p];
+  }
+  return n;
+}
+
+typedef struct { float cost; int idx; } cost_idx;
+static int cmp_cost_idx(const void *a, const void *b) {
+  const cost_idx *x = (const cost_idx *)a, *y = (const cost_idx *)b;
+  if (x->cost < y->cost) return -1;
+  if (x->cost > y->cost) return 1;
+  return (x->idx > y->idx) - (x->idx < y->idx);
+}
+
+int orc_plan(const orc_problem *pb, orc_result *res) {
+  const int N = pb->N, numDisc = pb->numDisc, W = numDisc + 1, P = pb->P, Pmc = pb->Pmc;
+  const int nobs = pb->numObs;
+  const float *obs = pb->obstacles;
+  const float dt = (float)0.05, lambda = (float)0.5, epsCost = (float)0.0002,
+              epsCP = (float)0.0002;
+  const int numBuckets = 2;
+  const float maxd2 = (float)(0.1 * pb->offsetMult * pb->offsetMult); /* mainPUMP.cu:201 */
+  const int maxHS = nobs > 5 ? 5 : nobs;                              /* mainPUMP.cu:241 */
+  memset(res->wavefront_sizes ? (void *)res->wavefront_sizes : (void *)&res->status, 0,
+         res->wavefront_sizes ? sizeof(int) * 32 : sizeof(int));
+  res->status = 0;
+  res->wf_trace_len = 0;
+
+  /* samples (mainPUMP.cu:249-250) */
+  float *samples = (float *)malloc(sizeof(float) * N * ORC_DIM);
+  if (pb->samples) memcpy(samples, pb->samples, sizeof(float) * N * ORC_DIM);
+  else orc_halton_samples(N, samples, pb->init, pb->goal, pb->lo, pb->hi);
+
+  /* pair BVPs and rn (mainPUMP.cu:261-304) */
+  const long long npairs = (long long)N * (N - 1);
+  float *copts = (float *)malloc(sizeof(float) * npairs);
+  float *topts = (float *)malloc(sizeof(float) * npairs);
+  orc_bvp_pairs(N, samples, 5, copts, topts);
+  const long long rnIdx = (long long)((N - 1) * (N) * (float)0.05);
+  const float rn = orc_select_kth(npairs, copts, rnIdx);
+  res->rn = rn;
+
+  /* edges (mainPUMP.cu:313-346) */
+  const long long E = orc_build_edges(N, copts, topts, rn, NULL, NULL, NULL, NULL);
+  res->numEdges = E;
+  int *src = (int *)malloc(sizeof(int) * (E + 1)), *dst = (int *)malloc(sizeof(int) * (E + 1));
+  float *coptE = (float *)malloc(sizeof(float) * (E + 1));
+  float *toptE = (float *)malloc(sizeof(float) * (E + 1));
+  orc_build_edges(N, copts, topts, rn, src, dst, coptE, toptE);
+  free(copts);
+  free(topts);
+  float *disc = (float *)malloc(sizeof(float) * (E + 1) * W * ORC_DIM);
+  orc_discretize_edges(E, src, dst, samples, numDisc, disc);
+  float *h = (float *)malloc(sizeof(float) * N);
+  orc_heuristic(N, samples, pb->goal, h);
+
+  /* go-adjacency in (i, j asc) order and edge lookup (mainPUMP.cu:338, 379-392) */
+  int *goStart = (int *)calloc(N + 1, sizeof(int));
+  for (long long e = 0; e < E; ++e) goStart[src[e] + 1]++;
+  for (int i = 0; i < N; ++i) goStart[i + 1] += goStart[i];
+  /* edges are already sorted by (src, dst): edge e is the k-th go edge of src[e] */
+
+  /* online (mainPUMP.cu:428-497) */
+  uint8_t *isFreeS = (uint8_t *)malloc(N);
+  orc_sample_free(N, samples, nobs, obs, isFreeS);
+  uint8_t *isFreeE = (uint8_t *)malloc(E + 1);
+  orc_free_edges(E, numDisc, disc, nobs, obs, isFreeE);
+  float *as = (float *)malloc(sizeof(float) * ((E * W * maxHS) * 3 + 1));
+  float *bs = (float *)malloc(sizeof(float) * (E * W * maxHS + 1));
+  int *cnt = (int *)calloc(E * W + 1, sizeof(int));
+  orc_cache_halfspaces(E, W, disc, isFreeE, nobs, obs, maxHS, maxd2, as, bs, cnt);
+  free(cnt);
+
+  /* exploration state (mainPUMP.cu:623-681) */
+  const int maxPathCount = (int)(2 * N * sqrt((double)N));
+  int *Ptab = (int *)malloc(sizeof(int) * (size_t)N * N);
+  int *Pcounts = (int *)calloc(N, sizeof(int));
+  int *pathPrev = (int *)calloc(maxPathCount + 1, sizeof(int));
+  int *pathNode = (int *)calloc(maxPathCount + 1, sizeof(int));
+  float *pathCost = (float *)calloc(maxPathCount + 1, sizeof(float));
+  float *pathTime = (float *)calloc(maxPathCount + 1, sizeof(float));
+  float *pathCP = (float *)calloc(maxPathCount + 1, sizeof(float));
+  float *d_pathTime = (float *)calloc(maxPathCount + 1, sizeof(float));
+  float *d_pathCP = (float *)malloc(sizeof(float) * (maxPathCount + 1));
+  int *G = (int *)malloc(sizeof(int) * numBuckets * (size_t)maxPathCount);
+  int sizeG[2] = {0, 0};
+  uint8_t *valid = (uint8_t *)malloc((size_t)P * (maxPathCount + 1));
+  int *wfPrev = (int *)malloc(sizeof(int) * (maxPathCount + 2));
+  int *wfNode = (int *)malloc(sizeof(int) * (maxPathCount + 2));
+  int *wfEdge = (int *)malloc(sizeof(int) * (maxPathCount + 2));
+  int *PnewCount = (int *)malloc(sizeof(int) * N);
+  for (size_t i = 0; i < (size_t)N * N; ++i) Ptab[i] = -1;
+  for (int i = 0; i < numBuckets * maxPathCount; ++i) G[i] = -1;
+  memset(valid, 1, (size_t)P * (maxPathCount + 1));
+  for (int i = 0; i <= maxPathCount; ++i) d_pathCP[i] = 1;
+
+  /* PUMP.cu:10-35 */
+  const float cpTarget = pb->cpTarget;
+  const float dr = lambda * rn;
+  const float cpMinSoln = cpTarget / pb->cpFactor;
+  const float cpCutoff = cpTarget * pb->cpFactor;
+  const int initIdx = 0, goalIdx = N - 1;
+  int numPaths = 1, Gidx = 0;
+  int goalCondition = 0, goalConditionNext = 0, emptyOpenSet = 0;
+  Ptab[initIdx * N + 0] = 0;
+  Pcounts[initIdx]++;
+  pathPrev[0] = -2; pathNode[0] = initIdx; pathCost[0] = 0; pathCP[0] = 0; pathTime[0] = 0;
+  sizeG[Gidx]++;
+  G[0] = 0;
+  float costThreshold = h[initIdx];
+  const int maxItrs = 20;
+  int itrs = 0, numConsidered = 0;
+  int status = 0;
+
+  while (itrs < maxItrs && !goalCondition && !emptyOpenSet) {
+    ++itrs;
+    if (goalConditionNext) goalCondition = 1;
+    int numNew = 0;
+    int overflow = 0;
+    /* PUMP.cu:47-66 */
+    for (int g = 0; g < sizeG[Gidx] && !overflow; ++g) {
+      int prev = G[Gidx * maxPathCount + g];
+      G[Gidx * maxPathCount + g] = -1;
+      int nodePrev = pathNode[prev];
+      for (int e = goStart[nodePrev]; e < goStart[nodePrev + 1]; ++e) {
+        int nodeNext = dst[e];
+        if (!isFreeE[e] || !isFreeS[nodeNext]) continue;
+        wfPrev[numNew] = prev; wfNode[numNew] = nodeNext; wfEdge[numNew] = e;
+        numNew++;
+        if (numNew > maxPathCount) { overflow = 1; break; }
+      }
+    }
+    if (overflow) { status = 1; break; }
+    if (res->wavefront_sizes && itrs <= 32) res->wavefront_sizes[itrs - 1] = numNew;
+    if (numNew == 0) break;
+    if (numPaths + numNew >= maxPathCount) { status = 1; break; }
+    if (res->wf_trace) {
+      for (int i = 0; i < numNew && res->wf_trace_len + 2 <= res->wf_trace_cap; ++i) {
+        res->wf_trace[res->wf_trace_len++] = wfPrev[i];
+        res->wf_trace[res->wf_trace_len++] = wfEdge[i];
+      }
+    }
+    sizeG[Gidx] = 0;
+    numConsidered += numNew;
+
+    /* PUMP.cu:94-160: device propagation reads the device copy of path times */
+    orc_hsmc_propagate(numNew, W, wfEdge, wfPrev, numPaths, as, bs, d_pathTime, toptE, dt, maxHS,
+                       pb->tmajor, pb->offsetMult, Pmc, valid, P, d_pathCP);
+    for (int i = 0; i < numNew; ++i) pathCP[numPaths + i] = d_pathCP[numPaths + i];
+
+    /* PUMP.cu:164-167 */
+    for (int i = 0; i < numNew; ++i) {
+      pathTime[numPaths + i] = pathTime[wfPrev[i]] + toptE[wfEdge[i]];
+      pathCost[numPaths + i] = pathCost[wfPrev[i]] + coptE[wfEdge[i]];
+    }
+    /* PUMP.cu:171-185 */
+    for (int i = 0; i < N; ++i) PnewCount[i] = 0;
+    for (int i = 0; i < numNew; ++i) {
+      int node = wfNode[i], pathIdx = numPaths + i;
+      if (pathCP[pathIdx] > cpCutoff) { wfNode[i] = -1; continue; }
+      Ptab[node * N + Pcounts[node] + PnewCount[node]] = pathIdx;
+      PnewCount[node]++;
+    }
+    /* PUMP.cu:188-218 */
+    for (int i = 0; i < numNew; ++i) {
+      int node = wfNode[i];
+      if (wfNode[i] == -1 || node == goalIdx) continue;
+      int pathIdx = numPaths + i;
+      for (int j = 0; j < Pcounts[node] + PnewCount[node]; ++j) {
+        int cmp = Ptab[node * N + j];
+        if (cmp == pathIdx) continue;
+        if (pathCP[cmp] < epsCP + pathCP[pathIdx] && pathCost[cmp] < epsCost + pathCost[pathIdx]) {
+          if (pathCP[cmp] + epsCP >= pathCP[pathIdx] &&
+              pathCost[cmp] + epsCost >= pathCost[pathIdx] && pathIdx < cmp)
+            continue;
+          wfNode[i] = -1;
+          break;
+        }
+      }
+    }
+    /* PUMP.cu:221-256 */
+    int numValid = 0;
+    for (int i = 0; i < numNew; ++i) {
+      int node = wfNode[i], pathIdx = numPaths + i;
+      if (wfNode[i] == -1 || wfNode[i] == 0) { wfNode[i] = -1; continue; }
+      int st = numPaths + numValid;
+      pathCP[st] = pathCP[pathIdx];
+      pathTime[st] = pathTime[pathIdx];
+      pathCost[st] = pathCost[pathIdx];
+      memmove(&valid[(size_t)P * st], &valid[(size_t)P * pathIdx], (size_t)P);
+      float dCost = (pathCost[st] + h[node] - costThreshold);
+      dCost = dCost > (float)0 ? dCost : (float)0;
+      int bucket = (((int)(dCost / dr)) + Gidx + 1) % numBuckets;
+      G[bucket * maxPathCount + sizeG[bucket]] = st;
+      sizeG[bucket]++;
+      pathPrev[st] = wfPrev[i];
+      pathNode[st] = wfNode[i];
+      Ptab[node * N + Pcounts[node]] = st;
+      Pcounts[node]++;
+      wfNode[i] = -1;
+      numValid++;
+    }
+    for (int i = 0; i < numValid; ++i) {
+      d_pathCP[numPaths + i] = pathCP[numPaths + i];
+      d_pathTime[numPaths + i] = pathTime[numPaths + i];
+    }
+    numPaths += numValid;
+    /* PUMP.cu:259-282 */
+    for (int i = 0; i < Pcounts[goalIdx]; ++i) {
+      int pi = Ptab[goalIdx * N + i];
+      if (pathCP[pi] <= cpMinSoln) { goalConditionNext = 1; goalCondition = 1; }
+    }
+    if (goalCondition) break;
+    emptyOpenSet = 1;
+    for (int b = 0; b < numBuckets; ++b) emptyOpenSet = emptyOpenSet && (sizeG[b] == 0);
+    if (emptyOpenSet) break;
+    Gidx = (Gidx + 1) % numBuckets;
+    costThreshold += dr;
+    if (numPaths >= maxPathCount) { status = 1; break; }
+  }
+  res->itrs = itrs;
+  res->numPaths = numPaths;
+  res->numConsidered = numConsidered;
+  res->goalPathCount = Pcounts[goalIdx];
+  res->success = 0;
+  res->solnPathIdx = -1;
+  res->numNodes = 0;
+  res->pathLen = 0;
+
+  /* solution search (PUMP.cu:349-405); the reference returns from PUMP()
+   * without a solution when maxPathCount is hit. */
+  const int Tcap = pb->T_table;
+  float *splitPath = (float *)malloc(sizeof(float) * ORC_DIM * (Tcap + 2));
+  float *xs = (float *)malloc(sizeof(float) * ORC_DIM * (maxItrs + 2));
+  int *nodes = (int *)malloc(sizeof(int) * (maxItrs + 2));
+  int pathNumSamples = 0, pathLength = 0;
+  float solnPathCP = 0, solnPathCost = 0;
+  int success = 0, solnPathIdx = -1;
+  if (status == 0) {
+    int gcount = Pcounts[goalIdx];
+    cost_idx *gp = (cost_idx *)malloc(sizeof(cost_idx) * (gcount + 1));
+    for (int i = 0; i < gcount; ++i) {
+      int pi = Ptab[goalIdx * N + i];
+      gp[i].cost = pathCost[pi];
+      gp[i].idx = pi;
+    }
+    qsort(gp, gcount, sizeof(cost_idx), cmp_cost_idx);
+    for (int k = 0; k < gcount; ++k) {
+      solnPathIdx = gp[k].idx;
+      pathNumSamples = build_xs(solnPathIdx, pathPrev, pathNode, samples, xs, nodes, maxItrs + 2);
+      orc_find_optimal_path(dt, splitPath, Tcap, xs, pathNumSamples, &pathLength);
+      if (pathLength < 0) { status = 2; break; }
+      orc_mccp(splitPath, pathLength, pb->pmajor, pb->T_table, pb->offsetMult, nobs, obs, Pmc,
+               &solnPathCP);
+      solnPathCost = pathCost[solnPathIdx];
+      if (solnPathCP < cpTarget) { success = 1; break; }
+    }
+    free(gp);
+  }
+
+  /* smoothing (PUMP.cu:406-545) */
+  float lastCP = solnPathCP, lastCost = solnPathCost;
+  int lastLen = pathLength;
+  float *lastPath = (float *)malloc(sizeof(float) * ORC_DIM * (Tcap + 2));
+  if (pathLength > 0) memcpy(lastPath, splitPath, sizeof(float) * ORC_DIM * pathLength);
+  if (success && status == 0) {
+    const int dtMult = 10;
+    const int optCap = Tcap * dtMult;
+    float *optPath = (float *)malloc(sizeof(float) * ORC_DIM * (optCap + 2));
+    float xsOpt2[12];
+    for (int d = 0; d < ORC_DIM; ++d) {
+      xsOpt2[d] = xs[d];
+      xsOpt2[ORC_DIM + d] = xs[(pathNumSamples - 1) * ORC_DIM + d];
+    }
+    int optLen = 0;
+    orc_find_optimal_path(dt / dtMult, optPath, optCap, xsOpt2, 2, &optLen);
+    if (optLen < 0) status = 2;
+    float *splitT = (float *)calloc(pathNumSamples, sizeof(float));
+    int *splitI = (int *)calloc(pathNumSamples, sizeof(int));
+    float *xsOpt = (float *)malloc(sizeof(float) * ORC_DIM * pathNumSamples);
+    float *xsSmooth = (float *)malloc(sizeof(float) * ORC_DIM * pathNumSamples);
+    float *smoothPath = (float *)malloc(sizeof(float) * ORC_DIM * (Tcap + 2));
+    if (status == 0) {
+      for (int i = 0; i < pathNumSamples - 1; ++i)
+        splitT[i + 1] = splitT[i] + orc_topt_bisection(&xs[i * ORC_DIM], &xs[(i + 1) * ORC_DIM], 2, NULL);
+      for (int i = 0; i < pathNumSamples; ++i)
+        splitI[i] = (int)((optLen - 1) * splitT[i] / splitT[pathNumSamples - 1]);
+      for (int i = 0; i < pathNumSamples; ++i)
+        for (int d = 0; d < ORC_DIM; ++d) xsOpt[i * ORC_DIM + d] = optPath[splitI[i] * ORC_DIM + d];
+      const int maxSmoothItrs = 30;
+      const float epsSmoothCP = (float)0.0002;
+      float alpha = 1.0f, alphaU = 1.0f, alphaL = 0.0f;
+      for (int it = 0; it < maxSmoothItrs; ++it) {
+        for (int i = 0; i < pathNumSamples * ORC_DIM; ++i)
+          xsSmooth[i] = (1 - alpha) * xs[i] + alpha * xsOpt[i];
+        int sLen = 0;
+        float sCost = 0;
+        orc_find_optimal_path(dt, smoothPath, Tcap, xsSmooth, pathNumSamples, &sLen);
+        if (sLen < 0) { status = 2; break; }
+        for (int i = 0; i < pathNumSamples - 1; ++i) {
+          float tau = orc_topt_bisection(&xsSmooth[i * ORC_DIM], &xsSmooth[(i + 1) * ORC_DIM], 2, NULL);
+          sCost += orc_cost(tau, &xsSmooth[i * ORC_DIM], &xsSmooth[(i + 1) * ORC_DIM]);
+        }
+        float cp = 0;
+        orc_mccp(smoothPath, sLen, pb->pmajor, pb->T_table, pb->offsetMult, nobs, obs, Pmc, &cp);
+        if (cp < cpTarget) alphaL = alpha;
+        if (cp >= cpTarget) alphaU = alpha;
+        alpha = (alphaL + alphaU) / 2;
+        int satisfies = cp < cpTarget;
+        int closer = cp > lastCP;
+        int eqLower = (cp == lastCP && sCost < lastCost);
+        if (satisfies && (closer || eqLower)) {
+          memcpy(lastPath, smoothPath, sizeof(float) * ORC_DIM * sLen);
+          lastLen = sLen;
+          lastCost = sCost;
+          lastCP = cp;
+        }
+        if (fabsf(cpTarget - cp) < epsSmoothCP && cpTarget - cp > 0) break;
+      }
+    }
+    free(optPath); free(splitT); free(splitI); free(xsOpt); free(xsSmooth); free(smoothPath);
+  }
+  res->success = success;
+  res->solnPathIdx = solnPathIdx;
+  res->solnCP = lastCP;
+  res->solnCost = lastCost;
+  res->pathLen = success ? lastLen : 0;
+  if (success && res->path)
+    memcpy(res->path, lastPath, sizeof(float) * ORC_DIM * (lastLen < res->path_cap ? lastLen : res->path_cap));
+  if (solnPathIdx >= 0) {
+    int n = build_xs(solnPathIdx, pathPrev, pathNode, samples, xs, nodes, maxItrs + 2);
+    res->numNodes = n;
+    if (res->nodes)
+      for (int k = 0; k < n && k < res->nodes_cap; ++k) res->nodes[k] = nodes[k];
+  }
+  res->status = status;
+
+  free(samples); free(src); free(dst); free(coptE); free(toptE); free(disc); free(h);
+  free(goStart); free(isFreeS); free(isFreeE); free(as); free(bs);
+  free(Ptab); free(Pcounts); free(pathPrev); free(pathNode); free(pathCost); free(pathTime);
+  free(pathCP); free(d_pathTime); free(d_pathCP); free(G); free(valid); free(wfPrev);
+  free(wfNode); free(wfEdge); free(PnewCount); free(splitPath); free(xs); free(nodes);
+  free(lastPath);
+  return status;
+}

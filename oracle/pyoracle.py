@@ -1,0 +1,269 @@
+"""ctypes binding of the C oracle (pump_oracle.c) -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module, as the checker or as the timed CPU baseline.  The product
+(``pump_gb300``) never imports it.
+
+``build()`` compiles the oracle with gcc (``-ffp-contract=off``: no fused
+multiply-add, the arithmetic the oracle restates) into ``oracle/_build``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
+SRC = os.path.join(HERE, "pump_oracle.c")
+
+_lock = threading.Lock()
+_lib = None
+
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+
+DEFAULT_SEED = 0x9E3779B97F4A7C15
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so (gcc, OpenMP, no FMA contraction)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
+        os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "pump_oracle.h"))
+    ):
+        return LIB_PATH
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+           "-shared", SRC, "-o", tmp, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class Problem(C.Structure):
+    _fields_ = [
+        ("N", C.c_int), ("numDisc", C.c_int), ("P", C.c_int), ("Pmc", C.c_int),
+        ("T_table", C.c_int), ("numObs", C.c_int), ("obstacles", C.c_void_p),
+        ("init", C.c_float * 6), ("goal", C.c_float * 6), ("lo", C.c_float * 6),
+        ("hi", C.c_float * 6), ("offsetMult", C.c_float), ("cpTarget", C.c_float),
+        ("cpFactor", C.c_float), ("tmajor", C.c_void_p), ("pmajor", C.c_void_p),
+        ("samples", C.c_void_p),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("rn", C.c_float), ("numEdges", C.c_longlong), ("itrs", C.c_int),
+        ("numPaths", C.c_int), ("numConsidered", C.c_int), ("goalPathCount", C.c_int),
+        ("success", C.c_int), ("solnPathIdx", C.c_int), ("solnCP", C.c_float),
+        ("solnCost", C.c_float), ("pathLen", C.c_int), ("path", C.c_void_p),
+        ("path_cap", C.c_int), ("nodes", C.c_void_p), ("nodes_cap", C.c_int),
+        ("numNodes", C.c_int), ("wavefront_sizes", C.c_void_p), ("wf_trace", C.c_void_p),
+        ("wf_trace_cap", C.c_longlong), ("wf_trace_len", C.c_longlong),
+    ]
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            L = C.CDLL(build())
+            L.orc_cost.restype = C.c_float
+            L.orc_cost.argtypes = [C.c_float, f32p, f32p]
+            L.orc_dcost.restype = C.c_float
+            L.orc_dcost.argtypes = [C.c_float, f32p, f32p]
+            L.orc_topt_bisection.restype = C.c_float
+            L.orc_topt_bisection.argtypes = [f32p, f32p, C.c_float, C.c_void_p]
+            L.orc_path_point.argtypes = [C.c_float, C.c_float, f32p, f32p, f32p]
+            L.orc_find_discretized_path.restype = C.c_float
+            L.orc_find_discretized_path.argtypes = [f32p, f32p, f32p, C.c_int]
+            L.orc_find_optimal_path.restype = C.c_float
+            L.orc_find_optimal_path.argtypes = [C.c_float, f32p, C.c_int, f32p, C.c_int,
+                                                C.POINTER(C.c_int)]
+            L.orc_bvp_pairs.argtypes = [C.c_int, f32p, C.c_float, f32p, f32p]
+            L.orc_halton.restype = C.c_float
+            L.orc_halton.argtypes = [C.c_int, C.c_int]
+            L.orc_halton_samples.argtypes = [C.c_int, f32p, f32p, f32p, f32p, f32p]
+            L.orc_sample_free.argtypes = [C.c_int, f32p, C.c_int, f32p, u8p]
+            L.orc_select_kth.restype = C.c_float
+            L.orc_select_kth.argtypes = [C.c_longlong, f32p, C.c_longlong]
+            L.orc_build_edges.restype = C.c_longlong
+            L.orc_build_edges.argtypes = [C.c_int, f32p, f32p, C.c_float, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p]
+            L.orc_discretize_edges.argtypes = [C.c_longlong, i32p, i32p, f32p, C.c_int, f32p]
+            L.orc_heuristic.argtypes = [C.c_int, f32p, f32p, f32p]
+            L.orc_is_motion_valid.restype = C.c_int
+            L.orc_is_motion_valid.argtypes = [f32p, f32p, C.c_int, f32p]
+            L.orc_free_edges.argtypes = [C.c_longlong, C.c_int, f32p, C.c_int, f32p, u8p]
+            L.orc_cache_halfspaces.argtypes = [C.c_longlong, C.c_int, f32p, u8p, C.c_int, f32p,
+                                               C.c_int, C.c_float, f32p, f32p, i32p]
+            L.orc_hsmc_propagate.argtypes = [C.c_int, C.c_int, i32p, i32p, C.c_int, f32p, f32p,
+                                             f32p, f32p, C.c_float, C.c_int, f32p, C.c_float,
+                                             C.c_int, u8p, C.c_int, f32p]
+            L.orc_mccp.restype = C.c_int
+            L.orc_mccp.argtypes = [f32p, C.c_int, f32p, C.c_int, C.c_float, C.c_int, f32p,
+                                   C.c_int, C.POINTER(C.c_float)]
+            L.orc_frontier_compact.restype = C.c_int
+            L.orc_frontier_compact.argtypes = [C.c_int, u8p, i32p]
+            L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                            C.POINTER(C.c_uint32)]
+            L.orc_det_log.restype = C.c_double
+            L.orc_det_log.argtypes = [C.c_double]
+            L.orc_det_sincos_2pi.argtypes = [C.c_double, C.POINTER(C.c_double),
+                                             C.POINTER(C.c_double)]
+            L.orc_particle_tables.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+            L.orc_particle_cov.argtypes = [C.c_int, f64p]
+            L.orc_plan.restype = C.c_int
+            L.orc_plan.argtypes = [C.POINTER(Problem), C.POINTER(Result)]
+            _lib = L
+    return _lib
+
+
+# ---------------------------------------------------------------- wrappers
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def particle_tables(seed=DEFAULT_SEED, P=2048, T=400, tmajor=True, pmajor=True):
+    tm = np.empty((T, P, 3), np.float32) if tmajor else None
+    pm = np.empty((P, T, 3), np.float32) if pmajor else None
+    lib().orc_particle_tables(C.c_uint64(seed), P, T,
+                              tm.ctypes.data if tm is not None else None,
+                              pm.ctypes.data if pm is not None else None)
+    return tm, pm
+
+
+def particle_cov(T):
+    out = np.empty(T * 3, np.float64)
+    lib().orc_particle_cov(T, out)
+    return out.reshape(T, 3)
+
+
+def halton_samples(N, init, goal, lo, hi):
+    s = np.empty((N, 6), np.float32)
+    lib().orc_halton_samples(N, s, f32(init), f32(goal), f32(lo), f32(hi))
+    return s
+
+
+def bvp_pairs(samples, tmax=5.0):
+    N = samples.shape[0]
+    c = np.empty(N * (N - 1), np.float32)
+    t = np.empty(N * (N - 1), np.float32)
+    lib().orc_bvp_pairs(N, f32(samples), tmax, c, t)
+    return c, t
+
+
+def topt(x0, x1, tmax=5.0):
+    ev = C.c_int(0)
+    r = lib().orc_topt_bisection(f32(x0), f32(x1), tmax, C.byref(ev))
+    return r, ev.value
+
+
+def cost(tau, x0, x1):
+    return lib().orc_cost(tau, f32(x0), f32(x1))
+
+
+def build_edges(copts, topts, N, rn):
+    L = lib()
+    E = L.orc_build_edges(N, f32(copts), f32(topts), rn, None, None, None, None)
+    src = np.empty(E, np.int32)
+    dst = np.empty(E, np.int32)
+    ce = np.empty(E, np.float32)
+    te = np.empty(E, np.float32)
+    L.orc_build_edges(N, f32(copts), f32(topts), rn, src.ctypes.data, dst.ctypes.data,
+                      ce.ctypes.data, te.ctypes.data)
+    return src, dst, ce, te
+
+
+def discretize_edges(src, dst, samples, numDisc):
+    E = src.shape[0]
+    out = np.empty((E, numDisc + 1, 6), np.float32)
+    lib().orc_discretize_edges(E, np.ascontiguousarray(src, np.int32),
+                               np.ascontiguousarray(dst, np.int32), f32(samples), numDisc, out)
+    return out
+
+
+def heuristic(samples, goal):
+    N = samples.shape[0]
+    h = np.empty(N, np.float32)
+    lib().orc_heuristic(N, f32(samples), f32(goal), h)
+    return h
+
+
+def sample_free(samples, obstacles):
+    N = samples.shape[0]
+    out = np.empty(N, np.uint8)
+    ob = f32(obstacles).reshape(-1)
+    lib().orc_sample_free(N, f32(samples), ob.size // 12, ob, out)
+    return out
+
+
+def free_edges(disc, obstacles):
+    E, W = disc.shape[0], disc.shape[1]
+    out = np.empty(E, np.uint8)
+    ob = f32(obstacles).reshape(-1)
+    lib().orc_free_edges(E, W - 1, f32(disc), ob.size // 12, ob, out)
+    return out
+
+
+def cache_halfspaces(disc, isfree, obstacles, maxHS, maxd2):
+    E, W = disc.shape[0], disc.shape[1]
+    ob = f32(obstacles).reshape(-1)
+    a = np.empty(E * W * maxHS * 3, np.float32)
+    b = np.empty(E * W * maxHS, np.float32)
+    cnt = np.full(E * W, -1, np.int32)
+    lib().orc_cache_halfspaces(E, W, f32(disc), np.ascontiguousarray(isfree, np.uint8),
+                               ob.size // 12, ob, maxHS, maxd2, a, b, cnt)
+    return a, b, cnt
+
+
+def mccp(path, T, pmajor, offsetMult, obstacles):
+    ob = f32(obstacles).reshape(-1)
+    cp = C.c_float(0)
+    Pmc, Ts = pmajor.shape[0], pmajor.shape[1]
+    hits = lib().orc_mccp(f32(path).reshape(-1), T, f32(pmajor).reshape(-1), Ts, offsetMult,
+                          ob.size // 12, ob, Pmc, C.byref(cp))
+    return hits, cp.value
+
+
+def plan(N, obstacles, init, goal, lo, hi, offsetMult, cpTarget, cpFactor, numDisc=8, P=128,
+         Pmc=2048, T_table=400, seed=DEFAULT_SEED, samples=None, trace_cap=0, tables=None):
+    """Whole query as the reference's main() + PUMP(); returns a dict."""
+    ob = f32(obstacles).reshape(-1)
+    tm, pm = tables if tables is not None else particle_tables(seed, Pmc, T_table)
+    pb = Problem()
+    pb.N, pb.numDisc, pb.P, pb.Pmc, pb.T_table = N, numDisc, P, Pmc, T_table
+    pb.numObs = ob.size // 12
+    pb.obstacles = ob.ctypes.data
+    for k in range(6):
+        pb.init[k], pb.goal[k], pb.lo[k], pb.hi[k] = init[k], goal[k], lo[k], hi[k]
+    pb.offsetMult, pb.cpTarget, pb.cpFactor = offsetMult, cpTarget, cpFactor
+    tm = f32(tm)
+    pm = f32(pm)
+    pb.tmajor, pb.pmajor = tm.ctypes.data, pm.ctypes.data
+    sm = f32(samples) if samples is not None else None
+    pb.samples = sm.ctypes.data if sm is not None else None
+    res = Result()
+    path = np.zeros((T_table + 2, 6), np.float32)
+    nodes = np.zeros(64, np.int32)
+    wfs = np.zeros(32, np.int32)
+    trace = np.zeros(max(trace_cap, 1), np.int32)
+    res.path, res.path_cap = path.ctypes.data, T_table + 2
+    res.nodes, res.nodes_cap = nodes.ctypes.data, 64
+    res.wavefront_sizes = wfs.ctypes.data
+    res.wf_trace, res.wf_trace_cap = (trace.ctypes.data, trace_cap) if trace_cap else (None, 0)
+    lib().orc_plan(C.byref(pb), C.byref(res))
+    out = {k: getattr(res, k) for k, _ in Result._fields_ if not k.endswith(("cap",)) and k not in (
+        "path", "nodes", "wavefront_sizes", "wf_trace")}
+    out["path"] = path[: res.pathLen].copy()
+    out["nodes"] = nodes[: res.numNodes].copy()
+    out["wavefront_sizes"] = wfs[: res.itrs].copy()
+    out["wf_trace"] = trace[: res.wf_trace_len].copy() if trace_cap else None
+    return out

@@ -1,0 +1,2 @@
+#pragma once
+#include <thrust/device_vector.h>
