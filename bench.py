@@ -1,0 +1,424 @@
+#!/usr/bin/env python3
+"""Benchmark of the PUMP hot path on one GB300 (or N replicas under torchrun).
+
+Metric (the reference's headline, quoted at NUM=4000): plan ms, edges/s
+through BVP + CC + MC-CP, queries/s.  Workload ("indoor4000"): N = 4000
+Halton samples in pos [0,1]^3 x vel [-1,1]^3, 40 boxes (30 walls of a 4 x 4
+room grid + 10 boxes), noise multiplier 2e-3, CP target 0.01, eta 2, 1024
+HSMC particles, 9 waypoints per edge, closed-form binary64 2pBVP (the
+configuration's "FP64 bisection"); synthetic, seeded.
+
+One step = one planning query's hot path:
+  value: the device-resident kernels of the query -- all N(N-1) pair BVPs,
+         the rn selection, edge compaction and waypoints, sample and edge
+         collision checks (E edges), half-spaces, and the HSMC propagation of
+         every exploration wavefront of the query (sum M expansions x 1024
+         particles) -- launched back to back on resident buffers, timed with
+         CUDA events on the launching stream; the L2 is flushed (512 MB
+         write) between steps.  Units per step: N(N-1) + E + sum M.
+  e2e:   the same units through pump_plan() with host buffers: host problem
+         in, path out, every host<->device copy and the host search logic
+         inside the timed region; ms_per_step of e2e is the plan latency.
+The CPU baseline is the C oracle (the reference's algorithm restated,
+OpenMP over all host cores) timed on bounded samples of each stage.
+
+--impl reference times that CPU path alone (the reference's CPU
+implementation of this path; the reference's own GPU program is not
+buildable on the GPU machine, whose image holds no copy of its sources).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "plan ms @NUM=4000; edges/s (BVP+CC+MC-CP); batched vs plain queries/s @CP"
+UNIT = "edges/s"
+WORKLOAD = "indoor4000"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--num", type=int, default=4000)
+    ap.add_argument("--mode", default="precision", choices=["precision", "parity"])
+    ap.add_argument("--particles", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args, query):
+    from pump_gb300 import workloads
+    obs = workloads.indoor(1000 * 1 + query)
+    return dict(N=args.num, obstacles=obs, offset_mult=np.float32(2e-3), cp=0.01, eta=2.0,
+                num_disc=8, P=args.particles, mode=1 if args.mode == "precision" else 0)
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("LOCAL_RANK", "0"),
+                                          "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=subprocess.PIPE, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_query(args, query=0):
+    """One whole query of the workload through the C oracle (the reference's
+    algorithm restated on the CPU, OpenMP over all host cores); returns
+    (edges/s, seconds, detail)."""
+    from oracle import pyoracle as O
+    from pump_gb300 import workloads
+    O.build()
+    w = workload(args, query)
+    N = w["N"]
+    tables = O.particle_tables(O.DEFAULT_SEED, 2048, 400)
+    t0 = time.perf_counter()
+    r = O.plan(N, w["obstacles"], workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI,
+               w["offset_mult"], w["cp"], w["eta"], numDisc=w["num_disc"], P=w["P"], tables=tables)
+    dt = time.perf_counter() - t0
+    units = N * (N - 1) + int(r["numEdges"]) + int(r["numConsidered"])
+    detail = {"cores": os.cpu_count() or 1,
+              "sample": "one whole query (N=%d: %d pair BVPs with the reference's bisection, "
+                        "%d edges checked, %d HSMC expansions x %d particles, solution search "
+                        "and smoothing) in %.1f s" % (N, N * (N - 1), int(r["numEdges"]),
+                                                       int(r["numConsidered"]), w["P"], dt),
+              "units": units, "success": int(r["success"])}
+    return units / dt, dt, detail
+
+
+# ------------------------------------------------------------------ ours
+def run_ours(args):
+    import torch
+    from pump_gb300 import lib
+    from pump_gb300.build import build as build_lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    build_lib()
+    L = lib.load()
+    torch.cuda.set_device(local)
+    ctx = lib.Context(local)
+    w = workload(args, rank)
+    N, obs, P = w["N"], w["obstacles"], w["P"]
+    W = w["num_disc"] + 1
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(a).copy()).cuda()
+
+    def empty(n, dt):
+        return torch.empty(int(max(n, 1)), dtype=dt, device="cuda")
+
+    # ---- one query through the C ABI (also gives the exploration trace)
+    pb = lib.Problem()
+    L.pump_problem_defaults(C.byref(pb))
+    obs_host = np.ascontiguousarray(obs, np.float32)
+    from pump_gb300 import workloads
+    pb.N, pb.num_disc, pb.num_hsmc = N, w["num_disc"], P
+    pb.num_obstacles, pb.obstacles = obs_host.shape[0], obs_host.ctypes.data
+    for k in range(6):
+        pb.init[k], pb.goal[k] = workloads.INIT[k], workloads.GOAL[k]
+        pb.lo[k], pb.hi[k] = workloads.LO[k], workloads.HI[k]
+    pb.offset_mult, pb.cp_target, pb.cp_factor = float(w["offset_mult"]), w["cp"], w["eta"]
+    pb.bvp_mode = w["mode"]
+    trace_buf = np.zeros(2 * 8_000_000, np.int32)
+    path_buf = np.zeros((400, 6), np.float32)
+
+    def plan(with_trace):
+        res = lib.PlanResult()
+        res.path, res.path_cap = path_buf.ctypes.data, 400
+        if with_trace:
+            res.wf_trace, res.wf_trace_cap = trace_buf.ctypes.data, trace_buf.size
+        st = L.pump_plan(ctx.handle, C.byref(pb), C.byref(res), None)
+        if st not in (lib.PUMP_OK, lib.PUMP_ERR_NO_SOLUTION):
+            lib.check(st)
+        return res
+
+    res0 = plan(True)
+    E = int(res0.num_edges)
+    sizes = [int(res0.wavefront_sizes[i]) for i in range(min(res0.iterations, 32))]
+    sizes = [s for s in sizes if s > 0]
+    trace = trace_buf[: res0.wf_trace_len].reshape(-1, 2).copy()
+    M_total = int(trace.shape[0])
+    units = N * (N - 1) + E + M_total
+
+    # ---- device-resident buffers for the kernel pipeline
+    from oracle import pyoracle  # noqa: F401  (only for the CPU baseline below)
+    samples = np.zeros((N, 6), np.float32)
+    # Halton samples as the planner generates them (sampler.cu:20-41)
+    from oracle.pyoracle import halton_samples
+    samples = halton_samples(N, workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI)
+    d_s, d_obs = dev(samples), dev(obs_host)
+    npairs = N * (N - 1)
+    d_c, d_t = empty(npairs, torch.float32), empty(npairs, torch.float32)
+    rn_idx = int(np.float32((N - 1) * N) * np.float32(0.05))
+    cap = rn_idx
+    d_src, d_dst = empty(cap, torch.int32), empty(cap, torch.int32)
+    d_ce, d_te = empty(cap, torch.float32), empty(cap, torch.float32)
+    d_go = empty(N + 1, torch.int32)
+    d_disc = empty(cap * W * 6, torch.float32)
+    d_fs, d_fe = empty(N, torch.uint8), empty(cap, torch.uint8)
+    maxHS = min(obs_host.shape[0], 5)
+    d_a, d_b = empty(cap * W * maxHS * 3, torch.float32), empty(cap * W * maxHS, torch.float32)
+    Pmc, T = 2048, 400
+    d_tab = empty(T * Pmc * 3, torch.float32)
+    lib.check(L.pump_particle_tables(pb.seed, Pmc, T, d_tab.data_ptr(), None, sh))
+    words = (P + 31) // 32
+    base = int(trace[:, 0].max()) + 1 if M_total else 1
+    d_valid = empty((base + max(sizes + [1])) * words, torch.int32)
+    d_valid.fill_(-1)
+    d_times = empty(base, torch.float32).zero_()
+    d_cp = empty(base + max(sizes + [1]), torch.float32)
+    d_err = empty(1, torch.int32).zero_()
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    d_prev = dev(trace[:, 0].astype(np.int32))
+    d_edge = dev(trace[:, 1].astype(np.int32))
+    maxd2 = float(np.float32(0.1 * np.float64(w["offset_mult"]) ** 2))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    rn = C.c_float(0)
+    Eo = C.c_longlong(0)
+    launches = {"n": 0}
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    kernel_ms = {}
+
+    def timed(name, fn, nk):
+        a, b = ev(), ev()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        kernel_ms.setdefault(name, []).append((a, b))
+        launches["n"] += nk
+
+    def step():
+        timed("bvp_pairs", lambda: lib.check(L.pump_bvp_pairs(d_s.data_ptr(), N, 5.0, w["mode"],
+                                                             d_c.data_ptr(), d_t.data_ptr(), sh)), 1)
+        timed("select_rn", lambda: lib.check(L.pump_select_kth(ctx.handle, d_c.data_ptr(), npairs,
+                                                              rn_idx, C.byref(rn), sh)), 6)
+        timed("build_edges", lambda: lib.check(L.pump_build_edges(
+            ctx.handle, d_c.data_ptr(), d_t.data_ptr(), N, rn.value, cap, d_src.data_ptr(),
+            d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(), d_go.data_ptr(), C.byref(Eo), sh)), 2)
+        timed("discretize", lambda: lib.check(L.pump_discretize_edges(
+            d_s.data_ptr(), d_src.data_ptr(), d_dst.data_ptr(), d_te.data_ptr(), Eo.value, W - 1,
+            d_disc.data_ptr(), sh)), 1)
+        timed("sample_free", lambda: lib.check(L.pump_sample_free(
+            d_obs.data_ptr(), obs_host.shape[0], d_s.data_ptr(), N, d_fs.data_ptr(), sh)), 1)
+        timed("free_edges", lambda: lib.check(L.pump_free_edges(
+            d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), Eo.value, W - 1,
+            d_fe.data_ptr(), sh)), 1)
+        timed("halfspaces", lambda: lib.check(L.pump_cache_halfspaces(
+            d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), d_fe.data_ptr(), Eo.value, W,
+            maxHS, maxd2, d_a.data_ptr(), d_b.data_ptr(), None, sh)), 1)
+
+        def hsmc_all():
+            for it, m in enumerate(sizes):
+                o = int(offs[it])
+                lib.check(L.pump_hsmc_propagate(
+                    m, W, d_edge.data_ptr() + 4 * o, d_prev.data_ptr() + 4 * o, E, base,
+                    d_a.data_ptr(), d_b.data_ptr(), maxHS, d_times.data_ptr(), d_te.data_ptr(), 0.05,
+                    d_tab.data_ptr(), Pmc, T, float(w["offset_mult"]), d_valid.data_ptr(), P,
+                    d_cp.data_ptr(), d_err.data_ptr(), sh))
+        timed("hsmc", hsmc_all, len(sizes))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert Eo.value == E, (Eo.value, E)
+    kernel_ms.clear()
+    launches["n"] = 0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        a, b = ev(), ev()
+        a.record(stream)
+        step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        step_ms.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    # e2e: pump_plan with host buffers (includes roadmap + online + search)
+    e2e_ms, plan_res = [], None
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        plan_res = plan(False)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    tot = sum(step_ms)
+    tot_e2e = sum(e2e_ms)
+    if dist:
+        t = torch.tensor([tot, tot_e2e], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot, tot_e2e = t.tolist()
+    ks = {k: sum(a.elapsed_time(b) for a, b in v) / args.steps for k, v in kernel_ms.items()}
+    out = None
+    if rank == 0:
+        value = world * units * args.steps / (tot / 1e3)
+        e2e_value = world * units * max(1, args.steps) / (tot_e2e / 1e3)
+        dom = max(ks, key=ks.get)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded indoor map, Halton samples)",
+            "config": {"workload": WORKLOAD, "N": N, "obstacles": int(obs_host.shape[0]),
+                       "hsmc_particles": P, "waypoints_per_edge": W, "noise_mult": 2e-3,
+                       "cp_target": 0.01, "eta": 2, "bvp": args.mode, "edges": E,
+                       "expansions": M_total, "units_per_step": units,
+                       "l2": "flushed between steps (512 MB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "plan_ms": statistics.median(e2e_ms),
+            "plan_stage_ms": {"roadmap": plan_res.ms_roadmap, "online": plan_res.ms_online,
+                              "explore": plan_res.ms_explore, "search": plan_res.ms_search},
+            "edges_per_s": {"bvp": N * (N - 1) / (ks["bvp_pairs"] / 1e3),
+                            "cc": E / (ks["free_edges"] / 1e3),
+                            "hsmc": M_total / (ks["hsmc"] / 1e3)},
+            "kernel_ms": {k: round(v, 4) for k, v in ks.items()},
+            "dominant_kernel": dom,
+            "queries_per_s_plain": 1e3 / statistics.median(e2e_ms),
+            "solution": {"success": int(plan_res.success), "cp": plan_res.soln_cp,
+                         "cost": plan_res.soln_cost, "paths": plan_res.num_paths},
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": int(plan_res.h2d_bytes),
+                    "d2h_bytes_per_step": int(plan_res.d2h_bytes)},
+            "gpu_launches": launches["n"],
+            "clocks": clk,
+        }
+        out["roofline"] = roofline(dom, ks, N, E, M_total, W, maxHS, P)
+        if not args.no_cpu_baseline:
+            v, _dt, det = cpu_query(args, 0)
+            out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",
+                                   "sample": det["sample"]}
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return out
+
+
+def roofline(dom, ks, N, E, M, W, H, P):
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    src = "measured" if "hbm_gbs" in peaks else "fallback"
+    # algorithmic HBM bytes per launch of each kernel (per unit x units)
+    algo = {
+        "bvp_pairs": 8.0 * N * (N - 1),                       # topt + copt out
+        "select_rn": 3 * 4.0 * N * (N - 1),                   # three reads of the costs
+        "build_edges": 4.0 * N * (N - 1) + 16.0 * E,          # costs read, 4 arrays out
+        "discretize": 12.0 * E + 24.0 * W * E,                # edge in, waypoints out
+        "free_edges": 24.0 * W * E + E,                       # waypoints in, mask out
+        "halfspaces": 24.0 * W * E + E + 16.0 * W * H * E,    # waypoints in, a/b out
+        "hsmc": M * (8 + 4 + 2 * 4 * ((P + 31) // 32) + 16.0 * W * H),
+    }
+    t = ks[dom] / 1e3
+    ach = algo.get(dom, 0.0) / t / 1e9
+    return {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+            "frac": ach / hbm, "traffic": None, "peak_source": src}
+
+
+def run_reference(args):
+    """The reference's CPU path of this workload (C oracle), one whole query
+    per step; rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    vals, secs = [], []
+    det = None
+    for k in range(args.warmup + args.steps):
+        v, dt, det = cpu_query(args, 0)
+        if k >= args.warmup:
+            vals.append(v)
+            secs.append(dt)
+    v = statistics.median(vals)
+    w = workload(args, 0)
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "impl": "reference", "data": "synthetic (seeded indoor map, Halton samples)",
+            "config": {"workload": WORKLOAD, "N": w["N"], "obstacles": int(w["obstacles"].shape[0]),
+                       "hsmc_particles": w["P"], "waypoints_per_edge": w["num_disc"] + 1,
+                       "noise_mult": 2e-3, "cp_target": 0.01, "eta": 2,
+                       "bvp": "reference finite-difference bisection"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",
+                             "sample": det["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

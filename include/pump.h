@@ -1,0 +1,235 @@
+/*
+ * pump.h -- C ABI of pump_gb300, a GB300-native (sm_103a) implementation of
+ * the PUMP planner's hot path (Parallel Uncertainty-aware Multiobjective
+ * Planning, 3D double integrator, 6D state).
+ *
+ * Each entry point replaces one function of the reference
+ * (StanfordASL/PUMP); the reference file:line is cited beside it.  Device
+ * buffers are caller-owned raw pointers; every call takes an explicit CUDA
+ * stream (pump_stream_t is cudaStream_t) and returns a pump_status_t instead
+ * of exiting the process (the reference calls exit(1) from CUDA_ERROR_CHECK,
+ * helper.cuh:22-30).  Calls are asynchronous on the stream unless they return
+ * a host value, in which case they synchronise the stream.
+ *
+ * Arithmetic ("parity" mode): every operation is evaluated in the type the
+ * reference's C++ source gives it (binary32, or binary64 where pow() or a
+ * double literal promotes it), rounded once, never fused into a
+ * multiply-add, and pow(x, n) for n = 2, 3, 4 is correctly rounded.  The
+ * reference's own code built for the CPU with that rule reproduces every
+ * result of this library bit for bit.  The "precision" BVP mode instead
+ * solves the optimal time from the analytic stationarity quartic in binary64.
+ *
+ * Masks are one byte per item (0/1) as the reference's bool arrays, except
+ * the HSMC particle masks, which are bit-packed: bit (p & 31) of word
+ * path * ceil(P/32) + p / 32 is particle p of that path.
+ *
+ * Thread safety: a pump_ctx may be used by one host thread at a time.
+ */
+#ifndef PUMP_GB300_H
+#define PUMP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *pump_stream_t; /* == cudaStream_t */
+typedef struct pump_ctx pump_ctx;
+
+typedef enum pump_status_t {
+  PUMP_OK = 0,
+  PUMP_ERR_BAD_INPUT = 1,   /* argument out of domain (sizes, pointers, file format) */
+  PUMP_ERR_CAPACITY = 2,    /* a fixed capacity of the reference would be exceeded */
+  PUMP_ERR_TIMEOUT = 3,     /* a bounded device wait or loop gave up */
+  PUMP_ERR_CUDA = 4,        /* CUDA runtime error (message in pump_last_error) */
+  PUMP_ERR_NO_SOLUTION = 5, /* planner finished without a path meeting the CP target */
+  PUMP_ERR_NO_MEMORY = 6
+} pump_status_t;
+
+enum { PUMP_DIM = 6 };
+
+/* BVP arithmetic modes for pump_bvp_pairs. */
+enum { PUMP_BVP_PARITY = 0, PUMP_BVP_PRECISION = 1 };
+
+const char *pump_status_string(pump_status_t s);
+/* Last error message of this thread (never NULL). */
+const char *pump_last_error(void);
+/* Library version string. */
+const char *pump_version(void);
+
+/* Context: owns scratch device memory reused across calls on one device. */
+pump_status_t pump_ctx_create(int device, pump_ctx **out);
+pump_status_t pump_ctx_destroy(pump_ctx *ctx);
+
+/* ------------------------------------------------------------------ 2pBVP */
+/* Optimal time and cost of the double-integrator two-point BVP for every
+ * ordered pair i != j of N samples (samples: N x 6 floats), written at
+ * idx = i*(N-1) + j - (i < j).
+ * Replaces fillCoptsTopts (2pBVP.cu:133-150) with toptBisection
+ * (2pBVP.cu:71-95) and cost (2pBVP.cu:97-107); mode PUMP_BVP_PRECISION
+ * returns the binary64 minimiser of the same cost instead. */
+pump_status_t pump_bvp_pairs(const float *d_samples, int N, float tmax, int mode, float *d_copts,
+                             float *d_topts, pump_stream_t stream);
+
+/* Optimal time / cost of the explicit pairs (d_x0[k], d_x1[k]), k < n
+ * (6 floats each); replaces host calls of toptBisection + cost
+ * (mainPUMP.cu:351-355, PUMP.cu:499-502). */
+pump_status_t pump_bvp_batch(const float *d_x0, const float *d_x1, int n, float tmax, int mode,
+                             float *d_topt, float *d_cost, pump_stream_t stream);
+
+/* k-th smallest of n floats (0-based), exact: the value the reference reads
+ * after thrust::sort (mainPUMP.cu:303-304).  Uses ctx scratch; synchronises
+ * the stream and returns the value in *h_kth. */
+pump_status_t pump_select_kth(pump_ctx *ctx, const float *d_v, long long n, long long k,
+                              float *h_kth, pump_stream_t stream);
+
+/* Roadmap edges: pairs with copt < rn in (i asc, j asc) order
+ * (mainPUMP.cu:327-346).  Writes E = *h_num_edges (synchronises), then
+ * d_src[E], d_dst[E], d_copt[E], d_topt[E] and the go-adjacency row starts
+ * d_go_start[N+1] (edges of node i are [go_start[i], go_start[i+1]), in j
+ * order, replacing nnGoEdges/nnIdxs of mainPUMP.cu:379-392).  Capacity
+ * max_edges; PUMP_ERR_CAPACITY if more edges qualify. */
+pump_status_t pump_build_edges(pump_ctx *ctx, const float *d_copts, const float *d_topts, int N,
+                               float rn, long long max_edges, int *d_src, int *d_dst,
+                               float *d_copt, float *d_topt, int *d_go_start,
+                               long long *h_num_edges, pump_stream_t stream);
+
+/* Edge waypoints disc[E][numDisc+1][6] (findDiscretizedPath, 2pBVP.cu:53-69
+ * and pathPoint 2pBVP.cu:117-131, as called at mainPUMP.cu:339).  d_topt
+ * is the edge's optimal time (identical to the one toptBisection recomputes
+ * there). */
+pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src, const int *d_dst,
+                                    const float *d_topt, long long E, int numDisc, float *d_disc,
+                                    pump_stream_t stream);
+
+/* ------------------------------------------------------ collision checks */
+/* isFree[i] = sample i is not strictly inside any box (sampleFree,
+ * sampler.cu:61-88).  obstacles: numObs x 12 floats (lo[6], hi[6]). */
+pump_status_t pump_sample_free(const float *d_obstacles, int numObs, const float *d_samples, int N,
+                               uint8_t *d_is_free, pump_stream_t stream);
+
+/* isFree[e] = every waypoint segment of edge e misses every box
+ * (freeEdges, collisionCheck.cu:5-37, isMotionValid :65-143). */
+pump_status_t pump_free_edges(const float *d_obstacles, int numObs, const float *d_disc,
+                              long long E, int numDisc, uint8_t *d_is_free, pump_stream_t stream);
+
+/* Half-spaces of every waypoint of free edges: setupAsBs (hsmc.cu:201-211)
+ * then cacheHalfspaces (hsmc.cu:10-99).  as[E][W][maxHS][3], bs[E][W][maxHS],
+ * count[E][W] (count of non-free edges is written 0). */
+pump_status_t pump_cache_halfspaces(const float *d_obstacles, int numObs, const float *d_disc,
+                                    const uint8_t *d_is_free_edge, long long E, int W, int maxHS,
+                                    float maxd2, float *d_as, float *d_bs, int *d_count,
+                                    pump_stream_t stream);
+
+/* --------------------------------------------------------------- HSMC */
+/* Particle tables of the closed-loop tracking-error model (the data of the
+ * reference's missing hardCoded.cu, hardCoded.cuh:12-19): position errors
+ * tmajor[T][P][3] (xcombTime) and pmajor[P][T][3] (xcomb); either may be
+ * NULL.  Philox4x32-10 keyed by seed, Box-Muller, binary64 dynamics. */
+pump_status_t pump_particle_tables(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
+                                   pump_stream_t stream);
+
+/* Half-space Monte Carlo propagation of num_new new paths, path base+i
+ * extending path prev[i] along edge[i]: propagateValidParticles
+ * (PUMP.cu:613-655) with the hit count of calculateCP_HSMC
+ * (PUMP.cu:745-758) fused.  valid: bit-packed, ceil(P/32) words per path;
+ * times[path] is the start time of each path; topt[edge] the edge time;
+ * offsets_t the time-major table with Pmc particles per row and T_rows rows.
+ * Device-side checks write *d_error (device, may be NULL): an edge outside
+ * [0, num_edges) or a parent outside [0, base) skips that path and records
+ * PUMP_ERR_BAD_INPUT; a time row past T_rows records PUMP_ERR_CAPACITY.
+ * Writes path_cp[base+i]. */
+pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_edge, const int *d_prev,
+                                  long long num_edges, int base, const float *d_as, const float *d_bs, int maxHS,
+                                  const float *d_times, const float *d_topt, float dt,
+                                  const float *d_offsets_t, int Pmc, int T_rows,
+                                  float offset_mult, uint32_t *d_valid, int P, float *d_path_cp,
+                                  int *d_error, pump_stream_t stream);
+
+/* Full Monte Carlo collision probability of n_paths dense paths at once
+ * (MCCP + thrust::reduce, collisionProbability.cu:4-92).  Path k has
+ * d_len[k] states starting at d_paths + d_offset[k]*6.  The particle
+ * offsets are read from the time-major table (T_rows rows of Pmc particles;
+ * the values equal the reference's particle-major xcomb, the layout only
+ * makes a warp's reads contiguous).  Writes d_hits[k] and
+ * d_cp[k] = hits / Pmc; a path longer than T_rows states sets *d_error
+ * (device, may be NULL) to PUMP_ERR_CAPACITY and counts no hits. */
+pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
+                         const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
+                         const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
+                         int *d_error, pump_stream_t stream);
+
+/* ------------------------------------------------------------- GMT */
+/* Stable compaction of a frontier flag array into the ascending list of set
+ * indices (thrust::exclusive_scan + fillWavefront, GMT.cu:48-54, 66-76,
+ * 166-176).  Writes d_active[0..count) and *d_count (device). */
+pump_status_t pump_frontier_compact(pump_ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
+                                    int *d_count, pump_stream_t stream);
+
+/* ---------------------------------------------------------- whole query */
+typedef struct pump_problem {
+  int N;              /* samples (the reference's compile-time NUM) */
+  int num_disc;       /* edge discretisation (mainPUMP.cu:57, default 8) */
+  int num_hsmc;       /* HSMC particles (mainPUMP.cu:68, default 128) */
+  int num_mc;         /* MC particles = table width (hardCoded.cuh:13, default 2048) */
+  int table_rows;     /* particle table rows at dt = 0.05 s (default 400) */
+  int num_obstacles;
+  const float *obstacles; /* host, num_obstacles x 12 */
+  float init[6], goal[6], lo[6], hi[6];
+  float offset_mult;  /* noise multiplier (input file line 5) */
+  float cp_target;    /* argv[2] */
+  float cp_factor;    /* argv[3] (eta) */
+  uint64_t seed;      /* particle stream key */
+  int bvp_mode;       /* PUMP_BVP_PARITY or PUMP_BVP_PRECISION */
+  const float *samples; /* optional host N x 6; NULL = Halton (sampler.cu:20-41) */
+} pump_problem;
+
+typedef struct pump_plan_result {
+  float rn;
+  long long num_edges;
+  int iterations;       /* exploration iterations */
+  int num_paths;        /* stored paths */
+  int num_considered;   /* wavefront expansions (sum over iterations) */
+  int goal_paths;
+  int success;
+  int soln_path_idx;
+  float soln_cp;        /* MC CP of the returned (smoothed) path */
+  float soln_cost;
+  int path_len;         /* states written to path (dt = 0.05 s) */
+  float *path;          /* host buffer, path_cap x 6 (may be NULL) */
+  int path_cap;
+  int *nodes;           /* host buffer for the node sequence, init first */
+  int nodes_cap;
+  int num_nodes;
+  /* stage wall times in milliseconds */
+  double ms_roadmap, ms_online, ms_explore, ms_search, ms_total;
+  /* HSMC expansions per iteration (first 32 iterations) */
+  int wavefront_sizes[32];
+  /* optional exploration trace: (parent path, edge) of every expansion in
+   * launch order; host buffer of wf_trace_cap ints (may be NULL) */
+  int *wf_trace;
+  long long wf_trace_cap;
+  long long wf_trace_len;
+  /* bytes copied host->device and device->host by this query */
+  long long h2d_bytes, d2h_bytes;
+} pump_plan_result;
+
+/* Fills a problem with the reference's defaults (mainPUMP.cu:51-72). */
+void pump_problem_defaults(pump_problem *pb);
+
+/* Reads the reference's input file (README.md:10-11, parsed as
+ * mainPUMP.cu:152-230) into pb; obstacles are stored in a buffer owned by
+ * the library until the next call from this thread. */
+pump_status_t pump_read_input(const char *path, pump_problem *pb);
+
+/* One planning query: roadmap, online checks, exploration, solution search
+ * and smoothing (mainPUMP.cu:248-687 and PUMP(), PUMP.cu:3-607). */
+pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
+                        pump_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PUMP_GB300_H */

@@ -1,0 +1,170 @@
+// Context, status reporting and the reference input-file reader.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "ctx.h"
+
+namespace pump {
+
+namespace {
+thread_local char g_last_error[512] = "";
+}
+
+pump_status_t set_error(pump_status_t s, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(g_last_error, sizeof g_last_error, fmt, ap);
+  va_end(ap);
+  return s;
+}
+
+pump_status_t cuda_status(cudaError_t e, const char *where) {
+  if (e == cudaSuccess) return PUMP_OK;
+  if (e == cudaErrorMemoryAllocation)
+    return set_error(PUMP_ERR_NO_MEMORY, "%s: %s", where, cudaGetErrorString(e));
+  return set_error(PUMP_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+pump_status_t launch_status(const char *kernel) { return cuda_status(cudaGetLastError(), kernel); }
+
+Ctx::~Ctx() {
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaSetDevice(device_);
+  for (int i = 0; i < kNumSlots; ++i)
+    if (buf_[i]) cudaFree(buf_[i]);
+  if (prev >= 0) cudaSetDevice(prev);
+}
+
+pump_status_t Ctx::activate() { return cuda_status(cudaSetDevice(device_), "cudaSetDevice"); }
+
+pump_status_t Ctx::scratch(int slot, size_t bytes, void **out) {
+  if (slot < 0 || slot >= kNumSlots) return set_error(PUMP_ERR_BAD_INPUT, "scratch slot %d", slot);
+  if (bytes == 0) bytes = 1;
+  if (cap_[slot] < bytes) {
+    if (buf_[slot]) {
+      // a buffer still in use by queued work must not be freed early
+      PUMP_CUDA_TRY(cudaDeviceSynchronize());
+      PUMP_CUDA_TRY(cudaFree(buf_[slot]));
+      buf_[slot] = nullptr;
+      cap_[slot] = 0;
+    }
+    size_t cap = bytes + bytes / 4;
+    PUMP_CUDA_TRY(cudaMalloc(&buf_[slot], cap));
+    cap_[slot] = cap;
+  }
+  *out = buf_[slot];
+  return PUMP_OK;
+}
+
+}  // namespace pump
+
+using namespace pump;
+
+extern "C" const char *pump_status_string(pump_status_t s) {
+  switch (s) {
+    case PUMP_OK: return "ok";
+    case PUMP_ERR_BAD_INPUT: return "bad input";
+    case PUMP_ERR_CAPACITY: return "capacity exceeded";
+    case PUMP_ERR_TIMEOUT: return "bounded wait gave up";
+    case PUMP_ERR_CUDA: return "CUDA error";
+    case PUMP_ERR_NO_SOLUTION: return "no solution";
+    case PUMP_ERR_NO_MEMORY: return "out of device memory";
+  }
+  return "unknown status";
+}
+
+extern "C" const char *pump_last_error(void) { return g_last_error; }
+
+extern "C" const char *pump_version(void) { return "pump_gb300 0.1 (sm_103a)"; }
+
+extern "C" pump_status_t pump_ctx_create(int device, pump_ctx **out) {
+  if (!out) return set_error(PUMP_ERR_BAD_INPUT, "pump_ctx_create: null out");
+  int n = 0;
+  PUMP_CUDA_TRY(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_ctx_create: device %d of %d", device, n);
+  Ctx *c = new (std::nothrow) Ctx(device);
+  if (!c) return set_error(PUMP_ERR_NO_MEMORY, "pump_ctx_create: host allocation");
+  *out = c->handle();
+  return c->activate();
+}
+
+extern "C" pump_status_t pump_ctx_destroy(pump_ctx *ctx) {
+  delete Ctx::from(ctx);
+  return PUMP_OK;
+}
+
+// Defaults of mainPUMP.cu:51-72 and obstacles.cu:3-10.
+extern "C" void pump_problem_defaults(pump_problem *pb) {
+  static const float kObs[36] = {
+      0.05f, 0.20f, -3.1f, -3.1f, -3.1f, -3.1f, 0.45f, 0.35f, 3.1f, 3.1f, 3.1f, 3.1f,
+      0.70f, 0.30f, -3.1f, -3.1f, -3.1f, -3.1f, 0.90f, 0.50f, 3.1f, 3.1f, 3.1f, 3.1f,
+      0.30f, 0.60f, -3.1f, -3.1f, -3.1f, -3.1f, 0.80f, 0.75f, 3.1f, 3.1f, 3.1f, 3.1f};
+  static const float kLo[6] = {0, 0, 0.01f, -1, -1, -0.5f};
+  static const float kHi[6] = {1, 1, 0.3f, 1, 1, 0.5f};
+  std::memset(pb, 0, sizeof *pb);
+  pb->N = 1000;
+  pb->num_disc = 8;
+  pb->num_hsmc = 128;
+  pb->num_mc = 2048;
+  pb->table_rows = 400;
+  pb->num_obstacles = 3;
+  pb->obstacles = kObs;
+  for (int d = 0; d < 6; ++d) {
+    pb->init[d] = d < 3 ? 0.1f : 0.0f;
+    pb->goal[d] = d < 3 ? 0.9f : 0.0f;
+    pb->lo[d] = kLo[d];
+    pb->hi[d] = kHi[d];
+  }
+  pb->offset_mult = 0.5f;
+  pb->cp_target = 0.01f;
+  pb->cp_factor = 2.0f;
+  pb->seed = 0x9E3779B97F4A7C15ull;
+  pb->bvp_mode = PUMP_BVP_PARITY;
+  pb->samples = nullptr;
+}
+
+namespace {
+thread_local std::vector<float> g_input_obstacles;
+}
+
+// Same field order and conversions as mainPUMP.cu:152-230: comma-separated
+// fields read with getline(',') and converted with stringstream >>.
+extern "C" pump_status_t pump_read_input(const char *path, pump_problem *pb) {
+  if (!path || !pb) return set_error(PUMP_ERR_BAD_INPUT, "pump_read_input: null argument");
+  std::ifstream file(path);
+  if (!file.good()) return set_error(PUMP_ERR_BAD_INPUT, "pump_read_input: cannot read %s", path);
+  std::string v;
+  auto rd = [&](float &out) {
+    std::getline(file, v, ',');
+    std::stringstream ss(v);
+    ss >> out;
+  };
+  for (int d = 0; d < 6; ++d) rd(pb->init[d]);
+  for (int d = 0; d < 6; ++d) rd(pb->goal[d]);
+  for (int d = 0; d < 6; ++d) rd(pb->lo[d]);
+  for (int d = 0; d < 6; ++d) rd(pb->hi[d]);
+  rd(pb->offset_mult);
+  {
+    std::getline(file, v, ',');
+    std::stringstream ss(v);
+    int n = 0;
+    ss >> n;
+    if (n < 0 || n > 1000000) return set_error(PUMP_ERR_BAD_INPUT, "pump_read_input: %d obstacles", n);
+    pb->num_obstacles = n;
+  }
+  g_input_obstacles.assign((size_t)pb->num_obstacles * 12, 0.0f);
+  for (size_t i = 0; i < g_input_obstacles.size(); ++i) rd(g_input_obstacles[i]);
+  pb->obstacles = g_input_obstacles.data();
+  return PUMP_OK;
+}

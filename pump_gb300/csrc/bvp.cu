@@ -1,0 +1,443 @@
+// Two-point BVP of the 3D double integrator: optimal time, cost and edge
+// waypoints (reference: 2pBVP.cu).
+//
+// Parity mode evaluates the reference's cost expression (2pBVP.cu:97-107)
+// term by term in its own evaluation types, with the pair-dependent,
+// tau-independent sub-expressions hoisted out of the bisection loop: each
+// hoisted value is computed by exactly the same operations the expression
+// performs, so every rounding is unchanged and only repeated work is
+// removed.  The finite-difference bisection (2pBVP.cu:71-95) is replicated
+// step for step.  Cost evaluation is binary64-bound (the expression promotes
+// through pow(double)), so these kernels are limited by the FP64 pipe.
+//
+// Precision mode minimises the same cost in closed form.  Written out, the
+// cost is c(t) = A0/t^3 + A1/t^2 + A2/t + A3 + A4 t with
+//   A0 = 12|p1-p0|^2, A1 = -12 (p1-p0).(v0+v1), A2 = 4(|v0|^2+v0.v1+|v1|^2),
+//   A3 = 2g(v0z-v1z), A4 = 1+g^2,
+// so c'(t) = 0 is the quartic Q(t) = A4 t^4 - A2 t^2 - 2 A1 t - 3 A0 = 0.
+// The kernel splits (0, tmax] at the real critical points of Q (Q'' = 0 at
+// sqrt(A2 / 6 A4)), finds every upward sign change of Q by safeguarded
+// Newton in binary64, and returns the candidate (those roots, and tmax when
+// Q(tmax) < 0) with the smallest cost.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace pump {
+namespace {
+
+// ---------------------------------------------------------------- parity
+struct PairCoef {
+  double s7;                                     // first seven (tau-free) terms
+  float k8, k9, k10, k11, k12, k13, k14, k15;    // float prefixes of the t-linear terms
+  double d16, d17, d18, d20, d22, d24;           // 4*pow(x,2) coefficients of t^2
+  float f19, f21, f23;                           // 4*x*y float coefficients of t^2
+  float f25, f26;                                // 2*g*x coefficients of t^3
+  float a29, b29, c29, a30, b30, c30;            // last two float terms
+};
+
+__device__ __forceinline__ PairCoef make_coef(const float *x0, const float *x1) {
+  const float g = PUMP_G;
+  PairCoef c;
+  double s = 12 * p2f(x0[0]);
+  s = s + 12 * p2f(x0[2]);
+  s = s + 12 * p2f(x0[1]);
+  s = s + 12 * p2f(x1[0]);
+  s = s + 12 * p2f(x1[2]);
+  s = s - (double)(24 * x0[1] * x1[1]);
+  s = s + 12 * p2f(x1[1]);
+  c.s7 = s;
+  c.k8 = 12 * x0[4] * x0[1];
+  c.k9 = 12 * x0[1] * x1[4];
+  c.k10 = 12 * x0[3] * x1[0];
+  c.k11 = 12 * x1[3] * x1[0];
+  c.k12 = 12 * x0[5] * x1[2];
+  c.k13 = 12 * x1[5] * x1[2];
+  c.k14 = 12 * x0[4] * x1[1];
+  c.k15 = 12 * x1[4] * x1[1];
+  c.d16 = 4 * p2f(x0[4]);
+  c.d17 = 4 * p2f(x0[3]);
+  c.d18 = 4 * p2f(x0[5]);
+  c.f19 = 4 * x0[4] * x1[4];
+  c.d20 = 4 * p2f(x1[4]);
+  c.f21 = 4 * x0[3] * x1[3];
+  c.d22 = 4 * p2f(x1[3]);
+  c.f23 = 4 * x0[5] * x1[5];
+  c.d24 = 4 * p2f(x1[5]);
+  c.f25 = 2 * g * x0[5];
+  c.f26 = 2 * g * x1[5];
+  c.a29 = 12 * x0[0];
+  c.b29 = -2 * x1[0];
+  c.c29 = x0[3] + x1[3];
+  c.a30 = 12 * x0[2];
+  c.b30 = -2 * x1[2];
+  c.c30 = x0[5] + x1[5];
+  return c;
+}
+
+// cost(tau, x0, x1), 2pBVP.cu:97-107, term order preserved.
+__device__ __forceinline__ float cost_eval(const PairCoef &c, float tau) {
+  const double g2 = p2f(PUMP_G);
+  const double dt = tau;
+  const double t2 = dt * dt, t3 = t2 * dt, t4 = t2 * t2;
+  double s = c.s7;
+  s = s + (double)(c.k8 * tau);
+  s = s + (double)(c.k9 * tau);
+  s = s - (double)(c.k10 * tau);
+  s = s - (double)(c.k11 * tau);
+  s = s - (double)(c.k12 * tau);
+  s = s - (double)(c.k13 * tau);
+  s = s - (double)(c.k14 * tau);
+  s = s - (double)(c.k15 * tau);
+  s = s + c.d16 * t2;
+  s = s + c.d17 * t2;
+  s = s + c.d18 * t2;
+  s = s + (double)c.f19 * t2;
+  s = s + c.d20 * t2;
+  s = s + (double)c.f21 * t2;
+  s = s + c.d22 * t2;
+  s = s + (double)c.f23 * t2;
+  s = s + c.d24 * t2;
+  s = s + (double)c.f25 * t3;
+  s = s - (double)c.f26 * t3;
+  s = s + t4;
+  s = s + g2 * t4;
+  s = s + (double)(c.a29 * (c.b29 + c.c29 * tau));
+  s = s + (double)(c.a30 * (c.b30 + c.c30 * tau));
+  return (float)((1.0 / t3) * s);
+}
+
+// dcost, 2pBVP.cu:109-115
+__device__ __forceinline__ float dcost_eval(const PairCoef &c, float tau) {
+  const float dtau = (float)0.000001;
+  return (cost_eval(c, tau + dtau / 2) - cost_eval(c, tau - dtau / 2)) / dtau;
+}
+
+// toptBisection, 2pBVP.cu:71-95.  The reference's halving loop (:78-80) is
+// unbounded; here it stops after 160 halvings (tl < 1e-50 has underflowed to
+// zero long before), exactly as the oracle does.
+__device__ float topt_bisection(const PairCoef &c, float tmax) {
+  float tu = tmax;
+  if (dcost_eval(c, tmax) < 0) return tmax;
+  float tl = (float)0.01;
+  int halvings = 0;
+  while (dcost_eval(c, tl) > 0 && halvings < 160) {
+    tl = tl / 2;
+    ++halvings;
+  }
+  float topt = 0;
+  float dcval = 1;
+  int itr = 0;
+  while ((double)fabsf(dcval) > 0.0001 && itr < 50) {
+    ++itr;
+    topt = (tu + tl) / 2;
+    dcval = dcost_eval(c, topt);
+    if (dcval > 0)
+      tu = topt;
+    else
+      tl = topt;
+  }
+  return topt;
+}
+
+// ------------------------------------------------------------- precision
+struct Quartic {
+  double A0, A1, A2, A3, A4;
+  __device__ double Q(double t) const { return ((A4 * t * t - A2) * t - 2.0 * A1) * t - 3.0 * A0; }
+  __device__ double dQ(double t) const { return (4.0 * A4 * t * t - 2.0 * A2) * t - 2.0 * A1; }
+  __device__ double d2Q(double t) const { return 12.0 * A4 * t * t - 2.0 * A2; }
+  __device__ double cost(double t) const {
+    return (((A0 / t + A1) / t + A2) / t + A3) + A4 * t;
+  }
+};
+
+__device__ __forceinline__ Quartic make_quartic(const float *x0, const float *x1) {
+  const double g = (double)PUMP_G;
+  const double dx = (double)x1[0] - x0[0], dy = (double)x1[1] - x0[1], dz = (double)x1[2] - x0[2];
+  const double sx = (double)x0[3] + x1[3], sy = (double)x0[4] + x1[4], sz = (double)x0[5] + x1[5];
+  Quartic q;
+  q.A0 = 12.0 * (dx * dx + dy * dy + dz * dz);
+  q.A1 = -12.0 * (dx * sx + dy * sy + dz * sz);
+  const double v00 = (double)x0[3] * x0[3] + (double)x0[4] * x0[4] + (double)x0[5] * x0[5];
+  const double v11 = (double)x1[3] * x1[3] + (double)x1[4] * x1[4] + (double)x1[5] * x1[5];
+  const double v01 = (double)x0[3] * x1[3] + (double)x0[4] * x1[4] + (double)x0[5] * x1[5];
+  q.A2 = 4.0 * (v00 + v01 + v11);
+  q.A3 = 2.0 * g * ((double)x0[5] - x1[5]);
+  q.A4 = 1.0 + g * g;
+  return q;
+}
+
+// Root of a function monotone on [a, b] with f(a) and f(b) of opposite sign
+// (fa = f(a)); Newton steps kept inside the shrinking bracket, bisection
+// otherwise.  Which = 0: Q, 1: Q'.
+template <int Which>
+__device__ double bracket_root(const Quartic &q, double a, double b, double fa) {
+  double x = 0.5 * (a + b);
+  for (int it = 0; it < 100; ++it) {
+    const double f = Which == 0 ? q.Q(x) : q.dQ(x);
+    const double df = Which == 0 ? q.dQ(x) : q.d2Q(x);
+    if (f == 0.0) return x;
+    if ((f < 0.0) == (fa < 0.0)) a = x; else b = x;
+    double xn = x - f / df;
+    if (!(xn > a && xn < b)) xn = 0.5 * (a + b);
+    if (fabs(xn - x) <= 1e-16 * fabs(x) || b - a <= 4e-16 * b) return xn;
+    x = xn;
+  }
+  return x;
+}
+
+__device__ double precise_topt(const Quartic &q, double tmax) {
+  // breakpoints of Q's monotone pieces inside (0, tmax)
+  double bp[4];
+  int nb = 0;
+  bp[nb++] = 0.0;
+  const double tc = sqrt(q.A2 / (6.0 * q.A4));  // Q'' = 0
+  const double d0 = q.dQ(0.0);
+  if (tc > 0.0 && tc < tmax) {
+    const double dc = q.dQ(tc);
+    if (d0 > 0.0 && dc < 0.0) bp[nb++] = bracket_root<1>(q, 0.0, tc, d0);
+    if (dc < 0.0 && q.dQ(tmax) > 0.0) bp[nb++] = bracket_root<1>(q, tc, tmax, dc);
+  } else if (tc <= 0.0) {
+    if (d0 < 0.0 && q.dQ(tmax) > 0.0) bp[nb++] = bracket_root<1>(q, 0.0, tmax, d0);
+  } else {  // tc >= tmax: Q' decreasing on (0, tmax)
+    if (d0 > 0.0 && q.dQ(tmax) < 0.0) bp[nb++] = bracket_root<1>(q, 0.0, tmax, d0);
+  }
+  bp[nb++] = tmax;
+  double best_t = tmax, best_c = 0.0;
+  bool have = false;
+  const double qmax = q.Q(tmax);
+  if (qmax < 0.0) {
+    best_c = q.cost(tmax);
+    have = true;
+  }
+  for (int k = 0; k + 1 < nb; ++k) {
+    const double a = bp[k], b = bp[k + 1];
+    const double fa = q.Q(a), fb = (b == tmax) ? qmax : q.Q(b);
+    if (fa < 0.0 && fb > 0.0) {
+      const double r = bracket_root<0>(q, a, b, fa);
+      const double cr = q.cost(r);
+      if (!have || cr < best_c) {
+        best_c = cr;
+        best_t = r;
+        have = true;
+      }
+    }
+  }
+  return best_t;
+}
+
+// --------------------------------------------------------------- kernels
+__global__ void __launch_bounds__(128) bvp_pairs_parity_kernel(const float *__restrict__ samples,
+                                                               int N, float tmax,
+                                                               float *__restrict__ copts,
+                                                               float *__restrict__ topts) {
+  const long long npairs = (long long)N * (N - 1);
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < npairs;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / (N - 1));
+    const int r = (int)(idx - (long long)i * (N - 1));
+    const int j = r + (r >= i);
+    float x0[kDim], x1[kDim];
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) {
+      x0[d] = __ldg(&samples[i * kDim + d]);
+      x1[d] = __ldg(&samples[j * kDim + d]);
+    }
+    const PairCoef c = make_coef(x0, x1);
+    const float tp = topt_bisection(c, tmax);
+    topts[idx] = tp;
+    copts[idx] = cost_eval(c, tp);
+  }
+}
+
+__global__ void __launch_bounds__(128) bvp_pairs_precision_kernel(const float *__restrict__ samples,
+                                                                  int N, float tmax,
+                                                                  float *__restrict__ copts,
+                                                                  float *__restrict__ topts) {
+  const long long npairs = (long long)N * (N - 1);
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < npairs;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / (N - 1));
+    const int r = (int)(idx - (long long)i * (N - 1));
+    const int j = r + (r >= i);
+    float x0[kDim], x1[kDim];
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) {
+      x0[d] = __ldg(&samples[i * kDim + d]);
+      x1[d] = __ldg(&samples[j * kDim + d]);
+    }
+    const Quartic q = make_quartic(x0, x1);
+    const double t = precise_topt(q, (double)tmax);
+    topts[idx] = (float)t;
+    copts[idx] = (float)q.cost(t);
+  }
+}
+
+__global__ void bvp_batch_kernel(const float *__restrict__ x0s, const float *__restrict__ x1s,
+                                 int n, float tmax, int mode, float *__restrict__ topt,
+                                 float *__restrict__ cost) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  float x0[kDim], x1[kDim];
+#pragma unroll
+  for (int d = 0; d < kDim; ++d) {
+    x0[d] = x0s[k * kDim + d];
+    x1[d] = x1s[k * kDim + d];
+  }
+  if (mode == PUMP_BVP_PARITY) {
+    const PairCoef c = make_coef(x0, x1);
+    const float tp = topt_bisection(c, tmax);
+    if (topt) topt[k] = tp;
+    if (cost) cost[k] = cost_eval(c, tp);
+  } else {
+    const Quartic q = make_quartic(x0, x1);
+    const double t = precise_topt(q, (double)tmax);
+    if (topt) topt[k] = (float)t;
+    if (cost) cost[k] = (float)q.cost(t);
+  }
+}
+
+// pathPoint, 2pBVP.cu:117-131, in the expression's own evaluation types.
+__device__ __forceinline__ void path_point(float t, float tau, const float *x0, const float *x1,
+                                           float *x) {
+  const double t2 = p2f(t), t3 = p3f(t), u2 = p2f(tau), u3 = p3f(tau);
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int a = k, b = k + 3;
+    double r = (double)(t * x0[b] + x0[a]);
+    r = r + (t3 * (double)(2 * x0[a] - 2 * x1[a] + (x0[b] + x1[b]) * tau)) / u3;
+    r = r - (t2 * (double)(3 * x0[a] - 3 * x1[a] + (2 * x0[b] + x1[b]) * tau)) / u2;
+    x[k] = (float)r;
+  }
+  {
+    double r = (double)(t * x0[5]) * u3 + (double)x0[2] * u3;
+    double q1 = -3. * x0[2] + 3. * x1[2] - 2. * x0[5] * tau - 1. * x1[5] * tau;
+    r = r + (t2 * (double)tau) * q1;
+    double q2 = 2. * x0[2] - 2. * x1[2] + (double)((x0[5] + x1[5]) * tau);
+    r = r + t3 * q2;
+    x[2] = (float)(r / u3);
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int a = k, b = k + 3;
+    float f1 = -(2 * t * (3 * x0[a] - 3 * x1[a] + x1[b] * tau));
+    double r = (double)f1 / u2;
+    r = r + (3 * t2 * (double)(2 * x0[a] - 2 * x1[a] + x1[b] * tau)) / u3;
+    double inner = 3 * t2 - (double)(4 * t * tau) + u2;
+    r = r + ((double)x0[b] * inner) / u2;
+    x[3 + k] = (float)r;
+  }
+  {
+    double r = (double)x0[5] * u3;
+    double q1 = -6. * x0[2] + 6. * x1[2] - 4. * x0[5] * tau - 2. * x1[5] * tau;
+    r = r + (double)(t * tau) * q1;
+    double q2 = 6. * x0[2] - 6. * x1[2] + 3. * x0[5] * tau + 3. * x1[5] * tau;
+    r = r + t2 * q2;
+    x[5] = (float)(r / u3);
+  }
+}
+
+// One thread per (edge, waypoint): findDiscretizedPath, 2pBVP.cu:53-69.
+__global__ void discretize_kernel(const float *__restrict__ samples, const int *__restrict__ src,
+                                  const int *__restrict__ dst, const float *__restrict__ toptE,
+                                  long long E, int numDisc, float *__restrict__ disc) {
+  const int W = numDisc + 1;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (tid >= E * W) return;
+  const long long e = tid / W;
+  const int i = (int)(tid - e * W);
+  const int a = src[e], b = dst[e];
+  float x0[kDim], x1[kDim], x[kDim];
+#pragma unroll
+  for (int d = 0; d < kDim; ++d) {
+    x0[d] = __ldg(&samples[a * kDim + d]);
+    x1[d] = __ldg(&samples[b * kDim + d]);
+  }
+  if (i == 0) {
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) x[d] = x0[d];
+  } else if (i == numDisc) {
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) x[d] = x1[d];
+  } else {
+    const float topt = toptE[e];
+    const float dt = topt / numDisc;
+    path_point(dt * i, topt, x0, x1, x);
+  }
+  float *o = disc + tid * kDim;
+#pragma unroll
+  for (int d = 0; d < kDim; ++d) o[d] = x[d];
+}
+
+// Dense path of findOptimalPath (2pBVP.cu:5-36) for one segment: the host
+// side computes the per-segment sample counts and time offsets (they are a
+// short sequential recurrence); this kernel evaluates the states.
+__global__ void path_states_kernel(const float *__restrict__ xs, const int *__restrict__ seg,
+                                   const float *__restrict__ tsample, const float *__restrict__ tau,
+                                   int total, float *__restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  const int s = seg[k];
+  float x[kDim];
+  path_point(tsample[k], tau[s], &xs[s * kDim], &xs[(s + 1) * kDim], x);
+#pragma unroll
+  for (int d = 0; d < kDim; ++d) out[k * kDim + d] = x[d];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
+                              const float *d_tau, int total, float *d_out, cudaStream_t stream) {
+  if (total <= 0) return PUMP_OK;
+  path_states_kernel<<<grid_for(total, 128), 128, 0, stream>>>(d_xs, d_seg, d_tsample, d_tau,
+                                                              total, d_out);
+  return launch_status("path_states_kernel");
+}
+
+}  // namespace pump
+
+using namespace pump;
+
+extern "C" pump_status_t pump_bvp_pairs(const float *d_samples, int N, float tmax, int mode,
+                                        float *d_copts, float *d_topts, pump_stream_t stream) {
+  if (N < 2 || !d_samples || !d_copts || !d_topts || !(tmax > 0))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_bvp_pairs: bad arguments (N=%d)", N);
+  const long long npairs = (long long)N * (N - 1);
+  const int threads = 128;
+  long long blocks = (npairs + threads - 1) / threads;
+  if (blocks > 2147483647LL) blocks = 2147483647LL;
+  if (mode == PUMP_BVP_PARITY)
+    bvp_pairs_parity_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(
+        d_samples, N, tmax, d_copts, d_topts);
+  else if (mode == PUMP_BVP_PRECISION)
+    bvp_pairs_precision_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(
+        d_samples, N, tmax, d_copts, d_topts);
+  else
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_bvp_pairs: unknown mode %d", mode);
+  return launch_status("bvp_pairs");
+}
+
+extern "C" pump_status_t pump_bvp_batch(const float *d_x0, const float *d_x1, int n, float tmax,
+                                        int mode, float *d_topt, float *d_cost,
+                                        pump_stream_t stream) {
+  if (n < 0 || (n > 0 && (!d_x0 || !d_x1)) || !(tmax > 0) ||
+      (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_bvp_batch: bad arguments");
+  if (n == 0) return PUMP_OK;
+  bvp_batch_kernel<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(d_x0, d_x1, n, tmax, mode,
+                                                                      d_topt, d_cost);
+  return launch_status("bvp_batch");
+}
+
+extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src,
+                                               const int *d_dst, const float *d_topt, long long E,
+                                               int numDisc, float *d_disc, pump_stream_t stream) {
+  if (E < 0 || numDisc < 1 || (E > 0 && (!d_samples || !d_src || !d_dst || !d_topt || !d_disc)))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_discretize_edges: bad arguments");
+  if (E == 0) return PUMP_OK;
+  const long long n = E * (numDisc + 1);
+  discretize_kernel<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(d_samples, d_src, d_dst,
+                                                                       d_topt, E, numDisc, d_disc);
+  return launch_status("discretize_edges");
+}

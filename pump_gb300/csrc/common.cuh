@@ -1,0 +1,54 @@
+// Shared definitions of the pump_gb300 CUDA sources.
+//
+// All translation units are compiled for sm_103a with -fmad=false: no
+// multiply-add is contracted unless written as an explicit fma(), so every
+// expression rounds exactly as the reference's C++ source does on a CPU.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pump.h"
+
+namespace pump {
+
+constexpr int kDim = 6;
+constexpr int kThreads = 256;
+constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs
+
+// Records msg as this thread's last error; returns s.
+pump_status_t set_error(pump_status_t s, const char *fmt, ...);
+// Maps a CUDA error to PUMP_ERR_CUDA with its message; PUMP_OK on success.
+pump_status_t cuda_status(cudaError_t e, const char *where);
+// cuda_status(cudaGetLastError()) after a launch.
+pump_status_t launch_status(const char *kernel);
+
+#define PUMP_CUDA_TRY(expr)                                     \
+  do {                                                          \
+    cudaError_t pump_ce_ = (expr);                                    \
+    if (pump_ce_ != cudaSuccess) return ::pump::cuda_status(pump_ce_, #expr); \
+  } while (0)
+#define PUMP_TRY(expr)                  \
+  do {                                  \
+    pump_status_t pump_st_ = (expr);          \
+    if (pump_st_ != PUMP_OK) return pump_st_;       \
+  } while (0)
+
+inline unsigned int grid_for(long long n, int threads) {
+  long long g = (n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  return (unsigned int)g;
+}
+
+// ---------------------------------------------------------------------------
+// Integer powers of a float promoted to double, correctly rounded: the square
+// of a float is exact in binary64, so each result below is rounded once.
+// (The reference writes pow(float, int), promoted to pow(double, double).)
+__host__ __device__ __forceinline__ double p2f(float x) { double d = x; return d * d; }
+__host__ __device__ __forceinline__ double p3f(float x) { double d = x; return (d * d) * d; }
+__host__ __device__ __forceinline__ double p4f(float x) { double d = x; double s = d * d; return s * s; }
+
+// `const float g = -9.81;` (2pBVP.cu:3)
+#define PUMP_G ((float)-9.81)
+
+}  // namespace pump

@@ -1,0 +1,385 @@
+// Particle stream, half-space Monte Carlo (HSMC) propagation and full Monte
+// Carlo collision probability (reference: PUMP.cu:613-758,
+// collisionProbability.cu:4-92, hardCoded.cuh:12-19).
+//
+// Particle stream.  The reference reads precomputed closed-loop tracking
+// errors (xcomb / xcombTime) from a data file that is not part of its source
+// tree.  They are regenerated here from a documented model: per axis a
+// double integrator at dt = 0.05 s under the PD tracking law a = w - (16 p +
+// 5.6 v), w ~ N(0, 4^2), starting from zero error, simulated in binary64.
+// Noise comes from Philox4x32-10 (Salmon et al., SC'11) at counter
+// (particle, step, 0, 0), turned into Gaussians by Box-Muller whose log and
+// sine/cosine are evaluated by fixed series with +,-,*,/ and sqrt only
+// (atanh series for log, Taylor series on a quarter period for sin/cos), so
+// the table is bit-identical on any IEEE machine that does not contract
+// multiply-adds.
+//
+// HSMC.  One block per new path, threads over particles.  The half-spaces of
+// a waypoint are the same for every particle of the path, so each test is a
+// block-uniform branch on b >= 1000 followed by a 3-term dot product against
+// the particle's offset row; offsets are read time-major so a warp reads 32
+// consecutive particles (384 contiguous bytes).  Validity is kept as a bit
+// per particle (__ballot_sync), and the hit count of calculateCP_HSMC is the
+// block's popcount sum, so the CP needs no second pass over a byte array.
+//
+// Monte Carlo CP.  Thread per (particle, path) over many paths per launch;
+// obstacles staged in shared memory; the same segment test as freeEdges.
+#include "collide.cuh"
+
+namespace pump {
+namespace {
+
+// ------------------------------------------------------- particle stream
+__device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                              uint32_t k0, uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+__device__ double det_log(double x) {
+  int e;
+  double m = frexp(x, &e);
+  if (m < 0.70710678118654752440) { m = m * 2.0; e = e - 1; }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double z = s * s;
+  double t = 1.0 / 25.0;
+  t = t * z + 1.0 / 23.0;
+  t = t * z + 1.0 / 21.0;
+  t = t * z + 1.0 / 19.0;
+  t = t * z + 1.0 / 17.0;
+  t = t * z + 1.0 / 15.0;
+  t = t * z + 1.0 / 13.0;
+  t = t * z + 1.0 / 11.0;
+  t = t * z + 1.0 / 9.0;
+  t = t * z + 1.0 / 7.0;
+  t = t * z + 1.0 / 5.0;
+  t = t * z + 1.0 / 3.0;
+  t = t * z + 1.0;
+  return (double)e * 0.69314718055994530942 + 2.0 * s * t;
+}
+
+__device__ void det_sincos_2pi(double u, double *s, double *c) {
+  const double q = u * 4.0;
+  const int k = (int)q;
+  const double f = q - (double)k;
+  const double th = f * 1.57079632679489661923;
+  const double z = th * th;
+  double sn = -1.0 / 15511210043330985984000000.0;
+  sn = sn * z + 1.0 / 25852016738884976640000.0;
+  sn = sn * z - 1.0 / 51090942171709440000.0;
+  sn = sn * z + 1.0 / 121645100408832000.0;
+  sn = sn * z - 1.0 / 355687428096000.0;
+  sn = sn * z + 1.0 / 1307674368000.0;
+  sn = sn * z - 1.0 / 6227020800.0;
+  sn = sn * z + 1.0 / 39916800.0;
+  sn = sn * z - 1.0 / 362880.0;
+  sn = sn * z + 1.0 / 5040.0;
+  sn = sn * z - 1.0 / 120.0;
+  sn = sn * z + 1.0 / 6.0;
+  sn = sn * z - 1.0;
+  sn = -(sn * th);
+  double cs = 1.0 / 620448401733239439360000.0;
+  cs = cs * z - 1.0 / 1124000727777607680000.0;
+  cs = cs * z + 1.0 / 2432902008176640000.0;
+  cs = cs * z - 1.0 / 6402373705728000.0;
+  cs = cs * z + 1.0 / 20922789888000.0;
+  cs = cs * z - 1.0 / 87178291200.0;
+  cs = cs * z + 1.0 / 479001600.0;
+  cs = cs * z - 1.0 / 3628800.0;
+  cs = cs * z + 1.0 / 40320.0;
+  cs = cs * z - 1.0 / 720.0;
+  cs = cs * z + 1.0 / 24.0;
+  cs = cs * z - 0.5;
+  cs = cs * z + 1.0;
+  switch (k & 3) {
+    case 0: *s = sn; *c = cs; break;
+    case 1: *s = cs; *c = -sn; break;
+    case 2: *s = -sn; *c = -cs; break;
+    default: *s = -cs; *c = sn; break;
+  }
+}
+
+constexpr double kDT = 0.05, kH2 = 0.00125, kKP = 16.0, kKD = 5.6, kSigmaW = 4.0;
+
+__global__ void particle_table_kernel(uint32_t k0, uint32_t k1, int P, int T,
+                                      float *__restrict__ tmajor, float *__restrict__ pmajor) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double pos[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
+  const double sc = 2.3283064365386962890625e-10;  // 2^-32
+  for (int t = 0; t < T; ++t) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float v = (float)pos[d];
+      if (tmajor) tmajor[((long long)t * P + p) * 3 + d] = v;
+      if (pmajor) pmajor[((long long)p * T + t) * 3 + d] = v;
+    }
+    uint32_t o[4];
+    philox4x32_10((uint32_t)p, (uint32_t)t, 0u, 0u, k0, k1, o);
+    const double u0 = ((double)o[0] + 0.5) * sc, u1 = ((double)o[1] + 0.5) * sc;
+    const double u2 = ((double)o[2] + 0.5) * sc, u3 = ((double)o[3] + 0.5) * sc;
+    const double r0 = sqrt(-2.0 * det_log(u0));
+    const double r1 = sqrt(-2.0 * det_log(u2));
+    double s0, c0, s1, c1;
+    det_sincos_2pi(u1, &s0, &c0);
+    det_sincos_2pi(u3, &s1, &c1);
+    const double z[3] = {r0 * c0, r0 * s0, r1 * c1};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double a = kSigmaW * z[d] - (kKP * pos[d] + kKD * vel[d]);
+      const double pn = (pos[d] + kDT * vel[d]) + kH2 * a;
+      const double vn = vel[d] + kDT * a;
+      pos[d] = pn;
+      vel[d] = vn;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ HSMC
+// Block = one new path; blockDim multiple of 32, threads loop over
+// particles in strides of blockDim.
+__global__ void __launch_bounds__(256) hsmc_kernel(
+    int W, const int *__restrict__ wf_edge, const int *__restrict__ wf_prev, long long num_edges,
+    int num_prev, const float *__restrict__ as, const float *__restrict__ bs, int maxHS,
+    const float *__restrict__ times, const float *__restrict__ topts, float dt,
+    const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
+    const uint32_t *valid_in, uint32_t *valid_out, int P, float *__restrict__ cp_out,
+    int *__restrict__ error) {
+  // valid_in[prev] is read, valid_out[w] / cp_out[w] written (the two may
+  // alias one path store with valid_out = store + base, as in the reference)
+  __shared__ int s_hits[8];
+  const int w = blockIdx.x;
+  const int edge = wf_edge[w], prev = wf_prev[w];
+  if (edge < 0 || edge >= num_edges || prev < 0 || prev >= num_prev) {  // block-uniform
+    if (threadIdx.x == 0 && error) atomicExch(error, (int)PUMP_ERR_BAD_INPUT);
+    return;
+  }
+  const int words = (P + 31) >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float dtLocal = topts[edge] / (W - 1);
+  const float t0 = times[prev];
+  const long long hsHead = (long long)edge * W * maxHS;
+  int hits = 0;
+  bool overflow = false;
+  for (int pbase = 0; pbase < P; pbase += blockDim.x) {
+    const int p = pbase + threadIdx.x;
+    const bool live = p < P;
+    bool vp = false;
+    if (live) vp = (valid_in[(long long)prev * words + (p >> 5)] >> (p & 31)) & 1u;
+    for (int i = 0; i < W; ++i) {
+      const float time = t0 + i * dtLocal;
+      int dtIdx = (int)(time / dt);
+      const long long h0 = hsHead + (long long)i * maxHS;
+      bool row_loaded = false;
+      float ox = 0.f, oy = 0.f, oz = 0.f;
+      for (int o = 0; o < maxHS; ++o) {
+        const float b = __ldg(&bs[h0 + o]);
+        if (b >= 1000) continue;  // block-uniform
+        if (!row_loaded) {
+          if (dtIdx < 0 || dtIdx >= T_rows) {
+            overflow = true;
+            dtIdx = dtIdx < 0 ? 0 : T_rows - 1;
+          }
+          if (live) {
+            const float *off = offsets_t + ((long long)dtIdx * Pmc + p) * 3;
+            ox = __ldg(&off[0]);
+            oy = __ldg(&off[1]);
+            oz = __ldg(&off[2]);
+          }
+          row_loaded = true;
+        }
+        const float *a = &as[(h0 + o) * 3];
+        float LHS = 0;
+        LHS += ox * __ldg(&a[0]);
+        LHS += oy * __ldg(&a[1]);
+        LHS += oz * __ldg(&a[2]);
+        vp = vp & (LHS * offset_mult < b);
+      }
+    }
+    const unsigned int bal = __ballot_sync(0xffffffffu, vp && live);
+    if (lane == 0 && (pbase >> 5) + warp < words) valid_out[(long long)w * words + (pbase >> 5) + warp] = bal;
+    hits += live && !vp;
+  }
+  // block reduction of the hit count
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) hits += __shfl_down_sync(0xffffffffu, hits, off);
+  if (lane == 0) s_hits[warp] = hits;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int total = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) total += s_hits[k];
+    cp_out[w] = ((float)total) / P;
+  }
+  if (overflow && error && lane == 0) atomicExch(error, (int)PUMP_ERR_CAPACITY);
+}
+
+// -------------------------------------------------------------- MC CP
+// grid (ceil(Pmc / blockDim), n_paths); collisionProbability.cu:39-92.
+__global__ void __launch_bounds__(256) mc_cp_kernel(
+    const float *__restrict__ paths, const int *__restrict__ offset, const int *__restrict__ len,
+    const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
+    const float *__restrict__ obs, int numObs, int k0, int *__restrict__ hits) {
+  extern __shared__ float4 s_obs4[];
+  float *s_obs = reinterpret_cast<float *>(s_obs4);
+  __shared__ int s_hits[8];
+  stage_obstacles(obs, numObs, s_obs);
+  const int k = k0 + blockIdx.y;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int T = len[k];
+  const float *path = paths + (long long)offset[k] * kDim;
+  int coll = 0;
+  if (p < Pmc && T <= T_rows) {
+    float v[3], w[3];
+    if (T - 2 > 0) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v[d] = path[d] + __ldg(&offsets_t[(long long)p * 3 + d]) * offset_mult;
+    }
+    for (int t = 0; t < T - 2; ++t) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        w[d] = path[(t + 1) * kDim + d] +
+               __ldg(&offsets_t[((long long)(t + 1) * Pmc + p) * 3 + d]) * offset_mult;
+      if (!segment_valid(v, w, numObs, s_obs)) {
+        coll = 1;
+        break;
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v[d] = w[d];
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) coll += __shfl_down_sync(0xffffffffu, coll, off);
+  if (lane == 0) s_hits[warp] = coll;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int total = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) total += s_hits[q];
+    if (total) atomicAdd(&hits[k], total);
+  }
+}
+
+__global__ void mc_cp_finish_kernel(const int *__restrict__ hits, const int *__restrict__ len,
+                                    int n, int Pmc, int T_rows, float *__restrict__ cp,
+                                    int *__restrict__ error) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  cp[k] = ((float)hits[k]) / ((float)Pmc);
+  if (len[k] > T_rows && error) atomicExch(error, (int)PUMP_ERR_CAPACITY);
+}
+
+__global__ void gather_words_kernel(const uint32_t *__restrict__ src, const int *__restrict__ map,
+                                    int n, int words, uint32_t *__restrict__ dst) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)n * words) return;
+  const int k = (int)(t / words), j = (int)(t - (long long)k * words);
+  dst[t] = src[(long long)map[k] * words + j];
+}
+
+}  // namespace
+
+pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
+                          const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
+                          const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
+                          int *d_error, cudaStream_t stream) {
+  if (n_paths <= 0) return PUMP_OK;
+  const size_t smem = (size_t)numObs * 12 * sizeof(float);
+  if (smem > 200 * 1024) return set_error(PUMP_ERR_CAPACITY, "mc_cp: %d obstacles", numObs);
+  if (smem > 48 * 1024)
+    PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)mc_cp_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PUMP_CUDA_TRY(cudaMemsetAsync(d_hits, 0, sizeof(int) * n_paths, stream));
+  for (int k0 = 0; k0 < n_paths; k0 += 65535) {
+    const int nk = n_paths - k0 < 65535 ? n_paths - k0 : 65535;
+    dim3 grid(grid_for(Pmc, 256), (unsigned)nk);
+    mc_cp_kernel<<<grid, 256, smem, stream>>>(d_paths, d_offset, d_len, d_offsets_t, Pmc, T_rows,
+                                              offset_mult, d_obstacles, numObs, k0, d_hits);
+    PUMP_TRY(launch_status("mc_cp_kernel"));
+  }
+  mc_cp_finish_kernel<<<grid_for(n_paths, 128), 128, 0, stream>>>(d_hits, d_len, n_paths, Pmc,
+                                                                  T_rows, d_cp, d_error);
+  return launch_status("mc_cp_finish_kernel");
+}
+
+pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int *d_prev,
+                                long long num_edges, int num_prev, const float *d_as, const float *d_bs, int maxHS,
+                                const float *d_times, const float *d_topt, float dt,
+                                const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
+                                const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
+                                float *d_cp_out, int *d_error, cudaStream_t stream) {
+  if (num_new <= 0) return PUMP_OK;
+  if (num_new > 2147483647) return set_error(PUMP_ERR_CAPACITY, "hsmc: wavefront too large");
+  int threads = ((P + 31) / 32) * 32;
+  if (threads > 256) threads = 256;
+  hsmc_kernel<<<num_new, threads, 0, stream>>>(W, d_edge, d_prev, num_edges, num_prev, d_as, d_bs,
+                                               maxHS, d_times, d_topt,
+                                               dt, d_offsets_t, Pmc, T_rows, offset_mult,
+                                               d_valid_in, d_valid_out, P, d_cp_out, d_error);
+  return launch_status("hsmc_kernel");
+}
+
+pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n, int words,
+                                 uint32_t *d_dst, cudaStream_t stream) {
+  if (n <= 0) return PUMP_OK;
+  const long long total = (long long)n * words;
+  gather_words_kernel<<<grid_for(total, 256), 256, 0, stream>>>(d_src, d_map, n, words, d_dst);
+  return launch_status("gather_words_kernel");
+}
+
+pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
+                                    cudaStream_t stream) {
+  particle_table_kernel<<<grid_for(P, 128), 128, 0, stream>>>((uint32_t)seed, (uint32_t)(seed >> 32),
+                                                             P, T, d_tmajor, d_pmajor);
+  return launch_status("particle_table_kernel");
+}
+
+}  // namespace pump
+
+using namespace pump;
+
+extern "C" pump_status_t pump_particle_tables(uint64_t seed, int P, int T, float *d_tmajor,
+                                              float *d_pmajor, pump_stream_t stream) {
+  if (P <= 0 || T <= 0 || (!d_tmajor && !d_pmajor))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_particle_tables: bad arguments");
+  return particle_tables_async(seed, P, T, d_tmajor, d_pmajor, (cudaStream_t)stream);
+}
+
+extern "C" pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_edge, const int *d_prev,
+                                             long long num_edges, int base, const float *d_as,
+                                             const float *d_bs,
+                                             int maxHS, const float *d_times, const float *d_topt,
+                                             float dt, const float *d_offsets_t, int Pmc,
+                                             int T_rows, float offset_mult, uint32_t *d_valid,
+                                             int P, float *d_path_cp, int *d_error,
+                                             pump_stream_t stream) {
+  if (num_new < 0 || W < 2 || maxHS < 0 || P <= 0 || P > Pmc || T_rows <= 0 || base < 0 ||
+      num_edges < 0 ||
+      (num_new > 0 && (!d_edge || !d_prev || !d_times || !d_topt || !d_offsets_t || !d_valid ||
+                       !d_path_cp || (maxHS > 0 && (!d_as || !d_bs)))))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_hsmc_propagate: bad arguments");
+  const size_t words = (size_t)((P + 31) / 32);
+  return hsmc_staged_async(num_new, W, d_edge, d_prev, num_edges, base, d_as, d_bs, maxHS, d_times,
+                           d_topt, dt,
+                           d_offsets_t, Pmc, T_rows, offset_mult, d_valid,
+                           d_valid + (size_t)base * words, P, d_path_cp + base, d_error,
+                           (cudaStream_t)stream);
+}
+
+extern "C" pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d_len,
+                                    int n_paths, const float *d_offsets_t, int Pmc, int T_rows,
+                                    float offset_mult, const float *d_obstacles, int numObs,
+                                    int *d_hits, float *d_cp, int *d_error, pump_stream_t stream) {
+  if (n_paths < 0 || Pmc <= 0 || T_rows <= 0 || numObs < 0 || (numObs > 0 && !d_obstacles) ||
+      (n_paths > 0 && (!d_paths || !d_offset || !d_len || !d_offsets_t || !d_hits || !d_cp)))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_mc_cp: bad arguments");
+  return mc_cp_async(d_paths, d_offset, d_len, n_paths, d_offsets_t, Pmc, T_rows, offset_mult,
+                     d_obstacles, numObs, d_hits, d_cp, d_error, (cudaStream_t)stream);
+}

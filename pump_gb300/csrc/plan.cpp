@@ -1,0 +1,729 @@
+// One PUMP planning query on the GPU (reference: mainPUMP.cu:248-687 and
+// PUMP(), PUMP.cu:3-607).
+//
+// Device work: pair BVPs, rn selection, edge compaction, waypoints,
+// heuristic, sample/edge collision checks, half-spaces, the particle table,
+// HSMC propagation of every wavefront, and the dense paths and Monte Carlo
+// CP of goal candidates and smoothing iterates.  Host work is the same
+// sequential bookkeeping the reference does on the host: wavefront
+// expansion, the CP cut-off, epsilon-dominance with the path-index
+// tie-break, survivor compaction into cost buckets, and the alpha bisection
+// of the smoothing loop.  Differences in structure, not in results:
+//  - the reference copies each survivor's particle mask with one
+//    cudaMemcpy (PUMP.cu:236-237); here survivors are gathered by one kernel;
+//  - the reference evaluates goal candidates one at a time until one meets
+//    the CP target (PUMP.cu:371-405); here all candidates' dense paths and
+//    MC CPs are computed in one batch and the first in (cost, index) order
+//    that meets the target is taken, which selects the same path;
+//  - adjacency is a CSR over edges sorted by (source, target) instead of the
+//    N x N nnIdxs table (mainPUMP.cu:315, 338).
+// Host arithmetic follows the reference's float expressions and is compiled
+// without multiply-add contraction.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <utility>
+#include <vector>
+
+#include "common.cuh"
+#include "ctx.h"
+
+namespace pump {
+
+pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int *d_prev,
+                                long long num_edges, int num_prev, const float *d_as, const float *d_bs, int maxHS,
+                                const float *d_times, const float *d_topt, float dt,
+                                const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
+                                const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
+                                float *d_cp_out, int *d_error, cudaStream_t stream);
+pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n, int words,
+                                 uint32_t *d_dst, cudaStream_t stream);
+pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
+                          const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
+                          const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
+                          int *d_error, cudaStream_t stream);
+pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
+                                    cudaStream_t stream);
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+double ms_since(clk::time_point t0) {
+  return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+}
+
+// Owning device buffer.
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { if (p) cudaFree(p); }
+  pump_status_t alloc(size_t count) {
+    if (count <= n && p) return PUMP_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    PUMP_CUDA_TRY(cudaMalloc(&p, sizeof(T) * (count ? count : 1)));
+    n = count;
+    return PUMP_OK;
+  }
+};
+
+// sampler.cu:43-57
+float halton(int n, int b) {
+  float hn = 0;
+  int n0 = n;
+  float f = 1 / ((float)b);
+  while (n0 > 0) {
+    float n1 = (float)(n0 / b);
+    int r = (int)(n0 - n1 * b);
+    hn += f * r;
+    f = f / b;
+    n0 = (int)n1;
+  }
+  return hn;
+}
+
+// sampler.cu:20-41 (bases 2, 3, 5, 7, 11, 13 with skip 0)
+void halton_samples(const pump_problem &pb, std::vector<float> &s) {
+  static const int bases[6] = {2, 3, 5, 7, 11, 13};
+  const int N = pb.N;
+  s.assign((size_t)N * kDim, 0.0f);
+  for (int d = 0; d < kDim; ++d)
+    for (int n = 0; n < N; ++n)
+      s[(size_t)n * kDim + d] = halton(n, bases[d]) * (pb.hi[d] - pb.lo[d]) + pb.lo[d];
+  for (int d = 0; d < kDim; ++d) {
+    s[d] = pb.init[d];
+    s[(size_t)(N - 1) * kDim + d] = pb.goal[d];
+  }
+}
+
+// Batch of dense paths along node sequences (findOptimalPath, 2pBVP.cu:5-36):
+// segment optimal times on the GPU, the sample-time recurrence on the host,
+// the states on the GPU.
+struct DensePaths {
+  std::vector<int> offset, len;  // per path, in states
+  int total = 0;
+};
+
+class Planner {
+ public:
+  Planner(Ctx *ctx, const pump_problem &pb, pump_plan_result *res, cudaStream_t s)
+      : ctx_(ctx), pb_(pb), res_(res), s_(s) {}
+  pump_status_t run();
+
+ private:
+  pump_status_t roadmap();
+  pump_status_t online();
+  pump_status_t explore();
+  pump_status_t search_and_smooth();
+  pump_status_t dense_paths(const std::vector<std::vector<float>> &xs, float dt, float tmax,
+                            DensePaths &out, DevBuf<float> &d_states);
+  pump_status_t topts_of(const std::vector<float> &x0, const std::vector<float> &x1, float tmax,
+                         std::vector<float> *topt, std::vector<float> *cost);
+  pump_status_t mc_cp_batch(const DevBuf<float> &d_states, const DensePaths &dp,
+                            std::vector<float> &cp);
+  pump_status_t sync() { return cuda_status(cudaStreamSynchronize(s_), "cudaStreamSynchronize"); }
+  template <class T>
+  pump_status_t h2d(T *d, const T *h, size_t n) {
+    if (n == 0) return PUMP_OK;
+    res_->h2d_bytes += (long long)(sizeof(T) * n);
+    return cuda_status(cudaMemcpyAsync(d, h, sizeof(T) * n, cudaMemcpyHostToDevice, s_), "H2D");
+  }
+  template <class T>
+  pump_status_t d2h(T *h, const T *d, size_t n) {
+    if (n == 0) return PUMP_OK;
+    res_->d2h_bytes += (long long)(sizeof(T) * n);
+    return cuda_status(cudaMemcpyAsync(h, d, sizeof(T) * n, cudaMemcpyDeviceToHost, s_), "D2H");
+  }
+  std::vector<float> node_states(int path_idx, std::vector<int> *nodes) const;
+
+  Ctx *ctx_;
+  const pump_problem &pb_;
+  pump_plan_result *res_;
+  cudaStream_t s_;
+
+  // problem constants (mainPUMP.cu:51-72)
+  const float dt_ = (float)0.05;
+  const float lambda_ = (float)0.5;
+  const int numBuckets_ = 2;
+  const float epsCost_ = (float)0.0002, epsCP_ = (float)0.0002;
+  int N_ = 0, W_ = 0, P_ = 0, words_ = 0, maxHS_ = 0, nobs_ = 0;
+
+  std::vector<float> samples_;
+  DevBuf<float> d_samples_, d_obs_, d_copts_, d_topts_;
+  DevBuf<int> d_src_, d_dst_, d_go_;
+  DevBuf<float> d_coptE_, d_toptE_, d_disc_, d_as_, d_bs_, d_tmajor_;
+  DevBuf<uint8_t> d_free_s_, d_free_e_;
+  long long E_ = 0;
+  float rn_ = 0;
+  std::vector<int> dst_, go_;
+  std::vector<float> coptE_, toptE_, h_;
+  std::vector<uint8_t> free_s_, free_e_;
+
+  // exploration state (mainPUMP.cu:623-681)
+  int maxPathCount_ = 0;
+  std::vector<int> pathPrev_, pathNode_;
+  std::vector<float> pathCost_, pathTime_, pathCP_;
+  std::vector<std::vector<int>> atNode_;
+  DevBuf<uint32_t> d_valid_, d_stage_;
+  DevBuf<float> d_pathTime_, d_cpStage_;
+  DevBuf<int> d_wfPrev_, d_wfEdge_, d_map_, d_err_;
+  int numPaths_ = 0;
+};
+
+pump_status_t Planner::run() {
+  const auto t0 = clk::now();
+  N_ = pb_.N;
+  W_ = pb_.num_disc + 1;
+  P_ = pb_.num_hsmc;
+  words_ = (P_ + 31) / 32;
+  nobs_ = pb_.num_obstacles;
+  maxHS_ = nobs_ > 5 ? 5 : nobs_;  // mainPUMP.cu:241
+  auto t = clk::now();
+  PUMP_TRY(roadmap());
+  res_->ms_roadmap = ms_since(t);
+  t = clk::now();
+  PUMP_TRY(online());
+  res_->ms_online = ms_since(t);
+  t = clk::now();
+  pump_status_t st = explore();
+  res_->ms_explore = ms_since(t);
+  if (st == PUMP_OK) {
+    t = clk::now();
+    st = search_and_smooth();
+    res_->ms_search = ms_since(t);
+  }
+  res_->ms_total = ms_since(t0);
+  return st;
+}
+
+pump_status_t Planner::roadmap() {
+  if (pb_.samples) samples_.assign(pb_.samples, pb_.samples + (size_t)N_ * kDim);
+  else halton_samples(pb_, samples_);
+  PUMP_TRY(d_samples_.alloc((size_t)N_ * kDim));
+  PUMP_TRY(h2d(d_samples_.p, samples_.data(), samples_.size()));
+  const long long npairs = (long long)N_ * (N_ - 1);
+  PUMP_TRY(d_copts_.alloc(npairs));
+  PUMP_TRY(d_topts_.alloc(npairs));
+  PUMP_TRY(pump_bvp_pairs(d_samples_.p, N_, 5.0f, pb_.bvp_mode, d_copts_.p, d_topts_.p,
+                          (pump_stream_t)s_));
+  // mainPUMP.cu:261-262: (int)((NUM-1)*(NUM)*rnPerc) with rnPerc a float
+  const long long rnIdx = (long long)((float)((long long)(N_ - 1) * N_) * (float)0.05);
+  const float *d_rn = nullptr;
+  PUMP_TRY(select_kth_device(ctx_, d_copts_.p, npairs, rnIdx, &d_rn, s_));
+  PUMP_TRY(d2h(&rn_, d_rn, 1));
+  PUMP_TRY(sync());
+  res_->rn = rn_;
+  const long long cap = rnIdx > 0 ? rnIdx : 1;
+  PUMP_TRY(d_src_.alloc(cap));
+  PUMP_TRY(d_dst_.alloc(cap));
+  PUMP_TRY(d_coptE_.alloc(cap));
+  PUMP_TRY(d_toptE_.alloc(cap));
+  PUMP_TRY(d_go_.alloc(N_ + 1));
+  PUMP_TRY(build_edges_device(ctx_, d_copts_.p, d_topts_.p, N_, rn_, cap, d_src_.p, d_dst_.p,
+                              d_coptE_.p, d_toptE_.p, d_go_.p, &E_, s_));
+  res_->num_edges = E_;
+  PUMP_TRY(d_disc_.alloc((size_t)E_ * W_ * kDim));
+  PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, d_toptE_.p, E_, pb_.num_disc,
+                                 d_disc_.p, (pump_stream_t)s_));
+  // heuristic h (mainPUMP.cu:351-355): cost of the optimal connection to the goal
+  {
+    std::vector<float> x0((size_t)(N_ - 1) * kDim), x1((size_t)(N_ - 1) * kDim);
+    for (int i = 0; i < N_ - 1; ++i)
+      for (int d = 0; d < kDim; ++d) {
+        x0[(size_t)i * kDim + d] = samples_[(size_t)i * kDim + d];
+        x1[(size_t)i * kDim + d] = pb_.goal[d];
+      }
+    std::vector<float> c;
+    PUMP_TRY(topts_of(x0, x1, 5.0f, nullptr, &c));
+    h_.assign(N_, 0.0f);
+    for (int i = 0; i < N_ - 1; ++i) h_[i] = c[i];
+  }
+  dst_.resize(E_);
+  go_.resize(N_ + 1);
+  coptE_.resize(E_);
+  toptE_.resize(E_);
+  PUMP_TRY(d2h(dst_.data(), d_dst_.p, E_));
+  PUMP_TRY(d2h(go_.data(), d_go_.p, N_ + 1));
+  PUMP_TRY(d2h(coptE_.data(), d_coptE_.p, E_));
+  PUMP_TRY(d2h(toptE_.data(), d_toptE_.p, E_));
+  return sync();
+}
+
+pump_status_t Planner::online() {
+  PUMP_TRY(d_obs_.alloc((size_t)nobs_ * 12));
+  PUMP_TRY(h2d(d_obs_.p, pb_.obstacles, (size_t)nobs_ * 12));
+  PUMP_TRY(d_free_s_.alloc(N_));
+  PUMP_TRY(d_free_e_.alloc(E_));
+  PUMP_TRY(pump_sample_free(d_obs_.p, nobs_, d_samples_.p, N_, d_free_s_.p, (pump_stream_t)s_));
+  PUMP_TRY(pump_free_edges(d_obs_.p, nobs_, d_disc_.p, E_, pb_.num_disc, d_free_e_.p,
+                           (pump_stream_t)s_));
+  // maxd2 = 0.1*offsetMult*offsetMult evaluated in double (mainPUMP.cu:201)
+  const float maxd2 = (float)(0.1 * (double)pb_.offset_mult * (double)pb_.offset_mult);
+  PUMP_TRY(d_as_.alloc((size_t)E_ * W_ * maxHS_ * 3));
+  PUMP_TRY(d_bs_.alloc((size_t)E_ * W_ * maxHS_));
+  PUMP_TRY(pump_cache_halfspaces(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_, maxd2,
+                                 d_as_.p, d_bs_.p, nullptr, (pump_stream_t)s_));
+  PUMP_TRY(d_tmajor_.alloc((size_t)pb_.table_rows * pb_.num_mc * 3));
+  PUMP_TRY(particle_tables_async(pb_.seed, pb_.num_mc, pb_.table_rows, d_tmajor_.p, nullptr, s_));
+  free_s_.resize(N_);
+  free_e_.resize(E_);
+  PUMP_TRY(d2h(free_s_.data(), d_free_s_.p, N_));
+  PUMP_TRY(d2h(free_e_.data(), d_free_e_.p, E_));
+  return sync();
+}
+
+pump_status_t Planner::explore() {
+  maxPathCount_ = (int)(2 * N_ * std::sqrt((double)N_));  // mainPUMP.cu:623
+  const int M = maxPathCount_;
+  pathPrev_.assign(M + 1, 0);
+  pathNode_.assign(M + 1, 0);
+  pathCost_.assign(M + 1, 0.0f);
+  pathTime_.assign(M + 1, 0.0f);
+  pathCP_.assign(M + 1, 0.0f);
+  atNode_.assign(N_, std::vector<int>());
+  PUMP_TRY(d_valid_.alloc((size_t)M * words_));
+  PUMP_TRY(d_stage_.alloc((size_t)(M + 1) * words_));
+  PUMP_TRY(d_cpStage_.alloc(M + 1));
+  PUMP_TRY(d_pathTime_.alloc(M + 1));
+  PUMP_TRY(d_wfPrev_.alloc(M + 1));
+  PUMP_TRY(d_wfEdge_.alloc(M + 1));
+  PUMP_TRY(d_map_.alloc(M + 1));
+  PUMP_TRY(d_err_.alloc(1));
+  PUMP_CUDA_TRY(cudaMemsetAsync(d_err_.p, 0, sizeof(int), s_));
+  // setupValidParticles (PUMP.cu:766-777) for path 0: all particles valid
+  PUMP_CUDA_TRY(cudaMemsetAsync(d_valid_.p, 0xFF, sizeof(uint32_t) * words_, s_));
+  if (P_ % 32) {
+    const uint32_t last = (1u << (P_ % 32)) - 1u;
+    PUMP_TRY(h2d(d_valid_.p + words_ - 1, &last, 1));
+  }
+  PUMP_CUDA_TRY(cudaMemsetAsync(d_pathTime_.p, 0, sizeof(float), s_));
+
+  // PUMP.cu:10-35
+  const float cpTarget = pb_.cp_target;
+  const float dr = lambda_ * rn_;
+  const float cpMinSoln = cpTarget / pb_.cp_factor;
+  const float cpCutoff = cpTarget * pb_.cp_factor;
+  const int initIdx = 0, goalIdx = N_ - 1;
+  int Gidx = 0;
+  bool goalCondition = false, goalConditionNext = false, emptyOpenSet = false;
+  std::vector<int> G[2];
+  atNode_[initIdx].push_back(0);
+  pathPrev_[0] = -2;
+  pathNode_[0] = initIdx;
+  pathCost_[0] = 0;
+  pathCP_[0] = 0;
+  pathTime_[0] = 0;
+  G[Gidx].push_back(0);
+  numPaths_ = 1;
+  float costThreshold = h_[initIdx];
+  const int maxItrs = 20;
+  int itrs = 0, considered = 0;
+  std::vector<int> wfPrev, wfNode, wfEdge, mapSrc;
+  std::vector<float> newCP;
+  std::vector<std::vector<int>> newAt(N_);
+  std::vector<int> touched;
+  pump_status_t status = PUMP_OK;
+  while (itrs < maxItrs && !goalCondition && !emptyOpenSet) {
+    ++itrs;
+    if (goalConditionNext) goalCondition = true;
+    // expansion (PUMP.cu:47-66)
+    wfPrev.clear();
+    wfNode.clear();
+    wfEdge.clear();
+    bool overflow = false;
+    for (size_t g = 0; g < G[Gidx].size() && !overflow; ++g) {
+      const int prev = G[Gidx][g];
+      const int nodePrev = pathNode_[prev];
+      for (int e = go_[nodePrev]; e < go_[nodePrev + 1]; ++e) {
+        const int nodeNext = dst_[e];
+        if (!free_e_[e] || !free_s_[nodeNext]) continue;
+        wfPrev.push_back(prev);
+        wfNode.push_back(nodeNext);
+        wfEdge.push_back(e);
+        if ((int)wfPrev.size() > M) { overflow = true; break; }
+      }
+    }
+    if (overflow) { status = set_error(PUMP_ERR_CAPACITY, "wavefront exceeds maxPathCount %d", M); break; }
+    const int numNew = (int)wfPrev.size();
+    if (itrs <= 32) res_->wavefront_sizes[itrs - 1] = numNew;
+    if (numNew == 0) break;
+    if (numPaths_ + numNew >= M) {
+      status = set_error(PUMP_ERR_CAPACITY, "paths exceed maxPathCount %d", M);
+      break;
+    }
+    G[Gidx].clear();
+    considered += numNew;
+    if (res_->wf_trace)
+      for (int i = 0; i < numNew && res_->wf_trace_len + 2 <= res_->wf_trace_cap; ++i) {
+        res_->wf_trace[res_->wf_trace_len++] = wfPrev[i];
+        res_->wf_trace[res_->wf_trace_len++] = wfEdge[i];
+      }
+
+    // HSMC of the wavefront (PUMP.cu:82-160)
+    PUMP_TRY(h2d(d_wfPrev_.p, wfPrev.data(), numNew));
+    PUMP_TRY(h2d(d_wfEdge_.p, wfEdge.data(), numNew));
+    PUMP_TRY(hsmc_staged_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p, d_bs_.p, maxHS_,
+                               d_pathTime_.p, d_toptE_.p, dt_, d_tmajor_.p, pb_.num_mc,
+                               pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p, P_,
+                               d_cpStage_.p, d_err_.p, s_));
+    newCP.resize(numNew);
+    PUMP_TRY(d2h(newCP.data(), d_cpStage_.p, numNew));
+    PUMP_TRY(sync());
+    for (int i = 0; i < numNew; ++i) pathCP_[numPaths_ + i] = newCP[i];
+
+    // PUMP.cu:164-167
+    for (int i = 0; i < numNew; ++i) {
+      pathTime_[numPaths_ + i] = pathTime_[wfPrev[i]] + toptE_[wfEdge[i]];
+      pathCost_[numPaths_ + i] = pathCost_[wfPrev[i]] + coptE_[wfEdge[i]];
+    }
+    // CP cut-off and candidate lists per node (PUMP.cu:171-185)
+    for (int node : touched) newAt[node].clear();
+    touched.clear();
+    for (int i = 0; i < numNew; ++i) {
+      const int node = wfNode[i], pathIdx = numPaths_ + i;
+      if (pathCP_[pathIdx] > cpCutoff) { wfNode[i] = -1; continue; }
+      if (newAt[node].empty()) touched.push_back(node);
+      newAt[node].push_back(pathIdx);
+    }
+    // epsilon dominance (PUMP.cu:188-218): stored paths, then new ones
+    for (int i = 0; i < numNew; ++i) {
+      const int node = wfNode[i];
+      if (node == -1 || node == goalIdx) continue;
+      const int pathIdx = numPaths_ + i;
+      const float cp = pathCP_[pathIdx], cost = pathCost_[pathIdx];
+      auto dominated_by = [&](int cmp) {
+        if (pathCP_[cmp] < epsCP_ + cp && pathCost_[cmp] < epsCost_ + cost) {
+          if (pathCP_[cmp] + epsCP_ >= cp && pathCost_[cmp] + epsCost_ >= cost && pathIdx < cmp)
+            return false;  // co-dominant: keep the lower path number
+          return true;
+        }
+        return false;
+      };
+      bool dead = false;
+      for (int cmp : atNode_[node])
+        if (cmp != pathIdx && dominated_by(cmp)) { dead = true; break; }
+      if (!dead)
+        for (int cmp : newAt[node])
+          if (cmp != pathIdx && dominated_by(cmp)) { dead = true; break; }
+      if (dead) wfNode[i] = -1;
+    }
+    // store survivors (PUMP.cu:221-256)
+    mapSrc.clear();
+    int numValid = 0;
+    for (int i = 0; i < numNew; ++i) {
+      const int node = wfNode[i], pathIdx = numPaths_ + i;
+      if (node == -1 || node == 0) continue;
+      const int st = numPaths_ + numValid;
+      pathCP_[st] = pathCP_[pathIdx];
+      pathTime_[st] = pathTime_[pathIdx];
+      pathCost_[st] = pathCost_[pathIdx];
+      mapSrc.push_back(i);
+      float dCost = (pathCost_[st] + h_[node] - costThreshold);
+      dCost = std::max((float)0, dCost);
+      const int bucket = (((int)(dCost / dr)) + Gidx + 1) % numBuckets_;
+      G[bucket].push_back(st);
+      pathPrev_[st] = wfPrev[i];
+      pathNode_[st] = node;
+      atNode_[node].push_back(st);
+      ++numValid;
+    }
+    PUMP_TRY(h2d(d_map_.p, mapSrc.data(), numValid));
+    PUMP_TRY(gather_words_async(d_stage_.p, d_map_.p, numValid, words_,
+                                d_valid_.p + (size_t)numPaths_ * words_, s_));
+    PUMP_TRY(h2d(d_pathTime_.p + numPaths_, pathTime_.data() + numPaths_, numValid));
+    numPaths_ += numValid;
+    // goal and open-set conditions (PUMP.cu:259-288)
+    for (int pi : atNode_[goalIdx])
+      if (pathCP_[pi] <= cpMinSoln) goalConditionNext = goalCondition = true;
+    if (goalCondition) break;
+    emptyOpenSet = G[0].empty() && G[1].empty();
+    if (emptyOpenSet) break;
+    Gidx = (Gidx + 1) % numBuckets_;
+    costThreshold += dr;
+    if (numPaths_ >= M) {
+      status = set_error(PUMP_ERR_CAPACITY, "paths reached maxPathCount %d", M);
+      break;
+    }
+  }
+  int err = 0;
+  PUMP_TRY(d2h(&err, d_err_.p, 1));
+  PUMP_TRY(sync());
+  res_->iterations = itrs;
+  res_->num_paths = numPaths_;
+  res_->num_considered = considered;
+  res_->goal_paths = (int)atNode_[goalIdx].size();
+  if (err) return set_error((pump_status_t)err, "particle table has too few rows for a path time");
+  return status;
+}
+
+std::vector<float> Planner::node_states(int path_idx, std::vector<int> *nodes) const {
+  std::vector<int> seq;
+  for (int p = path_idx; p != -2; p = pathPrev_[p]) seq.push_back(pathNode_[p]);
+  std::reverse(seq.begin(), seq.end());
+  std::vector<float> xs(seq.size() * kDim);
+  for (size_t k = 0; k < seq.size(); ++k)
+    for (int d = 0; d < kDim; ++d) xs[k * kDim + d] = samples_[(size_t)seq[k] * kDim + d];
+  if (nodes) *nodes = seq;
+  return xs;
+}
+
+pump_status_t Planner::topts_of(const std::vector<float> &x0, const std::vector<float> &x1,
+                                float tmax, std::vector<float> *topt, std::vector<float> *cost) {
+  const int n = (int)(x0.size() / kDim);
+  if (topt) topt->assign(n, 0.0f);
+  if (cost) cost->assign(n, 0.0f);
+  if (n == 0) return PUMP_OK;
+  DevBuf<float> d_x0, d_x1, d_t, d_c;
+  PUMP_TRY(d_x0.alloc(x0.size()));
+  PUMP_TRY(d_x1.alloc(x1.size()));
+  PUMP_TRY(d_t.alloc(n));
+  PUMP_TRY(d_c.alloc(n));
+  PUMP_TRY(h2d(d_x0.p, x0.data(), x0.size()));
+  PUMP_TRY(h2d(d_x1.p, x1.data(), x1.size()));
+  PUMP_TRY(pump_bvp_batch(d_x0.p, d_x1.p, n, tmax, pb_.bvp_mode, d_t.p, d_c.p, (pump_stream_t)s_));
+  if (topt) PUMP_TRY(d2h(topt->data(), d_t.p, n));
+  if (cost) PUMP_TRY(d2h(cost->data(), d_c.p, n));
+  return sync();
+}
+
+pump_status_t Planner::dense_paths(const std::vector<std::vector<float>> &xs, float dt, float tmax,
+                                   DensePaths &out, DevBuf<float> &d_states) {
+  std::vector<float> x0, x1;
+  std::vector<int> segBase(xs.size() + 1, 0);
+  for (size_t k = 0; k < xs.size(); ++k) {
+    const int n = (int)(xs[k].size() / kDim);
+    segBase[k + 1] = segBase[k] + (n > 1 ? n - 1 : 0);
+    for (int i = 0; i + 1 < n; ++i) {
+      x0.insert(x0.end(), &xs[k][i * kDim], &xs[k][(i + 1) * kDim]);
+      x1.insert(x1.end(), &xs[k][(i + 1) * kDim], &xs[k][(i + 2) * kDim]);
+    }
+  }
+  std::vector<float> topt;
+  PUMP_TRY(topts_of(x0, x1, tmax, &topt, nullptr));
+  // host recurrence of findOptimalPath (2pBVP.cu:15-32)
+  std::vector<float> allxs, tsample;
+  std::vector<int> seg;
+  out.offset.assign(xs.size(), 0);
+  out.len.assign(xs.size(), 0);
+  int total = 0;
+  for (size_t k = 0; k < xs.size(); ++k) {
+    const int n = (int)(xs[k].size() / kDim);
+    const int xbase = (int)(allxs.size() / kDim);
+    allxs.insert(allxs.end(), xs[k].begin(), xs[k].end());
+    out.offset[k] = total;
+    float toff = 0, t = 0;
+    int Tprev = 0;
+    for (int i = 0; i < n - 1; ++i) {
+      const float tp = topt[segBase[k] + i];
+      const int T = (int)((tp - toff) / dt + 1);
+      for (int tidx = 0; tidx < T; ++tidx) {
+        t = dt * tidx + toff;
+        seg.push_back(xbase + i);
+        tsample.push_back(t);
+      }
+      Tprev += T;
+      toff = (t - tp) + dt;
+    }
+    out.len[k] = Tprev;
+    total += Tprev;
+  }
+  out.total = total;
+  // tau indexed by global segment (xbase + i); rebuild as per-node-pair table
+  std::vector<float> tauByPair(allxs.size() / kDim, 0.0f);
+  {
+    int xb = 0, sb = 0;
+    for (size_t k = 0; k < xs.size(); ++k) {
+      const int n = (int)(xs[k].size() / kDim);
+      for (int i = 0; i + 1 < n; ++i) tauByPair[xb + i] = topt[sb + i];
+      xb += n;
+      sb += n > 1 ? n - 1 : 0;
+    }
+  }
+  PUMP_TRY(d_states.alloc((size_t)(total > 0 ? total : 1) * kDim));
+  if (total > 0) {
+    DevBuf<float> d_xs, d_ts, d_tau;
+    DevBuf<int> d_seg;
+    PUMP_TRY(d_xs.alloc(allxs.size()));
+    PUMP_TRY(d_ts.alloc(total));
+    PUMP_TRY(d_tau.alloc(tauByPair.size()));
+    PUMP_TRY(d_seg.alloc(total));
+    PUMP_TRY(h2d(d_xs.p, allxs.data(), allxs.size()));
+    PUMP_TRY(h2d(d_ts.p, tsample.data(), total));
+    PUMP_TRY(h2d(d_tau.p, tauByPair.data(), tauByPair.size()));
+    PUMP_TRY(h2d(d_seg.p, seg.data(), total));
+    PUMP_TRY(bvp_path_states(d_xs.p, d_seg.p, d_ts.p, d_tau.p, total, d_states.p, s_));
+    PUMP_TRY(sync());
+  }
+  return PUMP_OK;
+}
+
+pump_status_t Planner::mc_cp_batch(const DevBuf<float> &d_states, const DensePaths &dp,
+                                   std::vector<float> &cp) {
+  const int n = (int)dp.len.size();
+  cp.assign(n, 0.0f);
+  if (n == 0) return PUMP_OK;
+  for (int k = 0; k < n; ++k)
+    if (dp.len[k] > pb_.table_rows)
+      return set_error(PUMP_ERR_CAPACITY, "dense path of %d states exceeds the %d-row particle table",
+                       dp.len[k], pb_.table_rows);
+  DevBuf<int> d_off, d_len, d_hits;
+  DevBuf<float> d_cp;
+  PUMP_TRY(d_off.alloc(n));
+  PUMP_TRY(d_len.alloc(n));
+  PUMP_TRY(d_hits.alloc(n));
+  PUMP_TRY(d_cp.alloc(n));
+  PUMP_TRY(h2d(d_off.p, dp.offset.data(), n));
+  PUMP_TRY(h2d(d_len.p, dp.len.data(), n));
+  PUMP_TRY(mc_cp_async(d_states.p, d_off.p, d_len.p, n, d_tmajor_.p, pb_.num_mc, pb_.table_rows,
+                       pb_.offset_mult, d_obs_.p, nobs_, d_hits.p, d_cp.p, nullptr, s_));
+  PUMP_TRY(d2h(cp.data(), d_cp.p, n));
+  return sync();
+}
+
+pump_status_t Planner::search_and_smooth() {
+  const int goalIdx = N_ - 1;
+  const float cpTarget = pb_.cp_target;
+  // goal candidates in (cost, path index) order (PUMP.cu:355-362)
+  std::vector<std::pair<float, int>> goalPaths;
+  for (int pi : atNode_[goalIdx]) goalPaths.push_back(std::make_pair(pathCost_[pi], pi));
+  std::sort(goalPaths.begin(), goalPaths.end());
+  std::vector<std::vector<float>> cand;
+  for (auto &g : goalPaths) cand.push_back(node_states(g.second, nullptr));
+  DensePaths dp;
+  DevBuf<float> d_states;
+  PUMP_TRY(dense_paths(cand, dt_, 5.0f, dp, d_states));
+  std::vector<float> cps;
+  PUMP_TRY(mc_cp_batch(d_states, dp, cps));
+  int sel = -1;
+  for (size_t k = 0; k < goalPaths.size(); ++k)
+    if (cps[k] < cpTarget) { sel = (int)k; break; }
+  const int last = sel >= 0 ? sel : (int)goalPaths.size() - 1;
+  const bool success = sel >= 0;
+  res_->success = success ? 1 : 0;
+  res_->soln_path_idx = last >= 0 ? goalPaths[last].second : -1;
+  float solnPathCP = last >= 0 ? cps[last] : 0.0f;
+  float solnPathCost = last >= 0 ? pathCost_[goalPaths[last].second] : 0.0f;
+  std::vector<int> nodes;
+  std::vector<float> xs = last >= 0 ? node_states(goalPaths[last].second, &nodes) : std::vector<float>();
+  res_->num_nodes = (int)nodes.size();
+  if (res_->nodes)
+    for (int k = 0; k < (int)nodes.size() && k < res_->nodes_cap; ++k) res_->nodes[k] = nodes[k];
+
+  // smoothing (PUMP.cu:406-545)
+  std::vector<float> bestPath;
+  int bestLen = last >= 0 ? dp.len[last] : 0;
+  if (last >= 0 && bestLen > 0) {
+    bestPath.resize((size_t)bestLen * kDim);
+    PUMP_TRY(d2h(bestPath.data(), d_states.p + (size_t)dp.offset[last] * kDim, bestPath.size()));
+    PUMP_TRY(sync());
+  }
+  float lastCP = solnPathCP, lastCost = solnPathCost;
+  if (success) {
+    const int n = (int)(xs.size() / kDim);
+    const int dtMult = 10;
+    std::vector<std::vector<float>> two(1);
+    two[0].insert(two[0].end(), xs.begin(), xs.begin() + kDim);
+    two[0].insert(two[0].end(), xs.end() - kDim, xs.end());
+    DensePaths opt;
+    DevBuf<float> d_opt;
+    PUMP_TRY(dense_paths(two, dt_ / dtMult, 5.0f, opt, d_opt));
+    const int optLen = opt.len[0];
+    std::vector<float> optPath((size_t)optLen * kDim);
+    PUMP_TRY(d2h(optPath.data(), d_opt.p, optPath.size()));
+    // splitPathTopts with tmax 2 (PUMP.cu:445-450)
+    std::vector<float> a0, a1, tsplit;
+    for (int i = 0; i + 1 < n; ++i) {
+      a0.insert(a0.end(), &xs[i * kDim], &xs[(i + 1) * kDim]);
+      a1.insert(a1.end(), &xs[(i + 1) * kDim], &xs[(i + 2) * kDim]);
+    }
+    PUMP_TRY(topts_of(a0, a1, 2.0f, &tsplit, nullptr));
+    std::vector<float> splitT(n, 0.0f);
+    for (int i = 0; i + 1 < n; ++i) splitT[i + 1] = splitT[i] + tsplit[i];
+    std::vector<float> xsOpt((size_t)n * kDim);
+    for (int i = 0; i < n; ++i) {
+      const int idx = (int)((optLen - 1) * splitT[i] / splitT[n - 1]);
+      for (int d = 0; d < kDim; ++d) xsOpt[(size_t)i * kDim + d] = optPath[(size_t)idx * kDim + d];
+    }
+    const float epsSmoothCP = (float)0.0002;
+    float alpha = 1.0f, alphaU = 1.0f, alphaL = 0.0f;
+    std::vector<float> xsSmooth(xs.size());
+    for (int it = 0; it < 30; ++it) {
+      for (size_t i = 0; i < xs.size(); ++i) xsSmooth[i] = (1 - alpha) * xs[i] + alpha * xsOpt[i];
+      std::vector<std::vector<float>> one(1, xsSmooth);
+      DensePaths sp;
+      DevBuf<float> d_sp;
+      PUMP_TRY(dense_paths(one, dt_, 5.0f, sp, d_sp));
+      std::vector<float> b0, b1, sc;
+      for (int i = 0; i + 1 < n; ++i) {
+        b0.insert(b0.end(), &xsSmooth[i * kDim], &xsSmooth[(i + 1) * kDim]);
+        b1.insert(b1.end(), &xsSmooth[(i + 1) * kDim], &xsSmooth[(i + 2) * kDim]);
+      }
+      PUMP_TRY(topts_of(b0, b1, 2.0f, nullptr, &sc));
+      float smoothCost = 0;
+      for (float c : sc) smoothCost += c;
+      std::vector<float> cp1;
+      PUMP_TRY(mc_cp_batch(d_sp, sp, cp1));
+      const float cp = cp1[0];
+      if (cp < cpTarget) alphaL = alpha;
+      if (cp >= cpTarget) alphaU = alpha;
+      alpha = (alphaL + alphaU) / 2;
+      const bool satisfies = cp < cpTarget;
+      const bool closer = cp > lastCP;
+      const bool eqLower = (cp == lastCP && smoothCost < lastCost);
+      if (satisfies && (closer || eqLower)) {
+        bestLen = sp.len[0];
+        bestPath.resize((size_t)bestLen * kDim);
+        PUMP_TRY(d2h(bestPath.data(), d_sp.p, bestPath.size()));
+        PUMP_TRY(sync());
+        lastCost = smoothCost;
+        lastCP = cp;
+      }
+      if (std::fabs(cpTarget - cp) < epsSmoothCP && cpTarget - cp > 0) break;
+    }
+  }
+  res_->soln_cp = lastCP;
+  res_->soln_cost = lastCost;
+  res_->path_len = success ? bestLen : 0;
+  if (success && res_->path)
+    std::memcpy(res_->path, bestPath.data(),
+                sizeof(float) * kDim * (size_t)std::min(bestLen, res_->path_cap));
+  return success ? PUMP_OK : set_error(PUMP_ERR_NO_SOLUTION, "no goal path meets the CP target");
+}
+
+}  // namespace
+}  // namespace pump
+
+using namespace pump;
+
+extern "C" pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
+                                   pump_stream_t stream) {
+  if (!ctx || !pb || !res) return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: null argument");
+  if (pb->N < 2 || pb->num_disc < 1 || pb->num_hsmc < 1 || pb->num_mc < pb->num_hsmc ||
+      pb->table_rows < 2 || pb->num_obstacles < 0 || (pb->num_obstacles > 0 && !pb->obstacles) ||
+      !(pb->cp_factor > 0))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: problem out of domain");
+  float *path = res->path;
+  int path_cap = res->path_cap;
+  int *nodes = res->nodes;
+  int nodes_cap = res->nodes_cap;
+  int *trace = res->wf_trace;
+  long long trace_cap = res->wf_trace_cap;
+  std::memset(res, 0, sizeof *res);
+  res->path = path;
+  res->path_cap = path_cap;
+  res->nodes = nodes;
+  res->nodes_cap = nodes_cap;
+  res->wf_trace = trace;
+  res->wf_trace_cap = trace ? trace_cap : 0;
+  res->soln_path_idx = -1;
+  Ctx *c = Ctx::from(ctx);
+  PUMP_TRY(c->activate());
+  Planner planner(c, *pb, res, (cudaStream_t)stream);
+  return planner.run();
+}

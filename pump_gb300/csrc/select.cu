@@ -1,0 +1,398 @@
+// Order statistics and stable compaction (reference: mainPUMP.cu:289-346,
+// GMT.cu:48-76 and 166-176).
+//
+// rn selection: the reference sorts all N(N-1) pair costs (thrust::sort) and
+// reads element floor(0.05 N(N-1)).  Here an exact three-pass radix select
+// over order-preserving 32-bit keys (11, 11 and 10 bits) finds the same
+// element with three reads of the array and no sort.
+//
+// Edge list and frontier: single-pass stable compaction with decoupled
+// look-back (Merrill & Garland, "Single-pass Parallel Prefix Scan with
+// Decoupled Look-back", 2016).  A tile of 4096 items is processed row by row
+// (rows of 256 consecutive items), so the rank of every selected item follows
+// index order; a tile publishes its count, then its inclusive prefix, in a
+// 64-bit status word that later tiles read.  Tiles take their index from an
+// atomic counter, so every tile a block waits on has already started.  Every
+// wait is bounded: a block that spins past kSpinLimit sets the error word and
+// leaves, and the host reports PUMP_ERR_TIMEOUT.
+#include <cuda/atomic>
+
+#include "common.cuh"
+#include "ctx.h"
+
+namespace pump {
+namespace {
+
+constexpr int kCompactThreads = 256;
+constexpr int kCompactRows = 16;
+constexpr int kTile = kCompactThreads * kCompactRows;  // 4096 items
+constexpr unsigned long long kFlagAggregate = 1ull << 62;
+constexpr unsigned long long kFlagPrefix = 2ull << 62;
+constexpr unsigned long long kValueMask = (1ull << 62) - 1;
+constexpr long long kSpinLimit = 1ll << 22;
+
+__device__ __forceinline__ uint32_t float_key(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t k) {
+  uint32_t u = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+  return __uint_as_float(u);
+}
+
+// ---------------------------------------------------------- radix select
+struct SelectState {
+  uint32_t prefix;
+  uint32_t mask;
+  unsigned long long k;
+  float result;
+};
+
+__global__ void select_hist_kernel(const float *__restrict__ v, long long n,
+                                   const SelectState *__restrict__ st, int shift, int bits,
+                                   unsigned int *__restrict__ hist) {
+  __shared__ unsigned int sh[2048];
+  const int nb = 1 << bits;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) sh[b] = 0;
+  __syncthreads();
+  const uint32_t prefix = st->prefix, mask = st->mask;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t key = float_key(__ldg(&v[i]));
+    if ((key & mask) == prefix) atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    if (sh[b]) atomicAdd(&hist[b], sh[b]);
+}
+
+// One block of 1024 threads: find the bin holding rank k, narrow the prefix,
+// clear the histogram for the next pass.
+__global__ void select_pick_kernel(SelectState *st, int shift, int bits, unsigned int *hist) {
+  __shared__ unsigned long long cum[1024];
+  const int nb = 1 << bits;
+  const int per = nb / 1024;  // 1 or 2 bins per thread
+  const int t = threadIdx.x;
+  unsigned long long mine = 0;
+  for (int q = 0; q < per; ++q) mine += hist[t * per + q];
+  cum[t] = mine;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
+    unsigned long long add = t >= off ? cum[t - off] : 0;
+    __syncthreads();
+    cum[t] += add;
+    __syncthreads();
+  }
+  const unsigned long long k = st->k;
+  unsigned long long before = cum[t] - mine;
+  if (k >= before && k < cum[t]) {
+    unsigned long long c = before;
+    for (int q = 0; q < per; ++q) {
+      const unsigned int h = hist[t * per + q];
+      if (k < c + h) {
+        const uint32_t bin = (uint32_t)(t * per + q);
+        st->prefix |= bin << shift;
+        st->mask |= (uint32_t)(nb - 1) << shift;
+        st->k = k - c;
+        if (shift == 0) st->result = key_float(st->prefix);
+        break;
+      }
+      c += h;
+    }
+  }
+  __syncthreads();
+  for (int q = 0; q < per; ++q) hist[t * per + q] = 0;
+}
+
+// ------------------------------------------------------ stable compaction
+struct TileScratch {
+  unsigned long long *status;  // one word per tile, zeroed before launch
+  unsigned int *tile_counter;  // zeroed before launch
+  unsigned long long *total;   // selected count (written by the last tile)
+  int *error;                  // 1 = look-back wait gave up
+};
+
+// Exclusive prefix of this tile from its predecessors' status words.
+__device__ unsigned long long lookback(const TileScratch &ts, long long tile, unsigned long long agg,
+                                       bool *timed_out) {
+  using ref_t = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
+  if (tile == 0) {
+    ref_t(ts.status[0]).store(kFlagPrefix | agg, cuda::memory_order_release);
+    return 0;
+  }
+  ref_t(ts.status[tile]).store(kFlagAggregate | agg, cuda::memory_order_release);
+  unsigned long long excl = 0;
+  long long p = tile - 1;
+  long long spins = 0;
+  while (p >= 0) {
+    const unsigned long long s = ref_t(ts.status[p]).load(cuda::memory_order_acquire);
+    const unsigned long long flag = s & ~kValueMask;
+    if (flag == 0) {
+      if (++spins > kSpinLimit) {
+        *timed_out = true;
+        return 0;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    excl += s & kValueMask;
+    if (flag == kFlagPrefix) break;
+    --p;
+  }
+  ref_t(ts.status[tile]).store(kFlagPrefix | (excl + agg), cuda::memory_order_release);
+  return excl;
+}
+
+// Pred(i) -> bool, Emit(i, pos) writes item i at output position pos.
+template <class Pred, class Emit>
+__global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, Pred pred, Emit emit,
+                                                                  TileScratch ts) {
+  __shared__ unsigned int s_tile;
+  __shared__ unsigned int s_cnt[kCompactRows][kCompactThreads / 32];
+  __shared__ unsigned long long s_excl;
+  __shared__ bool s_timeout;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(ts.tile_counter, 1u);
+    s_timeout = false;
+  }
+  __syncthreads();
+  const long long tile = s_tile;
+  const long long base = tile * kTile;
+  unsigned int ballots[kCompactRows];
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    const long long i = base + r * kCompactThreads + threadIdx.x;
+    const bool f = i < n && pred(i);
+    ballots[r] = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) s_cnt[r][warp] = __popc(ballots[r]);
+  }
+  __syncthreads();
+  // exclusive scan of the 16 x 8 counts in (row, warp) order by warp 0
+  if (warp == 0) {
+    unsigned int v[4];
+    unsigned int run = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = lane * 4 + q;
+      v[q] = s_cnt[e / 8][e % 8];
+      run += v[q];
+    }
+    unsigned int incl = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned int o = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += o;
+    }
+    unsigned int ex = incl - run;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = lane * 4 + q;
+      s_cnt[e / 8][e % 8] = ex;
+      ex += v[q];
+    }
+    const unsigned int agg = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane == 0) {
+      bool to = false;
+      s_excl = lookback(ts, tile, agg, &to);
+      if (to) {
+        s_timeout = true;
+        atomicExch(ts.error, 1);
+      }
+      const long long ntiles = (n + kTile - 1) / kTile;
+      if (!to && tile == ntiles - 1) *ts.total = s_excl + agg;
+    }
+  }
+  __syncthreads();
+  if (s_timeout) return;
+  const unsigned long long excl = s_excl;
+  const unsigned int lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    if (ballots[r] & (1u << lane)) {
+      const long long i = base + r * kCompactThreads + threadIdx.x;
+      emit(i, (long long)(excl + s_cnt[r][warp] + __popc(ballots[r] & lt)));
+    }
+  }
+}
+
+struct EdgePred {
+  const float *copts;
+  float rn;
+  __device__ bool operator()(long long i) const { return __ldg(&copts[i]) < rn; }
+};
+struct EdgeEmit {
+  int N;
+  const float *copts, *topts;
+  long long cap;
+  int *src, *dst;
+  float *copt, *topt;
+  __device__ void operator()(long long idx, long long pos) const {
+    if (pos >= cap) return;
+    const int i = (int)(idx / (N - 1));
+    const int r = (int)(idx - (long long)i * (N - 1));
+    src[pos] = i;
+    dst[pos] = r + (r >= i);
+    copt[pos] = copts[idx];
+    topt[pos] = topts[idx];
+  }
+};
+struct FlagPred {
+  const uint8_t *flags;
+  __device__ bool operator()(long long i) const { return flags[i] != 0; }
+};
+struct IndexEmit {
+  int *out;
+  __device__ void operator()(long long idx, long long pos) const { out[pos] = (int)idx; }
+};
+
+// go_start[i] = first edge whose source is >= i (edges sorted by source).
+__global__ void go_start_kernel(const int *__restrict__ src, long long E, int N,
+                                int *__restrict__ go_start) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > N) return;
+  long long lo = 0, hi = E;
+  while (lo < hi) {
+    const long long mid = (lo + hi) >> 1;
+    if (src[mid] < i) lo = mid + 1; else hi = mid;
+  }
+  go_start[i] = (int)lo;
+}
+
+__global__ void copy_count_kernel(const unsigned long long *total, int *out) { *out = (int)*total; }
+
+template <class Pred, class Emit>
+pump_status_t run_compact(Ctx *ctx, long long n, Pred pred, Emit emit, cudaStream_t stream,
+                          TileScratch *ts_out) {
+  const long long ntiles = n > 0 ? (n + kTile - 1) / kTile : 1;
+  const size_t bytes = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
+  char *scratch = nullptr;
+  PUMP_TRY(ctx->scratch(Ctx::kCompact, bytes, (void **)&scratch));
+  TileScratch ts{};
+  ts.total = (unsigned long long *)scratch;
+  ts.status = ts.total + 1;
+  ts.tile_counter = (unsigned int *)(ts.status + ntiles + 1);
+  ts.error = (int *)(ts.tile_counter + 1);
+  PUMP_CUDA_TRY(cudaMemsetAsync(scratch, 0, bytes, stream));
+  if (n > 0) {
+    if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "compaction: too many tiles");
+    compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(n, pred, emit, ts);
+    PUMP_TRY(launch_status("compact_kernel"));
+  }
+  *ts_out = ts;
+  return PUMP_OK;
+}
+
+// Reads the selected count and the wait-bound error word (synchronises).
+pump_status_t finish_compact(const TileScratch &ts, unsigned long long *total, cudaStream_t stream) {
+  int err = 0;
+  PUMP_CUDA_TRY(cudaMemcpyAsync(total, ts.total, sizeof *total, cudaMemcpyDeviceToHost, stream));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(&err, ts.error, sizeof err, cudaMemcpyDeviceToHost, stream));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (err) return set_error(PUMP_ERR_TIMEOUT, "compaction: look-back wait exceeded its bound");
+  return PUMP_OK;
+}
+
+}  // namespace
+
+// Device-side k-th smallest: result lands in the ctx select state (device);
+// returns a device pointer to the float result.
+pump_status_t select_kth_device(Ctx *ctx, const float *d_v, long long n, long long k,
+                                const float **d_result, cudaStream_t stream) {
+  if (n <= 0 || k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "select_kth: k=%lld n=%lld", k, n);
+  char *scratch = nullptr;
+  const size_t bytes = sizeof(SelectState) + 2048 * sizeof(unsigned int);
+  PUMP_TRY(ctx->scratch(Ctx::kSelect, bytes, (void **)&scratch));
+  SelectState *st = (SelectState *)scratch;
+  unsigned int *hist = (unsigned int *)(scratch + sizeof(SelectState));
+  SelectState init{0u, 0u, (unsigned long long)k, 0.0f};
+  PUMP_CUDA_TRY(cudaMemcpyAsync(st, &init, sizeof init, cudaMemcpyHostToDevice, stream));
+  PUMP_CUDA_TRY(cudaMemsetAsync(hist, 0, 2048 * sizeof(unsigned int), stream));
+  long long blocks = (n + 1023) / 1024;
+  if (blocks > kNumSMs * 8) blocks = kNumSMs * 8;
+  const int shifts[3] = {21, 10, 0}, bits[3] = {11, 11, 10};
+  for (int pass = 0; pass < 3; ++pass) {
+    select_hist_kernel<<<(unsigned)blocks, 1024, 0, stream>>>(d_v, n, st, shifts[pass], bits[pass], hist);
+    PUMP_TRY(launch_status("select_hist_kernel"));
+    select_pick_kernel<<<1, 1024, 0, stream>>>(st, shifts[pass], bits[pass], hist);
+    PUMP_TRY(launch_status("select_pick_kernel"));
+  }
+  *d_result = &st->result;
+  return PUMP_OK;
+}
+
+pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N, float rn,
+                                 long long max_edges, int *d_src, int *d_dst, float *d_copt,
+                                 float *d_topt, int *d_go_start, long long *h_num_edges,
+                                 cudaStream_t stream) {
+  const long long npairs = (long long)N * (N - 1);
+  TileScratch ts{};
+  PUMP_TRY(run_compact(ctx, npairs, EdgePred{d_copts, rn},
+                       EdgeEmit{N, d_copts, d_topts, max_edges, d_src, d_dst, d_copt, d_topt},
+                       stream, &ts));
+  unsigned long long total = 0;
+  PUMP_TRY(finish_compact(ts, &total, stream));
+  *h_num_edges = (long long)total;
+  if ((long long)total > max_edges)
+    return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", total, max_edges);
+  if (d_go_start) {
+    go_start_kernel<<<grid_for(N + 1, 256), 256, 0, stream>>>(d_src, (long long)total, N, d_go_start);
+    PUMP_TRY(launch_status("go_start_kernel"));
+  }
+  return PUMP_OK;
+}
+
+// Device-side frontier compaction; *d_error_out (device) is nonzero when a
+// look-back wait gave up.
+pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
+                                      int *d_count, int **d_error_out, cudaStream_t stream) {
+  TileScratch ts{};
+  PUMP_TRY(run_compact(ctx, N, FlagPred{d_flags}, IndexEmit{d_active}, stream, &ts));
+  copy_count_kernel<<<1, 1, 0, stream>>>(ts.total, d_count);
+  if (d_error_out) *d_error_out = ts.error;
+  return launch_status("copy_count_kernel");
+}
+
+}  // namespace pump
+
+using namespace pump;
+
+extern "C" pump_status_t pump_select_kth(pump_ctx *ctx, const float *d_v, long long n, long long k,
+                                         float *h_kth, pump_stream_t stream) {
+  if (!ctx || !d_v || !h_kth) return set_error(PUMP_ERR_BAD_INPUT, "pump_select_kth: null argument");
+  Ctx *c = Ctx::from(ctx);
+  PUMP_TRY(c->activate());
+  const float *d_res = nullptr;
+  PUMP_TRY(select_kth_device(c, d_v, n, k, &d_res, (cudaStream_t)stream));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(h_kth, d_res, sizeof(float), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  PUMP_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return PUMP_OK;
+}
+
+extern "C" pump_status_t pump_build_edges(pump_ctx *ctx, const float *d_copts, const float *d_topts,
+                                          int N, float rn, long long max_edges, int *d_src,
+                                          int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
+                                          long long *h_num_edges, pump_stream_t stream) {
+  if (!ctx || N < 2 || !d_copts || !d_topts || !d_src || !d_dst || !d_copt || !d_topt ||
+      !h_num_edges || max_edges < 0)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_build_edges: bad arguments");
+  Ctx *c = Ctx::from(ctx);
+  PUMP_TRY(c->activate());
+  return build_edges_device(c, d_copts, d_topts, N, rn, max_edges, d_src, d_dst, d_copt, d_topt,
+                            d_go_start, h_num_edges, (cudaStream_t)stream);
+}
+
+extern "C" pump_status_t pump_frontier_compact(pump_ctx *ctx, const uint8_t *d_flags, int N,
+                                               int *d_active, int *d_count, pump_stream_t stream) {
+  if (!ctx || N < 0 || (N > 0 && (!d_flags || !d_active)) || !d_count)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_frontier_compact: bad arguments");
+  Ctx *c = Ctx::from(ctx);
+  PUMP_TRY(c->activate());
+  int *d_err = nullptr;
+  PUMP_TRY(frontier_compact_device(c, d_flags, N, d_active, d_count, &d_err, (cudaStream_t)stream));
+  int err = 0;
+  PUMP_CUDA_TRY(cudaMemcpyAsync(&err, d_err, sizeof err, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  PUMP_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  if (err) return set_error(PUMP_ERR_TIMEOUT, "pump_frontier_compact: look-back wait exceeded its bound");
+  return PUMP_OK;
+}

@@ -1,0 +1,89 @@
+"""Synthetic planning problems in the reference's input-file format.
+
+The reference reads one CSV file per query (README.md:10-11, parsed at
+mainPUMP.cu:152-230): init state, goal state, lower and upper state bounds
+(6 values each), the noise multiplier, the obstacle count, then 12 values per
+axis-aligned box (lower corner, upper corner, 6D).  The generators below
+produce the workloads the benchmarks are quoted on, seeded and reproducible:
+
+- ``random_boxes`` -- N samples in pos [0,1]^3 x vel [-1,1]^3, init
+  (0.1,0.1,0.1,0,0,0), goal (0.9,0.9,0.9,0,0,0), boxes with position centres
+  U[0.2,0.8] and sides U[lo,hi] spanning the whole velocity range (+-3.1, as
+  the reference's example files).
+- ``indoor`` -- the same bounds with 30 walls 0.02 thick and U[0.3,1] long on
+  the lines of a 4 x 4 room grid (full height), plus 10 boxes with sides
+  U[0.05,0.15].
+
+Boxes that contain the init or goal position are redrawn.  Seeds follow
+1000 * config + query.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+INIT = (0.1, 0.1, 0.1, 0.0, 0.0, 0.0)
+GOAL = (0.9, 0.9, 0.9, 0.0, 0.0, 0.0)
+LO = (0.0, 0.0, 0.0, -1.0, -1.0, -1.0)
+HI = (1.0, 1.0, 1.0, 1.0, 1.0, 1.0)
+VEL = 3.1
+
+
+def _contains(box, p):
+    return all(box[d] < p[d] < box[6 + d] for d in range(3))
+
+
+def _box(lo3, hi3):
+    return [lo3[0], lo3[1], lo3[2], -VEL, -VEL, -VEL, hi3[0], hi3[1], hi3[2], VEL, VEL, VEL]
+
+
+def random_boxes(n, seed, side=(0.05, 0.2), centre=(0.2, 0.8)):
+    rng = np.random.Generator(np.random.MT19937(seed))
+    out = []
+    while len(out) < n:
+        c = rng.uniform(centre[0], centre[1], 3)
+        s = rng.uniform(side[0], side[1], 3)
+        b = _box(c - s / 2, c + s / 2)
+        if _contains(b, INIT) or _contains(b, GOAL):
+            continue
+        out.append(b)
+    return np.asarray(out, np.float32).reshape(-1, 12)
+
+
+def indoor(seed, walls=30, boxes=10):
+    rng = np.random.Generator(np.random.MT19937(seed))
+    out = []
+    while len(out) < walls:
+        k = int(rng.integers(1, 4)) / 4.0
+        length = rng.uniform(0.3, 1.0)
+        start = rng.uniform(0.0, 1.0 - length)
+        if rng.integers(0, 2) == 0:  # wall in a plane x = k
+            b = _box((k - 0.01, start, 0.0), (k + 0.01, start + length, 1.0))
+        else:  # wall in a plane y = k
+            b = _box((start, k - 0.01, 0.0), (start + length, k + 0.01, 1.0))
+        if _contains(b, INIT) or _contains(b, GOAL):
+            continue
+        out.append(b)
+    rest = random_boxes(boxes, seed + 7919, side=(0.05, 0.15))
+    return np.concatenate([np.asarray(out, np.float32).reshape(-1, 12), rest], 0)
+
+
+def write_input(path, obstacles, offset_mult, init=INIT, goal=GOAL, lo=LO, hi=HI):
+    """Writes a problem in the reference's input format."""
+    def row(v):
+        return ",".join("%.9g" % float(x) for x in v) + ",\n"
+    obstacles = np.asarray(obstacles, np.float32).reshape(-1, 12)
+    with open(path, "w") as f:
+        f.write(row(init) + row(goal) + row(lo) + row(hi))
+        f.write("%.9g,\n%d,\n" % (offset_mult, obstacles.shape[0]))
+        for k, b in enumerate(obstacles):
+            line = ", ".join("%.9g" % float(x) for x in b)
+            f.write(line + (",\n" if k + 1 < obstacles.shape[0] else "\n"))
+
+
+CONFIGS = {
+    # the benchmark configurations (N, obstacles, noise, cp, eta, particles, waypoints)
+    "cfg0": dict(N=1000, num_disc=9, num_hsmc=128, offset_mult=1e-3, cp=0.01, eta=2.0,
+                 obstacles=lambda q=0: random_boxes(10, 1000 * 0 + q)),
+    "cfg1": dict(N=4000, num_disc=8, num_hsmc=1024, offset_mult=2e-3, cp=0.01, eta=2.0,
+                 obstacles=lambda q=0: indoor(1000 * 1 + q)),
+}

@@ -1,0 +1,295 @@
+"""GPU kernels through the C ABI against the oracle, bit for bit.
+
+Each test runs one entry point of include/pump.h on cuda:0 and compares its
+output with the oracle's (oracle/pump_oracle.c), which the golden fixtures
+pin to the reference program's own results.  Integer, index and mask outputs
+must be identical; floating-point outputs must be identical to the last bit
+(parity arithmetic is the reference's, see include/pump.h).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import bits_to_bytes, dev, empty, host, ptr, stream
+
+pytestmark = pytest.mark.gpu
+
+
+def same_bits(a, b):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def golden_problem(goldens, name):
+    g = goldens[name]
+    return (int(g["N"]), g["prob_obstacles"].astype(np.float32), g["prob_init"], g["prob_goal"],
+            g["prob_lo"], g["prob_hi"], np.float32(g["prob_offset_mult"]))
+
+
+@pytest.fixture(scope="module")
+def roadmap1000(oracle, goldens):
+    N, obs, init, goal, lo, hi, om = golden_problem(goldens, "ref_N1000_boxes10_noise0.3")
+    s = oracle.halton_samples(N, init, goal, lo, hi)
+    c, t = oracle.bvp_pairs(s)
+    k = int((N - 1) * N * np.float32(0.05))
+    rn = oracle.lib().orc_select_kth(c.size, c, k)
+    src, dst, ce, te = oracle.build_edges(c, t, N, rn)
+    disc = oracle.discretize_edges(src, dst, s, 8)
+    fe = oracle.free_edges(disc, obs)
+    return dict(N=N, obs=obs, om=om, samples=s, copts=c, topts=t, k=k, rn=rn, src=src, dst=dst,
+                ce=ce, te=te, disc=disc, fe=fe, goal=goal)
+
+
+def run_bvp_pairs(torch, L, s, mode=0, tmax=5.0):
+    N = s.shape[0]
+    d_s = dev(torch, s)
+    d_c = empty(torch, N * (N - 1), torch.float32)
+    d_t = empty(torch, N * (N - 1), torch.float32)
+    L.check(L.load().pump_bvp_pairs(ptr(d_s), N, tmax, mode, ptr(d_c), ptr(d_t), stream(torch)))
+    torch.cuda.synchronize()
+    return host(d_c, N * (N - 1)), host(d_t, N * (N - 1))
+
+
+@pytest.mark.parametrize("N", [2, 64, 1000])
+def test_bvp_pairs_parity_halton(N, gpu, pumplib, oracle, goldens):
+    torch, _ = gpu
+    _, _, init, goal, lo, hi, _ = golden_problem(goldens, "ref_N1000_input")
+    s = oracle.halton_samples(N, init, goal, lo, hi)
+    c, t = run_bvp_pairs(torch, pumplib, s)
+    rc, rt = oracle.bvp_pairs(s)
+    assert same_bits(t, rt), "topt mismatches: %d" % int((t != rt).sum())
+    assert same_bits(c, rc), "copt mismatches: %d" % int((c != rc).sum())
+
+
+def test_bvp_pairs_parity_random(gpu, pumplib, oracle):
+    torch, _ = gpu
+    rng = np.random.default_rng(7)
+    s = np.concatenate([rng.uniform(-1, 2, (300, 3)), rng.uniform(-3, 3, (300, 3))], 1).astype(np.float32)
+    c, t = run_bvp_pairs(torch, pumplib, s)
+    rc, rt = oracle.bvp_pairs(s)
+    assert same_bits(t, rt) and same_bits(c, rc)
+
+
+def test_bvp_batch_parity(gpu, pumplib, oracle):
+    torch, _ = gpu
+    L = pumplib.load()
+    rng = np.random.default_rng(11)
+    n = 2000
+    x0 = np.concatenate([rng.uniform(0, 1, (n, 3)), rng.uniform(-1, 1, (n, 3))], 1).astype(np.float32)
+    x1 = np.concatenate([rng.uniform(0, 1, (n, 3)), rng.uniform(-1, 1, (n, 3))], 1).astype(np.float32)
+    for tmax in (2.0, 5.0):
+        d0, d1 = dev(torch, x0), dev(torch, x1)
+        dt, dc = empty(torch, n, torch.float32), empty(torch, n, torch.float32)
+        pumplib.check(L.pump_bvp_batch(ptr(d0), ptr(d1), n, tmax, 0, ptr(dt), ptr(dc), stream(torch)))
+        t, c = host(dt, n), host(dc, n)
+        rt = np.array([oracle.topt(x0[k], x1[k], tmax)[0] for k in range(n)], np.float32)
+        rc = np.array([oracle.cost(rt[k], x0[k], x1[k]) for k in range(n)], np.float32)
+        assert same_bits(t, rt) and same_bits(c, rc)
+
+
+@pytest.mark.parametrize("n,k", [(1, 0), (1000, 0), (1000, 999), (100003, 5000), (5_000_000, 250_000)])
+def test_select_kth(n, k, gpu, pumplib):
+    torch, ctx = gpu
+    rng = np.random.default_rng(n)
+    v = rng.normal(0, 10, n).astype(np.float32)
+    v[: n // 10] = np.float32(3.25)  # many ties
+    if n > 4:
+        v[1], v[2], v[3] = -0.0, 0.0, np.float32(-1e-30)
+    out = C.c_float(0)
+    d = dev(torch, v)
+    pumplib.check(pumplib.load().pump_select_kth(ctx.handle, ptr(d), n, k, C.byref(out), stream(torch)))
+    expect = np.partition(v, k)[k]
+    assert out.value == expect or (out.value == 0 and expect == 0)
+
+
+def test_select_rn_of_pair_costs(gpu, pumplib, roadmap1000):
+    torch, ctx = gpu
+    r = roadmap1000
+    out = C.c_float(0)
+    d = dev(torch, r["copts"])
+    pumplib.check(pumplib.load().pump_select_kth(ctx.handle, ptr(d), r["copts"].size, r["k"],
+                                                 C.byref(out), stream(torch)))
+    assert np.float32(out.value) == np.float32(r["rn"])
+
+
+def test_build_edges_and_waypoints(gpu, pumplib, roadmap1000):
+    torch, ctx = gpu
+    L = pumplib.load()
+    r = roadmap1000
+    N = r["N"]
+    d_c, d_t = dev(torch, r["copts"]), dev(torch, r["topts"])
+    cap = r["k"]
+    d_src, d_dst = empty(torch, cap, torch.int32), empty(torch, cap, torch.int32)
+    d_ce, d_te = empty(torch, cap, torch.float32), empty(torch, cap, torch.float32)
+    d_go = empty(torch, N + 1, torch.int32)
+    E = C.c_longlong(0)
+    pumplib.check(L.pump_build_edges(ctx.handle, ptr(d_c), ptr(d_t), N, float(r["rn"]), cap,
+                                     ptr(d_src), ptr(d_dst), ptr(d_ce), ptr(d_te), ptr(d_go),
+                                     C.byref(E), stream(torch)))
+    E = E.value
+    assert E == r["src"].size
+    assert np.array_equal(host(d_src, E), r["src"]) and np.array_equal(host(d_dst, E), r["dst"])
+    assert same_bits(host(d_ce, E), r["ce"]) and same_bits(host(d_te, E), r["te"])
+    go = host(d_go, N + 1)
+    assert np.array_equal(go, np.searchsorted(r["src"], np.arange(N + 1), side="left"))
+    # capacity overflow reported, not written past the buffer
+    E2 = C.c_longlong(0)
+    st = L.pump_build_edges(ctx.handle, ptr(d_c), ptr(d_t), N, float(r["rn"]), E - 1, ptr(d_src),
+                            ptr(d_dst), ptr(d_ce), ptr(d_te), ptr(d_go), C.byref(E2), stream(torch))
+    assert st == pumplib.PUMP_ERR_CAPACITY and E2.value == E
+    # waypoints (findDiscretizedPath)
+    d_s = dev(torch, r["samples"])
+    d_src2, d_dst2, d_te2 = dev(torch, r["src"]), dev(torch, r["dst"]), dev(torch, r["te"])
+    d_disc = empty(torch, E * 9 * 6, torch.float32)
+    pumplib.check(L.pump_discretize_edges(ptr(d_s), ptr(d_src2), ptr(d_dst2), ptr(d_te2), E, 8,
+                                          ptr(d_disc), stream(torch)))
+    disc = host(d_disc, E * 54).reshape(E, 9, 6)
+    assert same_bits(disc, r["disc"]), "waypoint mismatches: %d" % int((disc != r["disc"]).sum())
+
+
+def test_collision_checks(gpu, pumplib, oracle, roadmap1000):
+    torch, _ = gpu
+    L = pumplib.load()
+    r = roadmap1000
+    N, obs = r["N"], r["obs"]
+    E = r["src"].size
+    d_obs, d_s, d_disc = dev(torch, obs), dev(torch, r["samples"]), dev(torch, r["disc"])
+    d_fs = empty(torch, N, torch.uint8)
+    pumplib.check(L.pump_sample_free(ptr(d_obs), obs.shape[0], ptr(d_s), N, ptr(d_fs), stream(torch)))
+    assert np.array_equal(host(d_fs, N), oracle.sample_free(r["samples"], obs))
+    d_fe = empty(torch, E, torch.uint8)
+    pumplib.check(L.pump_free_edges(ptr(d_obs), obs.shape[0], ptr(d_disc), E, 8, ptr(d_fe), stream(torch)))
+    assert np.array_equal(host(d_fe, E), r["fe"])
+    for om in (np.float32(0.3), np.float32(1.0)):
+        maxHS = min(obs.shape[0], 5)
+        maxd2 = np.float32(0.1 * np.float64(om) * np.float64(om))
+        d_a = empty(torch, E * 9 * maxHS * 3, torch.float32)
+        d_b = empty(torch, E * 9 * maxHS, torch.float32)
+        d_n = empty(torch, E * 9, torch.int32)
+        pumplib.check(L.pump_cache_halfspaces(ptr(d_obs), obs.shape[0], ptr(d_disc), ptr(d_fe), E, 9,
+                                              maxHS, float(maxd2), ptr(d_a), ptr(d_b), ptr(d_n),
+                                              stream(torch)))
+        a, b, n = oracle.cache_halfspaces(r["disc"], r["fe"], obs, maxHS, maxd2)
+        assert same_bits(host(d_a, a.size), a) and same_bits(host(d_b, b.size), b)
+        free_wp = np.repeat(r["fe"].astype(bool), 9)
+        assert np.array_equal(host(d_n, E * 9)[free_wp], n[free_wp])
+        assert np.all(host(d_n, E * 9)[~free_wp] == 0)
+
+
+def test_collision_checks_many_obstacles(gpu, pumplib, oracle, roadmap1000):
+    """More boxes than fit one block's threads (the reference's limit is 85)."""
+    torch, _ = gpu
+    L = pumplib.load()
+    from pump_gb300 import workloads
+    obs = workloads.random_boxes(300, 5, side=(0.02, 0.08))
+    r = roadmap1000
+    E = r["src"].size
+    d_obs, d_disc = dev(torch, obs), dev(torch, r["disc"])
+    d_fe = empty(torch, E, torch.uint8)
+    pumplib.check(L.pump_free_edges(ptr(d_obs), obs.shape[0], ptr(d_disc), E, 8, ptr(d_fe), stream(torch)))
+    assert np.array_equal(host(d_fe, E), oracle.free_edges(r["disc"], obs))
+
+
+@pytest.mark.parametrize("P,T", [(2048, 400), (100, 37)])
+def test_particle_tables(P, T, gpu, pumplib, oracle):
+    torch, _ = gpu
+    d_t = empty(torch, P * T * 3, torch.float32)
+    d_p = empty(torch, P * T * 3, torch.float32)
+    seed = 0x9E3779B97F4A7C15
+    pumplib.check(pumplib.load().pump_particle_tables(seed, P, T, ptr(d_t), ptr(d_p), stream(torch)))
+    tm, pm = oracle.particle_tables(seed, P, T)
+    assert same_bits(host(d_t, P * T * 3).reshape(T, P, 3), tm)
+    assert same_bits(host(d_p, P * T * 3).reshape(P, T, 3), pm)
+
+
+@pytest.mark.parametrize("P", [128, 1024, 100])
+def test_hsmc_propagate(P, gpu, pumplib, oracle, roadmap1000):
+    torch, _ = gpu
+    L = pumplib.load()
+    r = roadmap1000
+    obs, E = r["obs"], r["src"].size
+    om = np.float32(0.3)
+    maxHS = 5
+    maxd2 = np.float32(0.1 * np.float64(om) * np.float64(om))
+    a, b, _ = oracle.cache_halfspaces(r["disc"], r["fe"], obs, maxHS, maxd2)
+    Pmc, T = 2048, 400
+    tm, _ = oracle.particle_tables(0x1234, Pmc, T, pmajor=False)
+    rng = np.random.default_rng(P)
+    base = 50
+    n_new = 3000
+    edges = rng.choice(np.nonzero(r["fe"])[0], n_new).astype(np.int32)
+    prev = rng.integers(0, base, n_new).astype(np.int32)
+    times = np.zeros(base + n_new, np.float32)
+    times[:base] = rng.uniform(0, 6, base).astype(np.float32)
+    valid_bytes = np.zeros(((base + n_new), P), np.uint8)
+    valid_bytes[:base] = rng.random((base, P)) < 0.9
+    words = (P + 31) // 32
+    vb = np.zeros((base + n_new, words * 32), np.uint8)
+    vb[:, :P] = valid_bytes
+    packed = np.packbits(vb, axis=1, bitorder="little").view(np.uint32)
+    assert np.array_equal(bits_to_bytes(packed, P), vb[:, :P])
+    d_valid = dev(torch, packed)
+    d_cp = empty(torch, base + n_new, torch.float32)
+    d_err = dev(torch, np.zeros(1, np.int32))
+    # every device buffer stays referenced until the kernel has finished
+    d_edges, d_prev, d_a, d_b = dev(torch, edges), dev(torch, prev), dev(torch, a), dev(torch, b)
+    d_times, d_te, d_tm = dev(torch, times), dev(torch, r["te"]), dev(torch, tm)
+    pumplib.check(L.pump_hsmc_propagate(n_new, 9, ptr(d_edges), ptr(d_prev), E, base, ptr(d_a), ptr(d_b),
+                                        maxHS, ptr(d_times), ptr(d_te), 0.05, ptr(d_tm), Pmc, T,
+                                        float(om), ptr(d_valid), P, ptr(d_cp), ptr(d_err),
+                                        stream(torch)))
+    torch.cuda.synchronize()
+    got = bits_to_bytes(host(d_valid).reshape(base + n_new, words), P)
+    cp_o = np.zeros(base + n_new, np.float32)
+    oracle.lib().orc_hsmc_propagate(n_new, 9, edges, prev, base, a, b, times, r["te"], 0.05, maxHS,
+                                    tm.reshape(-1), om, Pmc, valid_bytes, P, cp_o)
+    assert np.array_equal(got[base:], valid_bytes[base:])
+    assert same_bits(host(d_cp)[base:base + n_new], cp_o[base:])
+    assert int(host(d_err)[0]) == 0
+    assert 0 < valid_bytes[base:].mean() < 1
+
+
+def test_mc_cp(gpu, pumplib, oracle, goldens):
+    torch, _ = gpu
+    L = pumplib.load()
+    g = goldens["ref_N1000_boxes10_noise0.3"]
+    obs = g["prob_obstacles"].astype(np.float32)
+    path = np.array([[float(x) for x in line.split()] for line in str(g["path_txt"]).splitlines()],
+                    np.float32)
+    Pmc, T = 2048, 400
+    tm, pm = oracle.particle_tables(0x9E3779B97F4A7C15, Pmc, T)
+    paths = [path, path[:10], path[::2].copy(), path + np.float32(0.01)]
+    lens = np.array([p.shape[0] for p in paths], np.int32)
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int32)
+    allp = np.concatenate(paths, 0).astype(np.float32)
+    hits = empty(torch, len(paths), torch.int32)
+    cps = empty(torch, len(paths), torch.float32)
+    d_allp, d_offs, d_lens = dev(torch, allp), dev(torch, offs), dev(torch, lens)
+    d_tm, d_obs = dev(torch, tm), dev(torch, obs)
+    for om in (np.float32(0.3), np.float32(1.0)):
+        pumplib.check(L.pump_mc_cp(ptr(d_allp), ptr(d_offs), ptr(d_lens), len(paths), ptr(d_tm), Pmc,
+                                   T, float(om), ptr(d_obs), obs.shape[0], ptr(hits), ptr(cps), 0,
+                                   stream(torch)))
+        torch.cuda.synchronize()
+        for k, p in enumerate(paths):
+            h, cp = oracle.mccp(p, p.shape[0], pm, om, obs)
+            assert int(host(hits)[k]) == h
+            assert np.float32(host(cps)[k]) == np.float32(cp)
+
+
+@pytest.mark.parametrize("N,density", [(0, 0.5), (1, 1.0), (4095, 0.3), (4096, 1.0), (100_000, 0.01),
+                                       (1_000_000, 0.5), (777_777, 0.0)])
+def test_frontier_compact(N, density, gpu, pumplib):
+    torch, ctx = gpu
+    rng = np.random.default_rng(N)
+    flags = (rng.random(N) < density).astype(np.uint8)
+    d_f = dev(torch, flags) if N else empty(torch, 1, torch.uint8)
+    d_a = empty(torch, N, torch.int32)
+    d_n = empty(torch, 1, torch.int32)
+    pumplib.check(pumplib.load().pump_frontier_compact(ctx.handle, ptr(d_f), N, ptr(d_a), ptr(d_n),
+                                                       stream(torch)))
+    n = int(host(d_n)[0])
+    expect = np.nonzero(flags)[0]
+    assert n == expect.size
+    assert np.array_equal(host(d_a, n), expect)

@@ -1,0 +1,85 @@
+"""Whole planning queries on the GPU (pump_plan) against the reference's own
+results recorded in the golden fixtures: exploration wavefront sizes, stored
+and considered path counts, goal paths, the chosen solution, its node
+sequence, its printed CP and cost, and path.txt byte for byte."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["ref_N64_input", "ref_N1000_input", "ref_N1000_boxes10_noise1e-3",
+         "ref_N1000_boxes10_noise0.3"]
+
+
+def make_problem(L, g, **over):
+    pb = L.Problem()
+    L.load().pump_problem_defaults(C.byref(pb))
+    obs = np.ascontiguousarray(g["prob_obstacles"], np.float32)
+    pb.N = int(g["N"])
+    pb.num_obstacles = obs.shape[0]
+    pb.obstacles = obs.ctypes.data
+    for k in range(6):
+        pb.init[k], pb.goal[k] = float(g["prob_init"][k]), float(g["prob_goal"][k])
+        pb.lo[k], pb.hi[k] = float(g["prob_lo"][k]), float(g["prob_hi"][k])
+    pb.offset_mult = float(g["prob_offset_mult"])
+    pb.cp_target, pb.cp_factor = float(g["cp_target"]), float(g["cp_factor"])
+    for k, v in over.items():
+        setattr(pb, k, v)
+    return pb, obs
+
+
+def run_plan(L, ctx, pb, rows=400):
+    res = L.PlanResult()
+    path = np.zeros((rows, 6), np.float32)
+    nodes = np.zeros(64, np.int32)
+    res.path, res.path_cap = path.ctypes.data, rows
+    res.nodes, res.nodes_cap = nodes.ctypes.data, 64
+    st = L.load().pump_plan(ctx.handle, C.byref(pb), C.byref(res), None)
+    return st, res, path[: res.path_len].copy(), nodes[: res.num_nodes].copy()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_plan_matches_reference(name, gpu, pumplib, goldens):
+    torch, ctx = gpu
+    g = goldens[name]
+    pb, _obs = make_problem(pumplib, g)
+    st, res, path, nodes = run_plan(pumplib, ctx, pb)
+    assert st in (pumplib.PUMP_OK, pumplib.PUMP_ERR_NO_SOLUTION), pumplib.load().pump_last_error()
+    sizes = np.array(res.wavefront_sizes[: res.iterations], np.int32)
+    if sizes.size and sizes[-1] == 0:
+        sizes = sizes[:-1]
+    assert np.array_equal(sizes, g["wavefront_sizes"])
+    assert res.num_paths == int(g["num_paths"])
+    assert res.num_considered == int(g["num_considered"])
+    assert res.goal_paths == int(g["goal_paths"])
+    assert res.success == int(g["success"])
+    if res.success:
+        assert res.soln_path_idx == int(g["soln_idx"])
+        assert np.array_equal(nodes, g["soln_nodes"])
+        assert "%g" % res.soln_cp == "%g" % float(g["soln_cp_printed"])
+        assert "%g" % res.soln_cost == "%g" % float(g["soln_cost_printed"])
+        text = "".join("".join("%g " % v for v in row) + "\n" for row in path.astype(np.float64))
+        assert text == str(g["path_txt"])
+
+
+def test_plan_matches_oracle_cfg0(gpu, pumplib, oracle):
+    """The benchmark's small configuration (10 boxes, 10 waypoints per edge)."""
+    torch, ctx = gpu
+    from pump_gb300 import workloads
+    obs = workloads.random_boxes(10, 0)
+    g = dict(N=np.array(1000), prob_obstacles=obs, prob_init=np.float32(workloads.INIT),
+             prob_goal=np.float32(workloads.GOAL), prob_lo=np.float32(workloads.LO),
+             prob_hi=np.float32(workloads.HI), prob_offset_mult=np.float32(1e-3),
+             cp_target=np.float32(0.01), cp_factor=np.float32(2))
+    pb, _o = make_problem(pumplib, g, num_disc=9)
+    st, res, path, nodes = run_plan(pumplib, ctx, pb)
+    r = oracle.plan(1000, obs, workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI,
+                    np.float32(1e-3), 0.01, 2.0, numDisc=9)
+    assert res.num_paths == r["numPaths"] and res.num_considered == r["numConsidered"]
+    assert res.success == r["success"] and res.soln_path_idx == r["solnPathIdx"]
+    assert np.array_equal(nodes, r["nodes"])
+    assert np.array_equal(path.view(np.uint32), r["path"].view(np.uint32))
+    assert np.float32(res.soln_cp) == np.float32(r["solnCP"])
+    assert np.float32(res.soln_cost) == np.float32(r["solnCost"])
