@@ -61,6 +61,20 @@ def parse():
     return ap.parse_args()
 
 
+def aggregate(dist, units, total_ms, device="cpu"):
+    """Replicas: every rank plans its own query (no data-path collective);
+    the job's throughput is the units of all ranks over the slowest rank's
+    time.  Returns (sum of units, max of each time in total_ms)."""
+    if dist is None:
+        return units, list(total_ms)
+    import torch
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(x) for x in total_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return u.item(), t.tolist()
+
+
 def workload(args, query):
     from pump_gb300 import workloads
     obs = workloads.indoor(1000 * 1 + query)
@@ -260,7 +274,7 @@ def run_ours(args):
             d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(), d_go.data_ptr(), C.byref(Eo), sh)), 2)
         timed("discretize", lambda: lib.check(L.pump_discretize_edges(
             d_s.data_ptr(), d_src.data_ptr(), d_dst.data_ptr(), d_te.data_ptr(), Eo.value, W - 1,
-            d_disc.data_ptr(), sh)), 1)
+            w["mode"], d_disc.data_ptr(), sh)), 1)
         timed("sample_free", lambda: lib.check(L.pump_sample_free(
             d_obs.data_ptr(), obs_host.shape[0], d_s.data_ptr(), N, d_fs.data_ptr(), sh)), 1)
         timed("free_edges", lambda: lib.check(L.pump_free_edges(
@@ -310,17 +324,12 @@ def run_ours(args):
     clk = clocks.stop()
     if dist:
         dist.barrier()
-    tot = sum(step_ms)
-    tot_e2e = sum(e2e_ms)
-    if dist:
-        t = torch.tensor([tot, tot_e2e], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot, tot_e2e = t.tolist()
+    all_units, (tot, tot_e2e) = aggregate(dist, units, [sum(step_ms), sum(e2e_ms)], "cuda")
     ks = {k: sum(a.elapsed_time(b) for a, b in v) / args.steps for k, v in kernel_ms.items()}
     out = None
     if rank == 0:
-        value = world * units * args.steps / (tot / 1e3)
-        e2e_value = world * units * max(1, args.steps) / (tot_e2e / 1e3)
+        value = all_units * args.steps / (tot / 1e3)
+        e2e_value = all_units * max(1, args.steps) / (tot_e2e / 1e3)
         dom = max(ks, key=ks.get)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

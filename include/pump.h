@@ -99,10 +99,12 @@ pump_status_t pump_build_edges(pump_ctx *ctx, const float *d_copts, const float 
 /* Edge waypoints disc[E][numDisc+1][6] (findDiscretizedPath, 2pBVP.cu:53-69
  * and pathPoint 2pBVP.cu:117-131, as called at mainPUMP.cu:339).  d_topt
  * is the edge's optimal time (identical to the one toptBisection recomputes
- * there). */
+ * there).  mode PUMP_BVP_PARITY evaluates pathPoint's expressions as the
+ * reference does (binary64 where they promote); PUMP_BVP_PRECISION
+ * evaluates the same cubic in binary32 (FP64 is kept for the time root). */
 pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src, const int *d_dst,
-                                    const float *d_topt, long long E, int numDisc, float *d_disc,
-                                    pump_stream_t stream);
+                                    const float *d_topt, long long E, int numDisc, int mode,
+                                    float *d_disc, pump_stream_t stream);
 
 /* ------------------------------------------------------ collision checks */
 /* isFree[i] = sample i is not strictly inside any box (sampleFree,

@@ -355,6 +355,63 @@ void orc_bvp_pairs(int N, const float *samples, float tmax, float *copts, float 
   }
 }
 
+/* ---------------- precision-mode reference (long double) ---------------- */
+typedef struct { long double A0, A1, A2, A3, A4; } orc_quartic;
+
+static orc_quartic orc_make_quartic(const float *x0, const float *x1) {
+  const long double g = (long double)ORC_G;
+  long double dx = (long double)x1[0] - x0[0], dy = (long double)x1[1] - x0[1],
+              dz = (long double)x1[2] - x0[2];
+  long double sx = (long double)x0[3] + x1[3], sy = (long double)x0[4] + x1[4],
+              sz = (long double)x0[5] + x1[5];
+  orc_quartic q;
+  q.A0 = 12.0L * (dx * dx + dy * dy + dz * dz);
+  q.A1 = -12.0L * (dx * sx + dy * sy + dz * sz);
+  q.A2 = 4.0L * ((long double)x0[3] * x0[3] + (long double)x0[4] * x0[4] + (long double)x0[5] * x0[5] +
+                 (long double)x0[3] * x1[3] + (long double)x0[4] * x1[4] + (long double)x0[5] * x1[5] +
+                 (long double)x1[3] * x1[3] + (long double)x1[4] * x1[4] + (long double)x1[5] * x1[5]);
+  q.A3 = 2.0L * g * ((long double)x0[5] - x1[5]);
+  q.A4 = 1.0L + g * g;
+  return q;
+}
+static long double orc_qc(const orc_quartic *q, long double t) {
+  return q->A0 / (t * t * t) + q->A1 / (t * t) + q->A2 / t + q->A3 + q->A4 * t;
+}
+static long double orc_qdc(const orc_quartic *q, long double t) {
+  return -3.0L * q->A0 / (t * t * t * t) - 2.0L * q->A1 / (t * t * t) - q->A2 / (t * t) + q->A4;
+}
+
+double orc_cost_exact(double t, const float *x0, const float *x1) {
+  orc_quartic q = orc_make_quartic(x0, x1);
+  return (double)orc_qc(&q, (long double)t);
+}
+
+void orc_bvp_precise(const float *x0, const float *x1, float tmax, double *topt, double *cost) {
+  orc_quartic q = orc_make_quartic(x0, x1);
+  const int K = 4000;
+  const long double tm = tmax, lo = 1e-4L * tm;
+  long double best_t = tm, best_c = orc_qc(&q, tm);
+  long double tp = lo, dp = orc_qdc(&q, lo);
+  for (int k = 1; k < K; ++k) {
+    long double t = lo * powl(tm / lo, (long double)k / (K - 1));
+    if (k == K - 1) t = tm;
+    long double d = orc_qdc(&q, t);
+    if (dp < 0 && d > 0) {
+      long double a = tp, b = t;
+      for (int it = 0; it < 200; ++it) {
+        long double m = 0.5L * (a + b);
+        if (orc_qdc(&q, m) < 0) a = m; else b = m;
+      }
+      long double r = 0.5L * (a + b), c = orc_qc(&q, r);
+      if (c < best_c) { best_c = c; best_t = r; }
+    }
+    tp = t;
+    dp = d;
+  }
+  *topt = (double)best_t;
+  *cost = (double)best_c;
+}
+
 /* ======================================================================
  * Sampler (sampler.cu)
  * ==================================================================== */

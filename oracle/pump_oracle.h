@@ -62,6 +62,17 @@ float orc_find_optimal_path(float dt, float *split, int cap, const float *xs, in
 /* 2pBVP.cu:133-150 over all ordered pairs i != j, idx = i*(N-1)+j-(i<j). */
 void orc_bvp_pairs(int N, const float *samples, float tmax, float *copts, float *topts);
 
+/* Precision-mode reference: the global minimiser over (0, tmax] of the same
+ * cost function written out as A0/t^3 + A1/t^2 + A2/t + A3 + A4 t, found in
+ * long double by scanning c' on a log grid of 4000 points over
+ * [1e-4 tmax, tmax], bisecting every -/+ sign change 200 times, and comparing
+ * the candidates with tmax.  An independent algorithm for checking the GPU's
+ * closed-form root solver. */
+void orc_bvp_precise(const float *x0, const float *x1, float tmax, double *topt, double *cost);
+/* Exact cost c(t) of a pair in long double (for stating the parity method's
+ * cost excess over the optimum). */
+double orc_cost_exact(double t, const float *x0, const float *x1);
+
 /* ---------------- sampler (sampler.cu) ---------------- */
 float orc_halton(int n, int b);                                           /* sampler.cu:43-57 */
 void orc_halton_samples(int N, float *samples, const float *init, const float *goal,

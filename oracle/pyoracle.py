@@ -118,6 +118,10 @@ def lib():
             L.orc_det_log.argtypes = [C.c_double]
             L.orc_det_sincos_2pi.argtypes = [C.c_double, C.POINTER(C.c_double),
                                              C.POINTER(C.c_double)]
+            L.orc_bvp_precise.argtypes = [f32p, f32p, C.c_float, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double)]
+            L.orc_cost_exact.restype = C.c_double
+            L.orc_cost_exact.argtypes = [C.c_double, f32p, f32p]
             L.orc_particle_tables.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
             L.orc_particle_cov.argtypes = [C.c_int, f64p]
             L.orc_plan.restype = C.c_int
@@ -168,6 +172,17 @@ def topt(x0, x1, tmax=5.0):
 
 def cost(tau, x0, x1):
     return lib().orc_cost(tau, f32(x0), f32(x1))
+
+
+def bvp_precise(x0, x1, tmax=5.0):
+    """Long-double global minimiser (topt, cost) of the pair cost."""
+    t, c = C.c_double(0), C.c_double(0)
+    lib().orc_bvp_precise(f32(x0), f32(x1), tmax, C.byref(t), C.byref(c))
+    return t.value, c.value
+
+
+def cost_exact(t, x0, x1):
+    return lib().orc_cost_exact(float(t), f32(x0), f32(x1))
 
 
 def build_edges(copts, topts, N, rn):

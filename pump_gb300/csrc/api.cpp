@@ -42,7 +42,26 @@ Ctx::~Ctx() {
   cudaSetDevice(device_);
   for (int i = 0; i < kNumSlots; ++i)
     if (buf_[i]) cudaFree(buf_[i]);
+  if (table_) cudaFree(table_);
   if (prev >= 0) cudaSetDevice(prev);
+}
+
+pump_status_t Ctx::particle_table(uint64_t seed, int P, int T, const float **out,
+                                  cudaStream_t stream) {
+  if (!table_ || table_seed_ != seed || table_P_ != P || table_T_ != T) {
+    if (table_) {
+      PUMP_CUDA_TRY(cudaDeviceSynchronize());
+      PUMP_CUDA_TRY(cudaFree(table_));
+      table_ = nullptr;
+    }
+    PUMP_CUDA_TRY(cudaMalloc(&table_, sizeof(float) * 3 * (size_t)P * T));
+    PUMP_TRY(particle_tables_async(seed, P, T, table_, nullptr, stream));
+    table_seed_ = seed;
+    table_P_ = P;
+    table_T_ = T;
+  }
+  *out = table_;
+  return PUMP_OK;
 }
 
 pump_status_t Ctx::activate() { return cuda_status(cudaSetDevice(device_), "cudaSetDevice"); }

@@ -145,10 +145,18 @@ struct Quartic {
   double A0, A1, A2, A3, A4;
   __device__ double Q(double t) const { return ((A4 * t * t - A2) * t - 2.0 * A1) * t - 3.0 * A0; }
   __device__ double dQ(double t) const { return (4.0 * A4 * t * t - 2.0 * A2) * t - 2.0 * A1; }
-  __device__ double d2Q(double t) const { return 12.0 * A4 * t * t - 2.0 * A2; }
   __device__ double cost(double t) const {
-    return (((A0 / t + A1) / t + A2) / t + A3) + A4 * t;
+    const double r = 1.0 / t;
+    return (((A0 * r + A1) * r + A2) * r + A3) + A4 * t;
   }
+};
+
+// The same polynomials in binary32 for the bracketing phase.
+struct QuarticF {
+  float A0, A1, A2, A4;
+  __device__ float Q(float t) const { return ((A4 * t * t - A2) * t - 2.0f * A1) * t - 3.0f * A0; }
+  __device__ float dQ(float t) const { return (4.0f * A4 * t * t - 2.0f * A2) * t - 2.0f * A1; }
+  __device__ float d2Q(float t) const { return 12.0f * A4 * t * t - 2.0f * A2; }
 };
 
 __device__ __forceinline__ Quartic make_quartic(const float *x0, const float *x1) {
@@ -167,61 +175,84 @@ __device__ __forceinline__ Quartic make_quartic(const float *x0, const float *x1
   return q;
 }
 
-// Root of a function monotone on [a, b] with f(a) and f(b) of opposite sign
-// (fa = f(a)); Newton steps kept inside the shrinking bracket, bisection
-// otherwise.  Which = 0: Q, 1: Q'.
-template <int Which>
-__device__ double bracket_root(const Quartic &q, double a, double b, double fa) {
-  double x = 0.5 * (a + b);
-  for (int it = 0; it < 100; ++it) {
-    const double f = Which == 0 ? q.Q(x) : q.dQ(x);
-    const double df = Which == 0 ? q.dQ(x) : q.d2Q(x);
-    if (f == 0.0) return x;
-    if ((f < 0.0) == (fa < 0.0)) a = x; else b = x;
-    double xn = x - f / df;
-    if (!(xn > a && xn < b)) xn = 0.5 * (a + b);
-    if (fabs(xn - x) <= 1e-16 * fabs(x) || b - a <= 4e-16 * b) return xn;
+// Root of a monotone function on [a, b] (sign change given) with fixed
+// convexity: Newton started at the end where the function and its curvature
+// have the same sign converges monotonically.  Binary32, explicit fma.
+template <int Deriv>
+__device__ float newton_f(const QuarticF &q, float a, float b, bool from_b) {
+  float x = from_b ? b : a;
+  for (int it = 0; it < 60; ++it) {
+    const float f = Deriv ? q.dQ(x) : q.Q(x);
+    const float df = Deriv ? q.d2Q(x) : q.dQ(x);
+    if (f == 0.0f || df == 0.0f) break;
+    float xn = x - f / df;
+    if (!(xn >= a && xn <= b)) xn = 0.5f * (a + b);
+    if (fabsf(xn - x) <= 1e-6f * fabsf(xn)) { x = xn; break; }
     x = xn;
   }
   return x;
 }
 
+// Binary64 Newton polish of a root of Q bracketed by [a, b] (Q(a) < 0 < Q(b)).
+__device__ double polish(const Quartic &q, double x, double a, double b) {
+  for (int it = 0; it < 6; ++it) {
+    const double f = q.Q(x);
+    if (f == 0.0) return x;
+    if (f < 0.0) a = x; else b = x;
+    double xn = x - f / q.dQ(x);
+    if (!(xn >= a && xn <= b)) xn = 0.5 * (a + b);
+    if (fabs(xn - x) <= 4.5e-16 * fabs(xn)) return xn;
+    x = xn;
+  }
+  return x;
+}
+
+// Global minimiser of the cost on (0, tmax].  (0, tmax] is split at the
+// inflection point tc of Q (Q'' = 0) and at the real roots of Q', so that on
+// every piece Q is monotone with fixed convexity; each upward sign change of
+// Q is a local minimum of the cost.
 __device__ double precise_topt(const Quartic &q, double tmax) {
-  // breakpoints of Q's monotone pieces inside (0, tmax)
-  double bp[4];
+  QuarticF qf;
+  qf.A0 = (float)q.A0; qf.A1 = (float)q.A1; qf.A2 = (float)q.A2; qf.A4 = (float)q.A4;
+  const float tmf = (float)tmax;
+  double bp[5];
   int nb = 0;
   bp[nb++] = 0.0;
-  const double tc = sqrt(q.A2 / (6.0 * q.A4));  // Q'' = 0
-  const double d0 = q.dQ(0.0);
+  const double tc = sqrt(q.A2 / (6.0 * q.A4));
+  const double d0 = -2.0 * q.A1;  // Q'(0)
   if (tc > 0.0 && tc < tmax) {
     const double dc = q.dQ(tc);
-    if (d0 > 0.0 && dc < 0.0) bp[nb++] = bracket_root<1>(q, 0.0, tc, d0);
-    if (dc < 0.0 && q.dQ(tmax) > 0.0) bp[nb++] = bracket_root<1>(q, tc, tmax, dc);
+    if (d0 > 0.0 && dc < 0.0)  // Q' decreasing and concave-down on (0, tc): Newton from 0
+      bp[nb++] = (double)newton_f<1>(qf, 0.0f, (float)tc, false);
+    bp[nb++] = tc;
+    if (dc < 0.0 && q.dQ(tmax) > 0.0)  // Q' increasing, convex on (tc, tmax): Newton from tmax
+      bp[nb++] = (double)newton_f<1>(qf, (float)tc, tmf, true);
   } else if (tc <= 0.0) {
-    if (d0 < 0.0 && q.dQ(tmax) > 0.0) bp[nb++] = bracket_root<1>(q, 0.0, tmax, d0);
-  } else {  // tc >= tmax: Q' decreasing on (0, tmax)
-    if (d0 > 0.0 && q.dQ(tmax) < 0.0) bp[nb++] = bracket_root<1>(q, 0.0, tmax, d0);
+    if (d0 < 0.0 && q.dQ(tmax) > 0.0) bp[nb++] = (double)newton_f<1>(qf, 0.0f, tmf, true);
+  } else if (d0 > 0.0 && q.dQ(tmax) < 0.0) {
+    bp[nb++] = (double)newton_f<1>(qf, 0.0f, tmf, false);
   }
   bp[nb++] = tmax;
   double best_t = tmax, best_c = 0.0;
   bool have = false;
-  const double qmax = q.Q(tmax);
-  if (qmax < 0.0) {
-    best_c = q.cost(tmax);
-    have = true;
-  }
+  double qa = q.Q(0.0);
   for (int k = 0; k + 1 < nb; ++k) {
     const double a = bp[k], b = bp[k + 1];
-    const double fa = q.Q(a), fb = (b == tmax) ? qmax : q.Q(b);
-    if (fa < 0.0 && fb > 0.0) {
-      const double r = bracket_root<0>(q, a, b, fa);
+    const double qb = q.Q(b);
+    if (qa < 0.0 && qb > 0.0) {
+      // convex piece (a >= tc): start from b; concave piece: start from a
+      const float xf = newton_f<0>(qf, (float)a, (float)b, a >= tc);
+      double x = (double)xf;
+      if (!(x > a && x < b)) x = 0.5 * (a + b);
+      const double r = polish(q, x, a, b);
       const double cr = q.cost(r);
-      if (!have || cr < best_c) {
-        best_c = cr;
-        best_t = r;
-        have = true;
-      }
+      if (!have || cr < best_c) { best_c = cr; best_t = r; have = true; }
     }
+    qa = qb;
+  }
+  if (qa < 0.0) {  // cost still decreasing at tmax
+    const double cm = q.cost(tmax);
+    if (!have || cm < best_c) { best_c = cm; best_t = tmax; have = true; }
   }
   return best_t;
 }
@@ -337,7 +368,26 @@ __device__ __forceinline__ void path_point(float t, float tau, const float *x0, 
   }
 }
 
+// The same trajectory as path_point (cubic position, quadratic velocity,
+// no gravity term) in binary32 Hermite form with s = t / tau; used by the
+// precision mode, where FP64 is reserved for the optimal-time root.
+__device__ __forceinline__ void path_point_f32(float t, float tau, const float *x0, const float *x1,
+                                               float *x) {
+  const float s = t / tau;
+  const float s2 = s * s, s3 = s2 * s;
+  const float h00 = fmaf(2.0f, s3, fmaf(-3.0f, s2, 1.0f)), h01 = fmaf(-2.0f, s3, 3.0f * s2);
+  const float h10 = tau * (s3 - 2.0f * s2 + s), h11 = tau * (s3 - s2);
+  const float g00 = (6.0f * s2 - 6.0f * s) / tau, g10 = fmaf(3.0f, s2, fmaf(-4.0f, s, 1.0f));
+  const float g11 = fmaf(3.0f, s2, -2.0f * s);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    x[k] = fmaf(h00, x0[k], fmaf(h01, x1[k], fmaf(h10, x0[k + 3], h11 * x1[k + 3])));
+    x[k + 3] = fmaf(g00, x0[k] - x1[k], fmaf(g10, x0[k + 3], g11 * x1[k + 3]));
+  }
+}
+
 // One thread per (edge, waypoint): findDiscretizedPath, 2pBVP.cu:53-69.
+template <int Mode>
 __global__ void discretize_kernel(const float *__restrict__ samples, const int *__restrict__ src,
                                   const int *__restrict__ dst, const float *__restrict__ toptE,
                                   long long E, int numDisc, float *__restrict__ disc) {
@@ -362,7 +412,8 @@ __global__ void discretize_kernel(const float *__restrict__ samples, const int *
   } else {
     const float topt = toptE[e];
     const float dt = topt / numDisc;
-    path_point(dt * i, topt, x0, x1, x);
+    if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
+    else path_point_f32(dt * i, topt, x0, x1, x);
   }
   float *o = disc + tid * kDim;
 #pragma unroll
@@ -432,12 +483,18 @@ extern "C" pump_status_t pump_bvp_batch(const float *d_x0, const float *d_x1, in
 
 extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src,
                                                const int *d_dst, const float *d_topt, long long E,
-                                               int numDisc, float *d_disc, pump_stream_t stream) {
-  if (E < 0 || numDisc < 1 || (E > 0 && (!d_samples || !d_src || !d_dst || !d_topt || !d_disc)))
+                                               int numDisc, int mode, float *d_disc,
+                                               pump_stream_t stream) {
+  if (E < 0 || numDisc < 1 || (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION) ||
+      (E > 0 && (!d_samples || !d_src || !d_dst || !d_topt || !d_disc)))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_discretize_edges: bad arguments");
   if (E == 0) return PUMP_OK;
   const long long n = E * (numDisc + 1);
-  discretize_kernel<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(d_samples, d_src, d_dst,
-                                                                       d_topt, E, numDisc, d_disc);
+  if (mode == PUMP_BVP_PARITY)
+    discretize_kernel<PUMP_BVP_PARITY><<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(
+        d_samples, d_src, d_dst, d_topt, E, numDisc, d_disc);
+  else
+    discretize_kernel<PUMP_BVP_PRECISION><<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
+        d_samples, d_src, d_dst, d_topt, E, numDisc, d_disc);
   return launch_status("discretize_edges");
 }

@@ -28,11 +28,18 @@ class Ctx {
   pump_status_t activate();
   // Device buffer of at least `bytes` for `slot` (contents undefined).
   pump_status_t scratch(int slot, size_t bytes, void **out);
+  // Time-major particle table for (seed, P, T), generated on first use and
+  // kept for later queries of this context (the reference loads its table
+  // once per process).
+  pump_status_t particle_table(uint64_t seed, int P, int T, const float **out, cudaStream_t stream);
 
  private:
   int device_;
   void *buf_[kNumSlots];
   size_t cap_[kNumSlots];
+  float *table_ = nullptr;
+  uint64_t table_seed_ = 0;
+  int table_P_ = 0, table_T_ = 0;
 };
 
 // Internal device-side entry points shared between translation units.
@@ -44,6 +51,8 @@ pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_
                                  long long *h_num_edges, cudaStream_t stream);
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                       int *d_count, int **d_error_out, cudaStream_t stream);
+pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
+                                    cudaStream_t stream);
 pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
                               const float *d_tau, int total, float *d_out, cudaStream_t stream);
 

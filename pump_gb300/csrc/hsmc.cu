@@ -109,36 +109,56 @@ __device__ void det_sincos_2pi(double u, double *s, double *c) {
 
 constexpr double kDT = 0.05, kH2 = 0.00125, kKP = 16.0, kKD = 5.6, kSigmaW = 4.0;
 
-__global__ void particle_table_kernel(uint32_t k0, uint32_t k1, int P, int T,
-                                      float *__restrict__ tmajor, float *__restrict__ pmajor) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
+// One warp per particle.  The Gaussians of 32 consecutive steps are
+// independent, so lane k computes step t0+k (Philox, Box-Muller); the
+// closed-loop recurrence is sequential, so every lane replays it over the 32
+// steps with the lanes' noise broadcast by shuffles, and lane k stores step
+// t0+k.  Arithmetic is identical to a scalar loop (same operations, same
+// order, no contraction).
+__global__ void __launch_bounds__(256) particle_table_kernel(uint32_t k0, uint32_t k1, int P, int T,
+                                                             float *__restrict__ tmajor,
+                                                             float *__restrict__ pmajor) {
+  const int lane = threadIdx.x & 31;
+  const int p = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  if (p >= P) return;  // warp-uniform
   double pos[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
   const double sc = 2.3283064365386962890625e-10;  // 2^-32
-  for (int t = 0; t < T; ++t) {
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const float v = (float)pos[d];
-      if (tmajor) tmajor[((long long)t * P + p) * 3 + d] = v;
-      if (pmajor) pmajor[((long long)p * T + t) * 3 + d] = v;
+  for (int t0 = 0; t0 < T; t0 += 32) {
+    const int t = t0 + lane;
+    double z[3] = {0, 0, 0};
+    if (t < T) {
+      uint32_t o[4];
+      philox4x32_10((uint32_t)p, (uint32_t)t, 0u, 0u, k0, k1, o);
+      const double u0 = ((double)o[0] + 0.5) * sc, u1 = ((double)o[1] + 0.5) * sc;
+      const double u2 = ((double)o[2] + 0.5) * sc, u3 = ((double)o[3] + 0.5) * sc;
+      const double r0 = sqrt(-2.0 * det_log(u0));
+      const double r1 = sqrt(-2.0 * det_log(u2));
+      double s0, c0, s1, c1;
+      det_sincos_2pi(u1, &s0, &c0);
+      det_sincos_2pi(u3, &s1, &c1);
+      z[0] = r0 * c0;
+      z[1] = r0 * s0;
+      z[2] = r1 * c1;
     }
-    uint32_t o[4];
-    philox4x32_10((uint32_t)p, (uint32_t)t, 0u, 0u, k0, k1, o);
-    const double u0 = ((double)o[0] + 0.5) * sc, u1 = ((double)o[1] + 0.5) * sc;
-    const double u2 = ((double)o[2] + 0.5) * sc, u3 = ((double)o[3] + 0.5) * sc;
-    const double r0 = sqrt(-2.0 * det_log(u0));
-    const double r1 = sqrt(-2.0 * det_log(u2));
-    double s0, c0, s1, c1;
-    det_sincos_2pi(u1, &s0, &c0);
-    det_sincos_2pi(u3, &s1, &c1);
-    const double z[3] = {r0 * c0, r0 * s0, r1 * c1};
+    const int steps = T - t0 < 32 ? T - t0 : 32;
+    for (int k = 0; k < steps; ++k) {
+      if (k == lane) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const double a = kSigmaW * z[d] - (kKP * pos[d] + kKD * vel[d]);
-      const double pn = (pos[d] + kDT * vel[d]) + kH2 * a;
-      const double vn = vel[d] + kDT * a;
-      pos[d] = pn;
-      vel[d] = vn;
+        for (int d = 0; d < 3; ++d) {
+          const float v = (float)pos[d];
+          if (tmajor) tmajor[((long long)(t0 + k) * P + p) * 3 + d] = v;
+          if (pmajor) pmajor[((long long)p * T + t0 + k) * 3 + d] = v;
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const double zk = __shfl_sync(0xffffffffu, z[d], k);
+        const double a = kSigmaW * zk - (kKP * pos[d] + kKD * vel[d]);
+        const double pn = (pos[d] + kDT * vel[d]) + kH2 * a;
+        const double vn = vel[d] + kDT * a;
+        pos[d] = pn;
+        vel[d] = vn;
+      }
     }
   }
 }
@@ -222,47 +242,46 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
 }
 
 // -------------------------------------------------------------- MC CP
-// grid (ceil(Pmc / blockDim), n_paths); collisionProbability.cu:39-92.
+// collisionProbability.cu:39-92.  A particle collides when any of the
+// segments t = 0 .. T-3 of its perturbed path hits a box; the reference walks
+// the segments in order and stops at the first hit, which gives the same
+// answer as testing all of them.  Block = 32 particles (the lanes) x 8 warps;
+// warp w tests segments t = w, w + 8, ...; the per-particle OR over warps is
+// taken in shared memory and the block adds its popcount to hits[k].
+// Grid (ceil(Pmc / 32), paths).
 __global__ void __launch_bounds__(256) mc_cp_kernel(
     const float *__restrict__ paths, const int *__restrict__ offset, const int *__restrict__ len,
     const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
     const float *__restrict__ obs, int numObs, int k0, int *__restrict__ hits) {
   extern __shared__ float4 s_obs4[];
   float *s_obs = reinterpret_cast<float *>(s_obs4);
-  __shared__ int s_hits[8];
+  __shared__ unsigned int s_hit[8];
   stage_obstacles(obs, numObs, s_obs);
   const int k = k0 + blockIdx.y;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int p = blockIdx.x * 32 + lane;
   const int T = len[k];
   const float *path = paths + (long long)offset[k] * kDim;
-  int coll = 0;
+  bool coll = false;
   if (p < Pmc && T <= T_rows) {
-    float v[3], w[3];
-    if (T - 2 > 0) {
+    for (int t = warp; t < T - 2 && !coll; t += 8) {
+      float v[3], w[3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) v[d] = path[d] + __ldg(&offsets_t[(long long)p * 3 + d]) * offset_mult;
-    }
-    for (int t = 0; t < T - 2; ++t) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d)
+      for (int d = 0; d < 3; ++d) {
+        v[d] = path[t * kDim + d] + __ldg(&offsets_t[((long long)t * Pmc + p) * 3 + d]) * offset_mult;
         w[d] = path[(t + 1) * kDim + d] +
                __ldg(&offsets_t[((long long)(t + 1) * Pmc + p) * 3 + d]) * offset_mult;
-      if (!segment_valid(v, w, numObs, s_obs)) {
-        coll = 1;
-        break;
       }
-#pragma unroll
-      for (int d = 0; d < 3; ++d) v[d] = w[d];
+      coll = !segment_valid(v, w, numObs, s_obs);
     }
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) coll += __shfl_down_sync(0xffffffffu, coll, off);
-  if (lane == 0) s_hits[warp] = coll;
+  const unsigned int bal = __ballot_sync(0xffffffffu, coll);
+  if (lane == 0) s_hit[warp] = bal;
   __syncthreads();
   if (threadIdx.x == 0) {
-    int total = 0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) total += s_hits[q];
+    unsigned int any = 0;
+    for (int q = 0; q < 8; ++q) any |= s_hit[q];
+    const int total = __popc(any);
     if (total) atomicAdd(&hits[k], total);
   }
 }
@@ -299,7 +318,7 @@ pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *
   PUMP_CUDA_TRY(cudaMemsetAsync(d_hits, 0, sizeof(int) * n_paths, stream));
   for (int k0 = 0; k0 < n_paths; k0 += 65535) {
     const int nk = n_paths - k0 < 65535 ? n_paths - k0 : 65535;
-    dim3 grid(grid_for(Pmc, 256), (unsigned)nk);
+    dim3 grid(grid_for(Pmc, 32), (unsigned)nk);
     mc_cp_kernel<<<grid, 256, smem, stream>>>(d_paths, d_offset, d_len, d_offsets_t, Pmc, T_rows,
                                               offset_mult, d_obstacles, numObs, k0, d_hits);
     PUMP_TRY(launch_status("mc_cp_kernel"));
@@ -336,8 +355,8 @@ pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n,
 
 pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
                                     cudaStream_t stream) {
-  particle_table_kernel<<<grid_for(P, 128), 128, 0, stream>>>((uint32_t)seed, (uint32_t)(seed >> 32),
-                                                             P, T, d_tmajor, d_pmajor);
+  particle_table_kernel<<<grid_for((long long)P * 32, 256), 256, 0, stream>>>(
+      (uint32_t)seed, (uint32_t)(seed >> 32), P, T, d_tmajor, d_pmajor);
   return launch_status("particle_table_kernel");
 }
 

@@ -43,8 +43,6 @@ pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *
                           const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                           const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
                           int *d_error, cudaStream_t stream);
-pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
-                                    cudaStream_t stream);
 
 namespace {
 
@@ -157,7 +155,8 @@ class Planner {
   std::vector<float> samples_;
   DevBuf<float> d_samples_, d_obs_, d_copts_, d_topts_;
   DevBuf<int> d_src_, d_dst_, d_go_;
-  DevBuf<float> d_coptE_, d_toptE_, d_disc_, d_as_, d_bs_, d_tmajor_;
+  DevBuf<float> d_coptE_, d_toptE_, d_disc_, d_as_, d_bs_;
+  const float *d_table_ = nullptr;  // context-cached particle table
   DevBuf<uint8_t> d_free_s_, d_free_e_;
   long long E_ = 0;
   float rn_ = 0;
@@ -174,6 +173,9 @@ class Planner {
   DevBuf<float> d_pathTime_, d_cpStage_;
   DevBuf<int> d_wfPrev_, d_wfEdge_, d_map_, d_err_;
   int numPaths_ = 0;
+  // reusable scratch of the batched BVP / dense-path / MC CP helpers
+  DevBuf<float> d_bx0_, d_bx1_, d_bt_, d_bc_, d_xs_, d_ts_, d_tau_, d_mcp_;
+  DevBuf<int> d_seg_, d_moff_, d_mlen_, d_mhits_;
 };
 
 pump_status_t Planner::run() {
@@ -230,7 +232,7 @@ pump_status_t Planner::roadmap() {
   res_->num_edges = E_;
   PUMP_TRY(d_disc_.alloc((size_t)E_ * W_ * kDim));
   PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, d_toptE_.p, E_, pb_.num_disc,
-                                 d_disc_.p, (pump_stream_t)s_));
+                                 pb_.bvp_mode, d_disc_.p, (pump_stream_t)s_));
   // heuristic h (mainPUMP.cu:351-355): cost of the optimal connection to the goal
   {
     std::vector<float> x0((size_t)(N_ - 1) * kDim), x1((size_t)(N_ - 1) * kDim);
@@ -269,8 +271,7 @@ pump_status_t Planner::online() {
   PUMP_TRY(d_bs_.alloc((size_t)E_ * W_ * maxHS_));
   PUMP_TRY(pump_cache_halfspaces(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_, maxd2,
                                  d_as_.p, d_bs_.p, nullptr, (pump_stream_t)s_));
-  PUMP_TRY(d_tmajor_.alloc((size_t)pb_.table_rows * pb_.num_mc * 3));
-  PUMP_TRY(particle_tables_async(pb_.seed, pb_.num_mc, pb_.table_rows, d_tmajor_.p, nullptr, s_));
+  PUMP_TRY(ctx_->particle_table(pb_.seed, pb_.num_mc, pb_.table_rows, &d_table_, s_));
   free_s_.resize(N_);
   free_e_.resize(E_);
   PUMP_TRY(d2h(free_s_.data(), d_free_s_.p, N_));
@@ -369,7 +370,7 @@ pump_status_t Planner::explore() {
     PUMP_TRY(h2d(d_wfPrev_.p, wfPrev.data(), numNew));
     PUMP_TRY(h2d(d_wfEdge_.p, wfEdge.data(), numNew));
     PUMP_TRY(hsmc_staged_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p, d_bs_.p, maxHS_,
-                               d_pathTime_.p, d_toptE_.p, dt_, d_tmajor_.p, pb_.num_mc,
+                               d_pathTime_.p, d_toptE_.p, dt_, d_table_, pb_.num_mc,
                                pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p, P_,
                                d_cpStage_.p, d_err_.p, s_));
     newCP.resize(numNew);
@@ -479,16 +480,16 @@ pump_status_t Planner::topts_of(const std::vector<float> &x0, const std::vector<
   if (topt) topt->assign(n, 0.0f);
   if (cost) cost->assign(n, 0.0f);
   if (n == 0) return PUMP_OK;
-  DevBuf<float> d_x0, d_x1, d_t, d_c;
-  PUMP_TRY(d_x0.alloc(x0.size()));
-  PUMP_TRY(d_x1.alloc(x1.size()));
-  PUMP_TRY(d_t.alloc(n));
-  PUMP_TRY(d_c.alloc(n));
-  PUMP_TRY(h2d(d_x0.p, x0.data(), x0.size()));
-  PUMP_TRY(h2d(d_x1.p, x1.data(), x1.size()));
-  PUMP_TRY(pump_bvp_batch(d_x0.p, d_x1.p, n, tmax, pb_.bvp_mode, d_t.p, d_c.p, (pump_stream_t)s_));
-  if (topt) PUMP_TRY(d2h(topt->data(), d_t.p, n));
-  if (cost) PUMP_TRY(d2h(cost->data(), d_c.p, n));
+  PUMP_TRY(d_bx0_.alloc(x0.size()));
+  PUMP_TRY(d_bx1_.alloc(x1.size()));
+  PUMP_TRY(d_bt_.alloc(n));
+  PUMP_TRY(d_bc_.alloc(n));
+  PUMP_TRY(h2d(d_bx0_.p, x0.data(), x0.size()));
+  PUMP_TRY(h2d(d_bx1_.p, x1.data(), x1.size()));
+  PUMP_TRY(pump_bvp_batch(d_bx0_.p, d_bx1_.p, n, tmax, pb_.bvp_mode, d_bt_.p, d_bc_.p,
+                          (pump_stream_t)s_));
+  if (topt) PUMP_TRY(d2h(topt->data(), d_bt_.p, n));
+  if (cost) PUMP_TRY(d2h(cost->data(), d_bc_.p, n));
   return sync();
 }
 
@@ -547,17 +548,15 @@ pump_status_t Planner::dense_paths(const std::vector<std::vector<float>> &xs, fl
   }
   PUMP_TRY(d_states.alloc((size_t)(total > 0 ? total : 1) * kDim));
   if (total > 0) {
-    DevBuf<float> d_xs, d_ts, d_tau;
-    DevBuf<int> d_seg;
-    PUMP_TRY(d_xs.alloc(allxs.size()));
-    PUMP_TRY(d_ts.alloc(total));
-    PUMP_TRY(d_tau.alloc(tauByPair.size()));
-    PUMP_TRY(d_seg.alloc(total));
-    PUMP_TRY(h2d(d_xs.p, allxs.data(), allxs.size()));
-    PUMP_TRY(h2d(d_ts.p, tsample.data(), total));
-    PUMP_TRY(h2d(d_tau.p, tauByPair.data(), tauByPair.size()));
-    PUMP_TRY(h2d(d_seg.p, seg.data(), total));
-    PUMP_TRY(bvp_path_states(d_xs.p, d_seg.p, d_ts.p, d_tau.p, total, d_states.p, s_));
+    PUMP_TRY(d_xs_.alloc(allxs.size()));
+    PUMP_TRY(d_ts_.alloc(total));
+    PUMP_TRY(d_tau_.alloc(tauByPair.size()));
+    PUMP_TRY(d_seg_.alloc(total));
+    PUMP_TRY(h2d(d_xs_.p, allxs.data(), allxs.size()));
+    PUMP_TRY(h2d(d_ts_.p, tsample.data(), total));
+    PUMP_TRY(h2d(d_tau_.p, tauByPair.data(), tauByPair.size()));
+    PUMP_TRY(h2d(d_seg_.p, seg.data(), total));
+    PUMP_TRY(bvp_path_states(d_xs_.p, d_seg_.p, d_ts_.p, d_tau_.p, total, d_states.p, s_));
     PUMP_TRY(sync());
   }
   return PUMP_OK;
@@ -565,25 +564,27 @@ pump_status_t Planner::dense_paths(const std::vector<std::vector<float>> &xs, fl
 
 pump_status_t Planner::mc_cp_batch(const DevBuf<float> &d_states, const DensePaths &dp,
                                    std::vector<float> &cp) {
+  // Paths longer than the particle table get CP -1 (checked by the caller
+  // only if it actually uses that path; speculative batches may hold some).
   const int n = (int)dp.len.size();
   cp.assign(n, 0.0f);
   if (n == 0) return PUMP_OK;
+  std::vector<int> len(dp.len);
   for (int k = 0; k < n; ++k)
-    if (dp.len[k] > pb_.table_rows)
-      return set_error(PUMP_ERR_CAPACITY, "dense path of %d states exceeds the %d-row particle table",
-                       dp.len[k], pb_.table_rows);
-  DevBuf<int> d_off, d_len, d_hits;
-  DevBuf<float> d_cp;
-  PUMP_TRY(d_off.alloc(n));
-  PUMP_TRY(d_len.alloc(n));
-  PUMP_TRY(d_hits.alloc(n));
-  PUMP_TRY(d_cp.alloc(n));
-  PUMP_TRY(h2d(d_off.p, dp.offset.data(), n));
-  PUMP_TRY(h2d(d_len.p, dp.len.data(), n));
-  PUMP_TRY(mc_cp_async(d_states.p, d_off.p, d_len.p, n, d_tmajor_.p, pb_.num_mc, pb_.table_rows,
-                       pb_.offset_mult, d_obs_.p, nobs_, d_hits.p, d_cp.p, nullptr, s_));
-  PUMP_TRY(d2h(cp.data(), d_cp.p, n));
-  return sync();
+    if (len[k] > pb_.table_rows) len[k] = 0;
+  PUMP_TRY(d_moff_.alloc(n));
+  PUMP_TRY(d_mlen_.alloc(n));
+  PUMP_TRY(d_mhits_.alloc(n));
+  PUMP_TRY(d_mcp_.alloc(n));
+  PUMP_TRY(h2d(d_moff_.p, dp.offset.data(), n));
+  PUMP_TRY(h2d(d_mlen_.p, len.data(), n));
+  PUMP_TRY(mc_cp_async(d_states.p, d_moff_.p, d_mlen_.p, n, d_table_, pb_.num_mc, pb_.table_rows,
+                       pb_.offset_mult, d_obs_.p, nobs_, d_mhits_.p, d_mcp_.p, nullptr, s_));
+  PUMP_TRY(d2h(cp.data(), d_mcp_.p, n));
+  PUMP_TRY(sync());
+  for (int k = 0; k < n; ++k)
+    if (dp.len[k] > pb_.table_rows) cp[k] = -1.0f;
+  return PUMP_OK;
 }
 
 pump_status_t Planner::search_and_smooth() {
@@ -601,8 +602,12 @@ pump_status_t Planner::search_and_smooth() {
   std::vector<float> cps;
   PUMP_TRY(mc_cp_batch(d_states, dp, cps));
   int sel = -1;
-  for (size_t k = 0; k < goalPaths.size(); ++k)
+  for (size_t k = 0; k < goalPaths.size(); ++k) {
+    if (cps[k] < 0)
+      return set_error(PUMP_ERR_CAPACITY, "goal path of %d states exceeds the %d-row particle table",
+                       dp.len[k], pb_.table_rows);
     if (cps[k] < cpTarget) { sel = (int)k; break; }
+  }
   const int last = sel >= 0 ? sel : (int)goalPaths.size() - 1;
   const bool success = sel >= 0;
   res_->success = success ? 1 : 0;
@@ -652,39 +657,68 @@ pump_status_t Planner::search_and_smooth() {
     }
     const float epsSmoothCP = (float)0.0002;
     float alpha = 1.0f, alphaU = 1.0f, alphaL = 0.0f;
-    std::vector<float> xsSmooth(xs.size());
-    for (int it = 0; it < 30; ++it) {
-      for (size_t i = 0; i < xs.size(); ++i) xsSmooth[i] = (1 - alpha) * xs[i] + alpha * xsOpt[i];
-      std::vector<std::vector<float>> one(1, xsSmooth);
+    // The alpha bisection is sequential (each step's alpha depends on the
+    // previous CP), but every step is a pure function of alpha.  So the 2^D - 1
+    // alphas the next D steps can visit are evaluated in one batch (dense
+    // paths, costs and MC CPs of all of them), then the reference's decisions
+    // are replayed in order over the results: the same sequence of alphas,
+    // best-path updates and early exit as PUMP.cu:492-541.
+    const int D = 5, K = (1 << D) - 1;
+    int it = 0;
+    bool stop = false;
+    while (it < 30 && !stop) {
+      // tree node k (heap order): children 2k+1 (cp < target) and 2k+2
+      std::vector<float> nl(K), nu(K), na(K);
+      nl[0] = alphaL; nu[0] = alphaU; na[0] = alpha;
+      for (int k = 0; 2 * k + 2 < K; ++k) {
+        nl[2 * k + 1] = na[k]; nu[2 * k + 1] = nu[k];
+        na[2 * k + 1] = (nl[2 * k + 1] + nu[2 * k + 1]) / 2;
+        nl[2 * k + 2] = nl[k]; nu[2 * k + 2] = na[k];
+        na[2 * k + 2] = (nl[2 * k + 2] + nu[2 * k + 2]) / 2;
+      }
+      std::vector<std::vector<float>> cand(K, std::vector<float>(xs.size()));
+      std::vector<float> b0, b1;
+      for (int k = 0; k < K; ++k) {
+        for (size_t i = 0; i < xs.size(); ++i) cand[k][i] = (1 - na[k]) * xs[i] + na[k] * xsOpt[i];
+        for (int i = 0; i + 1 < n; ++i) {
+          b0.insert(b0.end(), &cand[k][i * kDim], &cand[k][(i + 1) * kDim]);
+          b1.insert(b1.end(), &cand[k][(i + 1) * kDim], &cand[k][(i + 2) * kDim]);
+        }
+      }
       DensePaths sp;
       DevBuf<float> d_sp;
-      PUMP_TRY(dense_paths(one, dt_, 5.0f, sp, d_sp));
-      std::vector<float> b0, b1, sc;
-      for (int i = 0; i + 1 < n; ++i) {
-        b0.insert(b0.end(), &xsSmooth[i * kDim], &xsSmooth[(i + 1) * kDim]);
-        b1.insert(b1.end(), &xsSmooth[(i + 1) * kDim], &xsSmooth[(i + 2) * kDim]);
-      }
+      PUMP_TRY(dense_paths(cand, dt_, 5.0f, sp, d_sp));
+      std::vector<float> sc, cps;
       PUMP_TRY(topts_of(b0, b1, 2.0f, nullptr, &sc));
-      float smoothCost = 0;
-      for (float c : sc) smoothCost += c;
-      std::vector<float> cp1;
-      PUMP_TRY(mc_cp_batch(d_sp, sp, cp1));
-      const float cp = cp1[0];
-      if (cp < cpTarget) alphaL = alpha;
-      if (cp >= cpTarget) alphaU = alpha;
-      alpha = (alphaL + alphaU) / 2;
-      const bool satisfies = cp < cpTarget;
-      const bool closer = cp > lastCP;
-      const bool eqLower = (cp == lastCP && smoothCost < lastCost);
-      if (satisfies && (closer || eqLower)) {
-        bestLen = sp.len[0];
-        bestPath.resize((size_t)bestLen * kDim);
-        PUMP_TRY(d2h(bestPath.data(), d_sp.p, bestPath.size()));
-        PUMP_TRY(sync());
-        lastCost = smoothCost;
-        lastCP = cp;
+      PUMP_TRY(mc_cp_batch(d_sp, sp, cps));
+      int k = 0;
+      for (int depth = 0; depth < D && it < 30; ++depth, ++it) {
+        float smoothCost = 0;
+        for (int i = 0; i + 1 < n; ++i) smoothCost += sc[(size_t)k * (n - 1) + i];
+        const float cp = cps[k];
+        if (cp < 0)
+          return set_error(PUMP_ERR_CAPACITY, "smoothed path of %d states exceeds the %d-row particle table",
+                           sp.len[k], pb_.table_rows);
+        if (cp < cpTarget) alphaL = alpha;
+        if (cp >= cpTarget) alphaU = alpha;
+        alpha = (alphaL + alphaU) / 2;
+        const bool satisfies = cp < cpTarget;
+        const bool closer = cp > lastCP;
+        const bool eqLower = (cp == lastCP && smoothCost < lastCost);
+        if (satisfies && (closer || eqLower)) {
+          bestLen = sp.len[k];
+          bestPath.resize((size_t)bestLen * kDim);
+          PUMP_TRY(d2h(bestPath.data(), d_sp.p + (size_t)sp.offset[k] * kDim, bestPath.size()));
+          PUMP_TRY(sync());
+          lastCost = smoothCost;
+          lastCP = cp;
+        }
+        if (std::fabs(cpTarget - cp) < epsSmoothCP && cpTarget - cp > 0) {
+          stop = true;
+          break;
+        }
+        k = 2 * k + (cp < cpTarget ? 1 : 2);
       }
-      if (std::fabs(cpTarget - cp) < epsSmoothCP && cpTarget - cp > 0) break;
     }
   }
   res_->soln_cp = lastCP;

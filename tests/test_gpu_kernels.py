@@ -142,7 +142,7 @@ def test_build_edges_and_waypoints(gpu, pumplib, roadmap1000):
     d_s = dev(torch, r["samples"])
     d_src2, d_dst2, d_te2 = dev(torch, r["src"]), dev(torch, r["dst"]), dev(torch, r["te"])
     d_disc = empty(torch, E * 9 * 6, torch.float32)
-    pumplib.check(L.pump_discretize_edges(ptr(d_s), ptr(d_src2), ptr(d_dst2), ptr(d_te2), E, 8,
+    pumplib.check(L.pump_discretize_edges(ptr(d_s), ptr(d_src2), ptr(d_dst2), ptr(d_te2), E, 8, 0,
                                           ptr(d_disc), stream(torch)))
     disc = host(d_disc, E * 54).reshape(E, 9, 6)
     assert same_bits(disc, r["disc"]), "waypoint mismatches: %d" % int((disc != r["disc"]).sum())
@@ -293,3 +293,29 @@ def test_frontier_compact(N, density, gpu, pumplib):
     expect = np.nonzero(flags)[0]
     assert n == expect.size
     assert np.array_equal(host(d_a, n), expect)
+
+
+def test_bvp_pairs_precision_vs_long_double(gpu, pumplib, oracle, goldens):
+    """Precision mode: the binary64 closed-form minimiser against an
+    independent long-double grid-and-bisection oracle (cost within 2 float
+    ulps, optimal time within 1e-5 relative)."""
+    torch, _ = gpu
+    _, _, init, goal, lo, hi, _ = golden_problem(goldens, "ref_N1000_input")
+    N = 400
+    s = oracle.halton_samples(N, init, goal, lo, hi)
+    rng = np.random.default_rng(3)
+    s[1:-1, :3] += rng.normal(0, 0.05, (N - 2, 3)).astype(np.float32)  # break lattice symmetry
+    c, t = run_bvp_pairs(torch, pumplib, s, mode=1)
+    idx = rng.choice(N * (N - 1), 4000, replace=False)
+    bad_c, bad_t = 0, 0
+    for q in idx:
+        i = q // (N - 1)
+        r = q - i * (N - 1)
+        j = r + (r >= i)
+        topt_ref, cost_ref = oracle.bvp_precise(s[i], s[j])
+        if abs(float(c[q]) - cost_ref) > 2.4e-7 * abs(cost_ref):
+            bad_c += 1
+        if abs(float(t[q]) - topt_ref) > 1e-5 * topt_ref:
+            bad_t += 1
+    assert bad_c == 0
+    assert bad_t <= 2  # near-equal double minima may pick a different time at equal cost
