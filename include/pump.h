@@ -170,6 +170,12 @@ pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d
 pump_status_t pump_frontier_compact(pump_ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                     int *d_count, pump_stream_t stream);
 
+/* ------------------------------------------------------------ diagnostics */
+/* Measured binary64 FMA throughput of the current device in TFLOP/s (2 flops
+ * per FMA; eight independent chains per thread, all SMs).  The denominator
+ * of the 2pBVP kernels' roofline; the reference has no counterpart. */
+pump_status_t pump_probe_fp64_tflops(double *h_tflops, pump_stream_t stream);
+
 /* ---------------------------------------------------------- whole query */
 typedef struct pump_problem {
   int N;              /* samples (the reference's compile-time NUM) */

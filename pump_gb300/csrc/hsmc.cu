@@ -164,81 +164,143 @@ __global__ void __launch_bounds__(256) particle_table_kernel(uint32_t k0, uint32
 }
 
 // ------------------------------------------------------------------ HSMC
-// Block = one new path; blockDim multiple of 32, threads loop over
-// particles in strides of blockDim.
+// One warp per new path.  Lane l owns particles p = 32k + l (k < words), one
+// bit per particle in bits[k/32] bit (k%32), so offset loads of a k-step are
+// 32 consecutive particles (384 contiguous bytes) and word k of the packed
+// mask is a single __ballot_sync.  The warp first loads the edge's W x H
+// half-space b values (the reference skips a half-space when b >= 1000,
+// PUMP.cu:642) and ballots which are active; with none active the new mask
+// is the parent's and only the hit count is computed.  Every active
+// half-space is tested for every particle exactly as PUMP.cu:645-651 does
+// (binary32, no contraction); AND-ing the tests in another order gives the
+// same bits.
+constexpr int kMaxHsmcWords = 128;   // P <= 4096 particles
+constexpr int kMaxHsSlots = 256;     // W * maxHS <= 256
+
 __global__ void __launch_bounds__(256) hsmc_kernel(
-    int W, const int *__restrict__ wf_edge, const int *__restrict__ wf_prev, long long num_edges,
-    int num_prev, const float *__restrict__ as, const float *__restrict__ bs, int maxHS,
-    const float *__restrict__ times, const float *__restrict__ topts, float dt,
+    int num_new, int W, const int *__restrict__ wf_edge, const int *__restrict__ wf_prev,
+    long long num_edges, int num_prev, const float *__restrict__ as, const float *__restrict__ bs,
+    int maxHS, const float *__restrict__ times, const float *__restrict__ topts, float dt,
     const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
     const uint32_t *valid_in, uint32_t *valid_out, int P, float *__restrict__ cp_out,
     int *__restrict__ error) {
   // valid_in[prev] is read, valid_out[w] / cp_out[w] written (the two may
   // alias one path store with valid_out = store + base, as in the reference)
-  __shared__ int s_hits[8];
-  const int w = blockIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  if (w >= num_new) return;  // warp-uniform
   const int edge = wf_edge[w], prev = wf_prev[w];
-  if (edge < 0 || edge >= num_edges || prev < 0 || prev >= num_prev) {  // block-uniform
-    if (threadIdx.x == 0 && error) atomicExch(error, (int)PUMP_ERR_BAD_INPUT);
+  if (edge < 0 || edge >= num_edges || prev < 0 || prev >= num_prev) {
+    if (lane == 0 && error) atomicExch(error, (int)PUMP_ERR_BAD_INPUT);
     return;
   }
   const int words = (P + 31) >> 5;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const float dtLocal = topts[edge] / (W - 1);
-  const float t0 = times[prev];
-  const long long hsHead = (long long)edge * W * maxHS;
-  int hits = 0;
-  bool overflow = false;
-  for (int pbase = 0; pbase < P; pbase += blockDim.x) {
-    const int p = pbase + threadIdx.x;
-    const bool live = p < P;
-    bool vp = false;
-    if (live) vp = (valid_in[(long long)prev * words + (p >> 5)] >> (p & 31)) & 1u;
-    for (int i = 0; i < W; ++i) {
-      const float time = t0 + i * dtLocal;
-      int dtIdx = (int)(time / dt);
-      const long long h0 = hsHead + (long long)i * maxHS;
-      bool row_loaded = false;
-      float ox = 0.f, oy = 0.f, oz = 0.f;
-      for (int o = 0; o < maxHS; ++o) {
-        const float b = __ldg(&bs[h0 + o]);
-        if (b >= 1000) continue;  // block-uniform
-        if (!row_loaded) {
-          if (dtIdx < 0 || dtIdx >= T_rows) {
-            overflow = true;
-            dtIdx = dtIdx < 0 ? 0 : T_rows - 1;
-          }
-          if (live) {
-            const float *off = offsets_t + ((long long)dtIdx * Pmc + p) * 3;
-            ox = __ldg(&off[0]);
-            oy = __ldg(&off[1]);
-            oz = __ldg(&off[2]);
-          }
-          row_loaded = true;
-        }
-        const float *a = &as[(h0 + o) * 3];
-        float LHS = 0;
-        LHS += ox * __ldg(&a[0]);
-        LHS += oy * __ldg(&a[1]);
-        LHS += oz * __ldg(&a[2]);
-        vp = vp & (LHS * offset_mult < b);
+  const int slots = W * maxHS;
+  const long long hsHead = (long long)edge * slots;
+  // which half-space slots are active (b < 1000 or NaN, as !(b >= 1000))
+  uint32_t act[kMaxHsSlots / 32];
+  int nact = 0;
+#pragma unroll
+  for (int c = 0; c < kMaxHsSlots / 32; ++c) {
+    const int sidx = c * 32 + lane;
+    bool a = false;
+    if (c * 32 < slots && sidx < slots) a = !(__ldg(&bs[hsHead + sidx]) >= 1000);
+    act[c] = (c * 32 < slots) ? __ballot_sync(0xffffffffu, a) : 0u;
+    nact += __popc(act[c]);
+  }
+  // parent's words: lane j holds words j, j+32, ...
+  uint32_t mine[kMaxHsmcWords / 32];
+#pragma unroll
+  for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+    const int j = q * 32 + lane;
+    mine[q] = (j < words) ? valid_in[(long long)prev * words + j] : 0u;
+  }
+  int overflow = 0;
+  if (nact > 0) {
+    // unpack: bits[q] bit b = particle 32 * (32 q + b) + lane
+    uint32_t bits[kMaxHsmcWords / 32];
+#pragma unroll
+    for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+      bits[q] = 0u;
+      for (int b = 0; b < 32; ++b) {
+        const int k = q * 32 + b;
+        if (k >= words) break;
+        const uint32_t wk = __shfl_sync(0xffffffffu, mine[q], b);
+        bits[q] |= ((wk >> lane) & 1u) << b;
       }
     }
-    const unsigned int bal = __ballot_sync(0xffffffffu, vp && live);
-    if (lane == 0 && (pbase >> 5) + warp < words) valid_out[(long long)w * words + (pbase >> 5) + warp] = bal;
-    hits += live && !vp;
-  }
-  // block reduction of the hit count
+    const float dtLocal = topts[edge] / (W - 1);
+    const float t0 = times[prev];
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) hits += __shfl_down_sync(0xffffffffu, hits, off);
-  if (lane == 0) s_hits[warp] = hits;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int total = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) total += s_hits[k];
-    cp_out[w] = ((float)total) / P;
+    for (int c = 0; c < kMaxHsSlots / 32; ++c) {
+      uint32_t m = act[c];
+      while (m) {
+        const int sidx = c * 32 + __ffs(m) - 1;
+        m &= m - 1;
+        const int i = sidx / maxHS;
+        const float time = t0 + i * dtLocal;
+        int dtIdx = (int)(time / dt);
+        if (dtIdx < 0 || dtIdx >= T_rows) {
+          overflow = 1;
+          dtIdx = dtIdx < 0 ? 0 : T_rows - 1;
+        }
+        const float b = __ldg(&bs[hsHead + sidx]);
+        const float a0 = __ldg(&as[(hsHead + sidx) * 3 + 0]);
+        const float a1 = __ldg(&as[(hsHead + sidx) * 3 + 1]);
+        const float a2 = __ldg(&as[(hsHead + sidx) * 3 + 2]);
+        const float *row = offsets_t + (long long)dtIdx * Pmc * 3;
+#pragma unroll
+        for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+          if (q * 32 >= words) break;
+          uint32_t bq = bits[q];
+          for (int bb = 0; bb < 32; ++bb) {
+            const int k = q * 32 + bb;
+            if (k >= words) break;
+            const int p = 32 * k + lane;
+            if (p < P && ((bq >> bb) & 1u)) {
+              const float *off = row + (long long)p * 3;
+              float LHS = 0;
+              LHS += __ldg(&off[0]) * a0;
+              LHS += __ldg(&off[1]) * a1;
+              LHS += __ldg(&off[2]) * a2;
+              if (!(LHS * offset_mult < b)) bq &= ~(1u << bb);
+            }
+          }
+          bits[q] = bq;
+        }
+      }
+    }
+    // repack: word k = ballot of bit k over lanes; lane (k & 31) keeps it
+#pragma unroll
+    for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+      uint32_t keep = 0u;
+      for (int b = 0; b < 32; ++b) {
+        const int k = q * 32 + b;
+        if (k >= words) break;
+        const bool live = 32 * k + lane < P;
+        const uint32_t wk = __ballot_sync(0xffffffffu, live && ((bits[q] >> b) & 1u));
+        if (b == lane) keep = wk;
+      }
+      mine[q] = keep;
+    }
   }
-  if (overflow && error && lane == 0) atomicExch(error, (int)PUMP_ERR_CAPACITY);
+  int valid_count = 0;
+  const uint32_t tail = (P & 31) ? ((1u << (P & 31)) - 1u) : 0xffffffffu;
+#pragma unroll
+  for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+    const int j = q * 32 + lane;
+    if (j < words) {
+      if (j == words - 1) mine[q] &= tail;  // no bits past particle P-1
+      valid_out[(long long)w * words + j] = mine[q];
+      valid_count += __popc(mine[q]);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) valid_count += __shfl_down_sync(0xffffffffu, valid_count, off);
+  if (lane == 0) {
+    cp_out[w] = ((float)(P - valid_count)) / P;
+    if (overflow && error) atomicExch(error, (int)PUMP_ERR_CAPACITY);
+  }
 }
 
 // -------------------------------------------------------------- MC CP
@@ -335,11 +397,13 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
                                 const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
                                 float *d_cp_out, int *d_error, cudaStream_t stream) {
   if (num_new <= 0) return PUMP_OK;
-  if (num_new > 2147483647) return set_error(PUMP_ERR_CAPACITY, "hsmc: wavefront too large");
-  int threads = ((P + 31) / 32) * 32;
-  if (threads > 256) threads = 256;
-  hsmc_kernel<<<num_new, threads, 0, stream>>>(W, d_edge, d_prev, num_edges, num_prev, d_as, d_bs,
-                                               maxHS, d_times, d_topt,
+  if ((P + 31) / 32 > kMaxHsmcWords)
+    return set_error(PUMP_ERR_CAPACITY, "hsmc: %d particles exceed %d", P, 32 * kMaxHsmcWords);
+  if (W * maxHS > kMaxHsSlots)
+    return set_error(PUMP_ERR_CAPACITY, "hsmc: %d half-space slots per edge exceed %d", W * maxHS,
+                     kMaxHsSlots);
+  hsmc_kernel<<<grid_for((long long)num_new * 32, 256), 256, 0, stream>>>(
+      num_new, W, d_edge, d_prev, num_edges, num_prev, d_as, d_bs, maxHS, d_times, d_topt,
                                                dt, d_offsets_t, Pmc, T_rows, offset_mult,
                                                d_valid_in, d_valid_out, P, d_cp_out, d_error);
   return launch_status("hsmc_kernel");
