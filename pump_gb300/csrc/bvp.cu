@@ -15,10 +15,10 @@
 //   A0 = 12|p1-p0|^2, A1 = -12 (p1-p0).(v0+v1), A2 = 4(|v0|^2+v0.v1+|v1|^2),
 //   A3 = 2g(v0z-v1z), A4 = 1+g^2,
 // so c'(t) = 0 is the quartic Q(t) = A4 t^4 - A2 t^2 - 2 A1 t - 3 A0 = 0.
-// The kernel splits (0, tmax] at the real critical points of Q (Q'' = 0 at
-// sqrt(A2 / 6 A4)), finds every upward sign change of Q by safeguarded
-// Newton in binary64, and returns the candidate (those roots, and tmax when
-// Q(tmax) < 0) with the smallest cost.
+// The kernel brackets the roots of Q in binary32 (pieces split at the
+// inflection point and the real roots of Q'), refines each candidate minimum
+// with one binary64 Newton step and compares candidates (and tmax) by their
+// binary64 cost.
 #include <math.h>
 
 #include "common.cuh"
@@ -153,7 +153,7 @@ struct Quartic {
 
 // The same polynomials in binary32 for the bracketing phase.
 struct QuarticF {
-  float A0, A1, A2, A4;
+  float A0, A1, A2, A4;  // binary32 copies for the bracketing phase
   __device__ float Q(float t) const { return ((A4 * t * t - A2) * t - 2.0f * A1) * t - 3.0f * A0; }
   __device__ float dQ(float t) const { return (4.0f * A4 * t * t - 2.0f * A2) * t - 2.0f * A1; }
   __device__ float d2Q(float t) const { return 12.0f * A4 * t * t - 2.0f * A2; }
@@ -177,84 +177,88 @@ __device__ __forceinline__ Quartic make_quartic(const float *x0, const float *x1
 
 // Root of a monotone function on [a, b] (sign change given) with fixed
 // convexity: Newton started at the end where the function and its curvature
-// have the same sign converges monotonically.  Binary32, explicit fma.
+// have the same sign converges monotonically.  Binary32.
 template <int Deriv>
 __device__ float newton_f(const QuarticF &q, float a, float b, bool from_b) {
   float x = from_b ? b : a;
-  for (int it = 0; it < 60; ++it) {
+  for (int it = 0; it < 40; ++it) {
     const float f = Deriv ? q.dQ(x) : q.Q(x);
     const float df = Deriv ? q.d2Q(x) : q.dQ(x);
     if (f == 0.0f || df == 0.0f) break;
     float xn = x - f / df;
     if (!(xn >= a && xn <= b)) xn = 0.5f * (a + b);
-    if (fabsf(xn - x) <= 1e-6f * fabsf(xn)) { x = xn; break; }
+    if (fabsf(xn - x) <= 2e-7f * fabsf(xn)) { x = xn; break; }
     x = xn;
   }
   return x;
 }
 
-// Binary64 Newton polish of a root of Q bracketed by [a, b] (Q(a) < 0 < Q(b)).
-__device__ double polish(const Quartic &q, double x, double a, double b) {
-  for (int it = 0; it < 6; ++it) {
-    const double f = q.Q(x);
-    if (f == 0.0) return x;
-    if (f < 0.0) a = x; else b = x;
-    double xn = x - f / q.dQ(x);
-    if (!(xn >= a && xn <= b)) xn = 0.5 * (a + b);
-    if (fabs(xn - x) <= 4.5e-16 * fabs(xn)) return xn;
-    x = xn;
-  }
-  return x;
-}
-
-// Global minimiser of the cost on (0, tmax].  (0, tmax] is split at the
-// inflection point tc of Q (Q'' = 0) and at the real roots of Q', so that on
-// every piece Q is monotone with fixed convexity; each upward sign change of
-// Q is a local minimum of the cost.
-__device__ double precise_topt(const Quartic &q, double tmax) {
-  QuarticF qf;
-  qf.A0 = (float)q.A0; qf.A1 = (float)q.A1; qf.A2 = (float)q.A2; qf.A4 = (float)q.A4;
-  const float tmf = (float)tmax;
-  double bp[5];
+// Binary32 analysis of the stationarity quartic: the local minima of the cost
+// inside (0, tmax) (at most two) and whether the cost still decreases at
+// tmax.  (0, tmax] is split at the inflection point tc of Q (Q'' = 0) and at
+// the real roots of Q', so on every piece Q is monotone with fixed convexity
+// and each upward sign change of Q is found by monotone Newton.
+__device__ int minima_f32(const QuarticF &q, float tmax, float cand[2], bool *tmax_cand) {
+  float bp[5];
   int nb = 0;
-  bp[nb++] = 0.0;
-  const double tc = sqrt(q.A2 / (6.0 * q.A4));
-  const double d0 = -2.0 * q.A1;  // Q'(0)
-  if (tc > 0.0 && tc < tmax) {
-    const double dc = q.dQ(tc);
-    if (d0 > 0.0 && dc < 0.0)  // Q' decreasing and concave-down on (0, tc): Newton from 0
-      bp[nb++] = (double)newton_f<1>(qf, 0.0f, (float)tc, false);
+  bp[nb++] = 0.0f;
+  const float tc = sqrtf(q.A2 / (6.0f * q.A4));
+  const float d0 = -2.0f * q.A1;  // Q'(0)
+  if (tc > 0.0f && tc < tmax) {
+    const float dc = q.dQ(tc);
+    if (d0 > 0.0f && dc < 0.0f) bp[nb++] = newton_f<1>(q, 0.0f, tc, false);
     bp[nb++] = tc;
-    if (dc < 0.0 && q.dQ(tmax) > 0.0)  // Q' increasing, convex on (tc, tmax): Newton from tmax
-      bp[nb++] = (double)newton_f<1>(qf, (float)tc, tmf, true);
-  } else if (tc <= 0.0) {
-    if (d0 < 0.0 && q.dQ(tmax) > 0.0) bp[nb++] = (double)newton_f<1>(qf, 0.0f, tmf, true);
-  } else if (d0 > 0.0 && q.dQ(tmax) < 0.0) {
-    bp[nb++] = (double)newton_f<1>(qf, 0.0f, tmf, false);
+    if (dc < 0.0f && q.dQ(tmax) > 0.0f) bp[nb++] = newton_f<1>(q, tc, tmax, true);
+  } else if (tc <= 0.0f) {
+    if (d0 < 0.0f && q.dQ(tmax) > 0.0f) bp[nb++] = newton_f<1>(q, 0.0f, tmax, true);
+  } else if (d0 > 0.0f && q.dQ(tmax) < 0.0f) {
+    bp[nb++] = newton_f<1>(q, 0.0f, tmax, false);
   }
   bp[nb++] = tmax;
-  double best_t = tmax, best_c = 0.0;
-  bool have = false;
-  double qa = q.Q(0.0);
+  int nc = 0;
+  float qa = -3.0f * q.A0;  // Q(0)
   for (int k = 0; k + 1 < nb; ++k) {
-    const double a = bp[k], b = bp[k + 1];
-    const double qb = q.Q(b);
-    if (qa < 0.0 && qb > 0.0) {
-      // convex piece (a >= tc): start from b; concave piece: start from a
-      const float xf = newton_f<0>(qf, (float)a, (float)b, a >= tc);
-      double x = (double)xf;
-      if (!(x > a && x < b)) x = 0.5 * (a + b);
-      const double r = polish(q, x, a, b);
-      const double cr = q.cost(r);
-      if (!have || cr < best_c) { best_c = cr; best_t = r; have = true; }
-    }
+    const float a = bp[k], b = bp[k + 1];
+    const float qb = q.Q(b);
+    if (qa < 0.0f && qb > 0.0f && nc < 2) cand[nc++] = newton_f<0>(q, a, b, a >= tc);
     qa = qb;
   }
-  if (qa < 0.0) {  // cost still decreasing at tmax
-    const double cm = q.cost(tmax);
-    if (!have || cm < best_c) { best_c = cm; best_t = tmax; have = true; }
+  *tmax_cand = qa < 0.0f;
+  return nc;
+}
+
+// Global minimiser of the cost on (0, tmax]: candidates from the binary32
+// analysis, each refined by one binary64 Newton step on Q (quadratic
+// convergence takes a ~1e-6 relative root to ~1e-12) and compared by their
+// binary64 cost.  In the common case of one candidate the binary64 work is the
+// same straight-line sequence for every pair, so the FP64 pipe runs with full
+// warps.
+__device__ void precise_pair(const float *x0, const float *x1, float tmax, float *topt,
+                             float *cost) {
+  const Quartic q = make_quartic(x0, x1);
+  QuarticF qf;
+  qf.A0 = (float)q.A0; qf.A1 = (float)q.A1; qf.A2 = (float)q.A2; qf.A4 = (float)q.A4;
+  float cand[2];
+  bool tmax_cand = false;
+  const int nc = minima_f32(qf, tmax, cand, &tmax_cand);
+  double best_t = (double)tmax, best_c = 0.0;
+  bool have = false;
+  for (int k = 0; k < nc; ++k) {
+    double x = (double)cand[k];
+    const double f = q.Q(x), df = q.dQ(x);
+    if (df != 0.0) {
+      const double xn = x - f / df;
+      if (fabs(xn - x) <= 1e-3 * x && xn > 0.0 && xn <= (double)tmax) x = xn;
+    }
+    const double c = q.cost(x);
+    if (!have || c < best_c) { best_c = c; best_t = x; have = true; }
   }
-  return best_t;
+  if (tmax_cand || !have) {
+    const double c = q.cost((double)tmax);
+    if (!have || c < best_c) { best_c = c; best_t = (double)tmax; }
+  }
+  *topt = (float)best_t;
+  *cost = (float)best_c;
 }
 
 // --------------------------------------------------------------- kernels
@@ -281,6 +285,88 @@ __global__ void __launch_bounds__(128) bvp_pairs_parity_kernel(const float *__re
   }
 }
 
+// Persistent parity kernel.  The reference's bisection runs a different
+// number of steps per pair (tmax test, halving loop, up to 50 bisection
+// steps, then the final cost), so one thread per pair leaves most lanes of a
+// warp idle while the slowest pair finishes.  Here every lane runs a small
+// state machine over the same sequence of evaluations toptBisection performs
+// for its pair, and each warp iteration evaluates exactly two costs in every
+// lane (the two sides of dcost, or the final cost and a spare).  A lane whose
+// pair is done stores it and takes the next pair of the warp's chunk of
+// kParityChunk consecutive pairs (16 per lane on average, so lanes idle only
+// while a chunk's last pairs finish).  Per pair, the evaluated expressions and
+// their order are unchanged.
+constexpr int kParityChunk = 512;
+
+__global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
+    const float *__restrict__ samples, int N, float tmax, float *__restrict__ copts,
+    float *__restrict__ topts) {
+  const long long npairs = (long long)N * (N - 1);
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const float h = (float)0.000001 / 2;  // dtau / 2 of dcost
+  const float dtau = (float)0.000001;
+  const long long warp_id = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  long long chunk_next = warp_id * kParityChunk;
+  const long long chunk_end = chunk_next + kParityChunk < npairs ? chunk_next + kParityChunk : npairs;
+  // lane state
+  long long idx = -1;
+  int phase = 0, halvings = 0, itr = 0;
+  float tu = 0, tl = 0, topt = 0, dcval = 0;
+  PairCoef c{};
+  while (true) {
+    // lanes without a pair take the next pairs of the warp's chunk
+    const unsigned need = __ballot_sync(0xffffffffu, idx < 0);
+    if (need && chunk_next < chunk_end) {
+      const int avail = (int)(chunk_end - chunk_next);
+      const int rank = __popc(need & lt);
+      const bool mine = (need >> lane) & 1u;
+      if (mine && rank < avail) {
+        idx = chunk_next + rank;
+        const int i = (int)(idx / (N - 1));
+        const int r = (int)(idx - (long long)i * (N - 1));
+        const int j = r + (r >= i);
+        float x0[kDim], x1[kDim];
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) {
+          x0[d] = __ldg(&samples[i * kDim + d]);
+          x1[d] = __ldg(&samples[j * kDim + d]);
+        }
+        c = make_coef(x0, x1);
+        phase = 0;
+        tu = tmax;
+      }
+      chunk_next += __popc(need) < avail ? __popc(need) : avail;
+    }
+    if (__ballot_sync(0xffffffffu, idx >= 0) == 0u) break;  // nothing left
+    // the two evaluation points of this step
+    float ta, tb;
+    if (phase == 0) { ta = tmax + h; tb = tmax - h; }
+    else if (phase == 1) { ta = tl + h; tb = tl - h; }
+    else if (phase == 2) { ++itr; topt = (tu + tl) / 2; ta = topt + h; tb = topt - h; }
+    else { ta = topt; tb = topt; }
+    const float ca = cost_eval(c, ta);
+    const float cb = cost_eval(c, tb);
+    if (idx < 0) continue;
+    const float d = (ca - cb) / dtau;
+    if (phase == 0) {
+      if (d < 0) { topt = tmax; phase = 3; }
+      else { tl = (float)0.01; halvings = 0; phase = 1; }
+    } else if (phase == 1) {
+      if (d > 0 && halvings < 160) { tl = tl / 2; ++halvings; }
+      else { topt = 0; dcval = 1; itr = 0; phase = 2; }
+    } else if (phase == 2) {
+      dcval = d;
+      if (dcval > 0) tu = topt; else tl = topt;
+      if (!((double)fabsf(dcval) > 0.0001 && itr < 50)) phase = 3;
+    } else {
+      topts[idx] = topt;
+      copts[idx] = ca;
+      idx = -1;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128) bvp_pairs_precision_kernel(const float *__restrict__ samples,
                                                                   int N, float tmax,
                                                                   float *__restrict__ copts,
@@ -297,10 +383,10 @@ __global__ void __launch_bounds__(128) bvp_pairs_precision_kernel(const float *_
       x0[d] = __ldg(&samples[i * kDim + d]);
       x1[d] = __ldg(&samples[j * kDim + d]);
     }
-    const Quartic q = make_quartic(x0, x1);
-    const double t = precise_topt(q, (double)tmax);
-    topts[idx] = (float)t;
-    copts[idx] = (float)q.cost(t);
+    float tp, cp;
+    precise_pair(x0, x1, tmax, &tp, &cp);
+    topts[idx] = tp;
+    copts[idx] = cp;
   }
 }
 
@@ -321,10 +407,10 @@ __global__ void bvp_batch_kernel(const float *__restrict__ x0s, const float *__r
     if (topt) topt[k] = tp;
     if (cost) cost[k] = cost_eval(c, tp);
   } else {
-    const Quartic q = make_quartic(x0, x1);
-    const double t = precise_topt(q, (double)tmax);
-    if (topt) topt[k] = (float)t;
-    if (cost) cost[k] = (float)q.cost(t);
+    float tp, cp;
+    precise_pair(x0, x1, tmax, &tp, &cp);
+    if (topt) topt[k] = tp;
+    if (cost) cost[k] = cp;
   }
 }
 
@@ -458,10 +544,12 @@ extern "C" pump_status_t pump_bvp_pairs(const float *d_samples, int N, float tma
   const int threads = 128;
   long long blocks = (npairs + threads - 1) / threads;
   if (blocks > 2147483647LL) blocks = 2147483647LL;
-  if (mode == PUMP_BVP_PARITY)
-    bvp_pairs_parity_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(
+  if (mode == PUMP_BVP_PARITY) {
+    const long long nblk = (npairs + 4LL * kParityChunk - 1) / (4LL * kParityChunk);  // 4 warps
+    if (nblk > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "pump_bvp_pairs: N=%d", N);
+    bvp_pairs_parity_persistent<<<(unsigned)nblk, 128, 0, (cudaStream_t)stream>>>(
         d_samples, N, tmax, d_copts, d_topts);
-  else if (mode == PUMP_BVP_PRECISION)
+  } else if (mode == PUMP_BVP_PRECISION)
     bvp_pairs_precision_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(
         d_samples, N, tmax, d_copts, d_topts);
   else
