@@ -17,6 +17,8 @@
 // leaves, and the host reports PUMP_ERR_TIMEOUT.
 #include <cuda/atomic>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "ctx.h"
 
@@ -394,5 +396,94 @@ extern "C" pump_status_t pump_frontier_compact(pump_ctx *ctx, const uint8_t *d_f
   PUMP_CUDA_TRY(cudaMemcpyAsync(&err, d_err, sizeof err, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
   PUMP_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
   if (err) return set_error(PUMP_ERR_TIMEOUT, "pump_frontier_compact: look-back wait exceeded its bound");
+  return PUMP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Frontier compaction without any allocation.
+//
+// For callers that must not allocate device memory while they plan: a
+// real-time control loop that reserves all of its memory at start-up so that
+// no planning step can block in (or fail inside) the allocator, or a host
+// framework that owns the device memory budget through its own pool and does
+// not let plugins call cudaMalloc.  pump_frontier_compact takes its look-back
+// scratch from the context's grow-only buffers, which may call cudaMalloc on
+// first use or when N grows; this variant keeps that scratch in one
+// fixed-size array in device memory instead.
+//
+// The array is a file-scope __device__ variable: every GPU that loads the
+// library holds its 64 KiB until the process exits, and every call on that
+// GPU uses the same array.  Host code cannot use the variable's name as a
+// device address, so the address is looked up once per device with
+// cudaGetSymbolAddress (with that device current) on the first call made on
+// it; make that first call before any stream capture.  Each call clears the
+// words that must start at zero before its kernel runs; two calls that
+// overlap on the GPU (for example on two streams) share the array and race,
+// so serialise them.
+namespace pump {
+namespace {
+
+constexpr long long kNoAllocMaxTiles = 8192;                   // 8192 tiles of 4096 flags
+constexpr long long kNoAllocMaxFlags = kNoAllocMaxTiles * kTile;  // 33,554,432
+// word 0: selected count; words 1 .. tiles: tile status; the word after the
+// last status slot: tile counter (4 B) and error word (4 B)
+constexpr int kNoAllocWords = 1 + (int)kNoAllocMaxTiles + 1 + 1;
+
+static __device__ __align__(256) unsigned long long g_frontier_scratch[kNoAllocWords];
+
+std::mutex g_scratch_mutex;
+unsigned long long *g_scratch_addr[64] = {nullptr};
+
+pump_status_t frontier_scratch_address(unsigned long long **out) {
+  int dev = 0;
+  PUMP_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(PUMP_ERR_BAD_INPUT, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_frontier_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_frontier_scratch)");
+    g_scratch_addr[dev] = static_cast<unsigned long long *>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return PUMP_OK;
+}
+
+}  // namespace
+}  // namespace pump
+
+extern "C" pump_status_t pump_frontier_compact_noalloc(const uint8_t *d_flags, int N, int *d_active,
+                                                       int *d_count, pump_stream_t stream) {
+  if (N < 0 || (N > 0 && (!d_flags || !d_active)) || !d_count)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_frontier_compact_noalloc: bad arguments");
+  if ((long long)N > kNoAllocMaxFlags)
+    return set_error(PUMP_ERR_CAPACITY,
+                     "pump_frontier_compact_noalloc: N=%d exceeds the %lld flags its fixed "
+                     "scratch array covers; use pump_frontier_compact",
+                     N, kNoAllocMaxFlags);
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long *scratch = nullptr;
+  PUMP_TRY(frontier_scratch_address(&scratch));
+  const long long ntiles = N > 0 ? ((long long)N + kTile - 1) / kTile : 1;
+  TileScratch ts{};
+  ts.total = scratch;
+  ts.status = scratch + 1;
+  ts.tile_counter = reinterpret_cast<unsigned int *>(scratch + 2 + kNoAllocMaxTiles);
+  ts.error = reinterpret_cast<int *>(ts.tile_counter + 1);
+  // everything the look-back reads before writing starts at zero
+  PUMP_CUDA_TRY(cudaMemsetAsync(ts.total, 0, sizeof(unsigned long long) * (ntiles + 2), s));
+  PUMP_CUDA_TRY(cudaMemsetAsync(ts.tile_counter, 0, 2 * sizeof(unsigned int), s));
+  if (N > 0) {
+    compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, s>>>((long long)N, FlagPred{d_flags},
+                                                                IndexEmit{d_active}, ts);
+    PUMP_TRY(launch_status("compact_kernel (no-alloc)"));
+  }
+  copy_count_kernel<<<1, 1, 0, s>>>(ts.total, d_count);
+  PUMP_TRY(launch_status("copy_count_kernel (no-alloc)"));
+  int err = 0;
+  PUMP_CUDA_TRY(cudaMemcpyAsync(&err, ts.error, sizeof err, cudaMemcpyDeviceToHost, s));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(s));
+  if (err)
+    return set_error(PUMP_ERR_TIMEOUT, "pump_frontier_compact_noalloc: look-back wait exceeded its bound");
   return PUMP_OK;
 }
