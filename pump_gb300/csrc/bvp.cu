@@ -145,12 +145,18 @@ struct Quartic {
   double A0, A1, A2, A3, A4;
   __device__ double Q(double t) const { return ((A4 * t * t - A2) * t - 2.0 * A1) * t - 3.0 * A0; }
   __device__ double dQ(double t) const { return (4.0 * A4 * t * t - 2.0 * A2) * t - 2.0 * A1; }
-  // 1/t from the binary32 reciprocal refined by one binary64 Newton step
-  // (relative error ~1e-14, far below the float the cost is rounded to)
+  // 1/t from the hardware reciprocal estimate (rel. error < 2^-20) refined
+  // by two binary64 Newton steps (~1e-16, below the float the cost becomes)
   __device__ double cost(double t) const {
-    const double y = (double)__frcp_rn((float)t);
-    const double r = fma(y, fma(-t, y, 1.0), y);
+    const double y0 = rcp_approx(t);
+    const double y1 = fma(y0, fma(-t, y0, 1.0), y0);
+    const double r = fma(y1, fma(-t, y1, 1.0), y1);
     return (((A0 * r + A1) * r + A2) * r + A3) + A4 * t;
+  }
+  __device__ static double rcp_approx(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
   }
 };
 
@@ -236,31 +242,50 @@ __device__ int minima_f32(const QuarticF &q, float tmax, float cand[2], bool *tm
 // binary64 cost.  In the common case of one candidate the binary64 work is the
 // same straight-line sequence for every pair, so the FP64 pipe runs with full
 // warps.
+__device__ __forceinline__ QuarticF make_quartic_f32(const float *x0, const float *x1) {
+  const float g = PUMP_G;
+  const float dx = x1[0] - x0[0], dy = x1[1] - x0[1], dz = x1[2] - x0[2];
+  const float sx = x0[3] + x1[3], sy = x0[4] + x1[4], sz = x0[5] + x1[5];
+  QuarticF q;
+  q.A0 = 12.0f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  q.A1 = -12.0f * fmaf(dx, sx, fmaf(dy, sy, dz * sz));
+  q.A2 = 4.0f * (fmaf(x0[3], x0[3] + x1[3], fmaf(x0[4], x0[4] + x1[4], x0[5] * (x0[5] + x1[5]))) +
+                 fmaf(x1[3], x1[3], fmaf(x1[4], x1[4], x1[5] * x1[5])));
+  q.A4 = fmaf(g, g, 1.0f);
+  return q;
+}
+
+// One binary64 Newton step on Q from a binary32 root estimate (the
+// correction is ~1e-6 of x, so the 2^-20 reciprocal estimate of Q' leaves
+// ~1e-12 relative error).
+__device__ __forceinline__ double refine(const Quartic &q, double x) {
+  const double f = q.Q(x), df = q.dQ(x);
+  const double xn = fma(-f, Quartic::rcp_approx(df), x);
+  return fabs(xn - x) <= 1e-3 * x ? xn : x;  // keep the estimate if Q' is tiny
+}
+
 __device__ void precise_pair(const float *x0, const float *x1, float tmax, float *topt,
                              float *cost) {
-  const Quartic q = make_quartic(x0, x1);
-  QuarticF qf;
-  qf.A0 = (float)q.A0; qf.A1 = (float)q.A1; qf.A2 = (float)q.A2; qf.A4 = (float)q.A4;
+  const QuarticF qf = make_quartic_f32(x0, x1);
   float cand[2];
   bool tmax_cand = false;
   const int nc = minima_f32(qf, tmax, cand, &tmax_cand);
-  double best_t = (double)tmax, best_c = 0.0;
-  bool have = false;
-  for (int k = 0; k < nc; ++k) {
-    double x = (double)cand[k];
-    const double f = q.Q(x), df = q.dQ(x);
-    if (df != 0.0) {
-      // the correction f/df is ~1e-6 of x, so a binary32 reciprocal of df
-      // (~1e-7 relative) leaves ~1e-13 relative error in x
-      const double xn = x - f * (double)__frcp_rn((float)df);
-      if (fabs(xn - x) <= 1e-3 * x && xn > 0.0 && xn <= (double)tmax) x = xn;
-    }
-    const double c = q.cost(x);
-    if (!have || c < best_c) { best_c = c; best_t = x; have = true; }
+  const Quartic q = make_quartic(x0, x1);
+  // primary candidate, evaluated by every lane with the same instructions
+  const bool primary_root = nc > 0;
+  const double tm = (double)tmax;
+  const double xr = refine(q, (double)(primary_root ? cand[0] : tmax));
+  double best_t = primary_root ? xr : tm;
+  double best_c = q.cost(best_t);
+  // rare: a second interior minimum, or the cost still falling at tmax
+  if (nc > 1) {
+    const double t2 = refine(q, (double)cand[1]);
+    const double c2 = q.cost(t2);
+    if (c2 < best_c) { best_c = c2; best_t = t2; }
   }
-  if (tmax_cand || !have) {
-    const double c = q.cost((double)tmax);
-    if (!have || c < best_c) { best_c = c; best_t = (double)tmax; }
+  if (primary_root && tmax_cand) {
+    const double c3 = q.cost((double)tmax);
+    if (c3 < best_c) { best_c = c3; best_t = (double)tmax; }
   }
   *topt = (float)best_t;
   *cost = (float)best_c;
