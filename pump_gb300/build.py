@@ -24,6 +24,8 @@ LIB = os.path.join(OUT, "libpump.so")
 CLI = os.path.join(OUT, "pump")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# translation units not bound to the reference's roundings: contraction on
+FMAD_TRUE = {os.path.join(CSRC, "bvp_precise.cu")}
 HOST_FLAGS = "-fPIC,-ffp-contract=off,-fno-fast-math,-Wall,-Wno-unused-function"
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", HOST_FLAGS,
           "-I", INCLUDE, "-I", CSRC]
@@ -70,6 +72,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         objs.append(obj)
         if ptxas_info or _stale(obj, [src] + headers + [__file__]):
             cmd = [nv, "-c", src, "-o", obj] + ARCH + COMMON
+            if src in FMAD_TRUE:
+                cmd = [c if c != "-fmad=false" else "-fmad=true" for c in cmd]
             if ptxas_info and src.endswith(".cu"):
                 cmd += ["-Xptxas", "-v"]
             if src.endswith(".cpp"):

@@ -53,6 +53,10 @@ pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, i
                                       int *d_count, int **d_error_out, cudaStream_t stream);
 pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
                                     cudaStream_t stream);
+pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tmax, float *d_copts,
+                                         float *d_topts, cudaStream_t stream);
+pump_status_t bvp_batch_precision_launch(const float *d_x0, const float *d_x1, int n, float tmax,
+                                         float *d_topt, float *d_cost, cudaStream_t stream);
 pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
                               const float *d_tau, int total, float *d_out, cudaStream_t stream);
 
