@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--mode", default="precision", choices=["precision", "parity"])
     ap.add_argument("--particles", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=256, help="queries of the batched workload (0: skip)")
+    ap.add_argument("--workers", type=int, default=0, help="batched-mode workers (0: host cores)")
     return ap.parse_args()
 
 
@@ -155,6 +157,65 @@ def cpu_query(args, query=0):
 
 
 # ------------------------------------------------------------------ ours
+def measure_queries(args, lib, L, ctx):
+    """Batched vs plain queries/s on the batched workload (256 queries, N
+    log-uniform in [500, 8000], 5-100 boxes, init/goal in free space, CP
+    target in {0.001, 0.01, 0.05}, eta in {1, 2, 4}).  Plain: one pump_plan
+    after another on one stream; batched: pump_plan_batch.  A query counts
+    only when it returns a path whose Monte Carlo CP is below its target."""
+    from pump_gb300 import workloads
+    qs = workloads.batch_queries(args.batch)
+    keep = []
+    pbs = (lib.Problem * len(qs))()
+    for k, q in enumerate(qs):
+        pb = pbs[k]
+        L.pump_problem_defaults(C.byref(pb))
+        obs = np.ascontiguousarray(q["obstacles"], np.float32)
+        keep.append(obs)
+        pb.N, pb.num_obstacles, pb.obstacles = q["N"], obs.shape[0], obs.ctypes.data
+        for d in range(6):
+            pb.init[d], pb.goal[d] = q["init"][d], q["goal"][d]
+            pb.lo[d], pb.hi[d] = workloads.LO[d], workloads.HI[d]
+        pb.offset_mult, pb.cp_target, pb.cp_factor = float(q["offset_mult"]), q["cp"], q["eta"]
+        pb.bvp_mode = 1 if args.mode == "precision" else 0
+    paths = np.zeros((len(qs), 400, 6), np.float32)
+
+    def results():
+        res = (lib.PlanResult * len(qs))()
+        for k in range(len(qs)):
+            res[k].path, res[k].path_cap = paths[k].ctypes.data, 400
+        return res
+
+    def ok(res, sts):
+        return sum(1 for k in range(len(qs)) if sts[k] == lib.PUMP_OK and res[k].success
+                   and res[k].soln_cp < pbs[k].cp_target)
+    # warm both paths once on a few queries (contexts, particle tables)
+    warm = min(4, len(qs))
+    res = results()
+    sts = (C.c_int * len(qs))()
+    for k in range(warm):
+        sts[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res[k]), None)
+    workers = args.workers or (os.cpu_count() or 4)
+    L.pump_plan_batch(0, pbs, res, sts, warm, min(workers, warm))
+    res_p, sts_p = results(), (C.c_int * len(qs))()
+    t0 = time.perf_counter()
+    for k in range(len(qs)):
+        sts_p[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res_p[k]), None)
+    t_plain = time.perf_counter() - t0
+    res_b, sts_b = results(), (C.c_int * len(qs))()
+    t0 = time.perf_counter()
+    lib.check(L.pump_plan_batch(0, pbs, res_b, sts_b, len(qs), workers))
+    t_batch = time.perf_counter() - t0
+    same = all(res_p[k].success == res_b[k].success and res_p[k].soln_path_idx == res_b[k].soln_path_idx
+               and sts_p[k] == sts_b[k] for k in range(len(qs)))
+    ok_p, ok_b = ok(res_p, sts_p), ok(res_b, sts_b)
+    return {"workload": "batch256: N log-uniform [500, 8000], 5-100 boxes, noise 1e-3",
+            "queries": len(qs), "met_cp_target": ok_b, "workers": workers,
+            "plain_queries_per_s": ok_p / t_plain, "batched_queries_per_s": ok_b / t_batch,
+            "batched_over_plain": (ok_b / t_batch) / (ok_p / t_plain) if ok_p else None,
+            "plain_s": t_plain, "batched_s": t_batch, "identical_results": bool(same)}
+
+
 def run_ours(args):
     import torch
     from pump_gb300 import lib
@@ -362,6 +423,8 @@ def run_ours(args):
         fp64 = C.c_double(0)
         lib.check(L.pump_probe_fp64_tflops(C.byref(fp64), sh))
         out["roofline"] = roofline(dom, ks, N, E, M_total, W, maxHS, P, args.mode, fp64.value)
+        if args.batch > 0:
+            out["queries_per_s"] = measure_queries(args, lib, L, ctx)
         if not args.no_cpu_baseline:
             v, _dt, det = cpu_query(args, 0)
             out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",

@@ -249,6 +249,16 @@ pump_status_t pump_read_input(const char *path, pump_problem *pb);
 pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
                         pump_stream_t stream);
 
+/* Many independent queries at once.  `workers` host threads each own a
+ * context and a non-blocking CUDA stream on `device` and take queries in
+ * order from a shared counter, so one query's kernels and copies overlap
+ * another's host-side search.  results[k] is filled as pump_plan fills it
+ * (its path/nodes buffers are the caller's) and statuses[k] receives query
+ * k's status.  Returns PUMP_OK when every query ran, whatever its own status.
+ * The reference plans one query per process run (mainPUMP.cu:82-712). */
+pump_status_t pump_plan_batch(int device, const pump_problem *problems, pump_plan_result *results,
+                              pump_status_t *statuses, int n, int workers);
+
 #ifdef __cplusplus
 }
 #endif

@@ -135,29 +135,6 @@ __device__ float topt_bisection(const PairCoef &c, float tmax) {
 }
 
 // --------------------------------------------------------------- kernels
-__global__ void __launch_bounds__(128) bvp_pairs_parity_kernel(const float *__restrict__ samples,
-                                                               int N, float tmax,
-                                                               float *__restrict__ copts,
-                                                               float *__restrict__ topts) {
-  const long long npairs = (long long)N * (N - 1);
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < npairs;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / (N - 1));
-    const int r = (int)(idx - (long long)i * (N - 1));
-    const int j = r + (r >= i);
-    float x0[kDim], x1[kDim];
-#pragma unroll
-    for (int d = 0; d < kDim; ++d) {
-      x0[d] = __ldg(&samples[i * kDim + d]);
-      x1[d] = __ldg(&samples[j * kDim + d]);
-    }
-    const PairCoef c = make_coef(x0, x1);
-    const float tp = topt_bisection(c, tmax);
-    topts[idx] = tp;
-    copts[idx] = cost_eval(c, tp);
-  }
-}
-
 // Persistent parity kernel.  The reference's bisection runs a different
 // number of steps per pair (tmax test, halving loop, up to 50 bisection
 // steps, then the final cost), so one thread per pair leaves most lanes of a

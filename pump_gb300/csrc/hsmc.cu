@@ -111,10 +111,11 @@ constexpr double kDT = 0.05, kH2 = 0.00125, kKP = 16.0, kKD = 5.6, kSigmaW = 4.0
 
 // One warp per particle.  The Gaussians of 32 consecutive steps are
 // independent, so lane k computes step t0+k (Philox, Box-Muller); the
-// closed-loop recurrence is sequential, so every lane replays it over the 32
-// steps with the lanes' noise broadcast by shuffles, and lane k stores step
-// t0+k.  Arithmetic is identical to a scalar loop (same operations, same
-// order, no contraction).
+// closed-loop recurrence is sequential, so lane 0 runs it over the 32 steps
+// with the lanes' noise broadcast by shuffles (binary64 throughput is scarce
+// on this GPU: the other lanes do not repeat it) and stores every step.
+// Arithmetic is identical to a scalar loop (same operations, same order, no
+// contraction).
 __global__ void __launch_bounds__(256) particle_table_kernel(uint32_t k0, uint32_t k1, int P, int T,
                                                              float *__restrict__ tmajor,
                                                              float *__restrict__ pmajor) {
@@ -142,22 +143,21 @@ __global__ void __launch_bounds__(256) particle_table_kernel(uint32_t k0, uint32
     }
     const int steps = T - t0 < 32 ? T - t0 : 32;
     for (int k = 0; k < steps; ++k) {
-      if (k == lane) {
+      double zk[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) zk[d] = __shfl_sync(0xffffffffu, z[d], k);
+      if (lane == 0) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const float v = (float)pos[d];
           if (tmajor) tmajor[((long long)(t0 + k) * P + p) * 3 + d] = v;
           if (pmajor) pmajor[((long long)p * T + t0 + k) * 3 + d] = v;
+          const double a = kSigmaW * zk[d] - (kKP * pos[d] + kKD * vel[d]);
+          const double pn = (pos[d] + kDT * vel[d]) + kH2 * a;
+          const double vn = vel[d] + kDT * a;
+          pos[d] = pn;
+          vel[d] = vn;
         }
-      }
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const double zk = __shfl_sync(0xffffffffu, z[d], k);
-        const double a = kSigmaW * zk - (kKP * pos[d] + kKD * vel[d]);
-        const double pn = (pos[d] + kDT * vel[d]) + kH2 * a;
-        const double vn = vel[d] + kDT * a;
-        pos[d] = pn;
-        vel[d] = vn;
       }
     }
   }

@@ -20,7 +20,10 @@
 // Host arithmetic follows the reference's float expressions and is compiled
 // without multiply-add contraction.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <string>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <utility>
@@ -51,21 +54,28 @@ double ms_since(clk::time_point t0) {
   return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
 }
 
-// Owning device buffer.
+// Stream that the planner running on this host thread allocates on.
+thread_local cudaStream_t t_alloc_stream = nullptr;
+
+// Owning device buffer, allocated and freed in stream order on the planner's
+// stream (cudaMallocAsync / cudaFreeAsync): no call synchronises the device,
+// so planners on other streams keep running.
 template <class T>
 struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
-  ~DevBuf() { if (p) cudaFree(p); }
+  ~DevBuf() { if (p) cudaFreeAsync(p, s); }
   pump_status_t alloc(size_t count) {
     if (count <= n && p) return PUMP_OK;
-    if (p) cudaFree(p);
+    if (p) PUMP_CUDA_TRY(cudaFreeAsync(p, s));
     p = nullptr;
     n = 0;
-    PUMP_CUDA_TRY(cudaMalloc(&p, sizeof(T) * (count ? count : 1)));
+    s = t_alloc_stream;
+    PUMP_CUDA_TRY(cudaMallocAsync((void **)&p, sizeof(T) * (count ? count : 1), s));
     n = count;
     return PUMP_OK;
   }
@@ -180,6 +190,7 @@ class Planner {
 
 pump_status_t Planner::run() {
   const auto t0 = clk::now();
+  t_alloc_stream = s_;
   N_ = pb_.N;
   W_ = pb_.num_disc + 1;
   P_ = pb_.num_hsmc;
@@ -734,6 +745,41 @@ pump_status_t Planner::search_and_smooth() {
 }  // namespace pump
 
 using namespace pump;
+
+extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problems,
+                                         pump_plan_result *results, pump_status_t *statuses, int n,
+                                         int workers) {
+  if (n < 0 || (n > 0 && (!problems || !results || !statuses)) || workers < 1)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_plan_batch: bad arguments");
+  if (n == 0) return PUMP_OK;
+  if (workers > n) workers = n;
+  std::atomic<int> next(0);
+  std::vector<pump_status_t> setup(workers, PUMP_OK);
+  std::vector<std::string> msgs(workers);
+  auto worker = [&](int w) {
+    pump_ctx *ctx = nullptr;
+    pump_status_t st = pump_ctx_create(device, &ctx);
+    cudaStream_t s = nullptr;
+    if (st == PUMP_OK) st = cuda_status(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
+                                        "cudaStreamCreateWithFlags");
+    if (st != PUMP_OK) {
+      setup[w] = st;
+      msgs[w] = pump_last_error();
+    } else {
+      for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1))
+        statuses[k] = pump_plan(ctx, &problems[k], &results[k], (pump_stream_t)s);
+    }
+    if (s) cudaStreamDestroy(s);
+    if (ctx) pump_ctx_destroy(ctx);
+  };
+  std::vector<std::thread> pool;
+  for (int w = 1; w < workers; ++w) pool.emplace_back(worker, w);
+  worker(0);
+  for (auto &t : pool) t.join();
+  for (int w = 0; w < workers; ++w)
+    if (setup[w] != PUMP_OK) return set_error(setup[w], "pump_plan_batch worker %d: %s", w, msgs[w].c_str());
+  return PUMP_OK;
+}
 
 extern "C" pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
                                    pump_stream_t stream) {

@@ -90,6 +90,7 @@ _SIGS = {
     "pump_problem_defaults": (None, [C.POINTER(Problem)]),
     "pump_read_input": (i32, [C.c_char_p, C.POINTER(Problem)]),
     "pump_plan": (i32, [vp, C.POINTER(Problem), C.POINTER(PlanResult), vp]),
+    "pump_plan_batch": (i32, [i32, vp, vp, vp, i32, i32]),
 }
 
 

@@ -80,6 +80,32 @@ def write_input(path, obstacles, offset_mult, init=INIT, goal=GOAL, lo=LO, hi=HI
             f.write(line + (",\n" if k + 1 < obstacles.shape[0] else "\n"))
 
 
+def free_point(rng, obstacles):
+    """A position uniform in [0,1]^3 outside every box, zero velocity."""
+    while True:
+        p = rng.uniform(0.0, 1.0, 3)
+        if not any(_contains(b, p) for b in obstacles):
+            return (float(p[0]), float(p[1]), float(p[2]), 0.0, 0.0, 0.0)
+
+
+def batch_queries(n=256, seed=2000, n_range=(500, 8000), obs_range=(5, 100)):
+    """The batched workload: per query N log-uniform in n_range, a box count
+    uniform in obs_range (boxes as random_boxes), init and goal uniform in free
+    space, CP target from {0.001, 0.01, 0.05}, eta from {1, 2, 4}."""
+    rng = np.random.Generator(np.random.MT19937(seed))
+    out = []
+    for q in range(n):
+        N = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
+        nobs = int(rng.integers(obs_range[0], obs_range[1] + 1))
+        obs = random_boxes(nobs, seed * 1000 + q)
+        init = free_point(rng, obs)
+        goal = free_point(rng, obs)
+        out.append(dict(N=N, obstacles=obs, init=init, goal=goal,
+                        cp=float(rng.choice([0.001, 0.01, 0.05])),
+                        eta=float(rng.choice([1.0, 2.0, 4.0])), offset_mult=np.float32(1e-3)))
+    return out
+
+
 CONFIGS = {
     # the benchmark configurations (N, obstacles, noise, cp, eta, particles, waypoints)
     "cfg0": dict(N=1000, num_disc=9, num_hsmc=128, offset_mult=1e-3, cp=0.01, eta=2.0,

@@ -83,3 +83,40 @@ def test_plan_matches_oracle_cfg0(gpu, pumplib, oracle):
     assert np.array_equal(path.view(np.uint32), r["path"].view(np.uint32))
     assert np.float32(res.soln_cp) == np.float32(r["solnCP"])
     assert np.float32(res.soln_cost) == np.float32(r["solnCost"])
+
+
+def fill_problem(L, q, keep):
+    pb = L.Problem()
+    L.load().pump_problem_defaults(C.byref(pb))
+    obs = np.ascontiguousarray(q["obstacles"], np.float32)
+    keep.append(obs)
+    pb.N, pb.num_obstacles, pb.obstacles = q["N"], obs.shape[0], obs.ctypes.data
+    from pump_gb300 import workloads
+    for k in range(6):
+        pb.init[k], pb.goal[k] = q["init"][k], q["goal"][k]
+        pb.lo[k], pb.hi[k] = workloads.LO[k], workloads.HI[k]
+    pb.offset_mult, pb.cp_target, pb.cp_factor = float(q["offset_mult"]), q["cp"], q["eta"]
+    return pb
+
+
+def test_plan_batch_equals_single_queries(gpu, pumplib):
+    """Concurrent queries (pump_plan_batch, 4 workers) give exactly what each
+    query gives alone."""
+    torch, ctx = gpu
+    from pump_gb300 import workloads
+    L = pumplib.load()
+    qs = workloads.batch_queries(10, seed=77, n_range=(200, 900), obs_range=(5, 30))
+    keep = []
+    pbs = (pumplib.Problem * len(qs))(*[fill_problem(pumplib, q, keep) for q in qs])
+    res = (pumplib.PlanResult * len(qs))()
+    paths = [np.zeros((400, 6), np.float32) for _ in qs]
+    for k in range(len(qs)):
+        res[k].path, res[k].path_cap = paths[k].ctypes.data, 400
+    sts = (C.c_int * len(qs))()
+    pumplib.check(L.pump_plan_batch(0, pbs, res, sts, len(qs), 4))
+    for k, q in enumerate(qs):
+        st1, r1, p1, _ = run_plan(pumplib, ctx, pbs[k])
+        assert sts[k] == st1
+        assert (res[k].num_paths, res[k].success, res[k].soln_path_idx) == (r1.num_paths, r1.success,
+                                                                            r1.soln_path_idx)
+        assert np.array_equal(paths[k][: res[k].path_len].view(np.uint32), p1.view(np.uint32))
