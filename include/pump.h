@@ -129,7 +129,9 @@ pump_status_t pump_cache_halfspaces(const float *d_obstacles, int numObs, const 
 /* Particle tables of the closed-loop tracking-error model (the data of the
  * reference's missing hardCoded.cu, hardCoded.cuh:12-19): position errors
  * tmajor[T][P][3] (xcombTime) and pmajor[P][T][3] (xcomb); either may be
- * NULL.  Philox4x32-10 keyed by seed, Box-Muller, binary64 dynamics. */
+ * NULL.  Philox4x32-10 keyed by seed, Box-Muller, binary64 dynamics.  Uses a
+ * temporary of 24 B per (particle, step), allocated and freed in stream
+ * order on `stream`. */
 pump_status_t pump_particle_tables(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
                                    pump_stream_t stream);
 

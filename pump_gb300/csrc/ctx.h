@@ -29,17 +29,14 @@ class Ctx {
   // Device buffer of at least `bytes` for `slot` (contents undefined).
   pump_status_t scratch(int slot, size_t bytes, void **out);
   // Time-major particle table for (seed, P, T), generated on first use and
-  // kept for later queries of this context (the reference loads its table
-  // once per process).
+  // shared by every context on the device (the reference loads its table
+  // once per process); `stream` is ordered after its generation.
   pump_status_t particle_table(uint64_t seed, int P, int T, const float **out, cudaStream_t stream);
 
  private:
   int device_;
   void *buf_[kNumSlots];
   size_t cap_[kNumSlots];
-  float *table_ = nullptr;
-  uint64_t table_seed_ = 0;
-  int table_P_ = 0, table_T_ = 0;
 };
 
 // Internal device-side entry points shared between translation units.

@@ -109,57 +109,50 @@ __device__ void det_sincos_2pi(double u, double *s, double *c) {
 
 constexpr double kDT = 0.05, kH2 = 0.00125, kKP = 16.0, kKD = 5.6, kSigmaW = 4.0;
 
-// One warp per particle.  The Gaussians of 32 consecutive steps are
-// independent, so lane k computes step t0+k (Philox, Box-Muller); the
-// closed-loop recurrence is sequential, so lane 0 runs it over the 32 steps
-// with the lanes' noise broadcast by shuffles (binary64 throughput is scarce
-// on this GPU: the other lanes do not repeat it) and stores every step.
-// Arithmetic is identical to a scalar loop (same operations, same order, no
-// contraction).
-__global__ void __launch_bounds__(256) particle_table_kernel(uint32_t k0, uint32_t k1, int P, int T,
-                                                             float *__restrict__ tmajor,
-                                                             float *__restrict__ pmajor) {
-  const int lane = threadIdx.x & 31;
-  const int p = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-  if (p >= P) return;  // warp-uniform
-  double pos[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
+// The table in two launches.  Gaussians of every (particle, step) are
+// independent: one thread each (Philox, Box-Muller) into a binary64 buffer
+// z[t][p][3].  The closed-loop recurrence is sequential in time only: one
+// thread per (particle, axis) runs it over the steps.  (A binary64 warp
+// instruction occupies this GPU's FP64 pipe for the same time whether one
+// lane or 32 are active, so the recurrence must not run in one lane of a warp
+// while the others wait.)  Each value is produced by the same operations in
+// the same order as a scalar loop, without contraction.
+__global__ void __launch_bounds__(256) particle_gauss_kernel(uint32_t k0, uint32_t k1, int P, int T,
+                                                             double *__restrict__ z) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)P * T) return;
+  const int t = (int)(i / P), p = (int)(i - (long long)t * P);
   const double sc = 2.3283064365386962890625e-10;  // 2^-32
-  for (int t0 = 0; t0 < T; t0 += 32) {
-    const int t = t0 + lane;
-    double z[3] = {0, 0, 0};
-    if (t < T) {
-      uint32_t o[4];
-      philox4x32_10((uint32_t)p, (uint32_t)t, 0u, 0u, k0, k1, o);
-      const double u0 = ((double)o[0] + 0.5) * sc, u1 = ((double)o[1] + 0.5) * sc;
-      const double u2 = ((double)o[2] + 0.5) * sc, u3 = ((double)o[3] + 0.5) * sc;
-      const double r0 = sqrt(-2.0 * det_log(u0));
-      const double r1 = sqrt(-2.0 * det_log(u2));
-      double s0, c0, s1, c1;
-      det_sincos_2pi(u1, &s0, &c0);
-      det_sincos_2pi(u3, &s1, &c1);
-      z[0] = r0 * c0;
-      z[1] = r0 * s0;
-      z[2] = r1 * c1;
-    }
-    const int steps = T - t0 < 32 ? T - t0 : 32;
-    for (int k = 0; k < steps; ++k) {
-      double zk[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) zk[d] = __shfl_sync(0xffffffffu, z[d], k);
-      if (lane == 0) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const float v = (float)pos[d];
-          if (tmajor) tmajor[((long long)(t0 + k) * P + p) * 3 + d] = v;
-          if (pmajor) pmajor[((long long)p * T + t0 + k) * 3 + d] = v;
-          const double a = kSigmaW * zk[d] - (kKP * pos[d] + kKD * vel[d]);
-          const double pn = (pos[d] + kDT * vel[d]) + kH2 * a;
-          const double vn = vel[d] + kDT * a;
-          pos[d] = pn;
-          vel[d] = vn;
-        }
-      }
-    }
+  uint32_t o[4];
+  philox4x32_10((uint32_t)p, (uint32_t)t, 0u, 0u, k0, k1, o);
+  const double u0 = ((double)o[0] + 0.5) * sc, u1 = ((double)o[1] + 0.5) * sc;
+  const double u2 = ((double)o[2] + 0.5) * sc, u3 = ((double)o[3] + 0.5) * sc;
+  const double r0 = sqrt(-2.0 * det_log(u0));
+  const double r1 = sqrt(-2.0 * det_log(u2));
+  double s0, c0, s1, c1;
+  det_sincos_2pi(u1, &s0, &c0);
+  det_sincos_2pi(u3, &s1, &c1);
+  z[i * 3 + 0] = r0 * c0;
+  z[i * 3 + 1] = r0 * s0;
+  z[i * 3 + 2] = r1 * c1;
+}
+
+__global__ void __launch_bounds__(128) particle_table_kernel(const double *__restrict__ z, int P,
+                                                             int T, float *__restrict__ tmajor,
+                                                             float *__restrict__ pmajor) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P * 3) return;
+  const int p = i / 3, d = i - 3 * (i / 3);
+  double pos = 0, vel = 0;
+  for (int t = 0; t < T; ++t) {
+    const float v = (float)pos;
+    if (tmajor) tmajor[((long long)t * P + p) * 3 + d] = v;
+    if (pmajor) pmajor[((long long)p * T + t) * 3 + d] = v;
+    const double a = kSigmaW * z[((long long)t * P + p) * 3 + d] - (kKP * pos + kKD * vel);
+    const double pn = (pos + kDT * vel) + kH2 * a;
+    const double vn = vel + kDT * a;
+    pos = pn;
+    vel = vn;
   }
 }
 
@@ -417,11 +410,22 @@ pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n,
   return launch_status("gather_words_kernel");
 }
 
+// Generates the tables on `stream`; the binary64 noise buffer (24 B per
+// particle and step) is allocated and freed in stream order.
 pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
                                     cudaStream_t stream) {
-  particle_table_kernel<<<grid_for((long long)P * 32, 256), 256, 0, stream>>>(
-      (uint32_t)seed, (uint32_t)(seed >> 32), P, T, d_tmajor, d_pmajor);
-  return launch_status("particle_table_kernel");
+  double *z = nullptr;
+  PUMP_CUDA_TRY(cudaMallocAsync((void **)&z, sizeof(double) * 3 * (size_t)P * T, stream));
+  particle_gauss_kernel<<<grid_for((long long)P * T, 256), 256, 0, stream>>>(
+      (uint32_t)seed, (uint32_t)(seed >> 32), P, T, z);
+  pump_status_t st = launch_status("particle_gauss_kernel");
+  if (st == PUMP_OK) {
+    particle_table_kernel<<<grid_for((long long)P * 3, 128), 128, 0, stream>>>(z, P, T, d_tmajor,
+                                                                              d_pmajor);
+    st = launch_status("particle_table_kernel");
+  }
+  cudaFreeAsync(z, stream);
+  return st;
 }
 
 }  // namespace pump
