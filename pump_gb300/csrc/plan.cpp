@@ -31,6 +31,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "pairview.cuh"
 
 namespace pump {
 
@@ -110,6 +111,21 @@ void halton_samples(const pump_problem &pb, std::vector<float> &s) {
   }
 }
 
+// Pair BVPs of Halton points 1 .. M shared by a batch's queries (see
+// pairview.cuh); key = the BVP mode and the state bounds that scale the points.
+struct SharedRoadmap {
+  int mode;
+  float lo[6], hi[6];
+  long long M;
+  const float *d_copt, *d_topt;  // pump_bvp_pairs layout over the M points
+  bool matches(const pump_problem &pb) const {
+    if (pb.samples || pb.bvp_mode != mode || pb.N - 2 > M || pb.N < 4) return false;
+    for (int d = 0; d < 6; ++d)
+      if (pb.lo[d] != lo[d] || pb.hi[d] != hi[d]) return false;
+    return true;
+  }
+};
+
 // Batch of dense paths along node sequences (findOptimalPath, 2pBVP.cu:5-36):
 // segment optimal times on the GPU, the sample-time recurrence on the host,
 // the states on the GPU.
@@ -120,12 +136,14 @@ struct DensePaths {
 
 class Planner {
  public:
-  Planner(Ctx *ctx, const pump_problem &pb, pump_plan_result *res, cudaStream_t s)
-      : ctx_(ctx), pb_(pb), res_(res), s_(s) {}
+  Planner(Ctx *ctx, const pump_problem &pb, pump_plan_result *res, cudaStream_t s,
+          const SharedRoadmap *shared = nullptr)
+      : ctx_(ctx), pb_(pb), res_(res), s_(s), shared_(shared) {}
   pump_status_t run();
 
  private:
   pump_status_t roadmap();
+  pump_status_t pair_costs_shared(long long rnIdx, long long cap);
   pump_status_t online();
   pump_status_t explore();
   pump_status_t search_and_smooth();
@@ -154,6 +172,8 @@ class Planner {
   const pump_problem &pb_;
   pump_plan_result *res_;
   cudaStream_t s_;
+  const SharedRoadmap *shared_;
+  DevBuf<float> d_own_c_, d_own_t_;  // pairs touching init/goal (shared-roadmap path)
 
   // problem constants (mainPUMP.cu:51-72)
   const float dt_ = (float)0.05;
@@ -221,25 +241,29 @@ pump_status_t Planner::roadmap() {
   PUMP_TRY(d_samples_.alloc((size_t)N_ * kDim));
   PUMP_TRY(h2d(d_samples_.p, samples_.data(), samples_.size()));
   const long long npairs = (long long)N_ * (N_ - 1);
-  PUMP_TRY(d_copts_.alloc(npairs));
-  PUMP_TRY(d_topts_.alloc(npairs));
-  PUMP_TRY(pump_bvp_pairs(d_samples_.p, N_, 5.0f, pb_.bvp_mode, d_copts_.p, d_topts_.p,
-                          (pump_stream_t)s_));
   // mainPUMP.cu:261-262: (int)((NUM-1)*(NUM)*rnPerc) with rnPerc a float
   const long long rnIdx = (long long)((float)((long long)(N_ - 1) * N_) * (float)0.05);
-  const float *d_rn = nullptr;
-  PUMP_TRY(select_kth_device(ctx_, d_copts_.p, npairs, rnIdx, &d_rn, s_));
-  PUMP_TRY(d2h(&rn_, d_rn, 1));
-  PUMP_TRY(sync());
-  res_->rn = rn_;
   const long long cap = rnIdx > 0 ? rnIdx : 1;
   PUMP_TRY(d_src_.alloc(cap));
   PUMP_TRY(d_dst_.alloc(cap));
   PUMP_TRY(d_coptE_.alloc(cap));
   PUMP_TRY(d_toptE_.alloc(cap));
   PUMP_TRY(d_go_.alloc(N_ + 1));
-  PUMP_TRY(build_edges_device(ctx_, d_copts_.p, d_topts_.p, N_, rn_, cap, d_src_.p, d_dst_.p,
-                              d_coptE_.p, d_toptE_.p, d_go_.p, &E_, s_));
+  if (shared_ && shared_->matches(pb_)) {
+    PUMP_TRY(pair_costs_shared(rnIdx, cap));
+  } else {
+    PUMP_TRY(d_copts_.alloc(npairs));
+    PUMP_TRY(d_topts_.alloc(npairs));
+    PUMP_TRY(pump_bvp_pairs(d_samples_.p, N_, 5.0f, pb_.bvp_mode, d_copts_.p, d_topts_.p,
+                            (pump_stream_t)s_));
+    const float *d_rn = nullptr;
+    PUMP_TRY(select_kth_device(ctx_, d_copts_.p, npairs, rnIdx, &d_rn, s_));
+    PUMP_TRY(d2h(&rn_, d_rn, 1));
+    PUMP_TRY(sync());
+    res_->rn = rn_;
+    PUMP_TRY(build_edges_device(ctx_, d_copts_.p, d_topts_.p, N_, rn_, cap, d_src_.p, d_dst_.p,
+                                d_coptE_.p, d_toptE_.p, d_go_.p, &E_, s_));
+  }
   res_->num_edges = E_;
   PUMP_TRY(d_disc_.alloc((size_t)E_ * W_ * kDim));
   PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, d_toptE_.p, E_, pb_.num_disc,
@@ -266,6 +290,55 @@ pump_status_t Planner::roadmap() {
   PUMP_TRY(d2h(coptE_.data(), d_coptE_.p, E_));
   PUMP_TRY(d2h(toptE_.data(), d_toptE_.p, E_));
   return sync();
+}
+
+// The query's pair costs from the batch's shared Halton pairs plus its own
+// 4N-6 pairs touching init or goal (tmax 5, as pump_bvp_pairs): rn and the
+// edges come out exactly as from the query's own N(N-1) pair arrays.
+pump_status_t Planner::pair_costs_shared(long long rnIdx, long long cap) {
+  const int N = N_;
+  const size_t own = (size_t)(4 * N - 6);
+  std::vector<float> x0(own * kDim), x1(own * kDim);
+  size_t k = 0;
+  auto put = [&](int a, int b) {
+    for (int d = 0; d < kDim; ++d) {
+      x0[k * kDim + d] = samples_[(size_t)a * kDim + d];
+      x1[k * kDim + d] = samples_[(size_t)b * kDim + d];
+    }
+    ++k;
+  };
+  for (int j = 1; j <= N - 1; ++j) put(0, j);      // init row
+  for (int i = 1; i <= N - 1; ++i) put(i, 0);      // init col
+  for (int j = 1; j <= N - 2; ++j) put(N - 1, j);  // goal row
+  for (int i = 1; i <= N - 2; ++i) put(i, N - 1);  // goal col
+  PUMP_TRY(d_bx0_.alloc(x0.size()));
+  PUMP_TRY(d_bx1_.alloc(x1.size()));
+  PUMP_TRY(d_own_c_.alloc(own));
+  PUMP_TRY(d_own_t_.alloc(own));
+  PUMP_TRY(h2d(d_bx0_.p, x0.data(), x0.size()));
+  PUMP_TRY(h2d(d_bx1_.p, x1.data(), x1.size()));
+  PUMP_TRY(pump_bvp_batch(d_bx0_.p, d_bx1_.p, (int)own, 5.0f, pb_.bvp_mode, d_own_t_.p, d_own_c_.p,
+                          (pump_stream_t)s_));
+  PairView pv;
+  pv.N = N;
+  pv.M = shared_->M;
+  pv.sc = shared_->d_copt;
+  pv.st = shared_->d_topt;
+  pv.irc = d_own_c_.p;
+  pv.irt = d_own_t_.p;
+  pv.icc = d_own_c_.p + (N - 1);
+  pv.ict = d_own_t_.p + (N - 1);
+  pv.grc = d_own_c_.p + 2 * (N - 1);
+  pv.grt = d_own_t_.p + 2 * (N - 1);
+  pv.gcc = d_own_c_.p + 2 * (N - 1) + (N - 2);
+  pv.gct = d_own_t_.p + 2 * (N - 1) + (N - 2);
+  const float *d_rn = nullptr;
+  PUMP_TRY(select_kth_pairs(ctx_, pv, rnIdx, &d_rn, s_));
+  PUMP_TRY(d2h(&rn_, d_rn, 1));
+  PUMP_TRY(sync());
+  res_->rn = rn_;
+  return build_edges_pairs(ctx_, pv, rn_, cap, d_src_.p, d_dst_.p, d_coptE_.p, d_toptE_.p,
+                           d_go_.p, &E_, s_);
 }
 
 pump_status_t Planner::online() {
@@ -746,43 +819,10 @@ pump_status_t Planner::search_and_smooth() {
 
 using namespace pump;
 
-extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problems,
-                                         pump_plan_result *results, pump_status_t *statuses, int n,
-                                         int workers) {
-  if (n < 0 || (n > 0 && (!problems || !results || !statuses)) || workers < 1)
-    return set_error(PUMP_ERR_BAD_INPUT, "pump_plan_batch: bad arguments");
-  if (n == 0) return PUMP_OK;
-  if (workers > n) workers = n;
-  std::atomic<int> next(0);
-  std::vector<pump_status_t> setup(workers, PUMP_OK);
-  std::vector<std::string> msgs(workers);
-  auto worker = [&](int w) {
-    pump_ctx *ctx = nullptr;
-    pump_status_t st = pump_ctx_create(device, &ctx);
-    cudaStream_t s = nullptr;
-    if (st == PUMP_OK) st = cuda_status(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
-                                        "cudaStreamCreateWithFlags");
-    if (st != PUMP_OK) {
-      setup[w] = st;
-      msgs[w] = pump_last_error();
-    } else {
-      for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1))
-        statuses[k] = pump_plan(ctx, &problems[k], &results[k], (pump_stream_t)s);
-    }
-    if (s) cudaStreamDestroy(s);
-    if (ctx) pump_ctx_destroy(ctx);
-  };
-  std::vector<std::thread> pool;
-  for (int w = 1; w < workers; ++w) pool.emplace_back(worker, w);
-  worker(0);
-  for (auto &t : pool) t.join();
-  for (int w = 0; w < workers; ++w)
-    if (setup[w] != PUMP_OK) return set_error(setup[w], "pump_plan_batch worker %d: %s", w, msgs[w].c_str());
-  return PUMP_OK;
-}
-
-extern "C" pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
-                                   pump_stream_t stream) {
+namespace pump {
+namespace {
+pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
+                       pump_stream_t stream, const SharedRoadmap *shared) {
   if (!ctx || !pb || !res) return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: null argument");
   if (pb->N < 2 || pb->num_disc < 1 || pb->num_hsmc < 1 || pb->num_mc < pb->num_hsmc ||
       pb->table_rows < 2 || pb->num_obstacles < 0 || (pb->num_obstacles > 0 && !pb->obstacles) ||
@@ -804,6 +844,111 @@ extern "C" pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_p
   res->soln_path_idx = -1;
   Ctx *c = Ctx::from(ctx);
   PUMP_TRY(c->activate());
-  Planner planner(c, *pb, res, (cudaStream_t)stream);
+  Planner planner(c, *pb, res, (cudaStream_t)stream, shared);
   return planner.run();
+}
+}  // namespace
+}  // namespace pump
+
+extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problems,
+                                         pump_plan_result *results, pump_status_t *statuses, int n,
+                                         int workers) {
+  if (n < 0 || (n > 0 && (!problems || !results || !statuses)) || workers < 1)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_plan_batch: bad arguments");
+  if (n == 0) return PUMP_OK;
+  if (workers > n) workers = n;
+  // Shared roadmaps: one per (BVP mode, bounds) group of Halton queries, with
+  // the pair BVPs of Halton points 1 .. max(N) - 2 computed once.
+  PUMP_CUDA_TRY(cudaSetDevice(device));
+  std::vector<SharedRoadmap> groups;
+  std::vector<float *> owned;
+  cudaStream_t setup_stream = nullptr;
+  PUMP_CUDA_TRY(cudaStreamCreateWithFlags(&setup_stream, cudaStreamNonBlocking));
+  auto cleanup = [&]() {
+    for (float *p : owned) cudaFree(p);
+    cudaStreamDestroy(setup_stream);
+  };
+  for (int k = 0; k < n; ++k) {
+    const pump_problem &pb = problems[k];
+    if (pb.samples || pb.N < 4) continue;
+    SharedRoadmap *g = nullptr;
+    for (auto &x : groups) {
+      bool same = x.mode == pb.bvp_mode;
+      for (int d = 0; d < 6 && same; ++d) same = x.lo[d] == pb.lo[d] && x.hi[d] == pb.hi[d];
+      if (same) g = &x;
+    }
+    if (!g) {
+      SharedRoadmap x{};
+      x.mode = pb.bvp_mode;
+      for (int d = 0; d < 6; ++d) { x.lo[d] = pb.lo[d]; x.hi[d] = pb.hi[d]; }
+      x.M = 0;
+      groups.push_back(x);
+      g = &groups.back();
+    }
+    if (pb.N - 2 > g->M) g->M = pb.N - 2;
+  }
+  for (auto &g : groups) {
+    if (g.M < 2) { g.M = -1; continue; }
+    pump_problem hp{};
+    hp.N = (int)g.M + 2;
+    for (int d = 0; d < 6; ++d) { hp.lo[d] = g.lo[d]; hp.hi[d] = g.hi[d]; }
+    std::vector<float> all;
+    halton_samples(hp, all);  // points 0 .. M+1; the shared set is 1 .. M
+    float *d_pts = nullptr, *d_c = nullptr, *d_t = nullptr;
+    const long long np = g.M * (g.M - 1);
+    pump_status_t st = cuda_status(cudaMalloc(&d_pts, sizeof(float) * kDim * g.M), "cudaMalloc");
+    if (st == PUMP_OK) st = cuda_status(cudaMalloc(&d_c, sizeof(float) * np), "cudaMalloc");
+    if (st == PUMP_OK) st = cuda_status(cudaMalloc(&d_t, sizeof(float) * np), "cudaMalloc");
+    owned.push_back(d_pts);
+    owned.push_back(d_c);
+    owned.push_back(d_t);
+    if (st == PUMP_OK)
+      st = cuda_status(cudaMemcpyAsync(d_pts, all.data() + kDim, sizeof(float) * kDim * g.M,
+                                       cudaMemcpyHostToDevice, setup_stream), "H2D");
+    if (st == PUMP_OK)
+      st = pump_bvp_pairs(d_pts, (int)g.M, 5.0f, g.mode, d_c, d_t, (pump_stream_t)setup_stream);
+    if (st != PUMP_OK) { cleanup(); return st; }
+    g.d_copt = d_c;
+    g.d_topt = d_t;
+  }
+  {
+    pump_status_t st = cuda_status(cudaStreamSynchronize(setup_stream), "cudaStreamSynchronize");
+    if (st != PUMP_OK) { cleanup(); return st; }
+  }
+  std::atomic<int> next(0);
+  std::vector<pump_status_t> setup(workers, PUMP_OK);
+  std::vector<std::string> msgs(workers);
+  auto worker = [&](int w) {
+    pump_ctx *ctx = nullptr;
+    pump_status_t st = pump_ctx_create(device, &ctx);
+    cudaStream_t s = nullptr;
+    if (st == PUMP_OK) st = cuda_status(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
+                                        "cudaStreamCreateWithFlags");
+    if (st != PUMP_OK) {
+      setup[w] = st;
+      msgs[w] = pump_last_error();
+    } else {
+      for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+        const SharedRoadmap *g = nullptr;
+        for (const auto &x : groups)
+          if (x.M > 0 && x.matches(problems[k])) g = &x;
+        statuses[k] = plan_one(ctx, &problems[k], &results[k], (pump_stream_t)s, g);
+      }
+    }
+    if (s) cudaStreamDestroy(s);
+    if (ctx) pump_ctx_destroy(ctx);
+  };
+  std::vector<std::thread> pool;
+  for (int w = 1; w < workers; ++w) pool.emplace_back(worker, w);
+  worker(0);
+  for (auto &t : pool) t.join();
+  cleanup();
+  for (int w = 0; w < workers; ++w)
+    if (setup[w] != PUMP_OK) return set_error(setup[w], "pump_plan_batch worker %d: %s", w, msgs[w].c_str());
+  return PUMP_OK;
+}
+
+extern "C" pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
+                                   pump_stream_t stream) {
+  return plan_one(ctx, pb, res, stream, nullptr);
 }

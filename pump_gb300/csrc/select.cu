@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "pairview.cuh"
 
 namespace pump {
 namespace {
@@ -50,9 +51,23 @@ struct SelectState {
   float result;
 };
 
-__global__ void select_hist_kernel(const float *__restrict__ v, long long n,
-                                   const SelectState *__restrict__ st, int shift, int bits,
-                                   unsigned int *__restrict__ hist) {
+struct FlatSrc {
+  const float *v;
+  __device__ float operator()(long long i) const { return __ldg(&v[i]); }
+};
+struct PairCoptSrc {
+  PairView pv;
+  __device__ float operator()(long long idx) const {
+    int i, j;
+    pv.pair(idx, &i, &j);
+    return pv.copt(i, j);
+  }
+};
+
+// Src(i) -> the i-th value (a flat array, or a virtual pair array).
+template <class Src>
+__global__ void select_hist_kernel(Src src, long long n, const SelectState *__restrict__ st,
+                                   int shift, int bits, unsigned int *__restrict__ hist) {
   __shared__ unsigned int sh[2048];
   const int nb = 1 << bits;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sh[b] = 0;
@@ -60,7 +75,7 @@ __global__ void select_hist_kernel(const float *__restrict__ v, long long n,
   const uint32_t prefix = st->prefix, mask = st->mask;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-    const uint32_t key = float_key(__ldg(&v[i]));
+    const uint32_t key = float_key(src(i));
     if ((key & mask) == prefix) atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
   }
   __syncthreads();
@@ -239,6 +254,30 @@ struct EdgeEmit {
     topt[pos] = topts[idx];
   }
 };
+struct PairEdgePred {
+  PairView pv;
+  float rn;
+  __device__ bool operator()(long long idx) const {
+    int i, j;
+    pv.pair(idx, &i, &j);
+    return pv.copt(i, j) < rn;
+  }
+};
+struct PairEdgeEmit {
+  PairView pv;
+  long long cap;
+  int *src, *dst;
+  float *copt, *topt;
+  __device__ void operator()(long long idx, long long pos) const {
+    if (pos >= cap) return;
+    int i, j;
+    pv.pair(idx, &i, &j);
+    src[pos] = i;
+    dst[pos] = j;
+    copt[pos] = pv.copt(i, j);
+    topt[pos] = pv.topt(i, j);
+  }
+};
 struct FlagPred {
   const uint8_t *flags;
   __device__ bool operator()(long long i) const { return flags[i] != 0; }
@@ -295,12 +334,11 @@ pump_status_t finish_compact(const TileScratch &ts, unsigned long long *total, c
   return PUMP_OK;
 }
 
-}  // namespace
-
-// Device-side k-th smallest: result lands in the ctx select state (device);
-// returns a device pointer to the float result.
-pump_status_t select_kth_device(Ctx *ctx, const float *d_v, long long n, long long k,
-                                const float **d_result, cudaStream_t stream) {
+// Device-side k-th smallest of src(0 .. n-1): the result lands in the ctx
+// select state; *d_result points at it (device).
+template <class Src>
+pump_status_t select_kth_src(Ctx *ctx, Src src, long long n, long long k, const float **d_result,
+                             cudaStream_t stream) {
   if (n <= 0 || k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "select_kth: k=%lld n=%lld", k, n);
   char *scratch = nullptr;
   const size_t bytes = sizeof(SelectState) + 2048 * sizeof(unsigned int);
@@ -314,13 +352,25 @@ pump_status_t select_kth_device(Ctx *ctx, const float *d_v, long long n, long lo
   if (blocks > kNumSMs * 8) blocks = kNumSMs * 8;
   const int shifts[3] = {21, 10, 0}, bits[3] = {11, 11, 10};
   for (int pass = 0; pass < 3; ++pass) {
-    select_hist_kernel<<<(unsigned)blocks, 1024, 0, stream>>>(d_v, n, st, shifts[pass], bits[pass], hist);
+    select_hist_kernel<<<(unsigned)blocks, 1024, 0, stream>>>(src, n, st, shifts[pass], bits[pass], hist);
     PUMP_TRY(launch_status("select_hist_kernel"));
     select_pick_kernel<<<1, 1024, 0, stream>>>(st, shifts[pass], bits[pass], hist);
     PUMP_TRY(launch_status("select_pick_kernel"));
   }
   *d_result = &st->result;
   return PUMP_OK;
+}
+
+}  // namespace
+
+pump_status_t select_kth_device(Ctx *ctx, const float *d_v, long long n, long long k,
+                                const float **d_result, cudaStream_t stream) {
+  return select_kth_src(ctx, FlatSrc{d_v}, n, k, d_result, stream);
+}
+
+pump_status_t select_kth_pairs(Ctx *ctx, const PairView &pv, long long k, const float **d_result,
+                               cudaStream_t stream) {
+  return select_kth_src(ctx, PairCoptSrc{pv}, (long long)pv.N * (pv.N - 1), k, d_result, stream);
 }
 
 pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N, float rn,
@@ -346,6 +396,28 @@ pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_
 
 // Device-side frontier compaction; *d_error_out (device) is nonzero when a
 // look-back wait gave up.
+// Edges of one query of a batch from its pair view (same order and values as
+// build_edges_device on the query's own pair arrays).
+pump_status_t build_edges_pairs(Ctx *ctx, const PairView &pv, float rn, long long max_edges,
+                                int *d_src, int *d_dst, float *d_copt, float *d_topt,
+                                int *d_go_start, long long *h_num_edges, cudaStream_t stream) {
+  const int N = pv.N;
+  const long long npairs = (long long)N * (N - 1);
+  TileScratch ts{};
+  PUMP_TRY(run_compact(ctx, npairs, PairEdgePred{pv, rn},
+                       PairEdgeEmit{pv, max_edges, d_src, d_dst, d_copt, d_topt}, stream, &ts));
+  unsigned long long total = 0;
+  PUMP_TRY(finish_compact(ts, &total, stream));
+  *h_num_edges = (long long)total;
+  if ((long long)total > max_edges)
+    return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", total, max_edges);
+  if (d_go_start) {
+    go_start_kernel<<<grid_for(N + 1, 256), 256, 0, stream>>>(d_src, (long long)total, N, d_go_start);
+    PUMP_TRY(launch_status("go_start_kernel"));
+  }
+  return PUMP_OK;
+}
+
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                       int *d_count, int **d_error_out, cudaStream_t stream) {
   TileScratch ts{};

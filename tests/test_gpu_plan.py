@@ -101,22 +101,36 @@ def fill_problem(L, q, keep):
 
 def test_plan_batch_equals_single_queries(gpu, pumplib):
     """Concurrent queries (pump_plan_batch, 4 workers) give exactly what each
-    query gives alone."""
+    query gives alone: Halton queries of both BVP modes go through the batch's
+    shared roadmaps, the query with explicit samples plans on its own."""
     torch, ctx = gpu
     from pump_gb300 import workloads
     L = pumplib.load()
-    qs = workloads.batch_queries(10, seed=77, n_range=(200, 900), obs_range=(5, 30))
+    qs = workloads.batch_queries(12, seed=77, n_range=(200, 900), obs_range=(5, 30))
     keep = []
     pbs = (pumplib.Problem * len(qs))(*[fill_problem(pumplib, q, keep) for q in qs])
+    for k in range(len(qs)):
+        if k % 2:
+            pbs[k].bvp_mode = pumplib.PUMP_BVP_PRECISION
+    rng = np.random.default_rng(5)
+    own = rng.uniform(workloads.LO, workloads.HI, size=(pbs[3].N, 6)).astype(np.float32)
+    own[0], own[-1] = qs[3]["init"], qs[3]["goal"]
+    keep.append(own)
+    pbs[3].samples = own.ctypes.data
     res = (pumplib.PlanResult * len(qs))()
     paths = [np.zeros((400, 6), np.float32) for _ in qs]
     for k in range(len(qs)):
         res[k].path, res[k].path_cap = paths[k].ctypes.data, 400
     sts = (C.c_int * len(qs))()
     pumplib.check(L.pump_plan_batch(0, pbs, res, sts, len(qs), 4))
+    f32 = lambda x: np.float32(x).view(np.uint32)
     for k, q in enumerate(qs):
         st1, r1, p1, _ = run_plan(pumplib, ctx, pbs[k])
         assert sts[k] == st1
-        assert (res[k].num_paths, res[k].success, res[k].soln_path_idx) == (r1.num_paths, r1.success,
-                                                                            r1.soln_path_idx)
+        assert f32(res[k].rn) == f32(r1.rn)
+        assert (res[k].num_edges, res[k].iterations, res[k].num_paths, res[k].success,
+                res[k].soln_path_idx) == (r1.num_edges, r1.iterations, r1.num_paths, r1.success,
+                                          r1.soln_path_idx)
+        assert list(res[k].wavefront_sizes) == list(r1.wavefront_sizes)
+        assert f32(res[k].soln_cp) == f32(r1.soln_cp) and f32(res[k].soln_cost) == f32(r1.soln_cost)
         assert np.array_equal(paths[k][: res[k].path_len].view(np.uint32), p1.view(np.uint32))
