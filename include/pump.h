@@ -236,6 +236,13 @@ typedef struct pump_plan_result {
   long long wf_trace_len;
   /* bytes copied host->device and device->host by this query */
   long long h2d_bytes, d2h_bytes;
+  /* caller buffer (may be NULL): the reference's discretisation for the
+   * controller (PUMP.cu:553-579, the rows of discretizedPath.txt) at dt 0.05
+   * along the final smoothing iterate; ctrl_len is the row count even when
+   * it exceeds ctrl_cap (then the first ctrl_cap rows are written) */
+  float *ctrl_path;
+  int ctrl_cap;
+  int ctrl_len;
 } pump_plan_result;
 
 /* Fills a problem with the reference's defaults (mainPUMP.cu:51-72). */

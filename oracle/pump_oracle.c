@@ -713,6 +713,33 @@ static int cmp_cost_idx(const void *a, const void *b) {
   return (x->idx > y->idx) - (x->idx < y->idx);
 }
 
+int orc_control_path(const float *xs, int n, float *out, int cap) {
+  const float controlDt = 0.05f;
+  int rows = 1;
+  for (int i = 0; i < n - 1; ++i) {
+    float tau = orc_topt_bisection(&xs[i * ORC_DIM], &xs[(i + 1) * ORC_DIM], 2, NULL);
+    rows = (int)((float)rows + (tau / controlDt + 1));  /* PUMP.cu:556-560: int += float */
+  }
+  if (out && cap > 0) memset(out, 0, sizeof(float) * ORC_DIM * (size_t)cap);
+  float *seg = NULL;
+  int segCap = 0, cur = 0;
+  for (int i = 0; i < n - 1; ++i) {
+    float tau = orc_topt_bisection(&xs[i * ORC_DIM], &xs[(i + 1) * ORC_DIM], 2, NULL);
+    int nw = (int)(tau / controlDt + 1);
+    if (nw + 1 > segCap) {
+      segCap = nw + 1;
+      seg = (float *)realloc(seg, sizeof(float) * ORC_DIM * (size_t)segCap);
+    }
+    orc_find_discretized_path(seg, &xs[i * ORC_DIM], &xs[(i + 1) * ORC_DIM], nw);
+    for (int r = 0; r <= nw; ++r)
+      if (cur + r < cap && out)
+        memcpy(&out[(size_t)(cur + r) * ORC_DIM], &seg[(size_t)r * ORC_DIM], sizeof(float) * ORC_DIM);
+    cur += nw;
+  }
+  free(seg);
+  return rows;
+}
+
 int orc_plan(const orc_problem *pb, orc_result *res) {
   const int N = pb->N, numDisc = pb->numDisc, W = numDisc + 1, P = pb->P, Pmc = pb->Pmc;
   const int nobs = pb->numObs;
@@ -962,6 +989,8 @@ int orc_plan(const orc_problem *pb, orc_result *res) {
   /* smoothing (PUMP.cu:406-545) */
   float lastCP = solnPathCP, lastCost = solnPathCost;
   int lastLen = pathLength;
+  /* xsSmooth of PUMP.cu:411: zeros unless a smoothing iterate was computed */
+  float *xsFinal = (float *)calloc((size_t)ORC_DIM * (pathNumSamples > 0 ? pathNumSamples : 1), sizeof(float));
   float *lastPath = (float *)malloc(sizeof(float) * ORC_DIM * (Tcap + 2));
   if (pathLength > 0) memcpy(lastPath, splitPath, sizeof(float) * ORC_DIM * pathLength);
   if (success && status == 0) {
@@ -994,6 +1023,7 @@ int orc_plan(const orc_problem *pb, orc_result *res) {
       for (int it = 0; it < maxSmoothItrs; ++it) {
         for (int i = 0; i < pathNumSamples * ORC_DIM; ++i)
           xsSmooth[i] = (1 - alpha) * xs[i] + alpha * xsOpt[i];
+        memcpy(xsFinal, xsSmooth, sizeof(float) * ORC_DIM * pathNumSamples);
         int sLen = 0;
         float sCost = 0;
         orc_find_optimal_path(dt, smoothPath, Tcap, xsSmooth, pathNumSamples, &sLen);
@@ -1035,6 +1065,10 @@ int orc_plan(const orc_problem *pb, orc_result *res) {
       for (int k = 0; k < n && k < res->nodes_cap; ++k) res->nodes[k] = nodes[k];
   }
   res->status = status;
+  res->ctrlLen = 0;
+  if (status != 1) /* with maxPathCount hit the reference returns before this */
+    res->ctrlLen = orc_control_path(xsFinal, pathNumSamples, res->ctrl_path, res->ctrl_path ? res->ctrl_cap : 0);
+  free(xsFinal);
 
   free(samples); free(src); free(dst); free(coptE); free(toptE); free(disc); free(h);
   free(goStart); free(isFreeS); free(isFreeE); free(as); free(bs);

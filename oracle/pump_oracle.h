@@ -165,7 +165,18 @@ typedef struct orc_result {
   int *wf_trace;
   long long wf_trace_cap;
   long long wf_trace_len;
+  /* controller discretisation of the final smoothing iterate (PUMP.cu:553-569) */
+  float *ctrl_path;      /* capacity ctrl_cap states x 6 */
+  int ctrl_cap;
+  int ctrlLen;           /* rows the reference writes to discretizedPath.txt */
 } orc_result;
+
+/* The reference's discretisation for the controller (PUMP.cu:553-569): for
+ * each segment of the n node states xs, tau = toptBisection(.., 2) gives
+ * (int)(tau/0.05 + 1) intervals and findDiscretizedPath (tmax 5) fills them;
+ * the row count is accumulated as the reference does (an int += float).
+ * Writes min(rows, cap) rows to out (unwritten rows zero) and returns rows. */
+int orc_control_path(const float *xs, int n, float *out, int cap);
 
 /* Runs roadmap build, online checks, exploration, solution search and
  * smoothing exactly as the reference's main() and PUMP() do. */

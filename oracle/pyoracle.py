@@ -67,6 +67,7 @@ class Result(C.Structure):
         ("path_cap", C.c_int), ("nodes", C.c_void_p), ("nodes_cap", C.c_int),
         ("numNodes", C.c_int), ("wavefront_sizes", C.c_void_p), ("wf_trace", C.c_void_p),
         ("wf_trace_cap", C.c_longlong), ("wf_trace_len", C.c_longlong),
+        ("ctrl_path", C.c_void_p), ("ctrl_cap", C.c_int), ("ctrlLen", C.c_int),
     ]
 
 
@@ -274,9 +275,12 @@ def plan(N, obstacles, init, goal, lo, hi, offsetMult, cpTarget, cpFactor, numDi
     res.nodes, res.nodes_cap = nodes.ctypes.data, 64
     res.wavefront_sizes = wfs.ctypes.data
     res.wf_trace, res.wf_trace_cap = (trace.ctypes.data, trace_cap) if trace_cap else (None, 0)
+    ctrl = np.zeros((4096, 6), np.float32)
+    res.ctrl_path, res.ctrl_cap = ctrl.ctypes.data, ctrl.shape[0]
     lib().orc_plan(C.byref(pb), C.byref(res))
     out = {k: getattr(res, k) for k, _ in Result._fields_ if not k.endswith(("cap",)) and k not in (
-        "path", "nodes", "wavefront_sizes", "wf_trace")}
+        "path", "nodes", "wavefront_sizes", "wf_trace", "ctrl_path")}
+    out["ctrl_path"] = ctrl[: min(res.ctrlLen, ctrl.shape[0])].copy()
     out["path"] = path[: res.pathLen].copy()
     out["nodes"] = nodes[: res.numNodes].copy()
     out["wavefront_sizes"] = wfs[: res.itrs].copy()

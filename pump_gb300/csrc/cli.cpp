@@ -6,7 +6,9 @@
 // flags after the three positional arguments: --num N, --disc D (edge
 // discretisation), --particles P (HSMC particles), --precision (closed-form
 // binary64 BVP instead of the reference's bisection), --seed S.
-// Writes path.txt like PUMP.cu:591-594 when a solution is found.
+// Writes path.txt like PUMP.cu:591-594 when a solution is found and
+// discretizedPath.txt like PUMP.cu:571-579 whenever the search ran, and
+// prints the reference's final summary lines (PUMP.cu:582-604).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -46,17 +48,34 @@ int main(int argc, char **argv) {
   }
   std::vector<float> path((size_t)pb.table_rows * PUMP_DIM);
   std::vector<int> nodes(64);
+  std::vector<float> ctrl((size_t)8192 * PUMP_DIM);
   pump_plan_result res;
   std::memset(&res, 0, sizeof res);
   res.path = path.data();
   res.path_cap = pb.table_rows;
   res.nodes = nodes.data();
   res.nodes_cap = (int)nodes.size();
+  res.ctrl_path = ctrl.data();
+  res.ctrl_cap = 8192;
   st = pump_plan(ctx, &pb, &res, nullptr);
+  if (st == PUMP_OK || st == PUMP_ERR_NO_SOLUTION) {
+    if (res.ctrl_len > res.ctrl_cap) {  // rare: plan again with room for every row
+      ctrl.assign((size_t)res.ctrl_len * PUMP_DIM, 0.0f);
+      res.ctrl_path = ctrl.data();
+      res.ctrl_cap = res.ctrl_len;
+      st = pump_plan(ctx, &pb, &res, nullptr);
+    }
+    std::ofstream cs("discretizedPath.txt");
+    for (int i = 0; i < res.ctrl_len * PUMP_DIM; ++i) {
+      cs << ctrl[i] << ", ";
+      if ((i + 1) % PUMP_DIM == 0) cs << std::endl;
+    }
+  }
   std::cout << "number of goal paths found = " << res.goal_paths << " with a total number of paths = "
             << res.num_paths << " of " << res.num_considered << std::endl;
   std::cout << "****************** Final output ******************" << std::endl;
   if (st == PUMP_OK && res.success) {
+    std::cout << "Search took: " << res.ms_search / 1000 << " s" << std::endl;
     std::cout << "Solution path = " << res.soln_path_idx << " with cp = " << res.soln_cp
               << " and cost = " << res.soln_cost << std::endl;
     std::cout << "nodes = [";

@@ -147,6 +147,7 @@ class Planner {
   pump_status_t online();
   pump_status_t explore();
   pump_status_t search_and_smooth();
+  pump_status_t control_path(const std::vector<float> &xs);
   pump_status_t dense_paths(const std::vector<std::vector<float>> &xs, float dt, float tmax,
                             DensePaths &out, DevBuf<float> &d_states);
   pump_status_t topts_of(const std::vector<float> &x0, const std::vector<float> &x1, float tmax,
@@ -704,7 +705,9 @@ pump_status_t Planner::search_and_smooth() {
   if (res_->nodes)
     for (int k = 0; k < (int)nodes.size() && k < res_->nodes_cap; ++k) res_->nodes[k] = nodes[k];
 
-  // smoothing (PUMP.cu:406-545)
+  // smoothing (PUMP.cu:406-545); xsFinal is the reference's xsSmooth after
+  // the loop: the last iterate evaluated, zeros if smoothing did not run
+  std::vector<float> xsFinal(xs.size(), 0.0f);
   std::vector<float> bestPath;
   int bestLen = last >= 0 ? dp.len[last] : 0;
   if (last >= 0 && bestLen > 0) {
@@ -783,6 +786,7 @@ pump_status_t Planner::search_and_smooth() {
         if (cp < 0)
           return set_error(PUMP_ERR_CAPACITY, "smoothed path of %d states exceeds the %d-row particle table",
                            sp.len[k], pb_.table_rows);
+        xsFinal = cand[k];
         if (cp < cpTarget) alphaL = alpha;
         if (cp >= cpTarget) alphaU = alpha;
         alpha = (alphaL + alphaU) / 2;
@@ -811,7 +815,69 @@ pump_status_t Planner::search_and_smooth() {
   if (success && res_->path)
     std::memcpy(res_->path, bestPath.data(),
                 sizeof(float) * kDim * (size_t)std::min(bestLen, res_->path_cap));
+  PUMP_TRY(control_path(xsFinal));
   return success ? PUMP_OK : set_error(PUMP_ERR_NO_SOLUTION, "no goal path meets the CP target");
+}
+
+// Discretisation for the controller, PUMP.cu:553-569: per segment of the n
+// node states, tau = toptBisection(.., 2) sets (int)(tau/0.05 + 1) intervals
+// that findDiscretizedPath (tmax 5, 2pBVP.cu:53-69) fills; the row count is
+// accumulated as the reference does (an int += float), so trailing rows the
+// segments do not reach stay zero.
+pump_status_t Planner::control_path(const std::vector<float> &xs) {
+  const int n = (int)(xs.size() / kDim);
+  const float controlDt = 0.05f;
+  std::vector<float> a0, a1, tau2, topt5;
+  for (int i = 0; i + 1 < n; ++i) {
+    a0.insert(a0.end(), &xs[(size_t)i * kDim], &xs[(size_t)(i + 1) * kDim]);
+    a1.insert(a1.end(), &xs[(size_t)(i + 1) * kDim], &xs[(size_t)(i + 2) * kDim]);
+  }
+  PUMP_TRY(topts_of(a0, a1, 2.0f, &tau2, nullptr));
+  PUMP_TRY(topts_of(a0, a1, 5.0f, &topt5, nullptr));
+  int rows = 1;
+  for (int i = 0; i + 1 < n; ++i) rows = (int)((float)rows + (tau2[i] / controlDt + 1));
+  std::vector<float> out((size_t)rows * kDim, 0.0f);
+  std::vector<int> seg, row;
+  std::vector<float> ts;
+  int cur = 0;
+  for (int i = 0; i + 1 < n; ++i) {
+    const int nw = (int)(tau2[i] / controlDt + 1);
+    const float dt = topt5[i] / nw;
+    if (cur + nw >= rows)
+      return set_error(PUMP_ERR_CAPACITY, "control path: %d rows past %d", cur + nw + 1, rows);
+    std::memcpy(&out[(size_t)cur * kDim], &xs[(size_t)i * kDim], sizeof(float) * kDim);
+    for (int r = 1; r < nw; ++r) {
+      seg.push_back(i);
+      row.push_back(cur + r);
+      ts.push_back(dt * r);
+    }
+    cur += nw;
+    if (i + 2 == n)
+      std::memcpy(&out[(size_t)cur * kDim], &xs[(size_t)(i + 1) * kDim], sizeof(float) * kDim);
+  }
+  const int total = (int)seg.size();
+  if (total > 0) {
+    DevBuf<float> d_out;
+    PUMP_TRY(d_out.alloc((size_t)total * kDim));
+    PUMP_TRY(d_xs_.alloc(xs.size()));
+    PUMP_TRY(d_ts_.alloc(total));
+    PUMP_TRY(d_tau_.alloc(topt5.size()));
+    PUMP_TRY(d_seg_.alloc(total));
+    PUMP_TRY(h2d(d_xs_.p, xs.data(), xs.size()));
+    PUMP_TRY(h2d(d_ts_.p, ts.data(), total));
+    PUMP_TRY(h2d(d_tau_.p, topt5.data(), topt5.size()));
+    PUMP_TRY(h2d(d_seg_.p, seg.data(), total));
+    PUMP_TRY(bvp_path_states(d_xs_.p, d_seg_.p, d_ts_.p, d_tau_.p, total, d_out.p, s_));
+    std::vector<float> pts((size_t)total * kDim);
+    PUMP_TRY(d2h(pts.data(), d_out.p, pts.size()));
+    PUMP_TRY(sync());
+    for (int k = 0; k < total; ++k)
+      std::memcpy(&out[(size_t)row[k] * kDim], &pts[(size_t)k * kDim], sizeof(float) * kDim);
+  }
+  res_->ctrl_len = rows;
+  if (res_->ctrl_path && res_->ctrl_cap > 0)
+    std::memcpy(res_->ctrl_path, out.data(), sizeof(float) * kDim * (size_t)std::min(rows, res_->ctrl_cap));
+  return PUMP_OK;
 }
 
 }  // namespace
@@ -834,7 +900,11 @@ pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *
   int nodes_cap = res->nodes_cap;
   int *trace = res->wf_trace;
   long long trace_cap = res->wf_trace_cap;
+  float *ctrl = res->ctrl_path;
+  int ctrl_cap = res->ctrl_cap;
   std::memset(res, 0, sizeof *res);
+  res->ctrl_path = ctrl;
+  res->ctrl_cap = ctrl ? ctrl_cap : 0;
   res->path = path;
   res->path_cap = path_cap;
   res->nodes = nodes;

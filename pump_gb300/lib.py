@@ -63,6 +63,7 @@ class PlanResult(C.Structure):
         ("ms_search", C.c_double), ("ms_total", C.c_double), ("wavefront_sizes", i32 * 32),
         ("wf_trace", vp), ("wf_trace_cap", i64), ("wf_trace_len", i64),
         ("h2d_bytes", i64), ("d2h_bytes", i64),
+        ("ctrl_path", vp), ("ctrl_cap", i32), ("ctrl_len", i32),
     ]
 
 

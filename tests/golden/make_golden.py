@@ -121,6 +121,9 @@ def case(name, N, input_path, cp, eta, full, roadmap=True):
                 nodes[int(mm.group(1))] = [int(x) for x in mm.group(3).split(",")]
             g["soln_nodes"] = np.asarray(nodes[int(g["soln_idx"])][::-1], np.int32)
             g["path_txt"] = np.array(open(os.path.join(d, "path.txt")).read())
+        ctrl = os.path.join(d, "discretizedPath.txt")
+        if os.path.exists(ctrl):
+            g["ctrl_txt"] = np.array(open(ctrl).read())
         np.savez_compressed(os.path.join(OUT, name + ".npz"), **g)
         meta = {k: (v.tolist() if v.size < 8 else "array%s" % (v.shape,)) for k, v in g.items()}
         print(name, json.dumps(meta)[:400])

@@ -1,7 +1,8 @@
 """Whole planning queries on the GPU (pump_plan) against the reference's own
 results recorded in the golden fixtures: exploration wavefront sizes, stored
 and considered path counts, goal paths, the chosen solution, its node
-sequence, its printed CP and cost, and path.txt byte for byte."""
+sequence, its printed CP and cost, and path.txt and discretizedPath.txt byte
+for byte."""
 import ctypes as C
 
 import numpy as np
@@ -36,7 +37,10 @@ def run_plan(L, ctx, pb, rows=400):
     nodes = np.zeros(64, np.int32)
     res.path, res.path_cap = path.ctypes.data, rows
     res.nodes, res.nodes_cap = nodes.ctypes.data, 64
+    ctrl = np.zeros((4096, 6), np.float32)
+    res.ctrl_path, res.ctrl_cap = ctrl.ctypes.data, 4096
     st = L.load().pump_plan(ctx.handle, C.byref(pb), C.byref(res), None)
+    run_plan.ctrl = ctrl[: min(res.ctrl_len, 4096)].copy()
     return st, res, path[: res.path_len].copy(), nodes[: res.num_nodes].copy()
 
 
@@ -62,6 +66,8 @@ def test_plan_matches_reference(name, gpu, pumplib, goldens):
         assert "%g" % res.soln_cost == "%g" % float(g["soln_cost_printed"])
         text = "".join("".join("%g " % v for v in row) + "\n" for row in path.astype(np.float64))
         assert text == str(g["path_txt"])
+    ctrl = "".join("".join("%g, " % v for v in row) + "\n" for row in run_plan.ctrl.astype(np.float64))
+    assert ctrl == str(g["ctrl_txt"])
 
 
 def test_plan_matches_oracle_cfg0(gpu, pumplib, oracle):
@@ -83,6 +89,8 @@ def test_plan_matches_oracle_cfg0(gpu, pumplib, oracle):
     assert np.array_equal(path.view(np.uint32), r["path"].view(np.uint32))
     assert np.float32(res.soln_cp) == np.float32(r["solnCP"])
     assert np.float32(res.soln_cost) == np.float32(r["solnCost"])
+    assert res.ctrl_len == len(r["ctrl_path"])
+    assert np.array_equal(run_plan.ctrl.view(np.uint32), r["ctrl_path"].view(np.uint32))
 
 
 def fill_problem(L, q, keep):

@@ -86,6 +86,10 @@ def test_waypoints_masks_halfspaces(name, oracle, goldens, roadmaps):
     assert np.array_equal(a[::stride][:n].view(np.uint32), sub_a[:n].view(np.uint32))
 
 
+def ctrl_text(rows):
+    return "".join("".join("%g, " % v for v in row) + "\n" for row in np.asarray(rows, np.float64))
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_whole_query(name, oracle, goldens):
     """Exploration trace, stored paths and the returned path (PUMP.cu:3-607)."""
@@ -110,3 +114,5 @@ def test_whole_query(name, oracle, goldens):
         # path.txt as the reference prints it (printArray: "%g " per value)
         text = "".join("".join("%g " % v for v in row) + "\n" for row in r["path"].astype(np.float64))
         assert text == str(g["path_txt"])
+    # discretizedPath.txt (PUMP.cu:553-579: "%g, " per value, 6 per line)
+    assert ctrl_text(r["ctrl_path"]) == str(g["ctrl_txt"])
