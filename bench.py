@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--mode", default="precision", choices=["precision", "parity"])
     ap.add_argument("--particles", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-refine", action="store_true", help="skip the path-refinement workload")
     ap.add_argument("--batch", type=int, default=256, help="queries of the batched workload (0: skip)")
     ap.add_argument("--workers", type=int, default=0, help="batched-mode workers (0: host cores)")
     return ap.parse_args()
@@ -214,6 +215,117 @@ def measure_queries(args, lib, L, ctx):
             "plain_queries_per_s": ok_p / t_plain, "batched_queries_per_s": ok_b / t_batch,
             "batched_over_plain": (ok_b / t_batch) / (ok_p / t_plain) if ok_p else None,
             "plain_s": t_plain, "batched_s": t_batch, "identical_results": bool(same)}
+
+
+def measure_refine(args, lib, L, ctx, torch):
+    """Path refinement over 1024 returned paths (8-40 nodes each) on a
+    config-1-style indoor map (40 boxes, noise multiplier 2e-3): the paths are
+    the returned paths of 64 planning queries (N=1000, random free init/goal),
+    each resampled at 16 node counts; lambda log-uniform in [0.1, 100].
+    Times one objective+adjoint launch over all paths and the 30-step
+    descent (a captured CUDA graph), then judges every refined path with the
+    Monte Carlo CP over 4096 particles: accepted only if CP <= 0.01 and its
+    cost drops."""
+    from pump_gb300 import workloads
+    rng = np.random.Generator(np.random.MT19937(3000))
+    obs = workloads.indoor(1001).astype(np.float32)
+    nq = 64
+    pbs = (lib.Problem * nq)()
+    for k in range(nq):
+        pb = pbs[k]
+        L.pump_problem_defaults(C.byref(pb))
+        pb.N, pb.num_obstacles, pb.obstacles = 1000, obs.shape[0], obs.ctypes.data
+        a, b = workloads.free_point(rng, obs), workloads.free_point(rng, obs)
+        for d in range(6):
+            pb.init[d], pb.goal[d] = a[d], b[d]
+            pb.lo[d], pb.hi[d] = workloads.LO[d], workloads.HI[d]
+        pb.offset_mult, pb.cp_target, pb.cp_factor, pb.bvp_mode = 2e-3, 0.01, 2.0, 1
+    dense = np.zeros((nq, 400, 6), np.float32)
+    res = (lib.PlanResult * nq)()
+    for k in range(nq):
+        res[k].path, res[k].path_cap = dense[k].ctypes.data, 400
+    sts = (C.c_int * nq)()
+    lib.check(L.pump_plan_batch(0, pbs, res, sts, nq, os.cpu_count() or 4))
+    src = [dense[k][:res[k].path_len] for k in range(nq) if sts[k] == lib.PUMP_OK and res[k].path_len >= 8]
+    rows, offs, cnts = [], [], []
+    total = 0
+    for q in range(1024):
+        d = src[q % len(src)]
+        n = int(rng.integers(8, min(40, d.shape[0]) + 1))
+        idx = np.round(np.linspace(0, d.shape[0] - 1, n)).astype(int)
+        rows.append(d[idx])
+        offs.append(total)
+        cnts.append(n)
+        total += n
+    nodes = np.concatenate(rows).astype(np.float32)
+    offs, cnts = np.asarray(offs, np.int32), np.asarray(cnts, np.int32)
+    lam = np.exp(rng.uniform(np.log(0.1), np.log(100.0), 1024)).astype(np.float32)
+
+    def dev(x):
+        return torch.from_numpy(np.ascontiguousarray(x).copy()).cuda()
+    keep = [dev(nodes), dev(offs), dev(cnts), dev(lam), dev(obs)]
+    var = torch.empty(400, dtype=torch.float64, device="cuda")
+    lib.check(L.pump_position_variance(400, var.data_ptr(), None))
+    a = lib.RefineArgs()
+    a.d_nodes, a.n_nodes = keep[0].data_ptr(), nodes.shape[0]
+    a.d_node_offset, a.d_node_count, a.n_paths = keep[1].data_ptr(), keep[2].data_ptr(), 1024
+    a.d_lambda, a.W, a.tmax = keep[3].data_ptr(), 8, 5.0
+    a.d_obstacles, a.num_obstacles, a.offset_mult = keep[4].data_ptr(), obs.shape[0], 2e-3
+    a.d_pos_var, a.T_rows, a.dt, a.sigma_floor = var.data_ptr(), 400, 0.05, 1e-3
+    grad = torch.empty(nodes.size, dtype=torch.float32, device="cuda")
+    J = torch.empty(1024, dtype=torch.float32, device="cuda")
+    out = torch.empty(nodes.size, dtype=torch.float32, device="cuda")
+    Jo = torch.empty(1024, dtype=torch.float32, device="cuda")
+
+    def event_ms(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ts = []
+        for _ in range(reps):
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+    sh = torch.cuda.current_stream().cuda_stream
+    t_bwd = event_ms(lambda: lib.check(L.pump_refine_bwd(C.byref(a), grad.data_ptr(), J.data_ptr(), sh)), 10)
+    iters = 30
+    t_desc = event_ms(lambda: lib.check(L.pump_refine_paths(ctx.handle, C.byref(a), iters, out.data_ptr(),
+                                                             Jo.data_ptr(), sh)), 5)
+    torch.cuda.synchronize()
+    J0, J1 = J.cpu().numpy(), Jo.cpu().numpy()
+    refined = out.cpu().numpy().reshape(-1, 6)
+    table = torch.empty(400 * 4096 * 3, dtype=torch.float32, device="cuda")
+    lib.check(L.pump_particle_tables(0x9E3779B97F4A7C15, 4096, 400, table.data_ptr(), None, None))
+    torch.cuda.synchronize()
+
+    def judge(x):
+        cp, cost, ln = (np.zeros(1024, t) for t in (np.float32, np.float32, np.int32))
+        lib.check(L.pump_path_cp(ctx.handle, np.ascontiguousarray(x).ctypes.data, offs.ctypes.data,
+                                 cnts.ctypes.data, 1024, 1, table.data_ptr(), 4096, 400, 2e-3,
+                                 keep[4].data_ptr(), obs.shape[0], cp.ctypes.data, cost.ctypes.data,
+                                 ln.ctypes.data, None))
+        return cp, cost
+    t0 = time.perf_counter()
+    cp0, c0 = judge(nodes)
+    cp1, c1 = judge(refined)
+    t_judge = (time.perf_counter() - t0) / 2
+    valid0 = (cp0 >= 0) & (cp0 <= 0.01)
+    acc = valid0 & (cp1 >= 0) & (cp1 <= 0.01) & (c1 < c0)
+    terms = int(np.sum(cnts - 1)) * 8 * obs.shape[0]
+    return {"workload": "refine1024: 1024 returned paths x 8-40 nodes, indoor map (40 boxes), "
+                        "noise 2e-3, lambda log-uniform [0.1, 100], 8 waypoints per segment",
+            "objective_adjoint_ms": t_bwd, "paths_per_s": 1024 / (t_bwd / 1e3),
+            "waypoint_box_terms_per_s": terms / (t_bwd / 1e3),
+            "descent_iters": iters, "descent_ms": t_desc,
+            "J_reduction_median": float(np.median(1 - J1 / J0)),
+            "judge_ms": t_judge * 1e3, "judge_particles": 4096,
+            "paths_meeting_target_before": int(valid0.sum()),
+            "accepted": int(acc.sum()),
+            "cost_reduction_median_accepted": float(np.median(1 - c1[acc] / c0[acc])) if acc.any() else None}
 
 
 def run_ours(args):
@@ -425,6 +537,8 @@ def run_ours(args):
         out["roofline"] = roofline(dom, ks, N, E, M_total, W, maxHS, P, args.mode, fp64.value)
         if args.batch > 0:
             out["queries_per_s"] = measure_queries(args, lib, L, ctx)
+        if not args.no_refine:
+            out["refine"] = measure_refine(args, lib, L, ctx, torch)
         if not args.no_cpu_baseline:
             v, _dt, det = cpu_query(args, 0)
             out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port",

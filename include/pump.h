@@ -190,6 +190,82 @@ pump_status_t pump_probe_fp64_tflops(double *h_tflops, pump_stream_t stream);
 pump_status_t pump_frontier_compact_noalloc(const uint8_t *d_flags, int N, int *d_active,
                                             int *d_count, pump_stream_t stream);
 
+/* ------------------------------------------------------ path refinement */
+/* Gradient refinement of returned paths, the slot of the reference's
+ * alpha-bisection smoothing (PUMP.cu:406-545); no counterpart function in
+ * the reference.  For a path of n node states x_0 .. x_{n-1} the objective is
+ *   J = sum_i c(tau_i; x_i, x_{i+1}) + lambda * B
+ * with c the 2pBVP cost (2pBVP.cu:97-107) at its optimal time tau_i on
+ * (0, tmax] (the closed-form binary64 minimiser of the precision mode) and B
+ * a smoothed half-space bound of the collision probability: over the
+ * waypoints at s = k/W (k < W) of every segment (the cubic of pathPoint,
+ * 2pBVP.cu:117-131) and over every box, the sum of
+ * Phi(-d / (offset_mult * sigma(T))), where d is the distance from the
+ * waypoint to the box's closest point measured perpendicular to the
+ * waypoint's velocity (the half-space of cacheHalfspaces, hsmc.cu:70-96,
+ * without its distance gate and slot limit) and sigma^2(T) the closed-loop
+ * position variance per axis at the waypoint's time T (linear between steps
+ * of dt, the last row beyond the table) plus sigma_floor^2.  The gradient is
+ * taken with respect to the intermediate nodes x_1 .. x_{n-2}; tau_i enters
+ * through the implicit function theorem (dtau/dx = -c'_x / c''_tau; zero
+ * when tau_i = tmax).  Arithmetic: binary64 for tau_i, binary32 elsewhere. */
+enum { PUMP_REFINE_MAX_NODES = 257, PUMP_REFINE_MAX_W = 64, PUMP_REFINE_MAX_OBSTACLES = 8192 };
+
+typedef struct pump_refine_args {
+  const float *d_nodes;       /* node states of all paths, 6 floats each */
+  int n_nodes;                /* rows of d_nodes */
+  const int *d_node_offset;   /* first node row of path k */
+  const int *d_node_count;    /* nodes of path k, 2 .. PUMP_REFINE_MAX_NODES */
+  int n_paths;
+  const float *d_lambda;      /* bound weight per path */
+  int W;                      /* waypoints per segment, 1 .. PUMP_REFINE_MAX_W */
+  float tmax;                 /* optimal-time bracket (0, tmax] */
+  const float *d_obstacles;   /* num_obstacles x 12 (lo[6], hi[6]) */
+  int num_obstacles;          /* 0 .. PUMP_REFINE_MAX_OBSTACLES */
+  float offset_mult;          /* position error multiplier (input file line 5) */
+  const double *d_pos_var;    /* per-axis position variance per step (pump_position_variance) */
+  int T_rows;
+  float dt;                   /* table step, 0.05 s */
+  float sigma_floor;          /* added to sigma in quadrature (the variance is 0 at T = 0) */
+} pump_refine_args;
+
+/* Per-axis position variance of the particle model's closed loop at steps
+ * 0 .. T-1 (the covariance of the tracking error behind
+ * pump_particle_tables), propagated in binary64 on the device. */
+pump_status_t pump_position_variance(int T, double *d_var, pump_stream_t stream);
+
+/* J, the cost sum and B per path (any output may be NULL). */
+pump_status_t pump_refine_fwd(const pump_refine_args *a, float *d_J, float *d_cost, float *d_bound,
+                              pump_stream_t stream);
+
+/* dJ/dx for every node row of every path (rows of x_0 and x_{n-1} are 0),
+ * and J (may be NULL). */
+pump_status_t pump_refine_bwd(const pump_refine_args *a, float *d_grad, float *d_J,
+                              pump_stream_t stream);
+
+/* `iters` steps of gradient descent with a backtracking (Armijo) step per
+ * path, starting from a->d_nodes (not modified) and writing the refined
+ * nodes to d_nodes_out (same layout) and their J to d_J (may be NULL).  The
+ * loop of 2 launches per step is captured once into a CUDA graph kept in
+ * ctx and replayed while the arguments stay the same. */
+pump_status_t pump_refine_paths(pump_ctx *ctx, const pump_refine_args *a, int iters,
+                                float *d_nodes_out, float *d_J, pump_stream_t stream);
+
+/* Candidate paths given by node states, evaluated as the reference evaluates
+ * each goal candidate and smoothing iterate (PUMP.cu:370-385, 492-502), all
+ * at once: the dense path at dt = 0.05 of findOptimalPath (2pBVP.cu:5-36;
+ * optimal times by toptBisection with tmax 5, or the precision mode), its MC
+ * CP over the time-major particle table (collisionProbability,
+ * collisionProbability.cu:4-37), and the smoothing's cost (toptBisection
+ * with tmax 2 and cost per segment, PUMP.cu:499-502).  Host node arrays;
+ * h_cp[k] = -1 when path k's dense path has more states than the table has
+ * rows.  Synchronises the stream. */
+pump_status_t pump_path_cp(pump_ctx *ctx, const float *h_nodes, const int *h_offset,
+                           const int *h_count, int n_paths, int mode, const float *d_table_t,
+                           int Pmc, int T_rows, float offset_mult, const float *d_obstacles,
+                           int num_obstacles, float *h_cp, float *h_cost, int *h_len,
+                           pump_stream_t stream);
+
 /* ---------------------------------------------------------- whole query */
 typedef struct pump_problem {
   int N;              /* samples (the reference's compile-time NUM) */
@@ -206,6 +282,9 @@ typedef struct pump_problem {
   uint64_t seed;      /* particle stream key */
   int bvp_mode;       /* PUMP_BVP_PARITY or PUMP_BVP_PRECISION */
   const float *samples; /* optional host N x 6; NULL = Halton (sampler.cu:20-41) */
+  int refine_iters;   /* > 0: refine the returned path (pump_refine_paths), accepted
+                         only if its MC CP stays <= cp_target; 0 (default) = the reference */
+  float refine_lambda; /* bound weight of the refinement (default 10) */
 } pump_problem;
 
 typedef struct pump_plan_result {
@@ -243,6 +322,10 @@ typedef struct pump_plan_result {
   float *ctrl_path;
   int ctrl_cap;
   int ctrl_len;
+  /* refinement (problem.refine_iters > 0): the refined path's MC CP and
+   * cost, and whether it replaced the returned path */
+  float refine_cp, refine_cost;
+  int refined;
 } pump_plan_result;
 
 /* Fills a problem with the reference's defaults (mainPUMP.cu:51-72). */

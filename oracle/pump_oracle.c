@@ -1078,3 +1078,277 @@ int orc_plan(const orc_problem *pb, orc_result *res) {
   free(lastPath);
   return status;
 }
+
+/* ======================================================================
+ * Path refinement objective and adjoint (binary64 checker)
+ * ==================================================================== */
+typedef struct { double A0, A1, A2, A3, A4; } quartic64;
+
+static quartic64 quartic_of(const double *x0, const double *x1) {
+  const double g = (double)ORC_G;
+  quartic64 q;
+  double dd = 0, ds = 0;
+  for (int d = 0; d < 3; ++d) {
+    const double D = x1[d] - x0[d], S = x0[3 + d] + x1[3 + d];
+    dd += D * D;
+    ds += D * S;
+  }
+  double v00 = 0, v01 = 0, v11 = 0;
+  for (int d = 3; d < 6; ++d) {
+    v00 += x0[d] * x0[d];
+    v01 += x0[d] * x1[d];
+    v11 += x1[d] * x1[d];
+  }
+  q.A0 = 12 * dd;
+  q.A1 = -12 * ds;
+  q.A2 = 4 * (v00 + v01 + v11);
+  q.A3 = 2 * g * (x0[5] - x1[5]);
+  q.A4 = 1 + g * g;
+  return q;
+}
+static double q_cost(const quartic64 *q, double t) {
+  return q->A0 / (t * t * t) + q->A1 / (t * t) + q->A2 / t + q->A3 + q->A4 * t;
+}
+static double q_Q(const quartic64 *q, double t) {
+  return q->A4 * t * t * t * t - q->A2 * t * t - 2 * q->A1 * t - 3 * q->A0;
+}
+
+double orc_tau_exact(const double *x0, const double *x1, double tmax, int *clamped) {
+  /* minima of c are the upward zero crossings of Q = t^4 c'(t); bracket them
+   * on a fine grid from Q(0) = -3 A0, bisect to the last bit, compare costs
+   * (and tmax when Q(tmax) < 0) */
+  const quartic64 q = quartic_of(x0, x1);
+  const int G = 4096;
+  double best_t = tmax, best_c = INFINITY;
+  int have = 0;
+  double ta = 0, qa = q_Q(&q, 0);
+  for (int k = 1; k <= G; ++k) {
+    const double tb = tmax * k / G, qb = q_Q(&q, tb);
+    if (qa < 0 && qb >= 0) {
+      double lo = ta, hi = tb;
+      for (int it = 0; it < 200 && hi - lo > 0; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (q_Q(&q, mid) < 0) lo = mid; else hi = mid;
+      }
+      const double t = fabs(q_Q(&q, lo)) < fabs(q_Q(&q, hi)) ? lo : hi;
+      if (t > 0) {
+        const double c = q_cost(&q, t);
+        if (!have || c < best_c) { best_c = c; best_t = t; have = 1; }
+      }
+    }
+    ta = tb;
+    qa = qb;
+  }
+  int cl = 0;
+  if (qa < 0) {
+    const double c = q_cost(&q, tmax);
+    if (!have || c < best_c) { best_c = c; best_t = tmax; cl = 1; have = 1; }
+  }
+  if (clamped) *clamped = cl;
+  return best_t;
+}
+
+void orc_position_variance(int T, double *var) {
+  double *cov = (double *)malloc(sizeof(double) * 3 * (size_t)T);
+  orc_particle_cov(T, cov);
+  for (int t = 0; t < T; ++t) var[t] = cov[3 * t];
+  free(cov);
+}
+
+/* dA/dx for the 12 inputs (x0 then x1) */
+static void quartic_grad(const double *x0, const double *x1, double dA[4][12]) {
+  const double g = (double)ORC_G;
+  memset(dA, 0, sizeof(double) * 48);
+  for (int d = 0; d < 3; ++d) {
+    const double D = x1[d] - x0[d], S = x0[3 + d] + x1[3 + d];
+    dA[0][d] = -24 * D;
+    dA[0][6 + d] = 24 * D;
+    dA[1][d] = 12 * S;
+    dA[1][6 + d] = -12 * S;
+    dA[1][3 + d] = -12 * D;
+    dA[1][9 + d] = -12 * D;
+    dA[2][3 + d] = 4 * (2 * x0[3 + d] + x1[3 + d]);
+    dA[2][9 + d] = 4 * (2 * x1[3 + d] + x0[3 + d]);
+  }
+  dA[3][5] = 2 * g;
+  dA[3][11] = -2 * g;
+}
+
+static void hermite(double s, double h[4], double gd[3]) {
+  const double s2 = s * s, s3 = s2 * s;
+  h[0] = 2 * s3 - 3 * s2 + 1;  /* h00: p0 */
+  h[1] = -2 * s3 + 3 * s2;     /* h01: p1 */
+  h[2] = s3 - 2 * s2 + s;      /* h10: tau v0 */
+  h[3] = s3 - s2;              /* h11: tau v1 */
+  gd[0] = 6 * s2 - 6 * s;      /* (p0 - p1) / tau */
+  gd[1] = 3 * s2 - 4 * s + 1;  /* v0 */
+  gd[2] = 3 * s2 - 2 * s;      /* v1 */
+}
+
+static void variance_at(const orc_refine_args *a, double T, double *V, double *dVdT) {
+  const double u = T / a->dt;
+  if (!(u < (double)(a->T_rows - 1))) {
+    *V = a->posVar[a->T_rows - 1];
+    *dVdT = 0;
+    return;
+  }
+  const int j = (int)floor(u);
+  const double f = u - j;
+  *V = a->posVar[j] + f * (a->posVar[j + 1] - a->posVar[j]);
+  *dVdT = (a->posVar[j + 1] - a->posVar[j]) / a->dt;
+}
+
+#define REFINE_EPS_V 1e-12  /* added to v.v */
+#define REFINE_EPS_D 1e-12  /* added to a.a under the square root */
+
+/* One waypoint's bound terms over all boxes; with grads, adds dB/dp, dB/dv, dB/dS. */
+static double waypoint_terms(const orc_refine_args *a, const double *p, const double *v, double S,
+                             double *gp, double *gv, double *gS) {
+  double B = 0;
+  const double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + REFINE_EPS_V;
+  for (int o = 0; o < a->numObs; ++o) {
+    const float *box = &a->obstacles[o * 12];
+    double r[3];
+    int inside[3];
+    for (int d = 0; d < 3; ++d) {
+      const double lo = box[d], hi = box[6 + d];
+      const double q = p[d] < lo ? lo : (p[d] > hi ? hi : p[d]);
+      inside[d] = (p[d] >= lo && p[d] <= hi);
+      r[d] = q - p[d];
+    }
+    const double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+    const double beta = rv / vv;
+    double av[3], aa = 0;
+    for (int d = 0; d < 3; ++d) { av[d] = r[d] - beta * v[d]; aa += av[d] * av[d]; }
+    const double dist = sqrt(aa + REFINE_EPS_D);
+    const double z = dist / S;
+    B += 0.5 * erfc(z / sqrt(2.0));
+    if (gp) {
+      const double zb = -exp(-0.5 * z * z) * 0.39894228040143267794;  /* dPhi(-z)/dz = -phi(z) */
+      const double db = zb / S;
+      *gS += -zb * z / S;
+      double abar[3], rbar[3], vbar[3];
+      for (int d = 0; d < 3; ++d) abar[d] = db * av[d] / dist;
+      const double betabar = -(abar[0] * v[0] + abar[1] * v[1] + abar[2] * v[2]);
+      for (int d = 0; d < 3; ++d) {
+        rbar[d] = abar[d] + betabar * v[d] / vv;
+        vbar[d] = -beta * abar[d] + betabar * r[d] / vv;
+      }
+      const double vvbar = -betabar * beta / vv;
+      for (int d = 0; d < 3; ++d) {
+        vbar[d] += 2 * vvbar * v[d];
+        gv[d] += vbar[d];
+        if (!inside[d]) gp[d] += -rbar[d];
+      }
+    }
+  }
+  return B;
+}
+
+static double refine_eval(const orc_refine_args *a, const double *X, int n, double lambda,
+                          double *cost_out, double *bound_out, double *grad) {
+  const int nseg = n - 1;
+  double *tau = (double *)malloc(sizeof(double) * (nseg > 0 ? nseg : 1));
+  int *clamped = (int *)malloc(sizeof(int) * (nseg > 0 ? nseg : 1));
+  double *taubar = (double *)calloc(nseg > 0 ? nseg : 1, sizeof(double));
+  double *Tbar = (double *)calloc(nseg > 0 ? nseg : 1, sizeof(double));
+  double C = 0, B = 0;
+  if (grad) memset(grad, 0, sizeof(double) * 6 * (size_t)n);
+  for (int i = 0; i < nseg; ++i) {
+    const double *x0 = &X[6 * i], *x1 = &X[6 * (i + 1)];
+    tau[i] = orc_tau_exact(x0, x1, a->tmax, &clamped[i]);
+    const quartic64 q = quartic_of(x0, x1);
+    C += q_cost(&q, tau[i]);
+    if (grad) {
+      double dA[4][12];
+      quartic_grad(x0, x1, dA);
+      const double t = tau[i];
+      for (int m = 0; m < 12; ++m) {
+        const double dc = dA[0][m] / (t * t * t) + dA[1][m] / (t * t) + dA[2][m] / t + dA[3][m];
+        grad[6 * i + m] += dc;
+      }
+    }
+  }
+  double Tstart = 0;
+  for (int i = 0; i < nseg; ++i) {
+    const double *x0 = &X[6 * i], *x1 = &X[6 * (i + 1)];
+    const double t = tau[i];
+    for (int k = 0; k < a->W; ++k) {
+      const double s = (double)k / a->W;
+      double h[4], gd[3], p[3], v[3];
+      hermite(s, h, gd);
+      for (int d = 0; d < 3; ++d) {
+        p[d] = h[0] * x0[d] + h[1] * x1[d] + t * (h[2] * x0[3 + d] + h[3] * x1[3 + d]);
+        v[d] = gd[0] * (x0[d] - x1[d]) / t + gd[1] * x0[3 + d] + gd[2] * x1[3 + d];
+      }
+      const double T = Tstart + s * t;
+      double V, dVdT;
+      variance_at(a, T, &V, &dVdT);
+      const double S = a->offsetMult * sqrt(V + a->sigmaFloor * a->sigmaFloor);
+      double gp[3] = {0, 0, 0}, gv[3] = {0, 0, 0}, gS = 0;
+      B += waypoint_terms(a, p, v, S, grad ? gp : NULL, gv, &gS);
+      if (grad) {
+        for (int d = 0; d < 3; ++d) {
+          gp[d] *= lambda;
+          gv[d] *= lambda;
+        }
+        gS *= lambda;
+        const double Vbar = gS * a->offsetMult * a->offsetMult / (2 * S);
+        const double Tb = Vbar * dVdT;
+        double tb = s * Tb;
+        Tbar[i] += Tb;
+        for (int d = 0; d < 3; ++d) {
+          grad[6 * i + d] += h[0] * gp[d] + gd[0] / t * gv[d];
+          grad[6 * (i + 1) + d] += h[1] * gp[d] - gd[0] / t * gv[d];
+          grad[6 * i + 3 + d] += t * h[2] * gp[d] + gd[1] * gv[d];
+          grad[6 * (i + 1) + 3 + d] += t * h[3] * gp[d] + gd[2] * gv[d];
+          tb += (h[2] * x0[3 + d] + h[3] * x1[3 + d]) * gp[d];
+          tb += -gd[0] * (x0[d] - x1[d]) / (t * t) * gv[d];
+        }
+        taubar[i] += tb;
+      }
+    }
+    Tstart += t;
+  }
+  if (grad) {
+    /* T_i = tau_0 + .. + tau_{i-1}: each tau_j collects Tbar of later segments */
+    double suffix = 0;
+    for (int i = nseg - 1; i >= 0; --i) {
+      taubar[i] += suffix;
+      suffix += Tbar[i];
+    }
+    for (int i = 0; i < nseg; ++i) {
+      if (clamped[i]) continue;  /* tau = tmax does not move */
+      const double *x0 = &X[6 * i], *x1 = &X[6 * (i + 1)];
+      const quartic64 q = quartic_of(x0, x1);
+      double dA[4][12];
+      quartic_grad(x0, x1, dA);
+      const double t = tau[i], t2 = t * t, t3 = t2 * t, t4 = t3 * t, t5 = t4 * t;
+      /* F = c'(t) = -3 A0/t^4 - 2 A1/t^3 - A2/t^2 + A4 = 0, dtau/dx = -F_x / F_t */
+      const double Ft = 12 * q.A0 / t5 + 6 * q.A1 / t4 + 2 * q.A2 / t3;
+      for (int m = 0; m < 12; ++m) {
+        const double Fx = -3 * dA[0][m] / t4 - 2 * dA[1][m] / t3 - dA[2][m] / t2;
+        grad[6 * i + m] += taubar[i] * (-Fx / Ft);
+      }
+    }
+    for (int d = 0; d < 6; ++d) {
+      grad[d] = 0;
+      grad[6 * (n - 1) + d] = 0;
+    }
+  }
+  if (cost_out) *cost_out = C;
+  if (bound_out) *bound_out = B;
+  free(tau); free(clamped); free(taubar); free(Tbar);
+  return C + lambda * B;
+}
+
+double orc_refine_objective(const orc_refine_args *a, const double *nodes, int n, double lambda,
+                            double *cost, double *bound) {
+  return refine_eval(a, nodes, n, lambda, cost, bound, NULL);
+}
+
+double orc_refine_grad(const orc_refine_args *a, const double *nodes, int n, double lambda,
+                       double *grad) {
+  return refine_eval(a, nodes, n, lambda, NULL, NULL, grad);
+}

@@ -182,6 +182,43 @@ int orc_control_path(const float *xs, int n, float *out, int cap);
  * smoothing exactly as the reference's main() and PUMP() do. */
 int orc_plan(const orc_problem *pb, orc_result *res);
 
+/* ---------------- path refinement objective and its adjoint (binary64) ----------------
+ * Not a function of the reference: the objective the refinement after the
+ * search minimises, defined here in binary64 as the checker of the device
+ * adjoint.  For a path of n node states x_0..x_{n-1} (6 each):
+ *   J = sum_i c(tau_i; x_i, x_{i+1}) + lambda * B
+ * c is the reference's 2pBVP cost (2pBVP.cu:97-107) and tau_i its global
+ * minimiser on (0, tmax].  B sums, over the waypoints p(s), v(s) at
+ * s = k/W (k < W) of every segment (the cubic of pathPoint, 2pBVP.cu:117-131)
+ * and over every box, Phi(-d / (offsetMult * sigma(T))): d = |a| with a the
+ * offset from the waypoint to the box's closest point minus its component
+ * along the velocity (the half-space of cacheHalfspaces, hsmc.cu:70-96,
+ * without its distance gate or slot limit), sigma^2(T) = the closed-loop
+ * position variance at the waypoint's time T = tau_0 + .. + tau_{i-1} + s tau_i
+ * (linear between steps of dt, last row beyond the table) + sigmaFloor^2. */
+typedef struct orc_refine_args {
+  int W;
+  double tmax;
+  int numObs;
+  const float *obstacles;  /* numObs x 12: lo[6], hi[6] */
+  double offsetMult;
+  const double *posVar;    /* per-axis position variance per step, T_rows */
+  int T_rows;
+  double dt;
+  double sigmaFloor;
+} orc_refine_args;
+
+/* Global minimiser of the cost on (0, tmax] in binary64; *clamped = 1 when it
+ * is tmax with the cost still decreasing there. */
+double orc_tau_exact(const double *x0, const double *x1, double tmax, int *clamped);
+/* Per-axis position variance of the particle model per step (orc_particle_cov's first entry). */
+void orc_position_variance(int T, double *var);
+double orc_refine_objective(const orc_refine_args *a, const double *nodes, int n, double lambda,
+                            double *cost, double *bound);
+/* dJ/dx for every node (rows 0 and n-1 are zero); returns J. */
+double orc_refine_grad(const orc_refine_args *a, const double *nodes, int n, double lambda,
+                       double *grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,14 @@ class Result(C.Structure):
     ]
 
 
+class RefineArgs(C.Structure):
+    _fields_ = [
+        ("W", C.c_int), ("tmax", C.c_double), ("numObs", C.c_int), ("obstacles", C.c_void_p),
+        ("offsetMult", C.c_double), ("posVar", C.c_void_p), ("T_rows", C.c_int),
+        ("dt", C.c_double), ("sigmaFloor", C.c_double),
+    ]
+
+
 def lib():
     global _lib
     with _lock:
@@ -125,6 +133,15 @@ def lib():
             L.orc_cost_exact.argtypes = [C.c_double, f32p, f32p]
             L.orc_particle_tables.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
             L.orc_particle_cov.argtypes = [C.c_int, f64p]
+            L.orc_tau_exact.restype = C.c_double
+            L.orc_tau_exact.argtypes = [f64p, f64p, C.c_double, C.POINTER(C.c_int)]
+            L.orc_position_variance.restype = None
+            L.orc_position_variance.argtypes = [C.c_int, f64p]
+            L.orc_refine_objective.restype = C.c_double
+            L.orc_refine_objective.argtypes = [C.POINTER(RefineArgs), f64p, C.c_int, C.c_double,
+                                               C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.orc_refine_grad.restype = C.c_double
+            L.orc_refine_grad.argtypes = [C.POINTER(RefineArgs), f64p, C.c_int, C.c_double, f64p]
             L.orc_plan.restype = C.c_int
             L.orc_plan.argtypes = [C.POINTER(Problem), C.POINTER(Result)]
             _lib = L
@@ -249,6 +266,27 @@ def mccp(path, T, pmajor, offsetMult, obstacles):
     return hits, cp.value
 
 
+def path_cp(nodes, pmajor, offsetMult, obstacles, dt=np.float32(0.05)):
+    """A candidate path as the reference evaluates it (PUMP.cu:370-385,
+    492-502): the dense path of findOptimalPath (tmax 5), its MC CP, and the
+    cost sum with toptBisection tmax 2.  Returns (cp, cost, dense length);
+    cp -1 when the dense path has more states than the particle table."""
+    xs = f32(nodes).reshape(-1)
+    n = xs.size // 6
+    T_table = pmajor.shape[1]
+    split = np.zeros(((T_table + 2) * 6,), np.float32)
+    ln = C.c_int(0)
+    lib().orc_find_optimal_path(dt, split, T_table, xs, n, C.byref(ln))
+    c = np.float32(0)
+    for i in range(n - 1):
+        tau, _ = topt(xs[6 * i:6 * i + 6], xs[6 * i + 6:6 * i + 12], 2.0)
+        c = np.float32(c + np.float32(cost(tau, xs[6 * i:6 * i + 6], xs[6 * i + 6:6 * i + 12])))
+    if ln.value < 0 or ln.value > T_table:
+        return -1.0, float(c), ln.value
+    _, cp = mccp(split[: ln.value * 6], ln.value, pmajor, offsetMult, obstacles)
+    return cp, float(c), ln.value
+
+
 def plan(N, obstacles, init, goal, lo, hi, offsetMult, cpTarget, cpFactor, numDisc=8, P=128,
          Pmc=2048, T_table=400, seed=DEFAULT_SEED, samples=None, trace_cap=0, tables=None):
     """Whole query as the reference's main() + PUMP(); returns a dict."""
@@ -286,3 +324,41 @@ def plan(N, obstacles, init, goal, lo, hi, offsetMult, cpTarget, cpFactor, numDi
     out["wavefront_sizes"] = wfs[: res.itrs].copy()
     out["wf_trace"] = trace[: res.wf_trace_len].copy() if trace_cap else None
     return out
+
+
+def position_variance(T):
+    """Per-axis position variance of the particle model per step (binary64)."""
+    out = np.zeros(T, np.float64)
+    lib().orc_position_variance(T, out)
+    return out
+
+
+def tau_exact(x0, x1, tmax):
+    """Global minimiser of the 2pBVP cost on (0, tmax] in binary64 and whether it is tmax."""
+    a, b = np.ascontiguousarray(x0, np.float64), np.ascontiguousarray(x1, np.float64)
+    cl = C.c_int(0)
+    t = lib().orc_tau_exact(a, b, tmax, C.byref(cl))
+    return t, bool(cl.value)
+
+
+class Refine:
+    """Path refinement objective J = cost + lambda * bound and its adjoint in
+    binary64 (see pump_oracle.h)."""
+
+    def __init__(self, obstacles, offset_mult, W=8, tmax=5.0, T_rows=400, dt=0.05, sigma_floor=1e-3):
+        self.obs = f32(obstacles).reshape(-1)
+        self.var = position_variance(T_rows)
+        self.args = RefineArgs(W, tmax, self.obs.size // 12, self.obs.ctypes.data, float(offset_mult),
+                               self.var.ctypes.data, T_rows, dt, sigma_floor)
+
+    def objective(self, nodes, lam):
+        x = np.ascontiguousarray(nodes, np.float64).reshape(-1)
+        c, b = C.c_double(0), C.c_double(0)
+        J = lib().orc_refine_objective(C.byref(self.args), x, x.size // 6, lam, C.byref(c), C.byref(b))
+        return J, c.value, b.value
+
+    def grad(self, nodes, lam):
+        x = np.ascontiguousarray(nodes, np.float64).reshape(-1)
+        g = np.zeros_like(x)
+        J = lib().orc_refine_grad(C.byref(self.args), x, x.size // 6, lam, g)
+        return J, g.reshape(-1, 6)

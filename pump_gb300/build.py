@@ -25,7 +25,7 @@ CLI = os.path.join(OUT, "pump")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # translation units not bound to the reference's roundings: contraction on
-FMAD_TRUE = {os.path.join(CSRC, "bvp_precise.cu")}
+FMAD_TRUE = {os.path.join(CSRC, "bvp_precise.cu"), os.path.join(CSRC, "refine.cu")}
 HOST_FLAGS = "-fPIC,-ffp-contract=off,-fno-fast-math,-Wall,-Wno-unused-function"
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", HOST_FLAGS,
           "-I", INCLUDE, "-I", CSRC]

@@ -41,6 +41,7 @@ Ctx::~Ctx() {
   int prev = -1;
   cudaGetDevice(&prev);
   cudaSetDevice(device_);
+  if (refine_graph.exec) cudaGraphExecDestroy(refine_graph.exec);
   for (int i = 0; i < kNumSlots; ++i)
     if (buf_[i]) cudaFree(buf_[i]);
   if (prev >= 0) cudaSetDevice(prev);
@@ -167,6 +168,8 @@ extern "C" void pump_problem_defaults(pump_problem *pb) {
   pb->cp_factor = 2.0f;
   pb->seed = 0x9E3779B97F4A7C15ull;
   pb->bvp_mode = PUMP_BVP_PARITY;
+  pb->refine_iters = 0;
+  pb->refine_lambda = 10.0f;
   pb->samples = nullptr;
 }
 

@@ -18,6 +18,7 @@ class Ctx {
     kSelect = 0,   // radix-select state + histogram
     kCompact,      // compaction tile status words
     kPlanA,        // planner buffers (see plan.cpp)
+    kRefine,       // refinement descent state (refine.cu)
     kNumSlots
   };
   explicit Ctx(int device) : device_(device) {
@@ -34,6 +35,15 @@ class Ctx {
   // shared by every context on the device (the reference loads its table
   // once per process); `stream` is ordered after its generation.
   pump_status_t particle_table(uint64_t seed, int P, int T, const float **out, cudaStream_t stream);
+
+  // The captured refinement loop of the last pump_refine_paths call, replayed
+  // while its key (arguments, iterations, output and scratch pointers) is the same.
+  struct GraphCache {
+    unsigned char key[192];
+    size_t key_len = 0;
+    cudaGraphExec_t exec = nullptr;
+  };
+  GraphCache refine_graph;
 
  private:
   int device_;

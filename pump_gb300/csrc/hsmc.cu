@@ -156,6 +156,29 @@ __global__ void __launch_bounds__(128) particle_table_kernel(const double *__res
   }
 }
 
+// Per-axis position variance of the same closed loop: S' = A S A^T + g g^T
+// with A = [[1 - H2 KP, DT - H2 KD], [-DT KP, 1 - DT KD]] and g = [H2, DT]
+// sigma_w, from S = 0 (the particles start on the path).  A sequential
+// recurrence of a few hundred steps: one thread, binary64.
+__global__ void position_variance_kernel(int T, double *__restrict__ var) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const double a00 = 1.0 - kH2 * kKP, a01 = kDT - kH2 * kKD;
+  const double a10 = -(kDT * kKP), a11 = 1.0 - kDT * kKD;
+  const double g0 = kH2 * kSigmaW, g1 = kDT * kSigmaW;
+  double spp = 0, spv = 0, svv = 0;
+  for (int t = 0; t < T; ++t) {
+    var[t] = spp;
+    const double m00 = a00 * spp + a01 * spv, m01 = a00 * spv + a01 * svv;
+    const double m10 = a10 * spp + a11 * spv, m11 = a10 * spv + a11 * svv;
+    const double npp = m00 * a00 + m01 * a01 + g0 * g0;
+    const double npv = m00 * a10 + m01 * a11 + g0 * g1;
+    const double nvv = m10 * a10 + m11 * a11 + g1 * g1;
+    spp = npp;
+    spv = npv;
+    svv = nvv;
+  }
+}
+
 // ------------------------------------------------------------------ HSMC
 // One warp per new path.  Lane l owns particles p = 32k + l (k < words), one
 // bit per particle in bits[k/32] bit (k%32), so offset loads of a k-step are
@@ -437,6 +460,12 @@ extern "C" pump_status_t pump_particle_tables(uint64_t seed, int P, int T, float
   if (P <= 0 || T <= 0 || (!d_tmajor && !d_pmajor))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_particle_tables: bad arguments");
   return particle_tables_async(seed, P, T, d_tmajor, d_pmajor, (cudaStream_t)stream);
+}
+
+extern "C" pump_status_t pump_position_variance(int T, double *d_var, pump_stream_t stream) {
+  if (T <= 0 || !d_var) return set_error(PUMP_ERR_BAD_INPUT, "pump_position_variance: bad arguments");
+  position_variance_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(T, d_var);
+  return launch_status("position_variance");
 }
 
 extern "C" pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_edge, const int *d_prev,

@@ -140,6 +140,10 @@ class Planner {
           const SharedRoadmap *shared = nullptr)
       : ctx_(ctx), pb_(pb), res_(res), s_(s), shared_(shared) {}
   pump_status_t run();
+  // CP (dense path + MC over the table), smoothing cost and dense length of
+  // explicit candidate paths (pump_path_cp).
+  pump_status_t evaluate_paths(const std::vector<std::vector<float>> &xs, const float *d_table,
+                               const float *d_obs, int nobs, float *cp, float *cost, int *len);
 
  private:
   pump_status_t roadmap();
@@ -148,6 +152,9 @@ class Planner {
   pump_status_t explore();
   pump_status_t search_and_smooth();
   pump_status_t control_path(const std::vector<float> &xs);
+  pump_status_t refine(const std::vector<float> &xs, float cpTarget, float *lastCP,
+                       float *lastCost, std::vector<float> *bestPath, int *bestLen,
+                       std::vector<float> *xsFinal);
   pump_status_t dense_paths(const std::vector<std::vector<float>> &xs, float dt, float tmax,
                             DensePaths &out, DevBuf<float> &d_states);
   pump_status_t topts_of(const std::vector<float> &x0, const std::vector<float> &x1, float tmax,
@@ -188,6 +195,7 @@ class Planner {
   DevBuf<int> d_src_, d_dst_, d_go_;
   DevBuf<float> d_coptE_, d_toptE_, d_disc_, d_as_, d_bs_;
   const float *d_table_ = nullptr;  // context-cached particle table
+  const float *obs_p_ = nullptr;    // device obstacles used by the MC CP
   DevBuf<uint8_t> d_free_s_, d_free_e_;
   long long E_ = 0;
   float rn_ = 0;
@@ -345,6 +353,7 @@ pump_status_t Planner::pair_costs_shared(long long rnIdx, long long cap) {
 pump_status_t Planner::online() {
   PUMP_TRY(d_obs_.alloc((size_t)nobs_ * 12));
   PUMP_TRY(h2d(d_obs_.p, pb_.obstacles, (size_t)nobs_ * 12));
+  obs_p_ = d_obs_.p;
   PUMP_TRY(d_free_s_.alloc(N_));
   PUMP_TRY(d_free_e_.alloc(E_));
   PUMP_TRY(pump_sample_free(d_obs_.p, nobs_, d_samples_.p, N_, d_free_s_.p, (pump_stream_t)s_));
@@ -664,7 +673,7 @@ pump_status_t Planner::mc_cp_batch(const DevBuf<float> &d_states, const DensePat
   PUMP_TRY(h2d(d_moff_.p, dp.offset.data(), n));
   PUMP_TRY(h2d(d_mlen_.p, len.data(), n));
   PUMP_TRY(mc_cp_async(d_states.p, d_moff_.p, d_mlen_.p, n, d_table_, pb_.num_mc, pb_.table_rows,
-                       pb_.offset_mult, d_obs_.p, nobs_, d_mhits_.p, d_mcp_.p, nullptr, s_));
+                       pb_.offset_mult, obs_p_, nobs_, d_mhits_.p, d_mcp_.p, nullptr, s_));
   PUMP_TRY(d2h(cp.data(), d_mcp_.p, n));
   PUMP_TRY(sync());
   for (int k = 0; k < n; ++k)
@@ -708,6 +717,7 @@ pump_status_t Planner::search_and_smooth() {
   // smoothing (PUMP.cu:406-545); xsFinal is the reference's xsSmooth after
   // the loop: the last iterate evaluated, zeros if smoothing did not run
   std::vector<float> xsFinal(xs.size(), 0.0f);
+  std::vector<float> xsBest(xs);  // nodes of the path kept so far
   std::vector<float> bestPath;
   int bestLen = last >= 0 ? dp.len[last] : 0;
   if (last >= 0 && bestLen > 0) {
@@ -800,6 +810,7 @@ pump_status_t Planner::search_and_smooth() {
           PUMP_TRY(sync());
           lastCost = smoothCost;
           lastCP = cp;
+          xsBest = cand[k];
         }
         if (std::fabs(cpTarget - cp) < epsSmoothCP && cpTarget - cp > 0) {
           stop = true;
@@ -809,6 +820,8 @@ pump_status_t Planner::search_and_smooth() {
       }
     }
   }
+  if (success && pb_.refine_iters > 0)
+    PUMP_TRY(refine(xsBest, cpTarget, &lastCP, &lastCost, &bestPath, &bestLen, &xsFinal));
   res_->soln_cp = lastCP;
   res_->soln_cost = lastCost;
   res_->path_len = success ? bestLen : 0;
@@ -817,6 +830,112 @@ pump_status_t Planner::search_and_smooth() {
                 sizeof(float) * kDim * (size_t)std::min(bestLen, res_->path_cap));
   PUMP_TRY(control_path(xsFinal));
   return success ? PUMP_OK : set_error(PUMP_ERR_NO_SOLUTION, "no goal path meets the CP target");
+}
+
+pump_status_t Planner::evaluate_paths(const std::vector<std::vector<float>> &xs,
+                                      const float *d_table, const float *d_obs, int nobs,
+                                      float *cp, float *cost, int *len) {
+  d_table_ = d_table;
+  obs_p_ = d_obs;
+  nobs_ = nobs;
+  DensePaths dp;
+  DevBuf<float> d_states;
+  PUMP_TRY(dense_paths(xs, dt_, 5.0f, dp, d_states));
+  std::vector<float> cps;
+  PUMP_TRY(mc_cp_batch(d_states, dp, cps));
+  std::vector<float> a0, a1, sc;
+  for (const auto &x : xs)
+    for (size_t i = 0; i + 1 < x.size() / kDim; ++i) {
+      a0.insert(a0.end(), &x[i * kDim], &x[(i + 1) * kDim]);
+      a1.insert(a1.end(), &x[(i + 1) * kDim], &x[(i + 2) * kDim]);
+    }
+  PUMP_TRY(topts_of(a0, a1, 2.0f, nullptr, &sc));
+  size_t q = 0;
+  for (size_t k = 0; k < xs.size(); ++k) {
+    float c = 0;
+    for (size_t i = 0; i + 1 < xs[k].size() / kDim; ++i) c += sc[q++];
+    cp[k] = cps[k];
+    cost[k] = c;
+    len[k] = dp.len[k];
+  }
+  return PUMP_OK;
+}
+
+// Gradient refinement of the kept path's nodes (pump_refine_paths), judged
+// like every candidate of the search: the dense path at dt, its MC CP over
+// the particle table and the smoothing's cost (toptBisection tmax 2 + cost
+// per segment).  Accepted only if the CP stays <= the target and the cost
+// drops; then it replaces the returned path (and feeds the controller path).
+pump_status_t Planner::refine(const std::vector<float> &xs, float cpTarget, float *lastCP,
+                              float *lastCost, std::vector<float> *bestPath, int *bestLen,
+                              std::vector<float> *xsFinal) {
+  const int n = (int)(xs.size() / kDim);
+  if (n < 3 || n > PUMP_REFINE_MAX_NODES) return PUMP_OK;
+  DevBuf<float> d_x, d_out, d_lam, d_J;
+  DevBuf<int> d_off, d_cnt;
+  DevBuf<double> d_var;
+  PUMP_TRY(d_x.alloc(xs.size()));
+  PUMP_TRY(d_out.alloc(xs.size()));
+  PUMP_TRY(d_lam.alloc(1));
+  PUMP_TRY(d_J.alloc(1));
+  PUMP_TRY(d_off.alloc(1));
+  PUMP_TRY(d_cnt.alloc(1));
+  PUMP_TRY(d_var.alloc(pb_.table_rows));
+  const int zero = 0;
+  const float lam = pb_.refine_lambda;
+  PUMP_TRY(h2d(d_x.p, xs.data(), xs.size()));
+  PUMP_TRY(h2d(d_off.p, &zero, 1));
+  PUMP_TRY(h2d(d_cnt.p, &n, 1));
+  PUMP_TRY(h2d(d_lam.p, &lam, 1));
+  PUMP_TRY(pump_position_variance(pb_.table_rows, d_var.p, (pump_stream_t)s_));
+  pump_refine_args a{};
+  a.d_nodes = d_x.p;
+  a.n_nodes = n;
+  a.d_node_offset = d_off.p;
+  a.d_node_count = d_cnt.p;
+  a.n_paths = 1;
+  a.d_lambda = d_lam.p;
+  a.W = pb_.num_disc;
+  a.tmax = 5.0f;
+  a.d_obstacles = d_obs_.p;
+  a.num_obstacles = std::min(nobs_, (int)PUMP_REFINE_MAX_OBSTACLES);
+  a.offset_mult = pb_.offset_mult;
+  a.d_pos_var = d_var.p;
+  a.T_rows = pb_.table_rows;
+  a.dt = dt_;
+  a.sigma_floor = 1e-3f;
+  PUMP_TRY(pump_refine_paths(ctx_->handle(), &a, pb_.refine_iters, d_out.p, d_J.p,
+                             (pump_stream_t)s_));
+  std::vector<float> xr(xs.size());
+  PUMP_TRY(d2h(xr.data(), d_out.p, xr.size()));
+  PUMP_TRY(sync());
+  std::vector<std::vector<float>> one(1, xr);
+  DensePaths dp;
+  DevBuf<float> d_states;
+  PUMP_TRY(dense_paths(one, dt_, 5.0f, dp, d_states));
+  std::vector<float> cps;
+  PUMP_TRY(mc_cp_batch(d_states, dp, cps));
+  std::vector<float> a0, a1, sc;
+  for (int i = 0; i + 1 < n; ++i) {
+    a0.insert(a0.end(), &xr[(size_t)i * kDim], &xr[(size_t)(i + 1) * kDim]);
+    a1.insert(a1.end(), &xr[(size_t)(i + 1) * kDim], &xr[(size_t)(i + 2) * kDim]);
+  }
+  PUMP_TRY(topts_of(a0, a1, 2.0f, nullptr, &sc));
+  float cost = 0;
+  for (int i = 0; i + 1 < n; ++i) cost += sc[i];
+  res_->refine_cp = cps[0];
+  res_->refine_cost = cost;
+  if (cps[0] >= 0 && cps[0] <= cpTarget && cost < *lastCost) {
+    res_->refined = 1;
+    *bestLen = dp.len[0];
+    bestPath->resize((size_t)dp.len[0] * kDim);
+    PUMP_TRY(d2h(bestPath->data(), d_states.p, bestPath->size()));
+    PUMP_TRY(sync());
+    *lastCP = cps[0];
+    *lastCost = cost;
+    *xsFinal = xr;
+  }
+  return PUMP_OK;
 }
 
 // Discretisation for the controller, PUMP.cu:553-569: per segment of the n
@@ -1016,6 +1135,40 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
   for (int w = 0; w < workers; ++w)
     if (setup[w] != PUMP_OK) return set_error(setup[w], "pump_plan_batch worker %d: %s", w, msgs[w].c_str());
   return PUMP_OK;
+}
+
+extern "C" pump_status_t pump_path_cp(pump_ctx *ctx, const float *h_nodes, const int *h_offset,
+                                      const int *h_count, int n_paths, int mode,
+                                      const float *d_table_t, int Pmc, int T_rows,
+                                      float offset_mult, const float *d_obstacles,
+                                      int num_obstacles, float *h_cp, float *h_cost, int *h_len,
+                                      pump_stream_t stream) {
+  if (!ctx || n_paths < 0 || (n_paths > 0 && (!h_nodes || !h_offset || !h_count || !d_table_t ||
+                                              !h_cp || !h_cost || !h_len)) ||
+      Pmc <= 0 || T_rows < 2 || num_obstacles < 0 || (num_obstacles > 0 && !d_obstacles) ||
+      (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_path_cp: bad arguments");
+  if (n_paths == 0) return PUMP_OK;
+  std::vector<std::vector<float>> xs(n_paths);
+  for (int k = 0; k < n_paths; ++k) {
+    if (h_count[k] < 1 || h_offset[k] < 0)
+      return set_error(PUMP_ERR_BAD_INPUT, "pump_path_cp: path %d has %d nodes", k, h_count[k]);
+    xs[k].assign(h_nodes + (size_t)h_offset[k] * kDim,
+                 h_nodes + (size_t)(h_offset[k] + h_count[k]) * kDim);
+  }
+  pump_problem pb;
+  pump_problem_defaults(&pb);
+  pb.bvp_mode = mode;
+  pb.num_mc = Pmc;
+  pb.table_rows = T_rows;
+  pb.offset_mult = offset_mult;
+  pump_plan_result res;
+  std::memset(&res, 0, sizeof res);
+  Ctx *c = Ctx::from(ctx);
+  PUMP_TRY(c->activate());
+  t_alloc_stream = (cudaStream_t)stream;
+  Planner pl(c, pb, &res, (cudaStream_t)stream);
+  return pl.evaluate_paths(xs, d_table_t, d_obstacles, num_obstacles, h_cp, h_cost, h_len);
 }
 
 extern "C" pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,

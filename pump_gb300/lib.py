@@ -49,7 +49,16 @@ class Problem(C.Structure):
         ("num_obstacles", i32), ("obstacles", vp),
         ("init", f32 * 6), ("goal", f32 * 6), ("lo", f32 * 6), ("hi", f32 * 6),
         ("offset_mult", f32), ("cp_target", f32), ("cp_factor", f32), ("seed", C.c_uint64),
-        ("bvp_mode", i32), ("samples", vp),
+        ("bvp_mode", i32), ("samples", vp), ("refine_iters", i32), ("refine_lambda", f32),
+    ]
+
+
+class RefineArgs(C.Structure):
+    _fields_ = [
+        ("d_nodes", vp), ("n_nodes", i32), ("d_node_offset", vp), ("d_node_count", vp),
+        ("n_paths", i32), ("d_lambda", vp), ("W", i32), ("tmax", f32), ("d_obstacles", vp),
+        ("num_obstacles", i32), ("offset_mult", f32), ("d_pos_var", vp), ("T_rows", i32),
+        ("dt", f32), ("sigma_floor", f32),
     ]
 
 
@@ -64,6 +73,7 @@ class PlanResult(C.Structure):
         ("wf_trace", vp), ("wf_trace_cap", i64), ("wf_trace_len", i64),
         ("h2d_bytes", i64), ("d2h_bytes", i64),
         ("ctrl_path", vp), ("ctrl_cap", i32), ("ctrl_len", i32),
+        ("refine_cp", f32), ("refine_cost", f32), ("refined", i32),
     ]
 
 
@@ -92,6 +102,11 @@ _SIGS = {
     "pump_read_input": (i32, [C.c_char_p, C.POINTER(Problem)]),
     "pump_plan": (i32, [vp, C.POINTER(Problem), C.POINTER(PlanResult), vp]),
     "pump_plan_batch": (i32, [i32, vp, vp, vp, i32, i32]),
+    "pump_position_variance": (i32, [i32, vp, vp]),
+    "pump_path_cp": (i32, [vp, vp, vp, vp, i32, i32, vp, i32, i32, f32, vp, i32, vp, vp, vp, vp]),
+    "pump_refine_fwd": (i32, [C.POINTER(RefineArgs), vp, vp, vp, vp]),
+    "pump_refine_bwd": (i32, [C.POINTER(RefineArgs), vp, vp, vp]),
+    "pump_refine_paths": (i32, [vp, C.POINTER(RefineArgs), i32, vp, vp, vp]),
 }
 
 

@@ -106,6 +106,30 @@ def batch_queries(n=256, seed=2000, n_range=(500, 8000), obs_range=(5, 100)):
     return out
 
 
+def perturbed_paths(n_paths, seed, obstacles, n_range=(8, 40), spread=0.05, speed=0.3):
+    """Paths for the refinement objective: node count uniform in n_range,
+    free init and goal at rest, intermediate positions on the straight line
+    plus a sin-shaped Gaussian detour of scale `spread`, velocities
+    N(0, speed^2).  Returns (nodes (rows, 6) float32, offsets, counts)."""
+    rng = np.random.Generator(np.random.MT19937(seed))
+    rows, offs, cnts = [], [], []
+    total = 0
+    for _ in range(n_paths):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        a, b = free_point(rng, obstacles), free_point(rng, obstacles)
+        s = np.linspace(0.0, 1.0, n)[:, None]
+        X = np.zeros((n, 6))
+        X[:, :3] = a[:3] * (1 - s) + b[:3] * s + rng.normal(0, spread, (n, 3)) * np.sin(np.pi * s)
+        X[:, 3:] = rng.normal(0, speed, (n, 3))
+        X[0, :3], X[-1, :3] = a[:3], b[:3]
+        X[0, 3:] = X[-1, 3:] = 0
+        rows.append(X.astype(np.float32))
+        offs.append(total)
+        cnts.append(n)
+        total += n
+    return np.concatenate(rows), np.asarray(offs, np.int32), np.asarray(cnts, np.int32)
+
+
 CONFIGS = {
     # the benchmark configurations (N, obstacles, noise, cp, eta, particles, waypoints)
     "cfg0": dict(N=1000, num_disc=9, num_hsmc=128, offset_mult=1e-3, cp=0.01, eta=2.0,

@@ -142,3 +142,23 @@ def test_plan_batch_equals_single_queries(gpu, pumplib):
         assert list(res[k].wavefront_sizes) == list(r1.wavefront_sizes)
         assert f32(res[k].soln_cp) == f32(r1.soln_cp) and f32(res[k].soln_cost) == f32(r1.soln_cost)
         assert np.array_equal(paths[k][: res[k].path_len].view(np.uint32), p1.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["ref_N1000_boxes10_noise0.3", "ref_N1000_boxes10_noise1e-3"])
+def test_plan_with_refinement(name, gpu, pumplib, goldens):
+    """Refinement after the search: accepted only with MC CP <= target and a
+    lower cost; the search itself is unchanged."""
+    torch, ctx = gpu
+    g = goldens[name]
+    pb, _obs = make_problem(pumplib, g, refine_iters=30, refine_lambda=10.0)
+    st, res, path, nodes = run_plan(pumplib, ctx, pb)
+    assert st == pumplib.PUMP_OK, pumplib.load().pump_last_error()
+    assert res.success == 1 and res.soln_path_idx == int(g["soln_idx"])
+    assert np.array_equal(nodes, g["soln_nodes"])
+    assert np.isfinite(res.refine_cost) and res.refine_cp >= 0
+    if res.refined:
+        assert res.soln_cp <= float(g["cp_target"])
+        assert res.soln_cost == np.float32(res.refine_cost)
+        assert res.soln_cost < float(g["soln_cost_printed"]) * (1 + 1e-5)
+    else:
+        assert "%g" % res.soln_cost == "%g" % float(g["soln_cost_printed"])
