@@ -441,7 +441,7 @@ def run_ours(args):
         timed("bvp_pairs", lambda: lib.check(L.pump_bvp_pairs(d_s.data_ptr(), N, 5.0, w["mode"],
                                                              d_c.data_ptr(), d_t.data_ptr(), sh)), 1)
         timed("select_rn", lambda: lib.check(L.pump_select_kth(ctx.handle, d_c.data_ptr(), npairs,
-                                                              rn_idx, C.byref(rn), sh)), 6)
+                                                              rn_idx, C.byref(rn), sh)), 7)
         timed("build_edges", lambda: lib.check(L.pump_build_edges(
             ctx.handle, d_c.data_ptr(), d_t.data_ptr(), N, rn.value, cap, d_src.data_ptr(),
             d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(), d_go.data_ptr(), C.byref(Eo), sh)), 2)

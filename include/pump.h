@@ -69,7 +69,7 @@ pump_status_t pump_ctx_destroy(pump_ctx *ctx);
  * idx = i*(N-1) + j - (i < j).
  * Replaces fillCoptsTopts (2pBVP.cu:133-150) with toptBisection
  * (2pBVP.cu:71-95) and cost (2pBVP.cu:97-107); mode PUMP_BVP_PRECISION
- * returns the binary64 minimiser of the same cost instead. */
+ * returns the binary64 minimiser of the same cost instead (N <= 65535). */
 pump_status_t pump_bvp_pairs(const float *d_samples, int N, float tmax, int mode, float *d_copts,
                              float *d_topts, pump_stream_t stream);
 

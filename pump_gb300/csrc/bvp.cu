@@ -292,38 +292,48 @@ __device__ __forceinline__ void path_point_f32(float t, float tau, const float *
   }
 }
 
-// One thread per (edge, waypoint): findDiscretizedPath, 2pBVP.cu:53-69.
+// One thread per (edge, waypoint): findDiscretizedPath, 2pBVP.cu:53-69.  A
+// block's 256 waypoints are contiguous in disc, so they are assembled in
+// shared memory and stored as whole lines.
+constexpr int kDiscThreads = 256;
+
 template <int Mode>
-__global__ void discretize_kernel(const float *__restrict__ samples, const int *__restrict__ src,
-                                  const int *__restrict__ dst, const float *__restrict__ toptE,
-                                  long long E, int numDisc, float *__restrict__ disc) {
+__global__ void __launch_bounds__(kDiscThreads) discretize_kernel(
+    const float *__restrict__ samples, const int *__restrict__ src, const int *__restrict__ dst,
+    const float *__restrict__ toptE, long long E, int numDisc, float *__restrict__ disc) {
+  __shared__ __align__(16) float s_out[kDiscThreads * kDim];
   const int W = numDisc + 1;
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (tid >= E * W) return;
-  const long long e = tid / W;
-  const int i = (int)(tid - e * W);
-  const int a = src[e], b = dst[e];
-  float x0[kDim], x1[kDim], x[kDim];
+  const long long base = blockIdx.x * (long long)kDiscThreads;
+  const long long total = E * W;
+  const int nv = (int)(total - base < kDiscThreads ? total - base : kDiscThreads);
+  const long long tid = base + threadIdx.x;
+  if (threadIdx.x < nv) {
+    const long long e = tid / W;
+    const int i = (int)(tid - e * W);
+    const int a = src[e], b = dst[e];
+    float x0[kDim], x1[kDim], x[kDim];
 #pragma unroll
-  for (int d = 0; d < kDim; ++d) {
-    x0[d] = __ldg(&samples[a * kDim + d]);
-    x1[d] = __ldg(&samples[b * kDim + d]);
+    for (int d = 0; d < kDim; ++d) {
+      x0[d] = __ldg(&samples[a * kDim + d]);
+      x1[d] = __ldg(&samples[b * kDim + d]);
+    }
+    if (i == 0) {
+#pragma unroll
+      for (int d = 0; d < kDim; ++d) x[d] = x0[d];
+    } else if (i == numDisc) {
+#pragma unroll
+      for (int d = 0; d < kDim; ++d) x[d] = x1[d];
+    } else {
+      const float topt = toptE[e];
+      const float dt = topt / numDisc;
+      if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
+      else path_point_f32(dt * i, topt, x0, x1, x);
+    }
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) s_out[threadIdx.x * kDim + d] = x[d];
   }
-  if (i == 0) {
-#pragma unroll
-    for (int d = 0; d < kDim; ++d) x[d] = x0[d];
-  } else if (i == numDisc) {
-#pragma unroll
-    for (int d = 0; d < kDim; ++d) x[d] = x1[d];
-  } else {
-    const float topt = toptE[e];
-    const float dt = topt / numDisc;
-    if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
-    else path_point_f32(dt * i, topt, x0, x1, x);
-  }
-  float *o = disc + tid * kDim;
-#pragma unroll
-  for (int d = 0; d < kDim; ++d) o[d] = x[d];
+  __syncthreads();
+  block_store(disc + base * kDim, s_out, nv * kDim);
 }
 
 // Dense path of findOptimalPath (2pBVP.cu:5-36) for one segment: the host
@@ -400,10 +410,12 @@ extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int
   if (E == 0) return PUMP_OK;
   const long long n = E * (numDisc + 1);
   if (mode == PUMP_BVP_PARITY)
-    discretize_kernel<PUMP_BVP_PARITY><<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(
+    discretize_kernel<PUMP_BVP_PARITY><<<grid_for(n, kDiscThreads), kDiscThreads, 0,
+                                         (cudaStream_t)stream>>>(
         d_samples, d_src, d_dst, d_topt, E, numDisc, d_disc);
   else
-    discretize_kernel<PUMP_BVP_PRECISION><<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
+    discretize_kernel<PUMP_BVP_PRECISION><<<grid_for(n, kDiscThreads), kDiscThreads, 0,
+                                            (cudaStream_t)stream>>>(
         d_samples, d_src, d_dst, d_topt, E, numDisc, d_disc);
   return launch_status("discretize_edges");
 }

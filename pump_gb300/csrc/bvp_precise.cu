@@ -13,31 +13,45 @@ __device__ void precise_pair(const float *x0, const float *x1, float tmax, float
                              float *cost) {
   double t, c;
   precise_tau(x0, x1, tmax, &t, &c);
-  *topt = (float)t;
-  *cost = (float)c;
+  *topt = d2f_rn(t);
+  *cost = d2f_rn(c);
 }
 
-__global__ void __launch_bounds__(128) bvp_pairs_precision_kernel(const float *__restrict__ samples,
+__global__ void prepare_samples_kernel(const float *__restrict__ samples, int N,
+                                       SampleF *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  float x[kDim];
+#pragma unroll
+  for (int d = 0; d < kDim; ++d) x[d] = samples[i * kDim + d];
+  out[i] = to_sample_f(x);
+}
+
+__device__ __forceinline__ SampleF load_sample(const SampleF *__restrict__ s, int i) {
+  const float4 *q = reinterpret_cast<const float4 *>(s + i);
+  const float4 a = __ldg(q), b = __ldg(q + 1);
+  SampleF r;
+  r.p[0] = a.x; r.p[1] = a.y; r.p[2] = a.z;
+  r.v[0] = a.w; r.v[1] = b.x; r.v[2] = b.y;
+  r.vv.h = b.z; r.vv.l = b.w;
+  return r;
+}
+
+// Row i = blockIdx.y, column r = blockIdx.x * 128 + threadIdx.x (j = r, or
+// r + 1 past the diagonal): no index division per pair.
+__global__ void __launch_bounds__(128) bvp_pairs_precision_kernel(const SampleF *__restrict__ sf,
                                                                   int N, float tmax,
                                                                   float *__restrict__ copts,
                                                                   float *__restrict__ topts) {
-  const long long npairs = (long long)N * (N - 1);
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < npairs;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(idx / (N - 1));
-    const int r = (int)(idx - (long long)i * (N - 1));
-    const int j = r + (r >= i);
-    float x0[kDim], x1[kDim];
-#pragma unroll
-    for (int d = 0; d < kDim; ++d) {
-      x0[d] = __ldg(&samples[i * kDim + d]);
-      x1[d] = __ldg(&samples[j * kDim + d]);
-    }
-    float tp, cp;
-    precise_pair(x0, x1, tmax, &tp, &cp);
-    topts[idx] = tp;
-    copts[idx] = cp;
-  }
+  const int i = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= N - 1) return;
+  const int j = r + (r >= i);
+  double t, c;
+  precise_tau(load_sample(sf, i), load_sample(sf, j), tmax, &t, &c);
+  const long long idx = (long long)i * (N - 1) + r;
+  topts[idx] = d2f_rn(t);
+  copts[idx] = d2f_rn(c);
 }
 
 __global__ void bvp_batch_precision_kernel(const float *__restrict__ x0s,
@@ -61,12 +75,18 @@ __global__ void bvp_batch_precision_kernel(const float *__restrict__ x0s,
 
 pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tmax, float *d_copts,
                                          float *d_topts, cudaStream_t stream) {
-  const long long npairs = (long long)N * (N - 1);
-  long long blocks = (npairs + 127) / 128;
-  if (blocks > 2147483647LL) blocks = 2147483647LL;
-  bvp_pairs_precision_kernel<<<(unsigned)blocks, 128, 0, stream>>>(d_samples, N, tmax, d_copts,
-                                                                    d_topts);
-  return launch_status("bvp_pairs_precision");
+  if (N > 65535) return set_error(PUMP_ERR_CAPACITY, "bvp_pairs: N = %d exceeds 65535 rows", N);
+  const dim3 grid(grid_for(N - 1, 128), (unsigned)N);
+  SampleF *sd = nullptr;
+  PUMP_CUDA_TRY(cudaMallocAsync((void **)&sd, sizeof(SampleF) * (size_t)N, stream));
+  prepare_samples_kernel<<<grid_for(N, 128), 128, 0, stream>>>(d_samples, N, sd);
+  pump_status_t st = launch_status("prepare_samples");
+  if (st == PUMP_OK) {
+    bvp_pairs_precision_kernel<<<grid, 128, 0, stream>>>(sd, N, tmax, d_copts, d_topts);
+    st = launch_status("bvp_pairs_precision");
+  }
+  cudaFreeAsync(sd, stream);
+  return st;
 }
 
 pump_status_t bvp_batch_precision_launch(const float *d_x0, const float *d_x1, int n, float tmax,

@@ -62,6 +62,71 @@ __global__ void __launch_bounds__(256) free_edges_kernel(const float *__restrict
   is_free[e] = ok ? 1 : 0;
 }
 
+// freeEdges for a block of 128 consecutive edges whose waypoints (contiguous
+// in disc) are staged in shared memory.  Each thread first drops the boxes
+// that are broadphase-disjoint from its edge's bounding box (up to
+// kFilterObs boxes, one bit each; no filter if a waypoint is NaN), then runs
+// the reference's per-segment tests over the remaining boxes in index order.
+constexpr int kFeThreads = 128;
+constexpr int kFilterObs = 128;
+
+__global__ void __launch_bounds__(kFeThreads) free_edges_staged_kernel(
+    const float *__restrict__ obs, int numObs, const float *__restrict__ disc, long long E,
+    int numDisc, uint8_t *__restrict__ is_free) {
+  extern __shared__ float4 s_dyn4[];
+  float *s_obs = reinterpret_cast<float *>(s_dyn4);
+  float *s_wp = s_obs + ((numObs * 12 + 3) & ~3);
+  stage_obstacles(obs, numObs, s_obs);
+  const int W = numDisc + 1;
+  const long long e0 = blockIdx.x * (long long)kFeThreads;
+  const int nv = (int)(E - e0 < kFeThreads ? E - e0 : kFeThreads);
+  block_load(s_wp, disc + e0 * W * kDim, nv * W * kDim);
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t >= nv) return;
+  const float *wp = s_wp + t * W * kDim;
+  bool ok = true;
+  float v[3], w[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) v[d] = wp[d];
+  if (numObs <= kFilterObs) {
+    float emin[3], emax[3];
+    bool nan = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
+    for (int i = 0; i < W; ++i)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float x = wp[i * kDim + d];
+        nan = nan || x != x;
+        emin[d] = fminf(emin[d], x);
+        emax[d] = fmaxf(emax[d], x);
+      }
+    uint32_t mask[kFilterObs / 32];
+    const int words = (numObs + 31) / 32;
+#pragma unroll
+    for (int k = 0; k < kFilterObs / 32; ++k) mask[k] = 0;
+    for (int o = 0; o < numObs; ++o)
+      if (nan || !broadphase_valid(emin, emax, &s_obs[o * 12])) mask[o >> 5] |= 1u << (o & 31);
+    for (int i = 0; i < numDisc && ok; ++i) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kDim + d];
+      ok = segment_valid_masked(v, w, mask, words, s_obs);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v[d] = w[d];
+    }
+  } else {
+    for (int i = 0; i < numDisc && ok; ++i) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kDim + d];
+      ok = segment_valid(v, w, numObs, s_obs);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v[d] = w[d];
+    }
+  }
+  is_free[e0 + t] = ok ? 1 : 0;
+}
+
 // One thread per waypoint: setupAsBs (hsmc.cu:201-211) fused with
 // cacheHalfspaces (hsmc.cu:10-99); unused slots get the defaults a = -1,
 // b = 1111.
@@ -131,6 +196,93 @@ __global__ void __launch_bounds__(256) halfspace_kernel(const float *__restrict_
   if (count) count[wp] = stored;
 }
 
+// The same computation for a block of 256 consecutive waypoints, staged in
+// shared memory: the block's waypoints (contiguous in disc) are loaded and
+// its half-spaces (contiguous in as / bs) stored as whole lines.  Used when
+// maxHS <= kStagedMaxHS and the stage fits in shared memory.
+constexpr int kStagedMaxHS = 8;
+constexpr int kHsThreads = 256;
+
+__global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
+    const float *__restrict__ obs, int numObs, const float *__restrict__ disc,
+    const uint8_t *__restrict__ is_free_edge, long long E, int W, int maxHS, float maxd2,
+    float *__restrict__ as, float *__restrict__ bs, int *__restrict__ count) {
+  extern __shared__ float4 s_dyn4[];
+  float *s_obs = reinterpret_cast<float *>(s_dyn4);
+  float *s_wp = s_obs + ((numObs * 12 + 3) & ~3);
+  float *s_a = s_wp + kHsThreads * kDim;
+  float *s_b = s_a + kHsThreads * maxHS * 3;
+  stage_obstacles(obs, numObs, s_obs);
+  const long long wp0 = blockIdx.x * (long long)kHsThreads;
+  const long long total = E * W;
+  const int nv = (int)(total - wp0 < kHsThreads ? total - wp0 : kHsThreads);
+  block_load(s_wp, disc + wp0 * kDim, nv * kDim);
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < nv) {
+    const long long wp = wp0 + t;
+    float *a = s_a + t * maxHS * 3, *b = s_b + t * maxHS;
+    int stored = 0;
+    if (is_free_edge[wp / W]) {
+      float pos[3], vel[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        pos[d] = s_wp[t * kDim + d];
+        vel[d] = s_wp[t * kDim + 3 + d];
+      }
+      for (int o = 0; o < numObs && stored < maxHS; ++o) {
+        const float *l = &s_obs[o * 12], *u = l + 6;
+        float x[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {  // bvlsShortcut, bvls.cu:259-273
+          if (pos[d] <= l[d]) x[d] = l[d];
+          else if (pos[d] >= u[d]) x[d] = u[d];
+          else x[d] = pos[d];
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) x[d] = x[d] - pos[d];
+        float d2 = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) d2 += x[d] * x[d];
+        if (d2 > maxd2) continue;
+        float xdotv = 0, vdotv = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          xdotv += x[d] * vel[d];
+          vdotv += vel[d] * vel[d];
+        }
+        if (vdotv == 0) vdotv = (float)1e-5;
+        const float dotratio = xdotv / vdotv;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) x[d] = x[d] - dotratio * vel[d];
+        float xdotx = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          a[stored * 3 + d] = x[d];
+          xdotx += x[d] * x[d];
+        }
+        b[stored] = xdotx;
+        ++stored;
+      }
+    }
+    for (int h = stored; h < maxHS; ++h) {
+      a[h * 3 + 0] = -1.0f;
+      a[h * 3 + 1] = -1.0f;
+      a[h * 3 + 2] = -1.0f;
+      b[h] = 1111.0f;
+    }
+    if (count) count[wp] = stored;
+  }
+  __syncthreads();
+  block_store(as + wp0 * maxHS * 3, s_a, nv * maxHS * 3);
+  block_store(bs + wp0 * maxHS, s_b, nv * maxHS);
+}
+
+size_t halfspace_staged_smem(int numObs, int maxHS) {
+  return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)kHsThreads * kDim +
+                          (size_t)kHsThreads * maxHS * 4);
+}
+
 pump_status_t obstacle_smem(int numObs, size_t *bytes) {
   *bytes = (size_t)numObs * 12 * sizeof(float);
   if (*bytes > 200 * 1024)
@@ -172,6 +324,14 @@ extern "C" pump_status_t pump_free_edges(const float *d_obstacles, int numObs, c
   if (E == 0) return PUMP_OK;
   size_t smem;
   PUMP_TRY(obstacle_smem(numObs, &smem));
+  const size_t staged = sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) +
+                                         (size_t)kFeThreads * (numDisc + 1) * kDim);
+  if (staged <= 220 * 1024) {
+    PUMP_TRY(set_smem_attr((const void *)free_edges_staged_kernel, staged));
+    free_edges_staged_kernel<<<grid_for(E, kFeThreads), kFeThreads, staged, (cudaStream_t)stream>>>(
+        d_obstacles, numObs, d_disc, E, numDisc, d_is_free);
+    return launch_status("free_edges");
+  }
   PUMP_TRY(set_smem_attr((const void *)free_edges_kernel, smem));
   free_edges_kernel<<<grid_for(E, 256), 256, smem, (cudaStream_t)stream>>>(d_obstacles, numObs,
                                                                          d_disc, E, numDisc,
@@ -194,6 +354,13 @@ extern "C" pump_status_t pump_cache_halfspaces(const float *d_obstacles, int num
   }
   size_t smem;
   PUMP_TRY(obstacle_smem(numObs, &smem));
+  const size_t staged = halfspace_staged_smem(numObs, maxHS);
+  if (maxHS <= kStagedMaxHS && staged <= 220 * 1024) {
+    PUMP_TRY(set_smem_attr((const void *)halfspace_staged_kernel, staged));
+    halfspace_staged_kernel<<<grid_for(E * W, kHsThreads), kHsThreads, staged, (cudaStream_t)stream>>>(
+        d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, d_count);
+    return launch_status("cache_halfspaces");
+  }
   PUMP_TRY(set_smem_attr((const void *)halfspace_kernel, smem));
   halfspace_kernel<<<grid_for(E * W, 256), 256, smem, (cudaStream_t)stream>>>(
       d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, d_count);

@@ -69,4 +69,29 @@ __device__ __forceinline__ bool segment_valid(const float *v, const float *w, in
   return true;
 }
 
+// isMotionValid over the boxes whose bits are set in mask (box o is bit
+// o % 32 of mask[o / 32]), in index order.  A box that is broadphase-disjoint
+// from the whole edge's bounding box is disjoint from every segment's, so
+// dropping it from the mask beforehand leaves the result unchanged.
+__device__ __forceinline__ bool segment_valid_masked(const float *v, const float *w,
+                                                     const uint32_t *mask, int words,
+                                                     const float *s_obs) {
+  float bbMin[3], bbMax[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (v[d] > w[d]) { bbMin[d] = w[d]; bbMax[d] = v[d]; }
+    else { bbMin[d] = v[d]; bbMax[d] = w[d]; }
+  }
+  for (int k = 0; k < words; ++k) {
+    uint32_t m = mask[k];
+    while (m) {
+      const int o = k * 32 + __ffs(m) - 1;
+      m &= m - 1;
+      const float *ob = &s_obs[o * 12];
+      if (!broadphase_valid(bbMin, bbMax, ob) && !motion_valid(v, w, ob)) return false;
+    }
+  }
+  return true;
+}
+
 }  // namespace pump

@@ -48,6 +48,29 @@ __host__ __device__ __forceinline__ double p2f(float x) { double d = x; return d
 __host__ __device__ __forceinline__ double p3f(float x) { double d = x; return (d * d) * d; }
 __host__ __device__ __forceinline__ double p4f(float x) { double d = x; double s = d * d; return s * s; }
 
+// Block-wide contiguous copies between global and shared memory: 16-byte
+// accesses when the global address and the count allow, so a block's
+// per-thread records (strided, uncoalesced when each thread stores its own)
+// move as whole 128-byte lines.  Callers synchronise around them.
+__device__ __forceinline__ void block_store(float *__restrict__ dst, const float *src, int n) {
+  if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0 && (n & 3) == 0) {
+    float4 *d4 = reinterpret_cast<float4 *>(dst);
+    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+    for (int i = threadIdx.x; i < n / 4; i += blockDim.x) d4[i] = s4[i];
+  } else {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  }
+}
+__device__ __forceinline__ void block_load(float *dst, const float *__restrict__ src, int n) {
+  if ((reinterpret_cast<uintptr_t>(src) & 15) == 0 && (n & 3) == 0) {
+    float4 *d4 = reinterpret_cast<float4 *>(dst);
+    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+    for (int i = threadIdx.x; i < n / 4; i += blockDim.x) d4[i] = __ldg(&s4[i]);
+  } else {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = __ldg(&src[i]);
+  }
+}
+
 // `const float g = -9.81;` (2pBVP.cu:3)
 #define PUMP_G ((float)-9.81)
 

@@ -83,6 +83,19 @@ __global__ void select_hist_kernel(Src src, long long n, const SelectState *__re
     if (sh[b]) atomicAdd(&hist[b], sh[b]);
 }
 
+// Start state of a selection and a cleared histogram (a kernel instead of a
+// host-to-device copy: a copy from pageable host memory would wait for the
+// stream to drain first).
+__global__ void select_init_kernel(SelectState *st, unsigned long long k, unsigned int *hist) {
+  for (int i = threadIdx.x; i < 2048; i += blockDim.x) hist[i] = 0u;
+  if (threadIdx.x == 0) {
+    st->prefix = 0u;
+    st->mask = 0u;
+    st->k = k;
+    st->result = 0.0f;
+  }
+}
+
 // One block of 1024 threads: find the bin holding rank k, narrow the prefix,
 // clear the histogram for the next pass.
 __global__ void select_pick_kernel(SelectState *st, int shift, int bits, unsigned int *hist) {
@@ -345,9 +358,8 @@ pump_status_t select_kth_src(Ctx *ctx, Src src, long long n, long long k, const 
   PUMP_TRY(ctx->scratch(Ctx::kSelect, bytes, (void **)&scratch));
   SelectState *st = (SelectState *)scratch;
   unsigned int *hist = (unsigned int *)(scratch + sizeof(SelectState));
-  SelectState init{0u, 0u, (unsigned long long)k, 0.0f};
-  PUMP_CUDA_TRY(cudaMemcpyAsync(st, &init, sizeof init, cudaMemcpyHostToDevice, stream));
-  PUMP_CUDA_TRY(cudaMemsetAsync(hist, 0, 2048 * sizeof(unsigned int), stream));
+  select_init_kernel<<<1, 1024, 0, stream>>>(st, (unsigned long long)k, hist);
+  PUMP_TRY(launch_status("select_init_kernel"));
   long long blocks = (n + 1023) / 1024;
   if (blocks > kNumSMs * 8) blocks = kNumSMs * 8;
   const int shifts[3] = {21, 10, 0}, bits[3] = {11, 11, 10};
