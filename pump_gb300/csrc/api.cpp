@@ -82,6 +82,35 @@ pump_status_t Ctx::particle_table(uint64_t seed, int P, int T, const float **out
   return PUMP_OK;
 }
 
+cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t stream) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, stream);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      e = cudaMemPoolCreate(&pools[dev], &props);
+      if (e != cudaSuccess) {
+        pools[dev] = nullptr;
+        return e;
+      }
+      unsigned long long keep = ~0ull;
+      e = cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+      if (e != cudaSuccess) return e;
+    }
+    pool = pools[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, stream);
+}
+
 pump_status_t Ctx::activate() { return cuda_status(cudaSetDevice(device_), "cudaSetDevice"); }
 
 pump_status_t Ctx::scratch(int slot, size_t bytes, void **out) {

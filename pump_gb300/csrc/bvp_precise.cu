@@ -78,7 +78,7 @@ pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tm
   if (N > 65535) return set_error(PUMP_ERR_CAPACITY, "bvp_pairs: N = %d exceeds 65535 rows", N);
   const dim3 grid(grid_for(N - 1, 128), (unsigned)N);
   SampleF *sd = nullptr;
-  PUMP_CUDA_TRY(cudaMallocAsync((void **)&sd, sizeof(SampleF) * (size_t)N, stream));
+  PUMP_CUDA_TRY(pool_malloc_async((void **)&sd, sizeof(SampleF) * (size_t)N, stream));
   prepare_samples_kernel<<<grid_for(N, 128), 128, 0, stream>>>(d_samples, N, sd);
   pump_status_t st = launch_status("prepare_samples");
   if (st == PUMP_OK) {

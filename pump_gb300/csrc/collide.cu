@@ -198,16 +198,28 @@ __global__ void __launch_bounds__(256) halfspace_kernel(const float *__restrict_
 
 // The same computation for a block of 256 consecutive waypoints, staged in
 // shared memory: the block's waypoints (contiguous in disc) are loaded and
-// its half-spaces (contiguous in as / bs) stored as whole lines.  Used when
-// maxHS <= kStagedMaxHS and the stage fits in shared memory.
+// its half-spaces (contiguous in as / bs) stored as whole lines.  Before the
+// waypoints run, the boxes that cannot pass the distance gate anywhere on an
+// edge are dropped once per edge: if for some axis the gap g between the
+// edge's bounding box and the box has fl(g * g) > maxd2, every waypoint's
+// d2 (a rounded sum of non-negative squares, each at least as large by the
+// monotonicity of rounding) exceeds maxd2 as well.  Edges with a NaN
+// waypoint, or maps with more than kFilterObs boxes, are not filtered.  The
+// remaining boxes are visited in index order, so the first maxHS half-spaces
+// are the reference's.  Used when maxHS <= kStagedMaxHS and the stage fits in
+// shared memory.
 constexpr int kStagedMaxHS = 8;
 constexpr int kHsThreads = 256;
+constexpr int kHsMaxEdges = kHsThreads / 2 + 2;  // W >= 2
 
 __global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
     const float *__restrict__ obs, int numObs, const float *__restrict__ disc,
     const uint8_t *__restrict__ is_free_edge, long long E, int W, int maxHS, float maxd2,
     float *__restrict__ as, float *__restrict__ bs, int *__restrict__ count) {
   extern __shared__ float4 s_dyn4[];
+  __shared__ float s_eb[kHsMaxEdges][6];  // edge bounding box: min[3], max[3]
+  __shared__ uint32_t s_mask[kHsMaxEdges][kFilterObs / 32];
+  __shared__ uint8_t s_filter[kHsMaxEdges];  // 1: free edge whose boxes are filtered
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   float *s_wp = s_obs + ((numObs * 12 + 3) & ~3);
   float *s_a = s_wp + kHsThreads * kDim;
@@ -216,11 +228,57 @@ __global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
   const long long wp0 = blockIdx.x * (long long)kHsThreads;
   const long long total = E * W;
   const int nv = (int)(total - wp0 < kHsThreads ? total - wp0 : kHsThreads);
-  block_load(s_wp, disc + wp0 * kDim, nv * kDim);
-  __syncthreads();
+  const long long e0 = wp0 / W;
+  const int ne = (int)((wp0 + nv - 1) / W - e0) + 1;
   const int t = threadIdx.x;
+  block_load(s_wp, disc + wp0 * kDim, nv * kDim);
+  const bool filter = numObs <= kFilterObs;
+  if (t < ne) {
+    const long long e = e0 + t;
+    bool use = filter && is_free_edge[e];
+    float mn[3], mx[3];
+    const float *w = disc + e * W * kDim;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) mn[d] = mx[d] = __ldg(&w[d]);
+    for (int i = 0; i < W; ++i)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float x = __ldg(&w[i * kDim + d]);
+        use = use && x == x;
+        mn[d] = fminf(mn[d], x);
+        mx[d] = fmaxf(mx[d], x);
+      }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      s_eb[t][d] = mn[d];
+      s_eb[t][3 + d] = mx[d];
+    }
+    s_filter[t] = use;
+#pragma unroll
+    for (int k = 0; k < kFilterObs / 32; ++k) s_mask[t][k] = 0u;
+  }
+  __syncthreads();
+  if (filter) {
+    // (edge, box) pairs of the block: keep the boxes the gate can pass
+    for (int q = t; q < ne * numObs; q += kHsThreads) {
+      const int el = q / numObs, o = q - el * numObs;
+      if (!s_filter[el]) continue;
+      const float *l = &s_obs[o * 12], *u = l + 6;
+      bool keep = true;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float above = l[d] - s_eb[el][3 + d];  // box beyond the edge's max
+        const float below = u[d] - s_eb[el][d];      // box below the edge's min
+        if (above > 0.0f && above * above > maxd2) keep = false;
+        if (below < 0.0f && below * below > maxd2) keep = false;
+      }
+      if (keep) atomicOr(&s_mask[el][o >> 5], 1u << (o & 31));
+    }
+  }
+  __syncthreads();
   if (t < nv) {
     const long long wp = wp0 + t;
+    const int el = (int)(wp / W - e0);
     float *a = s_a + t * maxHS * 3, *b = s_b + t * maxHS;
     int stored = 0;
     if (is_free_edge[wp / W]) {
@@ -230,7 +288,21 @@ __global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
         pos[d] = s_wp[t * kDim + d];
         vel[d] = s_wp[t * kDim + 3 + d];
       }
-      for (int o = 0; o < numObs && stored < maxHS; ++o) {
+      const bool filt = s_filter[el];
+      const int words = filt ? (numObs + 31) / 32 : 0;
+      int o = -1;
+      uint32_t m = 0u;
+      int k = 0;
+      while (stored < maxHS) {
+        // next box in index order: from the edge's mask, or every box
+        if (filt) {
+          while (m == 0u && k < words) m = s_mask[el][k++];
+          if (m == 0u) break;
+          o = (k - 1) * 32 + __ffs(m) - 1;
+          m &= m - 1;
+        } else {
+          if (++o >= numObs) break;
+        }
         const float *l = &s_obs[o * 12], *u = l + 6;
         float x[3];
 #pragma unroll

@@ -22,6 +22,10 @@ pump_status_t set_error(pump_status_t s, const char *fmt, ...);
 pump_status_t cuda_status(cudaError_t e, const char *where);
 // cuda_status(cudaGetLastError()) after a launch.
 pump_status_t launch_status(const char *kernel);
+// Stream-ordered allocation from the library's pool on the current device
+// (freed with cudaFreeAsync); the pool keeps freed memory for reuse instead
+// of returning it to the driver at every synchronisation.
+cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t stream);
 
 #define PUMP_CUDA_TRY(expr)                                     \
   do {                                                          \

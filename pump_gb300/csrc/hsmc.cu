@@ -438,7 +438,7 @@ pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n,
 pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
                                     cudaStream_t stream) {
   double *z = nullptr;
-  PUMP_CUDA_TRY(cudaMallocAsync((void **)&z, sizeof(double) * 3 * (size_t)P * T, stream));
+  PUMP_CUDA_TRY(pool_malloc_async((void **)&z, sizeof(double) * 3 * (size_t)P * T, stream));
   particle_gauss_kernel<<<grid_for((long long)P * T, 256), 256, 0, stream>>>(
       (uint32_t)seed, (uint32_t)(seed >> 32), P, T, z);
   pump_status_t st = launch_status("particle_gauss_kernel");

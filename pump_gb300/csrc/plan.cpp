@@ -76,7 +76,7 @@ struct DevBuf {
     p = nullptr;
     n = 0;
     s = t_alloc_stream;
-    PUMP_CUDA_TRY(cudaMallocAsync((void **)&p, sizeof(T) * (count ? count : 1), s));
+    PUMP_CUDA_TRY(pool_malloc_async((void **)&p, sizeof(T) * (count ? count : 1), s));
     n = count;
     return PUMP_OK;
   }

@@ -142,22 +142,35 @@ struct TileScratch {
   int *error;                  // 1 = look-back wait gave up
 };
 
-// Exclusive prefix of this tile from its predecessors' status words.
-__device__ unsigned long long lookback(const TileScratch &ts, long long tile, unsigned long long agg,
-                                       bool *timed_out) {
+// Exclusive prefix of this tile from its predecessors' status words, read by
+// a whole warp: lane l reads the status of tile p - l, so one round trip to L2
+// covers 32 predecessors.  The lanes up to the nearest inclusive prefix must
+// all have published (at least an aggregate); otherwise the warp waits and
+// reads the window again.  Called by every lane of one warp; every lane
+// returns the same value.
+__device__ unsigned long long lookback_warp(const TileScratch &ts, long long tile,
+                                            unsigned long long agg, bool *timed_out) {
   using ref_t = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
+  const int lane = threadIdx.x & 31;
   if (tile == 0) {
-    ref_t(ts.status[0]).store(kFlagPrefix | agg, cuda::memory_order_release);
+    if (lane == 0) ref_t(ts.status[0]).store(kFlagPrefix | agg, cuda::memory_order_release);
     return 0;
   }
-  ref_t(ts.status[tile]).store(kFlagAggregate | agg, cuda::memory_order_release);
+  if (lane == 0) ref_t(ts.status[tile]).store(kFlagAggregate | agg, cuda::memory_order_release);
   unsigned long long excl = 0;
-  long long p = tile - 1;
+  long long p = tile - 1;  // nearest tile of the window
   long long spins = 0;
-  while (p >= 0) {
-    const unsigned long long s = ref_t(ts.status[p]).load(cuda::memory_order_acquire);
-    const unsigned long long flag = s & ~kValueMask;
-    if (flag == 0) {
+  while (true) {
+    const long long q = p - lane;
+    // before tile 0 the prefix is 0 (a published prefix of value 0)
+    const unsigned long long st =
+        q >= 0 ? ref_t(ts.status[q]).load(cuda::memory_order_acquire) : kFlagPrefix;
+    const unsigned long long flag = st & ~kValueMask;
+    const unsigned int pref = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
+    const unsigned int none = __ballot_sync(0xffffffffu, flag == 0);
+    const int stop = pref ? __ffs(pref) - 1 : 31;  // last lane needed in this window
+    const unsigned int need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
+    if (none & need) {
       if (++spins > kSpinLimit) {
         *timed_out = true;
         return 0;
@@ -165,11 +178,14 @@ __device__ unsigned long long lookback(const TileScratch &ts, long long tile, un
       __nanosleep(32);
       continue;
     }
-    excl += s & kValueMask;
-    if (flag == kFlagPrefix) break;
-    --p;
+    unsigned long long v = lane <= stop ? (st & kValueMask) : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    excl += v;
+    if (pref) break;
+    p -= 32;
   }
-  ref_t(ts.status[tile]).store(kFlagPrefix | (excl + agg), cuda::memory_order_release);
+  if (lane == 0) ref_t(ts.status[tile]).store(kFlagPrefix | (excl + agg), cuda::memory_order_release);
   return excl;
 }
 
@@ -222,15 +238,16 @@ __global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, P
       ex += v[q];
     }
     const unsigned int agg = __shfl_sync(0xffffffffu, incl, 31);
+    bool to = false;
+    const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
     if (lane == 0) {
-      bool to = false;
-      s_excl = lookback(ts, tile, agg, &to);
+      s_excl = ex_tile;
       if (to) {
         s_timeout = true;
         atomicExch(ts.error, 1);
       }
       const long long ntiles = (n + kTile - 1) / kTile;
-      if (!to && tile == ntiles - 1) *ts.total = s_excl + agg;
+      if (!to && tile == ntiles - 1) *ts.total = ex_tile + agg;
     }
   }
   __syncthreads();

@@ -21,6 +21,15 @@ def same_bits(a, b):
     return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
 
 
+def same_bits_or_nan(a, b):
+    """Identical bits, except that a NaN matches any NaN (GPU and host
+    arithmetic produce different NaN payloads)."""
+    a, b = np.ascontiguousarray(a, np.float32), np.ascontiguousarray(b, np.float32)
+    na, nb = np.isnan(a), np.isnan(b)
+    return (a.shape == b.shape and np.array_equal(na, nb)
+            and np.array_equal(a.view(np.uint32)[~na], b.view(np.uint32)[~nb]))
+
+
 def golden_problem(goldens, name):
     g = goldens[name]
     return (int(g["N"]), g["prob_obstacles"].astype(np.float32), g["prob_init"], g["prob_goal"],
@@ -175,6 +184,41 @@ def test_collision_checks(gpu, pumplib, oracle, roadmap1000):
         free_wp = np.repeat(r["fe"].astype(bool), 9)
         assert np.array_equal(host(d_n, E * 9)[free_wp], n[free_wp])
         assert np.all(host(d_n, E * 9)[~free_wp] == 0)
+
+
+@pytest.mark.parametrize("mapname", ["indoor40", "boxes100", "boxes200"])
+def test_halfspaces_maps_and_gates(mapname, gpu, pumplib, oracle, roadmap1000):
+    """Half-spaces on other maps and distance gates, including the gate of the
+    benchmark's noise multiplier (2e-3, gate radius 6e-4), a NaN waypoint on a
+    free edge, and more boxes than the per-edge box filter covers (128)."""
+    torch, _ = gpu
+    L = pumplib.load()
+    from pump_gb300 import workloads
+    obs = {"indoor40": lambda: workloads.indoor(1001),
+           "boxes100": lambda: workloads.random_boxes(100, 7, side=(0.02, 0.08)),
+           "boxes200": lambda: workloads.random_boxes(200, 8, side=(0.02, 0.06))}[mapname]()
+    obs = np.ascontiguousarray(obs, np.float32)
+    r = roadmap1000
+    E = r["src"].size
+    disc = r["disc"].copy()
+    fe = oracle.free_edges(disc, obs)
+    k = int(np.nonzero(fe)[0][len(np.nonzero(fe)[0]) // 2])
+    disc.reshape(E, 9, 6)[k, 4, 1] = np.nan  # one free edge with a NaN waypoint
+    d_obs, d_disc, d_fe = dev(torch, obs), dev(torch, disc), dev(torch, fe)
+    for om in (2e-3, 0.05, 0.3):
+        maxHS = min(obs.shape[0], 5)
+        maxd2 = np.float32(0.1 * om * om)
+        d_a = empty(torch, E * 9 * maxHS * 3, torch.float32)
+        d_b = empty(torch, E * 9 * maxHS, torch.float32)
+        d_n = empty(torch, E * 9, torch.int32)
+        pumplib.check(L.pump_cache_halfspaces(ptr(d_obs), obs.shape[0], ptr(d_disc), ptr(d_fe), E, 9,
+                                              maxHS, float(maxd2), ptr(d_a), ptr(d_b), ptr(d_n),
+                                              stream(torch)))
+        a, b, n = oracle.cache_halfspaces(disc, fe, obs, maxHS, maxd2)
+        assert np.isnan(a).any()  # the NaN waypoint reached the half-spaces
+        assert same_bits_or_nan(host(d_a, a.size), a) and same_bits_or_nan(host(d_b, b.size), b)
+        free_wp = np.repeat(fe.astype(bool), 9)
+        assert np.array_equal(host(d_n, E * 9)[free_wp], n[free_wp])
 
 
 def test_collision_checks_many_obstacles(gpu, pumplib, oracle, roadmap1000):
