@@ -326,6 +326,9 @@ typedef struct pump_plan_result {
    * cost, and whether it replaced the returned path */
   float refine_cp, refine_cost;
   int refined;
+  /* of ms_explore: time from each iteration's wavefront upload to its CP
+   * results on the host (copies and HSMC) */
+  double ms_explore_wait;
 } pump_plan_result;
 
 /* Fills a problem with the reference's defaults (mainPUMP.cu:51-72). */

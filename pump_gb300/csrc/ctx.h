@@ -63,6 +63,11 @@ pump_status_t select_kth_pairs(Ctx *ctx, const PairView &pv, long long k, const 
 pump_status_t build_edges_pairs(Ctx *ctx, const PairView &pv, float rn, long long max_edges,
                                 int *d_src, int *d_dst, float *d_copt, float *d_topt,
                                 int *d_go_start, long long *h_num_edges, cudaStream_t stream);
+pump_status_t open_edges_device(Ctx *ctx, const uint8_t *d_free_e, const uint8_t *d_free_s,
+                                const int *d_src, const int *d_dst, const float *d_copt,
+                                const float *d_topt, long long E, int N, int *d_fid, int *d_fsrc,
+                                int *d_fdst, float *d_fcopt, float *d_ftopt, int *d_fgo,
+                                long long *h_count, cudaStream_t stream);
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                       int *d_count, int **d_error_out, cudaStream_t stream);
 pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,

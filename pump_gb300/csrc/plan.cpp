@@ -199,9 +199,13 @@ class Planner {
   DevBuf<uint8_t> d_free_s_, d_free_e_;
   long long E_ = 0;
   float rn_ = 0;
-  std::vector<int> dst_, go_;
-  std::vector<float> coptE_, toptE_, h_;
-  std::vector<uint8_t> free_s_, free_e_;
+  std::vector<float> h_;
+  // the expandable edges (free, to a free node) in (source, destination)
+  // order: original edge id, destination, cost, time, and row starts per node
+  DevBuf<int> d_fid_, d_fsrc_, d_fdst_, d_fgo_;
+  DevBuf<float> d_fcopt_, d_ftopt_;
+  std::vector<int> fid_, fdst_, fgo_;
+  std::vector<float> fcopt_, ftopt_;
 
   // exploration state (mainPUMP.cu:623-681)
   int maxPathCount_ = 0;
@@ -290,14 +294,6 @@ pump_status_t Planner::roadmap() {
     h_.assign(N_, 0.0f);
     for (int i = 0; i < N_ - 1; ++i) h_[i] = c[i];
   }
-  dst_.resize(E_);
-  go_.resize(N_ + 1);
-  coptE_.resize(E_);
-  toptE_.resize(E_);
-  PUMP_TRY(d2h(dst_.data(), d_dst_.p, E_));
-  PUMP_TRY(d2h(go_.data(), d_go_.p, N_ + 1));
-  PUMP_TRY(d2h(coptE_.data(), d_coptE_.p, E_));
-  PUMP_TRY(d2h(toptE_.data(), d_toptE_.p, E_));
   return sync();
 }
 
@@ -366,10 +362,27 @@ pump_status_t Planner::online() {
   PUMP_TRY(pump_cache_halfspaces(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_, maxd2,
                                  d_as_.p, d_bs_.p, nullptr, (pump_stream_t)s_));
   PUMP_TRY(ctx_->particle_table(pb_.seed, pb_.num_mc, pb_.table_rows, &d_table_, s_));
-  free_s_.resize(N_);
-  free_e_.resize(E_);
-  PUMP_TRY(d2h(free_s_.data(), d_free_s_.p, N_));
-  PUMP_TRY(d2h(free_e_.data(), d_free_e_.p, E_));
+  const size_t cap = E_ > 0 ? (size_t)E_ : 1;
+  PUMP_TRY(d_fid_.alloc(cap));
+  PUMP_TRY(d_fsrc_.alloc(cap));
+  PUMP_TRY(d_fdst_.alloc(cap));
+  PUMP_TRY(d_fcopt_.alloc(cap));
+  PUMP_TRY(d_ftopt_.alloc(cap));
+  PUMP_TRY(d_fgo_.alloc(N_ + 1));
+  long long F = 0;
+  PUMP_TRY(open_edges_device(ctx_, d_free_e_.p, d_free_s_.p, d_src_.p, d_dst_.p, d_coptE_.p,
+                             d_toptE_.p, E_, N_, d_fid_.p, d_fsrc_.p, d_fdst_.p, d_fcopt_.p,
+                             d_ftopt_.p, d_fgo_.p, &F, s_));
+  fid_.resize(F);
+  fdst_.resize(F);
+  fcopt_.resize(F);
+  ftopt_.resize(F);
+  fgo_.resize(N_ + 1);
+  PUMP_TRY(d2h(fid_.data(), d_fid_.p, F));
+  PUMP_TRY(d2h(fdst_.data(), d_fdst_.p, F));
+  PUMP_TRY(d2h(fcopt_.data(), d_fcopt_.p, F));
+  PUMP_TRY(d2h(ftopt_.data(), d_ftopt_.p, F));
+  PUMP_TRY(d2h(fgo_.data(), d_fgo_.p, N_ + 1));
   return sync();
 }
 
@@ -419,7 +432,7 @@ pump_status_t Planner::explore() {
   float costThreshold = h_[initIdx];
   const int maxItrs = 20;
   int itrs = 0, considered = 0;
-  std::vector<int> wfPrev, wfNode, wfEdge, mapSrc;
+  std::vector<int> wfPrev, wfNode, wfEdge, wfOpen, mapSrc;
   std::vector<float> newCP;
   std::vector<std::vector<int>> newAt(N_);
   std::vector<int> touched;
@@ -431,16 +444,16 @@ pump_status_t Planner::explore() {
     wfPrev.clear();
     wfNode.clear();
     wfEdge.clear();
+    wfOpen.clear();
     bool overflow = false;
     for (size_t g = 0; g < G[Gidx].size() && !overflow; ++g) {
       const int prev = G[Gidx][g];
       const int nodePrev = pathNode_[prev];
-      for (int e = go_[nodePrev]; e < go_[nodePrev + 1]; ++e) {
-        const int nodeNext = dst_[e];
-        if (!free_e_[e] || !free_s_[nodeNext]) continue;
+      for (int f = fgo_[nodePrev]; f < fgo_[nodePrev + 1]; ++f) {  // free edges to free nodes
         wfPrev.push_back(prev);
-        wfNode.push_back(nodeNext);
-        wfEdge.push_back(e);
+        wfNode.push_back(fdst_[f]);
+        wfEdge.push_back(fid_[f]);
+        wfOpen.push_back(f);
         if ((int)wfPrev.size() > M) { overflow = true; break; }
       }
     }
@@ -461,6 +474,7 @@ pump_status_t Planner::explore() {
       }
 
     // HSMC of the wavefront (PUMP.cu:82-160)
+    const auto tw = clk::now();
     PUMP_TRY(h2d(d_wfPrev_.p, wfPrev.data(), numNew));
     PUMP_TRY(h2d(d_wfEdge_.p, wfEdge.data(), numNew));
     PUMP_TRY(hsmc_staged_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p, d_bs_.p, maxHS_,
@@ -470,12 +484,13 @@ pump_status_t Planner::explore() {
     newCP.resize(numNew);
     PUMP_TRY(d2h(newCP.data(), d_cpStage_.p, numNew));
     PUMP_TRY(sync());
+    res_->ms_explore_wait += ms_since(tw);
     for (int i = 0; i < numNew; ++i) pathCP_[numPaths_ + i] = newCP[i];
 
     // PUMP.cu:164-167
     for (int i = 0; i < numNew; ++i) {
-      pathTime_[numPaths_ + i] = pathTime_[wfPrev[i]] + toptE_[wfEdge[i]];
-      pathCost_[numPaths_ + i] = pathCost_[wfPrev[i]] + coptE_[wfEdge[i]];
+      pathTime_[numPaths_ + i] = pathTime_[wfPrev[i]] + ftopt_[wfOpen[i]];
+      pathCost_[numPaths_ + i] = pathCost_[wfPrev[i]] + fcopt_[wfOpen[i]];
     }
     // CP cut-off and candidate lists per node (PUMP.cu:171-185)
     for (int node : touched) newAt[node].clear();

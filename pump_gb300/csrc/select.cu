@@ -284,6 +284,25 @@ struct EdgeEmit {
     topt[pos] = topts[idx];
   }
 };
+// Edges the search can expand: free edge to a free node (PUMP.cu:52-53).
+struct OpenEdgePred {
+  const uint8_t *free_e, *free_s;
+  const int *dst;
+  __device__ bool operator()(long long e) const { return free_e[e] && free_s[dst[e]]; }
+};
+struct OpenEdgeEmit {
+  const int *src, *dst;
+  const float *copt, *topt;
+  int *f_id, *f_src, *f_dst;
+  float *f_copt, *f_topt;
+  __device__ void operator()(long long e, long long pos) const {
+    f_id[pos] = (int)e;
+    f_src[pos] = src[e];
+    f_dst[pos] = dst[e];
+    f_copt[pos] = copt[e];
+    f_topt[pos] = topt[e];
+  }
+};
 struct PairEdgePred {
   PairView pv;
   float rn;
@@ -421,6 +440,26 @@ pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_
     PUMP_TRY(launch_status("go_start_kernel"));
   }
   return PUMP_OK;
+}
+
+// The expandable edges in (source, destination) order with their row starts
+// per source node: the adjacency the search walks, without the edges it
+// would skip.
+pump_status_t open_edges_device(Ctx *ctx, const uint8_t *d_free_e, const uint8_t *d_free_s,
+                                const int *d_src, const int *d_dst, const float *d_copt,
+                                const float *d_topt, long long E, int N, int *d_fid, int *d_fsrc,
+                                int *d_fdst, float *d_fcopt, float *d_ftopt, int *d_fgo,
+                                long long *h_count, cudaStream_t stream) {
+  TileScratch ts{};
+  PUMP_TRY(run_compact(ctx, E, OpenEdgePred{d_free_e, d_free_s, d_dst},
+                       OpenEdgeEmit{d_src, d_dst, d_copt, d_topt, d_fid, d_fsrc, d_fdst, d_fcopt,
+                                    d_ftopt},
+                       stream, &ts));
+  unsigned long long total = 0;
+  PUMP_TRY(finish_compact(ts, &total, stream));
+  *h_count = (long long)total;
+  go_start_kernel<<<grid_for(N + 1, 256), 256, 0, stream>>>(d_fsrc, (long long)total, N, d_fgo);
+  return launch_status("go_start_kernel");
 }
 
 // Device-side frontier compaction; *d_error_out (device) is nonzero when a
