@@ -326,8 +326,8 @@ typedef struct pump_plan_result {
    * cost, and whether it replaced the returned path */
   float refine_cp, refine_cost;
   int refined;
-  /* of ms_explore: time from each iteration's wavefront upload to its CP
-   * results on the host (copies and HSMC) */
+  /* of ms_explore: time from each iteration's first launch to its counters
+   * back on the host (the iteration's device work and read-backs) */
   double ms_explore_wait;
 } pump_plan_result;
 

@@ -32,6 +32,7 @@
 #include "common.cuh"
 #include "ctx.h"
 #include "pairview.cuh"
+#include "search.h"
 
 namespace pump {
 
@@ -210,7 +211,7 @@ class Planner {
   // exploration state (mainPUMP.cu:623-681)
   int maxPathCount_ = 0;
   std::vector<int> pathPrev_, pathNode_;
-  std::vector<float> pathCost_, pathTime_, pathCP_;
+  std::vector<float> pathCost_;
   std::vector<std::vector<int>> atNode_;
   DevBuf<uint32_t> d_valid_, d_stage_;
   DevBuf<float> d_pathTime_, d_cpStage_;
@@ -386,23 +387,48 @@ pump_status_t Planner::online() {
   return sync();
 }
 
+// The search loop (PUMP.cu:39-290) with its state on the device
+// (search.cu): per iteration the host launches the expansion scan, reads the
+// wavefront size, launches expansion, HSMC, pruning and storing, and reads
+// the iteration's counters back.
 pump_status_t Planner::explore() {
   maxPathCount_ = (int)(2 * N_ * std::sqrt((double)N_));  // mainPUMP.cu:623
   const int M = maxPathCount_;
-  pathPrev_.assign(M + 1, 0);
-  pathNode_.assign(M + 1, 0);
-  pathCost_.assign(M + 1, 0.0f);
-  pathTime_.assign(M + 1, 0.0f);
-  pathCP_.assign(M + 1, 0.0f);
-  atNode_.assign(N_, std::vector<int>());
+  const size_t cap = (size_t)M + 1;
   PUMP_TRY(d_valid_.alloc((size_t)M * words_));
-  PUMP_TRY(d_stage_.alloc((size_t)(M + 1) * words_));
-  PUMP_TRY(d_cpStage_.alloc(M + 1));
-  PUMP_TRY(d_pathTime_.alloc(M + 1));
-  PUMP_TRY(d_wfPrev_.alloc(M + 1));
-  PUMP_TRY(d_wfEdge_.alloc(M + 1));
-  PUMP_TRY(d_map_.alloc(M + 1));
+  PUMP_TRY(d_stage_.alloc(cap * words_));
+  PUMP_TRY(d_cpStage_.alloc(cap));
+  PUMP_TRY(d_pathTime_.alloc(cap));
+  PUMP_TRY(d_wfPrev_.alloc(cap));
+  PUMP_TRY(d_wfEdge_.alloc(cap));
+  PUMP_TRY(d_map_.alloc(cap));
   PUMP_TRY(d_err_.alloc(1));
+  DevBuf<int> d_prev, d_node, d_g0, d_g1, d_nhead, d_nnext, d_wnode, d_wopen, d_newhead, d_newnext;
+  DevBuf<float> d_cost, d_cp, d_ncost, d_ntime, d_h;
+  DevBuf<unsigned int> d_off;
+  DevBuf<uint8_t> d_alive, d_dom, d_bucket;
+  DevBuf<SearchCtl> d_ctl;
+  PUMP_TRY(d_prev.alloc(cap));
+  PUMP_TRY(d_node.alloc(cap));
+  PUMP_TRY(d_cost.alloc(cap));
+  PUMP_TRY(d_cp.alloc(cap));
+  PUMP_TRY(d_g0.alloc(cap));
+  PUMP_TRY(d_g1.alloc(cap));
+  PUMP_TRY(d_nhead.alloc(N_));
+  PUMP_TRY(d_nnext.alloc(cap));
+  PUMP_TRY(d_wnode.alloc(cap));
+  PUMP_TRY(d_wopen.alloc(cap));
+  PUMP_TRY(d_off.alloc(cap));
+  PUMP_TRY(d_ncost.alloc(cap));
+  PUMP_TRY(d_ntime.alloc(cap));
+  PUMP_TRY(d_alive.alloc(cap));
+  PUMP_TRY(d_dom.alloc(cap));
+  PUMP_TRY(d_newhead.alloc(N_));
+  PUMP_TRY(d_newnext.alloc(cap));
+  PUMP_TRY(d_bucket.alloc(cap));
+  PUMP_TRY(d_h.alloc(N_));
+  PUMP_TRY(d_ctl.alloc(1));
+  PUMP_TRY(h2d(d_h.p, h_.data(), (size_t)N_));
   PUMP_CUDA_TRY(cudaMemsetAsync(d_err_.p, 0, sizeof(int), s_));
   // setupValidParticles (PUMP.cu:766-777) for path 0: all particles valid
   PUMP_CUDA_TRY(cudaMemsetAsync(d_valid_.p, 0xFF, sizeof(uint32_t) * words_, s_));
@@ -410,150 +436,107 @@ pump_status_t Planner::explore() {
     const uint32_t last = (1u << (P_ % 32)) - 1u;
     PUMP_TRY(h2d(d_valid_.p + words_ - 1, &last, 1));
   }
-  PUMP_CUDA_TRY(cudaMemsetAsync(d_pathTime_.p, 0, sizeof(float), s_));
+  SearchDev sd{};
+  sd.N = N_;
+  sd.goal = N_ - 1;
+  sd.fgo = d_fgo_.p;
+  sd.fid = d_fid_.p;
+  sd.fdst = d_fdst_.p;
+  sd.fcopt = d_fcopt_.p;
+  sd.ftopt = d_ftopt_.p;
+  sd.h = d_h.p;
+  sd.path_prev = d_prev.p;
+  sd.path_node = d_node.p;
+  sd.path_cost = d_cost.p;
+  sd.path_time = d_pathTime_.p;
+  sd.path_cp = d_cp.p;
+  sd.g_list[0] = d_g0.p;
+  sd.g_list[1] = d_g1.p;
+  sd.node_head = d_nhead.p;
+  sd.node_next = d_nnext.p;
+  sd.wf_prev = d_wfPrev_.p;
+  sd.wf_node = d_wnode.p;
+  sd.wf_edge = d_wfEdge_.p;
+  sd.wf_open = d_wopen.p;
+  sd.wf_off = d_off.p;
+  sd.new_cost = d_ncost.p;
+  sd.new_time = d_ntime.p;
+  sd.new_cp = d_cpStage_.p;
+  sd.alive = d_alive.p;
+  sd.dominated = d_dom.p;
+  sd.new_head = d_newhead.p;
+  sd.new_next = d_newnext.p;
+  sd.map_src = d_map_.p;
+  sd.bucket = d_bucket.p;
+  sd.ctl = d_ctl.p;
+  PUMP_TRY(search_init(sd, s_));
 
   // PUMP.cu:10-35
   const float cpTarget = pb_.cp_target;
   const float dr = lambda_ * rn_;
   const float cpMinSoln = cpTarget / pb_.cp_factor;
   const float cpCutoff = cpTarget * pb_.cp_factor;
-  const int initIdx = 0, goalIdx = N_ - 1;
   int Gidx = 0;
-  bool goalCondition = false, goalConditionNext = false, emptyOpenSet = false;
-  std::vector<int> G[2];
-  atNode_[initIdx].push_back(0);
-  pathPrev_[0] = -2;
-  pathNode_[0] = initIdx;
-  pathCost_[0] = 0;
-  pathCP_[0] = 0;
-  pathTime_[0] = 0;
-  G[Gidx].push_back(0);
+  int gCount[2] = {1, 0};
   numPaths_ = 1;
-  float costThreshold = h_[initIdx];
+  float costThreshold = h_[0];
   const int maxItrs = 20;
-  int itrs = 0, considered = 0;
-  std::vector<int> wfPrev, wfNode, wfEdge, wfOpen, mapSrc;
-  std::vector<float> newCP;
-  std::vector<std::vector<int>> newAt(N_);
-  std::vector<int> touched;
+  int itrs = 0;
+  long long considered = 0;
+  std::vector<int> trace_prev, trace_edge;
   pump_status_t status = PUMP_OK;
-  while (itrs < maxItrs && !goalCondition && !emptyOpenSet) {
+  SearchCtl ctl{};
+  while (itrs < maxItrs) {
     ++itrs;
-    if (goalConditionNext) goalCondition = true;
     // expansion (PUMP.cu:47-66)
-    wfPrev.clear();
-    wfNode.clear();
-    wfEdge.clear();
-    wfOpen.clear();
-    bool overflow = false;
-    for (size_t g = 0; g < G[Gidx].size() && !overflow; ++g) {
-      const int prev = G[Gidx][g];
-      const int nodePrev = pathNode_[prev];
-      for (int f = fgo_[nodePrev]; f < fgo_[nodePrev + 1]; ++f) {  // free edges to free nodes
-        wfPrev.push_back(prev);
-        wfNode.push_back(fdst_[f]);
-        wfEdge.push_back(fid_[f]);
-        wfOpen.push_back(f);
-        if ((int)wfPrev.size() > M) { overflow = true; break; }
-      }
+    const int nG = gCount[Gidx];
+    const auto tw = clk::now();
+    PUMP_TRY(search_expand_scan(ctx_, sd, Gidx, nG, s_));
+    unsigned long long nn = 0;
+    PUMP_TRY(d2h(&nn, &d_ctl.p->num_new, 1));
+    PUMP_TRY(sync());
+    if (nn > (unsigned long long)M) {
+      status = set_error(PUMP_ERR_CAPACITY, "wavefront exceeds maxPathCount %d", M);
+      break;
     }
-    if (overflow) { status = set_error(PUMP_ERR_CAPACITY, "wavefront exceeds maxPathCount %d", M); break; }
-    const int numNew = (int)wfPrev.size();
+    const int numNew = (int)nn;
     if (itrs <= 32) res_->wavefront_sizes[itrs - 1] = numNew;
     if (numNew == 0) break;
     if (numPaths_ + numNew >= M) {
       status = set_error(PUMP_ERR_CAPACITY, "paths exceed maxPathCount %d", M);
       break;
     }
-    G[Gidx].clear();
+    PUMP_TRY(search_expand_write(sd, Gidx, nG, s_));
     considered += numNew;
-    if (res_->wf_trace)
+    if (res_->wf_trace) {
+      trace_prev.resize(numNew);
+      trace_edge.resize(numNew);
+      PUMP_TRY(d2h(trace_prev.data(), d_wfPrev_.p, numNew));
+      PUMP_TRY(d2h(trace_edge.data(), d_wfEdge_.p, numNew));
+      PUMP_TRY(sync());
       for (int i = 0; i < numNew && res_->wf_trace_len + 2 <= res_->wf_trace_cap; ++i) {
-        res_->wf_trace[res_->wf_trace_len++] = wfPrev[i];
-        res_->wf_trace[res_->wf_trace_len++] = wfEdge[i];
+        res_->wf_trace[res_->wf_trace_len++] = trace_prev[i];
+        res_->wf_trace[res_->wf_trace_len++] = trace_edge[i];
       }
-
+    }
     // HSMC of the wavefront (PUMP.cu:82-160)
-    const auto tw = clk::now();
-    PUMP_TRY(h2d(d_wfPrev_.p, wfPrev.data(), numNew));
-    PUMP_TRY(h2d(d_wfEdge_.p, wfEdge.data(), numNew));
     PUMP_TRY(hsmc_staged_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p, d_bs_.p, maxHS_,
                                d_pathTime_.p, d_toptE_.p, dt_, d_table_, pb_.num_mc,
                                pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p, P_,
                                d_cpStage_.p, d_err_.p, s_));
-    newCP.resize(numNew);
-    PUMP_TRY(d2h(newCP.data(), d_cpStage_.p, numNew));
+    // cut-off, dominance, storing, buckets (PUMP.cu:164-256)
+    PUMP_TRY(search_prune(sd, numNew, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
+    PUMP_TRY(search_store(ctx_, sd, numNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
+                          d_stage_.p, d_valid_.p, words_, s_));
+    PUMP_TRY(d2h(&ctl, d_ctl.p, 1));
     PUMP_TRY(sync());
     res_->ms_explore_wait += ms_since(tw);
-    for (int i = 0; i < numNew; ++i) pathCP_[numPaths_ + i] = newCP[i];
-
-    // PUMP.cu:164-167
-    for (int i = 0; i < numNew; ++i) {
-      pathTime_[numPaths_ + i] = pathTime_[wfPrev[i]] + ftopt_[wfOpen[i]];
-      pathCost_[numPaths_ + i] = pathCost_[wfPrev[i]] + fcopt_[wfOpen[i]];
-    }
-    // CP cut-off and candidate lists per node (PUMP.cu:171-185)
-    for (int node : touched) newAt[node].clear();
-    touched.clear();
-    for (int i = 0; i < numNew; ++i) {
-      const int node = wfNode[i], pathIdx = numPaths_ + i;
-      if (pathCP_[pathIdx] > cpCutoff) { wfNode[i] = -1; continue; }
-      if (newAt[node].empty()) touched.push_back(node);
-      newAt[node].push_back(pathIdx);
-    }
-    // epsilon dominance (PUMP.cu:188-218): stored paths, then new ones
-    for (int i = 0; i < numNew; ++i) {
-      const int node = wfNode[i];
-      if (node == -1 || node == goalIdx) continue;
-      const int pathIdx = numPaths_ + i;
-      const float cp = pathCP_[pathIdx], cost = pathCost_[pathIdx];
-      auto dominated_by = [&](int cmp) {
-        if (pathCP_[cmp] < epsCP_ + cp && pathCost_[cmp] < epsCost_ + cost) {
-          if (pathCP_[cmp] + epsCP_ >= cp && pathCost_[cmp] + epsCost_ >= cost && pathIdx < cmp)
-            return false;  // co-dominant: keep the lower path number
-          return true;
-        }
-        return false;
-      };
-      bool dead = false;
-      for (int cmp : atNode_[node])
-        if (cmp != pathIdx && dominated_by(cmp)) { dead = true; break; }
-      if (!dead)
-        for (int cmp : newAt[node])
-          if (cmp != pathIdx && dominated_by(cmp)) { dead = true; break; }
-      if (dead) wfNode[i] = -1;
-    }
-    // store survivors (PUMP.cu:221-256)
-    mapSrc.clear();
-    int numValid = 0;
-    for (int i = 0; i < numNew; ++i) {
-      const int node = wfNode[i], pathIdx = numPaths_ + i;
-      if (node == -1 || node == 0) continue;
-      const int st = numPaths_ + numValid;
-      pathCP_[st] = pathCP_[pathIdx];
-      pathTime_[st] = pathTime_[pathIdx];
-      pathCost_[st] = pathCost_[pathIdx];
-      mapSrc.push_back(i);
-      float dCost = (pathCost_[st] + h_[node] - costThreshold);
-      dCost = std::max((float)0, dCost);
-      const int bucket = (((int)(dCost / dr)) + Gidx + 1) % numBuckets_;
-      G[bucket].push_back(st);
-      pathPrev_[st] = wfPrev[i];
-      pathNode_[st] = node;
-      atNode_[node].push_back(st);
-      ++numValid;
-    }
-    PUMP_TRY(h2d(d_map_.p, mapSrc.data(), numValid));
-    PUMP_TRY(gather_words_async(d_stage_.p, d_map_.p, numValid, words_,
-                                d_valid_.p + (size_t)numPaths_ * words_, s_));
-    PUMP_TRY(h2d(d_pathTime_.p + numPaths_, pathTime_.data() + numPaths_, numValid));
-    numPaths_ += numValid;
+    numPaths_ += (int)ctl.num_valid;
+    gCount[0] = ctl.g_count[0];
+    gCount[1] = ctl.g_count[1];
     // goal and open-set conditions (PUMP.cu:259-288)
-    for (int pi : atNode_[goalIdx])
-      if (pathCP_[pi] <= cpMinSoln) goalConditionNext = goalCondition = true;
-    if (goalCondition) break;
-    emptyOpenSet = G[0].empty() && G[1].empty();
-    if (emptyOpenSet) break;
+    if (ctl.goal_found) break;
+    if (gCount[0] == 0 && gCount[1] == 0) break;
     Gidx = (Gidx + 1) % numBuckets_;
     costThreshold += dr;
     if (numPaths_ >= M) {
@@ -561,13 +544,23 @@ pump_status_t Planner::explore() {
       break;
     }
   }
+  // stored paths back to the host for the solution search
+  pathPrev_.resize(numPaths_);
+  pathNode_.resize(numPaths_);
+  pathCost_.resize(numPaths_);
+  PUMP_TRY(d2h(pathPrev_.data(), d_prev.p, numPaths_));
+  PUMP_TRY(d2h(pathNode_.data(), d_node.p, numPaths_));
+  PUMP_TRY(d2h(pathCost_.data(), d_cost.p, numPaths_));
   int err = 0;
   PUMP_TRY(d2h(&err, d_err_.p, 1));
   PUMP_TRY(sync());
+  atNode_.assign(N_, std::vector<int>());
+  for (int p = 0; p < numPaths_; ++p)
+    if (pathNode_[p] == N_ - 1) atNode_[N_ - 1].push_back(p);
   res_->iterations = itrs;
   res_->num_paths = numPaths_;
-  res_->num_considered = considered;
-  res_->goal_paths = (int)atNode_[goalIdx].size();
+  res_->num_considered = (int)considered;
+  res_->goal_paths = (int)atNode_[N_ - 1].size();
   if (err) return set_error((pump_status_t)err, "particle table has too few rows for a path time");
   return status;
 }

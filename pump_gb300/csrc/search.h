@@ -1,0 +1,66 @@
+// Device-resident exploration (the search loop of PUMP.cu:39-290): the
+// state and the steps of one iteration, all on the device.  The host keeps
+// only the loop control (a few counters read back twice per iteration).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pump.h"
+
+namespace pump {
+
+class Ctx;
+
+// Counters of an iteration, read back by the host.
+struct SearchCtl {
+  unsigned long long num_new;    // wavefront size (expansion scan total)
+  unsigned long long num_valid;  // survivors stored this iteration
+  int g_count[2];                // bucket sizes (the reference's G lists)
+  int goal_found;                // a stored goal path has CP <= cpTarget / eta
+  int pad;
+};
+
+// Device arrays of one search (capacities: M + 1 paths and new paths, N nodes).
+struct SearchDev {
+  int N, goal;
+  // the expandable edges (row starts per node, original id, destination, cost, time)
+  const int *fgo, *fid, *fdst;
+  const float *fcopt, *ftopt, *h;
+  // stored paths
+  int *path_prev, *path_node;
+  float *path_cost, *path_time, *path_cp;
+  int *g_list[2];
+  int *node_head, *node_next;  // stored paths per node (linked lists)
+  // the wavefront of the current iteration
+  int *wf_prev, *wf_node, *wf_edge, *wf_open;
+  unsigned int *wf_off;          // expansion offsets per bucket entry
+  float *new_cost, *new_time;
+  const float *new_cp;           // HSMC output
+  uint8_t *alive, *dominated;
+  int *new_head, *new_next;      // new paths per node passing the CP cut-off
+  int *map_src;                  // survivor rank -> wavefront index
+  uint8_t *bucket;               // survivor rank -> bucket
+  SearchCtl *ctl;
+};
+
+// Path 0 at the initial node in bucket 0 (PUMP.cu:19-34).
+pump_status_t search_init(const SearchDev &sd, cudaStream_t s);
+// Expansion offsets of the n_g paths of bucket g_idx; the wavefront size
+// lands in ctl->num_new.
+pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n_g,
+                                 cudaStream_t s);
+// Writes the wavefront (PUMP.cu:47-66) and empties bucket g_idx.
+pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, cudaStream_t s);
+// New paths' time and cost, the CP cut-off (PUMP.cu:164-185), per-node lists
+// of the survivors of the cut-off, then epsilon dominance (PUMP.cu:188-218).
+pump_status_t search_prune(const SearchDev &sd, int num_new, int num_paths, float cp_cutoff,
+                           float eps_cp, float eps_cost, cudaStream_t s);
+// Stable compaction of the survivors into stored paths, bucket assignment,
+// per-node lists, goal test and bucket appends (PUMP.cu:221-282); the
+// particle masks of the survivors move from the stage to their stored slots.
+pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int num_new, int num_paths,
+                           int g_idx, float cost_threshold, float dr, float cp_min_soln,
+                           const uint32_t *stage, uint32_t *valid, int words, cudaStream_t s);
+
+}  // namespace pump

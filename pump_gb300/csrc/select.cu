@@ -6,33 +6,18 @@
 // over order-preserving 32-bit keys (11, 11 and 10 bits) finds the same
 // element with three reads of the array and no sort.
 //
-// Edge list and frontier: single-pass stable compaction with decoupled
-// look-back (Merrill & Garland, "Single-pass Parallel Prefix Scan with
-// Decoupled Look-back", 2016).  A tile of 4096 items is processed row by row
-// (rows of 256 consecutive items), so the rank of every selected item follows
-// index order; a tile publishes its count, then its inclusive prefix, in a
-// 64-bit status word that later tiles read.  Tiles take their index from an
-// atomic counter, so every tile a block waits on has already started.  Every
-// wait is bounded: a block that spins past kSpinLimit sets the error word and
-// leaves, and the host reports PUMP_ERR_TIMEOUT.
-#include <cuda/atomic>
-
+// Edge list and frontier: stable compaction (compact.cuh) of the pairs below
+// rn and of the frontier flags.
 #include <mutex>
 
 #include "common.cuh"
+#include "compact.cuh"
 #include "ctx.h"
 #include "pairview.cuh"
 
 namespace pump {
 namespace {
 
-constexpr int kCompactThreads = 256;
-constexpr int kCompactRows = 16;
-constexpr int kTile = kCompactThreads * kCompactRows;  // 4096 items
-constexpr unsigned long long kFlagAggregate = 1ull << 62;
-constexpr unsigned long long kFlagPrefix = 2ull << 62;
-constexpr unsigned long long kValueMask = (1ull << 62) - 1;
-constexpr long long kSpinLimit = 1ll << 22;
 
 __device__ __forceinline__ uint32_t float_key(float f) {
   uint32_t u = __float_as_uint(f);
@@ -134,135 +119,7 @@ __global__ void select_pick_kernel(SelectState *st, int shift, int bits, unsigne
   for (int q = 0; q < per; ++q) hist[t * per + q] = 0;
 }
 
-// ------------------------------------------------------ stable compaction
-struct TileScratch {
-  unsigned long long *status;  // one word per tile, zeroed before launch
-  unsigned int *tile_counter;  // zeroed before launch
-  unsigned long long *total;   // selected count (written by the last tile)
-  int *error;                  // 1 = look-back wait gave up
-};
-
-// Exclusive prefix of this tile from its predecessors' status words, read by
-// a whole warp: lane l reads the status of tile p - l, so one round trip to L2
-// covers 32 predecessors.  The lanes up to the nearest inclusive prefix must
-// all have published (at least an aggregate); otherwise the warp waits and
-// reads the window again.  Called by every lane of one warp; every lane
-// returns the same value.
-__device__ unsigned long long lookback_warp(const TileScratch &ts, long long tile,
-                                            unsigned long long agg, bool *timed_out) {
-  using ref_t = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
-  const int lane = threadIdx.x & 31;
-  if (tile == 0) {
-    if (lane == 0) ref_t(ts.status[0]).store(kFlagPrefix | agg, cuda::memory_order_release);
-    return 0;
-  }
-  if (lane == 0) ref_t(ts.status[tile]).store(kFlagAggregate | agg, cuda::memory_order_release);
-  unsigned long long excl = 0;
-  long long p = tile - 1;  // nearest tile of the window
-  long long spins = 0;
-  while (true) {
-    const long long q = p - lane;
-    // before tile 0 the prefix is 0 (a published prefix of value 0)
-    const unsigned long long st =
-        q >= 0 ? ref_t(ts.status[q]).load(cuda::memory_order_acquire) : kFlagPrefix;
-    const unsigned long long flag = st & ~kValueMask;
-    const unsigned int pref = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
-    const unsigned int none = __ballot_sync(0xffffffffu, flag == 0);
-    const int stop = pref ? __ffs(pref) - 1 : 31;  // last lane needed in this window
-    const unsigned int need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
-    if (none & need) {
-      if (++spins > kSpinLimit) {
-        *timed_out = true;
-        return 0;
-      }
-      __nanosleep(32);
-      continue;
-    }
-    unsigned long long v = lane <= stop ? (st & kValueMask) : 0ull;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    excl += v;
-    if (pref) break;
-    p -= 32;
-  }
-  if (lane == 0) ref_t(ts.status[tile]).store(kFlagPrefix | (excl + agg), cuda::memory_order_release);
-  return excl;
-}
-
-// Pred(i) -> bool, Emit(i, pos) writes item i at output position pos.
-template <class Pred, class Emit>
-__global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, Pred pred, Emit emit,
-                                                                  TileScratch ts) {
-  __shared__ unsigned int s_tile;
-  __shared__ unsigned int s_cnt[kCompactRows][kCompactThreads / 32];
-  __shared__ unsigned long long s_excl;
-  __shared__ bool s_timeout;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    s_tile = atomicAdd(ts.tile_counter, 1u);
-    s_timeout = false;
-  }
-  __syncthreads();
-  const long long tile = s_tile;
-  const long long base = tile * kTile;
-  unsigned int ballots[kCompactRows];
-#pragma unroll
-  for (int r = 0; r < kCompactRows; ++r) {
-    const long long i = base + r * kCompactThreads + threadIdx.x;
-    const bool f = i < n && pred(i);
-    ballots[r] = __ballot_sync(0xffffffffu, f);
-    if (lane == 0) s_cnt[r][warp] = __popc(ballots[r]);
-  }
-  __syncthreads();
-  // exclusive scan of the 16 x 8 counts in (row, warp) order by warp 0
-  if (warp == 0) {
-    unsigned int v[4];
-    unsigned int run = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = lane * 4 + q;
-      v[q] = s_cnt[e / 8][e % 8];
-      run += v[q];
-    }
-    unsigned int incl = run;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const unsigned int o = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += o;
-    }
-    unsigned int ex = incl - run;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = lane * 4 + q;
-      s_cnt[e / 8][e % 8] = ex;
-      ex += v[q];
-    }
-    const unsigned int agg = __shfl_sync(0xffffffffu, incl, 31);
-    bool to = false;
-    const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
-    if (lane == 0) {
-      s_excl = ex_tile;
-      if (to) {
-        s_timeout = true;
-        atomicExch(ts.error, 1);
-      }
-      const long long ntiles = (n + kTile - 1) / kTile;
-      if (!to && tile == ntiles - 1) *ts.total = ex_tile + agg;
-    }
-  }
-  __syncthreads();
-  if (s_timeout) return;
-  const unsigned long long excl = s_excl;
-  const unsigned int lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int r = 0; r < kCompactRows; ++r) {
-    if (ballots[r] & (1u << lane)) {
-      const long long i = base + r * kCompactThreads + threadIdx.x;
-      emit(i, (long long)(excl + s_cnt[r][warp] + __popc(ballots[r] & lt)));
-    }
-  }
-}
-
+// ------------------------------------------------------ compaction users
 struct EdgePred {
   const float *copts;
   float rn;
@@ -350,38 +207,6 @@ __global__ void go_start_kernel(const int *__restrict__ src, long long E, int N,
 }
 
 __global__ void copy_count_kernel(const unsigned long long *total, int *out) { *out = (int)*total; }
-
-template <class Pred, class Emit>
-pump_status_t run_compact(Ctx *ctx, long long n, Pred pred, Emit emit, cudaStream_t stream,
-                          TileScratch *ts_out) {
-  const long long ntiles = n > 0 ? (n + kTile - 1) / kTile : 1;
-  const size_t bytes = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
-  char *scratch = nullptr;
-  PUMP_TRY(ctx->scratch(Ctx::kCompact, bytes, (void **)&scratch));
-  TileScratch ts{};
-  ts.total = (unsigned long long *)scratch;
-  ts.status = ts.total + 1;
-  ts.tile_counter = (unsigned int *)(ts.status + ntiles + 1);
-  ts.error = (int *)(ts.tile_counter + 1);
-  PUMP_CUDA_TRY(cudaMemsetAsync(scratch, 0, bytes, stream));
-  if (n > 0) {
-    if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "compaction: too many tiles");
-    compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(n, pred, emit, ts);
-    PUMP_TRY(launch_status("compact_kernel"));
-  }
-  *ts_out = ts;
-  return PUMP_OK;
-}
-
-// Reads the selected count and the wait-bound error word (synchronises).
-pump_status_t finish_compact(const TileScratch &ts, unsigned long long *total, cudaStream_t stream) {
-  int err = 0;
-  PUMP_CUDA_TRY(cudaMemcpyAsync(total, ts.total, sizeof *total, cudaMemcpyDeviceToHost, stream));
-  PUMP_CUDA_TRY(cudaMemcpyAsync(&err, ts.error, sizeof err, cudaMemcpyDeviceToHost, stream));
-  PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
-  if (err) return set_error(PUMP_ERR_TIMEOUT, "compaction: look-back wait exceeded its bound");
-  return PUMP_OK;
-}
 
 // Device-side k-th smallest of src(0 .. n-1): the result lands in the ctx
 // select state; *d_result points at it (device).
