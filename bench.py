@@ -534,7 +534,8 @@ def run_ours(args):
         }
         fp64 = C.c_double(0)
         lib.check(L.pump_probe_fp64_tflops(C.byref(fp64), sh))
-        out["roofline"] = roofline(dom, ks, N, E, M_total, W, maxHS, P, args.mode, fp64.value)
+        out["roofline"] = roofline(dom, ks, N, E, M_total, W, maxHS, P, args.mode, fp64.value,
+                                   float(clk.get("sm_mhz") or 2070.0))
         if args.batch > 0:
             out["queries_per_s"] = measure_queries(args, lib, L, ctx)
         if not args.no_refine:
@@ -549,18 +550,28 @@ def run_ours(args):
     return out
 
 
-# Binary64 flops per ordered pair of the 2pBVP kernels (division counted as
-# one flop), counted from the kernels' source:
-#  precision: coefficients 41, one Newton step 19, cost 9 (one candidate
-#             minimum, the common case);
+# Binary64 flops per ordered pair of the 2pBVP kernels (a fused multiply-add
+# counts two), counted from the kernels' source and confirmed by ncu's
+# instruction mix on this workload (per pair: 10 DFMA, 6 DADD, 2 DMUL):
+#  precision: coefficient assembly in float-float on the FP32 pipe; binary64
+#             only for the six coefficients (hi + lo), the Newton residual
+#             Q(x) and step, and the cost at the root;
 #  parity:    40 per cost evaluation (23 additions, 15 multiplications, one
 #             division, one scaling) x 23 evaluations per pair (the mean over
 #             20,000 pairs of this workload's samples: 22 for the bisection
 #             plus the final cost) + 20 for the pair's hoisted coefficients.
-BVP_FP64_FLOPS_PER_PAIR = {"precision": 69.0, "parity": 40.0 * 23 + 20.0}
+BVP_FP64_FLOPS_PER_PAIR = {"precision": 28.0, "parity": 40.0 * 23 + 20.0}
+# The precision kernel is bound by instruction issue, not by one pipe: warp
+# instructions executed per pair on this workload (ncu smsp__inst_executed.sum
+# over one launch / pairs; profiles/bvp_pairs_precision_indoor4000.md), and
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum).
+BVP_PRECISION_WARP_INST_PER_PAIR = 42.5
+BVP_PRECISION_DRAM_BYTES_N4000 = 0.16e6 + 66.71e6
+SMSP_PER_SM = 4
+NUM_SMS = 152
 
 
-def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops):
+def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops, sm_mhz):
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -582,13 +593,28 @@ def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops):
         if k in ks and ks[k] > 0:
             a = b / (ks[k] / 1e3) / 1e9
             table[k] = {"bound": "hbm", "achieved_gbs": round(a, 1), "frac": round(a / hbm, 4)}
-    flops = BVP_FP64_FLOPS_PER_PAIR[mode] * N * (N - 1)
-    ach = flops / (ks["bvp_pairs"] / 1e3) / 1e12
-    table["bvp_pairs"] = {"bound": "fp64", "achieved_tflops": round(ach, 4),
-                          "frac": round(ach / fp64_tflops, 4)}
+    pairs = N * (N - 1)
+    t_bvp = ks["bvp_pairs"] / 1e3
+    fp64 = BVP_FP64_FLOPS_PER_PAIR[mode] * pairs / t_bvp / 1e12
+    table["bvp_pairs_fp64"] = {"bound": "fp64", "achieved_tflops": round(fp64, 4),
+                               "frac": round(fp64 / fp64_tflops, 4),
+                               "flops_per_pair": BVP_FP64_FLOPS_PER_PAIR[mode]}
+    issue_peak = NUM_SMS * SMSP_PER_SM * sm_mhz * 1e6 / 1e9  # warp instructions, G/s
+    if mode == "precision" and N == 4000:
+        issue = BVP_PRECISION_WARP_INST_PER_PAIR * pairs / t_bvp / 1e9
+        table["bvp_pairs"] = {"bound": "issue", "achieved_ginst": round(issue, 1),
+                              "frac": round(issue / issue_peak, 4)}
+    if dom == "bvp_pairs" and mode == "precision" and N == 4000:
+        return {"kernel": dom, "bound": "issue", "achieved": issue, "peak": issue_peak,
+                "unit": "G warp-instructions/s", "frac": issue / issue_peak,
+                "traffic": BVP_PRECISION_DRAM_BYTES_N4000,
+                "peak_source": "152 SMs x 4 schedulers x 1 warp instruction per clock at the "
+                               "SM clock sampled during the timed region (%.0f MHz)" % sm_mhz,
+                "inst_per_pair": BVP_PRECISION_WARP_INST_PER_PAIR,
+                "fp64_pipe": table["bvp_pairs_fp64"], "all": table}
     if dom == "bvp_pairs":
-        return {"kernel": dom, "bound": "fp64", "achieved": ach, "peak": fp64_tflops,
-                "unit": "TFLOP/s", "frac": ach / fp64_tflops, "traffic": None,
+        return {"kernel": dom, "bound": "fp64", "achieved": fp64, "peak": fp64_tflops,
+                "unit": "TFLOP/s", "frac": fp64 / fp64_tflops, "traffic": None,
                 "peak_source": "measured live (pump_probe_fp64_tflops: FP64 FMA pipe; the "
                                "driver's peak file holds only HBM and bf16 figures)",
                 "flops_per_pair": BVP_FP64_FLOPS_PER_PAIR[mode], "all": table}

@@ -95,12 +95,17 @@ __global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, P
   __syncthreads();
   const long long tile = s_tile;
   const long long base = tile * kTile;
-  unsigned int ballots[kCompactRows];
+  // all predicates first (their loads in flight together), then the ballots
+  bool f[kCompactRows];
 #pragma unroll
   for (int r = 0; r < kCompactRows; ++r) {
     const long long i = base + r * kCompactThreads + threadIdx.x;
-    const bool f = i < n && pred(i);
-    ballots[r] = __ballot_sync(0xffffffffu, f);
+    f[r] = i < n && pred(i);
+  }
+  unsigned int ballots[kCompactRows];
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    ballots[r] = __ballot_sync(0xffffffffu, f[r]);
     if (lane == 0) s_cnt[r][warp] = __popc(ballots[r]);
   }
   __syncthreads();
@@ -183,6 +188,97 @@ pump_status_t finish_compact(const TileScratch &ts, unsigned long long *total, c
   PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
   if (err) return set_error(PUMP_ERR_TIMEOUT, "compaction: look-back wait exceeded its bound");
   return PUMP_OK;
+}
+
+// The edge list (mainPUMP.cu:327-346): the pairs with copt < rn in index
+// order, written as (i, j, copt, topt).  A specialisation of compact_kernel
+// that reads both pair arrays coalesced in the first phase, so the emit
+// phase does not wait on a dependent read per selected pair.
+__global__ void __launch_bounds__(kCompactThreads) edge_compact_kernel(
+    long long n, int N, const float *__restrict__ copts, const float *__restrict__ topts, float rn,
+    long long cap, int *__restrict__ src, int *__restrict__ dst, float *__restrict__ copt,
+    float *__restrict__ topt, TileScratch ts) {
+  __shared__ unsigned int s_tile;
+  __shared__ unsigned int s_cnt[kCompactRows][kCompactThreads / 32];
+  __shared__ unsigned long long s_excl;
+  __shared__ bool s_timeout;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(ts.tile_counter, 1u);
+    s_timeout = false;
+  }
+  __syncthreads();
+  const long long tile = s_tile;
+  const long long base = tile * kTile;
+  float c[kCompactRows], t[kCompactRows];
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    const long long i = base + r * kCompactThreads + threadIdx.x;
+    c[r] = i < n ? __ldg(&copts[i]) : 0.0f;
+    t[r] = i < n ? __ldg(&topts[i]) : 0.0f;
+  }
+  unsigned int ballots[kCompactRows];
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    const long long i = base + r * kCompactThreads + threadIdx.x;
+    ballots[r] = __ballot_sync(0xffffffffu, i < n && c[r] < rn);
+    if (lane == 0) s_cnt[r][warp] = __popc(ballots[r]);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    unsigned int v[4];
+    unsigned int run = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = lane * 4 + q;
+      v[q] = s_cnt[e / 8][e % 8];
+      run += v[q];
+    }
+    unsigned int incl = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned int o = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += o;
+    }
+    unsigned int ex = incl - run;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = lane * 4 + q;
+      s_cnt[e / 8][e % 8] = ex;
+      ex += v[q];
+    }
+    const unsigned int agg = __shfl_sync(0xffffffffu, incl, 31);
+    bool to = false;
+    const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
+    if (lane == 0) {
+      s_excl = ex_tile;
+      if (to) {
+        s_timeout = true;
+        atomicExch(ts.error, 1);
+      }
+      const long long ntiles = (n + kTile - 1) / kTile;
+      if (!to && tile == ntiles - 1) *ts.total = ex_tile + agg;
+    }
+  }
+  __syncthreads();
+  if (s_timeout) return;
+  const unsigned long long excl = s_excl;
+  const unsigned int lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    if (ballots[r] & (1u << lane)) {
+      const long long i = base + r * kCompactThreads + threadIdx.x;
+      const long long pos = (long long)(excl + s_cnt[r][warp] + __popc(ballots[r] & lt));
+      if (pos < cap) {
+        const int a = (int)(i / (N - 1));
+        const int b = (int)(i - (long long)a * (N - 1));
+        src[pos] = a;
+        dst[pos] = b + (b >= a);
+        copt[pos] = c[r];
+        topt[pos] = t[r];
+      }
+    }
+  }
 }
 
 // Exclusive scan of n counts: out[i] = count(0) + .. + count(i-1), the total

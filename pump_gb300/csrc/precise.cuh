@@ -140,11 +140,11 @@ struct QuarticF {
 
 
 // Root of a monotone function on [a, b] (sign change given) with fixed
-// convexity: Newton started at the end where the function and its curvature
-// have the same sign converges monotonically.  Binary32.
+// convexity: Newton started at x0, on the side where the function and its
+// curvature have the same sign, converges monotonically.  Binary32.
 template <int Deriv>
-__device__ float newton_f(const QuarticF &q, float a, float b, bool from_b) {
-  float x = from_b ? b : a;
+__device__ float newton_f(const QuarticF &q, float a, float b, float x0) {
+  float x = x0;
   for (int it = 0; it < 40; ++it) {
     const float f = Deriv ? q.dQ(x) : q.Q(x);
     const float df = Deriv ? q.d2Q(x) : q.dQ(x);
@@ -167,11 +167,29 @@ __device__ __forceinline__ int minima_f32(const QuarticF &q, float tmax, float *
   int nc = 0;
   float a = 0.0f, qa = -3.0f * q.A0;  // left end of the current piece and Q there
   const float tc = sqrtf(q.A2 / (6.0f * q.A4));
+  // Fujiwara's bound on the roots of the monic Q / A4 and Q' / (4 A4)
+  // (2 max |a_k / a_n|^(1 / (n - k)), the constant term halved), with 1 %
+  // margin: right-end Newton starts there instead of at tmax when that is
+  // closer, on the same side of the root (checked), so it converges from the
+  // same side in about half the steps.
+  const float rA4 = 1.0f / q.A4;
+  const float bq = 2.02f * fmaxf(sqrtf(fabsf(q.A2 * rA4)),
+                                 fmaxf(cbrtf(fabsf(2.0f * q.A1 * rA4)),
+                                       sqrtf(sqrtf(fabsf(1.5f * q.A0 * rA4)))));
+  const float bd = 2.02f * fmaxf(sqrtf(fabsf(0.5f * q.A2 * rA4)), cbrtf(fabsf(0.25f * q.A1 * rA4)));
+  auto start_q = [&](float b) {
+    const float x = fminf(b, bq);
+    return q.Q(x) >= 0.0f ? x : b;
+  };
+  auto start_d = [&](float b) {
+    const float x = fminf(b, bd);
+    return q.dQ(x) >= 0.0f ? x : b;
+  };
   // close the piece [a, b]: an upward sign change of Q is a minimum of the cost
   auto piece = [&](float b) {
     const float qb = q.Q(b);
     if (qa < 0.0f && qb > 0.0f && nc < 2) {
-      const float r = newton_f<0>(q, a, b, a >= tc);
+      const float r = newton_f<0>(q, a, b, a >= tc ? start_q(b) : a);
       if (nc == 0) *cand0 = r; else *cand1 = r;
       ++nc;
     }
@@ -181,13 +199,13 @@ __device__ __forceinline__ int minima_f32(const QuarticF &q, float tmax, float *
   const float d0 = -2.0f * q.A1;  // Q'(0)
   if (tc > 0.0f && tc < tmax) {
     const float dc = q.dQ(tc);
-    if (d0 > 0.0f && dc < 0.0f) piece(newton_f<1>(q, 0.0f, tc, false));
+    if (d0 > 0.0f && dc < 0.0f) piece(newton_f<1>(q, 0.0f, tc, 0.0f));
     piece(tc);
-    if (dc < 0.0f && q.dQ(tmax) > 0.0f) piece(newton_f<1>(q, tc, tmax, true));
+    if (dc < 0.0f && q.dQ(tmax) > 0.0f) piece(newton_f<1>(q, tc, tmax, start_d(tmax)));
   } else if (tc <= 0.0f) {
-    if (d0 < 0.0f && q.dQ(tmax) > 0.0f) piece(newton_f<1>(q, 0.0f, tmax, true));
+    if (d0 < 0.0f && q.dQ(tmax) > 0.0f) piece(newton_f<1>(q, 0.0f, tmax, start_d(tmax)));
   } else if (d0 > 0.0f && q.dQ(tmax) < 0.0f) {
-    piece(newton_f<1>(q, 0.0f, tmax, false));
+    piece(newton_f<1>(q, 0.0f, tmax, 0.0f));
   }
   piece(tmax);
   *tmax_cand = qa < 0.0f;

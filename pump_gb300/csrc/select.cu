@@ -120,27 +120,6 @@ __global__ void select_pick_kernel(SelectState *st, int shift, int bits, unsigne
 }
 
 // ------------------------------------------------------ compaction users
-struct EdgePred {
-  const float *copts;
-  float rn;
-  __device__ bool operator()(long long i) const { return __ldg(&copts[i]) < rn; }
-};
-struct EdgeEmit {
-  int N;
-  const float *copts, *topts;
-  long long cap;
-  int *src, *dst;
-  float *copt, *topt;
-  __device__ void operator()(long long idx, long long pos) const {
-    if (pos >= cap) return;
-    const int i = (int)(idx / (N - 1));
-    const int r = (int)(idx - (long long)i * (N - 1));
-    src[pos] = i;
-    dst[pos] = r + (r >= i);
-    copt[pos] = copts[idx];
-    topt[pos] = topts[idx];
-  }
-};
 // Edges the search can expand: free edge to a free node (PUMP.cu:52-53).
 struct OpenEdgePred {
   const uint8_t *free_e, *free_s;
@@ -252,9 +231,23 @@ pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_
                                  cudaStream_t stream) {
   const long long npairs = (long long)N * (N - 1);
   TileScratch ts{};
-  PUMP_TRY(run_compact(ctx, npairs, EdgePred{d_copts, rn},
-                       EdgeEmit{N, d_copts, d_topts, max_edges, d_src, d_dst, d_copt, d_topt},
-                       stream, &ts));
+  {
+    const long long ntiles = npairs > 0 ? (npairs + kTile - 1) / kTile : 1;
+    const size_t bytes = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
+    char *scratch = nullptr;
+    PUMP_TRY(ctx->scratch(Ctx::kCompact, bytes, (void **)&scratch));
+    ts.total = (unsigned long long *)scratch;
+    ts.status = ts.total + 1;
+    ts.tile_counter = (unsigned int *)(ts.status + ntiles + 1);
+    ts.error = (int *)(ts.tile_counter + 1);
+    PUMP_CUDA_TRY(cudaMemsetAsync(scratch, 0, bytes, stream));
+    if (npairs > 0) {
+      if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "build_edges: too many tiles");
+      edge_compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(
+          npairs, N, d_copts, d_topts, rn, max_edges, d_src, d_dst, d_copt, d_topt, ts);
+      PUMP_TRY(launch_status("edge_compact_kernel"));
+    }
+  }
   unsigned long long total = 0;
   PUMP_TRY(finish_compact(ts, &total, stream));
   *h_num_edges = (long long)total;
