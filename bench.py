@@ -563,8 +563,8 @@ def run_ours(args):
 BVP_FP64_FLOPS_PER_PAIR = {"precision": 28.0, "parity": 40.0 * 23 + 20.0}
 # The precision kernel is bound by instruction issue, not by one pipe: warp
 # instructions executed per pair on this workload (ncu smsp__inst_executed.sum
-# over one launch / pairs; profiles/bvp_pairs_precision_indoor4000.md), and
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum).
+# over one launch of the N = 4000 workload / its pairs), and DRAM bytes per
+# launch (dram__bytes_read.sum + dram__bytes_write.sum of the same launch).
 BVP_PRECISION_WARP_INST_PER_PAIR = 42.5
 BVP_PRECISION_DRAM_BYTES_N4000 = 0.16e6 + 66.71e6
 SMSP_PER_SM = 4

@@ -676,6 +676,52 @@ int orc_mccp(const float *path, int T, const float *pmajor, int T_stride, float 
   return hits;
 }
 
+/* The same Monte Carlo CP with every collision-test operation in binary64
+ * (positions path + offset * offsetMult formed in binary64): the binary64
+ * reference the binary32 estimate of the precision mode is stated against. */
+static int motion_valid64(const double *v, const double *w, const float *o) {
+  double bbMin[3], bbMax[3];
+  for (int d = 0; d < 3; ++d) {
+    if (v[d] > w[d]) { bbMin[d] = w[d]; bbMax[d] = v[d]; }
+    else { bbMin[d] = v[d]; bbMax[d] = w[d]; }
+  }
+  for (int d = 0; d < 3; ++d)
+    if (bbMax[d] <= o[d] || o[6 + d] <= bbMin[d]) return 1;
+  for (int j = 0; j < 3; ++j) {
+    const double v_to_w = w[j] - v[j];
+    const double lambda = v[j] < o[j] ? (o[j] - v[j]) / v_to_w : (o[6 + j] - v[j]) / v_to_w;
+    int inside = 1;
+    for (int d = 0; d < 3 && inside; ++d) {
+      const double pr = v[d] + (w[d] - v[d]) * lambda;
+      if (d != j && !(o[d] <= pr && pr <= o[6 + d])) inside = 0;
+    }
+    if (inside) return 0;
+  }
+  return 1;
+}
+
+int orc_mccp64(const float *path, int T, const float *pmajor, int T_stride, float offsetMult,
+               int nobs, const float *obs, int Pmc) {
+  int hits = 0;
+#pragma omp parallel for reduction(+ : hits) schedule(dynamic, 64)
+  for (int p = 0; p < Pmc; ++p) {
+    int coll = 0;
+    for (int t = 0; t < T - 2 && !coll; ++t) {
+      double v[3], w[3];
+      for (int d = 0; d < 3; ++d) {
+        v[d] = (double)path[t * ORC_DIM + d] +
+               (double)pmajor[((long long)p * T_stride + t) * 3 + d] * (double)offsetMult;
+        w[d] = (double)path[(t + 1) * ORC_DIM + d] +
+               (double)pmajor[((long long)p * T_stride + t + 1) * 3 + d] * (double)offsetMult;
+      }
+      for (int o = 0; o < nobs && !coll; ++o)
+        if (!motion_valid64(v, w, &obs[o * 12])) coll = 1;
+    }
+    hits += coll;
+  }
+  return hits;
+}
+
 /* ======================================================================
  * Frontier compaction (GMT.cu:48-76, 166-176)
  * ==================================================================== */

@@ -122,6 +122,10 @@ int orc_mccp(const float *path, int T, const float *pmajor, int T_stride, float 
              int nobs, const float *obs, int Pmc, float *cp);
 
 /* ---------------- frontier compaction (GMT.cu:48-76, 166-176) ---------------- */
+/* orc_mccp with the collision tests in binary64; returns the hits. */
+int orc_mccp64(const float *path, int T, const float *pmajor, int T_stride, float offsetMult,
+               int nobs, const float *obs, int Pmc);
+
 /* Exclusive scan of flags then scatter of set indices; returns the count. */
 int orc_frontier_compact(int N, const uint8_t *flags, int *active);
 

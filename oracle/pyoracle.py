@@ -116,6 +116,8 @@ def lib():
             L.orc_hsmc_propagate.argtypes = [C.c_int, C.c_int, i32p, i32p, C.c_int, f32p, f32p,
                                              f32p, f32p, C.c_float, C.c_int, f32p, C.c_float,
                                              C.c_int, u8p, C.c_int, f32p]
+            L.orc_mccp64.restype = C.c_int
+            L.orc_mccp64.argtypes = [f32p, C.c_int, f32p, C.c_int, C.c_float, C.c_int, f32p, C.c_int]
             L.orc_mccp.restype = C.c_int
             L.orc_mccp.argtypes = [f32p, C.c_int, f32p, C.c_int, C.c_float, C.c_int, f32p,
                                    C.c_int, C.POINTER(C.c_float)]
@@ -285,6 +287,14 @@ def path_cp(nodes, pmajor, offsetMult, obstacles, dt=np.float32(0.05)):
         return -1.0, float(c), ln.value
     _, cp = mccp(split[: ln.value * 6], ln.value, pmajor, offsetMult, obstacles)
     return cp, float(c), ln.value
+
+
+def mccp64(path, T, pmajor, offsetMult, obstacles):
+    """Hits of the Monte Carlo CP with the collision tests in binary64."""
+    ob = f32(obstacles).reshape(-1)
+    Pmc, Ts = pmajor.shape[0], pmajor.shape[1]
+    return lib().orc_mccp64(f32(path).reshape(-1), T, f32(pmajor).reshape(-1), Ts, offsetMult,
+                            ob.size // 12, ob, Pmc)
 
 
 def plan(N, obstacles, init, goal, lo, hi, offsetMult, cpTarget, cpFactor, numDisc=8, P=128,
