@@ -76,6 +76,18 @@ pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tm
                                          float *d_topts, cudaStream_t stream);
 pump_status_t bvp_batch_precision_launch(const float *d_x0, const float *d_x1, int n, float tmax,
                                          float *d_topt, float *d_cost, cudaStream_t stream);
+// Device buffers of a batch of candidate paths (node states of each path,
+// contiguous): its segments as explicit pairs, their optimal times (tmax 5)
+// and smoothing costs (tmax 2), the dense path of findOptimalPath per path
+// at a fixed stride of rows_cap rows, and per path its length and cost.
+struct CandidateBufs {
+  const float *nodes;
+  const int *node_off, *node_cnt, *seg_base;
+  float *x0, *x1, *topt, *seg_cost, *seg_toff, *states, *cost;
+  int *seg_path, *seg_T, *seg_row, *len;
+};
+pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_seg, int mode,
+                                    float dt, bool with_cost, int rows_cap, cudaStream_t s);
 pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
                               const float *d_tau, int total, float *d_out, cudaStream_t stream);
 

@@ -3,12 +3,11 @@
 //
 // Device work: pair BVPs, rn selection, edge compaction, waypoints,
 // heuristic, sample/edge collision checks, half-spaces, the particle table,
-// HSMC propagation of every wavefront, and the dense paths and Monte Carlo
-// CP of goal candidates and smoothing iterates.  Host work is the same
-// sequential bookkeeping the reference does on the host: wavefront
-// expansion, the CP cut-off, epsilon-dominance with the path-index
-// tie-break, survivor compaction into cost buckets, and the alpha bisection
-// of the smoothing loop.  Differences in structure, not in results:
+// the search loop (search.cu: expansion, HSMC, CP cut-off, epsilon
+// dominance, survivor compaction, buckets), and the dense paths and Monte
+// Carlo CP of goal candidates and smoothing iterates.  The host keeps the
+// loop control of the search and the alpha bisection of the smoothing loop.
+// Differences in structure, not in results:
 //  - the reference copies each survivor's particle mask with one
 //    cudaMemcpy (PUMP.cu:236-237); here survivors are gathered by one kernel;
 //  - the reference evaluates goal candidates one at a time until one meets
@@ -127,13 +126,6 @@ struct SharedRoadmap {
   }
 };
 
-// Batch of dense paths along node sequences (findOptimalPath, 2pBVP.cu:5-36):
-// segment optimal times on the GPU, the sample-time recurrence on the host,
-// the states on the GPU.
-struct DensePaths {
-  std::vector<int> offset, len;  // per path, in states
-  int total = 0;
-};
 
 class Planner {
  public:
@@ -156,12 +148,15 @@ class Planner {
   pump_status_t refine(const std::vector<float> &xs, float cpTarget, float *lastCP,
                        float *lastCost, std::vector<float> *bestPath, int *bestLen,
                        std::vector<float> *xsFinal);
-  pump_status_t dense_paths(const std::vector<std::vector<float>> &xs, float dt, float tmax,
-                            DensePaths &out, DevBuf<float> &d_states);
+  // Candidate paths evaluated on the device (candidate_paths_async): per
+  // path the dense length, the smoothing's cost and the MC CP (-1 when the
+  // dense path has more states than the table has rows); states of path k
+  // at d_cstates_ + k * rows_cap rows.
+  pump_status_t eval_candidates(const std::vector<std::vector<float>> &xs, float dt, int rows_cap,
+                                bool with_cost, bool with_cp, std::vector<int> &len,
+                                std::vector<float> &cost, std::vector<float> &cp);
   pump_status_t topts_of(const std::vector<float> &x0, const std::vector<float> &x1, float tmax,
                          std::vector<float> *topt, std::vector<float> *cost);
-  pump_status_t mc_cp_batch(const DevBuf<float> &d_states, const DensePaths &dp,
-                            std::vector<float> &cp);
   pump_status_t sync() { return cuda_status(cudaStreamSynchronize(s_), "cudaStreamSynchronize"); }
   template <class T>
   pump_status_t h2d(T *d, const T *h, size_t n) {
@@ -219,7 +214,10 @@ class Planner {
   int numPaths_ = 0;
   // reusable scratch of the batched BVP / dense-path / MC CP helpers
   DevBuf<float> d_bx0_, d_bx1_, d_bt_, d_bc_, d_xs_, d_ts_, d_tau_, d_mcp_;
-  DevBuf<int> d_seg_, d_moff_, d_mlen_, d_mhits_;
+  DevBuf<int> d_seg_, d_mhits_;
+  // candidate batches
+  DevBuf<float> d_cnodes_, d_cx0_, d_cx1_, d_ctopt_, d_csegcost_, d_ctoff_, d_cstates_, d_ccost_;
+  DevBuf<int> d_cints_, d_csegpath_, d_csegT_, d_csegrow_, d_clen_;
 };
 
 pump_status_t Planner::run() {
@@ -595,97 +593,76 @@ pump_status_t Planner::topts_of(const std::vector<float> &x0, const std::vector<
   return sync();
 }
 
-pump_status_t Planner::dense_paths(const std::vector<std::vector<float>> &xs, float dt, float tmax,
-                                   DensePaths &out, DevBuf<float> &d_states) {
-  std::vector<float> x0, x1;
-  std::vector<int> segBase(xs.size() + 1, 0);
-  for (size_t k = 0; k < xs.size(); ++k) {
-    const int n = (int)(xs[k].size() / kDim);
-    segBase[k + 1] = segBase[k] + (n > 1 ? n - 1 : 0);
-    for (int i = 0; i + 1 < n; ++i) {
-      x0.insert(x0.end(), &xs[k][i * kDim], &xs[k][(i + 1) * kDim]);
-      x1.insert(x1.end(), &xs[k][(i + 1) * kDim], &xs[k][(i + 2) * kDim]);
-    }
-  }
-  std::vector<float> topt;
-  PUMP_TRY(topts_of(x0, x1, tmax, &topt, nullptr));
-  // host recurrence of findOptimalPath (2pBVP.cu:15-32)
-  std::vector<float> allxs, tsample;
-  std::vector<int> seg;
-  out.offset.assign(xs.size(), 0);
-  out.len.assign(xs.size(), 0);
-  int total = 0;
-  for (size_t k = 0; k < xs.size(); ++k) {
-    const int n = (int)(xs[k].size() / kDim);
-    const int xbase = (int)(allxs.size() / kDim);
-    allxs.insert(allxs.end(), xs[k].begin(), xs[k].end());
-    out.offset[k] = total;
-    float toff = 0, t = 0;
-    int Tprev = 0;
-    for (int i = 0; i < n - 1; ++i) {
-      const float tp = topt[segBase[k] + i];
-      const int T = (int)((tp - toff) / dt + 1);
-      for (int tidx = 0; tidx < T; ++tidx) {
-        t = dt * tidx + toff;
-        seg.push_back(xbase + i);
-        tsample.push_back(t);
-      }
-      Tprev += T;
-      toff = (t - tp) + dt;
-    }
-    out.len[k] = Tprev;
-    total += Tprev;
-  }
-  out.total = total;
-  // tau indexed by global segment (xbase + i); rebuild as per-node-pair table
-  std::vector<float> tauByPair(allxs.size() / kDim, 0.0f);
-  {
-    int xb = 0, sb = 0;
-    for (size_t k = 0; k < xs.size(); ++k) {
-      const int n = (int)(xs[k].size() / kDim);
-      for (int i = 0; i + 1 < n; ++i) tauByPair[xb + i] = topt[sb + i];
-      xb += n;
-      sb += n > 1 ? n - 1 : 0;
-    }
-  }
-  PUMP_TRY(d_states.alloc((size_t)(total > 0 ? total : 1) * kDim));
-  if (total > 0) {
-    PUMP_TRY(d_xs_.alloc(allxs.size()));
-    PUMP_TRY(d_ts_.alloc(total));
-    PUMP_TRY(d_tau_.alloc(tauByPair.size()));
-    PUMP_TRY(d_seg_.alloc(total));
-    PUMP_TRY(h2d(d_xs_.p, allxs.data(), allxs.size()));
-    PUMP_TRY(h2d(d_ts_.p, tsample.data(), total));
-    PUMP_TRY(h2d(d_tau_.p, tauByPair.data(), tauByPair.size()));
-    PUMP_TRY(h2d(d_seg_.p, seg.data(), total));
-    PUMP_TRY(bvp_path_states(d_xs_.p, d_seg_.p, d_ts_.p, d_tau_.p, total, d_states.p, s_));
-    PUMP_TRY(sync());
-  }
-  return PUMP_OK;
-}
-
-pump_status_t Planner::mc_cp_batch(const DevBuf<float> &d_states, const DensePaths &dp,
-                                   std::vector<float> &cp) {
-  // Paths longer than the particle table get CP -1 (checked by the caller
-  // only if it actually uses that path; speculative batches may hold some).
-  const int n = (int)dp.len.size();
+pump_status_t Planner::eval_candidates(const std::vector<std::vector<float>> &xs, float dt,
+                                      int rows_cap, bool with_cost, bool with_cp,
+                                      std::vector<int> &len, std::vector<float> &cost,
+                                      std::vector<float> &cp) {
+  const int n = (int)xs.size();
+  len.assign(n, 0);
+  cost.assign(n, 0.0f);
   cp.assign(n, 0.0f);
   if (n == 0) return PUMP_OK;
-  std::vector<int> len(dp.len);
-  for (int k = 0; k < n; ++k)
-    if (len[k] > pb_.table_rows) len[k] = 0;
-  PUMP_TRY(d_moff_.alloc(n));
-  PUMP_TRY(d_mlen_.alloc(n));
-  PUMP_TRY(d_mhits_.alloc(n));
-  PUMP_TRY(d_mcp_.alloc(n));
-  PUMP_TRY(h2d(d_moff_.p, dp.offset.data(), n));
-  PUMP_TRY(h2d(d_mlen_.p, len.data(), n));
-  PUMP_TRY(mc_cp_async(d_states.p, d_moff_.p, d_mlen_.p, n, d_table_, pb_.num_mc, pb_.table_rows,
-                       pb_.offset_mult, obs_p_, nobs_, d_mhits_.p, d_mcp_.p, nullptr, s_));
-  PUMP_TRY(d2h(cp.data(), d_mcp_.p, n));
+  // nodes | node offsets, counts, segment bases, dense-path offsets
+  std::vector<float> nodes;
+  std::vector<int> ints(4 * (size_t)n);
+  int rows = 0, segs = 0;
+  for (int k = 0; k < n; ++k) {
+    const int c = (int)(xs[k].size() / kDim);
+    ints[k] = rows;
+    ints[n + k] = c;
+    ints[2 * n + k] = segs;
+    ints[3 * n + k] = k * rows_cap;
+    nodes.insert(nodes.end(), xs[k].begin(), xs[k].end());
+    rows += c;
+    segs += c > 1 ? c - 1 : 0;
+  }
+  PUMP_TRY(d_cnodes_.alloc(nodes.size()));
+  PUMP_TRY(d_cints_.alloc(ints.size()));
+  PUMP_TRY(h2d(d_cnodes_.p, nodes.data(), nodes.size()));
+  PUMP_TRY(h2d(d_cints_.p, ints.data(), ints.size()));
+  const size_t sg = segs > 0 ? (size_t)segs : 1;
+  PUMP_TRY(d_cx0_.alloc(sg * kDim));
+  PUMP_TRY(d_cx1_.alloc(sg * kDim));
+  PUMP_TRY(d_ctopt_.alloc(sg));
+  PUMP_TRY(d_csegcost_.alloc(sg));
+  PUMP_TRY(d_ctoff_.alloc(sg));
+  PUMP_TRY(d_csegpath_.alloc(sg));
+  PUMP_TRY(d_csegT_.alloc(sg));
+  PUMP_TRY(d_csegrow_.alloc(sg));
+  PUMP_TRY(d_clen_.alloc(n));
+  PUMP_TRY(d_ccost_.alloc(n));
+  PUMP_TRY(d_cstates_.alloc((size_t)n * rows_cap * kDim));
+  CandidateBufs cb{};
+  cb.nodes = d_cnodes_.p;
+  cb.node_off = d_cints_.p;
+  cb.node_cnt = d_cints_.p + n;
+  cb.seg_base = d_cints_.p + 2 * n;
+  cb.x0 = d_cx0_.p;
+  cb.x1 = d_cx1_.p;
+  cb.topt = d_ctopt_.p;
+  cb.seg_cost = d_csegcost_.p;
+  cb.seg_toff = d_ctoff_.p;
+  cb.states = d_cstates_.p;
+  cb.cost = d_ccost_.p;
+  cb.seg_path = d_csegpath_.p;
+  cb.seg_T = d_csegT_.p;
+  cb.seg_row = d_csegrow_.p;
+  cb.len = d_clen_.p;
+  PUMP_TRY(candidate_paths_async(cb, n, segs, pb_.bvp_mode, dt, with_cost, rows_cap, s_));
+  if (with_cp) {
+    PUMP_TRY(d_mhits_.alloc(n));
+    PUMP_TRY(d_mcp_.alloc(n));
+    PUMP_TRY(mc_cp_async(d_cstates_.p, d_cints_.p + 3 * n, d_clen_.p, n, d_table_, pb_.num_mc,
+                         pb_.table_rows, pb_.offset_mult, obs_p_, nobs_, d_mhits_.p, d_mcp_.p,
+                         nullptr, s_));
+    PUMP_TRY(d2h(cp.data(), d_mcp_.p, n));
+  }
+  PUMP_TRY(d2h(len.data(), d_clen_.p, n));
+  if (with_cost) PUMP_TRY(d2h(cost.data(), d_ccost_.p, n));
   PUMP_TRY(sync());
-  for (int k = 0; k < n; ++k)
-    if (dp.len[k] > pb_.table_rows) cp[k] = -1.0f;
+  if (with_cp)
+    for (int k = 0; k < n; ++k)
+      if (len[k] > pb_.table_rows) cp[k] = -1.0f;
   return PUMP_OK;
 }
 
@@ -698,16 +675,15 @@ pump_status_t Planner::search_and_smooth() {
   std::sort(goalPaths.begin(), goalPaths.end());
   std::vector<std::vector<float>> cand;
   for (auto &g : goalPaths) cand.push_back(node_states(g.second, nullptr));
-  DensePaths dp;
-  DevBuf<float> d_states;
-  PUMP_TRY(dense_paths(cand, dt_, 5.0f, dp, d_states));
-  std::vector<float> cps;
-  PUMP_TRY(mc_cp_batch(d_states, dp, cps));
+  const int rowsCap = pb_.table_rows;
+  std::vector<int> glen;
+  std::vector<float> gcost, cps;
+  PUMP_TRY(eval_candidates(cand, dt_, rowsCap, false, true, glen, gcost, cps));
   int sel = -1;
   for (size_t k = 0; k < goalPaths.size(); ++k) {
     if (cps[k] < 0)
       return set_error(PUMP_ERR_CAPACITY, "goal path of %d states exceeds the %d-row particle table",
-                       dp.len[k], pb_.table_rows);
+                       glen[k], pb_.table_rows);
     if (cps[k] < cpTarget) { sel = (int)k; break; }
   }
   const int last = sel >= 0 ? sel : (int)goalPaths.size() - 1;
@@ -727,10 +703,10 @@ pump_status_t Planner::search_and_smooth() {
   std::vector<float> xsFinal(xs.size(), 0.0f);
   std::vector<float> xsBest(xs);  // nodes of the path kept so far
   std::vector<float> bestPath;
-  int bestLen = last >= 0 ? dp.len[last] : 0;
+  int bestLen = last >= 0 ? glen[last] : 0;
   if (last >= 0 && bestLen > 0) {
     bestPath.resize((size_t)bestLen * kDim);
-    PUMP_TRY(d2h(bestPath.data(), d_states.p + (size_t)dp.offset[last] * kDim, bestPath.size()));
+    PUMP_TRY(d2h(bestPath.data(), d_cstates_.p + (size_t)last * rowsCap * kDim, bestPath.size()));
     PUMP_TRY(sync());
   }
   float lastCP = solnPathCP, lastCost = solnPathCost;
@@ -740,12 +716,16 @@ pump_status_t Planner::search_and_smooth() {
     std::vector<std::vector<float>> two(1);
     two[0].insert(two[0].end(), xs.begin(), xs.begin() + kDim);
     two[0].insert(two[0].end(), xs.end() - kDim, xs.end());
-    DensePaths opt;
-    DevBuf<float> d_opt;
-    PUMP_TRY(dense_paths(two, dt_ / dtMult, 5.0f, opt, d_opt));
-    const int optLen = opt.len[0];
+    const int optCap = pb_.table_rows * dtMult;
+    std::vector<int> olen;
+    std::vector<float> ocost, ocp;
+    PUMP_TRY(eval_candidates(two, dt_ / dtMult, optCap, false, false, olen, ocost, ocp));
+    const int optLen = olen[0];
+    if (optLen > optCap)
+      return set_error(PUMP_ERR_CAPACITY, "unconstrained optimal path of %d states exceeds %d",
+                       optLen, optCap);
     std::vector<float> optPath((size_t)optLen * kDim);
-    PUMP_TRY(d2h(optPath.data(), d_opt.p, optPath.size()));
+    PUMP_TRY(d2h(optPath.data(), d_cstates_.p, optPath.size()));
     // splitPathTopts with tmax 2 (PUMP.cu:445-450)
     std::vector<float> a0, a1, tsplit;
     for (int i = 0; i + 1 < n; ++i) {
@@ -782,28 +762,18 @@ pump_status_t Planner::search_and_smooth() {
         na[2 * k + 2] = (nl[2 * k + 2] + nu[2 * k + 2]) / 2;
       }
       std::vector<std::vector<float>> cand(K, std::vector<float>(xs.size()));
-      std::vector<float> b0, b1;
-      for (int k = 0; k < K; ++k) {
+      for (int k = 0; k < K; ++k)
         for (size_t i = 0; i < xs.size(); ++i) cand[k][i] = (1 - na[k]) * xs[i] + na[k] * xsOpt[i];
-        for (int i = 0; i + 1 < n; ++i) {
-          b0.insert(b0.end(), &cand[k][i * kDim], &cand[k][(i + 1) * kDim]);
-          b1.insert(b1.end(), &cand[k][(i + 1) * kDim], &cand[k][(i + 2) * kDim]);
-        }
-      }
-      DensePaths sp;
-      DevBuf<float> d_sp;
-      PUMP_TRY(dense_paths(cand, dt_, 5.0f, sp, d_sp));
-      std::vector<float> sc, cps;
-      PUMP_TRY(topts_of(b0, b1, 2.0f, nullptr, &sc));
-      PUMP_TRY(mc_cp_batch(d_sp, sp, cps));
+      std::vector<int> slen;
+      std::vector<float> scost, cps;
+      PUMP_TRY(eval_candidates(cand, dt_, rowsCap, true, true, slen, scost, cps));
       int k = 0;
       for (int depth = 0; depth < D && it < 30; ++depth, ++it) {
-        float smoothCost = 0;
-        for (int i = 0; i + 1 < n; ++i) smoothCost += sc[(size_t)k * (n - 1) + i];
+        const float smoothCost = scost[k];
         const float cp = cps[k];
         if (cp < 0)
           return set_error(PUMP_ERR_CAPACITY, "smoothed path of %d states exceeds the %d-row particle table",
-                           sp.len[k], pb_.table_rows);
+                           slen[k], pb_.table_rows);
         xsFinal = cand[k];
         if (cp < cpTarget) alphaL = alpha;
         if (cp >= cpTarget) alphaU = alpha;
@@ -812,9 +782,9 @@ pump_status_t Planner::search_and_smooth() {
         const bool closer = cp > lastCP;
         const bool eqLower = (cp == lastCP && smoothCost < lastCost);
         if (satisfies && (closer || eqLower)) {
-          bestLen = sp.len[k];
+          bestLen = slen[k];
           bestPath.resize((size_t)bestLen * kDim);
-          PUMP_TRY(d2h(bestPath.data(), d_sp.p + (size_t)sp.offset[k] * kDim, bestPath.size()));
+          PUMP_TRY(d2h(bestPath.data(), d_cstates_.p + (size_t)k * rowsCap * kDim, bestPath.size()));
           PUMP_TRY(sync());
           lastCost = smoothCost;
           lastCP = cp;
@@ -846,25 +816,13 @@ pump_status_t Planner::evaluate_paths(const std::vector<std::vector<float>> &xs,
   d_table_ = d_table;
   obs_p_ = d_obs;
   nobs_ = nobs;
-  DensePaths dp;
-  DevBuf<float> d_states;
-  PUMP_TRY(dense_paths(xs, dt_, 5.0f, dp, d_states));
-  std::vector<float> cps;
-  PUMP_TRY(mc_cp_batch(d_states, dp, cps));
-  std::vector<float> a0, a1, sc;
-  for (const auto &x : xs)
-    for (size_t i = 0; i + 1 < x.size() / kDim; ++i) {
-      a0.insert(a0.end(), &x[i * kDim], &x[(i + 1) * kDim]);
-      a1.insert(a1.end(), &x[(i + 1) * kDim], &x[(i + 2) * kDim]);
-    }
-  PUMP_TRY(topts_of(a0, a1, 2.0f, nullptr, &sc));
-  size_t q = 0;
+  std::vector<int> ln;
+  std::vector<float> cs, cps;
+  PUMP_TRY(eval_candidates(xs, dt_, pb_.table_rows, true, true, ln, cs, cps));
   for (size_t k = 0; k < xs.size(); ++k) {
-    float c = 0;
-    for (size_t i = 0; i + 1 < xs[k].size() / kDim; ++i) c += sc[q++];
     cp[k] = cps[k];
-    cost[k] = c;
-    len[k] = dp.len[k];
+    cost[k] = cs[k];
+    len[k] = ln[k];
   }
   return PUMP_OK;
 }
@@ -918,26 +876,17 @@ pump_status_t Planner::refine(const std::vector<float> &xs, float cpTarget, floa
   PUMP_TRY(d2h(xr.data(), d_out.p, xr.size()));
   PUMP_TRY(sync());
   std::vector<std::vector<float>> one(1, xr);
-  DensePaths dp;
-  DevBuf<float> d_states;
-  PUMP_TRY(dense_paths(one, dt_, 5.0f, dp, d_states));
-  std::vector<float> cps;
-  PUMP_TRY(mc_cp_batch(d_states, dp, cps));
-  std::vector<float> a0, a1, sc;
-  for (int i = 0; i + 1 < n; ++i) {
-    a0.insert(a0.end(), &xr[(size_t)i * kDim], &xr[(size_t)(i + 1) * kDim]);
-    a1.insert(a1.end(), &xr[(size_t)(i + 1) * kDim], &xr[(size_t)(i + 2) * kDim]);
-  }
-  PUMP_TRY(topts_of(a0, a1, 2.0f, nullptr, &sc));
-  float cost = 0;
-  for (int i = 0; i + 1 < n; ++i) cost += sc[i];
+  std::vector<int> ln;
+  std::vector<float> cs, cps;
+  PUMP_TRY(eval_candidates(one, dt_, pb_.table_rows, true, true, ln, cs, cps));
+  const float cost = cs[0];
   res_->refine_cp = cps[0];
   res_->refine_cost = cost;
   if (cps[0] >= 0 && cps[0] <= cpTarget && cost < *lastCost) {
     res_->refined = 1;
-    *bestLen = dp.len[0];
-    bestPath->resize((size_t)dp.len[0] * kDim);
-    PUMP_TRY(d2h(bestPath->data(), d_states.p, bestPath->size()));
+    *bestLen = ln[0];
+    bestPath->resize((size_t)ln[0] * kDim);
+    PUMP_TRY(d2h(bestPath->data(), d_cstates_.p, bestPath->size()));
     PUMP_TRY(sync());
     *lastCP = cps[0];
     *lastCost = cost;
