@@ -408,6 +408,7 @@ def run_ours(args):
     d_fs, d_fe = empty(N, torch.uint8), empty(cap, torch.uint8)
     maxHS = min(obs_host.shape[0], 5)
     d_a, d_b = empty(cap * W * maxHS * 3, torch.float32), empty(cap * W * maxHS, torch.float32)
+    d_hn = empty(cap * W, torch.uint8)  # stored half-spaces per waypoint
     Pmc, T = 2048, 400
     d_tab = empty(T * Pmc * 3, torch.float32)
     lib.check(L.pump_particle_tables(pb.seed, Pmc, T, d_tab.data_ptr(), None, sh))
@@ -453,9 +454,9 @@ def run_ours(args):
         timed("free_edges", lambda: lib.check(L.pump_free_edges(
             d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), Eo.value, W - 1,
             d_fe.data_ptr(), sh)), 1)
-        timed("halfspaces", lambda: lib.check(L.pump_cache_halfspaces(
+        timed("halfspaces", lambda: lib.check(L.pump_cache_halfspaces_sparse(
             d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), d_fe.data_ptr(), Eo.value, W,
-            maxHS, maxd2, d_a.data_ptr(), d_b.data_ptr(), None, sh)), 1)
+            maxHS, maxd2, d_a.data_ptr(), d_b.data_ptr(), d_hn.data_ptr(), sh)), 1)
 
         def hsmc_all():
             for it, m in enumerate(sizes):
@@ -464,7 +465,7 @@ def run_ours(args):
                     m, W, d_edge.data_ptr() + 4 * o, d_prev.data_ptr() + 4 * o, E, base,
                     d_a.data_ptr(), d_b.data_ptr(), maxHS, d_times.data_ptr(), d_te.data_ptr(), 0.05,
                     d_tab.data_ptr(), Pmc, T, float(w["offset_mult"]), d_valid.data_ptr(), P,
-                    d_cp.data_ptr(), d_err.data_ptr(), sh))
+                    d_cp.data_ptr(), d_err.data_ptr(), d_hn.data_ptr(), sh))
         timed("hsmc", hsmc_all, len(sizes))
 
     for _ in range(args.warmup):
@@ -585,7 +586,7 @@ def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops, sm_mhz):
         "build_edges": 4.0 * N * (N - 1) + 16.0 * E,          # costs read, 4 arrays out
         "discretize": 16.0 * E + 24.0 * W * E,                # edge in, waypoints out
         "free_edges": 24.0 * W * E + E,                       # waypoints in, mask out
-        "halfspaces": 24.0 * W * E + E + 16.0 * W * H * E,    # waypoints in, a/b out
+        "halfspaces": 24.0 * W * E + E + 1.0 * W * E,         # waypoints in, counts out
         "hsmc": M * (8 + 4 + 2 * 4 * ((P + 31) // 32) + 4.0 * W * H),
     }
     table = {}

@@ -125,6 +125,18 @@ pump_status_t pump_cache_halfspaces(const float *d_obstacles, int numObs, const 
                                     float maxd2, float *d_as, float *d_bs, int *d_count,
                                     pump_stream_t stream);
 
+/* The same half-spaces without the defaults: only the stored ones are
+ * written (as[e][w][h] for h < count[e][w]; the slots past a waypoint's
+ * count keep what the buffers held) and count is one byte per waypoint.
+ * What the search reads is the same: pass d_count to pump_hsmc_propagate.
+ * maxHS <= 8.  Not a reference function: the reference's arrays are the
+ * dense layout above. */
+pump_status_t pump_cache_halfspaces_sparse(const float *d_obstacles, int numObs,
+                                           const float *d_disc, const uint8_t *d_is_free_edge,
+                                           long long E, int W, int maxHS, float maxd2,
+                                           float *d_as, float *d_bs, uint8_t *d_count,
+                                           pump_stream_t stream);
+
 /* --------------------------------------------------------------- HSMC */
 /* Particle tables of the closed-loop tracking-error model (the data of the
  * reference's missing hardCoded.cu, hardCoded.cuh:12-19): position errors
@@ -144,13 +156,15 @@ pump_status_t pump_particle_tables(uint64_t seed, int P, int T, float *d_tmajor,
  * Device-side checks write *d_error (device, may be NULL): an edge outside
  * [0, num_edges) or a parent outside [0, base) skips that path and records
  * PUMP_ERR_BAD_INPUT; a time row past T_rows records PUMP_ERR_CAPACITY.
- * Writes path_cp[base+i]. */
+ * Writes path_cp[base+i].  d_hs_count (may be NULL): the stored half-spaces
+ * per waypoint of pump_cache_halfspaces_sparse; with it only those slots are
+ * read, without it every slot is read and b >= 1000 marks an unused one. */
 pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_edge, const int *d_prev,
                                   long long num_edges, int base, const float *d_as, const float *d_bs, int maxHS,
                                   const float *d_times, const float *d_topt, float dt,
                                   const float *d_offsets_t, int Pmc, int T_rows,
                                   float offset_mult, uint32_t *d_valid, int P, float *d_path_cp,
-                                  int *d_error, pump_stream_t stream);
+                                  int *d_error, const uint8_t *d_hs_count, pump_stream_t stream);
 
 /* Full Monte Carlo collision probability of n_paths dense paths at once
  * (MCCP + thrust::reduce, collisionProbability.cu:4-92).  Path k has

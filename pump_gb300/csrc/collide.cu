@@ -212,10 +212,16 @@ constexpr int kStagedMaxHS = 8;
 constexpr int kHsThreads = 256;
 constexpr int kHsMaxEdges = kHsThreads / 2 + 2;  // W >= 2
 
+// Dense: every slot written (unused ones get the defaults), int counts.
+// Sparse (!Dense): only the stored half-spaces are written, straight to
+// global memory, with one-byte counts; slots at or past a waypoint's count
+// are left as they are (their readers stop at the count).
+template <bool Dense>
 __global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
     const float *__restrict__ obs, int numObs, const float *__restrict__ disc,
     const uint8_t *__restrict__ is_free_edge, long long E, int W, int maxHS, float maxd2,
-    float *__restrict__ as, float *__restrict__ bs, int *__restrict__ count) {
+    float *__restrict__ as, float *__restrict__ bs, int *__restrict__ count,
+    uint8_t *__restrict__ count8) {
   extern __shared__ float4 s_dyn4[];
   __shared__ float s_eb[kHsMaxEdges][6];  // edge bounding box: min[3], max[3]
   __shared__ uint32_t s_mask[kHsMaxEdges][kFilterObs / 32];
@@ -279,7 +285,8 @@ __global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
   if (t < nv) {
     const long long wp = wp0 + t;
     const int el = (int)(wp / W - e0);
-    float *a = s_a + t * maxHS * 3, *b = s_b + t * maxHS;
+    float *a = Dense ? s_a + t * maxHS * 3 : as + wp * maxHS * 3;
+    float *b = Dense ? s_b + t * maxHS : bs + wp * maxHS;
     int stored = 0;
     if (is_free_edge[wp / W]) {
       float pos[3], vel[3];
@@ -337,22 +344,28 @@ __global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
         ++stored;
       }
     }
-    for (int h = stored; h < maxHS; ++h) {
-      a[h * 3 + 0] = -1.0f;
-      a[h * 3 + 1] = -1.0f;
-      a[h * 3 + 2] = -1.0f;
-      b[h] = 1111.0f;
+    if (Dense) {
+      for (int h = stored; h < maxHS; ++h) {
+        a[h * 3 + 0] = -1.0f;
+        a[h * 3 + 1] = -1.0f;
+        a[h * 3 + 2] = -1.0f;
+        b[h] = 1111.0f;
+      }
+      if (count) count[wp] = stored;
+    } else {
+      count8[wp] = (uint8_t)stored;
     }
-    if (count) count[wp] = stored;
   }
-  __syncthreads();
-  block_store(as + wp0 * maxHS * 3, s_a, nv * maxHS * 3);
-  block_store(bs + wp0 * maxHS, s_b, nv * maxHS);
+  if (Dense) {
+    __syncthreads();
+    block_store(as + wp0 * maxHS * 3, s_a, nv * maxHS * 3);
+    block_store(bs + wp0 * maxHS, s_b, nv * maxHS);
+  }
 }
 
-size_t halfspace_staged_smem(int numObs, int maxHS) {
+size_t halfspace_staged_smem(int numObs, int maxHS, bool dense) {
   return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)kHsThreads * kDim +
-                          (size_t)kHsThreads * maxHS * 4);
+                          (dense ? (size_t)kHsThreads * maxHS * 4 : 0));
 }
 
 pump_status_t obstacle_smem(int numObs, size_t *bytes) {
@@ -426,15 +439,43 @@ extern "C" pump_status_t pump_cache_halfspaces(const float *d_obstacles, int num
   }
   size_t smem;
   PUMP_TRY(obstacle_smem(numObs, &smem));
-  const size_t staged = halfspace_staged_smem(numObs, maxHS);
+  const size_t staged = halfspace_staged_smem(numObs, maxHS, true);
   if (maxHS <= kStagedMaxHS && staged <= 220 * 1024) {
-    PUMP_TRY(set_smem_attr((const void *)halfspace_staged_kernel, staged));
-    halfspace_staged_kernel<<<grid_for(E * W, kHsThreads), kHsThreads, staged, (cudaStream_t)stream>>>(
-        d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, d_count);
+    PUMP_TRY(set_smem_attr((const void *)halfspace_staged_kernel<true>, staged));
+    halfspace_staged_kernel<true><<<grid_for(E * W, kHsThreads), kHsThreads, staged,
+                                    (cudaStream_t)stream>>>(
+        d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, d_count,
+        nullptr);
     return launch_status("cache_halfspaces");
   }
   PUMP_TRY(set_smem_attr((const void *)halfspace_kernel, smem));
   halfspace_kernel<<<grid_for(E * W, 256), 256, smem, (cudaStream_t)stream>>>(
       d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, d_count);
   return launch_status("cache_halfspaces");
+}
+
+extern "C" pump_status_t pump_cache_halfspaces_sparse(const float *d_obstacles, int numObs,
+                                                      const float *d_disc,
+                                                      const uint8_t *d_is_free_edge, long long E,
+                                                      int W, int maxHS, float maxd2, float *d_as,
+                                                      float *d_bs, uint8_t *d_count,
+                                                      pump_stream_t stream) {
+  if (numObs < 0 || E < 0 || W < 2 || maxHS < 0 || maxHS > kStagedMaxHS ||
+      (numObs > 0 && !d_obstacles) ||
+      (E > 0 && (!d_disc || !d_is_free_edge || !d_count || (maxHS > 0 && (!d_as || !d_bs)))))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_cache_halfspaces_sparse: bad arguments");
+  if (E == 0) return PUMP_OK;
+  if (maxHS == 0) {
+    PUMP_CUDA_TRY(cudaMemsetAsync(d_count, 0, (size_t)E * W, (cudaStream_t)stream));
+    return PUMP_OK;
+  }
+  const size_t staged = halfspace_staged_smem(numObs, maxHS, false);
+  if (staged > 220 * 1024)
+    return set_error(PUMP_ERR_CAPACITY, "%d obstacles exceed the shared-memory stage", numObs);
+  PUMP_TRY(set_smem_attr((const void *)halfspace_staged_kernel<false>, staged));
+  halfspace_staged_kernel<false><<<grid_for(E * W, kHsThreads), kHsThreads, staged,
+                                   (cudaStream_t)stream>>>(
+      d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, nullptr,
+      d_count);
+  return launch_status("cache_halfspaces_sparse");
 }

@@ -199,9 +199,12 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
     int maxHS, const float *__restrict__ times, const float *__restrict__ topts, float dt,
     const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
     const uint32_t *valid_in, uint32_t *valid_out, int P, float *__restrict__ cp_out,
-    int *__restrict__ error) {
+    int *__restrict__ error, const uint8_t *__restrict__ hs_count) {
   // valid_in[prev] is read, valid_out[w] / cp_out[w] written (the two may
-  // alias one path store with valid_out = store + base, as in the reference)
+  // alias one path store with valid_out = store + base, as in the reference).
+  // With hs_count (stored half-spaces per waypoint), slots at or past a
+  // waypoint's count are inactive without reading them (they hold the
+  // defaults b = 1111 in the dense layout); stored slots still need b < 1000.
   const int lane = threadIdx.x & 31;
   const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
   if (w >= num_new) return;  // warp-uniform
@@ -220,7 +223,11 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
   for (int c = 0; c < kMaxHsSlots / 32; ++c) {
     const int sidx = c * 32 + lane;
     bool a = false;
-    if (c * 32 < slots && sidx < slots) a = !(__ldg(&bs[hsHead + sidx]) >= 1000);
+    if (c * 32 < slots && sidx < slots) {
+      const bool stored =
+          !hs_count || sidx - (sidx / maxHS) * maxHS < (int)__ldg(&hs_count[(long long)edge * W + sidx / maxHS]);
+      a = stored && !(__ldg(&bs[hsHead + sidx]) >= 1000);
+    }
     act[c] = (c * 32 < slots) ? __ballot_sync(0xffffffffu, a) : 0u;
     nact += __popc(act[c]);
   }
@@ -411,7 +418,8 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
                                 const float *d_times, const float *d_topt, float dt,
                                 const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                                 const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
-                                float *d_cp_out, int *d_error, cudaStream_t stream) {
+                                float *d_cp_out, int *d_error, const uint8_t *d_hs_count,
+                                cudaStream_t stream) {
   if (num_new <= 0) return PUMP_OK;
   if ((P + 31) / 32 > kMaxHsmcWords)
     return set_error(PUMP_ERR_CAPACITY, "hsmc: %d particles exceed %d", P, 32 * kMaxHsmcWords);
@@ -421,7 +429,8 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
   hsmc_kernel<<<grid_for((long long)num_new * 32, 256), 256, 0, stream>>>(
       num_new, W, d_edge, d_prev, num_edges, num_prev, d_as, d_bs, maxHS, d_times, d_topt,
                                                dt, d_offsets_t, Pmc, T_rows, offset_mult,
-                                               d_valid_in, d_valid_out, P, d_cp_out, d_error);
+                                               d_valid_in, d_valid_out, P, d_cp_out, d_error,
+                                               d_hs_count);
   return launch_status("hsmc_kernel");
 }
 
@@ -475,7 +484,7 @@ extern "C" pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_ed
                                              float dt, const float *d_offsets_t, int Pmc,
                                              int T_rows, float offset_mult, uint32_t *d_valid,
                                              int P, float *d_path_cp, int *d_error,
-                                             pump_stream_t stream) {
+                                             const uint8_t *d_hs_count, pump_stream_t stream) {
   if (num_new < 0 || W < 2 || maxHS < 0 || P <= 0 || P > Pmc || T_rows <= 0 || base < 0 ||
       num_edges < 0 ||
       (num_new > 0 && (!d_edge || !d_prev || !d_times || !d_topt || !d_offsets_t || !d_valid ||
@@ -486,7 +495,7 @@ extern "C" pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_ed
                            d_topt, dt,
                            d_offsets_t, Pmc, T_rows, offset_mult, d_valid,
                            d_valid + (size_t)base * words, P, d_path_cp + base, d_error,
-                           (cudaStream_t)stream);
+                           d_hs_count, (cudaStream_t)stream);
 }
 
 extern "C" pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d_len,

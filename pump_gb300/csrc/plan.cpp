@@ -40,7 +40,8 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
                                 const float *d_times, const float *d_topt, float dt,
                                 const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                                 const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
-                                float *d_cp_out, int *d_error, cudaStream_t stream);
+                                float *d_cp_out, int *d_error, const uint8_t *d_hs_count,
+                                cudaStream_t stream);
 pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n, int words,
                                  uint32_t *d_dst, cudaStream_t stream);
 pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
@@ -192,7 +193,7 @@ class Planner {
   DevBuf<float> d_coptE_, d_toptE_, d_disc_, d_as_, d_bs_;
   const float *d_table_ = nullptr;  // context-cached particle table
   const float *obs_p_ = nullptr;    // device obstacles used by the MC CP
-  DevBuf<uint8_t> d_free_s_, d_free_e_;
+  DevBuf<uint8_t> d_free_s_, d_free_e_, d_hcount_;
   long long E_ = 0;
   float rn_ = 0;
   std::vector<float> h_;
@@ -358,8 +359,10 @@ pump_status_t Planner::online() {
   const float maxd2 = (float)(0.1 * (double)pb_.offset_mult * (double)pb_.offset_mult);
   PUMP_TRY(d_as_.alloc((size_t)E_ * W_ * maxHS_ * 3));
   PUMP_TRY(d_bs_.alloc((size_t)E_ * W_ * maxHS_));
-  PUMP_TRY(pump_cache_halfspaces(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_, maxd2,
-                                 d_as_.p, d_bs_.p, nullptr, (pump_stream_t)s_));
+  // only the stored half-spaces and their counts (the search reads no more)
+  PUMP_TRY(d_hcount_.alloc((size_t)E_ * W_));
+  PUMP_TRY(pump_cache_halfspaces_sparse(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_,
+                                        maxd2, d_as_.p, d_bs_.p, d_hcount_.p, (pump_stream_t)s_));
   PUMP_TRY(ctx_->particle_table(pb_.seed, pb_.num_mc, pb_.table_rows, &d_table_, s_));
   const size_t cap = E_ > 0 ? (size_t)E_ : 1;
   PUMP_TRY(d_fid_.alloc(cap));
@@ -521,7 +524,7 @@ pump_status_t Planner::explore() {
     PUMP_TRY(hsmc_staged_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p, d_bs_.p, maxHS_,
                                d_pathTime_.p, d_toptE_.p, dt_, d_table_, pb_.num_mc,
                                pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p, P_,
-                               d_cpStage_.p, d_err_.p, s_));
+                               d_cpStage_.p, d_err_.p, d_hcount_.p, s_));
     // cut-off, dominance, storing, buckets (PUMP.cu:164-256)
     PUMP_TRY(search_prune(sd, numNew, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
     PUMP_TRY(search_store(ctx_, sd, numNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln,

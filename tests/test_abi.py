@@ -29,7 +29,7 @@ def test_bad_arguments_rejected_on_host(pumplib):
     assert L.pump_bvp_pairs(None, 10, 5.0, 7, None, None, None) == pumplib.PUMP_ERR_BAD_INPUT
     assert L.pump_free_edges(None, 3, None, 10, 8, None, None) == pumplib.PUMP_ERR_BAD_INPUT
     assert L.pump_hsmc_propagate(1, 9, None, None, 10, 0, None, None, 5, None, None, 0.05, None,
-                                 2048, 400, 1.0, None, 128, None, None, None) == pumplib.PUMP_ERR_BAD_INPUT
+                                 2048, 400, 1.0, None, 128, None, None, None, None) == pumplib.PUMP_ERR_BAD_INPUT
     assert L.pump_select_kth(None, None, 10, 3, None, None) == pumplib.PUMP_ERR_BAD_INPUT
     assert L.pump_plan(None, None, None, None) == pumplib.PUMP_ERR_BAD_INPUT
     assert b"pump_plan" in L.pump_last_error()

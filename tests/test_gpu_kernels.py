@@ -282,7 +282,7 @@ def test_hsmc_propagate(P, gpu, pumplib, oracle, roadmap1000):
     pumplib.check(L.pump_hsmc_propagate(n_new, 9, ptr(d_edges), ptr(d_prev), E, base, ptr(d_a), ptr(d_b),
                                         maxHS, ptr(d_times), ptr(d_te), 0.05, ptr(d_tm), Pmc, T,
                                         float(om), ptr(d_valid), P, ptr(d_cp), ptr(d_err),
-                                        stream(torch)))
+                                        None, stream(torch)))
     torch.cuda.synchronize()
     got = bits_to_bytes(host(d_valid).reshape(base + n_new, words), P)
     cp_o = np.zeros(base + n_new, np.float32)
@@ -292,6 +292,66 @@ def test_hsmc_propagate(P, gpu, pumplib, oracle, roadmap1000):
     assert same_bits(host(d_cp)[base:base + n_new], cp_o[base:])
     assert int(host(d_err)[0]) == 0
     assert 0 < valid_bytes[base:].mean() < 1
+
+
+@pytest.mark.parametrize("om", [0.3, 2e-3])
+def test_sparse_halfspaces_and_hsmc(om, gpu, pumplib, oracle, roadmap1000):
+    """pump_cache_halfspaces_sparse writes the reference's stored half-spaces
+    and their counts only (slots past a count keep what the buffers held, NaN
+    here), and HSMC reading them through the counts gives the same particle
+    masks and CPs as the dense layout."""
+    torch, _ = gpu
+    L = pumplib.load()
+    r = roadmap1000
+    obs, E, W = r["obs"], r["src"].size, 9
+    om = np.float32(om)
+    maxHS = 5
+    maxd2 = np.float32(0.1 * np.float64(om) * np.float64(om))
+    a, b, n = oracle.cache_halfspaces(r["disc"], r["fe"], obs, maxHS, maxd2)
+    d_obs, d_disc, d_fe = dev(torch, obs), dev(torch, r["disc"]), dev(torch, r["fe"])
+    d_a = torch.full((E * W * maxHS * 3,), float("nan"), dtype=torch.float32, device="cuda")
+    d_b = torch.full((E * W * maxHS,), float("nan"), dtype=torch.float32, device="cuda")
+    d_n = torch.full((E * W,), 255, dtype=torch.uint8, device="cuda")
+    pumplib.check(L.pump_cache_halfspaces_sparse(ptr(d_obs), obs.shape[0], ptr(d_disc), ptr(d_fe), E,
+                                                 W, maxHS, float(maxd2), ptr(d_a), ptr(d_b), ptr(d_n),
+                                                 stream(torch)))
+    torch.cuda.synchronize()
+    cnt = host(d_n).astype(np.int32)
+    free_wp = np.repeat(r["fe"].astype(bool), W)
+    assert np.array_equal(cnt[free_wp], n[free_wp]) and np.all(cnt[~free_wp] == 0)
+    slot = np.arange(maxHS)[None, :] < cnt[:, None]
+    ga, gb = host(d_a).reshape(-1, maxHS, 3), host(d_b).reshape(-1, maxHS)
+    assert same_bits(gb[slot], b.reshape(-1, maxHS)[slot])
+    assert same_bits(ga[slot], a.reshape(-1, maxHS, 3)[slot])
+    assert np.all(np.isnan(gb[~slot]))
+    # HSMC through the counts vs the oracle on the dense layout
+    Pmc, T, P = 2048, 400, 1024
+    tm, _ = oracle.particle_tables(0x1234, Pmc, T, pmajor=False)
+    rng = np.random.default_rng(11)
+    base, n_new = 50, 3000
+    edges = rng.choice(np.nonzero(r["fe"])[0], n_new).astype(np.int32)
+    prev = rng.integers(0, base, n_new).astype(np.int32)
+    times = np.zeros(base + n_new, np.float32)
+    times[:base] = rng.uniform(0, 6, base).astype(np.float32)
+    valid_bytes = np.zeros((base + n_new, P), np.uint8)
+    valid_bytes[:base] = rng.random((base, P)) < 0.9
+    packed = np.packbits(valid_bytes, axis=1, bitorder="little").view(np.uint32)
+    d_valid, d_cp = dev(torch, packed), empty(torch, base + n_new, torch.float32)
+    d_err = dev(torch, np.zeros(1, np.int32))
+    d_edges, d_prev, d_times = dev(torch, edges), dev(torch, prev), dev(torch, times)
+    d_te, d_tm = dev(torch, r["te"]), dev(torch, tm)
+    pumplib.check(L.pump_hsmc_propagate(n_new, W, ptr(d_edges), ptr(d_prev), E, base, ptr(d_a), ptr(d_b),
+                                        maxHS, ptr(d_times), ptr(d_te), 0.05, ptr(d_tm), Pmc, T,
+                                        float(om), ptr(d_valid), P, ptr(d_cp), ptr(d_err), ptr(d_n),
+                                        stream(torch)))
+    torch.cuda.synchronize()
+    got = bits_to_bytes(host(d_valid).reshape(base + n_new, P // 32), P)
+    cp_o = np.zeros(base + n_new, np.float32)
+    oracle.lib().orc_hsmc_propagate(n_new, W, edges, prev, base, a, b, times, r["te"], 0.05, maxHS,
+                                    tm.reshape(-1), om, Pmc, valid_bytes, P, cp_o)
+    assert np.array_equal(got[base:], valid_bytes[base:])
+    assert same_bits(host(d_cp)[base:base + n_new], cp_o[base:])
+    assert int(host(d_err)[0]) == 0
 
 
 def test_mc_cp(gpu, pumplib, oracle, goldens):
