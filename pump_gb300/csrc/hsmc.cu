@@ -276,11 +276,14 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
         for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
           if (q * 32 >= words) break;
           uint32_t bq = bits[q];
+          if (bq == 0u) continue;  // this lane's particles of the group are all dead
+          // the test of a particle already dead is computed and discarded,
+          // so the loads do not wait on the bits and many are in flight
+#pragma unroll 8
           for (int bb = 0; bb < 32; ++bb) {
             const int k = q * 32 + bb;
-            if (k >= words) break;
             const int p = 32 * k + lane;
-            if (p < P && ((bq >> bb) & 1u)) {
+            if (k < words && p < P) {
               const float *off = row + (long long)p * 3;
               float LHS = 0;
               LHS += __ldg(&off[0]) * a0;
