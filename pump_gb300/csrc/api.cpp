@@ -73,8 +73,9 @@ pump_status_t Ctx::particle_table(uint64_t seed, int P, int T, const float **out
       return PUMP_OK;
     }
   TableEntry e{device_, seed, P, T, nullptr, nullptr};
-  PUMP_CUDA_TRY(cudaMalloc(&e.ptr, sizeof(float) * 3 * (size_t)P * T));
+  PUMP_CUDA_TRY(cudaMalloc(&e.ptr, sizeof(float) * 3 * ((size_t)P * T + T)));
   PUMP_TRY(particle_tables_async(seed, P, T, e.ptr, nullptr, stream));
+  PUMP_TRY(particle_rowmax_async(e.ptr, P, T, e.ptr + 3 * (size_t)P * T, stream));
   PUMP_CUDA_TRY(cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming));
   PUMP_CUDA_TRY(cudaEventRecord(e.ready, stream));
   g_tables.push_back(e);

@@ -33,7 +33,9 @@ class Ctx {
   pump_status_t scratch(int slot, size_t bytes, void **out);
   // Time-major particle table for (seed, P, T), generated on first use and
   // shared by every context on the device (the reference loads its table
-  // once per process); `stream` is ordered after its generation.
+  // once per process); `stream` is ordered after its generation.  The
+  // largest |offset| per row and axis (T x 3) follows the table's P x T x 3
+  // values in the same allocation.
   pump_status_t particle_table(uint64_t seed, int P, int T, const float **out, cudaStream_t stream);
 
   // The captured refinement loop of the last pump_refine_paths call, replayed
@@ -70,6 +72,8 @@ pump_status_t open_edges_device(Ctx *ctx, const uint8_t *d_free_e, const uint8_t
                                 long long *h_count, cudaStream_t stream);
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                       int *d_count, int **d_error_out, cudaStream_t stream);
+pump_status_t particle_rowmax_async(const float *d_table, int P, int T, float *d_rowmax,
+                                    cudaStream_t stream);
 pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor, float *d_pmajor,
                                     cudaStream_t stream);
 pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tmax, float *d_copts,

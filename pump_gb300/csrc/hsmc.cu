@@ -337,12 +337,26 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
 // warp w tests segments t = w, w + 8, ...; the per-particle OR over warps is
 // taken in shared memory and the block adds its popcount to hits[k].
 // Grid (ceil(Pmc / 32), paths).
+// MC CP of path k (blockIdx.y): 32 particles per block (one per lane), the
+// 8 warps splitting the path's segments.  With rowmax (the largest |offset|
+// per table row and axis), each block first marks, per segment, the boxes
+// that some particle's segment could touch: the path segment's bounding box
+// widened by fl(rowmax * |offset_mult|) on both ends.  A particle's position
+// fl(path + fl(offset * offset_mult)) lies inside that box by the
+// monotonicity of rounding, so a box disjoint from it is broadphase-disjoint
+// from every particle's segment and the reference's test of it passes; only
+// the marked boxes are tested, in index order.  Without rowmax (or with more
+// than kMcFilterObs boxes, or a NaN state) every box is tested.
+constexpr int kMcFilterObs = 128;
+
 __global__ void __launch_bounds__(256) mc_cp_kernel(
     const float *__restrict__ paths, const int *__restrict__ offset, const int *__restrict__ len,
     const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
-    const float *__restrict__ obs, int numObs, int k0, int *__restrict__ hits) {
+    const float *__restrict__ obs, int numObs, int k0, int *__restrict__ hits,
+    const float *__restrict__ rowmax) {
   extern __shared__ float4 s_obs4[];
   float *s_obs = reinterpret_cast<float *>(s_obs4);
+  uint32_t *s_mask = reinterpret_cast<uint32_t *>(s_obs + ((numObs * 12 + 3) & ~3));
   __shared__ unsigned int s_hit[8];
   stage_obstacles(obs, numObs, s_obs);
   const int k = k0 + blockIdx.y;
@@ -350,8 +364,31 @@ __global__ void __launch_bounds__(256) mc_cp_kernel(
   const int p = blockIdx.x * 32 + lane;
   const int T = len[k];
   const float *path = paths + (long long)offset[k] * kDim;
+  const bool filter = rowmax != nullptr && numObs <= kMcFilterObs && T <= T_rows;
+  if (filter) {
+    const float om = fabsf(offset_mult);
+    for (int t = threadIdx.x; t < T - 2; t += blockDim.x) {
+      float lo[3], hi[3];
+      bool nan = false;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float m0 = rowmax[t * 3 + d] * om, m1 = rowmax[(t + 1) * 3 + d] * om;
+        const float a = path[t * kDim + d], b = path[(t + 1) * kDim + d];
+        nan = nan || a != a || b != b;
+        lo[d] = fminf(a - m0, b - m1);
+        hi[d] = fmaxf(a + m0, b + m1);
+      }
+      uint32_t m[kMcFilterObs / 32] = {0u, 0u, 0u, 0u};
+      for (int o = 0; o < numObs; ++o)
+        if (nan || !broadphase_valid(lo, hi, &s_obs[o * 12])) m[o >> 5] |= 1u << (o & 31);
+#pragma unroll
+      for (int q = 0; q < kMcFilterObs / 32; ++q) s_mask[t * (kMcFilterObs / 32) + q] = m[q];
+    }
+    __syncthreads();
+  }
   bool coll = false;
   if (p < Pmc && T <= T_rows) {
+    const int words = (numObs + 31) / 32;
     for (int t = warp; t < T - 2 && !coll; t += 8) {
       float v[3], w[3];
 #pragma unroll
@@ -360,7 +397,8 @@ __global__ void __launch_bounds__(256) mc_cp_kernel(
         w[d] = path[(t + 1) * kDim + d] +
                __ldg(&offsets_t[((long long)(t + 1) * Pmc + p) * 3 + d]) * offset_mult;
       }
-      coll = !segment_valid(v, w, numObs, s_obs);
+      coll = filter ? !segment_valid_masked(v, w, &s_mask[t * (kMcFilterObs / 32)], words, s_obs)
+                    : !segment_valid(v, w, numObs, s_obs);
     }
   }
   const unsigned int bal = __ballot_sync(0xffffffffu, coll);
@@ -371,6 +409,30 @@ __global__ void __launch_bounds__(256) mc_cp_kernel(
     for (int q = 0; q < 8; ++q) any |= s_hit[q];
     const int total = __popc(any);
     if (total) atomicAdd(&hits[k], total);
+  }
+}
+
+// Largest |offset| per row and axis of the time-major table (T rows of P
+// particles), for the MC CP box filter.
+__global__ void particle_rowmax_kernel(const float *__restrict__ table, int P,
+                                       float *__restrict__ rowmax) {
+  const int t = blockIdx.x;
+  float m[3] = {0.0f, 0.0f, 0.0f};
+  for (int p = threadIdx.x; p < P; p += blockDim.x)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) m[d] = fmaxf(m[d], fabsf(table[((long long)t * P + p) * 3 + d]));
+  __shared__ float s_m[3][32];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    float v = m[d];
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) s_m[d][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    float v = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmaxf(v, s_m[threadIdx.x][w]);
+    rowmax[t * 3 + threadIdx.x] = v;
   }
 }
 
@@ -393,13 +455,26 @@ __global__ void gather_words_kernel(const uint32_t *__restrict__ src, const int 
 
 }  // namespace
 
+pump_status_t particle_rowmax_async(const float *d_table, int P, int T, float *d_rowmax,
+                                    cudaStream_t stream) {
+  particle_rowmax_kernel<<<T, 256, 0, stream>>>(d_table, P, d_rowmax);
+  return launch_status("particle_rowmax");
+}
+
 pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
                           const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                           const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
-                          int *d_error, cudaStream_t stream) {
+                          int *d_error, cudaStream_t stream, const float *d_rowmax) {
   if (n_paths <= 0) return PUMP_OK;
-  const size_t smem = (size_t)numObs * 12 * sizeof(float);
-  if (smem > 200 * 1024) return set_error(PUMP_ERR_CAPACITY, "mc_cp: %d obstacles", numObs);
+  if (numObs > kMcFilterObs) d_rowmax = nullptr;
+  size_t smem = sizeof(float) * (size_t)((numObs * 12 + 3) & ~3);
+  if (d_rowmax) smem += sizeof(uint32_t) * (kMcFilterObs / 32) * (size_t)T_rows;
+  if (smem > 200 * 1024) {
+    if (!d_rowmax) return set_error(PUMP_ERR_CAPACITY, "mc_cp: %d obstacles", numObs);
+    d_rowmax = nullptr;  // masks for this many rows do not fit: test every box
+    smem = sizeof(float) * (size_t)((numObs * 12 + 3) & ~3);
+    if (smem > 200 * 1024) return set_error(PUMP_ERR_CAPACITY, "mc_cp: %d obstacles", numObs);
+  }
   if (smem > 48 * 1024)
     PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)mc_cp_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -408,7 +483,8 @@ pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *
     const int nk = n_paths - k0 < 65535 ? n_paths - k0 : 65535;
     dim3 grid(grid_for(Pmc, 32), (unsigned)nk);
     mc_cp_kernel<<<grid, 256, smem, stream>>>(d_paths, d_offset, d_len, d_offsets_t, Pmc, T_rows,
-                                              offset_mult, d_obstacles, numObs, k0, d_hits);
+                                              offset_mult, d_obstacles, numObs, k0, d_hits,
+                                              d_rowmax);
     PUMP_TRY(launch_status("mc_cp_kernel"));
   }
   mc_cp_finish_kernel<<<grid_for(n_paths, 128), 128, 0, stream>>>(d_hits, d_len, n_paths, Pmc,
@@ -509,5 +585,5 @@ extern "C" pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, c
       (n_paths > 0 && (!d_paths || !d_offset || !d_len || !d_offsets_t || !d_hits || !d_cp)))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_mc_cp: bad arguments");
   return mc_cp_async(d_paths, d_offset, d_len, n_paths, d_offsets_t, Pmc, T_rows, offset_mult,
-                     d_obstacles, numObs, d_hits, d_cp, d_error, (cudaStream_t)stream);
+                     d_obstacles, numObs, d_hits, d_cp, d_error, (cudaStream_t)stream, nullptr);
 }

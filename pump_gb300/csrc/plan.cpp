@@ -47,7 +47,7 @@ pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n,
 pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
                           const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                           const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
-                          int *d_error, cudaStream_t stream);
+                          int *d_error, cudaStream_t stream, const float *d_rowmax);
 
 namespace {
 
@@ -191,7 +191,8 @@ class Planner {
   DevBuf<float> d_samples_, d_obs_, d_copts_, d_topts_;
   DevBuf<int> d_src_, d_dst_, d_go_;
   DevBuf<float> d_coptE_, d_toptE_, d_disc_, d_as_, d_bs_;
-  const float *d_table_ = nullptr;  // context-cached particle table
+  const float *d_table_ = nullptr;   // context-cached particle table
+  const float *d_rowmax_ = nullptr;  // its largest |offset| per row and axis
   const float *obs_p_ = nullptr;    // device obstacles used by the MC CP
   DevBuf<uint8_t> d_free_s_, d_free_e_, d_hcount_;
   long long E_ = 0;
@@ -364,6 +365,7 @@ pump_status_t Planner::online() {
   PUMP_TRY(pump_cache_halfspaces_sparse(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_,
                                         maxd2, d_as_.p, d_bs_.p, d_hcount_.p, (pump_stream_t)s_));
   PUMP_TRY(ctx_->particle_table(pb_.seed, pb_.num_mc, pb_.table_rows, &d_table_, s_));
+  d_rowmax_ = d_table_ + 3 * (size_t)pb_.num_mc * pb_.table_rows;
   const size_t cap = E_ > 0 ? (size_t)E_ : 1;
   PUMP_TRY(d_fid_.alloc(cap));
   PUMP_TRY(d_fsrc_.alloc(cap));
@@ -657,7 +659,7 @@ pump_status_t Planner::eval_candidates(const std::vector<std::vector<float>> &xs
     PUMP_TRY(d_mcp_.alloc(n));
     PUMP_TRY(mc_cp_async(d_cstates_.p, d_cints_.p + 3 * n, d_clen_.p, n, d_table_, pb_.num_mc,
                          pb_.table_rows, pb_.offset_mult, obs_p_, nobs_, d_mhits_.p, d_mcp_.p,
-                         nullptr, s_));
+                         nullptr, s_, d_rowmax_));
     PUMP_TRY(d2h(cp.data(), d_mcp_.p, n));
   }
   PUMP_TRY(d2h(len.data(), d_clen_.p, n));
@@ -819,6 +821,10 @@ pump_status_t Planner::evaluate_paths(const std::vector<std::vector<float>> &xs,
   d_table_ = d_table;
   obs_p_ = d_obs;
   nobs_ = nobs;
+  DevBuf<float> d_rowmax;
+  PUMP_TRY(d_rowmax.alloc(3 * (size_t)pb_.table_rows));
+  PUMP_TRY(particle_rowmax_async(d_table, pb_.num_mc, pb_.table_rows, d_rowmax.p, s_));
+  d_rowmax_ = d_rowmax.p;
   std::vector<int> ln;
   std::vector<float> cs, cps;
   PUMP_TRY(eval_candidates(xs, dt_, pb_.table_rows, true, true, ln, cs, cps));
