@@ -752,8 +752,10 @@ pump_status_t Planner::search_and_smooth() {
     // alphas the next D steps can visit are evaluated in one batch (dense
     // paths, costs and MC CPs of all of them), then the reference's decisions
     // are replayed in order over the results: the same sequence of alphas,
-    // best-path updates and early exit as PUMP.cu:492-541.
-    const int D = 5, K = (1 << D) - 1;
+    // best-path updates and early exit as PUMP.cu:492-541.  D = 3 (7 paths
+    // per batch): deeper batches save round trips but most of their Monte
+    // Carlo work is for alphas the bisection never visits.
+    const int D = 3, K = (1 << D) - 1;
     int it = 0;
     bool stop = false;
     while (it < 30 && !stop) {
