@@ -441,11 +441,10 @@ def run_ours(args):
     def step():
         timed("bvp_pairs", lambda: lib.check(L.pump_bvp_pairs(d_s.data_ptr(), N, 5.0, w["mode"],
                                                              d_c.data_ptr(), d_t.data_ptr(), sh)), 1)
-        timed("select_rn", lambda: lib.check(L.pump_select_kth(ctx.handle, d_c.data_ptr(), npairs,
-                                                              rn_idx, C.byref(rn), sh)), 7)
-        timed("build_edges", lambda: lib.check(L.pump_build_edges(
-            ctx.handle, d_c.data_ptr(), d_t.data_ptr(), N, rn.value, cap, d_src.data_ptr(),
-            d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(), d_go.data_ptr(), C.byref(Eo), sh)), 2)
+        timed("rn_edges", lambda: lib.check(L.pump_roadmap_edges(
+            ctx.handle, d_c.data_ptr(), d_t.data_ptr(), N, rn_idx, cap, d_src.data_ptr(),
+            d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(), d_go.data_ptr(), C.byref(rn),
+            C.byref(Eo), sh)), 12)
         timed("discretize", lambda: lib.check(L.pump_discretize_edges(
             d_s.data_ptr(), d_src.data_ptr(), d_dst.data_ptr(), d_te.data_ptr(), Eo.value, W - 1,
             w["mode"], d_disc.data_ptr(), sh)), 1)
@@ -582,8 +581,7 @@ def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops, sm_mhz):
     src = "measured" if "hbm_gbs" in peaks else "fallback"
     # algorithmic HBM bytes per launch of the memory-bound kernels
     algo = {
-        "select_rn": 3 * 4.0 * N * (N - 1),                   # three reads of the costs
-        "build_edges": 4.0 * N * (N - 1) + 16.0 * E,          # costs read, 4 arrays out
+        "rn_edges": 4.0 * N * (N - 1) + 20.0 * E,             # costs read, edge times, 4 arrays out
         "discretize": 16.0 * E + 24.0 * W * E,                # edge in, waypoints out
         "free_edges": 24.0 * W * E + E,                       # waypoints in, mask out
         "halfspaces": 24.0 * W * E + E + 1.0 * W * E,         # waypoints in, counts out

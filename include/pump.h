@@ -96,6 +96,17 @@ pump_status_t pump_build_edges(pump_ctx *ctx, const float *d_copts, const float 
                                float *d_copt, float *d_topt, int *d_go_start,
                                long long *h_num_edges, pump_stream_t stream);
 
+/* pump_select_kth(k) followed by pump_build_edges(rn) in one call
+ * (mainPUMP.cu:289-346: the thrust::sort of all pair costs, rn at index k,
+ * the edges below rn): the same rn (*h_rn), edge count and edge arrays,
+ * from one read of the pair costs.  A strided sample bounds rn from above;
+ * the pairs below the bound are selected and compacted; a sample that
+ * misses rank k falls back to the full passes.  Synchronises. */
+pump_status_t pump_roadmap_edges(pump_ctx *ctx, const float *d_copts, const float *d_topts, int N,
+                                 long long k, long long max_edges, int *d_src, int *d_dst,
+                                 float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
+                                 long long *h_num_edges, pump_stream_t stream);
+
 /* Edge waypoints disc[E][numDisc+1][6] (findDiscretizedPath, 2pBVP.cu:53-69
  * and pathPoint 2pBVP.cu:117-131, as called at mainPUMP.cu:339).  d_topt
  * is the edge's optimal time (identical to the one toptBisection recomputes

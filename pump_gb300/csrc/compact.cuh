@@ -30,37 +30,60 @@ struct TileScratch {
   unsigned int *tile_counter;  // zeroed before launch
   unsigned long long *total;   // selected count (written by the last tile)
   int *error;                  // 1 = look-back wait gave up
+  unsigned long long *offsets; // per-tile output offsets (three-kernel compaction)
 };
 
 // Exclusive prefix of this tile from its predecessors' status words, read by
-// a whole warp: lane l reads the status of tile p - l, so one round trip to L2
-// covers 32 predecessors.  The lanes up to the nearest inclusive prefix must
-// all have published (at least an aggregate); otherwise the warp waits and
-// reads the window again.  Called by every lane of one warp; every lane
-// returns the same value.
+// a whole warp in windows of 32 x kLookbackPerLane tiles: lane l reads the
+// status of tiles p - V l - v (v < V), so one round trip to L2 covers 128
+// predecessors and the published-prefix front advances by up to 128 tiles per
+// round trip.  The tiles up to the nearest inclusive prefix must all have
+// published (at least an aggregate); otherwise the warp waits and reads the
+// window again.  A status word carries its own value, so relaxed loads and
+// stores suffice (an acquire load would also order the lane's V loads one
+// after another).  Called by every lane of one warp; every lane returns the
+// same value.
+constexpr int kLookbackPerLane = 4;
 __device__ unsigned long long lookback_warp(const TileScratch &ts, long long tile,
                                             unsigned long long agg, bool *timed_out) {
   using ref_t = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
+  constexpr int V = kLookbackPerLane;
   const int lane = threadIdx.x & 31;
   if (tile == 0) {
-    if (lane == 0) ref_t(ts.status[0]).store(kFlagPrefix | agg, cuda::memory_order_release);
+    if (lane == 0) ref_t(ts.status[0]).store(kFlagPrefix | agg, cuda::memory_order_relaxed);
     return 0;
   }
-  if (lane == 0) ref_t(ts.status[tile]).store(kFlagAggregate | agg, cuda::memory_order_release);
+  if (lane == 0) ref_t(ts.status[tile]).store(kFlagAggregate | agg, cuda::memory_order_relaxed);
   unsigned long long excl = 0;
   long long p = tile - 1;  // nearest tile of the window
   long long spins = 0;
   while (true) {
-    const long long q = p - lane;
-    // before tile 0 the prefix is 0 (a published prefix of value 0)
-    const unsigned long long st =
-        q >= 0 ? ref_t(ts.status[q]).load(cuda::memory_order_acquire) : kFlagPrefix;
-    const unsigned long long flag = st & ~kValueMask;
-    const unsigned int pref = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
-    const unsigned int none = __ballot_sync(0xffffffffu, flag == 0);
-    const int stop = pref ? __ffs(pref) - 1 : 31;  // last lane needed in this window
-    const unsigned int need = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
-    if (none & need) {
+    unsigned long long st[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const long long q = p - (long long)V * lane - v;
+      // before tile 0 the prefix is 0 (a published prefix of value 0)
+      st[v] = q >= 0 ? ref_t(ts.status[q]).load(cuda::memory_order_relaxed) : kFlagPrefix;
+    }
+    int first = V;  // this lane's nearest entry holding a prefix
+#pragma unroll
+    for (int v = V - 1; v >= 0; --v)
+      if ((st[v] & ~kValueMask) == kFlagPrefix) first = v;
+    const unsigned int pref = __ballot_sync(0xffffffffu, first < V);
+    const int stop = pref ? __ffs(pref) - 1 : 32;  // lane holding the nearest prefix
+    // entries this lane contributes: all V before the stop lane, up to its
+    // prefix entry in the stop lane, none after it
+    const int used = lane < stop ? V : (lane == stop ? first + 1 : 0);
+    bool missing = false;
+    unsigned long long sum = 0;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      if (v < used) {
+        if ((st[v] & ~kValueMask) == 0) missing = true;
+        sum += st[v] & kValueMask;
+      }
+    }
+    if (__any_sync(0xffffffffu, missing)) {
       if (++spins > kSpinLimit) {
         *timed_out = true;
         return 0;
@@ -68,32 +91,92 @@ __device__ unsigned long long lookback_warp(const TileScratch &ts, long long til
       __nanosleep(32);
       continue;
     }
-    unsigned long long v = lane <= stop ? (st & kValueMask) : 0ull;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    excl += v;
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    excl += sum;
     if (pref) break;
-    p -= 32;
+    p -= 32 * V;
   }
-  if (lane == 0) ref_t(ts.status[tile]).store(kFlagPrefix | (excl + agg), cuda::memory_order_release);
+  if (lane == 0) ref_t(ts.status[tile]).store(kFlagPrefix | (excl + agg), cuda::memory_order_relaxed);
   return excl;
+}
+
+// Shared state of one compaction tile: per (row, warp) selected counts, turned
+// into exclusive offsets within the tile, and the tile's exclusive prefix.
+struct TileShared {
+  unsigned int cnt[kCompactRows][kCompactThreads / 32];
+  unsigned long long excl;
+  bool timeout;
+};
+
+// Called by every thread after lane 0 of each warp stored its row counts in
+// sh.cnt: warp 0 scans the 16 x 8 counts in (row, warp) order and finds the
+// tile's prefix by look-back; the last tile writes the total.  False when the
+// look-back wait gave up (the error word is set; the tile writes nothing).
+// Warp 0: the tile's 16 x 8 (row, warp) counts, in (row, warp) order, turned
+// into exclusive offsets in place; returns the tile's total (every lane).
+__device__ __forceinline__ unsigned int scan_tile_counts(
+    unsigned int (&cnt)[kCompactRows][kCompactThreads / 32]) {
+  const int lane = threadIdx.x & 31;
+  unsigned int v[4];
+  unsigned int run = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = lane * 4 + q;
+    v[q] = cnt[e / 8][e % 8];
+    run += v[q];
+  }
+  unsigned int incl = run;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned int o = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += o;
+  }
+  unsigned int ex = incl - run;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = lane * 4 + q;
+    cnt[e / 8][e % 8] = ex;
+    ex += v[q];
+  }
+  return __shfl_sync(0xffffffffu, incl, 31);
+}
+
+__device__ __forceinline__ bool tile_offsets(TileShared &sh, const TileScratch &ts, long long tile,
+                                             long long n) {
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  if ((threadIdx.x >> 5) == 0) {
+    const unsigned int agg = scan_tile_counts(sh.cnt);
+    bool to = false;
+    const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
+    if (lane == 0) {
+      sh.excl = ex_tile;
+      sh.timeout = to;
+      if (to) atomicExch(ts.error, 1);
+      const long long ntiles = (n + kTile - 1) / kTile;
+      if (!to && tile == ntiles - 1) *ts.total = ex_tile + agg;
+    }
+  }
+  __syncthreads();
+  return !sh.timeout;
+}
+
+// Tile index from the atomic counter (every tile a block waits on has started).
+__device__ __forceinline__ long long next_tile(const TileScratch &ts) {
+  __shared__ unsigned int s_tile;
+  if (threadIdx.x == 0) s_tile = atomicAdd(ts.tile_counter, 1u);
+  __syncthreads();
+  return s_tile;
 }
 
 // Pred(i) -> bool, Emit(i, pos) writes item i at output position pos.
 template <class Pred, class Emit>
 __global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, Pred pred, Emit emit,
                                                                   TileScratch ts) {
-  __shared__ unsigned int s_tile;
-  __shared__ unsigned int s_cnt[kCompactRows][kCompactThreads / 32];
-  __shared__ unsigned long long s_excl;
-  __shared__ bool s_timeout;
+  __shared__ TileShared sh;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    s_tile = atomicAdd(ts.tile_counter, 1u);
-    s_timeout = false;
-  }
-  __syncthreads();
-  const long long tile = s_tile;
+  const long long tile = next_tile(ts);
   const long long base = tile * kTile;
   // all predicates first (their loads in flight together), then the ballots
   bool f[kCompactRows];
@@ -106,63 +189,28 @@ __global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, P
 #pragma unroll
   for (int r = 0; r < kCompactRows; ++r) {
     ballots[r] = __ballot_sync(0xffffffffu, f[r]);
-    if (lane == 0) s_cnt[r][warp] = __popc(ballots[r]);
+    if (lane == 0) sh.cnt[r][warp] = __popc(ballots[r]);
   }
-  __syncthreads();
-  // exclusive scan of the 16 x 8 counts in (row, warp) order by warp 0
-  if (warp == 0) {
-    unsigned int v[4];
-    unsigned int run = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = lane * 4 + q;
-      v[q] = s_cnt[e / 8][e % 8];
-      run += v[q];
-    }
-    unsigned int incl = run;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const unsigned int o = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += o;
-    }
-    unsigned int ex = incl - run;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = lane * 4 + q;
-      s_cnt[e / 8][e % 8] = ex;
-      ex += v[q];
-    }
-    const unsigned int agg = __shfl_sync(0xffffffffu, incl, 31);
-    bool to = false;
-    const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
-    if (lane == 0) {
-      s_excl = ex_tile;
-      if (to) {
-        s_timeout = true;
-        atomicExch(ts.error, 1);
-      }
-      const long long ntiles = (n + kTile - 1) / kTile;
-      if (!to && tile == ntiles - 1) *ts.total = ex_tile + agg;
-    }
-  }
-  __syncthreads();
-  if (s_timeout) return;
-  const unsigned long long excl = s_excl;
+  if (!tile_offsets(sh, ts, tile, n)) return;
+  const unsigned long long excl = sh.excl;
   const unsigned int lt = (1u << lane) - 1u;
 #pragma unroll
   for (int r = 0; r < kCompactRows; ++r) {
     if (ballots[r] & (1u << lane)) {
       const long long i = base + r * kCompactThreads + threadIdx.x;
-      emit(i, (long long)(excl + s_cnt[r][warp] + __popc(ballots[r] & lt)));
+      emit(i, (long long)(excl + sh.cnt[r][warp] + __popc(ballots[r] & lt)));
     }
   }
 }
 
-template <class Pred, class Emit>
-pump_status_t run_compact(Ctx *ctx, long long n, Pred pred, Emit emit, cudaStream_t stream,
-                          TileScratch *ts_out) {
+// Zeroed tile status words, tile counter, total and error word for a pass
+// over n items (ctx compaction scratch); *ntiles_out = the tiles to launch.
+pump_status_t prepare_tiles(Ctx *ctx, long long n, cudaStream_t stream, TileScratch *ts_out,
+                            long long *ntiles_out) {
   const long long ntiles = n > 0 ? (n + kTile - 1) / kTile : 1;
-  const size_t bytes = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
+  if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "compaction: too many tiles");
+  const size_t zeroed = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
+  const size_t bytes = zeroed + sizeof(unsigned long long) * ntiles;
   char *scratch = nullptr;
   PUMP_TRY(ctx->scratch(Ctx::kCompact, bytes, (void **)&scratch));
   TileScratch ts{};
@@ -170,9 +218,20 @@ pump_status_t run_compact(Ctx *ctx, long long n, Pred pred, Emit emit, cudaStrea
   ts.status = ts.total + 1;
   ts.tile_counter = (unsigned int *)(ts.status + ntiles + 1);
   ts.error = (int *)(ts.tile_counter + 1);
-  PUMP_CUDA_TRY(cudaMemsetAsync(scratch, 0, bytes, stream));
+  ts.offsets = (unsigned long long *)(scratch + zeroed);
+  PUMP_CUDA_TRY(cudaMemsetAsync(scratch, 0, zeroed, stream));
+  *ts_out = ts;
+  *ntiles_out = ntiles;
+  return PUMP_OK;
+}
+
+template <class Pred, class Emit>
+pump_status_t run_compact(Ctx *ctx, long long n, Pred pred, Emit emit, cudaStream_t stream,
+                          TileScratch *ts_out) {
+  TileScratch ts{};
+  long long ntiles = 0;
+  PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));
   if (n > 0) {
-    if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "compaction: too many tiles");
     compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(n, pred, emit, ts);
     PUMP_TRY(launch_status("compact_kernel"));
   }
@@ -190,95 +249,162 @@ pump_status_t finish_compact(const TileScratch &ts, unsigned long long *total, c
   return PUMP_OK;
 }
 
-// The edge list (mainPUMP.cu:327-346): the pairs with copt < rn in index
-// order, written as (i, j, copt, topt).  A specialisation of compact_kernel
-// that reads both pair arrays coalesced in the first phase, so the emit
-// phase does not wait on a dependent read per selected pair.
-__global__ void __launch_bounds__(kCompactThreads) edge_compact_kernel(
-    long long n, int N, const float *__restrict__ copts, const float *__restrict__ topts, float rn,
-    long long cap, int *__restrict__ src, int *__restrict__ dst, float *__restrict__ copt,
-    float *__restrict__ topt, TileScratch ts) {
-  __shared__ unsigned int s_tile;
-  __shared__ unsigned int s_cnt[kCompactRows][kCompactThreads / 32];
-  __shared__ unsigned long long s_excl;
-  __shared__ bool s_timeout;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    s_tile = atomicAdd(ts.tile_counter, 1u);
-    s_timeout = false;
-  }
-  __syncthreads();
-  const long long tile = s_tile;
-  const long long base = tile * kTile;
-  float c[kCompactRows], t[kCompactRows];
+// --------------------------------------- three-kernel tile compaction
+// For large inputs: a count kernel (blocks stride over the tiles) adds each
+// warp's selected count into its tile's count; one block scans the tile
+// counts into output offsets; an emit kernel (the same striding) writes each
+// tile's selected items from its offset, ranks in index order as in
+// compact_kernel.  The input is read twice, but no block waits on another:
+// on large inputs the look-back front of compact_kernel, not the reads, sets
+// its pace.
+//
+// A loader L supplies the items: L::Item (per-item registers), L::State
+// (per-block constants, from ld.begin()), ld.load(base, n, v) (this thread's
+// kCompactRows items of the tile at base: item r is base + r * 256 + tid),
+// ld.sel(st, item) and ld.emit(i, item, pos).
+constexpr int kTileBlocks = kNumSMs * 4;
+
+template <class L>
+__device__ __forceinline__ void tile_ballots(const L &ld, const typename L::State &st,
+                                             long long base, long long n,
+                                             typename L::Item (&v)[kCompactRows],
+                                             unsigned int (&b)[kCompactRows]) {
+  ld.load(base, n, v);
 #pragma unroll
   for (int r = 0; r < kCompactRows; ++r) {
     const long long i = base + r * kCompactThreads + threadIdx.x;
-    c[r] = i < n ? __ldg(&copts[i]) : 0.0f;
-    t[r] = i < n ? __ldg(&topts[i]) : 0.0f;
+    b[r] = __ballot_sync(0xffffffffu, i < n && ld.sel(st, v[r]));
   }
-  unsigned int ballots[kCompactRows];
+}
+
+// counts[tile] += each warp's selected count (counts zeroed before launch).
+template <class L>
+__global__ void __launch_bounds__(kCompactThreads) tile_count_kernel(long long n, L ld,
+                                                                     unsigned int *counts) {
+  const int lane = threadIdx.x & 31;
+  const long long ntiles = (n + kTile - 1) / kTile;
+  const typename L::State st = ld.begin();
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    typename L::Item v[kCompactRows];
+    unsigned int b[kCompactRows];
+    tile_ballots(ld, st, tile * kTile, n, v, b);
+    unsigned int cnt = 0;
 #pragma unroll
-  for (int r = 0; r < kCompactRows; ++r) {
-    const long long i = base + r * kCompactThreads + threadIdx.x;
-    ballots[r] = __ballot_sync(0xffffffffu, i < n && c[r] < rn);
-    if (lane == 0) s_cnt[r][warp] = __popc(ballots[r]);
+    for (int r = 0; r < kCompactRows; ++r) cnt += __popc(b[r]);
+    if (lane == 0 && cnt) atomicAdd(&counts[tile], cnt);
   }
+}
+
+// One block of 1024 threads: offsets[t] = counts[0] + .. + counts[t-1] and
+// *total = the sum of all; each thread scans a contiguous run of tiles.
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned int *__restrict__ counts,
+                                                         long long ntiles,
+                                                         unsigned long long *__restrict__ offsets,
+                                                         unsigned long long *total) {
+  __shared__ unsigned long long s_warp[32];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const long long per = (ntiles + 1023) / 1024;
+  const long long t0 = t * per, t1 = t0 + per < ntiles ? t0 + per : ntiles;
+  unsigned long long sum = 0;
+  for (long long q = t0; q < t1; ++q) sum += counts[q];
+  unsigned long long incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    unsigned int v[4];
-    unsigned int run = 0;
+    const unsigned long long w = s_warp[lane];
+    unsigned long long wi = w;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = lane * 4 + q;
-      v[q] = s_cnt[e / 8][e % 8];
-      run += v[q];
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long u = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += u;
     }
-    unsigned int incl = run;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const unsigned int o = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += o;
-    }
-    unsigned int ex = incl - run;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = lane * 4 + q;
-      s_cnt[e / 8][e % 8] = ex;
-      ex += v[q];
-    }
-    const unsigned int agg = __shfl_sync(0xffffffffu, incl, 31);
-    bool to = false;
-    const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
-    if (lane == 0) {
-      s_excl = ex_tile;
-      if (to) {
-        s_timeout = true;
-        atomicExch(ts.error, 1);
-      }
-      const long long ntiles = (n + kTile - 1) / kTile;
-      if (!to && tile == ntiles - 1) *ts.total = ex_tile + agg;
-    }
+    s_warp[lane] = wi - w;
+    if (lane == 31) *total = wi;
   }
   __syncthreads();
-  if (s_timeout) return;
-  const unsigned long long excl = s_excl;
-  const unsigned int lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int r = 0; r < kCompactRows; ++r) {
-    if (ballots[r] & (1u << lane)) {
-      const long long i = base + r * kCompactThreads + threadIdx.x;
-      const long long pos = (long long)(excl + s_cnt[r][warp] + __popc(ballots[r] & lt));
-      if (pos < cap) {
-        const int a = (int)(i / (N - 1));
-        const int b = (int)(i - (long long)a * (N - 1));
-        src[pos] = a;
-        dst[pos] = b + (b >= a);
-        copt[pos] = c[r];
-        topt[pos] = t[r];
-      }
-    }
+  unsigned long long run = s_warp[warp] + incl - sum;
+  for (long long q = t0; q < t1; ++q) {
+    offsets[q] = run;
+    run += counts[q];
   }
+}
+
+template <class L>
+__global__ void __launch_bounds__(kCompactThreads) tile_emit_kernel(
+    long long n, L ld, const unsigned long long *__restrict__ offsets) {
+  __shared__ unsigned int cnt[kCompactRows][kCompactThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long ntiles = (n + kTile - 1) / kTile;
+  const typename L::State st = ld.begin();
+  const unsigned int lt = (1u << lane) - 1u;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long base = tile * kTile;
+    const unsigned long long off = __ldg(&offsets[tile]);
+    typename L::Item v[kCompactRows];
+    unsigned int b[kCompactRows];
+    tile_ballots(ld, st, base, n, v, b);
+    if (lane == 0) {
+#pragma unroll
+      for (int r = 0; r < kCompactRows; ++r) cnt[r][warp] = __popc(b[r]);
+    }
+    __syncthreads();
+    if (warp == 0) scan_tile_counts(cnt);
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kCompactRows; ++r)
+      if (b[r] & (1u << lane))
+        ld.emit(base + r * kCompactThreads + threadIdx.x, v[r],
+                (long long)(off + cnt[r][warp] + __popc(b[r] & lt)));
+    __syncthreads();  // cnt is rewritten by the next tile
+  }
+}
+
+// Three-kernel compaction of n items; the count lands in *ts_out->total (the
+// error word stays zero: nothing waits).
+template <class L>
+pump_status_t run_chunked(Ctx *ctx, long long n, const L &ld, cudaStream_t stream,
+                          TileScratch *ts_out) {
+  TileScratch ts{};
+  long long ntiles = 0;
+  PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));  // zeroed status words hold the counts
+  if (n > 0) {
+    const unsigned blocks = (unsigned)(ntiles < kTileBlocks ? ntiles : kTileBlocks);
+    unsigned int *counts = reinterpret_cast<unsigned int *>(ts.status);
+    tile_count_kernel<<<blocks, kCompactThreads, 0, stream>>>(n, ld, counts);
+    PUMP_TRY(launch_status("tile_count_kernel"));
+    tile_scan_kernel<<<1, 1024, 0, stream>>>(counts, ntiles, ts.offsets, ts.total);
+    PUMP_TRY(launch_status("tile_scan_kernel"));
+    tile_emit_kernel<<<blocks, kCompactThreads, 0, stream>>>(n, ld, ts.offsets);
+    PUMP_TRY(launch_status("tile_emit_kernel"));
+  }
+  *ts_out = ts;
+  return PUMP_OK;
+}
+
+// go_start[r] = the first edge whose source is >= r (edges sorted by source),
+// r = 0 .. N: thread e (0 .. E) writes the rows (src[e-1], src[e]], with
+// src[-1] = -1 and src[E] = N, so each row is written once.
+__global__ void row_starts_kernel(const int *__restrict__ src, long long E, int N,
+                                  int *__restrict__ go_start) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e <= E;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int prev = e > 0 ? src[e - 1] : -1;
+    const int cur = e < E ? src[e] : N;
+    for (int r = prev + 1; r <= cur; ++r) go_start[r] = (int)e;
+  }
+}
+
+pump_status_t row_starts(const int *d_src, long long E, int N, int *d_go_start,
+                         cudaStream_t stream) {
+  long long blocks = (E + 1 + 255) / 256;
+  if (blocks > kNumSMs * 8) blocks = kNumSMs * 8;
+  row_starts_kernel<<<(unsigned)blocks, 256, 0, stream>>>(d_src, E, N, d_go_start);
+  return launch_status("row_starts_kernel");
 }
 
 // Exclusive scan of n counts: out[i] = count(0) + .. + count(i-1), the total
@@ -349,18 +475,10 @@ __global__ void __launch_bounds__(kCompactThreads) scan_kernel(long long n, Coun
 template <class Count>
 pump_status_t run_scan(Ctx *ctx, long long n, Count count, unsigned int *out,
                        cudaStream_t stream, TileScratch *ts_out) {
-  const long long ntiles = n > 0 ? (n + kTile - 1) / kTile : 1;
-  const size_t bytes = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
-  char *scratch = nullptr;
-  PUMP_TRY(ctx->scratch(Ctx::kCompact, bytes, (void **)&scratch));
   TileScratch ts{};
-  ts.total = (unsigned long long *)scratch;
-  ts.status = ts.total + 1;
-  ts.tile_counter = (unsigned int *)(ts.status + ntiles + 1);
-  ts.error = (int *)(ts.tile_counter + 1);
-  PUMP_CUDA_TRY(cudaMemsetAsync(scratch, 0, bytes, stream));
+  long long ntiles = 0;
+  PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));
   if (n > 0) {
-    if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "scan: too many tiles");
     scan_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(n, count, out, ts);
     PUMP_TRY(launch_status("scan_kernel"));
   }

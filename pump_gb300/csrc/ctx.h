@@ -19,6 +19,7 @@ class Ctx {
     kCompact,      // compaction tile status words
     kPlanA,        // planner buffers (see plan.cpp)
     kRefine,       // refinement descent state (refine.cu)
+    kSuperset,     // rn bracket bound and the pairs below it (select.cu)
     kNumSlots
   };
   explicit Ctx(int device) : device_(device) {
@@ -65,6 +66,16 @@ pump_status_t select_kth_pairs(Ctx *ctx, const PairView &pv, long long k, const 
 pump_status_t build_edges_pairs(Ctx *ctx, const PairView &pv, float rn, long long max_edges,
                                 int *d_src, int *d_dst, float *d_copt, float *d_topt,
                                 int *d_go_start, long long *h_num_edges, cudaStream_t stream);
+// rn (the k-th smallest pair cost) and the edges below it in one read of the
+// pair costs, from the query's own pair arrays or its pair view.
+pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
+                              long long k, long long max_edges, int *d_src, int *d_dst,
+                              float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
+                              long long *h_num_edges, cudaStream_t stream);
+pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long long max_edges,
+                             int *d_src, int *d_dst, float *d_copt, float *d_topt,
+                             int *d_go_start, float *h_rn, long long *h_num_edges,
+                             cudaStream_t stream);
 pump_status_t open_edges_device(Ctx *ctx, const uint8_t *d_free_e, const uint8_t *d_free_s,
                                 const int *d_src, const int *d_dst, const float *d_copt,
                                 const float *d_topt, long long E, int N, int *d_fid, int *d_fsrc,

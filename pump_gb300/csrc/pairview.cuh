@@ -38,6 +38,16 @@ struct PairView {
     if (j == N - 1) return __ldg(&gcc[i - 1]);
     return __ldg(&sc[shared_index(i, j)]);
   }
+  // The bits of copt(i, j), loaded as an integer (sort keys never pass
+  // through a float value).
+  __device__ __forceinline__ uint32_t copt_bits(int i, int j) const {
+    const float *p = i == 0           ? &irc[j - 1]
+                     : j == 0         ? &icc[i - 1]
+                     : i == N - 1     ? &grc[j - 1]
+                     : j == N - 1     ? &gcc[i - 1]
+                                      : &sc[shared_index(i, j)];
+    return __ldg(reinterpret_cast<const unsigned int *>(p));
+  }
   __device__ __forceinline__ float topt(int i, int j) const {
     if (i == 0) return __ldg(&irt[j - 1]);
     if (j == 0) return __ldg(&ict[i - 1]);

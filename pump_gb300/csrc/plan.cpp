@@ -270,13 +270,9 @@ pump_status_t Planner::roadmap() {
     PUMP_TRY(d_topts_.alloc(npairs));
     PUMP_TRY(pump_bvp_pairs(d_samples_.p, N_, 5.0f, pb_.bvp_mode, d_copts_.p, d_topts_.p,
                             (pump_stream_t)s_));
-    const float *d_rn = nullptr;
-    PUMP_TRY(select_kth_device(ctx_, d_copts_.p, npairs, rnIdx, &d_rn, s_));
-    PUMP_TRY(d2h(&rn_, d_rn, 1));
-    PUMP_TRY(sync());
+    PUMP_TRY(rn_edges_device(ctx_, d_copts_.p, d_topts_.p, N_, rnIdx, cap, d_src_.p, d_dst_.p,
+                             d_coptE_.p, d_toptE_.p, d_go_.p, &rn_, &E_, s_));
     res_->rn = rn_;
-    PUMP_TRY(build_edges_device(ctx_, d_copts_.p, d_topts_.p, N_, rn_, cap, d_src_.p, d_dst_.p,
-                                d_coptE_.p, d_toptE_.p, d_go_.p, &E_, s_));
   }
   res_->num_edges = E_;
   PUMP_TRY(d_disc_.alloc((size_t)E_ * W_ * kDim));
@@ -338,13 +334,10 @@ pump_status_t Planner::pair_costs_shared(long long rnIdx, long long cap) {
   pv.grt = d_own_t_.p + 2 * (N - 1);
   pv.gcc = d_own_c_.p + 2 * (N - 1) + (N - 2);
   pv.gct = d_own_t_.p + 2 * (N - 1) + (N - 2);
-  const float *d_rn = nullptr;
-  PUMP_TRY(select_kth_pairs(ctx_, pv, rnIdx, &d_rn, s_));
-  PUMP_TRY(d2h(&rn_, d_rn, 1));
-  PUMP_TRY(sync());
+  PUMP_TRY(rn_edges_pairs(ctx_, pv, rnIdx, cap, d_src_.p, d_dst_.p, d_coptE_.p, d_toptE_.p,
+                          d_go_.p, &rn_, &E_, s_));
   res_->rn = rn_;
-  return build_edges_pairs(ctx_, pv, rn_, cap, d_src_.p, d_dst_.p, d_coptE_.p, d_toptE_.p,
-                           d_go_.p, &E_, s_);
+  return PUMP_OK;
 }
 
 pump_status_t Planner::online() {

@@ -8,6 +8,9 @@
 //
 // Edge list and frontier: stable compaction (compact.cuh) of the pairs below
 // rn and of the frontier flags.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -19,13 +22,20 @@ namespace pump {
 namespace {
 
 
-__device__ __forceinline__ uint32_t float_key(float f) {
-  uint32_t u = __float_as_uint(f);
+// Order-preserving 32-bit keys of binary32 values (negative NaNs first,
+// positive NaNs last), computed from the value's bits.  Keys are built from
+// integer loads of the cost arrays and results stored as integers: a value
+// that passes through a float register may come back with other NaN bits
+// (code generated for a float load feeding a select turned positive NaNs
+// into the key of -0.0).
+__device__ __forceinline__ uint32_t key_of_bits(uint32_t u) {
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
-__device__ __forceinline__ float key_float(uint32_t k) {
-  uint32_t u = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
-  return __uint_as_float(u);
+__device__ __forceinline__ uint32_t bits_of_key(uint32_t k) {
+  return (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+}
+__device__ __forceinline__ uint32_t ldg_bits(const float *p) {
+  return __ldg(reinterpret_cast<const unsigned int *>(p));
 }
 
 // ---------------------------------------------------------- radix select
@@ -33,35 +43,75 @@ struct SelectState {
   uint32_t prefix;
   uint32_t mask;
   unsigned long long k;
-  float result;
+  uint32_t result;  // the bits of the k-th value
 };
 
+// Sources of pair costs: src.bits(idx) for pair number idx, and
+// src.bits_at(idx, i, j) / src.at(idx, i, j) when the caller already knows
+// the pair (i, j) of idx.
 struct FlatSrc {
+  static constexpr bool kPairs = false;
   const float *v;
-  __device__ float operator()(long long i) const { return __ldg(&v[i]); }
+  __device__ uint32_t bits(long long i) const { return ldg_bits(&v[i]); }
+  __device__ uint32_t bits_at(long long i, int, int) const { return ldg_bits(&v[i]); }
+  __device__ float at(long long i, int, int) const { return __ldg(&v[i]); }
 };
 struct PairCoptSrc {
+  static constexpr bool kPairs = true;
   PairView pv;
-  __device__ float operator()(long long idx) const {
+  __device__ uint32_t bits(long long idx) const {
     int i, j;
     pv.pair(idx, &i, &j);
-    return pv.copt(i, j);
+    return pv.copt_bits(i, j);
   }
+  __device__ uint32_t bits_at(long long, int i, int j) const { return pv.copt_bits(i, j); }
+  __device__ float at(long long, int i, int j) const { return pv.copt(i, j); }
 };
+// Optimal times of the same pairs.
+struct FlatTopt {
+  const float *v;
+  __device__ float at(long long i, int, int) const { return __ldg(&v[i]); }
+};
+struct PairTopt {
+  PairView pv;
+  __device__ float at(long long, int i, int j) const { return pv.topt(i, j); }
+};
+
+constexpr int kSelectBatch = 8;
+constexpr int kSelectThreads = 256;
 
 // Src(i) -> the i-th value (a flat array, or a virtual pair array).
 template <class Src>
-__global__ void select_hist_kernel(Src src, long long n, const SelectState *__restrict__ st,
-                                   int shift, int bits, unsigned int *__restrict__ hist) {
+__global__ void __launch_bounds__(kSelectThreads) select_hist_kernel(Src src, long long n, const unsigned long long *d_n,
+                                   const SelectState *__restrict__ st, int shift, int bits,
+                                   unsigned int *__restrict__ hist) {
   __shared__ unsigned int sh[2048];
   const int nb = 1 << bits;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sh[b] = 0;
   __syncthreads();
   const uint32_t prefix = st->prefix, mask = st->mask;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-    const uint32_t key = float_key(src(i));
-    if ((key & mask) == prefix) atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
+  if (d_n && (long long)*d_n < n) n = (long long)*d_n;
+  // kSelectBatch loads in flight per thread before their shared-memory atomics
+  const long long stride = (long long)gridDim.x * blockDim.x * kSelectBatch;
+  // the loop bound is the warp's first item, so all 32 lanes reach the match
+  const long long w_first = blockIdx.x * (long long)blockDim.x * kSelectBatch + (threadIdx.x & ~31);
+  for (long long w0 = w_first; w0 < n; w0 += stride) {
+    const long long i0 = w0 + (threadIdx.x & 31);
+    uint32_t key[kSelectBatch];
+#pragma unroll
+    for (int u = 0; u < kSelectBatch; ++u) {
+      const long long i = i0 + (long long)u * blockDim.x;
+      key[u] = i < n ? key_of_bits(src.bits(i)) : 0u;
+    }
+    // equal bins within a warp are added once (many costs share a bin)
+#pragma unroll
+    for (int u = 0; u < kSelectBatch; ++u) {
+      const long long i = i0 + (long long)u * blockDim.x;
+      const bool in = i < n && (key[u] & mask) == prefix;
+      const uint32_t bin = in ? (key[u] >> shift) & (nb - 1) : 0xFFFFFFFFu;
+      const unsigned int peers = __match_any_sync(0xffffffffu, bin);
+      if (in && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&sh[bin], __popc(peers));
+    }
   }
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
@@ -71,19 +121,19 @@ __global__ void select_hist_kernel(Src src, long long n, const SelectState *__re
 // Start state of a selection and a cleared histogram (a kernel instead of a
 // host-to-device copy: a copy from pageable host memory would wait for the
 // stream to drain first).
-__global__ void select_init_kernel(SelectState *st, unsigned long long k, unsigned int *hist) {
+__global__ void __launch_bounds__(1024) select_init_kernel(SelectState *st, unsigned long long k, unsigned int *hist) {
   for (int i = threadIdx.x; i < 2048; i += blockDim.x) hist[i] = 0u;
   if (threadIdx.x == 0) {
     st->prefix = 0u;
     st->mask = 0u;
     st->k = k;
-    st->result = 0.0f;
+    st->result = 0u;
   }
 }
 
 // One block of 1024 threads: find the bin holding rank k, narrow the prefix,
 // clear the histogram for the next pass.
-__global__ void select_pick_kernel(SelectState *st, int shift, int bits, unsigned int *hist) {
+__global__ void __launch_bounds__(1024) select_pick_kernel(SelectState *st, int shift, int bits, unsigned int *hist) {
   __shared__ unsigned long long cum[1024];
   const int nb = 1 << bits;
   const int per = nb / 1024;  // 1 or 2 bins per thread
@@ -109,7 +159,7 @@ __global__ void select_pick_kernel(SelectState *st, int shift, int bits, unsigne
         st->prefix |= bin << shift;
         st->mask |= (uint32_t)(nb - 1) << shift;
         st->k = k - c;
-        if (shift == 0) st->result = key_float(st->prefix);
+        if (shift == 0) st->result = bits_of_key(st->prefix);
         break;
       }
       c += h;
@@ -139,30 +189,6 @@ struct OpenEdgeEmit {
     f_topt[pos] = topt[e];
   }
 };
-struct PairEdgePred {
-  PairView pv;
-  float rn;
-  __device__ bool operator()(long long idx) const {
-    int i, j;
-    pv.pair(idx, &i, &j);
-    return pv.copt(i, j) < rn;
-  }
-};
-struct PairEdgeEmit {
-  PairView pv;
-  long long cap;
-  int *src, *dst;
-  float *copt, *topt;
-  __device__ void operator()(long long idx, long long pos) const {
-    if (pos >= cap) return;
-    int i, j;
-    pv.pair(idx, &i, &j);
-    src[pos] = i;
-    dst[pos] = j;
-    copt[pos] = pv.copt(i, j);
-    topt[pos] = pv.topt(i, j);
-  }
-};
 struct FlagPred {
   const uint8_t *flags;
   __device__ bool operator()(long long i) const { return flags[i] != 0; }
@@ -172,26 +198,255 @@ struct IndexEmit {
   __device__ void operator()(long long idx, long long pos) const { out[pos] = (int)idx; }
 };
 
-// go_start[i] = first edge whose source is >= i (edges sorted by source).
-__global__ void go_start_kernel(const int *__restrict__ src, long long E, int N,
-                                int *__restrict__ go_start) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > N) return;
-  long long lo = 0, hi = E;
-  while (lo < hi) {
-    const long long mid = (lo + hi) >> 1;
-    if (src[mid] < i) lo = mid + 1; else hi = mid;
-  }
-  go_start[i] = (int)lo;
-}
-
 __global__ void copy_count_kernel(const unsigned long long *total, int *out) { *out = (int)*total; }
 
-// Device-side k-th smallest of src(0 .. n-1): the result lands in the ctx
-// select state; *d_result points at it (device).
+// ------------------------------------------------- rn and edges in one read
+// The reference sorts all N(N-1) pair costs to read rn and then scans them
+// again for the edges below rn.  Here a strided sample of kBracketSamples
+// costs gives a key bound key_hi (the upper edge of the 22-bit key bin of the
+// sample at a rank a few standard deviations above k): one compaction pass
+// keeps the pairs with key < key_hi (the superset, in index order, a few
+// percent of the pairs), the exact radix select for rank k runs over the
+// superset only, and the edges are compacted from it.  Every pair below rn
+// is in the superset whenever the superset holds more than k pairs, so rn
+// and the edges are exactly those of the full select; when it does not (the
+// sample misled) or the superset overflows its buffer, the host falls back to
+// the three-pass select and the full compaction.
+constexpr int kBracketSamples = 8192;
+
+// Rank r among the 2048 counts of hist (a block of 1024 threads, two bins
+// each): the bin and the rank within it land in *bin and *rem.
+__device__ void find_bin_2048(const unsigned int *hist, unsigned int r, unsigned int *s_warp,
+                              unsigned int *bin, unsigned int *rem) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const unsigned int h0 = hist[2 * t], h1 = hist[2 * t + 1];
+  const unsigned int v = h0 + h1;
+  unsigned int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const unsigned int w = s_warp[lane];
+    unsigned int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned int u = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += u;
+    }
+    s_warp[lane] = wi - w;
+  }
+  __syncthreads();
+  const unsigned int ex = s_warp[warp] + incl - v;
+  if (r >= ex && r < ex + v) {
+    if (r < ex + h0) {
+      *bin = 2 * t;
+      *rem = r - ex;
+    } else {
+      *bin = 2 * t + 1;
+      *rem = r - ex - h0;
+    }
+  }
+  __syncthreads();
+}
+
+// One block of 1024 threads: the keys of the samples at positions
+// floor((2q + 1) n / (2 S)), then two 11-bit radix steps to the 22-bit key
+// prefix of the sample of the given rank; *key_hi = the prefix's upper edge.
+template <class Src>
+__global__ void __launch_bounds__(1024) bracket_kernel(Src src, long long n, unsigned int rank,
+                                                       unsigned long long *key_hi) {
+  __shared__ uint32_t keys[kBracketSamples];
+  __shared__ unsigned int hist[2048];
+  __shared__ unsigned int s_warp[32];
+  __shared__ unsigned int s_bin, s_rem;
+  const int t = threadIdx.x;
+  for (int q = t; q < kBracketSamples; q += 1024) {
+    const long long pos = ((2LL * q + 1) * n) / (2LL * kBracketSamples);
+    keys[q] = key_of_bits(src.bits(pos));
+  }
+  uint32_t prefix = 0u, mask = 0u;
+  unsigned int r = rank;
+  for (int pass = 0; pass < 2; ++pass) {
+    const int shift = pass == 0 ? 21 : 10;
+    hist[2 * t] = 0u;
+    hist[2 * t + 1] = 0u;
+    __syncthreads();
+    for (int q = t; q < kBracketSamples; q += 1024) {
+      const uint32_t k = keys[q];
+      if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 2047u], 1u);
+    }
+    __syncthreads();
+    find_bin_2048(hist, r, s_warp, &s_bin, &s_rem);
+    prefix |= s_bin << shift;
+    mask |= 2047u << shift;
+    r = s_rem;
+  }
+  if (t == 0) *key_hi = ((unsigned long long)(prefix >> 10) + 1ull) << 10;
+}
+
+// Row a and column j of this thread's items of the tile at base (item r is
+// pair base + r * 256 + tid): one division per tile, then steps of 256.
+// Items at or past n get values that are never used.
+__device__ __forceinline__ void tile_pairs(long long base, int N, int (&a)[kCompactRows],
+                                           int (&j)[kCompactRows]) {
+  const long long i0 = base + threadIdx.x;
+  int aa = (int)(i0 / (N - 1));
+  int bb = (int)(i0 - (long long)aa * (N - 1));
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    if (r) {
+      bb += kCompactThreads;
+      while (bb >= N - 1) {
+        bb -= N - 1;
+        ++aa;
+      }
+    }
+    a[r] = aa;
+    j[r] = bb + (bb >= aa);
+  }
+}
+
+// The superset: pairs with key < key_hi, written as (pair number, cost) at
+// positions below cap.
+template <class Src>
+struct SupersetLoader {
+  using Item = uint32_t;  // the cost's bits
+  using State = unsigned long long;
+  Src src;
+  int N;
+  const unsigned long long *key_hi;
+  long long cap;
+  uint32_t *out_idx;
+  uint32_t *out_bits;
+  __device__ State begin() const { return *key_hi; }
+  __device__ void load(long long base, long long n, uint32_t (&c)[kCompactRows]) const {
+    if constexpr (Src::kPairs) {
+      int a[kCompactRows], j[kCompactRows];
+      tile_pairs(base, N, a, j);
+#pragma unroll
+      for (int r = 0; r < kCompactRows; ++r) {
+        const long long i = base + r * kCompactThreads + threadIdx.x;
+        c[r] = i < n ? src.bits_at(i, a[r], j[r]) : 0u;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < kCompactRows; ++r) {
+        const long long i = base + r * kCompactThreads + threadIdx.x;
+        c[r] = i < n ? src.bits_at(i, 0, 0) : 0u;
+      }
+    }
+  }
+  __device__ bool sel(State key_hi_v, uint32_t c) const {
+    return (unsigned long long)key_of_bits(c) < key_hi_v;
+  }
+  __device__ void emit(long long i, uint32_t c, long long pos) const {
+    if (pos < cap) {
+      out_idx[pos] = (uint32_t)i;
+      out_bits[pos] = c;
+    }
+  }
+};
+
+// Edges (mainPUMP.cu:327-346): pairs with cost < rn as (i, j, copt, topt);
+// the optimal time is read for the selected pairs only.
+struct PairItem {
+  float c;
+  int a, j;
+};
+template <class Src, class Topt>
+struct EdgeLoader {
+  using Item = PairItem;
+  using State = int;
+  Src src;
+  Topt tsrc;
+  int N;
+  float rn;
+  long long cap;
+  int *e_src, *e_dst;
+  float *e_copt, *e_topt;
+  __device__ State begin() const { return 0; }
+  __device__ void load(long long base, long long n, PairItem (&v)[kCompactRows]) const {
+    int a[kCompactRows], j[kCompactRows];
+    tile_pairs(base, N, a, j);
+#pragma unroll
+    for (int r = 0; r < kCompactRows; ++r) {
+      const long long i = base + r * kCompactThreads + threadIdx.x;
+      v[r].a = a[r];
+      v[r].j = j[r];
+      v[r].c = i < n ? src.at(i, a[r], j[r]) : 0.0f;
+    }
+  }
+  __device__ bool sel(State, const PairItem &v) const { return v.c < rn; }
+  __device__ void emit(long long i, const PairItem &v, long long pos) const {
+    if (pos >= cap) return;
+    e_src[pos] = v.a;
+    e_dst[pos] = v.j;
+    e_copt[pos] = v.c;
+    e_topt[pos] = tsrc.at(i, v.a, v.j);
+  }
+};
+
+// rn's bits and the superset size for one read-back.
+struct RnPack {
+  uint32_t rn_bits;
+  int pad;
+  unsigned long long n_sup;
+};
+__global__ void rn_pack_kernel(const float *rn, const unsigned long long *n_sup, RnPack *out) {
+  out->rn_bits = *reinterpret_cast<const unsigned int *>(rn);
+  out->pad = 0;
+  out->n_sup = *n_sup;
+}
+
+// Edges from the superset: entries with cost < rn, in superset (= pair) order.
+struct SupItem {
+  float c;
+  uint32_t id;
+};
+template <class Topt>
+struct SupEdgeLoader {
+  using Item = SupItem;
+  using State = int;
+  const uint32_t *idx;
+  const float *sc;
+  Topt tsrc;
+  int N;
+  float rn;
+  long long cap;
+  int *e_src, *e_dst;
+  float *e_copt, *e_topt;
+  __device__ State begin() const { return 0; }
+  __device__ void load(long long base, long long n, SupItem (&v)[kCompactRows]) const {
+#pragma unroll
+    for (int r = 0; r < kCompactRows; ++r) {
+      const long long q = base + r * kCompactThreads + threadIdx.x;
+      v[r].c = q < n ? __ldg(&sc[q]) : 0.0f;
+      v[r].id = q < n ? __ldg(&idx[q]) : 0u;
+    }
+  }
+  __device__ bool sel(State, const SupItem &v) const { return v.c < rn; }
+  __device__ void emit(long long, const SupItem &v, long long pos) const {
+    if (pos >= cap) return;
+    const uint32_t a = v.id / (uint32_t)(N - 1), b = v.id - a * (uint32_t)(N - 1);
+    const int j = (int)b + (b >= a ? 1 : 0);
+    e_src[pos] = (int)a;
+    e_dst[pos] = j;
+    e_copt[pos] = v.c;
+    e_topt[pos] = tsrc.at((long long)v.id, (int)a, j);
+  }
+};
+
+// Device-side k-th smallest of src(0 .. n-1), or of src(0 .. *d_n - 1) when
+// d_n (device) is given and below n: the result lands in the ctx select
+// state; *d_result points at it (device).
 template <class Src>
 pump_status_t select_kth_src(Ctx *ctx, Src src, long long n, long long k, const float **d_result,
-                             cudaStream_t stream) {
+                             cudaStream_t stream, const unsigned long long *d_n = nullptr,
+                             long long max_blocks = kNumSMs * 4) {
   if (n <= 0 || k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "select_kth: k=%lld n=%lld", k, n);
   char *scratch = nullptr;
   const size_t bytes = sizeof(SelectState) + 2048 * sizeof(unsigned int);
@@ -200,16 +455,18 @@ pump_status_t select_kth_src(Ctx *ctx, Src src, long long n, long long k, const 
   unsigned int *hist = (unsigned int *)(scratch + sizeof(SelectState));
   select_init_kernel<<<1, 1024, 0, stream>>>(st, (unsigned long long)k, hist);
   PUMP_TRY(launch_status("select_init_kernel"));
-  long long blocks = (n + 1023) / 1024;
-  if (blocks > kNumSMs * 8) blocks = kNumSMs * 8;
+  long long blocks = (n + (long long)kSelectThreads * kSelectBatch - 1) /
+                     ((long long)kSelectThreads * kSelectBatch);
+  if (blocks > max_blocks) blocks = max_blocks;
   const int shifts[3] = {21, 10, 0}, bits[3] = {11, 11, 10};
   for (int pass = 0; pass < 3; ++pass) {
-    select_hist_kernel<<<(unsigned)blocks, 1024, 0, stream>>>(src, n, st, shifts[pass], bits[pass], hist);
+    select_hist_kernel<<<(unsigned)blocks, kSelectThreads, 0, stream>>>(src, n, d_n, st, shifts[pass],
+                                                              bits[pass], hist);
     PUMP_TRY(launch_status("select_hist_kernel"));
     select_pick_kernel<<<1, 1024, 0, stream>>>(st, shifts[pass], bits[pass], hist);
     PUMP_TRY(launch_status("select_pick_kernel"));
   }
-  *d_result = &st->result;
+  *d_result = reinterpret_cast<const float *>(&st->result);
   return PUMP_OK;
 }
 
@@ -225,39 +482,34 @@ pump_status_t select_kth_pairs(Ctx *ctx, const PairView &pv, long long k, const 
   return select_kth_src(ctx, PairCoptSrc{pv}, (long long)pv.N * (pv.N - 1), k, d_result, stream);
 }
 
-pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N, float rn,
-                                 long long max_edges, int *d_src, int *d_dst, float *d_copt,
-                                 float *d_topt, int *d_go_start, long long *h_num_edges,
-                                 cudaStream_t stream) {
+namespace {
+// The edges below rn with their row starts, from any pair-cost source.
+template <class Src, class Topt>
+pump_status_t edges_src(Ctx *ctx, Src src, Topt tsrc, int N, float rn, long long max_edges,
+                        int *d_src, int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
+                        long long *h_num_edges, cudaStream_t stream) {
   const long long npairs = (long long)N * (N - 1);
   TileScratch ts{};
-  {
-    const long long ntiles = npairs > 0 ? (npairs + kTile - 1) / kTile : 1;
-    const size_t bytes = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
-    char *scratch = nullptr;
-    PUMP_TRY(ctx->scratch(Ctx::kCompact, bytes, (void **)&scratch));
-    ts.total = (unsigned long long *)scratch;
-    ts.status = ts.total + 1;
-    ts.tile_counter = (unsigned int *)(ts.status + ntiles + 1);
-    ts.error = (int *)(ts.tile_counter + 1);
-    PUMP_CUDA_TRY(cudaMemsetAsync(scratch, 0, bytes, stream));
-    if (npairs > 0) {
-      if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "build_edges: too many tiles");
-      edge_compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(
-          npairs, N, d_copts, d_topts, rn, max_edges, d_src, d_dst, d_copt, d_topt, ts);
-      PUMP_TRY(launch_status("edge_compact_kernel"));
-    }
-  }
+  PUMP_TRY(run_chunked(ctx, npairs,
+                       EdgeLoader<Src, Topt>{src, tsrc, N, rn, max_edges, d_src, d_dst, d_copt,
+                                             d_topt},
+                       stream, &ts));
   unsigned long long total = 0;
   PUMP_TRY(finish_compact(ts, &total, stream));
   *h_num_edges = (long long)total;
   if ((long long)total > max_edges)
     return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", total, max_edges);
-  if (d_go_start) {
-    go_start_kernel<<<grid_for(N + 1, 256), 256, 0, stream>>>(d_src, (long long)total, N, d_go_start);
-    PUMP_TRY(launch_status("go_start_kernel"));
-  }
+  if (d_go_start) PUMP_TRY(row_starts(d_src, (long long)total, N, d_go_start, stream));
   return PUMP_OK;
+}
+}  // namespace
+
+pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N, float rn,
+                                 long long max_edges, int *d_src, int *d_dst, float *d_copt,
+                                 float *d_topt, int *d_go_start, long long *h_num_edges,
+                                 cudaStream_t stream) {
+  return edges_src(ctx, FlatSrc{d_copts}, FlatTopt{d_topts}, N, rn, max_edges, d_src, d_dst,
+                   d_copt, d_topt, d_go_start, h_num_edges, stream);
 }
 
 // The expandable edges in (source, destination) order with their row starts
@@ -276,32 +528,107 @@ pump_status_t open_edges_device(Ctx *ctx, const uint8_t *d_free_e, const uint8_t
   unsigned long long total = 0;
   PUMP_TRY(finish_compact(ts, &total, stream));
   *h_count = (long long)total;
-  go_start_kernel<<<grid_for(N + 1, 256), 256, 0, stream>>>(d_fsrc, (long long)total, N, d_fgo);
-  return launch_status("go_start_kernel");
+  return row_starts(d_fsrc, (long long)total, N, d_fgo, stream);
 }
 
-// Device-side frontier compaction; *d_error_out (device) is nonzero when a
-// look-back wait gave up.
 // Edges of one query of a batch from its pair view (same order and values as
 // build_edges_device on the query's own pair arrays).
 pump_status_t build_edges_pairs(Ctx *ctx, const PairView &pv, float rn, long long max_edges,
                                 int *d_src, int *d_dst, float *d_copt, float *d_topt,
                                 int *d_go_start, long long *h_num_edges, cudaStream_t stream) {
-  const int N = pv.N;
-  const long long npairs = (long long)N * (N - 1);
+  return edges_src(ctx, PairCoptSrc{pv}, PairTopt{pv}, pv.N, rn, max_edges, d_src, d_dst, d_copt,
+                   d_topt, d_go_start, h_num_edges, stream);
+}
+
+namespace {
+// rn = the k-th smallest pair cost and the edges below it (same values and
+// order as select_kth + build_edges) from one read of the pair costs: the
+// bracket sample, the superset pass, the select over the superset, one
+// read-back, then the edges from the superset.  `fallback` runs the
+// three-pass select and the full compaction when the superset misses rank k,
+// overflows, or the pass does not apply (few pairs, 2^32 pairs or more).
+template <class Src, class Topt, class Fallback>
+pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, long long max_edges,
+                           int *d_src, int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
+                           float *h_rn, long long *h_num_edges, cudaStream_t stream,
+                           Fallback fallback) {
+  const long long n = (long long)N * (N - 1);
+  const int S = kBracketSamples;
+  if (k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "rn_edges: k=%lld n=%lld", k, n);
+  const double p = (double)(k + 1) / (double)n;
+  const long long rank = (long long)std::ceil(p * S + 8.0 * std::sqrt(S * p * (1.0 - p))) + 16;
+  if (n < 64LL * S || n >= (1LL << 32) || rank >= S) return fallback();
+  const long long cap = std::min(n, 2 * (rank + 1) * (n / S + 1) + 65536);
+  if (k >= cap) return fallback();
+  char *buf = nullptr;
+  PUMP_TRY(ctx->scratch(Ctx::kSuperset, 32 + (size_t)cap * 8, (void **)&buf));
+  unsigned long long *d_key_hi = (unsigned long long *)buf;
+  RnPack *d_pack = (RnPack *)(buf + 16);
+  uint32_t *sup_idx = (uint32_t *)(buf + 32);
+  float *sup_c = (float *)(sup_idx + cap);
+  bracket_kernel<<<1, 1024, 0, stream>>>(src, n, (unsigned int)rank, d_key_hi);
+  PUMP_TRY(launch_status("bracket_kernel"));
   TileScratch ts{};
-  PUMP_TRY(run_compact(ctx, npairs, PairEdgePred{pv, rn},
-                       PairEdgeEmit{pv, max_edges, d_src, d_dst, d_copt, d_topt}, stream, &ts));
+  PUMP_TRY(run_chunked(ctx, n,
+                       SupersetLoader<Src>{src, N, d_key_hi, cap, sup_idx, (uint32_t *)sup_c},
+                       stream, &ts));
+  const float *d_rn = nullptr;
+  PUMP_TRY(select_kth_src(ctx, FlatSrc{sup_c}, cap, k, &d_rn, stream, ts.total));
+  rn_pack_kernel<<<1, 1, 0, stream>>>(d_rn, ts.total, d_pack);
+  PUMP_TRY(launch_status("rn_pack_kernel"));
+  RnPack pk{};
+  PUMP_CUDA_TRY(cudaMemcpyAsync(&pk, d_pack, sizeof pk, cudaMemcpyDeviceToHost, stream));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
+  if ((long long)pk.n_sup <= k || (long long)pk.n_sup > cap) return fallback();
+  float rn;
+  std::memcpy(&rn, &pk.rn_bits, sizeof rn);
+  *h_rn = rn;
+  TileScratch ts2{};
+  PUMP_TRY(run_chunked(ctx, (long long)pk.n_sup,
+                       SupEdgeLoader<Topt>{sup_idx, sup_c, tsrc, N, rn, max_edges, d_src, d_dst,
+                                           d_copt, d_topt},
+                       stream, &ts2));
   unsigned long long total = 0;
-  PUMP_TRY(finish_compact(ts, &total, stream));
+  PUMP_TRY(finish_compact(ts2, &total, stream));
   *h_num_edges = (long long)total;
   if ((long long)total > max_edges)
     return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", total, max_edges);
-  if (d_go_start) {
-    go_start_kernel<<<grid_for(N + 1, 256), 256, 0, stream>>>(d_src, (long long)total, N, d_go_start);
-    PUMP_TRY(launch_status("go_start_kernel"));
-  }
+  if (d_go_start) PUMP_TRY(row_starts(d_src, (long long)total, N, d_go_start, stream));
   return PUMP_OK;
+}
+
+}  // namespace
+
+pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
+                              long long k, long long max_edges, int *d_src, int *d_dst,
+                              float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
+                              long long *h_num_edges, cudaStream_t stream) {
+  auto fallback = [&]() -> pump_status_t {
+    const float *d_rn = nullptr;
+    PUMP_TRY(select_kth_device(ctx, d_copts, (long long)N * (N - 1), k, &d_rn, stream));
+    PUMP_CUDA_TRY(cudaMemcpyAsync(h_rn, d_rn, sizeof(float), cudaMemcpyDeviceToHost, stream));
+    PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
+    return build_edges_device(ctx, d_copts, d_topts, N, *h_rn, max_edges, d_src, d_dst, d_copt,
+                              d_topt, d_go_start, h_num_edges, stream);
+  };
+  return rn_edges_src(ctx, FlatSrc{d_copts}, FlatTopt{d_topts}, N, k, max_edges, d_src, d_dst,
+                      d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream, fallback);
+}
+
+pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long long max_edges,
+                             int *d_src, int *d_dst, float *d_copt, float *d_topt,
+                             int *d_go_start, float *h_rn, long long *h_num_edges,
+                             cudaStream_t stream) {
+  auto fallback = [&]() -> pump_status_t {
+    const float *d_rn = nullptr;
+    PUMP_TRY(select_kth_pairs(ctx, pv, k, &d_rn, stream));
+    PUMP_CUDA_TRY(cudaMemcpyAsync(h_rn, d_rn, sizeof(float), cudaMemcpyDeviceToHost, stream));
+    PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
+    return build_edges_pairs(ctx, pv, *h_rn, max_edges, d_src, d_dst, d_copt, d_topt, d_go_start,
+                             h_num_edges, stream);
+  };
+  return rn_edges_src(ctx, PairCoptSrc{pv}, PairTopt{pv}, pv.N, k, max_edges, d_src, d_dst, d_copt,
+                      d_topt, d_go_start, h_rn, h_num_edges, stream, fallback);
 }
 
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
@@ -444,4 +771,18 @@ extern "C" pump_status_t pump_frontier_compact_noalloc(const uint8_t *d_flags, i
   if (err)
     return set_error(PUMP_ERR_TIMEOUT, "pump_frontier_compact_noalloc: look-back wait exceeded its bound");
   return PUMP_OK;
+}
+
+extern "C" pump_status_t pump_roadmap_edges(pump_ctx *ctx, const float *d_copts, const float *d_topts,
+                                            int N, long long k, long long max_edges, int *d_src,
+                                            int *d_dst, float *d_copt, float *d_topt,
+                                            int *d_go_start, float *h_rn, long long *h_num_edges,
+                                            pump_stream_t stream) {
+  if (!ctx || !d_copts || !d_topts || N < 2 || max_edges < 0 || !d_src || !d_dst || !d_copt ||
+      !d_topt || !h_rn || !h_num_edges)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_roadmap_edges: bad arguments");
+  Ctx *c = Ctx::from(ctx);
+  PUMP_TRY(c->activate());
+  return rn_edges_device(c, d_copts, d_topts, N, k, max_edges, d_src, d_dst, d_copt, d_topt,
+                         d_go_start, h_rn, h_num_edges, (cudaStream_t)stream);
 }

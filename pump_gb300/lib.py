@@ -88,6 +88,8 @@ _SIGS = {
     "pump_bvp_batch": (i32, [vp, vp, i32, f32, i32, vp, vp, vp]),
     "pump_select_kth": (i32, [vp, vp, i64, i64, C.POINTER(f32), vp]),
     "pump_build_edges": (i32, [vp, vp, vp, i32, f32, i64, vp, vp, vp, vp, vp, C.POINTER(i64), vp]),
+    "pump_roadmap_edges": (i32, [vp, vp, vp, i32, i64, i64, vp, vp, vp, vp, vp, C.POINTER(f32),
+                                 C.POINTER(i64), vp]),
     "pump_discretize_edges": (i32, [vp, vp, vp, vp, i64, i32, i32, vp, vp]),
     "pump_sample_free": (i32, [vp, i32, vp, i32, vp, vp]),
     "pump_free_edges": (i32, [vp, i32, vp, i64, i32, vp, vp]),

@@ -97,6 +97,32 @@ def test_bvp_batch_parity(gpu, pumplib, oracle):
         assert same_bits(t, rt) and same_bits(c, rc)
 
 
+def kth_in_key_order(v, k):
+    """The k-th smallest float32 in the order of the sign-magnitude keys:
+    negative NaNs first, then -inf .. -0.0, +0.0 .. +inf, positive NaNs."""
+    u = np.ascontiguousarray(v, np.float32).view(np.uint32)
+    key = np.where(u & 0x80000000, ~u, u | 0x80000000).astype(np.uint32)
+    kk = np.sort(key)[k]
+    b = kk & 0x7FFFFFFF if kk & 0x80000000 else ~kk & 0xFFFFFFFF
+    return np.array([b], np.uint32).view(np.float32)[0]
+
+
+@pytest.mark.parametrize("k", [0, 10, 100_000, 1_960_000, 1_999_999])
+def test_select_kth_nan(k, gpu, pumplib):
+    """NaNs of both signs keep their place in the key order (positive NaNs
+    above +inf, negative ones below -inf); the value comes back bit-exact."""
+    torch, ctx = gpu
+    v = np.arange(1, 2_000_001, dtype=np.float32)
+    v[::50] = np.float32("nan")
+    v.view(np.uint32)[7::97] = 0xFFC00000
+    v[3::101] *= -1
+    out = C.c_float(0)
+    d = dev(torch, v)
+    pumplib.check(pumplib.load().pump_select_kth(ctx.handle, ptr(d), v.size, k, C.byref(out),
+                                                 stream(torch)))
+    assert same_bits(np.float32(out.value), kth_in_key_order(v, k))
+
+
 @pytest.mark.parametrize("n,k", [(1, 0), (1000, 0), (1000, 999), (100003, 5000), (5_000_000, 250_000)])
 def test_select_kth(n, k, gpu, pumplib):
     torch, ctx = gpu
@@ -155,6 +181,96 @@ def test_build_edges_and_waypoints(gpu, pumplib, roadmap1000):
                                           ptr(d_disc), stream(torch)))
     disc = host(d_disc, E * 54).reshape(E, 9, 6)
     assert same_bits(disc, r["disc"]), "waypoint mismatches: %d" % int((disc != r["disc"]).sum())
+
+
+def roadmap_edges(torch, pumplib, ctx, c, t, N, k, cap):
+    """pump_roadmap_edges on host arrays: (rn, src, dst, copt, topt, go)."""
+    d_c, d_t = dev(torch, c), dev(torch, t)
+    d_src, d_dst = empty(torch, cap, torch.int32), empty(torch, cap, torch.int32)
+    d_ce, d_te = empty(torch, cap, torch.float32), empty(torch, cap, torch.float32)
+    d_go = empty(torch, N + 1, torch.int32)
+    rn, E = C.c_float(0), C.c_longlong(0)
+    pumplib.check(pumplib.load().pump_roadmap_edges(
+        ctx.handle, ptr(d_c), ptr(d_t), N, k, cap, ptr(d_src), ptr(d_dst), ptr(d_ce), ptr(d_te),
+        ptr(d_go), C.byref(rn), C.byref(E), stream(torch)))
+    E = E.value
+    return (np.float32(rn.value), host(d_src, E), host(d_dst, E), host(d_ce, E), host(d_te, E),
+            host(d_go, N + 1))
+
+
+def test_roadmap_edges_one_read(gpu, pumplib, roadmap1000):
+    """rn and the edges from one read of the pair costs equal pump_select_kth +
+    pump_build_edges (the oracle's sort and scan) bit for bit."""
+    torch, ctx = gpu
+    r = roadmap1000
+    N = r["N"]
+    rn, src, dst, ce, te, go = roadmap_edges(torch, pumplib, ctx, r["copts"], r["topts"], N, r["k"],
+                                             r["k"])
+    assert rn == np.float32(r["rn"])
+    assert np.array_equal(src, r["src"]) and np.array_equal(dst, r["dst"])
+    assert same_bits(ce, r["ce"]) and same_bits(te, r["te"])
+    assert np.array_equal(go, np.searchsorted(r["src"], np.arange(N + 1), side="left"))
+
+
+@pytest.mark.parametrize("pattern", ["plain", "sample_high", "sample_low", "ties", "small"])
+def test_roadmap_edges_patterns(pattern, gpu, pumplib, oracle):
+    """Cost patterns that defeat the strided sample (every sampled pair far
+    above or below the rest) or crowd rn with ties, and a roadmap too small
+    for the one-read pass: the result is the oracle's sort and scan."""
+    torch, ctx = gpu
+    N = 300 if pattern == "small" else 1200
+    n = N * (N - 1)
+    k = int(n * np.float32(0.05))
+    rng = np.random.default_rng(N)
+    c = rng.exponential(10.0, n).astype(np.float32)
+    t = rng.uniform(0.1, 5.0, n).astype(np.float32)
+    q = np.arange(8192, dtype=np.int64)
+    pos = ((2 * q + 1) * n) // (2 * 8192)
+    if pattern == "sample_high":
+        c[pos] = np.float32(1e6)
+    elif pattern == "sample_low":
+        c[pos] = np.float32(-1.0)
+    elif pattern == "ties":
+        v = np.partition(c, k)[k]
+        c[rng.random(n) < 0.1] = v
+    rn64 = oracle.lib().orc_select_kth(c.size, c, k)
+    src, dst, ce, te = oracle.build_edges(c, t, N, rn64)
+    rn, s2, d2, ce2, te2, go = roadmap_edges(torch, pumplib, ctx, c, t, N, k, k)
+    assert rn == np.float32(rn64)
+    assert np.array_equal(s2, src) and np.array_equal(d2, dst)
+    assert same_bits(ce2, ce) and same_bits(te2, te)
+    assert np.array_equal(go, np.searchsorted(src, np.arange(N + 1), side="left"))
+
+
+def test_roadmap_edges_nan_costs(gpu, pumplib):
+    """NaN costs (either sign) order as the full radix select orders them:
+    the one-read result equals pump_select_kth + pump_build_edges."""
+    torch, ctx = gpu
+    L = pumplib.load()
+    N = 1100
+    n = N * (N - 1)
+    k = int(n * np.float32(0.05))
+    rng = np.random.default_rng(11)
+    c = rng.normal(5.0, 3.0, n).astype(np.float32)
+    t = rng.uniform(0.1, 5.0, n).astype(np.float32)
+    c[rng.random(n) < 0.02] = np.float32("nan")
+    c.view(np.uint32)[rng.random(n) < 0.02] = 0xFFC00000  # negative NaN
+    rn, src, dst, ce, te, go = roadmap_edges(torch, pumplib, ctx, c, t, N, k, k)
+    assert same_bits(rn, kth_in_key_order(c, k))
+    out = C.c_float(0)
+    d_c, d_t = dev(torch, c), dev(torch, t)
+    pumplib.check(L.pump_select_kth(ctx.handle, ptr(d_c), n, k, C.byref(out), stream(torch)))
+    assert same_bits(np.float32(out.value), rn)
+    d_src, d_dst = empty(torch, k, torch.int32), empty(torch, k, torch.int32)
+    d_ce, d_te = empty(torch, k, torch.float32), empty(torch, k, torch.float32)
+    E = C.c_longlong(0)
+    pumplib.check(L.pump_build_edges(ctx.handle, ptr(d_c), ptr(d_t), N, out.value, k, ptr(d_src),
+                                     ptr(d_dst), ptr(d_ce), ptr(d_te), None, C.byref(E),
+                                     stream(torch)))
+    E = E.value
+    assert E == src.size
+    assert np.array_equal(host(d_src, E), src) and np.array_equal(host(d_dst, E), dst)
+    assert same_bits(host(d_ce, E), ce) and same_bits(host(d_te, E), te)
 
 
 def test_collision_checks(gpu, pumplib, oracle, roadmap1000):

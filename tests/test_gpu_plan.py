@@ -114,7 +114,7 @@ def test_plan_batch_equals_single_queries(gpu, pumplib):
     torch, ctx = gpu
     from pump_gb300 import workloads
     L = pumplib.load()
-    qs = workloads.batch_queries(12, seed=77, n_range=(200, 900), obs_range=(5, 30))
+    qs = workloads.batch_queries(12, seed=77, n_range=(200, 1400), obs_range=(5, 30))
     keep = []
     pbs = (pumplib.Problem * len(qs))(*[fill_problem(pumplib, q, keep) for q in qs])
     for k in range(len(qs)):
