@@ -217,21 +217,21 @@ __global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
   }
 }
 
-__global__ void bvp_batch_kernel(const float *__restrict__ x0s, const float *__restrict__ x1s,
-                                 int n, float tmax, float *__restrict__ topt,
-                                 float *__restrict__ cost) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+__global__ void bvp_batch_kernel(const BvpJobs jb) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= jb.n * jb.jobs) return;
+  const int j = k >= jb.n ? 1 : 0;
+  k -= j * jb.n;
   float x0[kDim], x1[kDim];
 #pragma unroll
   for (int d = 0; d < kDim; ++d) {
-    x0[d] = x0s[k * kDim + d];
-    x1[d] = x1s[k * kDim + d];
+    x0[d] = jb.x0[k * kDim + d];
+    x1[d] = jb.x1[k * kDim + d];
   }
   const PairCoef c = make_coef(x0, x1);
-  const float tp = topt_bisection(c, tmax);
-  if (topt) topt[k] = tp;
-  if (cost) cost[k] = cost_eval(c, tp);
+  const float tp = topt_bisection(c, jb.tmax[j]);
+  if (jb.topt[j]) jb.topt[j][k] = tp;
+  if (jb.cost[j]) jb.cost[j][k] = cost_eval(c, tp);
 }
 
 // pathPoint, 2pBVP.cu:117-131, in the expression's own evaluation types.
@@ -408,7 +408,9 @@ __global__ void candidate_times_kernel(const int *__restrict__ node_cnt,
 // States of every sample, one thread per (path, row): rows of path p start at
 // p * rows_cap (rows at or past rows_cap are not written); the row's segment
 // is the last one of the path whose first row is at or before it (segments
-// with no samples share their first row with the next).
+// with no samples share their first row with the next).  The precision mode
+// evaluates the cubic in binary32, as its edge waypoints do.
+template <int Mode>
 __global__ void candidate_states_kernel(const float *__restrict__ x0, const float *__restrict__ x1,
                                         const float *__restrict__ topt,
                                         const int *__restrict__ node_cnt,
@@ -435,7 +437,8 @@ __global__ void candidate_states_kernel(const float *__restrict__ x0, const floa
     a[d] = x0[s * kDim + d];
     c[d] = x1[s * kDim + d];
   }
-  path_point(dt * k + seg_toff[s], topt[s], a, c, x);
+  if (Mode == PUMP_BVP_PARITY) path_point(dt * k + seg_toff[s], topt[s], a, c, x);
+  else path_point_f32(dt * k + seg_toff[s], topt[s], a, c, x);
 #pragma unroll
   for (int d = 0; d < kDim; ++d) states[t * kDim + d] = x[d];
 }
@@ -450,22 +453,44 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
       cb.nodes, cb.node_off, cb.node_cnt, cb.seg_base, n_paths, cb.x0, cb.x1, cb.seg_path);
   PUMP_TRY(launch_status("candidate_segments"));
   if (n_seg > 0) {
-    PUMP_TRY(pump_bvp_batch(cb.x0, cb.x1, n_seg, 5.0f, mode, cb.topt, nullptr, (pump_stream_t)s));
-    if (with_cost)
-      PUMP_TRY(pump_bvp_batch(cb.x0, cb.x1, n_seg, 2.0f, mode, nullptr, cb.seg_cost,
-                              (pump_stream_t)s));
+    // optimal times (tmax 5) and smoothing costs (tmax 2) in one launch
+    BvpJobs jb{};
+    jb.x0 = cb.x0;
+    jb.x1 = cb.x1;
+    jb.n = n_seg;
+    jb.jobs = with_cost ? 2 : 1;
+    jb.tmax[0] = 5.0f;
+    jb.topt[0] = cb.topt;
+    jb.tmax[1] = 2.0f;
+    jb.cost[1] = cb.seg_cost;
+    PUMP_TRY(bvp_jobs_launch(jb, mode, s));
   }
   candidate_times_kernel<<<grid_for(n_paths, 64), 64, 0, s>>>(
       cb.node_cnt, cb.seg_base, n_paths, cb.topt, with_cost ? cb.seg_cost : nullptr, dt, cb.seg_T,
       cb.seg_toff, cb.seg_row, cb.len, with_cost ? cb.cost : nullptr);
   PUMP_TRY(launch_status("candidate_times"));
   if (n_seg > 0) {
-    candidate_states_kernel<<<grid_for((long long)n_paths * rows_cap, 128), 128, 0, s>>>(
-        cb.x0, cb.x1, cb.topt, cb.node_cnt, cb.seg_base, cb.seg_T, cb.seg_toff, cb.seg_row, cb.len,
-        n_paths, dt, rows_cap, cb.states);
+    const long long rows = (long long)n_paths * rows_cap;
+    if (mode == PUMP_BVP_PARITY)
+      candidate_states_kernel<PUMP_BVP_PARITY><<<grid_for(rows, 64), 64, 0, s>>>(
+          cb.x0, cb.x1, cb.topt, cb.node_cnt, cb.seg_base, cb.seg_T, cb.seg_toff, cb.seg_row,
+          cb.len, n_paths, dt, rows_cap, cb.states);
+    else
+      candidate_states_kernel<PUMP_BVP_PRECISION><<<grid_for(rows, 64), 64, 0, s>>>(
+          cb.x0, cb.x1, cb.topt, cb.node_cnt, cb.seg_base, cb.seg_T, cb.seg_toff, cb.seg_row,
+          cb.len, n_paths, dt, rows_cap, cb.states);
     PUMP_TRY(launch_status("candidate_states"));
   }
   return PUMP_OK;
+}
+
+pump_status_t bvp_jobs_launch(const BvpJobs &jb, int mode, cudaStream_t stream) {
+  if (jb.n <= 0) return PUMP_OK;
+  if (mode == PUMP_BVP_PRECISION) return bvp_jobs_precision_launch(jb, stream);
+  const long long total = (long long)jb.n * jb.jobs;
+  const int threads = total < 152LL * 128 ? 32 : 128;
+  bvp_batch_kernel<<<grid_for(total, threads), threads, 0, stream>>>(jb);
+  return launch_status("bvp_batch");
 }
 
 pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
@@ -507,11 +532,15 @@ extern "C" pump_status_t pump_bvp_batch(const float *d_x0, const float *d_x1, in
       (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_bvp_batch: bad arguments");
   if (n == 0) return PUMP_OK;
-  if (mode == PUMP_BVP_PRECISION)
-    return bvp_batch_precision_launch(d_x0, d_x1, n, tmax, d_topt, d_cost, (cudaStream_t)stream);
-  bvp_batch_kernel<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(d_x0, d_x1, n, tmax, d_topt,
-                                                                      d_cost);
-  return launch_status("bvp_batch");
+  BvpJobs jb{};
+  jb.x0 = d_x0;
+  jb.x1 = d_x1;
+  jb.n = n;
+  jb.jobs = 1;
+  jb.tmax[0] = tmax;
+  jb.topt[0] = d_topt;
+  jb.cost[0] = d_cost;
+  return bvp_jobs_launch(jb, mode, (cudaStream_t)stream);
 }
 
 extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src,

@@ -54,21 +54,21 @@ __global__ void __launch_bounds__(128) bvp_pairs_precision_kernel(const SampleF 
   copts[idx] = d2f_rn(c);
 }
 
-__global__ void bvp_batch_precision_kernel(const float *__restrict__ x0s,
-                                           const float *__restrict__ x1s, int n, float tmax,
-                                           float *__restrict__ topt, float *__restrict__ cost) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+__global__ void bvp_batch_precision_kernel(const BvpJobs jb) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= jb.n * jb.jobs) return;
+  const int j = k >= jb.n ? 1 : 0;
+  k -= j * jb.n;
   float x0[kDim], x1[kDim];
 #pragma unroll
   for (int d = 0; d < kDim; ++d) {
-    x0[d] = x0s[k * kDim + d];
-    x1[d] = x1s[k * kDim + d];
+    x0[d] = jb.x0[k * kDim + d];
+    x1[d] = jb.x1[k * kDim + d];
   }
   float tp, cp;
-  precise_pair(x0, x1, tmax, &tp, &cp);
-  if (topt) topt[k] = tp;
-  if (cost) cost[k] = cp;
+  precise_pair(x0, x1, jb.tmax[j], &tp, &cp);
+  if (jb.topt[j]) jb.topt[j][k] = tp;
+  if (jb.cost[j]) jb.cost[j][k] = cp;
 }
 
 }  // namespace
@@ -89,10 +89,10 @@ pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tm
   return st;
 }
 
-pump_status_t bvp_batch_precision_launch(const float *d_x0, const float *d_x1, int n, float tmax,
-                                         float *d_topt, float *d_cost, cudaStream_t stream) {
-  bvp_batch_precision_kernel<<<grid_for(n, 128), 128, 0, stream>>>(d_x0, d_x1, n, tmax, d_topt,
-                                                                  d_cost);
+pump_status_t bvp_jobs_precision_launch(const BvpJobs &jb, cudaStream_t stream) {
+  const long long total = (long long)jb.n * jb.jobs;
+  const int threads = total < 152LL * 128 ? 32 : 128;
+  bvp_batch_precision_kernel<<<grid_for(total, threads), threads, 0, stream>>>(jb);
   return launch_status("bvp_batch_precision");
 }
 

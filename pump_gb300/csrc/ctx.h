@@ -89,8 +89,18 @@ pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor
                                     cudaStream_t stream);
 pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tmax, float *d_copts,
                                          float *d_topts, cudaStream_t stream);
-pump_status_t bvp_batch_precision_launch(const float *d_x0, const float *d_x1, int n, float tmax,
-                                         float *d_topt, float *d_cost, cudaStream_t stream);
+// Explicit pairs (x0[k], x1[k]), k < n, each bisected for `jobs` (1 or 2)
+// optimal-time limits: job j writes topt[j][k] and cost[j][k] (either may be
+// null).  One thread per (job, pair); small batches use 32-thread blocks so
+// their binary64 bisections spread over more SMs.
+struct BvpJobs {
+  const float *x0, *x1;
+  int n, jobs;
+  float tmax[2];
+  float *topt[2], *cost[2];
+};
+pump_status_t bvp_jobs_launch(const BvpJobs &jb, int mode, cudaStream_t stream);
+pump_status_t bvp_jobs_precision_launch(const BvpJobs &jb, cudaStream_t stream);
 // Device buffers of a batch of candidate paths (node states of each path,
 // contiguous): its segments as explicit pairs, their optimal times (tmax 5)
 // and smoothing costs (tmax 2), the dense path of findOptimalPath per path
