@@ -407,8 +407,6 @@ def run_ours(args):
     d_disc = empty(cap * W * 6, torch.float32)
     d_fs, d_fe = empty(N, torch.uint8), empty(cap, torch.uint8)
     maxHS = min(obs_host.shape[0], 5)
-    d_a, d_b = empty(cap * W * maxHS * 3, torch.float32), empty(cap * W * maxHS, torch.float32)
-    d_hn = empty(cap * W, torch.uint8)  # stored half-spaces per waypoint
     Pmc, T = 2048, 400
     d_tab = empty(T * Pmc * 3, torch.float32)
     lib.check(L.pump_particle_tables(pb.seed, Pmc, T, d_tab.data_ptr(), None, sh))
@@ -453,18 +451,16 @@ def run_ours(args):
         timed("free_edges", lambda: lib.check(L.pump_free_edges(
             d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), Eo.value, W - 1,
             d_fe.data_ptr(), sh)), 1)
-        timed("halfspaces", lambda: lib.check(L.pump_cache_halfspaces_sparse(
-            d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), d_fe.data_ptr(), Eo.value, W,
-            maxHS, maxd2, d_a.data_ptr(), d_b.data_ptr(), d_hn.data_ptr(), sh)), 1)
-
+        # half-spaces derived inside the HSMC kernel from the boxes (the planner's path)
         def hsmc_all():
             for it, m in enumerate(sizes):
                 o = int(offs[it])
-                lib.check(L.pump_hsmc_propagate(
+                lib.check(L.pump_hsmc_propagate_boxes(
                     m, W, d_edge.data_ptr() + 4 * o, d_prev.data_ptr() + 4 * o, E, base,
-                    d_a.data_ptr(), d_b.data_ptr(), maxHS, d_times.data_ptr(), d_te.data_ptr(), 0.05,
-                    d_tab.data_ptr(), Pmc, T, float(w["offset_mult"]), d_valid.data_ptr(), P,
-                    d_cp.data_ptr(), d_err.data_ptr(), d_hn.data_ptr(), sh))
+                    d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), maxd2, maxHS,
+                    d_times.data_ptr(), d_te.data_ptr(), 0.05, d_tab.data_ptr(), Pmc, T,
+                    float(w["offset_mult"]), d_valid.data_ptr(), P, d_cp.data_ptr(),
+                    d_err.data_ptr(), sh))
         timed("hsmc", hsmc_all, len(sizes))
 
     for _ in range(args.warmup):
@@ -584,8 +580,8 @@ def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops, sm_mhz):
         "rn_edges": 4.0 * N * (N - 1) + 20.0 * E,             # costs read, edge times, 4 arrays out
         "discretize": 16.0 * E + 24.0 * W * E,                # edge in, waypoints out
         "free_edges": 24.0 * W * E + E,                       # waypoints in, mask out
-        "halfspaces": 24.0 * W * E + E + 1.0 * W * E,         # waypoints in, counts out
-        "hsmc": M * (8 + 4 + 2 * 4 * ((P + 31) // 32) + 4.0 * W * H),
+        # per new path: edge and parent ids, time, parent mask in, mask out, the edge's waypoints
+        "hsmc": M * (8 + 4 + 2 * 4 * ((P + 31) // 32) + 24.0 * W),
     }
     table = {}
     for k, b in algo.items():

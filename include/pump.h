@@ -177,6 +177,22 @@ pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_edge, const i
                                   float offset_mult, uint32_t *d_valid, int P, float *d_path_cp,
                                   int *d_error, const uint8_t *d_hs_count, pump_stream_t stream);
 
+/* pump_hsmc_propagate with the half-spaces derived inside the kernel from
+ * the boxes and the edge's waypoints (disc[edge][W][6]) instead of read from
+ * a cache: the same half-spaces pump_cache_halfspaces would store for the
+ * edge (first maxHS boxes in index order within the distance gate maxd2 of
+ * each waypoint, the reference's arithmetic), so masks and CPs are identical.
+ * Every edge named is treated as free (the search only propagates along
+ * free edges).  W <= 256 and W * maxHS <= 256; the boxes are staged in
+ * shared memory (PUMP_ERR_CAPACITY beyond about 3,800 boxes). */
+pump_status_t pump_hsmc_propagate_boxes(int num_new, int W, const int *d_edge, const int *d_prev,
+                                        long long num_edges, int base, const float *d_obstacles,
+                                        int numObs, const float *d_disc, float maxd2, int maxHS,
+                                        const float *d_times, const float *d_topt, float dt,
+                                        const float *d_offsets_t, int Pmc, int T_rows,
+                                        float offset_mult, uint32_t *d_valid, int P,
+                                        float *d_path_cp, int *d_error, pump_stream_t stream);
+
 /* Full Monte Carlo collision probability of n_paths dense paths at once
  * (MCCP + thrust::reduce, collisionProbability.cu:4-92).  Path k has
  * d_len[k] states starting at d_paths + d_offset[k]*6.  The particle

@@ -152,37 +152,11 @@ __global__ void __launch_bounds__(256) halfspace_kernel(const float *__restrict_
       vel[d] = __ldg(&disc[wp * kDim + 3 + d]);
     }
     for (int o = 0; o < numObs && stored < maxHS; ++o) {
-      const float *l = &s_obs[o * 12], *u = l + 6;
-      float x[3];
+      float a[3], b;
+      if (!halfspace_of_box(pos, vel, &s_obs[o * 12], maxd2, a, &b)) continue;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {  // bvlsShortcut, bvls.cu:259-273
-        if (pos[d] <= l[d]) x[d] = l[d];
-        else if (pos[d] >= u[d]) x[d] = u[d];
-        else x[d] = pos[d];
-      }
-#pragma unroll
-      for (int d = 0; d < 3; ++d) x[d] = x[d] - pos[d];
-      float d2 = 0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) d2 += x[d] * x[d];
-      if (d2 > maxd2) continue;
-      float xdotv = 0, vdotv = 0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        xdotv += x[d] * vel[d];
-        vdotv += vel[d] * vel[d];
-      }
-      if (vdotv == 0) vdotv = (float)1e-5;
-      const float dotratio = xdotv / vdotv;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) x[d] = x[d] - dotratio * vel[d];
-      float xdotx = 0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        as[hsIdx * 3 + d] = x[d];
-        xdotx += x[d] * x[d];
-      }
-      bs[hsIdx] = xdotx;
+      for (int d = 0; d < 3; ++d) as[hsIdx * 3 + d] = a[d];
+      bs[hsIdx] = b;
       ++stored;
       ++hsIdx;
     }
@@ -269,15 +243,7 @@ __global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
     for (int q = t; q < ne * numObs; q += kHsThreads) {
       const int el = q / numObs, o = q - el * numObs;
       if (!s_filter[el]) continue;
-      const float *l = &s_obs[o * 12], *u = l + 6;
-      bool keep = true;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const float above = l[d] - s_eb[el][3 + d];  // box beyond the edge's max
-        const float below = u[d] - s_eb[el][d];      // box below the edge's min
-        if (above > 0.0f && above * above > maxd2) keep = false;
-        if (below < 0.0f && below * below > maxd2) keep = false;
-      }
+      const bool keep = gate_keeps_box(s_eb[el], s_eb[el] + 3, &s_obs[o * 12], maxd2);
       if (keep) atomicOr(&s_mask[el][o >> 5], 1u << (o & 31));
     }
   }
@@ -310,37 +276,11 @@ __global__ void __launch_bounds__(kHsThreads) halfspace_staged_kernel(
         } else {
           if (++o >= numObs) break;
         }
-        const float *l = &s_obs[o * 12], *u = l + 6;
-        float x[3];
+        float ah[3], bh;
+        if (!halfspace_of_box(pos, vel, &s_obs[o * 12], maxd2, ah, &bh)) continue;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {  // bvlsShortcut, bvls.cu:259-273
-          if (pos[d] <= l[d]) x[d] = l[d];
-          else if (pos[d] >= u[d]) x[d] = u[d];
-          else x[d] = pos[d];
-        }
-#pragma unroll
-        for (int d = 0; d < 3; ++d) x[d] = x[d] - pos[d];
-        float d2 = 0;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) d2 += x[d] * x[d];
-        if (d2 > maxd2) continue;
-        float xdotv = 0, vdotv = 0;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          xdotv += x[d] * vel[d];
-          vdotv += vel[d] * vel[d];
-        }
-        if (vdotv == 0) vdotv = (float)1e-5;
-        const float dotratio = xdotv / vdotv;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) x[d] = x[d] - dotratio * vel[d];
-        float xdotx = 0;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          a[stored * 3 + d] = x[d];
-          xdotx += x[d] * x[d];
-        }
-        b[stored] = xdotx;
+        for (int d = 0; d < 3; ++d) a[stored * 3 + d] = ah[d];
+        b[stored] = bh;
         ++stored;
       }
     }

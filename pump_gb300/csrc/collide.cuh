@@ -94,4 +94,65 @@ __device__ __forceinline__ bool segment_valid_masked(const float *v, const float
   return true;
 }
 
+// The half-space box o contributes at a waypoint (pos, vel): cacheHalfspaces,
+// hsmc.cu:10-99, with bvlsShortcut (bvls.cu:259-273) for the closest point.
+// False when the point is farther than the distance gate (d2 > maxd2);
+// otherwise a[3] and b = a.a.  Every operation in the reference's order
+// (binary32; the callers' translation units do not contract).
+__device__ __forceinline__ bool halfspace_of_box(const float *pos, const float *vel,
+                                                 const float *box, float maxd2, float *a,
+                                                 float *b) {
+  const float *l = box, *u = box + 6;
+  float x[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (pos[d] <= l[d]) x[d] = l[d];
+    else if (pos[d] >= u[d]) x[d] = u[d];
+    else x[d] = pos[d];
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) x[d] = x[d] - pos[d];
+  float d2 = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) d2 += x[d] * x[d];
+  if (d2 > maxd2) return false;
+  float xdotv = 0, vdotv = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    xdotv += x[d] * vel[d];
+    vdotv += vel[d] * vel[d];
+  }
+  if (vdotv == 0) vdotv = (float)1e-5;
+  const float dotratio = xdotv / vdotv;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) x[d] = x[d] - dotratio * vel[d];
+  float xdotx = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    a[d] = x[d];
+    xdotx += x[d] * x[d];
+  }
+  *b = xdotx;
+  return true;
+}
+
+// Whether box can pass the distance gate at some waypoint of an edge whose
+// waypoints lie in [emin, emax]: if for some axis the gap g between that
+// bounding box and the box has fl(g * g) > maxd2, every waypoint's d2 (a
+// rounded sum of non-negative squares, each at least as large by the
+// monotonicity of rounding) exceeds maxd2 as well.
+__device__ __forceinline__ bool gate_keeps_box(const float *emin, const float *emax,
+                                               const float *box, float maxd2) {
+  const float *l = box, *u = box + 6;
+  bool keep = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float above = l[d] - emax[d];  // box beyond the edge's max
+    const float below = u[d] - emin[d];  // box below the edge's min
+    if (above > 0.0f && above * above > maxd2) keep = false;
+    if (below < 0.0f && below * below > maxd2) keep = false;
+  }
+  return keep;
+}
+
 }  // namespace pump

@@ -183,39 +183,188 @@ __global__ void position_variance_kernel(int T, double *__restrict__ var) {
 // One warp per new path.  Lane l owns particles p = 32k + l (k < words), one
 // bit per particle in bits[k/32] bit (k%32), so offset loads of a k-step are
 // 32 consecutive particles (384 contiguous bytes) and word k of the packed
-// mask is a single __ballot_sync.  The warp first loads the edge's W x H
-// half-space b values (the reference skips a half-space when b >= 1000,
-// PUMP.cu:642) and ballots which are active; with none active the new mask
-// is the parent's and only the hit count is computed.  Every active
-// half-space is tested for every particle exactly as PUMP.cu:645-651 does
-// (binary32, no contraction); AND-ing the tests in another order gives the
-// same bits.
+// mask is a single __ballot_sync.  The warp first finds the edge's W x H
+// half-space slots that are active (the reference skips a half-space when
+// b >= 1000, PUMP.cu:642); with none active the new mask is the parent's and
+// only the hit count is computed.  Every active half-space is tested for
+// every particle exactly as PUMP.cu:645-651 does (binary32, no
+// contraction); AND-ing the tests in another order gives the same bits.
+//
+// Two sources of half-spaces.  Cached: the arrays of pump_cache_halfspaces
+// (dense, or sparse with per-waypoint counts).  Boxes: the warp derives
+// them itself from the edge's waypoints and the obstacle set staged in
+// shared memory, with the same operations (halfspace_of_box), into its own
+// shared-memory slots.  It first drops the boxes that no waypoint of the
+// edge can bring within the distance gate (gate_keeps_box on the waypoints'
+// bounding box; none dropped when a waypoint is NaN or there are more than
+// kHsmcFilterObs boxes), then per waypoint takes the remaining boxes 32 at a
+// time, one per lane: the lanes whose box passes the gate are ranked by a
+// ballot and the first maxHS - stored of them, in index order, fill the next
+// slots, which are the slots cacheHalfspaces fills.  Only the edges a
+// wavefront propagates along get half-spaces, and no cache is written.
 constexpr int kMaxHsmcWords = 128;   // P <= 4096 particles
 constexpr int kMaxHsSlots = 256;     // W * maxHS <= 256
+constexpr int kHsmcThreads = 256;
+constexpr int kHsmcWarps = kHsmcThreads / 32;
+constexpr int kHsmcFilterObs = 128;
 
-__global__ void __launch_bounds__(256) hsmc_kernel(
-    int num_new, int W, const int *__restrict__ wf_edge, const int *__restrict__ wf_prev,
-    long long num_edges, int num_prev, const float *__restrict__ as, const float *__restrict__ bs,
-    int maxHS, const float *__restrict__ times, const float *__restrict__ topts, float dt,
-    const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
-    const uint32_t *valid_in, uint32_t *valid_out, int P, float *__restrict__ cp_out,
-    int *__restrict__ error, const uint8_t *__restrict__ hs_count) {
+struct HsmcParams {
+  int num_new, W;
+  const int *wf_edge, *wf_prev;
+  long long num_edges;
+  int num_prev;
+  // cached half-spaces
+  const float *as, *bs;
+  const uint8_t *hs_count;
+  // half-spaces from the boxes
+  const float *obs, *disc;
+  int numObs;
+  float maxd2;
+  int maxHS;
+  const float *times, *topts;
+  float dt;
+  const float *offsets_t;
+  int Pmc, T_rows;
+  float offset_mult;
+  const uint32_t *valid_in;
+  uint32_t *valid_out;
+  int P;
+  float *cp_out;
+  int *error;
+};
+
+// Shared memory of the boxes variant: the staged boxes, then per warp its
+// half-space slots (a0, a1, a2, b), stored counts per waypoint and the list
+// of boxes that survive the edge's gate bound.
+__host__ __device__ inline size_t hsmc_boxes_obs_floats(int numObs) {
+  return (size_t)((numObs * 12 + 3) & ~3);
+}
+__host__ __device__ inline size_t hsmc_boxes_smem(int numObs) {
+  return sizeof(float) * hsmc_boxes_obs_floats(numObs) +
+         (size_t)kHsmcWarps * (sizeof(float4) * kMaxHsSlots + kMaxHsSlots + sizeof(int) * kHsmcFilterObs);
+}
+
+template <bool Boxes>
+__global__ void __launch_bounds__(kHsmcThreads) hsmc_kernel(const HsmcParams p) {
   // valid_in[prev] is read, valid_out[w] / cp_out[w] written (the two may
   // alias one path store with valid_out = store + base, as in the reference).
   // With hs_count (stored half-spaces per waypoint), slots at or past a
   // waypoint's count are inactive without reading them (they hold the
   // defaults b = 1111 in the dense layout); stored slots still need b < 1000.
-  const int lane = threadIdx.x & 31;
+  extern __shared__ float4 s_dyn4[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned int lt = (1u << lane) - 1u;
+  float *s_obs = reinterpret_cast<float *>(s_dyn4);
+  float4 *hs = nullptr;
+  uint8_t *hcnt = nullptr;
+  int *klist = nullptr;
+  if (Boxes) {
+    stage_obstacles(p.obs, p.numObs, s_obs);  // block-wide, before any warp leaves
+    float4 *s_hs = reinterpret_cast<float4 *>(s_obs + hsmc_boxes_obs_floats(p.numObs));
+    hs = s_hs + warp * kMaxHsSlots;
+    uint8_t *s_cnt = reinterpret_cast<uint8_t *>(s_hs + kHsmcWarps * kMaxHsSlots);
+    hcnt = s_cnt + warp * kMaxHsSlots;
+    int *s_klist = reinterpret_cast<int *>(s_cnt + kHsmcWarps * kMaxHsSlots);
+    klist = s_klist + warp * kHsmcFilterObs;
+  }
   const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-  if (w >= num_new) return;  // warp-uniform
-  const int edge = wf_edge[w], prev = wf_prev[w];
-  if (edge < 0 || edge >= num_edges || prev < 0 || prev >= num_prev) {
-    if (lane == 0 && error) atomicExch(error, (int)PUMP_ERR_BAD_INPUT);
+  if (w >= p.num_new) return;  // warp-uniform
+  const int edge = p.wf_edge[w], prev = p.wf_prev[w];
+  if (edge < 0 || edge >= p.num_edges || prev < 0 || prev >= p.num_prev) {
+    if (lane == 0 && p.error) atomicExch(p.error, (int)PUMP_ERR_BAD_INPUT);
     return;
   }
+  const int W = p.W, maxHS = p.maxHS, P = p.P;
   const int words = (P + 31) >> 5;
   const int slots = W * maxHS;
   const long long hsHead = (long long)edge * slots;
+  // parent's words: lane j holds words j, j+32, ... (issued first: their
+  // latency overlaps the half-space work)
+  uint32_t mine[kMaxHsmcWords / 32];
+#pragma unroll
+  for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+    const int j = q * 32 + lane;
+    mine[q] = (j < words) ? p.valid_in[(long long)prev * words + j] : 0u;
+  }
+  if (Boxes) {
+    // lane i holds waypoint i (W <= 32; otherwise waypoints are read per step)
+    const float *ew = p.disc + (long long)edge * W * kDim;
+    float my[kDim];
+    const int mi = lane < W ? lane : 0;
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) my[d] = __ldg(&ew[mi * kDim + d]);
+    // the edge's waypoints bound the boxes worth testing
+    float mn[3], mx[3];
+    bool nan = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      mn[d] = mx[d] = my[d];
+      nan = nan || my[d] != my[d];
+    }
+    for (int i = lane + 32; i < W; i += 32)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float x = __ldg(&ew[i * kDim + d]);
+        nan = nan || x != x;
+        mn[d] = fminf(mn[d], x);
+        mx[d] = fmaxf(mx[d], x);
+      }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+        mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+      }
+    nan = __any_sync(0xffffffffu, nan);
+    const bool filt = !nan && p.numObs <= kHsmcFilterObs;
+    int nk = p.numObs;
+    if (filt) {
+      nk = 0;
+      for (int o0 = 0; o0 < p.numObs; o0 += 32) {
+        const int o = o0 + lane;
+        const bool keep = o < p.numObs && gate_keeps_box(mn, mx, &s_obs[o * 12], p.maxd2);
+        const unsigned int bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) klist[nk + __popc(bal & lt)] = o;
+        nk += __popc(bal);
+      }
+    }
+    for (int i = lane; i < W; i += 32) hcnt[i] = 0;
+    __syncwarp();
+    for (int i = 0; i < W && nk > 0; ++i) {
+      float pos[3], vel[3];
+      if (i < 32) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          pos[d] = __shfl_sync(0xffffffffu, my[d], i);
+          vel[d] = __shfl_sync(0xffffffffu, my[3 + d], i);
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          pos[d] = __ldg(&ew[i * kDim + d]);
+          vel[d] = __ldg(&ew[i * kDim + 3 + d]);
+        }
+      }
+      int stored = 0;
+      for (int c0 = 0; c0 < nk && stored < maxHS; c0 += 32) {
+        const int c = c0 + lane;
+        float ah[3] = {0.0f, 0.0f, 0.0f}, bh = 0.0f;
+        bool pass = false;
+        if (c < nk) {
+          const int o = filt ? klist[c] : c;
+          pass = halfspace_of_box(pos, vel, &s_obs[o * 12], p.maxd2, ah, &bh);
+        }
+        const unsigned int bal = __ballot_sync(0xffffffffu, pass);
+        const int rank = __popc(bal & lt);
+        if (pass && stored + rank < maxHS) hs[i * maxHS + stored + rank] = make_float4(ah[0], ah[1], ah[2], bh);
+        const int got = __popc(bal);
+        stored += got < maxHS - stored ? got : maxHS - stored;
+      }
+      if (lane == 0) hcnt[i] = (uint8_t)stored;
+    }
+    __syncwarp();
+  }
   // which half-space slots are active (b < 1000 or NaN, as !(b >= 1000))
   uint32_t act[kMaxHsSlots / 32];
   int nact = 0;
@@ -224,19 +373,16 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
     const int sidx = c * 32 + lane;
     bool a = false;
     if (c * 32 < slots && sidx < slots) {
-      const bool stored =
-          !hs_count || sidx - (sidx / maxHS) * maxHS < (int)__ldg(&hs_count[(long long)edge * W + sidx / maxHS]);
-      a = stored && !(__ldg(&bs[hsHead + sidx]) >= 1000);
+      const int i = sidx / maxHS, s = sidx - i * maxHS;
+      if (Boxes) {
+        a = s < (int)hcnt[i] && !(hs[sidx].w >= 1000);
+      } else {
+        const bool stored = !p.hs_count || s < (int)__ldg(&p.hs_count[(long long)edge * W + i]);
+        a = stored && !(__ldg(&p.bs[hsHead + sidx]) >= 1000);
+      }
     }
     act[c] = (c * 32 < slots) ? __ballot_sync(0xffffffffu, a) : 0u;
     nact += __popc(act[c]);
-  }
-  // parent's words: lane j holds words j, j+32, ...
-  uint32_t mine[kMaxHsmcWords / 32];
-#pragma unroll
-  for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
-    const int j = q * 32 + lane;
-    mine[q] = (j < words) ? valid_in[(long long)prev * words + j] : 0u;
   }
   int overflow = 0;
   if (nact > 0) {
@@ -252,8 +398,8 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
         bits[q] |= ((wk >> lane) & 1u) << b;
       }
     }
-    const float dtLocal = topts[edge] / (W - 1);
-    const float t0 = times[prev];
+    const float dtLocal = p.topts[edge] / (W - 1);
+    const float t0 = p.times[prev];
 #pragma unroll
     for (int c = 0; c < kMaxHsSlots / 32; ++c) {
       uint32_t m = act[c];
@@ -262,16 +408,25 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
         m &= m - 1;
         const int i = sidx / maxHS;
         const float time = t0 + i * dtLocal;
-        int dtIdx = (int)(time / dt);
-        if (dtIdx < 0 || dtIdx >= T_rows) {
+        int dtIdx = (int)(time / p.dt);
+        if (dtIdx < 0 || dtIdx >= p.T_rows) {
           overflow = 1;
-          dtIdx = dtIdx < 0 ? 0 : T_rows - 1;
+          dtIdx = dtIdx < 0 ? 0 : p.T_rows - 1;
         }
-        const float b = __ldg(&bs[hsHead + sidx]);
-        const float a0 = __ldg(&as[(hsHead + sidx) * 3 + 0]);
-        const float a1 = __ldg(&as[(hsHead + sidx) * 3 + 1]);
-        const float a2 = __ldg(&as[(hsHead + sidx) * 3 + 2]);
-        const float *row = offsets_t + (long long)dtIdx * Pmc * 3;
+        float a0, a1, a2, b;
+        if (Boxes) {
+          const float4 h = hs[sidx];
+          a0 = h.x;
+          a1 = h.y;
+          a2 = h.z;
+          b = h.w;
+        } else {
+          b = __ldg(&p.bs[hsHead + sidx]);
+          a0 = __ldg(&p.as[(hsHead + sidx) * 3 + 0]);
+          a1 = __ldg(&p.as[(hsHead + sidx) * 3 + 1]);
+          a2 = __ldg(&p.as[(hsHead + sidx) * 3 + 2]);
+        }
+        const float *row = p.offsets_t + (long long)dtIdx * p.Pmc * 3;
 #pragma unroll
         for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
           if (q * 32 >= words) break;
@@ -282,14 +437,14 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
 #pragma unroll 8
           for (int bb = 0; bb < 32; ++bb) {
             const int k = q * 32 + bb;
-            const int p = 32 * k + lane;
-            if (k < words && p < P) {
-              const float *off = row + (long long)p * 3;
+            const int pp = 32 * k + lane;
+            if (k < words && pp < P) {
+              const float *off = row + (long long)pp * 3;
               float LHS = 0;
               LHS += __ldg(&off[0]) * a0;
               LHS += __ldg(&off[1]) * a1;
               LHS += __ldg(&off[2]) * a2;
-              if (!(LHS * offset_mult < b)) bq &= ~(1u << bb);
+              if (!(LHS * p.offset_mult < b)) bq &= ~(1u << bb);
             }
           }
           bits[q] = bq;
@@ -317,15 +472,15 @@ __global__ void __launch_bounds__(256) hsmc_kernel(
     const int j = q * 32 + lane;
     if (j < words) {
       if (j == words - 1) mine[q] &= tail;  // no bits past particle P-1
-      valid_out[(long long)w * words + j] = mine[q];
+      p.valid_out[(long long)w * words + j] = mine[q];
       valid_count += __popc(mine[q]);
     }
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) valid_count += __shfl_down_sync(0xffffffffu, valid_count, off);
   if (lane == 0) {
-    cp_out[w] = ((float)(P - valid_count)) / P;
-    if (overflow && error) atomicExch(error, (int)PUMP_ERR_CAPACITY);
+    p.cp_out[w] = ((float)(P - valid_count)) / P;
+    if (overflow && p.error) atomicExch(p.error, (int)PUMP_ERR_CAPACITY);
   }
 }
 
@@ -505,12 +660,81 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
   if (W * maxHS > kMaxHsSlots)
     return set_error(PUMP_ERR_CAPACITY, "hsmc: %d half-space slots per edge exceed %d", W * maxHS,
                      kMaxHsSlots);
-  hsmc_kernel<<<grid_for((long long)num_new * 32, 256), 256, 0, stream>>>(
-      num_new, W, d_edge, d_prev, num_edges, num_prev, d_as, d_bs, maxHS, d_times, d_topt,
-                                               dt, d_offsets_t, Pmc, T_rows, offset_mult,
-                                               d_valid_in, d_valid_out, P, d_cp_out, d_error,
-                                               d_hs_count);
+  HsmcParams hp{};
+  hp.num_new = num_new;
+  hp.W = W;
+  hp.wf_edge = d_edge;
+  hp.wf_prev = d_prev;
+  hp.num_edges = num_edges;
+  hp.num_prev = num_prev;
+  hp.as = d_as;
+  hp.bs = d_bs;
+  hp.hs_count = d_hs_count;
+  hp.maxHS = maxHS;
+  hp.times = d_times;
+  hp.topts = d_topt;
+  hp.dt = dt;
+  hp.offsets_t = d_offsets_t;
+  hp.Pmc = Pmc;
+  hp.T_rows = T_rows;
+  hp.offset_mult = offset_mult;
+  hp.valid_in = d_valid_in;
+  hp.valid_out = d_valid_out;
+  hp.P = P;
+  hp.cp_out = d_cp_out;
+  hp.error = d_error;
+  hsmc_kernel<false><<<grid_for((long long)num_new * 32, kHsmcThreads), kHsmcThreads, 0, stream>>>(hp);
   return launch_status("hsmc_kernel");
+}
+
+bool hsmc_boxes_fits(int numObs, int W, int maxHS) {
+  return numObs >= 0 && W <= kMaxHsSlots && W * maxHS <= kMaxHsSlots &&
+         hsmc_boxes_smem(numObs) <= 220 * 1024;
+}
+
+pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int *d_prev,
+                               long long num_edges, int num_prev, const float *d_obs, int numObs,
+                               const float *d_disc, float maxd2, int maxHS, const float *d_times,
+                               const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
+                               int T_rows, float offset_mult, const uint32_t *d_valid_in,
+                               uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
+                               cudaStream_t stream) {
+  if (num_new <= 0) return PUMP_OK;
+  if ((P + 31) / 32 > kMaxHsmcWords)
+    return set_error(PUMP_ERR_CAPACITY, "hsmc: %d particles exceed %d", P, 32 * kMaxHsmcWords);
+  if (!hsmc_boxes_fits(numObs, W, maxHS))
+    return set_error(PUMP_ERR_CAPACITY, "hsmc: %d boxes or %d half-space slots per edge exceed the stage",
+                     numObs, W * maxHS);
+  HsmcParams hp{};
+  hp.num_new = num_new;
+  hp.W = W;
+  hp.wf_edge = d_edge;
+  hp.wf_prev = d_prev;
+  hp.num_edges = num_edges;
+  hp.num_prev = num_prev;
+  hp.obs = d_obs;
+  hp.numObs = numObs;
+  hp.disc = d_disc;
+  hp.maxd2 = maxd2;
+  hp.maxHS = maxHS;
+  hp.times = d_times;
+  hp.topts = d_topt;
+  hp.dt = dt;
+  hp.offsets_t = d_offsets_t;
+  hp.Pmc = Pmc;
+  hp.T_rows = T_rows;
+  hp.offset_mult = offset_mult;
+  hp.valid_in = d_valid_in;
+  hp.valid_out = d_valid_out;
+  hp.P = P;
+  hp.cp_out = d_cp_out;
+  hp.error = d_error;
+  const size_t smem = hsmc_boxes_smem(numObs);
+  if (smem > 48 * 1024)
+    PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)hsmc_kernel<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  hsmc_kernel<true><<<grid_for((long long)num_new * 32, kHsmcThreads), kHsmcThreads, smem, stream>>>(hp);
+  return launch_status("hsmc_kernel (boxes)");
 }
 
 pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n, int words,
@@ -575,6 +799,24 @@ extern "C" pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_ed
                            d_offsets_t, Pmc, T_rows, offset_mult, d_valid,
                            d_valid + (size_t)base * words, P, d_path_cp + base, d_error,
                            d_hs_count, (cudaStream_t)stream);
+}
+
+extern "C" pump_status_t pump_hsmc_propagate_boxes(
+    int num_new, int W, const int *d_edge, const int *d_prev, long long num_edges, int base,
+    const float *d_obstacles, int numObs, const float *d_disc, float maxd2, int maxHS,
+    const float *d_times, const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
+    int T_rows, float offset_mult, uint32_t *d_valid, int P, float *d_path_cp, int *d_error,
+    pump_stream_t stream) {
+  if (num_new < 0 || W < 2 || maxHS < 0 || P <= 0 || P > Pmc || T_rows <= 0 || base < 0 ||
+      num_edges < 0 || numObs < 0 || (numObs > 0 && !d_obstacles) ||
+      (num_new > 0 && (!d_edge || !d_prev || !d_times || !d_topt || !d_offsets_t || !d_valid ||
+                       !d_path_cp || !d_disc)))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_hsmc_propagate_boxes: bad arguments");
+  const size_t words = (size_t)((P + 31) / 32);
+  return hsmc_boxes_async(num_new, W, d_edge, d_prev, num_edges, base, d_obstacles, numObs, d_disc,
+                          maxd2, maxHS, d_times, d_topt, dt, d_offsets_t, Pmc, T_rows, offset_mult,
+                          d_valid, d_valid + (size_t)base * words, P, d_path_cp + base, d_error,
+                          (cudaStream_t)stream);
 }
 
 extern "C" pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d_len,

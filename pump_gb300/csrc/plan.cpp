@@ -42,6 +42,14 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
                                 const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
                                 float *d_cp_out, int *d_error, const uint8_t *d_hs_count,
                                 cudaStream_t stream);
+bool hsmc_boxes_fits(int numObs, int W, int maxHS);
+pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int *d_prev,
+                               long long num_edges, int num_prev, const float *d_obs, int numObs,
+                               const float *d_disc, float maxd2, int maxHS, const float *d_times,
+                               const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
+                               int T_rows, float offset_mult, const uint32_t *d_valid_in,
+                               uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
+                               cudaStream_t stream);
 pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n, int words,
                                  uint32_t *d_dst, cudaStream_t stream);
 pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
@@ -186,6 +194,8 @@ class Planner {
   const int numBuckets_ = 2;
   const float epsCost_ = (float)0.0002, epsCP_ = (float)0.0002;
   int N_ = 0, W_ = 0, P_ = 0, words_ = 0, maxHS_ = 0, nobs_ = 0;
+  float maxd2_ = 0;
+  bool hs_boxes_ = false;  // HSMC derives the half-spaces from the boxes
 
   std::vector<float> samples_;
   DevBuf<float> d_samples_, d_obs_, d_copts_, d_topts_;
@@ -350,13 +360,20 @@ pump_status_t Planner::online() {
   PUMP_TRY(pump_free_edges(d_obs_.p, nobs_, d_disc_.p, E_, pb_.num_disc, d_free_e_.p,
                            (pump_stream_t)s_));
   // maxd2 = 0.1*offsetMult*offsetMult evaluated in double (mainPUMP.cu:201)
-  const float maxd2 = (float)(0.1 * (double)pb_.offset_mult * (double)pb_.offset_mult);
-  PUMP_TRY(d_as_.alloc((size_t)E_ * W_ * maxHS_ * 3));
-  PUMP_TRY(d_bs_.alloc((size_t)E_ * W_ * maxHS_));
-  // only the stored half-spaces and their counts (the search reads no more)
-  PUMP_TRY(d_hcount_.alloc((size_t)E_ * W_));
-  PUMP_TRY(pump_cache_halfspaces_sparse(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_,
-                                        maxd2, d_as_.p, d_bs_.p, d_hcount_.p, (pump_stream_t)s_));
+  maxd2_ = (float)(0.1 * (double)pb_.offset_mult * (double)pb_.offset_mult);
+  // The half-spaces of cacheHalfspaces (mainPUMP.cu:366-374): derived by the
+  // HSMC kernel for the edges each wavefront propagates along when the boxes
+  // fit its shared-memory stage, else cached for every free edge up front
+  // (only the stored ones and their counts: the search reads no more).
+  hs_boxes_ = hsmc_boxes_fits(nobs_, W_, maxHS_);
+  if (!hs_boxes_) {
+    PUMP_TRY(d_as_.alloc((size_t)E_ * W_ * maxHS_ * 3));
+    PUMP_TRY(d_bs_.alloc((size_t)E_ * W_ * maxHS_));
+    PUMP_TRY(d_hcount_.alloc((size_t)E_ * W_));
+    PUMP_TRY(pump_cache_halfspaces_sparse(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_,
+                                          maxd2_, d_as_.p, d_bs_.p, d_hcount_.p,
+                                          (pump_stream_t)s_));
+  }
   PUMP_TRY(ctx_->particle_table(pb_.seed, pb_.num_mc, pb_.table_rows, &d_table_, s_));
   d_rowmax_ = d_table_ + 3 * (size_t)pb_.num_mc * pb_.table_rows;
   const size_t cap = E_ > 0 ? (size_t)E_ : 1;
@@ -516,10 +533,16 @@ pump_status_t Planner::explore() {
       }
     }
     // HSMC of the wavefront (PUMP.cu:82-160)
-    PUMP_TRY(hsmc_staged_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p, d_bs_.p, maxHS_,
-                               d_pathTime_.p, d_toptE_.p, dt_, d_table_, pb_.num_mc,
-                               pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p, P_,
-                               d_cpStage_.p, d_err_.p, d_hcount_.p, s_));
+    if (hs_boxes_)
+      PUMP_TRY(hsmc_boxes_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
+                                d_disc_.p, maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
+                                pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p,
+                                d_stage_.p, P_, d_cpStage_.p, d_err_.p, s_));
+    else
+      PUMP_TRY(hsmc_staged_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p,
+                                 d_bs_.p, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
+                                 pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p,
+                                 d_stage_.p, P_, d_cpStage_.p, d_err_.p, d_hcount_.p, s_));
     // cut-off, dominance, storing, buckets (PUMP.cu:164-256)
     PUMP_TRY(search_prune(sd, numNew, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
     PUMP_TRY(search_store(ctx_, sd, numNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln,

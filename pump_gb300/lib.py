@@ -98,6 +98,8 @@ _SIGS = {
     "pump_particle_tables": (i32, [C.c_uint64, i32, i32, vp, vp, vp]),
     "pump_hsmc_propagate": (i32, [i32, i32, vp, vp, i64, i32, vp, vp, i32, vp, vp, f32, vp, i32,
                                   i32, f32, vp, i32, vp, vp, vp, vp]),
+    "pump_hsmc_propagate_boxes": (i32, [i32, i32, vp, vp, i64, i32, vp, i32, vp, f32, i32, vp, vp,
+                                        f32, vp, i32, i32, f32, vp, i32, vp, vp, vp]),
     "pump_mc_cp": (i32, [vp, vp, vp, i32, vp, i32, i32, f32, vp, i32, vp, vp, vp, vp]),
     "pump_frontier_compact": (i32, [vp, vp, i32, vp, vp, vp]),
     "pump_frontier_compact_noalloc": (i32, [vp, i32, vp, vp, vp]),

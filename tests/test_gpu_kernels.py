@@ -468,6 +468,20 @@ def test_sparse_halfspaces_and_hsmc(om, gpu, pumplib, oracle, roadmap1000):
     assert np.array_equal(got[base:], valid_bytes[base:])
     assert same_bits(host(d_cp)[base:base + n_new], cp_o[base:])
     assert int(host(d_err)[0]) == 0
+    # half-spaces derived in the kernel from the boxes and waypoints: same bits
+    d_valid2, d_cp2 = dev(torch, packed), empty(torch, base + n_new, torch.float32)
+    d_err2 = dev(torch, np.zeros(1, np.int32))
+    pumplib.check(L.pump_hsmc_propagate_boxes(
+        n_new, W, ptr(d_edges), ptr(d_prev), E, base, ptr(d_obs), obs.shape[0], ptr(d_disc),
+        float(maxd2), maxHS, ptr(d_times), ptr(d_te), 0.05, ptr(d_tm), Pmc, T, float(om),
+        ptr(d_valid2), P, ptr(d_cp2), ptr(d_err2), stream(torch)))
+    torch.cuda.synchronize()
+    got2 = bits_to_bytes(host(d_valid2).reshape(base + n_new, P // 32), P)
+    assert np.array_equal(got2[base:], valid_bytes[base:])
+    assert same_bits(host(d_cp2)[base:base + n_new], cp_o[base:])
+    assert int(host(d_err2)[0]) == 0
+    if om >= 0.05:  # half-spaces are active: some particles die on the new edges
+        assert np.any(valid_bytes[base:] != valid_bytes[prev])
 
 
 def test_mc_cp(gpu, pumplib, oracle, goldens):
