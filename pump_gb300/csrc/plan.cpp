@@ -212,8 +212,6 @@ class Planner {
   // order: original edge id, destination, cost, time, and row starts per node
   DevBuf<int> d_fid_, d_fsrc_, d_fdst_, d_fgo_;
   DevBuf<float> d_fcopt_, d_ftopt_;
-  std::vector<int> fid_, fdst_, fgo_;
-  std::vector<float> fcopt_, ftopt_;
 
   // exploration state (mainPUMP.cu:623-681)
   int maxPathCount_ = 0;
@@ -387,16 +385,6 @@ pump_status_t Planner::online() {
   PUMP_TRY(open_edges_device(ctx_, d_free_e_.p, d_free_s_.p, d_src_.p, d_dst_.p, d_coptE_.p,
                              d_toptE_.p, E_, N_, d_fid_.p, d_fsrc_.p, d_fdst_.p, d_fcopt_.p,
                              d_ftopt_.p, d_fgo_.p, &F, s_));
-  fid_.resize(F);
-  fdst_.resize(F);
-  fcopt_.resize(F);
-  ftopt_.resize(F);
-  fgo_.resize(N_ + 1);
-  PUMP_TRY(d2h(fid_.data(), d_fid_.p, F));
-  PUMP_TRY(d2h(fdst_.data(), d_fdst_.p, F));
-  PUMP_TRY(d2h(fcopt_.data(), d_fcopt_.p, F));
-  PUMP_TRY(d2h(ftopt_.data(), d_ftopt_.p, F));
-  PUMP_TRY(d2h(fgo_.data(), d_fgo_.p, N_ + 1));
   return sync();
 }
 

@@ -321,6 +321,11 @@ def test_halfspaces_maps_and_gates(mapname, gpu, pumplib, oracle, roadmap1000):
     k = int(np.nonzero(fe)[0][len(np.nonzero(fe)[0]) // 2])
     disc.reshape(E, 9, 6)[k, 4, 1] = np.nan  # one free edge with a NaN waypoint
     d_obs, d_disc, d_fe = dev(torch, obs), dev(torch, disc), dev(torch, fe)
+    # the collision check on this map, NaN waypoint included
+    d_fe2 = empty(torch, E, torch.uint8)
+    pumplib.check(L.pump_free_edges(ptr(d_obs), obs.shape[0], ptr(d_disc), E, 8, ptr(d_fe2),
+                                    stream(torch)))
+    assert np.array_equal(host(d_fe2, E), oracle.free_edges(disc, obs))
     for om in (2e-3, 0.05, 0.3):
         maxHS = min(obs.shape[0], 5)
         maxd2 = np.float32(0.1 * om * om)
