@@ -31,6 +31,7 @@ struct TileScratch {
   unsigned long long *total;   // selected count (written by the last tile)
   int *error;                  // 1 = look-back wait gave up
   unsigned long long *offsets; // per-tile output offsets (three-kernel compaction)
+  unsigned long long *copy_to; // optional second destination of the total
 };
 
 // Exclusive prefix of this tile from its predecessors' status words, read by
@@ -155,7 +156,10 @@ __device__ __forceinline__ bool tile_offsets(TileShared &sh, const TileScratch &
       sh.timeout = to;
       if (to) atomicExch(ts.error, 1);
       const long long ntiles = (n + kTile - 1) / kTile;
-      if (!to && tile == ntiles - 1) *ts.total = ex_tile + agg;
+      if (!to && tile == ntiles - 1) {
+        *ts.total = ex_tile + agg;
+        if (ts.copy_to) *ts.copy_to = ex_tile + agg;
+      }
     }
   }
   __syncthreads();
@@ -459,7 +463,10 @@ __global__ void __launch_bounds__(kCompactThreads) scan_kernel(long long n, Coun
         atomicExch(ts.error, 1);
       }
       const long long ntiles = (n + kTile - 1) / kTile;
-      if (!to && tile == ntiles - 1) *ts.total = ex_tile + agg;
+      if (!to && tile == ntiles - 1) {
+        *ts.total = ex_tile + agg;
+        if (ts.copy_to) *ts.copy_to = ex_tile + agg;
+      }
     }
   }
   __syncthreads();
@@ -474,10 +481,12 @@ __global__ void __launch_bounds__(kCompactThreads) scan_kernel(long long n, Coun
 
 template <class Count>
 pump_status_t run_scan(Ctx *ctx, long long n, Count count, unsigned int *out,
-                       cudaStream_t stream, TileScratch *ts_out) {
+                       cudaStream_t stream, TileScratch *ts_out,
+                       unsigned long long *copy_to = nullptr) {
   TileScratch ts{};
   long long ntiles = 0;
   PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));
+  ts.copy_to = copy_to;
   if (n > 0) {
     scan_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(n, count, out, ts);
     PUMP_TRY(launch_status("scan_kernel"));

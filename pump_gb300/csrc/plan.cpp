@@ -220,7 +220,7 @@ class Planner {
   std::vector<std::vector<int>> atNode_;
   DevBuf<uint32_t> d_valid_, d_stage_;
   DevBuf<float> d_pathTime_, d_cpStage_;
-  DevBuf<int> d_wfPrev_, d_wfEdge_, d_map_, d_err_;
+  DevBuf<int> d_wfPrev_, d_wfEdge_, d_err_;
   int numPaths_ = 0;
   // reusable scratch of the batched BVP / dense-path / MC CP helpers
   DevBuf<float> d_bx0_, d_bx1_, d_bt_, d_bc_, d_xs_, d_ts_, d_tau_, d_mcp_;
@@ -402,12 +402,11 @@ pump_status_t Planner::explore() {
   PUMP_TRY(d_pathTime_.alloc(cap));
   PUMP_TRY(d_wfPrev_.alloc(cap));
   PUMP_TRY(d_wfEdge_.alloc(cap));
-  PUMP_TRY(d_map_.alloc(cap));
   PUMP_TRY(d_err_.alloc(1));
   DevBuf<int> d_prev, d_node, d_g0, d_g1, d_nhead, d_nnext, d_wnode, d_wopen, d_newhead, d_newnext;
   DevBuf<float> d_cost, d_cp, d_ncost, d_ntime, d_h;
   DevBuf<unsigned int> d_off;
-  DevBuf<uint8_t> d_alive, d_dom, d_bucket;
+  DevBuf<uint8_t> d_alive, d_dom;
   DevBuf<SearchCtl> d_ctl;
   PUMP_TRY(d_prev.alloc(cap));
   PUMP_TRY(d_node.alloc(cap));
@@ -426,7 +425,6 @@ pump_status_t Planner::explore() {
   PUMP_TRY(d_dom.alloc(cap));
   PUMP_TRY(d_newhead.alloc(N_));
   PUMP_TRY(d_newnext.alloc(cap));
-  PUMP_TRY(d_bucket.alloc(cap));
   PUMP_TRY(d_h.alloc(N_));
   PUMP_TRY(d_ctl.alloc(1));
   PUMP_TRY(h2d(d_h.p, h_.data(), (size_t)N_));
@@ -467,8 +465,6 @@ pump_status_t Planner::explore() {
   sd.dominated = d_dom.p;
   sd.new_head = d_newhead.p;
   sd.new_next = d_newnext.p;
-  sd.map_src = d_map_.p;
-  sd.bucket = d_bucket.p;
   sd.ctl = d_ctl.p;
   PUMP_TRY(search_init(sd, s_));
 
@@ -492,10 +488,12 @@ pump_status_t Planner::explore() {
     // expansion (PUMP.cu:47-66)
     const int nG = gCount[Gidx];
     const auto tw = clk::now();
-    PUMP_TRY(search_expand_scan(ctx_, sd, Gidx, nG, s_));
     unsigned long long nn = 0;
-    PUMP_TRY(d2h(&nn, &d_ctl.p->num_new, 1));
-    PUMP_TRY(sync());
+    if (nG > 0) {
+      PUMP_TRY(search_expand_scan(ctx_, sd, Gidx, nG, s_));
+      PUMP_TRY(d2h(&nn, &d_ctl.p->num_new, 1));
+      PUMP_TRY(sync());
+    }
     if (nn > (unsigned long long)M) {
       status = set_error(PUMP_ERR_CAPACITY, "wavefront exceeds maxPathCount %d", M);
       break;
@@ -538,6 +536,10 @@ pump_status_t Planner::explore() {
     PUMP_TRY(d2h(&ctl, d_ctl.p, 1));
     PUMP_TRY(sync());
     res_->ms_explore_wait += ms_since(tw);
+    if (ctl.wait_error) {
+      status = set_error(PUMP_ERR_TIMEOUT, "search store: look-back wait exceeded its bound");
+      break;
+    }
     numPaths_ += (int)ctl.num_valid;
     gCount[0] = ctl.g_count[0];
     gCount[1] = ctl.g_count[1];

@@ -31,6 +31,9 @@ __global__ void search_init_kernel(SearchDev sd) {
     sd.ctl->g_count[0] = 1;
     sd.ctl->g_count[1] = 0;
     sd.ctl->goal_found = 0;
+    sd.ctl->g_base[0] = 0;
+    sd.ctl->g_base[1] = 0;
+    sd.ctl->wait_error = 0;
   }
 }
 
@@ -46,12 +49,17 @@ struct ExpandCount {
   }
 };
 
-__global__ void copy_total_kernel(const unsigned long long *total, unsigned long long *dst) {
-  *dst = *total;
-}
-
-// One warp per bucket entry: its node's expandable edges in order.
-__global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g) {
+// One warp per bucket entry: its node's expandable edges in order.  The
+// wavefront's nodes get empty lists of new paths; thread 0 empties bucket
+// g_idx and records the bucket sizes the store pass appends after (the
+// expansion reads the bucket through n_g, not through its count).
+__global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g, int g_idx) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    SearchCtl *c = sd.ctl;
+    c->g_count[g_idx] = 0;
+    c->g_base[g_idx] = 0;
+    c->g_base[1 - g_idx] = c->g_count[1 - g_idx];
+  }
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
   for (long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32; k < n_g; k += warps) {
@@ -61,32 +69,28 @@ __global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g) {
     const unsigned int off = sd.wf_off[k];
     for (int q = lane; q < cnt; q += 32) {
       const int f = f0 + q;
+      const int dst = sd.fdst[f];
       sd.wf_prev[off + q] = prev;
-      sd.wf_node[off + q] = sd.fdst[f];
+      sd.wf_node[off + q] = dst;
       sd.wf_edge[off + q] = sd.fid[f];
       sd.wf_open[off + q] = f;
+      sd.new_head[dst] = -1;
     }
   }
 }
 
-__global__ void clear_bucket_kernel(SearchCtl *ctl, int g_idx) { ctl->g_count[g_idx] = 0; }
-
-// PUMP.cu:164-185: time and cost of the new paths, the CP cut-off, and a
-// reset of the per-node lists of new paths.
+// PUMP.cu:164-185: time and cost of the new paths and the CP cut-off; the
+// survivors of the cut-off are linked into their node's list of new paths
+// (emptied by the expansion kernel).
 __global__ void new_paths_kernel(SearchDev sd, int num_new, float cp_cutoff) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= num_new) return;
   const int prev = sd.wf_prev[i], f = sd.wf_open[i];
   sd.new_time[i] = sd.path_time[prev] + sd.ftopt[f];
   sd.new_cost[i] = sd.path_cost[prev] + sd.fcopt[f];
-  sd.alive[i] = sd.new_cp[i] > cp_cutoff ? 0 : 1;
-  sd.new_head[sd.wf_node[i]] = -1;
-}
-
-__global__ void link_new_kernel(SearchDev sd, int num_new) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= num_new || !sd.alive[i]) return;
-  sd.new_next[i] = atomicExch(&sd.new_head[sd.wf_node[i]], i);
+  const bool alive = !(sd.new_cp[i] > cp_cutoff);
+  sd.alive[i] = alive ? 1 : 0;
+  if (alive) sd.new_next[i] = atomicExch(&sd.new_head[sd.wf_node[i]], i);
 }
 
 // PUMP.cu:188-218: a new path (not at the goal) dies if a stored path at its
@@ -116,65 +120,112 @@ __global__ void dominance_kernel(SearchDev sd, int num_new, int num_paths, float
   sd.dominated[i] = dead;
 }
 
-// PUMP.cu:221-256: survivors (alive, not dominated, not at the initial
-// node) become stored paths num_paths + rank.
-struct StorePred {
-  SearchDev sd;
-  __device__ bool operator()(long long i) const {
-    return sd.alive[i] && !sd.dominated[i] && sd.wf_node[i] != 0;
+// PUMP.cu:221-282 in one pass.  A survivor (alive, not dominated, not at the
+// initial node) becomes stored path num_paths + r, r = its rank among the
+// survivors in wavefront order, and is appended to bucket b at
+// g_base[b] + r_b, r_b = its rank among the survivors of bucket b (the
+// reference appends survivors to the buckets in the order it stores them).
+// Both ranks come from one stable compaction: a tile's count is the pair
+// (survivors, survivors of bucket 1) packed into one word (31 bits each in
+// the look-back value, 16 bits each within a tile), so the look-back adds
+// both at once.  The last tile writes the survivor count and the bucket
+// sizes.  Each survivor also moves its particle mask from the stage.
+constexpr unsigned long long kLow31 = (1ull << 31) - 1ull;
+
+__global__ void __launch_bounds__(kCompactThreads) store_kernel(
+    SearchDev sd, int num_new, int num_paths, int g_idx, float cost_threshold, float dr,
+    float cp_min_soln, const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words,
+    TileScratch ts) {
+  __shared__ TileShared sh;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long n = num_new;
+  const long long tile = next_tile(ts);
+  const long long base = tile * kTile;
+  bool surv[kCompactRows];
+  uint8_t bkt[kCompactRows];
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    const long long i = base + r * kCompactThreads + threadIdx.x;
+    surv[r] = false;
+    bkt[r] = 0;
+    if (i < n && sd.alive[i] && !sd.dominated[i]) {
+      const int node = sd.wf_node[i];
+      if (node != 0) {
+        surv[r] = true;
+        float dcost = (sd.new_cost[i] + sd.h[node] - cost_threshold);
+        dcost = (0.0f < dcost) ? dcost : 0.0f;  // std::max((float)0, dCost)
+        bkt[r] = (uint8_t)((((int)(dcost / dr)) + g_idx + 1) % 2);
+      }
+    }
   }
-};
-struct StoreEmit {
-  SearchDev sd;
-  int num_paths, g_idx;
-  float cost_threshold, dr, cp_min_soln;
-  __device__ void operator()(long long i, long long rank) const {
+  unsigned int bs[kCompactRows], b1[kCompactRows];
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    bs[r] = __ballot_sync(0xffffffffu, surv[r]);
+    b1[r] = __ballot_sync(0xffffffffu, surv[r] && bkt[r] == 1);
+    if (lane == 0) sh.cnt[r][warp] = (unsigned int)__popc(bs[r]) | ((unsigned int)__popc(b1[r]) << 16);
+  }
+  // in-tile offsets of both counts (each at most kTile < 2^16), then the
+  // tile's pair in the look-back's packing
+  __syncthreads();
+  if (warp == 0) {
+    const unsigned int tt = scan_tile_counts(sh.cnt);
+    const unsigned long long agg =
+        (unsigned long long)(tt & 0xFFFFu) | ((unsigned long long)(tt >> 16) << 31);
+    bool to = false;
+    const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
+    if (lane == 0) {
+      sh.excl = ex_tile;
+      sh.timeout = to;
+      if (to) {
+        atomicExch(ts.error, 1);
+        atomicExch(&sd.ctl->wait_error, 1);
+      }
+      const long long ntiles = (n + kTile - 1) / kTile;
+      if (!to && tile == ntiles - 1) {
+        const unsigned long long tot = ex_tile + agg;
+        const int n_s = (int)(tot & kLow31), n_1 = (int)(tot >> 31);
+        *ts.total = (unsigned long long)n_s;
+        SearchCtl *c = sd.ctl;
+        c->num_valid = (unsigned long long)n_s;
+        c->g_count[0] = c->g_base[0] + (n_s - n_1);
+        c->g_count[1] = c->g_base[1] + n_1;
+      }
+    }
+  }
+  __syncthreads();
+  if (sh.timeout) return;
+  const long long ex_s = (long long)(sh.excl & kLow31), ex_1 = (long long)(sh.excl >> 31);
+  const int gb0 = sd.ctl->g_base[0], gb1 = sd.ctl->g_base[1];
+  const unsigned int lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < kCompactRows; ++r) {
+    if (!(bs[r] & (1u << lane))) continue;
+    const long long i = base + r * kCompactThreads + threadIdx.x;
+    const unsigned int in_tile = sh.cnt[r][warp];
+    const long long rank = ex_s + (in_tile & 0xFFFFu) + __popc(bs[r] & lt);
+    const long long rank1 = ex_1 + (in_tile >> 16) + __popc(b1[r] & lt);
     const int st = num_paths + (int)rank;
     const int node = sd.wf_node[i];
-    const float cost = sd.new_cost[i], cp = sd.new_cp[i];
+    const float cp = sd.new_cp[i];
     sd.path_prev[st] = sd.wf_prev[i];
     sd.path_node[st] = node;
-    sd.path_cost[st] = cost;
+    sd.path_cost[st] = sd.new_cost[i];
     sd.path_time[st] = sd.new_time[i];
     sd.path_cp[st] = cp;
-    sd.map_src[rank] = (int)i;
-    float dcost = (cost + sd.h[node] - cost_threshold);
-    dcost = (0.0f < dcost) ? dcost : 0.0f;  // std::max((float)0, dCost)
-    sd.bucket[rank] = (uint8_t)((((int)(dcost / dr)) + g_idx + 1) % 2);
+    if (bkt[r] == 1) sd.g_list[1][gb1 + (int)rank1] = st;
+    else sd.g_list[0][gb0 + (int)(rank - rank1)] = st;
     sd.node_next[st] = atomicExch(&sd.node_head[node], st);
     if (node == sd.goal && cp <= cp_min_soln) atomicOr(&sd.ctl->goal_found, 1);
-  }
-};
-
-struct BucketPred {
-  SearchDev sd;
-  int b;
-  __device__ bool operator()(long long k) const {
-    return (unsigned long long)k < sd.ctl->num_valid && sd.bucket[k] == b;
-  }
-};
-struct BucketEmit {
-  SearchDev sd;
-  int b, num_paths;
-  __device__ void operator()(long long k, long long pos) const {
-    sd.g_list[b][sd.ctl->g_count[b] + pos] = num_paths + (int)k;
-  }
-};
-
-__global__ void bucket_count_kernel(const unsigned long long *total, SearchCtl *ctl, int b) {
-  ctl->g_count[b] += (int)*total;
-}
-
-// Particle masks of the survivors: stage[map_src[k]] -> valid[k].
-__global__ void gather_survivors_kernel(const uint32_t *__restrict__ stage,
-                                        const int *__restrict__ map_src, const SearchCtl *ctl,
-                                        int bound, int words, uint32_t *__restrict__ valid) {
-  const long long n = (long long)bound * words;
-  const long long num = (long long)ctl->num_valid * words;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n && t < num;
-       t += (long long)gridDim.x * blockDim.x) {
-    const long long k = t / words;
-    valid[t] = stage[(long long)map_src[k] * words + (t - k * words)];
+    const uint32_t *src = stage + i * words;
+    uint32_t *dst = valid + (long long)st * words;
+    if ((words & 3) == 0) {
+      const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+      uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+      for (int q = 0; q < words / 4; ++q) d4[q] = s4[q];
+    } else {
+      for (int q = 0; q < words; ++q) dst[q] = src[q];
+    }
   }
 }
 
@@ -190,22 +241,16 @@ pump_status_t search_init(const SearchDev &sd, cudaStream_t s) {
 pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n_g,
                                  cudaStream_t s) {
   TileScratch ts{};
-  PUMP_TRY(run_scan(ctx, n_g, ExpandCount{sd.g_list[g_idx], sd.path_node, sd.fgo}, sd.wf_off, s,
-                    &ts));
-  copy_total_kernel<<<1, 1, 0, s>>>(ts.total, &sd.ctl->num_new);
-  return launch_status("copy_total");
+  return run_scan(ctx, n_g, ExpandCount{sd.g_list[g_idx], sd.path_node, sd.fgo}, sd.wf_off, s, &ts,
+                  &sd.ctl->num_new);
 }
 
 pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, cudaStream_t s) {
-  if (n_g > 0) {
-    const long long threads = (long long)n_g * 32;
-    long long blocks = (threads + 255) / 256;
-    if (blocks > kNumSMs * 16) blocks = kNumSMs * 16;
-    expand_write_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, sd.g_list[g_idx], n_g);
-    PUMP_TRY(launch_status("expand_write"));
-  }
-  clear_bucket_kernel<<<1, 1, 0, s>>>(sd.ctl, g_idx);
-  return launch_status("clear_bucket");
+  const long long threads = (long long)(n_g > 0 ? n_g : 1) * 32;
+  long long blocks = (threads + 255) / 256;
+  if (blocks > kNumSMs * 16) blocks = kNumSMs * 16;
+  expand_write_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, sd.g_list[g_idx], n_g, g_idx);
+  return launch_status("expand_write");
 }
 
 pump_status_t search_prune(const SearchDev &sd, int num_new, int num_paths, float cp_cutoff,
@@ -213,8 +258,6 @@ pump_status_t search_prune(const SearchDev &sd, int num_new, int num_paths, floa
   const unsigned g = grid_for(num_new, 256);
   new_paths_kernel<<<g, 256, 0, s>>>(sd, num_new, cp_cutoff);
   PUMP_TRY(launch_status("new_paths"));
-  link_new_kernel<<<g, 256, 0, s>>>(sd, num_new);
-  PUMP_TRY(launch_status("link_new"));
   dominance_kernel<<<g, 256, 0, s>>>(sd, num_new, num_paths, eps_cp, eps_cost);
   return launch_status("dominance");
 }
@@ -222,23 +265,14 @@ pump_status_t search_prune(const SearchDev &sd, int num_new, int num_paths, floa
 pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int num_new, int num_paths,
                            int g_idx, float cost_threshold, float dr, float cp_min_soln,
                            const uint32_t *stage, uint32_t *valid, int words, cudaStream_t s) {
+  if (num_new <= 0) return PUMP_OK;
   TileScratch ts{};
-  PUMP_TRY(run_compact(ctx, num_new, StorePred{sd},
-                       StoreEmit{sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln}, s, &ts));
-  copy_total_kernel<<<1, 1, 0, s>>>(ts.total, &sd.ctl->num_valid);
-  PUMP_TRY(launch_status("copy_total"));
-  for (int b = 0; b < 2; ++b) {
-    PUMP_TRY(run_compact(ctx, num_new, BucketPred{sd, b}, BucketEmit{sd, b, num_paths}, s, &ts));
-    bucket_count_kernel<<<1, 1, 0, s>>>(ts.total, sd.ctl, b);
-    PUMP_TRY(launch_status("bucket_count"));
-  }
-  const long long n = (long long)num_new * words;
-  long long blocks = (n + 255) / 256;
-  if (blocks > kNumSMs * 16) blocks = kNumSMs * 16;
-  if (blocks < 1) blocks = 1;
-  gather_survivors_kernel<<<(unsigned)blocks, 256, 0, s>>>(stage, sd.map_src, sd.ctl, num_new, words,
-                                                           valid + (size_t)num_paths * words);
-  return launch_status("gather_survivors");
+  long long ntiles = 0;
+  PUMP_TRY(prepare_tiles(ctx, num_new, s, &ts, &ntiles));
+  store_kernel<<<(unsigned)ntiles, kCompactThreads, 0, s>>>(sd, num_new, num_paths, g_idx,
+                                                           cost_threshold, dr, cp_min_soln, stage,
+                                                           valid, words, ts);
+  return launch_status("store_kernel");
 }
 
 }  // namespace pump

@@ -18,7 +18,8 @@ struct SearchCtl {
   unsigned long long num_valid;  // survivors stored this iteration
   int g_count[2];                // bucket sizes (the reference's G lists)
   int goal_found;                // a stored goal path has CP <= cpTarget / eta
-  int pad;
+  int g_base[2];                 // bucket sizes before this iteration's appends
+  int wait_error;                // 1: a look-back wait of the store pass gave up
 };
 
 // Device arrays of one search (capacities: M + 1 paths and new paths, N nodes).
@@ -39,26 +40,28 @@ struct SearchDev {
   const float *new_cp;           // HSMC output
   uint8_t *alive, *dominated;
   int *new_head, *new_next;      // new paths per node passing the CP cut-off
-  int *map_src;                  // survivor rank -> wavefront index
-  uint8_t *bucket;               // survivor rank -> bucket
   SearchCtl *ctl;
 };
 
 // Path 0 at the initial node in bucket 0 (PUMP.cu:19-34).
 pump_status_t search_init(const SearchDev &sd, cudaStream_t s);
 // Expansion offsets of the n_g paths of bucket g_idx; the wavefront size
-// lands in ctl->num_new.
+// lands in ctl->num_new (n_g > 0).
 pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n_g,
                                  cudaStream_t s);
-// Writes the wavefront (PUMP.cu:47-66) and empties bucket g_idx.
+// Writes the wavefront (PUMP.cu:47-66), empties bucket g_idx (recording the
+// bucket sizes the appends start from) and clears the per-node lists of new
+// paths at the wavefront's nodes.
 pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, cudaStream_t s);
-// New paths' time and cost, the CP cut-off (PUMP.cu:164-185), per-node lists
-// of the survivors of the cut-off, then epsilon dominance (PUMP.cu:188-218).
+// New paths' time and cost, the CP cut-off (PUMP.cu:164-185) with per-node
+// lists of the survivors of the cut-off, then epsilon dominance
+// (PUMP.cu:188-218).
 pump_status_t search_prune(const SearchDev &sd, int num_new, int num_paths, float cp_cutoff,
                            float eps_cp, float eps_cost, cudaStream_t s);
-// Stable compaction of the survivors into stored paths, bucket assignment,
-// per-node lists, goal test and bucket appends (PUMP.cu:221-282); the
-// particle masks of the survivors move from the stage to their stored slots.
+// One pass over the wavefront (PUMP.cu:221-282): survivors become stored
+// paths num_paths + rank in wavefront order, each is appended to its bucket
+// in the same order, linked into its node's list, goal-tested, and its
+// particle mask moves from the stage to its stored slot.
 pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int num_new, int num_paths,
                            int g_idx, float cost_threshold, float dr, float cp_min_soln,
                            const uint32_t *stage, uint32_t *valid, int words, cudaStream_t s);
