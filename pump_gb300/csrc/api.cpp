@@ -44,7 +44,26 @@ Ctx::~Ctx() {
   if (refine_graph.exec) cudaGraphExecDestroy(refine_graph.exec);
   for (int i = 0; i < kNumSlots; ++i)
     if (buf_[i]) cudaFree(buf_[i]);
+  for (int i = 0; i < kNumPin; ++i)
+    if (pin_[i]) cudaFreeHost(pin_[i]);
   if (prev >= 0) cudaSetDevice(prev);
+}
+
+pump_status_t Ctx::pinned(int slot, size_t bytes, void **out) {
+  if (slot < 0 || slot >= kNumPin) return set_error(PUMP_ERR_BAD_INPUT, "pinned slot %d", slot);
+  if (bytes == 0) bytes = 1;
+  if (pin_cap_[slot] < bytes) {
+    if (pin_[slot]) {
+      PUMP_CUDA_TRY(cudaFreeHost(pin_[slot]));
+      pin_[slot] = nullptr;
+      pin_cap_[slot] = 0;
+    }
+    const size_t cap = bytes + bytes / 2 + 4096;
+    PUMP_CUDA_TRY(cudaMallocHost(&pin_[slot], cap));
+    pin_cap_[slot] = cap;
+  }
+  *out = pin_[slot];
+  return PUMP_OK;
 }
 
 namespace {

@@ -359,9 +359,10 @@ __global__ void candidate_segments_kernel(const float *__restrict__ nodes,
                                           const int *__restrict__ node_cnt,
                                           const int *__restrict__ seg_base, int n_paths,
                                           float *__restrict__ x0, float *__restrict__ x1,
-                                          int *__restrict__ seg_path) {
+                                          int *__restrict__ seg_path, int *__restrict__ hits) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n_paths) return;
+  if (hits) hits[p] = 0;
   const int o = node_off[p], n = node_cnt[p], b = seg_base[p];
   for (int i = 0; i + 1 < n; ++i) {
 #pragma unroll
@@ -450,7 +451,7 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
                                     float dt, bool with_cost, int rows_cap, cudaStream_t s) {
   if (n_paths <= 0) return PUMP_OK;
   candidate_segments_kernel<<<grid_for(n_paths, 64), 64, 0, s>>>(
-      cb.nodes, cb.node_off, cb.node_cnt, cb.seg_base, n_paths, cb.x0, cb.x1, cb.seg_path);
+      cb.nodes, cb.node_off, cb.node_cnt, cb.seg_base, n_paths, cb.x0, cb.x1, cb.seg_path, cb.hits);
   PUMP_TRY(launch_status("candidate_segments"));
   if (n_seg > 0) {
     // optimal times (tmax 5) and smoothing costs (tmax 2) in one launch

@@ -22,8 +22,11 @@ class Ctx {
     kSuperset,     // rn bracket bound and the pairs below it (select.cu)
     kNumSlots
   };
+  // Pinned host staging buffers (uploads, read-backs of small results).
+  enum PinSlot { kPinIn = 0, kPinOut, kNumPin };
   explicit Ctx(int device) : device_(device) {
     for (int i = 0; i < kNumSlots; ++i) { buf_[i] = nullptr; cap_[i] = 0; }
+    for (int i = 0; i < kNumPin; ++i) { pin_[i] = nullptr; pin_cap_[i] = 0; }
   }
   ~Ctx();
   static Ctx *from(pump_ctx *c) { return reinterpret_cast<Ctx *>(c); }
@@ -32,6 +35,9 @@ class Ctx {
   pump_status_t activate();
   // Device buffer of at least `bytes` for `slot` (contents undefined).
   pump_status_t scratch(int slot, size_t bytes, void **out);
+  // Pinned host buffer of at least `bytes` for `slot` (grow-only; the caller
+  // has no copy to or from it in flight when it asks for more).
+  pump_status_t pinned(int slot, size_t bytes, void **out);
   // Time-major particle table for (seed, P, T), generated on first use and
   // shared by every context on the device (the reference loads its table
   // once per process); `stream` is ordered after its generation.  The
@@ -52,6 +58,8 @@ class Ctx {
   int device_;
   void *buf_[kNumSlots];
   size_t cap_[kNumSlots];
+  void *pin_[kNumPin];
+  size_t pin_cap_[kNumPin];
 };
 
 // Internal device-side entry points shared between translation units.
@@ -110,9 +118,16 @@ struct CandidateBufs {
   const int *node_off, *node_cnt, *seg_base;
   float *x0, *x1, *topt, *seg_cost, *seg_toff, *states, *cost;
   int *seg_path, *seg_T, *seg_row, *len;
+  int *hits;  // zeroed per path when not null (the MC CP counters)
 };
 pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_seg, int mode,
                                     float dt, bool with_cost, int rows_cap, cudaStream_t s);
+// MC CP hit counts of n_paths dense paths into d_hits (zeroed beforehand):
+// the kernels of mc_cp_async without its memset and CP division.
+pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const int *d_len,
+                               int n_paths, const float *d_offsets_t, int Pmc, int T_rows,
+                               float offset_mult, const float *d_obstacles, int numObs,
+                               int *d_hits, cudaStream_t stream, const float *d_rowmax);
 pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
                               const float *d_tau, int total, float *d_out, cudaStream_t stream);
 

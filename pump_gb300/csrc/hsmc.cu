@@ -616,10 +616,10 @@ pump_status_t particle_rowmax_async(const float *d_table, int P, int T, float *d
   return launch_status("particle_rowmax");
 }
 
-pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
-                          const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
-                          const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
-                          int *d_error, cudaStream_t stream, const float *d_rowmax) {
+pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const int *d_len,
+                               int n_paths, const float *d_offsets_t, int Pmc, int T_rows,
+                               float offset_mult, const float *d_obstacles, int numObs,
+                               int *d_hits, cudaStream_t stream, const float *d_rowmax) {
   if (n_paths <= 0) return PUMP_OK;
   if (numObs > kMcFilterObs) d_rowmax = nullptr;
   size_t smem = sizeof(float) * (size_t)((numObs * 12 + 3) & ~3);
@@ -633,7 +633,6 @@ pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *
   if (smem > 48 * 1024)
     PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)mc_cp_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  PUMP_CUDA_TRY(cudaMemsetAsync(d_hits, 0, sizeof(int) * n_paths, stream));
   for (int k0 = 0; k0 < n_paths; k0 += 65535) {
     const int nk = n_paths - k0 < 65535 ? n_paths - k0 : 65535;
     dim3 grid(grid_for(Pmc, 32), (unsigned)nk);
@@ -642,6 +641,17 @@ pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *
                                               d_rowmax);
     PUMP_TRY(launch_status("mc_cp_kernel"));
   }
+  return PUMP_OK;
+}
+
+pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
+                          const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
+                          const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
+                          int *d_error, cudaStream_t stream, const float *d_rowmax) {
+  if (n_paths <= 0) return PUMP_OK;
+  PUMP_CUDA_TRY(cudaMemsetAsync(d_hits, 0, sizeof(int) * n_paths, stream));
+  PUMP_TRY(mc_cp_hits_async(d_paths, d_offset, d_len, n_paths, d_offsets_t, Pmc, T_rows,
+                            offset_mult, d_obstacles, numObs, d_hits, stream, d_rowmax));
   mc_cp_finish_kernel<<<grid_for(n_paths, 128), 128, 0, stream>>>(d_hits, d_len, n_paths, Pmc,
                                                                   T_rows, d_cp, d_error);
   return launch_status("mc_cp_finish_kernel");

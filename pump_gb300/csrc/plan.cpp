@@ -223,11 +223,11 @@ class Planner {
   DevBuf<int> d_wfPrev_, d_wfEdge_, d_err_;
   int numPaths_ = 0;
   // reusable scratch of the batched BVP / dense-path / MC CP helpers
-  DevBuf<float> d_bx0_, d_bx1_, d_bt_, d_bc_, d_xs_, d_ts_, d_tau_, d_mcp_;
-  DevBuf<int> d_seg_, d_mhits_;
+  DevBuf<float> d_bx0_, d_bx1_, d_bt_, d_bc_, d_xs_, d_ts_, d_tau_;
+  DevBuf<int> d_seg_;
   // candidate batches
-  DevBuf<float> d_cnodes_, d_cx0_, d_cx1_, d_ctopt_, d_csegcost_, d_ctoff_, d_cstates_, d_ccost_;
-  DevBuf<int> d_cints_, d_csegpath_, d_csegT_, d_csegrow_, d_clen_;
+  DevBuf<float> d_cin_, d_cx0_, d_cx1_, d_ctopt_, d_csegcost_, d_ctoff_, d_cstates_, d_best_;
+  DevBuf<int> d_cout_, d_csegpath_, d_csegT_, d_csegrow_;
 };
 
 pump_status_t Planner::run() {
@@ -613,24 +613,33 @@ pump_status_t Planner::eval_candidates(const std::vector<std::vector<float>> &xs
   cost.assign(n, 0.0f);
   cp.assign(n, 0.0f);
   if (n == 0) return PUMP_OK;
-  // nodes | node offsets, counts, segment bases, dense-path offsets
-  std::vector<float> nodes;
-  std::vector<int> ints(4 * (size_t)n);
+  // one upload through pinned memory: nodes | node offsets, counts, segment
+  // bases, dense-path offsets
   int rows = 0, segs = 0;
   for (int k = 0; k < n; ++k) {
     const int c = (int)(xs[k].size() / kDim);
-    ints[k] = rows;
-    ints[n + k] = c;
-    ints[2 * n + k] = segs;
-    ints[3 * n + k] = k * rows_cap;
-    nodes.insert(nodes.end(), xs[k].begin(), xs[k].end());
     rows += c;
     segs += c > 1 ? c - 1 : 0;
   }
-  PUMP_TRY(d_cnodes_.alloc(nodes.size()));
-  PUMP_TRY(d_cints_.alloc(ints.size()));
-  PUMP_TRY(h2d(d_cnodes_.p, nodes.data(), nodes.size()));
-  PUMP_TRY(h2d(d_cints_.p, ints.data(), ints.size()));
+  const size_t nf = (size_t)rows * kDim;
+  const size_t in_bytes = sizeof(float) * nf + sizeof(int) * 4 * (size_t)n;
+  char *hin = nullptr;
+  PUMP_TRY(ctx_->pinned(Ctx::kPinIn, in_bytes, (void **)&hin));
+  float *hnodes = reinterpret_cast<float *>(hin);
+  int *hints = reinterpret_cast<int *>(hin + sizeof(float) * nf);
+  for (int k = 0, r = 0, sg = 0; k < n; ++k) {
+    const int c = (int)(xs[k].size() / kDim);
+    hints[k] = r;
+    hints[n + k] = c;
+    hints[2 * n + k] = sg;
+    hints[3 * n + k] = k * rows_cap;
+    std::memcpy(hnodes + (size_t)r * kDim, xs[k].data(), sizeof(float) * xs[k].size());
+    r += c;
+    sg += c > 1 ? c - 1 : 0;
+  }
+  PUMP_TRY(d_cin_.alloc(in_bytes / sizeof(float) + 1));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(d_cin_.p, hin, in_bytes, cudaMemcpyHostToDevice, s_));
+  const int *d_ints = reinterpret_cast<const int *>(d_cin_.p + nf);
   const size_t sg = segs > 0 ? (size_t)segs : 1;
   PUMP_TRY(d_cx0_.alloc(sg * kDim));
   PUMP_TRY(d_cx1_.alloc(sg * kDim));
@@ -640,40 +649,43 @@ pump_status_t Planner::eval_candidates(const std::vector<std::vector<float>> &xs
   PUMP_TRY(d_csegpath_.alloc(sg));
   PUMP_TRY(d_csegT_.alloc(sg));
   PUMP_TRY(d_csegrow_.alloc(sg));
-  PUMP_TRY(d_clen_.alloc(n));
-  PUMP_TRY(d_ccost_.alloc(n));
+  // results read back in one copy: MC hit counts | lengths | costs
+  PUMP_TRY(d_cout_.alloc(3 * (size_t)n));
   PUMP_TRY(d_cstates_.alloc((size_t)n * rows_cap * kDim));
   CandidateBufs cb{};
-  cb.nodes = d_cnodes_.p;
-  cb.node_off = d_cints_.p;
-  cb.node_cnt = d_cints_.p + n;
-  cb.seg_base = d_cints_.p + 2 * n;
+  cb.nodes = d_cin_.p;
+  cb.node_off = d_ints;
+  cb.node_cnt = d_ints + n;
+  cb.seg_base = d_ints + 2 * n;
   cb.x0 = d_cx0_.p;
   cb.x1 = d_cx1_.p;
   cb.topt = d_ctopt_.p;
   cb.seg_cost = d_csegcost_.p;
   cb.seg_toff = d_ctoff_.p;
   cb.states = d_cstates_.p;
-  cb.cost = d_ccost_.p;
+  cb.hits = with_cp ? d_cout_.p : nullptr;
+  cb.len = d_cout_.p + n;
+  cb.cost = reinterpret_cast<float *>(d_cout_.p + 2 * n);
   cb.seg_path = d_csegpath_.p;
   cb.seg_T = d_csegT_.p;
   cb.seg_row = d_csegrow_.p;
-  cb.len = d_clen_.p;
   PUMP_TRY(candidate_paths_async(cb, n, segs, pb_.bvp_mode, dt, with_cost, rows_cap, s_));
-  if (with_cp) {
-    PUMP_TRY(d_mhits_.alloc(n));
-    PUMP_TRY(d_mcp_.alloc(n));
-    PUMP_TRY(mc_cp_async(d_cstates_.p, d_cints_.p + 3 * n, d_clen_.p, n, d_table_, pb_.num_mc,
-                         pb_.table_rows, pb_.offset_mult, obs_p_, nobs_, d_mhits_.p, d_mcp_.p,
-                         nullptr, s_, d_rowmax_));
-    PUMP_TRY(d2h(cp.data(), d_mcp_.p, n));
-  }
-  PUMP_TRY(d2h(len.data(), d_clen_.p, n));
-  if (with_cost) PUMP_TRY(d2h(cost.data(), d_ccost_.p, n));
-  PUMP_TRY(sync());
   if (with_cp)
-    for (int k = 0; k < n; ++k)
-      if (len[k] > pb_.table_rows) cp[k] = -1.0f;
+    PUMP_TRY(mc_cp_hits_async(d_cstates_.p, d_ints + 3 * n, cb.len, n, d_table_, pb_.num_mc,
+                              pb_.table_rows, pb_.offset_mult, obs_p_, nobs_, cb.hits, s_,
+                              d_rowmax_));
+  int *hout = nullptr;
+  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(int) * 3 * (size_t)n, (void **)&hout));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hout, d_cout_.p, sizeof(int) * 3 * (size_t)n,
+                                cudaMemcpyDeviceToHost, s_));
+  PUMP_TRY(sync());
+  for (int k = 0; k < n; ++k) {
+    len[k] = hout[n + k];
+    if (with_cost) std::memcpy(&cost[k], &hout[2 * n + k], sizeof(float));
+    // collisionProbability.cu:89-91: hits / Pmc in binary32; a path longer
+    // than the particle table has no CP
+    if (with_cp) cp[k] = len[k] > pb_.table_rows ? -1.0f : ((float)hout[k]) / ((float)pb_.num_mc);
+  }
   return PUMP_OK;
 }
 
@@ -713,13 +725,17 @@ pump_status_t Planner::search_and_smooth() {
   // the loop: the last iterate evaluated, zeros if smoothing did not run
   std::vector<float> xsFinal(xs.size(), 0.0f);
   std::vector<float> xsBest(xs);  // nodes of the path kept so far
+  // the dense path kept so far stays on the device (d_best_) until the end
   std::vector<float> bestPath;
   int bestLen = last >= 0 ? glen[last] : 0;
-  if (last >= 0 && bestLen > 0) {
-    bestPath.resize((size_t)bestLen * kDim);
-    PUMP_TRY(d2h(bestPath.data(), d_cstates_.p + (size_t)last * rowsCap * kDim, bestPath.size()));
-    PUMP_TRY(sync());
-  }
+  PUMP_TRY(d_best_.alloc((size_t)rowsCap * kDim));
+  auto keep_best = [&](int k, int len) -> pump_status_t {
+    PUMP_CUDA_TRY(cudaMemcpyAsync(d_best_.p, d_cstates_.p + (size_t)k * rowsCap * kDim,
+                                  sizeof(float) * kDim * (size_t)len, cudaMemcpyDeviceToDevice,
+                                  s_));
+    return PUMP_OK;
+  };
+  if (last >= 0 && bestLen > 0) PUMP_TRY(keep_best(last, bestLen));
   float lastCP = solnPathCP, lastCost = solnPathCost;
   if (success) {
     const int n = (int)(xs.size() / kDim);
@@ -796,9 +812,7 @@ pump_status_t Planner::search_and_smooth() {
         const bool eqLower = (cp == lastCP && smoothCost < lastCost);
         if (satisfies && (closer || eqLower)) {
           bestLen = slen[k];
-          bestPath.resize((size_t)bestLen * kDim);
-          PUMP_TRY(d2h(bestPath.data(), d_cstates_.p + (size_t)k * rowsCap * kDim, bestPath.size()));
-          PUMP_TRY(sync());
+          PUMP_TRY(keep_best(k, bestLen));
           lastCost = smoothCost;
           lastCP = cp;
           xsBest = cand[k];
@@ -810,6 +824,11 @@ pump_status_t Planner::search_and_smooth() {
         k = 2 * k + (cp < cpTarget ? 1 : 2);
       }
     }
+  }
+  if (last >= 0 && bestLen > 0) {
+    bestPath.resize((size_t)bestLen * kDim);
+    PUMP_TRY(d2h(bestPath.data(), d_best_.p, bestPath.size()));
+    PUMP_TRY(sync());
   }
   if (success && pb_.refine_iters > 0)
     PUMP_TRY(refine(xsBest, cpTarget, &lastCP, &lastCost, &bestPath, &bestLen, &xsFinal));
