@@ -226,7 +226,7 @@ __global__ void bvp_batch_kernel(const BvpJobs jb) {
 #pragma unroll
   for (int d = 0; d < kDim; ++d) {
     x0[d] = jb.x0[k * kDim + d];
-    x1[d] = jb.x1[k * kDim + d];
+    x1[d] = jb.x1[(jb.x1_same ? 0 : k) * kDim + d];
   }
   const PairCoef c = make_coef(x0, x1);
   const float tp = topt_bisection(c, jb.tmax[j]);

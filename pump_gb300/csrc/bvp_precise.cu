@@ -63,7 +63,7 @@ __global__ void bvp_batch_precision_kernel(const BvpJobs jb) {
 #pragma unroll
   for (int d = 0; d < kDim; ++d) {
     x0[d] = jb.x0[k * kDim + d];
-    x1[d] = jb.x1[k * kDim + d];
+    x1[d] = jb.x1[(jb.x1_same ? 0 : k) * kDim + d];
   }
   float tp, cp;
   precise_pair(x0, x1, jb.tmax[j], &tp, &cp);

@@ -97,7 +97,8 @@ pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor
                                     cudaStream_t stream);
 pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tmax, float *d_copts,
                                          float *d_topts, cudaStream_t stream);
-// Explicit pairs (x0[k], x1[k]), k < n, each bisected for `jobs` (1 or 2)
+// Explicit pairs (x0[k], x1[k]), k < n (x1[0] for every k with x1_same),
+// each bisected for `jobs` (1 or 2)
 // optimal-time limits: job j writes topt[j][k] and cost[j][k] (either may be
 // null).  One thread per (job, pair); small batches use 32-thread blocks so
 // their binary64 bisections spread over more SMs.
@@ -106,6 +107,7 @@ struct BvpJobs {
   int n, jobs;
   float tmax[2];
   float *topt[2], *cost[2];
+  int x1_same;  // 1: every pair's end state is x1[0..5]
 };
 pump_status_t bvp_jobs_launch(const BvpJobs &jb, int mode, cudaStream_t stream);
 pump_status_t bvp_jobs_precision_launch(const BvpJobs &jb, cudaStream_t stream);

@@ -207,7 +207,8 @@ class Planner {
   DevBuf<uint8_t> d_free_s_, d_free_e_, d_hcount_;
   long long E_ = 0;
   float rn_ = 0;
-  std::vector<float> h_;
+  DevBuf<float> d_h_;  // heuristic per node (cost to the goal)
+  float h0_ = 0;
   // the expandable edges (free, to a free node) in (source, destination)
   // order: original edge id, destination, cost, time, and row starts per node
   DevBuf<int> d_fid_, d_fsrc_, d_fdst_, d_fgo_;
@@ -260,8 +261,34 @@ pump_status_t Planner::run() {
 pump_status_t Planner::roadmap() {
   if (pb_.samples) samples_.assign(pb_.samples, pb_.samples + (size_t)N_ * kDim);
   else halton_samples(pb_, samples_);
-  PUMP_TRY(d_samples_.alloc((size_t)N_ * kDim));
-  PUMP_TRY(h2d(d_samples_.p, samples_.data(), samples_.size()));
+  // one upload through pinned memory: the samples, then the goal state
+  const size_t nsf = (size_t)N_ * kDim;
+  float *hin = nullptr;
+  PUMP_TRY(ctx_->pinned(Ctx::kPinIn, sizeof(float) * (nsf + kDim), (void **)&hin));
+  std::memcpy(hin, samples_.data(), sizeof(float) * nsf);
+  for (int d = 0; d < kDim; ++d) hin[nsf + d] = pb_.goal[d];
+  PUMP_TRY(d_samples_.alloc(nsf + kDim));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(d_samples_.p, hin, sizeof(float) * (nsf + kDim),
+                                cudaMemcpyHostToDevice, s_));
+  // heuristic h (mainPUMP.cu:351-355): cost of the optimal connection of
+  // node i to the goal (h[N-1] = 0), kept on the device for the search; h[0]
+  // is read back with the roadmap's next synchronisation
+  PUMP_TRY(d_h_.alloc(N_));
+  PUMP_CUDA_TRY(cudaMemsetAsync(d_h_.p + (N_ - 1), 0, sizeof(float), s_));
+  {
+    BvpJobs jb{};
+    jb.x0 = d_samples_.p;
+    jb.x1 = d_samples_.p + nsf;
+    jb.x1_same = 1;
+    jb.n = N_ - 1;
+    jb.jobs = 1;
+    jb.tmax[0] = 5.0f;
+    jb.cost[0] = d_h_.p;
+    PUMP_TRY(bvp_jobs_launch(jb, pb_.bvp_mode, s_));
+  }
+  float *h0 = nullptr;
+  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float), (void **)&h0));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(h0, d_h_.p, sizeof(float), cudaMemcpyDeviceToHost, s_));
   const long long npairs = (long long)N_ * (N_ - 1);
   // mainPUMP.cu:261-262: (int)((NUM-1)*(NUM)*rnPerc) with rnPerc a float
   const long long rnIdx = (long long)((float)((long long)(N_ - 1) * N_) * (float)0.05);
@@ -286,20 +313,9 @@ pump_status_t Planner::roadmap() {
   PUMP_TRY(d_disc_.alloc((size_t)E_ * W_ * kDim));
   PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, d_toptE_.p, E_, pb_.num_disc,
                                  pb_.bvp_mode, d_disc_.p, (pump_stream_t)s_));
-  // heuristic h (mainPUMP.cu:351-355): cost of the optimal connection to the goal
-  {
-    std::vector<float> x0((size_t)(N_ - 1) * kDim), x1((size_t)(N_ - 1) * kDim);
-    for (int i = 0; i < N_ - 1; ++i)
-      for (int d = 0; d < kDim; ++d) {
-        x0[(size_t)i * kDim + d] = samples_[(size_t)i * kDim + d];
-        x1[(size_t)i * kDim + d] = pb_.goal[d];
-      }
-    std::vector<float> c;
-    PUMP_TRY(topts_of(x0, x1, 5.0f, nullptr, &c));
-    h_.assign(N_, 0.0f);
-    for (int i = 0; i < N_ - 1; ++i) h_[i] = c[i];
-  }
-  return sync();
+  PUMP_TRY(sync());
+  h0_ = *h0;
+  return PUMP_OK;
 }
 
 // The query's pair costs from the batch's shared Halton pairs plus its own
@@ -404,7 +420,7 @@ pump_status_t Planner::explore() {
   PUMP_TRY(d_wfEdge_.alloc(cap));
   PUMP_TRY(d_err_.alloc(1));
   DevBuf<int> d_prev, d_node, d_g0, d_g1, d_nhead, d_nnext, d_wnode, d_wopen, d_newhead, d_newnext;
-  DevBuf<float> d_cost, d_cp, d_ncost, d_ntime, d_h;
+  DevBuf<float> d_cost, d_cp, d_ncost, d_ntime;
   DevBuf<unsigned int> d_off;
   DevBuf<uint8_t> d_alive, d_dom;
   DevBuf<SearchCtl> d_ctl;
@@ -425,9 +441,7 @@ pump_status_t Planner::explore() {
   PUMP_TRY(d_dom.alloc(cap));
   PUMP_TRY(d_newhead.alloc(N_));
   PUMP_TRY(d_newnext.alloc(cap));
-  PUMP_TRY(d_h.alloc(N_));
   PUMP_TRY(d_ctl.alloc(1));
-  PUMP_TRY(h2d(d_h.p, h_.data(), (size_t)N_));
   PUMP_CUDA_TRY(cudaMemsetAsync(d_err_.p, 0, sizeof(int), s_));
   // setupValidParticles (PUMP.cu:766-777) for path 0: all particles valid
   PUMP_CUDA_TRY(cudaMemsetAsync(d_valid_.p, 0xFF, sizeof(uint32_t) * words_, s_));
@@ -443,7 +457,7 @@ pump_status_t Planner::explore() {
   sd.fdst = d_fdst_.p;
   sd.fcopt = d_fcopt_.p;
   sd.ftopt = d_ftopt_.p;
-  sd.h = d_h.p;
+  sd.h = d_h_.p;
   sd.path_prev = d_prev.p;
   sd.path_node = d_node.p;
   sd.path_cost = d_cost.p;
@@ -476,7 +490,7 @@ pump_status_t Planner::explore() {
   int Gidx = 0;
   int gCount[2] = {1, 0};
   numPaths_ = 1;
-  float costThreshold = h_[0];
+  float costThreshold = h0_;
   const int maxItrs = 20;
   int itrs = 0;
   long long considered = 0;
