@@ -485,6 +485,33 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
   return PUMP_OK;
 }
 
+namespace {
+__global__ void own_pairs_kernel(const float *__restrict__ samples, int N, float *__restrict__ x0,
+                                 float *__restrict__ x1) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n1 = N - 1, n2 = N - 2;
+  if (k >= 2 * n1 + 2 * n2) return;
+  int a, b;
+  if (k < n1) { a = 0; b = k + 1; }                           // init row
+  else if (k < 2 * n1) { a = k - n1 + 1; b = 0; }             // init column
+  else if (k < 2 * n1 + n2) { a = N - 1; b = k - 2 * n1 + 1; }  // goal row
+  else { a = k - 2 * n1 - n2 + 1; b = N - 1; }                // goal column
+#pragma unroll
+  for (int d = 0; d < kDim; ++d) {
+    x0[k * kDim + d] = samples[a * kDim + d];
+    x1[k * kDim + d] = samples[b * kDim + d];
+  }
+}
+}  // namespace
+
+pump_status_t own_pairs_async(const float *d_samples, int N, float *d_x0, float *d_x1,
+                              cudaStream_t stream) {
+  const int n = 4 * N - 6;
+  if (n <= 0) return PUMP_OK;
+  own_pairs_kernel<<<grid_for(n, 256), 256, 0, stream>>>(d_samples, N, d_x0, d_x1);
+  return launch_status("own_pairs_kernel");
+}
+
 pump_status_t bvp_jobs_launch(const BvpJobs &jb, int mode, cudaStream_t stream) {
   if (jb.n <= 0) return PUMP_OK;
   if (mode == PUMP_BVP_PRECISION) return bvp_jobs_precision_launch(jb, stream);

@@ -37,6 +37,41 @@ __global__ void sample_free_kernel(const float *__restrict__ obs, int numObs,
   is_free[node] = fr;
 }
 
+// halton, sampler.cu:43-57, in the same binary32 operations and order (this
+// translation unit does not contract multiply-adds).
+__device__ float halton_dev(int n, int b) {
+  float hn = 0;
+  int n0 = n;
+  float f = 1 / ((float)b);
+  while (n0 > 0) {
+    float n1 = (float)(n0 / b);
+    int r = (int)(n0 - n1 * b);
+    hn += f * r;
+    f = f / b;
+    n0 = (int)n1;
+  }
+  return hn;
+}
+
+struct SampleBox {
+  float lo[6], hi[6], init[6], goal[6];
+};
+
+// sampler.cu:20-41: sample n, dimension d = halton(n, base d) scaled into
+// [lo, hi]; sample 0 is init and sample N-1 the goal, copied exactly.  The
+// goal row is written once more after the N samples.
+__global__ void halton_kernel(int N, SampleBox bx, float *__restrict__ out) {
+  const int bases[6] = {2, 3, 5, 7, 11, 13};
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)(N + 1) * kDim) return;
+  const int n = (int)(t / kDim), d = (int)(t - (long long)n * kDim);
+  float v;
+  if (n == 0) v = bx.init[d];
+  else if (n >= N - 1) v = bx.goal[d];
+  else v = halton_dev(n, bases[d]) * (bx.hi[d] - bx.lo[d]) + bx.lo[d];
+  out[t] = v;
+}
+
 // One thread per edge: freeEdges, collisionCheck.cu:5-37.
 __global__ void __launch_bounds__(256) free_edges_kernel(const float *__restrict__ obs, int numObs,
                                                          const float *__restrict__ disc, long long E,
@@ -322,6 +357,20 @@ pump_status_t set_smem_attr(const void *fn, size_t bytes) {
 }
 
 }  // namespace
+
+pump_status_t halton_samples_async(int N, const float *lo, const float *hi, const float *init,
+                                   const float *goal, float *d_out, cudaStream_t stream) {
+  SampleBox bx;
+  for (int d = 0; d < 6; ++d) {
+    bx.lo[d] = lo[d];
+    bx.hi[d] = hi[d];
+    bx.init[d] = init[d];
+    bx.goal[d] = goal[d];
+  }
+  halton_kernel<<<grid_for((long long)(N + 1) * kDim, 256), 256, 0, stream>>>(N, bx, d_out);
+  return launch_status("halton_kernel");
+}
+
 }  // namespace pump
 
 using namespace pump;

@@ -130,6 +130,15 @@ pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const 
                                int n_paths, const float *d_offsets_t, int Pmc, int T_rows,
                                float offset_mult, const float *d_obstacles, int numObs,
                                int *d_hits, cudaStream_t stream, const float *d_rowmax);
+// Halton samples of a query (sampler.cu:20-41), N x 6, then the goal row
+// once more.
+pump_status_t halton_samples_async(int N, const float *lo, const float *hi, const float *init,
+                                   const float *goal, float *d_out, cudaStream_t stream);
+// The 4N-6 pairs of a query that touch its init or goal sample, as explicit
+// (x0, x1) rows: init row (0 -> j, j = 1 .. N-1), init column (i -> 0),
+// goal row (N-1 -> j, j = 1 .. N-2), goal column (i -> N-1).
+pump_status_t own_pairs_async(const float *d_samples, int N, float *d_x0, float *d_x1,
+                              cudaStream_t stream);
 pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
                               const float *d_tau, int total, float *d_out, cudaStream_t stream);
 

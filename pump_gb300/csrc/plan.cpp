@@ -259,17 +259,27 @@ pump_status_t Planner::run() {
 }
 
 pump_status_t Planner::roadmap() {
-  if (pb_.samples) samples_.assign(pb_.samples, pb_.samples + (size_t)N_ * kDim);
-  else halton_samples(pb_, samples_);
-  // one upload through pinned memory: the samples, then the goal state
+  // the samples (then the goal state once more) on the device: Halton points
+  // generated there, or the caller's samples uploaded through pinned memory.
+  // Pinned read-back (at the next synchronisation): h[0], then the Halton
+  // samples for the host's path reconstruction.
   const size_t nsf = (size_t)N_ * kDim;
-  float *hin = nullptr;
-  PUMP_TRY(ctx_->pinned(Ctx::kPinIn, sizeof(float) * (nsf + kDim), (void **)&hin));
-  std::memcpy(hin, samples_.data(), sizeof(float) * nsf);
-  for (int d = 0; d < kDim; ++d) hin[nsf + d] = pb_.goal[d];
   PUMP_TRY(d_samples_.alloc(nsf + kDim));
-  PUMP_CUDA_TRY(cudaMemcpyAsync(d_samples_.p, hin, sizeof(float) * (nsf + kDim),
-                                cudaMemcpyHostToDevice, s_));
+  float *hout = nullptr;
+  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float) * (1 + nsf), (void **)&hout));
+  if (pb_.samples) {
+    samples_.assign(pb_.samples, pb_.samples + nsf);
+    float *hin = nullptr;
+    PUMP_TRY(ctx_->pinned(Ctx::kPinIn, sizeof(float) * (nsf + kDim), (void **)&hin));
+    std::memcpy(hin, samples_.data(), sizeof(float) * nsf);
+    for (int d = 0; d < kDim; ++d) hin[nsf + d] = pb_.goal[d];
+    PUMP_CUDA_TRY(cudaMemcpyAsync(d_samples_.p, hin, sizeof(float) * (nsf + kDim),
+                                  cudaMemcpyHostToDevice, s_));
+  } else {
+    PUMP_TRY(halton_samples_async(N_, pb_.lo, pb_.hi, pb_.init, pb_.goal, d_samples_.p, s_));
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hout + 1, d_samples_.p, sizeof(float) * nsf,
+                                  cudaMemcpyDeviceToHost, s_));
+  }
   // heuristic h (mainPUMP.cu:351-355): cost of the optimal connection of
   // node i to the goal (h[N-1] = 0), kept on the device for the search; h[0]
   // is read back with the roadmap's next synchronisation
@@ -286,9 +296,7 @@ pump_status_t Planner::roadmap() {
     jb.cost[0] = d_h_.p;
     PUMP_TRY(bvp_jobs_launch(jb, pb_.bvp_mode, s_));
   }
-  float *h0 = nullptr;
-  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float), (void **)&h0));
-  PUMP_CUDA_TRY(cudaMemcpyAsync(h0, d_h_.p, sizeof(float), cudaMemcpyDeviceToHost, s_));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hout, d_h_.p, sizeof(float), cudaMemcpyDeviceToHost, s_));
   const long long npairs = (long long)N_ * (N_ - 1);
   // mainPUMP.cu:261-262: (int)((NUM-1)*(NUM)*rnPerc) with rnPerc a float
   const long long rnIdx = (long long)((float)((long long)(N_ - 1) * N_) * (float)0.05);
@@ -314,7 +322,8 @@ pump_status_t Planner::roadmap() {
   PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, d_toptE_.p, E_, pb_.num_disc,
                                  pb_.bvp_mode, d_disc_.p, (pump_stream_t)s_));
   PUMP_TRY(sync());
-  h0_ = *h0;
+  h0_ = hout[0];
+  if (!pb_.samples) samples_.assign(hout + 1, hout + 1 + nsf);
   return PUMP_OK;
 }
 
@@ -324,25 +333,11 @@ pump_status_t Planner::roadmap() {
 pump_status_t Planner::pair_costs_shared(long long rnIdx, long long cap) {
   const int N = N_;
   const size_t own = (size_t)(4 * N - 6);
-  std::vector<float> x0(own * kDim), x1(own * kDim);
-  size_t k = 0;
-  auto put = [&](int a, int b) {
-    for (int d = 0; d < kDim; ++d) {
-      x0[k * kDim + d] = samples_[(size_t)a * kDim + d];
-      x1[k * kDim + d] = samples_[(size_t)b * kDim + d];
-    }
-    ++k;
-  };
-  for (int j = 1; j <= N - 1; ++j) put(0, j);      // init row
-  for (int i = 1; i <= N - 1; ++i) put(i, 0);      // init col
-  for (int j = 1; j <= N - 2; ++j) put(N - 1, j);  // goal row
-  for (int i = 1; i <= N - 2; ++i) put(i, N - 1);  // goal col
-  PUMP_TRY(d_bx0_.alloc(x0.size()));
-  PUMP_TRY(d_bx1_.alloc(x1.size()));
+  PUMP_TRY(d_bx0_.alloc(own * kDim));
+  PUMP_TRY(d_bx1_.alloc(own * kDim));
+  PUMP_TRY(own_pairs_async(d_samples_.p, N, d_bx0_.p, d_bx1_.p, s_));
   PUMP_TRY(d_own_c_.alloc(own));
   PUMP_TRY(d_own_t_.alloc(own));
-  PUMP_TRY(h2d(d_bx0_.p, x0.data(), x0.size()));
-  PUMP_TRY(h2d(d_bx1_.p, x1.data(), x1.size()));
   PUMP_TRY(pump_bvp_batch(d_bx0_.p, d_bx1_.p, (int)own, 5.0f, pb_.bvp_mode, d_own_t_.p, d_own_c_.p,
                           (pump_stream_t)s_));
   PairView pv;
