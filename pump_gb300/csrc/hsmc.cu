@@ -210,6 +210,9 @@ constexpr int kHsmcFilterObs = 128;
 
 struct HsmcParams {
   int num_new, W;
+  // with num_new_dev the path count is *num_new_dev (0 when *skip_dev is set)
+  const unsigned long long *num_new_dev;
+  const int *skip_dev;
   const int *wf_edge, *wf_prev;
   long long num_edges;
   int num_prev;
@@ -244,31 +247,17 @@ __host__ __device__ inline size_t hsmc_boxes_smem(int numObs) {
          (size_t)kHsmcWarps * (sizeof(float4) * kMaxHsSlots + kMaxHsSlots + sizeof(int) * kHsmcFilterObs);
 }
 
+// New path w (the whole warp).  valid_in[prev] is read, valid_out[w] /
+// cp_out[w] written (the two may alias one path store with valid_out =
+// store + base, as in the reference).  With hs_count (stored half-spaces per
+// waypoint), slots at or past a waypoint's count are inactive without
+// reading them (they hold the defaults b = 1111 in the dense layout); stored
+// slots still need b < 1000.
 template <bool Boxes>
-__global__ void __launch_bounds__(kHsmcThreads) hsmc_kernel(const HsmcParams p) {
-  // valid_in[prev] is read, valid_out[w] / cp_out[w] written (the two may
-  // alias one path store with valid_out = store + base, as in the reference).
-  // With hs_count (stored half-spaces per waypoint), slots at or past a
-  // waypoint's count are inactive without reading them (they hold the
-  // defaults b = 1111 in the dense layout); stored slots still need b < 1000.
-  extern __shared__ float4 s_dyn4[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const float *s_obs,
+                                          float4 *hs, uint8_t *hcnt, int *klist) {
+  const int lane = threadIdx.x & 31;
   const unsigned int lt = (1u << lane) - 1u;
-  float *s_obs = reinterpret_cast<float *>(s_dyn4);
-  float4 *hs = nullptr;
-  uint8_t *hcnt = nullptr;
-  int *klist = nullptr;
-  if (Boxes) {
-    stage_obstacles(p.obs, p.numObs, s_obs);  // block-wide, before any warp leaves
-    float4 *s_hs = reinterpret_cast<float4 *>(s_obs + hsmc_boxes_obs_floats(p.numObs));
-    hs = s_hs + warp * kMaxHsSlots;
-    uint8_t *s_cnt = reinterpret_cast<uint8_t *>(s_hs + kHsmcWarps * kMaxHsSlots);
-    hcnt = s_cnt + warp * kMaxHsSlots;
-    int *s_klist = reinterpret_cast<int *>(s_cnt + kHsmcWarps * kMaxHsSlots);
-    klist = s_klist + warp * kHsmcFilterObs;
-  }
-  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-  if (w >= p.num_new) return;  // warp-uniform
   const int edge = p.wf_edge[w], prev = p.wf_prev[w];
   if (edge < 0 || edge >= p.num_edges || prev < 0 || prev >= p.num_prev) {
     if (lane == 0 && p.error) atomicExch(p.error, (int)PUMP_ERR_BAD_INPUT);
@@ -484,6 +473,32 @@ __global__ void __launch_bounds__(kHsmcThreads) hsmc_kernel(const HsmcParams p) 
   }
 }
 
+template <bool Boxes>
+__global__ void __launch_bounds__(kHsmcThreads) hsmc_kernel(const HsmcParams p) {
+  extern __shared__ float4 s_dyn4[];
+  const int warp = threadIdx.x >> 5;
+  float *s_obs = reinterpret_cast<float *>(s_dyn4);
+  float4 *hs = nullptr;
+  uint8_t *hcnt = nullptr;
+  int *klist = nullptr;
+  if (Boxes) {
+    stage_obstacles(p.obs, p.numObs, s_obs);  // block-wide, before any warp leaves
+    float4 *s_hs = reinterpret_cast<float4 *>(s_obs + hsmc_boxes_obs_floats(p.numObs));
+    hs = s_hs + warp * kMaxHsSlots;
+    uint8_t *s_cnt = reinterpret_cast<uint8_t *>(s_hs + kHsmcWarps * kMaxHsSlots);
+    hcnt = s_cnt + warp * kMaxHsSlots;
+    int *s_klist = reinterpret_cast<int *>(s_cnt + kHsmcWarps * kMaxHsSlots);
+    klist = s_klist + warp * kHsmcFilterObs;
+  }
+  int n = p.num_new;
+  if (p.num_new_dev) n = (p.skip_dev && *p.skip_dev) ? 0 : (int)*p.num_new_dev;
+  const int warps = (int)((gridDim.x * (long long)blockDim.x) >> 5);
+  for (int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); w < n; w += warps) {
+    hsmc_path<Boxes>(p, w, s_obs, hs, hcnt, klist);
+    __syncwarp();  // the warp's half-space slots are rewritten by its next path
+  }
+}
+
 // -------------------------------------------------------------- MC CP
 // collisionProbability.cu:39-92.  A particle collides when any of the
 // segments t = 0 .. T-3 of its perturbed path hits a box; the reference walks
@@ -663,7 +678,8 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
                                 const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                                 const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
                                 float *d_cp_out, int *d_error, const uint8_t *d_hs_count,
-                                cudaStream_t stream) {
+                                cudaStream_t stream, const unsigned long long *d_num_new,
+                                const int *d_skip) {
   if (num_new <= 0) return PUMP_OK;
   if ((P + 31) / 32 > kMaxHsmcWords)
     return set_error(PUMP_ERR_CAPACITY, "hsmc: %d particles exceed %d", P, 32 * kMaxHsmcWords);
@@ -693,7 +709,11 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
   hp.P = P;
   hp.cp_out = d_cp_out;
   hp.error = d_error;
-  hsmc_kernel<false><<<grid_for((long long)num_new * 32, kHsmcThreads), kHsmcThreads, 0, stream>>>(hp);
+  hp.num_new_dev = d_num_new;
+  hp.skip_dev = d_skip;
+  const unsigned blocks =
+      d_num_new ? (unsigned)(kNumSMs * 4) : grid_for((long long)num_new * 32, kHsmcThreads);
+  hsmc_kernel<false><<<blocks, kHsmcThreads, 0, stream>>>(hp);
   return launch_status("hsmc_kernel");
 }
 
@@ -708,7 +728,8 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                                const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
                                int T_rows, float offset_mult, const uint32_t *d_valid_in,
                                uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
-                               cudaStream_t stream) {
+                               cudaStream_t stream, const unsigned long long *d_num_new,
+                               const int *d_skip) {
   if (num_new <= 0) return PUMP_OK;
   if ((P + 31) / 32 > kMaxHsmcWords)
     return set_error(PUMP_ERR_CAPACITY, "hsmc: %d particles exceed %d", P, 32 * kMaxHsmcWords);
@@ -739,11 +760,15 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
   hp.P = P;
   hp.cp_out = d_cp_out;
   hp.error = d_error;
+  hp.num_new_dev = d_num_new;
+  hp.skip_dev = d_skip;
   const size_t smem = hsmc_boxes_smem(numObs);
   if (smem > 48 * 1024)
     PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)hsmc_kernel<true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  hsmc_kernel<true><<<grid_for((long long)num_new * 32, kHsmcThreads), kHsmcThreads, smem, stream>>>(hp);
+  const unsigned blocks =
+      d_num_new ? (unsigned)(kNumSMs * 4) : grid_for((long long)num_new * 32, kHsmcThreads);
+  hsmc_kernel<true><<<blocks, kHsmcThreads, smem, stream>>>(hp);
   return launch_status("hsmc_kernel (boxes)");
 }
 
@@ -808,7 +833,7 @@ extern "C" pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_ed
                            d_topt, dt,
                            d_offsets_t, Pmc, T_rows, offset_mult, d_valid,
                            d_valid + (size_t)base * words, P, d_path_cp + base, d_error,
-                           d_hs_count, (cudaStream_t)stream);
+                           d_hs_count, (cudaStream_t)stream, nullptr, nullptr);
 }
 
 extern "C" pump_status_t pump_hsmc_propagate_boxes(
@@ -826,7 +851,7 @@ extern "C" pump_status_t pump_hsmc_propagate_boxes(
   return hsmc_boxes_async(num_new, W, d_edge, d_prev, num_edges, base, d_obstacles, numObs, d_disc,
                           maxd2, maxHS, d_times, d_topt, dt, d_offsets_t, Pmc, T_rows, offset_mult,
                           d_valid, d_valid + (size_t)base * words, P, d_path_cp + base, d_error,
-                          (cudaStream_t)stream);
+                          (cudaStream_t)stream, nullptr, nullptr);
 }
 
 extern "C" pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d_len,

@@ -41,7 +41,8 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
                                 const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                                 const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
                                 float *d_cp_out, int *d_error, const uint8_t *d_hs_count,
-                                cudaStream_t stream);
+                                cudaStream_t stream, const unsigned long long *d_num_new,
+                                const int *d_skip);
 bool hsmc_boxes_fits(int numObs, int W, int maxHS);
 pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int *d_prev,
                                long long num_edges, int num_prev, const float *d_obs, int numObs,
@@ -49,7 +50,8 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                                const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
                                int T_rows, float offset_mult, const uint32_t *d_valid_in,
                                uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
-                               cudaStream_t stream);
+                               cudaStream_t stream, const unsigned long long *d_num_new,
+                               const int *d_skip);
 pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n, int words,
                                  uint32_t *d_dst, cudaStream_t stream);
 pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
@@ -494,57 +496,66 @@ pump_status_t Planner::explore() {
   SearchCtl ctl{};
   while (itrs < maxItrs) {
     ++itrs;
-    // expansion (PUMP.cu:47-66)
     const int nG = gCount[Gidx];
     const auto tw = clk::now();
-    unsigned long long nn = 0;
-    if (nG > 0) {
-      PUMP_TRY(search_expand_scan(ctx_, sd, Gidx, nG, s_));
+    if (nG == 0) {  // nothing to expand: an empty wavefront (PUMP.cu:66-70)
+      if (itrs <= 32) res_->wavefront_sizes[itrs - 1] = 0;
+      break;
+    }
+    // expansion (PUMP.cu:47-66).  The wavefront size stays on the device:
+    // HSMC, pruning and storing read it there (and do nothing when the
+    // iteration would overflow the path store), so the host waits once per
+    // iteration, for the counters.
+    PUMP_TRY(search_expand_scan(ctx_, sd, Gidx, nG, s_));
+    PUMP_TRY(search_expand_write(sd, Gidx, nG, numPaths_, M, s_));
+    if (res_->wf_trace) {
+      unsigned long long nn = 0;
       PUMP_TRY(d2h(&nn, &d_ctl.p->num_new, 1));
       PUMP_TRY(sync());
-    }
-    if (nn > (unsigned long long)M) {
-      status = set_error(PUMP_ERR_CAPACITY, "wavefront exceeds maxPathCount %d", M);
-      break;
-    }
-    const int numNew = (int)nn;
-    if (itrs <= 32) res_->wavefront_sizes[itrs - 1] = numNew;
-    if (numNew == 0) break;
-    if (numPaths_ + numNew >= M) {
-      status = set_error(PUMP_ERR_CAPACITY, "paths exceed maxPathCount %d", M);
-      break;
-    }
-    PUMP_TRY(search_expand_write(sd, Gidx, nG, s_));
-    considered += numNew;
-    if (res_->wf_trace) {
-      trace_prev.resize(numNew);
-      trace_edge.resize(numNew);
-      PUMP_TRY(d2h(trace_prev.data(), d_wfPrev_.p, numNew));
-      PUMP_TRY(d2h(trace_edge.data(), d_wfEdge_.p, numNew));
+      const int nt = nn <= (unsigned long long)M && numPaths_ + (long long)nn < M ? (int)nn : 0;
+      trace_prev.resize(nt);
+      trace_edge.resize(nt);
+      PUMP_TRY(d2h(trace_prev.data(), d_wfPrev_.p, nt));
+      PUMP_TRY(d2h(trace_edge.data(), d_wfEdge_.p, nt));
       PUMP_TRY(sync());
-      for (int i = 0; i < numNew && res_->wf_trace_len + 2 <= res_->wf_trace_cap; ++i) {
+      for (int i = 0; i < nt && res_->wf_trace_len + 2 <= res_->wf_trace_cap; ++i) {
         res_->wf_trace[res_->wf_trace_len++] = trace_prev[i];
         res_->wf_trace[res_->wf_trace_len++] = trace_edge[i];
       }
     }
     // HSMC of the wavefront (PUMP.cu:82-160)
+    const unsigned long long *d_nn = &d_ctl.p->num_new;
+    const int *d_ovf = &d_ctl.p->overflow;
     if (hs_boxes_)
-      PUMP_TRY(hsmc_boxes_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
+      PUMP_TRY(hsmc_boxes_async(M, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
                                 d_disc_.p, maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
                                 pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p,
-                                d_stage_.p, P_, d_cpStage_.p, d_err_.p, s_));
+                                d_stage_.p, P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf));
     else
-      PUMP_TRY(hsmc_staged_async(numNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p,
+      PUMP_TRY(hsmc_staged_async(M, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p,
                                  d_bs_.p, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
                                  pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p,
-                                 d_stage_.p, P_, d_cpStage_.p, d_err_.p, d_hcount_.p, s_));
+                                 d_stage_.p, P_, d_cpStage_.p, d_err_.p, d_hcount_.p, s_, d_nn,
+                                 d_ovf));
     // cut-off, dominance, storing, buckets (PUMP.cu:164-256)
-    PUMP_TRY(search_prune(sd, numNew, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
-    PUMP_TRY(search_store(ctx_, sd, numNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
+    PUMP_TRY(search_prune(sd, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
+    PUMP_TRY(search_store(ctx_, sd, M, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
                           d_stage_.p, d_valid_.p, words_, s_));
     PUMP_TRY(d2h(&ctl, d_ctl.p, 1));
     PUMP_TRY(sync());
     res_->ms_explore_wait += ms_since(tw);
+    if (ctl.overflow == 1) {
+      status = set_error(PUMP_ERR_CAPACITY, "wavefront exceeds maxPathCount %d", M);
+      break;
+    }
+    const int numNew = (int)ctl.num_new;
+    if (itrs <= 32) res_->wavefront_sizes[itrs - 1] = numNew;
+    if (numNew == 0) break;
+    if (ctl.overflow == 2) {
+      status = set_error(PUMP_ERR_CAPACITY, "paths exceed maxPathCount %d", M);
+      break;
+    }
+    considered += numNew;
     if (ctl.wait_error) {
       status = set_error(PUMP_ERR_TIMEOUT, "search store: look-back wait exceeded its bound");
       break;

@@ -20,7 +20,15 @@ struct SearchCtl {
   int goal_found;                // a stored goal path has CP <= cpTarget / eta
   int g_base[2];                 // bucket sizes before this iteration's appends
   int wait_error;                // 1: a look-back wait of the store pass gave up
+  int overflow;                  // 1: wavefront > maxPathCount, 2: paths would reach it
+  int pad;
 };
+
+// The wavefront size the kernels after the expansion work on: 0 when the
+// iteration would overflow the path store.
+__device__ __forceinline__ int wave_size(const SearchCtl *ctl) {
+  return ctl->overflow ? 0 : (int)ctl->num_new;
+}
 
 // Device arrays of one search (capacities: M + 1 paths and new paths, N nodes).
 struct SearchDev {
@@ -51,18 +59,24 @@ pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n
                                  cudaStream_t s);
 // Writes the wavefront (PUMP.cu:47-66), empties bucket g_idx (recording the
 // bucket sizes the appends start from) and clears the per-node lists of new
-// paths at the wavefront's nodes.
-pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, cudaStream_t s);
+// paths at the wavefront's nodes.  The wavefront size is read from
+// ctl->num_new; a wavefront larger than max_paths, or one that would bring
+// the stored paths to max_paths, sets ctl->overflow and is not written
+// (PUMP.cu:62-64, 73-76).
+pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int num_paths,
+                                  int max_paths, cudaStream_t s);
 // New paths' time and cost, the CP cut-off (PUMP.cu:164-185) with per-node
 // lists of the survivors of the cut-off, then epsilon dominance
-// (PUMP.cu:188-218).
-pump_status_t search_prune(const SearchDev &sd, int num_new, int num_paths, float cp_cutoff,
-                           float eps_cp, float eps_cost, cudaStream_t s);
+// (PUMP.cu:188-218); wavefront size from the device (wave_size).
+pump_status_t search_prune(const SearchDev &sd, int num_paths, float cp_cutoff, float eps_cp,
+                           float eps_cost, cudaStream_t s);
 // One pass over the wavefront (PUMP.cu:221-282): survivors become stored
 // paths num_paths + rank in wavefront order, each is appended to its bucket
 // in the same order, linked into its node's list, goal-tested, and its
 // particle mask moves from the stage to its stored slot.
-pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int num_new, int num_paths,
+// Wavefront size from the device (wave_size); max_new bounds it (sizes the
+// tile status words).
+pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int max_new, int num_paths,
                            int g_idx, float cost_threshold, float dr, float cp_min_soln,
                            const uint32_t *stage, uint32_t *valid, int words, cudaStream_t s);
 
