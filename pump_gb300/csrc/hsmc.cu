@@ -474,7 +474,7 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
 }
 
 template <bool Boxes>
-__global__ void __launch_bounds__(kHsmcThreads) hsmc_kernel(const HsmcParams p) {
+__global__ void __launch_bounds__(kHsmcThreads, 4) hsmc_kernel(const HsmcParams p) {
   extern __shared__ float4 s_dyn4[];
   const int warp = threadIdx.x >> 5;
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
