@@ -103,7 +103,6 @@ __global__ void __launch_bounds__(256) free_edges_kernel(const float *__restrict
 // kFilterObs boxes, one bit each; no filter if a waypoint is NaN), then runs
 // the reference's per-segment tests over the remaining boxes in index order.
 constexpr int kFeThreads = 128;
-constexpr int kFilterObs = 128;
 
 __global__ void __launch_bounds__(kFeThreads) free_edges_staged_kernel(
     const float *__restrict__ obs, int numObs, const float *__restrict__ disc, long long E,

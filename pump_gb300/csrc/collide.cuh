@@ -8,6 +8,10 @@
 
 namespace pump {
 
+// Edge-level box filters keep one bit per box in registers for maps of up to
+// this many boxes (more boxes: every box is tested).
+constexpr int kFilterObs = 128;
+
 // Cooperative copy of the obstacle array into shared memory (48 B per box,
 // so 16-byte vector loads always apply when the base is 16-byte aligned).
 __device__ __forceinline__ void stage_obstacles(const float *__restrict__ obs, int numObs,

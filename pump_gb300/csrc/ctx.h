@@ -84,11 +84,6 @@ pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long lon
                              int *d_src, int *d_dst, float *d_copt, float *d_topt,
                              int *d_go_start, float *h_rn, long long *h_num_edges,
                              cudaStream_t stream);
-pump_status_t open_edges_device(Ctx *ctx, const uint8_t *d_free_e, const uint8_t *d_free_s,
-                                const int *d_src, const int *d_dst, const float *d_copt,
-                                const float *d_topt, long long E, int N, int *d_fid, int *d_fsrc,
-                                int *d_fdst, float *d_fcopt, float *d_ftopt, int *d_fgo,
-                                long long *h_count, cudaStream_t stream);
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                       int *d_count, int **d_error_out, cudaStream_t stream);
 pump_status_t particle_rowmax_async(const float *d_table, int P, int T, float *d_rowmax,

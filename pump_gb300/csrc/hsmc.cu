@@ -615,14 +615,6 @@ __global__ void mc_cp_finish_kernel(const int *__restrict__ hits, const int *__r
   if (len[k] > T_rows && error) atomicExch(error, (int)PUMP_ERR_CAPACITY);
 }
 
-__global__ void gather_words_kernel(const uint32_t *__restrict__ src, const int *__restrict__ map,
-                                    int n, int words, uint32_t *__restrict__ dst) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)n * words) return;
-  const int k = (int)(t / words), j = (int)(t - (long long)k * words);
-  dst[t] = src[(long long)map[k] * words + j];
-}
-
 }  // namespace
 
 pump_status_t particle_rowmax_async(const float *d_table, int P, int T, float *d_rowmax,
@@ -770,14 +762,6 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
       d_num_new ? (unsigned)(kNumSMs * 4) : grid_for((long long)num_new * 32, kHsmcThreads);
   hsmc_kernel<true><<<blocks, kHsmcThreads, smem, stream>>>(hp);
   return launch_status("hsmc_kernel (boxes)");
-}
-
-pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n, int words,
-                                 uint32_t *d_dst, cudaStream_t stream) {
-  if (n <= 0) return PUMP_OK;
-  const long long total = (long long)n * words;
-  gather_words_kernel<<<grid_for(total, 256), 256, 0, stream>>>(d_src, d_map, n, words, d_dst);
-  return launch_status("gather_words_kernel");
 }
 
 // Generates the tables on `stream`; the binary64 noise buffer (24 B per

@@ -35,14 +35,6 @@
 
 namespace pump {
 
-pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int *d_prev,
-                                long long num_edges, int num_prev, const float *d_as, const float *d_bs, int maxHS,
-                                const float *d_times, const float *d_topt, float dt,
-                                const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
-                                const uint32_t *d_valid_in, uint32_t *d_valid_out, int P,
-                                float *d_cp_out, int *d_error, const uint8_t *d_hs_count,
-                                cudaStream_t stream, const unsigned long long *d_num_new,
-                                const int *d_skip);
 bool hsmc_boxes_fits(int numObs, int W, int maxHS);
 pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int *d_prev,
                                long long num_edges, int num_prev, const float *d_obs, int numObs,
@@ -52,8 +44,6 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                                uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
                                cudaStream_t stream, const unsigned long long *d_num_new,
                                const int *d_skip);
-pump_status_t gather_words_async(const uint32_t *d_src, const int *d_map, int n, int words,
-                                 uint32_t *d_dst, cudaStream_t stream);
 pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
                           const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                           const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
@@ -140,9 +130,12 @@ struct SharedRoadmap {
 
 class Planner {
  public:
+  // lazy: check each node's out-edges when the search first reaches it (the
+  // batch's throughput form); otherwise all edges are checked up front (the
+  // latency form).  Results are the same.
   Planner(Ctx *ctx, const pump_problem &pb, pump_plan_result *res, cudaStream_t s,
-          const SharedRoadmap *shared = nullptr)
-      : ctx_(ctx), pb_(pb), res_(res), s_(s), shared_(shared) {}
+          const SharedRoadmap *shared = nullptr, bool lazy = false)
+      : ctx_(ctx), pb_(pb), res_(res), s_(s), shared_(shared), lazy_(lazy) {}
   pump_status_t run();
   // CP (dense path + MC over the table), smoothing cost and dense length of
   // explicit candidate paths (pump_path_cp).
@@ -188,6 +181,7 @@ class Planner {
   pump_plan_result *res_;
   cudaStream_t s_;
   const SharedRoadmap *shared_;
+  bool lazy_ = false;
   DevBuf<float> d_own_c_, d_own_t_;  // pairs touching init/goal (shared-roadmap path)
 
   // problem constants (mainPUMP.cu:51-72)
@@ -197,24 +191,23 @@ class Planner {
   const float epsCost_ = (float)0.0002, epsCP_ = (float)0.0002;
   int N_ = 0, W_ = 0, P_ = 0, words_ = 0, maxHS_ = 0, nobs_ = 0;
   float maxd2_ = 0;
-  bool hs_boxes_ = false;  // HSMC derives the half-spaces from the boxes
 
   std::vector<float> samples_;
   DevBuf<float> d_samples_, d_obs_, d_copts_, d_topts_;
   DevBuf<int> d_src_, d_dst_, d_go_;
-  DevBuf<float> d_coptE_, d_toptE_, d_disc_, d_as_, d_bs_;
+  DevBuf<float> d_coptE_, d_toptE_, d_disc_;
   const float *d_table_ = nullptr;   // context-cached particle table
   const float *d_rowmax_ = nullptr;  // its largest |offset| per row and axis
   const float *obs_p_ = nullptr;    // device obstacles used by the MC CP
-  DevBuf<uint8_t> d_free_s_, d_free_e_, d_hcount_;
+  DevBuf<uint8_t> d_free_s_, d_free_e_;
+  DevBuf<int> d_open_cnt_;  // per node: expandable edges, -1 until checked
+  DevBuf<int> d_todo_;      // nodes checked in an iteration
+  DevBuf<int> d_scalar_;    // one int read back with the roadmap
+  int max_degree_ = 0;      // largest out-degree of the roadmap
   long long E_ = 0;
   float rn_ = 0;
   DevBuf<float> d_h_;  // heuristic per node (cost to the goal)
   float h0_ = 0;
-  // the expandable edges (free, to a free node) in (source, destination)
-  // order: original edge id, destination, cost, time, and row starts per node
-  DevBuf<int> d_fid_, d_fsrc_, d_fdst_, d_fgo_;
-  DevBuf<float> d_fcopt_, d_ftopt_;
 
   // exploration state (mainPUMP.cu:623-681)
   int maxPathCount_ = 0;
@@ -263,12 +256,12 @@ pump_status_t Planner::run() {
 pump_status_t Planner::roadmap() {
   // the samples (then the goal state once more) on the device: Halton points
   // generated there, or the caller's samples uploaded through pinned memory.
-  // Pinned read-back (at the next synchronisation): h[0], then the Halton
-  // samples for the host's path reconstruction.
+  // Pinned read-back (at the roadmap's synchronisation): h[0], the largest
+  // out-degree, then the Halton samples for the host's path reconstruction.
   const size_t nsf = (size_t)N_ * kDim;
   PUMP_TRY(d_samples_.alloc(nsf + kDim));
   float *hout = nullptr;
-  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float) * (1 + nsf), (void **)&hout));
+  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float) * (2 + nsf), (void **)&hout));
   if (pb_.samples) {
     samples_.assign(pb_.samples, pb_.samples + nsf);
     float *hin = nullptr;
@@ -279,7 +272,7 @@ pump_status_t Planner::roadmap() {
                                   cudaMemcpyHostToDevice, s_));
   } else {
     PUMP_TRY(halton_samples_async(N_, pb_.lo, pb_.hi, pb_.init, pb_.goal, d_samples_.p, s_));
-    PUMP_CUDA_TRY(cudaMemcpyAsync(hout + 1, d_samples_.p, sizeof(float) * nsf,
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hout + 2, d_samples_.p, sizeof(float) * nsf,
                                   cudaMemcpyDeviceToHost, s_));
   }
   // heuristic h (mainPUMP.cu:351-355): cost of the optimal connection of
@@ -320,12 +313,16 @@ pump_status_t Planner::roadmap() {
     res_->rn = rn_;
   }
   res_->num_edges = E_;
+  // the edges' waypoints (findDiscretizedPath) are written by the search's
+  // edge checks, for the nodes it reaches
   PUMP_TRY(d_disc_.alloc((size_t)E_ * W_ * kDim));
-  PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, d_toptE_.p, E_, pb_.num_disc,
-                                 pb_.bvp_mode, d_disc_.p, (pump_stream_t)s_));
+  PUMP_TRY(d_scalar_.alloc(1));
+  PUMP_TRY(max_degree_async(d_go_.p, N_, d_scalar_.p, s_));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hout + 1, d_scalar_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
   PUMP_TRY(sync());
   h0_ = hout[0];
-  if (!pb_.samples) samples_.assign(hout + 1, hout + 1 + nsf);
+  std::memcpy(&max_degree_, hout + 1, sizeof(int));
+  if (!pb_.samples) samples_.assign(hout + 2, hout + 2 + nsf);
   return PUMP_OK;
 }
 
@@ -366,39 +363,41 @@ pump_status_t Planner::online() {
   PUMP_TRY(h2d(d_obs_.p, pb_.obstacles, (size_t)nobs_ * 12));
   obs_p_ = d_obs_.p;
   PUMP_TRY(d_free_s_.alloc(N_));
-  PUMP_TRY(d_free_e_.alloc(E_));
   PUMP_TRY(pump_sample_free(d_obs_.p, nobs_, d_samples_.p, N_, d_free_s_.p, (pump_stream_t)s_));
-  PUMP_TRY(pump_free_edges(d_obs_.p, nobs_, d_disc_.p, E_, pb_.num_disc, d_free_e_.p,
-                           (pump_stream_t)s_));
+  // freeEdges (mainPUMP.cu:364) and the waypoints it tests
+  // (findDiscretizedPath, mainPUMP.cu:339).  Lazy: the search checks the
+  // out-edges of each node when it first reaches it (search_check), so edges
+  // it never expands are not checked and nothing it reads differs.  Eager:
+  // all edges here, then every node's count of expandable edges.
+  PUMP_TRY(d_free_e_.alloc(E_));
+  PUMP_TRY(d_open_cnt_.alloc(N_));
+  PUMP_TRY(d_todo_.alloc(N_));
+  PUMP_CUDA_TRY(cudaMemsetAsync(d_open_cnt_.p, 0xFF, sizeof(int) * (size_t)N_, s_));  // -1
+  if (!lazy_) {
+    PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, d_toptE_.p, E_, pb_.num_disc,
+                                   pb_.bvp_mode, d_disc_.p, (pump_stream_t)s_));
+    PUMP_TRY(pump_free_edges(d_obs_.p, nobs_, d_disc_.p, E_, pb_.num_disc, d_free_e_.p,
+                             (pump_stream_t)s_));
+    SearchDev sd{};
+    sd.N = N_;
+    sd.go = d_go_.p;
+    sd.dst = d_dst_.p;
+    sd.free_s = d_free_s_.p;
+    sd.free_e = d_free_e_.p;
+    sd.open_cnt = d_open_cnt_.p;
+    PUMP_TRY(search_count_open(sd, s_));
+  }
   // maxd2 = 0.1*offsetMult*offsetMult evaluated in double (mainPUMP.cu:201)
   maxd2_ = (float)(0.1 * (double)pb_.offset_mult * (double)pb_.offset_mult);
-  // The half-spaces of cacheHalfspaces (mainPUMP.cu:366-374): derived by the
-  // HSMC kernel for the edges each wavefront propagates along when the boxes
-  // fit its shared-memory stage, else cached for every free edge up front
-  // (only the stored ones and their counts: the search reads no more).
-  hs_boxes_ = hsmc_boxes_fits(nobs_, W_, maxHS_);
-  if (!hs_boxes_) {
-    PUMP_TRY(d_as_.alloc((size_t)E_ * W_ * maxHS_ * 3));
-    PUMP_TRY(d_bs_.alloc((size_t)E_ * W_ * maxHS_));
-    PUMP_TRY(d_hcount_.alloc((size_t)E_ * W_));
-    PUMP_TRY(pump_cache_halfspaces_sparse(d_obs_.p, nobs_, d_disc_.p, d_free_e_.p, E_, W_, maxHS_,
-                                          maxd2_, d_as_.p, d_bs_.p, d_hcount_.p,
-                                          (pump_stream_t)s_));
-  }
+  // The half-spaces of cacheHalfspaces (mainPUMP.cu:366-374) are derived by
+  // the HSMC kernel for the edges each wavefront propagates along
+  if (!hsmc_boxes_fits(nobs_, W_, maxHS_))
+    return set_error(PUMP_ERR_CAPACITY,
+                     "%d boxes or %d waypoints x %d half-spaces exceed the HSMC shared-memory stage",
+                     nobs_, W_, maxHS_);
   PUMP_TRY(ctx_->particle_table(pb_.seed, pb_.num_mc, pb_.table_rows, &d_table_, s_));
   d_rowmax_ = d_table_ + 3 * (size_t)pb_.num_mc * pb_.table_rows;
-  const size_t cap = E_ > 0 ? (size_t)E_ : 1;
-  PUMP_TRY(d_fid_.alloc(cap));
-  PUMP_TRY(d_fsrc_.alloc(cap));
-  PUMP_TRY(d_fdst_.alloc(cap));
-  PUMP_TRY(d_fcopt_.alloc(cap));
-  PUMP_TRY(d_ftopt_.alloc(cap));
-  PUMP_TRY(d_fgo_.alloc(N_ + 1));
-  long long F = 0;
-  PUMP_TRY(open_edges_device(ctx_, d_free_e_.p, d_free_s_.p, d_src_.p, d_dst_.p, d_coptE_.p,
-                             d_toptE_.p, E_, N_, d_fid_.p, d_fsrc_.p, d_fdst_.p, d_fcopt_.p,
-                             d_ftopt_.p, d_fgo_.p, &F, s_));
-  return sync();
+  return PUMP_OK;
 }
 
 // The search loop (PUMP.cu:39-290) with its state on the device
@@ -449,11 +448,14 @@ pump_status_t Planner::explore() {
   SearchDev sd{};
   sd.N = N_;
   sd.goal = N_ - 1;
-  sd.fgo = d_fgo_.p;
-  sd.fid = d_fid_.p;
-  sd.fdst = d_fdst_.p;
-  sd.fcopt = d_fcopt_.p;
-  sd.ftopt = d_ftopt_.p;
+  sd.go = d_go_.p;
+  sd.dst = d_dst_.p;
+  sd.copt = d_coptE_.p;
+  sd.topt = d_toptE_.p;
+  sd.free_s = d_free_s_.p;
+  sd.free_e = d_free_e_.p;
+  sd.open_cnt = d_open_cnt_.p;
+  sd.todo = d_todo_.p;
   sd.h = d_h_.p;
   sd.path_prev = d_prev.p;
   sd.path_node = d_node.p;
@@ -478,6 +480,14 @@ pump_status_t Planner::explore() {
   sd.new_next = d_newnext.p;
   sd.ctl = d_ctl.p;
   PUMP_TRY(search_init(sd, s_));
+  CheckArgs ca{};
+  ca.samples = d_samples_.p;
+  ca.disc = d_disc_.p;
+  ca.numDisc = pb_.num_disc;
+  ca.mode = pb_.bvp_mode;
+  ca.obs = d_obs_.p;
+  ca.numObs = nobs_;
+  ca.max_degree = max_degree_;
 
   // PUMP.cu:10-35
   const float cpTarget = pb_.cp_target;
@@ -506,6 +516,7 @@ pump_status_t Planner::explore() {
     // HSMC, pruning and storing read it there (and do nothing when the
     // iteration would overflow the path store), so the host waits once per
     // iteration, for the counters.
+    if (lazy_) PUMP_TRY(search_check(sd, Gidx, nG, ca, s_));
     PUMP_TRY(search_expand_scan(ctx_, sd, Gidx, nG, s_));
     PUMP_TRY(search_expand_write(sd, Gidx, nG, numPaths_, M, s_));
     if (res_->wf_trace) {
@@ -526,17 +537,10 @@ pump_status_t Planner::explore() {
     // HSMC of the wavefront (PUMP.cu:82-160)
     const unsigned long long *d_nn = &d_ctl.p->num_new;
     const int *d_ovf = &d_ctl.p->overflow;
-    if (hs_boxes_)
-      PUMP_TRY(hsmc_boxes_async(M, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
-                                d_disc_.p, maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
-                                pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p,
-                                d_stage_.p, P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf));
-    else
-      PUMP_TRY(hsmc_staged_async(M, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_as_.p,
-                                 d_bs_.p, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
-                                 pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p,
-                                 d_stage_.p, P_, d_cpStage_.p, d_err_.p, d_hcount_.p, s_, d_nn,
-                                 d_ovf));
+    PUMP_TRY(hsmc_boxes_async(M, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
+                              d_disc_.p, maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
+                              pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p,
+                              P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf));
     // cut-off, dominance, storing, buckets (PUMP.cu:164-256)
     PUMP_TRY(search_prune(sd, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
     PUMP_TRY(search_store(ctx_, sd, M, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
@@ -1019,7 +1023,7 @@ using namespace pump;
 
 namespace pump {
 namespace {
-pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
+pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res, bool lazy,
                        pump_stream_t stream, const SharedRoadmap *shared) {
   if (!ctx || !pb || !res) return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: null argument");
   if (pb->N < 2 || pb->num_disc < 1 || pb->num_hsmc < 1 || pb->num_mc < pb->num_hsmc ||
@@ -1046,7 +1050,7 @@ pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *
   res->soln_path_idx = -1;
   Ctx *c = Ctx::from(ctx);
   PUMP_TRY(c->activate());
-  Planner planner(c, *pb, res, (cudaStream_t)stream, shared);
+  Planner planner(c, *pb, res, (cudaStream_t)stream, shared, lazy);
   return planner.run();
 }
 }  // namespace
@@ -1134,7 +1138,7 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
         const SharedRoadmap *g = nullptr;
         for (const auto &x : groups)
           if (x.M > 0 && x.matches(problems[k])) g = &x;
-        statuses[k] = plan_one(ctx, &problems[k], &results[k], (pump_stream_t)s, g);
+        statuses[k] = plan_one(ctx, &problems[k], &results[k], true, (pump_stream_t)s, g);
       }
     }
     if (s) cudaStreamDestroy(s);
@@ -1186,5 +1190,5 @@ extern "C" pump_status_t pump_path_cp(pump_ctx *ctx, const float *h_nodes, const
 
 extern "C" pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res,
                                    pump_stream_t stream) {
-  return plan_one(ctx, pb, res, stream, nullptr);
+  return plan_one(ctx, pb, res, false, stream, nullptr);
 }

@@ -8,9 +8,11 @@
 // order.
 #include "search.h"
 
+#include "collide.cuh"
 #include "common.cuh"
 #include "compact.cuh"
 #include "ctx.h"
+#include "pathpoint.cuh"
 
 namespace pump {
 namespace {
@@ -35,6 +37,7 @@ __global__ void search_init_kernel(SearchDev sd) {
     sd.ctl->g_base[1] = 0;
     sd.ctl->wait_error = 0;
     sd.ctl->overflow = 0;
+    sd.ctl->todo = 0;
   }
 }
 
@@ -43,12 +46,173 @@ __global__ void search_init_kernel(SearchDev sd) {
 __global__ void search_init_head_kernel(SearchDev sd) { sd.node_head[0] = 0; }
 
 struct ExpandCount {
-  const int *g, *path_node, *fgo;
+  const int *g, *path_node, *open_cnt;
   __device__ unsigned int operator()(long long i) const {
-    const int node = path_node[g[i]];
-    return (unsigned int)(fgo[node + 1] - fgo[node]);
+    return (unsigned int)open_cnt[path_node[g[i]]];
   }
 };
+
+// Nodes of the bucket's paths reached for the first time: the thread that
+// moves a node's count from -1 to 0 lists it for checking.
+__global__ void claim_kernel(SearchDev sd, const int *g, int n_g) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_g; k += gridDim.x * blockDim.x) {
+    const int node = sd.path_node[g[k]];
+    if (sd.open_cnt[node] == -1 && atomicCAS(&sd.open_cnt[node], -1, 0) == -1)
+      sd.todo[atomicAdd(&sd.ctl->todo, 1)] = node;
+  }
+}
+
+// Work items (listed node, chunk of kChkEdges out-edges), chunks per node
+// up to the roadmap's largest degree, taken by blocks in turn so a node of
+// high degree is spread over several blocks.  Per chunk the waypoints
+// (discretize_kernel's arithmetic) are computed one thread per (edge,
+// waypoint) into shared memory and stored to disc as whole lines (the
+// chunk's records are contiguous), then one thread per edge runs the
+// reference's collision test from shared memory (free_edges_staged_kernel's:
+// boxes broadphase-disjoint from the edge's bounding box dropped first, an
+// exact filter; none dropped for a NaN waypoint or more than kFilterObs
+// boxes).  Each chunk adds its count of free edges to free nodes to the
+// node's count.
+constexpr int kChkThreads = 256;
+constexpr int kChkEdges = 256;
+
+size_t check_smem(int numObs, int numDisc) {
+  return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)kChkEdges * (numDisc + 1) * kDim);
+}
+
+template <int Mode>
+__global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckArgs ca) {
+  extern __shared__ float4 s_dyn4[];
+  __shared__ int s_open[kChkThreads / 32];
+  float *s_obs = reinterpret_cast<float *>(s_dyn4);
+  const int numDisc = ca.numDisc, W = numDisc + 1;
+  float *s_wp = s_obs + ((ca.numObs * 12 + 3) & ~3);  // kChkEdges x W x 6
+  stage_obstacles(ca.obs, ca.numObs, s_obs);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n_todo = sd.ctl->todo;
+  const int chunks = ca.max_degree > kChkEdges ? (ca.max_degree + kChkEdges - 1) / kChkEdges : 1;
+  const long long items = (long long)n_todo * chunks;
+  for (long long j = blockIdx.x; j < items; j += gridDim.x) {
+    const int t = (int)(j / chunks), c = (int)(j - (long long)t * chunks);
+    const int node = sd.todo[t];
+    const int e1 = sd.go[node + 1];
+    const int c0 = sd.go[node] + c * kChkEdges;
+    if (c0 >= e1) continue;  // block-uniform: this node has fewer chunks
+    int open = 0;
+    {
+      const int ne = e1 - c0 < kChkEdges ? e1 - c0 : kChkEdges;
+      for (int q = threadIdx.x; q < ne * W; q += kChkThreads) {
+        const int el = q / W, i = q - el * W;
+        const int e = c0 + el;
+        const int b = sd.dst[e];
+        float x0[kDim], x1[kDim], x[kDim];
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) {
+          x0[d] = __ldg(&ca.samples[node * kDim + d]);
+          x1[d] = __ldg(&ca.samples[b * kDim + d]);
+        }
+        if (i == 0) {
+#pragma unroll
+          for (int d = 0; d < kDim; ++d) x[d] = x0[d];
+        } else if (i == numDisc) {
+#pragma unroll
+          for (int d = 0; d < kDim; ++d) x[d] = x1[d];
+        } else {
+          const float topt = sd.topt[e];
+          const float dt = topt / numDisc;
+          if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
+          else path_point_f32(dt * i, topt, x0, x1, x);
+        }
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) s_wp[q * kDim + d] = x[d];
+      }
+      __syncthreads();
+      block_store(ca.disc + (long long)c0 * W * kDim, s_wp, ne * W * kDim);
+      if (threadIdx.x < ne) {
+        const int e = c0 + threadIdx.x;
+        const float *wp = s_wp + threadIdx.x * W * kDim;
+        bool ok = true;
+        float v[3], w[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[d] = wp[d];
+        if (ca.numObs <= kFilterObs) {
+          float emin[3], emax[3];
+          bool nan = false;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
+          for (int i = 0; i < W; ++i)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              const float x = wp[i * kDim + d];
+              nan = nan || x != x;
+              emin[d] = fminf(emin[d], x);
+              emax[d] = fmaxf(emax[d], x);
+            }
+          uint32_t mask[kFilterObs / 32] = {0u, 0u, 0u, 0u};
+          const int words = (ca.numObs + 31) / 32;
+          for (int o = 0; o < ca.numObs; ++o)
+            if (nan || !broadphase_valid(emin, emax, &s_obs[o * 12])) mask[o >> 5] |= 1u << (o & 31);
+          for (int i = 0; i < numDisc && ok; ++i) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kDim + d];
+            ok = segment_valid_masked(v, w, mask, words, s_obs);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) v[d] = w[d];
+          }
+        } else {
+          for (int i = 0; i < numDisc && ok; ++i) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kDim + d];
+            ok = segment_valid(v, w, ca.numObs, s_obs);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) v[d] = w[d];
+          }
+        }
+        sd.free_e[e] = ok ? 1 : 0;
+        open += (ok && sd.free_s[sd.dst[e]]) ? 1 : 0;
+      }
+      __syncthreads();  // s_wp is rewritten by the next item
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) open += __shfl_xor_sync(0xffffffffu, open, o);
+    if (lane == 0) s_open[warp] = open;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int q = 0; q < kChkThreads / 32; ++q) tot += s_open[q];
+      if (tot) atomicAdd(&sd.open_cnt[node], tot);
+    }
+    __syncthreads();  // s_open is rewritten by the next item
+  }
+}
+
+// One warp per node: open_cnt[node] = its free edges to free nodes.
+__global__ void count_open_kernel(SearchDev sd) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x / 32);
+  for (long long n = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32; n < sd.N; n += warps) {
+    int c = 0;
+    for (int e = sd.go[n] + lane; e < sd.go[n + 1]; e += 32) c += (sd.free_e[e] && sd.free_s[sd.dst[e]]) ? 1 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) sd.open_cnt[n] = c;
+  }
+}
+
+__global__ void max_degree_kernel(const int *__restrict__ go, int N, int *out) {
+  __shared__ int s_max[32];
+  int m = 0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) m = max(m, go[i + 1] - go[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int r = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) r = max(r, s_max[q]);
+    *out = r;
+  }
+}
 
 // One warp per bucket entry: its node's expandable edges in order.  The
 // wavefront's nodes get empty lists of new paths; thread 0 empties bucket
@@ -67,23 +231,36 @@ __global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g, int g_i
     c->g_base[1 - g_idx] = c->g_count[1 - g_idx];
     c->num_valid = 0;
     c->overflow = ovf;
+    c->todo = 0;  // this iteration's checks have run
   }
   if (ovf) return;
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
+  const unsigned int lt = (1u << lane) - 1u;
   for (long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32; k < n_g; k += warps) {
     const int prev = g[k];
     const int node = sd.path_node[prev];
-    const int f0 = sd.fgo[node], cnt = sd.fgo[node + 1] - f0;
-    const unsigned int off = sd.wf_off[k];
-    for (int q = lane; q < cnt; q += 32) {
-      const int f = f0 + q;
-      const int dst = sd.fdst[f];
-      sd.wf_prev[off + q] = prev;
-      sd.wf_node[off + q] = dst;
-      sd.wf_edge[off + q] = sd.fid[f];
-      sd.wf_open[off + q] = f;
-      sd.new_head[dst] = -1;
+    const int e0 = sd.go[node], e1 = sd.go[node + 1];
+    unsigned int off = sd.wf_off[k];
+    // the node's expandable edges in edge order (PUMP.cu:52-53)
+    for (int c0 = e0; c0 < e1; c0 += 32) {
+      const int e = c0 + lane;
+      int dst = 0;
+      bool open = false;
+      if (e < e1) {
+        dst = sd.dst[e];
+        open = sd.free_e[e] && sd.free_s[dst];
+      }
+      const unsigned int bal = __ballot_sync(0xffffffffu, open);
+      if (open) {
+        const unsigned int q = off + __popc(bal & lt);
+        sd.wf_prev[q] = prev;
+        sd.wf_node[q] = dst;
+        sd.wf_edge[q] = e;
+        sd.wf_open[q] = e;
+        sd.new_head[dst] = -1;
+      }
+      off += __popc(bal);
     }
   }
 }
@@ -95,8 +272,8 @@ __global__ void new_paths_kernel(SearchDev sd, float cp_cutoff) {
   const int n = wave_size(sd.ctl);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int prev = sd.wf_prev[i], f = sd.wf_open[i];
-    sd.new_time[i] = sd.path_time[prev] + sd.ftopt[f];
-    sd.new_cost[i] = sd.path_cost[prev] + sd.fcopt[f];
+    sd.new_time[i] = sd.path_time[prev] + sd.topt[f];
+    sd.new_cost[i] = sd.path_cost[prev] + sd.copt[f];
     const bool alive = !(sd.new_cp[i] > cp_cutoff);
     sd.alive[i] = alive ? 1 : 0;
     if (alive) sd.new_next[i] = atomicExch(&sd.new_head[sd.wf_node[i]], i);
@@ -256,11 +433,51 @@ pump_status_t search_init(const SearchDev &sd, cudaStream_t s) {
   return launch_status("search_init_head");
 }
 
+pump_status_t search_check(const SearchDev &sd, int g_idx, int n_g, const CheckArgs &ca,
+                           cudaStream_t s) {
+  if (n_g <= 0) return PUMP_OK;
+  const size_t smem = check_smem(ca.numObs, ca.numDisc);
+  if (smem > 220 * 1024)
+    return set_error(PUMP_ERR_CAPACITY, "%d obstacles and %d waypoints exceed the check stage",
+                     ca.numObs, ca.numDisc + 1);
+  claim_kernel<<<grid_for(n_g, 256), 256, 0, s>>>(sd, sd.g_list[g_idx], n_g);
+  PUMP_TRY(launch_status("claim_kernel"));
+  // at most one block per (claimed node, chunk), no more than the GPU holds
+  const long long chunks =
+      ca.max_degree > kChkEdges ? (ca.max_degree + kChkEdges - 1) / kChkEdges : 1;
+  const long long want = (long long)n_g * chunks;
+  const unsigned blocks = (unsigned)(want < kNumSMs * 8 ? want : kNumSMs * 8);
+  if (ca.mode == PUMP_BVP_PARITY) {
+    if (smem > 48 * 1024)
+      PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)check_kernel<PUMP_BVP_PARITY>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    check_kernel<PUMP_BVP_PARITY><<<blocks, kChkThreads, smem, s>>>(sd, ca);
+  } else {
+    if (smem > 48 * 1024)
+      PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)check_kernel<PUMP_BVP_PRECISION>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    check_kernel<PUMP_BVP_PRECISION><<<blocks, kChkThreads, smem, s>>>(sd, ca);
+  }
+  return launch_status("check_kernel");
+}
+
+pump_status_t search_count_open(const SearchDev &sd, cudaStream_t s) {
+  long long blocks = ((long long)sd.N * 32 + 255) / 256;
+  if (blocks > kNumSMs * 16) blocks = kNumSMs * 16;
+  count_open_kernel<<<(unsigned)(blocks > 0 ? blocks : 1), 256, 0, s>>>(sd);
+  return launch_status("count_open_kernel");
+}
+
+pump_status_t max_degree_async(const int *d_go, int N, int *d_out, cudaStream_t s) {
+  max_degree_kernel<<<1, 1024, 0, s>>>(d_go, N, d_out);
+  return launch_status("max_degree_kernel");
+}
+
 pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n_g,
                                  cudaStream_t s) {
   TileScratch ts{};
-  return run_scan(ctx, n_g, ExpandCount{sd.g_list[g_idx], sd.path_node, sd.fgo}, sd.wf_off, s, &ts,
-                  &sd.ctl->num_new);
+  return run_scan(ctx, n_g, ExpandCount{sd.g_list[g_idx], sd.path_node, sd.open_cnt}, sd.wf_off, s,
+                  &ts, &sd.ctl->num_new);
 }
 
 pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int num_paths,

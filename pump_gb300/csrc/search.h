@@ -21,7 +21,7 @@ struct SearchCtl {
   int g_base[2];                 // bucket sizes before this iteration's appends
   int wait_error;                // 1: a look-back wait of the store pass gave up
   int overflow;                  // 1: wavefront > maxPathCount, 2: paths would reach it
-  int pad;
+  int todo;                      // nodes claimed for edge checks this iteration
 };
 
 // The wavefront size the kernels after the expansion work on: 0 when the
@@ -33,9 +33,17 @@ __device__ __forceinline__ int wave_size(const SearchCtl *ctl) {
 // Device arrays of one search (capacities: M + 1 paths and new paths, N nodes).
 struct SearchDev {
   int N, goal;
-  // the expandable edges (row starts per node, original id, destination, cost, time)
-  const int *fgo, *fid, *fdst;
-  const float *fcopt, *ftopt, *h;
+  // the roadmap's edges (row starts per node, destination, cost, time), the
+  // free-sample mask, and the edges' free mask and each node's count of
+  // expandable edges (free edges to a free node; -1: not checked yet), both
+  // filled when the search first reaches the node (0 from its claim on,
+  // counted up by the checks)
+  const int *go, *dst;
+  const float *copt, *topt, *h;
+  const uint8_t *free_s;
+  uint8_t *free_e;
+  int *open_cnt;
+  int *todo;  // nodes whose out-edges this iteration checks (capacity N)
   // stored paths
   int *path_prev, *path_node;
   float *path_cost, *path_time, *path_cp;
@@ -51,8 +59,32 @@ struct SearchDev {
   SearchCtl *ctl;
 };
 
+// What the edge checks of search_check need: the samples and the edges'
+// waypoint layout (disc[e][W][6], written here), the obstacles and the BVP
+// mode of the waypoints.
+struct CheckArgs {
+  const float *samples;
+  float *disc;
+  int numDisc, mode;
+  const float *obs;
+  int numObs;
+  int max_degree;  // largest out-degree of the roadmap
+};
+
 // Path 0 at the initial node in bucket 0 (PUMP.cu:19-34).
 pump_status_t search_init(const SearchDev &sd, cudaStream_t s);
+// The nodes of bucket g_idx's paths that the search reaches for the first
+// time get their out-edges checked (freeEdges, collisionCheck.cu:5-37, with
+// the waypoints of findDiscretizedPath written on the way) and their count
+// of expandable edges.  The reference checks every edge up front; the search
+// reads only these, so the wavefronts are the same.
+pump_status_t search_check(const SearchDev &sd, int g_idx, int n_g, const CheckArgs &ca,
+                           cudaStream_t s);
+// Every node's count of expandable edges from the full free-edge mask (the
+// eager form: all edges checked up front).
+pump_status_t search_count_open(const SearchDev &sd, cudaStream_t s);
+// Largest out-degree of a CSR with row starts go[0..N] into *d_out (device).
+pump_status_t max_degree_async(const int *d_go, int N, int *d_out, cudaStream_t s);
 // Expansion offsets of the n_g paths of bucket g_idx; the wavefront size
 // lands in ctl->num_new (n_g > 0).
 pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n_g,

@@ -170,25 +170,6 @@ __global__ void __launch_bounds__(1024) select_pick_kernel(SelectState *st, int 
 }
 
 // ------------------------------------------------------ compaction users
-// Edges the search can expand: free edge to a free node (PUMP.cu:52-53).
-struct OpenEdgePred {
-  const uint8_t *free_e, *free_s;
-  const int *dst;
-  __device__ bool operator()(long long e) const { return free_e[e] && free_s[dst[e]]; }
-};
-struct OpenEdgeEmit {
-  const int *src, *dst;
-  const float *copt, *topt;
-  int *f_id, *f_src, *f_dst;
-  float *f_copt, *f_topt;
-  __device__ void operator()(long long e, long long pos) const {
-    f_id[pos] = (int)e;
-    f_src[pos] = src[e];
-    f_dst[pos] = dst[e];
-    f_copt[pos] = copt[e];
-    f_topt[pos] = topt[e];
-  }
-};
 struct FlagPred {
   const uint8_t *flags;
   __device__ bool operator()(long long i) const { return flags[i] != 0; }
@@ -510,25 +491,6 @@ pump_status_t build_edges_device(Ctx *ctx, const float *d_copts, const float *d_
                                  cudaStream_t stream) {
   return edges_src(ctx, FlatSrc{d_copts}, FlatTopt{d_topts}, N, rn, max_edges, d_src, d_dst,
                    d_copt, d_topt, d_go_start, h_num_edges, stream);
-}
-
-// The expandable edges in (source, destination) order with their row starts
-// per source node: the adjacency the search walks, without the edges it
-// would skip.
-pump_status_t open_edges_device(Ctx *ctx, const uint8_t *d_free_e, const uint8_t *d_free_s,
-                                const int *d_src, const int *d_dst, const float *d_copt,
-                                const float *d_topt, long long E, int N, int *d_fid, int *d_fsrc,
-                                int *d_fdst, float *d_fcopt, float *d_ftopt, int *d_fgo,
-                                long long *h_count, cudaStream_t stream) {
-  TileScratch ts{};
-  PUMP_TRY(run_compact(ctx, E, OpenEdgePred{d_free_e, d_free_s, d_dst},
-                       OpenEdgeEmit{d_src, d_dst, d_copt, d_topt, d_fid, d_fsrc, d_fdst, d_fcopt,
-                                    d_ftopt},
-                       stream, &ts));
-  unsigned long long total = 0;
-  PUMP_TRY(finish_compact(ts, &total, stream));
-  *h_count = (long long)total;
-  return row_starts(d_fsrc, (long long)total, N, d_fgo, stream);
 }
 
 // Edges of one query of a batch from its pair view (same order and values as
