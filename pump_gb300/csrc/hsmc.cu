@@ -703,8 +703,10 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
   hp.error = d_error;
   hp.num_new_dev = d_num_new;
   hp.skip_dev = d_skip;
-  const unsigned blocks =
-      d_num_new ? (unsigned)(kNumSMs * 4) : grid_for((long long)num_new * 32, kHsmcThreads);
+  // with a device-side count, num_new bounds it
+  const long long want = ((long long)num_new * 32 + kHsmcThreads - 1) / kHsmcThreads;
+  const unsigned blocks = d_num_new ? (unsigned)(want < kNumSMs * 4 ? want : kNumSMs * 4)
+                                    : grid_for((long long)num_new * 32, kHsmcThreads);
   hsmc_kernel<false><<<blocks, kHsmcThreads, 0, stream>>>(hp);
   return launch_status("hsmc_kernel");
 }
@@ -758,8 +760,10 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
   if (smem > 48 * 1024)
     PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)hsmc_kernel<true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const unsigned blocks =
-      d_num_new ? (unsigned)(kNumSMs * 4) : grid_for((long long)num_new * 32, kHsmcThreads);
+  // with a device-side count, num_new bounds it
+  const long long want = ((long long)num_new * 32 + kHsmcThreads - 1) / kHsmcThreads;
+  const unsigned blocks = d_num_new ? (unsigned)(want < kNumSMs * 4 ? want : kNumSMs * 4)
+                                    : grid_for((long long)num_new * 32, kHsmcThreads);
   hsmc_kernel<true><<<blocks, kHsmcThreads, smem, stream>>>(hp);
   return launch_status("hsmc_kernel (boxes)");
 }

@@ -534,16 +534,19 @@ pump_status_t Planner::explore() {
         res_->wf_trace[res_->wf_trace_len++] = trace_edge[i];
       }
     }
-    // HSMC of the wavefront (PUMP.cu:82-160)
+    // HSMC of the wavefront (PUMP.cu:82-160).  The wavefront holds at most
+    // the bucket's paths times the largest out-degree (and at most M).
     const unsigned long long *d_nn = &d_ctl.p->num_new;
     const int *d_ovf = &d_ctl.p->overflow;
-    PUMP_TRY(hsmc_boxes_async(M, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
+    const long long bound = (long long)nG * (max_degree_ > 0 ? max_degree_ : 1);
+    const int maxNew = bound < M ? (int)bound : M;
+    PUMP_TRY(hsmc_boxes_async(maxNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
                               d_disc_.p, maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
                               pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p,
                               P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf));
     // cut-off, dominance, storing, buckets (PUMP.cu:164-256)
-    PUMP_TRY(search_prune(sd, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
-    PUMP_TRY(search_store(ctx_, sd, M, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
+    PUMP_TRY(search_prune(sd, maxNew, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
+    PUMP_TRY(search_store(ctx_, sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
                           d_stage_.p, d_valid_.p, words_, s_));
     PUMP_TRY(d2h(&ctl, d_ctl.p, 1));
     PUMP_TRY(sync());

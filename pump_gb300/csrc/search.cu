@@ -490,11 +490,13 @@ pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int n
   return launch_status("expand_write");
 }
 
-pump_status_t search_prune(const SearchDev &sd, int num_paths, float cp_cutoff, float eps_cp,
-                           float eps_cost, cudaStream_t s) {
-  new_paths_kernel<<<kNumSMs * 4, 256, 0, s>>>(sd, cp_cutoff);
+pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float cp_cutoff,
+                           float eps_cp, float eps_cost, cudaStream_t s) {
+  long long blocks = ((long long)(max_new > 0 ? max_new : 1) + 255) / 256;
+  if (blocks > kNumSMs * 4) blocks = kNumSMs * 4;
+  new_paths_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, cp_cutoff);
   PUMP_TRY(launch_status("new_paths"));
-  dominance_kernel<<<kNumSMs * 4, 256, 0, s>>>(sd, num_paths, eps_cp, eps_cost);
+  dominance_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, num_paths, eps_cp, eps_cost);
   return launch_status("dominance");
 }
 

@@ -99,9 +99,10 @@ pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int n
                                   int max_paths, cudaStream_t s);
 // New paths' time and cost, the CP cut-off (PUMP.cu:164-185) with per-node
 // lists of the survivors of the cut-off, then epsilon dominance
-// (PUMP.cu:188-218); wavefront size from the device (wave_size).
-pump_status_t search_prune(const SearchDev &sd, int num_paths, float cp_cutoff, float eps_cp,
-                           float eps_cost, cudaStream_t s);
+// (PUMP.cu:188-218); wavefront size from the device (wave_size), at most
+// max_new (sizes the grids).
+pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float cp_cutoff,
+                           float eps_cp, float eps_cost, cudaStream_t s);
 // One pass over the wavefront (PUMP.cu:221-282): survivors become stored
 // paths num_paths + rank in wavefront order, each is appended to its bucket
 // in the same order, linked into its node's list, goal-tested, and its
