@@ -117,6 +117,22 @@ pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src, co
                                     const float *d_topt, long long E, int numDisc, int mode,
                                     float *d_disc, pump_stream_t stream);
 
+/* -------------------------------------------------------------- tuning */
+/* Launch-shape autotuner.  Kernels with several launch shapes that compute
+ * the same results (the precision pair BVP's, the waypoints' and the edge
+ * check's block sizes; the grid of the large compactions) pick their shape
+ * per shape class (a size's power-of-two bucket, the waypoint count, the
+ * box count) on the device: the first call of a class runs every candidate
+ * twice on its own inputs, on its stream, and keeps the fastest second run.
+ * Records are process-wide.  pump_tune_enable(0) (or PUMP_TUNE=0 in the
+ * environment) switches tuning off: every kernel then uses its default
+ * shape; pump_tune_reset forgets the records.  pump_tune_report writes one
+ * line per record (kernel, class, choice, candidate times in ms) into buf
+ * (truncated to len - 1 characters) and returns the full length. */
+void pump_tune_enable(int on);
+void pump_tune_reset(void);
+int pump_tune_report(char *buf, size_t len);
+
 /* ------------------------------------------------------ collision checks */
 /* isFree[i] = sample i is not strictly inside any box (sampleFree,
  * sampler.cu:61-88).  obstacles: numObs x 12 floats (lo[6], hi[6]). */

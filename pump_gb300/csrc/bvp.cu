@@ -14,9 +14,12 @@
 // bvp_precise.cu, compiled with multiply-add contraction.
 #include <math.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "ctx.h"
 #include "pathpoint.cuh"
+#include "tune.h"
 
 namespace pump {
 namespace {
@@ -238,12 +241,12 @@ __global__ void bvp_batch_kernel(const BvpJobs jb) {
 // One thread per (edge, waypoint): findDiscretizedPath, 2pBVP.cu:53-69.  A
 // block's 256 waypoints are contiguous in disc, so they are assembled in
 // shared memory and stored as whole lines.
-constexpr int kDiscThreads = 256;
-
-template <int Mode>
-__global__ void __launch_bounds__(kDiscThreads) discretize_kernel(
+// The block size T (128, 256, 512) is picked by the autotuner.
+template <int Mode, int T>
+__global__ void __launch_bounds__(T) discretize_kernel(
     const float *__restrict__ samples, const int *__restrict__ src, const int *__restrict__ dst,
     const float *__restrict__ toptE, long long E, int numDisc, float *__restrict__ disc) {
+  constexpr int kDiscThreads = T;
   __shared__ __align__(16) float s_out[kDiscThreads * kDim];
   const int W = numDisc + 1;
   const long long base = blockIdx.x * (long long)kDiscThreads;
@@ -277,6 +280,15 @@ __global__ void __launch_bounds__(kDiscThreads) discretize_kernel(
   }
   __syncthreads();
   block_store(disc + base * kDim, s_out, nv * kDim);
+}
+
+template <int Mode, int T>
+pump_status_t discretize_launch(const float *d_samples, const int *d_src, const int *d_dst,
+                                const float *d_topt, long long E, int numDisc, float *d_disc,
+                                cudaStream_t s) {
+  discretize_kernel<Mode, T><<<grid_for(E * (numDisc + 1), T), T, 0, s>>>(d_samples, d_src, d_dst,
+                                                                         d_topt, E, numDisc, d_disc);
+  return launch_status("discretize_edges");
 }
 
 // Dense path of findOptimalPath (2pBVP.cu:5-36) for one segment: the host
@@ -522,14 +534,24 @@ extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int
       (E > 0 && (!d_samples || !d_src || !d_dst || !d_topt || !d_disc)))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_discretize_edges: bad arguments");
   if (E == 0) return PUMP_OK;
-  const long long n = E * (numDisc + 1);
-  if (mode == PUMP_BVP_PARITY)
-    discretize_kernel<PUMP_BVP_PARITY><<<grid_for(n, kDiscThreads), kDiscThreads, 0,
-                                         (cudaStream_t)stream>>>(
-        d_samples, d_src, d_dst, d_topt, E, numDisc, d_disc);
-  else
-    discretize_kernel<PUMP_BVP_PRECISION><<<grid_for(n, kDiscThreads), kDiscThreads, 0,
-                                            (cudaStream_t)stream>>>(
-        d_samples, d_src, d_dst, d_topt, E, numDisc, d_disc);
-  return launch_status("discretize_edges");
+  cudaStream_t s = (cudaStream_t)stream;
+  // block sizes 128, 256 (default), 512
+  auto go = [&](auto block) -> pump_status_t {
+    constexpr int T = decltype(block)::value;
+    return mode == PUMP_BVP_PARITY
+               ? discretize_launch<PUMP_BVP_PARITY, T>(d_samples, d_src, d_dst, d_topt, E, numDisc,
+                                                      d_disc, s)
+               : discretize_launch<PUMP_BVP_PRECISION, T>(d_samples, d_src, d_dst, d_topt, E,
+                                                         numDisc, d_disc, s);
+  };
+  auto run = [&](int c) -> pump_status_t {
+    if (c == 0) return go(std::integral_constant<int, 128>{});
+    if (c == 1) return go(std::integral_constant<int, 256>{});
+    return go(std::integral_constant<int, 512>{});
+  };
+  int choice = 1;
+  bool ran = false;
+  const uint64_t key = ((uint64_t)mode << 40) | ((uint64_t)numDisc << 32) | tune_bucket(E);
+  PUMP_TRY(tune_choice(kTuneDiscretize, key, 3, 1, s, run, &choice, &ran));
+  return ran ? PUMP_OK : run(choice);
 }

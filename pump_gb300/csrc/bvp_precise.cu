@@ -4,6 +4,7 @@
 // roundings).
 #include "common.cuh"
 #include "ctx.h"
+#include "tune.h"
 #include "precise.cuh"
 
 namespace pump {
@@ -37,12 +38,14 @@ __device__ __forceinline__ SampleF load_sample(const SampleF *__restrict__ s, in
   return r;
 }
 
-// Row i = blockIdx.y, column r = blockIdx.x * 128 + threadIdx.x (j = r, or
-// r + 1 past the diagonal): no index division per pair.
-__global__ void __launch_bounds__(128) bvp_pairs_precision_kernel(const SampleF *__restrict__ sf,
-                                                                  int N, float tmax,
-                                                                  float *__restrict__ copts,
-                                                                  float *__restrict__ topts) {
+// Row i = blockIdx.y, column r = blockIdx.x * T + threadIdx.x (j = r, or
+// r + 1 past the diagonal): no index division per pair.  The block size T is
+// picked by the autotuner.
+template <int T>
+__global__ void __launch_bounds__(T) bvp_pairs_precision_kernel(const SampleF *__restrict__ sf,
+                                                                int N, float tmax,
+                                                                float *__restrict__ copts,
+                                                                float *__restrict__ topts) {
   const int i = blockIdx.y;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= N - 1) return;
@@ -76,14 +79,25 @@ __global__ void bvp_batch_precision_kernel(const BvpJobs jb) {
 pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tmax, float *d_copts,
                                          float *d_topts, cudaStream_t stream) {
   if (N > 65535) return set_error(PUMP_ERR_CAPACITY, "bvp_pairs: N = %d exceeds 65535 rows", N);
-  const dim3 grid(grid_for(N - 1, 128), (unsigned)N);
   SampleF *sd = nullptr;
   PUMP_CUDA_TRY(pool_malloc_async((void **)&sd, sizeof(SampleF) * (size_t)N, stream));
   prepare_samples_kernel<<<grid_for(N, 128), 128, 0, stream>>>(d_samples, N, sd);
   pump_status_t st = launch_status("prepare_samples");
+  // block sizes 64, 128 (default), 256
+  auto run = [&](int c) -> pump_status_t {
+    const int T = c == 0 ? 64 : (c == 1 ? 128 : 256);
+    const dim3 grid(grid_for(N - 1, T), (unsigned)N);
+    if (c == 0) bvp_pairs_precision_kernel<64><<<grid, 64, 0, stream>>>(sd, N, tmax, d_copts, d_topts);
+    else if (c == 1)
+      bvp_pairs_precision_kernel<128><<<grid, 128, 0, stream>>>(sd, N, tmax, d_copts, d_topts);
+    else bvp_pairs_precision_kernel<256><<<grid, 256, 0, stream>>>(sd, N, tmax, d_copts, d_topts);
+    return launch_status("bvp_pairs_precision");
+  };
   if (st == PUMP_OK) {
-    bvp_pairs_precision_kernel<<<grid, 128, 0, stream>>>(sd, N, tmax, d_copts, d_topts);
-    st = launch_status("bvp_pairs_precision");
+    int choice = 1;
+    bool ran = false;
+    st = tune_choice(kTuneBvpPairs, tune_bucket(N), 3, 1, stream, run, &choice, &ran);
+    if (st == PUMP_OK && !ran) st = run(choice);
   }
   cudaFreeAsync(sd, stream);
   return st;

@@ -8,9 +8,12 @@
 // for operation (binary32, no contraction): broadphase on the segment's
 // bounding box, then the face-projection narrow phase with lambda not
 // clamped to [0, 1], as in collisionCheck.cu:104-143.
+#include <type_traits>
+
 #include "common.cuh"
 
 #include "collide.cuh"
+#include "tune.h"
 
 namespace pump {
 namespace {
@@ -97,16 +100,17 @@ __global__ void __launch_bounds__(256) free_edges_kernel(const float *__restrict
   is_free[e] = ok ? 1 : 0;
 }
 
-// freeEdges for a block of 128 consecutive edges whose waypoints (contiguous
+// freeEdges for a block of T consecutive edges whose waypoints (contiguous
 // in disc) are staged in shared memory.  Each thread first drops the boxes
 // that are broadphase-disjoint from its edge's bounding box (up to
 // kFilterObs boxes, one bit each; no filter if a waypoint is NaN), then runs
 // the reference's per-segment tests over the remaining boxes in index order.
-constexpr int kFeThreads = 128;
-
-__global__ void __launch_bounds__(kFeThreads) free_edges_staged_kernel(
+// The block size T (64, 128, 256) is picked by the autotuner.
+template <int T>
+__global__ void __launch_bounds__(T) free_edges_staged_kernel(
     const float *__restrict__ obs, int numObs, const float *__restrict__ disc, long long E,
     int numDisc, uint8_t *__restrict__ is_free) {
+  constexpr int kFeThreads = T;
   extern __shared__ float4 s_dyn4[];
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   float *s_wp = s_obs + ((numObs * 12 + 3) & ~3);
@@ -397,13 +401,29 @@ extern "C" pump_status_t pump_free_edges(const float *d_obstacles, int numObs, c
   if (E == 0) return PUMP_OK;
   size_t smem;
   PUMP_TRY(obstacle_smem(numObs, &smem));
-  const size_t staged = sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) +
-                                         (size_t)kFeThreads * (numDisc + 1) * kDim);
-  if (staged <= 220 * 1024) {
-    PUMP_TRY(set_smem_attr((const void *)free_edges_staged_kernel, staged));
-    free_edges_staged_kernel<<<grid_for(E, kFeThreads), kFeThreads, staged, (cudaStream_t)stream>>>(
-        d_obstacles, numObs, d_disc, E, numDisc, d_is_free);
-    return launch_status("free_edges");
+  auto staged = [&](int T) {
+    return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)T * (numDisc + 1) * kDim);
+  };
+  if (staged(256) <= 220 * 1024) {
+    cudaStream_t s = (cudaStream_t)stream;
+    auto go = [&](auto block) -> pump_status_t {
+      constexpr int T = decltype(block)::value;
+      PUMP_TRY(set_smem_attr((const void *)free_edges_staged_kernel<T>, staged(T)));
+      free_edges_staged_kernel<T><<<grid_for(E, T), T, staged(T), s>>>(d_obstacles, numObs, d_disc,
+                                                                      E, numDisc, d_is_free);
+      return launch_status("free_edges");
+    };
+    // block sizes 64, 128 (default), 256
+    auto run = [&](int c) -> pump_status_t {
+      if (c == 0) return go(std::integral_constant<int, 64>{});
+      if (c == 1) return go(std::integral_constant<int, 128>{});
+      return go(std::integral_constant<int, 256>{});
+    };
+    int choice = 1;
+    bool ran = false;
+    const uint64_t key = ((uint64_t)numDisc << 32) | tune_bucket(numObs);
+    PUMP_TRY(tune_choice(kTuneFreeEdges, key, 3, 1, s, run, &choice, &ran));
+    return ran ? PUMP_OK : run(choice);
   }
   PUMP_TRY(set_smem_attr((const void *)free_edges_kernel, smem));
   free_edges_kernel<<<grid_for(E, 256), 256, smem, (cudaStream_t)stream>>>(d_obstacles, numObs,

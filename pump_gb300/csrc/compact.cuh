@@ -12,6 +12,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "tune.h"
 
 namespace pump {
 namespace {
@@ -369,15 +370,17 @@ __global__ void __launch_bounds__(kCompactThreads) tile_emit_kernel(
 }
 
 // Three-kernel compaction of n items; the count lands in *ts_out->total (the
-// error word stays zero: nothing waits).
+// error word stays zero: nothing waits).  blocks_per_sm sets the count and
+// emit grids (the autotuner's choice where a caller tunes it).
 template <class L>
 pump_status_t run_chunked(Ctx *ctx, long long n, const L &ld, cudaStream_t stream,
-                          TileScratch *ts_out) {
+                          TileScratch *ts_out, int blocks_per_sm = kTileBlocks / kNumSMs) {
   TileScratch ts{};
   long long ntiles = 0;
   PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));  // zeroed status words hold the counts
   if (n > 0) {
-    const unsigned blocks = (unsigned)(ntiles < kTileBlocks ? ntiles : kTileBlocks);
+    const long long grid = (long long)kNumSMs * blocks_per_sm;
+    const unsigned blocks = (unsigned)(ntiles < grid ? ntiles : grid);
     unsigned int *counts = reinterpret_cast<unsigned int *>(ts.status);
     tile_count_kernel<<<blocks, kCompactThreads, 0, stream>>>(n, ld, counts);
     PUMP_TRY(launch_status("tile_count_kernel"));
@@ -388,6 +391,19 @@ pump_status_t run_chunked(Ctx *ctx, long long n, const L &ld, cudaStream_t strea
   }
   *ts_out = ts;
   return PUMP_OK;
+}
+
+// run_chunked with the grid picked by the autotuner (2, 4 or 8 blocks per SM)
+// for shape class (kernel, the input size's power-of-two bucket).
+template <class L>
+pump_status_t run_chunked_tuned(Ctx *ctx, int kernel, long long n, const L &ld,
+                                cudaStream_t stream, TileScratch *ts_out) {
+  static const int kPerSm[3] = {2, 4, 8};
+  auto run = [&](int c) { return run_chunked(ctx, n, ld, stream, ts_out, kPerSm[c]); };
+  int choice = 1;
+  bool ran = false;
+  PUMP_TRY(tune_choice(kernel, tune_bucket(n), 3, 1, stream, run, &choice, &ran));
+  return ran ? PUMP_OK : run(choice);
 }
 
 // go_start[r] = the first edge whose source is >= r (edges sorted by source),

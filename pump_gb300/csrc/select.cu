@@ -471,10 +471,10 @@ pump_status_t edges_src(Ctx *ctx, Src src, Topt tsrc, int N, float rn, long long
                         long long *h_num_edges, cudaStream_t stream) {
   const long long npairs = (long long)N * (N - 1);
   TileScratch ts{};
-  PUMP_TRY(run_chunked(ctx, npairs,
-                       EdgeLoader<Src, Topt>{src, tsrc, N, rn, max_edges, d_src, d_dst, d_copt,
-                                             d_topt},
-                       stream, &ts));
+  PUMP_TRY(run_chunked_tuned(ctx, kTuneCompactEdges, npairs,
+                             EdgeLoader<Src, Topt>{src, tsrc, N, rn, max_edges, d_src, d_dst,
+                                                   d_copt, d_topt},
+                             stream, &ts));
   unsigned long long total = 0;
   PUMP_TRY(finish_compact(ts, &total, stream));
   *h_num_edges = (long long)total;
@@ -531,9 +531,9 @@ pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, lon
   bracket_kernel<<<1, 1024, 0, stream>>>(src, n, (unsigned int)rank, d_key_hi);
   PUMP_TRY(launch_status("bracket_kernel"));
   TileScratch ts{};
-  PUMP_TRY(run_chunked(ctx, n,
-                       SupersetLoader<Src>{src, N, d_key_hi, cap, sup_idx, (uint32_t *)sup_c},
-                       stream, &ts));
+  PUMP_TRY(run_chunked_tuned(ctx, kTuneCompactRn, n,
+                             SupersetLoader<Src>{src, N, d_key_hi, cap, sup_idx, (uint32_t *)sup_c},
+                             stream, &ts));
   const float *d_rn = nullptr;
   PUMP_TRY(select_kth_src(ctx, FlatSrc{sup_c}, cap, k, &d_rn, stream, ts.total));
   rn_pack_kernel<<<1, 1, 0, stream>>>(d_rn, ts.total, d_pack);
@@ -546,10 +546,10 @@ pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, lon
   std::memcpy(&rn, &pk.rn_bits, sizeof rn);
   *h_rn = rn;
   TileScratch ts2{};
-  PUMP_TRY(run_chunked(ctx, (long long)pk.n_sup,
-                       SupEdgeLoader<Topt>{sup_idx, sup_c, tsrc, N, rn, max_edges, d_src, d_dst,
-                                           d_copt, d_topt},
-                       stream, &ts2));
+  PUMP_TRY(run_chunked_tuned(ctx, kTuneCompactEdges, (long long)pk.n_sup,
+                             SupEdgeLoader<Topt>{sup_idx, sup_c, tsrc, N, rn, max_edges, d_src,
+                                                 d_dst, d_copt, d_topt},
+                             stream, &ts2));
   unsigned long long total = 0;
   PUMP_TRY(finish_compact(ts2, &total, stream));
   *h_num_edges = (long long)total;
