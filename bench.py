@@ -562,6 +562,11 @@ BVP_FP64_FLOPS_PER_PAIR = {"precision": 28.0, "parity": 40.0 * 23 + 20.0}
 # over one launch of the N = 4000 workload / its pairs), and DRAM bytes per
 # launch (dram__bytes_read.sum + dram__bytes_write.sum of the same launch).
 BVP_PRECISION_WARP_INST_PER_PAIR = 42.5
+# ncu smsp__inst_executed.sum on indoor4000 (profiles/kernels_indoor4000.md):
+# the edge check at block size 64 (the autotuner's choice there), per edge;
+# the waypoint kernel (any block size), per waypoint
+FREE_EDGES_WARP_INST_PER_EDGE_N4000 = 105558981 / 799800
+DISCRETIZE_WARP_INST_PER_WAYPOINT = 56798362 / (799800 * 9)
 BVP_PRECISION_DRAM_BYTES_N4000 = 0.16e6 + 66.71e6
 SMSP_PER_SM = 4
 NUM_SMS = 152
@@ -599,6 +604,14 @@ def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops, sm_mhz):
         issue = BVP_PRECISION_WARP_INST_PER_PAIR * pairs / t_bvp / 1e9
         table["bvp_pairs"] = {"bound": "issue", "achieved_ginst": round(issue, 1),
                               "frac": round(issue / issue_peak, 4)}
+    if mode == "precision" and N == 4000:
+        for k, units, per in (("free_edges", E, FREE_EDGES_WARP_INST_PER_EDGE_N4000),
+                              ("discretize", E * W, DISCRETIZE_WARP_INST_PER_WAYPOINT)):
+            if ks.get(k, 0) > 0:
+                g = per * units / (ks[k] / 1e3) / 1e9
+                table[k + "_issue"] = {"bound": "issue", "achieved_ginst": round(g, 1),
+                                       "frac": round(g / issue_peak, 4),
+                                       "warp_inst_per_unit": round(per, 2)}
     if dom == "bvp_pairs" and mode == "precision" and N == 4000:
         return {"kernel": dom, "bound": "issue", "achieved": issue, "peak": issue_peak,
                 "unit": "G warp-instructions/s", "frac": issue / issue_peak,

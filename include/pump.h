@@ -406,12 +406,15 @@ pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result 
  * order from a shared counter, so one query's kernels and copies overlap
  * another's host-side search.  results[k] is filled as pump_plan fills it
  * (its path/nodes buffers are the caller's) and statuses[k] receives query
- * k's status.  Returns PUMP_OK when every query ran, whatever its own status.
+ * k's status.  Returns PUMP_OK when every query ran, whatever its own status;
+ * pump_last_error() then names the first query (in query order) that failed
+ * with an error other than PUMP_ERR_NO_SOLUTION, and its message.
  * Queries with Halton samples (samples == NULL) that share a BVP mode and
  * state bounds share one roadmap: Halton point n depends on n and the bounds
  * only, so the pair BVPs of points 1 .. max(N)-2 are computed once per group
- * and each query adds only its 4N-6 pairs touching init or goal.  Results are
- * identical to pump_plan's.
+ * and each query adds only its 4N-6 pairs touching init or goal.  A query's
+ * edges are checked when its search first reaches their source node (its
+ * other edges are never checked).  Results are identical to pump_plan's.
  * The reference plans one query per process run (mainPUMP.cu:82-712). */
 pump_status_t pump_plan_batch(int device, const pump_problem *problems, pump_plan_result *results,
                               pump_status_t *statuses, int n, int workers);

@@ -131,6 +131,25 @@ cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t stream) {
   return cudaMallocFromPoolAsync(p, bytes, pool, stream);
 }
 
+pump_status_t smem_attr(const void *fn, size_t bytes) {
+  if (bytes <= 48 * 1024) return PUMP_OK;
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<int, const void *>, size_t>> set;
+  int dev = 0;
+  PUMP_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  for (auto &e : set)
+    if (e.first.first == dev && e.first.second == fn) {
+      if (e.second >= bytes) return PUMP_OK;
+      PUMP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      e.second = bytes;
+      return PUMP_OK;
+    }
+  PUMP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  set.push_back({{dev, fn}, bytes});
+  return PUMP_OK;
+}
+
 pump_status_t Ctx::activate() { return cuda_status(cudaSetDevice(device_), "cudaSetDevice"); }
 
 pump_status_t Ctx::scratch(int slot, size_t bytes, void **out) {

@@ -100,8 +100,8 @@ __global__ void __launch_bounds__(256) free_edges_kernel(const float *__restrict
   is_free[e] = ok ? 1 : 0;
 }
 
-// freeEdges for a block of T consecutive edges whose waypoints (contiguous
-// in disc) are staged in shared memory.  Each thread first drops the boxes
+// freeEdges for a block of T consecutive edges whose waypoint positions
+// (contiguous in disc) are staged in shared memory.  Each thread first drops the boxes
 // that are broadphase-disjoint from its edge's bounding box (up to
 // kFilterObs boxes, one bit each; no filter if a waypoint is NaN), then runs
 // the reference's per-segment tests over the remaining boxes in index order.
@@ -118,11 +118,18 @@ __global__ void __launch_bounds__(T) free_edges_staged_kernel(
   const int W = numDisc + 1;
   const long long e0 = blockIdx.x * (long long)kFeThreads;
   const int nv = (int)(E - e0 < kFeThreads ? E - e0 : kFeThreads);
-  block_load(s_wp, disc + e0 * W * kDim, nv * W * kDim);
+  {  // the block's waypoints are contiguous in disc; keep their positions
+    const float *src = disc + e0 * W * kDim;
+    for (int q = threadIdx.x; q < nv * W * kDim; q += kFeThreads) {
+      const int r = q / kDim, d = q - r * kDim;
+      if (d < 3) s_wp[r * 3 + d] = __ldg(&src[q]);
+    }
+  }
   __syncthreads();
   const int t = threadIdx.x;
   if (t >= nv) return;
-  const float *wp = s_wp + t * W * kDim;
+  constexpr int kPos = 3;  // floats per staged waypoint
+  const float *wp = s_wp + t * W * kPos;
   bool ok = true;
   float v[3], w[3];
 #pragma unroll
@@ -135,7 +142,7 @@ __global__ void __launch_bounds__(T) free_edges_staged_kernel(
     for (int i = 0; i < W; ++i)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const float x = wp[i * kDim + d];
+        const float x = wp[i * kPos + d];
         nan = nan || x != x;
         emin[d] = fminf(emin[d], x);
         emax[d] = fmaxf(emax[d], x);
@@ -148,7 +155,7 @@ __global__ void __launch_bounds__(T) free_edges_staged_kernel(
       if (nan || !broadphase_valid(emin, emax, &s_obs[o * 12])) mask[o >> 5] |= 1u << (o & 31);
     for (int i = 0; i < numDisc && ok; ++i) {
 #pragma unroll
-      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kDim + d];
+      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
       ok = segment_valid_masked(v, w, mask, words, s_obs);
 #pragma unroll
       for (int d = 0; d < 3; ++d) v[d] = w[d];
@@ -156,7 +163,7 @@ __global__ void __launch_bounds__(T) free_edges_staged_kernel(
   } else {
     for (int i = 0; i < numDisc && ok; ++i) {
 #pragma unroll
-      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kDim + d];
+      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
       ok = segment_valid(v, w, numObs, s_obs);
 #pragma unroll
       for (int d = 0; d < 3; ++d) v[d] = w[d];
@@ -353,12 +360,6 @@ pump_status_t obstacle_smem(int numObs, size_t *bytes) {
   return PUMP_OK;
 }
 
-pump_status_t set_smem_attr(const void *fn, size_t bytes) {
-  if (bytes > 48 * 1024)
-    PUMP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  return PUMP_OK;
-}
-
 }  // namespace
 
 pump_status_t halton_samples_async(int N, const float *lo, const float *hi, const float *init,
@@ -386,7 +387,7 @@ extern "C" pump_status_t pump_sample_free(const float *d_obstacles, int numObs,
   if (N == 0) return PUMP_OK;
   size_t smem;
   PUMP_TRY(obstacle_smem(numObs, &smem));
-  PUMP_TRY(set_smem_attr((const void *)sample_free_kernel, smem));
+  PUMP_TRY(smem_attr((const void *)sample_free_kernel, smem));
   sample_free_kernel<<<grid_for(N, 256), 256, smem, (cudaStream_t)stream>>>(d_obstacles, numObs,
                                                                           d_samples, N, d_is_free);
   return launch_status("sample_free");
@@ -402,13 +403,13 @@ extern "C" pump_status_t pump_free_edges(const float *d_obstacles, int numObs, c
   size_t smem;
   PUMP_TRY(obstacle_smem(numObs, &smem));
   auto staged = [&](int T) {
-    return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)T * (numDisc + 1) * kDim);
+    return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)T * (numDisc + 1) * 3);
   };
   if (staged(256) <= 220 * 1024) {
     cudaStream_t s = (cudaStream_t)stream;
     auto go = [&](auto block) -> pump_status_t {
       constexpr int T = decltype(block)::value;
-      PUMP_TRY(set_smem_attr((const void *)free_edges_staged_kernel<T>, staged(T)));
+      PUMP_TRY(smem_attr((const void *)free_edges_staged_kernel<T>, staged(T)));
       free_edges_staged_kernel<T><<<grid_for(E, T), T, staged(T), s>>>(d_obstacles, numObs, d_disc,
                                                                       E, numDisc, d_is_free);
       return launch_status("free_edges");
@@ -425,7 +426,7 @@ extern "C" pump_status_t pump_free_edges(const float *d_obstacles, int numObs, c
     PUMP_TRY(tune_choice(kTuneFreeEdges, key, 3, 1, s, run, &choice, &ran));
     return ran ? PUMP_OK : run(choice);
   }
-  PUMP_TRY(set_smem_attr((const void *)free_edges_kernel, smem));
+  PUMP_TRY(smem_attr((const void *)free_edges_kernel, smem));
   free_edges_kernel<<<grid_for(E, 256), 256, smem, (cudaStream_t)stream>>>(d_obstacles, numObs,
                                                                          d_disc, E, numDisc,
                                                                          d_is_free);
@@ -449,14 +450,14 @@ extern "C" pump_status_t pump_cache_halfspaces(const float *d_obstacles, int num
   PUMP_TRY(obstacle_smem(numObs, &smem));
   const size_t staged = halfspace_staged_smem(numObs, maxHS, true);
   if (maxHS <= kStagedMaxHS && staged <= 220 * 1024) {
-    PUMP_TRY(set_smem_attr((const void *)halfspace_staged_kernel<true>, staged));
+    PUMP_TRY(smem_attr((const void *)halfspace_staged_kernel<true>, staged));
     halfspace_staged_kernel<true><<<grid_for(E * W, kHsThreads), kHsThreads, staged,
                                     (cudaStream_t)stream>>>(
         d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, d_count,
         nullptr);
     return launch_status("cache_halfspaces");
   }
-  PUMP_TRY(set_smem_attr((const void *)halfspace_kernel, smem));
+  PUMP_TRY(smem_attr((const void *)halfspace_kernel, smem));
   halfspace_kernel<<<grid_for(E * W, 256), 256, smem, (cudaStream_t)stream>>>(
       d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, d_count);
   return launch_status("cache_halfspaces");
@@ -480,7 +481,7 @@ extern "C" pump_status_t pump_cache_halfspaces_sparse(const float *d_obstacles, 
   const size_t staged = halfspace_staged_smem(numObs, maxHS, false);
   if (staged > 220 * 1024)
     return set_error(PUMP_ERR_CAPACITY, "%d obstacles exceed the shared-memory stage", numObs);
-  PUMP_TRY(set_smem_attr((const void *)halfspace_staged_kernel<false>, staged));
+  PUMP_TRY(smem_attr((const void *)halfspace_staged_kernel<false>, staged));
   halfspace_staged_kernel<false><<<grid_for(E * W, kHsThreads), kHsThreads, staged,
                                    (cudaStream_t)stream>>>(
       d_obstacles, numObs, d_disc, d_is_free_edge, E, W, maxHS, maxd2, d_as, d_bs, nullptr,

@@ -26,6 +26,11 @@ pump_status_t launch_status(const char *kernel);
 // (freed with cudaFreeAsync); the pool keeps freed memory for reuse instead
 // of returning it to the driver at every synchronisation.
 cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t stream);
+// Opts kernel fn in to `bytes` of dynamic shared memory on the current
+// device.  The attribute is set only when the size grows, under a process-
+// wide lock, so host threads that launch the same kernel at once never
+// change it under one another's launches.
+pump_status_t smem_attr(const void *fn, size_t bytes);
 
 #define PUMP_CUDA_TRY(expr)                                     \
   do {                                                          \

@@ -637,9 +637,7 @@ pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const 
     smem = sizeof(float) * (size_t)((numObs * 12 + 3) & ~3);
     if (smem > 200 * 1024) return set_error(PUMP_ERR_CAPACITY, "mc_cp: %d obstacles", numObs);
   }
-  if (smem > 48 * 1024)
-    PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)mc_cp_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PUMP_TRY(smem_attr((const void *)mc_cp_kernel, smem));
   for (int k0 = 0; k0 < n_paths; k0 += 65535) {
     const int nk = n_paths - k0 < 65535 ? n_paths - k0 : 65535;
     dim3 grid(grid_for(Pmc, 32), (unsigned)nk);
@@ -757,9 +755,7 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
   hp.num_new_dev = d_num_new;
   hp.skip_dev = d_skip;
   const size_t smem = hsmc_boxes_smem(numObs);
-  if (smem > 48 * 1024)
-    PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)hsmc_kernel<true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PUMP_TRY(smem_attr((const void *)hsmc_kernel<true>, smem));
   // with a device-side count, num_new bounds it
   const long long want = ((long long)num_new * 32 + kHsmcThreads - 1) / kHsmcThreads;
   const unsigned blocks = d_num_new ? (unsigned)(want < kNumSMs * 4 ? want : kNumSMs * 4)

@@ -22,6 +22,7 @@
 #include <atomic>
 #include <chrono>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <cmath>
 #include <cstring>
@@ -1127,6 +1128,10 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
   std::atomic<int> next(0);
   std::vector<pump_status_t> setup(workers, PUMP_OK);
   std::vector<std::string> msgs(workers);
+  // the message of the first query (in query order) that failed
+  std::mutex fail_mu;
+  int first_fail = n;
+  std::string fail_msg;
   auto worker = [&](int w) {
     pump_ctx *ctx = nullptr;
     pump_status_t st = pump_ctx_create(device, &ctx);
@@ -1142,6 +1147,13 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
         for (const auto &x : groups)
           if (x.M > 0 && x.matches(problems[k])) g = &x;
         statuses[k] = plan_one(ctx, &problems[k], &results[k], true, (pump_stream_t)s, g);
+        if (statuses[k] != PUMP_OK && statuses[k] != PUMP_ERR_NO_SOLUTION) {
+          std::lock_guard<std::mutex> lk(fail_mu);
+          if (k < first_fail) {
+            first_fail = k;
+            fail_msg = pump_last_error();
+          }
+        }
       }
     }
     if (s) cudaStreamDestroy(s);
@@ -1154,6 +1166,7 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
   cleanup();
   for (int w = 0; w < workers; ++w)
     if (setup[w] != PUMP_OK) return set_error(setup[w], "pump_plan_batch worker %d: %s", w, msgs[w].c_str());
+  if (first_fail < n) set_error(PUMP_OK, "query %d: %s", first_fail, fail_msg.c_str());
   return PUMP_OK;
 }
 

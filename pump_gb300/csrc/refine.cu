@@ -402,11 +402,7 @@ pump_status_t check_args(const pump_refine_args *a, const char *fn) {
 template <bool Grad, int M>
 pump_status_t launch(const pump_refine_args &a, const Work &w, cudaStream_t stream) {
   const size_t smem = (size_t)a.num_obstacles * 6 * sizeof(float);
-  if (smem > 48 * 1024) {
-    cudaError_t ce = cudaFuncSetAttribute(refine_kernel<Grad, M>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (ce != cudaSuccess) return cuda_status(ce, "cudaFuncSetAttribute(refine)");
-  }
+  PUMP_TRY(smem_attr((const void *)refine_kernel<Grad, M>, smem));
   refine_kernel<Grad, M><<<a.n_paths, kRefThreads, smem, stream>>>(a, w);
   return launch_status("refine_kernel");
 }
@@ -478,12 +474,8 @@ extern "C" pump_status_t pump_refine_paths(pump_ctx *ctx, const pump_refine_args
     }
     // set the kernels' shared-memory limits outside the capture
     const size_t smem = (size_t)a->num_obstacles * 6 * sizeof(float);
-    if (smem > 48 * 1024) {
-      PUMP_CUDA_TRY(cudaFuncSetAttribute(refine_kernel<true, kStep>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      PUMP_CUDA_TRY(cudaFuncSetAttribute(refine_kernel<false, kAccept>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
+    PUMP_TRY(smem_attr((const void *)refine_kernel<true, kStep>, smem));
+    PUMP_TRY(smem_attr((const void *)refine_kernel<false, kAccept>, smem));
     cudaStream_t cs = nullptr;
     PUMP_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     pump_status_t st = cuda_status(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal),

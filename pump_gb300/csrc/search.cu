@@ -448,14 +448,10 @@ pump_status_t search_check(const SearchDev &sd, int g_idx, int n_g, const CheckA
   const long long want = (long long)n_g * chunks;
   const unsigned blocks = (unsigned)(want < kNumSMs * 8 ? want : kNumSMs * 8);
   if (ca.mode == PUMP_BVP_PARITY) {
-    if (smem > 48 * 1024)
-      PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)check_kernel<PUMP_BVP_PARITY>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PUMP_TRY(smem_attr((const void *)check_kernel<PUMP_BVP_PARITY>, smem));
     check_kernel<PUMP_BVP_PARITY><<<blocks, kChkThreads, smem, s>>>(sd, ca);
   } else {
-    if (smem > 48 * 1024)
-      PUMP_CUDA_TRY(cudaFuncSetAttribute((const void *)check_kernel<PUMP_BVP_PRECISION>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PUMP_TRY(smem_attr((const void *)check_kernel<PUMP_BVP_PRECISION>, smem));
     check_kernel<PUMP_BVP_PRECISION><<<blocks, kChkThreads, smem, s>>>(sd, ca);
   }
   return launch_status("check_kernel");

@@ -132,9 +132,10 @@ def test_plan_batch_equals_single_queries(gpu, pumplib):
     sts = (C.c_int * len(qs))()
     pumplib.check(L.pump_plan_batch(0, pbs, res, sts, len(qs), 4))
     f32 = lambda x: np.float32(x).view(np.uint32)
+    batch_error = L.pump_last_error().decode() if hasattr(L.pump_last_error(), "decode") else ""
     for k, q in enumerate(qs):
         st1, r1, p1, _ = run_plan(pumplib, ctx, pbs[k])
-        assert sts[k] == st1
+        assert sts[k] == st1, batch_error
         assert f32(res[k].rn) == f32(r1.rn)
         assert (res[k].num_edges, res[k].iterations, res[k].num_paths, res[k].success,
                 res[k].soln_path_idx) == (r1.num_edges, r1.iterations, r1.num_paths, r1.success,
