@@ -66,8 +66,8 @@ __global__ void claim_kernel(SearchDev sd, const int *g, int n_g) {
 // up to the roadmap's largest degree, taken by blocks in turn so a node of
 // high degree is spread over several blocks.  Per chunk the waypoints
 // (discretize_kernel's arithmetic) are computed one thread per (edge,
-// waypoint) into shared memory and stored to disc as whole lines (the
-// chunk's records are contiguous), then one thread per edge runs the
+// waypoint) and stored to disc (the chunk's records are contiguous), their
+// positions kept in shared memory; then one thread per edge runs the
 // reference's collision test from shared memory (free_edges_staged_kernel's:
 // boxes broadphase-disjoint from the edge's bounding box dropped first, an
 // exact filter; none dropped for a NaN waypoint or more than kFilterObs
@@ -77,7 +77,7 @@ constexpr int kChkThreads = 256;
 constexpr int kChkEdges = 256;
 
 size_t check_smem(int numObs, int numDisc) {
-  return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)kChkEdges * (numDisc + 1) * kDim);
+  return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)kChkEdges * (numDisc + 1) * 3);
 }
 
 template <int Mode>
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckA
   __shared__ int s_open[kChkThreads / 32];
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   const int numDisc = ca.numDisc, W = numDisc + 1;
-  float *s_wp = s_obs + ((ca.numObs * 12 + 3) & ~3);  // kChkEdges x W x 6
+  float *s_wp = s_obs + ((ca.numObs * 12 + 3) & ~3);  // kChkEdges x W x 3 positions
   stage_obstacles(ca.obs, ca.numObs, s_obs);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n_todo = sd.ctl->todo;
@@ -123,14 +123,20 @@ __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckA
           if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
           else path_point_f32(dt * i, topt, x0, x1, x);
         }
+        // consecutive threads write consecutive 24-byte records: a warp's
+        // stores cover one contiguous range
+        float2 *out = reinterpret_cast<float2 *>(ca.disc + ((long long)c0 * W + q) * kDim);
+        out[0] = make_float2(x[0], x[1]);
+        out[1] = make_float2(x[2], x[3]);
+        out[2] = make_float2(x[4], x[5]);
 #pragma unroll
-        for (int d = 0; d < kDim; ++d) s_wp[q * kDim + d] = x[d];
+        for (int d = 0; d < 3; ++d) s_wp[q * 3 + d] = x[d];
       }
       __syncthreads();
-      block_store(ca.disc + (long long)c0 * W * kDim, s_wp, ne * W * kDim);
       if (threadIdx.x < ne) {
         const int e = c0 + threadIdx.x;
-        const float *wp = s_wp + threadIdx.x * W * kDim;
+        constexpr int kPos = 3;  // floats per staged waypoint
+        const float *wp = s_wp + threadIdx.x * W * kPos;
         bool ok = true;
         float v[3], w[3];
 #pragma unroll
@@ -143,7 +149,7 @@ __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckA
           for (int i = 0; i < W; ++i)
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-              const float x = wp[i * kDim + d];
+              const float x = wp[i * kPos + d];
               nan = nan || x != x;
               emin[d] = fminf(emin[d], x);
               emax[d] = fmaxf(emax[d], x);
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckA
             if (nan || !broadphase_valid(emin, emax, &s_obs[o * 12])) mask[o >> 5] |= 1u << (o & 31);
           for (int i = 0; i < numDisc && ok; ++i) {
 #pragma unroll
-            for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kDim + d];
+            for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
             ok = segment_valid_masked(v, w, mask, words, s_obs);
 #pragma unroll
             for (int d = 0; d < 3; ++d) v[d] = w[d];
@@ -162,7 +168,7 @@ __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckA
         } else {
           for (int i = 0; i < numDisc && ok; ++i) {
 #pragma unroll
-            for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kDim + d];
+            for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
             ok = segment_valid(v, w, ca.numObs, s_obs);
 #pragma unroll
             for (int d = 0; d < 3; ++d) v[d] = w[d];
