@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-refine", action="store_true", help="skip the path-refinement workload")
     ap.add_argument("--batch", type=int, default=256, help="queries of the batched workload (0: skip)")
-    ap.add_argument("--workers", type=int, default=0, help="batched-mode workers (0: host cores)")
+    ap.add_argument("--workers", type=int, default=0,
+                    help="batched-mode workers (0: half the host cores, at most 8)")
     return ap.parse_args()
 
 
@@ -196,7 +197,10 @@ def measure_queries(args, lib, L, ctx):
     sts = (C.c_int * len(qs))()
     for k in range(warm):
         sts[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res[k]), None)
-    workers = args.workers or (os.cpu_count() or 4)
+    # a worker sweep on the GB300 machine (16 host cores, 128 uneven queries):
+    # 4 -> 1646, 8 -> 1934, 16 -> 1806, 32 -> 1598 q/s; past about 8 the GPU is
+    # saturated and more threads only contend
+    workers = args.workers or max(1, min(8, (os.cpu_count() or 8) // 2))
     L.pump_plan_batch(0, pbs, res, sts, warm, min(workers, warm))
     res_p, sts_p = results(), (C.c_int * len(qs))()
     t0 = time.perf_counter()

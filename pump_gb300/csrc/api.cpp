@@ -44,8 +44,10 @@ Ctx::~Ctx() {
   if (refine_graph.exec) cudaGraphExecDestroy(refine_graph.exec);
   for (int i = 0; i < kNumSlots; ++i)
     if (buf_[i]) cudaFree(buf_[i]);
+  for (void *p : retired_) cudaFree(p);
   for (int i = 0; i < kNumPin; ++i)
     if (pin_[i]) cudaFreeHost(pin_[i]);
+  for (void *p : retired_pinned_) cudaFreeHost(p);
   if (prev >= 0) cudaSetDevice(prev);
 }
 
@@ -54,7 +56,7 @@ pump_status_t Ctx::pinned(int slot, size_t bytes, void **out) {
   if (bytes == 0) bytes = 1;
   if (pin_cap_[slot] < bytes) {
     if (pin_[slot]) {
-      PUMP_CUDA_TRY(cudaFreeHost(pin_[slot]));
+      retired_pinned_.push_back(pin_[slot]);
       pin_[slot] = nullptr;
       pin_cap_[slot] = 0;
     }
@@ -157,13 +159,12 @@ pump_status_t Ctx::scratch(int slot, size_t bytes, void **out) {
   if (bytes == 0) bytes = 1;
   if (cap_[slot] < bytes) {
     if (buf_[slot]) {
-      // a buffer still in use by queued work must not be freed early
-      PUMP_CUDA_TRY(cudaDeviceSynchronize());
-      PUMP_CUDA_TRY(cudaFree(buf_[slot]));
+      // queued work may still use it: freed with the context
+      retired_.push_back(buf_[slot]);
       buf_[slot] = nullptr;
       cap_[slot] = 0;
     }
-    size_t cap = bytes + bytes / 4;
+    size_t cap = bytes + bytes / 2;
     PUMP_CUDA_TRY(cudaMalloc(&buf_[slot], cap));
     cap_[slot] = cap;
   }

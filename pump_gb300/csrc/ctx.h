@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <vector>
+
 #include "pump.h"
 
 namespace pump {
@@ -33,10 +35,12 @@ class Ctx {
   pump_ctx *handle() { return reinterpret_cast<pump_ctx *>(this); }
   int device() const { return device_; }
   pump_status_t activate();
-  // Device buffer of at least `bytes` for `slot` (contents undefined).
+  // Device buffer of at least `bytes` for `slot` (contents undefined).  A
+  // buffer that grows leaves the old one to be freed with the context, so
+  // growing never waits for the device.
   pump_status_t scratch(int slot, size_t bytes, void **out);
-  // Pinned host buffer of at least `bytes` for `slot` (grow-only; the caller
-  // has no copy to or from it in flight when it asks for more).
+  // Pinned host buffer of at least `bytes` for `slot` (grow-only; an
+  // outgrown buffer is freed with the context).
   pump_status_t pinned(int slot, size_t bytes, void **out);
   // Time-major particle table for (seed, P, T), generated on first use and
   // shared by every context on the device (the reference loads its table
@@ -60,6 +64,9 @@ class Ctx {
   size_t cap_[kNumSlots];
   void *pin_[kNumPin];
   size_t pin_cap_[kNumPin];
+  // outgrown buffers: queued work may still use them, so they are freed with
+  // the context instead of at once (a free would wait for the whole device)
+  std::vector<void *> retired_, retired_pinned_;
 };
 
 // Internal device-side entry points shared between translation units.

@@ -1060,6 +1060,43 @@ pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *
 }  // namespace
 }  // namespace pump
 
+namespace pump {
+namespace {
+// Contexts and streams of batch workers, kept across pump_plan_batch calls
+// so their scratch and pinned buffers are allocated once per process.
+std::mutex g_worker_mu;
+std::vector<std::pair<int, std::pair<pump_ctx *, cudaStream_t>>> g_idle_workers;
+
+pump_status_t take_worker(int device, pump_ctx **ctx, cudaStream_t *s) {
+  {
+    std::lock_guard<std::mutex> lk(g_worker_mu);
+    for (size_t i = 0; i < g_idle_workers.size(); ++i)
+      if (g_idle_workers[i].first == device) {
+        *ctx = g_idle_workers[i].second.first;
+        *s = g_idle_workers[i].second.second;
+        g_idle_workers.erase(g_idle_workers.begin() + i);
+        return Ctx::from(*ctx)->activate();
+      }
+  }
+  *ctx = nullptr;
+  *s = nullptr;
+  PUMP_TRY(pump_ctx_create(device, ctx));
+  return cuda_status(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking),
+                     "cudaStreamCreateWithFlags");
+}
+
+void give_worker(int device, pump_ctx *ctx, cudaStream_t s) {
+  if (!ctx || !s) {
+    if (s) cudaStreamDestroy(s);
+    if (ctx) pump_ctx_destroy(ctx);
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_worker_mu);
+  g_idle_workers.push_back({device, {ctx, s}});
+}
+}  // namespace
+}  // namespace pump
+
 extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problems,
                                          pump_plan_result *results, pump_status_t *statuses, int n,
                                          int workers) {
@@ -1134,10 +1171,8 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
   std::string fail_msg;
   auto worker = [&](int w) {
     pump_ctx *ctx = nullptr;
-    pump_status_t st = pump_ctx_create(device, &ctx);
     cudaStream_t s = nullptr;
-    if (st == PUMP_OK) st = cuda_status(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking),
-                                        "cudaStreamCreateWithFlags");
+    pump_status_t st = take_worker(device, &ctx, &s);
     if (st != PUMP_OK) {
       setup[w] = st;
       msgs[w] = pump_last_error();
@@ -1156,8 +1191,7 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
         }
       }
     }
-    if (s) cudaStreamDestroy(s);
-    if (ctx) pump_ctx_destroy(ctx);
+    give_worker(device, ctx, s);
   };
   std::vector<std::thread> pool;
   for (int w = 1; w < workers; ++w) pool.emplace_back(worker, w);
