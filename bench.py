@@ -191,17 +191,17 @@ def measure_queries(args, lib, L, ctx):
     def ok(res, sts):
         return sum(1 for k in range(len(qs)) if sts[k] == lib.PUMP_OK and res[k].success
                    and res[k].soln_cp < pbs[k].cp_target)
-    # warm both paths once on a few queries (contexts, particle tables)
-    warm = min(4, len(qs))
-    res = results()
-    sts = (C.c_int * len(qs))()
-    for k in range(warm):
-        sts[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res[k]), None)
     # a worker sweep on the GB300 machine (16 host cores, 128 uneven queries):
     # 4 -> 1646, 8 -> 1934, 16 -> 1806, 32 -> 1598 q/s; past about 8 the GPU is
     # saturated and more threads only contend
     workers = args.workers or max(1, min(8, (os.cpu_count() or 8) // 2))
-    L.pump_plan_batch(0, pbs, res, sts, warm, min(workers, warm))
+    # warm both paths on every query (contexts, particle tables, and the
+    # autotuner's first call of each shape class, which neither timed run pays)
+    res = results()
+    sts = (C.c_int * len(qs))()
+    for k in range(len(qs)):
+        sts[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res[k]), None)
+    L.pump_plan_batch(0, pbs, res, sts, len(qs), workers)
     res_p, sts_p = results(), (C.c_int * len(qs))()
     t0 = time.perf_counter()
     for k in range(len(qs)):
