@@ -386,6 +386,10 @@ typedef struct pump_plan_result {
   /* of ms_explore: time from each iteration's first launch to its counters
    * back on the host (the iteration's device work and read-backs) */
   double ms_explore_wait;
+  /* every stage: time the host spent waiting for the device (stream
+   * synchronisations), and how many times it waited */
+  double ms_wait;
+  int num_waits;
 } pump_plan_result;
 
 /* Fills a problem with the reference's defaults (mainPUMP.cu:51-72). */

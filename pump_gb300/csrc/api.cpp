@@ -48,7 +48,55 @@ Ctx::~Ctx() {
   for (int i = 0; i < kNumPin; ++i)
     if (pin_[i]) cudaFreeHost(pin_[i]);
   for (void *p : retired_pinned_) cudaFreeHost(p);
+  for (const ArenaChunk &c : arena_) cudaFree(c.p);
+  if (arena_done_) cudaEventDestroy(arena_done_);
   if (prev >= 0) cudaSetDevice(prev);
+}
+
+pump_status_t Ctx::arena_begin(cudaStream_t s) {
+  if (arena_pending_ && arena_stream_ != s) PUMP_CUDA_TRY(cudaStreamWaitEvent(s, arena_done_, 0));
+  if (arena_.size() > 1) {
+    // the last call needed several chunks: one chunk with room for all of
+    // them replaces them (freed in order on s, after the last call's work)
+    const size_t want = arena_total_ + arena_total_ / 4;
+    for (const ArenaChunk &c : arena_) PUMP_CUDA_TRY(cudaFreeAsync(c.p, s));
+    arena_.clear();
+    char *p = nullptr;
+    PUMP_CUDA_TRY(pool_malloc_async((void **)&p, want, s));
+    arena_.push_back({p, want});
+  }
+  arena_used_ = 0;
+  arena_total_ = 0;
+  arena_stream_ = s;
+  return PUMP_OK;
+}
+
+pump_status_t Ctx::arena_take(size_t bytes, void **out) {
+  bytes = (bytes + 255) & ~(size_t)255;
+  if (bytes == 0) bytes = 256;
+  if (arena_.empty() || arena_used_ + bytes > arena_.back().cap) {
+    size_t cap = arena_.empty() ? (size_t)64 << 20 : arena_.back().cap * 2;
+    if (cap < bytes) cap = bytes;
+    char *p = nullptr;
+    PUMP_CUDA_TRY(pool_malloc_async((void **)&p, cap, arena_stream_));
+    arena_.push_back({p, cap});
+    arena_used_ = 0;
+  }
+  *out = arena_.back().p + arena_used_;
+  arena_used_ += bytes;
+  arena_total_ += bytes;
+  return PUMP_OK;
+}
+
+void Ctx::arena_end(cudaStream_t s) {
+  if (!arena_done_ && cudaEventCreateWithFlags(&arena_done_, cudaEventDisableTiming) != cudaSuccess) {
+    arena_done_ = nullptr;
+    cudaStreamSynchronize(s);  // no event: the call's work is complete instead
+    arena_pending_ = false;
+    return;
+  }
+  arena_pending_ = cudaEventRecord(arena_done_, s) == cudaSuccess;
+  if (!arena_pending_) cudaStreamSynchronize(s);
 }
 
 pump_status_t Ctx::pinned(int slot, size_t bytes, void **out) {

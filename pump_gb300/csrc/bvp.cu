@@ -409,16 +409,18 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
       cb.nodes, cb.node_off, cb.node_cnt, cb.seg_base, n_paths, cb.x0, cb.x1, cb.seg_path, cb.hits);
   PUMP_TRY(launch_status("candidate_segments"));
   if (n_seg > 0) {
-    // optimal times (tmax 5) and smoothing costs (tmax 2) in one launch
+    // optimal times (tmax 5) and smoothing costs and times (tmax 2) in one
+    // launch
     BvpJobs jb{};
     jb.x0 = cb.x0;
     jb.x1 = cb.x1;
     jb.n = n_seg;
-    jb.jobs = with_cost ? 2 : 1;
+    jb.jobs = (with_cost || cb.topt2) ? 2 : 1;
     jb.tmax[0] = 5.0f;
     jb.topt[0] = cb.topt;
     jb.tmax[1] = 2.0f;
-    jb.cost[1] = cb.seg_cost;
+    jb.cost[1] = with_cost ? cb.seg_cost : nullptr;
+    jb.topt[1] = cb.topt2;
     PUMP_TRY(bvp_jobs_launch(jb, mode, s));
   }
   candidate_times_kernel<<<grid_for(n_paths, 64), 64, 0, s>>>(

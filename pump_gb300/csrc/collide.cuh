@@ -73,6 +73,20 @@ __device__ __forceinline__ bool segment_valid(const float *v, const float *w, in
   return true;
 }
 
+// One (segment, box) test of isMotionValid's loop (collisionCheck.cu:65-102):
+// true when the segment v-w hits box ob.  isMotionValid is the AND of
+// !segment_box_hit over its boxes, so any split of the boxes among threads
+// gives the same result.
+__device__ __forceinline__ bool segment_box_hit(const float *v, const float *w, const float *ob) {
+  float bbMin[3], bbMax[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (v[d] > w[d]) { bbMin[d] = w[d]; bbMax[d] = v[d]; }
+    else { bbMin[d] = v[d]; bbMax[d] = w[d]; }
+  }
+  return !broadphase_valid(bbMin, bbMax, ob) && !motion_valid(v, w, ob);
+}
+
 // isMotionValid over the boxes whose bits are set in mask (box o is bit
 // o % 32 of mask[o / 32]), in index order.  A box that is broadphase-disjoint
 // from the whole edge's bounding box is disjoint from every segment's, so

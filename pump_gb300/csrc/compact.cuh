@@ -209,10 +209,11 @@ __global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, P
 }
 
 // Zeroed tile status words, tile counter, total and error word for a pass
-// over n items (ctx compaction scratch); *ntiles_out = the tiles to launch.
+// over n items in tiles of tile_items (ctx compaction scratch);
+// *ntiles_out = the tiles to launch.
 pump_status_t prepare_tiles(Ctx *ctx, long long n, cudaStream_t stream, TileScratch *ts_out,
-                            long long *ntiles_out) {
-  const long long ntiles = n > 0 ? (n + kTile - 1) / kTile : 1;
+                            long long *ntiles_out, long long tile_items = kTile) {
+  const long long ntiles = n > 0 ? (n + tile_items - 1) / tile_items : 1;
   if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "compaction: too many tiles");
   const size_t zeroed = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
   const size_t bytes = zeroed + sizeof(unsigned long long) * ntiles;

@@ -25,7 +25,7 @@ class Ctx {
     kNumSlots
   };
   // Pinned host staging buffers (uploads, read-backs of small results).
-  enum PinSlot { kPinIn = 0, kPinOut, kNumPin };
+  enum PinSlot { kPinIn = 0, kPinOut, kPinOptIn, kPinOptOut, kPinPaths, kPinCtl, kNumPin };
   explicit Ctx(int device) : device_(device) {
     for (int i = 0; i < kNumSlots; ++i) { buf_[i] = nullptr; cap_[i] = 0; }
     for (int i = 0; i < kNumPin; ++i) { pin_[i] = nullptr; pin_cap_[i] = 0; }
@@ -49,6 +49,18 @@ class Ctx {
   // values in the same allocation.
   pump_status_t particle_table(uint64_t seed, int P, int T, const float **out, cudaStream_t stream);
 
+  // Per-call device arena: the planner's buffers of one call are carved from
+  // memory the context keeps across calls, so a call makes no allocation
+  // calls once the arena has reached the size its calls need.  arena_begin
+  // starts a call on stream s (ordered after the previous call's use of the
+  // arena, and with the previous call's chunks merged into one when it
+  // needed more than one); arena_take hands out 256-byte aligned regions
+  // (adding a chunk when the current one is full); arena_end marks the end
+  // of the call's use on s.  One call at a time per context.
+  pump_status_t arena_begin(cudaStream_t s);
+  pump_status_t arena_take(size_t bytes, void **out);
+  void arena_end(cudaStream_t s);
+
   // The captured refinement loop of the last pump_refine_paths call, replayed
   // while its key (arguments, iterations, output and scratch pointers) is the same.
   struct GraphCache {
@@ -67,6 +79,17 @@ class Ctx {
   // outgrown buffers: queued work may still use them, so they are freed with
   // the context instead of at once (a free would wait for the whole device)
   std::vector<void *> retired_, retired_pinned_;
+  // arena chunks in use by the current call (the first is kept across calls)
+  struct ArenaChunk {
+    char *p;
+    size_t cap;
+  };
+  std::vector<ArenaChunk> arena_;
+  size_t arena_used_ = 0;   // bytes taken from the last chunk
+  size_t arena_total_ = 0;  // bytes taken by the current call
+  cudaStream_t arena_stream_ = nullptr;
+  cudaEvent_t arena_done_ = nullptr;  // recorded at the end of each call
+  bool arena_pending_ = false;
 };
 
 // Internal device-side entry points shared between translation units.
@@ -122,7 +145,8 @@ struct CandidateBufs {
   const int *node_off, *node_cnt, *seg_base;
   float *x0, *x1, *topt, *seg_cost, *seg_toff, *states, *cost;
   int *seg_path, *seg_T, *seg_row, *len;
-  int *hits;  // zeroed per path when not null (the MC CP counters)
+  int *hits;     // zeroed per path when not null (the MC CP counters)
+  float *topt2;  // when not null: the segments' optimal times with tmax 2
 };
 pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_seg, int mode,
                                     float dt, bool with_cost, int rows_cap, cudaStream_t s);

@@ -57,30 +57,49 @@ double ms_since(clk::time_point t0) {
   return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
 }
 
-// Stream that the planner running on this host thread allocates on.
+// Stream that the planner running on this host thread allocates on, and the
+// context whose arena its buffers come from (null: stream-ordered pool).
 thread_local cudaStream_t t_alloc_stream = nullptr;
+thread_local Ctx *t_arena = nullptr;
 
-// Owning device buffer, allocated and freed in stream order on the planner's
-// stream (cudaMallocAsync / cudaFreeAsync): no call synchronises the device,
-// so planners on other streams keep running.
+// Device buffer of a planner call: a region of the context's arena while a
+// planner runs on this thread (released with the call), else allocated and
+// freed in stream order on the planner's stream (cudaMallocAsync /
+// cudaFreeAsync).  Neither synchronises the device, so planners on other
+// streams keep running; the arena also makes no allocation call per buffer,
+// which matters when many host threads plan at once.
 template <class T>
 struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
   cudaStream_t s = nullptr;
+  bool arena = false;
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
-  ~DevBuf() { if (p) cudaFreeAsync(p, s); }
+  ~DevBuf() { if (p && !arena) cudaFreeAsync(p, s); }
   pump_status_t alloc(size_t count) {
     if (count <= n && p) return PUMP_OK;
-    if (p) PUMP_CUDA_TRY(cudaFreeAsync(p, s));
+    if (p && !arena) PUMP_CUDA_TRY(cudaFreeAsync(p, s));
     p = nullptr;
     n = 0;
     s = t_alloc_stream;
-    PUMP_CUDA_TRY(pool_malloc_async((void **)&p, sizeof(T) * (count ? count : 1), s));
+    arena = t_arena != nullptr;
+    if (arena) PUMP_TRY(t_arena->arena_take(sizeof(T) * (count ? count : 1), (void **)&p));
+    else PUMP_CUDA_TRY(pool_malloc_async((void **)&p, sizeof(T) * (count ? count : 1), s));
     n = count;
     return PUMP_OK;
+  }
+};
+
+// The arena of ctx serves this thread's planner buffers while in scope.
+struct ArenaScope {
+  Ctx *c;
+  cudaStream_t s;
+  ArenaScope(Ctx *ctx, cudaStream_t stream) : c(ctx), s(stream) { t_arena = ctx; }
+  ~ArenaScope() {
+    t_arena = nullptr;
+    c->arena_end(s);
   }
 };
 
@@ -112,6 +131,29 @@ void halton_samples(const pump_problem &pb, std::vector<float> &s) {
     s[(size_t)(N - 1) * kDim + d] = pb.goal[d];
   }
 }
+
+// Device buffers of one batch of candidate paths and the pinned slots of its
+// upload and read-back.  A planner keeps two, so the unconstrained optimal
+// path is evaluated in the same round trip as the goal candidates.
+struct CandSet {
+  int pin_in, pin_out;
+  DevBuf<float> in, x0, x1, topt, topt2, segcost, toff, states;
+  DevBuf<int> out, segpath, segT, segrow;
+  // the batch launched last (read back by eval_read after a synchronisation)
+  int n = 0, segs = 0, states_rows = 0, table_rows = 0, num_mc = 0;
+  bool with_cost = false, with_cp = false, with_topts = false;
+  const char *hout = nullptr;
+  CandSet(int in_slot, int out_slot) : pin_in(in_slot), pin_out(out_slot) {}
+};
+
+// What eval_read returns: per path the dense length, the smoothing's cost and
+// the MC CP (-1 when the dense path has more states than the table has rows);
+// per segment (paths in order) the optimal times with tmax 5 and with tmax 2
+// when asked for; the first rows of path 0's dense states when asked for.
+struct CandResult {
+  std::vector<int> len;
+  std::vector<float> cost, cp, t5, t2, states;
+};
 
 // Pair BVPs of Halton points 1 .. M shared by a batch's queries (see
 // pairview.cuh); key = the BVP mode and the state bounds that scale the points.
@@ -149,20 +191,39 @@ class Planner {
   pump_status_t online();
   pump_status_t explore();
   pump_status_t search_and_smooth();
-  pump_status_t control_path(const std::vector<float> &xs);
+  // The controller's discretisation of node states xs; t5 and t2, when not
+  // null, are the segments' optimal times with tmax 5 and 2 (else computed
+  // here).  control_launch enqueues its work (after a pending read-back of
+  // the kept path, if any); control_finish runs after a synchronisation.
+  pump_status_t control_launch(const std::vector<float> &xs, const std::vector<float> *t5,
+                               const std::vector<float> *t2);
+  pump_status_t control_finish();
   pump_status_t refine(const std::vector<float> &xs, float cpTarget, float *lastCP,
                        float *lastCost, std::vector<float> *bestPath, int *bestLen,
                        std::vector<float> *xsFinal);
-  // Candidate paths evaluated on the device (candidate_paths_async): per
-  // path the dense length, the smoothing's cost and the MC CP (-1 when the
-  // dense path has more states than the table has rows); states of path k
-  // at d_cstates_ + k * rows_cap rows.
+  // Candidate paths evaluated on the device (candidate_paths_async) with
+  // the buffers of c: eval_launch enqueues the upload, the kernels and the
+  // read-back into pinned memory (states of path k at c.states + k *
+  // rows_cap rows; with_topts: the segments' optimal times with tmax 5 and
+  // 2; states_rows: read back that many rows of path 0's states);
+  // eval_read parses the read-back after a synchronisation.
+  pump_status_t eval_launch(CandSet &c, const std::vector<std::vector<float>> &xs, float dt,
+                            int rows_cap, bool with_cost, bool with_cp, bool with_topts,
+                            int states_rows);
+  void eval_read(const CandSet &c, CandResult *r) const;
+  // eval_launch, synchronisation and eval_read on the first buffer set
   pump_status_t eval_candidates(const std::vector<std::vector<float>> &xs, float dt, int rows_cap,
                                 bool with_cost, bool with_cp, std::vector<int> &len,
                                 std::vector<float> &cost, std::vector<float> &cp);
   pump_status_t topts_of(const std::vector<float> &x0, const std::vector<float> &x1, float tmax,
                          std::vector<float> *topt, std::vector<float> *cost);
-  pump_status_t sync() { return cuda_status(cudaStreamSynchronize(s_), "cudaStreamSynchronize"); }
+  pump_status_t sync() {
+    const auto t = clk::now();
+    const pump_status_t st = cuda_status(cudaStreamSynchronize(s_), "cudaStreamSynchronize");
+    res_->ms_wait += ms_since(t);
+    ++res_->num_waits;
+    return st;
+  }
   template <class T>
   pump_status_t h2d(T *d, const T *h, size_t n) {
     if (n == 0) return PUMP_OK;
@@ -220,11 +281,19 @@ class Planner {
   DevBuf<int> d_wfPrev_, d_wfEdge_, d_err_;
   int numPaths_ = 0;
   // reusable scratch of the batched BVP / dense-path / MC CP helpers
-  DevBuf<float> d_bx0_, d_bx1_, d_bt_, d_bc_, d_xs_, d_ts_, d_tau_;
-  DevBuf<int> d_seg_;
-  // candidate batches
-  DevBuf<float> d_cin_, d_cx0_, d_cx1_, d_ctopt_, d_csegcost_, d_ctoff_, d_cstates_, d_best_;
-  DevBuf<int> d_cout_, d_csegpath_, d_csegT_, d_csegrow_;
+  DevBuf<float> d_bx0_, d_bx1_, d_bt_, d_bc_, d_xs_;
+  // candidate batches: the search's and the unconstrained optimal path's;
+  // the dense path kept by the smoothing
+  CandSet cs_{Ctx::kPinIn, Ctx::kPinOut}, co_{Ctx::kPinOptIn, Ctx::kPinOptOut};
+  DevBuf<float> d_best_;
+  // the controller path being assembled (control_launch .. control_finish)
+  struct ControlJob {
+    int rows = 0, total = 0;
+    std::vector<float> out;
+    std::vector<int> row;
+    const float *pts = nullptr;  // pinned read-back of the sampled states
+  } ctrl_;
+  DevBuf<float> d_ctrl_;
 };
 
 pump_status_t Planner::run() {
@@ -505,6 +574,8 @@ pump_status_t Planner::explore() {
   std::vector<int> trace_prev, trace_edge;
   pump_status_t status = PUMP_OK;
   SearchCtl ctl{};
+  SearchCtl *hctl = nullptr;  // pinned read-back of the iteration's counters
+  PUMP_TRY(ctx_->pinned(Ctx::kPinCtl, sizeof(SearchCtl), (void **)&hctl));
   while (itrs < maxItrs) {
     ++itrs;
     const int nG = gCount[Gidx];
@@ -549,8 +620,10 @@ pump_status_t Planner::explore() {
     PUMP_TRY(search_prune(sd, maxNew, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
     PUMP_TRY(search_store(ctx_, sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
                           d_stage_.p, d_valid_.p, words_, s_));
-    PUMP_TRY(d2h(&ctl, d_ctl.p, 1));
+    res_->d2h_bytes += (long long)sizeof(SearchCtl);
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hctl, d_ctl.p, sizeof(SearchCtl), cudaMemcpyDeviceToHost, s_));
     PUMP_TRY(sync());
+    ctl = *hctl;
     res_->ms_explore_wait += ms_since(tw);
     if (ctl.overflow == 1) {
       status = set_error(PUMP_ERR_CAPACITY, "wavefront exceeds maxPathCount %d", M);
@@ -581,16 +654,22 @@ pump_status_t Planner::explore() {
       break;
     }
   }
-  // stored paths back to the host for the solution search
-  pathPrev_.resize(numPaths_);
-  pathNode_.resize(numPaths_);
-  pathCost_.resize(numPaths_);
-  PUMP_TRY(d2h(pathPrev_.data(), d_prev.p, numPaths_));
-  PUMP_TRY(d2h(pathNode_.data(), d_node.p, numPaths_));
-  PUMP_TRY(d2h(pathCost_.data(), d_cost.p, numPaths_));
-  int err = 0;
-  PUMP_TRY(d2h(&err, d_err_.p, 1));
+  // stored paths back to the host for the solution search, in one pinned
+  // read-back: prev | node | cost | the particle-table error word
+  const size_t np = (size_t)numPaths_;
+  int *hp = nullptr;
+  PUMP_TRY(ctx_->pinned(Ctx::kPinPaths, sizeof(int) * (3 * np + 1), (void **)&hp));
+  res_->d2h_bytes += (long long)(sizeof(int) * (3 * np + 1));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hp, d_prev.p, sizeof(int) * np, cudaMemcpyDeviceToHost, s_));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hp + np, d_node.p, sizeof(int) * np, cudaMemcpyDeviceToHost, s_));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hp + 2 * np, d_cost.p, sizeof(float) * np, cudaMemcpyDeviceToHost, s_));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hp + 3 * np, d_err_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
   PUMP_TRY(sync());
+  pathPrev_.assign(hp, hp + np);
+  pathNode_.assign(hp + np, hp + 2 * np);
+  pathCost_.resize(np);
+  std::memcpy(pathCost_.data(), hp + 2 * np, sizeof(float) * np);
+  const int err = hp[3 * np];
   atNode_.assign(N_, std::vector<int>());
   for (int p = 0; p < numPaths_; ++p)
     if (pathNode_[p] == N_ - 1) atNode_[N_ - 1].push_back(p);
@@ -632,88 +711,145 @@ pump_status_t Planner::topts_of(const std::vector<float> &x0, const std::vector<
   return sync();
 }
 
-pump_status_t Planner::eval_candidates(const std::vector<std::vector<float>> &xs, float dt,
-                                      int rows_cap, bool with_cost, bool with_cp,
-                                      std::vector<int> &len, std::vector<float> &cost,
-                                      std::vector<float> &cp) {
+pump_status_t Planner::eval_launch(CandSet &c, const std::vector<std::vector<float>> &xs,
+                                   float dt, int rows_cap, bool with_cost, bool with_cp,
+                                   bool with_topts, int states_rows) {
   const int n = (int)xs.size();
-  len.assign(n, 0);
-  cost.assign(n, 0.0f);
-  cp.assign(n, 0.0f);
+  c.n = n;
+  c.segs = 0;
+  c.states_rows = n > 0 ? states_rows : 0;
+  c.with_cost = with_cost;
+  c.with_cp = with_cp;
+  c.with_topts = with_topts;
+  c.table_rows = pb_.table_rows;
+  c.num_mc = pb_.num_mc;
+  c.hout = nullptr;
   if (n == 0) return PUMP_OK;
   // one upload through pinned memory: nodes | node offsets, counts, segment
   // bases, dense-path offsets
   int rows = 0, segs = 0;
   for (int k = 0; k < n; ++k) {
-    const int c = (int)(xs[k].size() / kDim);
-    rows += c;
-    segs += c > 1 ? c - 1 : 0;
+    const int cnt = (int)(xs[k].size() / kDim);
+    rows += cnt;
+    segs += cnt > 1 ? cnt - 1 : 0;
   }
+  c.segs = segs;
   const size_t nf = (size_t)rows * kDim;
   const size_t in_bytes = sizeof(float) * nf + sizeof(int) * 4 * (size_t)n;
   char *hin = nullptr;
-  PUMP_TRY(ctx_->pinned(Ctx::kPinIn, in_bytes, (void **)&hin));
+  PUMP_TRY(ctx_->pinned(c.pin_in, in_bytes, (void **)&hin));
   float *hnodes = reinterpret_cast<float *>(hin);
   int *hints = reinterpret_cast<int *>(hin + sizeof(float) * nf);
   for (int k = 0, r = 0, sg = 0; k < n; ++k) {
-    const int c = (int)(xs[k].size() / kDim);
+    const int cnt = (int)(xs[k].size() / kDim);
     hints[k] = r;
-    hints[n + k] = c;
+    hints[n + k] = cnt;
     hints[2 * n + k] = sg;
     hints[3 * n + k] = k * rows_cap;
     std::memcpy(hnodes + (size_t)r * kDim, xs[k].data(), sizeof(float) * xs[k].size());
-    r += c;
-    sg += c > 1 ? c - 1 : 0;
+    r += cnt;
+    sg += cnt > 1 ? cnt - 1 : 0;
   }
-  PUMP_TRY(d_cin_.alloc(in_bytes / sizeof(float) + 1));
-  PUMP_CUDA_TRY(cudaMemcpyAsync(d_cin_.p, hin, in_bytes, cudaMemcpyHostToDevice, s_));
-  const int *d_ints = reinterpret_cast<const int *>(d_cin_.p + nf);
+  PUMP_TRY(c.in.alloc(in_bytes / sizeof(float) + 1));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(c.in.p, hin, in_bytes, cudaMemcpyHostToDevice, s_));
+  const int *d_ints = reinterpret_cast<const int *>(c.in.p + nf);
   const size_t sg = segs > 0 ? (size_t)segs : 1;
-  PUMP_TRY(d_cx0_.alloc(sg * kDim));
-  PUMP_TRY(d_cx1_.alloc(sg * kDim));
-  PUMP_TRY(d_ctopt_.alloc(sg));
-  PUMP_TRY(d_csegcost_.alloc(sg));
-  PUMP_TRY(d_ctoff_.alloc(sg));
-  PUMP_TRY(d_csegpath_.alloc(sg));
-  PUMP_TRY(d_csegT_.alloc(sg));
-  PUMP_TRY(d_csegrow_.alloc(sg));
+  PUMP_TRY(c.x0.alloc(sg * kDim));
+  PUMP_TRY(c.x1.alloc(sg * kDim));
+  PUMP_TRY(c.topt.alloc(sg));
+  if (with_topts) PUMP_TRY(c.topt2.alloc(sg));
+  PUMP_TRY(c.segcost.alloc(sg));
+  PUMP_TRY(c.toff.alloc(sg));
+  PUMP_TRY(c.segpath.alloc(sg));
+  PUMP_TRY(c.segT.alloc(sg));
+  PUMP_TRY(c.segrow.alloc(sg));
   // results read back in one copy: MC hit counts | lengths | costs
-  PUMP_TRY(d_cout_.alloc(3 * (size_t)n));
-  PUMP_TRY(d_cstates_.alloc((size_t)n * rows_cap * kDim));
+  PUMP_TRY(c.out.alloc(3 * (size_t)n));
+  PUMP_TRY(c.states.alloc((size_t)n * rows_cap * kDim));
   CandidateBufs cb{};
-  cb.nodes = d_cin_.p;
+  cb.nodes = c.in.p;
   cb.node_off = d_ints;
   cb.node_cnt = d_ints + n;
   cb.seg_base = d_ints + 2 * n;
-  cb.x0 = d_cx0_.p;
-  cb.x1 = d_cx1_.p;
-  cb.topt = d_ctopt_.p;
-  cb.seg_cost = d_csegcost_.p;
-  cb.seg_toff = d_ctoff_.p;
-  cb.states = d_cstates_.p;
-  cb.hits = with_cp ? d_cout_.p : nullptr;
-  cb.len = d_cout_.p + n;
-  cb.cost = reinterpret_cast<float *>(d_cout_.p + 2 * n);
-  cb.seg_path = d_csegpath_.p;
-  cb.seg_T = d_csegT_.p;
-  cb.seg_row = d_csegrow_.p;
+  cb.x0 = c.x0.p;
+  cb.x1 = c.x1.p;
+  cb.topt = c.topt.p;
+  cb.topt2 = with_topts ? c.topt2.p : nullptr;
+  cb.seg_cost = c.segcost.p;
+  cb.seg_toff = c.toff.p;
+  cb.states = c.states.p;
+  cb.hits = with_cp ? c.out.p : nullptr;
+  cb.len = c.out.p + n;
+  cb.cost = reinterpret_cast<float *>(c.out.p + 2 * n);
+  cb.seg_path = c.segpath.p;
+  cb.seg_T = c.segT.p;
+  cb.seg_row = c.segrow.p;
   PUMP_TRY(candidate_paths_async(cb, n, segs, pb_.bvp_mode, dt, with_cost, rows_cap, s_));
   if (with_cp)
-    PUMP_TRY(mc_cp_hits_async(d_cstates_.p, d_ints + 3 * n, cb.len, n, d_table_, pb_.num_mc,
+    PUMP_TRY(mc_cp_hits_async(c.states.p, d_ints + 3 * n, cb.len, n, d_table_, pb_.num_mc,
                               pb_.table_rows, pb_.offset_mult, obs_p_, nobs_, cb.hits, s_,
                               d_rowmax_));
-  int *hout = nullptr;
-  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(int) * 3 * (size_t)n, (void **)&hout));
-  PUMP_CUDA_TRY(cudaMemcpyAsync(hout, d_cout_.p, sizeof(int) * 3 * (size_t)n,
+  // pinned read-back: 3n ints | 2 segs floats (with_topts) | states_rows x 6
+  // floats of path 0
+  const size_t seg_f = with_topts ? (size_t)segs : 0;
+  const size_t st_f = (size_t)c.states_rows * kDim;
+  const size_t out_bytes = sizeof(int) * 3 * (size_t)n + sizeof(float) * (2 * seg_f + st_f);
+  char *hout = nullptr;
+  PUMP_TRY(ctx_->pinned(c.pin_out, out_bytes, (void **)&hout));
+  float *hf = reinterpret_cast<float *>(hout + sizeof(int) * 3 * (size_t)n);
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hout, c.out.p, sizeof(int) * 3 * (size_t)n,
                                 cudaMemcpyDeviceToHost, s_));
-  PUMP_TRY(sync());
+  if (seg_f > 0) {
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hf, c.topt.p, sizeof(float) * seg_f, cudaMemcpyDeviceToHost, s_));
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hf + seg_f, c.topt2.p, sizeof(float) * seg_f,
+                                  cudaMemcpyDeviceToHost, s_));
+  }
+  if (st_f > 0)
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hf + 2 * seg_f, c.states.p, sizeof(float) * st_f,
+                                  cudaMemcpyDeviceToHost, s_));
+  c.hout = hout;
+  return PUMP_OK;
+}
+
+void Planner::eval_read(const CandSet &c, CandResult *r) const {
+  const int n = c.n;
+  r->len.assign(n, 0);
+  r->cost.assign(n, 0.0f);
+  r->cp.assign(n, 0.0f);
+  r->t5.clear();
+  r->t2.clear();
+  r->states.clear();
+  if (n == 0 || !c.hout) return;
+  const int *hi = reinterpret_cast<const int *>(c.hout);
+  const float *hf = reinterpret_cast<const float *>(c.hout + sizeof(int) * 3 * (size_t)n);
   for (int k = 0; k < n; ++k) {
-    len[k] = hout[n + k];
-    if (with_cost) std::memcpy(&cost[k], &hout[2 * n + k], sizeof(float));
+    r->len[k] = hi[n + k];
+    if (c.with_cost) std::memcpy(&r->cost[k], &hi[2 * n + k], sizeof(float));
     // collisionProbability.cu:89-91: hits / Pmc in binary32; a path longer
     // than the particle table has no CP
-    if (with_cp) cp[k] = len[k] > pb_.table_rows ? -1.0f : ((float)hout[k]) / ((float)pb_.num_mc);
+    if (c.with_cp)
+      r->cp[k] = r->len[k] > c.table_rows ? -1.0f : ((float)hi[k]) / ((float)c.num_mc);
   }
+  const size_t seg_f = c.with_topts ? (size_t)c.segs : 0;
+  if (seg_f > 0) {
+    r->t5.assign(hf, hf + seg_f);
+    r->t2.assign(hf + seg_f, hf + 2 * seg_f);
+  }
+  if (c.states_rows > 0)
+    r->states.assign(hf + 2 * seg_f, hf + 2 * seg_f + (size_t)c.states_rows * kDim);
+}
+
+pump_status_t Planner::eval_candidates(const std::vector<std::vector<float>> &xs, float dt,
+                                      int rows_cap, bool with_cost, bool with_cp,
+                                      std::vector<int> &len, std::vector<float> &cost,
+                                      std::vector<float> &cp) {
+  PUMP_TRY(eval_launch(cs_, xs, dt, rows_cap, with_cost, with_cp, false, 0));
+  if (!xs.empty()) PUMP_TRY(sync());
+  CandResult r;
+  eval_read(cs_, &r);
+  len.swap(r.len);
+  cost.swap(r.cost);
+  cp.swap(r.cp);
   return PUMP_OK;
 }
 
@@ -727,21 +863,37 @@ pump_status_t Planner::search_and_smooth() {
   std::vector<std::vector<float>> cand;
   for (auto &g : goalPaths) cand.push_back(node_states(g.second, nullptr));
   const int rowsCap = pb_.table_rows;
-  std::vector<int> glen;
-  std::vector<float> gcost, cps;
-  PUMP_TRY(eval_candidates(cand, dt_, rowsCap, false, true, glen, gcost, cps));
+  // One round trip for the goal candidates' dense lengths and MC CPs, their
+  // segments' optimal times with tmax 2 (the smoothing's split of the chosen
+  // path, PUMP.cu:445-450), and the unconstrained optimal path from init to
+  // goal at dt / 10 (PUMP.cu:434-441), which depends only on those two
+  // states (every goal path runs from the initial node to the goal node).
+  const int dtMult = 10;
+  const int optCap = pb_.table_rows * dtMult;
+  if (!cand.empty()) {
+    std::vector<std::vector<float>> two(1);
+    two[0].insert(two[0].end(), cand[0].begin(), cand[0].begin() + kDim);
+    two[0].insert(two[0].end(), cand[0].end() - kDim, cand[0].end());
+    PUMP_TRY(eval_launch(co_, two, dt_ / dtMult, optCap, false, false, false, optCap));
+  }
+  PUMP_TRY(eval_launch(cs_, cand, dt_, rowsCap, false, true, true, 0));
+  if (!cand.empty()) PUMP_TRY(sync());
+  CandResult gr;
+  eval_read(cs_, &gr);
+  const std::vector<int> &glen = gr.len;
+  const std::vector<float> &gcp = gr.cp;
   int sel = -1;
   for (size_t k = 0; k < goalPaths.size(); ++k) {
-    if (cps[k] < 0)
+    if (gcp[k] < 0)
       return set_error(PUMP_ERR_CAPACITY, "goal path of %d states exceeds the %d-row particle table",
                        glen[k], pb_.table_rows);
-    if (cps[k] < cpTarget) { sel = (int)k; break; }
+    if (gcp[k] < cpTarget) { sel = (int)k; break; }
   }
   const int last = sel >= 0 ? sel : (int)goalPaths.size() - 1;
   const bool success = sel >= 0;
   res_->success = success ? 1 : 0;
   res_->soln_path_idx = last >= 0 ? goalPaths[last].second : -1;
-  float solnPathCP = last >= 0 ? cps[last] : 0.0f;
+  float solnPathCP = last >= 0 ? gcp[last] : 0.0f;
   float solnPathCost = last >= 0 ? pathCost_[goalPaths[last].second] : 0.0f;
   std::vector<int> nodes;
   std::vector<float> xs = last >= 0 ? node_states(goalPaths[last].second, &nodes) : std::vector<float>();
@@ -750,15 +902,19 @@ pump_status_t Planner::search_and_smooth() {
     for (int k = 0; k < (int)nodes.size() && k < res_->nodes_cap; ++k) res_->nodes[k] = nodes[k];
 
   // smoothing (PUMP.cu:406-545); xsFinal is the reference's xsSmooth after
-  // the loop: the last iterate evaluated, zeros if smoothing did not run
+  // the loop: the last iterate evaluated, zeros if smoothing did not run.
+  // finalT5 / finalT2: its segments' optimal times (tmax 5, 2) from that
+  // evaluation, for the controller path.
   std::vector<float> xsFinal(xs.size(), 0.0f);
+  std::vector<float> finalT5, finalT2;
+  bool haveFinalT = false;
   std::vector<float> xsBest(xs);  // nodes of the path kept so far
   // the dense path kept so far stays on the device (d_best_) until the end
   std::vector<float> bestPath;
   int bestLen = last >= 0 ? glen[last] : 0;
   PUMP_TRY(d_best_.alloc((size_t)rowsCap * kDim));
   auto keep_best = [&](int k, int len) -> pump_status_t {
-    PUMP_CUDA_TRY(cudaMemcpyAsync(d_best_.p, d_cstates_.p + (size_t)k * rowsCap * kDim,
+    PUMP_CUDA_TRY(cudaMemcpyAsync(d_best_.p, cs_.states.p + (size_t)k * rowsCap * kDim,
                                   sizeof(float) * kDim * (size_t)len, cudaMemcpyDeviceToDevice,
                                   s_));
     return PUMP_OK;
@@ -767,33 +923,25 @@ pump_status_t Planner::search_and_smooth() {
   float lastCP = solnPathCP, lastCost = solnPathCost;
   if (success) {
     const int n = (int)(xs.size() / kDim);
-    const int dtMult = 10;
-    std::vector<std::vector<float>> two(1);
-    two[0].insert(two[0].end(), xs.begin(), xs.begin() + kDim);
-    two[0].insert(two[0].end(), xs.end() - kDim, xs.end());
-    const int optCap = pb_.table_rows * dtMult;
-    std::vector<int> olen;
-    std::vector<float> ocost, ocp;
-    PUMP_TRY(eval_candidates(two, dt_ / dtMult, optCap, false, false, olen, ocost, ocp));
-    const int optLen = olen[0];
+    CandResult orr;
+    eval_read(co_, &orr);
+    const int optLen = orr.len[0];
     if (optLen > optCap)
       return set_error(PUMP_ERR_CAPACITY, "unconstrained optimal path of %d states exceeds %d",
                        optLen, optCap);
-    std::vector<float> optPath((size_t)optLen * kDim);
-    PUMP_TRY(d2h(optPath.data(), d_cstates_.p, optPath.size()));
-    // splitPathTopts with tmax 2 (PUMP.cu:445-450)
-    std::vector<float> a0, a1, tsplit;
-    for (int i = 0; i + 1 < n; ++i) {
-      a0.insert(a0.end(), &xs[i * kDim], &xs[(i + 1) * kDim]);
-      a1.insert(a1.end(), &xs[(i + 1) * kDim], &xs[(i + 2) * kDim]);
+    // splitPathTopts with tmax 2 (PUMP.cu:445-450): the chosen candidate's
+    // segments, which follow those of the candidates before it
+    size_t sbase = 0;
+    for (int k = 0; k < last; ++k) {
+      const size_t cnt = cand[k].size() / kDim;
+      sbase += cnt > 1 ? cnt - 1 : 0;
     }
-    PUMP_TRY(topts_of(a0, a1, 2.0f, &tsplit, nullptr));
     std::vector<float> splitT(n, 0.0f);
-    for (int i = 0; i + 1 < n; ++i) splitT[i + 1] = splitT[i] + tsplit[i];
+    for (int i = 0; i + 1 < n; ++i) splitT[i + 1] = splitT[i] + gr.t2[sbase + i];
     std::vector<float> xsOpt((size_t)n * kDim);
     for (int i = 0; i < n; ++i) {
       const int idx = (int)((optLen - 1) * splitT[i] / splitT[n - 1]);
-      for (int d = 0; d < kDim; ++d) xsOpt[(size_t)i * kDim + d] = optPath[(size_t)idx * kDim + d];
+      for (int d = 0; d < kDim; ++d) xsOpt[(size_t)i * kDim + d] = orr.states[(size_t)idx * kDim + d];
     }
     const float epsSmoothCP = (float)0.0002;
     float alpha = 1.0f, alphaU = 1.0f, alphaL = 0.0f;
@@ -821,17 +969,22 @@ pump_status_t Planner::search_and_smooth() {
       std::vector<std::vector<float>> cand(K, std::vector<float>(xs.size()));
       for (int k = 0; k < K; ++k)
         for (size_t i = 0; i < xs.size(); ++i) cand[k][i] = (1 - na[k]) * xs[i] + na[k] * xsOpt[i];
-      std::vector<int> slen;
-      std::vector<float> scost, cps;
-      PUMP_TRY(eval_candidates(cand, dt_, rowsCap, true, true, slen, scost, cps));
+      PUMP_TRY(eval_launch(cs_, cand, dt_, rowsCap, true, true, true, 0));
+      PUMP_TRY(sync());
+      CandResult sr;
+      eval_read(cs_, &sr);
       int k = 0;
       for (int depth = 0; depth < D && it < 30; ++depth, ++it) {
-        const float smoothCost = scost[k];
-        const float cp = cps[k];
+        const float smoothCost = sr.cost[k];
+        const float cp = sr.cp[k];
         if (cp < 0)
           return set_error(PUMP_ERR_CAPACITY, "smoothed path of %d states exceeds the %d-row particle table",
-                           slen[k], pb_.table_rows);
+                           sr.len[k], pb_.table_rows);
         xsFinal = cand[k];
+        // every candidate has n nodes, so candidate k's segments start at k (n - 1)
+        finalT5.assign(sr.t5.begin() + (size_t)k * (n - 1), sr.t5.begin() + (size_t)(k + 1) * (n - 1));
+        finalT2.assign(sr.t2.begin() + (size_t)k * (n - 1), sr.t2.begin() + (size_t)(k + 1) * (n - 1));
+        haveFinalT = true;
         if (cp < cpTarget) alphaL = alpha;
         if (cp >= cpTarget) alphaU = alpha;
         alpha = (alphaL + alphaU) / 2;
@@ -839,7 +992,7 @@ pump_status_t Planner::search_and_smooth() {
         const bool closer = cp > lastCP;
         const bool eqLower = (cp == lastCP && smoothCost < lastCost);
         if (satisfies && (closer || eqLower)) {
-          bestLen = slen[k];
+          bestLen = sr.len[k];
           PUMP_TRY(keep_best(k, bestLen));
           lastCost = smoothCost;
           lastCP = cp;
@@ -853,20 +1006,39 @@ pump_status_t Planner::search_and_smooth() {
       }
     }
   }
-  if (last >= 0 && bestLen > 0) {
-    bestPath.resize((size_t)bestLen * kDim);
-    PUMP_TRY(d2h(bestPath.data(), d_best_.p, bestPath.size()));
-    PUMP_TRY(sync());
-  }
-  if (success && pb_.refine_iters > 0)
+  const bool haveBest = last >= 0 && bestLen > 0;
+  if (success && pb_.refine_iters > 0) {
+    if (haveBest) {
+      bestPath.resize((size_t)bestLen * kDim);
+      PUMP_TRY(d2h(bestPath.data(), d_best_.p, bestPath.size()));
+      PUMP_TRY(sync());
+    }
     PUMP_TRY(refine(xsBest, cpTarget, &lastCP, &lastCost, &bestPath, &bestLen, &xsFinal));
+    // the controller path's node states may have changed: its times are
+    // computed afresh
+    PUMP_TRY(control_launch(xsFinal, nullptr, nullptr));
+    PUMP_TRY(sync());
+  } else {
+    // the kept path's read-back and the controller path in one round trip
+    float *hbest = nullptr;
+    if (haveBest) {
+      PUMP_TRY(ctx_->pinned(Ctx::kPinPaths, sizeof(float) * kDim * (size_t)bestLen, (void **)&hbest));
+      res_->d2h_bytes += (long long)(sizeof(float) * kDim * (size_t)bestLen);
+      PUMP_CUDA_TRY(cudaMemcpyAsync(hbest, d_best_.p, sizeof(float) * kDim * (size_t)bestLen,
+                                    cudaMemcpyDeviceToHost, s_));
+    }
+    PUMP_TRY(control_launch(xsFinal, haveFinalT ? &finalT5 : nullptr,
+                            haveFinalT ? &finalT2 : nullptr));
+    PUMP_TRY(sync());
+    if (haveBest) bestPath.assign(hbest, hbest + (size_t)bestLen * kDim);
+  }
   res_->soln_cp = lastCP;
   res_->soln_cost = lastCost;
   res_->path_len = success ? bestLen : 0;
   if (success && res_->path)
     std::memcpy(res_->path, bestPath.data(),
                 sizeof(float) * kDim * (size_t)std::min(bestLen, res_->path_cap));
-  PUMP_TRY(control_path(xsFinal));
+  PUMP_TRY(control_finish());
   return success ? PUMP_OK : set_error(PUMP_ERR_NO_SOLUTION, "no goal path meets the CP target");
 }
 
@@ -950,7 +1122,7 @@ pump_status_t Planner::refine(const std::vector<float> &xs, float cpTarget, floa
     res_->refined = 1;
     *bestLen = ln[0];
     bestPath->resize((size_t)ln[0] * kDim);
-    PUMP_TRY(d2h(bestPath->data(), d_cstates_.p, bestPath->size()));
+    PUMP_TRY(d2h(bestPath->data(), cs_.states.p, bestPath->size()));
     PUMP_TRY(sync());
     *lastCP = cps[0];
     *lastCost = cost;
@@ -964,59 +1136,84 @@ pump_status_t Planner::refine(const std::vector<float> &xs, float cpTarget, floa
 // that findDiscretizedPath (tmax 5, 2pBVP.cu:53-69) fills; the row count is
 // accumulated as the reference does (an int += float), so trailing rows the
 // segments do not reach stay zero.
-pump_status_t Planner::control_path(const std::vector<float> &xs) {
+pump_status_t Planner::control_launch(const std::vector<float> &xs, const std::vector<float> *t5,
+                                      const std::vector<float> *t2) {
   const int n = (int)(xs.size() / kDim);
   const float controlDt = 0.05f;
-  std::vector<float> a0, a1, tau2, topt5;
-  for (int i = 0; i + 1 < n; ++i) {
-    a0.insert(a0.end(), &xs[(size_t)i * kDim], &xs[(size_t)(i + 1) * kDim]);
-    a1.insert(a1.end(), &xs[(size_t)(i + 1) * kDim], &xs[(size_t)(i + 2) * kDim]);
+  std::vector<float> tau2, topt5;
+  if (t5 && t2 && (int)t5->size() + 1 == n && (int)t2->size() + 1 == n) {
+    tau2 = *t2;
+    topt5 = *t5;
+  } else {
+    std::vector<float> a0, a1;
+    for (int i = 0; i + 1 < n; ++i) {
+      a0.insert(a0.end(), &xs[(size_t)i * kDim], &xs[(size_t)(i + 1) * kDim]);
+      a1.insert(a1.end(), &xs[(size_t)(i + 1) * kDim], &xs[(size_t)(i + 2) * kDim]);
+    }
+    PUMP_TRY(topts_of(a0, a1, 2.0f, &tau2, nullptr));
+    PUMP_TRY(topts_of(a0, a1, 5.0f, &topt5, nullptr));
   }
-  PUMP_TRY(topts_of(a0, a1, 2.0f, &tau2, nullptr));
-  PUMP_TRY(topts_of(a0, a1, 5.0f, &topt5, nullptr));
-  int rows = 1;
-  for (int i = 0; i + 1 < n; ++i) rows = (int)((float)rows + (tau2[i] / controlDt + 1));
-  std::vector<float> out((size_t)rows * kDim, 0.0f);
-  std::vector<int> seg, row;
+  ControlJob &cj = ctrl_;
+  cj.rows = 1;
+  for (int i = 0; i + 1 < n; ++i) cj.rows = (int)((float)cj.rows + (tau2[i] / controlDt + 1));
+  cj.out.assign((size_t)cj.rows * kDim, 0.0f);
+  cj.row.clear();
+  cj.pts = nullptr;
+  std::vector<int> seg;
   std::vector<float> ts;
   int cur = 0;
   for (int i = 0; i + 1 < n; ++i) {
     const int nw = (int)(tau2[i] / controlDt + 1);
     const float dt = topt5[i] / nw;
-    if (cur + nw >= rows)
-      return set_error(PUMP_ERR_CAPACITY, "control path: %d rows past %d", cur + nw + 1, rows);
-    std::memcpy(&out[(size_t)cur * kDim], &xs[(size_t)i * kDim], sizeof(float) * kDim);
+    if (cur + nw >= cj.rows)
+      return set_error(PUMP_ERR_CAPACITY, "control path: %d rows past %d", cur + nw + 1, cj.rows);
+    std::memcpy(&cj.out[(size_t)cur * kDim], &xs[(size_t)i * kDim], sizeof(float) * kDim);
     for (int r = 1; r < nw; ++r) {
       seg.push_back(i);
-      row.push_back(cur + r);
+      cj.row.push_back(cur + r);
       ts.push_back(dt * r);
     }
     cur += nw;
     if (i + 2 == n)
-      std::memcpy(&out[(size_t)cur * kDim], &xs[(size_t)(i + 1) * kDim], sizeof(float) * kDim);
+      std::memcpy(&cj.out[(size_t)cur * kDim], &xs[(size_t)(i + 1) * kDim], sizeof(float) * kDim);
   }
-  const int total = (int)seg.size();
-  if (total > 0) {
-    DevBuf<float> d_out;
-    PUMP_TRY(d_out.alloc((size_t)total * kDim));
-    PUMP_TRY(d_xs_.alloc(xs.size()));
-    PUMP_TRY(d_ts_.alloc(total));
-    PUMP_TRY(d_tau_.alloc(topt5.size()));
-    PUMP_TRY(d_seg_.alloc(total));
-    PUMP_TRY(h2d(d_xs_.p, xs.data(), xs.size()));
-    PUMP_TRY(h2d(d_ts_.p, ts.data(), total));
-    PUMP_TRY(h2d(d_tau_.p, topt5.data(), topt5.size()));
-    PUMP_TRY(h2d(d_seg_.p, seg.data(), total));
-    PUMP_TRY(bvp_path_states(d_xs_.p, d_seg_.p, d_ts_.p, d_tau_.p, total, d_out.p, s_));
-    std::vector<float> pts((size_t)total * kDim);
-    PUMP_TRY(d2h(pts.data(), d_out.p, pts.size()));
-    PUMP_TRY(sync());
-    for (int k = 0; k < total; ++k)
-      std::memcpy(&out[(size_t)row[k] * kDim], &pts[(size_t)k * kDim], sizeof(float) * kDim);
-  }
-  res_->ctrl_len = rows;
+  cj.total = (int)seg.size();
+  if (cj.total == 0) return PUMP_OK;
+  // one upload through pinned memory: node states | sample times | segment
+  // times | segment of each sample; the sampled states come back through
+  // pinned memory with the caller's synchronisation
+  const size_t nx = xs.size(), nt = (size_t)cj.total, nu = topt5.size();
+  const size_t in_f = nx + nt + nu + nt;
+  float *hin = nullptr;
+  PUMP_TRY(ctx_->pinned(Ctx::kPinIn, sizeof(float) * in_f, (void **)&hin));
+  std::memcpy(hin, xs.data(), sizeof(float) * nx);
+  std::memcpy(hin + nx, ts.data(), sizeof(float) * nt);
+  std::memcpy(hin + nx + nt, topt5.data(), sizeof(float) * nu);
+  std::memcpy(hin + nx + nt + nu, seg.data(), sizeof(int) * nt);
+  PUMP_TRY(d_xs_.alloc(in_f));
+  res_->h2d_bytes += (long long)(sizeof(float) * in_f);
+  PUMP_CUDA_TRY(cudaMemcpyAsync(d_xs_.p, hin, sizeof(float) * in_f, cudaMemcpyHostToDevice, s_));
+  PUMP_TRY(d_ctrl_.alloc(nt * kDim));
+  const float *d_x = d_xs_.p;
+  const int *d_seg = reinterpret_cast<const int *>(d_xs_.p + nx + nt + nu);
+  PUMP_TRY(bvp_path_states(d_x, d_seg, d_x + nx, d_x + nx + nt, cj.total, d_ctrl_.p, s_));
+  float *hpts = nullptr;
+  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float) * kDim * nt, (void **)&hpts));
+  res_->d2h_bytes += (long long)(sizeof(float) * kDim * nt);
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hpts, d_ctrl_.p, sizeof(float) * kDim * nt, cudaMemcpyDeviceToHost,
+                                s_));
+  cj.pts = hpts;
+  return PUMP_OK;
+}
+
+pump_status_t Planner::control_finish() {
+  ControlJob &cj = ctrl_;
+  for (int k = 0; k < cj.total && cj.pts; ++k)
+    std::memcpy(&cj.out[(size_t)cj.row[k] * kDim], &cj.pts[(size_t)k * kDim], sizeof(float) * kDim);
+  res_->ctrl_len = cj.rows;
   if (res_->ctrl_path && res_->ctrl_cap > 0)
-    std::memcpy(res_->ctrl_path, out.data(), sizeof(float) * kDim * (size_t)std::min(rows, res_->ctrl_cap));
+    std::memcpy(res_->ctrl_path, cj.out.data(),
+                sizeof(float) * kDim * (size_t)std::min(cj.rows, res_->ctrl_cap));
   return PUMP_OK;
 }
 
@@ -1054,6 +1251,8 @@ pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *
   res->soln_path_idx = -1;
   Ctx *c = Ctx::from(ctx);
   PUMP_TRY(c->activate());
+  PUMP_TRY(c->arena_begin((cudaStream_t)stream));
+  ArenaScope scope(c, (cudaStream_t)stream);
   Planner planner(c, *pb, res, (cudaStream_t)stream, shared, lazy);
   return planner.run();
 }

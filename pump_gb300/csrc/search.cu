@@ -63,18 +63,22 @@ __global__ void claim_kernel(SearchDev sd, const int *g, int n_g) {
 }
 
 // Work items (listed node, chunk of kChkEdges out-edges), chunks per node
-// up to the roadmap's largest degree, taken by blocks in turn so a node of
-// high degree is spread over several blocks.  Per chunk the waypoints
+// up to the roadmap's largest degree, taken by blocks in turn so a node's
+// edges are spread over many blocks.  Per chunk the waypoints
 // (discretize_kernel's arithmetic) are computed one thread per (edge,
 // waypoint) and stored to disc (the chunk's records are contiguous), their
-// positions kept in shared memory; then one thread per edge runs the
-// reference's collision test from shared memory (free_edges_staged_kernel's:
-// boxes broadphase-disjoint from the edge's bounding box dropped first, an
-// exact filter; none dropped for a NaN waypoint or more than kFilterObs
-// boxes).  Each chunk adds its count of free edges to free nodes to the
-// node's count.
+// positions kept in shared memory.  Then kChkLanes threads share each edge:
+// box o goes to lane o % kChkLanes, which tests it against every segment of
+// the edge (the reference's (segment, box) test), skipping first a box that
+// is broadphase-disjoint from the whole edge's bounding box (an exact filter;
+// none skipped when a waypoint is NaN).  The edge is free when no lane found
+// a hit: the reference's result is the AND over its (segment, box) pairs, so
+// the split changes no result, and a search iteration that reaches few nodes
+// runs a short chain of box tests per thread instead of all of them.  Each
+// chunk adds its count of free edges to free nodes to the node's count.
 constexpr int kChkThreads = 256;
-constexpr int kChkEdges = 256;
+constexpr int kChkLanes = 8;
+constexpr int kChkEdges = kChkThreads / kChkLanes;  // 32
 
 size_t check_smem(int numObs, int numDisc) {
   return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)kChkEdges * (numDisc + 1) * 3);
@@ -89,6 +93,7 @@ __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckA
   float *s_wp = s_obs + ((ca.numObs * 12 + 3) & ~3);  // kChkEdges x W x 3 positions
   stage_obstacles(ca.obs, ca.numObs, s_obs);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int el = threadIdx.x / kChkLanes, part = threadIdx.x % kChkLanes;
   const int n_todo = sd.ctl->todo;
   const int chunks = ca.max_degree > kChkEdges ? (ca.max_degree + kChkEdges - 1) / kChkEdges : 1;
   const long long items = (long long)n_todo * chunks;
@@ -98,97 +103,89 @@ __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckA
     const int e1 = sd.go[node + 1];
     const int c0 = sd.go[node] + c * kChkEdges;
     if (c0 >= e1) continue;  // block-uniform: this node has fewer chunks
-    int open = 0;
-    {
-      const int ne = e1 - c0 < kChkEdges ? e1 - c0 : kChkEdges;
-      for (int q = threadIdx.x; q < ne * W; q += kChkThreads) {
-        const int el = q / W, i = q - el * W;
-        const int e = c0 + el;
-        const int b = sd.dst[e];
-        float x0[kDim], x1[kDim], x[kDim];
+    const int ne = e1 - c0 < kChkEdges ? e1 - c0 : kChkEdges;
+    for (int q = threadIdx.x; q < ne * W; q += kChkThreads) {
+      const int eq = q / W, i = q - eq * W;
+      const int e = c0 + eq;
+      const int b = sd.dst[e];
+      float x0[kDim], x1[kDim], x[kDim];
 #pragma unroll
-        for (int d = 0; d < kDim; ++d) {
-          x0[d] = __ldg(&ca.samples[node * kDim + d]);
-          x1[d] = __ldg(&ca.samples[b * kDim + d]);
-        }
-        if (i == 0) {
-#pragma unroll
-          for (int d = 0; d < kDim; ++d) x[d] = x0[d];
-        } else if (i == numDisc) {
-#pragma unroll
-          for (int d = 0; d < kDim; ++d) x[d] = x1[d];
-        } else {
-          const float topt = sd.topt[e];
-          const float dt = topt / numDisc;
-          if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
-          else path_point_f32(dt * i, topt, x0, x1, x);
-        }
-        // consecutive threads write consecutive 24-byte records: a warp's
-        // stores cover one contiguous range
-        float2 *out = reinterpret_cast<float2 *>(ca.disc + ((long long)c0 * W + q) * kDim);
-        out[0] = make_float2(x[0], x[1]);
-        out[1] = make_float2(x[2], x[3]);
-        out[2] = make_float2(x[4], x[5]);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) s_wp[q * 3 + d] = x[d];
+      for (int d = 0; d < kDim; ++d) {
+        x0[d] = __ldg(&ca.samples[node * kDim + d]);
+        x1[d] = __ldg(&ca.samples[b * kDim + d]);
       }
-      __syncthreads();
-      if (threadIdx.x < ne) {
-        const int e = c0 + threadIdx.x;
-        constexpr int kPos = 3;  // floats per staged waypoint
-        const float *wp = s_wp + threadIdx.x * W * kPos;
-        bool ok = true;
+      if (i == 0) {
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) x[d] = x0[d];
+      } else if (i == numDisc) {
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) x[d] = x1[d];
+      } else {
+        const float topt = sd.topt[e];
+        const float dt = topt / numDisc;
+        if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
+        else path_point_f32(dt * i, topt, x0, x1, x);
+      }
+      // consecutive threads write consecutive 24-byte records: a warp's
+      // stores cover one contiguous range
+      float2 *out = reinterpret_cast<float2 *>(ca.disc + ((long long)c0 * W + q) * kDim);
+      out[0] = make_float2(x[0], x[1]);
+      out[1] = make_float2(x[2], x[3]);
+      out[2] = make_float2(x[4], x[5]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) s_wp[q * 3 + d] = x[d];
+    }
+    __syncthreads();
+    bool hit = false;
+    if (el < ne) {
+      constexpr int kPos = 3;  // floats per staged waypoint
+      const float *wp = s_wp + el * W * kPos;
+      float emin[3], emax[3];
+      bool nan = false;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
+      for (int i = 0; i < W; ++i)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const float x = wp[i * kPos + d];
+          nan = nan || x != x;
+          emin[d] = fminf(emin[d], x);
+          emax[d] = fmaxf(emax[d], x);
+        }
+      for (int o = part; o < ca.numObs && !hit; o += kChkLanes) {
+        const float *ob = &s_obs[o * 12];
+        if (!nan && broadphase_valid(emin, emax, ob)) continue;
         float v[3], w[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) v[d] = wp[d];
-        if (ca.numObs <= kFilterObs) {
-          float emin[3], emax[3];
-          bool nan = false;
+        for (int i = 0; i < numDisc && !hit; ++i) {
 #pragma unroll
-          for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
-          for (int i = 0; i < W; ++i)
+          for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
+          hit = segment_box_hit(v, w, ob);
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-              const float x = wp[i * kPos + d];
-              nan = nan || x != x;
-              emin[d] = fminf(emin[d], x);
-              emax[d] = fmaxf(emax[d], x);
-            }
-          uint32_t mask[kFilterObs / 32] = {0u, 0u, 0u, 0u};
-          const int words = (ca.numObs + 31) / 32;
-          for (int o = 0; o < ca.numObs; ++o)
-            if (nan || !broadphase_valid(emin, emax, &s_obs[o * 12])) mask[o >> 5] |= 1u << (o & 31);
-          for (int i = 0; i < numDisc && ok; ++i) {
-#pragma unroll
-            for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
-            ok = segment_valid_masked(v, w, mask, words, s_obs);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) v[d] = w[d];
-          }
-        } else {
-          for (int i = 0; i < numDisc && ok; ++i) {
-#pragma unroll
-            for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
-            ok = segment_valid(v, w, ca.numObs, s_obs);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) v[d] = w[d];
-          }
+          for (int d = 0; d < 3; ++d) v[d] = w[d];
         }
-        sd.free_e[e] = ok ? 1 : 0;
-        open += (ok && sd.free_s[sd.dst[e]]) ? 1 : 0;
       }
-      __syncthreads();  // s_wp is rewritten by the next item
+    }
+    // the edge's lanes are kChkLanes consecutive lanes of one warp
+    const unsigned int hits = __ballot_sync(0xffffffffu, hit);
+    int open = 0;
+    if (el < ne && part == 0) {
+      const int e = c0 + el;
+      const bool ok = ((hits >> (lane & ~(kChkLanes - 1))) & ((1u << kChkLanes) - 1u)) == 0u;
+      sd.free_e[e] = ok ? 1 : 0;
+      open = (ok && sd.free_s[sd.dst[e]]) ? 1 : 0;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) open += __shfl_xor_sync(0xffffffffu, open, o);
     if (lane == 0) s_open[warp] = open;
-    __syncthreads();
+    __syncthreads();  // also: every lane is done with s_wp
     if (threadIdx.x == 0) {
       int tot = 0;
       for (int q = 0; q < kChkThreads / 32; ++q) tot += s_open[q];
       if (tot) atomicAdd(&sd.open_cnt[node], tot);
     }
-    __syncthreads();  // s_open is rewritten by the next item
+    __syncthreads();  // s_open and s_wp are rewritten by the next item
   }
 }
 
@@ -326,58 +323,88 @@ __global__ void dominance_kernel(SearchDev sd, int num_paths, float eps_cp, floa
 // the look-back value, 16 bits each within a tile), so the look-back adds
 // both at once.  The last tile writes the survivor count and the bucket
 // sizes.  Each survivor also moves its particle mask from the stage.
+// A wavefront is typically a few thousand paths, so tiles are small (4 rows
+// of 256) to spread it over many blocks, and each thread issues all loads of
+// its rows before any node-list exchange or store, so their latencies
+// overlap instead of adding up row after row.
+constexpr int kStoreRows = 4;
+constexpr int kStoreTile = kCompactThreads * kStoreRows;  // 1024 items
+constexpr int kStoreWarps = kCompactThreads / 32;
+static_assert(kStoreRows * kStoreWarps == 32, "one (row, warp) count per lane of the scan");
 constexpr unsigned long long kLow31 = (1ull << 31) - 1ull;
 
 __global__ void __launch_bounds__(kCompactThreads) store_kernel(
     SearchDev sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
     const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words, TileScratch ts) {
-  __shared__ TileShared sh;
+  // per (row, warp): survivors | survivors of bucket 1 << 16, then their
+  // exclusive offsets within the tile; entry r * kStoreWarps + warp
+  __shared__ unsigned int s_cnt[kStoreRows * kStoreWarps];
+  __shared__ unsigned long long s_excl;
+  __shared__ int s_timeout;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long n = wave_size(sd.ctl);
-  const long long ntiles = (n + kTile - 1) / kTile;
+  const long long ntiles = (n + kStoreTile - 1) / kStoreTile;
   const unsigned int lt = (1u << lane) - 1u;
   // blocks take tiles in order from the counter until none is left
   while (true) {
     const long long tile = next_tile(ts);
     if (tile >= ntiles) return;  // block-uniform
-    const long long base = tile * kTile;
-    bool surv[kCompactRows];
-    uint8_t bkt[kCompactRows];
+    const long long base = tile * kStoreTile;
+    bool surv[kStoreRows];
+    int node[kStoreRows];
+    float cost[kStoreRows];
 #pragma unroll
-    for (int r = 0; r < kCompactRows; ++r) {
+    for (int r = 0; r < kStoreRows; ++r) {
       const long long i = base + r * kCompactThreads + threadIdx.x;
-      surv[r] = false;
+      uint8_t al = 0, dm = 1;
+      node[r] = 0;
+      cost[r] = 0.0f;
+      if (i < n) {
+        al = sd.alive[i];
+        dm = sd.dominated[i];
+        node[r] = sd.wf_node[i];
+        cost[r] = sd.new_cost[i];
+      }
+      surv[r] = al && !dm && node[r] != 0;
+    }
+    uint8_t bkt[kStoreRows];
+#pragma unroll
+    for (int r = 0; r < kStoreRows; ++r) {
       bkt[r] = 0;
-      if (i < n && sd.alive[i] && !sd.dominated[i]) {
-        const int node = sd.wf_node[i];
-        if (node != 0) {
-          surv[r] = true;
-          float dcost = (sd.new_cost[i] + sd.h[node] - cost_threshold);
-          dcost = (0.0f < dcost) ? dcost : 0.0f;  // std::max((float)0, dCost)
-          bkt[r] = (uint8_t)((((int)(dcost / dr)) + g_idx + 1) % 2);
-        }
+      if (surv[r]) {
+        float dcost = (cost[r] + sd.h[node[r]] - cost_threshold);
+        dcost = (0.0f < dcost) ? dcost : 0.0f;  // std::max((float)0, dCost)
+        bkt[r] = (uint8_t)((((int)(dcost / dr)) + g_idx + 1) % 2);
       }
     }
-    unsigned int bs[kCompactRows], b1[kCompactRows];
+    unsigned int bs[kStoreRows], b1[kStoreRows];
 #pragma unroll
-    for (int r = 0; r < kCompactRows; ++r) {
+    for (int r = 0; r < kStoreRows; ++r) {
       bs[r] = __ballot_sync(0xffffffffu, surv[r]);
       b1[r] = __ballot_sync(0xffffffffu, surv[r] && bkt[r] == 1);
       if (lane == 0)
-        sh.cnt[r][warp] = (unsigned int)__popc(bs[r]) | ((unsigned int)__popc(b1[r]) << 16);
+        s_cnt[r * kStoreWarps + warp] = (unsigned int)__popc(bs[r]) | ((unsigned int)__popc(b1[r]) << 16);
     }
-    // in-tile offsets of both counts (each at most kTile < 2^16), then the
-    // tile's pair in the look-back's packing
     __syncthreads();
     if (warp == 0) {
-      const unsigned int tt = scan_tile_counts(sh.cnt);
+      // (row, warp) order is lane order: one warp scan of the packed pairs
+      // (each half at most kStoreTile < 2^16, so the halves never carry)
+      const unsigned int v = s_cnt[lane];
+      unsigned int incl = v;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const unsigned int o = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += o;
+      }
+      s_cnt[lane] = incl - v;
+      const unsigned int tt = __shfl_sync(0xffffffffu, incl, 31);
       const unsigned long long agg =
           (unsigned long long)(tt & 0xFFFFu) | ((unsigned long long)(tt >> 16) << 31);
       bool to = false;
       const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
       if (lane == 0) {
-        sh.excl = ex_tile;
-        sh.timeout = to;
+        s_excl = ex_tile;
+        s_timeout = to ? 1 : 0;
         if (to) {
           atomicExch(ts.error, 1);
           atomicExch(&sd.ctl->wait_error, 1);
@@ -394,39 +421,58 @@ __global__ void __launch_bounds__(kCompactThreads) store_kernel(
       }
     }
     __syncthreads();
-    if (sh.timeout) return;
-    const long long ex_s = (long long)(sh.excl & kLow31), ex_1 = (long long)(sh.excl >> 31);
+    if (s_timeout) return;  // block-uniform
+    const long long ex_s = (long long)(s_excl & kLow31), ex_1 = (long long)(s_excl >> 31);
     const int gb0 = sd.ctl->g_base[0], gb1 = sd.ctl->g_base[1];
+    // loads of every survivor row first
+    int st[kStoreRows], slot[kStoreRows], prev[kStoreRows];
+    float tm[kStoreRows], cp[kStoreRows];
+    uint4 mk[kStoreRows];
 #pragma unroll
-    for (int r = 0; r < kCompactRows; ++r) {
-      if (!(bs[r] & (1u << lane))) continue;
+    for (int r = 0; r < kStoreRows; ++r) {
+      st[r] = slot[r] = prev[r] = 0;
+      tm[r] = cp[r] = 0.0f;
+      mk[r] = make_uint4(0u, 0u, 0u, 0u);
+      if (!surv[r]) continue;
       const long long i = base + r * kCompactThreads + threadIdx.x;
-      const unsigned int in_tile = sh.cnt[r][warp];
+      const unsigned int in_tile = s_cnt[r * kStoreWarps + warp];
       const long long rank = ex_s + (in_tile & 0xFFFFu) + __popc(bs[r] & lt);
       const long long rank1 = ex_1 + (in_tile >> 16) + __popc(b1[r] & lt);
-      const int st = num_paths + (int)rank;
-      const int node = sd.wf_node[i];
-      const float cp = sd.new_cp[i];
-      sd.path_prev[st] = sd.wf_prev[i];
-      sd.path_node[st] = node;
-      sd.path_cost[st] = sd.new_cost[i];
-      sd.path_time[st] = sd.new_time[i];
-      sd.path_cp[st] = cp;
-      if (bkt[r] == 1) sd.g_list[1][gb1 + (int)rank1] = st;
-      else sd.g_list[0][gb0 + (int)(rank - rank1)] = st;
-      sd.node_next[st] = atomicExch(&sd.node_head[node], st);
-      if (node == sd.goal && cp <= cp_min_soln) atomicOr(&sd.ctl->goal_found, 1);
-      const uint32_t *src = stage + i * words;
-      uint32_t *dst = valid + (long long)st * words;
-      if ((words & 3) == 0) {
-        const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
-        uint4 *d4 = reinterpret_cast<uint4 *>(dst);
-        for (int q = 0; q < words / 4; ++q) d4[q] = s4[q];
+      st[r] = num_paths + (int)rank;
+      slot[r] = bkt[r] == 1 ? gb1 + (int)rank1 : gb0 + (int)(rank - rank1);
+      prev[r] = sd.wf_prev[i];
+      tm[r] = sd.new_time[i];
+      cp[r] = sd.new_cp[i];
+      if (words == 4) mk[r] = reinterpret_cast<const uint4 *>(stage)[i];
+    }
+    // then the node-list exchanges (independent of one another)
+    int old[kStoreRows];
+#pragma unroll
+    for (int r = 0; r < kStoreRows; ++r)
+      old[r] = surv[r] ? atomicExch(&sd.node_head[node[r]], st[r]) : -1;
+    // then the stores
+#pragma unroll
+    for (int r = 0; r < kStoreRows; ++r) {
+      if (!surv[r]) continue;
+      const int p = st[r];
+      sd.path_prev[p] = prev[r];
+      sd.path_node[p] = node[r];
+      sd.path_cost[p] = cost[r];
+      sd.path_time[p] = tm[r];
+      sd.path_cp[p] = cp[r];
+      (bkt[r] == 1 ? sd.g_list[1] : sd.g_list[0])[slot[r]] = p;
+      sd.node_next[p] = old[r];
+      if (node[r] == sd.goal && cp[r] <= cp_min_soln) atomicOr(&sd.ctl->goal_found, 1);
+      uint32_t *dst = valid + (long long)p * words;
+      if (words == 4) {
+        *reinterpret_cast<uint4 *>(dst) = mk[r];
       } else {
+        const long long i = base + r * kCompactThreads + threadIdx.x;
+        const uint32_t *src = stage + i * words;
         for (int q = 0; q < words; ++q) dst[q] = src[q];
       }
     }
-    __syncthreads();  // sh and the tile index are reused by the next tile
+    __syncthreads();  // s_cnt, s_excl and the tile index are reused by the next tile
   }
 }
 
@@ -507,7 +553,7 @@ pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int max_new, int num_p
                            const uint32_t *stage, uint32_t *valid, int words, cudaStream_t s) {
   TileScratch ts{};
   long long ntiles = 0;
-  PUMP_TRY(prepare_tiles(ctx, max_new > 0 ? max_new : 1, s, &ts, &ntiles));
+  PUMP_TRY(prepare_tiles(ctx, max_new > 0 ? max_new : 1, s, &ts, &ntiles, kStoreTile));
   const unsigned blocks = (unsigned)(ntiles < kNumSMs * 4 ? ntiles : kNumSMs * 4);
   store_kernel<<<blocks, kCompactThreads, 0, s>>>(sd, num_paths, g_idx, cost_threshold, dr,
                                                   cp_min_soln, stage, valid, words, ts);

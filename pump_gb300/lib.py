@@ -74,7 +74,7 @@ class PlanResult(C.Structure):
         ("h2d_bytes", i64), ("d2h_bytes", i64),
         ("ctrl_path", vp), ("ctrl_cap", i32), ("ctrl_len", i32),
         ("refine_cp", f32), ("refine_cost", f32), ("refined", i32),
-        ("ms_explore_wait", C.c_double),
+        ("ms_explore_wait", C.c_double), ("ms_wait", C.c_double), ("num_waits", i32),
     ]
 
 
