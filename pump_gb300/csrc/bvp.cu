@@ -307,107 +307,84 @@ __global__ void path_states_kernel(const float *__restrict__ xs, const int *__re
 }
 
 // ------------------------------------------------ candidate paths on device
-// Segments of the candidate paths (node i -> i + 1 of each path) as explicit
-// pairs for the batched BVP.
-__global__ void candidate_segments_kernel(const float *__restrict__ nodes,
-                                          const int *__restrict__ node_off,
-                                          const int *__restrict__ node_cnt,
-                                          const int *__restrict__ seg_base, int n_paths,
-                                          float *__restrict__ x0, float *__restrict__ x1,
-                                          int *__restrict__ seg_path, int *__restrict__ hits) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n_paths) return;
-  if (hits) hits[p] = 0;
-  const int o = node_off[p], n = node_cnt[p], b = seg_base[p];
-  for (int i = 0; i + 1 < n; ++i) {
-#pragma unroll
-    for (int d = 0; d < kDim; ++d) {
-      x0[(b + i) * kDim + d] = nodes[(o + i) * kDim + d];
-      x1[(b + i) * kDim + d] = nodes[(o + i + 1) * kDim + d];
-    }
-    seg_path[b + i] = p;
-  }
-}
-
-// The time recurrence of findOptimalPath (2pBVP.cu:15-32) per path: samples
-// per segment T = (int)((topt - toff) / dt + 1) at t = dt * k + toff, the
-// carry toff = (t - topt) + dt (t is the last sample written, from an
-// earlier segment when T <= 0), and the smoothing's cost sum over the
-// segments (PUMP.cu:499-502) in segment order.
-__global__ void candidate_times_kernel(const int *__restrict__ node_cnt,
-                                       const int *__restrict__ seg_base, int n_paths,
-                                       const float *__restrict__ topt,
-                                       const float *__restrict__ seg_cost, float dt,
-                                       int *__restrict__ seg_T, float *__restrict__ seg_toff,
-                                       int *__restrict__ seg_row, int *__restrict__ len,
-                                       float *__restrict__ cost) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n_paths) return;
-  const int n = node_cnt[p], b = seg_base[p];
-  float toff = 0, t = 0, c = 0;
-  int rows = 0;
-  for (int i = 0; i + 1 < n; ++i) {
-    const float tp = topt[b + i];
-    const int T = (int)((tp - toff) / dt + 1);
-    seg_T[b + i] = T;
-    seg_toff[b + i] = toff;
-    seg_row[b + i] = rows;
-    if (T > 0) t = dt * (T - 1) + toff;  // the last sample's time
-    rows += T;
-    toff = (t - tp) + dt;
-    if (seg_cost) c += seg_cost[b + i];
-  }
-  len[p] = rows;
-  if (cost) cost[p] = c;
-}
-
-// States of every sample, one thread per (path, row): rows of path p start at
-// p * rows_cap (rows at or past rows_cap are not written); the row's segment
+// Per candidate path, from its segments' optimal times: the time recurrence
+// of findOptimalPath (2pBVP.cu:15-32), samples per segment T = (int)((topt -
+// toff) / dt + 1) at t = dt * k + toff, the carry toff = (t - topt) + dt (t
+// is the last sample written, from an earlier segment when T <= 0), and the
+// smoothing's cost sum over the segments (PUMP.cu:499-502) in segment order;
+// then the state of every sample.  Blocks (path, y): every block runs the
+// path's recurrence into shared memory (a few dozen segments, one thread),
+// block y = 0 writes the path's length and cost (and zeroes its MC hit
+// counter), and the blocks share the path's rows.  Rows of path p start at
+// p * rows_cap (rows at or past rows_cap are not written); a row's segment
 // is the last one of the path whose first row is at or before it (segments
 // with no samples share their first row with the next).  The precision mode
 // evaluates the cubic in binary32, as its edge waypoints do.
+constexpr int kRowThreads = 128;
+
 template <int Mode>
-__global__ void candidate_states_kernel(const float *__restrict__ x0, const float *__restrict__ x1,
-                                        const float *__restrict__ topt,
-                                        const int *__restrict__ node_cnt,
-                                        const int *__restrict__ seg_base,
-                                        const int *__restrict__ seg_T,
-                                        const float *__restrict__ seg_toff,
-                                        const int *__restrict__ seg_row,
-                                        const int *__restrict__ len, int n_paths, float dt,
-                                        int rows_cap, float *__restrict__ states) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)n_paths * rows_cap) return;
-  const int p = (int)(t / rows_cap), r = (int)(t - (long long)p * rows_cap);
-  if (r >= len[p]) return;
-  const int b = seg_base[p];
-  int lo = 0, hi = node_cnt[p] - 2;  // segments b + lo .. b + hi
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (seg_row[b + mid] <= r) lo = mid; else hi = mid - 1;
+__global__ void __launch_bounds__(kRowThreads) candidate_rows_kernel(
+    const float *__restrict__ x0, const float *__restrict__ x1, const float *__restrict__ topt,
+    const float *__restrict__ seg_cost, const int *__restrict__ node_cnt,
+    const int *__restrict__ seg_base, float dt, int rows_cap, int *__restrict__ len,
+    float *__restrict__ cost, int *__restrict__ hits, float *__restrict__ states) {
+  extern __shared__ int s_seg[];  // per segment: first row, then toff
+  __shared__ int s_len;
+  const int p = blockIdx.x;
+  const int n = node_cnt[p], b = seg_base[p], ns = n > 1 ? n - 1 : 0;
+  int *srow = s_seg;
+  float *stoff = reinterpret_cast<float *>(s_seg + ns);
+  if (threadIdx.x == 0) {
+    float toff = 0, t = 0, c = 0;
+    int rows = 0;
+    for (int i = 0; i + 1 < n; ++i) {
+      const float tp = topt[b + i];
+      const int T = (int)((tp - toff) / dt + 1);
+      stoff[i] = toff;
+      srow[i] = rows;
+      if (T > 0) t = dt * (T - 1) + toff;  // the last sample's time
+      rows += T;
+      toff = (t - tp) + dt;
+      if (seg_cost) c += seg_cost[b + i];
+    }
+    s_len = rows;
+    if (blockIdx.y == 0) {
+      len[p] = rows;
+      if (cost) cost[p] = c;
+      if (hits) hits[p] = 0;
+    }
   }
-  const int s = b + lo, k = r - seg_row[s];
-  float a[kDim], c[kDim], x[kDim];
+  __syncthreads();
+  if (ns == 0) return;
+  const int L = s_len < rows_cap ? s_len : rows_cap;
+  for (int r = blockIdx.y * kRowThreads + threadIdx.x; r < L; r += gridDim.y * kRowThreads) {
+    int lo = 0, hi = ns - 1;  // segments b + lo .. b + hi
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (srow[mid] <= r) lo = mid; else hi = mid - 1;
+    }
+    const int s = b + lo, k = r - srow[lo];
+    float a[kDim], c[kDim], x[kDim];
 #pragma unroll
-  for (int d = 0; d < kDim; ++d) {
-    a[d] = x0[s * kDim + d];
-    c[d] = x1[s * kDim + d];
+    for (int d = 0; d < kDim; ++d) {
+      a[d] = x0[s * kDim + d];
+      c[d] = x1[s * kDim + d];
+    }
+    if (Mode == PUMP_BVP_PARITY) path_point(dt * k + stoff[lo], topt[s], a, c, x);
+    else path_point_f32(dt * k + stoff[lo], topt[s], a, c, x);
+    const long long t = (long long)p * rows_cap + r;
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) states[t * kDim + d] = x[d];
   }
-  if (Mode == PUMP_BVP_PARITY) path_point(dt * k + seg_toff[s], topt[s], a, c, x);
-  else path_point_f32(dt * k + seg_toff[s], topt[s], a, c, x);
-#pragma unroll
-  for (int d = 0; d < kDim; ++d) states[t * kDim + d] = x[d];
 }
 
 }  // namespace
 
 // ------------------------------------------------------------------ host
-pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_seg, int mode,
-                                    float dt, bool with_cost, int rows_cap, cudaStream_t s) {
+pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_seg, int max_segs,
+                                    int mode, float dt, bool with_cost, int rows_cap,
+                                    cudaStream_t s) {
   if (n_paths <= 0) return PUMP_OK;
-  candidate_segments_kernel<<<grid_for(n_paths, 64), 64, 0, s>>>(
-      cb.nodes, cb.node_off, cb.node_cnt, cb.seg_base, n_paths, cb.x0, cb.x1, cb.seg_path, cb.hits);
-  PUMP_TRY(launch_status("candidate_segments"));
   if (n_seg > 0) {
     // optimal times (tmax 5) and smoothing costs and times (tmax 2) in one
     // launch
@@ -423,23 +400,22 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
     jb.topt[1] = cb.topt2;
     PUMP_TRY(bvp_jobs_launch(jb, mode, s));
   }
-  candidate_times_kernel<<<grid_for(n_paths, 64), 64, 0, s>>>(
-      cb.node_cnt, cb.seg_base, n_paths, cb.topt, with_cost ? cb.seg_cost : nullptr, dt, cb.seg_T,
-      cb.seg_toff, cb.seg_row, cb.len, with_cost ? cb.cost : nullptr);
-  PUMP_TRY(launch_status("candidate_times"));
-  if (n_seg > 0) {
-    const long long rows = (long long)n_paths * rows_cap;
-    if (mode == PUMP_BVP_PARITY)
-      candidate_states_kernel<PUMP_BVP_PARITY><<<grid_for(rows, 64), 64, 0, s>>>(
-          cb.x0, cb.x1, cb.topt, cb.node_cnt, cb.seg_base, cb.seg_T, cb.seg_toff, cb.seg_row,
-          cb.len, n_paths, dt, rows_cap, cb.states);
-    else
-      candidate_states_kernel<PUMP_BVP_PRECISION><<<grid_for(rows, 64), 64, 0, s>>>(
-          cb.x0, cb.x1, cb.topt, cb.node_cnt, cb.seg_base, cb.seg_T, cb.seg_toff, cb.seg_row,
-          cb.len, n_paths, dt, rows_cap, cb.states);
-    PUMP_TRY(launch_status("candidate_states"));
-  }
-  return PUMP_OK;
+  const size_t smem = sizeof(int) * 2 * (size_t)(max_segs > 0 ? max_segs : 1);
+  if (smem > 48 * 1024)
+    return set_error(PUMP_ERR_CAPACITY, "candidate path of %d segments exceeds the row stage", max_segs);
+  int ny = (rows_cap + kRowThreads - 1) / kRowThreads;
+  if (ny > 64) ny = 64;
+  if (ny < 1) ny = 1;
+  const dim3 grid((unsigned)n_paths, (unsigned)ny);
+  if (mode == PUMP_BVP_PARITY)
+    candidate_rows_kernel<PUMP_BVP_PARITY><<<grid, kRowThreads, smem, s>>>(
+        cb.x0, cb.x1, cb.topt, with_cost ? cb.seg_cost : nullptr, cb.node_cnt, cb.seg_base, dt,
+        rows_cap, cb.len, with_cost ? cb.cost : nullptr, cb.hits, cb.states);
+  else
+    candidate_rows_kernel<PUMP_BVP_PRECISION><<<grid, kRowThreads, smem, s>>>(
+        cb.x0, cb.x1, cb.topt, with_cost ? cb.seg_cost : nullptr, cb.node_cnt, cb.seg_base, dt,
+        rows_cap, cb.len, with_cost ? cb.cost : nullptr, cb.hits, cb.states);
+  return launch_status("candidate_rows");
 }
 
 namespace {

@@ -136,20 +136,23 @@ struct BvpJobs {
 };
 pump_status_t bvp_jobs_launch(const BvpJobs &jb, int mode, cudaStream_t stream);
 pump_status_t bvp_jobs_precision_launch(const BvpJobs &jb, cudaStream_t stream);
-// Device buffers of a batch of candidate paths (node states of each path,
-// contiguous): its segments as explicit pairs, their optimal times (tmax 5)
-// and smoothing costs (tmax 2), the dense path of findOptimalPath per path
-// at a fixed stride of rows_cap rows, and per path its length and cost.
+// Device buffers of a batch of candidate paths: per path its node count and
+// first segment; its segments (node i -> i + 1) as explicit pairs x0, x1,
+// paths in order; their optimal times (tmax 5) and smoothing costs (tmax 2),
+// the dense path of findOptimalPath per path at a fixed stride of rows_cap
+// rows, and per path its length and cost.
 struct CandidateBufs {
-  const float *nodes;
-  const int *node_off, *node_cnt, *seg_base;
-  float *x0, *x1, *topt, *seg_cost, *seg_toff, *states, *cost;
-  int *seg_path, *seg_T, *seg_row, *len;
+  const int *node_cnt, *seg_base;
+  const float *x0, *x1;
+  float *topt, *seg_cost, *states, *cost;
+  int *len;
   int *hits;     // zeroed per path when not null (the MC CP counters)
   float *topt2;  // when not null: the segments' optimal times with tmax 2
 };
-pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_seg, int mode,
-                                    float dt, bool with_cost, int rows_cap, cudaStream_t s);
+// max_segs: the most segments of one path.
+pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_seg, int max_segs,
+                                    int mode, float dt, bool with_cost, int rows_cap,
+                                    cudaStream_t s);
 // MC CP hit counts of n_paths dense paths into d_hits (zeroed beforehand):
 // the kernels of mc_cp_async without its memset and CP division.
 pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const int *d_len,

@@ -25,6 +25,7 @@
 // Monte Carlo CP.  Thread per (particle, path) over many paths per launch;
 // obstacles staged in shared memory; the same segment test as freeEdges.
 #include "collide.cuh"
+#include "search.h"
 
 namespace pump {
 namespace {
@@ -234,6 +235,9 @@ struct HsmcParams {
   int P;
   float *cp_out;
   int *error;
+  // the search's new-path step after each CP (when epi_on)
+  HsmcEpilogue epi;
+  int epi_on;
 };
 
 // Shared memory of the boxes variant: the staged boxes, then per warp its
@@ -468,8 +472,19 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) valid_count += __shfl_down_sync(0xffffffffu, valid_count, off);
   if (lane == 0) {
-    p.cp_out[w] = ((float)(P - valid_count)) / P;
+    const float cp = ((float)(P - valid_count)) / P;
+    p.cp_out[w] = cp;
     if (overflow && p.error) atomicExch(p.error, (int)PUMP_ERR_CAPACITY);
+    if (p.epi_on) {
+      // PUMP.cu:164-185: time, cost and the CP cut-off of new path w
+      const HsmcEpilogue &e = p.epi;
+      const int f = e.wf_open[w];
+      e.new_time[w] = e.path_time[prev] + e.topt[f];
+      e.new_cost[w] = e.path_cost[prev] + e.copt[f];
+      const bool alive = !(cp > e.cp_cutoff);
+      e.alive[w] = alive ? 1 : 0;
+      if (alive) e.new_next[w] = atomicExch(&e.new_head[e.wf_node[w]], w);
+    }
   }
 }
 
@@ -721,7 +736,7 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                                int T_rows, float offset_mult, const uint32_t *d_valid_in,
                                uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
                                cudaStream_t stream, const unsigned long long *d_num_new,
-                               const int *d_skip) {
+                               const int *d_skip, const HsmcEpilogue *epi) {
   if (num_new <= 0) return PUMP_OK;
   if ((P + 31) / 32 > kMaxHsmcWords)
     return set_error(PUMP_ERR_CAPACITY, "hsmc: %d particles exceed %d", P, 32 * kMaxHsmcWords);
@@ -754,6 +769,10 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
   hp.error = d_error;
   hp.num_new_dev = d_num_new;
   hp.skip_dev = d_skip;
+  if (epi) {
+    hp.epi = *epi;
+    hp.epi_on = 1;
+  }
   const size_t smem = hsmc_boxes_smem(numObs);
   PUMP_TRY(smem_attr((const void *)hsmc_kernel<true>, smem));
   // with a device-side count, num_new bounds it
@@ -835,7 +854,7 @@ extern "C" pump_status_t pump_hsmc_propagate_boxes(
   return hsmc_boxes_async(num_new, W, d_edge, d_prev, num_edges, base, d_obstacles, numObs, d_disc,
                           maxd2, maxHS, d_times, d_topt, dt, d_offsets_t, Pmc, T_rows, offset_mult,
                           d_valid, d_valid + (size_t)base * words, P, d_path_cp + base, d_error,
-                          (cudaStream_t)stream, nullptr, nullptr);
+                          (cudaStream_t)stream, nullptr, nullptr, nullptr);
 }
 
 extern "C" pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d_len,

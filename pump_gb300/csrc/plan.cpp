@@ -44,7 +44,7 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                                int T_rows, float offset_mult, const uint32_t *d_valid_in,
                                uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
                                cudaStream_t stream, const unsigned long long *d_num_new,
-                               const int *d_skip);
+                               const int *d_skip, const HsmcEpilogue *epi);
 pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
                           const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                           const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
@@ -137,8 +137,8 @@ void halton_samples(const pump_problem &pb, std::vector<float> &s) {
 // path is evaluated in the same round trip as the goal candidates.
 struct CandSet {
   int pin_in, pin_out;
-  DevBuf<float> in, x0, x1, topt, topt2, segcost, toff, states;
-  DevBuf<int> out, segpath, segT, segrow;
+  DevBuf<float> in, topt, topt2, segcost, states;
+  DevBuf<int> out;
   // the batch launched last (read back by eval_read after a synchronisation)
   int n = 0, segs = 0, states_rows = 0, table_rows = 0, num_mc = 0;
   bool with_cost = false, with_cp = false, with_topts = false;
@@ -573,6 +573,10 @@ pump_status_t Planner::explore() {
   long long considered = 0;
   std::vector<int> trace_prev, trace_edge;
   pump_status_t status = PUMP_OK;
+  const HsmcEpilogue epi = search_hsmc_epilogue(sd, cpCutoff);
+  // nodes listed for edge checks: the initial node, then at most the paths
+  // the last iteration stored
+  int maxTodo = 1;
   SearchCtl ctl{};
   SearchCtl *hctl = nullptr;  // pinned read-back of the iteration's counters
   PUMP_TRY(ctx_->pinned(Ctx::kPinCtl, sizeof(SearchCtl), (void **)&hctl));
@@ -588,7 +592,9 @@ pump_status_t Planner::explore() {
     // HSMC, pruning and storing read it there (and do nothing when the
     // iteration would overflow the path store), so the host waits once per
     // iteration, for the counters.
-    if (lazy_) PUMP_TRY(search_check(sd, Gidx, nG, ca, s_));
+    // edge checks of the nodes listed so far (the initial node, then the
+    // nodes first reached by the last iteration's stored paths)
+    if (lazy_) PUMP_TRY(search_check(sd, maxTodo, ca, s_));
     PUMP_TRY(search_expand_scan(ctx_, sd, Gidx, nG, s_));
     PUMP_TRY(search_expand_write(sd, Gidx, nG, numPaths_, M, s_));
     if (res_->wf_trace) {
@@ -615,9 +621,10 @@ pump_status_t Planner::explore() {
     PUMP_TRY(hsmc_boxes_async(maxNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
                               d_disc_.p, maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
                               pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p,
-                              P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf));
-    // cut-off, dominance, storing, buckets (PUMP.cu:164-256)
-    PUMP_TRY(search_prune(sd, maxNew, numPaths_, cpCutoff, epsCP_, epsCost_, s_));
+                              P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf, &epi));
+    // cut-off (written by the HSMC kernel), dominance, storing, buckets
+    // (PUMP.cu:164-256)
+    PUMP_TRY(search_prune(sd, maxNew, numPaths_, cpCutoff, epsCP_, epsCost_, true, s_));
     PUMP_TRY(search_store(ctx_, sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
                           d_stage_.p, d_valid_.p, words_, s_));
     res_->d2h_bytes += (long long)sizeof(SearchCtl);
@@ -642,6 +649,7 @@ pump_status_t Planner::explore() {
       break;
     }
     numPaths_ += (int)ctl.num_valid;
+    maxTodo = (int)ctl.num_valid;
     gCount[0] = ctl.g_count[0];
     gCount[1] = ctl.g_count[1];
     // goal and open-set conditions (PUMP.cu:259-288)
@@ -725,68 +733,59 @@ pump_status_t Planner::eval_launch(CandSet &c, const std::vector<std::vector<flo
   c.num_mc = pb_.num_mc;
   c.hout = nullptr;
   if (n == 0) return PUMP_OK;
-  // one upload through pinned memory: nodes | node offsets, counts, segment
-  // bases, dense-path offsets
-  int rows = 0, segs = 0;
+  // one upload through pinned memory: the segments' start states | their end
+  // states | per path node counts, first segments, dense-path offsets
+  int segs = 0, max_segs = 0;
   for (int k = 0; k < n; ++k) {
     const int cnt = (int)(xs[k].size() / kDim);
-    rows += cnt;
-    segs += cnt > 1 ? cnt - 1 : 0;
+    const int ns = cnt > 1 ? cnt - 1 : 0;
+    segs += ns;
+    max_segs = ns > max_segs ? ns : max_segs;
   }
   c.segs = segs;
-  const size_t nf = (size_t)rows * kDim;
-  const size_t in_bytes = sizeof(float) * nf + sizeof(int) * 4 * (size_t)n;
+  const size_t sf = (size_t)segs * kDim;
+  const size_t in_bytes = sizeof(float) * 2 * sf + sizeof(int) * 3 * (size_t)n;
   char *hin = nullptr;
   PUMP_TRY(ctx_->pinned(c.pin_in, in_bytes, (void **)&hin));
-  float *hnodes = reinterpret_cast<float *>(hin);
-  int *hints = reinterpret_cast<int *>(hin + sizeof(float) * nf);
-  for (int k = 0, r = 0, sg = 0; k < n; ++k) {
+  float *hx0 = reinterpret_cast<float *>(hin);
+  float *hx1 = hx0 + sf;
+  int *hints = reinterpret_cast<int *>(hin + sizeof(float) * 2 * sf);
+  for (int k = 0, sg = 0; k < n; ++k) {
     const int cnt = (int)(xs[k].size() / kDim);
-    hints[k] = r;
-    hints[n + k] = cnt;
-    hints[2 * n + k] = sg;
-    hints[3 * n + k] = k * rows_cap;
-    std::memcpy(hnodes + (size_t)r * kDim, xs[k].data(), sizeof(float) * xs[k].size());
-    r += cnt;
-    sg += cnt > 1 ? cnt - 1 : 0;
+    hints[k] = cnt;
+    hints[n + k] = sg;
+    hints[2 * n + k] = k * rows_cap;
+    for (int i = 0; i + 1 < cnt; ++i, ++sg) {
+      std::memcpy(hx0 + (size_t)sg * kDim, xs[k].data() + (size_t)i * kDim, sizeof(float) * kDim);
+      std::memcpy(hx1 + (size_t)sg * kDim, xs[k].data() + (size_t)(i + 1) * kDim,
+                  sizeof(float) * kDim);
+    }
   }
   PUMP_TRY(c.in.alloc(in_bytes / sizeof(float) + 1));
   PUMP_CUDA_TRY(cudaMemcpyAsync(c.in.p, hin, in_bytes, cudaMemcpyHostToDevice, s_));
-  const int *d_ints = reinterpret_cast<const int *>(c.in.p + nf);
+  const int *d_ints = reinterpret_cast<const int *>(c.in.p + 2 * sf);
   const size_t sg = segs > 0 ? (size_t)segs : 1;
-  PUMP_TRY(c.x0.alloc(sg * kDim));
-  PUMP_TRY(c.x1.alloc(sg * kDim));
   PUMP_TRY(c.topt.alloc(sg));
   if (with_topts) PUMP_TRY(c.topt2.alloc(sg));
   PUMP_TRY(c.segcost.alloc(sg));
-  PUMP_TRY(c.toff.alloc(sg));
-  PUMP_TRY(c.segpath.alloc(sg));
-  PUMP_TRY(c.segT.alloc(sg));
-  PUMP_TRY(c.segrow.alloc(sg));
   // results read back in one copy: MC hit counts | lengths | costs
   PUMP_TRY(c.out.alloc(3 * (size_t)n));
   PUMP_TRY(c.states.alloc((size_t)n * rows_cap * kDim));
   CandidateBufs cb{};
-  cb.nodes = c.in.p;
-  cb.node_off = d_ints;
-  cb.node_cnt = d_ints + n;
-  cb.seg_base = d_ints + 2 * n;
-  cb.x0 = c.x0.p;
-  cb.x1 = c.x1.p;
+  cb.node_cnt = d_ints;
+  cb.seg_base = d_ints + n;
+  cb.x0 = c.in.p;
+  cb.x1 = c.in.p + sf;
   cb.topt = c.topt.p;
   cb.topt2 = with_topts ? c.topt2.p : nullptr;
   cb.seg_cost = c.segcost.p;
-  cb.seg_toff = c.toff.p;
   cb.states = c.states.p;
   cb.hits = with_cp ? c.out.p : nullptr;
   cb.len = c.out.p + n;
   cb.cost = reinterpret_cast<float *>(c.out.p + 2 * n);
-  cb.seg_path = c.segpath.p;
-  cb.seg_T = c.segT.p;
-  cb.seg_row = c.segrow.p;
-  PUMP_TRY(candidate_paths_async(cb, n, segs, pb_.bvp_mode, dt, with_cost, rows_cap, s_));
+  PUMP_TRY(candidate_paths_async(cb, n, segs, max_segs, pb_.bvp_mode, dt, with_cost, rows_cap, s_));
   if (with_cp)
-    PUMP_TRY(mc_cp_hits_async(c.states.p, d_ints + 3 * n, cb.len, n, d_table_, pb_.num_mc,
+    PUMP_TRY(mc_cp_hits_async(c.states.p, d_ints + 2 * n, cb.len, n, d_table_, pb_.num_mc,
                               pb_.table_rows, pb_.offset_mult, obs_p_, nobs_, cb.hits, s_,
                               d_rowmax_));
   // pinned read-back: 3n ints | 2 segs floats (with_topts) | states_rows x 6

@@ -37,7 +37,14 @@ __global__ void search_init_kernel(SearchDev sd) {
     sd.ctl->g_base[1] = 0;
     sd.ctl->wait_error = 0;
     sd.ctl->overflow = 0;
-    sd.ctl->todo = 0;
+    // the initial node is listed for its edge checks unless its edges were
+    // checked up front
+    const bool listed = sd.open_cnt[0] == -1;
+    if (listed) {
+      sd.open_cnt[0] = 0;
+      sd.todo[0] = 0;
+    }
+    sd.ctl->todo = listed ? 1 : 0;
   }
 }
 
@@ -51,16 +58,6 @@ struct ExpandCount {
     return (unsigned int)open_cnt[path_node[g[i]]];
   }
 };
-
-// Nodes of the bucket's paths reached for the first time: the thread that
-// moves a node's count from -1 to 0 lists it for checking.
-__global__ void claim_kernel(SearchDev sd, const int *g, int n_g) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_g; k += gridDim.x * blockDim.x) {
-    const int node = sd.path_node[g[k]];
-    if (sd.open_cnt[node] == -1 && atomicCAS(&sd.open_cnt[node], -1, 0) == -1)
-      sd.todo[atomicAdd(&sd.ctl->todo, 1)] = node;
-  }
-}
 
 // Work items (listed node, chunk of kChkEdges out-edges), chunks per node
 // up to the roadmap's largest degree, taken by blocks in turn so a node's
@@ -445,11 +442,17 @@ __global__ void __launch_bounds__(kCompactThreads) store_kernel(
       cp[r] = sd.new_cp[i];
       if (words == 4) mk[r] = reinterpret_cast<const uint4 *>(stage)[i];
     }
-    // then the node-list exchanges (independent of one another)
+    // then the node-list exchanges (independent of one another), and the
+    // nodes reached for the first time listed for their edge checks (the
+    // thread that moves a node's count from -1 to 0 lists it)
     int old[kStoreRows];
 #pragma unroll
     for (int r = 0; r < kStoreRows; ++r)
       old[r] = surv[r] ? atomicExch(&sd.node_head[node[r]], st[r]) : -1;
+#pragma unroll
+    for (int r = 0; r < kStoreRows; ++r)
+      if (surv[r] && sd.open_cnt[node[r]] == -1 && atomicCAS(&sd.open_cnt[node[r]], -1, 0) == -1)
+        sd.todo[atomicAdd(&sd.ctl->todo, 1)] = node[r];
     // then the stores
 #pragma unroll
     for (int r = 0; r < kStoreRows; ++r) {
@@ -485,19 +488,16 @@ pump_status_t search_init(const SearchDev &sd, cudaStream_t s) {
   return launch_status("search_init_head");
 }
 
-pump_status_t search_check(const SearchDev &sd, int g_idx, int n_g, const CheckArgs &ca,
-                           cudaStream_t s) {
-  if (n_g <= 0) return PUMP_OK;
+pump_status_t search_check(const SearchDev &sd, int max_todo, const CheckArgs &ca, cudaStream_t s) {
+  if (max_todo <= 0) return PUMP_OK;
   const size_t smem = check_smem(ca.numObs, ca.numDisc);
   if (smem > 220 * 1024)
     return set_error(PUMP_ERR_CAPACITY, "%d obstacles and %d waypoints exceed the check stage",
                      ca.numObs, ca.numDisc + 1);
-  claim_kernel<<<grid_for(n_g, 256), 256, 0, s>>>(sd, sd.g_list[g_idx], n_g);
-  PUMP_TRY(launch_status("claim_kernel"));
-  // at most one block per (claimed node, chunk), no more than the GPU holds
+  // at most one block per (listed node, chunk), no more than the GPU holds
   const long long chunks =
       ca.max_degree > kChkEdges ? (ca.max_degree + kChkEdges - 1) / kChkEdges : 1;
-  const long long want = (long long)n_g * chunks;
+  const long long want = (long long)max_todo * chunks;
   const unsigned blocks = (unsigned)(want < kNumSMs * 8 ? want : kNumSMs * 8);
   if (ca.mode == PUMP_BVP_PARITY) {
     PUMP_TRY(smem_attr((const void *)check_kernel<PUMP_BVP_PARITY>, smem));
@@ -538,12 +538,31 @@ pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int n
   return launch_status("expand_write");
 }
 
+HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff) {
+  HsmcEpilogue e{};
+  e.wf_open = sd.wf_open;
+  e.wf_node = sd.wf_node;
+  e.path_time = sd.path_time;
+  e.path_cost = sd.path_cost;
+  e.topt = sd.topt;
+  e.copt = sd.copt;
+  e.new_time = sd.new_time;
+  e.new_cost = sd.new_cost;
+  e.alive = sd.alive;
+  e.new_head = sd.new_head;
+  e.new_next = sd.new_next;
+  e.cp_cutoff = cp_cutoff;
+  return e;
+}
+
 pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float cp_cutoff,
-                           float eps_cp, float eps_cost, cudaStream_t s) {
+                           float eps_cp, float eps_cost, bool new_paths_done, cudaStream_t s) {
   long long blocks = ((long long)(max_new > 0 ? max_new : 1) + 255) / 256;
   if (blocks > kNumSMs * 4) blocks = kNumSMs * 4;
-  new_paths_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, cp_cutoff);
-  PUMP_TRY(launch_status("new_paths"));
+  if (!new_paths_done) {
+    new_paths_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, cp_cutoff);
+    PUMP_TRY(launch_status("new_paths"));
+  }
   dominance_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, num_paths, eps_cp, eps_cost);
   return launch_status("dominance");
 }

@@ -71,15 +71,29 @@ struct CheckArgs {
   int max_degree;  // largest out-degree of the roadmap
 };
 
+// What the HSMC kernel writes for the search after a new path's CP (the
+// first half of PUMP.cu:164-185): its time and cost, whether it survives the
+// CP cut-off, and each survivor linked into its node's list of new paths
+// (emptied by the expansion).
+struct HsmcEpilogue {
+  const int *wf_open, *wf_node;
+  const float *path_time, *path_cost, *topt, *copt;
+  float *new_time, *new_cost;
+  uint8_t *alive;
+  int *new_head, *new_next;
+  float cp_cutoff;
+};
+
 // Path 0 at the initial node in bucket 0 (PUMP.cu:19-34).
 pump_status_t search_init(const SearchDev &sd, cudaStream_t s);
-// The nodes of bucket g_idx's paths that the search reaches for the first
-// time get their out-edges checked (freeEdges, collisionCheck.cu:5-37, with
-// the waypoints of findDiscretizedPath written on the way) and their count
-// of expandable edges.  The reference checks every edge up front; the search
-// reads only these, so the wavefronts are the same.
-pump_status_t search_check(const SearchDev &sd, int g_idx, int n_g, const CheckArgs &ca,
-                           cudaStream_t s);
+// The nodes listed in todo (the initial node, then the nodes of stored
+// paths as the store pass reaches them for the first time) get their
+// out-edges checked (freeEdges, collisionCheck.cu:5-37, with the waypoints
+// of findDiscretizedPath written on the way) and their count of expandable
+// edges, before any path at them is expanded.  The reference checks every
+// edge up front; the search reads only these, so the wavefronts are the
+// same.  max_todo bounds the listed count (sizes the grid).
+pump_status_t search_check(const SearchDev &sd, int max_todo, const CheckArgs &ca, cudaStream_t s);
 // Every node's count of expandable edges from the full free-edge mask (the
 // eager form: all edges checked up front).
 pump_status_t search_count_open(const SearchDev &sd, cudaStream_t s);
@@ -98,11 +112,13 @@ pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n
 pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int num_paths,
                                   int max_paths, cudaStream_t s);
 // New paths' time and cost, the CP cut-off (PUMP.cu:164-185) with per-node
-// lists of the survivors of the cut-off, then epsilon dominance
-// (PUMP.cu:188-218); wavefront size from the device (wave_size), at most
-// max_new (sizes the grids).
+// lists of the survivors of the cut-off (unless the HSMC kernel wrote them:
+// new_paths_done), then epsilon dominance (PUMP.cu:188-218); wavefront size
+// from the device (wave_size), at most max_new (sizes the grids).
 pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float cp_cutoff,
-                           float eps_cp, float eps_cost, cudaStream_t s);
+                           float eps_cp, float eps_cost, bool new_paths_done, cudaStream_t s);
+// The search's part of the HSMC kernel for this search state.
+HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff);
 // One pass over the wavefront (PUMP.cu:221-282): survivors become stored
 // paths num_paths + rank in wavefront order, each is appended to its bucket
 // in the same order, linked into its node's list, goal-tested, and its
