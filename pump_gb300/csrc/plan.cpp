@@ -137,8 +137,8 @@ void halton_samples(const pump_problem &pb, std::vector<float> &s) {
 // path is evaluated in the same round trip as the goal candidates.
 struct CandSet {
   int pin_in, pin_out;
-  DevBuf<float> in, topt, topt2, segcost, states;
-  DevBuf<int> out;
+  DevBuf<float> in, segcost, states;
+  DevBuf<int> out;  // hits | lengths | costs | optimal times (tmax 5, then 2)
   // the batch launched last (read back by eval_read after a synchronisation)
   int n = 0, segs = 0, states_rows = 0, table_rows = 0, num_mc = 0;
   bool with_cost = false, with_cp = false, with_topts = false;
@@ -765,19 +765,20 @@ pump_status_t Planner::eval_launch(CandSet &c, const std::vector<std::vector<flo
   PUMP_CUDA_TRY(cudaMemcpyAsync(c.in.p, hin, in_bytes, cudaMemcpyHostToDevice, s_));
   const int *d_ints = reinterpret_cast<const int *>(c.in.p + 2 * sf);
   const size_t sg = segs > 0 ? (size_t)segs : 1;
-  PUMP_TRY(c.topt.alloc(sg));
-  if (with_topts) PUMP_TRY(c.topt2.alloc(sg));
   PUMP_TRY(c.segcost.alloc(sg));
-  // results read back in one copy: MC hit counts | lengths | costs
-  PUMP_TRY(c.out.alloc(3 * (size_t)n));
+  // results read back in one copy: MC hit counts | lengths | costs, then the
+  // segments' optimal times with tmax 5 and (with_topts) 2
+  const size_t seg_f = with_topts ? (size_t)segs : 0;
+  PUMP_TRY(c.out.alloc(3 * (size_t)n + sg + seg_f));
   PUMP_TRY(c.states.alloc((size_t)n * rows_cap * kDim));
+  float *d_topt = reinterpret_cast<float *>(c.out.p + 3 * (size_t)n);
   CandidateBufs cb{};
   cb.node_cnt = d_ints;
   cb.seg_base = d_ints + n;
   cb.x0 = c.in.p;
   cb.x1 = c.in.p + sf;
-  cb.topt = c.topt.p;
-  cb.topt2 = with_topts ? c.topt2.p : nullptr;
+  cb.topt = d_topt;
+  cb.topt2 = with_topts ? d_topt + segs : nullptr;
   cb.seg_cost = c.segcost.p;
   cb.states = c.states.p;
   cb.hits = with_cp ? c.out.p : nullptr;
@@ -790,19 +791,12 @@ pump_status_t Planner::eval_launch(CandSet &c, const std::vector<std::vector<flo
                               d_rowmax_));
   // pinned read-back: 3n ints | 2 segs floats (with_topts) | states_rows x 6
   // floats of path 0
-  const size_t seg_f = with_topts ? (size_t)segs : 0;
   const size_t st_f = (size_t)c.states_rows * kDim;
-  const size_t out_bytes = sizeof(int) * 3 * (size_t)n + sizeof(float) * (2 * seg_f + st_f);
+  const size_t head = sizeof(int) * 3 * (size_t)n + sizeof(float) * 2 * seg_f;
   char *hout = nullptr;
-  PUMP_TRY(ctx_->pinned(c.pin_out, out_bytes, (void **)&hout));
+  PUMP_TRY(ctx_->pinned(c.pin_out, head + sizeof(float) * st_f, (void **)&hout));
   float *hf = reinterpret_cast<float *>(hout + sizeof(int) * 3 * (size_t)n);
-  PUMP_CUDA_TRY(cudaMemcpyAsync(hout, c.out.p, sizeof(int) * 3 * (size_t)n,
-                                cudaMemcpyDeviceToHost, s_));
-  if (seg_f > 0) {
-    PUMP_CUDA_TRY(cudaMemcpyAsync(hf, c.topt.p, sizeof(float) * seg_f, cudaMemcpyDeviceToHost, s_));
-    PUMP_CUDA_TRY(cudaMemcpyAsync(hf + seg_f, c.topt2.p, sizeof(float) * seg_f,
-                                  cudaMemcpyDeviceToHost, s_));
-  }
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hout, c.out.p, head, cudaMemcpyDeviceToHost, s_));
   if (st_f > 0)
     PUMP_CUDA_TRY(cudaMemcpyAsync(hf + 2 * seg_f, c.states.p, sizeof(float) * st_f,
                                   cudaMemcpyDeviceToHost, s_));
