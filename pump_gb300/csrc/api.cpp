@@ -182,21 +182,32 @@ cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t stream) {
 }
 
 pump_status_t smem_attr(const void *fn, size_t bytes) {
-  if (bytes <= 48 * 1024) return PUMP_OK;
+  // the default limit (48 KB) covers a kernel's static and dynamic shared
+  // memory together, so the kernel's static size is read once per function
+  struct Entry {
+    int dev;
+    const void *fn;
+    size_t static_bytes, dyn_max;  // dyn_max: dynamic size allowed so far
+  };
   static std::mutex mu;
-  static std::vector<std::pair<std::pair<int, const void *>, size_t>> set;
+  static std::vector<Entry> set;
+  constexpr size_t kDefault = 48 * 1024;
   int dev = 0;
   PUMP_CUDA_TRY(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(mu);
-  for (auto &e : set)
-    if (e.first.first == dev && e.first.second == fn) {
-      if (e.second >= bytes) return PUMP_OK;
-      PUMP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-      e.second = bytes;
-      return PUMP_OK;
-    }
+  Entry *e = nullptr;
+  for (auto &x : set)
+    if (x.dev == dev && x.fn == fn) e = &x;
+  if (!e) {
+    cudaFuncAttributes fa{};
+    PUMP_CUDA_TRY(cudaFuncGetAttributes(&fa, fn));
+    const size_t st = fa.sharedSizeBytes;
+    set.push_back({dev, fn, st, st < kDefault ? kDefault - st : 0});
+    e = &set.back();
+  }
+  if (bytes <= e->dyn_max) return PUMP_OK;
   PUMP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  set.push_back({{dev, fn}, bytes});
+  e->dyn_max = bytes;
   return PUMP_OK;
 }
 

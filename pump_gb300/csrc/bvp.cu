@@ -238,56 +238,62 @@ __global__ void bvp_batch_kernel(const BvpJobs jb) {
   if (jb.cost[j]) jb.cost[j][k] = cost_eval(c, tp);
 }
 
-// One thread per (edge, waypoint): findDiscretizedPath, 2pBVP.cu:53-69.  A
-// block's 256 waypoints are contiguous in disc, so they are assembled in
-// shared memory and stored as whole lines.
-// The block size T (128, 256, 512) is picked by the autotuner.
+// One thread per edge: findDiscretizedPath, 2pBVP.cu:53-69.  The edge's end
+// states and time are loaded once for all of its W waypoints; a block's T
+// edges (T x W x 6 floats, contiguous in disc) are assembled in shared
+// memory and stored as whole lines, so the kernel's DRAM traffic is the
+// waypoint records it writes.  The block size T (64, 128, 256) is picked by
+// the autotuner.
+template <int T>
+size_t discretize_smem(int numDisc) {
+  return sizeof(float) * (size_t)T * (numDisc + 1) * kDim;
+}
+
 template <int Mode, int T>
 __global__ void __launch_bounds__(T) discretize_kernel(
     const float *__restrict__ samples, const int *__restrict__ src, const int *__restrict__ dst,
     const float *__restrict__ toptE, long long E, int numDisc, float *__restrict__ disc) {
-  constexpr int kDiscThreads = T;
-  __shared__ __align__(16) float s_out[kDiscThreads * kDim];
+  extern __shared__ float4 s_dyn4[];
+  float *s_out = reinterpret_cast<float *>(s_dyn4);
   const int W = numDisc + 1;
-  const long long base = blockIdx.x * (long long)kDiscThreads;
-  const long long total = E * W;
-  const int nv = (int)(total - base < kDiscThreads ? total - base : kDiscThreads);
-  const long long tid = base + threadIdx.x;
+  const long long e0 = blockIdx.x * (long long)T;
+  const int nv = (int)(E - e0 < T ? E - e0 : T);
   if (threadIdx.x < nv) {
-    const long long e = tid / W;
-    const int i = (int)(tid - e * W);
+    const long long e = e0 + threadIdx.x;
     const int a = src[e], b = dst[e];
+    const float topt = toptE[e];
     float x0[kDim], x1[kDim], x[kDim];
 #pragma unroll
     for (int d = 0; d < kDim; ++d) {
       x0[d] = __ldg(&samples[a * kDim + d]);
       x1[d] = __ldg(&samples[b * kDim + d]);
     }
-    if (i == 0) {
+    float *o = s_out + threadIdx.x * W * kDim;
 #pragma unroll
-      for (int d = 0; d < kDim; ++d) x[d] = x0[d];
-    } else if (i == numDisc) {
-#pragma unroll
-      for (int d = 0; d < kDim; ++d) x[d] = x1[d];
-    } else {
-      const float topt = toptE[e];
-      const float dt = topt / numDisc;
+    for (int d = 0; d < kDim; ++d) {
+      o[d] = x0[d];
+      o[numDisc * kDim + d] = x1[d];
+    }
+    const float dt = topt / numDisc;
+    for (int i = 1; i < numDisc; ++i) {
       if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
       else path_point_f32(dt * i, topt, x0, x1, x);
-    }
 #pragma unroll
-    for (int d = 0; d < kDim; ++d) s_out[threadIdx.x * kDim + d] = x[d];
+      for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+    }
   }
   __syncthreads();
-  block_store(disc + base * kDim, s_out, nv * kDim);
+  block_store(disc + e0 * W * kDim, s_out, nv * W * kDim);
 }
 
 template <int Mode, int T>
 pump_status_t discretize_launch(const float *d_samples, const int *d_src, const int *d_dst,
                                 const float *d_topt, long long E, int numDisc, float *d_disc,
                                 cudaStream_t s) {
-  discretize_kernel<Mode, T><<<grid_for(E * (numDisc + 1), T), T, 0, s>>>(d_samples, d_src, d_dst,
-                                                                         d_topt, E, numDisc, d_disc);
+  const size_t smem = discretize_smem<T>(numDisc);
+  PUMP_TRY(smem_attr((const void *)discretize_kernel<Mode, T>, smem));
+  discretize_kernel<Mode, T><<<grid_for(E, T), T, smem, s>>>(d_samples, d_src, d_dst, d_topt, E,
+                                                             numDisc, d_disc);
   return launch_status("discretize_edges");
 }
 
@@ -401,12 +407,15 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
     PUMP_TRY(bvp_jobs_launch(jb, mode, s));
   }
   const size_t smem = sizeof(int) * 2 * (size_t)(max_segs > 0 ? max_segs : 1);
-  if (smem > 48 * 1024)
+  if (smem > 200 * 1024)
     return set_error(PUMP_ERR_CAPACITY, "candidate path of %d segments exceeds the row stage", max_segs);
   int ny = (rows_cap + kRowThreads - 1) / kRowThreads;
   if (ny > 64) ny = 64;
   if (ny < 1) ny = 1;
   const dim3 grid((unsigned)n_paths, (unsigned)ny);
+  PUMP_TRY(smem_attr(mode == PUMP_BVP_PARITY ? (const void *)candidate_rows_kernel<PUMP_BVP_PARITY>
+                                             : (const void *)candidate_rows_kernel<PUMP_BVP_PRECISION>,
+                     smem));
   if (mode == PUMP_BVP_PARITY)
     candidate_rows_kernel<PUMP_BVP_PARITY><<<grid, kRowThreads, smem, s>>>(
         cb.x0, cb.x1, cb.topt, with_cost ? cb.seg_cost : nullptr, cb.node_cnt, cb.seg_base, dt,
@@ -513,7 +522,10 @@ extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int
     return set_error(PUMP_ERR_BAD_INPUT, "pump_discretize_edges: bad arguments");
   if (E == 0) return PUMP_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  // block sizes 128, 256 (default), 512
+  if (discretize_smem<256>(numDisc) > 220 * 1024)
+    return set_error(PUMP_ERR_CAPACITY, "pump_discretize_edges: %d waypoints per edge exceed the stage",
+                     numDisc + 1);
+  // block sizes 64, 128 (default), 256
   auto go = [&](auto block) -> pump_status_t {
     constexpr int T = decltype(block)::value;
     return mode == PUMP_BVP_PARITY
@@ -523,9 +535,9 @@ extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int
                                                          numDisc, d_disc, s);
   };
   auto run = [&](int c) -> pump_status_t {
-    if (c == 0) return go(std::integral_constant<int, 128>{});
-    if (c == 1) return go(std::integral_constant<int, 256>{});
-    return go(std::integral_constant<int, 512>{});
+    if (c == 0) return go(std::integral_constant<int, 64>{});
+    if (c == 1) return go(std::integral_constant<int, 128>{});
+    return go(std::integral_constant<int, 256>{});
   };
   int choice = 1;
   bool ran = false;

@@ -100,43 +100,55 @@ __global__ void __launch_bounds__(256) free_edges_kernel(const float *__restrict
   is_free[e] = ok ? 1 : 0;
 }
 
-// freeEdges for a block of T consecutive edges whose waypoint positions
-// (contiguous in disc) are staged in shared memory.  Each thread first drops the boxes
-// that are broadphase-disjoint from its edge's bounding box (up to
-// kFilterObs boxes, one bit each; no filter if a waypoint is NaN), then runs
-// the reference's per-segment tests over the remaining boxes in index order.
-// The block size T (64, 128, 256) is picked by the autotuner.
+// freeEdges (collisionCheck.cu:5-37) over the waypoints in disc, block of T
+// edges.  The block's waypoint positions (contiguous in disc) are staged in
+// shared memory; each thread takes the bounding box of its edge's waypoints.
+// Then each warp walks the boxes in order: the edges of the warp whose
+// bounding box a box is not broadphase-disjoint from (every edge when a
+// waypoint is NaN) append the pair (edge, box) to the warp's queue, and
+// whenever 32 pairs are queued the warp tests them, one pair per lane: the
+// pair's segments against its box, the reference's (segment, box) test.  An
+// edge is free when none of its pairs hits.  The reference's result is the
+// AND over the (segment, box) pairs, and a box disjoint from the edge's
+// bounding box passes for every segment, so the filter and the order change
+// no result; the queue keeps the lanes busy where per-lane box lists would
+// leave most of a warp waiting for its longest list.  The block size T (64,
+// 128, 256) is picked by the autotuner.
+constexpr int kQueueSlots = 64;  // per warp: a ring of two rounds of pairs
+
 template <int T>
-__global__ void __launch_bounds__(T) free_edges_staged_kernel(
+__global__ void __launch_bounds__(T) free_edges_queue_kernel(
     const float *__restrict__ obs, int numObs, const float *__restrict__ disc, long long E,
     int numDisc, uint8_t *__restrict__ is_free) {
-  constexpr int kFeThreads = T;
   extern __shared__ float4 s_dyn4[];
+  __shared__ int s_queue[T / 32][kQueueSlots];
+  __shared__ uint8_t s_hit[T];
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   float *s_wp = s_obs + ((numObs * 12 + 3) & ~3);
-  stage_obstacles(obs, numObs, s_obs);
   const int W = numDisc + 1;
-  const long long e0 = blockIdx.x * (long long)kFeThreads;
-  const int nv = (int)(E - e0 < kFeThreads ? E - e0 : kFeThreads);
+  const long long e0 = blockIdx.x * (long long)T;
+  const int nv = (int)(E - e0 < T ? E - e0 : T);
   {  // the block's waypoints are contiguous in disc; keep their positions
+    // (24-byte records: an 8-byte load of x, y and a 4-byte load of z)
     const float *src = disc + e0 * W * kDim;
-    for (int q = threadIdx.x; q < nv * W * kDim; q += kFeThreads) {
-      const int r = q / kDim, d = q - r * kDim;
-      if (d < 3) s_wp[r * 3 + d] = __ldg(&src[q]);
+    for (int r = threadIdx.x; r < nv * W; r += T) {
+      const float2 xy = __ldg(reinterpret_cast<const float2 *>(src + (long long)r * kDim));
+      const float z = __ldg(src + (long long)r * kDim + 2);
+      s_wp[r * 3] = xy.x;
+      s_wp[r * 3 + 1] = xy.y;
+      s_wp[r * 3 + 2] = z;
     }
   }
-  __syncthreads();
-  const int t = threadIdx.x;
-  if (t >= nv) return;
+  s_hit[threadIdx.x] = 0;
+  stage_obstacles(obs, numObs, s_obs);  // ends with __syncthreads
   constexpr int kPos = 3;  // floats per staged waypoint
-  const float *wp = s_wp + t * W * kPos;
-  bool ok = true;
-  float v[3], w[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) v[d] = wp[d];
-  if (numObs <= kFilterObs) {
-    float emin[3], emax[3];
-    bool nan = false;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const unsigned int lt = (1u << lane) - 1u;
+  const bool active = t < nv;
+  float emin[3], emax[3];
+  bool nan = false;
+  if (active) {
+    const float *wp = s_wp + t * W * kPos;
 #pragma unroll
     for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
     for (int i = 0; i < W; ++i)
@@ -147,29 +159,51 @@ __global__ void __launch_bounds__(T) free_edges_staged_kernel(
         emin[d] = fminf(emin[d], x);
         emax[d] = fmaxf(emax[d], x);
       }
-    uint32_t mask[kFilterObs / 32];
-    const int words = (numObs + 31) / 32;
+  }
+  int *q = s_queue[warp];
+  // one queued pair: the edge's lane in the warp (high half), the box
+  auto test_pair = [&](int ent) {
+    const int el = warp * 32 + (ent >> 16), o = ent & 0xFFFF;
+    if (s_hit[el]) return;  // the edge already hit a box
+    const float *wp = s_wp + el * W * kPos;
+    const float *ob = &s_obs[o * 12];
+    float v[3], w[3];
 #pragma unroll
-    for (int k = 0; k < kFilterObs / 32; ++k) mask[k] = 0;
-    for (int o = 0; o < numObs; ++o)
-      if (nan || !broadphase_valid(emin, emax, &s_obs[o * 12])) mask[o >> 5] |= 1u << (o & 31);
-    for (int i = 0; i < numDisc && ok; ++i) {
+    for (int d = 0; d < 3; ++d) v[d] = wp[d];
+    for (int i = 0; i < numDisc; ++i) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
-      ok = segment_valid_masked(v, w, mask, words, s_obs);
+      if (segment_box_hit(v, w, ob)) {
+        s_hit[el] = 1;
+        return;
+      }
 #pragma unroll
       for (int d = 0; d < 3; ++d) v[d] = w[d];
     }
-  } else {
-    for (int i = 0; i < numDisc && ok; ++i) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
-      ok = segment_valid(v, w, numObs, s_obs);
-#pragma unroll
-      for (int d = 0; d < 3; ++d) v[d] = w[d];
+  };
+  int head = 0, tail = 0;  // warp-uniform
+  const float4 *s_obs4 = reinterpret_cast<const float4 *>(s_obs);
+  for (int o = 0; o < numObs; ++o) {
+    // broadphaseValidQ of the edge's bounding box, without branches: box o
+    // is lo = (x0, y0, z0) at floats 0-2 and hi = (x1, y1, z1) at floats 6-8
+    const float4 a = s_obs4[o * 3], b = s_obs4[o * 3 + 1], c = s_obs4[o * 3 + 2];
+    const bool disjoint = (emax[0] <= a.x) | (b.z <= emin[0]) | (emax[1] <= a.y) |
+                          (b.w <= emin[1]) | (emax[2] <= a.z) | (c.x <= emin[2]);
+    const bool need = active && (nan || !disjoint);
+    const unsigned int bal = __ballot_sync(0xffffffffu, need);
+    if (need) q[(tail + __popc(bal & lt)) & (kQueueSlots - 1)] = (lane << 16) | o;
+    tail += __popc(bal);
+    if (tail - head >= 32) {
+      __syncwarp();
+      test_pair(q[(head + lane) & (kQueueSlots - 1)]);
+      head += 32;
+      __syncwarp();  // the slots just taken are rewritten by later boxes
     }
   }
-  is_free[e0 + t] = ok ? 1 : 0;
+  __syncwarp();
+  if (lane < tail - head) test_pair(q[(head + lane) & (kQueueSlots - 1)]);
+  __syncwarp();
+  if (active) is_free[e0 + t] = s_hit[t] ? 0 : 1;
 }
 
 // One thread per waypoint: setupAsBs (hsmc.cu:201-211) fused with
@@ -405,13 +439,13 @@ extern "C" pump_status_t pump_free_edges(const float *d_obstacles, int numObs, c
   auto staged = [&](int T) {
     return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)T * (numDisc + 1) * 3);
   };
-  if (staged(256) <= 220 * 1024) {
+  if (staged(256) <= 200 * 1024 && numObs <= 0xFFFF) {
     cudaStream_t s = (cudaStream_t)stream;
     auto go = [&](auto block) -> pump_status_t {
       constexpr int T = decltype(block)::value;
-      PUMP_TRY(smem_attr((const void *)free_edges_staged_kernel<T>, staged(T)));
-      free_edges_staged_kernel<T><<<grid_for(E, T), T, staged(T), s>>>(d_obstacles, numObs, d_disc,
-                                                                      E, numDisc, d_is_free);
+      PUMP_TRY(smem_attr((const void *)free_edges_queue_kernel<T>, staged(T)));
+      free_edges_queue_kernel<T><<<grid_for(E, T), T, staged(T), s>>>(d_obstacles, numObs, d_disc,
+                                                                     E, numDisc, d_is_free);
       return launch_status("free_edges");
     };
     // block sizes 64, 128 (default), 256

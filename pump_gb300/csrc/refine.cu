@@ -476,6 +476,7 @@ extern "C" pump_status_t pump_refine_paths(pump_ctx *ctx, const pump_refine_args
     const size_t smem = (size_t)a->num_obstacles * 6 * sizeof(float);
     PUMP_TRY(smem_attr((const void *)refine_kernel<true, kStep>, smem));
     PUMP_TRY(smem_attr((const void *)refine_kernel<false, kAccept>, smem));
+    PUMP_TRY(smem_attr((const void *)refine_kernel<false, kPlain>, smem));
     cudaStream_t cs = nullptr;
     PUMP_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     pump_status_t st = cuda_status(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal),
