@@ -423,6 +423,20 @@ pump_status_t pump_plan(pump_ctx *ctx, const pump_problem *pb, pump_plan_result 
 pump_status_t pump_plan_batch(int device, const pump_problem *problems, pump_plan_result *results,
                               pump_status_t *statuses, int n, int workers);
 
+/* Search loop form (process-wide; no reference counterpart).  As a graph,
+ * the whole loop of PUMP.cu:39-290 is one launch of a CUDA graph per query:
+ * a conditional while node repeats the iteration's kernels, and a control
+ * kernel keeps the loop's counters on the device.  Each context
+ * instantiates the graph once per shape class and reuses it.  Otherwise the
+ * host drives the loop, one synchronisation per iteration.  Results are the
+ * same.  level 0: the host drives every loop; 1 (the default): pump_plan's
+ * loops run as graphs, pump_plan_batch's workers drive theirs (many graph
+ * loops at once ran slower than host-driven ones); 2: both run as graphs.
+ * A result that asks for the wavefront trace is always host-driven.  The
+ * environment variable PUMP_SEARCH_GRAPH (0, 1, 2) sets the starting
+ * level. */
+void pump_search_graph(int level);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,6 +42,8 @@ Ctx::~Ctx() {
   cudaGetDevice(&prev);
   cudaSetDevice(device_);
   if (refine_graph.exec) cudaGraphExecDestroy(refine_graph.exec);
+  for (const LoopGraph &g : loop_graphs) cudaGraphExecDestroy(g.exec);
+  if (capture_stream) cudaStreamDestroy(capture_stream);
   for (int i = 0; i < kNumSlots; ++i)
     if (buf_[i]) cudaFree(buf_[i]);
   for (void *p : retired_) cudaFree(p);

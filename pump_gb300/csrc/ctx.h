@@ -22,10 +22,11 @@ class Ctx {
     kPlanA,        // planner buffers (see plan.cpp)
     kRefine,       // refinement descent state (refine.cu)
     kSuperset,     // rn bracket bound and the pairs below it (select.cu)
+    kLoop,         // the search loop graph's argument block and tile scratch
     kNumSlots
   };
   // Pinned host staging buffers (uploads, read-backs of small results).
-  enum PinSlot { kPinIn = 0, kPinOut, kPinOptIn, kPinOptOut, kPinPaths, kPinCtl, kNumPin };
+  enum PinSlot { kPinIn = 0, kPinOut, kPinOptIn, kPinOptOut, kPinPaths, kPinCtl, kPinLoop, kNumPin };
   explicit Ctx(int device) : device_(device) {
     for (int i = 0; i < kNumSlots; ++i) { buf_[i] = nullptr; cap_[i] = 0; }
     for (int i = 0; i < kNumPin; ++i) { pin_[i] = nullptr; pin_cap_[i] = 0; }
@@ -69,6 +70,18 @@ class Ctx {
     cudaGraphExec_t exec = nullptr;
   };
   GraphCache refine_graph;
+
+  // Instantiated graphs of the search loop (search_loop_graph), one per
+  // shape class, reused by every query on this context, and the stream they
+  // are captured on.
+  struct LoopGraph {
+    int lazy, mode, obs_cap, num_disc;
+    long long scan_cap, store_cap;
+    void *base;
+    cudaGraphExec_t exec;
+  };
+  std::vector<LoopGraph> loop_graphs;
+  cudaStream_t capture_stream = nullptr;
 
  private:
   int device_;

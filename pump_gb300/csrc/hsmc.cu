@@ -209,36 +209,6 @@ constexpr int kHsmcThreads = 256;
 constexpr int kHsmcWarps = kHsmcThreads / 32;
 constexpr int kHsmcFilterObs = 128;
 
-struct HsmcParams {
-  int num_new, W;
-  // with num_new_dev the path count is *num_new_dev (0 when *skip_dev is set)
-  const unsigned long long *num_new_dev;
-  const int *skip_dev;
-  const int *wf_edge, *wf_prev;
-  long long num_edges;
-  int num_prev;
-  // cached half-spaces
-  const float *as, *bs;
-  const uint8_t *hs_count;
-  // half-spaces from the boxes
-  const float *obs, *disc;
-  int numObs;
-  float maxd2;
-  int maxHS;
-  const float *times, *topts;
-  float dt;
-  const float *offsets_t;
-  int Pmc, T_rows;
-  float offset_mult;
-  const uint32_t *valid_in;
-  uint32_t *valid_out;
-  int P;
-  float *cp_out;
-  int *error;
-  // the search's new-path step after each CP (when epi_on)
-  HsmcEpilogue epi;
-  int epi_on;
-};
 
 // Shared memory of the boxes variant: the staged boxes, then per warp its
 // half-space slots (a0, a1, a2, b), stored counts per waypoint and the list
@@ -489,9 +459,13 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
 }
 
 template <bool Boxes>
-__global__ void __launch_bounds__(kHsmcThreads, 4) hsmc_kernel(const HsmcParams p) {
+__device__ __forceinline__ void hsmc_run(const HsmcParams &p) {
   extern __shared__ float4 s_dyn4[];
   const int warp = threadIdx.x >> 5;
+  int n = p.num_new;
+  if (p.num_new_dev) n = (p.skip_dev && *p.skip_dev) ? 0 : (int)*p.num_new_dev;
+  // a block with no path leaves before staging anything (block-uniform)
+  if ((long long)blockIdx.x * (blockDim.x >> 5) >= n) return;
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   float4 *hs = nullptr;
   uint8_t *hcnt = nullptr;
@@ -505,13 +479,25 @@ __global__ void __launch_bounds__(kHsmcThreads, 4) hsmc_kernel(const HsmcParams 
     int *s_klist = reinterpret_cast<int *>(s_cnt + kHsmcWarps * kMaxHsSlots);
     klist = s_klist + warp * kHsmcFilterObs;
   }
-  int n = p.num_new;
-  if (p.num_new_dev) n = (p.skip_dev && *p.skip_dev) ? 0 : (int)*p.num_new_dev;
   const int warps = (int)((gridDim.x * (long long)blockDim.x) >> 5);
   for (int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); w < n; w += warps) {
     hsmc_path<Boxes>(p, w, s_obs, hs, hcnt, klist);
     __syncwarp();  // the warp's half-space slots are rewritten by its next path
   }
+}
+
+template <bool Boxes>
+__global__ void __launch_bounds__(kHsmcThreads, 4) hsmc_kernel(const HsmcParams p) {
+  hsmc_run<Boxes>(p);
+}
+
+// The search loop on the device: the parameters from device memory, the
+// stored-path count (the bound on parents) from the loop state.
+__global__ void __launch_bounds__(kHsmcThreads, 4) hsmc_loop_kernel(const HsmcParams *hp,
+                                                                    const LoopState *L) {
+  HsmcParams p = *hp;
+  p.num_prev = L->num_paths;
+  hsmc_run<true>(p);
 }
 
 // -------------------------------------------------------------- MC CP
@@ -729,15 +715,14 @@ bool hsmc_boxes_fits(int numObs, int W, int maxHS) {
          hsmc_boxes_smem(numObs) <= 220 * 1024;
 }
 
-pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int *d_prev,
-                               long long num_edges, int num_prev, const float *d_obs, int numObs,
-                               const float *d_disc, float maxd2, int maxHS, const float *d_times,
-                               const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
-                               int T_rows, float offset_mult, const uint32_t *d_valid_in,
-                               uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
-                               cudaStream_t stream, const unsigned long long *d_num_new,
-                               const int *d_skip, const HsmcEpilogue *epi) {
-  if (num_new <= 0) return PUMP_OK;
+pump_status_t hsmc_boxes_fill(int num_new, int W, const int *d_edge, const int *d_prev,
+                              long long num_edges, int num_prev, const float *d_obs, int numObs,
+                              const float *d_disc, float maxd2, int maxHS, const float *d_times,
+                              const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
+                              int T_rows, float offset_mult, const uint32_t *d_valid_in,
+                              uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
+                              const unsigned long long *d_num_new, const int *d_skip,
+                              const HsmcEpilogue *epi, HsmcParams *out) {
   if ((P + 31) / 32 > kMaxHsmcWords)
     return set_error(PUMP_ERR_CAPACITY, "hsmc: %d particles exceed %d", P, 32 * kMaxHsmcWords);
   if (!hsmc_boxes_fits(numObs, W, maxHS))
@@ -773,6 +758,24 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
     hp.epi = *epi;
     hp.epi_on = 1;
   }
+  *out = hp;
+  return PUMP_OK;
+}
+
+pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int *d_prev,
+                               long long num_edges, int num_prev, const float *d_obs, int numObs,
+                               const float *d_disc, float maxd2, int maxHS, const float *d_times,
+                               const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
+                               int T_rows, float offset_mult, const uint32_t *d_valid_in,
+                               uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
+                               cudaStream_t stream, const unsigned long long *d_num_new,
+                               const int *d_skip, const HsmcEpilogue *epi) {
+  if (num_new <= 0) return PUMP_OK;
+  HsmcParams hp{};
+  PUMP_TRY(hsmc_boxes_fill(num_new, W, d_edge, d_prev, num_edges, num_prev, d_obs, numObs, d_disc,
+                           maxd2, maxHS, d_times, d_topt, dt, d_offsets_t, Pmc, T_rows, offset_mult,
+                           d_valid_in, d_valid_out, P, d_cp_out, d_error, d_num_new, d_skip, epi,
+                           &hp));
   const size_t smem = hsmc_boxes_smem(numObs);
   PUMP_TRY(smem_attr((const void *)hsmc_kernel<true>, smem));
   // with a device-side count, num_new bounds it
@@ -781,6 +784,16 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                                     : grid_for((long long)num_new * 32, kHsmcThreads);
   hsmc_kernel<true><<<blocks, kHsmcThreads, smem, stream>>>(hp);
   return launch_status("hsmc_kernel (boxes)");
+}
+
+pump_status_t hsmc_loop_prepare(int numObs) {
+  return smem_attr((const void *)hsmc_loop_kernel, hsmc_boxes_smem(numObs));
+}
+
+pump_status_t hsmc_loop_launch(const HsmcParams *d_hp, const LoopState *d_L, int numObs,
+                               int blocks, cudaStream_t stream) {
+  hsmc_loop_kernel<<<blocks, kHsmcThreads, hsmc_boxes_smem(numObs), stream>>>(d_hp, d_L);
+  return launch_status("hsmc_loop_kernel");
 }
 
 // Generates the tables on `stream`; the binary64 noise buffer (24 B per

@@ -17,7 +17,7 @@
 namespace pump {
 namespace {
 
-__global__ void search_init_kernel(SearchDev sd) {
+__device__ __forceinline__ void search_init_body(const SearchDev &sd) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < sd.N; i += gridDim.x * blockDim.x)
     sd.node_head[i] = -1;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -47,6 +47,8 @@ __global__ void search_init_kernel(SearchDev sd) {
     sd.ctl->todo = listed ? 1 : 0;
   }
 }
+
+__global__ void search_init_kernel(SearchDev sd) { search_init_body(sd); }
 
 // node_head[0] = path 0 after the per-node reset (separate launch: the
 // reset above is grid-strided).
@@ -82,18 +84,19 @@ size_t check_smem(int numObs, int numDisc) {
 }
 
 template <int Mode>
-__global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckArgs ca) {
+__device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs &ca) {
   extern __shared__ float4 s_dyn4[];
   __shared__ int s_open[kChkThreads / 32];
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   const int numDisc = ca.numDisc, W = numDisc + 1;
   float *s_wp = s_obs + ((ca.numObs * 12 + 3) & ~3);  // kChkEdges x W x 3 positions
-  stage_obstacles(ca.obs, ca.numObs, s_obs);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int el = threadIdx.x / kChkLanes, part = threadIdx.x % kChkLanes;
   const int n_todo = sd.ctl->todo;
   const int chunks = ca.max_degree > kChkEdges ? (ca.max_degree + kChkEdges - 1) / kChkEdges : 1;
   const long long items = (long long)n_todo * chunks;
+  if (blockIdx.x >= items) return;  // no item: leave before staging (block-uniform)
+  stage_obstacles(ca.obs, ca.numObs, s_obs);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int el = threadIdx.x / kChkLanes, part = threadIdx.x % kChkLanes;
   for (long long j = blockIdx.x; j < items; j += gridDim.x) {
     const int t = (int)(j / chunks), c = (int)(j - (long long)t * chunks);
     const int node = sd.todo[t];
@@ -186,6 +189,11 @@ __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckA
   }
 }
 
+template <int Mode>
+__global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckArgs ca) {
+  check_body<Mode>(sd, ca);
+}
+
 // One warp per node: open_cnt[node] = its free edges to free nodes.
 __global__ void count_open_kernel(SearchDev sd) {
   const int lane = threadIdx.x & 31;
@@ -218,8 +226,8 @@ __global__ void max_degree_kernel(const int *__restrict__ go, int N, int *out) {
 // wavefront's nodes get empty lists of new paths; thread 0 empties bucket
 // g_idx and records the bucket sizes the store pass appends after (the
 // expansion reads the bucket through n_g, not through its count).
-__global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g, int g_idx,
-                                    int num_paths, int max_paths) {
+__device__ __forceinline__ void expand_write_body(const SearchDev &sd, const int *g, int n_g,
+                                                  int g_idx, int num_paths, int max_paths) {
   const unsigned long long nn = sd.ctl->num_new;
   const int ovf = nn > (unsigned long long)max_paths
                       ? 1
@@ -265,6 +273,11 @@ __global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g, int g_i
   }
 }
 
+__global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g, int g_idx,
+                                    int num_paths, int max_paths) {
+  expand_write_body(sd, g, n_g, g_idx, num_paths, max_paths);
+}
+
 // PUMP.cu:164-185: time and cost of the new paths and the CP cut-off; the
 // survivors of the cut-off are linked into their node's list of new paths
 // (emptied by the expansion kernel).
@@ -304,10 +317,15 @@ __device__ void dominance_one(SearchDev sd, int i, int num_paths, float eps_cp, 
   sd.dominated[i] = dead;
 }
 
-__global__ void dominance_kernel(SearchDev sd, int num_paths, float eps_cp, float eps_cost) {
+__device__ __forceinline__ void dominance_body(const SearchDev &sd, int num_paths, float eps_cp,
+                                               float eps_cost) {
   const int n = wave_size(sd.ctl);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     dominance_one(sd, i, num_paths, eps_cp, eps_cost);
+}
+
+__global__ void dominance_kernel(SearchDev sd, int num_paths, float eps_cp, float eps_cost) {
+  dominance_body(sd, num_paths, eps_cp, eps_cost);
 }
 
 // PUMP.cu:221-282 in one pass.  A survivor (alive, not dominated, not at the
@@ -329,10 +347,12 @@ constexpr int kStoreTile = kCompactThreads * kStoreRows;  // 1024 items
 constexpr int kStoreWarps = kCompactThreads / 32;
 static_assert(kStoreRows * kStoreWarps == 32, "one (row, warp) count per lane of the scan");
 constexpr unsigned long long kLow31 = (1ull << 31) - 1ull;
+static_assert(kLoopScanTile == kTile && kLoopStoreTile == kStoreTile, "loop tile sizes");
 
-__global__ void __launch_bounds__(kCompactThreads) store_kernel(
-    SearchDev sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
-    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words, TileScratch ts) {
+__device__ __forceinline__ void store_body(
+    const SearchDev &sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
+    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words,
+    const TileScratch &ts) {
   // per (row, warp): survivors | survivors of bucket 1 << 16, then their
   // exclusive offsets within the tile; entry r * kStoreWarps + warp
   __shared__ unsigned int s_cnt[kStoreRows * kStoreWarps];
@@ -479,6 +499,128 @@ __global__ void __launch_bounds__(kCompactThreads) store_kernel(
   }
 }
 
+__global__ void __launch_bounds__(kCompactThreads) store_kernel(
+    SearchDev sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
+    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words, TileScratch ts) {
+  store_body(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts);
+}
+
+// ------------------------------------------- the search loop on the device
+// Graph form of the loop: every kernel reads its arguments from the
+// context's LoopArgs block; the per-iteration values come from the loop
+// state, which the control kernel updates after each iteration.
+
+__device__ __forceinline__ TileScratch tiles_of(const LoopTiles &t) {
+  TileScratch ts{};
+  ts.status = t.status;
+  ts.tile_counter = t.tile_counter;
+  ts.total = t.total;
+  ts.error = t.error;
+  return ts;
+}
+
+// search_init_kernel, the particle-table error word and path 0's particle
+// mask (all P particles valid).
+__global__ void loop_init_kernel(const LoopArgs *a) {
+  const SearchDev sd = a->sd;
+  search_init_body(sd);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a->err = 0;
+  const int words = a->words, P = a->P;
+  uint32_t *valid = a->valid;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < words; q += gridDim.x * blockDim.x) {
+    const int rem = P - q * 32;
+    valid[q] = rem >= 32 ? 0xFFFFFFFFu : ((1u << rem) - 1u);
+  }
+}
+
+// search_init_head_kernel, then the while node's first iteration.
+__global__ void loop_arm_kernel(const LoopArgs *a, cudaGraphConditionalHandle h) {
+  a->sd.node_head[0] = 0;
+  cudaGraphSetConditional(h, 1u);
+}
+
+template <int Mode>
+__global__ void __launch_bounds__(kChkThreads, 4) check_loop_kernel(const LoopArgs *a) {
+  const SearchDev sd = a->sd;
+  const CheckArgs ca = a->ca;
+  check_body<Mode>(sd, ca);
+}
+
+__global__ void __launch_bounds__(kCompactThreads) scan_loop_kernel(const LoopArgs *a) {
+  const SearchDev sd = a->sd;
+  const int g_idx = a->L.g_idx;
+  const long long n = a->L.n_g;
+  const ExpandCount c{g_idx ? sd.g_list[1] : sd.g_list[0], sd.path_node, sd.open_cnt};
+  TileScratch ts = tiles_of(a->scan);
+  ts.copy_to = &sd.ctl->num_new;
+  scan_tiles(n, c, sd.wf_off, ts);
+}
+
+__global__ void expand_write_loop_kernel(const LoopArgs *a) {
+  const SearchDev sd = a->sd;
+  const int g_idx = a->L.g_idx;
+  expand_write_body(sd, g_idx ? sd.g_list[1] : sd.g_list[0], a->L.n_g, g_idx, a->L.num_paths,
+                    a->L.max_paths);
+}
+
+__global__ void dominance_loop_kernel(const LoopArgs *a) {
+  const SearchDev sd = a->sd;
+  dominance_body(sd, a->L.num_paths, a->eps_cp, a->eps_cost);
+}
+
+__global__ void __launch_bounds__(kCompactThreads, 3) store_loop_kernel(const LoopArgs *a) {
+  const SearchDev sd = a->sd;
+  const TileScratch ts = tiles_of(a->store);
+  store_body(sd, a->L.num_paths, a->L.g_idx, a->L.cost_threshold, a->L.dr, a->cp_min_soln,
+             a->stage, a->valid, a->words, ts);
+}
+
+// The host loop's bookkeeping after an iteration's counters are back
+// (PUMP.cu:259-288), then the condition of the next iteration.  A guard
+// ends the loop after 64 iterations whatever the state says.
+__global__ void loop_control_kernel(LoopArgs *a, cudaGraphConditionalHandle h) {
+  LoopState &L = a->L;
+  const SearchCtl c = *a->sd.ctl;
+  int cont = 0;
+  ++L.guard;
+  if (c.overflow == 1) {
+    L.status = kLoopWavefrontOverflow;
+  } else {
+    const int num_new = (int)c.num_new;
+    if (L.itrs <= 32) L.wavefront_sizes[L.itrs - 1] = num_new;
+    if (num_new == 0) {
+    } else if (c.overflow == 2) {
+      L.status = kLoopPathsWouldOverflow;
+    } else {
+      L.considered += num_new;
+      if (c.wait_error || *a->scan.error) {
+        L.status = kLoopWaitError;
+      } else {
+        L.num_paths += (int)c.num_valid;
+        L.g_count[0] = c.g_count[0];
+        L.g_count[1] = c.g_count[1];
+        if (!c.goal_found && !(c.g_count[0] == 0 && c.g_count[1] == 0)) {
+          L.g_idx = (L.g_idx + 1) % 2;
+          L.cost_threshold += L.dr;
+          if (L.num_paths >= L.max_paths) {
+            L.status = kLoopPathsFull;
+          } else if (L.itrs < L.max_itrs) {
+            ++L.itrs;
+            L.n_g = L.g_count[L.g_idx];
+            if (L.n_g == 0) {
+              if (L.itrs <= 32) L.wavefront_sizes[L.itrs - 1] = 0;
+            } else {
+              cont = 1;
+            }
+          }
+        }
+      }
+    }
+  }
+  if (L.guard >= 64) cont = 0;
+  cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
 }  // namespace
 
 pump_status_t search_init(const SearchDev &sd, cudaStream_t s) {
@@ -577,6 +719,88 @@ pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int max_new, int num_p
   store_kernel<<<blocks, kCompactThreads, 0, s>>>(sd, num_paths, g_idx, cost_threshold, dr,
                                                   cp_min_soln, stage, valid, words, ts);
   return launch_status("store_kernel");
+}
+
+pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numObs, int numDisc,
+                                const LoopTiles &scan, const LoopTiles &store,
+                                cudaStream_t capture_stream, cudaGraphExec_t *out) {
+  *out = nullptr;
+  const size_t chk_smem = check_smem(numObs, numDisc);
+  if (chk_smem > 220 * 1024)
+    return set_error(PUMP_ERR_CAPACITY, "%d obstacles and %d waypoints exceed the check stage",
+                     numObs, numDisc + 1);
+  const void *chk = mode == PUMP_BVP_PARITY ? (const void *)check_loop_kernel<PUMP_BVP_PARITY>
+                                            : (const void *)check_loop_kernel<PUMP_BVP_PRECISION>;
+  if (lazy) PUMP_TRY(smem_attr(chk, chk_smem));
+  PUMP_TRY(hsmc_loop_prepare(numObs));
+  cudaGraph_t g = nullptr;
+  PUMP_CUDA_TRY(cudaGraphCreate(&g, 0));
+  // the while node's condition starts at 0 and is set by the arm kernel
+  // upstream of it, so the body runs only if the device sets it
+  pump_status_t st = PUMP_OK;
+  cudaGraphConditionalHandle h{};
+  cudaGraphNode_t n_init = nullptr, n_arm = nullptr, n_loop = nullptr;
+  cudaGraphNodeParams cp{};
+  st = cuda_status(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault),
+                   "cudaGraphConditionalHandleCreate");
+  if (st == PUMP_OK) {
+    cudaKernelNodeParams kp{};
+    void *init_args[1] = {&d_args};
+    kp.func = (void *)loop_init_kernel;
+    kp.gridDim = dim3(kNumSMs * 2);
+    kp.blockDim = dim3(256);
+    kp.kernelParams = init_args;
+    st = cuda_status(cudaGraphAddKernelNode(&n_init, g, nullptr, 0, &kp), "cudaGraphAddKernelNode");
+  }
+  if (st == PUMP_OK) {
+    cudaKernelNodeParams kp{};
+    void *arm_args[2] = {&d_args, &h};
+    kp.func = (void *)loop_arm_kernel;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.kernelParams = arm_args;
+    st = cuda_status(cudaGraphAddKernelNode(&n_arm, g, &n_init, 1, &kp), "cudaGraphAddKernelNode");
+  }
+  if (st == PUMP_OK) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    st = cuda_status(cudaGraphAddNode(&n_loop, g, &n_arm, nullptr, 1, &cp), "cudaGraphAddNode");
+  }
+  if (st == PUMP_OK) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t cs = capture_stream;
+    st = cuda_status(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeRelaxed),
+                     "cudaStreamBeginCaptureToGraph");
+    if (st == PUMP_OK) {
+      const size_t scan_zero = sizeof(unsigned long long) * (size_t)(scan.cap + 2) + 8;
+      const size_t store_zero = sizeof(unsigned long long) * (size_t)(store.cap + 2) + 8;
+      // fixed grids (the kernels loop over the device-side counts)
+      const int g_check = kNumSMs * 8, g_scan = kNumSMs * 2, g_wide = kNumSMs * 4;
+      if (lazy) {
+        if (mode == PUMP_BVP_PARITY)
+          check_loop_kernel<PUMP_BVP_PARITY><<<g_check, kChkThreads, chk_smem, cs>>>(d_args);
+        else
+          check_loop_kernel<PUMP_BVP_PRECISION><<<g_check, kChkThreads, chk_smem, cs>>>(d_args);
+      }
+      cudaMemsetAsync(scan.total, 0, scan_zero, cs);
+      scan_loop_kernel<<<g_scan, kCompactThreads, 0, cs>>>(d_args);
+      expand_write_loop_kernel<<<g_wide, 256, 0, cs>>>(d_args);
+      hsmc_loop_launch(&d_args->hp, &d_args->L, numObs, g_wide, cs);
+      dominance_loop_kernel<<<g_wide, 256, 0, cs>>>(d_args);
+      cudaMemsetAsync(store.total, 0, store_zero, cs);
+      store_loop_kernel<<<g_wide, kCompactThreads, 0, cs>>>(d_args);
+      loop_control_kernel<<<1, 1, 0, cs>>>(d_args, h);
+      cudaGraph_t captured = nullptr;
+      const pump_status_t ce = cuda_status(cudaStreamEndCapture(cs, &captured), "cudaStreamEndCapture");
+      st = ce == PUMP_OK ? launch_status("search loop capture") : ce;
+    }
+  }
+  if (st == PUMP_OK) st = cuda_status(cudaGraphInstantiate(out, g, 0), "cudaGraphInstantiate");
+  cudaGraphDestroy(g);
+  return st;
 }
 
 }  // namespace pump

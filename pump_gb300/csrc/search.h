@@ -84,6 +84,90 @@ struct HsmcEpilogue {
   float cp_cutoff;
 };
 
+// Arguments of the HSMC kernel (hsmc.cu).
+struct HsmcParams {
+  int num_new, W;
+  // with num_new_dev the path count is *num_new_dev (0 when *skip_dev is set)
+  const unsigned long long *num_new_dev;
+  const int *skip_dev;
+  const int *wf_edge, *wf_prev;
+  long long num_edges;
+  int num_prev;
+  // cached half-spaces
+  const float *as, *bs;
+  const uint8_t *hs_count;
+  // half-spaces from the boxes
+  const float *obs, *disc;
+  int numObs;
+  float maxd2;
+  int maxHS;
+  const float *times, *topts;
+  float dt;
+  const float *offsets_t;
+  int Pmc, T_rows;
+  float offset_mult;
+  const uint32_t *valid_in;
+  uint32_t *valid_out;
+  int P;
+  float *cp_out;
+  int *error;
+  // the search's new-path step after each CP (when epi_on)
+  HsmcEpilogue epi;
+  int epi_on;
+};
+
+// The search loop run on the device: a CUDA graph whose conditional while
+// node repeats one iteration's kernels.  The iteration's kernels read the
+// values the host loop passes as arguments from this state, and the control
+// kernel at the end of each iteration updates it exactly as the host loop
+// does (PUMP.cu:39-290), then sets the while node's condition.
+struct LoopState {
+  // per query
+  int max_itrs, max_paths;
+  float dr;
+  // the loop
+  int itrs, g_idx, n_g, num_paths, status, guard;
+  float cost_threshold;
+  long long considered;
+  int g_count[2];
+  int wavefront_sizes[32];
+};
+enum LoopStatus {
+  kLoopOk = 0,
+  kLoopWavefrontOverflow,  // wavefront larger than maxPathCount
+  kLoopPathsWouldOverflow, // stored paths would reach maxPathCount
+  kLoopWaitError,          // a look-back wait of the store pass gave up
+  kLoopPathsFull           // stored paths reached maxPathCount
+};
+
+// Items per look-back tile of the loop's scan and store passes.
+constexpr int kLoopScanTile = 4096;
+constexpr int kLoopStoreTile = 1024;
+
+// Tile scratch of one look-back pass of the loop (zeroed before each pass):
+// total, status words (one per tile, from status[0]), tile counter, error.
+struct LoopTiles {
+  unsigned long long *total, *status;
+  unsigned int *tile_counter;
+  int *error;
+  long long cap;  // tiles
+};
+
+// Everything the loop's kernels read, at one device address per context.
+struct LoopArgs {
+  SearchDev sd;
+  CheckArgs ca;
+  HsmcParams hp;
+  LoopState L;
+  LoopTiles scan, store;
+  // the store pass
+  float cp_min_soln, eps_cp, eps_cost, cp_cutoff;
+  const uint32_t *stage;
+  uint32_t *valid;
+  int words, P;
+  int *err;  // the particle-table error word (zeroed at the start)
+};
+
 // Path 0 at the initial node in bucket 0 (PUMP.cu:19-34).
 pump_status_t search_init(const SearchDev &sd, cudaStream_t s);
 // The nodes listed in todo (the initial node, then the nodes of stored
@@ -128,5 +212,28 @@ HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff);
 pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int max_new, int num_paths,
                            int g_idx, float cost_threshold, float dr, float cp_min_soln,
                            const uint32_t *stage, uint32_t *valid, int words, cudaStream_t s);
+
+// The graph of the search loop for the argument block at d_args (device):
+// init, then a while node over {[lazy: edge checks], scan, expansion, HSMC,
+// dominance, store, control}.  Launch shapes are fixed (grid-stride and
+// tile-counter loops); dynamic shared memory is sized for numObs boxes and
+// numDisc waypoints per edge.  Kernel attributes are set here, before the
+// capture.
+pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numObs, int numDisc,
+                                const LoopTiles &scan, const LoopTiles &store,
+                                cudaStream_t capture_stream, cudaGraphExec_t *out);
+
+// HSMC in the loop graph (hsmc.cu).
+pump_status_t hsmc_loop_prepare(int numObs);
+pump_status_t hsmc_loop_launch(const HsmcParams *d_hp, const LoopState *d_L, int numObs,
+                               int blocks, cudaStream_t stream);
+pump_status_t hsmc_boxes_fill(int num_new, int W, const int *d_edge, const int *d_prev,
+                              long long num_edges, int num_prev, const float *d_obs, int numObs,
+                              const float *d_disc, float maxd2, int maxHS, const float *d_times,
+                              const float *d_topt, float dt, const float *d_offsets_t, int Pmc,
+                              int T_rows, float offset_mult, const uint32_t *d_valid_in,
+                              uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
+                              const unsigned long long *d_num_new, const int *d_skip,
+                              const HsmcEpilogue *epi, HsmcParams *out);
 
 }  // namespace pump

@@ -163,3 +163,50 @@ def test_plan_with_refinement(name, gpu, pumplib, goldens):
         assert res.soln_cost < float(g["soln_cost_printed"]) * (1 + 1e-5)
     else:
         assert "%g" % res.soln_cost == "%g" % float(g["soln_cost_printed"])
+
+
+def _fields(res):
+    f32 = lambda x: int(np.float32(x).view(np.uint32))
+    return (res.num_edges, res.iterations, res.num_paths, res.num_considered, res.goal_paths,
+            res.success, res.soln_path_idx, f32(res.soln_cp), f32(res.soln_cost), res.path_len,
+            res.ctrl_len, tuple(res.wavefront_sizes))
+
+
+def test_search_graph_equals_host_loop(gpu, pumplib, goldens):
+    """The search loop as one graph launch (conditional while node, counters
+    kept by a control kernel) gives exactly the host-driven loop's results,
+    for single queries (edges checked up front) and batches (edges checked
+    when the search reaches their nodes)."""
+    torch, ctx = gpu
+    L = pumplib.load()
+    from pump_gb300 import workloads
+    try:
+        for name in CASES:
+            pb, _obs = make_problem(pumplib, goldens[name])
+            out = []
+            for on in (0, 1):
+                L.pump_search_graph(on)
+                st, res, path, nodes = run_plan(pumplib, ctx, pb)
+                out.append((st, _fields(res), path.view(np.uint32).tobytes(), nodes.tobytes(),
+                            run_plan.ctrl.view(np.uint32).tobytes()))
+            assert out[0] == out[1], name
+        qs = workloads.batch_queries(8, seed=91, n_range=(200, 1200), obs_range=(5, 60))
+        keep = []
+        pbs = (pumplib.Problem * len(qs))(*[fill_problem(pumplib, q, keep) for q in qs])
+        for k in range(len(qs)):
+            if k % 2:
+                pbs[k].bvp_mode = pumplib.PUMP_BVP_PRECISION
+        got = []
+        for level in (0, 2):  # batch workers host-driven, then as graphs
+            L.pump_search_graph(level)
+            res = (pumplib.PlanResult * len(qs))()
+            paths = [np.zeros((400, 6), np.float32) for _ in qs]
+            for k in range(len(qs)):
+                res[k].path, res[k].path_cap = paths[k].ctypes.data, 400
+            sts = (C.c_int * len(qs))()
+            pumplib.check(L.pump_plan_batch(0, pbs, res, sts, len(qs), 3))
+            got.append([(sts[k], _fields(res[k]), paths[k][: res[k].path_len].view(np.uint32).tobytes())
+                        for k in range(len(qs))])
+        assert got[0] == got[1]
+    finally:
+        L.pump_search_graph(1)
