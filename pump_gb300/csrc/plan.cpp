@@ -205,6 +205,9 @@ class Planner {
   // The search loop as one launch of the context's loop graph; fills the
   // counters the host loop keeps (iterations, stored and considered paths,
   // wavefront sizes) and the loop's status.
+  // The context's loop region for M paths: the graph's argument block, then
+  // the tile scratch of the expansion scan and of the store pass.
+  pump_status_t loop_region(int M, char **base, size_t *args_b, LoopTiles *scan, LoopTiles *store);
   pump_status_t explore_graph(const SearchDev &sd, const CheckArgs &ca, const HsmcEpilogue &epi,
                               int M, float cpCutoff, float cpMinSoln, float dr, int *itrs,
                               long long *considered, pump_status_t *status);
@@ -609,10 +612,21 @@ pump_status_t Planner::explore() {
   SearchCtl ctl{};
   SearchCtl *hctl = nullptr;  // pinned read-back of the iteration's counters
   PUMP_TRY(ctx_->pinned(Ctx::kPinCtl, sizeof(SearchCtl), (void **)&hctl));
+  LoopTiles scanT{}, storeT{};
   if (graph_loop) {
     const auto tw = clk::now();
     PUMP_TRY(explore_graph(sd, ca, epi, M, cpCutoff, cpMinSoln, dr, &itrs, &considered, &status));
     res_->ms_explore_wait += ms_since(tw);
+  } else {
+    // the tile scratch of the scan and the store pass, zeroed once here and
+    // then by each iteration's expansion kernel
+    char *base = nullptr;
+    size_t args_b = 0;
+    PUMP_TRY(loop_region(M, &base, &args_b, &scanT, &storeT));
+    PUMP_CUDA_TRY(cudaMemsetAsync(base + args_b, 0,
+                                  sizeof(unsigned long long) * (size_t)(loop_tile_words(scanT.cap) +
+                                                                        loop_tile_words(storeT.cap)),
+                                  s_));
   }
   while (!graph_loop && itrs < maxItrs) {
     ++itrs;
@@ -629,8 +643,8 @@ pump_status_t Planner::explore() {
     // edge checks of the nodes listed so far (the initial node, then the
     // nodes first reached by the last iteration's stored paths)
     if (lazy_) PUMP_TRY(search_check(sd, maxTodo, ca, s_));
-    PUMP_TRY(search_expand_scan(ctx_, sd, Gidx, nG, s_));
-    PUMP_TRY(search_expand_write(sd, Gidx, nG, numPaths_, M, s_));
+    PUMP_TRY(search_expand_scan(sd, Gidx, nG, scanT, s_));
+    PUMP_TRY(search_expand_write(sd, Gidx, nG, numPaths_, M, scanT, storeT, s_));
     if (res_->wf_trace) {
       unsigned long long nn = 0;
       PUMP_TRY(d2h(&nn, &d_ctl.p->num_new, 1));
@@ -659,10 +673,10 @@ pump_status_t Planner::explore() {
     // cut-off (written by the HSMC kernel), dominance, storing, buckets
     // (PUMP.cu:164-256)
     PUMP_TRY(search_prune(sd, maxNew, numPaths_, cpCutoff, epsCP_, epsCost_, true, s_));
-    PUMP_TRY(search_store(ctx_, sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln,
-                          d_stage_.p, d_valid_.p, words_, s_));
+    // the store pass's last block leaves the counters in hctl (pinned)
+    PUMP_TRY(search_store(sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln, d_stage_.p,
+                          d_valid_.p, words_, storeT, hctl, s_));
     res_->d2h_bytes += (long long)sizeof(SearchCtl);
-    PUMP_CUDA_TRY(cudaMemcpyAsync(hctl, d_ctl.p, sizeof(SearchCtl), cudaMemcpyDeviceToHost, s_));
     PUMP_TRY(sync());
     ctl = *hctl;
     res_->ms_explore_wait += ms_since(tw);
@@ -723,10 +737,8 @@ pump_status_t Planner::explore() {
   return status;
 }
 
-pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
-                                     const HsmcEpilogue &epi, int M, float cpCutoff,
-                                     float cpMinSoln, float dr, int *itrs, long long *considered,
-                                     pump_status_t *status) {
+pump_status_t Planner::loop_region(int M, char **base, size_t *args_b, LoopTiles *scan,
+                                   LoopTiles *store) {
   // tile capacities of the scan (over a bucket) and the store pass (over a
   // wavefront), both at most M + 1 items, in power-of-two classes
   auto pow2 = [](long long v) {
@@ -737,27 +749,41 @@ pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
   const long long scan_cap = pow2((M + 1 + kLoopScanTile - 1) / kLoopScanTile + 1);
   const long long store_cap = pow2((M + 1 + kLoopStoreTile - 1) / kLoopStoreTile + 1);
   auto round256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  const size_t args_b = round256(sizeof(LoopArgs));
-  const size_t scan_b = round256(sizeof(unsigned long long) * (size_t)(scan_cap + 2) + 8);
-  const size_t store_b = round256(sizeof(unsigned long long) * (size_t)(store_cap + 2) + 8);
-  char *base = nullptr;
-  PUMP_TRY(ctx_->scratch(Ctx::kLoop, args_b + scan_b + store_b, (void **)&base));
+  *args_b = round256(sizeof(LoopArgs));
+  const size_t scan_b = sizeof(unsigned long long) * (size_t)loop_tile_words(scan_cap);
+  const size_t store_b = sizeof(unsigned long long) * (size_t)loop_tile_words(store_cap);
+  PUMP_TRY(ctx_->scratch(Ctx::kLoop, *args_b + scan_b + store_b, (void **)base));
   auto tiles_at = [](char *p, long long cap) {
     LoopTiles t{};
     t.total = reinterpret_cast<unsigned long long *>(p);
     t.status = t.total + 1;
     t.tile_counter = reinterpret_cast<unsigned int *>(t.status + cap + 1);
     t.error = reinterpret_cast<int *>(t.tile_counter + 1);
+    t.done = reinterpret_cast<unsigned int *>(t.error + 1);
     t.cap = cap;
     return t;
   };
+  *scan = tiles_at(*base + *args_b, scan_cap);
+  *store = tiles_at(*base + *args_b + scan_b, store_cap);
+  return PUMP_OK;
+}
+
+pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
+                                     const HsmcEpilogue &epi, int M, float cpCutoff,
+                                     float cpMinSoln, float dr, int *itrs, long long *considered,
+                                     pump_status_t *status) {
+  char *base = nullptr;
+  size_t args_b = 0;
+  LoopTiles scan{}, store{};
+  PUMP_TRY(loop_region(M, &base, &args_b, &scan, &store));
+  const long long scan_cap = scan.cap, store_cap = store.cap;
   LoopArgs *la = nullptr;
   PUMP_TRY(ctx_->pinned(Ctx::kPinLoop, sizeof(LoopArgs), (void **)&la));
   std::memset(la, 0, sizeof *la);
   la->sd = sd;
   la->ca = ca;
-  la->scan = tiles_at(base + args_b, scan_cap);
-  la->store = tiles_at(base + args_b + scan_b, store_cap);
+  la->scan = scan;
+  la->store = store;
   la->cp_min_soln = cpMinSoln;
   la->eps_cp = epsCP_;
   la->eps_cost = epsCost_;

@@ -227,7 +227,16 @@ __global__ void max_degree_kernel(const int *__restrict__ go, int N, int *out) {
 // g_idx and records the bucket sizes the store pass appends after (the
 // expansion reads the bucket through n_g, not through its count).
 __device__ __forceinline__ void expand_write_body(const SearchDev &sd, const int *g, int n_g,
-                                                  int g_idx, int num_paths, int max_paths) {
+                                                  int g_idx, int num_paths, int max_paths,
+                                                  const LoopTiles &scan, const LoopTiles &store) {
+  {  // the scan's scratch is free again (next iteration); the store's (this one)
+    const long long na = loop_tile_words(scan.cap), nb = loop_tile_words(store.cap);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < na + nb; i += stride) {
+      if (i < na) scan.total[i] = 0ull;
+      else store.total[i - na] = 0ull;
+    }
+  }
   const unsigned long long nn = sd.ctl->num_new;
   const int ovf = nn > (unsigned long long)max_paths
                       ? 1
@@ -274,8 +283,8 @@ __device__ __forceinline__ void expand_write_body(const SearchDev &sd, const int
 }
 
 __global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g, int g_idx,
-                                    int num_paths, int max_paths) {
-  expand_write_body(sd, g, n_g, g_idx, num_paths, max_paths);
+                                    int num_paths, int max_paths, LoopTiles scan, LoopTiles store) {
+  expand_write_body(sd, g, n_g, g_idx, num_paths, max_paths, scan, store);
 }
 
 // PUMP.cu:164-185: time and cost of the new paths and the CP cut-off; the
@@ -349,7 +358,7 @@ static_assert(kStoreRows * kStoreWarps == 32, "one (row, warp) count per lane of
 constexpr unsigned long long kLow31 = (1ull << 31) - 1ull;
 static_assert(kLoopScanTile == kTile && kLoopStoreTile == kStoreTile, "loop tile sizes");
 
-__device__ __forceinline__ void store_body(
+__device__ __forceinline__ void store_tiles(
     const SearchDev &sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
     const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words,
     const TileScratch &ts) {
@@ -499,10 +508,40 @@ __device__ __forceinline__ void store_body(
   }
 }
 
+__device__ __forceinline__ void store_body(
+    const SearchDev &sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
+    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words,
+    const TileScratch &ts, unsigned int *done, SearchCtl *host_ctl) {
+  store_tiles(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts);
+  if (!host_ctl) return;
+  // the last block to finish copies the counters to the host
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(done, 1u) == gridDim.x - 1) {
+      __threadfence();
+      const volatile SearchCtl *c = sd.ctl;
+      host_ctl->num_new = c->num_new;
+      host_ctl->num_valid = c->num_valid;
+      host_ctl->g_count[0] = c->g_count[0];
+      host_ctl->g_count[1] = c->g_count[1];
+      host_ctl->goal_found = c->goal_found;
+      host_ctl->g_base[0] = c->g_base[0];
+      host_ctl->g_base[1] = c->g_base[1];
+      host_ctl->wait_error = c->wait_error;
+      host_ctl->overflow = c->overflow;
+      host_ctl->todo = c->todo;
+      __threadfence_system();
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kCompactThreads) store_kernel(
     SearchDev sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
-    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words, TileScratch ts) {
-  store_body(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts);
+    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words, TileScratch ts,
+    unsigned int *done, SearchCtl *host_ctl) {
+  store_body(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts, done,
+             host_ctl);
 }
 
 // ------------------------------------------- the search loop on the device
@@ -525,6 +564,14 @@ __global__ void loop_init_kernel(const LoopArgs *a) {
   const SearchDev sd = a->sd;
   search_init_body(sd);
   if (blockIdx.x == 0 && threadIdx.x == 0) *a->err = 0;
+  {  // the first iteration's tile scratch
+    const long long na = loop_tile_words(a->scan.cap), nb = loop_tile_words(a->store.cap);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < na + nb; i += stride) {
+      if (i < na) a->scan.total[i] = 0ull;
+      else a->store.total[i - na] = 0ull;
+    }
+  }
   const int words = a->words, P = a->P;
   uint32_t *valid = a->valid;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < words; q += gridDim.x * blockDim.x) {
@@ -560,7 +607,7 @@ __global__ void expand_write_loop_kernel(const LoopArgs *a) {
   const SearchDev sd = a->sd;
   const int g_idx = a->L.g_idx;
   expand_write_body(sd, g_idx ? sd.g_list[1] : sd.g_list[0], a->L.n_g, g_idx, a->L.num_paths,
-                    a->L.max_paths);
+                    a->L.max_paths, a->scan, a->store);
 }
 
 __global__ void dominance_loop_kernel(const LoopArgs *a) {
@@ -572,7 +619,7 @@ __global__ void __launch_bounds__(kCompactThreads, 3) store_loop_kernel(const Lo
   const SearchDev sd = a->sd;
   const TileScratch ts = tiles_of(a->store);
   store_body(sd, a->L.num_paths, a->L.g_idx, a->L.cost_threshold, a->L.dr, a->cp_min_soln,
-             a->stage, a->valid, a->words, ts);
+             a->stage, a->valid, a->words, ts, nullptr, nullptr);
 }
 
 // The host loop's bookkeeping after an iteration's counters are back
@@ -663,20 +710,30 @@ pump_status_t max_degree_async(const int *d_go, int N, int *d_out, cudaStream_t 
   return launch_status("max_degree_kernel");
 }
 
-pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n_g,
+pump_status_t search_expand_scan(const SearchDev &sd, int g_idx, int n_g, const LoopTiles &scan,
                                  cudaStream_t s) {
+  if (n_g <= 0) return PUMP_OK;
   TileScratch ts{};
-  return run_scan(ctx, n_g, ExpandCount{sd.g_list[g_idx], sd.path_node, sd.open_cnt}, sd.wf_off, s,
-                  &ts, &sd.ctl->num_new);
+  ts.status = scan.status;
+  ts.tile_counter = scan.tile_counter;
+  ts.total = scan.total;
+  ts.error = scan.error;
+  ts.copy_to = &sd.ctl->num_new;
+  const long long ntiles = ((long long)n_g + kTile - 1) / kTile;
+  if (ntiles > scan.cap) return set_error(PUMP_ERR_CAPACITY, "expansion scan: %lld tiles", ntiles);
+  scan_kernel<<<(unsigned)ntiles, kCompactThreads, 0, s>>>(
+      n_g, ExpandCount{sd.g_list[g_idx], sd.path_node, sd.open_cnt}, sd.wf_off, ts);
+  return launch_status("scan_kernel");
 }
 
 pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int num_paths,
-                                  int max_paths, cudaStream_t s) {
+                                  int max_paths, const LoopTiles &scan, const LoopTiles &store,
+                                  cudaStream_t s) {
   const long long threads = (long long)(n_g > 0 ? n_g : 1) * 32;
   long long blocks = (threads + 255) / 256;
   if (blocks > kNumSMs * 16) blocks = kNumSMs * 16;
   expand_write_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, sd.g_list[g_idx], n_g, g_idx, num_paths,
-                                                      max_paths);
+                                                      max_paths, scan, store);
   return launch_status("expand_write");
 }
 
@@ -709,15 +766,21 @@ pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, floa
   return launch_status("dominance");
 }
 
-pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int max_new, int num_paths,
-                           int g_idx, float cost_threshold, float dr, float cp_min_soln,
-                           const uint32_t *stage, uint32_t *valid, int words, cudaStream_t s) {
+pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int g_idx,
+                           float cost_threshold, float dr, float cp_min_soln, const uint32_t *stage,
+                           uint32_t *valid, int words, const LoopTiles &store, SearchCtl *host_ctl,
+                           cudaStream_t s) {
   TileScratch ts{};
-  long long ntiles = 0;
-  PUMP_TRY(prepare_tiles(ctx, max_new > 0 ? max_new : 1, s, &ts, &ntiles, kStoreTile));
+  ts.status = store.status;
+  ts.tile_counter = store.tile_counter;
+  ts.total = store.total;
+  ts.error = store.error;
+  const long long ntiles = ((long long)(max_new > 0 ? max_new : 1) + kStoreTile - 1) / kStoreTile;
+  if (ntiles > store.cap) return set_error(PUMP_ERR_CAPACITY, "store pass: %lld tiles", ntiles);
   const unsigned blocks = (unsigned)(ntiles < kNumSMs * 4 ? ntiles : kNumSMs * 4);
   store_kernel<<<blocks, kCompactThreads, 0, s>>>(sd, num_paths, g_idx, cost_threshold, dr,
-                                                  cp_min_soln, stage, valid, words, ts);
+                                                  cp_min_soln, stage, valid, words, ts, store.done,
+                                                  host_ctl);
   return launch_status("store_kernel");
 }
 
@@ -775,8 +838,6 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
                                                    cudaStreamCaptureModeRelaxed),
                      "cudaStreamBeginCaptureToGraph");
     if (st == PUMP_OK) {
-      const size_t scan_zero = sizeof(unsigned long long) * (size_t)(scan.cap + 2) + 8;
-      const size_t store_zero = sizeof(unsigned long long) * (size_t)(store.cap + 2) + 8;
       // fixed grids (the kernels loop over the device-side counts)
       const int g_check = kNumSMs * 8, g_scan = kNumSMs * 2, g_wide = kNumSMs * 4;
       if (lazy) {
@@ -785,12 +846,10 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
         else
           check_loop_kernel<PUMP_BVP_PRECISION><<<g_check, kChkThreads, chk_smem, cs>>>(d_args);
       }
-      cudaMemsetAsync(scan.total, 0, scan_zero, cs);
       scan_loop_kernel<<<g_scan, kCompactThreads, 0, cs>>>(d_args);
       expand_write_loop_kernel<<<g_wide, 256, 0, cs>>>(d_args);
       hsmc_loop_launch(&d_args->hp, &d_args->L, numObs, g_wide, cs);
       dominance_loop_kernel<<<g_wide, 256, 0, cs>>>(d_args);
-      cudaMemsetAsync(store.total, 0, store_zero, cs);
       store_loop_kernel<<<g_wide, kCompactThreads, 0, cs>>>(d_args);
       loop_control_kernel<<<1, 1, 0, cs>>>(d_args, h);
       cudaGraph_t captured = nullptr;

@@ -145,13 +145,18 @@ constexpr int kLoopScanTile = 4096;
 constexpr int kLoopStoreTile = 1024;
 
 // Tile scratch of one look-back pass of the loop (zeroed before each pass):
-// total, status words (one per tile, from status[0]), tile counter, error.
+// total, status words (one per tile, from status[0]), tile counter, error
+// word, and the count of blocks that finished the pass.
 struct LoopTiles {
   unsigned long long *total, *status;
   unsigned int *tile_counter;
   int *error;
+  unsigned int *done;
   long long cap;  // tiles
 };
+// 8-byte words of a LoopTiles region for cap tiles (total, cap + 1 status
+// words, tile counter and error word, done count).
+__host__ __device__ inline long long loop_tile_words(long long cap) { return cap + 4; }
 
 // Everything the loop's kernels read, at one device address per context.
 struct LoopArgs {
@@ -184,17 +189,20 @@ pump_status_t search_count_open(const SearchDev &sd, cudaStream_t s);
 // Largest out-degree of a CSR with row starts go[0..N] into *d_out (device).
 pump_status_t max_degree_async(const int *d_go, int N, int *d_out, cudaStream_t s);
 // Expansion offsets of the n_g paths of bucket g_idx; the wavefront size
-// lands in ctl->num_new (n_g > 0).
-pump_status_t search_expand_scan(Ctx *ctx, const SearchDev &sd, int g_idx, int n_g,
+// lands in ctl->num_new (n_g > 0).  The scan's tile scratch must be zeroed
+// (search_expand_write zeroes it for the next iteration).
+pump_status_t search_expand_scan(const SearchDev &sd, int g_idx, int n_g, const LoopTiles &scan,
                                  cudaStream_t s);
 // Writes the wavefront (PUMP.cu:47-66), empties bucket g_idx (recording the
 // bucket sizes the appends start from) and clears the per-node lists of new
 // paths at the wavefront's nodes.  The wavefront size is read from
 // ctl->num_new; a wavefront larger than max_paths, or one that would bring
 // the stored paths to max_paths, sets ctl->overflow and is not written
-// (PUMP.cu:62-64, 73-76).
+// (PUMP.cu:62-64, 73-76).  It also zeroes the tile scratch of this
+// iteration's store pass and of the next iteration's scan.
 pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int num_paths,
-                                  int max_paths, cudaStream_t s);
+                                  int max_paths, const LoopTiles &scan, const LoopTiles &store,
+                                  cudaStream_t s);
 // New paths' time and cost, the CP cut-off (PUMP.cu:164-185) with per-node
 // lists of the survivors of the cut-off (unless the HSMC kernel wrote them:
 // new_paths_done), then epsilon dominance (PUMP.cu:188-218); wavefront size
@@ -208,10 +216,13 @@ HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff);
 // in the same order, linked into its node's list, goal-tested, and its
 // particle mask moves from the stage to its stored slot.
 // Wavefront size from the device (wave_size); max_new bounds it (sizes the
-// tile status words).
-pump_status_t search_store(Ctx *ctx, const SearchDev &sd, int max_new, int num_paths,
-                           int g_idx, float cost_threshold, float dr, float cp_min_soln,
-                           const uint32_t *stage, uint32_t *valid, int words, cudaStream_t s);
+// grid).  The store's tile scratch must be zeroed.  With host_ctl (pinned
+// host memory), the last block to finish copies the iteration's counters
+// there, so the host reads them after its synchronisation without a copy.
+pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int g_idx,
+                           float cost_threshold, float dr, float cp_min_soln, const uint32_t *stage,
+                           uint32_t *valid, int words, const LoopTiles &store, SearchCtl *host_ctl,
+                           cudaStream_t s);
 
 // The graph of the search loop for the argument block at d_args (device):
 // init, then a while node over {[lazy: edge checks], scan, expansion, HSMC,
