@@ -333,7 +333,8 @@ __global__ void __launch_bounds__(kRowThreads) candidate_rows_kernel(
     const float *__restrict__ x0, const float *__restrict__ x1, const float *__restrict__ topt,
     const float *__restrict__ seg_cost, const int *__restrict__ node_cnt,
     const int *__restrict__ seg_base, float dt, int rows_cap, int *__restrict__ len,
-    float *__restrict__ cost, int *__restrict__ hits, float *__restrict__ states) {
+    float *__restrict__ cost, int *__restrict__ hits, float *__restrict__ states,
+    unsigned int *done) {
   extern __shared__ int s_seg[];  // per segment: first row, then toff
   __shared__ int s_len;
   const int p = blockIdx.x;
@@ -358,6 +359,7 @@ __global__ void __launch_bounds__(kRowThreads) candidate_rows_kernel(
       len[p] = rows;
       if (cost) cost[p] = c;
       if (hits) hits[p] = 0;
+      if (done && p == 0) *done = 0u;
     }
   }
   __syncthreads();
@@ -419,11 +421,11 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
   if (mode == PUMP_BVP_PARITY)
     candidate_rows_kernel<PUMP_BVP_PARITY><<<grid, kRowThreads, smem, s>>>(
         cb.x0, cb.x1, cb.topt, with_cost ? cb.seg_cost : nullptr, cb.node_cnt, cb.seg_base, dt,
-        rows_cap, cb.len, with_cost ? cb.cost : nullptr, cb.hits, cb.states);
+        rows_cap, cb.len, with_cost ? cb.cost : nullptr, cb.hits, cb.states, cb.done);
   else
     candidate_rows_kernel<PUMP_BVP_PRECISION><<<grid, kRowThreads, smem, s>>>(
         cb.x0, cb.x1, cb.topt, with_cost ? cb.seg_cost : nullptr, cb.node_cnt, cb.seg_base, dt,
-        rows_cap, cb.len, with_cost ? cb.cost : nullptr, cb.hits, cb.states);
+        rows_cap, cb.len, with_cost ? cb.cost : nullptr, cb.hits, cb.states, cb.done);
   return launch_status("candidate_rows");
 }
 

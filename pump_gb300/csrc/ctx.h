@@ -161,17 +161,22 @@ struct CandidateBufs {
   int *len;
   int *hits;     // zeroed per path when not null (the MC CP counters)
   float *topt2;  // when not null: the segments' optimal times with tmax 2
+  unsigned int *done;  // zeroed when not null (the MC CP's finished-block count)
 };
 // max_segs: the most segments of one path.
 pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_seg, int max_segs,
                                     int mode, float dt, bool with_cost, int rows_cap,
                                     cudaStream_t s);
 // MC CP hit counts of n_paths dense paths into d_hits (zeroed beforehand):
-// the kernels of mc_cp_async without its memset and CP division.
+// the kernels of mc_cp_async without its memset and CP division.  With
+// copy_dst (host memory; n_paths <= 65535), the last block to finish copies
+// copy_words words from copy_src to it; *done must be zero before the launch.
 pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const int *d_len,
                                int n_paths, const float *d_offsets_t, int Pmc, int T_rows,
                                float offset_mult, const float *d_obstacles, int numObs,
-                               int *d_hits, cudaStream_t stream, const float *d_rowmax);
+                               int *d_hits, cudaStream_t stream, const float *d_rowmax,
+                               const int *copy_src = nullptr, int *copy_dst = nullptr,
+                               int copy_words = 0, unsigned int *done = nullptr);
 // Halton samples of a query (sampler.cu:20-41), N x 6, then the goal row
 // once more.
 pump_status_t halton_samples_async(int N, const float *lo, const float *hi, const float *init,

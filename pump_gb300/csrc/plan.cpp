@@ -947,7 +947,7 @@ pump_status_t Planner::eval_launch(CandSet &c, const std::vector<std::vector<flo
   // results read back in one copy: MC hit counts | lengths | costs, then the
   // segments' optimal times with tmax 5 and (with_topts) 2
   const size_t seg_f = with_topts ? (size_t)segs : 0;
-  PUMP_TRY(c.out.alloc(3 * (size_t)n + sg + seg_f));
+  PUMP_TRY(c.out.alloc(3 * (size_t)n + sg + seg_f + 1));  // + the MC CP's finished-block count
   PUMP_TRY(c.states.alloc((size_t)n * rows_cap * kDim));
   float *d_topt = reinterpret_cast<float *>(c.out.p + 3 * (size_t)n);
   CandidateBufs cb{};
@@ -960,21 +960,28 @@ pump_status_t Planner::eval_launch(CandSet &c, const std::vector<std::vector<flo
   cb.seg_cost = c.segcost.p;
   cb.states = c.states.p;
   cb.hits = with_cp ? c.out.p : nullptr;
+  // pinned read-back: 3n ints | 2 segs floats (with_topts) | states_rows x 6
+  // floats of path 0.  With the MC CP, its last block copies the head (a
+  // single launch holds at most 65535 paths).
+  const size_t st_f = (size_t)c.states_rows * kDim;
+  const size_t head = sizeof(int) * 3 * (size_t)n + sizeof(float) * 2 * seg_f;
+  const size_t head_words = head / sizeof(int);
+  const bool copy_out = with_cp && n <= 65535;
+  char *hout = nullptr;
+  PUMP_TRY(ctx_->pinned(c.pin_out, head + sizeof(float) * st_f, (void **)&hout));
+  cb.done = copy_out ? reinterpret_cast<unsigned int *>(c.out.p + head_words) : nullptr;
   cb.len = c.out.p + n;
   cb.cost = reinterpret_cast<float *>(c.out.p + 2 * n);
   PUMP_TRY(candidate_paths_async(cb, n, segs, max_segs, pb_.bvp_mode, dt, with_cost, rows_cap, s_));
   if (with_cp)
     PUMP_TRY(mc_cp_hits_async(c.states.p, d_ints + 2 * n, cb.len, n, d_table_, pb_.num_mc,
                               pb_.table_rows, pb_.offset_mult, obs_p_, nobs_, cb.hits, s_,
-                              d_rowmax_));
-  // pinned read-back: 3n ints | 2 segs floats (with_topts) | states_rows x 6
-  // floats of path 0
-  const size_t st_f = (size_t)c.states_rows * kDim;
-  const size_t head = sizeof(int) * 3 * (size_t)n + sizeof(float) * 2 * seg_f;
-  char *hout = nullptr;
-  PUMP_TRY(ctx_->pinned(c.pin_out, head + sizeof(float) * st_f, (void **)&hout));
+                              d_rowmax_, copy_out ? c.out.p : nullptr,
+                              copy_out ? reinterpret_cast<int *>(hout) : nullptr,
+                              (int)head_words, cb.done));
   float *hf = reinterpret_cast<float *>(hout + sizeof(int) * 3 * (size_t)n);
-  PUMP_CUDA_TRY(cudaMemcpyAsync(hout, c.out.p, head, cudaMemcpyDeviceToHost, s_));
+  if (!copy_out)
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hout, c.out.p, head, cudaMemcpyDeviceToHost, s_));
   if (st_f > 0)
     PUMP_CUDA_TRY(cudaMemcpyAsync(hf + 2 * seg_f, c.states.p, sizeof(float) * st_f,
                                   cudaMemcpyDeviceToHost, s_));
