@@ -82,6 +82,9 @@ class Ctx {
   };
   std::vector<LoopGraph> loop_graphs;
   cudaStream_t capture_stream = nullptr;
+  // Values of the completion words that kernels write to pinned memory for
+  // a host waiting on them (one per wait, never repeated on this context).
+  unsigned int seq_counter = 0;
 
  private:
   int device_;
@@ -170,13 +173,15 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
 // MC CP hit counts of n_paths dense paths into d_hits (zeroed beforehand):
 // the kernels of mc_cp_async without its memset and CP division.  With
 // copy_dst (host memory; n_paths <= 65535), the last block to finish copies
-// copy_words words from copy_src to it; *done must be zero before the launch.
+// copy_words words from copy_src to it, then writes seq to
+// copy_dst[copy_words]; *done must be zero before the launch.
 pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const int *d_len,
                                int n_paths, const float *d_offsets_t, int Pmc, int T_rows,
                                float offset_mult, const float *d_obstacles, int numObs,
                                int *d_hits, cudaStream_t stream, const float *d_rowmax,
                                const int *copy_src = nullptr, int *copy_dst = nullptr,
-                               int copy_words = 0, unsigned int *done = nullptr);
+                               int copy_words = 0, unsigned int *done = nullptr,
+                               unsigned int seq = 0);
 // Halton samples of a query (sampler.cu:20-41), N x 6, then the goal row
 // once more.
 pump_status_t halton_samples_async(int N, const float *lo, const float *hi, const float *init,

@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(256) mc_cp_kernel(
     const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
     const float *__restrict__ obs, int numObs, int k0, int *__restrict__ hits,
     const float *__restrict__ rowmax, const int *copy_src, int *copy_dst, int copy_words,
-    unsigned int *done) {
+    unsigned int *done, unsigned int seq) {
   extern __shared__ float4 s_obs4[];
   float *s_obs = reinterpret_cast<float *>(s_obs4);
   uint32_t *s_mask = reinterpret_cast<uint32_t *>(s_obs + ((numObs * 12 + 3) & ~3));
@@ -595,7 +595,12 @@ __global__ void __launch_bounds__(256) mc_cp_kernel(
       __threadfence();
       const volatile int *src = copy_src;
       for (int i = threadIdx.x; i < copy_words; i += blockDim.x) copy_dst[i] = src[i];
-      __threadfence_system();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence_system();
+        // then the sequence word after the copy, for a host that waits on it
+        *reinterpret_cast<volatile unsigned int *>(copy_dst + copy_words) = seq;
+      }
     }
   }
 }
@@ -646,7 +651,7 @@ pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const 
                                float offset_mult, const float *d_obstacles, int numObs,
                                int *d_hits, cudaStream_t stream, const float *d_rowmax,
                                const int *copy_src, int *copy_dst, int copy_words,
-                               unsigned int *done) {
+                               unsigned int *done, unsigned int seq) {
   if (n_paths <= 0) return PUMP_OK;
   if (copy_dst && n_paths > 65535)
     return set_error(PUMP_ERR_BAD_INPUT, "mc_cp: copy-out with %d paths", n_paths);
@@ -665,7 +670,8 @@ pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const 
     dim3 grid(grid_for(Pmc, 32), (unsigned)nk);
     mc_cp_kernel<<<grid, 256, smem, stream>>>(d_paths, d_offset, d_len, d_offsets_t, Pmc, T_rows,
                                               offset_mult, d_obstacles, numObs, k0, d_hits,
-                                              d_rowmax, copy_src, copy_dst, copy_words, done);
+                                              d_rowmax, copy_src, copy_dst, copy_words, done,
+                                              seq);
     PUMP_TRY(launch_status("mc_cp_kernel"));
   }
   return PUMP_OK;
@@ -679,7 +685,7 @@ pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *
   PUMP_CUDA_TRY(cudaMemsetAsync(d_hits, 0, sizeof(int) * n_paths, stream));
   PUMP_TRY(mc_cp_hits_async(d_paths, d_offset, d_len, n_paths, d_offsets_t, Pmc, T_rows,
                             offset_mult, d_obstacles, numObs, d_hits, stream, d_rowmax, nullptr,
-                            nullptr, 0, nullptr));
+                            nullptr, 0, nullptr, 0u));
   mc_cp_finish_kernel<<<grid_for(n_paths, 128), 128, 0, stream>>>(d_hits, d_len, n_paths, Pmc,
                                                                   T_rows, d_cp, d_error);
   return launch_status("mc_cp_finish_kernel");

@@ -155,6 +155,8 @@ struct CandSet {
   int n = 0, segs = 0, states_rows = 0, table_rows = 0, num_mc = 0;
   bool with_cost = false, with_cp = false, with_topts = false;
   const char *hout = nullptr;
+  size_t head_bytes = 0;  // results before the completion word
+  unsigned int seq = 0;   // completion word value (0: none, wait on the stream)
   CandSet(int in_slot, int out_slot) : pin_in(in_slot), pin_out(out_slot) {}
 };
 
@@ -244,6 +246,37 @@ class Planner {
     res_->ms_wait += ms_since(t);
     ++res_->num_waits;
     return st;
+  }
+  // Waits until the stream's last kernel has written `want` to the pinned
+  // completion word (written after the results it guards), without a driver
+  // call per wait; every 0.5 ms the stream's status is checked, so a fault,
+  // or a stream that finished without writing the word, ends the wait with
+  // an error.
+  pump_status_t wait_seq(const unsigned int *word, unsigned int want) {
+    const auto t = clk::now();
+    auto checked = t;
+    while (__atomic_load_n(word, __ATOMIC_ACQUIRE) != want) {
+      const auto now = clk::now();
+      if (now - checked < std::chrono::microseconds(500)) continue;
+      checked = now;
+      const cudaError_t e = cudaStreamQuery(s_);
+      if (e == cudaErrorNotReady) continue;
+      if (e != cudaSuccess) return cuda_status(e, "cudaStreamQuery");
+      if (__atomic_load_n(word, __ATOMIC_ACQUIRE) == want) break;
+      return set_error(PUMP_ERR_CUDA, "stream finished without writing its completion word");
+    }
+    res_->ms_wait += ms_since(t);
+    ++res_->num_waits;
+    return PUMP_OK;
+  }
+  // The next completion word value of this context.
+  unsigned int next_seq() { return ++ctx_->seq_counter; }
+  // Waits for the candidate batch launched last on c (its completion word,
+  // or the stream).
+  pump_status_t wait_cand(const CandSet &c) {
+    if (c.n == 0) return PUMP_OK;
+    if (!c.seq) return sync();
+    return wait_seq(reinterpret_cast<const unsigned int *>(c.hout + c.head_bytes), c.seq);
   }
   template <class T>
   pump_status_t h2d(T *d, const T *h, size_t n) {
@@ -674,10 +707,12 @@ pump_status_t Planner::explore() {
     // (PUMP.cu:164-256)
     PUMP_TRY(search_prune(sd, maxNew, numPaths_, cpCutoff, epsCP_, epsCost_, true, s_));
     // the store pass's last block leaves the counters in hctl (pinned)
+    const unsigned int sq = next_seq();
+    *reinterpret_cast<volatile unsigned int *>(&hctl->seq) = sq - 1u;
     PUMP_TRY(search_store(sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln, d_stage_.p,
-                          d_valid_.p, words_, storeT, hctl, s_));
+                          d_valid_.p, words_, storeT, hctl, sq, s_));
     res_->d2h_bytes += (long long)sizeof(SearchCtl);
-    PUMP_TRY(sync());
+    PUMP_TRY(wait_seq(&hctl->seq, sq));
     ctl = *hctl;
     res_->ms_explore_wait += ms_since(tw);
     if (ctl.overflow == 1) {
@@ -963,13 +998,18 @@ pump_status_t Planner::eval_launch(CandSet &c, const std::vector<std::vector<flo
   // pinned read-back: 3n ints | 2 segs floats (with_topts) | states_rows x 6
   // floats of path 0.  With the MC CP, its last block copies the head (a
   // single launch holds at most 65535 paths).
+  // (then the completion word, then the states at a 16-byte boundary)
   const size_t st_f = (size_t)c.states_rows * kDim;
   const size_t head = sizeof(int) * 3 * (size_t)n + sizeof(float) * 2 * seg_f;
   const size_t head_words = head / sizeof(int);
+  const size_t st_off = (head + sizeof(unsigned int) + 15) & ~(size_t)15;
   const bool copy_out = with_cp && n <= 65535;
   char *hout = nullptr;
-  PUMP_TRY(ctx_->pinned(c.pin_out, head + sizeof(float) * st_f, (void **)&hout));
+  PUMP_TRY(ctx_->pinned(c.pin_out, st_off + sizeof(float) * st_f, (void **)&hout));
   cb.done = copy_out ? reinterpret_cast<unsigned int *>(c.out.p + head_words) : nullptr;
+  c.head_bytes = head;
+  c.seq = copy_out ? next_seq() : 0u;
+  if (copy_out) *reinterpret_cast<volatile unsigned int *>(hout + head) = c.seq - 1u;
   cb.len = c.out.p + n;
   cb.cost = reinterpret_cast<float *>(c.out.p + 2 * n);
   PUMP_TRY(candidate_paths_async(cb, n, segs, max_segs, pb_.bvp_mode, dt, with_cost, rows_cap, s_));
@@ -978,12 +1018,11 @@ pump_status_t Planner::eval_launch(CandSet &c, const std::vector<std::vector<flo
                               pb_.table_rows, pb_.offset_mult, obs_p_, nobs_, cb.hits, s_,
                               d_rowmax_, copy_out ? c.out.p : nullptr,
                               copy_out ? reinterpret_cast<int *>(hout) : nullptr,
-                              (int)head_words, cb.done));
-  float *hf = reinterpret_cast<float *>(hout + sizeof(int) * 3 * (size_t)n);
+                              (int)head_words, cb.done, c.seq));
   if (!copy_out)
     PUMP_CUDA_TRY(cudaMemcpyAsync(hout, c.out.p, head, cudaMemcpyDeviceToHost, s_));
   if (st_f > 0)
-    PUMP_CUDA_TRY(cudaMemcpyAsync(hf + 2 * seg_f, c.states.p, sizeof(float) * st_f,
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hout + st_off, c.states.p, sizeof(float) * st_f,
                                   cudaMemcpyDeviceToHost, s_));
   c.hout = hout;
   return PUMP_OK;
@@ -1013,8 +1052,11 @@ void Planner::eval_read(const CandSet &c, CandResult *r) const {
     r->t5.assign(hf, hf + seg_f);
     r->t2.assign(hf + seg_f, hf + 2 * seg_f);
   }
-  if (c.states_rows > 0)
-    r->states.assign(hf + 2 * seg_f, hf + 2 * seg_f + (size_t)c.states_rows * kDim);
+  if (c.states_rows > 0) {
+    const float *hs = reinterpret_cast<const float *>(
+        c.hout + ((c.head_bytes + sizeof(unsigned int) + 15) & ~(size_t)15));
+    r->states.assign(hs, hs + (size_t)c.states_rows * kDim);
+  }
 }
 
 pump_status_t Planner::eval_candidates(const std::vector<std::vector<float>> &xs, float dt,
@@ -1022,7 +1064,7 @@ pump_status_t Planner::eval_candidates(const std::vector<std::vector<float>> &xs
                                       std::vector<int> &len, std::vector<float> &cost,
                                       std::vector<float> &cp) {
   PUMP_TRY(eval_launch(cs_, xs, dt, rows_cap, with_cost, with_cp, false, 0));
-  if (!xs.empty()) PUMP_TRY(sync());
+  PUMP_TRY(wait_cand(cs_));
   CandResult r;
   eval_read(cs_, &r);
   len.swap(r.len);
@@ -1055,7 +1097,8 @@ pump_status_t Planner::search_and_smooth() {
     PUMP_TRY(eval_launch(co_, two, dt_ / dtMult, optCap, false, false, false, optCap));
   }
   PUMP_TRY(eval_launch(cs_, cand, dt_, rowsCap, false, true, true, 0));
-  if (!cand.empty()) PUMP_TRY(sync());
+  // the optimal path's copies precede the candidates' kernels in the stream
+  PUMP_TRY(wait_cand(cs_));
   CandResult gr;
   eval_read(cs_, &gr);
   const std::vector<int> &glen = gr.len;
@@ -1148,7 +1191,7 @@ pump_status_t Planner::search_and_smooth() {
       for (int k = 0; k < K; ++k)
         for (size_t i = 0; i < xs.size(); ++i) cand[k][i] = (1 - na[k]) * xs[i] + na[k] * xsOpt[i];
       PUMP_TRY(eval_launch(cs_, cand, dt_, rowsCap, true, true, true, 0));
-      PUMP_TRY(sync());
+      PUMP_TRY(wait_cand(cs_));
       CandResult sr;
       eval_read(cs_, &sr);
       int k = 0;

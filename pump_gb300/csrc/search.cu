@@ -511,7 +511,7 @@ __device__ __forceinline__ void store_tiles(
 __device__ __forceinline__ void store_body(
     const SearchDev &sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
     const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words,
-    const TileScratch &ts, unsigned int *done, SearchCtl *host_ctl) {
+    const TileScratch &ts, unsigned int *done, SearchCtl *host_ctl, unsigned int seq) {
   store_tiles(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts);
   if (!host_ctl) return;
   // the last block to finish copies the counters to the host
@@ -532,6 +532,7 @@ __device__ __forceinline__ void store_body(
       host_ctl->overflow = c->overflow;
       host_ctl->todo = c->todo;
       __threadfence_system();
+      *reinterpret_cast<volatile unsigned int *>(&host_ctl->seq) = seq;
     }
   }
 }
@@ -539,9 +540,9 @@ __device__ __forceinline__ void store_body(
 __global__ void __launch_bounds__(kCompactThreads) store_kernel(
     SearchDev sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
     const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words, TileScratch ts,
-    unsigned int *done, SearchCtl *host_ctl) {
+    unsigned int *done, SearchCtl *host_ctl, unsigned int seq) {
   store_body(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts, done,
-             host_ctl);
+             host_ctl, seq);
 }
 
 // ------------------------------------------- the search loop on the device
@@ -619,7 +620,7 @@ __global__ void __launch_bounds__(kCompactThreads, 3) store_loop_kernel(const Lo
   const SearchDev sd = a->sd;
   const TileScratch ts = tiles_of(a->store);
   store_body(sd, a->L.num_paths, a->L.g_idx, a->L.cost_threshold, a->L.dr, a->cp_min_soln,
-             a->stage, a->valid, a->words, ts, nullptr, nullptr);
+             a->stage, a->valid, a->words, ts, nullptr, nullptr, 0u);
 }
 
 // The host loop's bookkeeping after an iteration's counters are back
@@ -769,7 +770,7 @@ pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, floa
 pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int g_idx,
                            float cost_threshold, float dr, float cp_min_soln, const uint32_t *stage,
                            uint32_t *valid, int words, const LoopTiles &store, SearchCtl *host_ctl,
-                           cudaStream_t s) {
+                           unsigned int seq, cudaStream_t s) {
   TileScratch ts{};
   ts.status = store.status;
   ts.tile_counter = store.tile_counter;
@@ -780,7 +781,7 @@ pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int 
   const unsigned blocks = (unsigned)(ntiles < kNumSMs * 4 ? ntiles : kNumSMs * 4);
   store_kernel<<<blocks, kCompactThreads, 0, s>>>(sd, num_paths, g_idx, cost_threshold, dr,
                                                   cp_min_soln, stage, valid, words, ts, store.done,
-                                                  host_ctl);
+                                                  host_ctl, seq);
   return launch_status("store_kernel");
 }
 

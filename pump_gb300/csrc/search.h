@@ -22,6 +22,7 @@ struct SearchCtl {
   int wait_error;                // 1: a look-back wait of the store pass gave up
   int overflow;                  // 1: wavefront > maxPathCount, 2: paths would reach it
   int todo;                      // nodes claimed for edge checks this iteration
+  unsigned int seq;              // host copy: written last, after the fields above
 };
 
 // The wavefront size the kernels after the expansion work on: 0 when the
@@ -218,11 +219,12 @@ HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff);
 // Wavefront size from the device (wave_size); max_new bounds it (sizes the
 // grid).  The store's tile scratch must be zeroed.  With host_ctl (pinned
 // host memory), the last block to finish copies the iteration's counters
-// there, so the host reads them after its synchronisation without a copy.
+// there and then writes seq to host_ctl->seq, so the host can wait for that
+// word instead of synchronising the stream.
 pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int g_idx,
                            float cost_threshold, float dr, float cp_min_soln, const uint32_t *stage,
                            uint32_t *valid, int words, const LoopTiles &store, SearchCtl *host_ctl,
-                           cudaStream_t s);
+                           unsigned int seq, cudaStream_t s);
 
 // The graph of the search loop for the argument block at d_args (device):
 // init, then a while node over {[lazy: edge checks], scan, expansion, HSMC,
