@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--no-refine", action="store_true", help="skip the path-refinement workload")
     ap.add_argument("--batch", type=int, default=256, help="queries of the batched workload (0: skip)")
     ap.add_argument("--workers", type=int, default=0,
-                    help="batched-mode workers (0: three quarters of the host cores, at most 12)")
+                    help="batched-mode workers (0: the host cores less two, at most 14)")
     return ap.parse_args()
 
 
@@ -194,7 +194,7 @@ def measure_queries(args, lib, L, ctx):
     # a worker sweep on the GB300 machine (16 host cores, 128 uneven queries):
     # 4 -> 1646, 8 -> 1934, 16 -> 1806, 32 -> 1598 q/s; past about 8 the GPU is
     # saturated and more threads only contend
-    workers = args.workers or max(1, min(12, (3 * (os.cpu_count() or 8)) // 4))
+    workers = args.workers or max(1, min(14, (os.cpu_count() or 8) - 2))
     # warm both paths on every query (contexts, particle tables, and the
     # autotuner's first call of each shape class, which neither timed run pays)
     res = results()
