@@ -705,7 +705,7 @@ pump_status_t Planner::explore() {
                               P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf, &epi));
     // cut-off (written by the HSMC kernel), dominance, storing, buckets
     // (PUMP.cu:164-256)
-    PUMP_TRY(search_prune(sd, maxNew, numPaths_, cpCutoff, epsCP_, epsCost_, true, s_));
+    PUMP_TRY(search_prune(sd, maxNew, numPaths_, epsCP_, epsCost_, s_));
     // the store pass's last block leaves the counters in hctl (pinned)
     const unsigned int sq = next_seq();
     *reinterpret_cast<volatile unsigned int *>(&hctl->seq) = sq - 1u;

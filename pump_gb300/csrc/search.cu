@@ -287,20 +287,6 @@ __global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g, int g_i
   expand_write_body(sd, g, n_g, g_idx, num_paths, max_paths, scan, store);
 }
 
-// PUMP.cu:164-185: time and cost of the new paths and the CP cut-off; the
-// survivors of the cut-off are linked into their node's list of new paths
-// (emptied by the expansion kernel).
-__global__ void new_paths_kernel(SearchDev sd, float cp_cutoff) {
-  const int n = wave_size(sd.ctl);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int prev = sd.wf_prev[i], f = sd.wf_open[i];
-    sd.new_time[i] = sd.path_time[prev] + sd.topt[f];
-    sd.new_cost[i] = sd.path_cost[prev] + sd.copt[f];
-    const bool alive = !(sd.new_cp[i] > cp_cutoff);
-    sd.alive[i] = alive ? 1 : 0;
-    if (alive) sd.new_next[i] = atomicExch(&sd.new_head[sd.wf_node[i]], i);
-  }
-}
 
 // PUMP.cu:188-218: a new path (not at the goal) dies if a stored path at its
 // node, or another new path there that passed the cut-off, epsilon-dominates
@@ -755,14 +741,10 @@ HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff) {
   return e;
 }
 
-pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float cp_cutoff,
-                           float eps_cp, float eps_cost, bool new_paths_done, cudaStream_t s) {
+pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float eps_cp,
+                           float eps_cost, cudaStream_t s) {
   long long blocks = ((long long)(max_new > 0 ? max_new : 1) + 255) / 256;
   if (blocks > kNumSMs * 4) blocks = kNumSMs * 4;
-  if (!new_paths_done) {
-    new_paths_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, cp_cutoff);
-    PUMP_TRY(launch_status("new_paths"));
-  }
   dominance_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, num_paths, eps_cp, eps_cost);
   return launch_status("dominance");
 }

@@ -204,12 +204,12 @@ pump_status_t search_expand_scan(const SearchDev &sd, int g_idx, int n_g, const 
 pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int num_paths,
                                   int max_paths, const LoopTiles &scan, const LoopTiles &store,
                                   cudaStream_t s);
-// New paths' time and cost, the CP cut-off (PUMP.cu:164-185) with per-node
-// lists of the survivors of the cut-off (unless the HSMC kernel wrote them:
-// new_paths_done), then epsilon dominance (PUMP.cu:188-218); wavefront size
-// from the device (wave_size), at most max_new (sizes the grids).
-pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float cp_cutoff,
-                           float eps_cp, float eps_cost, bool new_paths_done, cudaStream_t s);
+// Epsilon dominance (PUMP.cu:188-218) over the new paths the HSMC kernel
+// wrote with their time, cost, CP cut-off and per-node lists (its
+// HsmcEpilogue); wavefront size from the device (wave_size), at most
+// max_new (sizes the grid).
+pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float eps_cp,
+                           float eps_cost, cudaStream_t s);
 // The search's part of the HSMC kernel for this search state.
 HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff);
 // One pass over the wavefront (PUMP.cu:221-282): survivors become stored
