@@ -411,7 +411,12 @@ pump_status_t run_chunked_tuned(Ctx *ctx, int kernel, long long n, const L &ld,
 // r = 0 .. N: thread e (0 .. E) writes the rows (src[e-1], src[e]], with
 // src[-1] = -1 and src[E] = N, so each row is written once.
 __global__ void row_starts_kernel(const int *__restrict__ src, long long E, int N,
-                                  int *__restrict__ go_start) {
+                                  int *__restrict__ go_start,
+                                  const unsigned long long *__restrict__ E_dev) {
+  if (E_dev) {  // the count from the device, never past the bound E
+    const long long d = (long long)*E_dev;
+    if (d < E) E = d;
+  }
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e <= E;
        e += (long long)gridDim.x * blockDim.x) {
     const int prev = e > 0 ? src[e - 1] : -1;
@@ -420,11 +425,13 @@ __global__ void row_starts_kernel(const int *__restrict__ src, long long E, int 
   }
 }
 
+// Row starts of the edges' sources (sorted); with E_dev the edge count is
+// read on the device and E only sizes the grid (an upper bound).
 pump_status_t row_starts(const int *d_src, long long E, int N, int *d_go_start,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, const unsigned long long *E_dev = nullptr) {
   long long blocks = (E + 1 + 255) / 256;
   if (blocks > kNumSMs * 8) blocks = kNumSMs * 8;
-  row_starts_kernel<<<(unsigned)blocks, 256, 0, stream>>>(d_src, E, N, d_go_start);
+  row_starts_kernel<<<(unsigned)blocks, 256, 0, stream>>>(d_src, E, N, d_go_start, E_dev);
   return launch_status("row_starts_kernel");
 }
 

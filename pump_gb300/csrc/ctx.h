@@ -121,15 +121,21 @@ pump_status_t build_edges_pairs(Ctx *ctx, const PairView &pv, float rn, long lon
                                 int *d_src, int *d_dst, float *d_copt, float *d_topt,
                                 int *d_go_start, long long *h_num_edges, cudaStream_t stream);
 // rn (the k-th smallest pair cost) and the edges below it in one read of the
-// pair costs, from the query's own pair arrays or its pair view.
+// pair costs, from the query's own pair arrays or its pair view.  With
+// deferred_total, the edge count may be left on the device: then
+// *h_num_edges is -1, *deferred_total points at the count (read it after a
+// synchronisation; it exceeds max_edges when the edges did not fit, and then
+// only max_edges were written) and the row starts are already built.
 pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
                               long long k, long long max_edges, int *d_src, int *d_dst,
                               float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
-                              long long *h_num_edges, cudaStream_t stream);
+                              long long *h_num_edges, cudaStream_t stream,
+                              const unsigned long long **deferred_total = nullptr);
 pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long long max_edges,
                              int *d_src, int *d_dst, float *d_copt, float *d_topt,
                              int *d_go_start, float *h_rn, long long *h_num_edges,
-                             cudaStream_t stream);
+                             cudaStream_t stream,
+                             const unsigned long long **deferred_total = nullptr);
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                       int *d_count, int **d_error_out, cudaStream_t stream);
 pump_status_t particle_rowmax_async(const float *d_table, int P, int T, float *d_rowmax,

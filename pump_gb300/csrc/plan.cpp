@@ -322,6 +322,7 @@ class Planner {
   DevBuf<int> d_scalar_;    // one int read back with the roadmap
   int max_degree_ = 0;      // largest out-degree of the roadmap
   long long E_ = 0;
+  const unsigned long long *d_total_ = nullptr;  // edge count left on the device by the roadmap
   float rn_ = 0;
   DevBuf<float> d_h_;  // heuristic per node (cost to the goal)
   float h0_ = 0;
@@ -386,7 +387,9 @@ pump_status_t Planner::roadmap() {
   const size_t nsf = (size_t)N_ * kDim;
   PUMP_TRY(d_samples_.alloc(nsf + kDim));
   float *hout = nullptr;
-  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float) * (2 + nsf), (void **)&hout));
+  // (then the edge count when it stays on the device until this read-back)
+  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float) * (2 + nsf) + sizeof(unsigned long long),
+                        (void **)&hout));
   if (pb_.samples) {
     samples_.assign(pb_.samples, pb_.samples + nsf);
     float *hin = nullptr;
@@ -434,17 +437,27 @@ pump_status_t Planner::roadmap() {
     PUMP_TRY(pump_bvp_pairs(d_samples_.p, N_, 5.0f, pb_.bvp_mode, d_copts_.p, d_topts_.p,
                             (pump_stream_t)s_));
     PUMP_TRY(rn_edges_device(ctx_, d_copts_.p, d_topts_.p, N_, rnIdx, cap, d_src_.p, d_dst_.p,
-                             d_coptE_.p, d_toptE_.p, d_go_.p, &rn_, &E_, s_));
+                             d_coptE_.p, d_toptE_.p, d_go_.p, &rn_, &E_, s_, &d_total_));
     res_->rn = rn_;
   }
-  res_->num_edges = E_;
-  // the edges' waypoints (findDiscretizedPath) are written by the search's
-  // edge checks, for the nodes it reaches
-  PUMP_TRY(d_disc_.alloc((size_t)E_ * W_ * kDim));
+  // the edges' waypoints (findDiscretizedPath) are written by the edge
+  // checks; with the edge count still on the device, sized for the capacity
+  PUMP_TRY(d_disc_.alloc((size_t)(E_ >= 0 ? E_ : cap) * W_ * kDim));
   PUMP_TRY(d_scalar_.alloc(1));
   PUMP_TRY(max_degree_async(d_go_.p, N_, d_scalar_.p, s_));
   PUMP_CUDA_TRY(cudaMemcpyAsync(hout + 1, d_scalar_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
+  unsigned long long *htotal = reinterpret_cast<unsigned long long *>(hout + 2 + nsf);
+  if (d_total_)
+    PUMP_CUDA_TRY(cudaMemcpyAsync(htotal, d_total_, sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, s_));
   PUMP_TRY(sync());
+  if (d_total_) {
+    if ((long long)*htotal > cap)
+      return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", *htotal,
+                       cap);
+    E_ = (long long)*htotal;
+  }
+  res_->num_edges = E_;
   h0_ = hout[0];
   std::memcpy(&max_degree_, hout + 1, sizeof(int));
   if (!pb_.samples) samples_.assign(hout + 2, hout + 2 + nsf);
@@ -478,7 +491,7 @@ pump_status_t Planner::pair_costs_shared(long long rnIdx, long long cap) {
   pv.gcc = d_own_c_.p + 2 * (N - 1) + (N - 2);
   pv.gct = d_own_t_.p + 2 * (N - 1) + (N - 2);
   PUMP_TRY(rn_edges_pairs(ctx_, pv, rnIdx, cap, d_src_.p, d_dst_.p, d_coptE_.p, d_toptE_.p,
-                          d_go_.p, &rn_, &E_, s_));
+                          d_go_.p, &rn_, &E_, s_, &d_total_));
   res_->rn = rn_;
   return PUMP_OK;
 }

@@ -513,7 +513,8 @@ template <class Src, class Topt, class Fallback>
 pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, long long max_edges,
                            int *d_src, int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
                            float *h_rn, long long *h_num_edges, cudaStream_t stream,
-                           Fallback fallback) {
+                           Fallback fallback, const unsigned long long **deferred_total) {
+  if (deferred_total) *deferred_total = nullptr;
   const long long n = (long long)N * (N - 1);
   const int S = kBracketSamples;
   if (k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "rn_edges: k=%lld n=%lld", k, n);
@@ -550,6 +551,14 @@ pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, lon
                              SupEdgeLoader<Topt>{sup_idx, sup_c, tsrc, N, rn, max_edges, d_src,
                                                  d_dst, d_copt, d_topt},
                              stream, &ts2));
+  if (deferred_total) {
+    // the count stays on the device (the three-kernel compaction never
+    // waits, so it has no error word): the caller reads it later
+    *deferred_total = ts2.total;
+    *h_num_edges = -1;
+    if (d_go_start) PUMP_TRY(row_starts(d_src, max_edges, N, d_go_start, stream, ts2.total));
+    return PUMP_OK;
+  }
   unsigned long long total = 0;
   PUMP_TRY(finish_compact(ts2, &total, stream));
   *h_num_edges = (long long)total;
@@ -564,7 +573,8 @@ pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, lon
 pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
                               long long k, long long max_edges, int *d_src, int *d_dst,
                               float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
-                              long long *h_num_edges, cudaStream_t stream) {
+                              long long *h_num_edges, cudaStream_t stream,
+                              const unsigned long long **deferred_total) {
   auto fallback = [&]() -> pump_status_t {
     const float *d_rn = nullptr;
     PUMP_TRY(select_kth_device(ctx, d_copts, (long long)N * (N - 1), k, &d_rn, stream));
@@ -574,13 +584,14 @@ pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_top
                               d_topt, d_go_start, h_num_edges, stream);
   };
   return rn_edges_src(ctx, FlatSrc{d_copts}, FlatTopt{d_topts}, N, k, max_edges, d_src, d_dst,
-                      d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream, fallback);
+                      d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream, fallback,
+                      deferred_total);
 }
 
 pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long long max_edges,
                              int *d_src, int *d_dst, float *d_copt, float *d_topt,
                              int *d_go_start, float *h_rn, long long *h_num_edges,
-                             cudaStream_t stream) {
+                             cudaStream_t stream, const unsigned long long **deferred_total) {
   auto fallback = [&]() -> pump_status_t {
     const float *d_rn = nullptr;
     PUMP_TRY(select_kth_pairs(ctx, pv, k, &d_rn, stream));
@@ -590,7 +601,7 @@ pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long lon
                              h_num_edges, stream);
   };
   return rn_edges_src(ctx, PairCoptSrc{pv}, PairTopt{pv}, pv.N, k, max_edges, d_src, d_dst, d_copt,
-                      d_topt, d_go_start, h_rn, h_num_edges, stream, fallback);
+                      d_topt, d_go_start, h_rn, h_num_edges, stream, fallback, deferred_total);
 }
 
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
