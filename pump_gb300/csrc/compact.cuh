@@ -435,156 +435,5 @@ pump_status_t row_starts(const int *d_src, long long E, int N, int *d_go_start,
   return launch_status("row_starts_kernel");
 }
 
-// Exclusive scan of n counts: out[i] = count(0) + .. + count(i-1), the total
-// written by the last tile to *ts.total.  Each thread takes kCompactRows
-// consecutive items; tiles chain through the same look-back as compaction.
-template <class Count>
-__global__ void __launch_bounds__(kCompactThreads) scan_kernel(long long n, Count count,
-                                                               unsigned int *out, TileScratch ts) {
-  __shared__ unsigned int s_tile;
-  __shared__ unsigned long long s_warp[kCompactThreads / 32];
-  __shared__ unsigned long long s_excl;
-  __shared__ bool s_timeout;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    s_tile = atomicAdd(ts.tile_counter, 1u);
-    s_timeout = false;
-  }
-  __syncthreads();
-  const long long tile = s_tile;
-  const long long i0 = tile * kTile + (long long)threadIdx.x * kCompactRows;
-  unsigned int v[kCompactRows];
-  unsigned long long sum = 0;
-#pragma unroll
-  for (int r = 0; r < kCompactRows; ++r) {
-    v[r] = i0 + r < n ? count(i0 + r) : 0u;
-    sum += v[r];
-  }
-  unsigned long long incl = sum;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned long long u = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += u;
-  }
-  if (lane == 31) s_warp[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    const unsigned long long w = lane < kCompactThreads / 32 ? s_warp[lane] : 0ull;
-    unsigned long long wi = w;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long u = __shfl_up_sync(0xffffffffu, wi, o);
-      if (lane >= o) wi += u;
-    }
-    if (lane < kCompactThreads / 32) s_warp[lane] = wi - w;
-    const unsigned long long agg = __shfl_sync(0xffffffffu, wi, 31);
-    bool to = false;
-    const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
-    if (lane == 0) {
-      s_excl = ex_tile;
-      if (to) {
-        s_timeout = true;
-        atomicExch(ts.error, 1);
-      }
-      const long long ntiles = (n + kTile - 1) / kTile;
-      if (!to && tile == ntiles - 1) {
-        *ts.total = ex_tile + agg;
-        if (ts.copy_to) *ts.copy_to = ex_tile + agg;
-      }
-    }
-  }
-  __syncthreads();
-  if (s_timeout) return;
-  unsigned long long run = s_excl + s_warp[warp] + (incl - sum);
-#pragma unroll
-  for (int r = 0; r < kCompactRows; ++r) {
-    if (i0 + r < n) out[i0 + r] = (unsigned int)run;
-    run += v[r];
-  }
-}
-
-// scan_kernel's tiles taken in turn from the tile counter by a fixed grid,
-// for callers whose item count is known only on the device (the search
-// loop's graph).  Same offsets and total as scan_kernel.
-template <class Count>
-__device__ __forceinline__ void scan_tiles(long long n, const Count &count, unsigned int *out,
-                                           const TileScratch &ts) {
-  __shared__ unsigned long long s_warp[kCompactThreads / 32];
-  __shared__ unsigned long long s_excl;
-  __shared__ bool s_timeout;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long ntiles = (n + kTile - 1) / kTile;
-  while (true) {
-    if (threadIdx.x == 0) s_timeout = false;
-    const long long tile = next_tile(ts);  // synchronises the block
-    if (tile >= ntiles) return;            // block-uniform
-    const long long i0 = tile * kTile + (long long)threadIdx.x * kCompactRows;
-    unsigned int v[kCompactRows];
-    unsigned long long sum = 0;
-#pragma unroll
-    for (int r = 0; r < kCompactRows; ++r) {
-      v[r] = i0 + r < n ? count(i0 + r) : 0u;
-      sum += v[r];
-    }
-    unsigned long long incl = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long u = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += u;
-    }
-    if (lane == 31) s_warp[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-      const unsigned long long w = lane < kCompactThreads / 32 ? s_warp[lane] : 0ull;
-      unsigned long long wi = w;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long u = __shfl_up_sync(0xffffffffu, wi, o);
-        if (lane >= o) wi += u;
-      }
-      if (lane < kCompactThreads / 32) s_warp[lane] = wi - w;
-      const unsigned long long agg = __shfl_sync(0xffffffffu, wi, 31);
-      bool to = false;
-      const unsigned long long ex_tile = lookback_warp(ts, tile, agg, &to);
-      if (lane == 0) {
-        s_excl = ex_tile;
-        if (to) {
-          s_timeout = true;
-          atomicExch(ts.error, 1);
-        }
-        if (!to && tile == ntiles - 1) {
-          *ts.total = ex_tile + agg;
-          if (ts.copy_to) *ts.copy_to = ex_tile + agg;
-        }
-      }
-    }
-    __syncthreads();
-    if (s_timeout) return;  // block-uniform
-    unsigned long long run = s_excl + s_warp[warp] + (incl - sum);
-#pragma unroll
-    for (int r = 0; r < kCompactRows; ++r) {
-      if (i0 + r < n) out[i0 + r] = (unsigned int)run;
-      run += v[r];
-    }
-    __syncthreads();  // the shared words are rewritten by the next tile
-  }
-}
-
-template <class Count>
-pump_status_t run_scan(Ctx *ctx, long long n, Count count, unsigned int *out,
-                       cudaStream_t stream, TileScratch *ts_out,
-                       unsigned long long *copy_to = nullptr) {
-  TileScratch ts{};
-  long long ntiles = 0;
-  PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));
-  ts.copy_to = copy_to;
-  if (n > 0) {
-    scan_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(n, count, out, ts);
-    PUMP_TRY(launch_status("scan_kernel"));
-  }
-  *ts_out = ts;
-  return PUMP_OK;
-}
-
 }  // namespace
 }  // namespace pump

@@ -689,8 +689,7 @@ pump_status_t Planner::explore() {
     // edge checks of the nodes listed so far (the initial node, then the
     // nodes first reached by the last iteration's stored paths)
     if (lazy_) PUMP_TRY(search_check(sd, maxTodo, ca, s_));
-    PUMP_TRY(search_expand_scan(sd, Gidx, nG, scanT, s_));
-    PUMP_TRY(search_expand_write(sd, Gidx, nG, numPaths_, M, scanT, storeT, s_));
+    PUMP_TRY(search_expand(sd, Gidx, nG, numPaths_, M, scanT, storeT, s_));
     if (res_->wf_trace) {
       unsigned long long nn = 0;
       PUMP_TRY(d2h(&nn, &d_ctl.p->num_new, 1));
@@ -723,7 +722,7 @@ pump_status_t Planner::explore() {
     const unsigned int sq = next_seq();
     *reinterpret_cast<volatile unsigned int *>(&hctl->seq) = sq - 1u;
     PUMP_TRY(search_store(sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln, d_stage_.p,
-                          d_valid_.p, words_, storeT, hctl, sq, s_));
+                          d_valid_.p, words_, storeT, scanT, hctl, sq, s_));
     res_->d2h_bytes += (long long)sizeof(SearchCtl);
     PUMP_TRY(wait_seq(&hctl->seq, sq));
     ctl = *hctl;

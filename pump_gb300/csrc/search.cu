@@ -54,12 +54,6 @@ __global__ void search_init_kernel(SearchDev sd) { search_init_body(sd); }
 // reset above is grid-strided).
 __global__ void search_init_head_kernel(SearchDev sd) { sd.node_head[0] = 0; }
 
-struct ExpandCount {
-  const int *g, *path_node, *open_cnt;
-  __device__ unsigned int operator()(long long i) const {
-    return (unsigned int)open_cnt[path_node[g[i]]];
-  }
-};
 
 // Work items (listed node, chunk of kChkEdges out-edges), chunks per node
 // up to the roadmap's largest degree, taken by blocks in turn so a node's
@@ -222,69 +216,124 @@ __global__ void max_degree_kernel(const int *__restrict__ go, int N, int *out) {
   }
 }
 
-// One warp per bucket entry: its node's expandable edges in order.  The
-// wavefront's nodes get empty lists of new paths; thread 0 empties bucket
-// g_idx and records the bucket sizes the store pass appends after (the
-// expansion reads the bucket through n_g, not through its count).
-__device__ __forceinline__ void expand_write_body(const SearchDev &sd, const int *g, int n_g,
-                                                  int g_idx, int num_paths, int max_paths,
-                                                  const LoopTiles &scan, const LoopTiles &store) {
-  {  // the scan's scratch is free again (next iteration); the store's (this one)
-    const long long na = loop_tile_words(scan.cap), nb = loop_tile_words(store.cap);
+// Zeroes a tile-scratch region (grid-stride).
+__device__ __forceinline__ void zero_tiles(const LoopTiles &t) {
+  const long long n = loop_tile_words(t.cap);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
+    t.total[i] = 0ull;
+}
+
+// The expansion in one pass (PUMP.cu:47-66): the bucket's paths in tiles
+// of kExpTile, taken in order from the tile counter.  A path's offset in the
+// wavefront is its exclusive prefix of expandable-edge counts (in-tile scan,
+// then the tile's prefix by look-back), and one warp per path writes its
+// free edges to free nodes in edge order, clearing the per-node lists of new
+// paths at their nodes.  The last tile writes the wavefront size and flags
+// an iteration that would overflow: a wavefront larger than max_paths, or
+// one that would bring the stored paths to max_paths (PUMP.cu:62-64, 73-76).
+// The kernels after it then see an empty wavefront, and writes past the
+// wavefront's capacity (max_paths + 1) are dropped.  The same kernel empties
+// the bucket, records the bucket sizes the appends start from, and zeroes
+// the store pass's tile scratch for this iteration.
+constexpr int kExpTile = 32;       // paths per tile: one per lane of the scanning warp
+constexpr int kExpThreads = 1024;  // one warp writes each of the tile's paths
+static_assert(kLoopScanTile == kExpTile, "expansion tile size");
+
+__device__ __forceinline__ void expand_body(const SearchDev &sd, const int *g, int n_g, int g_idx,
+                                            int num_paths, int max_paths, const TileScratch &ts,
+                                            const LoopTiles &store) {
+  {
+    const long long nb = loop_tile_words(store.cap);
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < na + nb; i += stride) {
-      if (i < na) scan.total[i] = 0ull;
-      else store.total[i - na] = 0ull;
-    }
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nb; i += stride)
+      store.total[i] = 0ull;
   }
-  const unsigned long long nn = sd.ctl->num_new;
-  const int ovf = nn > (unsigned long long)max_paths
-                      ? 1
-                      : ((unsigned long long)num_paths + nn >= (unsigned long long)max_paths ? 2 : 0);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     SearchCtl *c = sd.ctl;
     c->g_count[g_idx] = 0;
     c->g_base[g_idx] = 0;
     c->g_base[1 - g_idx] = c->g_count[1 - g_idx];
     c->num_valid = 0;
-    c->overflow = ovf;
     c->todo = 0;  // this iteration's checks have run
   }
-  if (ovf) return;
-  const int lane = threadIdx.x & 31;
-  const long long warps = (long long)gridDim.x * (blockDim.x / 32);
+  __shared__ unsigned int s_off[kExpTile];
+  __shared__ int s_timeout;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned int lt = (1u << lane) - 1u;
-  for (long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32; k < n_g; k += warps) {
-    const int prev = g[k];
-    const int node = sd.path_node[prev];
-    const int e0 = sd.go[node], e1 = sd.go[node + 1];
-    unsigned int off = sd.wf_off[k];
-    // the node's expandable edges in edge order (PUMP.cu:52-53)
-    for (int c0 = e0; c0 < e1; c0 += 32) {
-      const int e = c0 + lane;
-      int dst = 0;
-      bool open = false;
-      if (e < e1) {
-        dst = sd.dst[e];
-        open = sd.free_e[e] && sd.free_s[dst];
+  const long long ntiles = ((long long)n_g + kExpTile - 1) / kExpTile;
+  const unsigned long long cap = (unsigned long long)max_paths + 1ull;
+  while (true) {
+    const long long tile = next_tile(ts);  // synchronises the block
+    if (tile >= ntiles) break;             // block-uniform
+    if (warp == 0) {
+      const long long i = tile * kExpTile + lane;
+      const unsigned int cnt = i < n_g ? (unsigned int)sd.open_cnt[sd.path_node[g[i]]] : 0u;
+      unsigned int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
       }
-      const unsigned int bal = __ballot_sync(0xffffffffu, open);
-      if (open) {
-        const unsigned int q = off + __popc(bal & lt);
-        sd.wf_prev[q] = prev;
-        sd.wf_node[q] = dst;
-        sd.wf_edge[q] = e;
-        sd.wf_open[q] = e;
-        sd.new_head[dst] = -1;
+      const unsigned int agg = __shfl_sync(0xffffffffu, incl, 31);
+      bool to = false;
+      const unsigned long long ex = lookback_warp(ts, tile, agg, &to);
+      s_off[lane] = (unsigned int)(ex + (incl - cnt));
+      if (lane == 0) {
+        s_timeout = to ? 1 : 0;
+        if (to) {
+          atomicExch(ts.error, 1);
+          atomicExch(&sd.ctl->wait_error, 1);
+        }
+        if (!to && tile == ntiles - 1) {
+          const unsigned long long nn = ex + agg;
+          sd.ctl->num_new = nn;
+          sd.ctl->overflow =
+              nn > (unsigned long long)max_paths
+                  ? 1
+                  : ((unsigned long long)num_paths + nn >= (unsigned long long)max_paths ? 2 : 0);
+        }
       }
-      off += __popc(bal);
     }
+    __syncthreads();
+    if (s_timeout) break;  // block-uniform
+    const long long rest = (long long)n_g - tile * kExpTile;
+    const int in_tile = (int)(rest < kExpTile ? rest : kExpTile);
+    for (int p = warp; p < in_tile; p += kExpThreads / 32) {
+      const long long k = tile * kExpTile + p;
+      const int prev = g[k];
+      const int node = sd.path_node[prev];
+      const int e0 = sd.go[node], e1 = sd.go[node + 1];
+      unsigned int off = s_off[p];
+      // the node's expandable edges in edge order (PUMP.cu:52-53)
+      for (int c0 = e0; c0 < e1; c0 += 32) {
+        const int e = c0 + lane;
+        int dst = 0;
+        bool open = false;
+        if (e < e1) {
+          dst = sd.dst[e];
+          open = sd.free_e[e] && sd.free_s[dst];
+        }
+        const unsigned int bal = __ballot_sync(0xffffffffu, open);
+        const unsigned int q = off + __popc(bal & lt);
+        if (open && q < cap) {
+          sd.wf_prev[q] = prev;
+          sd.wf_node[q] = dst;
+          sd.wf_edge[q] = e;
+          sd.wf_open[q] = e;
+          sd.new_head[dst] = -1;
+        }
+        off += __popc(bal);
+      }
+    }
+    __syncthreads();  // s_off is rewritten by the next tile
   }
 }
 
-__global__ void expand_write_kernel(SearchDev sd, const int *g, int n_g, int g_idx,
-                                    int num_paths, int max_paths, LoopTiles scan, LoopTiles store) {
-  expand_write_body(sd, g, n_g, g_idx, num_paths, max_paths, scan, store);
+__global__ void __launch_bounds__(kExpThreads) expand_kernel(SearchDev sd, const int *g, int n_g,
+                                                          int g_idx, int num_paths, int max_paths,
+                                                          TileScratch ts, LoopTiles store) {
+  expand_body(sd, g, n_g, g_idx, num_paths, max_paths, ts, store);
 }
 
 
@@ -342,7 +391,7 @@ constexpr int kStoreTile = kCompactThreads * kStoreRows;  // 1024 items
 constexpr int kStoreWarps = kCompactThreads / 32;
 static_assert(kStoreRows * kStoreWarps == 32, "one (row, warp) count per lane of the scan");
 constexpr unsigned long long kLow31 = (1ull << 31) - 1ull;
-static_assert(kLoopScanTile == kTile && kLoopStoreTile == kStoreTile, "loop tile sizes");
+static_assert(kLoopStoreTile == kStoreTile, "store tile size");
 
 __device__ __forceinline__ void store_tiles(
     const SearchDev &sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
@@ -526,7 +575,8 @@ __device__ __forceinline__ void store_body(
 __global__ void __launch_bounds__(kCompactThreads) store_kernel(
     SearchDev sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
     const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words, TileScratch ts,
-    unsigned int *done, SearchCtl *host_ctl, unsigned int seq) {
+    unsigned int *done, SearchCtl *host_ctl, unsigned int seq, LoopTiles scan) {
+  zero_tiles(scan);  // for the next iteration's expansion
   store_body(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts, done,
              host_ctl, seq);
 }
@@ -580,21 +630,12 @@ __global__ void __launch_bounds__(kChkThreads, 4) check_loop_kernel(const LoopAr
   check_body<Mode>(sd, ca);
 }
 
-__global__ void __launch_bounds__(kCompactThreads) scan_loop_kernel(const LoopArgs *a) {
+__global__ void __launch_bounds__(kExpThreads) expand_loop_kernel(const LoopArgs *a) {
   const SearchDev sd = a->sd;
   const int g_idx = a->L.g_idx;
-  const long long n = a->L.n_g;
-  const ExpandCount c{g_idx ? sd.g_list[1] : sd.g_list[0], sd.path_node, sd.open_cnt};
-  TileScratch ts = tiles_of(a->scan);
-  ts.copy_to = &sd.ctl->num_new;
-  scan_tiles(n, c, sd.wf_off, ts);
-}
-
-__global__ void expand_write_loop_kernel(const LoopArgs *a) {
-  const SearchDev sd = a->sd;
-  const int g_idx = a->L.g_idx;
-  expand_write_body(sd, g_idx ? sd.g_list[1] : sd.g_list[0], a->L.n_g, g_idx, a->L.num_paths,
-                    a->L.max_paths, a->scan, a->store);
+  const TileScratch ts = tiles_of(a->scan);
+  expand_body(sd, g_idx ? sd.g_list[1] : sd.g_list[0], a->L.n_g, g_idx, a->L.num_paths,
+              a->L.max_paths, ts, a->store);
 }
 
 __global__ void dominance_loop_kernel(const LoopArgs *a) {
@@ -602,19 +643,24 @@ __global__ void dominance_loop_kernel(const LoopArgs *a) {
   dominance_body(sd, a->L.num_paths, a->eps_cp, a->eps_cost);
 }
 
-__global__ void __launch_bounds__(kCompactThreads, 3) store_loop_kernel(const LoopArgs *a) {
-  const SearchDev sd = a->sd;
-  const TileScratch ts = tiles_of(a->store);
-  store_body(sd, a->L.num_paths, a->L.g_idx, a->L.cost_threshold, a->L.dr, a->cp_min_soln,
-             a->stage, a->valid, a->words, ts, nullptr, nullptr, 0u);
-}
-
 // The host loop's bookkeeping after an iteration's counters are back
-// (PUMP.cu:259-288), then the condition of the next iteration.  A guard
-// ends the loop after 64 iterations whatever the state says.
-__global__ void loop_control_kernel(LoopArgs *a, cudaGraphConditionalHandle h) {
+// (PUMP.cu:259-288), then the condition of the next iteration; run by the
+// store pass's last block to finish.  A guard ends the loop after 64
+// iterations whatever the state says.
+__device__ void loop_control(LoopArgs *a, cudaGraphConditionalHandle h) {
   LoopState &L = a->L;
-  const SearchCtl c = *a->sd.ctl;
+  SearchCtl c;
+  {  // written by other blocks of this iteration's kernels
+    const volatile SearchCtl *v = a->sd.ctl;
+    c.num_new = v->num_new;
+    c.num_valid = v->num_valid;
+    c.g_count[0] = v->g_count[0];
+    c.g_count[1] = v->g_count[1];
+    c.goal_found = v->goal_found;
+    c.wait_error = v->wait_error;
+    c.overflow = v->overflow;
+  }
+  const int scan_error = *reinterpret_cast<const volatile int *>(a->scan.error);
   int cont = 0;
   ++L.guard;
   if (c.overflow == 1) {
@@ -627,7 +673,7 @@ __global__ void loop_control_kernel(LoopArgs *a, cudaGraphConditionalHandle h) {
       L.status = kLoopPathsWouldOverflow;
     } else {
       L.considered += num_new;
-      if (c.wait_error || *a->scan.error) {
+      if (c.wait_error || scan_error) {
         L.status = kLoopWaitError;
       } else {
         L.num_paths += (int)c.num_valid;
@@ -654,6 +700,28 @@ __global__ void loop_control_kernel(LoopArgs *a, cudaGraphConditionalHandle h) {
   if (L.guard >= 64) cont = 0;
   cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
+
+__global__ void __launch_bounds__(kCompactThreads, 3) store_loop_kernel(
+    LoopArgs *a, cudaGraphConditionalHandle h) {
+  const SearchDev sd = a->sd;
+  const TileScratch ts = tiles_of(a->store);
+  zero_tiles(a->scan);  // for the next iteration's expansion
+  store_tiles(sd, a->L.num_paths, a->L.g_idx, a->L.cost_threshold, a->L.dr, a->cp_min_soln,
+              a->stage, a->valid, a->words, ts);
+  // the last block to finish runs the loop's control step
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(a->store.done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    loop_control(a, h);
+  }
+}
+
 
 }  // namespace
 
@@ -697,31 +765,20 @@ pump_status_t max_degree_async(const int *d_go, int N, int *d_out, cudaStream_t 
   return launch_status("max_degree_kernel");
 }
 
-pump_status_t search_expand_scan(const SearchDev &sd, int g_idx, int n_g, const LoopTiles &scan,
-                                 cudaStream_t s) {
+pump_status_t search_expand(const SearchDev &sd, int g_idx, int n_g, int num_paths, int max_paths,
+                           const LoopTiles &scan, const LoopTiles &store, cudaStream_t s) {
   if (n_g <= 0) return PUMP_OK;
   TileScratch ts{};
   ts.status = scan.status;
   ts.tile_counter = scan.tile_counter;
   ts.total = scan.total;
   ts.error = scan.error;
-  ts.copy_to = &sd.ctl->num_new;
-  const long long ntiles = ((long long)n_g + kTile - 1) / kTile;
-  if (ntiles > scan.cap) return set_error(PUMP_ERR_CAPACITY, "expansion scan: %lld tiles", ntiles);
-  scan_kernel<<<(unsigned)ntiles, kCompactThreads, 0, s>>>(
-      n_g, ExpandCount{sd.g_list[g_idx], sd.path_node, sd.open_cnt}, sd.wf_off, ts);
-  return launch_status("scan_kernel");
-}
-
-pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int num_paths,
-                                  int max_paths, const LoopTiles &scan, const LoopTiles &store,
-                                  cudaStream_t s) {
-  const long long threads = (long long)(n_g > 0 ? n_g : 1) * 32;
-  long long blocks = (threads + 255) / 256;
-  if (blocks > kNumSMs * 16) blocks = kNumSMs * 16;
-  expand_write_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, sd.g_list[g_idx], n_g, g_idx, num_paths,
-                                                      max_paths, scan, store);
-  return launch_status("expand_write");
+  const long long ntiles = ((long long)n_g + kExpTile - 1) / kExpTile;
+  if (ntiles > scan.cap) return set_error(PUMP_ERR_CAPACITY, "expansion: %lld tiles", ntiles);
+  const unsigned blocks = (unsigned)(ntiles < kNumSMs * 2 ? ntiles : kNumSMs * 2);
+  expand_kernel<<<blocks, kExpThreads, 0, s>>>(sd, sd.g_list[g_idx], n_g, g_idx, num_paths,
+                                               max_paths, ts, store);
+  return launch_status("expand_kernel");
 }
 
 HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff) {
@@ -751,8 +808,9 @@ pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, floa
 
 pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int g_idx,
                            float cost_threshold, float dr, float cp_min_soln, const uint32_t *stage,
-                           uint32_t *valid, int words, const LoopTiles &store, SearchCtl *host_ctl,
-                           unsigned int seq, cudaStream_t s) {
+                           uint32_t *valid, int words, const LoopTiles &store,
+                           const LoopTiles &scan, SearchCtl *host_ctl, unsigned int seq,
+                           cudaStream_t s) {
   TileScratch ts{};
   ts.status = store.status;
   ts.tile_counter = store.tile_counter;
@@ -763,7 +821,7 @@ pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int 
   const unsigned blocks = (unsigned)(ntiles < kNumSMs * 4 ? ntiles : kNumSMs * 4);
   store_kernel<<<blocks, kCompactThreads, 0, s>>>(sd, num_paths, g_idx, cost_threshold, dr,
                                                   cp_min_soln, stage, valid, words, ts, store.done,
-                                                  host_ctl, seq);
+                                                  host_ctl, seq, scan);
   return launch_status("store_kernel");
 }
 
@@ -822,19 +880,17 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
                      "cudaStreamBeginCaptureToGraph");
     if (st == PUMP_OK) {
       // fixed grids (the kernels loop over the device-side counts)
-      const int g_check = kNumSMs * 8, g_scan = kNumSMs * 2, g_wide = kNumSMs * 4;
+      const int g_check = kNumSMs * 8, g_wide = kNumSMs * 4;
       if (lazy) {
         if (mode == PUMP_BVP_PARITY)
           check_loop_kernel<PUMP_BVP_PARITY><<<g_check, kChkThreads, chk_smem, cs>>>(d_args);
         else
           check_loop_kernel<PUMP_BVP_PRECISION><<<g_check, kChkThreads, chk_smem, cs>>>(d_args);
       }
-      scan_loop_kernel<<<g_scan, kCompactThreads, 0, cs>>>(d_args);
-      expand_write_loop_kernel<<<g_wide, 256, 0, cs>>>(d_args);
+      expand_loop_kernel<<<kNumSMs * 2, kExpThreads, 0, cs>>>(d_args);
       hsmc_loop_launch(&d_args->hp, &d_args->L, numObs, g_wide, cs);
       dominance_loop_kernel<<<g_wide, 256, 0, cs>>>(d_args);
-      store_loop_kernel<<<g_wide, kCompactThreads, 0, cs>>>(d_args);
-      loop_control_kernel<<<1, 1, 0, cs>>>(d_args, h);
+      store_loop_kernel<<<g_wide, kCompactThreads, 0, cs>>>(d_args, h);
       cudaGraph_t captured = nullptr;
       const pump_status_t ce = cuda_status(cudaStreamEndCapture(cs, &captured), "cudaStreamEndCapture");
       st = ce == PUMP_OK ? launch_status("search loop capture") : ce;

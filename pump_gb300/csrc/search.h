@@ -141,8 +141,8 @@ enum LoopStatus {
   kLoopPathsFull           // stored paths reached maxPathCount
 };
 
-// Items per look-back tile of the loop's scan and store passes.
-constexpr int kLoopScanTile = 4096;
+// Items per look-back tile of the loop's expansion and store passes.
+constexpr int kLoopScanTile = 32;
 constexpr int kLoopStoreTile = 1024;
 
 // Tile scratch of one look-back pass of the loop (zeroed before each pass):
@@ -189,21 +189,17 @@ pump_status_t search_check(const SearchDev &sd, int max_todo, const CheckArgs &c
 pump_status_t search_count_open(const SearchDev &sd, cudaStream_t s);
 // Largest out-degree of a CSR with row starts go[0..N] into *d_out (device).
 pump_status_t max_degree_async(const int *d_go, int N, int *d_out, cudaStream_t s);
-// Expansion offsets of the n_g paths of bucket g_idx; the wavefront size
-// lands in ctl->num_new (n_g > 0).  The scan's tile scratch must be zeroed
-// (search_expand_write zeroes it for the next iteration).
-pump_status_t search_expand_scan(const SearchDev &sd, int g_idx, int n_g, const LoopTiles &scan,
-                                 cudaStream_t s);
-// Writes the wavefront (PUMP.cu:47-66), empties bucket g_idx (recording the
-// bucket sizes the appends start from) and clears the per-node lists of new
-// paths at the wavefront's nodes.  The wavefront size is read from
-// ctl->num_new; a wavefront larger than max_paths, or one that would bring
-// the stored paths to max_paths, sets ctl->overflow and is not written
-// (PUMP.cu:62-64, 73-76).  It also zeroes the tile scratch of this
-// iteration's store pass and of the next iteration's scan.
-pump_status_t search_expand_write(const SearchDev &sd, int g_idx, int n_g, int num_paths,
-                                  int max_paths, const LoopTiles &scan, const LoopTiles &store,
-                                  cudaStream_t s);
+// The expansion (PUMP.cu:47-66) in one pass over the n_g paths of bucket
+// g_idx (n_g > 0): writes the wavefront in order, its size to ctl->num_new,
+// and flags (ctl->overflow) a wavefront larger than max_paths, or one that
+// would bring the stored paths to max_paths (PUMP.cu:62-64, 73-76); the
+// kernels after it then see an empty wavefront.  Empties bucket g_idx,
+// records the bucket sizes the appends start from, clears the per-node lists
+// of new paths at the wavefront's nodes and zeroes the store pass's tile
+// scratch.  Its own tile scratch (scan) must be zeroed (the store pass
+// zeroes it for the next iteration).
+pump_status_t search_expand(const SearchDev &sd, int g_idx, int n_g, int num_paths, int max_paths,
+                           const LoopTiles &scan, const LoopTiles &store, cudaStream_t s);
 // Epsilon dominance (PUMP.cu:188-218) over the new paths the HSMC kernel
 // wrote with their time, cost, CP cut-off and per-node lists (its
 // HsmcEpilogue); wavefront size from the device (wave_size), at most
@@ -217,18 +213,20 @@ HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff);
 // in the same order, linked into its node's list, goal-tested, and its
 // particle mask moves from the stage to its stored slot.
 // Wavefront size from the device (wave_size); max_new bounds it (sizes the
-// grid).  The store's tile scratch must be zeroed.  With host_ctl (pinned
+// grid).  The store's tile scratch must be zeroed; it zeroes the
+// expansion's (scan) for the next iteration.  With host_ctl (pinned
 // host memory), the last block to finish copies the iteration's counters
 // there and then writes seq to host_ctl->seq, so the host can wait for that
 // word instead of synchronising the stream.
 pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int g_idx,
                            float cost_threshold, float dr, float cp_min_soln, const uint32_t *stage,
-                           uint32_t *valid, int words, const LoopTiles &store, SearchCtl *host_ctl,
-                           unsigned int seq, cudaStream_t s);
+                           uint32_t *valid, int words, const LoopTiles &store,
+                           const LoopTiles &scan, SearchCtl *host_ctl, unsigned int seq,
+                           cudaStream_t s);
 
 // The graph of the search loop for the argument block at d_args (device):
 // init, then a while node over {[lazy: edge checks], scan, expansion, HSMC,
-// dominance, store, control}.  Launch shapes are fixed (grid-stride and
+// dominance, store with the control step}.  Launch shapes are fixed (grid-stride and
 // tile-counter loops); dynamic shared memory is sized for numObs boxes and
 // numDisc waypoints per edge.  Kernel attributes are set here, before the
 // capture.
