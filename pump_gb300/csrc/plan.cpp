@@ -556,7 +556,7 @@ pump_status_t Planner::explore() {
   DevBuf<int> d_prev, d_node, d_g0, d_g1, d_nhead, d_nnext, d_wnode, d_wopen, d_newhead, d_newnext;
   DevBuf<float> d_cost, d_cp, d_ncost, d_ntime;
   DevBuf<unsigned int> d_off;
-  DevBuf<uint8_t> d_alive, d_dom;
+  DevBuf<uint8_t> d_alive;
   DevBuf<SearchCtl> d_ctl;
   PUMP_TRY(d_prev.alloc(cap));
   PUMP_TRY(d_node.alloc(cap));
@@ -572,7 +572,6 @@ pump_status_t Planner::explore() {
   PUMP_TRY(d_ncost.alloc(cap));
   PUMP_TRY(d_ntime.alloc(cap));
   PUMP_TRY(d_alive.alloc(cap));
-  PUMP_TRY(d_dom.alloc(cap));
   PUMP_TRY(d_newhead.alloc(N_));
   PUMP_TRY(d_newnext.alloc(cap));
   PUMP_TRY(d_ctl.alloc(1));
@@ -623,7 +622,6 @@ pump_status_t Planner::explore() {
   sd.new_time = d_ntime.p;
   sd.new_cp = d_cpStage_.p;
   sd.alive = d_alive.p;
-  sd.dominated = d_dom.p;
   sd.new_head = d_newhead.p;
   sd.new_next = d_newnext.p;
   sd.ctl = d_ctl.p;
@@ -715,13 +713,13 @@ pump_status_t Planner::explore() {
                               d_disc_.p, maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
                               pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p,
                               P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf, &epi));
-    // cut-off (written by the HSMC kernel), dominance, storing, buckets
+    // cut-off (written by the HSMC kernel), dominance and storing, buckets
     // (PUMP.cu:164-256)
-    PUMP_TRY(search_prune(sd, maxNew, numPaths_, epsCP_, epsCost_, s_));
     // the store pass's last block leaves the counters in hctl (pinned)
     const unsigned int sq = next_seq();
     *reinterpret_cast<volatile unsigned int *>(&hctl->seq) = sq - 1u;
-    PUMP_TRY(search_store(sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln, d_stage_.p,
+    PUMP_TRY(search_store(sd, maxNew, numPaths_, Gidx, costThreshold, dr, cpMinSoln, epsCP_,
+                          epsCost_, d_stage_.p,
                           d_valid_.p, words_, storeT, scanT, hctl, sq, s_));
     res_->d2h_bytes += (long long)sizeof(SearchCtl);
     PUMP_TRY(wait_seq(&hctl->seq, sq));

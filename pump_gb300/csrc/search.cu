@@ -339,40 +339,32 @@ __global__ void __launch_bounds__(kExpThreads) expand_kernel(SearchDev sd, const
 
 // PUMP.cu:188-218: a new path (not at the goal) dies if a stored path at its
 // node, or another new path there that passed the cut-off, epsilon-dominates
-// it; co-dominant paths keep the lower path number.
-__device__ void dominance_one(SearchDev sd, int i, int num_paths, float eps_cp, float eps_cost) {
-  const int node = sd.wf_node[i];
-  uint8_t dead = 0;
-  if (sd.alive[i] && node != sd.goal) {
-    const int path_idx = num_paths + i;
-    const float cp = sd.new_cp[i], cost = sd.new_cost[i];
-    auto dominated_by = [&](float cp_c, float cost_c, int idx_c) {
-      if (cp_c < eps_cp + cp && cost_c < eps_cost + cost) {
-        if (cp_c + eps_cp >= cp && cost_c + eps_cost >= cost && path_idx < idx_c) return false;
-        return true;
-      }
-      return false;
-    };
-    for (int c = sd.node_head[node]; c >= 0 && !dead; c = sd.node_next[c])
-      if (dominated_by(sd.path_cp[c], sd.path_cost[c], c)) dead = 1;
-    for (int j = sd.new_head[node]; j >= 0 && !dead; j = sd.new_next[j])
-      if (j != i && dominated_by(sd.new_cp[j], sd.new_cost[j], num_paths + j)) dead = 1;
+// it; co-dominant paths keep the lower path number.  Tested inside the store
+// pass, which prepends its survivors to the stored lists meanwhile: the walk
+// reads the lists through L2 and skips entries stored in this pass (index
+// num_paths or above), so it sees each list as it was when the pass began (a
+// survivor is published only after its link is written).
+__device__ __forceinline__ bool dominated_in_store(const SearchDev &sd, int i, int node,
+                                                   int num_paths, float eps_cp, float eps_cost) {
+  const int path_idx = num_paths + i;
+  const float cp = sd.new_cp[i], cost = sd.new_cost[i];
+  auto dominated_by = [&](float cp_c, float cost_c, int idx_c) {
+    if (cp_c < eps_cp + cp && cost_c < eps_cost + cost) {
+      if (cp_c + eps_cp >= cp && cost_c + eps_cost >= cost && path_idx < idx_c) return false;
+      return true;
+    }
+    return false;
+  };
+  for (int c = __ldcg(&sd.node_head[node]); c >= 0; c = __ldcg(&sd.node_next[c])) {
+    if (c >= num_paths) continue;
+    if (dominated_by(sd.path_cp[c], sd.path_cost[c], c)) return true;
   }
-  sd.dominated[i] = dead;
+  for (int j = sd.new_head[node]; j >= 0; j = sd.new_next[j])
+    if (j != i && dominated_by(sd.new_cp[j], sd.new_cost[j], num_paths + j)) return true;
+  return false;
 }
 
-__device__ __forceinline__ void dominance_body(const SearchDev &sd, int num_paths, float eps_cp,
-                                               float eps_cost) {
-  const int n = wave_size(sd.ctl);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    dominance_one(sd, i, num_paths, eps_cp, eps_cost);
-}
-
-__global__ void dominance_kernel(SearchDev sd, int num_paths, float eps_cp, float eps_cost) {
-  dominance_body(sd, num_paths, eps_cp, eps_cost);
-}
-
-// PUMP.cu:221-282 in one pass.  A survivor (alive, not dominated, not at the
+// PUMP.cu:188-282 in one pass.  A survivor (alive, not dominated, not at the
 // initial node) becomes stored path num_paths + r, r = its rank among the
 // survivors in wavefront order, and is appended to bucket b at
 // g_base[b] + r_b, r_b = its rank among the survivors of bucket b (the
@@ -382,21 +374,22 @@ __global__ void dominance_kernel(SearchDev sd, int num_paths, float eps_cp, floa
 // the look-back value, 16 bits each within a tile), so the look-back adds
 // both at once.  The last tile writes the survivor count and the bucket
 // sizes.  Each survivor also moves its particle mask from the stage.
-// A wavefront is typically a few thousand paths, so tiles are small (4 rows
-// of 256) to spread it over many blocks, and each thread issues all loads of
-// its rows before any node-list exchange or store, so their latencies
-// overlap instead of adding up row after row.
-constexpr int kStoreRows = 4;
-constexpr int kStoreTile = kCompactThreads * kStoreRows;  // 1024 items
+// A wavefront is typically a few thousand paths, so tiles are small (256
+// paths, one per thread, whose dominance walks run side by side) to spread
+// it over many blocks, and each thread issues all loads of its path before
+// any node-list push or store.
+constexpr int kStoreRows = 1;
+constexpr int kStoreTile = kCompactThreads * kStoreRows;  // 256 items
 constexpr int kStoreWarps = kCompactThreads / 32;
-static_assert(kStoreRows * kStoreWarps == 32, "one (row, warp) count per lane of the scan");
+constexpr int kStoreCounts = kStoreRows * kStoreWarps;
+static_assert(kStoreCounts <= 32, "one (row, warp) count per lane of the scan");
 constexpr unsigned long long kLow31 = (1ull << 31) - 1ull;
 static_assert(kLoopStoreTile == kStoreTile, "store tile size");
 
 __device__ __forceinline__ void store_tiles(
     const SearchDev &sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
-    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words,
-    const TileScratch &ts) {
+    float eps_cp, float eps_cost, const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid,
+    int words, const TileScratch &ts) {
   // per (row, warp): survivors | survivors of bucket 1 << 16, then their
   // exclusive offsets within the tile; entry r * kStoreWarps + warp
   __shared__ unsigned int s_cnt[kStoreRows * kStoreWarps];
@@ -417,16 +410,20 @@ __device__ __forceinline__ void store_tiles(
 #pragma unroll
     for (int r = 0; r < kStoreRows; ++r) {
       const long long i = base + r * kCompactThreads + threadIdx.x;
-      uint8_t al = 0, dm = 1;
+      uint8_t al = 0;
       node[r] = 0;
       cost[r] = 0.0f;
       if (i < n) {
         al = sd.alive[i];
-        dm = sd.dominated[i];
         node[r] = sd.wf_node[i];
         cost[r] = sd.new_cost[i];
       }
-      surv[r] = al && !dm && node[r] != 0;
+      // dominance is tested only for live paths not at the goal (or at the
+      // initial node, which stores nothing)
+      bool dead = false;
+      if (al && node[r] != sd.goal && node[r] != 0)
+        dead = dominated_in_store(sd, (int)i, node[r], num_paths, eps_cp, eps_cost);
+      surv[r] = al && !dead && node[r] != 0;
     }
     uint8_t bkt[kStoreRows];
 #pragma unroll
@@ -450,14 +447,14 @@ __device__ __forceinline__ void store_tiles(
     if (warp == 0) {
       // (row, warp) order is lane order: one warp scan of the packed pairs
       // (each half at most kStoreTile < 2^16, so the halves never carry)
-      const unsigned int v = s_cnt[lane];
+      const unsigned int v = lane < kStoreCounts ? s_cnt[lane] : 0u;
       unsigned int incl = v;
 #pragma unroll
       for (int off = 1; off < 32; off <<= 1) {
         const unsigned int o = __shfl_up_sync(0xffffffffu, incl, off);
         if (lane >= off) incl += o;
       }
-      s_cnt[lane] = incl - v;
+      if (lane < kStoreCounts) s_cnt[lane] = incl - v;
       const unsigned int tt = __shfl_sync(0xffffffffu, incl, 31);
       const unsigned long long agg =
           (unsigned long long)(tt & 0xFFFFu) | ((unsigned long long)(tt >> 16) << 31);
@@ -506,13 +503,23 @@ __device__ __forceinline__ void store_tiles(
       cp[r] = sd.new_cp[i];
       if (words == 4) mk[r] = reinterpret_cast<const uint4 *>(stage)[i];
     }
-    // then the node-list exchanges (independent of one another), and the
-    // nodes reached for the first time listed for their edge checks (the
-    // thread that moves a node's count from -1 to 0 lists it)
-    int old[kStoreRows];
+    // then the survivors pushed onto their nodes' stored lists: the link is
+    // written (through L2) before the entry is published, so a concurrent
+    // dominance walk never follows an unset link; and the nodes reached for
+    // the first time listed for their edge checks (the thread that moves a
+    // node's count from -1 to 0 lists it)
 #pragma unroll
-    for (int r = 0; r < kStoreRows; ++r)
-      old[r] = surv[r] ? atomicExch(&sd.node_head[node[r]], st[r]) : -1;
+    for (int r = 0; r < kStoreRows; ++r) {
+      if (!surv[r]) continue;
+      int h = __ldcg(&sd.node_head[node[r]]);
+      while (true) {
+        __stcg(&sd.node_next[st[r]], h);
+        __threadfence();
+        const int seen = atomicCAS(&sd.node_head[node[r]], h, st[r]);
+        if (seen == h) break;
+        h = seen;
+      }
+    }
 #pragma unroll
     for (int r = 0; r < kStoreRows; ++r)
       if (surv[r] && sd.open_cnt[node[r]] == -1 && atomicCAS(&sd.open_cnt[node[r]], -1, 0) == -1)
@@ -528,7 +535,6 @@ __device__ __forceinline__ void store_tiles(
       sd.path_time[p] = tm[r];
       sd.path_cp[p] = cp[r];
       (bkt[r] == 1 ? sd.g_list[1] : sd.g_list[0])[slot[r]] = p;
-      sd.node_next[p] = old[r];
       if (node[r] == sd.goal && cp[r] <= cp_min_soln) atomicOr(&sd.ctl->goal_found, 1);
       uint32_t *dst = valid + (long long)p * words;
       if (words == 4) {
@@ -545,9 +551,10 @@ __device__ __forceinline__ void store_tiles(
 
 __device__ __forceinline__ void store_body(
     const SearchDev &sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
-    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words,
-    const TileScratch &ts, unsigned int *done, SearchCtl *host_ctl, unsigned int seq) {
-  store_tiles(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts);
+    float eps_cp, float eps_cost, const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid,
+    int words, const TileScratch &ts, unsigned int *done, SearchCtl *host_ctl, unsigned int seq) {
+  store_tiles(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, eps_cp, eps_cost, stage, valid,
+              words, ts);
   if (!host_ctl) return;
   // the last block to finish copies the counters to the host
   __syncthreads();
@@ -574,11 +581,12 @@ __device__ __forceinline__ void store_body(
 
 __global__ void __launch_bounds__(kCompactThreads) store_kernel(
     SearchDev sd, int num_paths, int g_idx, float cost_threshold, float dr, float cp_min_soln,
-    const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid, int words, TileScratch ts,
-    unsigned int *done, SearchCtl *host_ctl, unsigned int seq, LoopTiles scan) {
+    float eps_cp, float eps_cost, const uint32_t *__restrict__ stage, uint32_t *__restrict__ valid,
+    int words, TileScratch ts, unsigned int *done, SearchCtl *host_ctl, unsigned int seq,
+    LoopTiles scan) {
   zero_tiles(scan);  // for the next iteration's expansion
-  store_body(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, stage, valid, words, ts, done,
-             host_ctl, seq);
+  store_body(sd, num_paths, g_idx, cost_threshold, dr, cp_min_soln, eps_cp, eps_cost, stage, valid,
+             words, ts, done, host_ctl, seq);
 }
 
 // ------------------------------------------- the search loop on the device
@@ -638,10 +646,6 @@ __global__ void __launch_bounds__(kExpThreads) expand_loop_kernel(const LoopArgs
               a->L.max_paths, ts, a->store);
 }
 
-__global__ void dominance_loop_kernel(const LoopArgs *a) {
-  const SearchDev sd = a->sd;
-  dominance_body(sd, a->L.num_paths, a->eps_cp, a->eps_cost);
-}
 
 // The host loop's bookkeeping after an iteration's counters are back
 // (PUMP.cu:259-288), then the condition of the next iteration; run by the
@@ -701,13 +705,13 @@ __device__ void loop_control(LoopArgs *a, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
-__global__ void __launch_bounds__(kCompactThreads, 3) store_loop_kernel(
+__global__ void __launch_bounds__(kCompactThreads, 2) store_loop_kernel(
     LoopArgs *a, cudaGraphConditionalHandle h) {
   const SearchDev sd = a->sd;
   const TileScratch ts = tiles_of(a->store);
   zero_tiles(a->scan);  // for the next iteration's expansion
   store_tiles(sd, a->L.num_paths, a->L.g_idx, a->L.cost_threshold, a->L.dr, a->cp_min_soln,
-              a->stage, a->valid, a->words, ts);
+              a->eps_cp, a->eps_cost, a->stage, a->valid, a->words, ts);
   // the last block to finish runs the loop's control step
   __shared__ bool s_last;
   __syncthreads();
@@ -798,16 +802,10 @@ HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff) {
   return e;
 }
 
-pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float eps_cp,
-                           float eps_cost, cudaStream_t s) {
-  long long blocks = ((long long)(max_new > 0 ? max_new : 1) + 255) / 256;
-  if (blocks > kNumSMs * 4) blocks = kNumSMs * 4;
-  dominance_kernel<<<(unsigned)blocks, 256, 0, s>>>(sd, num_paths, eps_cp, eps_cost);
-  return launch_status("dominance");
-}
 
 pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int g_idx,
-                           float cost_threshold, float dr, float cp_min_soln, const uint32_t *stage,
+                           float cost_threshold, float dr, float cp_min_soln, float eps_cp,
+                           float eps_cost, const uint32_t *stage,
                            uint32_t *valid, int words, const LoopTiles &store,
                            const LoopTiles &scan, SearchCtl *host_ctl, unsigned int seq,
                            cudaStream_t s) {
@@ -820,8 +818,8 @@ pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int 
   if (ntiles > store.cap) return set_error(PUMP_ERR_CAPACITY, "store pass: %lld tiles", ntiles);
   const unsigned blocks = (unsigned)(ntiles < kNumSMs * 4 ? ntiles : kNumSMs * 4);
   store_kernel<<<blocks, kCompactThreads, 0, s>>>(sd, num_paths, g_idx, cost_threshold, dr,
-                                                  cp_min_soln, stage, valid, words, ts, store.done,
-                                                  host_ctl, seq, scan);
+                                                  cp_min_soln, eps_cp, eps_cost, stage, valid,
+                                                  words, ts, store.done, host_ctl, seq, scan);
   return launch_status("store_kernel");
 }
 
@@ -889,7 +887,6 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
       }
       expand_loop_kernel<<<kNumSMs * 2, kExpThreads, 0, cs>>>(d_args);
       hsmc_loop_launch(&d_args->hp, &d_args->L, numObs, g_wide, cs);
-      dominance_loop_kernel<<<g_wide, 256, 0, cs>>>(d_args);
       store_loop_kernel<<<g_wide, kCompactThreads, 0, cs>>>(d_args, h);
       cudaGraph_t captured = nullptr;
       const pump_status_t ce = cuda_status(cudaStreamEndCapture(cs, &captured), "cudaStreamEndCapture");

@@ -55,7 +55,7 @@ struct SearchDev {
   unsigned int *wf_off;          // expansion offsets per bucket entry
   float *new_cost, *new_time;
   const float *new_cp;           // HSMC output
-  uint8_t *alive, *dominated;
+  uint8_t *alive;
   int *new_head, *new_next;      // new paths per node passing the CP cut-off
   SearchCtl *ctl;
 };
@@ -143,7 +143,7 @@ enum LoopStatus {
 
 // Items per look-back tile of the loop's expansion and store passes.
 constexpr int kLoopScanTile = 32;
-constexpr int kLoopStoreTile = 1024;
+constexpr int kLoopStoreTile = 256;
 
 // Tile scratch of one look-back pass of the loop (zeroed before each pass):
 // total, status words (one per tile, from status[0]), tile counter, error
@@ -200,15 +200,12 @@ pump_status_t max_degree_async(const int *d_go, int N, int *d_out, cudaStream_t 
 // zeroes it for the next iteration).
 pump_status_t search_expand(const SearchDev &sd, int g_idx, int n_g, int num_paths, int max_paths,
                            const LoopTiles &scan, const LoopTiles &store, cudaStream_t s);
-// Epsilon dominance (PUMP.cu:188-218) over the new paths the HSMC kernel
-// wrote with their time, cost, CP cut-off and per-node lists (its
-// HsmcEpilogue); wavefront size from the device (wave_size), at most
-// max_new (sizes the grid).
-pump_status_t search_prune(const SearchDev &sd, int max_new, int num_paths, float eps_cp,
-                           float eps_cost, cudaStream_t s);
 // The search's part of the HSMC kernel for this search state.
 HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff);
-// One pass over the wavefront (PUMP.cu:221-282): survivors become stored
+// One pass over the wavefront (PUMP.cu:188-282): a new path survives if it
+// passed the CP cut-off, is not epsilon-dominated (PUMP.cu:188-218, tested
+// here against the lists as they were when the pass began) and is not at
+// the initial node; survivors become stored
 // paths num_paths + rank in wavefront order, each is appended to its bucket
 // in the same order, linked into its node's list, goal-tested, and its
 // particle mask moves from the stage to its stored slot.
@@ -219,15 +216,16 @@ HsmcEpilogue search_hsmc_epilogue(const SearchDev &sd, float cp_cutoff);
 // there and then writes seq to host_ctl->seq, so the host can wait for that
 // word instead of synchronising the stream.
 pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int g_idx,
-                           float cost_threshold, float dr, float cp_min_soln, const uint32_t *stage,
+                           float cost_threshold, float dr, float cp_min_soln, float eps_cp,
+                           float eps_cost, const uint32_t *stage,
                            uint32_t *valid, int words, const LoopTiles &store,
                            const LoopTiles &scan, SearchCtl *host_ctl, unsigned int seq,
                            cudaStream_t s);
 
 // The graph of the search loop for the argument block at d_args (device):
 // init, then a while node over {[lazy: edge checks], scan, expansion, HSMC,
-// dominance, store with the control step}.  Launch shapes are fixed (grid-stride and
-// tile-counter loops); dynamic shared memory is sized for numObs boxes and
+// store with the dominance test and the control step}.  Launch shapes are
+// fixed (grid-stride and tile-counter loops); dynamic shared memory is sized for numObs boxes and
 // numDisc waypoints per edge.  Kernel attributes are set here, before the
 // capture.
 pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numObs, int numDisc,
