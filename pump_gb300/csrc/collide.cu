@@ -101,21 +101,10 @@ __global__ void __launch_bounds__(256) free_edges_kernel(const float *__restrict
 }
 
 // freeEdges (collisionCheck.cu:5-37) over the waypoints in disc, block of T
-// edges.  The block's waypoint positions (contiguous in disc) are staged in
-// shared memory; each thread takes the bounding box of its edge's waypoints.
-// Then each warp walks the boxes in order: the edges of the warp whose
-// bounding box a box is not broadphase-disjoint from (every edge when a
-// waypoint is NaN) append the pair (edge, box) to the warp's queue, and
-// whenever 32 pairs are queued the warp tests them, one pair per lane: the
-// pair's segments against its box, the reference's (segment, box) test.  An
-// edge is free when none of its pairs hits.  The reference's result is the
-// AND over the (segment, box) pairs, and a box disjoint from the edge's
-// bounding box passes for every segment, so the filter and the order change
-// no result; the queue keeps the lanes busy where per-lane box lists would
-// leave most of a warp waiting for its longest list.  The block size T (64,
-// 128, 256) is picked by the autotuner.
-constexpr int kQueueSlots = 64;  // per warp: a ring of two rounds of pairs
-
+// edges: the block's waypoint positions (contiguous in disc) are staged in
+// shared memory, then each warp tests its 32 edges with the pair queue of
+// warp_queue_hits.  The block size T (64, 128, 256) is picked by the
+// autotuner.
 template <int T>
 __global__ void __launch_bounds__(T) free_edges_queue_kernel(
     const float *__restrict__ obs, int numObs, const float *__restrict__ disc, long long E,
@@ -139,71 +128,11 @@ __global__ void __launch_bounds__(T) free_edges_queue_kernel(
       s_wp[r * 3 + 2] = z;
     }
   }
-  s_hit[threadIdx.x] = 0;
   stage_obstacles(obs, numObs, s_obs);  // ends with __syncthreads
-  constexpr int kPos = 3;  // floats per staged waypoint
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const unsigned int lt = (1u << lane) - 1u;
-  const bool active = t < nv;
-  float emin[3], emax[3];
-  bool nan = false;
-  if (active) {
-    const float *wp = s_wp + t * W * kPos;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
-    for (int i = 0; i < W; ++i)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const float x = wp[i * kPos + d];
-        nan = nan || x != x;
-        emin[d] = fminf(emin[d], x);
-        emax[d] = fmaxf(emax[d], x);
-      }
-  }
-  int *q = s_queue[warp];
-  // one queued pair: the edge's lane in the warp (high half), the box
-  auto test_pair = [&](int ent) {
-    const int el = warp * 32 + (ent >> 16), o = ent & 0xFFFF;
-    if (s_hit[el]) return;  // the edge already hit a box
-    const float *wp = s_wp + el * W * kPos;
-    const float *ob = &s_obs[o * 12];
-    float v[3], w[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) v[d] = wp[d];
-    for (int i = 0; i < numDisc; ++i) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
-      if (segment_box_hit(v, w, ob)) {
-        s_hit[el] = 1;
-        return;
-      }
-#pragma unroll
-      for (int d = 0; d < 3; ++d) v[d] = w[d];
-    }
-  };
-  int head = 0, tail = 0;  // warp-uniform
-  const float4 *s_obs4 = reinterpret_cast<const float4 *>(s_obs);
-  for (int o = 0; o < numObs; ++o) {
-    // broadphaseValidQ of the edge's bounding box, without branches: box o
-    // is lo = (x0, y0, z0) at floats 0-2 and hi = (x1, y1, z1) at floats 6-8
-    const float4 a = s_obs4[o * 3], b = s_obs4[o * 3 + 1], c = s_obs4[o * 3 + 2];
-    const bool disjoint = (emax[0] <= a.x) | (b.z <= emin[0]) | (emax[1] <= a.y) |
-                          (b.w <= emin[1]) | (emax[2] <= a.z) | (c.x <= emin[2]);
-    const bool need = active && (nan || !disjoint);
-    const unsigned int bal = __ballot_sync(0xffffffffu, need);
-    if (need) q[(tail + __popc(bal & lt)) & (kQueueSlots - 1)] = (lane << 16) | o;
-    tail += __popc(bal);
-    if (tail - head >= 32) {
-      __syncwarp();
-      test_pair(q[(head + lane) & (kQueueSlots - 1)]);
-      head += 32;
-      __syncwarp();  // the slots just taken are rewritten by later boxes
-    }
-  }
-  __syncwarp();
-  if (lane < tail - head) test_pair(q[(head + lane) & (kQueueSlots - 1)]);
-  __syncwarp();
-  if (active) is_free[e0 + t] = s_hit[t] ? 0 : 1;
+  const int t = threadIdx.x, warp = t >> 5;
+  const bool hit = warp_queue_hits(s_wp + warp * 32 * W * 3, W, s_obs, numObs, t < nv,
+                                   s_queue[warp], s_hit + warp * 32);
+  if (t < nv) is_free[e0 + t] = hit ? 0 : 1;
 }
 
 // One thread per waypoint: setupAsBs (hsmc.cu:201-211) fused with

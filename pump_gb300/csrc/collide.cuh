@@ -112,6 +112,92 @@ __device__ __forceinline__ bool segment_valid_masked(const float *v, const float
   return true;
 }
 
+// Slots of the per-warp ring of (edge, box) pairs of warp_queue_hits.
+constexpr int kQueueSlots = 64;
+
+// freeEdges's test (collisionCheck.cu:5-143) for the 32 edges of one warp:
+// lane l holds edge l (when active), its W waypoint positions at
+// s_wp_warp + l * W * 3 in shared memory; the boxes are at s_obs.  Each
+// lane takes the bounding box of its edge's waypoints.  Then the warp walks
+// the boxes in order: the edges whose bounding box a box is not
+// broadphase-disjoint from (every edge when a waypoint is NaN) append the
+// pair (edge, box) to the warp's ring q, and whenever 32 pairs are queued
+// the warp tests them, one pair per lane: the pair's segments against its
+// box, the reference's (segment, box) test.  The reference's result is the
+// AND over the (segment, box) pairs, and a box disjoint from the edge's
+// bounding box passes for every segment, so the filter and the order change
+// no result; the queue keeps the lanes busy where per-lane box lists would
+// leave most of a warp waiting for its longest list.  q: the warp's
+// kQueueSlots ints, hit: its 32 bytes, both in shared memory.  Returns
+// whether this lane's edge hits a box.
+__device__ __forceinline__ bool warp_queue_hits(const float *s_wp_warp, int W, const float *s_obs,
+                                                int numObs, bool active, int *q, uint8_t *hit) {
+  constexpr int kPos = 3;  // floats per staged waypoint
+  const int lane = threadIdx.x & 31;
+  const unsigned int lt = (1u << lane) - 1u;
+  const int numDisc = W - 1;
+  hit[lane] = 0;
+  __syncwarp();
+  float emin[3], emax[3];
+  bool nan = false;
+  if (active) {
+    const float *wp = s_wp_warp + lane * W * kPos;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
+    for (int i = 0; i < W; ++i)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float x = wp[i * kPos + d];
+        nan = nan || x != x;
+        emin[d] = fminf(emin[d], x);
+        emax[d] = fmaxf(emax[d], x);
+      }
+  }
+  // one queued pair: the edge's lane (high half), the box
+  auto test_pair = [&](int ent) {
+    const int el = ent >> 16, o = ent & 0xFFFF;
+    if (hit[el]) return;  // the edge already hit a box
+    const float *wp = s_wp_warp + el * W * kPos;
+    const float *ob = &s_obs[o * 12];
+    float v[3], w[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] = wp[d];
+    for (int i = 0; i < numDisc; ++i) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
+      if (segment_box_hit(v, w, ob)) {
+        hit[el] = 1;
+        return;
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v[d] = w[d];
+    }
+  };
+  int head = 0, tail = 0;  // warp-uniform
+  const float4 *s_obs4 = reinterpret_cast<const float4 *>(s_obs);
+  for (int o = 0; o < numObs; ++o) {
+    // broadphaseValidQ of the edge's bounding box, without branches: box o
+    // is lo = (x0, y0, z0) at floats 0-2 and hi = (x1, y1, z1) at floats 6-8
+    const float4 a = s_obs4[o * 3], b = s_obs4[o * 3 + 1], c = s_obs4[o * 3 + 2];
+    const bool disjoint = (emax[0] <= a.x) | (b.z <= emin[0]) | (emax[1] <= a.y) |
+                          (b.w <= emin[1]) | (emax[2] <= a.z) | (c.x <= emin[2]);
+    const bool need = active && (nan || !disjoint);
+    const unsigned int bal = __ballot_sync(0xffffffffu, need);
+    if (need) q[(tail + __popc(bal & lt)) & (kQueueSlots - 1)] = (lane << 16) | o;
+    tail += __popc(bal);
+    if (tail - head >= 32) {
+      __syncwarp();
+      test_pair(q[(head + lane) & (kQueueSlots - 1)]);
+      head += 32;
+      __syncwarp();  // the slots just taken are rewritten by later boxes
+    }
+  }
+  __syncwarp();
+  if (lane < tail - head) test_pair(q[(head + lane) & (kQueueSlots - 1)]);
+  __syncwarp();
+  return hit[lane] != 0;
+}
+
 // The half-space box o contributes at a waypoint (pos, vel): cacheHalfspaces,
 // hsmc.cu:10-99, with bvlsShortcut (bvls.cu:259-273) for the closest point.
 // False when the point is farther than the distance gate (d2 > maxd2);

@@ -69,23 +69,30 @@ __global__ void search_init_head_kernel(SearchDev sd) { sd.node_head[0] = 0; }
 // the split changes no result, and a search iteration that reaches few nodes
 // runs a short chain of box tests per thread instead of all of them.  Each
 // chunk adds its count of free edges to free nodes to the node's count.
+// The wide form, for iterations that list many nodes: 256-edge chunks, and
+// each warp tests its 32 edges with the pair queue of warp_queue_hits (the
+// eager edge check's test), which keeps the lanes busy where the narrow
+// form's box split leaves them waiting on the longest box list.
 constexpr int kChkThreads = 256;
 constexpr int kChkLanes = 8;
 constexpr int kChkEdges = kChkThreads / kChkLanes;  // 32
+constexpr int kChkWideEdges = kChkThreads;          // 256
 
-size_t check_smem(int numObs, int numDisc) {
-  return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)kChkEdges * (numDisc + 1) * 3);
+size_t check_smem(int numObs, int numDisc, bool wide) {
+  return sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) +
+                          (size_t)(wide ? kChkWideEdges : kChkEdges) * (numDisc + 1) * 3);
 }
 
-template <int Mode>
+template <int Mode, bool Wide>
 __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs &ca) {
+  constexpr int kEdges = Wide ? kChkWideEdges : kChkEdges;
   extern __shared__ float4 s_dyn4[];
   __shared__ int s_open[kChkThreads / 32];
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   const int numDisc = ca.numDisc, W = numDisc + 1;
-  float *s_wp = s_obs + ((ca.numObs * 12 + 3) & ~3);  // kChkEdges x W x 3 positions
+  float *s_wp = s_obs + ((ca.numObs * 12 + 3) & ~3);  // kEdges x W x 3 positions
   const int n_todo = sd.ctl->todo;
-  const int chunks = ca.max_degree > kChkEdges ? (ca.max_degree + kChkEdges - 1) / kChkEdges : 1;
+  const int chunks = ca.max_degree > kEdges ? (ca.max_degree + kEdges - 1) / kEdges : 1;
   const long long items = (long long)n_todo * chunks;
   if (blockIdx.x >= items) return;  // no item: leave before staging (block-uniform)
   stage_obstacles(ca.obs, ca.numObs, s_obs);
@@ -95,9 +102,9 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
     const int t = (int)(j / chunks), c = (int)(j - (long long)t * chunks);
     const int node = sd.todo[t];
     const int e1 = sd.go[node + 1];
-    const int c0 = sd.go[node] + c * kChkEdges;
+    const int c0 = sd.go[node] + c * kEdges;
     if (c0 >= e1) continue;  // block-uniform: this node has fewer chunks
-    const int ne = e1 - c0 < kChkEdges ? e1 - c0 : kChkEdges;
+    const int ne = e1 - c0 < kEdges ? e1 - c0 : kEdges;
     for (int q = threadIdx.x; q < ne * W; q += kChkThreads) {
       const int eq = q / W, i = q - eq * W;
       const int e = c0 + eq;
@@ -130,6 +137,30 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
       for (int d = 0; d < 3; ++d) s_wp[q * 3 + d] = x[d];
     }
     __syncthreads();
+    if constexpr (Wide) {
+      __shared__ int s_q[kChkThreads / 32][kQueueSlots];
+      __shared__ uint8_t s_h[kChkThreads];
+      const bool active = (int)threadIdx.x < ne;
+      const bool h = warp_queue_hits(s_wp + warp * 32 * W * 3, W, s_obs, ca.numObs, active,
+                                     s_q[warp], s_h + warp * 32);
+      int open = 0;
+      if (active) {
+        const int e = c0 + threadIdx.x;
+        sd.free_e[e] = h ? 0 : 1;
+        open = (!h && sd.free_s[sd.dst[e]]) ? 1 : 0;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) open += __shfl_xor_sync(0xffffffffu, open, o);
+      if (lane == 0) s_open[warp] = open;
+      __syncthreads();  // also: every lane is done with s_wp
+      if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int q = 0; q < kChkThreads / 32; ++q) tot += s_open[q];
+        if (tot) atomicAdd(&sd.open_cnt[node], tot);
+      }
+      __syncthreads();  // s_open and s_wp are rewritten by the next item
+      continue;
+    }
     bool hit = false;
     if (el < ne) {
       constexpr int kPos = 3;  // floats per staged waypoint
@@ -183,9 +214,9 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
   }
 }
 
-template <int Mode>
+template <int Mode, bool Wide>
 __global__ void __launch_bounds__(kChkThreads) check_kernel(SearchDev sd, CheckArgs ca) {
-  check_body<Mode>(sd, ca);
+  check_body<Mode, Wide>(sd, ca);
 }
 
 // One warp per node: open_cnt[node] = its free edges to free nodes.
@@ -635,7 +666,7 @@ template <int Mode>
 __global__ void __launch_bounds__(kChkThreads, 4) check_loop_kernel(const LoopArgs *a) {
   const SearchDev sd = a->sd;
   const CheckArgs ca = a->ca;
-  check_body<Mode>(sd, ca);
+  check_body<Mode, false>(sd, ca);
 }
 
 __global__ void __launch_bounds__(kExpThreads) expand_loop_kernel(const LoopArgs *a) {
@@ -738,21 +769,33 @@ pump_status_t search_init(const SearchDev &sd, cudaStream_t s) {
 
 pump_status_t search_check(const SearchDev &sd, int max_todo, const CheckArgs &ca, cudaStream_t s) {
   if (max_todo <= 0) return PUMP_OK;
-  const size_t smem = check_smem(ca.numObs, ca.numDisc);
+  // the wide form when its items alone fill the GPU twice over (and its
+  // stage fits): few listed nodes keep the narrow form's short chains
+  const long long wide_items =
+      (long long)max_todo * ((ca.max_degree + kChkWideEdges - 1) / kChkWideEdges);
+  const bool wide = wide_items >= 2LL * kNumSMs && ca.numObs <= 0xFFFF &&
+                    check_smem(ca.numObs, ca.numDisc, true) <= 200 * 1024;
+  const size_t smem = check_smem(ca.numObs, ca.numDisc, wide);
   if (smem > 220 * 1024)
     return set_error(PUMP_ERR_CAPACITY, "%d obstacles and %d waypoints exceed the check stage",
                      ca.numObs, ca.numDisc + 1);
   // at most one block per (listed node, chunk), no more than the GPU holds
-  const long long chunks =
-      ca.max_degree > kChkEdges ? (ca.max_degree + kChkEdges - 1) / kChkEdges : 1;
+  const int edges = wide ? kChkWideEdges : kChkEdges;
+  const long long chunks = ca.max_degree > edges ? (ca.max_degree + edges - 1) / edges : 1;
   const long long want = (long long)max_todo * chunks;
   const unsigned blocks = (unsigned)(want < kNumSMs * 8 ? want : kNumSMs * 8);
+  const void *fn = ca.mode == PUMP_BVP_PARITY
+                       ? (wide ? (const void *)check_kernel<PUMP_BVP_PARITY, true>
+                               : (const void *)check_kernel<PUMP_BVP_PARITY, false>)
+                       : (wide ? (const void *)check_kernel<PUMP_BVP_PRECISION, true>
+                               : (const void *)check_kernel<PUMP_BVP_PRECISION, false>);
+  PUMP_TRY(smem_attr(fn, smem));
   if (ca.mode == PUMP_BVP_PARITY) {
-    PUMP_TRY(smem_attr((const void *)check_kernel<PUMP_BVP_PARITY>, smem));
-    check_kernel<PUMP_BVP_PARITY><<<blocks, kChkThreads, smem, s>>>(sd, ca);
+    if (wide) check_kernel<PUMP_BVP_PARITY, true><<<blocks, kChkThreads, smem, s>>>(sd, ca);
+    else check_kernel<PUMP_BVP_PARITY, false><<<blocks, kChkThreads, smem, s>>>(sd, ca);
   } else {
-    PUMP_TRY(smem_attr((const void *)check_kernel<PUMP_BVP_PRECISION>, smem));
-    check_kernel<PUMP_BVP_PRECISION><<<blocks, kChkThreads, smem, s>>>(sd, ca);
+    if (wide) check_kernel<PUMP_BVP_PRECISION, true><<<blocks, kChkThreads, smem, s>>>(sd, ca);
+    else check_kernel<PUMP_BVP_PRECISION, false><<<blocks, kChkThreads, smem, s>>>(sd, ca);
   }
   return launch_status("check_kernel");
 }
@@ -827,7 +870,7 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
                                 const LoopTiles &scan, const LoopTiles &store,
                                 cudaStream_t capture_stream, cudaGraphExec_t *out) {
   *out = nullptr;
-  const size_t chk_smem = check_smem(numObs, numDisc);
+  const size_t chk_smem = check_smem(numObs, numDisc, false);
   if (chk_smem > 220 * 1024)
     return set_error(PUMP_ERR_CAPACITY, "%d obstacles and %d waypoints exceed the check stage",
                      numObs, numDisc + 1);
