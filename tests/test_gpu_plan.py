@@ -210,3 +210,29 @@ def test_search_graph_equals_host_loop(gpu, pumplib, goldens):
         assert got[0] == got[1]
     finally:
         L.pump_search_graph(1)
+
+
+def test_plan_batch_equals_single_large(gpu, pumplib):
+    """Larger batch queries (N 3000-6000, 40-100 boxes), whose search
+    iterations list enough nodes for the wide form of the lazy edge checks
+    (256-edge chunks, per-warp pair queue): the batch still gives exactly
+    what each query gives alone."""
+    torch, ctx = gpu
+    from pump_gb300 import workloads
+    L = pumplib.load()
+    qs = workloads.batch_queries(3, seed=123, n_range=(3000, 6000), obs_range=(40, 100))
+    keep = []
+    pbs = (pumplib.Problem * len(qs))(*[fill_problem(pumplib, q, keep) for q in qs])
+    for k in range(len(qs)):
+        pbs[k].bvp_mode = pumplib.PUMP_BVP_PRECISION
+    res = (pumplib.PlanResult * len(qs))()
+    paths = [np.zeros((400, 6), np.float32) for _ in qs]
+    for k in range(len(qs)):
+        res[k].path, res[k].path_cap = paths[k].ctypes.data, 400
+    sts = (C.c_int * len(qs))()
+    pumplib.check(L.pump_plan_batch(0, pbs, res, sts, len(qs), 2))
+    for k in range(len(qs)):
+        st1, r1, p1, _ = run_plan(pumplib, ctx, pbs[k])
+        assert sts[k] == st1
+        assert _fields(res[k]) == _fields(r1)
+        assert np.array_equal(paths[k][: res[k].path_len].view(np.uint32), p1.view(np.uint32))
