@@ -332,6 +332,58 @@ def measure_refine(args, lib, L, ctx, torch):
             "cost_reduction_median_accepted": float(np.median(1 - c1[acc] / c0[acc])) if acc.any() else None}
 
 
+# Throughput probe of the binary64 FMA pipe, the denominator of the pair
+# BVP's FP64 roofline (the peaks file holds HBM copy and bf16 GEMM figures
+# only): eight independent DFMA chains per thread, 8 blocks of 256 threads
+# per SM, 2 flops per DFMA.  A benchmark aid, not part of the library: it is
+# compiled here into the build directory on first use.
+FP64_PROBE_SRC = r"""
+#include <cuda_runtime.h>
+__global__ void __launch_bounds__(256) dfma_kernel(int iters, double seed, double *sink) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = seed + threadIdx.x * 1e-9 + k;
+  const double m = 0.999999999, c = 1e-12;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], m, c);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == 42.0) sink[0] = s;  // keeps the chains live; never true
+}
+extern "C" int fp64_probe_launch(int blocks, int iters, double *sink, void *stream) {
+  dfma_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(iters, 1.0, sink);
+  return (int)cudaGetLastError();
+}
+"""
+
+
+def fp64_peak_tflops(torch):
+    from pump_gb300.build import OUT, nvcc
+    so = os.path.join(OUT, "libfp64probe.so")
+    if not os.path.exists(so):
+        src = os.path.join(OUT, "fp64probe.cu")
+        with open(src, "w") as f:
+            f.write(FP64_PROBE_SRC)
+        subprocess.run([nvcc(), "-shared", "-Xcompiler", "-fPIC", "-O3", "-gencode",
+                        "arch=compute_103a,code=sm_103a", src, "-o", so], check=True)
+    P = C.CDLL(so)
+    P.fp64_probe_launch.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    blocks = torch.cuda.get_device_properties(0).multi_processor_count * 8
+    sink = torch.empty(1, dtype=torch.float64, device="cuda")
+    sh = torch.cuda.current_stream().cuda_stream
+    iters = 4096
+    assert P.fp64_probe_launch(blocks, iters // 8, sink.data_ptr(), sh) == 0
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    assert P.fp64_probe_launch(blocks, iters, sink.data_ptr(), sh) == 0
+    b.record()
+    b.synchronize()
+    return 2.0 * 8.0 * iters * blocks * 256 / (a.elapsed_time(b) * 1e-3) / 1e12
+
+
 def run_ours(args):
     import torch
     from pump_gb300 import lib
@@ -532,10 +584,8 @@ def run_ours(args):
             "gpu_launches": launches["n"],
             "clocks": clk,
         }
-        fp64 = C.c_double(0)
-        lib.check(L.pump_probe_fp64_tflops(C.byref(fp64), sh))
-        out["roofline"] = roofline(dom, ks, N, E, M_total, W, maxHS, P, args.mode, fp64.value,
-                                   float(clk.get("sm_mhz") or 2070.0))
+        out["roofline"] = roofline(dom, ks, N, E, M_total, W, maxHS, P, args.mode,
+                                   fp64_peak_tflops(torch), float(clk.get("sm_mhz") or 2070.0))
         if args.batch > 0:
             out["queries_per_s"] = measure_queries(args, lib, L, ctx)
         if not args.no_refine:
@@ -628,7 +678,7 @@ def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops, sm_mhz):
     if dom == "bvp_pairs":
         return {"kernel": dom, "bound": "fp64", "achieved": fp64, "peak": fp64_tflops,
                 "unit": "TFLOP/s", "frac": fp64 / fp64_tflops, "traffic": None,
-                "peak_source": "measured live (pump_probe_fp64_tflops: FP64 FMA pipe; the "
+                "peak_source": "measured live (bench.py's DFMA probe: FP64 FMA pipe; the "
                                "driver's peak file holds only HBM and bf16 figures)",
                 "flops_per_pair": BVP_FP64_FLOPS_PER_PAIR[mode], "all": table}
     t = ks[dom] / 1e3

@@ -229,20 +229,15 @@ pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d
 pump_status_t pump_frontier_compact(pump_ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                     int *d_count, pump_stream_t stream);
 
-/* ------------------------------------------------------------ diagnostics */
-/* Measured binary64 FMA throughput of the current device in TFLOP/s (2 flops
- * per FMA; eight independent chains per thread, all SMs).  The denominator
- * of the 2pBVP kernels' roofline; the reference has no counterpart. */
-pump_status_t pump_probe_fp64_tflops(double *h_tflops, pump_stream_t stream);
-
 /* The same compaction for callers that may not allocate device memory while
  * they run (a real-time loop that reserves all memory at start-up, or a host
  * framework that owns the memory budget and forbids cudaMalloc in plugins).
  * No counterpart in the reference.  Scratch is a fixed 64 KiB array in device
  * memory owned by the library (held by every GPU that loads it until the
  * process exits), so N is limited to 33,554,432 flags (PUMP_ERR_CAPACITY
- * beyond).  The first call on a device looks up the array's address; make it
- * before any stream capture.  All calls share the array: calls that overlap
+ * beyond).  The first call on a device (and the first after a device reset,
+ * or in another CUDA context) looks up the array's address; make it before
+ * any stream capture.  All calls share the array: calls that overlap
  * on the GPU race and must be serialised.  Synchronises the stream. */
 pump_status_t pump_frontier_compact_noalloc(const uint8_t *d_flags, int N, int *d_active,
                                             int *d_count, pump_stream_t stream);

@@ -2,7 +2,8 @@
 # Builds the reference PUMP program for the CPU, as the parity oracle.
 #
 # Test infrastructure only.  Reads the reference sources where they lie
-# (PUMP_REFERENCE_DIR, default /root/reference) and writes only into
+# (PUMP_REFERENCE_DIR, default: the directory "reference" beside the
+# repository) and writes only into
 # oracle/_ref/ (git-ignored).  For each sample count N in PUMPREF_NUMS the
 # reference's NUM is a compile-time constant (Makefile:1-5), so one pair of
 # artefacts is built per N:
@@ -28,7 +29,7 @@
 # oracle implement.  Nothing here is needed at run time on a GPU machine.
 set -euo pipefail
 HERE=$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)
-REF=${PUMP_REFERENCE_DIR:-/root/reference}
+REF=${PUMP_REFERENCE_DIR:-$(cd "$HERE/../.." && pwd)/reference}
 OUT="$HERE/_ref"
 NUMS=${PUMPREF_NUMS:-"64 1000"}
 CUDA_HOME=${CUDA_HOME:-/usr/local/cuda}

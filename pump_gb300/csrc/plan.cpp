@@ -1515,10 +1515,18 @@ pump_status_t take_worker(int device, pump_ctx **ctx, cudaStream_t *s) {
                      "cudaStreamCreateWithFlags");
 }
 
-void give_worker(int device, pump_ctx *ctx, cudaStream_t s) {
-  if (!ctx || !s) {
+// A worker goes back to the idle pool only when its stream is idle and its
+// last query did not end in a CUDA error or a timed-out device wait: such a
+// context or stream may hold queued work or a sticky error, so it is
+// destroyed and the next call creates a fresh one.
+void give_worker(int device, pump_ctx *ctx, cudaStream_t s, pump_status_t last) {
+  const bool healthy = ctx && s && last != PUMP_ERR_CUDA && last != PUMP_ERR_TIMEOUT &&
+                       cudaStreamQuery(s) == cudaSuccess;
+  if (!healthy) {
+    if (s) cudaStreamSynchronize(s);
     if (s) cudaStreamDestroy(s);
     if (ctx) pump_ctx_destroy(ctx);
+    cudaGetLastError();
     return;
   }
   std::lock_guard<std::mutex> lk(g_worker_mu);
@@ -1607,6 +1615,7 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
     pump_ctx *ctx = nullptr;
     cudaStream_t s = nullptr;
     pump_status_t st = take_worker(device, &ctx, &s);
+    pump_status_t last = st;
     if (st != PUMP_OK) {
       setup[w] = st;
       msgs[w] = pump_last_error();
@@ -1616,6 +1625,7 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
         for (const auto &x : groups)
           if (x.M > 0 && x.matches(problems[k])) g = &x;
         statuses[k] = plan_one(ctx, &problems[k], &results[k], true, (pump_stream_t)s, g);
+        last = statuses[k];
         if (statuses[k] != PUMP_OK && statuses[k] != PUMP_ERR_NO_SOLUTION) {
           std::lock_guard<std::mutex> lk(fail_mu);
           if (k < first_fail) {
@@ -1623,9 +1633,21 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
             fail_msg = pump_last_error();
           }
         }
+        if (last == PUMP_ERR_CUDA || last == PUMP_ERR_TIMEOUT) {
+          // the rest of this worker's queries run on a fresh context and stream
+          give_worker(device, ctx, s, last);
+          ctx = nullptr;
+          s = nullptr;
+          last = take_worker(device, &ctx, &s);
+          if (last != PUMP_OK) {
+            setup[w] = last;
+            msgs[w] = pump_last_error();
+            break;
+          }
+        }
       }
     }
-    give_worker(device, ctx, s);
+    give_worker(device, ctx, s, last);
   };
   std::vector<std::thread> pool;
   for (int w = 1; w < workers; ++w) pool.emplace_back(worker, w);

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "compact.cuh"
@@ -672,9 +673,11 @@ extern "C" pump_status_t pump_frontier_compact(pump_ctx *ctx, const uint8_t *d_f
 // The array is a file-scope __device__ variable: every GPU that loads the
 // library holds its 64 KiB until the process exits, and every call on that
 // GPU uses the same array.  Host code cannot use the variable's name as a
-// device address, so the address is looked up once per device with
-// cudaGetSymbolAddress (with that device current) on the first call made on
-// it; make that first call before any stream capture.  Each call clears the
+// device address, so the address is looked up with cudaGetSymbolAddress
+// (with the device current) on the first call made in each CUDA context on
+// it -- once per device for the usual primary context, again after a device
+// reset or in another context; make that first call before any stream
+// capture.  Each call clears the
 // words that must start at zero before its kernel runs; two calls that
 // overlap on the GPU (for example on two streams) share the array and race,
 // so serialise them.
@@ -683,27 +686,67 @@ namespace {
 
 constexpr long long kNoAllocMaxTiles = 8192;                   // 8192 tiles of 4096 flags
 constexpr long long kNoAllocMaxFlags = kNoAllocMaxTiles * kTile;  // 33,554,432
-// word 0: selected count; words 1 .. tiles: tile status; the word after the
-// last status slot: tile counter (4 B) and error word (4 B)
+// word 0: selected count; words 1 .. 8192: tile status; word 8193: unused;
+// word 8194: tile counter (4 B) and error word (4 B)
 constexpr int kNoAllocWords = 1 + (int)kNoAllocMaxTiles + 1 + 1;
 
 static __device__ __align__(256) unsigned long long g_frontier_scratch[kNoAllocWords];
 
+// The array's address belongs to the CUDA context that loaded the library's
+// module, so it is cached per context: keyed by the context's unique id
+// (cuCtxGetId), which a device reset or a different (non-primary) context on
+// the same device changes, so a stale address is never reused.  The driver
+// functions are reached through the runtime's entry-point query, so the
+// library needs no link against libcuda.
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+
 std::mutex g_scratch_mutex;
-unsigned long long *g_scratch_addr[64] = {nullptr};
+struct ScratchAddr {
+  unsigned long long ctx_id;
+  unsigned long long *addr;
+};
+std::vector<ScratchAddr> g_scratch_addr;
+
+// *id = the current context's id, or 0 when no context is current yet.
+pump_status_t current_context_id(unsigned long long *id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    PUMP_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1));
+    PUMP_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return set_error(PUMP_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId unavailable");
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  void *ctx = nullptr;
+  *id = 0;
+  if (get_current(&ctx) != 0) return set_error(PUMP_ERR_CUDA, "cuCtxGetCurrent failed");
+  if (ctx && get_id(ctx, id) != 0) return set_error(PUMP_ERR_CUDA, "cuCtxGetId failed");
+  return PUMP_OK;
+}
 
 pump_status_t frontier_scratch_address(unsigned long long **out) {
-  int dev = 0;
-  PUMP_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return set_error(PUMP_ERR_BAD_INPUT, "device %d out of range", dev);
+  unsigned long long id = 0;
+  PUMP_TRY(current_context_id(&id));
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_frontier_scratch);
-    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_frontier_scratch)");
-    g_scratch_addr[dev] = static_cast<unsigned long long *>(p);
-  }
-  *out = g_scratch_addr[dev];
+  for (const ScratchAddr &a : g_scratch_addr)
+    if (id != 0 && a.ctx_id == id) {
+      *out = a.addr;
+      return PUMP_OK;
+    }
+  // set-up for this context: the lookup also makes the device's primary
+  // context current when no context was
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_frontier_scratch);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_frontier_scratch)");
+  if (id == 0) PUMP_TRY(current_context_id(&id));
+  if (id == 0) return set_error(PUMP_ERR_CUDA, "no current CUDA context after the symbol lookup");
+  g_scratch_addr.push_back({id, static_cast<unsigned long long *>(p)});
+  *out = static_cast<unsigned long long *>(p);
   return PUMP_OK;
 }
 

@@ -107,7 +107,6 @@ _SIGS = {
     "pump_mc_cp": (i32, [vp, vp, vp, i32, vp, i32, i32, f32, vp, i32, vp, vp, vp, vp]),
     "pump_frontier_compact": (i32, [vp, vp, i32, vp, vp, vp]),
     "pump_frontier_compact_noalloc": (i32, [vp, i32, vp, vp, vp]),
-    "pump_probe_fp64_tflops": (i32, [C.POINTER(C.c_double), vp]),
     "pump_problem_defaults": (None, [C.POINTER(Problem)]),
     "pump_read_input": (i32, [C.c_char_p, C.POINTER(Problem)]),
     "pump_plan": (i32, [vp, C.POINTER(Problem), C.POINTER(PlanResult), vp]),

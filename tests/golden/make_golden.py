@@ -28,7 +28,9 @@ from pump_gb300 import workloads  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 REF = os.path.join(ROOT, "oracle", "_ref")
-REFERENCE_INPUT = os.environ.get("PUMP_REFERENCE_DIR", "/root/reference") + "/input.txt"
+REFERENCE_DIR = os.environ.get("PUMP_REFERENCE_DIR",
+                               os.path.join(os.path.dirname(ROOT), "reference"))
+REFERENCE_INPUT = os.path.join(REFERENCE_DIR, "input.txt")
 STRIDE = 97
 
 

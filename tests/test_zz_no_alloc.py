@@ -41,7 +41,27 @@ def test_noalloc_matches_allocating_entry_point_twice(gpu, pumplib):
         n1, n2 = int(host(d_n1)[0]), int(host(d_n2)[0])
         assert n1 == n2 == int(flags.sum())
         assert np.array_equal(host(d_a1, n1), host(d_a2, n2))
-        # and again on the same input
+        # and again on the same input, with the outputs cleared so that a call
+        # that wrote the count but not the indices cannot pass
         d_n2.fill_(-1)
+        d_a2.fill_(-1)
         pumplib.check(L.pump_frontier_compact_noalloc(ptr(d_f), N, ptr(d_a2), ptr(d_n2), stream(torch)))
         assert int(host(d_n2)[0]) == n1 and np.array_equal(host(d_a1, n1), host(d_a2, n1))
+
+
+@pytest.mark.gpu
+def test_noalloc_empty_and_all_set(gpu, pumplib):
+    """N = 0 writes a zero count (after a call that left a non-zero count in
+    the shared array); a frontier with every flag set lists 0 .. N-1."""
+    torch, ctx = gpu
+    L = pumplib.load()
+    N = 70_001
+    d_f = dev(torch, np.ones(N, np.uint8))
+    d_a, d_n = empty(torch, N, torch.int32), empty(torch, 1, torch.int32)
+    d_a.fill_(-1)
+    pumplib.check(L.pump_frontier_compact_noalloc(ptr(d_f), N, ptr(d_a), ptr(d_n), stream(torch)))
+    assert int(host(d_n)[0]) == N
+    assert np.array_equal(host(d_a, N), np.arange(N, dtype=np.int32))
+    d_n.fill_(-1)
+    pumplib.check(L.pump_frontier_compact_noalloc(ptr(d_f), 0, ptr(d_a), ptr(d_n), stream(torch)))
+    assert int(host(d_n)[0]) == 0
