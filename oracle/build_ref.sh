@@ -27,6 +27,12 @@
 # Both use refcpu/ipow.cpp (correctly rounded integer powers) and never
 # contract multiply-adds, which is the arithmetic the library and the C
 # oracle implement.  Nothing here is needed at run time on a GPU machine.
+#
+# An entry N:P of PUMPREF_NUMS builds the program with the reference's HSMC
+# particle count numHSMCParticles (a const int, mainPUMP.cu:68, 128 in the
+# tree) set to P: a copy of mainPUMP.cu with that one line changed is put in
+# a temporary directory searched before the reference tree.  The artefacts
+# are then named pump_ref_N<N>_P<P> / libpumpref_cpu_N<N>_P<P>.so.
 set -euo pipefail
 HERE=$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)
 REF=${PUMP_REFERENCE_DIR:-$(cd "$HERE/../.." && pwd)/reference}
@@ -52,7 +58,19 @@ g++ -O2 $FP -fPIC -c "$HERE/refcpu/ref_helpers.cpp" -o "$TMP/ref_helpers.o"
 sed 's/<<<[^>]*>>>//' "$REF/PUMP.cu" > "$TMP/PUMP.cu"
 sed 's/<<<[^>]*>>>//' "$REF/collisionProbability.cu" > "$TMP/collisionProbability.cu"
 
-for N in $NUMS; do
+for NP in $NUMS; do
+  N=${NP%%:*}
+  P=${NP#*:}
+  TAG=N$N
+  INC=()
+  if [ "$P" != "$NP" ] && [ "$P" != 128 ]; then
+    TAG=N${N}_P$P
+    mkdir -p "$TMP/$TAG"
+    sed "s/^const int numHSMCParticles = 128;/const int numHSMCParticles = $P;/" "$REF/mainPUMP.cu" \
+      > "$TMP/$TAG/mainPUMP.cu"
+    grep -q "^const int numHSMCParticles = $P;" "$TMP/$TAG/mainPUMP.cu"
+    INC=(-I"$TMP/$TAG")
+  fi
   DEFS="-DDIM=6 -DNUM=$N"
   # CPU kernel library (reference kernels as host C++)
   g++ -O2 $FP -fPIC -shared -fopenmp -w -Wl,-Bsymbolic \
@@ -60,13 +78,13 @@ for N in $NUMS; do
     -x c++ "$REF/2pBVP.cu" "$REF/collisionCheck.cu" "$REF/sampler.cu" "$REF/bvls.cu" \
     "$REF/hsmc.cu" "$TMP/PUMP.cu" "$TMP/collisionProbability.cu" \
     "$HERE/refcpu/launcher.cpp" -x none "$TMP/ipow.o" "$TMP/ref_helpers.o" \
-    -o "$OUT/libpumpref_cpu_N$N.so"
+    -o "$OUT/libpumpref_cpu_$TAG.so"
   # reference program: nvcc host pass over the unmodified sources
-  "$NVCC" -cuda -x cu "$HERE/refcpu/ref_all.cu" -I"$HERE/refcpu/stub_thrust" -I"$REF" $DEFS -O3 -w \
-    -gencode arch=compute_103a,code=sm_103a -o "$TMP/ref_all_N$N.cpp.ii"
-  g++ -O2 $FP -w -c -x c++ "$TMP/ref_all_N$N.cpp.ii" -o "$TMP/ref_all_N$N.o"
-  g++ -O2 $FP $DEFS -I"$CUDA_HOME/include" -c "$HERE/refcpu/fake_cudart.cpp" -o "$TMP/fake_cudart_N$N.o"
-  g++ -o "$OUT/pump_ref_N$N" "$TMP/ref_all_N$N.o" "$TMP/fake_cudart_N$N.o" "$TMP/ref_support.o" \
+  "$NVCC" -cuda -x cu "$HERE/refcpu/ref_all.cu" -I"$HERE/refcpu/stub_thrust" "${INC[@]}" -I"$REF" $DEFS \
+    -O3 -w -gencode arch=compute_103a,code=sm_103a -o "$TMP/ref_all_$TAG.cpp.ii"
+  g++ -O2 $FP -w -c -x c++ "$TMP/ref_all_$TAG.cpp.ii" -o "$TMP/ref_all_$TAG.o"
+  g++ -O2 $FP $DEFS -I"$CUDA_HOME/include" -c "$HERE/refcpu/fake_cudart.cpp" -o "$TMP/fake_cudart_$TAG.o"
+  g++ -o "$OUT/pump_ref_$TAG" "$TMP/ref_all_$TAG.o" "$TMP/fake_cudart_$TAG.o" "$TMP/ref_support.o" \
     "$TMP/ipow.o" "$TMP/ref_helpers.o" "$TMP/pump_oracle.o" -ldl -fopenmp
-  echo "built $OUT/pump_ref_N$N and $OUT/libpumpref_cpu_N$N.so"
+  echo "built $OUT/pump_ref_$TAG and $OUT/libpumpref_cpu_$TAG.so"
 done

@@ -372,3 +372,80 @@ class Refine:
         g = np.zeros_like(x)
         J = lib().orc_refine_grad(C.byref(self.args), x, x.size // 6, lam, g)
         return J, g.reshape(-1, 6)
+
+
+# ------------------------------------------------- binary64 restatements
+# Vectorised numpy forms of the precision mode's two changed quantities, used
+# to check every edge of a roadmap (the long-double orc_bvp_precise takes about
+# a millisecond per pair, so it checks samples only).
+G32 = float(np.float32(-9.81))  # the reference's `const float g = -9.81` (2pBVP.cu:3)
+
+
+def cost_coeffs64(x0, x1):
+    """Coefficients of the pair cost of 2pBVP.cu:97-107 written as
+    c(t) = A0/t^3 + A1/t^2 + A2/t + A3 + A4 t, in binary64, for arrays of
+    states x0, x1 (n, 6).  Expanding the reference's bracket gives
+    A0 = 12 |p0 - p1|^2, A1 = 12 (p0 - p1).(v0 + v1),
+    A2 = 4 (|v0|^2 + |v1|^2 + v0.v1), A3 = 2 g (v0z - v1z), A4 = 1 + g^2."""
+    x0 = np.asarray(x0, np.float64).reshape(-1, 6)
+    x1 = np.asarray(x1, np.float64).reshape(-1, 6)
+    dp = x0[:, :3] - x1[:, :3]
+    v0, v1 = x0[:, 3:], x1[:, 3:]
+    A0 = 12.0 * np.sum(dp * dp, 1)
+    A1 = 12.0 * np.sum(dp * (v0 + v1), 1)
+    A2 = 4.0 * (np.sum(v0 * v0, 1) + np.sum(v1 * v1, 1) + np.sum(v0 * v1, 1))
+    A3 = 2.0 * G32 * (x0[:, 5] - x1[:, 5])
+    A4 = np.full_like(A0, 1.0 + G32 * G32)
+    return A0, A1, A2, A3, A4
+
+
+def cost64(t, A):
+    A0, A1, A2, A3, A4 = A
+    return A0 / t**3 + A1 / t**2 + A2 / t + A3 + A4 * t
+
+
+def bvp_binary64(x0, x1, tmax=5.0):
+    """Global minimiser (topt, cost) of the pair cost on (0, tmax] in binary64
+    for arrays of pairs: the real roots of the stationarity quartic
+    Q(t) = A4 t^4 - A2 t^2 - 2 A1 t - 3 A0 (c'(t) = Q(t) / t^4) from the
+    eigenvalues of its companion matrix, two Newton steps on Q, and the least
+    cost among those in (0, tmax] and tmax itself."""
+    A = cost_coeffs64(x0, x1)
+    A0, A1, A2, A3, A4 = A
+    n = A0.size
+    comp = np.zeros((n, 4, 4))
+    # monic quartic t^4 + b t^2 + c t + d with b = -A2/A4, c = -2 A1/A4, d = -3 A0/A4
+    comp[:, 0, 1] = A2 / A4
+    comp[:, 0, 2] = 2.0 * A1 / A4
+    comp[:, 0, 3] = 3.0 * A0 / A4
+    comp[:, 1, 0] = comp[:, 2, 1] = comp[:, 3, 2] = 1.0
+    roots = np.linalg.eigvals(comp)
+    real = np.abs(roots.imag) <= 1e-7 * np.maximum(np.abs(roots.real), 1e-30)
+    r = np.where(real, roots.real, np.nan)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        for _ in range(2):
+            q = A4[:, None] * r**4 - A2[:, None] * r**2 - 2 * A1[:, None] * r - 3 * A0[:, None]
+            dq = 4 * A4[:, None] * r**3 - 2 * A2[:, None] * r - 2 * A1[:, None]
+            r = np.where(dq != 0, r - q / dq, r)
+    r = np.where((r > 0) & (r <= tmax), r, np.nan)
+    cand = np.concatenate([r, np.full((n, 1), float(tmax))], 1)
+    c = cost64(cand, tuple(a[:, None] for a in A))
+    c = np.where(np.isnan(c), np.inf, c)
+    k = np.argmin(c, 1)
+    rows = np.arange(n)
+    return cand[rows, k], c[rows, k]
+
+
+def path_point64(t, tau, x0, x1):
+    """pathPoint (2pBVP.cu:117-131) in binary64 for arrays: t, tau (n,),
+    x0, x1 (n, 6); returns (n, 6)."""
+    t = np.asarray(t, np.float64)[:, None]
+    u = np.asarray(tau, np.float64)[:, None]
+    a = np.asarray(x0, np.float64).reshape(-1, 6)
+    b = np.asarray(x1, np.float64).reshape(-1, 6)
+    p0, p1, v0, v1 = a[:, :3], b[:, :3], a[:, 3:], b[:, 3:]
+    pos = (t * v0 + p0 + t**3 * (2 * p0 - 2 * p1 + (v0 + v1) * u) / u**3
+           - t**2 * (3 * p0 - 3 * p1 + (2 * v0 + v1) * u) / u**2)
+    vel = (-(2 * t * (3 * p0 - 3 * p1 + v1 * u)) / u**2 + (3 * t**2 * (2 * p0 - 2 * p1 + v1 * u)) / u**3
+           + (v0 * (3 * t**2 - 4 * t * u + u**2)) / u**2)
+    return np.concatenate([pos, vel], 1)
