@@ -50,8 +50,20 @@ typedef enum pump_status_t {
 
 enum { PUMP_DIM = 6 };
 
-/* BVP arithmetic modes for pump_bvp_pairs. */
-enum { PUMP_BVP_PARITY = 0, PUMP_BVP_PRECISION = 1 };
+/* BVP arithmetic modes for pump_bvp_pairs.
+ *  PUMP_BVP_PARITY: the reference's algorithm in the arithmetic of its host
+ *    code (every operation rounded once, no contraction, pow(x, n) correctly
+ *    rounded), which is also what the reference built for a CPU computes.
+ *  PUMP_BVP_PRECISION: the binary64 minimiser of the same cost.
+ *  PUMP_BVP_PARITY_GPU: the pair times and costs in the arithmetic of the
+ *    reference's own GPU kernel (fillCoptsTopts, 2pBVP.cu:133-150, compiled by
+ *    nvcc with its default multiply-add contraction and CUDA's binary64 pow):
+ *    bit for bit what that kernel computes on the GB300.  For a planning
+ *    query it applies to the pair matrix (rn, the edges, their costs and the
+ *    times HSMC and the search use); the waypoints, the heuristic and the
+ *    solution search use the parity arithmetic, as the reference's host code
+ *    computes them. */
+enum { PUMP_BVP_PARITY = 0, PUMP_BVP_PRECISION = 1, PUMP_BVP_PARITY_GPU = 2 };
 
 const char *pump_status_string(pump_status_t s);
 /* Last error message of this thread (never NULL). */
@@ -112,7 +124,10 @@ pump_status_t pump_roadmap_edges(pump_ctx *ctx, const float *d_copts, const floa
  * is the edge's optimal time (identical to the one toptBisection recomputes
  * there).  mode PUMP_BVP_PARITY evaluates pathPoint's expressions as the
  * reference does (binary64 where they promote); PUMP_BVP_PRECISION
- * evaluates the same cubic in binary32 (FP64 is kept for the time root). */
+ * evaluates the same cubic in binary32 (FP64 is kept for the time root);
+ * PUMP_BVP_PARITY_GPU ignores d_topt (which holds the GPU kernel's times) and
+ * recomputes each edge's time with the host arithmetic, as
+ * findDiscretizedPath does, then evaluates as PUMP_BVP_PARITY. */
 pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src, const int *d_dst,
                                     const float *d_topt, long long E, int numDisc, int mode,
                                     float *d_disc, pump_stream_t stream);
@@ -229,6 +244,17 @@ pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d
 pump_status_t pump_frontier_compact(pump_ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                     int *d_count, pump_stream_t stream);
 
+/* Diagnostic of the bounded device waits (no counterpart in the reference).
+ * Every spin of the library's kernels on a word another block publishes (the
+ * decoupled look-back of the compactions, the edge lists and the search's
+ * store pass) gives up after a bound and records an error that the calling
+ * entry point returns as PUMP_ERR_TIMEOUT, leaving the context usable.  This
+ * runs that look-back wait, with at most spin_limit polls, on a status word
+ * that nothing publishes, and returns what the wait reported: PUMP_ERR_TIMEOUT
+ * when the bound ended it (the expected result), PUMP_OK if it did not.
+ * Synchronises the stream. */
+pump_status_t pump_selftest_wait(pump_ctx *ctx, long long spin_limit, pump_stream_t stream);
+
 /* The same compaction for callers that may not allocate device memory while
  * they run (a real-time loop that reserves all memory at start-up, or a host
  * framework that owns the memory budget and forbids cudaMalloc in plugins).
@@ -337,6 +363,10 @@ typedef struct pump_problem {
   int refine_iters;   /* > 0: refine the returned path (pump_refine_paths), accepted
                          only if its MC CP stays <= cp_target; 0 (default) = the reference */
   float refine_lambda; /* bound weight of the refinement (default 10) */
+  int max_paths;      /* stored-path capacity; 0 (default) = the reference's
+                         maxPathCount = (int)(2 N sqrt(N)) (mainPUMP.cu:623).  The
+                         reference overruns its arrays past it (PUMP.cu:62-76);
+                         here the query ends with PUMP_ERR_CAPACITY */
 } pump_problem;
 
 typedef struct pump_plan_result {

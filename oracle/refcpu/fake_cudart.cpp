@@ -9,7 +9,11 @@
  *    kernel library (launcher.cpp), which runs the reference's own kernel
  *    bodies compiled as host C++;
  *  - with PUMPREF_DUMP=<dir>, the outputs of each launch are appended to
- *    binary files in <dir> (the golden-vector dump).
+ *    binary files in <dir> (the golden-vector dump);
+ *  - with PUMPREF_BVP_FROM=<dir>, the fillCoptsTopts launch reads its outputs
+ *    from <dir>/copts.f32 and <dir>/topts.f32 instead of computing them: the
+ *    pair times and costs of the reference's own kernel run on a GPU, so the
+ *    rest of the program runs on what the reference's GPU computed there.
  *
  * Particle table extension: the reference reads the time-major particle
  * table at row time/dt without a bound (PUMP.cu:637-647), i.e. past its
@@ -146,16 +150,34 @@ cudaError_t __cudaGetKernel(cudaKernel_t *k, const void *hostFun) {
   *k = (cudaKernel_t)hostFun;
   return cudaSuccess;
 }
+// Reads n floats from dir/name into p; exits on a missing or short file.
+void read_floats(const char *dir, const char *name, float *p, size_t n) {
+  const std::string path = std::string(dir) + "/" + name;
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f || std::fread(p, sizeof(float), n, f) != n) {
+    std::fprintf(stderr, "PUMPREF_BVP_FROM: cannot read %zu floats from %s\n", n, path.c_str());
+    std::exit(3);
+  }
+  std::fclose(f);
+}
+
 cudaError_t __cudaLaunchKernel(cudaKernel_t k, dim3 g, dim3 b, void **args, size_t, cudaStream_t) {
   auto it = names().find((const void *)k);
   if (it == names().end()) return cudaErrorInvalidDeviceFunction;
-  if (launcher()(it->second.c_str(), g.x, g.y, g.z, b.x, b.y, b.z, args)) return cudaErrorLaunchFailure;
   // identifier of the Itanium-mangled name "_Z<len><identifier>..."
   std::string nm = it->second;
   if (nm.rfind("_Z", 0) == 0) {
     size_t i = 2, len = 0;
     while (i < nm.size() && nm[i] >= '0' && nm[i] <= '9') len = len * 10 + (nm[i++] - '0');
     nm = nm.substr(i, len);
+  }
+  const char *bvp_from = std::getenv("PUMPREF_BVP_FROM");
+  if (bvp_from && nm == "fillCoptsTopts") {
+    const size_t n = (size_t)NUM * (NUM - 1);
+    read_floats(bvp_from, "copts.f32", arg<float *>(args, 1), n);
+    read_floats(bvp_from, "topts.f32", arg<float *>(args, 2), n);
+  } else if (launcher()(it->second.c_str(), g.x, g.y, g.z, b.x, b.y, b.z, args)) {
+    return cudaErrorLaunchFailure;
   }
   dump_after(nm, args);
   return cudaSuccess;

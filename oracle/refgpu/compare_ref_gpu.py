@@ -27,9 +27,12 @@ code bit for bit, as inputs to both sides):
   mccp         MCCP over dense polyline paths (at the problem's noise
                multiplier and at 0.3, where particles do hit boxes)
 
-Writes OUTDIR/compare.json (counts and times) and OUTDIR/refgpu_bvp_N<N>.npz
+Writes OUTDIR/compare.json (counts and times), OUTDIR/refgpu_bvp_N<N>.npz
 (the reference GPU's pair times and costs: SHA-256 of the whole arrays, a
-strided subset, rn and the edge count).
+strided subset, rn and the edge count; committed as tests/golden/) and
+OUTDIR/refgpu_bvp_diff_N<N>.npz (the pairs where the reference GPU differs
+from the parity arithmetic, from which tests/golden/make_golden.py rebuilds
+the whole arrays).
 """
 from __future__ import annotations
 
@@ -193,10 +196,15 @@ def compare(cfg_name, out_dir, torch, lib, L, ctx, ref):
                            rt[np.intersect1d(e_ref, e_our)].view(np.uint32)
                            != ot[np.intersect1d(e_ref, e_our)].view(np.uint32)))}
     i_idx = (np.arange(0, npairs, STRIDE, dtype=np.int64))
+    # the pairs where the reference GPU differs from the parity arithmetic (which
+    # the CPU build of the reference reproduces): with them the reference GPU's
+    # whole arrays can be rebuilt on a machine without a GPU
+    diff = np.flatnonzero(mc | mt).astype(np.int64)
+    np.savez_compressed(os.path.join(out_dir, "refgpu_bvp_diff_N%d.npz" % N), idx=diff,
+                        copts=rc[diff], topts=rt[diff], copts_sha=sha(rc), topts_sha=sha(rt))
     np.savez_compressed(os.path.join(out_dir, "refgpu_bvp_N%d.npz" % N),
                         copts_sha=sha(rc), topts_sha=sha(rt), stride=STRIDE,
                         copts_strided=rc[i_idx], topts_strided=rt[i_idx],
-                        mismatch_idx=np.flatnonzero(mc | mt).astype(np.int64)[:200000],
                         rn=np.float32(rn_ref), num_edges=np.int64(e_ref.size), k=np.int64(k))
 
     # ---- common downstream inputs: the parity roadmap and waypoints

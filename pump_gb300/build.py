@@ -24,8 +24,12 @@ LIB = os.path.join(OUT, "libpump.so")
 CLI = os.path.join(OUT, "pump")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# translation units not bound to the reference's roundings: contraction on
-FMAD_TRUE = {os.path.join(CSRC, "bvp_precise.cu"), os.path.join(CSRC, "refine.cu")}
+# translation units compiled with multiply-add contraction: the precision
+# mode and the refinement (not bound to the reference's roundings), and the
+# pair BVP in the reference GPU kernel's own arithmetic (contracted as nvcc
+# contracts the reference)
+FMAD_TRUE = {os.path.join(CSRC, "bvp_precise.cu"), os.path.join(CSRC, "refine.cu"),
+             os.path.join(CSRC, "bvp_refgpu.cu")}
 HOST_FLAGS = "-fPIC,-ffp-contract=off,-fno-fast-math,-Wall,-Wno-unused-function"
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", HOST_FLAGS,
           "-I", INCLUDE, "-I", CSRC]

@@ -301,6 +301,7 @@ extern "C" void pump_problem_defaults(pump_problem *pb) {
   pb->refine_iters = 0;
   pb->refine_lambda = 10.0f;
   pb->samples = nullptr;
+  pb->max_paths = 0;
 }
 
 namespace {

@@ -274,10 +274,13 @@ __global__ void __launch_bounds__(T) discretize_kernel(
       o[d] = x0[d];
       o[numDisc * kDim + d] = x1[d];
     }
-    const float dt = topt / numDisc;
+    // the GPU-arithmetic mode's d_topt holds the reference GPU kernel's times;
+    // findDiscretizedPath recomputes the time with the host arithmetic
+    const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_bisection(make_coef(x0, x1), 5.0f) : topt;
+    const float dt = tau / numDisc;
     for (int i = 1; i < numDisc; ++i) {
-      if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
-      else path_point_f32(dt * i, topt, x0, x1, x);
+      if (Mode != PUMP_BVP_PRECISION) path_point(dt * i, tau, x0, x1, x);
+      else path_point_f32(dt * i, tau, x0, x1, x);
 #pragma unroll
       for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
     }
@@ -393,6 +396,7 @@ pump_status_t candidate_paths_async(const CandidateBufs &cb, int n_paths, int n_
                                     int mode, float dt, bool with_cost, int rows_cap,
                                     cudaStream_t s) {
   if (n_paths <= 0) return PUMP_OK;
+  mode = host_bvp_mode(mode);  // findOptimalPath and the smoothing run on the reference's host
   if (n_seg > 0) {
     // optimal times (tmax 5) and smoothing costs and times (tmax 2) in one
     // launch
@@ -459,10 +463,35 @@ pump_status_t own_pairs_async(const float *d_samples, int N, float *d_x0, float 
 pump_status_t bvp_jobs_launch(const BvpJobs &jb, int mode, cudaStream_t stream) {
   if (jb.n <= 0) return PUMP_OK;
   if (mode == PUMP_BVP_PRECISION) return bvp_jobs_precision_launch(jb, stream);
+  if (mode == PUMP_BVP_PARITY_GPU) return bvp_jobs_refgpu_launch(jb, stream);
   const long long total = (long long)jb.n * jb.jobs;
   const int threads = total < 152LL * 128 ? 32 : 128;
   bvp_batch_kernel<<<grid_for(total, threads), threads, 0, stream>>>(jb);
   return launch_status("bvp_batch");
+}
+
+namespace {
+__global__ void edge_topts_parity_kernel(const float *__restrict__ samples, const int *__restrict__ src,
+                                         const int *__restrict__ dst, long long E,
+                                         float *__restrict__ topt) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  float x0[kDim], x1[kDim];
+  const int a = src[e], b = dst[e];
+#pragma unroll
+  for (int d = 0; d < kDim; ++d) {
+    x0[d] = __ldg(&samples[a * kDim + d]);
+    x1[d] = __ldg(&samples[b * kDim + d]);
+  }
+  topt[e] = topt_bisection(make_coef(x0, x1), 5.0f);
+}
+}  // namespace
+
+pump_status_t edge_topts_parity_async(const float *d_samples, const int *d_src, const int *d_dst,
+                                      long long E, float *d_topt, cudaStream_t stream) {
+  if (E <= 0) return PUMP_OK;
+  edge_topts_parity_kernel<<<grid_for(E, 128), 128, 0, stream>>>(d_samples, d_src, d_dst, E, d_topt);
+  return launch_status("edge_topts_parity");
 }
 
 pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
@@ -492,6 +521,8 @@ extern "C" pump_status_t pump_bvp_pairs(const float *d_samples, int N, float tma
         d_samples, N, tmax, d_copts, d_topts);
   } else if (mode == PUMP_BVP_PRECISION) {
     PUMP_TRY(bvp_pairs_precision_launch(d_samples, N, tmax, d_copts, d_topts, (cudaStream_t)stream));
+  } else if (mode == PUMP_BVP_PARITY_GPU) {
+    PUMP_TRY(bvp_pairs_refgpu_launch(d_samples, N, tmax, d_copts, d_topts, (cudaStream_t)stream));
   } else
     return set_error(PUMP_ERR_BAD_INPUT, "pump_bvp_pairs: unknown mode %d", mode);
   return launch_status("bvp_pairs");
@@ -501,7 +532,7 @@ extern "C" pump_status_t pump_bvp_batch(const float *d_x0, const float *d_x1, in
                                         int mode, float *d_topt, float *d_cost,
                                         pump_stream_t stream) {
   if (n < 0 || (n > 0 && (!d_x0 || !d_x1)) || !(tmax > 0) ||
-      (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION))
+      (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION && mode != PUMP_BVP_PARITY_GPU))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_bvp_batch: bad arguments");
   if (n == 0) return PUMP_OK;
   BvpJobs jb{};
@@ -519,7 +550,8 @@ extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int
                                                const int *d_dst, const float *d_topt, long long E,
                                                int numDisc, int mode, float *d_disc,
                                                pump_stream_t stream) {
-  if (E < 0 || numDisc < 1 || (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION) ||
+  if (E < 0 || numDisc < 1 ||
+      (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION && mode != PUMP_BVP_PARITY_GPU) ||
       (E > 0 && (!d_samples || !d_src || !d_dst || !d_topt || !d_disc)))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_discretize_edges: bad arguments");
   if (E == 0) return PUMP_OK;
@@ -530,11 +562,14 @@ extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int
   // block sizes 64, 128 (default), 256
   auto go = [&](auto block) -> pump_status_t {
     constexpr int T = decltype(block)::value;
-    return mode == PUMP_BVP_PARITY
-               ? discretize_launch<PUMP_BVP_PARITY, T>(d_samples, d_src, d_dst, d_topt, E, numDisc,
-                                                      d_disc, s)
-               : discretize_launch<PUMP_BVP_PRECISION, T>(d_samples, d_src, d_dst, d_topt, E,
-                                                         numDisc, d_disc, s);
+    if (mode == PUMP_BVP_PARITY)
+      return discretize_launch<PUMP_BVP_PARITY, T>(d_samples, d_src, d_dst, d_topt, E, numDisc,
+                                                   d_disc, s);
+    if (mode == PUMP_BVP_PARITY_GPU)
+      return discretize_launch<PUMP_BVP_PARITY_GPU, T>(d_samples, d_src, d_dst, d_topt, E, numDisc,
+                                                       d_disc, s);
+    return discretize_launch<PUMP_BVP_PRECISION, T>(d_samples, d_src, d_dst, d_topt, E, numDisc,
+                                                    d_disc, s);
   };
   auto run = [&](int c) -> pump_status_t {
     if (c == 0) return go(std::integral_constant<int, 64>{});

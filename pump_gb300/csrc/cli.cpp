@@ -5,7 +5,9 @@
 // read from the environment variable PUMP_NUM (default 1000).  Optional
 // flags after the three positional arguments: --num N, --disc D (edge
 // discretisation), --particles P (HSMC particles), --precision (closed-form
-// binary64 BVP instead of the reference's bisection), --seed S.
+// binary64 BVP instead of the reference's bisection), --gpu-arith (the pair
+// BVPs in the arithmetic of the reference's own GPU kernel, PUMP_BVP_PARITY_GPU;
+// by default the parity arithmetic of the reference's host code), --seed S.
 // Writes path.txt like PUMP.cu:591-594 when a solution is found and
 // discretizedPath.txt like PUMP.cu:571-579 whenever the search ran, and
 // prints the reference's final summary lines (PUMP.cu:582-604).
@@ -34,6 +36,7 @@ int main(int argc, char **argv) {
     else if (!std::strcmp(argv[a], "--particles") && a + 1 < argc) pb.num_hsmc = std::atoi(argv[++a]);
     else if (!std::strcmp(argv[a], "--seed") && a + 1 < argc) pb.seed = std::strtoull(argv[++a], nullptr, 0);
     else if (!std::strcmp(argv[a], "--precision")) pb.bvp_mode = PUMP_BVP_PRECISION;
+    else if (!std::strcmp(argv[a], "--gpu-arith")) pb.bvp_mode = PUMP_BVP_PARITY_GPU;
   }
   pb.cp_target = (float)std::atof(argv[2]);
   pb.cp_factor = (float)std::atof(argv[3]);

@@ -47,7 +47,8 @@ struct TileScratch {
 // same value.
 constexpr int kLookbackPerLane = 4;
 __device__ unsigned long long lookback_warp(const TileScratch &ts, long long tile,
-                                            unsigned long long agg, bool *timed_out) {
+                                            unsigned long long agg, bool *timed_out,
+                                            long long spin_limit = kSpinLimit) {
   using ref_t = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
   constexpr int V = kLookbackPerLane;
   const int lane = threadIdx.x & 31;
@@ -86,7 +87,7 @@ __device__ unsigned long long lookback_warp(const TileScratch &ts, long long til
       }
     }
     if (__any_sync(0xffffffffu, missing)) {
-      if (++spins > kSpinLimit) {
+      if (++spins > spin_limit) {
         *timed_out = true;
         return 0;
       }

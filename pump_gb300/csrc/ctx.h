@@ -158,6 +158,18 @@ struct BvpJobs {
 };
 pump_status_t bvp_jobs_launch(const BvpJobs &jb, int mode, cudaStream_t stream);
 pump_status_t bvp_jobs_precision_launch(const BvpJobs &jb, cudaStream_t stream);
+// the reference GPU kernel's arithmetic (bvp_refgpu.cu)
+pump_status_t bvp_pairs_refgpu_launch(const float *d_samples, int N, float tmax, float *d_copts,
+                                      float *d_topts, cudaStream_t stream);
+pump_status_t bvp_jobs_refgpu_launch(const BvpJobs &jb, cudaStream_t stream);
+// Optimal time of every edge (src[e], dst[e]) in the parity arithmetic
+// (toptBisection as the reference's host code runs it, tmax 5): the time the
+// reference's findDiscretizedPath recomputes for the waypoints.
+pump_status_t edge_topts_parity_async(const float *d_samples, const int *d_src, const int *d_dst,
+                                      long long E, float *d_topt, cudaStream_t stream);
+// The BVP arithmetic of the reference's host code for a planner mode: the
+// parity arithmetic for both parity modes, the precision mode otherwise.
+inline int host_bvp_mode(int mode) { return mode == PUMP_BVP_PRECISION ? PUMP_BVP_PRECISION : PUMP_BVP_PARITY; }
 // Device buffers of a batch of candidate paths: per path its node count and
 // first segment; its segments (node i -> i + 1) as explicit pairs x0, x1,
 // paths in order; their optimal times (tmax 5) and smoothing costs (tmax 2),

@@ -313,6 +313,13 @@ class Planner {
   DevBuf<float> d_samples_, d_obs_, d_copts_, d_topts_;
   DevBuf<int> d_src_, d_dst_, d_go_;
   DevBuf<float> d_coptE_, d_toptE_, d_disc_;
+  // PUMP_BVP_PARITY_GPU: each edge's optimal time in the host arithmetic, the
+  // time the reference's findDiscretizedPath evaluates the waypoints at
+  // (d_toptE_ holds the GPU kernel's times, which the search and HSMC use)
+  DevBuf<float> d_toptH_;
+  const float *waypoint_topts() const {
+    return pb_.bvp_mode == PUMP_BVP_PARITY_GPU ? d_toptH_.p : d_toptE_.p;
+  }
   const float *d_table_ = nullptr;   // context-cached particle table
   const float *d_rowmax_ = nullptr;  // its largest |offset| per row and axis
   const float *obs_p_ = nullptr;    // device obstacles used by the MC CP
@@ -417,7 +424,7 @@ pump_status_t Planner::roadmap() {
     jb.jobs = 1;
     jb.tmax[0] = 5.0f;
     jb.cost[0] = d_h_.p;
-    PUMP_TRY(bvp_jobs_launch(jb, pb_.bvp_mode, s_));
+    PUMP_TRY(bvp_jobs_launch(jb, host_bvp_mode(pb_.bvp_mode), s_));
   }
   PUMP_CUDA_TRY(cudaMemcpyAsync(hout, d_h_.p, sizeof(float), cudaMemcpyDeviceToHost, s_));
   const long long npairs = (long long)N_ * (N_ - 1);
@@ -458,6 +465,10 @@ pump_status_t Planner::roadmap() {
     E_ = (long long)*htotal;
   }
   res_->num_edges = E_;
+  if (pb_.bvp_mode == PUMP_BVP_PARITY_GPU) {
+    PUMP_TRY(d_toptH_.alloc(E_ > 0 ? E_ : 1));
+    PUMP_TRY(edge_topts_parity_async(d_samples_.p, d_src_.p, d_dst_.p, E_, d_toptH_.p, s_));
+  }
   h0_ = hout[0];
   std::memcpy(&max_degree_, hout + 1, sizeof(int));
   if (!pb_.samples) samples_.assign(hout + 2, hout + 2 + nsf);
@@ -512,8 +523,9 @@ pump_status_t Planner::online() {
   PUMP_TRY(d_todo_.alloc(N_));
   PUMP_CUDA_TRY(cudaMemsetAsync(d_open_cnt_.p, 0xFF, sizeof(int) * (size_t)N_, s_));  // -1
   if (!lazy_) {
-    PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, d_toptE_.p, E_, pb_.num_disc,
-                                   pb_.bvp_mode, d_disc_.p, (pump_stream_t)s_));
+    PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, waypoint_topts(), E_,
+                                   pb_.num_disc, host_bvp_mode(pb_.bvp_mode), d_disc_.p,
+                                   (pump_stream_t)s_));
     PUMP_TRY(pump_free_edges(d_obs_.p, nobs_, d_disc_.p, E_, pb_.num_disc, d_free_e_.p,
                              (pump_stream_t)s_));
     SearchDev sd{};
@@ -543,7 +555,8 @@ pump_status_t Planner::online() {
 // wavefront size, launches expansion, HSMC, pruning and storing, and reads
 // the iteration's counters back.
 pump_status_t Planner::explore() {
-  maxPathCount_ = (int)(2 * N_ * std::sqrt((double)N_));  // mainPUMP.cu:623
+  maxPathCount_ = pb_.max_paths > 0 ? pb_.max_paths
+                                    : (int)(2 * N_ * std::sqrt((double)N_));  // mainPUMP.cu:623
   const int M = maxPathCount_;
   const size_t cap = (size_t)M + 1;
   PUMP_TRY(d_valid_.alloc((size_t)M * words_));
@@ -630,7 +643,8 @@ pump_status_t Planner::explore() {
   ca.samples = d_samples_.p;
   ca.disc = d_disc_.p;
   ca.numDisc = pb_.num_disc;
-  ca.mode = pb_.bvp_mode;
+  ca.mode = host_bvp_mode(pb_.bvp_mode);
+  ca.wp_topt = waypoint_topts();
   ca.obs = d_obs_.p;
   ca.numObs = nobs_;
   ca.max_degree = max_degree_;
@@ -859,7 +873,7 @@ pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
   // shared memory sized for the box count rounded up to 32 (exact for large
   // maps, which sit close to the shared-memory limit)
   const int obs_cap = nobs_ > 1024 ? nobs_ : (nobs_ <= 32 ? 32 : ((nobs_ + 31) / 32) * 32);
-  const int lazy = lazy_ ? 1 : 0, mode = pb_.bvp_mode, num_disc = pb_.num_disc;
+  const int lazy = lazy_ ? 1 : 0, mode = host_bvp_mode(pb_.bvp_mode), num_disc = pb_.num_disc;
   std::vector<Ctx::LoopGraph> &gs = ctx_->loop_graphs;
   for (size_t i = 0; i < gs.size();) {  // graphs of an outgrown argument block
     if (gs[i].base != base) {
@@ -935,7 +949,7 @@ pump_status_t Planner::topts_of(const std::vector<float> &x0, const std::vector<
   PUMP_TRY(d_bc_.alloc(n));
   PUMP_TRY(h2d(d_bx0_.p, x0.data(), x0.size()));
   PUMP_TRY(h2d(d_bx1_.p, x1.data(), x1.size()));
-  PUMP_TRY(pump_bvp_batch(d_bx0_.p, d_bx1_.p, n, tmax, pb_.bvp_mode, d_bt_.p, d_bc_.p,
+  PUMP_TRY(pump_bvp_batch(d_bx0_.p, d_bx1_.p, n, tmax, host_bvp_mode(pb_.bvp_mode), d_bt_.p, d_bc_.p,
                           (pump_stream_t)s_));
   if (topt) PUMP_TRY(d2h(topt->data(), d_bt_.p, n));
   if (cost) PUMP_TRY(d2h(cost->data(), d_bc_.p, n));
@@ -1460,7 +1474,9 @@ pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *
   if (!ctx || !pb || !res) return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: null argument");
   if (pb->N < 2 || pb->num_disc < 1 || pb->num_hsmc < 1 || pb->num_mc < pb->num_hsmc ||
       pb->table_rows < 2 || pb->num_obstacles < 0 || (pb->num_obstacles > 0 && !pb->obstacles) ||
-      !(pb->cp_factor > 0))
+      !(pb->cp_factor > 0) || pb->max_paths < 0 ||
+      (pb->bvp_mode != PUMP_BVP_PARITY && pb->bvp_mode != PUMP_BVP_PRECISION &&
+       pb->bvp_mode != PUMP_BVP_PARITY_GPU))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: problem out of domain");
   float *path = res->path;
   int path_cap = res->path_cap;
@@ -1669,7 +1685,7 @@ extern "C" pump_status_t pump_path_cp(pump_ctx *ctx, const float *h_nodes, const
   if (!ctx || n_paths < 0 || (n_paths > 0 && (!h_nodes || !h_offset || !h_count || !d_table_t ||
                                               !h_cp || !h_cost || !h_len)) ||
       Pmc <= 0 || T_rows < 2 || num_obstacles < 0 || (num_obstacles > 0 && !d_obstacles) ||
-      (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION))
+      (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION && mode != PUMP_BVP_PARITY_GPU))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_path_cp: bad arguments");
   if (n_paths == 0) return PUMP_OK;
   std::vector<std::vector<float>> xs(n_paths);

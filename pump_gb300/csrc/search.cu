@@ -122,7 +122,7 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
 #pragma unroll
         for (int d = 0; d < kDim; ++d) x[d] = x1[d];
       } else {
-        const float topt = sd.topt[e];
+        const float topt = ca.wp_topt[e];
         const float dt = topt / numDisc;
         if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
         else path_point_f32(dt * i, topt, x0, x1, x);

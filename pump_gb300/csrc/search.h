@@ -66,7 +66,8 @@ struct SearchDev {
 struct CheckArgs {
   const float *samples;
   float *disc;
-  int numDisc, mode;
+  int numDisc, mode;       // mode: PUMP_BVP_PARITY or PUMP_BVP_PRECISION waypoints
+  const float *wp_topt;    // per edge, the optimal time its waypoints are evaluated at
   const float *obs;
   int numObs;
   int max_degree;  // largest out-degree of the roadmap

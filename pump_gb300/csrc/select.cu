@@ -659,6 +659,41 @@ extern "C" pump_status_t pump_frontier_compact(pump_ctx *ctx, const uint8_t *d_f
 }
 
 // ---------------------------------------------------------------------------
+// Bounded-wait self-test: tile 1 of a look-back whose tile 0 never publishes
+// (its status word is zeroed and nothing writes it), so the wait can end only
+// through its bound.  One warp; words[0..1] are the two status words,
+// words[2] receives 1 when the wait gave up.
+namespace pump {
+namespace {
+__global__ void selftest_wait_kernel(unsigned long long *words, long long spin_limit) {
+  TileScratch ts{};
+  ts.status = words;
+  bool timed_out = false;
+  lookback_warp(ts, 1, 1, &timed_out, spin_limit);
+  if ((threadIdx.x & 31) == 0) words[2] = timed_out ? 1ull : 0ull;
+}
+}  // namespace
+}  // namespace pump
+
+extern "C" pump_status_t pump_selftest_wait(pump_ctx *ctx, long long spin_limit, pump_stream_t stream) {
+  if (!ctx || spin_limit < 0 || spin_limit > kSpinLimit)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_selftest_wait: bad arguments");
+  Ctx *c = Ctx::from(ctx);
+  PUMP_TRY(c->activate());
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long *words = nullptr;
+  PUMP_TRY(c->scratch(Ctx::kCompact, 3 * sizeof(unsigned long long), (void **)&words));
+  PUMP_CUDA_TRY(cudaMemsetAsync(words, 0, 3 * sizeof(unsigned long long), s));
+  selftest_wait_kernel<<<1, 32, 0, s>>>(words, spin_limit);
+  PUMP_TRY(launch_status("selftest_wait_kernel"));
+  unsigned long long gave_up = 0;
+  PUMP_CUDA_TRY(cudaMemcpyAsync(&gave_up, words + 2, sizeof gave_up, cudaMemcpyDeviceToHost, s));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(s));
+  if (gave_up) return set_error(PUMP_ERR_TIMEOUT, "pump_selftest_wait: the wait gave up after %lld polls", spin_limit);
+  return PUMP_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Frontier compaction without any allocation.
 //
 // For callers that must not allocate device memory while they plan: a

@@ -27,6 +27,7 @@ PUMP_ERR_NO_SOLUTION = 5
 PUMP_ERR_NO_MEMORY = 6
 PUMP_BVP_PARITY = 0
 PUMP_BVP_PRECISION = 1
+PUMP_BVP_PARITY_GPU = 2
 
 _lock = threading.Lock()
 _lib = None
@@ -50,6 +51,7 @@ class Problem(C.Structure):
         ("init", f32 * 6), ("goal", f32 * 6), ("lo", f32 * 6), ("hi", f32 * 6),
         ("offset_mult", f32), ("cp_target", f32), ("cp_factor", f32), ("seed", C.c_uint64),
         ("bvp_mode", i32), ("samples", vp), ("refine_iters", i32), ("refine_lambda", f32),
+        ("max_paths", i32),
     ]
 
 
@@ -107,6 +109,7 @@ _SIGS = {
     "pump_mc_cp": (i32, [vp, vp, vp, i32, vp, i32, i32, f32, vp, i32, vp, vp, vp, vp]),
     "pump_frontier_compact": (i32, [vp, vp, i32, vp, vp, vp]),
     "pump_frontier_compact_noalloc": (i32, [vp, i32, vp, vp, vp]),
+    "pump_selftest_wait": (i32, [vp, i64, vp]),
     "pump_problem_defaults": (None, [C.POINTER(Problem)]),
     "pump_read_input": (i32, [C.c_char_p, C.POINTER(Problem)]),
     "pump_plan": (i32, [vp, C.POINTER(Problem), C.POINTER(PlanResult), vp]),

@@ -9,6 +9,11 @@ a strided subset plus a SHA-256 of the whole array.
 
 Run from the repository root (needs the reference sources and gcc/nvcc):
     bash oracle/build_ref.sh && python tests/golden/make_golden.py
+and for the N = 4000 benchmark problem (1024 HSMC particles):
+    PUMPREF_NUMS=4000:1024 bash oracle/build_ref.sh && python tests/golden/make_golden.py indoor4000
+and the same problems with the pair BVPs of the reference's own GPU kernel
+(the diff files written by oracle/refgpu/compare_ref_gpu.py on the GPU):
+    python tests/golden/make_golden.py refgpu DIFF_DIR
 """
 from __future__ import annotations
 
@@ -38,11 +43,14 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def run_ref(N, input_path, cp, eta, dump):
+def run_ref(N, input_path, cp, eta, dump, P=128, bvp_from=None):
+    tag = "N%d" % N if P == 128 else "N%d_P%d" % (N, P)
     env = dict(os.environ)
-    env["PUMPREF_KERNEL_LIB"] = os.path.join(REF, "libpumpref_cpu_N%d.so" % N)
+    if bvp_from:
+        env["PUMPREF_BVP_FROM"] = bvp_from
+    env["PUMPREF_KERNEL_LIB"] = os.path.join(REF, "libpumpref_cpu_%s.so" % tag)
     env["PUMPREF_DUMP"] = dump
-    exe = os.path.join(REF, "pump_ref_N%d" % N)
+    exe = os.path.join(REF, "pump_ref_%s" % tag)
     r = subprocess.run([exe, input_path, str(cp), str(eta)], cwd=dump, env=env,
                        capture_output=True, text=True, timeout=1800)
     if r.returncode != 0:
@@ -80,12 +88,17 @@ def read_problem(path):
     return dict(init=init, goal=goal, lo=lo, hi=hi, offset_mult=om, obstacles=obs)
 
 
-def case(name, N, input_path, cp, eta, full, roadmap=True):
+def case(name, N, input_path, cp, eta, full, roadmap=True, P=128, stride=STRIDE, bvp_from=None):
+    """One fixture.  P: the reference build's HSMC particle count
+    (oracle/build_ref.sh entry N:P); stride: of the strided subsets;
+    bvp_from: a directory with the pair arrays of the reference's GPU kernel
+    (copts.f32, topts.f32) that the run uses instead of computing them."""
     with tempfile.TemporaryDirectory() as d:
-        out = run_ref(N, input_path, cp, eta, d)
+        out = run_ref(N, input_path, cp, eta, d, P, bvp_from)
         f = lambda n, t: np.fromfile(os.path.join(d, n), t)  # noqa: E731
         g = {"prob_" + k: np.asarray(v) for k, v in read_problem(input_path).items()}
         g["N"], g["cp_target"], g["cp_factor"] = np.array(N), np.float32(cp), np.float32(eta)
+        g["hsmc_particles"], g["stride"] = np.array(P), np.array(stride)
         samples = f("samples.f32", np.float32).reshape(N, 6)
         copts, topts = f("copts.f32", np.float32), f("topts.f32", np.float32)
         disc = f("discMotions.f32", np.float32)
@@ -95,7 +108,7 @@ def case(name, N, input_path, cp, eta, full, roadmap=True):
         for key, arr in (("copts", copts), ("topts", topts), ("disc", disc), ("as", a), ("bs", b)):
             g[key + "_sha"] = np.array(sha(arr))
             if roadmap or key in ("as", "bs"):
-                g[key + "_sub"] = arr if full else arr[::STRIDE].copy()
+                g[key + "_sub"] = arr if full else arr[::stride].copy()
         g["free_edges_bits"] = np.packbits(free_e)
         g["free_edges_n"] = np.array(free_e.size)
         g["free_samples"] = free_s
@@ -131,8 +144,57 @@ def case(name, N, input_path, cp, eta, full, roadmap=True):
         print(name, json.dumps(meta)[:400])
 
 
+def gpu_pairs(N, diff_path, out_dir):
+    """The pair arrays of the reference's own fillCoptsTopts run on the GPU
+    (oracle/refgpu/compare_ref_gpu.py): the parity arithmetic's arrays (the
+    CPU build of the reference computes them; the oracle reproduces them bit
+    for bit) with the pairs listed in diff_path replaced, checked against the
+    SHA-256 of the GPU's whole arrays; written to out_dir/copts.f32 and
+    topts.f32."""
+    from oracle import pyoracle as O
+    s = O.halton_samples(N, workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI)
+    c, t = O.bvp_pairs(s)
+    d = np.load(diff_path)
+    c[d["idx"]] = d["copts"]
+    t[d["idx"]] = d["topts"]
+    assert sha(c) == str(d["copts_sha"]) and sha(t) == str(d["topts_sha"]), "diff does not rebuild the GPU arrays"
+    c.tofile(os.path.join(out_dir, "copts.f32"))
+    t.tofile(os.path.join(out_dir, "topts.f32"))
+    return out_dir
+
+
 def main():
+    only = sys.argv[1:]
     tmp = tempfile.mkdtemp()
+    if only and only[0] == "refgpu":
+        # whole queries of the reference program whose pair BVPs are those of its
+        # own GPU kernel: python tests/golden/make_golden.py refgpu DIFF_DIR, where
+        # DIFF_DIR holds refgpu_bvp_diff_N1000.npz and refgpu_bvp_diff_N4000.npz
+        # written by oracle/refgpu/compare_ref_gpu.py on the GPU machine
+        diff_dir = only[1]
+        g1000 = gpu_pairs(1000, os.path.join(diff_dir, "refgpu_bvp_diff_N1000.npz"),
+                          tempfile.mkdtemp(dir=tmp))
+        obs = workloads.random_boxes(10, 0)
+        for om, tag in ((1e-3, "1e-3"), (0.3, "0.3")):
+            p = os.path.join(tmp, "boxes10_noise%s.txt" % tag)
+            workloads.write_input(p, obs, om)
+            case("refgpu_N1000_boxes10_noise" + tag, 1000, p, 0.01, 2, full=False, roadmap=False,
+                 bvp_from=g1000)
+        g4000 = gpu_pairs(4000, os.path.join(diff_dir, "refgpu_bvp_diff_N4000.npz"),
+                          tempfile.mkdtemp(dir=tmp))
+        p = os.path.join(tmp, "indoor4000.txt")
+        workloads.write_input(p, workloads.indoor(1000), 2e-3)
+        case("refgpu_N4000_indoor_P1024", 4000, p, 0.01, 2, full=False, roadmap=False, P=1024,
+             stride=9973, bvp_from=g4000)
+        return
+    if only == ["indoor4000"]:
+        # the benchmark problem: N = 4000, indoor map (40 boxes), noise 2e-3,
+        # 1024 HSMC particles (the reference built with numHSMCParticles = 1024:
+        # bash oracle/build_ref.sh with PUMPREF_NUMS=4000:1024)
+        p = os.path.join(tmp, "indoor4000.txt")
+        workloads.write_input(p, workloads.indoor(1000), 2e-3)
+        case("ref_N4000_indoor_P1024", 4000, p, 0.01, 2, full=False, roadmap=False, P=1024, stride=9973)
+        return
     obs = workloads.random_boxes(10, 0)
     p_low = os.path.join(tmp, "boxes10_noise1e-3.txt")
     p_high = os.path.join(tmp, "boxes10_noise0.3.txt")

@@ -97,6 +97,49 @@ def test_bvp_batch_parity(gpu, pumplib, oracle):
         assert same_bits(t, rt) and same_bits(c, rc)
 
 
+@pytest.mark.parametrize("N", [1000, 4000])
+def test_bvp_pairs_gpu_arithmetic_matches_reference_kernel(N, gpu, pumplib, oracle, goldens):
+    """PUMP_BVP_PARITY_GPU against the reference's own fillCoptsTopts run on
+    the GB300 (tests/golden/refgpu_bvp_N*.npz, oracle/refgpu): every pair's
+    time and cost bit for bit (SHA-256 of both whole arrays), on the Halton
+    samples of the benchmark problems."""
+    import hashlib
+    from pump_gb300 import workloads
+    torch, _ = gpu
+    g = goldens["refgpu_bvp_N%d" % N]
+    s = oracle.halton_samples(N, workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI)
+    c, t = run_bvp_pairs(torch, pumplib, s, mode=pumplib.PUMP_BVP_PARITY_GPU)
+    st = int(g["stride"])
+    assert same_bits(c[::st], g["copts_strided"]) and same_bits(t[::st], g["topts_strided"])
+    assert hashlib.sha256(c.tobytes()).hexdigest() == str(g["copts_sha"])
+    assert hashlib.sha256(t.tobytes()).hexdigest() == str(g["topts_sha"])
+    # the rn and edge count the reference's GPU arrays give
+    k = int(g["k"])
+    rn = np.partition(c, k)[k]
+    assert np.float32(rn) == np.float32(g["rn"]) and int((c < rn).sum()) == int(g["num_edges"])
+
+
+def test_bvp_batch_gpu_arithmetic_equals_pairs(gpu, pumplib, oracle):
+    """The explicit-pair kernel of PUMP_BVP_PARITY_GPU gives what the pair
+    kernel gives for the same pairs (the planner's shared roadmaps use both)."""
+    from pump_gb300 import workloads
+    torch, _ = gpu
+    L = pumplib.load()
+    N = 300
+    s = oracle.halton_samples(N, workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI)
+    c, t = run_bvp_pairs(torch, pumplib, s, mode=pumplib.PUMP_BVP_PARITY_GPU)
+    rng = np.random.default_rng(12)
+    idx = rng.choice(N * (N - 1), 3000, replace=False)
+    i = idx // (N - 1)
+    r = idx - i * (N - 1)
+    j = r + (r >= i)
+    d0, d1 = dev(torch, s[i]), dev(torch, s[j])
+    dt, dc = empty(torch, idx.size, torch.float32), empty(torch, idx.size, torch.float32)
+    pumplib.check(L.pump_bvp_batch(ptr(d0), ptr(d1), idx.size, 5.0, pumplib.PUMP_BVP_PARITY_GPU,
+                                   ptr(dt), ptr(dc), stream(torch)))
+    assert same_bits(host(dt, idx.size), t[idx]) and same_bits(host(dc, idx.size), c[idx])
+
+
 def kth_in_key_order(v, k):
     """The k-th smallest float32 in the order of the sign-magnitude keys:
     negative NaNs first, then -inf .. -0.0, +0.0 .. +inf, positive NaNs."""
@@ -413,6 +456,55 @@ def test_hsmc_propagate(P, gpu, pumplib, oracle, roadmap1000):
     assert same_bits(host(d_cp)[base:base + n_new], cp_o[base:])
     assert int(host(d_err)[0]) == 0
     assert 0 < valid_bytes[base:].mean() < 1
+
+
+def test_hsmc_device_checks(gpu, pumplib, oracle, roadmap1000):
+    """HSMC's device-side checks: an edge index outside [0, E) and a parent
+    outside [0, base) skip their paths and record PUMP_ERR_BAD_INPUT; a time
+    row past the particle table records PUMP_ERR_CAPACITY (the reference
+    reads both without a bound, PUMP.cu:626-647).  Every other path is
+    computed as the oracle computes it."""
+    torch, _ = gpu
+    L = pumplib.load()
+    r = roadmap1000
+    obs, E = r["obs"], r["src"].size
+    om, maxHS, P, Pmc = np.float32(0.3), 5, 128, 2048
+    maxd2 = np.float32(0.1 * np.float64(om) * np.float64(om))
+    a, b, _ = oracle.cache_halfspaces(r["disc"], r["fe"], obs, maxHS, maxd2)
+    rng = np.random.default_rng(31)
+    base, n_new = 40, 500
+    edges = rng.choice(np.nonzero(r["fe"])[0], n_new).astype(np.int32)
+    prev = rng.integers(0, base, n_new).astype(np.int32)
+    times = np.zeros(base + n_new, np.float32)
+    times[:base] = rng.uniform(0, 4, base).astype(np.float32)
+    valid_bytes = np.zeros((base + n_new, P), np.uint8)
+    valid_bytes[:base] = rng.random((base, P)) < 0.9
+    packed = np.packbits(valid_bytes, axis=1, bitorder="little").view(np.uint32)
+    for T, bad, want in ((400, True, pumplib.PUMP_ERR_BAD_INPUT), (60, False, pumplib.PUMP_ERR_CAPACITY)):
+        tm, _ = oracle.particle_tables(0x1234, Pmc, T, pmajor=False)
+        e2, p2 = edges.copy(), prev.copy()
+        if bad:
+            e2[3], p2[5] = E, base  # one past the end of each
+        d_valid = dev(torch, packed)
+        d_cp = empty(torch, base + n_new, torch.float32)
+        d_err = dev(torch, np.zeros(1, np.int32))
+        keep = [dev(torch, x) for x in (e2, p2, a, b, times, r["te"], tm)]
+        pumplib.check(L.pump_hsmc_propagate(n_new, 9, ptr(keep[0]), ptr(keep[1]), E, base, ptr(keep[2]),
+                                            ptr(keep[3]), maxHS, ptr(keep[4]), ptr(keep[5]), 0.05,
+                                            ptr(keep[6]), Pmc, T, float(om), ptr(d_valid), P, ptr(d_cp),
+                                            ptr(d_err), None, stream(torch)))
+        torch.cuda.synchronize()
+        assert int(host(d_err)[0]) == want
+        if bad:
+            got = bits_to_bytes(host(d_valid).reshape(base + n_new, -1), P)
+            vb = valid_bytes.copy()
+            cp_o = np.zeros(base + n_new, np.float32)
+            oracle.lib().orc_hsmc_propagate(n_new, 9, edges, prev, base, a, b, times, r["te"], 0.05, maxHS,
+                                            tm.reshape(-1), om, Pmc, vb, P, cp_o)
+            ok = np.ones(n_new, bool)
+            ok[[3, 5]] = False
+            assert np.array_equal(got[base:][ok], vb[base:][ok])
+            assert same_bits(host(d_cp)[base:base + n_new][ok], cp_o[base:][ok])
 
 
 @pytest.mark.parametrize("om", [0.3, 2e-3])

@@ -11,7 +11,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 CASES = ["ref_N64_input", "ref_N1000_input", "ref_N1000_boxes10_noise1e-3",
-         "ref_N1000_boxes10_noise0.3"]
+         "ref_N1000_boxes10_noise0.3", "ref_N4000_indoor_P1024"]
 
 
 def make_problem(L, g, **over):
@@ -31,7 +31,7 @@ def make_problem(L, g, **over):
     return pb, obs
 
 
-def run_plan(L, ctx, pb, rows=400):
+def run_plan(L, ctx, pb, rows=400, trace_cap=0):
     res = L.PlanResult()
     path = np.zeros((rows, 6), np.float32)
     nodes = np.zeros(64, np.int32)
@@ -39,22 +39,38 @@ def run_plan(L, ctx, pb, rows=400):
     res.nodes, res.nodes_cap = nodes.ctypes.data, 64
     ctrl = np.zeros((4096, 6), np.float32)
     res.ctrl_path, res.ctrl_cap = ctrl.ctypes.data, 4096
+    trace = np.zeros(max(trace_cap, 1), np.int32)
+    if trace_cap:
+        res.wf_trace, res.wf_trace_cap = trace.ctypes.data, trace_cap
     st = L.load().pump_plan(ctx.handle, C.byref(pb), C.byref(res), None)
     run_plan.ctrl = ctrl[: min(res.ctrl_len, 4096)].copy()
+    run_plan.trace = trace[: res.wf_trace_len].copy() if trace_cap else None
     return st, res, path[: res.path_len].copy(), nodes[: res.num_nodes].copy()
 
 
-@pytest.mark.parametrize("name", CASES)
+# Whole queries of the reference program whose pair BVPs come from its own
+# GPU kernel (tests/golden/make_golden.py refgpu): the library's
+# PUMP_BVP_PARITY_GPU mode
+GPU_CASES = ["refgpu_N1000_boxes10_noise1e-3", "refgpu_N1000_boxes10_noise0.3",
+             "refgpu_N4000_indoor_P1024"]
+
+
+@pytest.mark.parametrize("name", CASES + GPU_CASES)
 def test_plan_matches_reference(name, gpu, pumplib, goldens):
+    """The whole query, including the exploration trace: the (parent path,
+    edge) of every expansion in the reference's launch order."""
     torch, ctx = gpu
     g = goldens[name]
-    pb, _obs = make_problem(pumplib, g)
-    st, res, path, nodes = run_plan(pumplib, ctx, pb)
+    P = int(g["hsmc_particles"]) if "hsmc_particles" in g else 128
+    mode = pumplib.PUMP_BVP_PARITY_GPU if name.startswith("refgpu_") else pumplib.PUMP_BVP_PARITY
+    pb, _obs = make_problem(pumplib, g, num_hsmc=P, bvp_mode=mode)
+    st, res, path, nodes = run_plan(pumplib, ctx, pb, trace_cap=g["wavefront_trace"].size + 16)
     assert st in (pumplib.PUMP_OK, pumplib.PUMP_ERR_NO_SOLUTION), pumplib.load().pump_last_error()
     sizes = np.array(res.wavefront_sizes[: res.iterations], np.int32)
     if sizes.size and sizes[-1] == 0:
         sizes = sizes[:-1]
     assert np.array_equal(sizes, g["wavefront_sizes"])
+    assert np.array_equal(run_plan.trace, g["wavefront_trace"])
     assert res.num_paths == int(g["num_paths"])
     assert res.num_considered == int(g["num_considered"])
     assert res.goal_paths == int(g["goal_paths"])
@@ -109,8 +125,8 @@ def fill_problem(L, q, keep):
 
 def test_plan_batch_equals_single_queries(gpu, pumplib):
     """Concurrent queries (pump_plan_batch, 4 workers) give exactly what each
-    query gives alone: Halton queries of both BVP modes go through the batch's
-    shared roadmaps, the query with explicit samples plans on its own."""
+    query gives alone: Halton queries of the three BVP modes go through the
+    batch's shared roadmaps, the query with explicit samples plans on its own."""
     torch, ctx = gpu
     from pump_gb300 import workloads
     L = pumplib.load()
@@ -118,8 +134,8 @@ def test_plan_batch_equals_single_queries(gpu, pumplib):
     keep = []
     pbs = (pumplib.Problem * len(qs))(*[fill_problem(pumplib, q, keep) for q in qs])
     for k in range(len(qs)):
-        if k % 2:
-            pbs[k].bvp_mode = pumplib.PUMP_BVP_PRECISION
+        pbs[k].bvp_mode = (pumplib.PUMP_BVP_PARITY, pumplib.PUMP_BVP_PRECISION,
+                           pumplib.PUMP_BVP_PARITY_GPU)[k % 3]
     rng = np.random.default_rng(5)
     own = rng.uniform(workloads.LO, workloads.HI, size=(pbs[3].N, 6)).astype(np.float32)
     own[0], own[-1] = qs[3]["init"], qs[3]["goal"]
@@ -181,8 +197,11 @@ def test_search_graph_equals_host_loop(gpu, pumplib, goldens):
     L = pumplib.load()
     from pump_gb300 import workloads
     try:
-        for name in CASES:
-            pb, _obs = make_problem(pumplib, goldens[name])
+        for name in CASES + GPU_CASES:
+            g = goldens[name]
+            P = int(g["hsmc_particles"]) if "hsmc_particles" in g else 128
+            mode = pumplib.PUMP_BVP_PARITY_GPU if name in GPU_CASES else pumplib.PUMP_BVP_PARITY
+            pb, _obs = make_problem(pumplib, g, num_hsmc=P, bvp_mode=mode)
             out = []
             for on in (0, 1):
                 L.pump_search_graph(on)
@@ -194,8 +213,8 @@ def test_search_graph_equals_host_loop(gpu, pumplib, goldens):
         keep = []
         pbs = (pumplib.Problem * len(qs))(*[fill_problem(pumplib, q, keep) for q in qs])
         for k in range(len(qs)):
-            if k % 2:
-                pbs[k].bvp_mode = pumplib.PUMP_BVP_PRECISION
+            pbs[k].bvp_mode = (pumplib.PUMP_BVP_PARITY, pumplib.PUMP_BVP_PRECISION,
+                               pumplib.PUMP_BVP_PARITY_GPU)[k % 3]
         got = []
         for level in (0, 2):  # batch workers host-driven, then as graphs
             L.pump_search_graph(level)

@@ -18,7 +18,7 @@ def sha(a):
 
 
 CASES = ["ref_N64_input", "ref_N1000_input", "ref_N1000_boxes10_noise1e-3",
-         "ref_N1000_boxes10_noise0.3"]
+         "ref_N1000_boxes10_noise0.3", "ref_N4000_indoor_P1024"]
 
 
 def problem(g):
@@ -66,10 +66,12 @@ def test_waypoints_masks_halfspaces(name, oracle, goldens, roadmaps):
     # the reference sizes its edge arrays at rnIdx (>= E); rows past E are unused
     disc_ref_prefix = r["disc"].reshape(-1)
     assert E <= nref
+    stride = int(g["stride"]) if "stride" in g else 97
     if E == nref:
         assert sha(r["disc"]) == str(g["disc_sha"])
-    else:
-        assert np.array_equal(disc_ref_prefix[::97][: g["disc_sub"].size], g["disc_sub"][: disc_ref_prefix[::97].size])
+    elif "disc_sub" in g:
+        sub = disc_ref_prefix[::stride]
+        assert np.array_equal(sub[: g["disc_sub"].size], g["disc_sub"][: sub.size])
     fe = oracle.free_edges(r["disc"], obs)
     ref_fe = np.unpackbits(g["free_edges_bits"])[:nref]
     assert np.array_equal(fe, ref_fe[:E])
@@ -81,7 +83,7 @@ def test_waypoints_masks_halfspaces(name, oracle, goldens, roadmaps):
     if E == nref:
         assert sha(a) == str(g["as_sha"]) and sha(b) == str(g["bs_sha"])
     sub_a = g["as_sub"]
-    stride = 1 if sub_a.size == a.size else 97
+    stride = 1 if sub_a.size == a.size else stride
     n = min(sub_a.size, a[::stride].size)
     assert np.array_equal(a[::stride][:n].view(np.uint32), sub_a[:n].view(np.uint32))
 
@@ -95,8 +97,9 @@ def test_whole_query(name, oracle, goldens):
     """Exploration trace, stored paths and the returned path (PUMP.cu:3-607)."""
     g = goldens[name]
     N, obs, init, goal, lo, hi, om = problem(g)
+    P = int(g["hsmc_particles"]) if "hsmc_particles" in g else 128
     r = oracle.plan(N, obs, init, goal, lo, hi, om, float(g["cp_target"]), float(g["cp_factor"]),
-                    T_table=400, trace_cap=4_000_000)
+                    P=P, T_table=400, trace_cap=4_000_000)
     sizes = r["wavefront_sizes"]
     if sizes.size and sizes[-1] == 0:  # last iteration found nothing to expand: no launch
         sizes = sizes[:-1]
@@ -116,3 +119,18 @@ def test_whole_query(name, oracle, goldens):
         assert text == str(g["path_txt"])
     # discretizedPath.txt (PUMP.cu:553-579: "%g, " per value, 6 per line)
     assert ctrl_text(r["ctrl_path"]) == str(g["ctrl_txt"])
+
+
+@pytest.mark.parametrize("name", ["refgpu_N1000_boxes10_noise1e-3", "refgpu_N1000_boxes10_noise0.3",
+                                  "refgpu_N4000_indoor_P1024"])
+def test_gpu_bvp_goldens_ran_on_the_reference_gpu_pairs(name, goldens, roadmaps):
+    """The whole-query fixtures of the reference GPU's arithmetic were made on
+    exactly the pair arrays its fillCoptsTopts wrote on the GB300 (the SHA-256
+    of refgpu_bvp_N*.npz), on the same samples; those arrays differ from the
+    parity arithmetic's (which the oracle and the CPU build compute)."""
+    g = goldens[name]
+    ref = goldens["refgpu_bvp_N%d" % int(g["N"])]
+    assert str(g["copts_sha"]) == str(ref["copts_sha"]) and str(g["topts_sha"]) == str(ref["topts_sha"])
+    r = roadmaps(name)
+    assert np.array_equal(r["samples"].view(np.uint32), g["samples"].view(np.uint32))
+    assert sha(r["copts"]) != str(g["copts_sha"])
