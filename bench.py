@@ -11,20 +11,30 @@ configuration's "FP64 bisection"); synthetic, seeded.
 One step = one planning query's hot path:
   value: the device-resident kernels of the query -- all N(N-1) pair BVPs,
          the rn selection, edge compaction and waypoints, sample and edge
-         collision checks (E edges), half-spaces, and the HSMC propagation of
-         every exploration wavefront of the query (sum M expansions x 1024
-         particles) -- launched back to back on resident buffers, timed with
-         CUDA events on the launching stream; the L2 is flushed (512 MB
-         write) between steps.  Units per step: N(N-1) + E + sum M.
+         collision checks (E edges), and the HSMC propagation of every
+         exploration wavefront of the query (sum M expansions x 1024
+         particles, half-spaces derived in the kernel): the query's own HSMC
+         launches replayed from its exploration trace with the stored parent
+         paths' real start times and particle masks -- launched back to back
+         on resident buffers, timed with CUDA events on the launching stream;
+         the L2 is flushed (512 MB write) between steps.  Units per step:
+         N(N-1) + E + sum M.
   e2e:   the same units through pump_plan() with host buffers: host problem
          in, path out, every host<->device copy and the host search logic
          inside the timed region; ms_per_step of e2e is the plan latency.
+The headline uses the precision BVP (the configuration's binary64 root).
+The same workload is also reported in the two arithmetics that are bit-exact
+with a build of the reference: "parity" (the reference's host arithmetic,
+as its CPU build computes) and "parity_gpu" (the pair matrix as the
+reference's own GPU kernel computes it), each with its device pipeline, plan
+latency and (parity) batched vs plain queries/s.
 The CPU baseline is the C oracle (the reference's algorithm restated,
-OpenMP over all host cores) timed on bounded samples of each stage.
+OpenMP over all host cores) timed on one whole query.
 
---impl reference times that CPU path alone (the reference's CPU
-implementation of this path; the reference's own GPU program is not
-buildable on the GPU machine, whose image holds no copy of its sources).
+--impl reference times that CPU path alone: the reference's CPU
+implementation of this path (the C oracle, a restatement pinned bit for bit
+to the reference's own code built for the CPU), one whole query per step on
+all host cores.
 """
 from __future__ import annotations
 
@@ -55,10 +65,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--num", type=int, default=4000)
-    ap.add_argument("--mode", default="precision", choices=["precision", "parity"])
+    ap.add_argument("--mode", default="precision", choices=["precision", "parity", "parity_gpu"])
     ap.add_argument("--particles", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-refine", action="store_true", help="skip the path-refinement workload")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the records of the two bit-exact arithmetics")
+    ap.add_argument("--no-large", action="store_true", help="skip the large configuration (N = 32000)")
     ap.add_argument("--batch", type=int, default=256, help="queries of the batched workload (0: skip)")
     ap.add_argument("--workers", type=int, default=0,
                     help="batched-mode workers (0: the host cores less two, at most 14)")
@@ -83,7 +96,7 @@ def workload(args, query):
     from pump_gb300 import workloads
     obs = workloads.indoor(1000 * 1 + query)
     return dict(N=args.num, obstacles=obs, offset_mult=np.float32(2e-3), cp=0.01, eta=2.0,
-                num_disc=8, P=args.particles, mode=1 if args.mode == "precision" else 0)
+                num_disc=8, P=args.particles)
 
 
 # ---------------------------------------------------------------- clocks
@@ -159,7 +172,7 @@ def cpu_query(args, query=0):
 
 
 # ------------------------------------------------------------------ ours
-def measure_queries(args, lib, L, ctx):
+def measure_queries(args, lib, L, ctx, mode):
     """Batched vs plain queries/s on the batched workload (256 queries, N
     log-uniform in [500, 8000], 5-100 boxes, init/goal in free space, CP
     target in {0.001, 0.01, 0.05}, eta in {1, 2, 4}).  Plain: one pump_plan
@@ -179,13 +192,14 @@ def measure_queries(args, lib, L, ctx):
             pb.init[d], pb.goal[d] = q["init"][d], q["goal"][d]
             pb.lo[d], pb.hi[d] = workloads.LO[d], workloads.HI[d]
         pb.offset_mult, pb.cp_target, pb.cp_factor = float(q["offset_mult"]), q["cp"], q["eta"]
-        pb.bvp_mode = 1 if args.mode == "precision" else 0
-    paths = np.zeros((len(qs), 400, 6), np.float32)
+        pb.bvp_mode = Query.MODES[mode]
+    paths = {}
 
-    def results():
+    def results(tag):
+        paths[tag] = np.zeros((len(qs), 400, 6), np.float32)
         res = (lib.PlanResult * len(qs))()
         for k in range(len(qs)):
-            res[k].path, res[k].path_cap = paths[k].ctypes.data, 400
+            res[k].path, res[k].path_cap = paths[tag][k].ctypes.data, 400
         return res
 
     def ok(res, sts):
@@ -197,25 +211,33 @@ def measure_queries(args, lib, L, ctx):
     workers = args.workers or max(1, min(14, (os.cpu_count() or 8) - 2))
     # warm both paths on every query (contexts, particle tables, and the
     # autotuner's first call of each shape class, which neither timed run pays)
-    res = results()
+    res = results("warm")
     sts = (C.c_int * len(qs))()
     for k in range(len(qs)):
         sts[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res[k]), None)
     L.pump_plan_batch(0, pbs, res, sts, len(qs), workers)
-    res_p, sts_p = results(), (C.c_int * len(qs))()
+    res_p, sts_p = results("plain"), (C.c_int * len(qs))()
     t0 = time.perf_counter()
     for k in range(len(qs)):
         sts_p[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res_p[k]), None)
     t_plain = time.perf_counter() - t0
-    res_b, sts_b = results(), (C.c_int * len(qs))()
+    res_b, sts_b = results("batched"), (C.c_int * len(qs))()
     t0 = time.perf_counter()
     lib.check(L.pump_plan_batch(0, pbs, res_b, sts_b, len(qs), workers))
     t_batch = time.perf_counter() - t0
+    # identical results: status, solution index, CP and cost bits, and the
+    # returned path's states bit for bit
+    f32 = lambda x: np.float32(x).view(np.uint32)  # noqa: E731
     same = all(res_p[k].success == res_b[k].success and res_p[k].soln_path_idx == res_b[k].soln_path_idx
-               and sts_p[k] == sts_b[k] for k in range(len(qs)))
+               and sts_p[k] == sts_b[k] and res_p[k].path_len == res_b[k].path_len
+               and f32(res_p[k].soln_cp) == f32(res_b[k].soln_cp)
+               and f32(res_p[k].soln_cost) == f32(res_b[k].soln_cost)
+               and np.array_equal(paths["plain"][k][: res_p[k].path_len].view(np.uint32),
+                                  paths["batched"][k][: res_b[k].path_len].view(np.uint32))
+               for k in range(len(qs)))
     ok_p, ok_b = ok(res_p, sts_p), ok(res_b, sts_b)
     return {"workload": "batch256: N log-uniform [500, 8000], 5-100 boxes, noise 1e-3",
-            "queries": len(qs), "met_cp_target": ok_b, "workers": workers,
+            "bvp": mode, "queries": len(qs), "met_cp_target": ok_b, "workers": workers,
             "plain_queries_per_s": ok_p / t_plain, "batched_queries_per_s": ok_b / t_batch,
             "batched_over_plain": (ok_b / t_batch) / (ok_p / t_plain) if ok_p else None,
             "plain_s": t_plain, "batched_s": t_batch, "identical_results": bool(same)}
@@ -384,6 +406,183 @@ def fp64_peak_tflops(torch):
     return 2.0 * 8.0 * iters * blocks * 256 / (a.elapsed_time(b) * 1e-3) / 1e12
 
 
+class Query:
+    """One planning problem through the C ABI on one context and stream:
+    plan() runs pump_plan; pipeline() times the device-resident kernels of
+    the same query (see the module docstring)."""
+
+    MODES = {"parity": 0, "precision": 1, "parity_gpu": 2}
+
+    def __init__(self, lib, L, ctx, torch, w, mode):
+        from pump_gb300 import workloads
+        self.lib, self.L, self.ctx, self.torch, self.w = lib, L, ctx, torch, w
+        self.mode = self.MODES[mode]
+        self.obs = np.ascontiguousarray(w["obstacles"], np.float32)
+        pb = lib.Problem()
+        L.pump_problem_defaults(C.byref(pb))
+        pb.N, pb.num_disc, pb.num_hsmc = w["N"], w["num_disc"], w["P"]
+        pb.num_mc = w.get("num_mc", pb.num_mc)
+        pb.num_obstacles, pb.obstacles = self.obs.shape[0], self.obs.ctypes.data
+        for k in range(6):
+            pb.init[k], pb.goal[k] = workloads.INIT[k], workloads.GOAL[k]
+            pb.lo[k], pb.hi[k] = workloads.LO[k], workloads.HI[k]
+        pb.offset_mult, pb.cp_target, pb.cp_factor = float(w["offset_mult"]), w["cp"], w["eta"]
+        pb.bvp_mode = self.mode
+        self.pb = pb
+        self.path = np.zeros((pb.table_rows, 6), np.float32)
+
+    def plan(self, trace=False, paths_cap=0):
+        """One pump_plan call; with trace, also the exploration trace, and
+        with paths_cap >= the stored paths, their times and particle masks
+        (with the trace, every HSMC launch's inputs)."""
+        lib, pb = self.lib, self.pb
+        res = lib.PlanResult()
+        res.path, res.path_cap = self.path.ctypes.data, pb.table_rows
+        if trace:
+            self.trace_buf = np.zeros(2 * 40_000_000, np.int32)
+            res.wf_trace, res.wf_trace_cap = self.trace_buf.ctypes.data, self.trace_buf.size
+        if paths_cap:
+            self.ptime = np.zeros(paths_cap, np.float32)
+            self.pvalid = np.zeros(paths_cap * ((pb.num_hsmc + 31) // 32), np.uint32)
+            res.path_time, res.path_valid, res.path_state_cap = (self.ptime.ctypes.data,
+                                                                 self.pvalid.ctypes.data, paths_cap)
+        st = self.L.pump_plan(self.ctx.handle, C.byref(pb), C.byref(res), None)
+        if st not in (lib.PUMP_OK, lib.PUMP_ERR_NO_SOLUTION):
+            lib.check(st)
+        return res
+
+    def pipeline(self, steps, warmup, flush, clocks=None):
+        """Device-resident kernels of one query per step; returns the timing
+        record.  HSMC replays the query's own launches: its (parent, edge)
+        trace with the stored parents' real times and particle masks."""
+        torch, lib, L, w = self.torch, self.lib, self.L, self.w
+        stream = torch.cuda.current_stream()
+        sh = stream.cuda_stream
+        res0 = self.plan()
+        res0 = self.plan(trace=True, paths_cap=max(1, int(res0.num_paths)))
+        N, P, W = w["N"], w["P"], w["num_disc"] + 1
+        E = int(res0.num_edges)
+        nobs = self.obs.shape[0]
+        sizes = [int(res0.wavefront_sizes[i]) for i in range(min(res0.iterations, 32))]
+        sizes = [x for x in sizes if x > 0]
+        trace = self.trace_buf[: res0.wf_trace_len].reshape(-1, 2).copy()
+        M_total = int(trace.shape[0])
+        units = N * (N - 1) + E + M_total
+        words = (P + 31) // 32
+        base = int(res0.num_paths)
+
+        def dev(a):
+            return torch.from_numpy(np.ascontiguousarray(a).copy()).cuda()
+
+        def empty(n, dt):
+            return torch.empty(int(max(n, 1)), dtype=dt, device="cuda")
+
+        f6 = lambda v: (C.c_float * 6)(*[float(x) for x in v])  # noqa: E731
+        pb = self.pb
+        d_s = empty(N * 6, torch.float32)
+        lib.check(L.pump_halton_samples(N, f6(pb.lo), f6(pb.hi), f6(pb.init), f6(pb.goal),
+                                        d_s.data_ptr(), sh))
+        d_obs = dev(self.obs)
+        npairs = N * (N - 1)
+        d_c, d_t = empty(npairs, torch.float32), empty(npairs, torch.float32)
+        rn_idx = int(np.float32((N - 1) * N) * np.float32(0.05))
+        cap = rn_idx
+        d_src, d_dst = empty(cap, torch.int32), empty(cap, torch.int32)
+        d_ce, d_te = empty(cap, torch.float32), empty(cap, torch.float32)
+        d_go = empty(N + 1, torch.int32)
+        d_disc = empty(cap * W * 6, torch.float32)
+        d_fs, d_fe = empty(N, torch.uint8), empty(cap, torch.uint8)
+        maxHS = min(nobs, 5)
+        Pmc, T = int(pb.num_mc), int(pb.table_rows)
+        d_tab = empty(T * Pmc * 3, torch.float32)
+        lib.check(L.pump_particle_tables(pb.seed, Pmc, T, d_tab.data_ptr(), None, sh))
+        # parents: the stored paths' masks and times; new paths go after them
+        valid = np.zeros((base + max(sizes + [1])) * words, np.uint32)
+        valid[: base * words] = self.pvalid[: base * words]
+        d_valid = dev(valid.view(np.int32))
+        d_times = dev(self.ptime[:base])
+        d_cp = empty(base + max(sizes + [1]), torch.float32)
+        d_err = empty(1, torch.int32).zero_()
+        offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        d_prev = dev(trace[:, 0].astype(np.int32))
+        d_edge = dev(trace[:, 1].astype(np.int32))
+        maxd2 = float(np.float32(0.1 * np.float64(w["offset_mult"]) ** 2))
+        rn = C.c_float(0)
+        Eo = C.c_longlong(0)
+        launches = {"n": 0}
+        ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+        kernel_ms = {}
+        mode = self.mode
+
+        def timed(name, fn, nk):
+            a, b = ev(), ev()
+            a.record(stream)
+            fn()
+            b.record(stream)
+            kernel_ms.setdefault(name, []).append((a, b))
+            launches["n"] += nk
+
+        def step():
+            timed("bvp_pairs", lambda: lib.check(L.pump_bvp_pairs(d_s.data_ptr(), N, 5.0, mode,
+                                                                 d_c.data_ptr(), d_t.data_ptr(), sh)), 1)
+            timed("rn_edges", lambda: lib.check(L.pump_roadmap_edges(
+                self.ctx.handle, d_c.data_ptr(), d_t.data_ptr(), N, rn_idx, cap, d_src.data_ptr(),
+                d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(), d_go.data_ptr(), C.byref(rn),
+                C.byref(Eo), sh)), 12)
+            timed("discretize", lambda: lib.check(L.pump_discretize_edges(
+                d_s.data_ptr(), d_src.data_ptr(), d_dst.data_ptr(), d_te.data_ptr(), Eo.value, W - 1,
+                mode, d_disc.data_ptr(), sh)), 1)
+            timed("sample_free", lambda: lib.check(L.pump_sample_free(
+                d_obs.data_ptr(), nobs, d_s.data_ptr(), N, d_fs.data_ptr(), sh)), 1)
+            timed("free_edges", lambda: lib.check(L.pump_free_edges(
+                d_obs.data_ptr(), nobs, d_disc.data_ptr(), Eo.value, W - 1, d_fe.data_ptr(), sh)), 1)
+
+            # half-spaces derived inside the HSMC kernel from the boxes (the planner's path)
+            def hsmc_all():
+                for it, m in enumerate(sizes):
+                    o = int(offs[it])
+                    lib.check(L.pump_hsmc_propagate_boxes(
+                        m, W, d_edge.data_ptr() + 4 * o, d_prev.data_ptr() + 4 * o, E, base,
+                        d_obs.data_ptr(), nobs, d_disc.data_ptr(), maxd2, maxHS, d_times.data_ptr(),
+                        d_te.data_ptr(), 0.05, d_tab.data_ptr(), Pmc, T, float(w["offset_mult"]),
+                        d_valid.data_ptr(), P, d_cp.data_ptr(), d_err.data_ptr(), sh))
+            timed("hsmc", hsmc_all, len(sizes))
+
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        assert Eo.value == E, (Eo.value, E)
+        assert int(d_err.item()) == 0
+        kernel_ms.clear()
+        launches["n"] = 0
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        step_ms = []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            a, b = ev(), ev()
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(a.elapsed_time(b))
+        torch.cuda.synchronize()
+        ks = {k: sum(a.elapsed_time(b) for a, b in v) / steps for k, v in kernel_ms.items()}
+        return {"units": units, "E": E, "M": M_total, "W": W, "maxHS": maxHS, "sizes": sizes,
+                "step_ms": step_ms, "kernel_ms": ks, "launches": launches["n"],
+                "per_step_units": {"pairs": npairs, "edges": E, "expansions": M_total}}
+
+    def e2e(self, reps):
+        """pump_plan latencies (host problem in, path out)."""
+        out, res = [], None
+        for _ in range(max(1, reps)):
+            t0 = time.perf_counter()
+            res = self.plan()
+            out.append((time.perf_counter() - t0) * 1e3)
+        return out, res
+
+
 def run_ours(args):
     import torch
     from pump_gb300 import lib
@@ -402,155 +601,21 @@ def run_ours(args):
     torch.cuda.set_device(local)
     ctx = lib.Context(local)
     w = workload(args, rank)
-    N, obs, P = w["N"], w["obstacles"], w["P"]
-    W = w["num_disc"] + 1
-    stream = torch.cuda.current_stream()
-    sh = stream.cuda_stream
-
-    def dev(a):
-        return torch.from_numpy(np.ascontiguousarray(a).copy()).cuda()
-
-    def empty(n, dt):
-        return torch.empty(int(max(n, 1)), dtype=dt, device="cuda")
-
-    # ---- one query through the C ABI (also gives the exploration trace)
-    pb = lib.Problem()
-    L.pump_problem_defaults(C.byref(pb))
-    obs_host = np.ascontiguousarray(obs, np.float32)
-    from pump_gb300 import workloads
-    pb.N, pb.num_disc, pb.num_hsmc = N, w["num_disc"], P
-    pb.num_obstacles, pb.obstacles = obs_host.shape[0], obs_host.ctypes.data
-    for k in range(6):
-        pb.init[k], pb.goal[k] = workloads.INIT[k], workloads.GOAL[k]
-        pb.lo[k], pb.hi[k] = workloads.LO[k], workloads.HI[k]
-    pb.offset_mult, pb.cp_target, pb.cp_factor = float(w["offset_mult"]), w["cp"], w["eta"]
-    pb.bvp_mode = w["mode"]
-    trace_buf = np.zeros(2 * 8_000_000, np.int32)
-    path_buf = np.zeros((400, 6), np.float32)
-
-    def plan(with_trace):
-        res = lib.PlanResult()
-        res.path, res.path_cap = path_buf.ctypes.data, 400
-        if with_trace:
-            res.wf_trace, res.wf_trace_cap = trace_buf.ctypes.data, trace_buf.size
-        st = L.pump_plan(ctx.handle, C.byref(pb), C.byref(res), None)
-        if st not in (lib.PUMP_OK, lib.PUMP_ERR_NO_SOLUTION):
-            lib.check(st)
-        return res
-
-    res0 = plan(True)
-    E = int(res0.num_edges)
-    sizes = [int(res0.wavefront_sizes[i]) for i in range(min(res0.iterations, 32))]
-    sizes = [s for s in sizes if s > 0]
-    trace = trace_buf[: res0.wf_trace_len].reshape(-1, 2).copy()
-    M_total = int(trace.shape[0])
-    units = N * (N - 1) + E + M_total
-
-    # ---- device-resident buffers for the kernel pipeline
-    from oracle import pyoracle  # noqa: F401  (only for the CPU baseline below)
-    samples = np.zeros((N, 6), np.float32)
-    # Halton samples as the planner generates them (sampler.cu:20-41)
-    from oracle.pyoracle import halton_samples
-    samples = halton_samples(N, workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI)
-    d_s, d_obs = dev(samples), dev(obs_host)
-    npairs = N * (N - 1)
-    d_c, d_t = empty(npairs, torch.float32), empty(npairs, torch.float32)
-    rn_idx = int(np.float32((N - 1) * N) * np.float32(0.05))
-    cap = rn_idx
-    d_src, d_dst = empty(cap, torch.int32), empty(cap, torch.int32)
-    d_ce, d_te = empty(cap, torch.float32), empty(cap, torch.float32)
-    d_go = empty(N + 1, torch.int32)
-    d_disc = empty(cap * W * 6, torch.float32)
-    d_fs, d_fe = empty(N, torch.uint8), empty(cap, torch.uint8)
-    maxHS = min(obs_host.shape[0], 5)
-    Pmc, T = 2048, 400
-    d_tab = empty(T * Pmc * 3, torch.float32)
-    lib.check(L.pump_particle_tables(pb.seed, Pmc, T, d_tab.data_ptr(), None, sh))
-    words = (P + 31) // 32
-    base = int(trace[:, 0].max()) + 1 if M_total else 1
-    d_valid = empty((base + max(sizes + [1])) * words, torch.int32)
-    d_valid.fill_(-1)
-    d_times = empty(base, torch.float32).zero_()
-    d_cp = empty(base + max(sizes + [1]), torch.float32)
-    d_err = empty(1, torch.int32).zero_()
-    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
-    d_prev = dev(trace[:, 0].astype(np.int32))
-    d_edge = dev(trace[:, 1].astype(np.int32))
-    maxd2 = float(np.float32(0.1 * np.float64(w["offset_mult"]) ** 2))
+    N, P = w["N"], w["P"]
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    rn = C.c_float(0)
-    Eo = C.c_longlong(0)
-    launches = {"n": 0}
-    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
-    kernel_ms = {}
-
-    def timed(name, fn, nk):
-        a, b = ev(), ev()
-        a.record(stream)
-        fn()
-        b.record(stream)
-        kernel_ms.setdefault(name, []).append((a, b))
-        launches["n"] += nk
-
-    def step():
-        timed("bvp_pairs", lambda: lib.check(L.pump_bvp_pairs(d_s.data_ptr(), N, 5.0, w["mode"],
-                                                             d_c.data_ptr(), d_t.data_ptr(), sh)), 1)
-        timed("rn_edges", lambda: lib.check(L.pump_roadmap_edges(
-            ctx.handle, d_c.data_ptr(), d_t.data_ptr(), N, rn_idx, cap, d_src.data_ptr(),
-            d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(), d_go.data_ptr(), C.byref(rn),
-            C.byref(Eo), sh)), 12)
-        timed("discretize", lambda: lib.check(L.pump_discretize_edges(
-            d_s.data_ptr(), d_src.data_ptr(), d_dst.data_ptr(), d_te.data_ptr(), Eo.value, W - 1,
-            w["mode"], d_disc.data_ptr(), sh)), 1)
-        timed("sample_free", lambda: lib.check(L.pump_sample_free(
-            d_obs.data_ptr(), obs_host.shape[0], d_s.data_ptr(), N, d_fs.data_ptr(), sh)), 1)
-        timed("free_edges", lambda: lib.check(L.pump_free_edges(
-            d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), Eo.value, W - 1,
-            d_fe.data_ptr(), sh)), 1)
-        # half-spaces derived inside the HSMC kernel from the boxes (the planner's path)
-        def hsmc_all():
-            for it, m in enumerate(sizes):
-                o = int(offs[it])
-                lib.check(L.pump_hsmc_propagate_boxes(
-                    m, W, d_edge.data_ptr() + 4 * o, d_prev.data_ptr() + 4 * o, E, base,
-                    d_obs.data_ptr(), obs_host.shape[0], d_disc.data_ptr(), maxd2, maxHS,
-                    d_times.data_ptr(), d_te.data_ptr(), 0.05, d_tab.data_ptr(), Pmc, T,
-                    float(w["offset_mult"]), d_valid.data_ptr(), P, d_cp.data_ptr(),
-                    d_err.data_ptr(), sh))
-        timed("hsmc", hsmc_all, len(sizes))
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    assert Eo.value == E, (Eo.value, E)
-    kernel_ms.clear()
-    launches["n"] = 0
+    q = Query(lib, L, ctx, torch, w, args.mode)
     if dist:
         dist.barrier()
-    torch.cuda.synchronize()
     clocks = ClockSampler()
-    clocks.start()
-    step_ms = []
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        a, b = ev(), ev()
-        a.record(stream)
-        step()
-        b.record(stream)
-        torch.cuda.synchronize()
-        step_ms.append(a.elapsed_time(b))
-    torch.cuda.synchronize()
+    pipe = q.pipeline(args.steps, args.warmup, flush, clocks)
     # e2e: pump_plan with host buffers (includes roadmap + online + search)
-    e2e_ms, plan_res = [], None
-    for _ in range(max(1, args.steps)):
-        t0 = time.perf_counter()
-        plan_res = plan(False)
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms, plan_res = q.e2e(args.steps)
     clk = clocks.stop()
     if dist:
         dist.barrier()
-    all_units, (tot, tot_e2e) = aggregate(dist, units, [sum(step_ms), sum(e2e_ms)], "cuda")
-    ks = {k: sum(a.elapsed_time(b) for a, b in v) / args.steps for k, v in kernel_ms.items()}
+    units, E, M_total, W = pipe["units"], pipe["E"], pipe["M"], pipe["W"]
+    all_units, (tot, tot_e2e) = aggregate(dist, units, [sum(pipe["step_ms"]), sum(e2e_ms)], "cuda")
+    ks = pipe["kernel_ms"]
     out = None
     if rank == 0:
         value = all_units * args.steps / (tot / 1e3)
@@ -561,7 +626,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded indoor map, Halton samples)",
-            "config": {"workload": WORKLOAD, "N": N, "obstacles": int(obs_host.shape[0]),
+            "config": {"workload": WORKLOAD, "N": N, "obstacles": int(q.obs.shape[0]),
                        "hsmc_particles": P, "waypoints_per_edge": W, "noise_mult": 2e-3,
                        "cp_target": 0.01, "eta": 2, "bvp": args.mode, "edges": E,
                        "expansions": M_total, "units_per_step": units,
@@ -581,13 +646,21 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(plan_res.h2d_bytes),
                     "d2h_bytes_per_step": int(plan_res.d2h_bytes)},
-            "gpu_launches": launches["n"],
+            "gpu_launches": pipe["launches"],
             "clocks": clk,
         }
-        out["roofline"] = roofline(dom, ks, N, E, M_total, W, maxHS, P, args.mode,
+        out["roofline"] = roofline(dom, ks, N, E, M_total, W, pipe["maxHS"], P, args.mode,
                                    fp64_peak_tflops(torch), float(clk.get("sm_mhz") or 2070.0))
         if args.batch > 0:
-            out["queries_per_s"] = measure_queries(args, lib, L, ctx)
+            out["queries_per_s"] = measure_queries(args, lib, L, ctx, args.mode)
+        # the two arithmetics that are bit-exact with a build of the reference,
+        # on the same workload
+        if not args.no_parity and args.mode == "precision":
+            out["parity"] = mode_record(lib, L, ctx, torch, w, "parity", args, flush, batch=args.batch)
+            out["parity_gpu"] = mode_record(lib, L, ctx, torch, w, "parity_gpu", args, flush, batch=0,
+                                            steps=2, warmup=1)
+        if not args.no_large and args.mode == "precision":
+            out["large"] = large_record(lib, L, ctx, torch, flush)
         if not args.no_refine:
             out["refine"] = measure_refine(args, lib, L, ctx, torch)
         if not args.no_cpu_baseline:
@@ -598,6 +671,74 @@ def run_ours(args):
     if dist:
         dist.destroy_process_group()
     return out
+
+
+BIT_EXACT_AGAINST = {
+    "parity": "the reference program built for the CPU (x86 host arithmetic, no contraction): "
+              "whole queries match tests/golden/ref_*.npz bit for bit",
+    "parity_gpu": "the reference's own fillCoptsTopts on the GB300 for the pair matrix, its host "
+                  "arithmetic elsewhere: whole queries match tests/golden/refgpu_*.npz bit for bit",
+}
+
+
+def large_record(lib, L, ctx, torch, flush):
+    """The large configuration (N = 32000, 200 boxes with sides U[0.02, 0.1],
+    noise 5e-3, 4096 particles for HSMC and MC CP, 16 waypoints per edge,
+    CP target 0.005, eta 2, precision BVP): one step of the device pipeline
+    after one warm-up, and the plan latency.  The reference cannot run it
+    unmodified (its sample count is a compile-time array size and its
+    particle tables hold 2048 particles), so it has no CPU baseline here."""
+    from pump_gb300 import workloads
+    cfg = workloads.CONFIGS["cfg4"]
+    w = dict(N=cfg["N"], obstacles=cfg["obstacles"](0), offset_mult=np.float32(cfg["offset_mult"]),
+             cp=cfg["cp"], eta=cfg["eta"], num_disc=cfg["num_disc"], P=cfg["num_hsmc"],
+             num_mc=cfg["num_mc"])
+    q = Query(lib, L, ctx, torch, w, "precision")
+    pipe = q.pipeline(1, 1, flush)
+    e2e_ms, res = q.e2e(2)
+    ks = pipe["kernel_ms"]
+    N, E = w["N"], pipe["E"]
+    return {"config": {"workload": "large32000", "N": N, "obstacles": int(q.obs.shape[0]),
+                       "hsmc_particles": w["P"], "mc_particles": w["num_mc"],
+                       "waypoints_per_edge": w["num_disc"] + 1, "noise_mult": 5e-3, "cp_target": 0.005,
+                       "eta": 2, "bvp": "precision", "edges": E, "expansions": pipe["M"]},
+            "value": pipe["units"] / (pipe["step_ms"][0] / 1e3), "unit": UNIT,
+            "ms_per_step": pipe["step_ms"][0],
+            "kernel_ms": {k: round(v, 3) for k, v in ks.items()},
+            "edges_per_s": {"bvp": N * (N - 1) / (ks["bvp_pairs"] / 1e3), "cc": E / (ks["free_edges"] / 1e3),
+                            "hsmc": pipe["M"] / (ks["hsmc"] / 1e3) if ks.get("hsmc") else None},
+            "plan_ms": statistics.median(e2e_ms),
+            "plan_stage_ms": {"roadmap": res.ms_roadmap, "online": res.ms_online,
+                              "explore": res.ms_explore, "search": res.ms_search},
+            "e2e": {"value": pipe["units"] * len(e2e_ms) / (sum(e2e_ms) / 1e3), "unit": UNIT,
+                    "h2d_bytes_per_step": int(res.h2d_bytes), "d2h_bytes_per_step": int(res.d2h_bytes)},
+            "solution": {"success": int(res.success), "cp": res.soln_cp, "cost": res.soln_cost,
+                         "paths": res.num_paths, "iterations": res.iterations}}
+
+
+def mode_record(lib, L, ctx, torch, w, mode, args, flush, batch, steps=None, warmup=None):
+    """The same workload in one of the bit-exact arithmetics: the device
+    pipeline's edges/s, the plan latency (e2e edges/s) and, with batch > 0,
+    batched vs plain queries/s."""
+    steps = steps or args.steps
+    warmup = warmup or args.warmup
+    q = Query(lib, L, ctx, torch, w, mode)
+    pipe = q.pipeline(steps, warmup, flush)
+    e2e_ms, res = q.e2e(steps)
+    ks = pipe["kernel_ms"]
+    rec = {"bvp": mode, "bit_exact_against": BIT_EXACT_AGAINST[mode],
+           "value": pipe["units"] * steps / (sum(pipe["step_ms"]) / 1e3), "unit": UNIT,
+           "ms_per_step": sum(pipe["step_ms"]) / steps,
+           "kernel_ms": {k: round(v, 4) for k, v in ks.items()},
+           "plan_ms": statistics.median(e2e_ms),
+           "e2e": {"value": pipe["units"] * len(e2e_ms) / (sum(e2e_ms) / 1e3), "unit": UNIT,
+                   "h2d_bytes_per_step": int(res.h2d_bytes), "d2h_bytes_per_step": int(res.d2h_bytes)},
+           "edges": pipe["E"], "expansions": pipe["M"],
+           "solution": {"success": int(res.success), "cp": res.soln_cp, "cost": res.soln_cost,
+                        "paths": res.num_paths}}
+    if batch > 0:
+        rec["queries_per_s"] = measure_queries(args, lib, L, ctx, mode)
+    return rec
 
 
 # Binary64 flops per ordered pair of the 2pBVP kernels (a fused multiply-add

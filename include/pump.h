@@ -148,6 +148,14 @@ void pump_tune_enable(int on);
 void pump_tune_reset(void);
 int pump_tune_report(char *buf, size_t len);
 
+/* The reference's Halton samples (createSamplesHalton(0, ...), sampler.cu:20-41,
+ * as mainPUMP.cu:250 calls it): sample n, coordinate d = halton(n, base d)
+ * scaled into [lo[d], hi[d]] in binary32 as the reference evaluates it,
+ * sample 0 = init and sample N-1 = goal; writes d_samples[N][6] on the
+ * device (host arrays of 6 floats for lo, hi, init, goal). */
+pump_status_t pump_halton_samples(int N, const float *lo, const float *hi, const float *init,
+                                  const float *goal, float *d_samples, pump_stream_t stream);
+
 /* ------------------------------------------------------ collision checks */
 /* isFree[i] = sample i is not strictly inside any box (sampleFree,
  * sampler.cu:61-88).  obstacles: numObs x 12 floats (lo[6], hi[6]). */
@@ -415,6 +423,14 @@ typedef struct pump_plan_result {
    * synchronisations), and how many times it waited */
   double ms_wait;
   int num_waits;
+  /* optional caller buffers (either may be NULL): the stored paths' start
+   * times (the reference's pathTime, PUMP.cu:185-240) and their HSMC particle
+   * masks (bit-packed, ceil(num_hsmc / 32) words per path), written when
+   * path_state_cap >= num_paths.  With the exploration trace they give every
+   * HSMC launch's inputs. */
+  float *path_time;
+  uint32_t *path_valid;
+  int path_state_cap;
 } pump_plan_result;
 
 /* Fills a problem with the reference's defaults (mainPUMP.cu:51-72). */

@@ -61,12 +61,12 @@ struct SampleBox {
 };
 
 // sampler.cu:20-41: sample n, dimension d = halton(n, base d) scaled into
-// [lo, hi]; sample 0 is init and sample N-1 the goal, copied exactly.  The
-// goal row is written once more after the N samples.
-__global__ void halton_kernel(int N, SampleBox bx, float *__restrict__ out) {
+// [lo, hi]; sample 0 is init and sample N-1 the goal, copied exactly.  With
+// rows = N + 1 the goal row is written once more after the N samples.
+__global__ void halton_kernel(int N, int rows, SampleBox bx, float *__restrict__ out) {
   const int bases[6] = {2, 3, 5, 7, 11, 13};
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)(N + 1) * kDim) return;
+  if (t >= (long long)rows * kDim) return;
   const int n = (int)(t / kDim), d = (int)(t - (long long)n * kDim);
   float v;
   if (n == 0) v = bx.init[d];
@@ -326,7 +326,9 @@ pump_status_t obstacle_smem(int numObs, size_t *bytes) {
 }  // namespace
 
 pump_status_t halton_samples_async(int N, const float *lo, const float *hi, const float *init,
-                                   const float *goal, float *d_out, cudaStream_t stream) {
+                                   const float *goal, float *d_out, cudaStream_t stream,
+                                   bool goal_row) {
+  const int rows = goal_row ? N + 1 : N;
   SampleBox bx;
   for (int d = 0; d < 6; ++d) {
     bx.lo[d] = lo[d];
@@ -334,13 +336,21 @@ pump_status_t halton_samples_async(int N, const float *lo, const float *hi, cons
     bx.init[d] = init[d];
     bx.goal[d] = goal[d];
   }
-  halton_kernel<<<grid_for((long long)(N + 1) * kDim, 256), 256, 0, stream>>>(N, bx, d_out);
+  halton_kernel<<<grid_for((long long)rows * kDim, 256), 256, 0, stream>>>(N, rows, bx, d_out);
   return launch_status("halton_kernel");
 }
 
 }  // namespace pump
 
 using namespace pump;
+
+extern "C" pump_status_t pump_halton_samples(int N, const float *lo, const float *hi,
+                                             const float *init, const float *goal,
+                                             float *d_samples, pump_stream_t stream) {
+  if (N < 2 || !lo || !hi || !init || !goal || !d_samples)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_halton_samples: bad arguments");
+  return halton_samples_async(N, lo, hi, init, goal, d_samples, (cudaStream_t)stream, false);
+}
 
 extern "C" pump_status_t pump_sample_free(const float *d_obstacles, int numObs,
                                           const float *d_samples, int N, uint8_t *d_is_free,

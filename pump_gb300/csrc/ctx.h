@@ -200,10 +200,11 @@ pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const 
                                const int *copy_src = nullptr, int *copy_dst = nullptr,
                                int copy_words = 0, unsigned int *done = nullptr,
                                unsigned int seq = 0);
-// Halton samples of a query (sampler.cu:20-41), N x 6, then the goal row
-// once more.
+// Halton samples of a query (sampler.cu:20-41), N x 6, then (goal_row) the
+// goal row once more.
 pump_status_t halton_samples_async(int N, const float *lo, const float *hi, const float *init,
-                                   const float *goal, float *d_out, cudaStream_t stream);
+                                   const float *goal, float *d_out, cudaStream_t stream,
+                                   bool goal_row = true);
 // The 4N-6 pairs of a query that touch its init or goal sample, as explicit
 // (x0, x1) rows: init row (0 -> j, j = 1 .. N-1), init column (i -> 0),
 // goal row (N-1 -> j, j = 1 .. N-2), goal column (i -> N-1).

@@ -779,6 +779,19 @@ pump_status_t Planner::explore() {
   PUMP_CUDA_TRY(cudaMemcpyAsync(hp + np, d_node.p, sizeof(int) * np, cudaMemcpyDeviceToHost, s_));
   PUMP_CUDA_TRY(cudaMemcpyAsync(hp + 2 * np, d_cost.p, sizeof(float) * np, cudaMemcpyDeviceToHost, s_));
   PUMP_CUDA_TRY(cudaMemcpyAsync(hp + 3 * np, d_err_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
+  // the stored paths' times and particle masks, when the caller asked for them
+  if (np > 0 && res_->path_state_cap >= (int)np) {
+    if (res_->path_time) {
+      PUMP_CUDA_TRY(cudaMemcpyAsync(res_->path_time, d_pathTime_.p, sizeof(float) * np,
+                                    cudaMemcpyDeviceToHost, s_));
+      res_->d2h_bytes += (long long)(sizeof(float) * np);
+    }
+    if (res_->path_valid) {
+      PUMP_CUDA_TRY(cudaMemcpyAsync(res_->path_valid, d_valid_.p, sizeof(uint32_t) * np * words_,
+                                    cudaMemcpyDeviceToHost, s_));
+      res_->d2h_bytes += (long long)(sizeof(uint32_t) * np * words_);
+    }
+  }
   PUMP_TRY(sync());
   pathPrev_.assign(hp, hp + np);
   pathNode_.assign(hp + np, hp + 2 * np);
@@ -1486,7 +1499,13 @@ pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *
   long long trace_cap = res->wf_trace_cap;
   float *ctrl = res->ctrl_path;
   int ctrl_cap = res->ctrl_cap;
+  float *ptime = res->path_time;
+  uint32_t *pvalid = res->path_valid;
+  const int pstate_cap = res->path_state_cap;
   std::memset(res, 0, sizeof *res);
+  res->path_time = ptime;
+  res->path_valid = pvalid;
+  res->path_state_cap = pstate_cap;
   res->ctrl_path = ctrl;
   res->ctrl_cap = ctrl ? ctrl_cap : 0;
   res->path = path;

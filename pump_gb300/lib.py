@@ -77,6 +77,7 @@ class PlanResult(C.Structure):
         ("ctrl_path", vp), ("ctrl_cap", i32), ("ctrl_len", i32),
         ("refine_cp", f32), ("refine_cost", f32), ("refined", i32),
         ("ms_explore_wait", C.c_double), ("ms_wait", C.c_double), ("num_waits", i32),
+        ("path_time", vp), ("path_valid", vp), ("path_state_cap", i32),
     ]
 
 
@@ -110,6 +111,7 @@ _SIGS = {
     "pump_frontier_compact": (i32, [vp, vp, i32, vp, vp, vp]),
     "pump_frontier_compact_noalloc": (i32, [vp, i32, vp, vp, vp]),
     "pump_selftest_wait": (i32, [vp, i64, vp]),
+    "pump_halton_samples": (i32, [i32, vp, vp, vp, vp, vp, vp]),
     "pump_problem_defaults": (None, [C.POINTER(Problem)]),
     "pump_read_input": (i32, [C.c_char_p, C.POINTER(Problem)]),
     "pump_plan": (i32, [vp, C.POINTER(Problem), C.POINTER(PlanResult), vp]),

@@ -13,6 +13,7 @@ produce the workloads the benchmarks are quoted on, seeded and reproducible:
 - ``indoor`` -- the same bounds with 30 walls 0.02 thick and U[0.3,1] long on
   the lines of a 4 x 4 room grid (full height), plus 10 boxes with sides
   U[0.05,0.15].
+- ``large_boxes`` -- 200 boxes with centres U[0,1] and sides U[0.02,0.1].
 
 Boxes that contain the init or goal position are redrawn.  Seeds follow
 1000 * config + query.
@@ -130,10 +131,19 @@ def perturbed_paths(n_paths, seed, obstacles, n_range=(8, 40), spread=0.05, spee
     return np.concatenate(rows), np.asarray(offs, np.int32), np.asarray(cnts, np.int32)
 
 
+def large_boxes(seed, n=200):
+    """The large configuration's map: n boxes with position centres U[0, 1]
+    and sides U[0.02, 0.1] (spanning the velocity range)."""
+    return random_boxes(n, seed, side=(0.02, 0.1), centre=(0.0, 1.0))
+
+
 CONFIGS = {
     # the benchmark configurations (N, obstacles, noise, cp, eta, particles, waypoints)
     "cfg0": dict(N=1000, num_disc=9, num_hsmc=128, offset_mult=1e-3, cp=0.01, eta=2.0,
                  obstacles=lambda q=0: random_boxes(10, 1000 * 0 + q)),
     "cfg1": dict(N=4000, num_disc=8, num_hsmc=1024, offset_mult=2e-3, cp=0.01, eta=2.0,
                  obstacles=lambda q=0: indoor(1000 * 1 + q)),
+    # the large configuration: 4096 particles for HSMC and for the Monte Carlo CP
+    "cfg4": dict(N=32000, num_disc=15, num_hsmc=4096, num_mc=4096, offset_mult=5e-3, cp=0.005,
+                 eta=2.0, obstacles=lambda q=0: large_boxes(1000 * 4 + q)),
 }

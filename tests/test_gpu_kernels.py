@@ -691,3 +691,22 @@ def test_mc_cp_binary32_vs_binary64(gpu, pumplib, oracle):
         h64 = np.array([oracle.mccp64(p, p.shape[0], pm, np.float32(om), obs) for p in paths])
         assert np.all(np.abs(h32 - h64) <= 2), (om, np.abs(h32 - h64).max())
         assert np.count_nonzero(h64) > 10
+
+
+@pytest.mark.parametrize("N", [2, 1000, 4001])
+def test_halton_samples(N, gpu, pumplib, oracle, goldens):
+    """pump_halton_samples: the reference's Halton samples (createSamplesHalton,
+    sampler.cu:20-41) bit for bit, init first and goal last; nothing written
+    past the N rows."""
+    torch, _ = gpu
+    _, _, init, goal, lo, hi, _ = golden_problem(goldens, "ref_N1000_input")
+    f6 = lambda v: (C.c_float * 6)(*[float(x) for x in v])  # noqa: E731
+    d = empty(torch, N * 6 + 6, torch.float32)
+    d.fill_(7.0)
+    pumplib.check(pumplib.load().pump_halton_samples(N, f6(lo), f6(hi), f6(init), f6(goal), ptr(d),
+                                                     stream(torch)))
+    got = host(d)
+    assert same_bits(got[: N * 6].reshape(N, 6), oracle.halton_samples(N, init, goal, lo, hi))
+    assert np.all(got[N * 6:] == 7.0)
+    if N == 1000:
+        assert same_bits(got[: N * 6].reshape(N, 6), goldens["ref_N1000_input"]["samples"])

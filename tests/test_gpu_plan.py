@@ -255,3 +255,30 @@ def test_plan_batch_equals_single_large(gpu, pumplib):
         assert sts[k] == st1
         assert _fields(res[k]) == _fields(r1)
         assert np.array_equal(paths[k][: res[k].path_len].view(np.uint32), p1.view(np.uint32))
+
+
+def test_plan_path_state_readback(gpu, pumplib, goldens):
+    """The stored paths' times and particle masks a caller can ask for
+    (pump_plan_result.path_time / path_valid): path 0 is the initial node at
+    time 0 with every particle valid, every time lies inside the particle
+    table, every stored path passed the CP cut-off (its invalid fraction,
+    as calculateCP_HSMC computes it, is at most cpTarget * cpFactor,
+    PUMP.cu:12, 175-178), and the query's other results are unchanged."""
+    torch, ctx = gpu
+    L = pumplib.load()
+    g = goldens["ref_N1000_boxes10_noise0.3"]
+    pb, _obs = make_problem(pumplib, g)
+    st, res, path, _n = run_plan(pumplib, ctx, pb)
+    n, P = res.num_paths, pb.num_hsmc
+    words = (P + 31) // 32
+    ptime = np.zeros(n, np.float32)
+    pvalid = np.zeros(n * words, np.uint32)
+    res2 = pumplib.PlanResult()
+    res2.path_time, res2.path_valid, res2.path_state_cap = ptime.ctypes.data, pvalid.ctypes.data, n
+    assert L.pump_plan(ctx.handle, C.byref(pb), C.byref(res2), None) == st
+    assert (res2.num_paths, res2.soln_path_idx) == (n, res.soln_path_idx)
+    assert ptime[0] == 0 and np.all(pvalid[:words] == 0xFFFFFFFF)
+    assert np.all(ptime[1:] > 0) and np.all(ptime < 0.05 * (pb.table_rows - 1))
+    valid = np.unpackbits(pvalid.view(np.uint8).reshape(n, -1), axis=1, bitorder="little")[:, :P]
+    cp = (P - valid.sum(1)).astype(np.float32) / np.float32(P)
+    assert np.all(cp <= np.float32(pb.cp_target) * np.float32(pb.cp_factor))
