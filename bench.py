@@ -175,7 +175,8 @@ def cpu_query(args, query=0):
 def measure_queries(args, lib, L, ctx, mode):
     """Batched vs plain queries/s on the batched workload (256 queries, N
     log-uniform in [500, 8000], 5-100 boxes, init/goal in free space, CP
-    target in {0.001, 0.01, 0.05}, eta in {1, 2, 4}).  Plain: one pump_plan
+    target in {0.001, 0.01, 0.05}, eta in {1, 2, 4}, 4-32 waypoints per edge
+    by edge length).  Plain: one pump_plan
     after another on one stream; batched: pump_plan_batch.  A query counts
     only when it returns a path whose Monte Carlo CP is below its target."""
     from pump_gb300 import workloads
@@ -193,6 +194,7 @@ def measure_queries(args, lib, L, ctx, mode):
             pb.lo[d], pb.hi[d] = workloads.LO[d], workloads.HI[d]
         pb.offset_mult, pb.cp_target, pb.cp_factor = float(q["offset_mult"]), q["cp"], q["eta"]
         pb.bvp_mode = Query.MODES[mode]
+        pb.num_disc, pb.disc_len, pb.disc_min = q["num_disc"], q["disc_len"], q["disc_min"]
     paths = {}
 
     def results(tag):
@@ -236,7 +238,8 @@ def measure_queries(args, lib, L, ctx, mode):
                                   paths["batched"][k][: res_b[k].path_len].view(np.uint32))
                for k in range(len(qs)))
     ok_p, ok_b = ok(res_p, sts_p), ok(res_b, sts_b)
-    return {"workload": "batch256: N log-uniform [500, 8000], 5-100 boxes, noise 1e-3",
+    return {"workload": "batch256: N log-uniform [500, 8000], 5-100 boxes, noise 1e-3, waypoints "
+                        "per edge by edge length (at most 0.025 apart, 4 to 32)",
             "bvp": mode, "queries": len(qs), "met_cp_target": ok_b, "workers": workers,
             "plain_queries_per_s": ok_p / t_plain, "batched_queries_per_s": ok_b / t_batch,
             "batched_over_plain": (ok_b / t_batch) / (ok_p / t_plain) if ok_p else None,
@@ -439,7 +442,7 @@ class Query:
         res = lib.PlanResult()
         res.path, res.path_cap = self.path.ctypes.data, pb.table_rows
         if trace:
-            self.trace_buf = np.zeros(2 * 40_000_000, np.int32)
+            self.trace_buf = np.zeros(self.trace_cap, np.int32)
             res.wf_trace, res.wf_trace_cap = self.trace_buf.ctypes.data, self.trace_buf.size
         if paths_cap:
             self.ptime = np.zeros(paths_cap, np.float32)
@@ -459,7 +462,9 @@ class Query:
         stream = torch.cuda.current_stream()
         sh = stream.cuda_stream
         res0 = self.plan()
+        self.trace_cap = 2 * int(res0.num_considered) + 2
         res0 = self.plan(trace=True, paths_cap=max(1, int(res0.num_paths)))
+        assert res0.wf_trace_len == 2 * res0.num_considered, "exploration trace truncated"
         N, P, W = w["N"], w["P"], w["num_disc"] + 1
         E = int(res0.num_edges)
         nobs = self.obs.shape[0]
@@ -660,7 +665,10 @@ def run_ours(args):
             out["parity_gpu"] = mode_record(lib, L, ctx, torch, w, "parity_gpu", args, flush, batch=0,
                                             steps=2, warmup=1)
         if not args.no_large and args.mode == "precision":
-            out["large"] = large_record(lib, L, ctx, torch, flush)
+            try:
+                out["large"] = large_record(lib, L, ctx, torch, flush)
+            except lib.PumpError as e:  # reported, not fatal to the headline
+                out["large"] = {"config": {"workload": "large32000"}, "error": str(e)}
         if not args.no_refine:
             out["refine"] = measure_refine(args, lib, L, ctx, torch)
         if not args.no_cpu_baseline:

@@ -132,6 +132,26 @@ pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src, co
                                     const float *d_topt, long long E, int numDisc, int mode,
                                     float *d_disc, pump_stream_t stream);
 
+/* Waypoint counts by edge length and the ragged waypoint layout (no
+ * counterpart in the reference, whose numDisc is one value per problem,
+ * mainPUMP.cu:57).  Edge e (d_src[e] -> d_dst[e]) gets numDisc_e =
+ * ceil(L_e / disc_len) clamped to [min_disc, max_disc] (max_disc for every
+ * edge when disc_len <= 0), L_e = sqrtf((dx*dx + dy*dy) + dz*dz) of its end
+ * positions in binary32.  Writes d_off[E + 1]: edge e's waypoints are
+ * records d_off[e] .. d_off[e+1]-1 (numDisc_e + 1 of them) of a waypoint
+ * array, and *h_total = d_off[E].  Synchronises. */
+pump_status_t pump_disc_offsets(const float *d_samples, const int *d_src, const int *d_dst,
+                                long long E, float disc_len, int min_disc, int max_disc,
+                                long long *d_off, long long *h_total, pump_stream_t stream);
+
+/* pump_discretize_edges over the ragged layout: numDisc_e + 1 waypoints of
+ * edge e at records d_off[e] .. of d_disc (numDisc_e <= max_disc).  An edge
+ * whose count lies outside [2, max_disc + 1] is PUMP_ERR_BAD_INPUT (its
+ * block writes nothing).  Synchronises. */
+pump_status_t pump_discretize_edges_off(const float *d_samples, const int *d_src, const int *d_dst,
+                                        const float *d_topt, long long E, const long long *d_off,
+                                        int max_disc, int mode, float *d_disc, pump_stream_t stream);
+
 /* -------------------------------------------------------------- tuning */
 /* Launch-shape autotuner.  Kernels with several launch shapes that compute
  * the same results (the precision pair BVP's, the waypoints' and the edge
@@ -166,6 +186,13 @@ pump_status_t pump_sample_free(const float *d_obstacles, int numObs, const float
  * (freeEdges, collisionCheck.cu:5-37, isMotionValid :65-143). */
 pump_status_t pump_free_edges(const float *d_obstacles, int numObs, const float *d_disc,
                               long long E, int numDisc, uint8_t *d_is_free, pump_stream_t stream);
+
+/* pump_free_edges over the ragged layout of pump_disc_offsets (each edge's
+ * own segments).  PUMP_ERR_BAD_INPUT for an edge count outside
+ * [2, max_disc + 1].  Synchronises. */
+pump_status_t pump_free_edges_off(const float *d_obstacles, int numObs, const float *d_disc,
+                                  const long long *d_off, long long E, int max_disc,
+                                  uint8_t *d_is_free, pump_stream_t stream);
 
 /* Half-spaces of every waypoint of free edges: setupAsBs (hsmc.cu:201-211)
  * then cacheHalfspaces (hsmc.cu:10-99).  as[E][W][maxHS][3], bs[E][W][maxHS],
@@ -231,6 +258,21 @@ pump_status_t pump_hsmc_propagate_boxes(int num_new, int W, const int *d_edge, c
                                         const float *d_offsets_t, int Pmc, int T_rows,
                                         float offset_mult, uint32_t *d_valid, int P,
                                         float *d_path_cp, int *d_error, pump_stream_t stream);
+
+/* pump_hsmc_propagate_boxes over the ragged layout: each edge's waypoints
+ * are records d_disc_off[e] .. d_disc_off[e+1]-1 of d_disc (2 .. max_w of
+ * them; an edge outside that range records PUMP_ERR_BAD_INPUT in *d_error
+ * and its path is skipped), and its waypoint times are t + i * topt /
+ * (W_e - 1).  max_w * maxHS <= 256. */
+pump_status_t pump_hsmc_propagate_boxes_off(int num_new, int max_w, const int *d_edge,
+                                            const int *d_prev, long long num_edges, int base,
+                                            const float *d_obstacles, int numObs,
+                                            const float *d_disc, const long long *d_disc_off,
+                                            float maxd2, int maxHS, const float *d_times,
+                                            const float *d_topt, float dt,
+                                            const float *d_offsets_t, int Pmc, int T_rows,
+                                            float offset_mult, uint32_t *d_valid, int P,
+                                            float *d_path_cp, int *d_error, pump_stream_t stream);
 
 /* Full Monte Carlo collision probability of n_paths dense paths at once
  * (MCCP + thrust::reduce, collisionProbability.cu:4-92).  Path k has
@@ -373,8 +415,14 @@ typedef struct pump_problem {
   float refine_lambda; /* bound weight of the refinement (default 10) */
   int max_paths;      /* stored-path capacity; 0 (default) = the reference's
                          maxPathCount = (int)(2 N sqrt(N)) (mainPUMP.cu:623).  The
-                         reference overruns its arrays past it (PUMP.cu:62-76);
+                         reference ends the search past it (PUMP.cu:62-76);
                          here the query ends with PUMP_ERR_CAPACITY */
+  float disc_len;     /* > 0: waypoints per edge by edge length (no counterpart in
+                         the reference, which uses num_disc for every edge):
+                         edge e gets numDisc_e = ceil(L_e / disc_len) clamped to
+                         [disc_min, num_disc], L_e the binary32 distance of its end
+                         positions (pump_disc_offsets); 0 (default): num_disc */
+  int disc_min;       /* the smallest per-edge numDisc (default 3, 4 waypoints) */
 } pump_problem;
 
 typedef struct pump_plan_result {

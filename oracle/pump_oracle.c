@@ -492,12 +492,54 @@ long long orc_build_edges(int N, const float *copts, const float *topts, float r
   return e;
 }
 
-void orc_discretize_edges(long long E, const int *src, const int *dst, const float *samples,
-                          int numDisc, float *disc) {
+/* Per-edge waypoint counts by edge length (no counterpart in the reference,
+ * whose numDisc is one value per problem, mainPUMP.cu:57): with discLen > 0,
+ * numDisc_e = ceil(L_e / discLen) clamped to [minDisc, maxDisc], L_e the
+ * binary32 distance between the edge's end positions, sqrtf((dx*dx + dy*dy)
+ * + dz*dz) with d = p1 - p0; otherwise every edge has maxDisc.  Writes
+ * off[e] = sum over e' < e of (numDisc_e' + 1), off[E] included; returns
+ * off[E]. */
+static int disc_count(const float *x0, const float *x1, float discLen, int minDisc, int maxDisc) {
+  if (!(discLen > 0)) return maxDisc;
+  const float dx = x1[0] - x0[0], dy = x1[1] - x0[1], dz = x1[2] - x0[2];
+  const float L = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float q = ceilf(L / discLen);
+  if (!(q >= (float)minDisc)) return minDisc; /* also NaN */
+  if (q > (float)maxDisc) return maxDisc;
+  return (int)q;
+}
+
+long long orc_disc_offsets(long long E, const int *src, const int *dst, const float *samples,
+                           float discLen, int minDisc, int maxDisc, long long *off) {
+  long long t = 0;
+  for (long long e = 0; e < E; ++e) {
+    off[e] = t;
+    t += disc_count(&samples[src[e] * ORC_DIM], &samples[dst[e] * ORC_DIM], discLen, minDisc,
+                    maxDisc) + 1;
+  }
+  off[E] = t;
+  return t;
+}
+
+static long long *uniform_offsets(long long E, int W) {
+  long long *off = (long long *)malloc(sizeof(long long) * (E + 1));
+  for (long long e = 0; e <= E; ++e) off[e] = e * W;
+  return off;
+}
+
+void orc_discretize_edges_off(long long E, const int *src, const int *dst, const float *samples,
+                              const long long *off, float *disc) {
 #pragma omp parallel for schedule(dynamic, 256)
   for (long long e = 0; e < E; ++e)
-    orc_find_discretized_path(&disc[e * (numDisc + 1) * ORC_DIM], &samples[src[e] * ORC_DIM],
-                              &samples[dst[e] * ORC_DIM], numDisc);
+    orc_find_discretized_path(&disc[off[e] * ORC_DIM], &samples[src[e] * ORC_DIM],
+                              &samples[dst[e] * ORC_DIM], (int)(off[e + 1] - off[e] - 1));
+}
+
+void orc_discretize_edges(long long E, const int *src, const int *dst, const float *samples,
+                          int numDisc, float *disc) {
+  long long *off = uniform_offsets(E, numDisc + 1);
+  orc_discretize_edges_off(E, src, dst, samples, off, disc);
+  free(off);
 }
 
 void orc_heuristic(int N, const float *samples, const float *goal, float *h) {
@@ -553,33 +595,61 @@ int orc_is_motion_valid(const float *v, const float *w, int nobs, const float *o
   return 1;
 }
 
-void orc_free_edges(long long E, int numDisc, const float *disc, int nobs, const float *obs,
-                    uint8_t *isFreeEdge) {
+void orc_free_edges_off(long long E, const long long *off, const float *disc, int nobs,
+                        const float *obs, uint8_t *isFreeEdge) {
 #pragma omp parallel for schedule(dynamic, 256)
   for (long long e = 0; e < E; ++e) {
     int ok = 1;
+    const int numDisc = (int)(off[e + 1] - off[e] - 1);
     for (int i = 0; i < numDisc && ok; ++i) {
-      const float *v = &disc[(e * (numDisc + 1) + i) * ORC_DIM];
+      const float *v = &disc[(off[e] + i) * ORC_DIM];
       ok = orc_is_motion_valid(v, v + ORC_DIM, nobs, obs);
     }
     isFreeEdge[e] = (uint8_t)ok;
   }
 }
 
+void orc_free_edges(long long E, int numDisc, const float *disc, int nobs, const float *obs,
+                    uint8_t *isFreeEdge) {
+  long long *off = uniform_offsets(E, numDisc + 1);
+  orc_free_edges_off(E, off, disc, nobs, obs, isFreeEdge);
+  free(off);
+}
+
 /* ======================================================================
  * Half-spaces (hsmc.cu, bvls.cu:259-273)
  * ==================================================================== */
-void orc_cache_halfspaces(long long E, int W, const float *disc, const uint8_t *isFreeEdge,
-                          int nobs, const float *obs, int maxHS, float maxd2, float *as,
-                          float *bs, int *count) {
-  const long long nhs = E * W * maxHS;
+static void halfspaces_of_waypoint(long long wp, const float *disc, int nobs, const float *obs,
+                                   int maxHS, float maxd2, float *as, float *bs, int *count);
+
+void orc_cache_halfspaces_off(long long E, const long long *off, const float *disc,
+                              const uint8_t *isFreeEdge, int nobs, const float *obs, int maxHS,
+                              float maxd2, float *as, float *bs, int *count) {
+  const long long nhs = off[E] * maxHS;
   for (long long i = 0; i < nhs; ++i) {
     as[i * 3 + 0] = -1; as[i * 3 + 1] = -1; as[i * 3 + 2] = -1;
     bs[i] = 1111;
   }
-#pragma omp parallel for schedule(dynamic, 1024)
-  for (long long wp = 0; wp < E * W; ++wp) {
-    if (!isFreeEdge[wp / W]) continue;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long e = 0; e < E; ++e) {
+    if (!isFreeEdge[e]) continue;
+    for (long long wp = off[e]; wp < off[e + 1]; ++wp)
+      halfspaces_of_waypoint(wp, disc, nobs, obs, maxHS, maxd2, as, bs, count);
+  }
+}
+
+void orc_cache_halfspaces(long long E, int W, const float *disc, const uint8_t *isFreeEdge,
+                          int nobs, const float *obs, int maxHS, float maxd2, float *as,
+                          float *bs, int *count) {
+  long long *off = uniform_offsets(E, W);
+  orc_cache_halfspaces_off(E, off, disc, isFreeEdge, nobs, obs, maxHS, maxd2, as, bs, count);
+  free(off);
+}
+
+/* cacheHalfspaces (hsmc.cu:10-99) for one waypoint of a free edge */
+static void halfspaces_of_waypoint(long long wp, const float *disc, int nobs, const float *obs,
+                                   int maxHS, float maxd2, float *as, float *bs, int *count) {
+  {
     const float *pos = &disc[wp * ORC_DIM], *vel = pos + 3;
     long long hsIdx = wp * maxHS;
     int stored = 0;
@@ -620,19 +690,20 @@ void orc_cache_halfspaces(long long E, int W, const float *disc, const uint8_t *
 /* ======================================================================
  * HSMC propagation and CP (PUMP.cu:613-655, 745-758)
  * ==================================================================== */
-void orc_hsmc_propagate(int numNew, int W, const int *wfEdge, const int *wfPrev, int base,
-                        const float *as, const float *bs, const float *times, const float *topts,
-                        float dt, int maxHS, const float *offsetsT, float offsetMult, int Pmc,
-                        uint8_t *valid, int P, float *pathCP) {
+void orc_hsmc_propagate_off(int numNew, const long long *off, const int *wfEdge, const int *wfPrev,
+                            int base, const float *as, const float *bs, const float *times,
+                            const float *topts, float dt, int maxHS, const float *offsetsT,
+                            float offsetMult, int Pmc, uint8_t *valid, int P, float *pathCP) {
 #pragma omp parallel for schedule(dynamic, 16)
   for (int w = 0; w < numNew; ++w) {
     const int edge = wfEdge[w], prev = wfPrev[w];
     const long long pathIdx = (long long)base + w;
+    const int W = (int)(off[edge + 1] - off[edge]);
     int collisions = 0;
     for (int p = 0; p < P; ++p) {
       int vp = valid[(long long)prev * P + p];
       float dtLocal = topts[edge] / (W - 1);
-      long long hsHead = (long long)edge * W * maxHS;
+      long long hsHead = off[edge] * maxHS;
       for (int i = 0; i < W; ++i) {
         float time = times[prev] + i * dtLocal;
         int dtIdx = (int)(time / dt);
@@ -650,6 +721,19 @@ void orc_hsmc_propagate(int numNew, int W, const int *wfEdge, const int *wfPrev,
     }
     if (pathCP) pathCP[pathIdx] = ((float)collisions) / P;
   }
+}
+
+void orc_hsmc_propagate(int numNew, int W, const int *wfEdge, const int *wfPrev, int base,
+                        const float *as, const float *bs, const float *times, const float *topts,
+                        float dt, int maxHS, const float *offsetsT, float offsetMult, int Pmc,
+                        uint8_t *valid, int P, float *pathCP) {
+  long long E = 0;
+  for (int w = 0; w < numNew; ++w)
+    if (wfEdge[w] + 1 > E) E = wfEdge[w] + 1;
+  long long *off = uniform_offsets(E, W);
+  orc_hsmc_propagate_off(numNew, off, wfEdge, wfPrev, base, as, bs, times, topts, dt, maxHS,
+                         offsetsT, offsetMult, Pmc, valid, P, pathCP);
+  free(off);
 }
 
 /* ======================================================================
@@ -787,7 +871,7 @@ int orc_control_path(const float *xs, int n, float *out, int cap) {
 }
 
 int orc_plan(const orc_problem *pb, orc_result *res) {
-  const int N = pb->N, numDisc = pb->numDisc, W = numDisc + 1, P = pb->P, Pmc = pb->Pmc;
+  const int N = pb->N, numDisc = pb->numDisc, P = pb->P, Pmc = pb->Pmc;
   const int nobs = pb->numObs;
   const float *obs = pb->obstacles;
   const float dt = (float)0.05, lambda = (float)0.5, epsCost = (float)0.0002,
@@ -823,8 +907,11 @@ int orc_plan(const orc_problem *pb, orc_result *res) {
   orc_build_edges(N, copts, topts, rn, src, dst, coptE, toptE);
   free(copts);
   free(topts);
-  float *disc = (float *)malloc(sizeof(float) * (E + 1) * W * ORC_DIM);
-  orc_discretize_edges(E, src, dst, samples, numDisc, disc);
+  /* waypoints (mainPUMP.cu:327-346): numDisc per edge, or by edge length */
+  long long *off = (long long *)malloc(sizeof(long long) * (E + 1));
+  const long long nwp = orc_disc_offsets(E, src, dst, samples, pb->discLen, pb->discMin, numDisc, off);
+  float *disc = (float *)malloc(sizeof(float) * (nwp + 1) * ORC_DIM);
+  orc_discretize_edges_off(E, src, dst, samples, off, disc);
   float *h = (float *)malloc(sizeof(float) * N);
   orc_heuristic(N, samples, pb->goal, h);
 
@@ -838,11 +925,11 @@ int orc_plan(const orc_problem *pb, orc_result *res) {
   uint8_t *isFreeS = (uint8_t *)malloc(N);
   orc_sample_free(N, samples, nobs, obs, isFreeS);
   uint8_t *isFreeE = (uint8_t *)malloc(E + 1);
-  orc_free_edges(E, numDisc, disc, nobs, obs, isFreeE);
-  float *as = (float *)malloc(sizeof(float) * ((E * W * maxHS) * 3 + 1));
-  float *bs = (float *)malloc(sizeof(float) * (E * W * maxHS + 1));
-  int *cnt = (int *)calloc(E * W + 1, sizeof(int));
-  orc_cache_halfspaces(E, W, disc, isFreeE, nobs, obs, maxHS, maxd2, as, bs, cnt);
+  orc_free_edges_off(E, off, disc, nobs, obs, isFreeE);
+  float *as = (float *)malloc(sizeof(float) * ((nwp * maxHS) * 3 + 1));
+  float *bs = (float *)malloc(sizeof(float) * (nwp * maxHS + 1));
+  int *cnt = (int *)calloc(nwp + 1, sizeof(int));
+  orc_cache_halfspaces_off(E, off, disc, isFreeE, nobs, obs, maxHS, maxd2, as, bs, cnt);
   free(cnt);
 
   /* exploration state (mainPUMP.cu:623-681) */
@@ -918,7 +1005,7 @@ int orc_plan(const orc_problem *pb, orc_result *res) {
     numConsidered += numNew;
 
     /* PUMP.cu:94-160: device propagation reads the device copy of path times */
-    orc_hsmc_propagate(numNew, W, wfEdge, wfPrev, numPaths, as, bs, d_pathTime, toptE, dt, maxHS,
+    orc_hsmc_propagate_off(numNew, off, wfEdge, wfPrev, numPaths, as, bs, d_pathTime, toptE, dt, maxHS,
                        pb->tmajor, pb->offsetMult, Pmc, valid, P, d_pathCP);
     for (int i = 0; i < numNew; ++i) pathCP[numPaths + i] = d_pathCP[numPaths + i];
 
@@ -1116,7 +1203,7 @@ int orc_plan(const orc_problem *pb, orc_result *res) {
     res->ctrlLen = orc_control_path(xsFinal, pathNumSamples, res->ctrl_path, res->ctrl_path ? res->ctrl_cap : 0);
   free(xsFinal);
 
-  free(samples); free(src); free(dst); free(coptE); free(toptE); free(disc); free(h);
+  free(samples); free(src); free(dst); free(coptE); free(toptE); free(disc); free(h); free(off);
   free(goStart); free(isFreeS); free(isFreeE); free(as); free(bs);
   free(Ptab); free(Pcounts); free(pathPrev); free(pathNode); free(pathCost); free(pathTime);
   free(pathCP); free(d_pathTime); free(d_pathCP); free(G); free(valid); free(wfPrev);

@@ -91,6 +91,26 @@ long long orc_build_edges(int N, const float *copts, const float *topts, float r
 /* Waypoints of every edge (mainPUMP.cu:339): disc[E][numDisc+1][6]. */
 void orc_discretize_edges(long long E, const int *src, const int *dst, const float *samples,
                           int numDisc, float *disc);
+/* Per-edge waypoint counts by edge length (no reference counterpart; the
+ * reference uses one numDisc per problem): numDisc_e = ceil(L_e / discLen)
+ * clamped to [minDisc, maxDisc] (maxDisc everywhere when discLen <= 0), L_e
+ * = sqrtf((dx*dx + dy*dy) + dz*dz) of the end positions in binary32.  off[e]
+ * is edge e's first waypoint, off[E] the total (returned). */
+long long orc_disc_offsets(long long E, const int *src, const int *dst, const float *samples,
+                           float discLen, int minDisc, int maxDisc, long long *off);
+/* The waypoint stages over that ragged layout: edge e's waypoints are rows
+ * off[e] .. off[e+1]-1 of disc, its half-spaces rows off[e]*maxHS ... */
+void orc_discretize_edges_off(long long E, const int *src, const int *dst, const float *samples,
+                              const long long *off, float *disc);
+void orc_free_edges_off(long long E, const long long *off, const float *disc, int nobs,
+                        const float *obs, uint8_t *isFreeEdge);
+void orc_cache_halfspaces_off(long long E, const long long *off, const float *disc,
+                              const uint8_t *isFreeEdge, int nobs, const float *obs, int maxHS,
+                              float maxd2, float *as, float *bs, int *count);
+void orc_hsmc_propagate_off(int numNew, const long long *off, const int *wfEdge, const int *wfPrev,
+                            int base, const float *as, const float *bs, const float *times,
+                            const float *topts, float dt, int maxHS, const float *offsetsT,
+                            float offsetMult, int Pmc, uint8_t *valid, int P, float *pathCP);
 /* Heuristic h (mainPUMP.cu:351-355). */
 void orc_heuristic(int N, const float *samples, const float *goal, float *h);
 
@@ -143,6 +163,9 @@ typedef struct orc_problem {
   const float *tmajor;   /* T_table x Pmc x 3 */
   const float *pmajor;   /* Pmc x T_table x 3 */
   const float *samples;  /* optional N x 6; NULL = Halton as the reference */
+  float discLen;         /* > 0: per-edge waypoint counts by edge length (orc_disc_offsets,
+                            numDisc the largest); 0: numDisc on every edge, as the reference */
+  int discMin;           /* the smallest per-edge numDisc */
 } orc_problem;
 
 typedef struct orc_result {

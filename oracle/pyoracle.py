@@ -54,7 +54,7 @@ class Problem(C.Structure):
         ("init", C.c_float * 6), ("goal", C.c_float * 6), ("lo", C.c_float * 6),
         ("hi", C.c_float * 6), ("offsetMult", C.c_float), ("cpTarget", C.c_float),
         ("cpFactor", C.c_float), ("tmajor", C.c_void_p), ("pmajor", C.c_void_p),
-        ("samples", C.c_void_p),
+        ("samples", C.c_void_p), ("discLen", C.c_float), ("discMin", C.c_int),
     ]
 
 
@@ -144,6 +144,16 @@ def lib():
                                                C.POINTER(C.c_double), C.POINTER(C.c_double)]
             L.orc_refine_grad.restype = C.c_double
             L.orc_refine_grad.argtypes = [C.POINTER(RefineArgs), f64p, C.c_int, C.c_double, f64p]
+            L.orc_disc_offsets.restype = C.c_longlong
+            L.orc_disc_offsets.argtypes = [C.c_longlong, i32p, i32p, f32p, C.c_float, C.c_int,
+                                           C.c_int, C.c_void_p]
+            L.orc_discretize_edges_off.argtypes = [C.c_longlong, i32p, i32p, f32p, C.c_void_p, f32p]
+            L.orc_free_edges_off.argtypes = [C.c_longlong, C.c_void_p, f32p, C.c_int, f32p, u8p]
+            L.orc_cache_halfspaces_off.argtypes = [C.c_longlong, C.c_void_p, f32p, u8p, C.c_int, f32p,
+                                                   C.c_int, C.c_float, f32p, f32p, i32p]
+            L.orc_hsmc_propagate_off.argtypes = [C.c_int, C.c_void_p, i32p, i32p, C.c_int, f32p, f32p,
+                                                 f32p, f32p, C.c_float, C.c_int, f32p, C.c_float,
+                                                 C.c_int, u8p, C.c_int, f32p]
             L.orc_plan.restype = C.c_int
             L.orc_plan.argtypes = [C.POINTER(Problem), C.POINTER(Result)]
             _lib = L
@@ -225,6 +235,33 @@ def discretize_edges(src, dst, samples, numDisc):
     return out
 
 
+def disc_offsets(src, dst, samples, discLen, minDisc, maxDisc):
+    """Per-edge waypoint counts by edge length: the first waypoint of each
+    edge in the ragged layout, E + 1 entries (no reference counterpart)."""
+    E = src.shape[0]
+    off = np.zeros(E + 1, np.int64)
+    lib().orc_disc_offsets(E, np.ascontiguousarray(src, np.int32), np.ascontiguousarray(dst, np.int32),
+                           f32(samples), discLen, minDisc, maxDisc, off.ctypes.data)
+    return off
+
+
+def discretize_edges_off(src, dst, samples, off):
+    out = np.empty((int(off[-1]), 6), np.float32)
+    lib().orc_discretize_edges_off(src.shape[0], np.ascontiguousarray(src, np.int32),
+                                   np.ascontiguousarray(dst, np.int32), f32(samples),
+                                   np.ascontiguousarray(off, np.int64).ctypes.data, out)
+    return out
+
+
+def free_edges_off(disc, off, obstacles):
+    E = off.size - 1
+    out = np.empty(E, np.uint8)
+    ob = f32(obstacles).reshape(-1)
+    lib().orc_free_edges_off(E, np.ascontiguousarray(off, np.int64).ctypes.data, f32(disc), ob.size // 12,
+                             ob, out)
+    return out
+
+
 def heuristic(samples, goal):
     N = samples.shape[0]
     h = np.empty(N, np.float32)
@@ -298,8 +335,11 @@ def mccp64(path, T, pmajor, offsetMult, obstacles):
 
 
 def plan(N, obstacles, init, goal, lo, hi, offsetMult, cpTarget, cpFactor, numDisc=8, P=128,
-         Pmc=2048, T_table=400, seed=DEFAULT_SEED, samples=None, trace_cap=0, tables=None):
-    """Whole query as the reference's main() + PUMP(); returns a dict."""
+         Pmc=2048, T_table=400, seed=DEFAULT_SEED, samples=None, trace_cap=0, tables=None,
+         discLen=0.0, discMin=3):
+    """Whole query as the reference's main() + PUMP(); returns a dict.
+    discLen > 0: per-edge waypoint counts by edge length (numDisc the largest,
+    discMin the smallest), see disc_offsets."""
     ob = f32(obstacles).reshape(-1)
     tm, pm = tables if tables is not None else particle_tables(seed, Pmc, T_table)
     pb = Problem()
@@ -309,6 +349,7 @@ def plan(N, obstacles, init, goal, lo, hi, offsetMult, cpTarget, cpFactor, numDi
     for k in range(6):
         pb.init[k], pb.goal[k], pb.lo[k], pb.hi[k] = init[k], goal[k], lo[k], hi[k]
     pb.offsetMult, pb.cpTarget, pb.cpFactor = offsetMult, cpTarget, cpFactor
+    pb.discLen, pb.discMin = discLen, discMin
     tm = f32(tm)
     pm = f32(pm)
     pb.tmajor, pb.pmajor = tm.ctypes.data, pm.ctypes.data

@@ -302,6 +302,8 @@ extern "C" void pump_problem_defaults(pump_problem *pb) {
   pb->refine_lambda = 10.0f;
   pb->samples = nullptr;
   pb->max_paths = 0;
+  pb->disc_len = 0.0f;
+  pb->disc_min = 3;
 }
 
 namespace {

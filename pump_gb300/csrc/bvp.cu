@@ -289,6 +289,176 @@ __global__ void __launch_bounds__(T) discretize_kernel(
   block_store(disc + e0 * W * kDim, s_out, nv * W * kDim);
 }
 
+// ---------------------------------------------- per-edge waypoint counts
+// numDisc of an edge by its length (no counterpart in the reference, whose
+// numDisc is one value per problem, mainPUMP.cu:57): ceil(L / disc_len)
+// clamped to [min_disc, max_disc], L the binary32 distance between the end
+// positions, sqrtf((dx*dx + dy*dy) + dz*dz), each operation rounded once;
+// max_disc for every edge when disc_len <= 0.
+__device__ __forceinline__ int disc_count(const float *x0, const float *x1, float disc_len,
+                                          int min_disc, int max_disc) {
+  if (!(disc_len > 0)) return max_disc;
+  const float dx = x1[0] - x0[0], dy = x1[1] - x0[1], dz = x1[2] - x0[2];
+  const float L = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float q = ceilf(L / disc_len);
+  if (!(q >= (float)min_disc)) return min_disc;  // also NaN
+  if (q > (float)max_disc) return max_disc;
+  return (int)q;
+}
+
+__device__ __forceinline__ int edge_waypoints(const float *__restrict__ samples, int a, int b,
+                                              float disc_len, int min_disc, int max_disc) {
+  float x0[3], x1[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    x0[d] = __ldg(&samples[a * kDim + d]);
+    x1[d] = __ldg(&samples[b * kDim + d]);
+  }
+  return disc_count(x0, x1, disc_len, min_disc, max_disc) + 1;
+}
+
+// The edges' first waypoints in the ragged layout (an exclusive scan of the
+// per-edge waypoint counts), in three passes that never wait on each other:
+// per-tile sums, one block scanning the tile sums, and per-tile scans.
+constexpr int kOffThreads = 256;
+constexpr int kOffPerThread = 16;
+constexpr int kOffTile = kOffThreads * kOffPerThread;  // 4096 edges
+
+__global__ void __launch_bounds__(kOffThreads) disc_tile_sums_kernel(
+    const float *__restrict__ samples, const int *__restrict__ src, const int *__restrict__ dst,
+    long long E, float disc_len, int min_disc, int max_disc, long long *__restrict__ tile_sum) {
+  __shared__ long long s_part[kOffThreads / 32];
+  const long long e0 = blockIdx.x * (long long)kOffTile;
+  long long sum = 0;
+  for (int k = 0; k < kOffPerThread; ++k) {
+    const long long e = e0 + (long long)k * kOffThreads + threadIdx.x;
+    if (e < E) sum += edge_waypoints(samples, src[e], dst[e], disc_len, min_disc, max_disc);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t = 0;
+    for (int w = 0; w < kOffThreads / 32; ++w) t += s_part[w];
+    tile_sum[blockIdx.x] = t;
+  }
+}
+
+// One block of 1024 threads: tile_sum becomes its exclusive prefix in place,
+// and off[E] the total.
+__global__ void __launch_bounds__(1024) disc_tile_scan_kernel(long long *tile_sum, long long ntiles,
+                                                              long long *off_end) {
+  __shared__ long long s[1024];
+  const int t = threadIdx.x;
+  const long long per = (ntiles + 1023) / 1024;
+  const long long b = t * per, e = b + per < ntiles ? b + per : ntiles;
+  long long mine = 0;
+  for (long long i = b; i < e; ++i) mine += tile_sum[i];
+  s[t] = mine;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
+    const long long add = t >= o ? s[t - o] : 0;
+    __syncthreads();
+    s[t] += add;
+    __syncthreads();
+  }
+  long long run = s[t] - mine;
+  for (long long i = b; i < e; ++i) {
+    const long long v = tile_sum[i];
+    tile_sum[i] = run;
+    run += v;
+  }
+  if (t == 1023) *off_end = s[1023];
+}
+
+// Per tile: each thread's kOffPerThread consecutive edges, scanned in order.
+__global__ void __launch_bounds__(kOffThreads) disc_offsets_kernel(
+    const float *__restrict__ samples, const int *__restrict__ src, const int *__restrict__ dst,
+    long long E, float disc_len, int min_disc, int max_disc, const long long *__restrict__ tile_prefix,
+    long long *__restrict__ off) {
+  __shared__ long long s_part[kOffThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long e0 = blockIdx.x * (long long)kOffTile + (long long)threadIdx.x * kOffPerThread;
+  int cnt[kOffPerThread];
+  long long mine = 0;
+#pragma unroll
+  for (int k = 0; k < kOffPerThread; ++k) {
+    const long long e = e0 + k;
+    cnt[k] = e < E ? edge_waypoints(samples, src[e], dst[e], disc_len, min_disc, max_disc) : 0;
+    mine += cnt[k];
+  }
+  // exclusive prefix of `mine` over the block, in thread order
+  long long incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) s_part[warp] = incl;
+  __syncthreads();
+  long long before = 0;
+  for (int w = 0; w < warp; ++w) before += s_part[w];
+  long long run = tile_prefix[blockIdx.x] + before + incl - mine;
+#pragma unroll
+  for (int k = 0; k < kOffPerThread; ++k) {
+    const long long e = e0 + k;
+    if (e < E) off[e] = run;
+    run += cnt[k];
+  }
+}
+
+// findDiscretizedPath (2pBVP.cu:53-69) over the ragged layout: edge e's
+// waypoints are records off[e] .. off[e+1]-1, numDisc_e = off[e+1]-off[e]-1.
+// A block's T edges write one contiguous range, assembled in shared memory
+// (T x max_w records) and stored as whole lines.
+// An edge whose count is outside [2, max_disc + 1] makes its block write
+// nothing and sets *error (when given) to PUMP_ERR_BAD_INPUT.
+template <int Mode, int T>
+__global__ void __launch_bounds__(T) discretize_off_kernel(
+    const float *__restrict__ samples, const int *__restrict__ src, const int *__restrict__ dst,
+    const float *__restrict__ toptE, long long E, const long long *__restrict__ off, int max_disc,
+    float *__restrict__ disc, int *error) {
+  extern __shared__ float4 s_dyn4[];
+  float *s_out = reinterpret_cast<float *>(s_dyn4);
+  const long long e0 = blockIdx.x * (long long)T;
+  const int nv = (int)(E - e0 < T ? E - e0 : T);
+  const long long base = off[e0];
+  const long long cnt = threadIdx.x < nv ? off[e0 + threadIdx.x + 1] - off[e0 + threadIdx.x] : 2;
+  if (__syncthreads_or(cnt < 2 || cnt > max_disc + 1)) {
+    if (threadIdx.x == 0 && error) atomicExch(error, (int)PUMP_ERR_BAD_INPUT);
+    return;
+  }
+  if (threadIdx.x < nv) {
+    const long long e = e0 + threadIdx.x;
+    const int a = src[e], b = dst[e];
+    const int numDisc = (int)cnt - 1;
+    float x0[kDim], x1[kDim], x[kDim];
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) {
+      x0[d] = __ldg(&samples[a * kDim + d]);
+      x1[d] = __ldg(&samples[b * kDim + d]);
+    }
+    float *o = s_out + (off[e] - base) * kDim;
+#pragma unroll
+    for (int d = 0; d < kDim; ++d) {
+      o[d] = x0[d];
+      o[numDisc * kDim + d] = x1[d];
+    }
+    const float topt = toptE[e];
+    const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_bisection(make_coef(x0, x1), 5.0f) : topt;
+    const float dt = tau / numDisc;
+    for (int i = 1; i < numDisc; ++i) {
+      if (Mode != PUMP_BVP_PRECISION) path_point(dt * i, tau, x0, x1, x);
+      else path_point_f32(dt * i, tau, x0, x1, x);
+#pragma unroll
+      for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+    }
+  }
+  __syncthreads();
+  block_store(disc + base * kDim, s_out, (int)(off[e0 + nv] - base) * kDim);
+}
+
 template <int Mode, int T>
 pump_status_t discretize_launch(const float *d_samples, const int *d_src, const int *d_dst,
                                 const float *d_topt, long long E, int numDisc, float *d_disc,
@@ -544,6 +714,95 @@ extern "C" pump_status_t pump_bvp_batch(const float *d_x0, const float *d_x1, in
   jb.topt[0] = d_topt;
   jb.cost[0] = d_cost;
   return bvp_jobs_launch(jb, mode, (cudaStream_t)stream);
+}
+
+namespace pump {
+size_t disc_offsets_scratch(long long E) {
+  return sizeof(long long) * (size_t)((E + kOffTile - 1) / kOffTile + 1);
+}
+
+pump_status_t disc_offsets_async(const float *d_samples, const int *d_src, const int *d_dst,
+                                 long long E, float disc_len, int min_disc, int max_disc,
+                                 long long *d_off, long long *d_scratch, cudaStream_t s) {
+  if (E <= 0) return cuda_status(cudaMemsetAsync(d_off, 0, sizeof(long long), s), "cudaMemsetAsync");
+  const long long ntiles = (E + kOffTile - 1) / kOffTile;
+  if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "disc offsets: %lld edges", E);
+  disc_tile_sums_kernel<<<(unsigned)ntiles, kOffThreads, 0, s>>>(d_samples, d_src, d_dst, E, disc_len,
+                                                                  min_disc, max_disc, d_scratch);
+  PUMP_TRY(launch_status("disc_tile_sums_kernel"));
+  disc_tile_scan_kernel<<<1, 1024, 0, s>>>(d_scratch, ntiles, d_off + E);
+  PUMP_TRY(launch_status("disc_tile_scan_kernel"));
+  disc_offsets_kernel<<<(unsigned)ntiles, kOffThreads, 0, s>>>(d_samples, d_src, d_dst, E, disc_len,
+                                                                min_disc, max_disc, d_scratch, d_off);
+  return launch_status("disc_offsets_kernel");
+}
+
+pump_status_t discretize_off_async(const float *d_samples, const int *d_src, const int *d_dst,
+                                   const float *d_topt, long long E, const long long *d_off,
+                                   int max_disc, int mode, float *d_disc, cudaStream_t s,
+                                   int *error) {
+  if (E <= 0) return PUMP_OK;
+  constexpr int T = 64;
+  const size_t smem = sizeof(float) * (size_t)T * (max_disc + 1) * kDim;
+  if (smem > 220 * 1024)
+    return set_error(PUMP_ERR_CAPACITY, "%d waypoints per edge exceed the stage", max_disc + 1);
+  auto go = [&](auto m) -> pump_status_t {
+    constexpr int M = decltype(m)::value;
+    PUMP_TRY(smem_attr((const void *)discretize_off_kernel<M, T>, smem));
+    discretize_off_kernel<M, T><<<grid_for(E, T), T, smem, s>>>(d_samples, d_src, d_dst, d_topt, E,
+                                                               d_off, max_disc, d_disc, error);
+    return launch_status("discretize_off_kernel");
+  };
+  if (mode == PUMP_BVP_PARITY) return go(std::integral_constant<int, PUMP_BVP_PARITY>{});
+  if (mode == PUMP_BVP_PARITY_GPU) return go(std::integral_constant<int, PUMP_BVP_PARITY_GPU>{});
+  return go(std::integral_constant<int, PUMP_BVP_PRECISION>{});
+}
+}  // namespace pump
+
+extern "C" pump_status_t pump_disc_offsets(const float *d_samples, const int *d_src, const int *d_dst,
+                                           long long E, float disc_len, int min_disc, int max_disc,
+                                           long long *d_off, long long *h_total,
+                                           pump_stream_t stream) {
+  if (E < 0 || min_disc < 1 || max_disc < min_disc || !d_off || !h_total ||
+      (E > 0 && (!d_samples || !d_src || !d_dst)))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_disc_offsets: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  long long *scratch = nullptr;
+  PUMP_CUDA_TRY(pool_malloc_async((void **)&scratch, disc_offsets_scratch(E), s));
+  const pump_status_t st = disc_offsets_async(d_samples, d_src, d_dst, E, disc_len, min_disc,
+                                              max_disc, d_off, scratch, s);
+  cudaFreeAsync(scratch, s);
+  PUMP_TRY(st);
+  PUMP_CUDA_TRY(cudaMemcpyAsync(h_total, d_off + E, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(s));
+  return PUMP_OK;
+}
+
+extern "C" pump_status_t pump_discretize_edges_off(const float *d_samples, const int *d_src,
+                                                   const int *d_dst, const float *d_topt, long long E,
+                                                   const long long *d_off, int max_disc, int mode,
+                                                   float *d_disc, pump_stream_t stream) {
+  if (E < 0 || max_disc < 1 ||
+      (mode != PUMP_BVP_PARITY && mode != PUMP_BVP_PRECISION && mode != PUMP_BVP_PARITY_GPU) ||
+      (E > 0 && (!d_samples || !d_src || !d_dst || !d_topt || !d_off || !d_disc)))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_discretize_edges_off: bad arguments");
+  if (E == 0) return PUMP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  int *d_err = nullptr;
+  PUMP_CUDA_TRY(pool_malloc_async((void **)&d_err, sizeof(int), s));
+  pump_status_t st = cuda_status(cudaMemsetAsync(d_err, 0, sizeof(int), s), "cudaMemsetAsync");
+  if (st == PUMP_OK)
+    st = discretize_off_async(d_samples, d_src, d_dst, d_topt, E, d_off, max_disc, mode, d_disc, s, d_err);
+  int err = 0;
+  if (st == PUMP_OK)
+    st = cuda_status(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+  cudaFreeAsync(d_err, s);
+  if (st == PUMP_OK) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  PUMP_TRY(st);
+  if (err)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_discretize_edges_off: an edge's waypoint count is "
+                                         "outside [2, max_disc + 1]");
+  return PUMP_OK;
 }
 
 extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int *d_src,

@@ -135,6 +135,53 @@ __global__ void __launch_bounds__(T) free_edges_queue_kernel(
   if (t < nv) is_free[e0 + t] = hit ? 0 : 1;
 }
 
+// free_edges_queue_kernel over the ragged waypoint layout: edge e's
+// waypoints are records off[e] .. off[e+1]-1 (2 .. max_disc + 1 of them; a
+// block holding an edge outside that range writes nothing and sets *error,
+// when given, to PUMP_ERR_BAD_INPUT).  Each warp's lanes take their ranges
+// from per-warp tables of first record and count.
+template <int T>
+__global__ void __launch_bounds__(T) free_edges_off_kernel(
+    const float *__restrict__ obs, int numObs, const float *__restrict__ disc,
+    const long long *__restrict__ off, long long E, int max_disc, uint8_t *__restrict__ is_free,
+    int *error) {
+  extern __shared__ float4 s_dyn4[];
+  __shared__ int s_queue[T / 32][kQueueSlots];
+  __shared__ uint8_t s_hit[T];
+  __shared__ int s_first[T], s_cnt[T];
+  float *s_obs = reinterpret_cast<float *>(s_dyn4);
+  float *s_wp = s_obs + ((numObs * 12 + 3) & ~3);
+  const long long e0 = blockIdx.x * (long long)T;
+  const int nv = (int)(E - e0 < T ? E - e0 : T);
+  const int t = threadIdx.x, warp = t >> 5;
+  const long long base = off[e0];
+  const long long cnt = t < nv ? off[e0 + t + 1] - off[e0 + t] : 0;
+  if (__syncthreads_or(t < nv && (cnt < 2 || cnt > max_disc + 1))) {
+    if (t == 0 && error) atomicExch(error, (int)PUMP_ERR_BAD_INPUT);
+    return;
+  }
+  // lane ranges relative to the warp's first record
+  const long long wbase = off[e0 + (warp * 32 < nv ? warp * 32 : 0)];
+  s_first[t] = t < nv ? (int)(off[e0 + t] - wbase) : 0;
+  s_cnt[t] = (int)cnt;
+  const int total = (int)(off[e0 + nv] - base);
+  {
+    const float *src = disc + base * kDim;
+    for (int r = t; r < total; r += T) {
+      const float2 xy = __ldg(reinterpret_cast<const float2 *>(src + (long long)r * kDim));
+      const float z = __ldg(src + (long long)r * kDim + 2);
+      s_wp[r * 3] = xy.x;
+      s_wp[r * 3 + 1] = xy.y;
+      s_wp[r * 3 + 2] = z;
+    }
+  }
+  stage_obstacles(obs, numObs, s_obs);  // ends with __syncthreads
+  const bool hit = warp_queue_hits(s_wp + (wbase - base) * 3,
+                                   RaggedLanes{s_first + warp * 32, s_cnt + warp * 32}, s_obs, numObs,
+                                   t < nv, s_queue[warp], s_hit + warp * 32);
+  if (t < nv) is_free[e0 + t] = hit ? 0 : 1;
+}
+
 // One thread per waypoint: setupAsBs (hsmc.cu:201-211) fused with
 // cacheHalfspaces (hsmc.cu:10-99); unused slots get the defaults a = -1,
 // b = 1111.
@@ -404,6 +451,47 @@ extern "C" pump_status_t pump_free_edges(const float *d_obstacles, int numObs, c
                                                                          d_disc, E, numDisc,
                                                                          d_is_free);
   return launch_status("free_edges");
+}
+
+namespace pump {
+pump_status_t free_edges_off_async(const float *d_obstacles, int numObs, const float *d_disc,
+                                   const long long *d_off, long long E, int max_disc,
+                                   uint8_t *d_is_free, cudaStream_t s, int *error) {
+  if (E <= 0) return PUMP_OK;
+  constexpr int T = 128;
+  const size_t smem = sizeof(float) * ((size_t)((numObs * 12 + 3) & ~3) + (size_t)T * (max_disc + 1) * 3);
+  if (smem > 200 * 1024 || numObs > 0xFFFF)
+    return set_error(PUMP_ERR_CAPACITY, "%d boxes and %d waypoints per edge exceed the edge check's stage",
+                     numObs, max_disc + 1);
+  PUMP_TRY(smem_attr((const void *)free_edges_off_kernel<T>, smem));
+  free_edges_off_kernel<T><<<grid_for(E, T), T, smem, s>>>(d_obstacles, numObs, d_disc, d_off, E,
+                                                          max_disc, d_is_free, error);
+  return launch_status("free_edges_off");
+}
+}  // namespace pump
+
+extern "C" pump_status_t pump_free_edges_off(const float *d_obstacles, int numObs, const float *d_disc,
+                                             const long long *d_off, long long E, int max_disc,
+                                             uint8_t *d_is_free, pump_stream_t stream) {
+  if (numObs < 0 || E < 0 || max_disc < 1 || (numObs > 0 && !d_obstacles) ||
+      (E > 0 && (!d_disc || !d_off || !d_is_free)))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_free_edges_off: bad arguments");
+  if (E == 0) return PUMP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  int *d_err = nullptr;
+  PUMP_CUDA_TRY(pool_malloc_async((void **)&d_err, sizeof(int), s));
+  pump_status_t st = cuda_status(cudaMemsetAsync(d_err, 0, sizeof(int), s), "cudaMemsetAsync");
+  if (st == PUMP_OK) st = free_edges_off_async(d_obstacles, numObs, d_disc, d_off, E, max_disc, d_is_free, s, d_err);
+  int err = 0;
+  if (st == PUMP_OK)
+    st = cuda_status(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+  cudaFreeAsync(d_err, s);
+  if (st == PUMP_OK) st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  PUMP_TRY(st);
+  if (err)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_free_edges_off: an edge's waypoint count is outside "
+                                         "[2, max_disc + 1]");
+  return PUMP_OK;
 }
 
 extern "C" pump_status_t pump_cache_halfspaces(const float *d_obstacles, int numObs,

@@ -130,18 +130,41 @@ constexpr int kQueueSlots = 64;
 // leave most of a warp waiting for its longest list.  q: the warp's
 // kQueueSlots ints, hit: its 32 bytes, both in shared memory.  Returns
 // whether this lane's edge hits a box.
-__device__ __forceinline__ bool warp_queue_hits(const float *s_wp_warp, int W, const float *s_obs,
+//
+// The lanes' waypoint ranges come from a layout: every edge W waypoints
+// (UniformLanes: lane l's at record l * W), or per-edge counts (RaggedLanes:
+// first record and count per lane, in per-warp shared arrays).
+struct UniformLanes {
+  int W;
+  __device__ int first(int l) const { return l * W; }
+  __device__ int count(int) const { return W; }
+};
+struct RaggedLanes {
+  const int *f, *c;  // per lane: first staged record, waypoint count
+  __device__ int first(int l) const { return f[l]; }
+  __device__ int count(int l) const { return c[l]; }
+};
+// per-lane ranges from staged offsets: lane l's records o[l] - o[0] ..
+// o[l+1] - o[0] - 1
+struct OffsetLanes {
+  const int *o;
+  __device__ int first(int l) const { return o[l] - o[0]; }
+  __device__ int count(int l) const { return o[l + 1] - o[l]; }
+};
+
+template <class Lanes>
+__device__ __forceinline__ bool warp_queue_hits(const float *s_wp_warp, Lanes lay, const float *s_obs,
                                                 int numObs, bool active, int *q, uint8_t *hit) {
   constexpr int kPos = 3;  // floats per staged waypoint
   const int lane = threadIdx.x & 31;
   const unsigned int lt = (1u << lane) - 1u;
-  const int numDisc = W - 1;
   hit[lane] = 0;
   __syncwarp();
   float emin[3], emax[3];
   bool nan = false;
   if (active) {
-    const float *wp = s_wp_warp + lane * W * kPos;
+    const float *wp = s_wp_warp + lay.first(lane) * kPos;
+    const int W = lay.count(lane);
 #pragma unroll
     for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
     for (int i = 0; i < W; ++i)
@@ -157,7 +180,8 @@ __device__ __forceinline__ bool warp_queue_hits(const float *s_wp_warp, int W, c
   auto test_pair = [&](int ent) {
     const int el = ent >> 16, o = ent & 0xFFFF;
     if (hit[el]) return;  // the edge already hit a box
-    const float *wp = s_wp_warp + el * W * kPos;
+    const float *wp = s_wp_warp + lay.first(el) * kPos;
+    const int numDisc = lay.count(el) - 1;
     const float *ob = &s_obs[o * 12];
     float v[3], w[3];
 #pragma unroll
@@ -196,6 +220,11 @@ __device__ __forceinline__ bool warp_queue_hits(const float *s_wp_warp, int W, c
   if (lane < tail - head) test_pair(q[(head + lane) & (kQueueSlots - 1)]);
   __syncwarp();
   return hit[lane] != 0;
+}
+
+__device__ __forceinline__ bool warp_queue_hits(const float *s_wp_warp, int W, const float *s_obs,
+                                                int numObs, bool active, int *q, uint8_t *hit) {
+  return warp_queue_hits(s_wp_warp, UniformLanes{W}, s_obs, numObs, active, q, hit);
 }
 
 // The half-space box o contributes at a waypoint (pos, vel): cacheHalfspaces,

@@ -167,6 +167,22 @@ pump_status_t bvp_jobs_refgpu_launch(const BvpJobs &jb, cudaStream_t stream);
 // reference's findDiscretizedPath recomputes for the waypoints.
 pump_status_t edge_topts_parity_async(const float *d_samples, const int *d_src, const int *d_dst,
                                       long long E, float *d_topt, cudaStream_t stream);
+// Per-edge waypoint counts by edge length and their ragged layout (bvp.cu):
+// d_off[E + 1] (the first record of each edge, the total at E) from
+// d_scratch of disc_offsets_scratch(E) bytes; the waypoints over that layout
+// (*error, when given, records an edge count outside [2, max_disc + 1]).
+size_t disc_offsets_scratch(long long E);
+pump_status_t disc_offsets_async(const float *d_samples, const int *d_src, const int *d_dst,
+                                 long long E, float disc_len, int min_disc, int max_disc,
+                                 long long *d_off, long long *d_scratch, cudaStream_t s);
+pump_status_t discretize_off_async(const float *d_samples, const int *d_src, const int *d_dst,
+                                   const float *d_topt, long long E, const long long *d_off,
+                                   int max_disc, int mode, float *d_disc, cudaStream_t s,
+                                   int *error = nullptr);
+// freeEdges over the ragged layout (collide.cu).
+pump_status_t free_edges_off_async(const float *d_obstacles, int numObs, const float *d_disc,
+                                   const long long *d_off, long long E, int max_disc,
+                                   uint8_t *d_is_free, cudaStream_t s, int *error = nullptr);
 // The BVP arithmetic of the reference's host code for a planner mode: the
 // parity arithmetic for both parity modes, the precision mode otherwise.
 inline int host_bvp_mode(int mode) { return mode == PUMP_BVP_PRECISION ? PUMP_BVP_PRECISION : PUMP_BVP_PARITY; }

@@ -237,7 +237,19 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
     if (lane == 0 && p.error) atomicExch(p.error, (int)PUMP_ERR_BAD_INPUT);
     return;
   }
-  const int W = p.W, maxHS = p.maxHS, P = p.P;
+  // the edge's waypoints: W records per edge, or its own range (at most p.W)
+  int W = p.W;
+  long long wp0 = (long long)edge * W;
+  if (Boxes && p.disc_off) {
+    wp0 = p.disc_off[edge];
+    const long long n = p.disc_off[edge + 1] - wp0;
+    if (n < 2 || n > p.W) {
+      if (lane == 0 && p.error) atomicExch(p.error, (int)PUMP_ERR_BAD_INPUT);
+      return;
+    }
+    W = (int)n;
+  }
+  const int maxHS = p.maxHS, P = p.P;
   const int words = (P + 31) >> 5;
   const int slots = W * maxHS;
   const long long hsHead = (long long)edge * slots;
@@ -251,7 +263,7 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
   }
   if (Boxes) {
     // lane i holds waypoint i (W <= 32; otherwise waypoints are read per step)
-    const float *ew = p.disc + (long long)edge * W * kDim;
+    const float *ew = p.disc + wp0 * kDim;
     float my[kDim];
     const int mi = lane < W ? lane : 0;
 #pragma unroll
@@ -750,7 +762,8 @@ pump_status_t hsmc_boxes_fill(int num_new, int W, const int *d_edge, const int *
                               int T_rows, float offset_mult, const uint32_t *d_valid_in,
                               uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
                               const unsigned long long *d_num_new, const int *d_skip,
-                              const HsmcEpilogue *epi, HsmcParams *out) {
+                              const HsmcEpilogue *epi, HsmcParams *out,
+                              const long long *d_disc_off) {
   if ((P + 31) / 32 > kMaxHsmcWords)
     return set_error(PUMP_ERR_CAPACITY, "hsmc: %d particles exceed %d", P, 32 * kMaxHsmcWords);
   if (!hsmc_boxes_fits(numObs, W, maxHS))
@@ -766,6 +779,7 @@ pump_status_t hsmc_boxes_fill(int num_new, int W, const int *d_edge, const int *
   hp.obs = d_obs;
   hp.numObs = numObs;
   hp.disc = d_disc;
+  hp.disc_off = d_disc_off;
   hp.maxd2 = maxd2;
   hp.maxHS = maxHS;
   hp.times = d_times;
@@ -797,13 +811,14 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                                int T_rows, float offset_mult, const uint32_t *d_valid_in,
                                uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
                                cudaStream_t stream, const unsigned long long *d_num_new,
-                               const int *d_skip, const HsmcEpilogue *epi) {
+                               const int *d_skip, const HsmcEpilogue *epi,
+                               const long long *d_disc_off) {
   if (num_new <= 0) return PUMP_OK;
   HsmcParams hp{};
   PUMP_TRY(hsmc_boxes_fill(num_new, W, d_edge, d_prev, num_edges, num_prev, d_obs, numObs, d_disc,
                            maxd2, maxHS, d_times, d_topt, dt, d_offsets_t, Pmc, T_rows, offset_mult,
                            d_valid_in, d_valid_out, P, d_cp_out, d_error, d_num_new, d_skip, epi,
-                           &hp));
+                           &hp, d_disc_off));
   const size_t smem = hsmc_boxes_smem(numObs);
   PUMP_TRY(smem_attr((const void *)hsmc_kernel<true>, smem));
   // with a device-side count, num_new bounds it
@@ -880,6 +895,24 @@ extern "C" pump_status_t pump_hsmc_propagate(int num_new, int W, const int *d_ed
                            d_hs_count, (cudaStream_t)stream, nullptr, nullptr);
 }
 
+extern "C" pump_status_t pump_hsmc_propagate_boxes_off(
+    int num_new, int max_w, const int *d_edge, const int *d_prev, long long num_edges, int base,
+    const float *d_obstacles, int numObs, const float *d_disc, const long long *d_disc_off,
+    float maxd2, int maxHS, const float *d_times, const float *d_topt, float dt,
+    const float *d_offsets_t, int Pmc, int T_rows, float offset_mult, uint32_t *d_valid, int P,
+    float *d_path_cp, int *d_error, pump_stream_t stream) {
+  if (num_new < 0 || max_w < 2 || maxHS < 0 || P <= 0 || P > Pmc || T_rows <= 0 || base < 0 ||
+      num_edges < 0 || numObs < 0 || (numObs > 0 && !d_obstacles) ||
+      (num_new > 0 && (!d_edge || !d_prev || !d_times || !d_topt || !d_offsets_t || !d_valid ||
+                       !d_path_cp || !d_disc || !d_disc_off)))
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_hsmc_propagate_boxes_off: bad arguments");
+  const size_t words = (size_t)((P + 31) / 32);
+  return hsmc_boxes_async(num_new, max_w, d_edge, d_prev, num_edges, base, d_obstacles, numObs,
+                          d_disc, maxd2, maxHS, d_times, d_topt, dt, d_offsets_t, Pmc, T_rows,
+                          offset_mult, d_valid, d_valid + (size_t)base * words, P, d_path_cp + base,
+                          d_error, (cudaStream_t)stream, nullptr, nullptr, nullptr, d_disc_off);
+}
+
 extern "C" pump_status_t pump_hsmc_propagate_boxes(
     int num_new, int W, const int *d_edge, const int *d_prev, long long num_edges, int base,
     const float *d_obstacles, int numObs, const float *d_disc, float maxd2, int maxHS,
@@ -895,7 +928,7 @@ extern "C" pump_status_t pump_hsmc_propagate_boxes(
   return hsmc_boxes_async(num_new, W, d_edge, d_prev, num_edges, base, d_obstacles, numObs, d_disc,
                           maxd2, maxHS, d_times, d_topt, dt, d_offsets_t, Pmc, T_rows, offset_mult,
                           d_valid, d_valid + (size_t)base * words, P, d_path_cp + base, d_error,
-                          (cudaStream_t)stream, nullptr, nullptr, nullptr);
+                          (cudaStream_t)stream, nullptr, nullptr, nullptr, nullptr);
 }
 
 extern "C" pump_status_t pump_mc_cp(const float *d_paths, const int *d_offset, const int *d_len,

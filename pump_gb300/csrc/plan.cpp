@@ -45,7 +45,8 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                                int T_rows, float offset_mult, const uint32_t *d_valid_in,
                                uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
                                cudaStream_t stream, const unsigned long long *d_num_new,
-                               const int *d_skip, const HsmcEpilogue *epi);
+                               const int *d_skip, const HsmcEpilogue *epi,
+                               const long long *d_disc_off = nullptr);
 pump_status_t mc_cp_async(const float *d_paths, const int *d_offset, const int *d_len, int n_paths,
                           const float *d_offsets_t, int Pmc, int T_rows, float offset_mult,
                           const float *d_obstacles, int numObs, int *d_hits, float *d_cp,
@@ -317,6 +318,10 @@ class Planner {
   // time the reference's findDiscretizedPath evaluates the waypoints at
   // (d_toptE_ holds the GPU kernel's times, which the search and HSMC use)
   DevBuf<float> d_toptH_;
+  // per-edge waypoint counts by edge length (pb_.disc_len > 0): edge e's
+  // waypoints are records d_disc_off_[e] .. d_disc_off_[e+1]-1 of d_disc_
+  DevBuf<long long> d_disc_off_, d_disc_scratch_;
+  const long long *disc_off() const { return pb_.disc_len > 0 ? d_disc_off_.p : nullptr; }
   const float *waypoint_topts() const {
     return pb_.bvp_mode == PUMP_BVP_PARITY_GPU ? d_toptH_.p : d_toptE_.p;
   }
@@ -469,6 +474,12 @@ pump_status_t Planner::roadmap() {
     PUMP_TRY(d_toptH_.alloc(E_ > 0 ? E_ : 1));
     PUMP_TRY(edge_topts_parity_async(d_samples_.p, d_src_.p, d_dst_.p, E_, d_toptH_.p, s_));
   }
+  if (pb_.disc_len > 0) {  // the waypoint array (sized for num_disc per edge) holds the ragged layout
+    PUMP_TRY(d_disc_off_.alloc(E_ + 1));
+    PUMP_TRY(d_disc_scratch_.alloc(disc_offsets_scratch(E_) / sizeof(long long) + 1));
+    PUMP_TRY(disc_offsets_async(d_samples_.p, d_src_.p, d_dst_.p, E_, pb_.disc_len, pb_.disc_min,
+                                pb_.num_disc, d_disc_off_.p, d_disc_scratch_.p, s_));
+  }
   h0_ = hout[0];
   std::memcpy(&max_degree_, hout + 1, sizeof(int));
   if (!pb_.samples) samples_.assign(hout + 2, hout + 2 + nsf);
@@ -522,12 +533,19 @@ pump_status_t Planner::online() {
   PUMP_TRY(d_open_cnt_.alloc(N_));
   PUMP_TRY(d_todo_.alloc(N_));
   PUMP_CUDA_TRY(cudaMemsetAsync(d_open_cnt_.p, 0xFF, sizeof(int) * (size_t)N_, s_));  // -1
-  if (!lazy_) {
+  if (!lazy_ && disc_off()) {
+    PUMP_TRY(discretize_off_async(d_samples_.p, d_src_.p, d_dst_.p, waypoint_topts(), E_, disc_off(),
+                                  pb_.num_disc, host_bvp_mode(pb_.bvp_mode), d_disc_.p, s_));
+    PUMP_TRY(free_edges_off_async(d_obs_.p, nobs_, d_disc_.p, disc_off(), E_, pb_.num_disc,
+                                  d_free_e_.p, s_));
+  } else if (!lazy_) {
     PUMP_TRY(pump_discretize_edges(d_samples_.p, d_src_.p, d_dst_.p, waypoint_topts(), E_,
                                    pb_.num_disc, host_bvp_mode(pb_.bvp_mode), d_disc_.p,
                                    (pump_stream_t)s_));
     PUMP_TRY(pump_free_edges(d_obs_.p, nobs_, d_disc_.p, E_, pb_.num_disc, d_free_e_.p,
                              (pump_stream_t)s_));
+  }
+  if (!lazy_) {
     SearchDev sd{};
     sd.N = N_;
     sd.go = d_go_.p;
@@ -645,6 +663,7 @@ pump_status_t Planner::explore() {
   ca.numDisc = pb_.num_disc;
   ca.mode = host_bvp_mode(pb_.bvp_mode);
   ca.wp_topt = waypoint_topts();
+  ca.disc_off = disc_off();
   ca.obs = d_obs_.p;
   ca.numObs = nobs_;
   ca.max_degree = max_degree_;
@@ -726,7 +745,7 @@ pump_status_t Planner::explore() {
     PUMP_TRY(hsmc_boxes_async(maxNew, W_, d_wfEdge_.p, d_wfPrev_.p, E_, numPaths_, d_obs_.p, nobs_,
                               d_disc_.p, maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_,
                               pb_.num_mc, pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p,
-                              P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf, &epi));
+                              P_, d_cpStage_.p, d_err_.p, s_, d_nn, d_ovf, &epi, disc_off()));
     // cut-off (written by the HSMC kernel), dominance and storing, buckets
     // (PUMP.cu:164-256)
     // the store pass's last block leaves the counters in hctl (pinned)
@@ -869,7 +888,7 @@ pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
                            maxd2_, maxHS_, d_pathTime_.p, d_toptE_.p, dt_, d_table_, pb_.num_mc,
                            pb_.table_rows, pb_.offset_mult, d_valid_.p, d_stage_.p, P_,
                            d_cpStage_.p, d_err_.p, &sd.ctl->num_new, &sd.ctl->overflow, &epi,
-                           &la->hp));
+                           &la->hp, disc_off()));
   LoopState &L = la->L;
   L.max_itrs = maxItrs_;
   L.max_paths = M;
@@ -1487,7 +1506,8 @@ pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *
   if (!ctx || !pb || !res) return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: null argument");
   if (pb->N < 2 || pb->num_disc < 1 || pb->num_hsmc < 1 || pb->num_mc < pb->num_hsmc ||
       pb->table_rows < 2 || pb->num_obstacles < 0 || (pb->num_obstacles > 0 && !pb->obstacles) ||
-      !(pb->cp_factor > 0) || pb->max_paths < 0 ||
+      !(pb->cp_factor > 0) || pb->max_paths < 0 || !(pb->disc_len >= 0) ||
+      (pb->disc_len > 0 && (pb->disc_min < 1 || pb->disc_min > pb->num_disc)) ||
       (pb->bvp_mode != PUMP_BVP_PARITY && pb->bvp_mode != PUMP_BVP_PRECISION &&
        pb->bvp_mode != PUMP_BVP_PARITY_GPU))
     return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: problem out of domain");

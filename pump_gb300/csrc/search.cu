@@ -88,8 +88,10 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
   constexpr int kEdges = Wide ? kChkWideEdges : kChkEdges;
   extern __shared__ float4 s_dyn4[];
   __shared__ int s_open[kChkThreads / 32];
+  __shared__ int s_off[kEdges + 1];  // ragged layout: the chunk's edges' first records
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   const int numDisc = ca.numDisc, W = numDisc + 1;
+  const long long *off = ca.disc_off;
   float *s_wp = s_obs + ((ca.numObs * 12 + 3) & ~3);  // kEdges x W x 3 positions
   const int n_todo = sd.ctl->todo;
   const int chunks = ca.max_degree > kEdges ? (ca.max_degree + kEdges - 1) / kEdges : 1;
@@ -105,8 +107,35 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
     const int c0 = sd.go[node] + c * kEdges;
     if (c0 >= e1) continue;  // block-uniform: this node has fewer chunks
     const int ne = e1 - c0 < kEdges ? e1 - c0 : kEdges;
-    for (int q = threadIdx.x; q < ne * W; q += kChkThreads) {
-      const int eq = q / W, i = q - eq * W;
+    // the chunk's records: ne * W, or the edges' own ranges (ragged layout)
+    long long rbase = (long long)c0 * W;
+    int total = ne * W;
+    if (off) {
+      for (int k = threadIdx.x; k <= ne; k += kChkThreads) s_off[k] = (int)(off[c0 + k] - off[c0]);
+      __syncthreads();
+      rbase = off[c0];
+      total = s_off[ne];
+      if (total > kEdges * W) {  // a count past the staged capacity (never from disc_offsets)
+        __syncthreads();
+        continue;
+      }
+    }
+    for (int q = threadIdx.x; q < total; q += kChkThreads) {
+      int eq, i, nd = numDisc;
+      if (off) {  // the chunk edge holding record q
+        int lo = 0, hi = ne;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (s_off[mid] <= q) lo = mid;
+          else hi = mid;
+        }
+        eq = lo;
+        i = q - s_off[eq];
+        nd = s_off[eq + 1] - s_off[eq] - 1;
+      } else {
+        eq = q / W;
+        i = q - eq * W;
+      }
       const int e = c0 + eq;
       const int b = sd.dst[e];
       float x0[kDim], x1[kDim], x[kDim];
@@ -118,18 +147,18 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
       if (i == 0) {
 #pragma unroll
         for (int d = 0; d < kDim; ++d) x[d] = x0[d];
-      } else if (i == numDisc) {
+      } else if (i == nd) {
 #pragma unroll
         for (int d = 0; d < kDim; ++d) x[d] = x1[d];
       } else {
         const float topt = ca.wp_topt[e];
-        const float dt = topt / numDisc;
+        const float dt = topt / nd;
         if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
         else path_point_f32(dt * i, topt, x0, x1, x);
       }
       // consecutive threads write consecutive 24-byte records: a warp's
       // stores cover one contiguous range
-      float2 *out = reinterpret_cast<float2 *>(ca.disc + ((long long)c0 * W + q) * kDim);
+      float2 *out = reinterpret_cast<float2 *>(ca.disc + (rbase + q) * kDim);
       out[0] = make_float2(x[0], x[1]);
       out[1] = make_float2(x[2], x[3]);
       out[2] = make_float2(x[4], x[5]);
@@ -141,8 +170,11 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
       __shared__ int s_q[kChkThreads / 32][kQueueSlots];
       __shared__ uint8_t s_h[kChkThreads];
       const bool active = (int)threadIdx.x < ne;
-      const bool h = warp_queue_hits(s_wp + warp * 32 * W * 3, W, s_obs, ca.numObs, active,
-                                     s_q[warp], s_h + warp * 32);
+      const bool h = off ? warp_queue_hits(s_wp + (warp * 32 < ne ? s_off[warp * 32] : 0) * 3,
+                                           OffsetLanes{s_off + warp * 32}, s_obs, ca.numObs, active,
+                                           s_q[warp], s_h + warp * 32)
+                         : warp_queue_hits(s_wp + warp * 32 * W * 3, W, s_obs, ca.numObs, active,
+                                           s_q[warp], s_h + warp * 32);
       int open = 0;
       if (active) {
         const int e = c0 + threadIdx.x;
@@ -164,12 +196,13 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
     bool hit = false;
     if (el < ne) {
       constexpr int kPos = 3;  // floats per staged waypoint
-      const float *wp = s_wp + el * W * kPos;
+      const float *wp = s_wp + (off ? s_off[el] : el * W) * kPos;
+      const int We = off ? s_off[el + 1] - s_off[el] : W, nde = We - 1;
       float emin[3], emax[3];
       bool nan = false;
 #pragma unroll
       for (int d = 0; d < 3; ++d) emin[d] = emax[d] = wp[d];
-      for (int i = 0; i < W; ++i)
+      for (int i = 0; i < We; ++i)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const float x = wp[i * kPos + d];
@@ -183,7 +216,7 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
         float v[3], w[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) v[d] = wp[d];
-        for (int i = 0; i < numDisc && !hit; ++i) {
+        for (int i = 0; i < nde && !hit; ++i) {
 #pragma unroll
           for (int d = 0; d < 3; ++d) w[d] = wp[(i + 1) * kPos + d];
           hit = segment_box_hit(v, w, ob);

@@ -68,6 +68,9 @@ struct CheckArgs {
   float *disc;
   int numDisc, mode;       // mode: PUMP_BVP_PARITY or PUMP_BVP_PRECISION waypoints
   const float *wp_topt;    // per edge, the optimal time its waypoints are evaluated at
+  // the ragged waypoint layout (may be null: numDisc + 1 records per edge):
+  // edge e's records disc_off[e] .. disc_off[e+1]-1, at most numDisc + 1
+  const long long *disc_off;
   const float *obs;
   int numObs;
   int max_degree;  // largest out-degree of the roadmap
@@ -98,8 +101,11 @@ struct HsmcParams {
   // cached half-spaces
   const float *as, *bs;
   const uint8_t *hs_count;
-  // half-spaces from the boxes
+  // half-spaces from the boxes; disc_off (may be null): the ragged waypoint
+  // layout, edge e's waypoints at records disc_off[e] .. disc_off[e+1]-1
+  // (2 .. W of them), otherwise W records per edge
   const float *obs, *disc;
+  const long long *disc_off;
   int numObs;
   float maxd2;
   int maxHS;
@@ -244,6 +250,7 @@ pump_status_t hsmc_boxes_fill(int num_new, int W, const int *d_edge, const int *
                               int T_rows, float offset_mult, const uint32_t *d_valid_in,
                               uint32_t *d_valid_out, int P, float *d_cp_out, int *d_error,
                               const unsigned long long *d_num_new, const int *d_skip,
-                              const HsmcEpilogue *epi, HsmcParams *out);
+                              const HsmcEpilogue *epi, HsmcParams *out,
+                              const long long *d_disc_off = nullptr);
 
 }  // namespace pump

@@ -51,7 +51,7 @@ class Problem(C.Structure):
         ("init", f32 * 6), ("goal", f32 * 6), ("lo", f32 * 6), ("hi", f32 * 6),
         ("offset_mult", f32), ("cp_target", f32), ("cp_factor", f32), ("seed", C.c_uint64),
         ("bvp_mode", i32), ("samples", vp), ("refine_iters", i32), ("refine_lambda", f32),
-        ("max_paths", i32),
+        ("max_paths", i32), ("disc_len", f32), ("disc_min", i32),
     ]
 
 
@@ -112,6 +112,11 @@ _SIGS = {
     "pump_frontier_compact_noalloc": (i32, [vp, i32, vp, vp, vp]),
     "pump_selftest_wait": (i32, [vp, i64, vp]),
     "pump_halton_samples": (i32, [i32, vp, vp, vp, vp, vp, vp]),
+    "pump_disc_offsets": (i32, [vp, vp, vp, i64, f32, i32, i32, vp, C.POINTER(i64), vp]),
+    "pump_discretize_edges_off": (i32, [vp, vp, vp, vp, i64, vp, i32, i32, vp, vp]),
+    "pump_free_edges_off": (i32, [vp, i32, vp, vp, i64, i32, vp, vp]),
+    "pump_hsmc_propagate_boxes_off": (i32, [i32, i32, vp, vp, i64, i32, vp, i32, vp, vp, f32, i32, vp,
+                                            vp, f32, vp, i32, i32, f32, vp, i32, vp, vp, vp]),
     "pump_problem_defaults": (None, [C.POINTER(Problem)]),
     "pump_read_input": (i32, [C.c_char_p, C.POINTER(Problem)]),
     "pump_plan": (i32, [vp, C.POINTER(Problem), C.POINTER(PlanResult), vp]),

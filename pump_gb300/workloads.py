@@ -89,10 +89,16 @@ def free_point(rng, obstacles):
             return (float(p[0]), float(p[1]), float(p[2]), 0.0, 0.0, 0.0)
 
 
+# Waypoints per edge of the batched workload: by edge length, at most
+# BATCH_DISC_LEN apart in position, between 4 and 32 per edge (num_disc 3..31)
+BATCH_DISC_LEN, BATCH_DISC_MIN, BATCH_DISC_MAX = 0.025, 3, 31
+
+
 def batch_queries(n=256, seed=2000, n_range=(500, 8000), obs_range=(5, 100)):
     """The batched workload: per query N log-uniform in n_range, a box count
     uniform in obs_range (boxes as random_boxes), init and goal uniform in free
-    space, CP target from {0.001, 0.01, 0.05}, eta from {1, 2, 4}."""
+    space, CP target from {0.001, 0.01, 0.05}, eta from {1, 2, 4}; waypoints
+    per edge by edge length (disc_len, disc_min, num_disc: 4 to 32)."""
     rng = np.random.Generator(np.random.MT19937(seed))
     out = []
     for q in range(n):
@@ -103,7 +109,8 @@ def batch_queries(n=256, seed=2000, n_range=(500, 8000), obs_range=(5, 100)):
         goal = free_point(rng, obs)
         out.append(dict(N=N, obstacles=obs, init=init, goal=goal,
                         cp=float(rng.choice([0.001, 0.01, 0.05])),
-                        eta=float(rng.choice([1.0, 2.0, 4.0])), offset_mult=np.float32(1e-3)))
+                        eta=float(rng.choice([1.0, 2.0, 4.0])), offset_mult=np.float32(1e-3),
+                        disc_len=BATCH_DISC_LEN, disc_min=BATCH_DISC_MIN, num_disc=BATCH_DISC_MAX))
     return out
 
 
@@ -143,7 +150,10 @@ CONFIGS = {
                  obstacles=lambda q=0: random_boxes(10, 1000 * 0 + q)),
     "cfg1": dict(N=4000, num_disc=8, num_hsmc=1024, offset_mult=2e-3, cp=0.01, eta=2.0,
                  obstacles=lambda q=0: indoor(1000 * 1 + q)),
-    # the large configuration: 4096 particles for HSMC and for the Monte Carlo CP
+    # the large configuration: 4096 particles for HSMC and for the Monte Carlo CP.
+    # Its fourth wavefront holds 14.1 M new paths, past the reference's path
+    # store of 2 N sqrt(N) = 11.4 M (where the reference ends the search,
+    # PUMP.cu:62-76), so the store is 2^24 paths.
     "cfg4": dict(N=32000, num_disc=15, num_hsmc=4096, num_mc=4096, offset_mult=5e-3, cp=0.005,
-                 eta=2.0, obstacles=lambda q=0: large_boxes(1000 * 4 + q)),
+                 eta=2.0, max_paths=1 << 24, obstacles=lambda q=0: large_boxes(1000 * 4 + q)),
 }

@@ -36,10 +36,12 @@ def large(gpu, pumplib, oracle):
         pb.lo[d], pb.hi[d] = workloads.LO[d], workloads.HI[d]
     pb.offset_mult, pb.cp_target, pb.cp_factor = cfg["offset_mult"], cfg["cp"], cfg["eta"]
     pb.bvp_mode = pumplib.PUMP_BVP_PRECISION
+    pb.max_paths = cfg["max_paths"]
     return dict(torch=torch, ctx=ctx, L=L, cfg=cfg, N=N, obs=obs, pb=pb)
 
 
 def test_large_roadmap_stages(large, pumplib, oracle):
+    large["roadmap"] = {}
     """Pair BVPs on a strided sample against the binary64 minimiser (1 ulp in
     cost), rn the exact k-th smallest of all 1.02e9 costs, the edges exactly
     the pairs below rn in (i, j) order, waypoints and edge checks on a
@@ -79,6 +81,7 @@ def test_large_roadmap_stages(large, pumplib, oracle):
                                        ptr(d_dst), ptr(d_ce), ptr(d_te), ptr(d_go), C.byref(rn),
                                        C.byref(Ec), stream(torch)))
     E = int(Ec.value)
+    large["roadmap"] = dict(d_s=d_s, src=host(d_src, E), dst=host(d_dst, E), te=host(d_te, E))
     rnv = torch.tensor(rn.value, dtype=torch.float32, device="cuda")
     below, at_most = int((d_c < rnv).sum()), int((d_c <= rnv).sum())
     assert below <= k < at_most  # rn is element k of the sorted costs
@@ -114,26 +117,79 @@ def test_large_roadmap_stages(large, pumplib, oracle):
 
 
 def test_large_plan(large, pumplib, oracle):
-    """The whole query: it runs within the library's capacities, its first
-    HSMC launch (the expansions of the initial path) gives the masks the
-    oracle's propagateValidParticles gives on the same waypoints and
-    half-spaces, and the returned path's Monte Carlo CP, re-judged by the
+    """The whole query, with a path store of 2^24: its largest wavefront holds
+    14.1 M new paths, past the reference's 2 N sqrt(N) = 11.4 M, where the
+    reference ends the search (PUMP.cu:62-76); with the default store the
+    query ends with PUMP_ERR_CAPACITY there.  The first HSMC launch (the
+    initial path's expansions, 4096 particles, 200 boxes) gives the masks and
+    CPs the oracle's cacheHalfspaces + propagateValidParticles give on the
+    same waypoints, and the returned path's Monte Carlo CP, re-judged by the
     oracle with the 4096-particle table, is the reported CP and within the
     target."""
     torch, L, ctx, pb, obs, N = large["torch"], large["L"], large["ctx"], large["pb"], large["obs"], large["N"]
+    nd = large["cfg"]["num_disc"]
+    W = nd + 1
+    store = pb.max_paths
+    pb.max_paths = 0
+    res = pumplib.PlanResult()
+    assert L.pump_plan(ctx.handle, C.byref(pb), C.byref(res), None) == pumplib.PUMP_ERR_CAPACITY
+    pb.max_paths = store
     res = pumplib.PlanResult()
     path = np.zeros((pb.table_rows, 6), np.float32)
     res.path, res.path_cap = path.ctypes.data, pb.table_rows
-    trace = np.zeros(4_000_000, np.int32)
+    trace = np.zeros(2 * 20_000_000, np.int32)
     res.wf_trace, res.wf_trace_cap = trace.ctypes.data, trace.size
     st = L.pump_plan(ctx.handle, C.byref(pb), C.byref(res), None)
-    assert st in (pumplib.PUMP_OK, pumplib.PUMP_ERR_NO_SOLUTION), L.pump_last_error()
-    print("large plan: edges %d, iterations %d, paths %d, expansions %d, success %d, cp %g, %.1f ms"
-          % (res.num_edges, res.iterations, res.num_paths, res.num_considered, res.success,
-             res.soln_cp, res.ms_total))
-    assert res.num_edges > 0.9 * 0.05 * N * (N - 1) and res.num_considered > 0
-    if res.success:
-        T = res.path_len
-        _, pm = oracle.particle_tables(int(pb.seed), int(pb.num_mc), int(pb.table_rows), tmajor=False)
-        hits, cp = oracle.mccp(path[:T], T, pm, np.float32(pb.offset_mult), obs)
-        assert np.float32(cp) == np.float32(res.soln_cp) and cp <= pb.cp_target
+    assert st == pumplib.PUMP_OK, L.pump_last_error()
+    print("large plan: edges %d, iterations %d, paths %d, expansions %d, sizes %s, cp %g, %.1f ms"
+          % (res.num_edges, res.iterations, res.num_paths, res.num_considered,
+             list(res.wavefront_sizes)[: res.iterations], res.soln_cp, res.ms_total))
+    assert res.success == 1 and res.wf_trace_len == 2 * res.num_considered
+    # the first wavefront against the oracle
+    m = int(res.wavefront_sizes[0])
+    tr = trace[: 2 * m].reshape(m, 2)
+    assert np.all(tr[:, 0] == 0)
+    r = large["roadmap"]
+    e = tr[:, 1].astype(np.int64)
+    src, dst, te = r["src"][e], r["dst"][e], r["te"][e]
+    d_src, d_dst, d_te = dev(torch, src), dev(torch, dst), dev(torch, te)
+    d_disc = empty(torch, m * W * 6, torch.float32)
+    pumplib.check(L.pump_discretize_edges(ptr(r["d_s"]), ptr(d_src), ptr(d_dst), ptr(d_te), m, nd,
+                                          pumplib.PUMP_BVP_PRECISION, ptr(d_disc), stream(torch)))
+    disc = host(d_disc).reshape(m, W, 6)
+    P, Pmc, T = int(pb.num_hsmc), int(pb.num_mc), int(pb.table_rows)
+    om = np.float32(pb.offset_mult)
+    maxd2 = np.float32(0.1 * np.float64(om) * np.float64(om))
+    maxHS = 5
+    a, b, _ = oracle.cache_halfspaces(disc, np.ones(m, np.uint8), obs, maxHS, maxd2)
+    tm, _ = oracle.particle_tables(int(pb.seed), Pmc, T, pmajor=False)
+    valid = np.zeros((1 + m, P), np.uint8)
+    valid[0] = 1
+    cp_o = np.zeros(1 + m, np.float32)
+    edges_local = np.arange(m, dtype=np.int32)
+    prev = np.zeros(m, np.int32)
+    times = np.zeros(1, np.float32)
+    oracle.lib().orc_hsmc_propagate(m, W, edges_local, prev, 1, a, b, times, te, 0.05, maxHS,
+                                    tm.reshape(-1), om, Pmc, valid, P, cp_o)
+    words = P // 32
+    packed = np.zeros((1 + m, words), np.uint32)
+    packed[0] = 0xFFFFFFFF
+    d_valid = dev(torch, packed.view(np.int32))
+    d_cp = empty(torch, 1 + m, torch.float32)
+    d_err = dev(torch, np.zeros(1, np.int32))
+    d_obs, d_e, d_p, d_t, d_tm = (dev(torch, x) for x in (obs, edges_local, prev, times, tm))
+    pumplib.check(L.pump_hsmc_propagate_boxes(m, W, ptr(d_e), ptr(d_p), m, 1, ptr(d_obs), obs.shape[0],
+                                              ptr(d_disc), float(maxd2), maxHS, ptr(d_t), ptr(d_te), 0.05,
+                                              ptr(d_tm), Pmc, T, float(om), ptr(d_valid), P, ptr(d_cp),
+                                              ptr(d_err), stream(torch)))
+    got = np.unpackbits(host(d_valid).view(np.uint32).reshape(1 + m, words).view(np.uint8), axis=1,
+                        bitorder="little")
+    assert int(host(d_err)[0]) == 0
+    assert np.array_equal(got[1:, :P], valid[1:])
+    assert np.array_equal(host(d_cp)[1:].view(np.uint32), cp_o[1:].view(np.uint32))
+    assert 0 < valid[1:].mean() <= 1
+    # the returned path, re-judged
+    T_len = res.path_len
+    _, pm = oracle.particle_tables(int(pb.seed), Pmc, T, tmajor=False)
+    hits, cp = oracle.mccp(path[:T_len], T_len, pm, om, obs)
+    assert np.float32(cp) == np.float32(res.soln_cp) and cp <= pb.cp_target

@@ -56,3 +56,29 @@ def test_path_point64_matches_reference_arithmetic(oracle):
     got = oracle.path_point64(t, tau, x0, x1)
     scale = np.maximum(1.0, np.abs(got))
     assert np.all(np.abs(ref - got) <= 4e-6 * scale)
+
+
+def test_disc_offsets_by_edge_length(oracle):
+    """Per-edge waypoint counts by edge length: ceil(L / disc_len) clamped to
+    [min, max], L = sqrt((dx*dx + dy*dy) + dz*dz) in binary32, each operation
+    rounded once; the offsets are their running sum plus one per edge; with
+    disc_len 0 every edge gets max."""
+    s = oracle.halton_samples(500, workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI)
+    rng = np.random.default_rng(6)
+    src = rng.integers(0, 500, 3000).astype(np.int32)
+    dst = rng.integers(0, 500, 3000).astype(np.int32)
+    for disc_len, lo, hi in ((0.025, 3, 31), (0.1, 1, 8), (0.0, 3, 8)):
+        off = oracle.disc_offsets(src, dst, s, disc_len, lo, hi)
+        d = (s[dst, :3] - s[src, :3]).astype(np.float32)
+        L = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+        nd = np.full(src.size, hi) if disc_len == 0 else np.clip(
+            np.ceil(L / np.float32(disc_len)), lo, hi).astype(np.int64)
+        assert np.array_equal(np.diff(off), nd + 1) and off[0] == 0
+    # the ragged waypoint stages with uniform offsets are the uniform ones
+    c, t = oracle.bvp_pairs(s[:60])
+    k = int(np.float32(59 * 60) * np.float32(0.05))
+    rn = oracle.lib().orc_select_kth(c.size, c, k)
+    es, ed, _ce, _te = oracle.build_edges(c, t, 60, rn)
+    off = oracle.disc_offsets(es, ed, s[:60], 0.0, 3, 8)
+    assert np.array_equal(oracle.discretize_edges_off(es, ed, s[:60], off).reshape(-1, 9, 6),
+                          oracle.discretize_edges(es, ed, s[:60], 8))
