@@ -425,6 +425,7 @@ class Query:
         L.pump_problem_defaults(C.byref(pb))
         pb.N, pb.num_disc, pb.num_hsmc = w["N"], w["num_disc"], w["P"]
         pb.num_mc = w.get("num_mc", pb.num_mc)
+        pb.max_paths = w.get("max_paths", 0)
         pb.num_obstacles, pb.obstacles = self.obs.shape[0], self.obs.ctypes.data
         for k in range(6):
             pb.init[k], pb.goal[k] = workloads.INIT[k], workloads.GOAL[k]
@@ -692,15 +693,17 @@ BIT_EXACT_AGAINST = {
 def large_record(lib, L, ctx, torch, flush):
     """The large configuration (N = 32000, 200 boxes with sides U[0.02, 0.1],
     noise 5e-3, 4096 particles for HSMC and MC CP, 16 waypoints per edge,
-    CP target 0.005, eta 2, precision BVP): one step of the device pipeline
-    after one warm-up, and the plan latency.  The reference cannot run it
+    CP target 0.005, eta 2, precision BVP, a path store of 2^24 paths: its
+    largest wavefront holds 14.1 M new paths, past the reference's 2 N
+    sqrt(N) = 11.4 M): one step of the device pipeline after one warm-up,
+    and the plan latency.  The reference cannot run it
     unmodified (its sample count is a compile-time array size and its
     particle tables hold 2048 particles), so it has no CPU baseline here."""
     from pump_gb300 import workloads
     cfg = workloads.CONFIGS["cfg4"]
     w = dict(N=cfg["N"], obstacles=cfg["obstacles"](0), offset_mult=np.float32(cfg["offset_mult"]),
              cp=cfg["cp"], eta=cfg["eta"], num_disc=cfg["num_disc"], P=cfg["num_hsmc"],
-             num_mc=cfg["num_mc"])
+             num_mc=cfg["num_mc"], max_paths=cfg["max_paths"])
     q = Query(lib, L, ctx, torch, w, "precision")
     pipe = q.pipeline(1, 1, flush)
     e2e_ms, res = q.e2e(2)
