@@ -528,13 +528,26 @@ class Query:
             kernel_ms.setdefault(name, []).append((a, b))
             launches["n"] += nk
 
+        stage = (C.c_float * 3)()
+        stage_ms = {}
+        # our kernels per pump_roadmap call: in the precision arithmetic the
+        # sample preparation, the bracket sample's costs, the bracket and the
+        # counted pair pass, the superset scan and emit; otherwise the pair
+        # pass, the bracket, the superset count, scan and emit; then the
+        # select (init, 3 histograms, 3 picks), the edge count, scan and
+        # emit, the row starts and the read-back pack
+        roadmap_launches = 6 + 13 if mode == lib.PUMP_BVP_PRECISION else 5 + 13
+
+        def roadmap():
+            lib.check(L.pump_roadmap(self.ctx.handle, d_s.data_ptr(), N, 5.0, mode, rn_idx, cap,
+                                     d_c.data_ptr(), d_t.data_ptr(), d_src.data_ptr(),
+                                     d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(),
+                                     d_go.data_ptr(), C.byref(rn), C.byref(Eo), stage, sh))
+            for name, v in zip(("rn_bracket", "bvp_pairs", "rn_edges"), stage):
+                stage_ms.setdefault(name, []).append(float(v))
+
         def step():
-            timed("bvp_pairs", lambda: lib.check(L.pump_bvp_pairs(d_s.data_ptr(), N, 5.0, mode,
-                                                                 d_c.data_ptr(), d_t.data_ptr(), sh)), 1)
-            timed("rn_edges", lambda: lib.check(L.pump_roadmap_edges(
-                self.ctx.handle, d_c.data_ptr(), d_t.data_ptr(), N, rn_idx, cap, d_src.data_ptr(),
-                d_dst.data_ptr(), d_ce.data_ptr(), d_te.data_ptr(), d_go.data_ptr(), C.byref(rn),
-                C.byref(Eo), sh)), 12)
+            timed("roadmap", roadmap, roadmap_launches)
             timed("discretize", lambda: lib.check(L.pump_discretize_edges(
                 d_s.data_ptr(), d_src.data_ptr(), d_dst.data_ptr(), d_te.data_ptr(), Eo.value, W - 1,
                 mode, d_disc.data_ptr(), sh)), 1)
@@ -575,6 +588,9 @@ class Query:
             step_ms.append(a.elapsed_time(b))
         torch.cuda.synchronize()
         ks = {k: sum(a.elapsed_time(b) for a, b in v) / steps for k, v in kernel_ms.items()}
+        # the pair kernel and the stages around it, from the library's own
+        # events on the same stream (the timed steps' calls only)
+        ks.update({k: sum(v[-steps:]) / steps for k, v in stage_ms.items()})
         return {"units": units, "E": E, "M": M_total, "W": W, "maxHS": maxHS, "sizes": sizes,
                 "step_ms": step_ms, "kernel_ms": ks, "launches": launches["n"],
                 "per_step_units": {"pairs": npairs, "edges": E, "expansions": M_total}}
@@ -626,7 +642,9 @@ def run_ours(args):
     if rank == 0:
         value = all_units * args.steps / (tot / 1e3)
         e2e_value = all_units * max(1, args.steps) / (tot_e2e / 1e3)
-        dom = max(ks, key=ks.get)
+        # the dominant kernel: "roadmap" is the whole pump_roadmap call, whose
+        # stages (the pair kernel among them) are listed on their own
+        dom = max((k for k in ks if k != "roadmap"), key=ks.get)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True,

@@ -119,6 +119,22 @@ pump_status_t pump_roadmap_edges(pump_ctx *ctx, const float *d_copts, const floa
                                  float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
                                  long long *h_num_edges, pump_stream_t stream);
 
+/* The roadmap's device half in one call (mainPUMP.cu:248-346):
+ * fillCoptsTopts over all N(N-1) ordered pairs of d_samples[N][6] (tmax,
+ * arithmetic bvp_mode, as pump_bvp_pairs) into d_copts/d_topts, then rn =
+ * the k-th smallest pair cost and the edges below it, as
+ * pump_roadmap_edges.  The outputs are those of the two calls.  In
+ * PUMP_BVP_PRECISION the pair kernel counts the rn superset while it stores
+ * the costs, so the costs are read once more instead of twice.
+ * h_stage_ms (optional, 3 floats): CUDA-event times, in ms, of the work
+ * before the pair kernel (sample preparation and the rn bracket's sample),
+ * of the pair kernel, and of the rest.  Synchronises. */
+pump_status_t pump_roadmap(pump_ctx *ctx, const float *d_samples, int N, float tmax, int bvp_mode,
+                           long long k, long long max_edges, float *d_copts, float *d_topts,
+                           int *d_src, int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
+                           float *h_rn, long long *h_num_edges, float *h_stage_ms,
+                           pump_stream_t stream);
+
 /* Edge waypoints disc[E][numDisc+1][6] (findDiscretizedPath, 2pBVP.cu:53-69
  * and pathPoint 2pBVP.cu:117-131, as called at mainPUMP.cu:339).  d_topt
  * is the edge's optimal time (identical to the one toptBisection recomputes

@@ -25,12 +25,34 @@ namespace pump {
 namespace {
 
 // ---------------------------------------------------------------- parity
+// binary32 -> binary64 conversion, exact, on the integer pipe: the binary64
+// bit pattern of a normal binary32 (or a zero) is its sign, its exponent
+// rebiased by 1023 - 127 and its 23 mantissa bits shifted up by 29.
+// Subnormal, infinite and NaN inputs take the hardware conversion.  On this
+// GPU the binary64 pipe, which also executes conversions, bounds the parity
+// kernel, so moving them to integer instructions shortens it.
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xFFu;
+  if (e == 0xFFu || (e == 0u && (u & 0x7FFFFFu) != 0u)) return (double)f;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if (e == 0u) return __longlong_as_double((long long)sign);  // +-0
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
+// The bisection's stopping test compares a binary32 |dcval| with the
+// binary64 constant 0.0001 (2pBVP.cu:86).  binary32 0.0001f is below 0.0001
+// and the next binary32 above it, so (double)x > 0.0001 exactly when
+// x > 0.0001f (NaN false either way): the test runs in binary32.
+constexpr float kDcvalTol = 0.0001f;
+
 struct PairCoef {
   double s7;                                     // first seven (tau-free) terms
   float k8, k9, k10, k11, k12, k13, k14, k15;    // float prefixes of the t-linear terms
   double d16, d17, d18, d20, d22, d24;           // 4*pow(x,2) coefficients of t^2
-  float f19, f21, f23;                           // 4*x*y float coefficients of t^2
-  float f25, f26;                                // 2*g*x coefficients of t^3
+  double f19, f21, f23;                          // 4*x*y binary32 coefficients of t^2, converted
+  double f25, f26;                               // 2*g*x binary32 coefficients of t^3, converted
   float a29, b29, c29, a30, b30, c30;            // last two float terms
 };
 
@@ -56,14 +78,14 @@ __device__ __forceinline__ PairCoef make_coef(const float *x0, const float *x1) 
   c.d16 = 4 * p2f(x0[4]);
   c.d17 = 4 * p2f(x0[3]);
   c.d18 = 4 * p2f(x0[5]);
-  c.f19 = 4 * x0[4] * x1[4];
+  c.f19 = f2d(4 * x0[4] * x1[4]);
   c.d20 = 4 * p2f(x1[4]);
-  c.f21 = 4 * x0[3] * x1[3];
+  c.f21 = f2d(4 * x0[3] * x1[3]);
   c.d22 = 4 * p2f(x1[3]);
-  c.f23 = 4 * x0[5] * x1[5];
+  c.f23 = f2d(4 * x0[5] * x1[5]);
   c.d24 = 4 * p2f(x1[5]);
-  c.f25 = 2 * g * x0[5];
-  c.f26 = 2 * g * x1[5];
+  c.f25 = f2d(2 * g * x0[5]);
+  c.f26 = f2d(2 * g * x1[5]);
   c.a29 = 12 * x0[0];
   c.b29 = -2 * x1[0];
   c.c29 = x0[3] + x1[3];
@@ -76,32 +98,32 @@ __device__ __forceinline__ PairCoef make_coef(const float *x0, const float *x1) 
 // cost(tau, x0, x1), 2pBVP.cu:97-107, term order preserved.
 __device__ __forceinline__ float cost_eval(const PairCoef &c, float tau) {
   const double g2 = p2f(PUMP_G);
-  const double dt = tau;
+  const double dt = f2d(tau);
   const double t2 = dt * dt, t3 = t2 * dt, t4 = t2 * t2;
   double s = c.s7;
-  s = s + (double)(c.k8 * tau);
-  s = s + (double)(c.k9 * tau);
-  s = s - (double)(c.k10 * tau);
-  s = s - (double)(c.k11 * tau);
-  s = s - (double)(c.k12 * tau);
-  s = s - (double)(c.k13 * tau);
-  s = s - (double)(c.k14 * tau);
-  s = s - (double)(c.k15 * tau);
+  s = s + f2d(c.k8 * tau);
+  s = s + f2d(c.k9 * tau);
+  s = s - f2d(c.k10 * tau);
+  s = s - f2d(c.k11 * tau);
+  s = s - f2d(c.k12 * tau);
+  s = s - f2d(c.k13 * tau);
+  s = s - f2d(c.k14 * tau);
+  s = s - f2d(c.k15 * tau);
   s = s + c.d16 * t2;
   s = s + c.d17 * t2;
   s = s + c.d18 * t2;
-  s = s + (double)c.f19 * t2;
+  s = s + c.f19 * t2;
   s = s + c.d20 * t2;
-  s = s + (double)c.f21 * t2;
+  s = s + c.f21 * t2;
   s = s + c.d22 * t2;
-  s = s + (double)c.f23 * t2;
+  s = s + c.f23 * t2;
   s = s + c.d24 * t2;
-  s = s + (double)c.f25 * t3;
-  s = s - (double)c.f26 * t3;
+  s = s + c.f25 * t3;
+  s = s - c.f26 * t3;
   s = s + t4;
   s = s + g2 * t4;
-  s = s + (double)(c.a29 * (c.b29 + c.c29 * tau));
-  s = s + (double)(c.a30 * (c.b30 + c.c30 * tau));
+  s = s + f2d(c.a29 * (c.b29 + c.c29 * tau));
+  s = s + f2d(c.a30 * (c.b30 + c.c30 * tau));
   return (float)((1.0 / t3) * s);
 }
 
@@ -126,7 +148,7 @@ __device__ float topt_bisection(const PairCoef &c, float tmax) {
   float topt = 0;
   float dcval = 1;
   int itr = 0;
-  while ((double)fabsf(dcval) > 0.0001 && itr < 50) {
+  while (fabsf(dcval) > kDcvalTol && itr < 50) {
     ++itr;
     topt = (tu + tl) / 2;
     dcval = dcost_eval(c, topt);
@@ -212,7 +234,7 @@ __global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
     } else if (phase == 2) {
       dcval = d;
       if (dcval > 0) tu = topt; else tl = topt;
-      if (!((double)fabsf(dcval) > 0.0001 && itr < 50)) phase = 3;
+      if (!(fabsf(dcval) > kDcvalTol && itr < 50)) phase = 3;
     } else {
       topts[idx] = topt;
       copts[idx] = ca;

@@ -57,6 +57,58 @@ __global__ void __launch_bounds__(T) bvp_pairs_precision_kernel(const SampleF *_
   copts[idx] = d2f_rn(c);
 }
 
+// Costs of the bracket-sample pairs: pair number floor((2q + 1) n / (2 S))
+// for q < S, n = N(N-1).
+__global__ void bracket_costs_kernel(const SampleF *__restrict__ sf, int N, float tmax, int S,
+                                     unsigned int *__restrict__ out_bits) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= S) return;
+  const long long n = (long long)N * (N - 1);
+  const long long pos = ((2LL * q + 1) * n) / (2LL * S);
+  const int i = (int)(pos / (N - 1));
+  const int r = (int)(pos - (long long)i * (N - 1));
+  const int j = r + (r >= i);
+  double t, c;
+  precise_tau(load_sample(sf, i), load_sample(sf, j), tmax, &t, &c);
+  out_bits[q] = __float_as_uint(d2f_rn(c));
+}
+
+// bvp_pairs_precision_kernel plus the count pass of the rn superset: each
+// warp adds its pairs whose cost's order key is below *key_hi to the counts
+// of their 4096-pair tiles (a warp's 32 consecutive pairs meet at most two
+// tiles: one atomic for each).  A warp wholly past its row's end leaves at
+// once; the others reach the ballots with every lane.
+template <int T>
+__global__ void __launch_bounds__(T) bvp_pairs_precision_counted_kernel(
+    const SampleF *__restrict__ sf, int N, float tmax, float *__restrict__ copts,
+    float *__restrict__ topts, const unsigned long long *__restrict__ key_hi,
+    unsigned int *__restrict__ tile_counts) {
+  const int i = blockIdx.y;
+  const int lane = threadIdx.x & 31;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r - lane >= N - 1) return;
+  const long long idx = (long long)i * (N - 1) + r;
+  bool sel = false;
+  if (r < N - 1) {
+    const int j = r + (r >= i);
+    double t, c;
+    precise_tau(load_sample(sf, i), load_sample(sf, j), tmax, &t, &c);
+    const unsigned int cb = __float_as_uint(d2f_rn(c));
+    topts[idx] = d2f_rn(t);
+    reinterpret_cast<unsigned int *>(copts)[idx] = cb;
+    sel = (unsigned long long)key_of_bits(cb) < __ldg(key_hi);
+  }
+  const unsigned int m = __ballot_sync(0xffffffffu, sel);
+  if (m) {
+    const long long t0 = (idx - lane) / kRnCountTile;
+    const unsigned int in0 = __ballot_sync(0xffffffffu, sel && idx / kRnCountTile == t0);
+    if (lane == 0) {
+      if (in0) atomicAdd(&tile_counts[t0], (unsigned int)__popc(in0));
+      if (m & ~in0) atomicAdd(&tile_counts[t0 + 1], (unsigned int)__popc(m & ~in0));
+    }
+  }
+}
+
 __global__ void bvp_batch_precision_kernel(const BvpJobs jb) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= jb.n * jb.jobs) return;
@@ -98,6 +150,36 @@ pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tm
     bool ran = false;
     st = tune_choice(kTuneBvpPairs, tune_bucket(N), 3, 1, stream, run, &choice, &ran);
     if (st == PUMP_OK && !ran) st = run(choice);
+  }
+  cudaFreeAsync(sd, stream);
+  return st;
+}
+
+pump_status_t bvp_pairs_precision_counted(const float *d_samples, int N, float tmax,
+                                          float *d_copts, float *d_topts, int S,
+                                          float *d_sample_costs,
+                                          const std::function<pump_status_t()> &bracket,
+                                          const unsigned long long *d_key_hi,
+                                          unsigned int *d_tile_counts, cudaStream_t stream) {
+  if (N > 65535) return set_error(PUMP_ERR_CAPACITY, "bvp_pairs: N = %d exceeds 65535 rows", N);
+  SampleF *sd = nullptr;
+  PUMP_CUDA_TRY(pool_malloc_async((void **)&sd, sizeof(SampleF) * (size_t)N, stream));
+  prepare_samples_kernel<<<grid_for(N, 128), 128, 0, stream>>>(d_samples, N, sd);
+  pump_status_t st = launch_status("prepare_samples");
+  if (st == PUMP_OK) {
+    bracket_costs_kernel<<<grid_for(S, 64), 64, 0, stream>>>(
+        sd, N, tmax, S, reinterpret_cast<unsigned int *>(d_sample_costs));
+    st = launch_status("bracket_costs");
+  }
+  if (st == PUMP_OK) st = bracket();
+  if (st == PUMP_OK) {
+    // the block size of the plain pass's default (the tuner's three shapes
+    // measure within 1 % of each other)
+    constexpr int T = 128;
+    const dim3 grid(grid_for(N - 1, T), (unsigned)N);
+    bvp_pairs_precision_counted_kernel<T><<<grid, T, 0, stream>>>(sd, N, tmax, d_copts, d_topts,
+                                                                 d_key_hi, d_tile_counts);
+    st = launch_status("bvp_pairs_precision_counted");
   }
   cudaFreeAsync(sd, stream);
   return st;

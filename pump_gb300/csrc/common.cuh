@@ -49,6 +49,19 @@ inline unsigned int grid_for(long long n, int threads) {
   return (unsigned int)g;
 }
 
+// Order-preserving 32-bit keys of binary32 values (negative NaNs first,
+// positive NaNs last), computed from the value's bits.  Keys are built from
+// integer loads of the cost arrays and results stored as integers: a value
+// that passes through a float register may come back with other NaN bits
+// (code generated for a float load feeding a select turned positive NaNs
+// into the key of -0.0).
+__device__ __forceinline__ uint32_t key_of_bits(uint32_t u) {
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ uint32_t bits_of_key(uint32_t k) {
+  return (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+}
+
 // ---------------------------------------------------------------------------
 // Integer powers of a float promoted to double, correctly rounded: the square
 // of a float is exact in binary64, so each result below is rounded once.

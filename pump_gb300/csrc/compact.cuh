@@ -284,11 +284,23 @@ __device__ __forceinline__ void tile_ballots(const L &ld, const typename L::Stat
   }
 }
 
+// The item count: n, or *d_n when d_n is given and below n (a count left on
+// the device by an earlier kernel; n is then the bound the grid was sized for).
+__device__ __forceinline__ long long device_count(long long n, const unsigned long long *d_n) {
+  if (d_n) {
+    const unsigned long long d = *d_n;
+    if ((long long)d < n) n = (long long)d;
+  }
+  return n;
+}
+
 // counts[tile] += each warp's selected count (counts zeroed before launch).
 template <class L>
 __global__ void __launch_bounds__(kCompactThreads) tile_count_kernel(long long n, L ld,
-                                                                     unsigned int *counts) {
+                                                                     unsigned int *counts,
+                                                                     const unsigned long long *d_n) {
   const int lane = threadIdx.x & 31;
+  n = device_count(n, d_n);
   const long long ntiles = (n + kTile - 1) / kTile;
   const typename L::State st = ld.begin();
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -303,11 +315,13 @@ __global__ void __launch_bounds__(kCompactThreads) tile_count_kernel(long long n
 }
 
 // One block of 1024 threads: offsets[t] = counts[0] + .. + counts[t-1] and
-// *total = the sum of all; each thread scans a contiguous run of tiles.
+// *total (and *copy_to, when given) = the sum of all; each thread scans a
+// contiguous run of tiles.
 __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned int *__restrict__ counts,
                                                          long long ntiles,
                                                          unsigned long long *__restrict__ offsets,
-                                                         unsigned long long *total) {
+                                                         unsigned long long *total,
+                                                         unsigned long long *copy_to) {
   __shared__ unsigned long long s_warp[32];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const long long per = (ntiles + 1023) / 1024;
@@ -331,7 +345,10 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned int *__r
       if (lane >= o) wi += u;
     }
     s_warp[lane] = wi - w;
-    if (lane == 31) *total = wi;
+    if (lane == 31) {
+      *total = wi;
+      if (copy_to) *copy_to = wi;
+    }
   }
   __syncthreads();
   unsigned long long run = s_warp[warp] + incl - sum;
@@ -343,9 +360,11 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const unsigned int *__r
 
 template <class L>
 __global__ void __launch_bounds__(kCompactThreads) tile_emit_kernel(
-    long long n, L ld, const unsigned long long *__restrict__ offsets) {
+    long long n, L ld, const unsigned long long *__restrict__ offsets,
+    const unsigned long long *d_n) {
   __shared__ unsigned int cnt[kCompactRows][kCompactThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  n = device_count(n, d_n);
   const long long ntiles = (n + kTile - 1) / kTile;
   const typename L::State st = ld.begin();
   const unsigned int lt = (1u << lane) - 1u;
@@ -371,25 +390,43 @@ __global__ void __launch_bounds__(kCompactThreads) tile_emit_kernel(
   }
 }
 
-// Three-kernel compaction of n items; the count lands in *ts_out->total (the
-// error word stays zero: nothing waits).  blocks_per_sm sets the count and
-// emit grids (the autotuner's choice where a caller tunes it).
+// The scan and emit kernels of a three-kernel compaction whose tile counts
+// are in place (ts from prepare_tiles; ntiles tiles).
+template <class L>
+pump_status_t run_chunked_emit(long long n, long long ntiles, const L &ld, cudaStream_t stream,
+                               const TileScratch &ts, int blocks_per_sm,
+                               const unsigned long long *d_n) {
+  const long long grid = (long long)kNumSMs * blocks_per_sm;
+  const unsigned blocks = (unsigned)(ntiles < grid ? ntiles : grid);
+  tile_scan_kernel<<<1, 1024, 0, stream>>>(reinterpret_cast<unsigned int *>(ts.status), ntiles,
+                                           ts.offsets, ts.total, ts.copy_to);
+  PUMP_TRY(launch_status("tile_scan_kernel"));
+  tile_emit_kernel<<<blocks, kCompactThreads, 0, stream>>>(n, ld, ts.offsets, d_n);
+  return launch_status("tile_emit_kernel");
+}
+
+// Three-kernel compaction of n items (or of *d_n, when given and below n);
+// the count lands in *ts_out->total and, when given, in *copy_to (the
+// compaction scratch, and with it *total, is reused by the next compaction
+// on the context).  The error word stays zero: nothing waits.
+// blocks_per_sm sets the count and emit grids (the autotuner's choice where
+// a caller tunes it).
 template <class L>
 pump_status_t run_chunked(Ctx *ctx, long long n, const L &ld, cudaStream_t stream,
-                          TileScratch *ts_out, int blocks_per_sm = kTileBlocks / kNumSMs) {
+                          TileScratch *ts_out, int blocks_per_sm = kTileBlocks / kNumSMs,
+                          const unsigned long long *d_n = nullptr,
+                          unsigned long long *copy_to = nullptr) {
   TileScratch ts{};
   long long ntiles = 0;
   PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));  // zeroed status words hold the counts
+  ts.copy_to = copy_to;
   if (n > 0) {
     const long long grid = (long long)kNumSMs * blocks_per_sm;
     const unsigned blocks = (unsigned)(ntiles < grid ? ntiles : grid);
     unsigned int *counts = reinterpret_cast<unsigned int *>(ts.status);
-    tile_count_kernel<<<blocks, kCompactThreads, 0, stream>>>(n, ld, counts);
+    tile_count_kernel<<<blocks, kCompactThreads, 0, stream>>>(n, ld, counts, d_n);
     PUMP_TRY(launch_status("tile_count_kernel"));
-    tile_scan_kernel<<<1, 1024, 0, stream>>>(counts, ntiles, ts.offsets, ts.total);
-    PUMP_TRY(launch_status("tile_scan_kernel"));
-    tile_emit_kernel<<<blocks, kCompactThreads, 0, stream>>>(n, ld, ts.offsets);
-    PUMP_TRY(launch_status("tile_emit_kernel"));
+    PUMP_TRY(run_chunked_emit(n, ntiles, ld, stream, ts, blocks_per_sm, d_n));
   }
   *ts_out = ts;
   return PUMP_OK;
@@ -399,9 +436,27 @@ pump_status_t run_chunked(Ctx *ctx, long long n, const L &ld, cudaStream_t strea
 // for shape class (kernel, the input size's power-of-two bucket).
 template <class L>
 pump_status_t run_chunked_tuned(Ctx *ctx, int kernel, long long n, const L &ld,
-                                cudaStream_t stream, TileScratch *ts_out) {
+                                cudaStream_t stream, TileScratch *ts_out,
+                                const unsigned long long *d_n = nullptr,
+                                unsigned long long *copy_to = nullptr) {
   static const int kPerSm[3] = {2, 4, 8};
-  auto run = [&](int c) { return run_chunked(ctx, n, ld, stream, ts_out, kPerSm[c]); };
+  auto run = [&](int c) {
+    return run_chunked(ctx, n, ld, stream, ts_out, kPerSm[c], d_n, copy_to);
+  };
+  int choice = 1;
+  bool ran = false;
+  PUMP_TRY(tune_choice(kernel, tune_bucket(n), 3, 1, stream, run, &choice, &ran));
+  return ran ? PUMP_OK : run(choice);
+}
+
+// run_chunked_emit with the emit grid of the autotuner's record for
+// (kernel, n's bucket); a first call tunes the scan and emit pair (each
+// candidate rewrites the same outputs from the same counts).
+template <class L>
+pump_status_t run_chunked_emit_tuned(int kernel, long long n, long long ntiles, const L &ld,
+                                     cudaStream_t stream, const TileScratch &ts) {
+  static const int kPerSm[3] = {2, 4, 8};
+  auto run = [&](int c) { return run_chunked_emit(n, ntiles, ld, stream, ts, kPerSm[c], nullptr); };
   int choice = 1;
   bool ran = false;
   PUMP_TRY(tune_choice(kernel, tune_bucket(n), 3, 1, stream, run, &choice, &ran));

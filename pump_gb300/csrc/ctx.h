@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <functional>
 #include <vector>
 
 #include "pump.h"
@@ -120,22 +121,54 @@ pump_status_t select_kth_pairs(Ctx *ctx, const PairView &pv, long long k, const 
 pump_status_t build_edges_pairs(Ctx *ctx, const PairView &pv, float rn, long long max_edges,
                                 int *d_src, int *d_dst, float *d_copt, float *d_topt,
                                 int *d_go_start, long long *h_num_edges, cudaStream_t stream);
+// rn and the edge count of the one-read rn selection, left on the device
+// until the caller's next read-back.  ok = 0: the superset of the pass
+// missed rank k or overflowed its buffer; rn_bits and edges are then
+// meaningless and the caller runs the matching *_fallback function.  edges
+// exceeds max_edges when the edges did not fit (only max_edges were written).
+struct RnEdgesPack {
+  uint32_t rn_bits;
+  int ok;
+  unsigned long long edges;
+};
+
 // rn (the k-th smallest pair cost) and the edges below it in one read of the
 // pair costs, from the query's own pair arrays or its pair view.  With
-// deferred_total, the edge count may be left on the device: then
-// *h_num_edges is -1, *deferred_total points at the count (read it after a
-// synchronisation; it exceeds max_edges when the edges did not fit, and then
-// only max_edges were written) and the row starts are already built.
+// `deferred`, nothing is read back: *h_num_edges is -1, *deferred points at
+// the device pack (read it after a synchronisation) and the row starts are
+// already built from the device count.
 pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
                               long long k, long long max_edges, int *d_src, int *d_dst,
                               float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
                               long long *h_num_edges, cudaStream_t stream,
-                              const unsigned long long **deferred_total = nullptr);
+                              const RnEdgesPack **deferred = nullptr);
 pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long long max_edges,
                              int *d_src, int *d_dst, float *d_copt, float *d_topt,
                              int *d_go_start, float *h_rn, long long *h_num_edges,
-                             cudaStream_t stream,
-                             const unsigned long long **deferred_total = nullptr);
+                             cudaStream_t stream, const RnEdgesPack **deferred = nullptr);
+// The exact three-pass select over all pairs and the full compaction
+// (synchronises): what a pack with ok = 0 falls back to.
+pump_status_t rn_edges_fallback_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
+                                       long long k, long long max_edges, int *d_src, int *d_dst,
+                                       float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
+                                       long long *h_num_edges, cudaStream_t stream);
+pump_status_t rn_edges_fallback_pairs(Ctx *ctx, const PairView &pv, long long k,
+                                      long long max_edges, int *d_src, int *d_dst, float *d_copt,
+                                      float *d_topt, int *d_go_start, float *h_rn,
+                                      long long *h_num_edges, cudaStream_t stream);
+// All N(N-1) pair BVPs of the samples (tmax, arithmetic bvp_mode), then rn
+// and the edges as rn_edges_device.  In the precision arithmetic the pair
+// kernel also counts the rn superset as it stores the costs (the bracket
+// sample's costs are computed first), so the costs are read once after the
+// pair pass instead of twice.  stage_ms (optional, non-deferred only; 3
+// floats): CUDA-event times of what precedes the pair kernel (the samples'
+// preparation and the bracket), the pair kernel, and the rest.
+pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float tmax,
+                                  int bvp_mode, long long k, long long max_edges, float *d_copts,
+                                  float *d_topts, int *d_src, int *d_dst, float *d_copt,
+                                  float *d_topt, int *d_go_start, float *h_rn,
+                                  long long *h_num_edges, cudaStream_t stream,
+                                  const RnEdgesPack **deferred = nullptr, float *stage_ms = nullptr);
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                       int *d_count, int **d_error_out, cudaStream_t stream);
 pump_status_t particle_rowmax_async(const float *d_table, int P, int T, float *d_rowmax,
@@ -144,6 +177,20 @@ pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor
                                     cudaStream_t stream);
 pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tmax, float *d_copts,
                                          float *d_topts, cudaStream_t stream);
+// Pairs per count tile of the rn superset pass (the tile of compact.cuh).
+constexpr int kRnCountTile = 4096;
+// The precision pair pass with the rn superset counted as the costs are
+// stored: first the costs of the S bracket-sample pairs (positions
+// floor((2q + 1) n / (2 S)) of the N(N-1) pair order) into d_sample_costs,
+// then bracket() (launches the kernel that turns them into *d_key_hi), then
+// all pairs, adding to d_tile_counts[p / kRnCountTile] the pairs p whose
+// cost's order key is below *d_key_hi (the counts start zeroed).
+pump_status_t bvp_pairs_precision_counted(const float *d_samples, int N, float tmax,
+                                          float *d_copts, float *d_topts, int S,
+                                          float *d_sample_costs,
+                                          const std::function<pump_status_t()> &bracket,
+                                          const unsigned long long *d_key_hi,
+                                          unsigned int *d_tile_counts, cudaStream_t stream);
 // Explicit pairs (x0[k], x1[k]), k < n (x1[0] for every k with x1_same),
 // each bisected for `jobs` (1 or 2)
 // optimal-time limits: job j writes topt[j][k] and cost[j][k] (either may be

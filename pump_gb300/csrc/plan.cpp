@@ -334,7 +334,11 @@ class Planner {
   DevBuf<int> d_scalar_;    // one int read back with the roadmap
   int max_degree_ = 0;      // largest out-degree of the roadmap
   long long E_ = 0;
-  const unsigned long long *d_total_ = nullptr;  // edge count left on the device by the roadmap
+  // rn and the edge count left on the device by the roadmap (null when they
+  // were read back already), and the pair view of a batched query's costs
+  const RnEdgesPack *d_pack_ = nullptr;
+  PairView pv_{};
+  bool use_pv_ = false;
   float rn_ = 0;
   DevBuf<float> d_h_;  // heuristic per node (cost to the goal)
   float h0_ = 0;
@@ -399,8 +403,9 @@ pump_status_t Planner::roadmap() {
   const size_t nsf = (size_t)N_ * kDim;
   PUMP_TRY(d_samples_.alloc(nsf + kDim));
   float *hout = nullptr;
-  // (then the edge count when it stays on the device until this read-back)
-  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float) * (2 + nsf) + sizeof(unsigned long long),
+  // (then rn and the edge count when they stay on the device until this
+  // read-back; 2 + nsf floats keep the pack 8-byte aligned)
+  PUMP_TRY(ctx_->pinned(Ctx::kPinOut, sizeof(float) * (2 + nsf) + sizeof(RnEdgesPack),
                         (void **)&hout));
   if (pb_.samples) {
     samples_.assign(pb_.samples, pb_.samples + nsf);
@@ -441,16 +446,15 @@ pump_status_t Planner::roadmap() {
   PUMP_TRY(d_coptE_.alloc(cap));
   PUMP_TRY(d_toptE_.alloc(cap));
   PUMP_TRY(d_go_.alloc(N_ + 1));
+  use_pv_ = false;
   if (shared_ && shared_->matches(pb_)) {
     PUMP_TRY(pair_costs_shared(rnIdx, cap));
   } else {
     PUMP_TRY(d_copts_.alloc(npairs));
     PUMP_TRY(d_topts_.alloc(npairs));
-    PUMP_TRY(pump_bvp_pairs(d_samples_.p, N_, 5.0f, pb_.bvp_mode, d_copts_.p, d_topts_.p,
-                            (pump_stream_t)s_));
-    PUMP_TRY(rn_edges_device(ctx_, d_copts_.p, d_topts_.p, N_, rnIdx, cap, d_src_.p, d_dst_.p,
-                             d_coptE_.p, d_toptE_.p, d_go_.p, &rn_, &E_, s_, &d_total_));
-    res_->rn = rn_;
+    PUMP_TRY(roadmap_pairs_edges(ctx_, d_samples_.p, N_, 5.0f, pb_.bvp_mode, rnIdx, cap, d_copts_.p,
+                                 d_topts_.p, d_src_.p, d_dst_.p, d_coptE_.p, d_toptE_.p, d_go_.p,
+                                 &rn_, &E_, s_, &d_pack_));
   }
   // the edges' waypoints (findDiscretizedPath) are written by the edge
   // checks; with the edge count still on the device, sized for the capacity
@@ -458,17 +462,36 @@ pump_status_t Planner::roadmap() {
   PUMP_TRY(d_scalar_.alloc(1));
   PUMP_TRY(max_degree_async(d_go_.p, N_, d_scalar_.p, s_));
   PUMP_CUDA_TRY(cudaMemcpyAsync(hout + 1, d_scalar_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
-  unsigned long long *htotal = reinterpret_cast<unsigned long long *>(hout + 2 + nsf);
-  if (d_total_)
-    PUMP_CUDA_TRY(cudaMemcpyAsync(htotal, d_total_, sizeof(unsigned long long),
-                                  cudaMemcpyDeviceToHost, s_));
+  RnEdgesPack *hpack = reinterpret_cast<RnEdgesPack *>(hout + 2 + nsf);
+  if (d_pack_)
+    PUMP_CUDA_TRY(cudaMemcpyAsync(hpack, d_pack_, sizeof(RnEdgesPack), cudaMemcpyDeviceToHost, s_));
   PUMP_TRY(sync());
-  if (d_total_) {
-    if ((long long)*htotal > cap)
-      return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", *htotal,
-                       cap);
-    E_ = (long long)*htotal;
+  if (d_pack_) {
+    const RnEdgesPack pk = *hpack;
+    d_pack_ = nullptr;
+    if (!pk.ok) {
+      // the bracket sample misled the one-read pass: the exact select over
+      // all pairs and the full compaction (rebuilding the row starts), then
+      // the largest out-degree again
+      if (use_pv_)
+        PUMP_TRY(rn_edges_fallback_pairs(ctx_, pv_, rnIdx, cap, d_src_.p, d_dst_.p, d_coptE_.p,
+                                         d_toptE_.p, d_go_.p, &rn_, &E_, s_));
+      else
+        PUMP_TRY(rn_edges_fallback_device(ctx_, d_copts_.p, d_topts_.p, N_, rnIdx, cap, d_src_.p,
+                                          d_dst_.p, d_coptE_.p, d_toptE_.p, d_go_.p, &rn_, &E_,
+                                          s_));
+      PUMP_TRY(max_degree_async(d_go_.p, N_, d_scalar_.p, s_));
+      PUMP_CUDA_TRY(cudaMemcpyAsync(hout + 1, d_scalar_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
+      PUMP_TRY(sync());
+    } else {
+      if ((long long)pk.edges > cap)
+        return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld",
+                         pk.edges, cap);
+      std::memcpy(&rn_, &pk.rn_bits, sizeof(float));
+      E_ = (long long)pk.edges;
+    }
   }
+  res_->rn = rn_;
   res_->num_edges = E_;
   if (pb_.bvp_mode == PUMP_BVP_PARITY_GPU) {
     PUMP_TRY(d_toptH_.alloc(E_ > 0 ? E_ : 1));
@@ -499,7 +522,7 @@ pump_status_t Planner::pair_costs_shared(long long rnIdx, long long cap) {
   PUMP_TRY(d_own_t_.alloc(own));
   PUMP_TRY(pump_bvp_batch(d_bx0_.p, d_bx1_.p, (int)own, 5.0f, pb_.bvp_mode, d_own_t_.p, d_own_c_.p,
                           (pump_stream_t)s_));
-  PairView pv;
+  PairView &pv = pv_;
   pv.N = N;
   pv.M = shared_->M;
   pv.sc = shared_->d_copt;
@@ -512,10 +535,9 @@ pump_status_t Planner::pair_costs_shared(long long rnIdx, long long cap) {
   pv.grt = d_own_t_.p + 2 * (N - 1);
   pv.gcc = d_own_c_.p + 2 * (N - 1) + (N - 2);
   pv.gct = d_own_t_.p + 2 * (N - 1) + (N - 2);
-  PUMP_TRY(rn_edges_pairs(ctx_, pv, rnIdx, cap, d_src_.p, d_dst_.p, d_coptE_.p, d_toptE_.p,
-                          d_go_.p, &rn_, &E_, s_, &d_total_));
-  res_->rn = rn_;
-  return PUMP_OK;
+  use_pv_ = true;
+  return rn_edges_pairs(ctx_, pv, rnIdx, cap, d_src_.p, d_dst_.p, d_coptE_.p, d_toptE_.p, d_go_.p,
+                        &rn_, &E_, s_, &d_pack_);
 }
 
 pump_status_t Planner::online() {

@@ -23,18 +23,6 @@ namespace pump {
 namespace {
 
 
-// Order-preserving 32-bit keys of binary32 values (negative NaNs first,
-// positive NaNs last), computed from the value's bits.  Keys are built from
-// integer loads of the cost arrays and results stored as integers: a value
-// that passes through a float register may come back with other NaN bits
-// (code generated for a float load feeding a select turned positive NaNs
-// into the key of -0.0).
-__device__ __forceinline__ uint32_t key_of_bits(uint32_t u) {
-  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ uint32_t bits_of_key(uint32_t k) {
-  return (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
-}
 __device__ __forceinline__ uint32_t ldg_bits(const float *p) {
   return __ldg(reinterpret_cast<const unsigned int *>(p));
 }
@@ -372,19 +360,19 @@ struct EdgeLoader {
   }
 };
 
-// rn's bits and the superset size for one read-back.
-struct RnPack {
-  uint32_t rn_bits;
-  int pad;
-  unsigned long long n_sup;
-};
-__global__ void rn_pack_kernel(const float *rn, const unsigned long long *n_sup, RnPack *out) {
+// rn's bits, whether the superset held rank k within its buffer, and the
+// edge count, for one read-back.
+__global__ void rn_pack_kernel(const float *rn, const unsigned long long *n_sup,
+                               const unsigned long long *edges, long long k, long long cap,
+                               RnEdgesPack *out) {
+  const unsigned long long ns = *n_sup;
   out->rn_bits = *reinterpret_cast<const unsigned int *>(rn);
-  out->pad = 0;
-  out->n_sup = *n_sup;
+  out->ok = (long long)ns > k && (long long)ns <= cap;
+  out->edges = *edges;
 }
 
 // Edges from the superset: entries with cost < rn, in superset (= pair) order.
+// rn is read on the device (the select's result).
 struct SupItem {
   float c;
   uint32_t id;
@@ -392,16 +380,16 @@ struct SupItem {
 template <class Topt>
 struct SupEdgeLoader {
   using Item = SupItem;
-  using State = int;
+  using State = float;
   const uint32_t *idx;
   const float *sc;
   Topt tsrc;
   int N;
-  float rn;
+  const float *rn;
   long long cap;
   int *e_src, *e_dst;
   float *e_copt, *e_topt;
-  __device__ State begin() const { return 0; }
+  __device__ State begin() const { return *rn; }
   __device__ void load(long long base, long long n, SupItem (&v)[kCompactRows]) const {
 #pragma unroll
     for (int r = 0; r < kCompactRows; ++r) {
@@ -410,7 +398,7 @@ struct SupEdgeLoader {
       v[r].id = q < n ? __ldg(&idx[q]) : 0u;
     }
   }
-  __device__ bool sel(State, const SupItem &v) const { return v.c < rn; }
+  __device__ bool sel(State rn_v, const SupItem &v) const { return v.c < rn_v; }
   __device__ void emit(long long, const SupItem &v, long long pos) const {
     if (pos >= cap) return;
     const uint32_t a = v.id / (uint32_t)(N - 1), b = v.id - a * (uint32_t)(N - 1);
@@ -504,105 +492,234 @@ pump_status_t build_edges_pairs(Ctx *ctx, const PairView &pv, float rn, long lon
 }
 
 namespace {
+// The one-read pass's shape for k of n pairs: the bracket sample's rank and
+// the superset buffer's capacity; false when the pass does not apply (few
+// pairs, 2^32 pairs or more, or a rank the sample cannot bracket).
+struct RnPlan {
+  long long rank, cap;
+};
+bool rn_plan(long long n, long long k, RnPlan *pl) {
+  const int S = kBracketSamples;
+  const double p = (double)(k + 1) / (double)n;
+  pl->rank = (long long)std::ceil(p * S + 8.0 * std::sqrt(S * p * (1.0 - p))) + 16;
+  if (n < 64LL * S || n >= (1LL << 32) || pl->rank >= S) return false;
+  pl->cap = std::min(n, 2 * (pl->rank + 1) * (n / S + 1) + 65536);
+  return k < pl->cap;
+}
+
+// Scratch of the one-read pass: the bracket key, the read-back pack, the
+// superset's size (kept here: the compaction scratch holding the pass's own
+// count is reused by the edge compaction), the bracket sample's costs and
+// the superset (pair numbers, then costs).
+struct RnScratch {
+  unsigned long long *key_hi;
+  RnEdgesPack *pack;
+  unsigned long long *n_sup;
+  float *sample_costs;
+  uint32_t *sup_idx;
+  float *sup_c;
+};
+pump_status_t rn_scratch(Ctx *ctx, long long cap, RnScratch *rs) {
+  char *buf = nullptr;
+  const size_t head = 64 + sizeof(float) * kBracketSamples;
+  PUMP_TRY(ctx->scratch(Ctx::kSuperset, head + (size_t)cap * 8, (void **)&buf));
+  rs->key_hi = (unsigned long long *)buf;
+  rs->pack = (RnEdgesPack *)(buf + 16);
+  rs->n_sup = (unsigned long long *)(buf + 32);
+  rs->sample_costs = (float *)(buf + 64);
+  rs->sup_idx = (uint32_t *)(buf + head);
+  rs->sup_c = (float *)(rs->sup_idx + cap);
+  return PUMP_OK;
+}
+
+// After the superset (pair order, its count in *rs.n_sup): the select
+// over it for rank k, the edges below rn compacted from it, the row starts
+// and the pack, all on the device.  Then either the deferred pack pointer,
+// or one read-back: rn and the edge count, or the fallback when the
+// superset missed rank k or overflowed.
+template <class Topt, class Fallback>
+pump_status_t rn_edges_tail(Ctx *ctx, const RnScratch &rs, Topt tsrc,
+                            int N, long long k, long long cap, long long max_edges, int *d_src,
+                            int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
+                            float *h_rn, long long *h_num_edges, cudaStream_t stream,
+                            Fallback fallback, const RnEdgesPack **deferred) {
+  const float *d_rn = nullptr;
+  PUMP_TRY(select_kth_src(ctx, FlatSrc{rs.sup_c}, cap, k, &d_rn, stream, rs.n_sup));
+  TileScratch ts2{};
+  PUMP_TRY(run_chunked_tuned(ctx, kTuneCompactEdges, cap,
+                             SupEdgeLoader<Topt>{rs.sup_idx, rs.sup_c, tsrc, N, d_rn, max_edges,
+                                                 d_src, d_dst, d_copt, d_topt},
+                             stream, &ts2, rs.n_sup));
+  if (d_go_start) PUMP_TRY(row_starts(d_src, max_edges, N, d_go_start, stream, ts2.total));
+  rn_pack_kernel<<<1, 1, 0, stream>>>(d_rn, rs.n_sup, ts2.total, k, cap, rs.pack);
+  PUMP_TRY(launch_status("rn_pack_kernel"));
+  if (deferred) {
+    *deferred = rs.pack;
+    *h_num_edges = -1;
+    return PUMP_OK;
+  }
+  RnEdgesPack pk{};
+  PUMP_CUDA_TRY(cudaMemcpyAsync(&pk, rs.pack, sizeof pk, cudaMemcpyDeviceToHost, stream));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (!pk.ok) return fallback();
+  std::memcpy(h_rn, &pk.rn_bits, sizeof(float));
+  *h_num_edges = (long long)pk.edges;
+  if ((long long)pk.edges > max_edges)
+    return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", pk.edges,
+                     max_edges);
+  return PUMP_OK;
+}
+
 // rn = the k-th smallest pair cost and the edges below it (same values and
 // order as select_kth + build_edges) from one read of the pair costs: the
-// bracket sample, the superset pass, the select over the superset, one
-// read-back, then the edges from the superset.  `fallback` runs the
-// three-pass select and the full compaction when the superset misses rank k,
-// overflows, or the pass does not apply (few pairs, 2^32 pairs or more).
+// bracket sample, the superset pass, then rn_edges_tail.  `fallback` runs
+// the three-pass select and the full compaction when the pass does not
+// apply or (after the read-back) the superset missed rank k or overflowed.
 template <class Src, class Topt, class Fallback>
 pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, long long max_edges,
                            int *d_src, int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
                            float *h_rn, long long *h_num_edges, cudaStream_t stream,
-                           Fallback fallback, const unsigned long long **deferred_total) {
-  if (deferred_total) *deferred_total = nullptr;
+                           Fallback fallback, const RnEdgesPack **deferred) {
+  if (deferred) *deferred = nullptr;
   const long long n = (long long)N * (N - 1);
-  const int S = kBracketSamples;
   if (k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "rn_edges: k=%lld n=%lld", k, n);
-  const double p = (double)(k + 1) / (double)n;
-  const long long rank = (long long)std::ceil(p * S + 8.0 * std::sqrt(S * p * (1.0 - p))) + 16;
-  if (n < 64LL * S || n >= (1LL << 32) || rank >= S) return fallback();
-  const long long cap = std::min(n, 2 * (rank + 1) * (n / S + 1) + 65536);
-  if (k >= cap) return fallback();
-  char *buf = nullptr;
-  PUMP_TRY(ctx->scratch(Ctx::kSuperset, 32 + (size_t)cap * 8, (void **)&buf));
-  unsigned long long *d_key_hi = (unsigned long long *)buf;
-  RnPack *d_pack = (RnPack *)(buf + 16);
-  uint32_t *sup_idx = (uint32_t *)(buf + 32);
-  float *sup_c = (float *)(sup_idx + cap);
-  bracket_kernel<<<1, 1024, 0, stream>>>(src, n, (unsigned int)rank, d_key_hi);
+  RnPlan pl;
+  if (!rn_plan(n, k, &pl)) return fallback();
+  RnScratch rs;
+  PUMP_TRY(rn_scratch(ctx, pl.cap, &rs));
+  bracket_kernel<<<1, 1024, 0, stream>>>(src, n, (unsigned int)pl.rank, rs.key_hi);
   PUMP_TRY(launch_status("bracket_kernel"));
   TileScratch ts{};
   PUMP_TRY(run_chunked_tuned(ctx, kTuneCompactRn, n,
-                             SupersetLoader<Src>{src, N, d_key_hi, cap, sup_idx, (uint32_t *)sup_c},
-                             stream, &ts));
-  const float *d_rn = nullptr;
-  PUMP_TRY(select_kth_src(ctx, FlatSrc{sup_c}, cap, k, &d_rn, stream, ts.total));
-  rn_pack_kernel<<<1, 1, 0, stream>>>(d_rn, ts.total, d_pack);
-  PUMP_TRY(launch_status("rn_pack_kernel"));
-  RnPack pk{};
-  PUMP_CUDA_TRY(cudaMemcpyAsync(&pk, d_pack, sizeof pk, cudaMemcpyDeviceToHost, stream));
-  PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
-  if ((long long)pk.n_sup <= k || (long long)pk.n_sup > cap) return fallback();
-  float rn;
-  std::memcpy(&rn, &pk.rn_bits, sizeof rn);
-  *h_rn = rn;
-  TileScratch ts2{};
-  PUMP_TRY(run_chunked_tuned(ctx, kTuneCompactEdges, (long long)pk.n_sup,
-                             SupEdgeLoader<Topt>{sup_idx, sup_c, tsrc, N, rn, max_edges, d_src,
-                                                 d_dst, d_copt, d_topt},
-                             stream, &ts2));
-  if (deferred_total) {
-    // the count stays on the device (the three-kernel compaction never
-    // waits, so it has no error word): the caller reads it later
-    *deferred_total = ts2.total;
-    *h_num_edges = -1;
-    if (d_go_start) PUMP_TRY(row_starts(d_src, max_edges, N, d_go_start, stream, ts2.total));
-    return PUMP_OK;
-  }
-  unsigned long long total = 0;
-  PUMP_TRY(finish_compact(ts2, &total, stream));
-  *h_num_edges = (long long)total;
-  if ((long long)total > max_edges)
-    return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", total, max_edges);
-  if (d_go_start) PUMP_TRY(row_starts(d_src, (long long)total, N, d_go_start, stream));
-  return PUMP_OK;
+                             SupersetLoader<Src>{src, N, rs.key_hi, pl.cap, rs.sup_idx,
+                                                 (uint32_t *)rs.sup_c},
+                             stream, &ts, nullptr, rs.n_sup));
+  return rn_edges_tail(ctx, rs, tsrc, N, k, pl.cap, max_edges, d_src, d_dst, d_copt, d_topt,
+                       d_go_start, h_rn, h_num_edges, stream, fallback, deferred);
 }
 
 }  // namespace
+
+pump_status_t rn_edges_fallback_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
+                                       long long k, long long max_edges, int *d_src, int *d_dst,
+                                       float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
+                                       long long *h_num_edges, cudaStream_t stream) {
+  const float *d_rn = nullptr;
+  PUMP_TRY(select_kth_device(ctx, d_copts, (long long)N * (N - 1), k, &d_rn, stream));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(h_rn, d_rn, sizeof(float), cudaMemcpyDeviceToHost, stream));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
+  return build_edges_device(ctx, d_copts, d_topts, N, *h_rn, max_edges, d_src, d_dst, d_copt,
+                            d_topt, d_go_start, h_num_edges, stream);
+}
+
+pump_status_t rn_edges_fallback_pairs(Ctx *ctx, const PairView &pv, long long k,
+                                      long long max_edges, int *d_src, int *d_dst, float *d_copt,
+                                      float *d_topt, int *d_go_start, float *h_rn,
+                                      long long *h_num_edges, cudaStream_t stream) {
+  const float *d_rn = nullptr;
+  PUMP_TRY(select_kth_pairs(ctx, pv, k, &d_rn, stream));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(h_rn, d_rn, sizeof(float), cudaMemcpyDeviceToHost, stream));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
+  return build_edges_pairs(ctx, pv, *h_rn, max_edges, d_src, d_dst, d_copt, d_topt, d_go_start,
+                           h_num_edges, stream);
+}
 
 pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
                               long long k, long long max_edges, int *d_src, int *d_dst,
                               float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
                               long long *h_num_edges, cudaStream_t stream,
-                              const unsigned long long **deferred_total) {
+                              const RnEdgesPack **deferred) {
   auto fallback = [&]() -> pump_status_t {
-    const float *d_rn = nullptr;
-    PUMP_TRY(select_kth_device(ctx, d_copts, (long long)N * (N - 1), k, &d_rn, stream));
-    PUMP_CUDA_TRY(cudaMemcpyAsync(h_rn, d_rn, sizeof(float), cudaMemcpyDeviceToHost, stream));
-    PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
-    return build_edges_device(ctx, d_copts, d_topts, N, *h_rn, max_edges, d_src, d_dst, d_copt,
-                              d_topt, d_go_start, h_num_edges, stream);
+    if (deferred) *deferred = nullptr;
+    return rn_edges_fallback_device(ctx, d_copts, d_topts, N, k, max_edges, d_src, d_dst, d_copt,
+                                    d_topt, d_go_start, h_rn, h_num_edges, stream);
   };
   return rn_edges_src(ctx, FlatSrc{d_copts}, FlatTopt{d_topts}, N, k, max_edges, d_src, d_dst,
-                      d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream, fallback,
-                      deferred_total);
+                      d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream, fallback, deferred);
 }
 
 pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long long max_edges,
                              int *d_src, int *d_dst, float *d_copt, float *d_topt,
                              int *d_go_start, float *h_rn, long long *h_num_edges,
-                             cudaStream_t stream, const unsigned long long **deferred_total) {
+                             cudaStream_t stream, const RnEdgesPack **deferred) {
   auto fallback = [&]() -> pump_status_t {
-    const float *d_rn = nullptr;
-    PUMP_TRY(select_kth_pairs(ctx, pv, k, &d_rn, stream));
-    PUMP_CUDA_TRY(cudaMemcpyAsync(h_rn, d_rn, sizeof(float), cudaMemcpyDeviceToHost, stream));
-    PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
-    return build_edges_pairs(ctx, pv, *h_rn, max_edges, d_src, d_dst, d_copt, d_topt, d_go_start,
-                             h_num_edges, stream);
+    if (deferred) *deferred = nullptr;
+    return rn_edges_fallback_pairs(ctx, pv, k, max_edges, d_src, d_dst, d_copt, d_topt,
+                                   d_go_start, h_rn, h_num_edges, stream);
   };
   return rn_edges_src(ctx, PairCoptSrc{pv}, PairTopt{pv}, pv.N, k, max_edges, d_src, d_dst, d_copt,
-                      d_topt, d_go_start, h_rn, h_num_edges, stream, fallback, deferred_total);
+                      d_topt, d_go_start, h_rn, h_num_edges, stream, fallback, deferred);
+}
+
+pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float tmax,
+                                  int bvp_mode, long long k, long long max_edges, float *d_copts,
+                                  float *d_topts, int *d_src, int *d_dst, float *d_copt,
+                                  float *d_topt, int *d_go_start, float *h_rn,
+                                  long long *h_num_edges, cudaStream_t stream,
+                                  const RnEdgesPack **deferred, float *stage_ms) {
+  if (deferred) *deferred = nullptr;
+  if (N < 2) return set_error(PUMP_ERR_BAD_INPUT, "roadmap: N = %d", N);
+  const long long n = (long long)N * (N - 1);
+  if (k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "roadmap: k=%lld n=%lld", k, n);
+  // stage events: start, pair pass start, pair pass end, end
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  struct EvGuard {
+    cudaEvent_t *e;
+    ~EvGuard() {
+      for (int q = 0; q < 4; ++q)
+        if (e[q]) cudaEventDestroy(e[q]);
+    }
+  } guard{ev};
+  if (stage_ms && !deferred) {
+    for (int q = 0; q < 4; ++q) PUMP_CUDA_TRY(cudaEventCreate(&ev[q]));
+    PUMP_CUDA_TRY(cudaEventRecord(ev[0], stream));
+  }
+  auto finish = [&](pump_status_t st) -> pump_status_t {
+    if (st != PUMP_OK || !ev[0]) return st;
+    PUMP_CUDA_TRY(cudaEventRecord(ev[3], stream));
+    PUMP_CUDA_TRY(cudaEventSynchronize(ev[3]));
+    for (int q = 0; q < 3; ++q)
+      PUMP_CUDA_TRY(cudaEventElapsedTime(&stage_ms[q], ev[q], ev[q + 1]));
+    return st;
+  };
+  RnPlan pl;
+  if (bvp_mode != PUMP_BVP_PRECISION || !rn_plan(n, k, &pl)) {
+    if (ev[1]) PUMP_CUDA_TRY(cudaEventRecord(ev[1], stream));
+    PUMP_TRY(pump_bvp_pairs(d_samples, N, tmax, bvp_mode, d_copts, d_topts, (pump_stream_t)stream));
+    if (ev[2]) PUMP_CUDA_TRY(cudaEventRecord(ev[2], stream));
+    return finish(rn_edges_device(ctx, d_copts, d_topts, N, k, max_edges, d_src, d_dst, d_copt,
+                                  d_topt, d_go_start, h_rn, h_num_edges, stream, deferred));
+  }
+  RnScratch rs;
+  PUMP_TRY(rn_scratch(ctx, pl.cap, &rs));
+  TileScratch ts{};
+  long long ntiles = 0;
+  PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));  // the zeroed tile counts
+  ts.copy_to = rs.n_sup;
+  static_assert(kRnCountTile == kTile, "count tiles of the pair pass are the compaction's tiles");
+  auto bracket = [&]() -> pump_status_t {
+    bracket_kernel<<<1, 1024, 0, stream>>>(FlatSrc{rs.sample_costs}, (long long)kBracketSamples,
+                                           (unsigned int)pl.rank, rs.key_hi);
+    PUMP_TRY(launch_status("bracket_kernel"));
+    if (ev[1]) PUMP_CUDA_TRY(cudaEventRecord(ev[1], stream));
+    return PUMP_OK;
+  };
+  PUMP_TRY(bvp_pairs_precision_counted(d_samples, N, tmax, d_copts, d_topts, kBracketSamples,
+                                       rs.sample_costs, bracket, rs.key_hi,
+                                       reinterpret_cast<unsigned int *>(ts.status), stream));
+  if (ev[2]) PUMP_CUDA_TRY(cudaEventRecord(ev[2], stream));
+  PUMP_TRY(run_chunked_emit_tuned(kTuneCompactRnEmit, n, ntiles,
+                                  SupersetLoader<FlatSrc>{FlatSrc{d_copts}, N, rs.key_hi, pl.cap,
+                                                          rs.sup_idx, (uint32_t *)rs.sup_c},
+                                  stream, ts));
+  auto fallback = [&]() -> pump_status_t {
+    if (deferred) *deferred = nullptr;
+    return rn_edges_fallback_device(ctx, d_copts, d_topts, N, k, max_edges, d_src, d_dst, d_copt,
+                                    d_topt, d_go_start, h_rn, h_num_edges, stream);
+  };
+  return finish(rn_edges_tail(ctx, rs, FlatTopt{d_topts}, N, k, pl.cap, max_edges, d_src,
+                              d_dst, d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream,
+                              fallback, deferred));
 }
 
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
@@ -822,6 +939,25 @@ extern "C" pump_status_t pump_frontier_compact_noalloc(const uint8_t *d_flags, i
   if (err)
     return set_error(PUMP_ERR_TIMEOUT, "pump_frontier_compact_noalloc: look-back wait exceeded its bound");
   return PUMP_OK;
+}
+
+extern "C" pump_status_t pump_roadmap(pump_ctx *ctx, const float *d_samples, int N, float tmax,
+                                      int bvp_mode, long long k, long long max_edges,
+                                      float *d_copts, float *d_topts, int *d_src, int *d_dst,
+                                      float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
+                                      long long *h_num_edges, float *h_stage_ms,
+                                      pump_stream_t stream) {
+  if (!ctx || !d_samples || N < 2 || max_edges < 0 || !d_copts || !d_topts || !d_src || !d_dst ||
+      !d_copt || !d_topt || !h_rn || !h_num_edges)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_roadmap: bad arguments");
+  if (bvp_mode != PUMP_BVP_PARITY && bvp_mode != PUMP_BVP_PRECISION &&
+      bvp_mode != PUMP_BVP_PARITY_GPU)
+    return set_error(PUMP_ERR_BAD_INPUT, "pump_roadmap: bvp_mode %d", bvp_mode);
+  Ctx *c = Ctx::from(ctx);
+  PUMP_TRY(c->activate());
+  return roadmap_pairs_edges(c, d_samples, N, tmax, bvp_mode, k, max_edges, d_copts, d_topts, d_src,
+                             d_dst, d_copt, d_topt, d_go_start, h_rn, h_num_edges,
+                             (cudaStream_t)stream, nullptr, h_stage_ms);
 }
 
 extern "C" pump_status_t pump_roadmap_edges(pump_ctx *ctx, const float *d_copts, const float *d_topts,

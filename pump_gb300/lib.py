@@ -93,6 +93,8 @@ _SIGS = {
     "pump_build_edges": (i32, [vp, vp, vp, i32, f32, i64, vp, vp, vp, vp, vp, C.POINTER(i64), vp]),
     "pump_roadmap_edges": (i32, [vp, vp, vp, i32, i64, i64, vp, vp, vp, vp, vp, C.POINTER(f32),
                                  C.POINTER(i64), vp]),
+    "pump_roadmap": (i32, [vp, vp, i32, f32, i32, i64, i64, vp, vp, vp, vp, vp, vp, vp,
+                           C.POINTER(f32), C.POINTER(i64), vp, vp]),
     "pump_discretize_edges": (i32, [vp, vp, vp, vp, i64, i32, i32, vp, vp]),
     "pump_sample_free": (i32, [vp, i32, vp, i32, vp, vp]),
     "pump_free_edges": (i32, [vp, i32, vp, i64, i32, vp, vp]),

@@ -316,6 +316,99 @@ def test_roadmap_edges_nan_costs(gpu, pumplib):
     assert same_bits(host(d_ce, E), ce) and same_bits(host(d_te, E), te)
 
 
+def roadmap_one_call(torch, pumplib, ctx, s, k, mode, stage_ms=None):
+    """pump_roadmap on host samples: (copts, topts, rn, src, dst, copt, topt, go)."""
+    N = s.shape[0]
+    n = N * (N - 1)
+    d_s = dev(torch, s)
+    d_c, d_t = empty(torch, n, torch.float32), empty(torch, n, torch.float32)
+    d_src, d_dst = empty(torch, k, torch.int32), empty(torch, k, torch.int32)
+    d_ce, d_te = empty(torch, k, torch.float32), empty(torch, k, torch.float32)
+    d_go = empty(torch, N + 1, torch.int32)
+    rn, E = C.c_float(0), C.c_longlong(0)
+    pumplib.check(pumplib.load().pump_roadmap(
+        ctx.handle, ptr(d_s), N, 5.0, mode, k, k, ptr(d_c), ptr(d_t), ptr(d_src), ptr(d_dst),
+        ptr(d_ce), ptr(d_te), ptr(d_go), C.byref(rn), C.byref(E), stage_ms, stream(torch)))
+    E = E.value
+    return (host(d_c, n), host(d_t, n), np.float32(rn.value), host(d_src, E), host(d_dst, E),
+            host(d_ce, E), host(d_te, E), host(d_go, N + 1))
+
+
+def roadmap_sample_sets():
+    from pump_gb300 import workloads
+    from oracle.pyoracle import halton_samples
+    lo, hi = np.asarray(workloads.LO, np.float32), np.asarray(workloads.HI, np.float32)
+    rng = np.random.default_rng(5)
+    uni = (lo + (hi - lo) * rng.random((2100, 6))).astype(np.float32)
+    # four tight clusters: the strided sample sees rows of very uneven density
+    cen = lo + (hi - lo) * rng.random((4, 6))
+    clu = (cen[rng.integers(0, 4, 1800)] + rng.normal(0, 0.02, (1800, 6))).astype(np.float32)
+    return {"halton1000": halton_samples(1000, workloads.INIT, workloads.GOAL, workloads.LO,
+                                         workloads.HI),
+            "uniform2100": uni, "clusters1800": clu}
+
+
+@pytest.mark.parametrize("case", ["halton1000", "uniform2100", "clusters1800"])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_roadmap_one_call(case, mode, gpu, pumplib):
+    """pump_roadmap (pair BVPs counting the rn superset as they store the
+    costs, in the precision arithmetic) gives the bytes of pump_bvp_pairs +
+    pump_roadmap_edges, in every arithmetic."""
+    torch, ctx = gpu
+    L = pumplib.load()
+    s = roadmap_sample_sets()[case]
+    if mode != 1:
+        s = s[:800]  # the bisection arithmetics: 639,200 pairs, still the one-read pass
+    N = s.shape[0]
+    n = N * (N - 1)
+    k = int(np.float32(n) * np.float32(0.05))
+    c, t = run_bvp_pairs(torch, pumplib, s, mode)
+    ref = (c, t) + roadmap_edges(torch, pumplib, ctx, c, t, N, k, k)
+    ms = (C.c_float * 3)()
+    got = roadmap_one_call(torch, pumplib, ctx, s, k, mode, ms)
+    names = ["copts", "topts", "rn", "src", "dst", "copt", "topt", "go"]
+    for name, a, b in zip(names, ref, got):
+        assert same_bits(np.atleast_1d(a), np.atleast_1d(b)), (case, mode, name)
+    assert ms[0] >= 0 and ms[1] > 0 and ms[2] > 0
+    # a second call on the same context (scratch reused) gives the same bytes
+    again = roadmap_one_call(torch, pumplib, ctx, s, k, mode)
+    for name, a, b in zip(names, got, again):
+        assert same_bits(np.atleast_1d(a), np.atleast_1d(b)), (case, mode, name)
+
+
+def test_roadmap_one_call_parity_oracle(gpu, pumplib, roadmap1000):
+    """In the parity arithmetic pump_roadmap's rn and edges are the oracle's."""
+    torch, ctx = gpu
+    r = roadmap1000
+    c, t, rn, src, dst, ce, te, go = roadmap_one_call(torch, pumplib, ctx, r["samples"], r["k"], 0)
+    assert same_bits(c, r["copts"]) and same_bits(t, r["topts"])
+    assert rn == np.float32(r["rn"])
+    assert np.array_equal(src, r["src"]) and np.array_equal(dst, r["dst"])
+    assert same_bits(ce, r["ce"]) and same_bits(te, r["te"])
+    assert np.array_equal(go, np.searchsorted(r["src"], np.arange(r["N"] + 1), side="left"))
+
+
+def test_roadmap_one_call_capacity(gpu, pumplib, roadmap1000):
+    """Fewer edge slots than edges: PUMP_ERR_CAPACITY with the true count."""
+    torch, ctx = gpu
+    L = pumplib.load()
+    r = roadmap1000
+    N, k = r["N"], r["k"]
+    d_s = dev(torch, r["samples"])
+    n = N * (N - 1)
+    d_c, d_t = empty(torch, n, torch.float32), empty(torch, n, torch.float32)
+    cap = k // 2  # about k edges qualify
+    d_src, d_dst = empty(torch, cap, torch.int32), empty(torch, cap, torch.int32)
+    d_ce, d_te = empty(torch, cap, torch.float32), empty(torch, cap, torch.float32)
+    rn, E = C.c_float(0), C.c_longlong(0)
+    st = L.pump_roadmap(ctx.handle, ptr(d_s), N, 5.0, 1, k, cap, ptr(d_c), ptr(d_t), ptr(d_src),
+                        ptr(d_dst), ptr(d_ce), ptr(d_te), None, C.byref(rn), C.byref(E), None,
+                        stream(torch))
+    torch.cuda.synchronize()
+    assert st == pumplib.PUMP_ERR_CAPACITY
+    assert E.value > cap
+
+
 def test_collision_checks(gpu, pumplib, oracle, roadmap1000):
     torch, _ = gpu
     L = pumplib.load()

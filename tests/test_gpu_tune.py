@@ -41,6 +41,29 @@ def roadmap_outputs(torch, pumplib, ctx, N, obs):
             host(d_ce, E), host(d_te, E), host(d_go, N + 1), host(d_disc, E * 54), host(d_fe, E)]
 
 
+def roadmap_one_call(torch, pumplib, ctx, N):
+    """pump_roadmap (pair BVPs, rn and edges in one call): the first eight
+    outputs of roadmap_outputs."""
+    from pump_gb300 import workloads
+    from oracle.pyoracle import halton_samples
+    L = pumplib.load()
+    s = halton_samples(N, workloads.INIT, workloads.GOAL, workloads.LO, workloads.HI)
+    d_s = dev(torch, s)
+    n = N * (N - 1)
+    k = int(np.float32(n) * np.float32(0.05))
+    d_c, d_t = empty(torch, n, torch.float32), empty(torch, n, torch.float32)
+    d_src, d_dst = empty(torch, k, torch.int32), empty(torch, k, torch.int32)
+    d_ce, d_te = empty(torch, k, torch.float32), empty(torch, k, torch.float32)
+    d_go = empty(torch, N + 1, torch.int32)
+    rn, E = C.c_float(0), C.c_longlong(0)
+    pumplib.check(L.pump_roadmap(ctx.handle, ptr(d_s), N, 5.0, pumplib.PUMP_BVP_PRECISION, k, k,
+                                 ptr(d_c), ptr(d_t), ptr(d_src), ptr(d_dst), ptr(d_ce), ptr(d_te),
+                                 ptr(d_go), C.byref(rn), C.byref(E), None, stream(torch)))
+    E = E.value
+    return [host(d_c, n), host(d_t, n), np.float32(rn.value), host(d_src, E), host(d_dst, E),
+            host(d_ce, E), host(d_te, E), host(d_go, N + 1)]
+
+
 def test_tuned_shapes_compute_the_defaults(gpu, pumplib):
     torch, ctx = gpu
     from pump_gb300 import workloads
@@ -50,20 +73,28 @@ def test_tuned_shapes_compute_the_defaults(gpu, pumplib):
     L.pump_tune_enable(0)
     try:
         ref = roadmap_outputs(torch, pumplib, ctx, N, obs)
+        ref_one = roadmap_one_call(torch, pumplib, ctx, N)
     finally:
         L.pump_tune_enable(1)
     L.pump_tune_reset()
     first = roadmap_outputs(torch, pumplib, ctx, N, obs)   # tunes every class
     again = roadmap_outputs(torch, pumplib, ctx, N, obs)   # reuses the records
-    for a, b, c in zip(ref, first, again):
-        a, b, c = np.atleast_1d(a), np.atleast_1d(b), np.atleast_1d(c)
-        assert a.shape == b.shape == c.shape
-        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
-        assert np.array_equal(a.view(np.uint8), c.view(np.uint8))
+    one = roadmap_one_call(torch, pumplib, ctx, N)         # tunes the counted pass's emit grid
+    one_again = roadmap_one_call(torch, pumplib, ctx, N)
+    # the separate calls (defaults, tuning, tuned) and the one call (defaults,
+    # tuning, tuned) all give the same bytes
+    outs = [first, again, ref_one, one, one_again]
+    for q, a in enumerate(ref):
+        a = np.atleast_1d(a)
+        for o in outs:
+            if q < len(o):
+                b = np.atleast_1d(o[q])
+                assert a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8)), q
     size = L.pump_tune_report(None, 0)
     buf = C.create_string_buffer(size + 1)
     L.pump_tune_report(buf, size + 1)
     text = buf.value.decode()
-    for name in ("bvp_pairs_precision", "discretize", "free_edges", "compact_rn", "compact_edges"):
+    for name in ("bvp_pairs_precision", "discretize", "free_edges", "compact_rn", "compact_edges",
+                 "compact_rn_emit"):
         assert name in text, text
-    assert len(text.strip().splitlines()) == 5, text
+    assert len(text.strip().splitlines()) == 6, text
