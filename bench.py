@@ -531,12 +531,11 @@ class Query:
         stage = (C.c_float * 3)()
         stage_ms = {}
         # our kernels per pump_roadmap call: in the precision arithmetic the
-        # sample preparation, the bracket sample's costs, the bracket and the
-        # counted pair pass, the superset scan and emit; otherwise the pair
-        # pass, the bracket, the superset count, scan and emit; then the
-        # select (init, 3 histograms, 3 picks), the edge count, scan and
-        # emit, the row starts and the read-back pack
-        roadmap_launches = 6 + 13 if mode == lib.PUMP_BVP_PRECISION else 5 + 13
+        # samples with the rn bracket and the pair kernel staging the
+        # superset; otherwise the pair kernel, the bracket and the superset's
+        # count, scan and emit; then the finishing kernel (select, edges, row
+        # starts, pack)
+        roadmap_launches = 2 + 1 if mode == lib.PUMP_BVP_PRECISION else 5 + 1
 
         def roadmap():
             lib.check(L.pump_roadmap(self.ctx.handle, d_s.data_ptr(), N, 5.0, mode, rn_idx, cap,

@@ -6,6 +6,7 @@
 #include "ctx.h"
 #include "tune.h"
 #include "precise.cuh"
+#include "bracket.cuh"
 
 namespace pump {
 namespace {
@@ -57,56 +58,81 @@ __global__ void __launch_bounds__(T) bvp_pairs_precision_kernel(const SampleF *_
   copts[idx] = d2f_rn(c);
 }
 
-// Costs of the bracket-sample pairs: pair number floor((2q + 1) n / (2 S))
-// for q < S, n = N(N-1).
-__global__ void bracket_costs_kernel(const SampleF *__restrict__ sf, int N, float tmax, int S,
-                                     unsigned int *__restrict__ out_bits) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= S) return;
+// The samples' binary64 forms and the rn bracket, one launch: blocks below
+// nprep prepare 1024 samples each; the kBracketSamples / 1024 blocks after
+// them compute the costs of the bracket-sample pairs (pair number
+// floor((2q + 1) n / (2 S)), from the raw samples) and store their order
+// keys, and the one of those that finishes last (a counter of finished
+// blocks, reset by that block) runs the bracket's radix steps over all of
+// them.
+__global__ void __launch_bounds__(1024) prepare_bracket_kernel(
+    const float *__restrict__ samples, int N, float tmax, int nprep, SampleF *__restrict__ sf,
+    unsigned int rank, uint32_t *keys_g, unsigned int *done, unsigned long long *key_hi) {
+  if ((int)blockIdx.x < nprep) {
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    if (i < N) {
+      float x[kDim];
+#pragma unroll
+      for (int d = 0; d < kDim; ++d) x[d] = samples[i * kDim + d];
+      sf[i] = to_sample_f(x);
+    }
+    return;
+  }
+  __shared__ uint32_t keys[kBracketSamples];
+  __shared__ bool s_last;
+  const int q = ((int)blockIdx.x - nprep) * 1024 + threadIdx.x;
   const long long n = (long long)N * (N - 1);
-  const long long pos = ((2LL * q + 1) * n) / (2LL * S);
+  const long long pos = ((2LL * q + 1) * n) / (2LL * kBracketSamples);
   const int i = (int)(pos / (N - 1));
   const int r = (int)(pos - (long long)i * (N - 1));
   const int j = r + (r >= i);
+  float a[kDim], b[kDim];
+#pragma unroll
+  for (int d = 0; d < kDim; ++d) {
+    a[d] = samples[i * kDim + d];
+    b[d] = samples[j * kDim + d];
+  }
   double t, c;
-  precise_tau(load_sample(sf, i), load_sample(sf, j), tmax, &t, &c);
-  out_bits[q] = __float_as_uint(d2f_rn(c));
+  precise_tau(a, b, tmax, &t, &c);
+  keys_g[q] = key_of_bits(__float_as_uint(d2f_rn(c)));
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == kBracketSamples / 1024 - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int p = threadIdx.x; p < kBracketSamples; p += 1024) keys[p] = __ldcg(&keys_g[p]);
+  __syncthreads();
+  bracket_radix(keys, rank, key_hi);
+  if (threadIdx.x == 0) *done = 0u;
 }
 
-// bvp_pairs_precision_kernel plus the count pass of the rn superset: each
-// warp adds its pairs whose cost's order key is below *key_hi to the counts
-// of their 4096-pair tiles (a warp's 32 consecutive pairs meet at most two
-// tiles: one atomic for each).  A warp wholly past its row's end leaves at
-// once; the others reach the ballots with every lane.
-template <int T>
-__global__ void __launch_bounds__(T) bvp_pairs_precision_counted_kernel(
+// All pairs, one block per 128 consecutive pairs of a row (row i =
+// blockIdx.y): each pair's cost and time are stored, and each warp stores
+// the ballot of its 32 pairs whose cost's order key is below *key_hi (bit
+// l = pair l of the warp), warp tile (row, column block, warp) in pair
+// order.  No thread waits for another.
+constexpr int kPairTile = 128;
+__global__ void __launch_bounds__(kPairTile) bvp_pairs_masked_kernel(
     const SampleF *__restrict__ sf, int N, float tmax, float *__restrict__ copts,
     float *__restrict__ topts, const unsigned long long *__restrict__ key_hi,
-    unsigned int *__restrict__ tile_counts) {
+    uint32_t *__restrict__ masks) {
   const int i = blockIdx.y;
-  const int lane = threadIdx.x & 31;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r - lane >= N - 1) return;
-  const long long idx = (long long)i * (N - 1) + r;
+  const int r = blockIdx.x * kPairTile + threadIdx.x;
   bool sel = false;
   if (r < N - 1) {
     const int j = r + (r >= i);
+    const long long idx = (long long)i * (N - 1) + r;
     double t, c;
     precise_tau(load_sample(sf, i), load_sample(sf, j), tmax, &t, &c);
     const unsigned int cb = __float_as_uint(d2f_rn(c));
-    topts[idx] = d2f_rn(t);
     reinterpret_cast<unsigned int *>(copts)[idx] = cb;
+    topts[idx] = d2f_rn(t);
     sel = (unsigned long long)key_of_bits(cb) < __ldg(key_hi);
   }
-  const unsigned int m = __ballot_sync(0xffffffffu, sel);
-  if (m) {
-    const long long t0 = (idx - lane) / kRnCountTile;
-    const unsigned int in0 = __ballot_sync(0xffffffffu, sel && idx / kRnCountTile == t0);
-    if (lane == 0) {
-      if (in0) atomicAdd(&tile_counts[t0], (unsigned int)__popc(in0));
-      if (m & ~in0) atomicAdd(&tile_counts[t0 + 1], (unsigned int)__popc(m & ~in0));
-    }
-  }
+  const unsigned int bal = __ballot_sync(0xffffffffu, sel);
+  if ((threadIdx.x & 31) == 0)
+    masks[((long long)i * gridDim.x + blockIdx.x) * (kPairTile / 32) + (threadIdx.x >> 5)] = bal;
 }
 
 __global__ void bvp_batch_precision_kernel(const BvpJobs jb) {
@@ -155,32 +181,36 @@ pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tm
   return st;
 }
 
-pump_status_t bvp_pairs_precision_counted(const float *d_samples, int N, float tmax,
-                                          float *d_copts, float *d_topts, int S,
-                                          float *d_sample_costs,
-                                          const std::function<pump_status_t()> &bracket,
-                                          const unsigned long long *d_key_hi,
-                                          unsigned int *d_tile_counts, cudaStream_t stream) {
-  if (N > 65535) return set_error(PUMP_ERR_CAPACITY, "bvp_pairs: N = %d exceeds 65535 rows", N);
+pump_status_t bvp_pairs_precision_superset(Ctx *ctx, const float *d_samples, int N, float tmax,
+                                           float *d_copts, float *d_topts, const PairSuperset &ps,
+                                           cudaStream_t stream, cudaEvent_t between) {
+  const long long n = (long long)N * (N - 1);
+  if (N < 2 || N > 65535 || n >= (1LL << 32))
+    return set_error(PUMP_ERR_CAPACITY, "bvp_pairs_superset: N = %d", N);
+  const unsigned int nbx = grid_for(N - 1, kPairTile);
+  const int per_row = (int)nbx * (kPairTile / 32);
+  uint32_t *masks = nullptr;
+  PUMP_TRY(ctx->scratch(Ctx::kPairStage, sizeof(uint32_t) * (size_t)per_row * N, (void **)&masks));
+  ps.out->masks = masks;
+  ps.out->nmasks = (long long)per_row * N;
+  ps.out->masks_per_row = per_row;
   SampleF *sd = nullptr;
   PUMP_CUDA_TRY(pool_malloc_async((void **)&sd, sizeof(SampleF) * (size_t)N, stream));
-  prepare_samples_kernel<<<grid_for(N, 128), 128, 0, stream>>>(d_samples, N, sd);
-  pump_status_t st = launch_status("prepare_samples");
+  const int nprep = (N + 1023) / 1024;
+  static_assert(kBracketSamples % 1024 == 0, "whole bracket blocks");
+  prepare_bracket_kernel<<<nprep + kBracketSamples / 1024, 1024, 0, stream>>>(
+      d_samples, N, tmax, nprep, sd, ps.rank, ps.sample_keys, ps.done, ps.key_hi);
+  pump_status_t st = launch_status("prepare_bracket");
+  if (st == PUMP_OK && between && cudaEventRecord(between, stream) != cudaSuccess)
+    st = set_error(PUMP_ERR_CUDA, "cudaEventRecord");
   if (st == PUMP_OK) {
-    bracket_costs_kernel<<<grid_for(S, 64), 64, 0, stream>>>(
-        sd, N, tmax, S, reinterpret_cast<unsigned int *>(d_sample_costs));
-    st = launch_status("bracket_costs");
+    const dim3 grid(nbx, (unsigned)N);
+    bvp_pairs_masked_kernel<<<grid, kPairTile, 0, stream>>>(sd, N, tmax, d_copts, d_topts,
+                                                           ps.key_hi, masks);
+    st = launch_status("bvp_pairs_masked");
   }
-  if (st == PUMP_OK) st = bracket();
-  if (st == PUMP_OK) {
-    // the block size of the plain pass's default (the tuner's three shapes
-    // measure within 1 % of each other)
-    constexpr int T = 128;
-    const dim3 grid(grid_for(N - 1, T), (unsigned)N);
-    bvp_pairs_precision_counted_kernel<T><<<grid, T, 0, stream>>>(sd, N, tmax, d_copts, d_topts,
-                                                                 d_key_hi, d_tile_counts);
-    st = launch_status("bvp_pairs_precision_counted");
-  }
+  if (st == PUMP_OK && ps.after_pairs && cudaEventRecord(ps.after_pairs, stream) != cudaSuccess)
+    st = set_error(PUMP_ERR_CUDA, "cudaEventRecord");
   cudaFreeAsync(sd, stream);
   return st;
 }

@@ -176,14 +176,22 @@ __device__ __forceinline__ long long next_tile(const TileScratch &ts) {
   return s_tile;
 }
 
-// Pred(i) -> bool, Emit(i, pos) writes item i at output position pos.
+// Pred(i) -> bool, Emit(i, pos) writes item i at output position pos.  With
+// d_n the item count is *d_n when below n (n, the host's bound, sized the
+// grid): tiles wholly past it leave at once (no tile waits on a later one).
 template <class Pred, class Emit>
 __global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, Pred pred, Emit emit,
-                                                                  TileScratch ts) {
+                                                                  TileScratch ts,
+                                                                  const unsigned long long *d_n) {
   __shared__ TileShared sh;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long tile = next_tile(ts);
   const long long base = tile * kTile;
+  if (d_n) {
+    const unsigned long long d = *d_n;
+    if ((long long)d < n) n = (long long)d;
+    if (base >= n && tile > 0) return;
+  }
   // all predicates first (their loads in flight together), then the ballots
   bool f[kCompactRows];
 #pragma unroll
@@ -213,13 +221,14 @@ __global__ void __launch_bounds__(kCompactThreads) compact_kernel(long long n, P
 // over n items in tiles of tile_items (ctx compaction scratch);
 // *ntiles_out = the tiles to launch.
 pump_status_t prepare_tiles(Ctx *ctx, long long n, cudaStream_t stream, TileScratch *ts_out,
-                            long long *ntiles_out, long long tile_items = kTile) {
+                            long long *ntiles_out, long long tile_items = kTile,
+                            int slot = Ctx::kCompact) {
   const long long ntiles = n > 0 ? (n + tile_items - 1) / tile_items : 1;
   if (ntiles > 2147483647LL) return set_error(PUMP_ERR_CAPACITY, "compaction: too many tiles");
   const size_t zeroed = sizeof(unsigned long long) * (ntiles + 2) + sizeof(unsigned int) * 4;
   const size_t bytes = zeroed + sizeof(unsigned long long) * ntiles;
   char *scratch = nullptr;
-  PUMP_TRY(ctx->scratch(Ctx::kCompact, bytes, (void **)&scratch));
+  PUMP_TRY(ctx->scratch(slot, bytes, (void **)&scratch));
   TileScratch ts{};
   ts.total = (unsigned long long *)scratch;
   ts.status = ts.total + 1;
@@ -234,12 +243,12 @@ pump_status_t prepare_tiles(Ctx *ctx, long long n, cudaStream_t stream, TileScra
 
 template <class Pred, class Emit>
 pump_status_t run_compact(Ctx *ctx, long long n, Pred pred, Emit emit, cudaStream_t stream,
-                          TileScratch *ts_out) {
+                          TileScratch *ts_out, const unsigned long long *d_n = nullptr) {
   TileScratch ts{};
   long long ntiles = 0;
   PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));
   if (n > 0) {
-    compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(n, pred, emit, ts);
+    compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, stream>>>(n, pred, emit, ts, d_n);
     PUMP_TRY(launch_status("compact_kernel"));
   }
   *ts_out = ts;
@@ -443,20 +452,6 @@ pump_status_t run_chunked_tuned(Ctx *ctx, int kernel, long long n, const L &ld,
   auto run = [&](int c) {
     return run_chunked(ctx, n, ld, stream, ts_out, kPerSm[c], d_n, copy_to);
   };
-  int choice = 1;
-  bool ran = false;
-  PUMP_TRY(tune_choice(kernel, tune_bucket(n), 3, 1, stream, run, &choice, &ran));
-  return ran ? PUMP_OK : run(choice);
-}
-
-// run_chunked_emit with the emit grid of the autotuner's record for
-// (kernel, n's bucket); a first call tunes the scan and emit pair (each
-// candidate rewrites the same outputs from the same counts).
-template <class L>
-pump_status_t run_chunked_emit_tuned(int kernel, long long n, long long ntiles, const L &ld,
-                                     cudaStream_t stream, const TileScratch &ts) {
-  static const int kPerSm[3] = {2, 4, 8};
-  auto run = [&](int c) { return run_chunked_emit(n, ntiles, ld, stream, ts, kPerSm[c], nullptr); };
   int choice = 1;
   bool ran = false;
   PUMP_TRY(tune_choice(kernel, tune_bucket(n), 3, 1, stream, run, &choice, &ran));

@@ -24,6 +24,7 @@ class Ctx {
     kRefine,       // refinement descent state (refine.cu)
     kSuperset,     // rn bracket bound and the pairs below it (select.cu)
     kLoop,         // the search loop graph's argument block and tile scratch
+    kPairStage,    // per warp of the pair pass: the mask of its rn superset pairs
     kNumSlots
   };
   // Pinned host staging buffers (uploads, read-backs of small results).
@@ -130,6 +131,8 @@ struct RnEdgesPack {
   uint32_t rn_bits;
   int ok;
   unsigned long long edges;
+  int error;  // a look-back wait of the pass gave up (PUMP_ERR_TIMEOUT)
+  int pad;
 };
 
 // rn (the k-th smallest pair cost) and the edges below it in one read of the
@@ -146,6 +149,11 @@ pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long lon
                              int *d_src, int *d_dst, float *d_copt, float *d_topt,
                              int *d_go_start, float *h_rn, long long *h_num_edges,
                              cudaStream_t stream, const RnEdgesPack **deferred = nullptr);
+// A read-back pack: PUMP_ERR_TIMEOUT when a wait gave up, fallback() when
+// ok = 0, else rn and the edge count (PUMP_ERR_CAPACITY past max_edges).
+pump_status_t rn_edges_unpack(const RnEdgesPack &pk, long long k, long long max_edges, float *h_rn,
+                              long long *h_num_edges,
+                              const std::function<pump_status_t()> &fallback);
 // The exact three-pass select over all pairs and the full compaction
 // (synchronises): what a pack with ok = 0 falls back to.
 pump_status_t rn_edges_fallback_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
@@ -158,11 +166,11 @@ pump_status_t rn_edges_fallback_pairs(Ctx *ctx, const PairView &pv, long long k,
                                       long long *h_num_edges, cudaStream_t stream);
 // All N(N-1) pair BVPs of the samples (tmax, arithmetic bvp_mode), then rn
 // and the edges as rn_edges_device.  In the precision arithmetic the pair
-// kernel also counts the rn superset as it stores the costs (the bracket
-// sample's costs are computed first), so the costs are read once after the
-// pair pass instead of twice.  stage_ms (optional, non-deferred only; 3
-// floats): CUDA-event times of what precedes the pair kernel (the samples'
-// preparation and the bracket), the pair kernel, and the rest.
+// kernel also writes the rn superset as it stores the costs (the bracket
+// sample's costs are computed first), so the costs are not read again.
+// stage_ms (optional, non-deferred only; 3 floats): CUDA-event times of what
+// precedes the pair kernel (the samples' preparation and the bracket), the
+// pair kernel, and the rest.
 pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float tmax,
                                   int bvp_mode, long long k, long long max_edges, float *d_copts,
                                   float *d_topts, int *d_src, int *d_dst, float *d_copt,
@@ -177,20 +185,34 @@ pump_status_t particle_tables_async(uint64_t seed, int P, int T, float *d_tmajor
                                     cudaStream_t stream);
 pump_status_t bvp_pairs_precision_launch(const float *d_samples, int N, float tmax, float *d_copts,
                                          float *d_topts, cudaStream_t stream);
-// Pairs per count tile of the rn superset pass (the tile of compact.cuh).
-constexpr int kRnCountTile = 4096;
-// The precision pair pass with the rn superset counted as the costs are
-// stored: first the costs of the S bracket-sample pairs (positions
-// floor((2q + 1) n / (2 S)) of the N(N-1) pair order) into d_sample_costs,
-// then bracket() (launches the kernel that turns them into *d_key_hi), then
-// all pairs, adding to d_tile_counts[p / kRnCountTile] the pairs p whose
-// cost's order key is below *d_key_hi (the counts start zeroed).
-pump_status_t bvp_pairs_precision_counted(const float *d_samples, int N, float tmax,
-                                          float *d_copts, float *d_topts, int S,
-                                          float *d_sample_costs,
-                                          const std::function<pump_status_t()> &bracket,
-                                          const unsigned long long *d_key_hi,
-                                          unsigned int *d_tile_counts, cudaStream_t stream);
+// The precision pair pass marking the rn superset as it stores the costs.
+// One kernel prepares the samples and computes the bracket sample's costs
+// (pair numbers floor((2q + 1) n / (2 S)), S = the bracket's sample count)
+// and, in its last block, the bracket bound *key_hi for the given rank.
+// The pair kernel then stores every pair's cost and time and, per warp of
+// 32 consecutive pairs of a row, the mask of those whose cost's order key is
+// below *key_hi; *out describes the masks (masks_per_row per row of the
+// pair matrix, each covering pairs 32 m .. 32 m + 31 of its row, bits past
+// the row's end zero).  N <= 65535; sample_keys holds S words; done is one
+// word, zero before the call (the kernel leaves it zero).  `between`
+// (optional) is recorded before the pair kernel, after_pairs (optional)
+// after it.
+struct PairStage {
+  const uint32_t *masks;
+  long long nmasks;
+  int masks_per_row;
+};
+struct PairSuperset {
+  unsigned int rank;
+  unsigned long long *key_hi;
+  uint32_t *sample_keys;
+  unsigned int *done;
+  cudaEvent_t after_pairs;
+  PairStage *out;
+};
+pump_status_t bvp_pairs_precision_superset(Ctx *ctx, const float *d_samples, int N, float tmax,
+                                           float *d_copts, float *d_topts, const PairSuperset &ps,
+                                           cudaStream_t stream, cudaEvent_t between = nullptr);
 // Explicit pairs (x0[k], x1[k]), k < n (x1[0] for every k with x1_same),
 // each bisected for `jobs` (1 or 2)
 // optimal-time limits: job j writes topt[j][k] and cost[j][k] (either may be

@@ -469,10 +469,10 @@ pump_status_t Planner::roadmap() {
   if (d_pack_) {
     const RnEdgesPack pk = *hpack;
     d_pack_ = nullptr;
-    if (!pk.ok) {
-      // the bracket sample misled the one-read pass: the exact select over
-      // all pairs and the full compaction (rebuilding the row starts), then
-      // the largest out-degree again
+    // the bracket sample misled the one-read pass: the exact select over all
+    // pairs and the full compaction (rebuilding the row starts), then the
+    // largest out-degree again
+    auto fallback = [&]() -> pump_status_t {
       if (use_pv_)
         PUMP_TRY(rn_edges_fallback_pairs(ctx_, pv_, rnIdx, cap, d_src_.p, d_dst_.p, d_coptE_.p,
                                          d_toptE_.p, d_go_.p, &rn_, &E_, s_));
@@ -482,14 +482,9 @@ pump_status_t Planner::roadmap() {
                                           s_));
       PUMP_TRY(max_degree_async(d_go_.p, N_, d_scalar_.p, s_));
       PUMP_CUDA_TRY(cudaMemcpyAsync(hout + 1, d_scalar_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
-      PUMP_TRY(sync());
-    } else {
-      if ((long long)pk.edges > cap)
-        return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld",
-                         pk.edges, cap);
-      std::memcpy(&rn_, &pk.rn_bits, sizeof(float));
-      E_ = (long long)pk.edges;
-    }
+      return sync();
+    };
+    PUMP_TRY(rn_edges_unpack(pk, rnIdx, cap, &rn_, &E_, fallback));
   }
   res_->rn = rn_;
   res_->num_edges = E_;

@@ -15,7 +15,9 @@
 #include <vector>
 
 #include "common.cuh"
+#include "bracket.cuh"
 #include "compact.cuh"
+#include "rnfinish.cuh"
 #include "ctx.h"
 #include "pairview.cuh"
 
@@ -69,12 +71,55 @@ struct PairTopt {
 constexpr int kSelectBatch = 8;
 constexpr int kSelectThreads = 256;
 
-// Src(i) -> the i-th value (a flat array, or a virtual pair array).
+// One block of kSelectThreads threads after a pass's histogram is complete:
+// find the bin holding rank k, narrow the prefix, clear the histogram for
+// the next pass.
+__device__ void select_pick(SelectState *st, int shift, int bits, unsigned int *hist) {
+  __shared__ unsigned long long cum[kSelectThreads];
+  const int nb = 1 << bits;
+  const int per = nb / kSelectThreads;  // 4 or 8 bins per thread
+  const int t = threadIdx.x;
+  unsigned long long mine = 0;
+  for (int q = 0; q < per; ++q) mine += __ldcg(&hist[t * per + q]);
+  cum[t] = mine;
+  __syncthreads();
+  for (int off = 1; off < kSelectThreads; off <<= 1) {  // inclusive Hillis-Steele scan
+    unsigned long long add = t >= off ? cum[t - off] : 0;
+    __syncthreads();
+    cum[t] += add;
+    __syncthreads();
+  }
+  const unsigned long long k = st->k;
+  const unsigned long long before = cum[t] - mine;
+  if (k >= before && k < cum[t]) {
+    unsigned long long c = before;
+    for (int q = 0; q < per; ++q) {
+      const unsigned int h = __ldcg(&hist[t * per + q]);
+      if (k < c + h) {
+        const uint32_t bin = (uint32_t)(t * per + q);
+        st->prefix |= bin << shift;
+        st->mask |= (uint32_t)(nb - 1) << shift;
+        st->k = k - c;
+        if (shift == 0) st->result = bits_of_key(st->prefix);
+        break;
+      }
+      c += h;
+    }
+  }
+  __syncthreads();
+  for (int q = 0; q < per; ++q) hist[t * per + q] = 0;
+}
+
+// Src(i) -> the i-th value (a flat array, or a virtual pair array).  One
+// pass of the radix select: every block adds its keys' bins (under the
+// state's prefix) to hist; the block that finishes last (a counter of
+// finished blocks, *done, reset by that block) picks the bin of rank k.
 template <class Src>
 __global__ void __launch_bounds__(kSelectThreads) select_hist_kernel(Src src, long long n, const unsigned long long *d_n,
-                                   const SelectState *__restrict__ st, int shift, int bits,
-                                   unsigned int *__restrict__ hist) {
+                                   SelectState *__restrict__ st, int shift, int bits,
+                                   unsigned int *__restrict__ hist, unsigned int *done) {
   __shared__ unsigned int sh[2048];
+  __shared__ bool s_last;
   const int nb = 1 << bits;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sh[b] = 0;
   __syncthreads();
@@ -105,57 +150,30 @@ __global__ void __launch_bounds__(kSelectThreads) select_hist_kernel(Src src, lo
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
     if (sh[b]) atomicAdd(&hist[b], sh[b]);
+  // the last block to finish sees every block's additions
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  select_pick(st, shift, bits, hist);
+  if (threadIdx.x == 0) *done = 0u;
 }
 
-// Start state of a selection and a cleared histogram (a kernel instead of a
-// host-to-device copy: a copy from pageable host memory would wait for the
-// stream to drain first).
-__global__ void __launch_bounds__(1024) select_init_kernel(SelectState *st, unsigned long long k, unsigned int *hist) {
+// Start state of a selection, a cleared histogram and block counter (a
+// kernel instead of a host-to-device copy: a copy from pageable host memory
+// would wait for the stream to drain first).
+__global__ void __launch_bounds__(1024) select_init_kernel(SelectState *st, unsigned long long k,
+                                                           unsigned int *hist, unsigned int *done) {
   for (int i = threadIdx.x; i < 2048; i += blockDim.x) hist[i] = 0u;
   if (threadIdx.x == 0) {
     st->prefix = 0u;
     st->mask = 0u;
     st->k = k;
     st->result = 0u;
+    *done = 0u;
   }
-}
-
-// One block of 1024 threads: find the bin holding rank k, narrow the prefix,
-// clear the histogram for the next pass.
-__global__ void __launch_bounds__(1024) select_pick_kernel(SelectState *st, int shift, int bits, unsigned int *hist) {
-  __shared__ unsigned long long cum[1024];
-  const int nb = 1 << bits;
-  const int per = nb / 1024;  // 1 or 2 bins per thread
-  const int t = threadIdx.x;
-  unsigned long long mine = 0;
-  for (int q = 0; q < per; ++q) mine += hist[t * per + q];
-  cum[t] = mine;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
-    unsigned long long add = t >= off ? cum[t - off] : 0;
-    __syncthreads();
-    cum[t] += add;
-    __syncthreads();
-  }
-  const unsigned long long k = st->k;
-  unsigned long long before = cum[t] - mine;
-  if (k >= before && k < cum[t]) {
-    unsigned long long c = before;
-    for (int q = 0; q < per; ++q) {
-      const unsigned int h = hist[t * per + q];
-      if (k < c + h) {
-        const uint32_t bin = (uint32_t)(t * per + q);
-        st->prefix |= bin << shift;
-        st->mask |= (uint32_t)(nb - 1) << shift;
-        st->k = k - c;
-        if (shift == 0) st->result = bits_of_key(st->prefix);
-        break;
-      }
-      c += h;
-    }
-  }
-  __syncthreads();
-  for (int q = 0; q < per; ++q) hist[t * per + q] = 0;
 }
 
 // ------------------------------------------------------ compaction users
@@ -171,91 +189,19 @@ struct IndexEmit {
 __global__ void copy_count_kernel(const unsigned long long *total, int *out) { *out = (int)*total; }
 
 // ------------------------------------------------- rn and edges in one read
-// The reference sorts all N(N-1) pair costs to read rn and then scans them
-// again for the edges below rn.  Here a strided sample of kBracketSamples
-// costs gives a key bound key_hi (the upper edge of the 22-bit key bin of the
-// sample at a rank a few standard deviations above k): one compaction pass
-// keeps the pairs with key < key_hi (the superset, in index order, a few
-// percent of the pairs), the exact radix select for rank k runs over the
-// superset only, and the edges are compacted from it.  Every pair below rn
-// is in the superset whenever the superset holds more than k pairs, so rn
-// and the edges are exactly those of the full select; when it does not (the
-// sample misled) or the superset overflows its buffer, the host falls back to
-// the three-pass select and the full compaction.
-constexpr int kBracketSamples = 8192;
-
-// Rank r among the 2048 counts of hist (a block of 1024 threads, two bins
-// each): the bin and the rank within it land in *bin and *rem.
-__device__ void find_bin_2048(const unsigned int *hist, unsigned int r, unsigned int *s_warp,
-                              unsigned int *bin, unsigned int *rem) {
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const unsigned int h0 = hist[2 * t], h1 = hist[2 * t + 1];
-  const unsigned int v = h0 + h1;
-  unsigned int incl = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned int u = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += u;
-  }
-  if (lane == 31) s_warp[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    const unsigned int w = s_warp[lane];
-    unsigned int wi = w;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned int u = __shfl_up_sync(0xffffffffu, wi, o);
-      if (lane >= o) wi += u;
-    }
-    s_warp[lane] = wi - w;
-  }
-  __syncthreads();
-  const unsigned int ex = s_warp[warp] + incl - v;
-  if (r >= ex && r < ex + v) {
-    if (r < ex + h0) {
-      *bin = 2 * t;
-      *rem = r - ex;
-    } else {
-      *bin = 2 * t + 1;
-      *rem = r - ex - h0;
-    }
-  }
-  __syncthreads();
-}
-
+// (the bracket: bracket.cuh)
 // One block of 1024 threads: the keys of the samples at positions
-// floor((2q + 1) n / (2 S)), then two 11-bit radix steps to the 22-bit key
-// prefix of the sample of the given rank; *key_hi = the prefix's upper edge.
+// floor((2q + 1) n / (2 S)), then the bracket's radix steps.
 template <class Src>
 __global__ void __launch_bounds__(1024) bracket_kernel(Src src, long long n, unsigned int rank,
                                                        unsigned long long *key_hi) {
   __shared__ uint32_t keys[kBracketSamples];
-  __shared__ unsigned int hist[2048];
-  __shared__ unsigned int s_warp[32];
-  __shared__ unsigned int s_bin, s_rem;
-  const int t = threadIdx.x;
-  for (int q = t; q < kBracketSamples; q += 1024) {
+  for (int q = threadIdx.x; q < kBracketSamples; q += 1024) {
     const long long pos = ((2LL * q + 1) * n) / (2LL * kBracketSamples);
     keys[q] = key_of_bits(src.bits(pos));
   }
-  uint32_t prefix = 0u, mask = 0u;
-  unsigned int r = rank;
-  for (int pass = 0; pass < 2; ++pass) {
-    const int shift = pass == 0 ? 21 : 10;
-    hist[2 * t] = 0u;
-    hist[2 * t + 1] = 0u;
-    __syncthreads();
-    for (int q = t; q < kBracketSamples; q += 1024) {
-      const uint32_t k = keys[q];
-      if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 2047u], 1u);
-    }
-    __syncthreads();
-    find_bin_2048(hist, r, s_warp, &s_bin, &s_rem);
-    prefix |= s_bin << shift;
-    mask |= 2047u << shift;
-    r = s_rem;
-  }
-  if (t == 0) *key_hi = ((unsigned long long)(prefix >> 10) + 1ull) << 10;
+  __syncthreads();
+  bracket_radix(keys, rank, key_hi);
 }
 
 // Row a and column j of this thread's items of the tile at base (item r is
@@ -360,53 +306,18 @@ struct EdgeLoader {
   }
 };
 
-// rn's bits, whether the superset held rank k within its buffer, and the
-// edge count, for one read-back.
-__global__ void rn_pack_kernel(const float *rn, const unsigned long long *n_sup,
-                               const unsigned long long *edges, long long k, long long cap,
-                               RnEdgesPack *out) {
-  const unsigned long long ns = *n_sup;
-  out->rn_bits = *reinterpret_cast<const unsigned int *>(rn);
-  out->ok = (long long)ns > k && (long long)ns <= cap;
-  out->edges = *edges;
-}
-
-// Edges from the superset: entries with cost < rn, in superset (= pair) order.
-// rn is read on the device (the select's result).
-struct SupItem {
-  float c;
-  uint32_t id;
+// The optimal time of superset entry q (pair number id, pair (a, j)) for
+// the edge list: from the superset's own time column, or from the pair
+// arrays.
+struct SupToptColumn {
+  const float *t;
+  __device__ float at(long long q, uint32_t, int, int) const { return __ldcg(&t[q]); }
 };
 template <class Topt>
-struct SupEdgeLoader {
-  using Item = SupItem;
-  using State = float;
-  const uint32_t *idx;
-  const float *sc;
+struct SupToptPairs {
   Topt tsrc;
-  int N;
-  const float *rn;
-  long long cap;
-  int *e_src, *e_dst;
-  float *e_copt, *e_topt;
-  __device__ State begin() const { return *rn; }
-  __device__ void load(long long base, long long n, SupItem (&v)[kCompactRows]) const {
-#pragma unroll
-    for (int r = 0; r < kCompactRows; ++r) {
-      const long long q = base + r * kCompactThreads + threadIdx.x;
-      v[r].c = q < n ? __ldg(&sc[q]) : 0.0f;
-      v[r].id = q < n ? __ldg(&idx[q]) : 0u;
-    }
-  }
-  __device__ bool sel(State rn_v, const SupItem &v) const { return v.c < rn_v; }
-  __device__ void emit(long long, const SupItem &v, long long pos) const {
-    if (pos >= cap) return;
-    const uint32_t a = v.id / (uint32_t)(N - 1), b = v.id - a * (uint32_t)(N - 1);
-    const int j = (int)b + (b >= a ? 1 : 0);
-    e_src[pos] = (int)a;
-    e_dst[pos] = j;
-    e_copt[pos] = v.c;
-    e_topt[pos] = tsrc.at((long long)v.id, (int)a, j);
+  __device__ float at(long long, uint32_t id, int a, int j) const {
+    return tsrc.at((long long)id, a, j);
   }
 };
 
@@ -419,11 +330,12 @@ pump_status_t select_kth_src(Ctx *ctx, Src src, long long n, long long k, const 
                              long long max_blocks = kNumSMs * 4) {
   if (n <= 0 || k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "select_kth: k=%lld n=%lld", k, n);
   char *scratch = nullptr;
-  const size_t bytes = sizeof(SelectState) + 2048 * sizeof(unsigned int);
+  const size_t bytes = sizeof(SelectState) + 2049 * sizeof(unsigned int);
   PUMP_TRY(ctx->scratch(Ctx::kSelect, bytes, (void **)&scratch));
   SelectState *st = (SelectState *)scratch;
   unsigned int *hist = (unsigned int *)(scratch + sizeof(SelectState));
-  select_init_kernel<<<1, 1024, 0, stream>>>(st, (unsigned long long)k, hist);
+  unsigned int *done = hist + 2048;
+  select_init_kernel<<<1, 1024, 0, stream>>>(st, (unsigned long long)k, hist, done);
   PUMP_TRY(launch_status("select_init_kernel"));
   long long blocks = (n + (long long)kSelectThreads * kSelectBatch - 1) /
                      ((long long)kSelectThreads * kSelectBatch);
@@ -431,10 +343,8 @@ pump_status_t select_kth_src(Ctx *ctx, Src src, long long n, long long k, const 
   const int shifts[3] = {21, 10, 0}, bits[3] = {11, 11, 10};
   for (int pass = 0; pass < 3; ++pass) {
     select_hist_kernel<<<(unsigned)blocks, kSelectThreads, 0, stream>>>(src, n, d_n, st, shifts[pass],
-                                                              bits[pass], hist);
+                                                              bits[pass], hist, done);
     PUMP_TRY(launch_status("select_hist_kernel"));
-    select_pick_kernel<<<1, 1024, 0, stream>>>(st, shifts[pass], bits[pass], hist);
-    PUMP_TRY(launch_status("select_pick_kernel"));
   }
   *d_result = reinterpret_cast<const float *>(&st->result);
   return PUMP_OK;
@@ -507,52 +417,114 @@ bool rn_plan(long long n, long long k, RnPlan *pl) {
   return k < pl->cap;
 }
 
-// Scratch of the one-read pass: the bracket key, the read-back pack, the
-// superset's size (kept here: the compaction scratch holding the pass's own
-// count is reused by the edge compaction), the bracket sample's costs and
-// the superset (pair numbers, then costs).
+// Scratch of the one-read pass.  A zeroed head (per call): the bracket key,
+// the read-back pack, the superset's size, the bracket's block counter, the
+// finishing kernel's barrier words and error word, then its three select
+// histograms; after it the finishing kernel's
+// per-block partial sums, the bracket sample's keys and the superset (pair
+// numbers, costs, times).
+constexpr int kMaxFinishBlocks = 1024;
 struct RnScratch {
   unsigned long long *key_hi;
   RnEdgesPack *pack;
   unsigned long long *n_sup;
-  float *sample_costs;
+  unsigned int *done, *bar;
+  int *error;
+  unsigned int *hist;
+  unsigned long long *partial;
+  uint32_t *sample_keys;
   uint32_t *sup_idx;
-  float *sup_c;
+  float *sup_c, *sup_t;
 };
-pump_status_t rn_scratch(Ctx *ctx, long long cap, RnScratch *rs) {
+pump_status_t rn_scratch(Ctx *ctx, long long cap, cudaStream_t stream, RnScratch *rs) {
   char *buf = nullptr;
-  const size_t head = 64 + sizeof(float) * kBracketSamples;
-  PUMP_TRY(ctx->scratch(Ctx::kSuperset, head + (size_t)cap * 8, (void **)&buf));
+  constexpr size_t kWords = 128;
+  constexpr size_t kZeroed = kWords + 3 * 2048 * sizeof(unsigned int);
+  const size_t head = kZeroed + 2 * kMaxFinishBlocks * sizeof(unsigned long long) +
+                      sizeof(uint32_t) * kBracketSamples;
+  PUMP_TRY(ctx->scratch(Ctx::kSuperset, head + (size_t)cap * 12, (void **)&buf));
+  static_assert(sizeof(RnEdgesPack) <= 32, "pack fits its slot");
   rs->key_hi = (unsigned long long *)buf;
   rs->pack = (RnEdgesPack *)(buf + 16);
-  rs->n_sup = (unsigned long long *)(buf + 32);
-  rs->sample_costs = (float *)(buf + 64);
+  rs->n_sup = (unsigned long long *)(buf + 48);
+  rs->done = (unsigned int *)(buf + 56);
+  rs->bar = (unsigned int *)(buf + 64);
+  rs->error = (int *)(buf + 72);
+  rs->hist = (unsigned int *)(buf + kWords);
+  rs->partial = (unsigned long long *)(buf + kZeroed);
+  rs->sample_keys = (uint32_t *)(rs->partial + 2 * kMaxFinishBlocks);
   rs->sup_idx = (uint32_t *)(buf + head);
   rs->sup_c = (float *)(rs->sup_idx + cap);
+  rs->sup_t = rs->sup_c + cap;
+  PUMP_CUDA_TRY(cudaMemsetAsync(buf, 0, kZeroed, stream));
   return PUMP_OK;
 }
 
-// After the superset (pair order, its count in *rs.n_sup): the select
-// over it for rank k, the edges below rn compacted from it, the row starts
-// and the pack, all on the device.  Then either the deferred pack pointer,
-// or one read-back: rn and the edge count, or the fallback when the
-// superset missed rank k or overflowed.
-template <class Topt, class Fallback>
-pump_status_t rn_edges_tail(Ctx *ctx, const RnScratch &rs, Topt tsrc,
-                            int N, long long k, long long cap, long long max_edges, int *d_src,
+// One block per SM for the finishing kernel (cooperative launch).
+template <class TSup>
+pump_status_t rn_finish_launch(const RnFinish<TSup> &a, cudaStream_t stream) {
+  int dev = 0, sms = 0, coop = 0, occ = 0;
+  PUMP_CUDA_TRY(cudaGetDevice(&dev));
+  PUMP_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PUMP_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  PUMP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rn_finish_kernel<TSup>,
+                                                              kFinishThreads, 0));
+  if (!coop || occ < 1)
+    return set_error(PUMP_ERR_CUDA, "rn_finish: cooperative launch unavailable");
+  const int grid = std::min(sms, kMaxFinishBlocks);
+  void *args[] = {(void *)&a};
+  PUMP_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)rn_finish_kernel<TSup>, grid,
+                                            kFinishThreads, args, 0, stream));
+  return PUMP_OK;
+}
+
+// After the pair pass (the superset as per-warp masks over the pair arrays
+// d_copts/d_topts, or contiguous in rs.sup_* with its size in *n_in): the
+// finishing kernel (select over the
+// superset for rank k, the edges below rn, the row starts, the pack).
+// Then either the deferred pack pointer, or one read-back: rn and the edge
+// count, PUMP_ERR_TIMEOUT when a wait gave up, or the fallback when the
+// superset missed rank k or overflowed.  err_pass: an earlier pass's
+// wait-bound error word (or null).
+template <class TSup, class Fallback>
+pump_status_t rn_edges_tail(const RnScratch &rs, const PairStage *stage, const float *d_copts,
+                            const float *d_topts, const unsigned long long *n_in, TSup tsup,
+                            const int *err_pass, int N,
+                            long long k, long long cap, long long max_edges, int *d_src,
                             int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
                             float *h_rn, long long *h_num_edges, cudaStream_t stream,
                             Fallback fallback, const RnEdgesPack **deferred) {
-  const float *d_rn = nullptr;
-  PUMP_TRY(select_kth_src(ctx, FlatSrc{rs.sup_c}, cap, k, &d_rn, stream, rs.n_sup));
-  TileScratch ts2{};
-  PUMP_TRY(run_chunked_tuned(ctx, kTuneCompactEdges, cap,
-                             SupEdgeLoader<Topt>{rs.sup_idx, rs.sup_c, tsrc, N, d_rn, max_edges,
-                                                 d_src, d_dst, d_copt, d_topt},
-                             stream, &ts2, rs.n_sup));
-  if (d_go_start) PUMP_TRY(row_starts(d_src, max_edges, N, d_go_start, stream, ts2.total));
-  rn_pack_kernel<<<1, 1, 0, stream>>>(d_rn, rs.n_sup, ts2.total, k, cap, rs.pack);
-  PUMP_TRY(launch_status("rn_pack_kernel"));
+  RnFinish<TSup> a{};
+  if (stage) {
+    a.masks = stage->masks;
+    a.nmasks = stage->nmasks;
+    a.masks_per_row = stage->masks_per_row;
+    a.copts = d_copts;
+    a.topts = d_topts;
+  }
+  a.n_in = n_in;
+  a.sup_idx = rs.sup_idx;
+  a.sup_c = rs.sup_c;
+  a.sup_t = rs.sup_t;
+  a.tsup = tsup;
+  a.cap = cap;
+  a.k = k;
+  a.max_edges = max_edges;
+  a.N = N;
+  a.e_src = d_src;
+  a.e_dst = d_dst;
+  a.e_copt = d_copt;
+  a.e_topt = d_topt;
+  a.go_start = d_go_start;
+  a.hist = rs.hist;
+  a.partial = rs.partial;
+  a.bar = rs.bar;
+  a.n_sup = rs.n_sup;
+  a.err_in = err_pass;
+  a.error = rs.error;
+  a.pack = rs.pack;
+  a.spin_limit = kBarrierSpin;
+  PUMP_TRY(rn_finish_launch(a, stream));
   if (deferred) {
     *deferred = rs.pack;
     *h_num_edges = -1;
@@ -561,13 +533,7 @@ pump_status_t rn_edges_tail(Ctx *ctx, const RnScratch &rs, Topt tsrc,
   RnEdgesPack pk{};
   PUMP_CUDA_TRY(cudaMemcpyAsync(&pk, rs.pack, sizeof pk, cudaMemcpyDeviceToHost, stream));
   PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
-  if (!pk.ok) return fallback();
-  std::memcpy(h_rn, &pk.rn_bits, sizeof(float));
-  *h_num_edges = (long long)pk.edges;
-  if ((long long)pk.edges > max_edges)
-    return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", pk.edges,
-                     max_edges);
-  return PUMP_OK;
+  return rn_edges_unpack(pk, k, max_edges, h_rn, h_num_edges, fallback);
 }
 
 // rn = the k-th smallest pair cost and the edges below it (same values and
@@ -586,7 +552,7 @@ pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, lon
   RnPlan pl;
   if (!rn_plan(n, k, &pl)) return fallback();
   RnScratch rs;
-  PUMP_TRY(rn_scratch(ctx, pl.cap, &rs));
+  PUMP_TRY(rn_scratch(ctx, pl.cap, stream, &rs));
   bracket_kernel<<<1, 1024, 0, stream>>>(src, n, (unsigned int)pl.rank, rs.key_hi);
   PUMP_TRY(launch_status("bracket_kernel"));
   TileScratch ts{};
@@ -594,11 +560,27 @@ pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, lon
                              SupersetLoader<Src>{src, N, rs.key_hi, pl.cap, rs.sup_idx,
                                                  (uint32_t *)rs.sup_c},
                              stream, &ts, nullptr, rs.n_sup));
-  return rn_edges_tail(ctx, rs, tsrc, N, k, pl.cap, max_edges, d_src, d_dst, d_copt, d_topt,
-                       d_go_start, h_rn, h_num_edges, stream, fallback, deferred);
+  return rn_edges_tail(rs, nullptr, nullptr, nullptr, rs.n_sup, SupToptPairs<Topt>{tsrc}, nullptr,
+                       N, k, pl.cap,
+                       max_edges, d_src, d_dst, d_copt, d_topt, d_go_start, h_rn, h_num_edges,
+                       stream, fallback, deferred);
 }
 
 }  // namespace
+
+pump_status_t rn_edges_unpack(const RnEdgesPack &pk, long long k, long long max_edges, float *h_rn,
+                              long long *h_num_edges, const std::function<pump_status_t()> &fallback) {
+  (void)k;
+  if (pk.error)
+    return set_error(PUMP_ERR_TIMEOUT, "rn and edges: a look-back wait exceeded its bound");
+  if (!pk.ok) return fallback();
+  std::memcpy(h_rn, &pk.rn_bits, sizeof(float));
+  *h_num_edges = (long long)pk.edges;
+  if ((long long)pk.edges > max_edges)
+    return set_error(PUMP_ERR_CAPACITY, "build_edges: %llu edges exceed capacity %lld", pk.edges,
+                     max_edges);
+  return PUMP_OK;
+}
 
 pump_status_t rn_edges_fallback_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
                                        long long k, long long max_edges, int *d_src, int *d_dst,
@@ -661,7 +643,7 @@ pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float
   if (N < 2) return set_error(PUMP_ERR_BAD_INPUT, "roadmap: N = %d", N);
   const long long n = (long long)N * (N - 1);
   if (k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "roadmap: k=%lld n=%lld", k, n);
-  // stage events: start, pair pass start, pair pass end, end
+  // stage events: start, pair kernel start, pair kernel end, end
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   struct EvGuard {
     cudaEvent_t *e;
@@ -683,7 +665,7 @@ pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float
     return st;
   };
   RnPlan pl;
-  if (bvp_mode != PUMP_BVP_PRECISION || !rn_plan(n, k, &pl)) {
+  if (bvp_mode != PUMP_BVP_PRECISION || !rn_plan(n, k, &pl) || N > 65535) {
     if (ev[1]) PUMP_CUDA_TRY(cudaEventRecord(ev[1], stream));
     PUMP_TRY(pump_bvp_pairs(d_samples, N, tmax, bvp_mode, d_copts, d_topts, (pump_stream_t)stream));
     if (ev[2]) PUMP_CUDA_TRY(cudaEventRecord(ev[2], stream));
@@ -691,35 +673,28 @@ pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float
                                   d_topt, d_go_start, h_rn, h_num_edges, stream, deferred));
   }
   RnScratch rs;
-  PUMP_TRY(rn_scratch(ctx, pl.cap, &rs));
-  TileScratch ts{};
-  long long ntiles = 0;
-  PUMP_TRY(prepare_tiles(ctx, n, stream, &ts, &ntiles));  // the zeroed tile counts
-  ts.copy_to = rs.n_sup;
-  static_assert(kRnCountTile == kTile, "count tiles of the pair pass are the compaction's tiles");
-  auto bracket = [&]() -> pump_status_t {
-    bracket_kernel<<<1, 1024, 0, stream>>>(FlatSrc{rs.sample_costs}, (long long)kBracketSamples,
-                                           (unsigned int)pl.rank, rs.key_hi);
-    PUMP_TRY(launch_status("bracket_kernel"));
-    if (ev[1]) PUMP_CUDA_TRY(cudaEventRecord(ev[1], stream));
-    return PUMP_OK;
-  };
-  PUMP_TRY(bvp_pairs_precision_counted(d_samples, N, tmax, d_copts, d_topts, kBracketSamples,
-                                       rs.sample_costs, bracket, rs.key_hi,
-                                       reinterpret_cast<unsigned int *>(ts.status), stream));
-  if (ev[2]) PUMP_CUDA_TRY(cudaEventRecord(ev[2], stream));
-  PUMP_TRY(run_chunked_emit_tuned(kTuneCompactRnEmit, n, ntiles,
-                                  SupersetLoader<FlatSrc>{FlatSrc{d_copts}, N, rs.key_hi, pl.cap,
-                                                          rs.sup_idx, (uint32_t *)rs.sup_c},
-                                  stream, ts));
+  PUMP_TRY(rn_scratch(ctx, pl.cap, stream, &rs));
+  PairStage stage{};
+  PairSuperset ps{};
+  ps.rank = (unsigned int)pl.rank;
+  ps.key_hi = rs.key_hi;
+  ps.sample_keys = rs.sample_keys;
+  ps.done = rs.done;
+  ps.after_pairs = ev[2];
+  ps.out = &stage;
+  // the samples and bracket launch comes first; the pair kernel's own time
+  // is ev[1]..ev[2]
+  PUMP_TRY(bvp_pairs_precision_superset(ctx, d_samples, N, tmax, d_copts, d_topts, ps, stream,
+                                        ev[1]));
   auto fallback = [&]() -> pump_status_t {
     if (deferred) *deferred = nullptr;
     return rn_edges_fallback_device(ctx, d_copts, d_topts, N, k, max_edges, d_src, d_dst, d_copt,
                                     d_topt, d_go_start, h_rn, h_num_edges, stream);
   };
-  return finish(rn_edges_tail(ctx, rs, FlatTopt{d_topts}, N, k, pl.cap, max_edges, d_src,
-                              d_dst, d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream,
-                              fallback, deferred));
+  return finish(rn_edges_tail(rs, &stage, d_copts, d_topts, nullptr, SupToptColumn{rs.sup_t},
+                              nullptr, N, k, pl.cap,
+                              max_edges, d_src, d_dst, d_copt, d_topt, d_go_start, h_rn,
+                              h_num_edges, stream, fallback, deferred));
 }
 
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
@@ -928,7 +903,7 @@ extern "C" pump_status_t pump_frontier_compact_noalloc(const uint8_t *d_flags, i
   PUMP_CUDA_TRY(cudaMemsetAsync(ts.tile_counter, 0, 2 * sizeof(unsigned int), s));
   if (N > 0) {
     compact_kernel<<<(unsigned)ntiles, kCompactThreads, 0, s>>>((long long)N, FlagPred{d_flags},
-                                                                IndexEmit{d_active}, ts);
+                                                                IndexEmit{d_active}, ts, nullptr);
     PUMP_TRY(launch_status("compact_kernel (no-alloc)"));
   }
   copy_count_kernel<<<1, 1, 0, s>>>(ts.total, d_count);

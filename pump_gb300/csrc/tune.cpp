@@ -16,7 +16,7 @@ namespace pump {
 namespace {
 
 const char *const kTuneNames[kNumTune] = {"bvp_pairs_precision", "discretize", "free_edges",
-                                           "compact_rn", "compact_edges", "compact_rn_emit"};
+                                           "compact_rn", "compact_edges"};
 
 struct Record {
   int choice;

@@ -23,7 +23,6 @@ enum TuneKernel {
   kTuneFreeEdges,      // free_edges_staged_kernel block size
   kTuneCompactRn,      // three-kernel compaction grid: rn superset pass
   kTuneCompactEdges,   // three-kernel compaction grid: edge lists
-  kTuneCompactRnEmit,  // rn superset emit grid after the counted pair pass
   kNumTune
 };
 

@@ -343,12 +343,16 @@ def roadmap_sample_sets():
     # four tight clusters: the strided sample sees rows of very uneven density
     cen = lo + (hi - lo) * rng.random((4, 6))
     clu = (cen[rng.integers(0, 4, 1800)] + rng.normal(0, 0.02, (1800, 6))).astype(np.float32)
+    # four states repeated 200 times each: the pair costs take a few values,
+    # so the superset under the bracket (a quarter of all pairs) overflows
+    # its buffer and the pass falls back to the full select
+    ties = np.repeat(uni[:4], 200, axis=0)
     return {"halton1000": halton_samples(1000, workloads.INIT, workloads.GOAL, workloads.LO,
                                          workloads.HI),
-            "uniform2100": uni, "clusters1800": clu}
+            "uniform2100": uni, "clusters1800": clu, "ties800": ties}
 
 
-@pytest.mark.parametrize("case", ["halton1000", "uniform2100", "clusters1800"])
+@pytest.mark.parametrize("case", ["halton1000", "uniform2100", "clusters1800", "ties800"])
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_roadmap_one_call(case, mode, gpu, pumplib):
     """pump_roadmap (pair BVPs counting the rn superset as they store the
