@@ -782,16 +782,17 @@ def mode_record(lib, L, ctx, torch, w, mode, args, flush, batch, steps=None, war
 BVP_FP64_FLOPS_PER_PAIR = {"precision": 28.0, "parity": 40.0 * 23 + 20.0}
 # The precision kernel is bound by instruction issue, not by one pipe: warp
 # instructions executed per pair on this workload (ncu smsp__inst_executed.sum
-# over one launch of the N = 4000 workload / its pairs), and DRAM bytes per
-# launch (dram__bytes_read.sum + dram__bytes_write.sum of the same launch).
-BVP_PRECISION_WARP_INST_PER_PAIR = 42.5
+# over one launch of the N = 4000 workload's pair kernel, the one marking the
+# rn superset, / its pairs), and DRAM bytes per launch
+# (dram__bytes_read.sum + dram__bytes_write.sum of the same launch).
+BVP_PRECISION_WARP_INST_PER_PAIR = 703111934 / 15996000
 # ncu smsp__inst_executed.sum on indoor4000: the edge check (pair-queue
 # kernel) at block size 128, the autotuner's choice there (64 and 256 differ
 # by under 0.3 %), per edge; the waypoint kernel (thread per edge, block size
 # 128), per waypoint
 FREE_EDGES_WARP_INST_PER_EDGE_N4000 = 88103877 / 799800
 DISCRETIZE_WARP_INST_PER_WAYPOINT = 18258294 / (799800 * 9)
-BVP_PRECISION_DRAM_BYTES_N4000 = 0.16e6 + 66.71e6
+BVP_PRECISION_DRAM_BYTES_N4000 = 0.16e6 + 69.18e6
 SMSP_PER_SM = 4
 NUM_SMS = 152
 

@@ -59,12 +59,15 @@ __global__ void __launch_bounds__(T) bvp_pairs_precision_kernel(const SampleF *_
 }
 
 // The samples' binary64 forms and the rn bracket, one launch: blocks below
-// nprep prepare 1024 samples each; the kBracketSamples / 1024 blocks after
-// them compute the costs of the bracket-sample pairs (pair number
-// floor((2q + 1) n / (2 S)), from the raw samples) and store their order
-// keys, and the one of those that finishes last (a counter of finished
-// blocks, reset by that block) runs the bracket's radix steps over all of
-// them.
+// nprep prepare 1024 samples each; the kBracketBlocks blocks after them
+// compute, in their first kBracketPerBlock threads, the costs of the
+// bracket-sample pairs (pair number floor((2q + 1) n / (2 S)), from the raw
+// samples; spread over many SMs, as the binary64 pipe of one SM would take
+// several times longer) and store their order keys, and the one of those
+// that finishes last (a counter of finished blocks, reset by that block)
+// runs the bracket's radix steps over all of them with its 1024 threads.
+constexpr int kBracketPerBlock = 128;
+constexpr int kBracketBlocks = kBracketSamples / kBracketPerBlock;
 __global__ void __launch_bounds__(1024) prepare_bracket_kernel(
     const float *__restrict__ samples, int N, float tmax, int nprep, SampleF *__restrict__ sf,
     unsigned int rank, uint32_t *keys_g, unsigned int *done, unsigned long long *key_hi) {
@@ -80,24 +83,26 @@ __global__ void __launch_bounds__(1024) prepare_bracket_kernel(
   }
   __shared__ uint32_t keys[kBracketSamples];
   __shared__ bool s_last;
-  const int q = ((int)blockIdx.x - nprep) * 1024 + threadIdx.x;
-  const long long n = (long long)N * (N - 1);
-  const long long pos = ((2LL * q + 1) * n) / (2LL * kBracketSamples);
-  const int i = (int)(pos / (N - 1));
-  const int r = (int)(pos - (long long)i * (N - 1));
-  const int j = r + (r >= i);
-  float a[kDim], b[kDim];
+  if (threadIdx.x < kBracketPerBlock) {
+    const int q = ((int)blockIdx.x - nprep) * kBracketPerBlock + threadIdx.x;
+    const long long n = (long long)N * (N - 1);
+    const long long pos = ((2LL * q + 1) * n) / (2LL * kBracketSamples);
+    const int i = (int)(pos / (N - 1));
+    const int r = (int)(pos - (long long)i * (N - 1));
+    const int j = r + (r >= i);
+    float a[kDim], b[kDim];
 #pragma unroll
-  for (int d = 0; d < kDim; ++d) {
-    a[d] = samples[i * kDim + d];
-    b[d] = samples[j * kDim + d];
+    for (int d = 0; d < kDim; ++d) {
+      a[d] = samples[i * kDim + d];
+      b[d] = samples[j * kDim + d];
+    }
+    double t, c;
+    precise_tau(a, b, tmax, &t, &c);
+    keys_g[q] = key_of_bits(__float_as_uint(d2f_rn(c)));
   }
-  double t, c;
-  precise_tau(a, b, tmax, &t, &c);
-  keys_g[q] = key_of_bits(__float_as_uint(d2f_rn(c)));
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == kBracketSamples / 1024 - 1;
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == kBracketBlocks - 1;
   __syncthreads();
   if (!s_last) return;
   __threadfence();
@@ -197,8 +202,8 @@ pump_status_t bvp_pairs_precision_superset(Ctx *ctx, const float *d_samples, int
   SampleF *sd = nullptr;
   PUMP_CUDA_TRY(pool_malloc_async((void **)&sd, sizeof(SampleF) * (size_t)N, stream));
   const int nprep = (N + 1023) / 1024;
-  static_assert(kBracketSamples % 1024 == 0, "whole bracket blocks");
-  prepare_bracket_kernel<<<nprep + kBracketSamples / 1024, 1024, 0, stream>>>(
+  static_assert(kBracketSamples % kBracketPerBlock == 0, "whole bracket blocks");
+  prepare_bracket_kernel<<<nprep + kBracketBlocks, 1024, 0, stream>>>(
       d_samples, N, tmax, nprep, sd, ps.rank, ps.sample_keys, ps.done, ps.key_hi);
   pump_status_t st = launch_status("prepare_bracket");
   if (st == PUMP_OK && between && cudaEventRecord(between, stream) != cudaSuccess)

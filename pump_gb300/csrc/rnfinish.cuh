@@ -35,16 +35,16 @@ constexpr long long kBarrierSpin = 1ll << 22;  // polls (each with a 100 ns slee
 template <class TSup>
 struct RnFinish {
   // the pair pass's superset masks (non-null: nmasks warp masks,
-  // masks_per_row per row of the pair matrix, the costs and times in
-  // copts/topts) or a contiguous superset of *n_in entries already in sup_*
+  // masks_per_row per row of the pair matrix, the costs in copts) or a
+  // contiguous superset of *n_in entries already in sup_idx and sup_c
   const uint32_t *masks;
   long long nmasks;
   int masks_per_row;
-  const float *copts, *topts;
+  const float *copts;
   const unsigned long long *n_in;
   uint32_t *sup_idx;
-  float *sup_c, *sup_t;
-  TSup tsup;  // the optimal time of superset entry q
+  float *sup_c;
+  TSup tsup;  // the optimal time of superset entry q (pair id, pair (i, j))
   long long cap, k, max_edges;
   int N;
   int *e_src, *e_dst;
@@ -65,9 +65,9 @@ struct RnFinish {
 __device__ bool finish_barrier(unsigned int *bar, int *error, long long spin_limit) {
   using ref_t = cuda::atomic_ref<unsigned int, cuda::thread_scope_device>;
   __shared__ int s_ok;
-  __threadfence();
-  __syncthreads();
+  __syncthreads();  // the block's writes are ordered before thread 0's fence
   if (threadIdx.x == 0) {
+    __threadfence();
     ref_t gen(bar[1]);
     const unsigned int g = gen.load(cuda::memory_order_acquire);
     int ok = 1;
@@ -85,6 +85,7 @@ __device__ bool finish_barrier(unsigned int *bar, int *error, long long spin_lim
         __nanosleep(100);
       }
     }
+    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
@@ -164,7 +165,10 @@ __global__ void __launch_bounds__(kFinishThreads) rn_finish_kernel(const RnFinis
   const int B = gridDim.x, b = blockIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const unsigned int lt = (1u << lane) - 1u;
-  // ---- the superset, contiguous and in pair order
+  for (int q = tid; q < 2048; q += kFinishThreads) s_hist[q] = 0u;
+  __syncthreads();
+  // ---- the superset, contiguous and in pair order; its first radix pass
+  // (the top 11 key bits) is counted as it is gathered
   unsigned long long total = 0;
   if (a.masks) {
     const long long per = (a.nmasks + B - 1) / B;
@@ -210,7 +214,7 @@ __global__ void __launch_bounds__(kFinishThreads) rn_finish_kernel(const RnFinis
       // entry e of the chunk: the mask whose range holds e (the last with
       // offset <= e), its (e - offset)-th set bit, the pair number
       for (unsigned int e0 = 0; e0 < chunk; e0 += kFinishThreads * kFinishBatchA) {
-        uint32_t vi[kFinishBatchA], vc[kFinishBatchA], vt[kFinishBatchA];
+        uint32_t vi[kFinishBatchA], vc[kFinishBatchA];
 #pragma unroll
         for (int u = 0; u < kFinishBatchA; ++u) {
           const unsigned int e = e0 + u * kFinishThreads + tid;
@@ -227,7 +231,6 @@ __global__ void __launch_bounds__(kFinishThreads) rn_finish_kernel(const RnFinis
             const long long idx = row * (a.N - 1) + col;
             vi[u] = (uint32_t)idx;
             vc[u] = __ldcg(reinterpret_cast<const uint32_t *>(a.copts) + idx);
-            vt[u] = __ldcg(reinterpret_cast<const uint32_t *>(a.topts) + idx);
           }
         }
 #pragma unroll
@@ -237,13 +240,17 @@ __global__ void __launch_bounds__(kFinishThreads) rn_finish_kernel(const RnFinis
           if (e < chunk && (long long)pos < a.cap) {
             a.sup_idx[pos] = vi[u];
             reinterpret_cast<uint32_t *>(a.sup_c)[pos] = vc[u];
-            reinterpret_cast<uint32_t *>(a.sup_t)[pos] = vt[u];
           }
+          const uint32_t bin = e < chunk ? key_of_bits(vc[u]) >> 21 : 0xFFFFFFFFu;
+          const unsigned int peers = __match_any_sync(0xffffffffu, bin);
+          if (e < chunk && lane == __ffs(peers) - 1) atomicAdd(&s_hist[bin], __popc(peers));
         }
       }
       run += chunk;
       __syncthreads();
     }
+    for (int q = tid; q < 2048; q += kFinishThreads)
+      if (s_hist[q]) atomicAdd(&a.hist[q], s_hist[q]);
     if (!finish_barrier(a.bar, a.error, a.spin_limit)) return;
   } else {
     total = *a.n_in;
@@ -260,34 +267,37 @@ __global__ void __launch_bounds__(kFinishThreads) rn_finish_kernel(const RnFinis
     s_mask = 0u;
     s_k = (unsigned long long)a.k;
   }
+  __syncthreads();
 #pragma unroll 1
   for (int pass = 0; pass < 3; ++pass) {
     const int shift = pass == 0 ? 21 : (pass == 1 ? 10 : 0);
     const int nb = pass == 2 ? 1024 : 2048;
-    for (int q = tid; q < nb; q += kFinishThreads) s_hist[q] = 0u;
-    __syncthreads();
-    const uint32_t prefix = s_prefix, mask = s_mask;
-    for (long long b0 = q0; b0 < q1; b0 += (long long)kFinishThreads * kFinishBatch) {
-      uint32_t key[kFinishBatch];
-#pragma unroll
-      for (int u = 0; u < kFinishBatch; ++u) {
-        const long long q = b0 + u * kFinishThreads + tid;
-        key[u] = q < q1 ? key_of_bits(__ldcg(&sup_bits[q])) : 0u;
-      }
-#pragma unroll
-      for (int u = 0; u < kFinishBatch; ++u) {
-        const long long q = b0 + u * kFinishThreads + tid;
-        const bool in = q < q1 && (key[u] & mask) == prefix;
-        const uint32_t bin = in ? (key[u] >> shift) & (nb - 1) : 0xFFFFFFFFu;
-        const unsigned int peers = __match_any_sync(0xffffffffu, bin);
-        if (in && lane == __ffs(peers) - 1) atomicAdd(&s_hist[bin], __popc(peers));
-      }
-    }
-    __syncthreads();
     unsigned int *gh = a.hist + pass * 2048;
-    for (int q = tid; q < nb; q += kFinishThreads)
-      if (s_hist[q]) atomicAdd(&gh[q], s_hist[q]);
-    if (!finish_barrier(a.bar, a.error, a.spin_limit)) return;
+    const uint32_t prefix = s_prefix, mask = s_mask;
+    if (pass > 0 || !a.masks) {  // (the gather counted the first pass)
+      for (int q = tid; q < nb; q += kFinishThreads) s_hist[q] = 0u;
+      __syncthreads();
+      for (long long b0 = q0; b0 < q1; b0 += (long long)kFinishThreads * kFinishBatch) {
+        uint32_t key[kFinishBatch];
+#pragma unroll
+        for (int u = 0; u < kFinishBatch; ++u) {
+          const long long q = b0 + u * kFinishThreads + tid;
+          key[u] = q < q1 ? key_of_bits(__ldcg(&sup_bits[q])) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kFinishBatch; ++u) {
+          const long long q = b0 + u * kFinishThreads + tid;
+          const bool in = q < q1 && (key[u] & mask) == prefix;
+          const uint32_t bin = in ? (key[u] >> shift) & (nb - 1) : 0xFFFFFFFFu;
+          const unsigned int peers = __match_any_sync(0xffffffffu, bin);
+          if (in && lane == __ffs(peers) - 1) atomicAdd(&s_hist[bin], __popc(peers));
+        }
+      }
+      __syncthreads();
+      for (int q = tid; q < nb; q += kFinishThreads)
+        if (s_hist[q]) atomicAdd(&gh[q], s_hist[q]);
+      if (!finish_barrier(a.bar, a.error, a.spin_limit)) return;
+    }
     // the pick: nb / kFinishThreads bins per thread, scanned; the thread
     // holding rank k narrows the prefix
     const int per = nb / kFinishThreads;
@@ -362,6 +372,17 @@ __global__ void __launch_bounds__(kFinishThreads) rn_finish_kernel(const RnFinis
       c[u] = valid ? __ldcg(&a.sup_c[q]) : rn;
       id[u] = valid ? __ldcg(&a.sup_idx[q]) : 0u;
     }
+    // the optimal times of the batch's edges, loaded together
+    float t[kFinishBatch];
+    int ii[kFinishBatch], jj[kFinishBatch];
+#pragma unroll
+    for (int u = 0; u < kFinishBatch; ++u) {
+      const long long q = b0 + u * 32 + lane;
+      const uint32_t i = id[u] / (uint32_t)(a.N - 1), r = id[u] - i * (uint32_t)(a.N - 1);
+      ii[u] = (int)i;
+      jj[u] = (int)r + (r >= i ? 1 : 0);
+      t[u] = q < w1 && c[u] < rn ? a.tsup.at(q, id[u], ii[u], jj[u]) : 0.0f;
+    }
 #pragma unroll
     for (int u = 0; u < kFinishBatch; ++u) {
       const long long q = b0 + u * 32 + lane;
@@ -369,12 +390,10 @@ __global__ void __launch_bounds__(kFinishThreads) rn_finish_kernel(const RnFinis
       const unsigned int bal = __ballot_sync(0xffffffffu, f);
       const unsigned long long pos = run + __popc(bal & lt);
       if (f && (long long)pos < a.max_edges) {
-        const uint32_t i = id[u] / (uint32_t)(a.N - 1), r = id[u] - i * (uint32_t)(a.N - 1);
-        const int j = (int)r + (r >= i ? 1 : 0);
-        a.e_src[pos] = (int)i;
-        a.e_dst[pos] = j;
+        a.e_src[pos] = ii[u];
+        a.e_dst[pos] = jj[u];
         a.e_copt[pos] = c[u];
-        a.e_topt[pos] = a.tsup.at(q, id[u], (int)i, j);
+        a.e_topt[pos] = t[u];
       }
       run += __popc(bal);
     }

@@ -307,12 +307,7 @@ struct EdgeLoader {
 };
 
 // The optimal time of superset entry q (pair number id, pair (a, j)) for
-// the edge list: from the superset's own time column, or from the pair
-// arrays.
-struct SupToptColumn {
-  const float *t;
-  __device__ float at(long long q, uint32_t, int, int) const { return __ldcg(&t[q]); }
-};
+// the edge list, from the pair arrays.
 template <class Topt>
 struct SupToptPairs {
   Topt tsrc;
@@ -422,7 +417,7 @@ bool rn_plan(long long n, long long k, RnPlan *pl) {
 // finishing kernel's barrier words and error word, then its three select
 // histograms; after it the finishing kernel's
 // per-block partial sums, the bracket sample's keys and the superset (pair
-// numbers, costs, times).
+// numbers, costs).
 constexpr int kMaxFinishBlocks = 1024;
 struct RnScratch {
   unsigned long long *key_hi;
@@ -434,7 +429,7 @@ struct RnScratch {
   unsigned long long *partial;
   uint32_t *sample_keys;
   uint32_t *sup_idx;
-  float *sup_c, *sup_t;
+  float *sup_c;
 };
 pump_status_t rn_scratch(Ctx *ctx, long long cap, cudaStream_t stream, RnScratch *rs) {
   char *buf = nullptr;
@@ -442,7 +437,7 @@ pump_status_t rn_scratch(Ctx *ctx, long long cap, cudaStream_t stream, RnScratch
   constexpr size_t kZeroed = kWords + 3 * 2048 * sizeof(unsigned int);
   const size_t head = kZeroed + 2 * kMaxFinishBlocks * sizeof(unsigned long long) +
                       sizeof(uint32_t) * kBracketSamples;
-  PUMP_TRY(ctx->scratch(Ctx::kSuperset, head + (size_t)cap * 12, (void **)&buf));
+  PUMP_TRY(ctx->scratch(Ctx::kSuperset, head + (size_t)cap * 8, (void **)&buf));
   static_assert(sizeof(RnEdgesPack) <= 32, "pack fits its slot");
   rs->key_hi = (unsigned long long *)buf;
   rs->pack = (RnEdgesPack *)(buf + 16);
@@ -455,7 +450,6 @@ pump_status_t rn_scratch(Ctx *ctx, long long cap, cudaStream_t stream, RnScratch
   rs->sample_keys = (uint32_t *)(rs->partial + 2 * kMaxFinishBlocks);
   rs->sup_idx = (uint32_t *)(buf + head);
   rs->sup_c = (float *)(rs->sup_idx + cap);
-  rs->sup_t = rs->sup_c + cap;
   PUMP_CUDA_TRY(cudaMemsetAsync(buf, 0, kZeroed, stream));
   return PUMP_OK;
 }
@@ -478,9 +472,9 @@ pump_status_t rn_finish_launch(const RnFinish<TSup> &a, cudaStream_t stream) {
   return PUMP_OK;
 }
 
-// After the pair pass (the superset as per-warp masks over the pair arrays
-// d_copts/d_topts, or contiguous in rs.sup_* with its size in *n_in): the
-// finishing kernel (select over the
+// After the pair pass (the superset as per-warp masks over the pair costs
+// d_copts, or contiguous in rs.sup_idx / rs.sup_c with its size in *n_in):
+// the finishing kernel (select over the
 // superset for rank k, the edges below rn, the row starts, the pack).
 // Then either the deferred pack pointer, or one read-back: rn and the edge
 // count, PUMP_ERR_TIMEOUT when a wait gave up, or the fallback when the
@@ -488,7 +482,7 @@ pump_status_t rn_finish_launch(const RnFinish<TSup> &a, cudaStream_t stream) {
 // wait-bound error word (or null).
 template <class TSup, class Fallback>
 pump_status_t rn_edges_tail(const RnScratch &rs, const PairStage *stage, const float *d_copts,
-                            const float *d_topts, const unsigned long long *n_in, TSup tsup,
+                            const unsigned long long *n_in, TSup tsup,
                             const int *err_pass, int N,
                             long long k, long long cap, long long max_edges, int *d_src,
                             int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
@@ -500,12 +494,10 @@ pump_status_t rn_edges_tail(const RnScratch &rs, const PairStage *stage, const f
     a.nmasks = stage->nmasks;
     a.masks_per_row = stage->masks_per_row;
     a.copts = d_copts;
-    a.topts = d_topts;
   }
   a.n_in = n_in;
   a.sup_idx = rs.sup_idx;
   a.sup_c = rs.sup_c;
-  a.sup_t = rs.sup_t;
   a.tsup = tsup;
   a.cap = cap;
   a.k = k;
@@ -560,7 +552,7 @@ pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, lon
                              SupersetLoader<Src>{src, N, rs.key_hi, pl.cap, rs.sup_idx,
                                                  (uint32_t *)rs.sup_c},
                              stream, &ts, nullptr, rs.n_sup));
-  return rn_edges_tail(rs, nullptr, nullptr, nullptr, rs.n_sup, SupToptPairs<Topt>{tsrc}, nullptr,
+  return rn_edges_tail(rs, nullptr, nullptr, rs.n_sup, SupToptPairs<Topt>{tsrc}, nullptr,
                        N, k, pl.cap,
                        max_edges, d_src, d_dst, d_copt, d_topt, d_go_start, h_rn, h_num_edges,
                        stream, fallback, deferred);
@@ -691,7 +683,7 @@ pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float
     return rn_edges_fallback_device(ctx, d_copts, d_topts, N, k, max_edges, d_src, d_dst, d_copt,
                                     d_topt, d_go_start, h_rn, h_num_edges, stream);
   };
-  return finish(rn_edges_tail(rs, &stage, d_copts, d_topts, nullptr, SupToptColumn{rs.sup_t},
+  return finish(rn_edges_tail(rs, &stage, d_copts, nullptr, SupToptPairs<FlatTopt>{FlatTopt{d_topts}},
                               nullptr, N, k, pl.cap,
                               max_edges, d_src, d_dst, d_copt, d_topt, d_go_start, h_rn,
                               h_num_edges, stream, fallback, deferred));
