@@ -218,15 +218,23 @@ def measure_queries(args, lib, L, ctx, mode):
     for k in range(len(qs)):
         sts[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res[k]), None)
     L.pump_plan_batch(0, pbs, res, sts, len(qs), workers)
+    # each form timed three times (the median is reported: a batch of 256
+    # queries takes under 0.1 s, and single runs vary by several percent)
     res_p, sts_p = results("plain"), (C.c_int * len(qs))()
-    t0 = time.perf_counter()
-    for k in range(len(qs)):
-        sts_p[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res_p[k]), None)
-    t_plain = time.perf_counter() - t0
+    tp = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        for k in range(len(qs)):
+            sts_p[k] = L.pump_plan(ctx.handle, C.byref(pbs[k]), C.byref(res_p[k]), None)
+        tp.append(time.perf_counter() - t0)
+    t_plain = statistics.median(tp)
     res_b, sts_b = results("batched"), (C.c_int * len(qs))()
-    t0 = time.perf_counter()
-    lib.check(L.pump_plan_batch(0, pbs, res_b, sts_b, len(qs), workers))
-    t_batch = time.perf_counter() - t0
+    tb = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        lib.check(L.pump_plan_batch(0, pbs, res_b, sts_b, len(qs), workers))
+        tb.append(time.perf_counter() - t0)
+    t_batch = statistics.median(tb)
     # identical results: status, solution index, CP and cost bits, and the
     # returned path's states bit for bit
     f32 = lambda x: np.float32(x).view(np.uint32)  # noqa: E731
@@ -243,7 +251,8 @@ def measure_queries(args, lib, L, ctx, mode):
             "bvp": mode, "queries": len(qs), "met_cp_target": ok_b, "workers": workers,
             "plain_queries_per_s": ok_p / t_plain, "batched_queries_per_s": ok_b / t_batch,
             "batched_over_plain": (ok_b / t_batch) / (ok_p / t_plain) if ok_p else None,
-            "plain_s": t_plain, "batched_s": t_batch, "identical_results": bool(same)}
+            "plain_s": t_plain, "batched_s": t_batch, "plain_s_runs": tp, "batched_s_runs": tb,
+            "identical_results": bool(same)}
 
 
 def measure_refine(args, lib, L, ctx, torch):

@@ -77,7 +77,7 @@ class Ctx {
   // shape class, reused by every query on this context, and the stream they
   // are captured on.
   struct LoopGraph {
-    int lazy, mode, obs_cap, num_disc;
+    int lazy, mode, obs_cap, num_disc, max_hs, particles;
     long long scan_cap, store_cap;
     void *base;
     cudaGraphExec_t exec;
@@ -139,12 +139,15 @@ struct RnEdgesPack {
 // pair costs, from the query's own pair arrays or its pair view.  With
 // `deferred`, nothing is read back: *h_num_edges is -1, *deferred points at
 // the device pack (read it after a synchronisation) and the row starts are
-// already built from the device count.
+// already built from the device count.  After the superset pass the rest
+// runs as one cooperative launch (`cooperative`, the lower latency for a
+// query that has the GPU to itself) or as separate launches that share the
+// GPU with concurrent queries (always for a pair view: batch workers).
 pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_topts, int N,
                               long long k, long long max_edges, int *d_src, int *d_dst,
                               float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
                               long long *h_num_edges, cudaStream_t stream,
-                              const RnEdgesPack **deferred = nullptr);
+                              const RnEdgesPack **deferred = nullptr, bool cooperative = true);
 pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long long max_edges,
                              int *d_src, int *d_dst, float *d_copt, float *d_topt,
                              int *d_go_start, float *h_rn, long long *h_num_edges,
@@ -170,13 +173,15 @@ pump_status_t rn_edges_fallback_pairs(Ctx *ctx, const PairView &pv, long long k,
 // sample's costs are computed first), so the costs are not read again.
 // stage_ms (optional, non-deferred only; 3 floats): CUDA-event times of what
 // precedes the pair kernel (the samples' preparation and the bracket), the
-// pair kernel, and the rest.
+// pair kernel, and the rest.  cooperative = false: the pair kernel without
+// the superset masks and the separate-launch tail (for concurrent queries).
 pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float tmax,
                                   int bvp_mode, long long k, long long max_edges, float *d_copts,
                                   float *d_topts, int *d_src, int *d_dst, float *d_copt,
                                   float *d_topt, int *d_go_start, float *h_rn,
                                   long long *h_num_edges, cudaStream_t stream,
-                                  const RnEdgesPack **deferred = nullptr, float *stage_ms = nullptr);
+                                  const RnEdgesPack **deferred = nullptr, float *stage_ms = nullptr,
+                                  bool cooperative = true);
 pump_status_t frontier_compact_device(Ctx *ctx, const uint8_t *d_flags, int N, int *d_active,
                                       int *d_count, int **d_error_out, cudaStream_t stream);
 pump_status_t particle_rowmax_async(const float *d_table, int P, int T, float *d_rowmax,

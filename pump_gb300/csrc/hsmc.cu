@@ -205,8 +205,10 @@ __global__ void position_variance_kernel(int T, double *__restrict__ var) {
 // wavefront propagates along get half-spaces, and no cache is written.
 constexpr int kMaxHsmcWords = 128;   // P <= 4096 particles
 constexpr int kMaxHsSlots = 256;     // W * maxHS <= 256
-constexpr int kHsmcThreads = 256;
+constexpr int kHsmcThreads = 128;
 constexpr int kHsmcWarps = kHsmcThreads / 32;
+// blocks of a launch that loops over a device-side path count
+constexpr int kHsmcPersistBlocks = kNumSMs * 8;
 constexpr int kHsmcFilterObs = 128;
 
 
@@ -216,9 +218,14 @@ constexpr int kHsmcFilterObs = 128;
 __host__ __device__ inline size_t hsmc_boxes_obs_floats(int numObs) {
   return (size_t)((numObs * 12 + 3) & ~3);
 }
-__host__ __device__ inline size_t hsmc_boxes_smem(int numObs) {
+// Per warp: W * maxHS half-space slots and W stored counts (rounded to 16
+// bytes), sized for the launch's W and maxHS.
+__host__ __device__ inline int hsmc_hs_stride(int W, int maxHS) { return W * maxHS; }
+__host__ __device__ inline int hsmc_cnt_stride(int W) { return (W + 15) & ~15; }
+__host__ __device__ inline size_t hsmc_boxes_smem(int numObs, int W, int maxHS) {
   return sizeof(float) * hsmc_boxes_obs_floats(numObs) +
-         (size_t)kHsmcWarps * (sizeof(float4) * kMaxHsSlots + kMaxHsSlots + sizeof(int) * kHsmcFilterObs);
+         (size_t)kHsmcWarps * (sizeof(float4) * hsmc_hs_stride(W, maxHS) + hsmc_cnt_stride(W) +
+                               sizeof(int) * kHsmcFilterObs);
 }
 
 // New path w (the whole warp).  valid_in[prev] is read, valid_out[w] /
@@ -227,7 +234,7 @@ __host__ __device__ inline size_t hsmc_boxes_smem(int numObs) {
 // waypoint), slots at or past a waypoint's count are inactive without
 // reading them (they hold the defaults b = 1111 in the dense layout); stored
 // slots still need b < 1000.
-template <bool Boxes>
+template <bool Boxes, int Q>
 __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const float *s_obs,
                                           float4 *hs, uint8_t *hcnt, int *klist) {
   const int lane = threadIdx.x & 31;
@@ -255,9 +262,9 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
   const long long hsHead = (long long)edge * slots;
   // parent's words: lane j holds words j, j+32, ... (issued first: their
   // latency overlaps the half-space work)
-  uint32_t mine[kMaxHsmcWords / 32];
+  uint32_t mine[Q];
 #pragma unroll
-  for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+  for (int q = 0; q < Q; ++q) {
     const int j = q * 32 + lane;
     mine[q] = (j < words) ? p.valid_in[(long long)prev * words + j] : 0u;
   }
@@ -362,9 +369,9 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
   int overflow = 0;
   if (nact > 0) {
     // unpack: bits[q] bit b = particle 32 * (32 q + b) + lane
-    uint32_t bits[kMaxHsmcWords / 32];
+    uint32_t bits[Q];
 #pragma unroll
-    for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+    for (int q = 0; q < Q; ++q) {
       bits[q] = 0u;
       for (int b = 0; b < 32; ++b) {
         const int k = q * 32 + b;
@@ -403,7 +410,7 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
         }
         const float *row = p.offsets_t + (long long)dtIdx * p.Pmc * 3;
 #pragma unroll
-        for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+        for (int q = 0; q < Q; ++q) {
           if (q * 32 >= words) break;
           uint32_t bq = bits[q];
           if (bq == 0u) continue;  // this lane's particles of the group are all dead
@@ -428,7 +435,7 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
     }
     // repack: word k = ballot of bit k over lanes; lane (k & 31) keeps it
 #pragma unroll
-    for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+    for (int q = 0; q < Q; ++q) {
       uint32_t keep = 0u;
       for (int b = 0; b < 32; ++b) {
         const int k = q * 32 + b;
@@ -443,7 +450,7 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
   int valid_count = 0;
   const uint32_t tail = (P & 31) ? ((1u << (P & 31)) - 1u) : 0xffffffffu;
 #pragma unroll
-  for (int q = 0; q < kMaxHsmcWords / 32; ++q) {
+  for (int q = 0; q < Q; ++q) {
     const int j = q * 32 + lane;
     if (j < words) {
       if (j == words - 1) mine[q] &= tail;  // no bits past particle P-1
@@ -470,7 +477,7 @@ __device__ __forceinline__ void hsmc_path(const HsmcParams &p, int w, const floa
   }
 }
 
-template <bool Boxes>
+template <bool Boxes, int Q>
 __device__ __forceinline__ void hsmc_run(const HsmcParams &p) {
   extern __shared__ float4 s_dyn4[];
   const int warp = threadIdx.x >> 5;
@@ -484,32 +491,56 @@ __device__ __forceinline__ void hsmc_run(const HsmcParams &p) {
   int *klist = nullptr;
   if (Boxes) {
     stage_obstacles(p.obs, p.numObs, s_obs);  // block-wide, before any warp leaves
+    const int hs_stride = hsmc_hs_stride(p.W, p.maxHS), cnt_stride = hsmc_cnt_stride(p.W);
     float4 *s_hs = reinterpret_cast<float4 *>(s_obs + hsmc_boxes_obs_floats(p.numObs));
-    hs = s_hs + warp * kMaxHsSlots;
-    uint8_t *s_cnt = reinterpret_cast<uint8_t *>(s_hs + kHsmcWarps * kMaxHsSlots);
-    hcnt = s_cnt + warp * kMaxHsSlots;
-    int *s_klist = reinterpret_cast<int *>(s_cnt + kHsmcWarps * kMaxHsSlots);
+    hs = s_hs + warp * hs_stride;
+    uint8_t *s_cnt = reinterpret_cast<uint8_t *>(s_hs + kHsmcWarps * hs_stride);
+    hcnt = s_cnt + warp * cnt_stride;
+    int *s_klist = reinterpret_cast<int *>(s_cnt + kHsmcWarps * cnt_stride);
     klist = s_klist + warp * kHsmcFilterObs;
   }
   const int warps = (int)((gridDim.x * (long long)blockDim.x) >> 5);
   for (int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); w < n; w += warps) {
-    hsmc_path<Boxes>(p, w, s_obs, hs, hcnt, klist);
+    hsmc_path<Boxes, Q>(p, w, s_obs, hs, hcnt, klist);
     __syncwarp();  // the warp's half-space slots are rewritten by its next path
   }
 }
 
-template <bool Boxes>
-__global__ void __launch_bounds__(kHsmcThreads, 4) hsmc_kernel(const HsmcParams p) {
-  hsmc_run<Boxes>(p);
+// Q = 32-bit particle words per lane: P <= 1024 Q.
+template <bool Boxes, int Q>
+__global__ void __launch_bounds__(kHsmcThreads, 8) hsmc_kernel(const HsmcParams p) {
+  hsmc_run<Boxes, Q>(p);
 }
 
 // The search loop on the device: the parameters from device memory, the
 // stored-path count (the bound on parents) from the loop state.
-__global__ void __launch_bounds__(kHsmcThreads, 4) hsmc_loop_kernel(const HsmcParams *hp,
+template <int Q>
+__global__ void __launch_bounds__(kHsmcThreads, 8) hsmc_loop_kernel(const HsmcParams *hp,
                                                                     const LoopState *L) {
   HsmcParams p = *hp;
   p.num_prev = L->num_paths;
-  hsmc_run<true>(p);
+  hsmc_run<true, Q>(p);
+}
+
+// The kernel of P particles (Q = ceil(P / 1024), 1, 2 or 4).
+inline int hsmc_q(int P) {
+  const int q = (P + 1023) / 1024;
+  return q <= 1 ? 1 : (q <= 2 ? 2 : 4);
+}
+template <bool Boxes>
+const void *hsmc_kernel_for(int P) {
+  switch (hsmc_q(P)) {
+    case 1: return (const void *)hsmc_kernel<Boxes, 1>;
+    case 2: return (const void *)hsmc_kernel<Boxes, 2>;
+    default: return (const void *)hsmc_kernel<Boxes, 4>;
+  }
+}
+inline const void *hsmc_loop_kernel_for(int P) {
+  switch (hsmc_q(P)) {
+    case 1: return (const void *)hsmc_loop_kernel<1>;
+    case 2: return (const void *)hsmc_loop_kernel<2>;
+    default: return (const void *)hsmc_loop_kernel<4>;
+  }
 }
 
 // -------------------------------------------------------------- MC CP
@@ -744,15 +775,17 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
   hp.skip_dev = d_skip;
   // with a device-side count, num_new bounds it
   const long long want = ((long long)num_new * 32 + kHsmcThreads - 1) / kHsmcThreads;
-  const unsigned blocks = d_num_new ? (unsigned)(want < kNumSMs * 4 ? want : kNumSMs * 4)
+  const unsigned blocks = d_num_new ? (unsigned)(want < kHsmcPersistBlocks ? want : kHsmcPersistBlocks)
                                     : grid_for((long long)num_new * 32, kHsmcThreads);
-  hsmc_kernel<false><<<blocks, kHsmcThreads, 0, stream>>>(hp);
+  void *args[] = {(void *)&hp};
+  PUMP_CUDA_TRY(cudaLaunchKernel(hsmc_kernel_for<false>(P), dim3(blocks), dim3(kHsmcThreads), args,
+                                 0, stream));
   return launch_status("hsmc_kernel");
 }
 
 bool hsmc_boxes_fits(int numObs, int W, int maxHS) {
   return numObs >= 0 && W <= kMaxHsSlots && W * maxHS <= kMaxHsSlots &&
-         hsmc_boxes_smem(numObs) <= 220 * 1024;
+         hsmc_boxes_smem(numObs, W, maxHS) <= 220 * 1024;
 }
 
 pump_status_t hsmc_boxes_fill(int num_new, int W, const int *d_edge, const int *d_prev,
@@ -819,23 +852,27 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
                            maxd2, maxHS, d_times, d_topt, dt, d_offsets_t, Pmc, T_rows, offset_mult,
                            d_valid_in, d_valid_out, P, d_cp_out, d_error, d_num_new, d_skip, epi,
                            &hp, d_disc_off));
-  const size_t smem = hsmc_boxes_smem(numObs);
-  PUMP_TRY(smem_attr((const void *)hsmc_kernel<true>, smem));
+  const size_t smem = hsmc_boxes_smem(numObs, W, maxHS);
+  const void *kern = hsmc_kernel_for<true>(P);
+  PUMP_TRY(smem_attr(kern, smem));
   // with a device-side count, num_new bounds it
   const long long want = ((long long)num_new * 32 + kHsmcThreads - 1) / kHsmcThreads;
-  const unsigned blocks = d_num_new ? (unsigned)(want < kNumSMs * 4 ? want : kNumSMs * 4)
+  const unsigned blocks = d_num_new ? (unsigned)(want < kHsmcPersistBlocks ? want : kHsmcPersistBlocks)
                                     : grid_for((long long)num_new * 32, kHsmcThreads);
-  hsmc_kernel<true><<<blocks, kHsmcThreads, smem, stream>>>(hp);
+  void *args[] = {(void *)&hp};
+  PUMP_CUDA_TRY(cudaLaunchKernel(kern, dim3(blocks), dim3(kHsmcThreads), args, smem, stream));
   return launch_status("hsmc_kernel (boxes)");
 }
 
-pump_status_t hsmc_loop_prepare(int numObs) {
-  return smem_attr((const void *)hsmc_loop_kernel, hsmc_boxes_smem(numObs));
+pump_status_t hsmc_loop_prepare(int numObs, int W, int maxHS, int P) {
+  return smem_attr(hsmc_loop_kernel_for(P), hsmc_boxes_smem(numObs, W, maxHS));
 }
 
-pump_status_t hsmc_loop_launch(const HsmcParams *d_hp, const LoopState *d_L, int numObs,
-                               int blocks, cudaStream_t stream) {
-  hsmc_loop_kernel<<<blocks, kHsmcThreads, hsmc_boxes_smem(numObs), stream>>>(d_hp, d_L);
+pump_status_t hsmc_loop_launch(const HsmcParams *d_hp, const LoopState *d_L, int numObs, int W,
+                               int maxHS, int P, int blocks, cudaStream_t stream) {
+  void *args[] = {(void *)&d_hp, (void *)&d_L};
+  PUMP_CUDA_TRY(cudaLaunchKernel(hsmc_loop_kernel_for(P), dim3(blocks), dim3(kHsmcThreads), args,
+                                 hsmc_boxes_smem(numObs, W, maxHS), stream));
   return launch_status("hsmc_loop_kernel");
 }
 

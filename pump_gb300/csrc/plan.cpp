@@ -452,9 +452,11 @@ pump_status_t Planner::roadmap() {
   } else {
     PUMP_TRY(d_copts_.alloc(npairs));
     PUMP_TRY(d_topts_.alloc(npairs));
+    // a batch worker (shared pairs or the lazy throughput form) shares the
+    // GPU with the others: no cooperative launch
     PUMP_TRY(roadmap_pairs_edges(ctx_, d_samples_.p, N_, 5.0f, pb_.bvp_mode, rnIdx, cap, d_copts_.p,
                                  d_topts_.p, d_src_.p, d_dst_.p, d_coptE_.p, d_toptE_.p, d_go_.p,
-                                 &rn_, &E_, s_, &d_pack_));
+                                 &rn_, &E_, s_, &d_pack_, nullptr, shared_ == nullptr && !lazy_));
   }
   // the edges' waypoints (findDiscretizedPath) are written by the edge
   // checks; with the edge count still on the device, sized for the capacity
@@ -935,14 +937,17 @@ pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
   cudaGraphExec_t exec = nullptr;
   for (const Ctx::LoopGraph &g : gs)
     if (g.lazy == lazy && g.mode == mode && g.obs_cap == obs_cap && g.num_disc == num_disc &&
-        g.scan_cap == scan_cap && g.store_cap == store_cap)
+        g.max_hs == maxHS_ && g.particles == pb_.num_hsmc && g.scan_cap == scan_cap &&
+        g.store_cap == store_cap)
       exec = g.exec;
   if (!exec) {
     if (!ctx_->capture_stream)
       PUMP_CUDA_TRY(cudaStreamCreateWithFlags(&ctx_->capture_stream, cudaStreamNonBlocking));
     PUMP_TRY(search_loop_graph(reinterpret_cast<LoopArgs *>(base), lazy_, mode, obs_cap, num_disc,
-                               la->scan, la->store, ctx_->capture_stream, &exec));
-    gs.push_back({lazy, mode, obs_cap, num_disc, scan_cap, store_cap, base, exec});
+                               maxHS_, pb_.num_hsmc, la->scan, la->store, ctx_->capture_stream,
+                               &exec));
+    gs.push_back({lazy, mode, obs_cap, num_disc, maxHS_, pb_.num_hsmc, scan_cap, store_cap, base,
+                  exec});
   }
   PUMP_CUDA_TRY(cudaGraphLaunch(exec, s_));
   LoopState *hl = nullptr;

@@ -900,7 +900,7 @@ pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int 
 }
 
 pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numObs, int numDisc,
-                                const LoopTiles &scan, const LoopTiles &store,
+                                int maxHS, int P, const LoopTiles &scan, const LoopTiles &store,
                                 cudaStream_t capture_stream, cudaGraphExec_t *out) {
   *out = nullptr;
   const size_t chk_smem = check_smem(numObs, numDisc, false);
@@ -910,7 +910,7 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
   const void *chk = mode == PUMP_BVP_PARITY ? (const void *)check_loop_kernel<PUMP_BVP_PARITY>
                                             : (const void *)check_loop_kernel<PUMP_BVP_PRECISION>;
   if (lazy) PUMP_TRY(smem_attr(chk, chk_smem));
-  PUMP_TRY(hsmc_loop_prepare(numObs));
+  PUMP_TRY(hsmc_loop_prepare(numObs, numDisc + 1, maxHS, P));
   cudaGraph_t g = nullptr;
   PUMP_CUDA_TRY(cudaGraphCreate(&g, 0));
   // the while node's condition starts at 0 and is set by the arm kernel
@@ -962,7 +962,8 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
           check_loop_kernel<PUMP_BVP_PRECISION><<<g_check, kChkThreads, chk_smem, cs>>>(d_args);
       }
       expand_loop_kernel<<<kNumSMs * 2, kExpThreads, 0, cs>>>(d_args);
-      hsmc_loop_launch(&d_args->hp, &d_args->L, numObs, g_wide, cs);
+      // HSMC's blocks are half as wide (4 warps): twice as many per SM
+      hsmc_loop_launch(&d_args->hp, &d_args->L, numObs, numDisc + 1, maxHS, P, 2 * g_wide, cs);
       store_loop_kernel<<<g_wide, kCompactThreads, 0, cs>>>(d_args, h);
       cudaGraph_t captured = nullptr;
       const pump_status_t ce = cuda_status(cudaStreamEndCapture(cs, &captured), "cudaStreamEndCapture");

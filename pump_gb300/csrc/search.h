@@ -236,13 +236,13 @@ pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int 
 // numDisc waypoints per edge.  Kernel attributes are set here, before the
 // capture.
 pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numObs, int numDisc,
-                                const LoopTiles &scan, const LoopTiles &store,
+                                int maxHS, int P, const LoopTiles &scan, const LoopTiles &store,
                                 cudaStream_t capture_stream, cudaGraphExec_t *out);
 
 // HSMC in the loop graph (hsmc.cu).
-pump_status_t hsmc_loop_prepare(int numObs);
-pump_status_t hsmc_loop_launch(const HsmcParams *d_hp, const LoopState *d_L, int numObs,
-                               int blocks, cudaStream_t stream);
+pump_status_t hsmc_loop_prepare(int numObs, int W, int maxHS, int P);
+pump_status_t hsmc_loop_launch(const HsmcParams *d_hp, const LoopState *d_L, int numObs, int W,
+                               int maxHS, int P, int blocks, cudaStream_t stream);
 pump_status_t hsmc_boxes_fill(int num_new, int W, const int *d_edge, const int *d_prev,
                               long long num_edges, int num_prev, const float *d_obs, int numObs,
                               const float *d_disc, float maxd2, int maxHS, const float *d_times,

@@ -306,6 +306,48 @@ struct EdgeLoader {
   }
 };
 
+// rn's bits, whether the superset held rank k within its buffer, the edge
+// count and the compaction's wait-bound error word, for one read-back (the
+// tail of the one-read pass that runs as separate launches).
+__global__ void rn_pack_kernel(const float *rn, const unsigned long long *n_sup,
+                               const unsigned long long *edges, long long k, long long cap,
+                               const int *err, RnEdgesPack *out) {
+  const unsigned long long ns = *n_sup;
+  out->rn_bits = *reinterpret_cast<const unsigned int *>(rn);
+  out->ok = (long long)ns > k && (long long)ns <= cap;
+  out->edges = *edges;
+  out->error = *err != 0;
+  out->pad = 0;
+}
+
+// Edges from the superset (one-pass compaction): entries with cost < rn, in
+// superset (= pair) order; rn is read on the device (the select's result).
+struct SupBelowRn {
+  const float *sc;
+  const float *rn;
+  __device__ bool operator()(long long q) const { return __ldg(&sc[q]) < *rn; }
+};
+template <class TSup>
+struct SupEdgeEmit {
+  const uint32_t *idx;
+  const float *sc;
+  TSup tsup;
+  int N;
+  long long cap;
+  int *e_src, *e_dst;
+  float *e_copt, *e_topt;
+  __device__ void operator()(long long q, long long pos) const {
+    if (pos >= cap) return;
+    const uint32_t id = __ldg(&idx[q]);
+    const uint32_t a = id / (uint32_t)(N - 1), b = id - a * (uint32_t)(N - 1);
+    const int j = (int)b + (b >= a ? 1 : 0);
+    e_src[pos] = (int)a;
+    e_dst[pos] = j;
+    e_copt[pos] = __ldg(&sc[q]);
+    e_topt[pos] = tsup.at(q, id, (int)a, j);
+  }
+};
+
 // The optimal time of superset entry q (pair number id, pair (a, j)) for
 // the edge list, from the pair arrays.
 template <class Topt>
@@ -528,16 +570,50 @@ pump_status_t rn_edges_tail(const RnScratch &rs, const PairStage *stage, const f
   return rn_edges_unpack(pk, k, max_edges, h_rn, h_num_edges, fallback);
 }
 
+// The same after a contiguous superset, as separate launches that each
+// take part of the GPU: the radix select, the one-pass edge compaction, the
+// row starts and the pack.  Queries planned concurrently (batch workers) use
+// this form: the finishing kernel's cooperative launch takes every SM's
+// register file at once, so it would wait for the other workers' kernels to
+// drain.
+template <class TSup, class Fallback>
+pump_status_t rn_edges_tail_streamed(Ctx *ctx, const RnScratch &rs, TSup tsup, int N, long long k,
+                                     long long cap, long long max_edges, int *d_src, int *d_dst,
+                                     float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
+                                     long long *h_num_edges, cudaStream_t stream,
+                                     Fallback fallback, const RnEdgesPack **deferred) {
+  const float *d_rn = nullptr;
+  PUMP_TRY(select_kth_src(ctx, FlatSrc{rs.sup_c}, cap, k, &d_rn, stream, rs.n_sup));
+  TileScratch ts2{};
+  PUMP_TRY(run_compact(ctx, cap, SupBelowRn{rs.sup_c, d_rn},
+                       SupEdgeEmit<TSup>{rs.sup_idx, rs.sup_c, tsup, N, max_edges, d_src, d_dst,
+                                         d_copt, d_topt},
+                       stream, &ts2, rs.n_sup));
+  if (d_go_start) PUMP_TRY(row_starts(d_src, max_edges, N, d_go_start, stream, ts2.total));
+  rn_pack_kernel<<<1, 1, 0, stream>>>(d_rn, rs.n_sup, ts2.total, k, cap, ts2.error, rs.pack);
+  PUMP_TRY(launch_status("rn_pack_kernel"));
+  if (deferred) {
+    *deferred = rs.pack;
+    *h_num_edges = -1;
+    return PUMP_OK;
+  }
+  RnEdgesPack pk{};
+  PUMP_CUDA_TRY(cudaMemcpyAsync(&pk, rs.pack, sizeof pk, cudaMemcpyDeviceToHost, stream));
+  PUMP_CUDA_TRY(cudaStreamSynchronize(stream));
+  return rn_edges_unpack(pk, k, max_edges, h_rn, h_num_edges, fallback);
+}
+
 // rn = the k-th smallest pair cost and the edges below it (same values and
 // order as select_kth + build_edges) from one read of the pair costs: the
-// bracket sample, the superset pass, then rn_edges_tail.  `fallback` runs
-// the three-pass select and the full compaction when the pass does not
-// apply or (after the read-back) the superset missed rank k or overflowed.
+// bracket sample, the superset pass, then rn_edges_tail (cooperative) or
+// rn_edges_tail_streamed.  `fallback` runs the three-pass select and the
+// full compaction when the pass does not apply or (after the read-back) the
+// superset missed rank k or overflowed.
 template <class Src, class Topt, class Fallback>
 pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, long long max_edges,
                            int *d_src, int *d_dst, float *d_copt, float *d_topt, int *d_go_start,
                            float *h_rn, long long *h_num_edges, cudaStream_t stream,
-                           Fallback fallback, const RnEdgesPack **deferred) {
+                           Fallback fallback, const RnEdgesPack **deferred, bool cooperative) {
   if (deferred) *deferred = nullptr;
   const long long n = (long long)N * (N - 1);
   if (k < 0 || k >= n) return set_error(PUMP_ERR_BAD_INPUT, "rn_edges: k=%lld n=%lld", k, n);
@@ -552,6 +628,10 @@ pump_status_t rn_edges_src(Ctx *ctx, Src src, Topt tsrc, int N, long long k, lon
                              SupersetLoader<Src>{src, N, rs.key_hi, pl.cap, rs.sup_idx,
                                                  (uint32_t *)rs.sup_c},
                              stream, &ts, nullptr, rs.n_sup));
+  if (!cooperative)
+    return rn_edges_tail_streamed(ctx, rs, SupToptPairs<Topt>{tsrc}, N, k, pl.cap, max_edges, d_src,
+                                  d_dst, d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream,
+                                  fallback, deferred);
   return rn_edges_tail(rs, nullptr, nullptr, rs.n_sup, SupToptPairs<Topt>{tsrc}, nullptr,
                        N, k, pl.cap,
                        max_edges, d_src, d_dst, d_copt, d_topt, d_go_start, h_rn, h_num_edges,
@@ -602,14 +682,15 @@ pump_status_t rn_edges_device(Ctx *ctx, const float *d_copts, const float *d_top
                               long long k, long long max_edges, int *d_src, int *d_dst,
                               float *d_copt, float *d_topt, int *d_go_start, float *h_rn,
                               long long *h_num_edges, cudaStream_t stream,
-                              const RnEdgesPack **deferred) {
+                              const RnEdgesPack **deferred, bool cooperative) {
   auto fallback = [&]() -> pump_status_t {
     if (deferred) *deferred = nullptr;
     return rn_edges_fallback_device(ctx, d_copts, d_topts, N, k, max_edges, d_src, d_dst, d_copt,
                                     d_topt, d_go_start, h_rn, h_num_edges, stream);
   };
   return rn_edges_src(ctx, FlatSrc{d_copts}, FlatTopt{d_topts}, N, k, max_edges, d_src, d_dst,
-                      d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream, fallback, deferred);
+                      d_copt, d_topt, d_go_start, h_rn, h_num_edges, stream, fallback, deferred,
+                      cooperative);
 }
 
 pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long long max_edges,
@@ -622,7 +703,7 @@ pump_status_t rn_edges_pairs(Ctx *ctx, const PairView &pv, long long k, long lon
                                    d_go_start, h_rn, h_num_edges, stream);
   };
   return rn_edges_src(ctx, PairCoptSrc{pv}, PairTopt{pv}, pv.N, k, max_edges, d_src, d_dst, d_copt,
-                      d_topt, d_go_start, h_rn, h_num_edges, stream, fallback, deferred);
+                      d_topt, d_go_start, h_rn, h_num_edges, stream, fallback, deferred, false);
 }
 
 pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float tmax,
@@ -630,7 +711,8 @@ pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float
                                   float *d_topts, int *d_src, int *d_dst, float *d_copt,
                                   float *d_topt, int *d_go_start, float *h_rn,
                                   long long *h_num_edges, cudaStream_t stream,
-                                  const RnEdgesPack **deferred, float *stage_ms) {
+                                  const RnEdgesPack **deferred, float *stage_ms,
+                                  bool cooperative) {
   if (deferred) *deferred = nullptr;
   if (N < 2) return set_error(PUMP_ERR_BAD_INPUT, "roadmap: N = %d", N);
   const long long n = (long long)N * (N - 1);
@@ -657,12 +739,13 @@ pump_status_t roadmap_pairs_edges(Ctx *ctx, const float *d_samples, int N, float
     return st;
   };
   RnPlan pl;
-  if (bvp_mode != PUMP_BVP_PRECISION || !rn_plan(n, k, &pl) || N > 65535) {
+  if (bvp_mode != PUMP_BVP_PRECISION || !rn_plan(n, k, &pl) || N > 65535 || !cooperative) {
     if (ev[1]) PUMP_CUDA_TRY(cudaEventRecord(ev[1], stream));
     PUMP_TRY(pump_bvp_pairs(d_samples, N, tmax, bvp_mode, d_copts, d_topts, (pump_stream_t)stream));
     if (ev[2]) PUMP_CUDA_TRY(cudaEventRecord(ev[2], stream));
     return finish(rn_edges_device(ctx, d_copts, d_topts, N, k, max_edges, d_src, d_dst, d_copt,
-                                  d_topt, d_go_start, h_rn, h_num_edges, stream, deferred));
+                                  d_topt, d_go_start, h_rn, h_num_edges, stream, deferred,
+                                  cooperative));
   }
   RnScratch rs;
   PUMP_TRY(rn_scratch(ctx, pl.cap, stream, &rs));
