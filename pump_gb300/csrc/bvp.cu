@@ -127,21 +127,171 @@ __device__ __forceinline__ float cost_eval(const PairCoef &c, float tau) {
   return (float)((1.0 / t3) * s);
 }
 
+// ------------------------------------------- the cost off the binary64 pipe
+// cost_eval rounds 25 binary64 additions and about 15 binary64 products, and
+// the GB300 executes binary64 at 1/64 of its binary32 rate, so the parity
+// kernels are bound by that pipe.  cost_fast gets the same binary32 result
+// from binary32 arithmetic in most evaluations: it evaluates the bracket sum
+// V (the same terms; the t^2, t^3 and t^4 coefficients summed per pair) and
+// V / t^3 in float-float arithmetic (Dekker's and Knuth's error-free
+// TwoSum and TwoProduct; double-float addition, multiplication and division
+// as in Bailey's double-double library, with binary32 parts), and bounds the
+// distance of cost_eval's binary64 value from it:
+//   - cost_eval's sum: each of its 25 additions and ~15 products is rounded
+//     once (|error| <= 2^-53 of the partial sum or product; t^3 and t^4 are
+//     themselves rounded products), so its error is at most 2^-52 x 27 x
+//     (|s7| + the sum of the terms' magnitudes) = 2^-47.2 x that sum;
+//   - the float-float evaluation: at most 2^-42 x that sum (about 20
+//     operations, each within 2^-46 of its operands' magnitudes);
+//   - the final 1 / t^3 and the product (three more binary64 roundings) and
+//     the float-float division: at most 2^-42 of the result.
+// When that interval around the float-float value lies inside the binary32
+// rounding cell of its high part (it does not reach the midpoint to either
+// neighbour), cost_eval's (float) conversion gives that high part, which is
+// returned.  Otherwise (and for tau outside [1e-4, 1e4], or a non-finite or
+// subnormal result) the binary64 evaluation runs.  The file is compiled
+// without multiply-add contraction, which the error-free transformations
+// need (TwoProduct calls fmaf explicitly).
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ FF ff_two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+  FF s = ff_two_sum(x.hi, y.hi);
+  const FF t = ff_two_sum(x.lo, y.lo);
+  s.lo = s.lo + t.hi;
+  s = ff_fast_two_sum(s.hi, s.lo);
+  s.lo = s.lo + t.lo;
+  return ff_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ FF ff_add_f(FF x, float b) {
+  FF s = ff_two_sum(x.hi, b);
+  s.lo = s.lo + x.lo;
+  return ff_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ FF ff_mul(FF x, FF y) {
+  FF p = ff_two_prod(x.hi, y.hi);
+  p.lo = p.lo + (x.hi * y.lo + x.lo * y.hi);
+  return ff_fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ FF ff_mul_f(FF x, float b) {
+  FF p = ff_two_prod(x.hi, b);
+  p.lo = p.lo + x.lo * b;
+  return ff_fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ FF ff_div(FF x, FF y) {
+  const float q1 = __fdiv_rn(x.hi, y.hi);
+  const FF qy = ff_mul_f(y, q1);
+  const FF r = ff_add(x, {-qy.hi, -qy.lo});
+  const float q2 = __fdiv_rn(r.hi, y.hi);
+  return ff_fast_two_sum(q1, q2);
+}
+
+// Per-pair float-float data of cost_fast: s7 (cost_eval's binary64 value,
+// split), the sums of the t^2 and t^3 coefficients and their magnitudes.
+struct PairFF {
+  FF s7, d2, d3;
+  float abs_d2, abs_d3;
+};
+__device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1, const PairCoef &c) {
+  PairFF f;
+  f.s7.hi = __double2float_rn(c.s7);
+  f.s7.lo = __double2float_rn(c.s7 - (double)f.s7.hi);
+  // 4 x^2 (exact as a TwoProduct scaled by 4) and the float coefficients
+  const float sq[6] = {x0[4], x0[3], x0[5], x1[4], x1[3], x1[5]};
+  FF d = {0.0f, 0.0f};
+  float ad = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    FF t = ff_two_prod(sq[q], sq[q]);
+    t.hi *= 4.0f;
+    t.lo *= 4.0f;
+    d = ff_add(d, t);
+    ad += t.hi;
+  }
+  const float g = PUMP_G;
+  const float fl[3] = {4 * x0[4] * x1[4], 4 * x0[3] * x1[3], 4 * x0[5] * x1[5]};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    d = ff_add_f(d, fl[q]);
+    ad += fabsf(fl[q]);
+  }
+  f.d2 = d;
+  f.abs_d2 = ad;
+  const float f25 = 2 * g * x0[5], f26 = 2 * g * x1[5];
+  f.d3 = ff_two_sum(f25, -f26);
+  f.abs_d3 = fabsf(f25) + fabsf(f26);
+  return f;
+}
+
+__device__ __forceinline__ float cost_fast(const PairCoef &c, const PairFF &f, float tau) {
+  if (!(tau >= 1e-4f && tau <= 1e4f)) return cost_eval(c, tau);
+  // the float terms, as cost_eval rounds them
+  const float k[8] = {c.k8 * tau,    c.k9 * tau,    -(c.k10 * tau), -(c.k11 * tau),
+                      -(c.k12 * tau), -(c.k13 * tau), -(c.k14 * tau), -(c.k15 * tau)};
+  const float a29 = c.a29 * (c.b29 + c.c29 * tau);
+  const float a30 = c.a30 * (c.b30 + c.c30 * tau);
+  FF v = f.s7;
+  float mag = fabsf(f.s7.hi);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    v = ff_add_f(v, k[q]);
+    mag += fabsf(k[q]);
+  }
+  const FF t2 = ff_two_prod(tau, tau);
+  const FF t3 = ff_mul_f(t2, tau);
+  const FF t4 = ff_mul(t2, t2);
+  // 1 + g^2, the t^4 coefficient (g^2 exact as a TwoProduct)
+  const float g = PUMP_G;
+  const FF g2 = ff_two_prod(g, g);
+  const FF d4 = ff_add_f(g2, 1.0f);
+  v = ff_add(v, ff_mul(f.d2, t2));
+  v = ff_add(v, ff_mul(f.d3, t3));
+  v = ff_add(v, ff_mul(d4, t4));
+  v = ff_add_f(v, a29);
+  v = ff_add_f(v, a30);
+  mag += f.abs_d2 * t2.hi + f.abs_d3 * t3.hi + d4.hi * t4.hi + fabsf(a29) + fabsf(a30);
+  const FF w = ff_div(v, t3);
+  // the bound on |cost_eval's binary64 value - w| (margins for the binary32
+  // evaluation of the bound itself)
+  const float aw = fabsf(w.hi);
+  const float bound = (mag * 1.01f) * 0x1p-42f / t3.hi + aw * 0x1p-42f;
+  const unsigned int u = __float_as_uint(aw);
+  const unsigned int e = u >> 23;
+  if (e < 2u || e > 253u) return cost_eval(c, tau);  // zero, subnormal, huge, inf, NaN
+  const float ulp_up = __uint_as_float(u + 1u) - aw, ulp_dn = aw - __uint_as_float(u - 1u);
+  const float room = 0.5f * fminf(ulp_up, ulp_dn) - fabsf(w.lo);
+  if (!(bound < 0.99f * room)) return cost_eval(c, tau);
+  return w.hi;
+}
+
 // dcost, 2pBVP.cu:109-115
-__device__ __forceinline__ float dcost_eval(const PairCoef &c, float tau) {
+__device__ __forceinline__ float dcost_eval(const PairCoef &c, const PairFF &f, float tau) {
   const float dtau = (float)0.000001;
-  return (cost_eval(c, tau + dtau / 2) - cost_eval(c, tau - dtau / 2)) / dtau;
+  return (cost_fast(c, f, tau + dtau / 2) - cost_fast(c, f, tau - dtau / 2)) / dtau;
 }
 
 // toptBisection, 2pBVP.cu:71-95.  The reference's halving loop (:78-80) is
 // unbounded; here it stops after 160 halvings (tl < 1e-50 has underflowed to
 // zero long before), exactly as the oracle does.
-__device__ float topt_bisection(const PairCoef &c, float tmax) {
+__device__ float topt_bisection(const PairCoef &c, const PairFF &f, float tmax) {
   float tu = tmax;
-  if (dcost_eval(c, tmax) < 0) return tmax;
+  if (dcost_eval(c, f, tmax) < 0) return tmax;
   float tl = (float)0.01;
   int halvings = 0;
-  while (dcost_eval(c, tl) > 0 && halvings < 160) {
+  while (dcost_eval(c, f, tl) > 0 && halvings < 160) {
     tl = tl / 2;
     ++halvings;
   }
@@ -151,13 +301,19 @@ __device__ float topt_bisection(const PairCoef &c, float tmax) {
   while (fabsf(dcval) > kDcvalTol && itr < 50) {
     ++itr;
     topt = (tu + tl) / 2;
-    dcval = dcost_eval(c, topt);
+    dcval = dcost_eval(c, f, topt);
     if (dcval > 0)
       tu = topt;
     else
       tl = topt;
   }
   return topt;
+}
+
+// toptBisection of the pair (x0, x1).
+__device__ __forceinline__ float topt_parity(const float *x0, const float *x1, float tmax) {
+  const PairCoef c = make_coef(x0, x1);
+  return topt_bisection(c, make_pair_ff(x0, x1, c), tmax);
 }
 
 // --------------------------------------------------------------- kernels
@@ -190,6 +346,7 @@ __global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
   int phase = 0, halvings = 0, itr = 0;
   float tu = 0, tl = 0, topt = 0, dcval = 0;
   PairCoef c{};
+  PairFF pf{};
   while (true) {
     // lanes without a pair take the next pairs of the warp's chunk
     const unsigned need = __ballot_sync(0xffffffffu, idx < 0);
@@ -209,6 +366,7 @@ __global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
           x1[d] = __ldg(&samples[j * kDim + d]);
         }
         c = make_coef(x0, x1);
+        pf = make_pair_ff(x0, x1, c);
         phase = 0;
         tu = tmax;
       }
@@ -221,8 +379,8 @@ __global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
     else if (phase == 1) { ta = tl + h; tb = tl - h; }
     else if (phase == 2) { ++itr; topt = (tu + tl) / 2; ta = topt + h; tb = topt - h; }
     else { ta = topt; tb = topt; }
-    const float ca = cost_eval(c, ta);
-    const float cb = cost_eval(c, tb);
+    const float ca = cost_fast(c, pf, ta);
+    const float cb = cost_fast(c, pf, tb);
     if (idx < 0) continue;
     const float d = (ca - cb) / dtau;
     if (phase == 0) {
@@ -255,9 +413,10 @@ __global__ void bvp_batch_kernel(const BvpJobs jb) {
     x1[d] = jb.x1[(jb.x1_same ? 0 : k) * kDim + d];
   }
   const PairCoef c = make_coef(x0, x1);
-  const float tp = topt_bisection(c, jb.tmax[j]);
+  const PairFF f = make_pair_ff(x0, x1, c);
+  const float tp = topt_bisection(c, f, jb.tmax[j]);
   if (jb.topt[j]) jb.topt[j][k] = tp;
-  if (jb.cost[j]) jb.cost[j][k] = cost_eval(c, tp);
+  if (jb.cost[j]) jb.cost[j][k] = cost_fast(c, f, tp);
 }
 
 // One thread per edge: findDiscretizedPath, 2pBVP.cu:53-69.  The edge's end
@@ -298,7 +457,7 @@ __global__ void __launch_bounds__(T) discretize_kernel(
     }
     // the GPU-arithmetic mode's d_topt holds the reference GPU kernel's times;
     // findDiscretizedPath recomputes the time with the host arithmetic
-    const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_bisection(make_coef(x0, x1), 5.0f) : topt;
+    const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_parity(x0, x1, 5.0f) : topt;
     const float dt = tau / numDisc;
     for (int i = 1; i < numDisc; ++i) {
       if (Mode != PUMP_BVP_PRECISION) path_point(dt * i, tau, x0, x1, x);
@@ -468,7 +627,7 @@ __global__ void __launch_bounds__(T) discretize_off_kernel(
       o[numDisc * kDim + d] = x1[d];
     }
     const float topt = toptE[e];
-    const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_bisection(make_coef(x0, x1), 5.0f) : topt;
+    const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_parity(x0, x1, 5.0f) : topt;
     const float dt = tau / numDisc;
     for (int i = 1; i < numDisc; ++i) {
       if (Mode != PUMP_BVP_PRECISION) path_point(dt * i, tau, x0, x1, x);
@@ -675,7 +834,7 @@ __global__ void edge_topts_parity_kernel(const float *__restrict__ samples, cons
     x0[d] = __ldg(&samples[a * kDim + d]);
     x1[d] = __ldg(&samples[b * kDim + d]);
   }
-  topt[e] = topt_bisection(make_coef(x0, x1), 5.0f);
+  topt[e] = topt_parity(x0, x1, 5.0f);
 }
 }  // namespace
 
