@@ -199,14 +199,33 @@ __device__ __forceinline__ FF ff_div(FF x, FF y) {
   return ff_fast_two_sum(q1, q2);
 }
 
-// Per-pair float-float data of cost_fast: s7 (cost_eval's binary64 value,
-// split), the sums of the t^2 and t^3 coefficients and their magnitudes.
+// Per-pair data of cost_ff: the binary32 coefficients of cost_eval's
+// t-linear and last two terms, s7 (cost_eval's binary64 value, split), the
+// sums of the t^2 and t^3 coefficients and their magnitudes.  Without the
+// binary64 coefficients of PairCoef (rebuilt from the two states when an
+// evaluation falls back), a kernel holding a pair needs fewer registers.
 struct PairFF {
+  float k8, k9, k10, k11, k12, k13, k14, k15;
+  float a29, b29, c29, a30, b30, c30;
   FF s7, d2, d3;
   float abs_d2, abs_d3;
 };
 __device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1, const PairCoef &c) {
   PairFF f;
+  f.k8 = c.k8;
+  f.k9 = c.k9;
+  f.k10 = c.k10;
+  f.k11 = c.k11;
+  f.k12 = c.k12;
+  f.k13 = c.k13;
+  f.k14 = c.k14;
+  f.k15 = c.k15;
+  f.a29 = c.a29;
+  f.b29 = c.b29;
+  f.c29 = c.c29;
+  f.a30 = c.a30;
+  f.b30 = c.b30;
+  f.c30 = c.c30;
   f.s7.hi = __double2float_rn(c.s7);
   f.s7.lo = __double2float_rn(c.s7 - (double)f.s7.hi);
   // 4 x^2 (exact as a TwoProduct scaled by 4) and the float coefficients
@@ -236,13 +255,15 @@ __device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1,
   return f;
 }
 
-__device__ __forceinline__ float cost_fast(const PairCoef &c, const PairFF &f, float tau) {
-  if (!(tau >= 1e-4f && tau <= 1e4f)) return cost_eval(c, tau);
+// The certified value, or *ok = false (then cost_eval gives the result).
+__device__ __forceinline__ float cost_ff(const PairFF &f, float tau, bool *ok) {
+  *ok = false;
+  if (!(tau >= 1e-4f && tau <= 1e4f)) return 0.0f;
   // the float terms, as cost_eval rounds them
-  const float k[8] = {c.k8 * tau,    c.k9 * tau,    -(c.k10 * tau), -(c.k11 * tau),
-                      -(c.k12 * tau), -(c.k13 * tau), -(c.k14 * tau), -(c.k15 * tau)};
-  const float a29 = c.a29 * (c.b29 + c.c29 * tau);
-  const float a30 = c.a30 * (c.b30 + c.c30 * tau);
+  const float k[8] = {f.k8 * tau,    f.k9 * tau,    -(f.k10 * tau), -(f.k11 * tau),
+                      -(f.k12 * tau), -(f.k13 * tau), -(f.k14 * tau), -(f.k15 * tau)};
+  const float a29 = f.a29 * (f.b29 + f.c29 * tau);
+  const float a30 = f.a30 * (f.b30 + f.c30 * tau);
   FF v = f.s7;
   float mag = fabsf(f.s7.hi);
 #pragma unroll
@@ -270,11 +291,17 @@ __device__ __forceinline__ float cost_fast(const PairCoef &c, const PairFF &f, f
   const float bound = (mag * 1.01f) * 0x1p-42f / t3.hi + aw * 0x1p-42f;
   const unsigned int u = __float_as_uint(aw);
   const unsigned int e = u >> 23;
-  if (e < 2u || e > 253u) return cost_eval(c, tau);  // zero, subnormal, huge, inf, NaN
+  if (e < 2u || e > 253u) return 0.0f;  // zero, subnormal, huge, inf, NaN
   const float ulp_up = __uint_as_float(u + 1u) - aw, ulp_dn = aw - __uint_as_float(u - 1u);
   const float room = 0.5f * fminf(ulp_up, ulp_dn) - fabsf(w.lo);
-  if (!(bound < 0.99f * room)) return cost_eval(c, tau);
+  *ok = bound < 0.99f * room;
   return w.hi;
+}
+
+__device__ __forceinline__ float cost_fast(const PairCoef &c, const PairFF &f, float tau) {
+  bool ok;
+  const float v = cost_ff(f, tau, &ok);
+  return ok ? v : cost_eval(c, tau);
 }
 
 // dcost, 2pBVP.cu:109-115
@@ -328,9 +355,19 @@ __device__ __forceinline__ float topt_parity(const float *x0, const float *x1, f
 // kParityChunk consecutive pairs (16 per lane on average, so lanes idle only
 // while a chunk's last pairs finish).  Per pair, the evaluated expressions and
 // their order are unchanged.
+//
+// A lane whose evaluation the float-float bound does not certify waits
+// (keeping its state and the certified side of the pair) until
+// kFallbackLanes lanes of its warp wait, or until no lane of the warp can
+// go on: then the waiting lanes run the binary64 evaluation together.  The
+// binary64 instructions cost a warp the same for one lane as for 32, so this
+// spends them on several lanes at once.
+// Launch bounds (128, 6): 80 registers, 6 blocks per SM (9.9 ms at N = 4000,
+// 10.1 with 96 registers and 5 blocks).
 constexpr int kParityChunk = 512;
+constexpr int kFallbackLanes = 8;
 
-__global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
+__global__ void __launch_bounds__(128, 6) bvp_pairs_parity_persistent(
     const float *__restrict__ samples, int N, float tmax, float *__restrict__ copts,
     float *__restrict__ topts) {
   const long long npairs = (long long)N * (N - 1);
@@ -345,8 +382,12 @@ __global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
   long long idx = -1;
   int phase = 0, halvings = 0, itr = 0;
   float tu = 0, tl = 0, topt = 0, dcval = 0;
-  PairCoef c{};
+  float x0[kDim], x1[kDim];
   PairFF pf{};
+  // the step's evaluation points and values; pending: a value waits for the
+  // binary64 evaluation (ok_a / ok_b: that side is certified already)
+  float ta = 0, tb = 0, ca = 0, cb = 0;
+  bool pending = false, ok_a = true, ok_b = true;
   while (true) {
     // lanes without a pair take the next pairs of the warp's chunk
     const unsigned need = __ballot_sync(0xffffffffu, idx < 0);
@@ -359,29 +400,39 @@ __global__ void __launch_bounds__(128) bvp_pairs_parity_persistent(
         const int i = (int)(idx / (N - 1));
         const int r = (int)(idx - (long long)i * (N - 1));
         const int j = r + (r >= i);
-        float x0[kDim], x1[kDim];
 #pragma unroll
         for (int d = 0; d < kDim; ++d) {
           x0[d] = __ldg(&samples[i * kDim + d]);
           x1[d] = __ldg(&samples[j * kDim + d]);
         }
-        c = make_coef(x0, x1);
-        pf = make_pair_ff(x0, x1, c);
+        pf = make_pair_ff(x0, x1, make_coef(x0, x1));
         phase = 0;
         tu = tmax;
       }
       chunk_next += __popc(need) < avail ? __popc(need) : avail;
     }
-    if (__ballot_sync(0xffffffffu, idx >= 0) == 0u) break;  // nothing left
-    // the two evaluation points of this step
-    float ta, tb;
-    if (phase == 0) { ta = tmax + h; tb = tmax - h; }
-    else if (phase == 1) { ta = tl + h; tb = tl - h; }
-    else if (phase == 2) { ++itr; topt = (tu + tl) / 2; ta = topt + h; tb = topt - h; }
-    else { ta = topt; tb = topt; }
-    const float ca = cost_fast(c, pf, ta);
-    const float cb = cost_fast(c, pf, tb);
-    if (idx < 0) continue;
+    const unsigned active = __ballot_sync(0xffffffffu, idx >= 0);
+    if (active == 0u) break;  // nothing left
+    if (idx >= 0 && !pending) {
+      // the two evaluation points of this step
+      if (phase == 0) { ta = tmax + h; tb = tmax - h; }
+      else if (phase == 1) { ta = tl + h; tb = tl - h; }
+      else if (phase == 2) { ++itr; topt = (tu + tl) / 2; ta = topt + h; tb = topt - h; }
+      else { ta = topt; tb = topt; }
+      ca = cost_ff(pf, ta, &ok_a);
+      cb = cost_ff(pf, tb, &ok_b);
+      pending = !(ok_a && ok_b);
+    }
+    const unsigned waiting = __ballot_sync(0xffffffffu, pending);
+    if (waiting && (__popc(waiting) >= kFallbackLanes || waiting == active)) {
+      if (pending) {
+        const PairCoef c = make_coef(x0, x1);
+        if (!ok_a) ca = cost_eval(c, ta);
+        if (!ok_b) cb = cost_eval(c, tb);
+        pending = false;
+      }
+    }
+    if (idx < 0 || pending) continue;
     const float d = (ca - cb) / dtau;
     if (phase == 0) {
       if (d < 0) { topt = tmax; phase = 3; }
