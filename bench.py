@@ -433,7 +433,8 @@ class Query:
         pb = lib.Problem()
         L.pump_problem_defaults(C.byref(pb))
         pb.N, pb.num_disc, pb.num_hsmc = w["N"], w["num_disc"], w["P"]
-        pb.num_mc = w.get("num_mc", pb.num_mc)
+        # the Monte Carlo CP uses at least as many particles as HSMC
+        pb.num_mc = max(w.get("num_mc", pb.num_mc), w["P"])
         pb.max_paths = w.get("max_paths", 0)
         pb.num_obstacles, pb.obstacles = self.obs.shape[0], self.obs.ctypes.data
         for k in range(6):

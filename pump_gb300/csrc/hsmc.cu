@@ -209,6 +209,12 @@ constexpr int kHsmcThreads = 128;
 constexpr int kHsmcWarps = kHsmcThreads / 32;
 // blocks of a launch that loops over a device-side path count
 constexpr int kHsmcPersistBlocks = kNumSMs * 8;
+// Paths per block chunk: a block's warps take the chunk's paths one at a
+// time from a shared-memory counter, so a warp whose paths are cheap (no
+// active half-space: the parent's masks copied) takes more of them while
+// another tests particles, instead of leaving its slot idle until the
+// block's slowest warp ends.
+constexpr int kHsmcChunk = 4 * kHsmcWarps;
 constexpr int kHsmcFilterObs = 128;
 
 
@@ -484,7 +490,7 @@ __device__ __forceinline__ void hsmc_run(const HsmcParams &p) {
   int n = p.num_new;
   if (p.num_new_dev) n = (p.skip_dev && *p.skip_dev) ? 0 : (int)*p.num_new_dev;
   // a block with no path leaves before staging anything (block-uniform)
-  if ((long long)blockIdx.x * (blockDim.x >> 5) >= n) return;
+  if ((long long)blockIdx.x * kHsmcChunk >= n) return;
   float *s_obs = reinterpret_cast<float *>(s_dyn4);
   float4 *hs = nullptr;
   uint8_t *hcnt = nullptr;
@@ -499,10 +505,23 @@ __device__ __forceinline__ void hsmc_run(const HsmcParams &p) {
     int *s_klist = reinterpret_cast<int *>(s_cnt + kHsmcWarps * cnt_stride);
     klist = s_klist + warp * kHsmcFilterObs;
   }
-  const int warps = (int)((gridDim.x * (long long)blockDim.x) >> 5);
-  for (int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); w < n; w += warps) {
-    hsmc_path<Boxes, Q>(p, w, s_obs, hs, hcnt, klist);
-    __syncwarp();  // the warp's half-space slots are rewritten by its next path
+  __shared__ int s_next;
+  const int lane = threadIdx.x & 31;
+  const long long nchunks = ((long long)n + kHsmcChunk - 1) / kHsmcChunk;
+  for (long long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {  // block-uniform
+    __syncthreads();  // every warp is done with the previous chunk's counter
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    const long long base = ch * kHsmcChunk;
+    const int cnt = (int)((long long)n - base < kHsmcChunk ? (long long)n - base : kHsmcChunk);
+    while (true) {
+      int t = 0;
+      if (lane == 0) t = atomicAdd(&s_next, 1);
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if (t >= cnt) break;  // warp-uniform
+      hsmc_path<Boxes, Q>(p, (int)(base + t), s_obs, hs, hcnt, klist);
+      __syncwarp();  // the warp's half-space slots are rewritten by its next path
+    }
   }
 }
 
@@ -774,9 +793,9 @@ pump_status_t hsmc_staged_async(int num_new, int W, const int *d_edge, const int
   hp.num_new_dev = d_num_new;
   hp.skip_dev = d_skip;
   // with a device-side count, num_new bounds it
-  const long long want = ((long long)num_new * 32 + kHsmcThreads - 1) / kHsmcThreads;
+  const long long want = ((long long)num_new + kHsmcChunk - 1) / kHsmcChunk;
   const unsigned blocks = d_num_new ? (unsigned)(want < kHsmcPersistBlocks ? want : kHsmcPersistBlocks)
-                                    : grid_for((long long)num_new * 32, kHsmcThreads);
+                                    : grid_for(num_new, kHsmcChunk);
   void *args[] = {(void *)&hp};
   PUMP_CUDA_TRY(cudaLaunchKernel(hsmc_kernel_for<false>(P), dim3(blocks), dim3(kHsmcThreads), args,
                                  0, stream));
@@ -856,9 +875,9 @@ pump_status_t hsmc_boxes_async(int num_new, int W, const int *d_edge, const int 
   const void *kern = hsmc_kernel_for<true>(P);
   PUMP_TRY(smem_attr(kern, smem));
   // with a device-side count, num_new bounds it
-  const long long want = ((long long)num_new * 32 + kHsmcThreads - 1) / kHsmcThreads;
+  const long long want = ((long long)num_new + kHsmcChunk - 1) / kHsmcChunk;
   const unsigned blocks = d_num_new ? (unsigned)(want < kHsmcPersistBlocks ? want : kHsmcPersistBlocks)
-                                    : grid_for((long long)num_new * 32, kHsmcThreads);
+                                    : grid_for(num_new, kHsmcChunk);
   void *args[] = {(void *)&hp};
   PUMP_CUDA_TRY(cudaLaunchKernel(kern, dim3(blocks), dim3(kHsmcThreads), args, smem, stream));
   return launch_status("hsmc_kernel (boxes)");
