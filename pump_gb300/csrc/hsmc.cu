@@ -214,7 +214,9 @@ constexpr int kHsmcPersistBlocks = kNumSMs * 8;
 // active half-space: the parent's masks copied) takes more of them while
 // another tests particles, instead of leaving its slot idle until the
 // block's slowest warp ends.
-constexpr int kHsmcChunk = 4 * kHsmcWarps;
+// Two paths per warp: a mid-size wavefront (a few thousand paths) still
+// spreads over every warp of the launch.
+constexpr int kHsmcChunk = 2 * kHsmcWarps;
 constexpr int kHsmcFilterObs = 128;
 
 
