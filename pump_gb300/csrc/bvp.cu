@@ -137,12 +137,14 @@ __device__ __forceinline__ float cost_eval(const PairCoef &c, float tau) {
 // TwoSum and TwoProduct; double-float addition, multiplication and division
 // as in Bailey's double-double library, with binary32 parts), and bounds the
 // distance of cost_eval's binary64 value from it:
-//   - cost_eval's sum: each of its 25 additions and ~15 products is rounded
-//     once (|error| <= 2^-53 of the partial sum or product; t^3 and t^4 are
-//     themselves rounded products), so its error is at most 2^-52 x 27 x
-//     (|s7| + the sum of the terms' magnitudes) = 2^-47.2 x that sum;
-//   - the float-float evaluation: at most 2^-42 x that sum (about 20
-//     operations, each within 2^-46 of its operands' magnitudes);
+//   - cost_eval's sum: each of its 31 additions (s7's six included) and ~15
+//     products is rounded once (|error| <= 2^-53 of the partial sum or
+//     product; t^3 and t^4 are themselves rounded products), so its error is
+//     at most 2^-52 x 33 x (the sum of the terms' magnitudes) = 2^-47 x that
+//     sum;
+//   - the float-float evaluation: at most 2^-42 x that sum (about 30
+//     operations, each within 2^-47 of its operands' magnitudes); the bound
+//     below takes 2^-41, twice the two together;
 //   - the final 1 / t^3 and the product (three more binary64 roundings) and
 //     the float-float division: at most 2^-42 of the result.
 // When that interval around the float-float value lies inside the binary32
@@ -199,48 +201,76 @@ __device__ __forceinline__ FF ff_div(FF x, FF y) {
   return ff_fast_two_sum(q1, q2);
 }
 
-// Per-pair data of cost_ff: the binary32 coefficients of cost_eval's
-// t-linear and last two terms, s7 (cost_eval's binary64 value, split), the
-// sums of the t^2 and t^3 coefficients and their magnitudes.  Without the
-// binary64 coefficients of PairCoef (rebuilt from the two states when an
-// evaluation falls back), a kernel holding a pair needs fewer registers.
+// Per-pair data of cost_ff, built without binary64 arithmetic (the GB300's
+// binary64 conversions and products would cost the pair kernel a quarter of
+// its time): the binary32 coefficients of cost_eval's t-linear and last two
+// terms; s7 as the float-float sum of its seven terms (each exact: 12 x^2 is
+// a TwoProduct scaled by 4 and then by 3 with a TwoProduct, 24 x y is the
+// binary32 product cost_eval converts) and the sum of their magnitudes; the
+// sums of the t^2 and t^3 coefficients and their magnitudes.  cost_eval's
+// own s7 differs from the exact sum by its six binary64 roundings, which
+// cost_ff's bound covers.
 struct PairFF {
   float k8, k9, k10, k11, k12, k13, k14, k15;
   float a29, b29, c29, a30, b30, c30;
   FF s7, d2, d3;
-  float abs_d2, abs_d3;
+  float abs_s7, abs_d2, abs_d3;
 };
-__device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1, const PairCoef &c) {
+__device__ __forceinline__ FF ff_12sq(float x) {
+  FF t = ff_two_prod(x, x);
+  t.hi *= 4.0f;
+  t.lo *= 4.0f;
+  FF p = ff_two_prod(t.hi, 3.0f);
+  p.lo = p.lo + t.lo * 3.0f;
+  return ff_fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1) {
+  const float g = PUMP_G;
   PairFF f;
-  f.k8 = c.k8;
-  f.k9 = c.k9;
-  f.k10 = c.k10;
-  f.k11 = c.k11;
-  f.k12 = c.k12;
-  f.k13 = c.k13;
-  f.k14 = c.k14;
-  f.k15 = c.k15;
-  f.a29 = c.a29;
-  f.b29 = c.b29;
-  f.c29 = c.c29;
-  f.a30 = c.a30;
-  f.b30 = c.b30;
-  f.c30 = c.c30;
-  f.s7.hi = __double2float_rn(c.s7);
-  f.s7.lo = __double2float_rn(c.s7 - (double)f.s7.hi);
+  // the binary32 terms, as make_coef computes them
+  f.k8 = 12 * x0[4] * x0[1];
+  f.k9 = 12 * x0[1] * x1[4];
+  f.k10 = 12 * x0[3] * x1[0];
+  f.k11 = 12 * x1[3] * x1[0];
+  f.k12 = 12 * x0[5] * x1[2];
+  f.k13 = 12 * x1[5] * x1[2];
+  f.k14 = 12 * x0[4] * x1[1];
+  f.k15 = 12 * x1[4] * x1[1];
+  f.a29 = 12 * x0[0];
+  f.b29 = -2 * x1[0];
+  f.c29 = x0[3] + x1[3];
+  f.a30 = 12 * x0[2];
+  f.b30 = -2 * x1[2];
+  f.c30 = x0[5] + x1[5];
+  // s7, make_coef's first seven terms
+  FF s = ff_12sq(x0[0]);
+  float as = s.hi;
+  const float sq[5] = {x0[2], x0[1], x1[0], x1[2], x1[1]};
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    if (q == 4) {
+      const float c24 = 24 * x0[1] * x1[1];
+      s = ff_add_f(s, -c24);
+      as += fabsf(c24);
+    }
+    const FF t = ff_12sq(sq[q]);
+    s = ff_add(s, t);
+    as += t.hi;
+  }
+  f.s7 = s;
+  f.abs_s7 = as;
   // 4 x^2 (exact as a TwoProduct scaled by 4) and the float coefficients
-  const float sq[6] = {x0[4], x0[3], x0[5], x1[4], x1[3], x1[5]};
+  const float sq4[6] = {x0[4], x0[3], x0[5], x1[4], x1[3], x1[5]};
   FF d = {0.0f, 0.0f};
   float ad = 0.0f;
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
-    FF t = ff_two_prod(sq[q], sq[q]);
+    FF t = ff_two_prod(sq4[q], sq4[q]);
     t.hi *= 4.0f;
     t.lo *= 4.0f;
     d = ff_add(d, t);
     ad += t.hi;
   }
-  const float g = PUMP_G;
   const float fl[3] = {4 * x0[4] * x1[4], 4 * x0[3] * x1[3], 4 * x0[5] * x1[5]};
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
@@ -265,7 +295,7 @@ __device__ __forceinline__ float cost_ff(const PairFF &f, float tau, bool *ok) {
   const float a29 = f.a29 * (f.b29 + f.c29 * tau);
   const float a30 = f.a30 * (f.b30 + f.c30 * tau);
   FF v = f.s7;
-  float mag = fabsf(f.s7.hi);
+  float mag = f.abs_s7;
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     v = ff_add_f(v, k[q]);
@@ -288,7 +318,7 @@ __device__ __forceinline__ float cost_ff(const PairFF &f, float tau, bool *ok) {
   // the bound on |cost_eval's binary64 value - w| (margins for the binary32
   // evaluation of the bound itself)
   const float aw = fabsf(w.hi);
-  const float bound = (mag * 1.01f) * 0x1p-42f / t3.hi + aw * 0x1p-42f;
+  const float bound = (mag * 1.01f) * 0x1p-41f / t3.hi + aw * 0x1p-42f;
   const unsigned int u = __float_as_uint(aw);
   const unsigned int e = u >> 23;
   if (e < 2u || e > 253u) return 0.0f;  // zero, subnormal, huge, inf, NaN
@@ -340,7 +370,7 @@ __device__ float topt_bisection(const PairCoef &c, const PairFF &f, float tmax) 
 // toptBisection of the pair (x0, x1).
 __device__ __forceinline__ float topt_parity(const float *x0, const float *x1, float tmax) {
   const PairCoef c = make_coef(x0, x1);
-  return topt_bisection(c, make_pair_ff(x0, x1, c), tmax);
+  return topt_bisection(c, make_pair_ff(x0, x1), tmax);
 }
 
 // --------------------------------------------------------------- kernels
@@ -405,7 +435,7 @@ __global__ void __launch_bounds__(128, 6) bvp_pairs_parity_persistent(
           x0[d] = __ldg(&samples[i * kDim + d]);
           x1[d] = __ldg(&samples[j * kDim + d]);
         }
-        pf = make_pair_ff(x0, x1, make_coef(x0, x1));
+        pf = make_pair_ff(x0, x1);
         phase = 0;
         tu = tmax;
       }
@@ -464,7 +494,7 @@ __global__ void bvp_batch_kernel(const BvpJobs jb) {
     x1[d] = jb.x1[(jb.x1_same ? 0 : k) * kDim + d];
   }
   const PairCoef c = make_coef(x0, x1);
-  const PairFF f = make_pair_ff(x0, x1, c);
+  const PairFF f = make_pair_ff(x0, x1);
   const float tp = topt_bisection(c, f, jb.tmax[j]);
   if (jb.topt[j]) jb.topt[j][k] = tp;
   if (jb.cost[j]) jb.cost[j][k] = cost_fast(c, f, tp);
