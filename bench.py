@@ -793,7 +793,10 @@ def mode_record(lib, L, ctx, torch, w, mode, args, flush, batch, steps=None, war
 #             evaluations are binary32 arithmetic and the kernel is rated by
 #             instruction issue (below), this figure kept as the
 #             arithmetic a binary64 evaluation would do.
-BVP_FP64_FLOPS_PER_PAIR = {"precision": 28.0, "parity": 40.0 * 23 + 20.0}
+# the reference's GPU kernel evaluates the same binary64 expression as its
+# CPU build (one cost: 40 operations; topt: 23 cost pairs less the shared ones)
+BVP_FP64_FLOPS_PER_PAIR = {"precision": 28.0, "parity": 40.0 * 23 + 20.0,
+                           "parity_gpu": 40.0 * 23 + 20.0}
 # ncu smsp__inst_executed.sum of one parity pair-kernel launch at N = 1000
 # (999,000 pairs), per pair
 BVP_PARITY_WARP_INST_PER_PAIR = 520217704 / 999000

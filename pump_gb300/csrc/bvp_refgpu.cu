@@ -28,6 +28,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "ffcost.cuh"
 
 namespace pump {
 namespace {
@@ -97,8 +98,13 @@ __device__ float topt_dev(const float *a, const float *b, const CoordPow &p, flo
 // All ordered pairs: per lane, the evaluations of toptBisection as a state
 // machine (phase 0: the tmax test, 1: halving, 2: bisection, 3: the final
 // cost), two cost evaluations per step; a lane whose pair is done takes the
-// next pair of its warp's chunk of kChunk pairs.
+// next pair of its warp's chunk of kChunk pairs.  Each evaluation is first
+// certified in float-float (cost_ff, ffcost.cuh); a lane whose value is not
+// certified waits until kFallback lanes of its warp wait (or no lane can go
+// on), and they evaluate the reference's expression (CUDA's pow included)
+// together.
 constexpr int kChunk = 512;
+constexpr int kFallback = 8;
 
 __global__ void __launch_bounds__(128) bvp_pairs_refgpu_kernel(const float *__restrict__ samples,
                                                                int N, float tmax,
@@ -116,7 +122,9 @@ __global__ void __launch_bounds__(128) bvp_pairs_refgpu_kernel(const float *__re
   int phase = 0, halvings = 0, itr = 0;
   float tu = 0, tl = 0, topt = 0, dcval = 0;
   float a[kDim], b[kDim];
-  CoordPow p{};
+  PairFF pf{};
+  float ta = 0, tb = 0, ca = 0, cb = 0;
+  bool pending = false, ok_a = true, ok_b = true;
   while (true) {
     const unsigned need = __ballot_sync(0xffffffffu, idx < 0);
     if (need && chunk_next < chunk_end) {
@@ -132,21 +140,33 @@ __global__ void __launch_bounds__(128) bvp_pairs_refgpu_kernel(const float *__re
           a[d] = __ldg(&samples[i * kDim + d]);
           b[d] = __ldg(&samples[j * kDim + d]);
         }
-        p = coord_pow(a, b);
+        pf = make_pair_ff(a, b);
         phase = 0;
         tu = tmax;
       }
       chunk_next += __popc(need) < avail ? __popc(need) : avail;
     }
-    if (__ballot_sync(0xffffffffu, idx >= 0) == 0u) break;
-    float ta, tb;
-    if (phase == 0) { ta = tmax + h; tb = tmax - h; }
-    else if (phase == 1) { ta = tl + h; tb = tl - h; }
-    else if (phase == 2) { ++itr; topt = (tu + tl) / 2; ta = topt + h; tb = topt - h; }
-    else { ta = topt; tb = topt; }
-    const float ca = cost_dev(ta, a, b, p);
-    const float cb = cost_dev(tb, a, b, p);
-    if (idx < 0) continue;
+    const unsigned active = __ballot_sync(0xffffffffu, idx >= 0);
+    if (active == 0u) break;
+    if (idx >= 0 && !pending) {
+      if (phase == 0) { ta = tmax + h; tb = tmax - h; }
+      else if (phase == 1) { ta = tl + h; tb = tl - h; }
+      else if (phase == 2) { ++itr; topt = (tu + tl) / 2; ta = topt + h; tb = topt - h; }
+      else { ta = topt; tb = topt; }
+      ca = cost_ff(pf, ta, &ok_a);
+      cb = cost_ff(pf, tb, &ok_b);
+      pending = !(ok_a && ok_b);
+    }
+    const unsigned waiting = __ballot_sync(0xffffffffu, pending);
+    if (waiting && (__popc(waiting) >= kFallback || waiting == active)) {
+      if (pending) {
+        const CoordPow p = coord_pow(a, b);
+        if (!ok_a) ca = cost_dev(ta, a, b, p);
+        if (!ok_b) cb = cost_dev(tb, a, b, p);
+        pending = false;
+      }
+    }
+    if (idx < 0 || pending) continue;
     const float d = (ca - cb) / dtau;
     if (phase == 0) {
       if (d < 0) { topt = tmax; phase = 3; }
