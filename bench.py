@@ -172,13 +172,21 @@ def cpu_query(args, query=0):
 
 
 # ------------------------------------------------------------------ ours
+# pump_batch_groups for the grouped form of the batch: a group is launched
+# at 16 waiting queries, when every worker is waiting, or after 200 us
+GROUPS = (16, 200)
+
+
 def measure_queries(args, lib, L, ctx, mode):
     """Batched vs plain queries/s on the batched workload (256 queries, N
     log-uniform in [500, 8000], 5-100 boxes, init/goal in free space, CP
     target in {0.001, 0.01, 0.05}, eta in {1, 2, 4}, 4-32 waypoints per edge
     by edge length).  Plain: one pump_plan
-    after another on one stream; batched: pump_plan_batch.  A query counts
-    only when it returns a path whose Monte Carlo CP is below its target."""
+    after another on one stream; batched: pump_plan_batch, each worker
+    driving its own query's search loop; grouped: pump_plan_batch with the
+    search loops of waiting queries run in groups (pump_batch_groups).  A
+    query counts only when it returns a path whose Monte Carlo CP is below
+    its target."""
     from pump_gb300 import workloads
     qs = workloads.batch_queries(args.batch)
     keep = []
@@ -235,24 +243,44 @@ def measure_queries(args, lib, L, ctx, mode):
         lib.check(L.pump_plan_batch(0, pbs, res_b, sts_b, len(qs), workers))
         tb.append(time.perf_counter() - t0)
     t_batch = statistics.median(tb)
+    # the grouped form: the search loops of up to 16 waiting queries run as
+    # one launch of the loop graph (pump_batch_groups)
+    res_g, sts_g = results("grouped"), (C.c_int * len(qs))()
+    tg = []
+    try:
+        L.pump_batch_groups(*GROUPS)
+        lib.check(L.pump_plan_batch(0, pbs, res_g, sts_g, len(qs), workers))  # its graphs
+        for _ in range(3):
+            t0 = time.perf_counter()
+            lib.check(L.pump_plan_batch(0, pbs, res_g, sts_g, len(qs), workers))
+            tg.append(time.perf_counter() - t0)
+    finally:
+        L.pump_batch_groups(1, 100)
+    t_group = statistics.median(tg)
     # identical results: status, solution index, CP and cost bits, and the
     # returned path's states bit for bit
     f32 = lambda x: np.float32(x).view(np.uint32)  # noqa: E731
-    same = all(res_p[k].success == res_b[k].success and res_p[k].soln_path_idx == res_b[k].soln_path_idx
-               and sts_p[k] == sts_b[k] and res_p[k].path_len == res_b[k].path_len
-               and f32(res_p[k].soln_cp) == f32(res_b[k].soln_cp)
-               and f32(res_p[k].soln_cost) == f32(res_b[k].soln_cost)
-               and np.array_equal(paths["plain"][k][: res_p[k].path_len].view(np.uint32),
-                                  paths["batched"][k][: res_b[k].path_len].view(np.uint32))
-               for k in range(len(qs)))
-    ok_p, ok_b = ok(res_p, sts_p), ok(res_b, sts_b)
+
+    def same_as_plain(res_b, sts_b, tag):
+        return all(res_p[k].success == res_b[k].success and res_p[k].soln_path_idx == res_b[k].soln_path_idx
+                   and sts_p[k] == sts_b[k] and res_p[k].path_len == res_b[k].path_len
+                   and f32(res_p[k].soln_cp) == f32(res_b[k].soln_cp)
+                   and f32(res_p[k].soln_cost) == f32(res_b[k].soln_cost)
+                   and np.array_equal(paths["plain"][k][: res_p[k].path_len].view(np.uint32),
+                                      paths[tag][k][: res_b[k].path_len].view(np.uint32))
+                   for k in range(len(qs)))
+    same = same_as_plain(res_b, sts_b, "batched")
+    ok_p, ok_b, ok_g = ok(res_p, sts_p), ok(res_b, sts_b), ok(res_g, sts_g)
     return {"workload": "batch256: N log-uniform [500, 8000], 5-100 boxes, noise 1e-3, waypoints "
                         "per edge by edge length (at most 0.025 apart, 4 to 32)",
             "bvp": mode, "queries": len(qs), "met_cp_target": ok_b, "workers": workers,
             "plain_queries_per_s": ok_p / t_plain, "batched_queries_per_s": ok_b / t_batch,
             "batched_over_plain": (ok_b / t_batch) / (ok_p / t_plain) if ok_p else None,
             "plain_s": t_plain, "batched_s": t_batch, "plain_s_runs": tp, "batched_s_runs": tb,
-            "identical_results": bool(same)}
+            "identical_results": bool(same),
+            "grouped": {"max_group": GROUPS[0], "window_us": GROUPS[1],
+                        "queries_per_s": ok_g / t_group, "s_runs": tg,
+                        "identical_results": bool(same_as_plain(res_g, sts_g, "grouped"))}}
 
 
 def measure_refine(args, lib, L, ctx, torch):

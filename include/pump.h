@@ -542,6 +542,22 @@ pump_status_t pump_plan_batch(int device, const pump_problem *problems, pump_pla
  * level. */
 void pump_search_graph(int level);
 
+/* Grouped search loops of pump_plan_batch (process-wide; no reference
+ * counterpart).  With max_group > 1, a worker whose query reaches its
+ * search loop joins the group being formed; the group's loop runs as one
+ * launch of a loop graph whose kernels serve all of its queries in each
+ * iteration (the expansion, edge checks and store pass give each query a
+ * share of their grid; HSMC's blocks take the chunks of every query's
+ * wavefront in turn), and whose while node repeats the iteration until every
+ * query's loop has ended.  A group is launched when it holds max_group
+ * queries (at most 16), when every worker still planning is waiting or
+ * running a group, or when its first query has waited window_us
+ * microseconds; two groups may run at once.  Each query's results are the
+ * same as pump_plan's.  max_group 1 (the default): each worker drives its
+ * own loop (pump_search_graph).  The environment variable PUMP_BATCH_GROUPS
+ * ("max_group" or "max_group,window_us") sets the starting values. */
+void pump_batch_groups(int max_group, int window_us);
+
 #ifdef __cplusplus
 }
 #endif

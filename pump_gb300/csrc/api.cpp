@@ -44,6 +44,7 @@ Ctx::~Ctx() {
   if (refine_graph.exec) cudaGraphExecDestroy(refine_graph.exec);
   for (const LoopGraph &g : loop_graphs) cudaGraphExecDestroy(g.exec);
   if (capture_stream) cudaStreamDestroy(capture_stream);
+  if (loop_ready) cudaEventDestroy(loop_ready);
   for (int i = 0; i < kNumSlots; ++i)
     if (buf_[i]) cudaFree(buf_[i]);
   for (void *p : retired_) cudaFree(p);

@@ -84,6 +84,8 @@ class Ctx {
   };
   std::vector<LoopGraph> loop_graphs;
   cudaStream_t capture_stream = nullptr;
+  // recorded after a grouped search loop's argument block (pump_plan_batch)
+  cudaEvent_t loop_ready = nullptr;
   // Values of the completion words that kernels write to pinned memory for
   // a host waiting on them (one per wait, never repeated on this context).
   unsigned int seq_counter = 0;

@@ -533,14 +533,84 @@ __global__ void __launch_bounds__(kHsmcThreads, 8) hsmc_kernel(const HsmcParams 
   hsmc_run<Boxes, Q>(p);
 }
 
-// The search loop on the device: the parameters from device memory, the
-// stored-path count (the bound on parents) from the loop state.
+// The search loop on the device, for every query of a group: the chunks of
+// the active queries' wavefronts in query order are the blocks' work items,
+// taken in turn (grid-stride).  A block stages a query's parameters (the
+// stored-path count, the bound on parents, from its loop state) and boxes
+// when its next chunk belongs to another query.  The shared memory holds the
+// layout of the group's largest box count, waypoint count and half-space
+// count.
 template <int Q>
-__global__ void __launch_bounds__(kHsmcThreads, 8) hsmc_loop_kernel(const HsmcParams *hp,
-                                                                    const LoopState *L) {
-  HsmcParams p = *hp;
-  p.num_prev = L->num_paths;
-  hsmc_run<true, Q>(p);
+__global__ void __launch_bounds__(kHsmcThreads, 8) hsmc_loop_kernel(const LoopGroup *g) {
+  extern __shared__ float4 s_dyn4[];
+  __shared__ int s_first[kLoopGroupMax + 1];  // first chunk of each query
+  __shared__ HsmcParams s_p;
+  __shared__ int s_next;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nq = g->nq;
+  if (warp == 0) {
+    int c = 0;
+    if (lane < nq) {
+      const LoopArgs *a = g->args[lane];
+      if (*reinterpret_cast<const volatile int *>(&a->L.active)) {
+        const HsmcParams &hp = a->hp;
+        const int n = (hp.skip_dev && *hp.skip_dev) ? 0 : (int)*hp.num_new_dev;
+        c = (n + kHsmcChunk - 1) / kHsmcChunk;
+      }
+    }
+    // inclusive scan over the queries (nq <= 32 lanes)
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, c, o);
+      if (lane >= o) c += u;
+    }
+    if (lane == 0) s_first[0] = 0;
+    if (lane < kLoopGroupMax) s_first[lane + 1] = c;
+  }
+  __syncthreads();
+  const int total = s_first[nq];
+  // a block with no chunk leaves before staging anything (block-uniform)
+  if ((int)blockIdx.x >= total) return;
+  float *s_obs = reinterpret_cast<float *>(s_dyn4);
+  int cur = -1;
+  for (int ch = blockIdx.x; ch < total; ch += gridDim.x) {  // block-uniform
+    int q = 0;
+    while (q + 1 < nq && s_first[q + 1] <= ch) ++q;
+    __syncthreads();  // every warp is done with the previous chunk (its counter, its query)
+    if (q != cur) {
+      if (warp == 0) {  // the query's parameters, word by word
+        static_assert(sizeof(HsmcParams) % sizeof(int) == 0, "HsmcParams words");
+        const int *src = reinterpret_cast<const int *>(&g->args[q]->hp);
+        int *dst = reinterpret_cast<int *>(&s_p);
+        for (int i = lane; i < (int)(sizeof(HsmcParams) / sizeof(int)); i += 32) dst[i] = src[i];
+        __syncwarp();
+        if (lane == 0) s_p.num_prev = g->args[q]->L.num_paths;
+      }
+      __syncthreads();
+      stage_obstacles(s_p.obs, s_p.numObs, s_obs);  // ends with a barrier
+      cur = q;
+    }
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    const HsmcParams p = s_p;
+    // this query's layout of the shared memory
+    const int hs_stride = hsmc_hs_stride(p.W, p.maxHS), cnt_stride = hsmc_cnt_stride(p.W);
+    float4 *s_hs = reinterpret_cast<float4 *>(s_obs + hsmc_boxes_obs_floats(p.numObs));
+    uint8_t *s_cnt = reinterpret_cast<uint8_t *>(s_hs + kHsmcWarps * hs_stride);
+    int *s_klist = reinterpret_cast<int *>(s_cnt + kHsmcWarps * cnt_stride);
+    const int n = (p.skip_dev && *p.skip_dev) ? 0 : (int)*p.num_new_dev;
+    const int base = (ch - s_first[q]) * kHsmcChunk;
+    const int cnt = n - base < kHsmcChunk ? n - base : kHsmcChunk;
+    while (true) {
+      int t = 0;
+      if (lane == 0) t = atomicAdd(&s_next, 1);
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if (t >= cnt) break;  // warp-uniform
+      hsmc_path<true, Q>(p, base + t, s_obs, s_hs + warp * hs_stride, s_cnt + warp * cnt_stride,
+                         s_klist + warp * kHsmcFilterObs);
+      __syncwarp();  // the warp's half-space slots are rewritten by its next path
+    }
+  }
 }
 
 // The kernel of P particles (Q = ceil(P / 1024), 1, 2 or 4).
@@ -889,9 +959,9 @@ pump_status_t hsmc_loop_prepare(int numObs, int W, int maxHS, int P) {
   return smem_attr(hsmc_loop_kernel_for(P), hsmc_boxes_smem(numObs, W, maxHS));
 }
 
-pump_status_t hsmc_loop_launch(const HsmcParams *d_hp, const LoopState *d_L, int numObs, int W,
-                               int maxHS, int P, int blocks, cudaStream_t stream) {
-  void *args[] = {(void *)&d_hp, (void *)&d_L};
+pump_status_t hsmc_loop_launch(const LoopGroup *d_group, int numObs, int W, int maxHS, int P,
+                               int blocks, cudaStream_t stream) {
+  void *args[] = {(void *)&d_group};
   PUMP_CUDA_TRY(cudaLaunchKernel(hsmc_loop_kernel_for(P), dim3(blocks), dim3(kHsmcThreads), args,
                                  hsmc_boxes_smem(numObs, W, maxHS), stream));
   return launch_status("hsmc_loop_kernel");

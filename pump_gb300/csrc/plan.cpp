@@ -22,6 +22,7 @@
 #include <atomic>
 #include <chrono>
 #include <string>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <cmath>
@@ -32,6 +33,7 @@
 
 #include "common.cuh"
 #include "ctx.h"
+#include "loopbatch.h"
 #include "pairview.cuh"
 #include "search.h"
 
@@ -103,6 +105,30 @@ std::atomic<int> &search_graph_flag() {
     return (e && e[0] >= '0' && e[0] <= '2') ? e[0] - '0' : 1;
   }());
   return flag;
+}
+
+// Grouped search loops of pump_plan_batch (pump_batch_groups): queries per
+// group (1: none) and the window in microseconds; the environment variable
+// PUMP_BATCH_GROUPS ("max_group" or "max_group,window_us") sets the
+// starting values.
+std::atomic<int> *batch_group_flags() {
+  static std::atomic<int> flags[2];
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int g = 1, w = 100;
+    if (const char *e = std::getenv("PUMP_BATCH_GROUPS")) {
+      char *end = nullptr;
+      const long v = std::strtol(e, &end, 10);
+      if (end != e) g = (int)(v < 1 ? 1 : (v > kLoopGroupMax ? kLoopGroupMax : v));
+      if (end && *end == ',') {
+        const long u = std::strtol(end + 1, nullptr, 10);
+        w = (int)(u < 0 ? 0 : (u > 100000 ? 100000 : u));
+      }
+    }
+    flags[0].store(g);
+    flags[1].store(w);
+  });
+  return flags;
 }
 
 // The arena of ctx serves this thread's planner buffers while in scope.
@@ -190,10 +216,12 @@ class Planner {
  public:
   // lazy: check each node's out-edges when the search first reaches it (the
   // batch's throughput form); otherwise all edges are checked up front (the
-  // latency form).  Results are the same.
+  // latency form).  Results are the same.  batcher: the search loop runs in
+  // a group of the batch's queries (one graph launch for the group).
   Planner(Ctx *ctx, const pump_problem &pb, pump_plan_result *res, cudaStream_t s,
-          const SharedRoadmap *shared = nullptr, bool lazy = false)
-      : ctx_(ctx), pb_(pb), res_(res), s_(s), shared_(shared), lazy_(lazy) {}
+          const SharedRoadmap *shared = nullptr, bool lazy = false,
+          LoopBatcher *batcher = nullptr)
+      : ctx_(ctx), pb_(pb), res_(res), s_(s), shared_(shared), lazy_(lazy), batcher_(batcher) {}
   pump_status_t run();
   // CP (dense path + MC over the table), smoothing cost and dense length of
   // explicit candidate paths (pump_path_cp).
@@ -214,6 +242,9 @@ class Planner {
   pump_status_t explore_graph(const SearchDev &sd, const CheckArgs &ca, const HsmcEpilogue &epi,
                               int M, float cpCutoff, float cpMinSoln, float dr, int *itrs,
                               long long *considered, pump_status_t *status);
+  // The loop's counters and status from the argument block after the loop.
+  pump_status_t loop_result(const LoopArgs *d_args, int M, int *itrs, long long *considered,
+                            pump_status_t *status);
   pump_status_t search_and_smooth();
   // The controller's discretisation of node states xs; t5 and t2, when not
   // null, are the segments' optimal times with tmax 5 and 2 (else computed
@@ -299,6 +330,7 @@ class Planner {
   cudaStream_t s_;
   const SharedRoadmap *shared_;
   bool lazy_ = false;
+  LoopBatcher *batcher_ = nullptr;
   DevBuf<float> d_own_c_, d_own_t_;  // pairs touching init/goal (shared-roadmap path)
 
   // problem constants (mainPUMP.cu:51-72)
@@ -628,11 +660,13 @@ pump_status_t Planner::explore() {
   // The loop runs on the device as one graph launch (search_loop_graph)
   // unless the wavefront trace is wanted (the host reads it between the
   // expansion and the rest of each iteration).  Batch workers (lazy edge
-  // checks) drive it from the host unless asked otherwise: with 12 workers
-  // the graphs' loops took 1.6 ms per query against 0.95 ms host-driven
-  // (alone: 0.36 against 0.39 ms).
+  // checks) run it in groups of queries (batcher_), or drive it from the
+  // host: with 12 workers each launching its own query's graph, the loops
+  // took 1.6 ms per query against 0.95 ms host-driven (alone: 0.36 against
+  // 0.39 ms).
   const int graph_level = search_graph_flag().load();
-  const bool graph_loop = !res_->wf_trace && (graph_level >= 2 || (graph_level == 1 && !lazy_));
+  const bool graph_loop =
+      !res_->wf_trace && (batcher_ || graph_level >= 2 || (graph_level == 1 && !lazy_));
   if (!graph_loop) {
     PUMP_CUDA_TRY(cudaMemsetAsync(d_err_.p, 0, sizeof(int), s_));
     // setupValidParticles (PUMP.cu:766-777) for path 0: all particles valid
@@ -859,7 +893,8 @@ pump_status_t Planner::loop_region(int M, char **base, size_t *args_b, LoopTiles
   const long long scan_cap = pow2((M + 1 + kLoopScanTile - 1) / kLoopScanTile + 1);
   const long long store_cap = pow2((M + 1 + kLoopStoreTile - 1) / kLoopStoreTile + 1);
   auto round256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  *args_b = round256(sizeof(LoopArgs));
+  // the argument block, then the one-query group of this context's graphs
+  *args_b = round256(sizeof(LoopArgs)) + round256(sizeof(LoopGroup));
   const size_t scan_b = sizeof(unsigned long long) * (size_t)loop_tile_words(scan_cap);
   const size_t store_b = sizeof(unsigned long long) * (size_t)loop_tile_words(store_cap);
   PUMP_TRY(ctx_->scratch(Ctx::kLoop, *args_b + scan_b + store_b, (void **)base));
@@ -887,9 +922,11 @@ pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
   LoopTiles scan{}, store{};
   PUMP_TRY(loop_region(M, &base, &args_b, &scan, &store));
   const long long scan_cap = scan.cap, store_cap = store.cap;
+  // pinned staging of the argument block and of the one-query group
+  const size_t group_off = (sizeof(LoopArgs) + 255) & ~(size_t)255;
   LoopArgs *la = nullptr;
-  PUMP_TRY(ctx_->pinned(Ctx::kPinLoop, sizeof(LoopArgs), (void **)&la));
-  std::memset(la, 0, sizeof *la);
+  PUMP_TRY(ctx_->pinned(Ctx::kPinLoop, group_off + sizeof(LoopGroup), (void **)&la));
+  std::memset(la, 0, group_off + sizeof(LoopGroup));
   la->sd = sd;
   la->ca = ca;
   la->scan = scan;
@@ -918,13 +955,30 @@ pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
   L.num_paths = 1;
   L.cost_threshold = h0_;
   L.g_count[0] = 1;
-  res_->h2d_bytes += (long long)sizeof(LoopArgs);
-  PUMP_CUDA_TRY(cudaMemcpyAsync(base, la, sizeof(LoopArgs), cudaMemcpyHostToDevice, s_));
-  // the context's graph for this shape class (built on first use)
+  LoopArgs *d_args = reinterpret_cast<LoopArgs *>(base);
   // shared memory sized for the box count rounded up to 32 (exact for large
   // maps, which sit close to the shared-memory limit)
   const int obs_cap = nobs_ > 1024 ? nobs_ : (nobs_ <= 32 ? 32 : ((nobs_ + 31) / 32) * 32);
   const int lazy = lazy_ ? 1 : 0, mode = host_bvp_mode(pb_.bvp_mode), num_disc = pb_.num_disc;
+  if (batcher_) {
+    // the loop runs in the group the batcher launches, after this stream's
+    // work up to the argument block
+    res_->h2d_bytes += (long long)sizeof(LoopArgs);
+    PUMP_CUDA_TRY(cudaMemcpyAsync(base, la, sizeof(LoopArgs), cudaMemcpyHostToDevice, s_));
+    if (!ctx_->loop_ready)
+      PUMP_CUDA_TRY(cudaEventCreateWithFlags(&ctx_->loop_ready, cudaEventDisableTiming));
+    PUMP_CUDA_TRY(cudaEventRecord(ctx_->loop_ready, s_));
+    const LoopShape shape{lazy, mode, obs_cap, num_disc, maxHS_, pb_.num_hsmc};
+    PUMP_TRY(batcher_->run(d_args, shape, ctx_->loop_ready));
+    return loop_result(d_args, M, itrs, considered, status);
+  }
+  LoopGroup *hg = reinterpret_cast<LoopGroup *>(reinterpret_cast<char *>(la) + group_off);
+  hg->args[0] = d_args;
+  hg->nq = 1;
+  LoopGroup *d_group = reinterpret_cast<LoopGroup *>(base + group_off);
+  res_->h2d_bytes += (long long)(group_off + sizeof(LoopGroup));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(base, la, group_off + sizeof(LoopGroup), cudaMemcpyHostToDevice, s_));
+  // the context's graph for this shape class (built on first use)
   std::vector<Ctx::LoopGraph> &gs = ctx_->loop_graphs;
   for (size_t i = 0; i < gs.size();) {  // graphs of an outgrown argument block
     if (gs[i].base != base) {
@@ -943,18 +997,21 @@ pump_status_t Planner::explore_graph(const SearchDev &sd, const CheckArgs &ca,
   if (!exec) {
     if (!ctx_->capture_stream)
       PUMP_CUDA_TRY(cudaStreamCreateWithFlags(&ctx_->capture_stream, cudaStreamNonBlocking));
-    PUMP_TRY(search_loop_graph(reinterpret_cast<LoopArgs *>(base), lazy_, mode, obs_cap, num_disc,
-                               maxHS_, pb_.num_hsmc, la->scan, la->store, ctx_->capture_stream,
-                               &exec));
+    PUMP_TRY(search_loop_graph(d_group, 1, lazy_, mode, obs_cap, num_disc, maxHS_, pb_.num_hsmc,
+                               ctx_->capture_stream, &exec));
     gs.push_back({lazy, mode, obs_cap, num_disc, maxHS_, pb_.num_hsmc, scan_cap, store_cap, base,
                   exec});
   }
   PUMP_CUDA_TRY(cudaGraphLaunch(exec, s_));
+  return loop_result(d_args, M, itrs, considered, status);
+}
+
+pump_status_t Planner::loop_result(const LoopArgs *d_args, int M, int *itrs,
+                                   long long *considered, pump_status_t *status) {
   LoopState *hl = nullptr;
   PUMP_TRY(ctx_->pinned(Ctx::kPinCtl, sizeof(LoopState), (void **)&hl));
   res_->d2h_bytes += (long long)sizeof(LoopState);
-  PUMP_CUDA_TRY(cudaMemcpyAsync(hl, &reinterpret_cast<LoopArgs *>(base)->L, sizeof(LoopState),
-                                cudaMemcpyDeviceToHost, s_));
+  PUMP_CUDA_TRY(cudaMemcpyAsync(hl, &d_args->L, sizeof(LoopState), cudaMemcpyDeviceToHost, s_));
   PUMP_TRY(sync());
   const LoopState r = *hl;
   *itrs = r.itrs;
@@ -1524,7 +1581,8 @@ using namespace pump;
 namespace pump {
 namespace {
 pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *res, bool lazy,
-                       pump_stream_t stream, const SharedRoadmap *shared) {
+                       pump_stream_t stream, const SharedRoadmap *shared,
+                       LoopBatcher *batcher = nullptr) {
   if (!ctx || !pb || !res) return set_error(PUMP_ERR_BAD_INPUT, "pump_plan: null argument");
   if (pb->N < 2 || pb->num_disc < 1 || pb->num_hsmc < 1 || pb->num_mc < pb->num_hsmc ||
       pb->table_rows < 2 || pb->num_obstacles < 0 || (pb->num_obstacles > 0 && !pb->obstacles) ||
@@ -1561,7 +1619,7 @@ pump_status_t plan_one(pump_ctx *ctx, const pump_problem *pb, pump_plan_result *
   PUMP_TRY(c->activate());
   PUMP_TRY(c->arena_begin((cudaStream_t)stream));
   ArenaScope scope(c, (cudaStream_t)stream);
-  Planner planner(c, *pb, res, (cudaStream_t)stream, shared, lazy);
+  Planner planner(c, *pb, res, (cudaStream_t)stream, shared, lazy, batcher);
   return planner.run();
 }
 }  // namespace
@@ -1614,6 +1672,12 @@ void give_worker(int device, pump_ctx *ctx, cudaStream_t s, pump_status_t last) 
 
 extern "C" void pump_search_graph(int level) {
   search_graph_flag().store(level < 0 ? 0 : (level > 2 ? 2 : level));
+}
+
+extern "C" void pump_batch_groups(int max_group, int window_us) {
+  batch_group_flags()[0].store(max_group < 1 ? 1 : (max_group > kLoopGroupMax ? kLoopGroupMax
+                                                                                : max_group));
+  batch_group_flags()[1].store(window_us < 0 ? 0 : window_us);
 }
 
 extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problems,
@@ -1681,6 +1745,18 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
     pump_status_t st = cuda_status(cudaStreamSynchronize(setup_stream), "cudaStreamSynchronize");
     if (st != PUMP_OK) { cleanup(); return st; }
   }
+  // grouped search loops (pump_batch_groups): two groups may run at once
+  std::unique_ptr<LoopBatcher> batcher;
+  const int group_max = batch_group_flags()[0].load();
+  if (group_max > 1 && workers > 1) {
+    batcher.reset(new LoopBatcher(device, workers, group_max, batch_group_flags()[1].load(), 2));
+    if (batcher->status() != PUMP_OK) {
+      const pump_status_t st = batcher->status();
+      batcher.reset();
+      cleanup();
+      return st;
+    }
+  }
   std::atomic<int> next(0);
   std::vector<pump_status_t> setup(workers, PUMP_OK);
   std::vector<std::string> msgs(workers);
@@ -1689,6 +1765,13 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
   int first_fail = n;
   std::string fail_msg;
   auto worker = [&](int w) {
+    // groups stop waiting for this worker once it has no more queries
+    struct Leave {
+      LoopBatcher *b;
+      ~Leave() {
+        if (b) b->leave();
+      }
+    } leave{batcher.get()};
     pump_ctx *ctx = nullptr;
     cudaStream_t s = nullptr;
     pump_status_t st = take_worker(device, &ctx, &s);
@@ -1701,7 +1784,8 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
         const SharedRoadmap *g = nullptr;
         for (const auto &x : groups)
           if (x.M > 0 && x.matches(problems[k])) g = &x;
-        statuses[k] = plan_one(ctx, &problems[k], &results[k], true, (pump_stream_t)s, g);
+        statuses[k] = plan_one(ctx, &problems[k], &results[k], true, (pump_stream_t)s, g,
+                               batcher.get());
         last = statuses[k];
         if (statuses[k] != PUMP_OK && statuses[k] != PUMP_ERR_NO_SOLUTION) {
           std::lock_guard<std::mutex> lk(fail_mu);
@@ -1730,6 +1814,7 @@ extern "C" pump_status_t pump_plan_batch(int device, const pump_problem *problem
   for (int w = 1; w < workers; ++w) pool.emplace_back(worker, w);
   worker(0);
   for (auto &t : pool) t.join();
+  batcher.reset();
   cleanup();
   for (int w = 0; w < workers; ++w)
     if (setup[w] != PUMP_OK) return set_error(setup[w], "pump_plan_batch worker %d: %s", w, msgs[w].c_str());

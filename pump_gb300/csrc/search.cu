@@ -654,9 +654,17 @@ __global__ void __launch_bounds__(kCompactThreads) store_kernel(
 }
 
 // ------------------------------------------- the search loop on the device
-// Graph form of the loop: every kernel reads its arguments from the
-// context's LoopArgs block; the per-iteration values come from the loop
-// state, which the control kernel updates after each iteration.
+// Graph form of the loop: every kernel reads its arguments from its query's
+// LoopArgs block (blockIdx.y of the group); the per-iteration values come
+// from the loop state, which the control step updates after each iteration.
+
+// The argument block of this block's query, or null when the block has no
+// query or the query's loop has ended (block-uniform).
+__device__ __forceinline__ LoopArgs *loop_query(const LoopGroup *g) {
+  if ((int)blockIdx.y >= g->nq) return nullptr;
+  LoopArgs *a = g->args[blockIdx.y];
+  return *reinterpret_cast<const volatile int *>(&a->L.active) ? a : nullptr;
+}
 
 __device__ __forceinline__ TileScratch tiles_of(const LoopTiles &t) {
   TileScratch ts{};
@@ -668,8 +676,11 @@ __device__ __forceinline__ TileScratch tiles_of(const LoopTiles &t) {
 }
 
 // search_init_kernel, the particle-table error word and path 0's particle
-// mask (all P particles valid).
-__global__ void loop_init_kernel(const LoopArgs *a) {
+// mask (all P particles valid), per query of the group.
+__global__ void loop_init_kernel(LoopGroup *g) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) g->store_done = 0u;
+  if ((int)blockIdx.y >= g->nq) return;
+  const LoopArgs *a = g->args[blockIdx.y];
   const SearchDev sd = a->sd;
   search_init_body(sd);
   if (blockIdx.x == 0 && threadIdx.x == 0) *a->err = 0;
@@ -689,20 +700,29 @@ __global__ void loop_init_kernel(const LoopArgs *a) {
   }
 }
 
-// search_init_head_kernel, then the while node's first iteration.
-__global__ void loop_arm_kernel(const LoopArgs *a, cudaGraphConditionalHandle h) {
-  a->sd.node_head[0] = 0;
-  cudaGraphSetConditional(h, 1u);
+// search_init_head_kernel, then the while node's first iteration (one block
+// per query).
+__global__ void loop_arm_kernel(LoopGroup *g, cudaGraphConditionalHandle h) {
+  if ((int)blockIdx.y < g->nq) {
+    LoopArgs *a = g->args[blockIdx.y];
+    a->sd.node_head[0] = 0;
+    a->L.active = 1;
+  }
+  if (blockIdx.y == 0) cudaGraphSetConditional(h, g->nq > 0 ? 1u : 0u);
 }
 
 template <int Mode>
-__global__ void __launch_bounds__(kChkThreads, 4) check_loop_kernel(const LoopArgs *a) {
+__global__ void __launch_bounds__(kChkThreads, 4) check_loop_kernel(const LoopGroup *g) {
+  const LoopArgs *a = loop_query(g);
+  if (!a) return;
   const SearchDev sd = a->sd;
   const CheckArgs ca = a->ca;
   check_body<Mode, false>(sd, ca);
 }
 
-__global__ void __launch_bounds__(kExpThreads) expand_loop_kernel(const LoopArgs *a) {
+__global__ void __launch_bounds__(kExpThreads) expand_loop_kernel(const LoopGroup *g) {
+  const LoopArgs *a = loop_query(g);
+  if (!a) return;
   const SearchDev sd = a->sd;
   const int g_idx = a->L.g_idx;
   const TileScratch ts = tiles_of(a->scan);
@@ -712,10 +732,10 @@ __global__ void __launch_bounds__(kExpThreads) expand_loop_kernel(const LoopArgs
 
 
 // The host loop's bookkeeping after an iteration's counters are back
-// (PUMP.cu:259-288), then the condition of the next iteration; run by the
-// store pass's last block to finish.  A guard ends the loop after 64
-// iterations whatever the state says.
-__device__ void loop_control(LoopArgs *a, cudaGraphConditionalHandle h) {
+// (PUMP.cu:259-288), then whether the query's loop goes on; run by the
+// store pass's last block of the query to finish.  A guard ends the loop
+// after 64 iterations whatever the state says.
+__device__ void loop_control(LoopArgs *a) {
   LoopState &L = a->L;
   SearchCtl c;
   {  // written by other blocks of this iteration's kernels
@@ -766,27 +786,46 @@ __device__ void loop_control(LoopArgs *a, cudaGraphConditionalHandle h) {
     }
   }
   if (L.guard >= 64) cont = 0;
-  cudaGraphSetConditional(h, cont ? 1u : 0u);
+  L.active = cont;
 }
 
 __global__ void __launch_bounds__(kCompactThreads, 2) store_loop_kernel(
-    LoopArgs *a, cudaGraphConditionalHandle h) {
-  const SearchDev sd = a->sd;
-  const TileScratch ts = tiles_of(a->store);
-  zero_tiles(a->scan);  // for the next iteration's expansion
-  store_tiles(sd, a->L.num_paths, a->L.g_idx, a->L.cost_threshold, a->L.dr, a->cp_min_soln,
-              a->eps_cp, a->eps_cost, a->stage, a->valid, a->words, ts);
-  // the last block to finish runs the loop's control step
+    LoopGroup *g, cudaGraphConditionalHandle h) {
   __shared__ bool s_last;
+  LoopArgs *a = loop_query(g);
+  if (a) {
+    const SearchDev sd = a->sd;
+    const TileScratch ts = tiles_of(a->store);
+    zero_tiles(a->scan);  // for the next iteration's expansion
+    store_tiles(sd, a->L.num_paths, a->L.g_idx, a->L.cost_threshold, a->L.dr, a->cp_min_soln,
+                a->eps_cp, a->eps_cost, a->stage, a->valid, a->words, ts);
+    // the query's last block to finish runs its control step
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_last = atomicAdd(a->store.done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+      __threadfence();
+      loop_control(a);
+    }
+  }
+  // the launch's last block to finish (every query's control step is done)
+  // sets the while node's condition: another iteration while any query goes on
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    s_last = atomicAdd(a->store.done, 1u) == gridDim.x - 1;
+    s_last = atomicAdd(&g->store_done, 1u) == gridDim.x * gridDim.y - 1;
   }
   __syncthreads();
   if (s_last && threadIdx.x == 0) {
     __threadfence();
-    loop_control(a, h);
+    unsigned int any = 0u;
+    for (int q = 0; q < g->nq; ++q)
+      any |= *reinterpret_cast<const volatile int *>(&g->args[q]->L.active) ? 1u : 0u;
+    g->store_done = 0u;
+    cudaGraphSetConditional(h, any);
   }
 }
 
@@ -899,10 +938,12 @@ pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int 
   return launch_status("store_kernel");
 }
 
-pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numObs, int numDisc,
-                                int maxHS, int P, const LoopTiles &scan, const LoopTiles &store,
-                                cudaStream_t capture_stream, cudaGraphExec_t *out) {
+pump_status_t search_loop_graph(LoopGroup *d_group, int gcap, bool lazy, int mode, int numObs,
+                                int numDisc, int maxHS, int P, cudaStream_t capture_stream,
+                                cudaGraphExec_t *out) {
   *out = nullptr;
+  if (gcap < 1 || gcap > kLoopGroupMax)
+    return set_error(PUMP_ERR_BAD_INPUT, "search loop graph: %d queries per group", gcap);
   const size_t chk_smem = check_smem(numObs, numDisc, false);
   if (chk_smem > 220 * 1024)
     return set_error(PUMP_ERR_CAPACITY, "%d obstacles and %d waypoints exceed the check stage",
@@ -911,6 +952,11 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
                                             : (const void *)check_loop_kernel<PUMP_BVP_PRECISION>;
   if (lazy) PUMP_TRY(smem_attr(chk, chk_smem));
   PUMP_TRY(hsmc_loop_prepare(numObs, numDisc + 1, maxHS, P));
+  // each query's share of a kernel's grid (the whole grid for one query)
+  auto share = [gcap](int whole, int least) {
+    const int b = whole / gcap;
+    return (unsigned)(b > least ? b : least);
+  };
   cudaGraph_t g = nullptr;
   PUMP_CUDA_TRY(cudaGraphCreate(&g, 0));
   // the while node's condition starts at 0 and is set by the arm kernel
@@ -923,18 +969,18 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
                    "cudaGraphConditionalHandleCreate");
   if (st == PUMP_OK) {
     cudaKernelNodeParams kp{};
-    void *init_args[1] = {&d_args};
+    void *init_args[1] = {&d_group};
     kp.func = (void *)loop_init_kernel;
-    kp.gridDim = dim3(kNumSMs * 2);
+    kp.gridDim = dim3(share(kNumSMs * 2, 2), gcap);
     kp.blockDim = dim3(256);
     kp.kernelParams = init_args;
     st = cuda_status(cudaGraphAddKernelNode(&n_init, g, nullptr, 0, &kp), "cudaGraphAddKernelNode");
   }
   if (st == PUMP_OK) {
     cudaKernelNodeParams kp{};
-    void *arm_args[2] = {&d_args, &h};
+    void *arm_args[2] = {&d_group, &h};
     kp.func = (void *)loop_arm_kernel;
-    kp.gridDim = dim3(1);
+    kp.gridDim = dim3(1, gcap);
     kp.blockDim = dim3(1);
     kp.kernelParams = arm_args;
     st = cuda_status(cudaGraphAddKernelNode(&n_arm, g, &n_init, 1, &kp), "cudaGraphAddKernelNode");
@@ -956,15 +1002,17 @@ pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numOb
       // fixed grids (the kernels loop over the device-side counts)
       const int g_check = kNumSMs * 8, g_wide = kNumSMs * 4;
       if (lazy) {
+        const dim3 gd(share(g_check, 8), gcap);
         if (mode == PUMP_BVP_PARITY)
-          check_loop_kernel<PUMP_BVP_PARITY><<<g_check, kChkThreads, chk_smem, cs>>>(d_args);
+          check_loop_kernel<PUMP_BVP_PARITY><<<gd, kChkThreads, chk_smem, cs>>>(d_group);
         else
-          check_loop_kernel<PUMP_BVP_PRECISION><<<g_check, kChkThreads, chk_smem, cs>>>(d_args);
+          check_loop_kernel<PUMP_BVP_PRECISION><<<gd, kChkThreads, chk_smem, cs>>>(d_group);
       }
-      expand_loop_kernel<<<kNumSMs * 2, kExpThreads, 0, cs>>>(d_args);
-      // HSMC's blocks are half as wide (4 warps): twice as many per SM
-      hsmc_loop_launch(&d_args->hp, &d_args->L, numObs, numDisc + 1, maxHS, P, 2 * g_wide, cs);
-      store_loop_kernel<<<g_wide, kCompactThreads, 0, cs>>>(d_args, h);
+      expand_loop_kernel<<<dim3(share(kNumSMs * 2, 2), gcap), kExpThreads, 0, cs>>>(d_group);
+      // HSMC's blocks are half as wide (4 warps): twice as many per SM; its
+      // grid is not split (blocks take chunks of every query's wavefront)
+      hsmc_loop_launch(d_group, numObs, numDisc + 1, maxHS, P, 2 * g_wide, cs);
+      store_loop_kernel<<<dim3(share(g_wide, 4), gcap), kCompactThreads, 0, cs>>>(d_group, h);
       cudaGraph_t captured = nullptr;
       const pump_status_t ce = cuda_status(cudaStreamEndCapture(cs, &captured), "cudaStreamEndCapture");
       st = ce == PUMP_OK ? launch_status("search loop capture") : ce;

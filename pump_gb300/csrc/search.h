@@ -135,6 +135,7 @@ struct LoopState {
   float dr;
   // the loop
   int itrs, g_idx, n_g, num_paths, status, guard;
+  int active;  // 1 while the loop goes on (the graph's kernels skip a finished query)
   float cost_threshold;
   long long considered;
   int g_count[2];
@@ -179,6 +180,18 @@ struct LoopArgs {
   uint32_t *valid;
   int words, P;
   int *err;  // the particle-table error word (zeroed at the start)
+};
+
+// The searches one loop graph runs side by side: query y of a launch is
+// args[y] (y < nq).  The graph's kernels give each query a share of their
+// grid (blockIdx.y), except HSMC, whose blocks take the chunks of all the
+// queries' wavefronts in turn; every kernel skips a query whose loop has
+// ended.  The while node repeats the iteration while any query goes on.
+constexpr int kLoopGroupMax = 16;
+struct LoopGroup {
+  LoopArgs *args[kLoopGroupMax];
+  int nq;
+  unsigned int store_done;  // store-pass blocks (all queries) done with this iteration
 };
 
 // Path 0 at the initial node in bucket 0 (PUMP.cu:19-34).
@@ -229,20 +242,21 @@ pump_status_t search_store(const SearchDev &sd, int max_new, int num_paths, int 
                            const LoopTiles &scan, SearchCtl *host_ctl, unsigned int seq,
                            cudaStream_t s);
 
-// The graph of the search loop for the argument block at d_args (device):
-// init, then a while node over {[lazy: edge checks], scan, expansion, HSMC,
-// store with the dominance test and the control step}.  Launch shapes are
-// fixed (grid-stride and tile-counter loops); dynamic shared memory is sized for numObs boxes and
-// numDisc waypoints per edge.  Kernel attributes are set here, before the
-// capture.
-pump_status_t search_loop_graph(LoopArgs *d_args, bool lazy, int mode, int numObs, int numDisc,
-                                int maxHS, int P, const LoopTiles &scan, const LoopTiles &store,
-                                cudaStream_t capture_stream, cudaGraphExec_t *out);
+// The graph of the search loop for the group at d_group (device; at most
+// gcap queries): init, then a while node over {[lazy: edge checks],
+// expansion, HSMC, store with the dominance test and the control step}.
+// Launch shapes are fixed (grid-stride and tile-counter loops); dynamic
+// shared memory is sized for numObs boxes, numDisc waypoints per edge,
+// maxHS half-spaces and P particles, each at least the group's largest.
+// Kernel attributes are set here, before the capture.
+pump_status_t search_loop_graph(LoopGroup *d_group, int gcap, bool lazy, int mode, int numObs,
+                                int numDisc, int maxHS, int P, cudaStream_t capture_stream,
+                                cudaGraphExec_t *out);
 
-// HSMC in the loop graph (hsmc.cu).
+// HSMC in the loop graph (hsmc.cu): all active queries of the group.
 pump_status_t hsmc_loop_prepare(int numObs, int W, int maxHS, int P);
-pump_status_t hsmc_loop_launch(const HsmcParams *d_hp, const LoopState *d_L, int numObs, int W,
-                               int maxHS, int P, int blocks, cudaStream_t stream);
+pump_status_t hsmc_loop_launch(const LoopGroup *d_group, int numObs, int W, int maxHS, int P,
+                               int blocks, cudaStream_t stream);
 pump_status_t hsmc_boxes_fill(int num_new, int W, const int *d_edge, const int *d_prev,
                               long long num_edges, int num_prev, const float *d_obs, int numObs,
                               const float *d_disc, float maxd2, int maxHS, const float *d_times,

@@ -107,6 +107,7 @@ _SIGS = {
                                         f32, vp, i32, i32, f32, vp, i32, vp, vp, vp]),
     "pump_tune_enable": (None, [i32]),
     "pump_search_graph": (None, [i32]),
+    "pump_batch_groups": (None, [i32, i32]),
     "pump_tune_reset": (None, []),
     "pump_tune_report": (i32, [C.c_char_p, C.c_size_t]),
     "pump_mc_cp": (i32, [vp, vp, vp, i32, vp, i32, i32, f32, vp, i32, vp, vp, vp, vp]),

@@ -231,6 +231,41 @@ def test_search_graph_equals_host_loop(gpu, pumplib, goldens):
         L.pump_search_graph(1)
 
 
+@pytest.mark.parametrize("groups", [(16, 5000), (3, 0)])
+def test_plan_batch_groups_equal_single_queries(groups, gpu, pumplib):
+    """Grouped search loops (pump_batch_groups): the queries of a group run
+    in one launch of the loop graph, each with its own box count, sample
+    count and waypoints by edge length; every query gives exactly what it
+    gives alone.  (16 queries, 5 ms window: large groups; 3 queries, no
+    window: groups of whatever is waiting.)  The three BVP modes are mixed,
+    so groups also split by mode."""
+    torch, ctx = gpu
+    from pump_gb300 import workloads
+    L = pumplib.load()
+    qs = workloads.batch_queries(20, seed=303, n_range=(200, 2500), obs_range=(5, 100))
+    keep = []
+    pbs = (pumplib.Problem * len(qs))(*[fill_problem(pumplib, q, keep) for q in qs])
+    for k, q in enumerate(qs):
+        pbs[k].num_disc, pbs[k].disc_len, pbs[k].disc_min = q["num_disc"], q["disc_len"], q["disc_min"]
+        pbs[k].bvp_mode = (pumplib.PUMP_BVP_PRECISION, pumplib.PUMP_BVP_PARITY,
+                           pumplib.PUMP_BVP_PRECISION, pumplib.PUMP_BVP_PARITY_GPU)[k % 4]
+    res = (pumplib.PlanResult * len(qs))()
+    paths = [np.zeros((400, 6), np.float32) for _ in qs]
+    for k in range(len(qs)):
+        res[k].path, res[k].path_cap = paths[k].ctypes.data, 400
+    sts = (C.c_int * len(qs))()
+    try:
+        L.pump_batch_groups(*groups)
+        pumplib.check(L.pump_plan_batch(0, pbs, res, sts, len(qs), 6))
+    finally:
+        L.pump_batch_groups(1, 100)
+    for k in range(len(qs)):
+        st1, r1, p1, _ = run_plan(pumplib, ctx, pbs[k])
+        assert sts[k] == st1, k
+        assert _fields(res[k]) == _fields(r1), k
+        assert np.array_equal(paths[k][: res[k].path_len].view(np.uint32), p1.view(np.uint32)), k
+
+
 def test_plan_batch_equals_single_large(gpu, pumplib):
     """Larger batch queries (N 3000-6000, 40-100 boxes), whose search
     iterations list enough nodes for the wide form of the lazy edge checks
