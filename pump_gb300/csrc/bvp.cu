@@ -342,11 +342,37 @@ __global__ void __launch_bounds__(T) discretize_kernel(
     // findDiscretizedPath recomputes the time with the host arithmetic
     const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_parity(x0, x1, 5.0f) : topt;
     const float dt = tau / numDisc;
-    for (int i = 1; i < numDisc; ++i) {
-      if (Mode != PUMP_BVP_PRECISION) path_point(dt * i, tau, x0, x1, x);
-      else path_point_f32(dt * i, tau, x0, x1, x);
+    if (Mode != PUMP_BVP_PRECISION) {
+      // float-float waypoints; the uncertified ones (a few in a hundred) in
+      // binary64 afterwards, each lane taking its next one per round, so a
+      // warp runs the binary64 evaluation about once instead of once per
+      // waypoint index where some lane needs it
+      const PathFF pe = path_ff_edge(tau, x0, x1);
+      unsigned int redo = 0u;  // waypoints i < 32 left for binary64
+      for (int i = 1; i < numDisc; ++i) {
+        if (!path_point_try(dt * i, tau, x0, x1, pe, x)) {
+          if (i < 32) {
+            redo |= 1u << i;
+            continue;
+          }
+          path_point(dt * i, tau, x0, x1, x);
+        }
 #pragma unroll
-      for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+        for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+      }
+      while (redo) {
+        const int i = __ffs(redo) - 1;
+        redo &= redo - 1u;
+        path_point(dt * i, tau, x0, x1, x);
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+      }
+    } else {
+      for (int i = 1; i < numDisc; ++i) {
+        path_point_f32(dt * i, tau, x0, x1, x);
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+      }
     }
   }
   __syncthreads();
@@ -512,11 +538,37 @@ __global__ void __launch_bounds__(T) discretize_off_kernel(
     const float topt = toptE[e];
     const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_parity(x0, x1, 5.0f) : topt;
     const float dt = tau / numDisc;
-    for (int i = 1; i < numDisc; ++i) {
-      if (Mode != PUMP_BVP_PRECISION) path_point(dt * i, tau, x0, x1, x);
-      else path_point_f32(dt * i, tau, x0, x1, x);
+    if (Mode != PUMP_BVP_PRECISION) {
+      // float-float waypoints; the uncertified ones (a few in a hundred) in
+      // binary64 afterwards, each lane taking its next one per round, so a
+      // warp runs the binary64 evaluation about once instead of once per
+      // waypoint index where some lane needs it
+      const PathFF pe = path_ff_edge(tau, x0, x1);
+      unsigned int redo = 0u;  // waypoints i < 32 left for binary64
+      for (int i = 1; i < numDisc; ++i) {
+        if (!path_point_try(dt * i, tau, x0, x1, pe, x)) {
+          if (i < 32) {
+            redo |= 1u << i;
+            continue;
+          }
+          path_point(dt * i, tau, x0, x1, x);
+        }
 #pragma unroll
-      for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+        for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+      }
+      while (redo) {
+        const int i = __ffs(redo) - 1;
+        redo &= redo - 1u;
+        path_point(dt * i, tau, x0, x1, x);
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+      }
+    } else {
+      for (int i = 1; i < numDisc; ++i) {
+        path_point_f32(dt * i, tau, x0, x1, x);
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) o[i * kDim + d] = x[d];
+      }
     }
   }
   __syncthreads();
@@ -544,7 +596,7 @@ __global__ void path_states_kernel(const float *__restrict__ xs, const int *__re
   if (k >= total) return;
   const int s = seg[k];
   float x[kDim];
-  path_point(tsample[k], tau[s], &xs[s * kDim], &xs[(s + 1) * kDim], x);
+  path_point_fast(tsample[k], tau[s], &xs[s * kDim], &xs[(s + 1) * kDim], x);
 #pragma unroll
   for (int d = 0; d < kDim; ++d) out[k * kDim + d] = x[d];
 }
@@ -615,7 +667,7 @@ __global__ void __launch_bounds__(kRowThreads) candidate_rows_kernel(
       a[d] = x0[s * kDim + d];
       c[d] = x1[s * kDim + d];
     }
-    if (Mode == PUMP_BVP_PARITY) path_point(dt * k + stoff[lo], topt[s], a, c, x);
+    if (Mode == PUMP_BVP_PARITY) path_point_fast(dt * k + stoff[lo], topt[s], a, c, x);
     else path_point_f32(dt * k + stoff[lo], topt[s], a, c, x);
     const long long t = (long long)p * rows_cap + r;
 #pragma unroll

@@ -153,7 +153,7 @@ __device__ __forceinline__ void check_body(const SearchDev &sd, const CheckArgs 
       } else {
         const float topt = ca.wp_topt[e];
         const float dt = topt / nd;
-        if (Mode == PUMP_BVP_PARITY) path_point(dt * i, topt, x0, x1, x);
+        if (Mode == PUMP_BVP_PARITY) path_point_fast(dt * i, topt, x0, x1, x);
         else path_point_f32(dt * i, topt, x0, x1, x);
       }
       // consecutive threads write consecutive 24-byte records: a warp's
@@ -302,6 +302,7 @@ __device__ __forceinline__ void zero_tiles(const LoopTiles &t) {
 // the store pass's tile scratch for this iteration.
 constexpr int kExpTile = 32;       // paths per tile: one per lane of the scanning warp
 constexpr int kExpThreads = 1024;  // one warp writes each of the tile's paths
+constexpr int kExpChunks = 4;      // 32-edge chunks of a path loaded together
 static_assert(kLoopScanTile == kExpTile, "expansion tile size");
 
 __device__ __forceinline__ void expand_body(const SearchDev &sd, const int *g, int n_g, int g_idx,
@@ -322,6 +323,7 @@ __device__ __forceinline__ void expand_body(const SearchDev &sd, const int *g, i
     c->todo = 0;  // this iteration's checks have run
   }
   __shared__ unsigned int s_off[kExpTile];
+  __shared__ int s_prev[kExpTile], s_node[kExpTile];
   __shared__ int s_timeout;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned int lt = (1u << lane) - 1u;
@@ -332,7 +334,14 @@ __device__ __forceinline__ void expand_body(const SearchDev &sd, const int *g, i
     if (tile >= ntiles) break;             // block-uniform
     if (warp == 0) {
       const long long i = tile * kExpTile + lane;
-      const unsigned int cnt = i < n_g ? (unsigned int)sd.open_cnt[sd.path_node[g[i]]] : 0u;
+      unsigned int cnt = 0u;
+      if (i < n_g) {
+        const int prev = g[i];
+        const int node = sd.path_node[prev];
+        s_prev[lane] = prev;  // the path warps start from these
+        s_node[lane] = node;
+        cnt = (unsigned int)sd.open_cnt[node];
+      }
       unsigned int incl = cnt;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -364,30 +373,39 @@ __device__ __forceinline__ void expand_body(const SearchDev &sd, const int *g, i
     const long long rest = (long long)n_g - tile * kExpTile;
     const int in_tile = (int)(rest < kExpTile ? rest : kExpTile);
     for (int p = warp; p < in_tile; p += kExpThreads / 32) {
-      const long long k = tile * kExpTile + p;
-      const int prev = g[k];
-      const int node = sd.path_node[prev];
-      const int e0 = sd.go[node], e1 = sd.go[node + 1];
+      const int prev = s_prev[p];
+      const int node = s_node[p];
+      const int e0 = __ldg(&sd.go[node]), e1 = __ldg(&sd.go[node + 1]);
       unsigned int off = s_off[p];
-      // the node's expandable edges in edge order (PUMP.cu:52-53)
-      for (int c0 = e0; c0 < e1; c0 += 32) {
-        const int e = c0 + lane;
-        int dst = 0;
-        bool open = false;
-        if (e < e1) {
-          dst = sd.dst[e];
-          open = sd.free_e[e] && sd.free_s[dst];
+      // the node's expandable edges in edge order (PUMP.cu:52-53), kExpChunks
+      // chunks of 32 edges at a time: their loads are issued together (the
+      // roadmap arrays are read-only here), then the chunks are written in
+      // order
+      for (int b0 = e0; b0 < e1; b0 += 32 * kExpChunks) {
+        int dst[kExpChunks];
+        bool open[kExpChunks];
+#pragma unroll
+        for (int c = 0; c < kExpChunks; ++c) {
+          const int e = b0 + 32 * c + lane;
+          dst[c] = e < e1 ? __ldg(&sd.dst[e]) : 0;
+          open[c] = e < e1 && __ldg(&sd.free_e[e]) != 0;
         }
-        const unsigned int bal = __ballot_sync(0xffffffffu, open);
-        const unsigned int q = off + __popc(bal & lt);
-        if (open && q < cap) {
-          sd.wf_prev[q] = prev;
-          sd.wf_node[q] = dst;
-          sd.wf_edge[q] = e;
-          sd.wf_open[q] = e;
-          sd.new_head[dst] = -1;
+#pragma unroll
+        for (int c = 0; c < kExpChunks; ++c) open[c] = open[c] && __ldg(&sd.free_s[dst[c]]) != 0;
+#pragma unroll
+        for (int c = 0; c < kExpChunks; ++c) {
+          const int e = b0 + 32 * c + lane;
+          const unsigned int bal = __ballot_sync(0xffffffffu, open[c]);
+          const unsigned int q = off + __popc(bal & lt);
+          if (open[c] && q < cap) {
+            sd.wf_prev[q] = prev;
+            sd.wf_node[q] = dst[c];
+            sd.wf_edge[q] = e;
+            sd.wf_open[q] = e;
+            sd.new_head[dst[c]] = -1;
+          }
+          off += __popc(bal);
         }
-        off += __popc(bal);
       }
     }
     __syncthreads();  // s_off is rewritten by the next tile
@@ -720,10 +738,10 @@ __global__ void __launch_bounds__(kChkThreads, 4) check_loop_kernel(const LoopGr
   check_body<Mode, false>(sd, ca);
 }
 
-__global__ void __launch_bounds__(kExpThreads) expand_loop_kernel(const LoopGroup *g) {
+__global__ void __launch_bounds__(kExpThreads, 1) expand_loop_kernel(const LoopGroup *g) {
   const LoopArgs *a = loop_query(g);
   if (!a) return;
-  const SearchDev sd = a->sd;
+  const SearchDev &sd = a->sd;  // fields read from the argument block as used
   const int g_idx = a->L.g_idx;
   const TileScratch ts = tiles_of(a->scan);
   expand_body(sd, g_idx ? sd.g_list[1] : sd.g_list[0], a->L.n_g, g_idx, a->L.num_paths,
