@@ -169,12 +169,6 @@ __device__ float topt_bisection(const PairCoef &c, const PairFF &f, float tmax) 
   return topt;
 }
 
-// toptBisection of the pair (x0, x1).
-__device__ __forceinline__ float topt_parity(const float *x0, const float *x1, float tmax) {
-  const PairCoef c = make_coef(x0, x1);
-  return topt_bisection(c, make_pair_ff(x0, x1), tmax);
-}
-
 // --------------------------------------------------------------- kernels
 // Persistent parity kernel.  The reference's bisection runs a different
 // number of steps per pair (tmax test, halving loop, up to 50 bisection
@@ -338,9 +332,7 @@ __global__ void __launch_bounds__(T) discretize_kernel(
       o[d] = x0[d];
       o[numDisc * kDim + d] = x1[d];
     }
-    // the GPU-arithmetic mode's d_topt holds the reference GPU kernel's times;
-    // findDiscretizedPath recomputes the time with the host arithmetic
-    const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_parity(x0, x1, 5.0f) : topt;
+    const float tau = topt;
     const float dt = tau / numDisc;
     if (Mode != PUMP_BVP_PRECISION) {
       // float-float waypoints; the uncertified ones (a few in a hundred) in
@@ -535,8 +527,7 @@ __global__ void __launch_bounds__(T) discretize_off_kernel(
       o[d] = x0[d];
       o[numDisc * kDim + d] = x1[d];
     }
-    const float topt = toptE[e];
-    const float tau = Mode == PUMP_BVP_PARITY_GPU ? topt_parity(x0, x1, 5.0f) : topt;
+    const float tau = toptE[e];
     const float dt = tau / numDisc;
     if (Mode != PUMP_BVP_PRECISION) {
       // float-float waypoints; the uncertified ones (a few in a hundred) in
@@ -757,6 +748,9 @@ pump_status_t bvp_jobs_launch(const BvpJobs &jb, int mode, cudaStream_t stream) 
 }
 
 namespace {
+// Each edge's optimal time in the host arithmetic (tmax 5), one thread per
+// edge (the lane-refill kernel of all pairs took 1.15 ms on the N = 4000
+// query's 799,800 edges, this one about 0.9 ms).
 __global__ void edge_topts_parity_kernel(const float *__restrict__ samples, const int *__restrict__ src,
                                          const int *__restrict__ dst, long long E,
                                          float *__restrict__ topt) {
@@ -769,7 +763,7 @@ __global__ void edge_topts_parity_kernel(const float *__restrict__ samples, cons
     x0[d] = __ldg(&samples[a * kDim + d]);
     x1[d] = __ldg(&samples[b * kDim + d]);
   }
-  topt[e] = topt_parity(x0, x1, 5.0f);
+  topt[e] = topt_bisection(make_coef(x0, x1), make_pair_ff(x0, x1), 5.0f);
 }
 }  // namespace
 
@@ -779,6 +773,31 @@ pump_status_t edge_topts_parity_async(const float *d_samples, const int *d_src, 
   edge_topts_parity_kernel<<<grid_for(E, 128), 128, 0, stream>>>(d_samples, d_src, d_dst, E, d_topt);
   return launch_status("edge_topts_parity");
 }
+
+namespace {
+// The times the waypoint entry points evaluate at: d_topt itself, or, in the
+// GPU-arithmetic mode (whose d_topt holds the reference GPU kernel's times),
+// each edge's time in the host arithmetic, as the reference's
+// findDiscretizedPath (host code) recomputes it, in a stream-ordered buffer
+// freed with the object.
+struct HostTopts {
+  const float *topt = nullptr;
+  float *own = nullptr;
+  cudaStream_t s = nullptr;
+  pump_status_t make(const float *d_samples, const int *d_src, const int *d_dst,
+                     const float *d_topt, long long E, int mode, cudaStream_t stream) {
+    topt = d_topt;
+    if (mode != PUMP_BVP_PARITY_GPU) return PUMP_OK;
+    s = stream;
+    PUMP_CUDA_TRY(pool_malloc_async((void **)&own, sizeof(float) * (size_t)E, stream));
+    topt = own;
+    return edge_topts_parity_async(d_samples, d_src, d_dst, E, own, stream);
+  }
+  ~HostTopts() {
+    if (own) cudaFreeAsync(own, s);
+  }
+};
+}  // namespace
 
 pump_status_t bvp_path_states(const float *d_xs, const int *d_seg, const float *d_tsample,
                               const float *d_tau, int total, float *d_out, cudaStream_t stream) {
@@ -869,8 +888,9 @@ pump_status_t discretize_off_async(const float *d_samples, const int *d_src, con
                                                                d_off, max_disc, d_disc, error);
     return launch_status("discretize_off_kernel");
   };
-  if (mode == PUMP_BVP_PARITY) return go(std::integral_constant<int, PUMP_BVP_PARITY>{});
-  if (mode == PUMP_BVP_PARITY_GPU) return go(std::integral_constant<int, PUMP_BVP_PARITY_GPU>{});
+  // the GPU-arithmetic mode's waypoints are the parity mode's (host code),
+  // at times in the host arithmetic (HostTopts)
+  if (mode != PUMP_BVP_PRECISION) return go(std::integral_constant<int, PUMP_BVP_PARITY>{});
   return go(std::integral_constant<int, PUMP_BVP_PRECISION>{});
 }
 }  // namespace pump
@@ -904,11 +924,13 @@ extern "C" pump_status_t pump_discretize_edges_off(const float *d_samples, const
     return set_error(PUMP_ERR_BAD_INPUT, "pump_discretize_edges_off: bad arguments");
   if (E == 0) return PUMP_OK;
   cudaStream_t s = (cudaStream_t)stream;
+  HostTopts ht;
+  PUMP_TRY(ht.make(d_samples, d_src, d_dst, d_topt, E, mode, s));
   int *d_err = nullptr;
   PUMP_CUDA_TRY(pool_malloc_async((void **)&d_err, sizeof(int), s));
   pump_status_t st = cuda_status(cudaMemsetAsync(d_err, 0, sizeof(int), s), "cudaMemsetAsync");
   if (st == PUMP_OK)
-    st = discretize_off_async(d_samples, d_src, d_dst, d_topt, E, d_off, max_disc, mode, d_disc, s, d_err);
+    st = discretize_off_async(d_samples, d_src, d_dst, ht.topt, E, d_off, max_disc, mode, d_disc, s, d_err);
   int err = 0;
   if (st == PUMP_OK)
     st = cuda_status(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
@@ -934,16 +956,17 @@ extern "C" pump_status_t pump_discretize_edges(const float *d_samples, const int
   if (discretize_smem<256>(numDisc) > 220 * 1024)
     return set_error(PUMP_ERR_CAPACITY, "pump_discretize_edges: %d waypoints per edge exceed the stage",
                      numDisc + 1);
-  // block sizes 64, 128 (default), 256
+  HostTopts ht;
+  PUMP_TRY(ht.make(d_samples, d_src, d_dst, d_topt, E, mode, s));
+  const float *topt = ht.topt;
+  // block sizes 64, 128 (default), 256; the GPU-arithmetic mode's waypoints
+  // are the parity mode's at the host arithmetic's times
   auto go = [&](auto block) -> pump_status_t {
     constexpr int T = decltype(block)::value;
-    if (mode == PUMP_BVP_PARITY)
-      return discretize_launch<PUMP_BVP_PARITY, T>(d_samples, d_src, d_dst, d_topt, E, numDisc,
+    if (mode != PUMP_BVP_PRECISION)
+      return discretize_launch<PUMP_BVP_PARITY, T>(d_samples, d_src, d_dst, topt, E, numDisc,
                                                    d_disc, s);
-    if (mode == PUMP_BVP_PARITY_GPU)
-      return discretize_launch<PUMP_BVP_PARITY_GPU, T>(d_samples, d_src, d_dst, d_topt, E, numDisc,
-                                                       d_disc, s);
-    return discretize_launch<PUMP_BVP_PRECISION, T>(d_samples, d_src, d_dst, d_topt, E, numDisc,
+    return discretize_launch<PUMP_BVP_PRECISION, T>(d_samples, d_src, d_dst, topt, E, numDisc,
                                                     d_disc, s);
   };
   auto run = [&](int c) -> pump_status_t {

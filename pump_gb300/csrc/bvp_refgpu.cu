@@ -95,6 +95,25 @@ __device__ float topt_dev(const float *a, const float *b, const CoordPow &p, flo
   return topt;
 }
 
+// The reference expression's costs at ta and tb (each when wanted); out of
+// line, so that the registers of the binary64 powers do not count against
+// the pair kernel's occupancy (80-96 registers instead of 106: 10.57 ms ->
+// 10.04 ms at N = 4000 with 5 blocks of 128 per SM, 10.27 ms with 6).
+struct PairStates {
+  float a[kDim], b[kDim];
+};
+struct CostPair {
+  float ca, cb;
+};
+__device__ __noinline__ CostPair refgpu_costs(const PairStates st, float ta, float tb, bool want_a,
+                                              bool want_b) {
+  const CoordPow p = coord_pow(st.a, st.b);
+  CostPair r{0.0f, 0.0f};
+  if (want_a) r.ca = cost_dev(ta, st.a, st.b, p);
+  if (want_b) r.cb = cost_dev(tb, st.a, st.b, p);
+  return r;
+}
+
 // All ordered pairs: per lane, the evaluations of toptBisection as a state
 // machine (phase 0: the tmax test, 1: halving, 2: bisection, 3: the final
 // cost), two cost evaluations per step; a lane whose pair is done takes the
@@ -106,7 +125,7 @@ __device__ float topt_dev(const float *a, const float *b, const CoordPow &p, flo
 constexpr int kChunk = 512;
 constexpr int kFallback = 8;
 
-__global__ void __launch_bounds__(128) bvp_pairs_refgpu_kernel(const float *__restrict__ samples,
+__global__ void __launch_bounds__(128, 5) bvp_pairs_refgpu_kernel(const float *__restrict__ samples,
                                                                int N, float tmax,
                                                                float *__restrict__ copts,
                                                                float *__restrict__ topts) {
@@ -160,9 +179,15 @@ __global__ void __launch_bounds__(128) bvp_pairs_refgpu_kernel(const float *__re
     const unsigned waiting = __ballot_sync(0xffffffffu, pending);
     if (waiting && (__popc(waiting) >= kFallback || waiting == active)) {
       if (pending) {
-        const CoordPow p = coord_pow(a, b);
-        if (!ok_a) ca = cost_dev(ta, a, b, p);
-        if (!ok_b) cb = cost_dev(tb, a, b, p);
+        PairStates st;
+#pragma unroll
+        for (int d = 0; d < kDim; ++d) {
+          st.a[d] = a[d];
+          st.b[d] = b[d];
+        }
+        const CostPair r = refgpu_costs(st, ta, tb, !ok_a, !ok_b);
+        if (!ok_a) ca = r.ca;
+        if (!ok_b) cb = r.cb;
         pending = false;
       }
     }
@@ -177,7 +202,9 @@ __global__ void __launch_bounds__(128) bvp_pairs_refgpu_kernel(const float *__re
     } else if (phase == 2) {
       dcval = d;
       if (dcval > 0) tu = topt; else tl = topt;
-      if (!(fabsf(dcval) > 0.0001 && itr < 50)) phase = 3;
+      // (double)|dcval| > 0.0001 exactly when |dcval| > 0.0001f: binary32
+      // 0.0001f is below 0.0001 and the next binary32 above it
+      if (!(fabsf(dcval) > 0.0001f && itr < 50)) phase = 3;
     } else {
       topts[idx] = topt;
       copts[idx] = ca;

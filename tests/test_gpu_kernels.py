@@ -241,6 +241,38 @@ def roadmap_edges(torch, pumplib, ctx, c, t, N, k, cap):
             host(d_go, N + 1))
 
 
+def test_waypoints_gpu_arithmetic_mode(gpu, pumplib, roadmap1000):
+    """pump_discretize_edges and pump_discretize_edges_off in the reference
+    GPU kernel's mode evaluate the reference's host findDiscretizedPath: the
+    parity waypoints at each edge's time in the host arithmetic (whatever
+    times d_topt holds), bit for bit; the parity waypoints themselves match
+    the oracle (test_build_edges_and_waypoints)."""
+    torch, _ = gpu
+    L = pumplib.load()
+    r = roadmap1000
+    s, src, dst = r["samples"], r["src"], r["dst"]
+    E = src.size
+    # the host-arithmetic times: pump_bvp_batch in parity mode, tmax 5
+    d0, d1 = dev(torch, s[src]), dev(torch, s[dst])
+    d_th, d_c = empty(torch, E, torch.float32), empty(torch, E, torch.float32)
+    pumplib.check(L.pump_bvp_batch(ptr(d0), ptr(d1), E, 5.0, pumplib.PUMP_BVP_PARITY, ptr(d_th),
+                                   ptr(d_c), stream(torch)))
+    d_s, d_src, d_dst = dev(torch, s), dev(torch, src), dev(torch, dst)
+    d_junk = dev(torch, np.full(E, 0.37, np.float32))  # GPU-kernel times are not used
+    out = {}
+    for mode, d_t in ((pumplib.PUMP_BVP_PARITY, d_th), (pumplib.PUMP_BVP_PARITY_GPU, d_junk)):
+        d_disc = empty(torch, E * 9 * 6, torch.float32)
+        pumplib.check(L.pump_discretize_edges(ptr(d_s), ptr(d_src), ptr(d_dst), ptr(d_t), E, 8, mode,
+                                              ptr(d_disc), stream(torch)))
+        d_off = dev(torch, np.arange(E + 1, dtype=np.int64) * 9)
+        d_disc2 = empty(torch, E * 9 * 6, torch.float32)
+        pumplib.check(L.pump_discretize_edges_off(ptr(d_s), ptr(d_src), ptr(d_dst), ptr(d_t), E,
+                                                  ptr(d_off), 8, mode, ptr(d_disc2), stream(torch)))
+        out[mode] = (host(d_disc, E * 54), host(d_disc2, E * 54))
+    a, b = out[pumplib.PUMP_BVP_PARITY], out[pumplib.PUMP_BVP_PARITY_GPU]
+    assert same_bits(a[0], b[0]) and same_bits(a[1], b[1]) and same_bits(a[0], a[1])
+
+
 def test_roadmap_edges_one_read(gpu, pumplib, roadmap1000):
     """rn and the edges from one read of the pair costs equal pump_select_kth +
     pump_build_edges (the oracle's sort and scan) bit for bit."""
