@@ -826,8 +826,10 @@ def mode_record(lib, L, ctx, torch, w, mode, args, flush, batch, steps=None, war
 BVP_FP64_FLOPS_PER_PAIR = {"precision": 28.0, "parity": 40.0 * 23 + 20.0,
                            "parity_gpu": 40.0 * 23 + 20.0}
 # ncu smsp__inst_executed.sum of one parity pair-kernel launch at N = 1000
-# (999,000 pairs), per pair
+# (999,000 pairs), per pair; the same for the reference-GPU arithmetic's
+# pair kernel
 BVP_PARITY_WARP_INST_PER_PAIR = 520217704 / 999000
+BVP_REFGPU_WARP_INST_PER_PAIR = 539004721 / 999000
 # The precision kernel is bound by instruction issue, not by one pipe: warp
 # instructions executed per pair on this workload (ncu smsp__inst_executed.sum
 # over one launch of the N = 4000 workload's pair kernel, the one marking the
@@ -881,11 +883,13 @@ def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops, sm_mhz):
         issue = BVP_PRECISION_WARP_INST_PER_PAIR * pairs / t_bvp / 1e9
         table["bvp_pairs"] = {"bound": "issue", "achieved_ginst": round(issue, 1),
                               "frac": round(issue / issue_peak, 4)}
-    if mode == "parity":
-        issue = BVP_PARITY_WARP_INST_PER_PAIR * pairs / t_bvp / 1e9
+    inst_pp = {"parity": BVP_PARITY_WARP_INST_PER_PAIR,
+               "parity_gpu": BVP_REFGPU_WARP_INST_PER_PAIR}.get(mode)
+    if inst_pp is not None:
+        issue = inst_pp * pairs / t_bvp / 1e9
         table["bvp_pairs"] = {"bound": "issue", "achieved_ginst": round(issue, 1),
                               "frac": round(issue / issue_peak, 4),
-                              "inst_per_pair": round(BVP_PARITY_WARP_INST_PER_PAIR, 1)}
+                              "inst_per_pair": round(inst_pp, 1)}
     if mode == "precision" and N == 4000:
         for k, units, per in (("free_edges", E, FREE_EDGES_WARP_INST_PER_EDGE_N4000),
                               ("discretize", E * W, DISCRETIZE_WARP_INST_PER_WAYPOINT)):
@@ -902,12 +906,12 @@ def roofline(dom, ks, N, E, M, W, H, P, mode, fp64_tflops, sm_mhz):
                                "SM clock sampled during the timed region (%.0f MHz)" % sm_mhz,
                 "inst_per_pair": BVP_PRECISION_WARP_INST_PER_PAIR,
                 "fp64_pipe": table["bvp_pairs_fp64"], "all": table}
-    if dom == "bvp_pairs" and mode == "parity":
+    if dom == "bvp_pairs" and inst_pp is not None:
         return {"kernel": dom, "bound": "issue", "achieved": issue, "peak": issue_peak,
                 "unit": "G warp-instructions/s", "frac": issue / issue_peak, "traffic": None,
                 "peak_source": "152 SMs x 4 schedulers x 1 warp instruction per clock at the "
                                "SM clock sampled during the timed region (%.0f MHz)" % sm_mhz,
-                "inst_per_pair": BVP_PARITY_WARP_INST_PER_PAIR, "all": table}
+                "inst_per_pair": inst_pp, "all": table}
     if dom == "bvp_pairs":
         return {"kernel": dom, "bound": "fp64", "achieved": fp64, "peak": fp64_tflops,
                 "unit": "TFLOP/s", "frac": fp64 / fp64_tflops, "traffic": None,
