@@ -41,9 +41,11 @@ namespace {
 // rounding cell of its high part (it does not reach the midpoint to either
 // neighbour), cost_eval's (float) conversion gives that high part, which is
 // returned.  Otherwise (and for tau outside [1e-4, 1e4], or a non-finite or
-// subnormal result) the binary64 evaluation runs.  The file is compiled
-// without multiply-add contraction, which the error-free transformations
-// need (TwoProduct calls fmaf explicitly).
+// subnormal result) the binary64 evaluation runs.  The binary32 terms that
+// the reference rounds are products written as __fmul_rn, which no compiler
+// fuses into the sums that follow (bvp_refgpu.cu is compiled with
+// contraction, and a product with a single use would otherwise become a
+// multiply-add); TwoProduct calls fmaf explicitly.
 struct FF {
   float hi, lo;
 };
@@ -105,6 +107,7 @@ struct PairFF {
   float a29, b29, c29, a30, b30, c30;
   FF s7, d2, d3;
   float abs_s7, abs_d2, abs_d3;
+  float abs_k;  // |k8| + ... + |k15| (times tau: the t-linear terms' magnitudes)
 };
 __device__ __forceinline__ FF ff_12sq(float x) {
   FF t = ff_two_prod(x, x);
@@ -126,6 +129,8 @@ __device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1)
   f.k13 = 12 * x1[5] * x1[2];
   f.k14 = 12 * x0[4] * x1[1];
   f.k15 = 12 * x1[4] * x1[1];
+  f.abs_k = ((fabsf(f.k8) + fabsf(f.k9)) + (fabsf(f.k10) + fabsf(f.k11))) +
+            ((fabsf(f.k12) + fabsf(f.k13)) + (fabsf(f.k14) + fabsf(f.k15)));
   f.a29 = 12 * x0[0];
   f.b29 = -2 * x1[0];
   f.c29 = x0[3] + x1[3];
@@ -139,7 +144,7 @@ __device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1)
 #pragma unroll
   for (int q = 0; q < 5; ++q) {
     if (q == 4) {
-      const float c24 = 24 * x0[1] * x1[1];
+      const float c24 = __fmul_rn(24 * x0[1], x1[1]);
       s = ff_add_f(s, -c24);
       as += fabsf(c24);
     }
@@ -161,7 +166,8 @@ __device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1)
     d = ff_add(d, t);
     ad += t.hi;
   }
-  const float fl[3] = {4 * x0[4] * x1[4], 4 * x0[3] * x1[3], 4 * x0[5] * x1[5]};
+  const float fl[3] = {__fmul_rn(4 * x0[4], x1[4]), __fmul_rn(4 * x0[3], x1[3]),
+                       __fmul_rn(4 * x0[5], x1[5])};
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     d = ff_add_f(d, fl[q]);
@@ -169,7 +175,7 @@ __device__ __forceinline__ PairFF make_pair_ff(const float *x0, const float *x1)
   }
   f.d2 = d;
   f.abs_d2 = ad;
-  const float f25 = 2 * g * x0[5], f26 = 2 * g * x1[5];
+  const float f25 = __fmul_rn(2 * g, x0[5]), f26 = __fmul_rn(2 * g, x1[5]);
   f.d3 = ff_two_sum(f25, -f26);
   f.abs_d3 = fabsf(f25) + fabsf(f26);
   return f;
@@ -180,17 +186,21 @@ __device__ __forceinline__ float cost_ff(const PairFF &f, float tau, bool *ok) {
   *ok = false;
   if (!(tau >= 1e-4f && tau <= 1e4f)) return 0.0f;
   // the float terms, as cost_eval rounds them
-  const float k[8] = {f.k8 * tau,    f.k9 * tau,    -(f.k10 * tau), -(f.k11 * tau),
-                      -(f.k12 * tau), -(f.k13 * tau), -(f.k14 * tau), -(f.k15 * tau)};
-  const float a29 = f.a29 * (f.b29 + f.c29 * tau);
-  const float a30 = f.a30 * (f.b30 + f.c30 * tau);
+  const float k[8] = {__fmul_rn(f.k8, tau),     __fmul_rn(f.k9, tau),
+                      -__fmul_rn(f.k10, tau),    -__fmul_rn(f.k11, tau),
+                      -__fmul_rn(f.k12, tau),    -__fmul_rn(f.k13, tau),
+                      -__fmul_rn(f.k14, tau),    -__fmul_rn(f.k15, tau)};
+  // b + c tau as the reference writes it (contracted where the reference's
+  // build contracts it), the outer product rounded (the reference converts
+  // it to binary64 before adding it)
+  const float a29 = __fmul_rn(f.a29, f.b29 + f.c29 * tau);
+  const float a30 = __fmul_rn(f.a30, f.b30 + f.c30 * tau);
   FF v = f.s7;
-  float mag = f.abs_s7;
+  // |k[q]| = |k_q| tau to within 2^-24 of each, and abs_k is the sum of the
+  // |k_q| to within 2^-21: inside the bound's 1 % margin
+  float mag = f.abs_s7 + f.abs_k * tau;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    v = ff_add_f(v, k[q]);
-    mag += fabsf(k[q]);
-  }
+  for (int q = 0; q < 8; ++q) v = ff_add_f(v, k[q]);
   const FF t2 = ff_two_prod(tau, tau);
   const FF t3 = ff_mul_f(t2, tau);
   const FF t4 = ff_mul(t2, t2);
