@@ -32,11 +32,19 @@ namespace {
 //     product; t^3 and t^4 are themselves rounded products), so its error is
 //     at most 2^-52 x 33 x (the sum of the terms' magnitudes) = 2^-47 x that
 //     sum;
-//   - the float-float evaluation: at most 2^-42 x that sum (about 30
-//     operations, each within 2^-47 of its operands' magnitudes); the bound
-//     below takes 2^-41, twice the two together;
+//   - the float-float evaluation, counted with worst-case constants per
+//     operation (u = 2^-24; double-word bounds of Joldes, Muller and
+//     Popescu, 2017, and 7 u^2 (|x| + |y|) for the fast sum): s7 and the
+//     t^2 coefficient's sums (make_pair_ff) 21 u^2 and 30 u^2 with their
+//     product, the t^3 and t^4 terms 7.5 u^2 and 14 u^2, the eight binary32
+//     terms 16 u^2, the three fast sums 21 u^2, the last two terms 4 u^2:
+//     at most 114 u^2 = 2^-41.2 x that sum;
+//   - the bound below takes 2^-41 x 1.01 of the sum (129 u^2), above the
+//     two together (116 u^2; the reference's GPU kernel's binary64 value is
+//     within 2.1 u^2 of it, see above);
 //   - the final 1 / t^3 and the product (three more binary64 roundings) and
-//     the float-float division: at most 2^-42 of the result.
+//     the float-float division (its residual a fast sum): at most 2^-42 of
+//     the result.
 // When that interval around the float-float value lies inside the binary32
 // rounding cell of its high part (it does not reach the midpoint to either
 // neighbour), cost_eval's (float) conversion gives that high part, which is
@@ -68,6 +76,14 @@ __device__ __forceinline__ FF ff_add(FF x, FF y) {
   s.lo = s.lo + t.hi;
   s = ff_fast_two_sum(s.hi, s.lo);
   s.lo = s.lo + t.lo;
+  return ff_fast_two_sum(s.hi, s.lo);
+}
+// Double-word sum without the second TwoSum ("sloppy" addition): its error
+// is at most about 8 u^2 (|x| + |y|), u = 2^-24, also under cancellation,
+// which is all cost_ff's bound (taken over the terms' magnitudes) needs.
+__device__ __forceinline__ FF ff_add_fast(FF x, FF y) {
+  FF s = ff_two_sum(x.hi, y.hi);
+  s.lo = s.lo + (x.lo + y.lo);
   return ff_fast_two_sum(s.hi, s.lo);
 }
 __device__ __forceinline__ FF ff_add_f(FF x, float b) {
@@ -208,13 +224,22 @@ __device__ __forceinline__ float cost_ff(const PairFF &f, float tau, bool *ok) {
   const float g = PUMP_G;
   const FF g2 = ff_two_prod(g, g);
   const FF d4 = ff_add_f(g2, 1.0f);
-  v = ff_add(v, ff_mul(f.d2, t2));
-  v = ff_add(v, ff_mul(f.d3, t3));
-  v = ff_add(v, ff_mul(d4, t4));
+  v = ff_add_fast(v, ff_mul(f.d2, t2));
+  v = ff_add_fast(v, ff_mul(f.d3, t3));
+  v = ff_add_fast(v, ff_mul(d4, t4));
   v = ff_add_f(v, a29);
   v = ff_add_f(v, a30);
   mag += f.abs_d2 * t2.hi + f.abs_d3 * t3.hi + d4.hi * t4.hi + fabsf(a29) + fabsf(a30);
-  const FF w = ff_div(v, t3);
+  // v / t3 as ff_div, the residual v - q1 t3 with the fast sum (its error,
+  // 8 u^2 of |v| + |q1 t3|, is 2^-44 of the quotient)
+  FF w;
+  {
+    const float q1 = __fdiv_rn(v.hi, t3.hi);
+    const FF qy = ff_mul_f(t3, q1);
+    const FF r = ff_add_fast(v, {-qy.hi, -qy.lo});
+    const float q2 = __fdiv_rn(r.hi, t3.hi);
+    w = ff_fast_two_sum(q1, q2);
+  }
   // the bound on |cost_eval's binary64 value - w| (margins for the binary32
   // evaluation of the bound itself)
   const float aw = fabsf(w.hi);
