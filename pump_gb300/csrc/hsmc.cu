@@ -638,12 +638,14 @@ inline const void *hsmc_loop_kernel_for(int P) {
 // collisionProbability.cu:39-92.  A particle collides when any of the
 // segments t = 0 .. T-3 of its perturbed path hits a box; the reference walks
 // the segments in order and stops at the first hit, which gives the same
-// answer as testing all of them.  Block = 32 particles (the lanes) x 8 warps;
-// warp w tests segments t = w, w + 8, ...; the per-particle OR over warps is
-// taken in shared memory and the block adds its popcount to hits[k].
-// Grid (ceil(Pmc / 32), paths).
+// answer as testing all of them.  Block = 32 particles (the lanes) x
+// kMcWarps warps; warp w tests segments t = w, w + kMcWarps, ...; the
+// per-particle OR over warps is taken in shared memory and the block adds
+// its popcount to hits[k].  Grid (ceil(Pmc / 32), paths).
 // MC CP of path k (blockIdx.y): 32 particles per block (one per lane), the
-// 8 warps splitting the path's segments.  With rowmax (the largest |offset|
+// kMcWarps warps splitting the path's segments (16: a smoothing batch of a
+// few paths is a few hundred blocks, so the segments are split finely to
+// shorten each warp's chain).  With rowmax (the largest |offset|
 // per table row and axis), each block first marks, per segment, the boxes
 // that some particle's segment could touch: the path segment's bounding box
 // widened by fl(rowmax * |offset_mult|) on both ends.  A particle's position
@@ -653,8 +655,9 @@ inline const void *hsmc_loop_kernel_for(int P) {
 // the marked boxes are tested, in index order.  Without rowmax (or with more
 // than kMcFilterObs boxes, or a NaN state) every box is tested.
 constexpr int kMcFilterObs = 128;
+constexpr int kMcWarps = 16;
 
-__global__ void __launch_bounds__(256) mc_cp_kernel(
+__global__ void __launch_bounds__(32 * kMcWarps) mc_cp_kernel(
     const float *__restrict__ paths, const int *__restrict__ offset, const int *__restrict__ len,
     const float *__restrict__ offsets_t, int Pmc, int T_rows, float offset_mult,
     const float *__restrict__ obs, int numObs, int k0, int *__restrict__ hits,
@@ -663,7 +666,7 @@ __global__ void __launch_bounds__(256) mc_cp_kernel(
   extern __shared__ float4 s_obs4[];
   float *s_obs = reinterpret_cast<float *>(s_obs4);
   uint32_t *s_mask = reinterpret_cast<uint32_t *>(s_obs + ((numObs * 12 + 3) & ~3));
-  __shared__ unsigned int s_hit[8];
+  __shared__ unsigned int s_hit[kMcWarps];
   stage_obstacles(obs, numObs, s_obs);
   const int k = k0 + blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -695,7 +698,7 @@ __global__ void __launch_bounds__(256) mc_cp_kernel(
   bool coll = false;
   if (p < Pmc && T <= T_rows) {
     const int words = (numObs + 31) / 32;
-    for (int t = warp; t < T - 2 && !coll; t += 8) {
+    for (int t = warp; t < T - 2 && !coll; t += kMcWarps) {
       float v[3], w[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
@@ -712,7 +715,7 @@ __global__ void __launch_bounds__(256) mc_cp_kernel(
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned int any = 0;
-    for (int q = 0; q < 8; ++q) any |= s_hit[q];
+    for (int q = 0; q < kMcWarps; ++q) any |= s_hit[q];
     const int total = __popc(any);
     if (total) atomicAdd(&hits[k], total);
   }
@@ -802,7 +805,7 @@ pump_status_t mc_cp_hits_async(const float *d_paths, const int *d_offset, const 
   for (int k0 = 0; k0 < n_paths; k0 += 65535) {
     const int nk = n_paths - k0 < 65535 ? n_paths - k0 : 65535;
     dim3 grid(grid_for(Pmc, 32), (unsigned)nk);
-    mc_cp_kernel<<<grid, 256, smem, stream>>>(d_paths, d_offset, d_len, d_offsets_t, Pmc, T_rows,
+    mc_cp_kernel<<<grid, 32 * kMcWarps, smem, stream>>>(d_paths, d_offset, d_len, d_offsets_t, Pmc, T_rows,
                                               offset_mult, d_obstacles, numObs, k0, d_hits,
                                               d_rowmax, copy_src, copy_dst, copy_words, done,
                                               seq);
