@@ -326,7 +326,7 @@ def compare(cfg_name, out_dir, torch, lib, L, ctx, ref):
 
 
 def main():
-    out_dir = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "refgpu")
+    out_dir = sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.getcwd(), "refgpu_compare")
     os.makedirs(out_dir, exist_ok=True)
     import torch
     from pump_gb300 import lib
