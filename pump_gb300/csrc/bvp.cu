@@ -192,6 +192,7 @@ __device__ float topt_bisection(const PairCoef &c, const PairFF &f, float tmax) 
 // 10.1 with 96 registers and 5 blocks).
 constexpr int kParityChunk = 512;
 constexpr int kFallbackLanes = 8;
+constexpr int kRefillLanes = 8;
 
 __global__ void __launch_bounds__(128, 6) bvp_pairs_parity_persistent(
     const float *__restrict__ samples, int N, float tmax, float *__restrict__ copts,
@@ -215,9 +216,12 @@ __global__ void __launch_bounds__(128, 6) bvp_pairs_parity_persistent(
   float ta = 0, tb = 0, ca = 0, cb = 0;
   bool pending = false, ok_a = true, ok_b = true;
   while (true) {
-    // lanes without a pair take the next pairs of the warp's chunk
+    // lanes without a pair take the next pairs of the warp's chunk, once
+    // kRefillLanes of them wait (or no lane has a pair): the pair set-up
+    // then runs for several lanes at once (N = 4000: 7.38 ms refilling each
+    // lane at once, 6.40 ms with 4 lanes, 6.10 ms with 8, 6.59 ms with 16)
     const unsigned need = __ballot_sync(0xffffffffu, idx < 0);
-    if (need && chunk_next < chunk_end) {
+    if (need && chunk_next < chunk_end && (__popc(need) >= kRefillLanes || need == 0xffffffffu)) {
       const int avail = (int)(chunk_end - chunk_next);
       const int rank = __popc(need & lt);
       const bool mine = (need >> lane) & 1u;

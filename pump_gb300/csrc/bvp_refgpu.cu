@@ -124,6 +124,7 @@ __device__ __noinline__ CostPair refgpu_costs(const PairStates st, float ta, flo
 // together.
 constexpr int kChunk = 512;
 constexpr int kFallback = 8;
+constexpr int kRefill = 8;
 
 __global__ void __launch_bounds__(128, 5) bvp_pairs_refgpu_kernel(const float *__restrict__ samples,
                                                                int N, float tmax,
@@ -145,8 +146,10 @@ __global__ void __launch_bounds__(128, 5) bvp_pairs_refgpu_kernel(const float *_
   float ta = 0, tb = 0, ca = 0, cb = 0;
   bool pending = false, ok_a = true, ok_b = true;
   while (true) {
+    // (refilled once kRefill lanes wait, or none has a pair, as in the parity
+    // kernel)
     const unsigned need = __ballot_sync(0xffffffffu, idx < 0);
-    if (need && chunk_next < chunk_end) {
+    if (need && chunk_next < chunk_end && (__popc(need) >= kRefill || need == 0xffffffffu)) {
       const int avail = (int)(chunk_end - chunk_next);
       const int rank = __popc(need & lt);
       if (((need >> lane) & 1u) && rank < avail) {
