@@ -828,8 +828,8 @@ BVP_FP64_FLOPS_PER_PAIR = {"precision": 28.0, "parity": 40.0 * 23 + 20.0,
 # ncu smsp__inst_executed.sum of one parity pair-kernel launch at N = 1000
 # (999,000 pairs), per pair; the same for the reference-GPU arithmetic's
 # pair kernel
-BVP_PARITY_WARP_INST_PER_PAIR = 520217704 / 999000
-BVP_REFGPU_WARP_INST_PER_PAIR = 539004721 / 999000
+BVP_PARITY_WARP_INST_PER_PAIR = 395849939 / 999000
+BVP_REFGPU_WARP_INST_PER_PAIR = 416223561 / 999000
 # The precision kernel is bound by instruction issue, not by one pipe: warp
 # instructions executed per pair on this workload (ncu smsp__inst_executed.sum
 # over one launch of the N = 4000 workload's pair kernel, the one marking the
